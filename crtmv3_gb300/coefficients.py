@@ -1,0 +1,216 @@
+"""ODPS TauCoeff and SpcCoeff tables: in-memory form and binary file I/O.
+
+The record order follows the reference writers so that files made here have
+the reference's on-disk layout:
+
+* ODPS TauCoeff: ``src/Coefficients/TauCoeff/ODPS/ODPS_Binary_IO.f90:1042-1180``
+  (Release/Version, Algorithm, dimensions, Group_Index, sensor ids, channel
+  list, component ids, absorber ids, reference profile, n_Predictors/Pos_Index,
+  C as REAL(Single)).  The coefficient index of channel ``l``, component ``j``,
+  predictor ``i`` and layer ``k`` is ``Pos_Index(j,l) + (i-1)*n_Layers + k - 1``
+  (1-based; ``ODPS_AtmAbsorption.f90:198-204``).
+* SpcCoeff (Release 8, Version 3 with PolAngle):
+  ``src/Coefficients/SpcCoeff/SpcCoeff_Binary_IO.f90:660-711``.
+"""
+from __future__ import annotations
+
+import dataclasses
+from typing import Optional
+
+import numpy as np
+
+from .fortran_io import RecordReader, RecordWriter
+
+# Sensor types (``ODPS_Define.f90:90-95``)
+MICROWAVE_SENSOR = 1
+INFRARED_SENSOR = 2
+VISIBLE_SENSOR = 3
+ULTRAVIOLET_SENSOR = 4
+
+ODPS_ALGORITHM = 2          # ``src/CRTM_Parameters.f90:128``
+ODPS_RELEASE = 2            # ``ODPS_Define.f90:79``
+ODPS_VERSION = 1
+SPCCOEFF_RELEASE = 8        # ``SpcCoeff_Define.f90:152``
+SPCCOEFF_VERSION = 3
+SL = 20                     # sensor id length
+
+# Predictor groups (``ODPS_Predictor.f90:85-116``)
+N_COMPONENTS_G = {1: 8, 2: 5, 3: 2}
+N_ABSORBERS_G = {1: 6, 2: 3, 3: 1}
+N_PREDICTORS_G = {
+    1: (7, 18, 7, 11, 11, 14, 10, 11),
+    2: (7, 15, 7, 11, 10),
+    3: (7, 14),
+}
+COMPONENT_ID_G = {
+    1: (7, 101, 15, 114, 121, 120, 119, 118),
+    2: (20, 101, 15, 114, 121),
+    3: (113, 12),
+}
+# HITRAN absorber ids per group, in the order the predictor code indexes them
+ABSORBER_ID_G = {1: (1, 3, 2, 4, 5, 6), 2: (1, 3, 2), 3: (1,)}
+
+H2O_ID, CO2_ID, O3_ID, N2O_ID, CO_ID, CH4_ID = 1, 2, 3, 4, 5, 6
+MASS_MIXING_RATIO_UNITS = 3     # g/kg
+VOLUME_MIXING_RATIO_UNITS = 1   # ppmv
+
+
+@dataclasses.dataclass
+class ODPSCoeff:
+    """The ODPS TauCoeff structure (``ODPS_Define.f90:110-200``), OPTRAN omitted."""
+    group_index: int
+    sensor_id: str
+    sensor_type: int
+    sensor_channel: np.ndarray          # (L,) int32
+    ref_level_pressure: np.ndarray      # (K+1,) hPa
+    ref_pressure: np.ndarray            # (K,)
+    ref_temperature: np.ndarray         # (K,)
+    ref_absorber: np.ndarray            # (K, Jm)
+    min_absorber: np.ndarray            # (K, Jm)
+    max_absorber: np.ndarray            # (K, Jm)
+    n_predictors: np.ndarray            # (J, L) int32
+    pos_index: np.ndarray               # (J, L) int32, 1-based
+    c: np.ndarray                       # (n_Coeffs,) float32
+    wmo_satellite_id: int = 1023
+    wmo_sensor_id: int = 2047
+
+    @property
+    def n_layers(self) -> int:
+        return int(self.ref_pressure.shape[0])
+
+    @property
+    def n_components(self) -> int:
+        return N_COMPONENTS_G[self.group_index]
+
+    @property
+    def n_absorbers(self) -> int:
+        return N_ABSORBERS_G[self.group_index]
+
+    @property
+    def n_channels(self) -> int:
+        return int(self.sensor_channel.shape[0])
+
+    @property
+    def component_id(self) -> np.ndarray:
+        return np.asarray(COMPONENT_ID_G[self.group_index], dtype=np.int32)
+
+    @property
+    def absorber_id(self) -> np.ndarray:
+        return np.asarray(ABSORBER_ID_G[self.group_index], dtype=np.int32)
+
+    def coeff_block(self, j: int, l: int) -> np.ndarray:
+        """Coefficients of component ``j`` and channel ``l`` (0-based) as (np, K)."""
+        npred = int(self.n_predictors[j, l])
+        if npred <= 0:
+            return np.zeros((0, self.n_layers), np.float32)
+        p0 = int(self.pos_index[j, l]) - 1
+        return self.c[p0:p0 + npred * self.n_layers].reshape(npred, self.n_layers)
+
+
+def write_odps(path: str, tc: ODPSCoeff, byteorder: str = "<") -> None:
+    K, J, Jm, L = tc.n_layers, tc.n_components, tc.n_absorbers, tc.n_channels
+    with open(path, "wb") as f:
+        w = RecordWriter(f, byteorder)
+        w.record(np.array([ODPS_RELEASE, ODPS_VERSION], np.int32))
+        w.record(np.array([ODPS_ALGORITHM], np.int32))
+        w.record(np.array([K, J, Jm, L, tc.c.size, 6, 0], np.int32))
+        w.record(np.array([tc.group_index], np.int32))
+        w.record(tc.sensor_id.ljust(SL)[:SL].encode("ascii"),
+                 np.array([tc.wmo_satellite_id, tc.wmo_sensor_id, tc.sensor_type], np.int32))
+        w.record(tc.sensor_channel.astype(np.int32))
+        w.record(tc.component_id)
+        w.record(tc.absorber_id)
+        w.record(tc.ref_level_pressure.astype(np.float64), tc.ref_pressure.astype(np.float64),
+                 tc.ref_temperature.astype(np.float64), tc.ref_absorber.astype(np.float64),
+                 tc.min_absorber.astype(np.float64), tc.max_absorber.astype(np.float64))
+        w.record(tc.n_predictors.astype(np.int32), tc.pos_index.astype(np.int32))
+        if tc.c.size > 0:
+            w.record(tc.c.astype(np.float32))
+
+
+def read_odps(path: str) -> ODPSCoeff:
+    with open(path, "rb") as f:
+        r = RecordReader(f)
+        release, version = r.split(r.record(), [("i4", (2,))])[0]
+        if release != ODPS_RELEASE:
+            raise IOError(f"ODPS release {release} not supported")
+        (alg,) = r.split(r.record(), [("i4", ())])
+        if alg != ODPS_ALGORITHM:
+            raise IOError(f"TauCoeff algorithm {alg} is not ODPS")
+        dims = r.split(r.record(), [("i4", (7,))])[0]
+        K, J, Jm, L, n_coeffs, _n_opindex, n_ocoeffs = (int(x) for x in dims)
+        (group,) = r.split(r.record(), [("i4", ())])
+        sid, ids = r.split(r.record(), [("S", SL), ("i4", (3,))])
+        chans = r.split(r.record(), [("i4", (L,))])[0]
+        r.record()  # component ids (fixed by group)
+        r.record()  # absorber ids (fixed by group)
+        lev, lay, temp, ra, mn, mx = r.split(r.record(), [
+            ("f8", (K + 1,)), ("f8", (K,)), ("f8", (K,)),
+            ("f8", (K, Jm)), ("f8", (K, Jm)), ("f8", (K, Jm))])
+        npred, pos = r.split(r.record(), [("i4", (J, L)), ("i4", (J, L))])
+        c = np.zeros(0, np.float32)
+        if n_coeffs > 0:
+            c = r.split(r.record(), [("f4", (n_coeffs,))])[0]
+        if n_ocoeffs > 0:
+            raise IOError("ODPS files with OPTRAN coefficients are not supported")
+    return ODPSCoeff(int(group), sid, int(ids[2]), chans, lev, lay, temp, ra, mn, mx,
+                     npred, pos, c, int(ids[0]), int(ids[1]))
+
+
+@dataclasses.dataclass
+class SpcCoeff:
+    """Spectral coefficients (``SpcCoeff_Define.f90:160-200``)."""
+    sensor_id: str
+    sensor_type: int
+    sensor_channel: np.ndarray
+    frequency: np.ndarray
+    wavenumber: np.ndarray
+    planck_c1: np.ndarray
+    planck_c2: np.ndarray
+    band_c1: np.ndarray
+    band_c2: np.ndarray
+    cosmic_background_radiance: np.ndarray
+    solar_irradiance: np.ndarray
+    polarization: Optional[np.ndarray] = None
+    pol_angle: Optional[np.ndarray] = None
+    channel_flag: Optional[np.ndarray] = None
+    wmo_satellite_id: int = 1023
+    wmo_sensor_id: int = 2047
+
+    @property
+    def n_channels(self) -> int:
+        return int(self.sensor_channel.shape[0])
+
+
+def write_spccoeff(path: str, sc: SpcCoeff, byteorder: str = "<") -> None:
+    L = sc.n_channels
+    pol = sc.polarization if sc.polarization is not None else np.zeros(L, np.int32)
+    pang = sc.pol_angle if sc.pol_angle is not None else np.zeros(L)
+    flag = sc.channel_flag if sc.channel_flag is not None else np.zeros(L, np.int32)
+    with open(path, "wb") as f:
+        w = RecordWriter(f, byteorder)
+        w.record(np.array([SPCCOEFF_RELEASE, SPCCOEFF_VERSION], np.int32))
+        w.record(np.array([L], np.int32))
+        w.record(sc.sensor_id.ljust(SL)[:SL].encode("ascii"),
+                 np.array([sc.sensor_type, sc.wmo_satellite_id, sc.wmo_sensor_id], np.int32))
+        w.record(sc.sensor_channel.astype(np.int32), pol.astype(np.int32), pang.astype(np.float64),
+                 flag.astype(np.int32), sc.frequency, sc.wavenumber, sc.planck_c1, sc.planck_c2,
+                 sc.band_c1, sc.band_c2, sc.cosmic_background_radiance, sc.solar_irradiance)
+        w.record(np.array([0], np.int32))  # antenna correction data absent
+        w.record(np.array([0], np.int32))  # NLTE correction data absent
+
+
+def read_spccoeff(path: str) -> SpcCoeff:
+    with open(path, "rb") as f:
+        r = RecordReader(f)
+        release, version = r.split(r.record(), [("i4", (2,))])[0]
+        if release != SPCCOEFF_RELEASE or version < 3:
+            raise IOError(f"SpcCoeff release/version {release}/{version} not supported")
+        (L,) = r.split(r.record(), [("i4", ())])
+        L = int(L)
+        sid, ids = r.split(r.record(), [("S", SL), ("i4", (3,))])
+        fields = r.split(r.record(), [("i4", (L,)), ("i4", (L,)), ("f8", (L,)), ("i4", (L,))]
+                         + [("f8", (L,))] * 8)
+    ch, pol, pang, flag, freq, wn, c1, c2, b1, b2, cb, si = fields
+    return SpcCoeff(sid, int(ids[0]), ch, freq, wn, c1, c2, b1, b2, cb, si, pol, pang, flag,
+                    int(ids[1]), int(ids[2]))

@@ -1,0 +1,397 @@
+"""Seeded synthetic profiles and coefficient tables for the benchmark workloads.
+
+No real coefficient files or profile sets are used: every input is generated
+here from the distributions below and written with the repository's own
+coefficient writers (``coefficients.py``), so the oracle and the GPU library
+read identical files.
+
+Profiles (all workloads): levels log-spaced from 0.005 hPa (the reference's
+``TOA_PRESSURE``, ``src/CRTM_Parameters.f90:157``) to the surface; temperature a
+US-standard lapse profile plus Gaussian noise; water vapour exponential with a
+2 km scale height (surface 5-20 g/kg); ozone a Chapman-shaped layer peaking
+near 10 hPa; CO2 400 +- 10 ppmv; CH4, N2O and CO near background values.
+Ocean surface with skin temperature U[270, 305] K, sensor zenith U[0, 60] deg.
+
+ODPS coefficients: for each channel and each active component a column
+optical depth is drawn log-uniformly; the component's layer optical depth at
+the reference profile is that column spread over layers by a physical shape
+(pressure-broadened dry air, water vapour, ozone, well-mixed trace gases).
+The leading predictor of each component carries that optical depth and the
+remaining predictors add small Gaussian perturbations, so layer optical depths
+span about 1e-4 to 2 and occasionally go negative (exercising the clamp).
+"""
+from __future__ import annotations
+
+import os
+from typing import Dict, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import coefficients as co
+from .structures import AtmosphereBatch, GeometryBatch, OptionsBatch, SurfaceBatch
+
+TOA_PRESSURE = 0.005
+SURFACE_PRESSURE = 1100.0
+C1_RADIATION = 1.191042722e-05   # 2hc^2 in mW/(m2.sr.cm-4)
+C2_RADIATION = 1.4387752         # hc/k in K.cm
+TSPACE = 2.7253                  # ``src/CRTM_Parameters.f90:173``
+
+# background mixing ratios (ppmv) and the water vapour floor (g/kg)
+BACKGROUND_PPMV = {co.CO2_ID: 400.0, co.N2O_ID: 0.32, co.CO_ID: 0.10, co.CH4_ID: 1.80}
+H2O_FLOOR = 3.0e-3
+
+
+def height_km(p: np.ndarray) -> np.ndarray:
+    return -7.0 * np.log(np.asarray(p) / 1013.25)
+
+
+def us_standard_temperature(z: np.ndarray) -> np.ndarray:
+    """Piecewise-linear US standard atmosphere temperature (K) at height z (km)."""
+    zs = np.array([0.0, 11.0, 20.0, 32.0, 47.0, 51.0, 71.0, 86.0, 200.0])
+    ts = np.array([288.15, 216.65, 216.65, 228.65, 270.65, 270.65, 214.65, 186.87, 186.87])
+    return np.interp(np.clip(z, 0.0, 200.0), zs, ts)
+
+
+def layer_mean_pressure(lev: np.ndarray) -> np.ndarray:
+    return (lev[..., 1:] - lev[..., :-1]) / np.log(lev[..., 1:] / lev[..., :-1])
+
+
+def h2o_profile(p: np.ndarray, q_sfc) -> np.ndarray:
+    q = np.asarray(q_sfc)[..., None] * np.exp(-np.clip(height_km(p), 0.0, None) / 2.0)
+    return np.maximum(q, H2O_FLOOR)
+
+
+def o3_profile(p: np.ndarray, amp) -> np.ndarray:
+    """Chapman layer in height with its peak at the 10 hPa height."""
+    x = (height_km(p) - height_km(10.0)) / 5.0
+    return np.asarray(amp)[..., None] * np.exp(1.0 - x - np.exp(-x)) + 0.03
+
+
+def ref_level_pressure(n_layers: int = 100) -> np.ndarray:
+    """The ODPS reference grid: p^(1/3.5) quadratic in the level index."""
+    s0, s1 = TOA_PRESSURE ** (1 / 3.5), SURFACE_PRESSURE ** (1 / 3.5)
+    x = np.arange(n_layers + 1) / n_layers
+    return (s0 + (s1 - s0) * (0.35 * x + 0.65 * x * x)) ** 3.5
+
+
+def absorber_set(group: int) -> Tuple[int, ...]:
+    return co.ABSORBER_ID_G[group]
+
+
+def _profile_absorber(aid: int, p: np.ndarray, rng, P: int, q_sfc, o3_amp) -> np.ndarray:
+    if aid == co.H2O_ID:
+        return h2o_profile(p, q_sfc)
+    if aid == co.O3_ID:
+        return o3_profile(p, o3_amp)
+    base = BACKGROUND_PPMV[aid]
+    if aid == co.CO2_ID:
+        col = base + rng.uniform(-10.0, 10.0, size=P)
+    else:
+        col = base * rng.uniform(0.9, 1.1, size=P)
+    return np.broadcast_to(col[:, None], p.shape) * (1.0 + 0.01 * rng.standard_normal(p.shape))
+
+
+def generate_profiles(n_profiles: int, n_layers, absorber_ids: Sequence[int], seed: int,
+                      p_sfc: float = SURFACE_PRESSURE):
+    """Profiles, ocean surfaces and view geometries.
+
+    ``n_layers`` is an int or a (P,) array for ragged batches.
+    Returns (AtmosphereBatch, SurfaceBatch, GeometryBatch).
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    P = n_profiles
+    nl = np.broadcast_to(np.asarray(n_layers, dtype=np.int32), (P,)).copy()
+    K = int(nl.max())
+    lev = np.zeros((P, K + 1))
+    for m in range(P):
+        n = int(nl[m])
+        lev[m, :n + 1] = np.geomspace(TOA_PRESSURE, p_sfc, n + 1)
+        lev[m, n + 1:] = p_sfc
+    lev_pad = lev.copy()
+    # padding levels past a short profile's surface keep positive thickness
+    for m in range(P):
+        n = int(nl[m])
+        if n < K:
+            lev_pad[m, n + 1:] = p_sfc * (1.0 + 0.01 * np.arange(1, K - n + 1))
+    lay = layer_mean_pressure(lev_pad)
+    temp = us_standard_temperature(height_km(lay)) + rng.normal(0.0, 5.0, size=lay.shape)
+    temp = np.clip(temp, 160.0, 340.0)
+    q_sfc = rng.uniform(5.0, 20.0, size=P)
+    o3_amp = rng.uniform(4.0, 9.0, size=P)
+    absorbers = np.stack([_profile_absorber(a, lay, rng, P, q_sfc, o3_amp)
+                          for a in absorber_ids], axis=1)
+    units = np.array([co.MASS_MIXING_RATIO_UNITS if a == co.H2O_ID else co.VOLUME_MIXING_RATIO_UNITS
+                      for a in absorber_ids], np.int32)
+    for m in range(P):
+        n = int(nl[m])
+        lev[m, n + 1:] = 0.0
+        lay[m, n:] = 0.0
+        temp[m, n:] = 0.0
+        absorbers[m, :, n:] = 0.0
+    atm = AtmosphereBatch(nl, lev, lay, temp, np.ascontiguousarray(absorbers),
+                          np.asarray(absorber_ids, np.int32), units)
+    sfc = SurfaceBatch.ocean(rng.uniform(270.0, 305.0, size=P))
+    geo = GeometryBatch.nadir_like(rng.uniform(0.0, 60.0, size=P))
+    return atm, sfc, geo
+
+
+# ---------------------------------------------------------------------------
+# Coefficients
+# ---------------------------------------------------------------------------
+
+def _ref_profile(group: int, lev: np.ndarray):
+    lay = layer_mean_pressure(lev)
+    T = us_standard_temperature(height_km(lay))
+    ab = []
+    for a in absorber_set(group):
+        if a == co.H2O_ID:
+            ab.append(h2o_profile(lay[None], np.array([10.0]))[0])
+        elif a == co.O3_ID:
+            ab.append(o3_profile(lay[None], np.array([6.0]))[0])
+        else:
+            ab.append(np.full(lay.shape, BACKGROUND_PPMV[a]))
+    return lay, T, np.stack(ab, axis=1)
+
+
+def predictors_numpy(group: int, T, A, Tref, Aref, lev, secang):
+    """Predictors X[..., k, i, j] of ``ODPS_Predictor.f90:645-1095`` for arrays
+    T (..., K), A (..., K, Jm); used only to scale synthetic coefficients."""
+    K = T.shape[-1]
+    pdp = np.empty(K)
+    pdp[0] = lev[0] * (lev[1] - lev[0])
+    pdp[1:] = lev[1:K] * (lev[1:K] - lev[0:K - 1])
+    Tz = np.cumsum(T, -1) / np.cumsum(Tref)
+    Tzp = np.cumsum(pdp * T, -1) / np.cumsum(pdp * Tref)
+    GAzp = np.cumsum(pdp[:, None] * A, -2) / np.cumsum(pdp[:, None] * Aref, 0)
+    GATzp = np.cumsum(pdp[:, None] * A * T[..., None], -2) / np.cumsum(pdp[:, None] * Aref * Tref[:, None], 0)
+    dT = T - Tref
+    t = T / Tref
+    t2 = t * t
+    dT2 = dT * np.abs(dT)
+    s = secang
+    R = A / Aref
+    nmax = max(co.N_PREDICTORS_G[group])
+    X = np.zeros(T.shape + (nmax, co.N_COMPONENTS_G[group]))
+    h2o = R[..., 0]
+    h2o_a = s * h2o
+    h2o_r = np.sqrt(h2o_a)
+    h2o_s = h2o_a * h2o_a
+    dry = [s + 0 * t, s * t, s * t2, t, s * s + 0 * t, t2, Tz]
+    for i, v in enumerate(dry):
+        X[..., i, 0] = v
+    if group == 3:
+        h2otz = h2o / GATzp[..., 0]
+        wet = [h2o_a / t, h2o_a / t * h2o, h2o_a / t2 * h2o / t2, h2o_a / t2, h2o_a / t2 * h2o,
+               h2o_a / t2 ** 2, h2o_a, h2o_a * dT, (s * GAzp[..., 0]) ** 2, s * GAzp[..., 0],
+               s + 0 * t, h2o_s * h2o_a, h2o_s * h2o_s, h2otz]
+        for i, v in enumerate(wet):
+            X[..., i, 1] = v
+        return X
+    o3 = R[..., 1]
+    co2 = R[..., 2]
+    o3_a = s * o3
+    o3_r = np.sqrt(o3_a)
+    g_o3 = GAzp[..., 1]
+    h2otz = h2o / GATzp[..., 0]
+    wco = [h2o_a / t, h2o_a / t * h2o, h2o_a / t2 * h2o / t2, h2o_a / t2, h2o_a / t2 * h2o,
+           h2o_a / t2 ** 2, h2o_a]
+    ozo = [o3_a, o3_a * dT, o3_a * o3 * g_o3, o3_a * o3_a, o3_a * g_o3, o3_a * np.sqrt(s * g_o3),
+           o3_r * dT, o3_r, o3_r * o3 / g_o3, s * g_o3, (s * g_o3) ** 2]
+    co2p = [s * t, s * t2, t, t2, s + 0 * t, s * co2, s * Tzp, (s * GAzp[..., 2]) ** 2, Tzp ** 3,
+            s * Tzp * np.sqrt(t)]
+    wlo = [h2o_a, h2o_a * dT, h2o_s, h2o_a * dT2, np.sqrt(h2o_r), h2o_s * h2o_a, h2o_r,
+           h2o_r * dT, h2o_s * h2o_s, h2otz, h2o_r * h2otz, (s * GAzp[..., 0]) ** 2,
+           s * GAzp[..., 0], s + 0 * t, s * co2]
+    for i, v in enumerate(wlo):
+        X[..., i, 1] = v
+    for i, v in enumerate(wco):
+        X[..., i, 2] = v
+    for i, v in enumerate(ozo):
+        X[..., i, 3] = v
+    for i, v in enumerate(co2p):
+        X[..., i, 4] = v
+    if group == 1:
+        n2o, co_, ch4 = R[..., 3], R[..., 4], R[..., 5]
+        n2o_a, co_a, ch4_a = s * n2o, s * co_, s * ch4
+        n2o_r, co_r, ch4_r = np.sqrt(n2o_a), np.sqrt(co_a), np.sqrt(ch4_a)
+        g_co, g_ch4, g_n2o = GAzp[..., 4], GAzp[..., 5], GAzp[..., 3]
+        co_ac = co_a * co_ / g_co
+        ch4_z = s * g_ch4
+        X[..., 10, 4] = co_a
+        X[..., 15, 1] = ch4_a
+        X[..., 16, 1] = ch4_a * ch4_a * dT
+        X[..., 17, 1] = co_a
+        cop = [co_a, co_a * dT, np.sqrt(co_r), co_r * dT, co_a * co_a, co_r, co_a * dT2, co_ac,
+               co_ac / co_r, co_ac * np.sqrt(g_co)]
+        ch4p = [ch4_a * dT, ch4_r, ch4_a * ch4_a, ch4_a, ch4 * dT, ch4_z, ch4_z ** 2, np.sqrt(ch4_r),
+                GATzp[..., 5], s * GATzp[..., 5], ch4_r * ch4 / g_ch4]
+        n2op = [n2o_a * dT, n2o_r, n2o * dT, n2o_a ** 0.25, n2o_a, s * g_n2o, s * GATzp[..., 3],
+                n2o_a * n2o_a, GATzp[..., 3], n2o_r * n2o / g_n2o, ch4_a, ch4_a * g_ch4, co_a,
+                co_a * s * g_co]
+        for i, v in enumerate(n2op):
+            X[..., i, 5] = v
+        for i, v in enumerate(cop):
+            X[..., i, 6] = v
+        for i, v in enumerate(ch4p):
+            X[..., i, 7] = v
+    return X
+
+
+# Probability that a component is active in a channel, and its column-OD range.
+_COMPONENT_RULES = {
+    # group: list over components of (probability, (lo, hi) column optical depth)
+    1: [(1.0, (0.005, 3.0)), (1.0, (0.001, 20.0)), (1.0, (0.001, 2.0)), (0.3, (0.01, 8.0)),
+        (0.5, (0.01, 30.0)), (0.2, (0.005, 2.0)), (0.15, (0.005, 2.0)), (0.2, (0.005, 2.0))],
+    2: [(1.0, (0.005, 3.0)), (0.8, (0.001, 15.0)), (0.5, (0.001, 1.5)), (0.3, (0.01, 6.0)),
+        (0.3, (0.01, 20.0))],
+    3: [(1.0, (0.005, 6.0)), (1.0, (0.001, 10.0))],
+}
+
+
+def _component_shapes(group: int, lev: np.ndarray, lay: np.ndarray, A: np.ndarray) -> np.ndarray:
+    """Fraction of each component's column optical depth in each reference layer."""
+    dp = np.diff(lev)
+    broad = np.sqrt(lay / SURFACE_PRESSURE)
+    J = co.N_COMPONENTS_G[group]
+    ids = absorber_set(group)
+    f = np.zeros((J, lay.size))
+    f[0] = dp * broad
+    if group == 3:
+        f[1] = dp * A[:, 0] * broad
+    else:
+        f[1] = dp * A[:, 0] * broad
+        f[2] = dp * A[:, 0] ** 2 * lay / SURFACE_PRESSURE
+        f[3] = dp * A[:, ids.index(co.O3_ID)]
+        f[4] = dp * broad
+        for j in range(5, J):
+            f[j] = dp * broad
+    return f / f.sum(axis=1, keepdims=True)
+
+
+def generate_odps(group: int, n_channels: int, seed: int, sensor_id: str, sensor_type: int,
+                  n_ref_layers: int = 100, max_predictors_per_channel: Optional[int] = None) -> co.ODPSCoeff:
+    """A synthetic ODPS TauCoeff for ``n_channels`` channels of predictor ``group``."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lev = ref_level_pressure(n_ref_layers)
+    lay, Tref, Aref = _ref_profile(group, lev)
+    K = n_ref_layers
+    J = co.N_COMPONENTS_G[group]
+    ncp = co.N_PREDICTORS_G[group]
+    # typical predictor values over sample states near the reference
+    ns = 48
+    srng = np.random.Generator(np.random.PCG64(seed + 7))
+    Ts = Tref[None] + srng.normal(0.0, 5.0, (ns, K))
+    As = Aref[None] * np.exp(srng.normal(0.0, 0.3, (ns, K, Aref.shape[1])))
+    sec = 1.0 / np.cos(np.deg2rad(30.0))
+    Xs = predictors_numpy(group, Ts, As, Tref, Aref, lev, sec)
+    x_mean = Xs.mean(axis=0)
+    x_rms = np.sqrt((Xs ** 2).mean(axis=0)) + 1e-30
+    shapes = _component_shapes(group, lev, lay, Aref)
+    rules = _COMPONENT_RULES[group]
+    npred = np.zeros((J, n_channels), np.int32)
+    pos = np.zeros((J, n_channels), np.int32)
+    blocks = []
+    cursor = 1
+    for l in range(n_channels):
+        budget = max_predictors_per_channel
+        for j in range(J):
+            prob, (lo, hi) = rules[j]
+            if j > 0 and rng.uniform() >= prob:
+                continue
+            n = int(rng.integers(max(1, ncp[j] - 4), ncp[j] + 1))
+            if budget is not None:
+                n = min(n, budget - (0 if j > 0 else 0))
+                if j == 0:
+                    n = min(ncp[0], budget)
+                if n <= 0:
+                    continue
+                budget -= n
+            col = np.exp(rng.uniform(np.log(lo), np.log(hi)))
+            od = col * shapes[j]
+            c = np.empty((n, K))
+            c[0] = od / x_mean[:, 0, j]
+            if n > 1:
+                c[1:] = (od[None, :] / x_rms[:, 1:n, j].T) * rng.normal(0.0, 0.05, (n - 1, K)) / np.sqrt(n - 1)
+            npred[j, l] = n
+            pos[j, l] = cursor
+            cursor += n * K
+            blocks.append(c.astype(np.float32).ravel())
+    cvec = np.concatenate(blocks) if blocks else np.zeros(0, np.float32)
+    ids = absorber_set(group)
+    amin = Aref * 0.001
+    amax = Aref * 50.0
+    for jj, a in enumerate(ids):
+        if a != co.H2O_ID:
+            amin[:, jj] = Aref[:, jj] * 0.02
+            amax[:, jj] = Aref[:, jj] * 20.0
+    return co.ODPSCoeff(group, sensor_id, sensor_type, np.arange(1, n_channels + 1, dtype=np.int32),
+                        lev, lay, Tref, Aref, amin, amax, npred, pos, cvec)
+
+
+def generate_spccoeff(sensor_id: str, sensor_type: int, n_channels: int, seed: int) -> co.SpcCoeff:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    L = n_channels
+    if sensor_type == co.MICROWAVE_SENSOR:
+        freq = np.sort(rng.uniform(23.0, 190.0, L))           # GHz
+        wn = freq / 29.9792458
+        b1 = np.zeros(L)
+        b2 = np.ones(L)
+    else:
+        wn = np.sort(rng.uniform(650.0, 2550.0, L))
+        freq = wn * 29.9792458
+        b1 = rng.uniform(0.0, 0.3, L)
+        b2 = rng.uniform(0.9995, 1.0, L)
+    c1 = C1_RADIATION * wn ** 3
+    c2 = C2_RADIATION * wn
+    cbr = np.zeros(L)
+    if sensor_type == co.MICROWAVE_SENSOR:
+        cbr = c1 / (np.exp(c2 / (b1 + b2 * TSPACE)) - 1.0)
+    return co.SpcCoeff(sensor_id, sensor_type, np.arange(1, L + 1, dtype=np.int32), freq, wn,
+                       c1, c2, b1, b2, cbr, np.zeros(L))
+
+
+# ---------------------------------------------------------------------------
+# Workloads
+# ---------------------------------------------------------------------------
+
+SENSORS = {
+    # sensor id: (group, channels, sensor type, seed)
+    "mwsynth_c22": (2, 22, co.MICROWAVE_SENSOR, 11),
+    "irsynth_c2211": (1, 2211, co.INFRARED_SENSOR, 12),
+    "mwsynth_c16": (3, 16, co.MICROWAVE_SENSOR, 13),
+    "irsynth_c616": (1, 616, co.INFRARED_SENSOR, 14),
+}
+
+
+def write_sensor_files(coeff_dir: str, sensor_id: str) -> None:
+    """Write ``<sensor>.TauCoeff.bin`` and ``<sensor>.SpcCoeff.bin`` if missing."""
+    os.makedirs(coeff_dir, exist_ok=True)
+    tau = os.path.join(coeff_dir, f"{sensor_id}.TauCoeff.bin")
+    spc = os.path.join(coeff_dir, f"{sensor_id}.SpcCoeff.bin")
+    if os.path.exists(tau) and os.path.exists(spc):
+        return
+    group, L, stype, seed = SENSORS[sensor_id]
+    budget = 20 if sensor_id == "mwsynth_c22" else None
+    tc = generate_odps(group, L, seed, sensor_id, stype, max_predictors_per_channel=budget)
+    sc = generate_spccoeff(sensor_id, stype, L, seed + 100)
+    co.write_odps(tau + ".tmp", tc)
+    co.write_spccoeff(spc + ".tmp", sc)
+    os.replace(tau + ".tmp", tau)
+    os.replace(spc + ".tmp", spc)
+
+
+def emissivity_for(sensor_type: int, n_profiles: int, n_channels: int, seed: int) -> np.ndarray:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    if sensor_type == co.MICROWAVE_SENSOR:
+        return rng.uniform(0.5, 0.7, (n_profiles, n_channels))
+    return rng.uniform(0.95, 0.99, (n_profiles, n_channels))
+
+
+def clear_sky_workload(sensor_id: str, n_profiles: int, n_layers, seed: int):
+    """Profiles + options for a clear-sky run of one synthetic sensor."""
+    group, L, stype, _ = SENSORS[sensor_id]
+    atm, sfc, geo = generate_profiles(n_profiles, n_layers, absorber_set(group)
+                                      if group != 2 or sensor_id != "mwsynth_c22"
+                                      else (co.H2O_ID, co.O3_ID), seed)
+    opt = OptionsBatch(emissivity=emissivity_for(stype, n_profiles, L, seed + 1))
+    return atm, sfc, geo, opt

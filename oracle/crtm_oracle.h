@@ -1,0 +1,84 @@
+/*
+ * CPU FP64 oracle for the CRTM ODPS + Emission forward / K-matrix / adjoint path.
+ *
+ * TEST INFRASTRUCTURE ONLY: this library is the checker for the GPU library,
+ * and the timed CPU baseline of bench.py.  Only tests/, __graft_entry__.smoke()
+ * and bench.py's CPU-baseline leg may load it.  It is never part of the
+ * product path.
+ *
+ * It restates, from the reference's Fortran behaviour, the routines named in
+ * crtm_oracle.c (each function cites the file:line it follows).
+ *
+ * Parity unpinned: the reference (Fortran 2003, netCDF-Fortran required) has
+ * no compiler in this environment and ships no numeric golden vectors for
+ * this path (its coefficient files and result files are Git-LFS stubs), so
+ * this oracle is pinned by known-answer cases, finite differences and
+ * tangent-linear/adjoint symmetry instead of by reference outputs.
+ *
+ * The batch layout is the one of include/crtm_gpu.h.
+ */
+#ifndef CRTM_ORACLE_H
+#define CRTM_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct or_handle_s or_handle;
+
+/* Load <dir>/<sensor_id>.TauCoeff.bin and .SpcCoeff.bin; returns NULL on error. */
+or_handle* or_init(const char* coeff_dir, const char* sensor_id);
+void or_destroy(or_handle* h);
+int or_n_channels(const or_handle* h);
+int or_n_ref_layers(const or_handle* h);
+int or_group(const or_handle* h);
+const char* or_last_error(void);
+
+typedef struct {
+  int n_profiles;
+  int max_layers;            /* stride of layer arrays                       */
+  const int* n_layers;       /* [P]                                          */
+  int n_absorbers;           /* user absorbers                               */
+  const int* absorber_id;    /* [Jabs]                                       */
+  const double* level_pressure; /* [P][max_layers+1]                         */
+  const double* pressure;       /* [P][max_layers]                           */
+  const double* temperature;    /* [P][max_layers]                           */
+  const double* absorber;       /* [P][Jabs][max_layers]                     */
+  const double* surface_land_coverage, *surface_water_coverage,
+              * surface_snow_coverage, *surface_ice_coverage;     /* [P] */
+  const double* surface_land_temperature, *surface_water_temperature,
+              * surface_snow_temperature, *surface_ice_temperature; /* [P] */
+  const double* sensor_zenith_angle;   /* [P] degrees */
+  const double* source_zenith_angle;   /* [P] degrees */
+  const double* surface_altitude;      /* [P] */
+  const double* emissivity;            /* [P][L] */
+} or_batch;
+
+/* Forward: radiance and brightness temperature [P][L]; layer_od [P][L][max_layers] optional. */
+int or_forward(const or_handle* h, const or_batch* b, double* radiance, double* bt,
+               double* layer_od, int n_threads);
+
+/* K-matrix with seed d(BT)=bt_k[P][L] (NULL: 1).  Outputs, overwritten:
+ * temperature_k [P][L][Kmax], absorber_k [P][L][Jabs][Kmax], water_temperature_k [P][L],
+ * surface_emissivity_k [P][L]; radiance/bt as in the forward. */
+int or_k_matrix(const or_handle* h, const or_batch* b, const double* bt_k,
+                double* radiance, double* bt, double* temperature_k, double* absorber_k,
+                double* water_temperature_k, double* surface_emissivity_k, int n_threads);
+
+/* Adjoint: like the K-matrix but summed over channels: temperature_ad [P][Kmax],
+ * absorber_ad [P][Jabs][Kmax], water_temperature_ad [P]. */
+int or_adjoint(const or_handle* h, const or_batch* b, const double* bt_ad,
+               double* radiance, double* bt, double* temperature_ad, double* absorber_ad,
+               double* water_temperature_ad, int n_threads);
+
+/* Tangent-linear BT for perturbations of T and absorbers (used by symmetry tests):
+ * temperature_tl [P][Kmax], absorber_tl [P][Jabs][Kmax], water_temperature_tl [P];
+ * bt_tl [P][L] out.  Computed by central differences of the forward model with step h. */
+int or_tangent_fd(const or_handle* hd, const or_batch* b, const double* temperature_tl,
+                  const double* absorber_tl, const double* water_temperature_tl, double step,
+                  double* bt_tl, int n_threads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,162 @@
+"""ctypes binding of the CPU FP64 oracle (test infrastructure only).
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
+this module; it is the checker, never the product.  Parity unpinned: see
+crtm_oracle.h.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+
+_dp = ct.POINTER(ct.c_double)
+_ip = ct.POINTER(ct.c_int)
+
+
+class OrBatch(ct.Structure):
+    _fields_ = [("n_profiles", ct.c_int), ("max_layers", ct.c_int), ("n_layers", _ip),
+                ("n_absorbers", ct.c_int), ("absorber_id", _ip),
+                ("level_pressure", _dp), ("pressure", _dp), ("temperature", _dp),
+                ("absorber", _dp),
+                ("surface_land_coverage", _dp), ("surface_water_coverage", _dp),
+                ("surface_snow_coverage", _dp), ("surface_ice_coverage", _dp),
+                ("surface_land_temperature", _dp), ("surface_water_temperature", _dp),
+                ("surface_snow_temperature", _dp), ("surface_ice_temperature", _dp),
+                ("sensor_zenith_angle", _dp), ("source_zenith_angle", _dp),
+                ("surface_altitude", _dp), ("emissivity", _dp)]
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "crtm_oracle.c")
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+        subprocess.run(["make", "-C", HERE, "-B", "liboracle.so"], check=True,
+                       stdout=subprocess.DEVNULL)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ct.CDLL(LIB)
+        L.or_init.restype = ct.c_void_p
+        L.or_init.argtypes = [ct.c_char_p, ct.c_char_p]
+        L.or_destroy.argtypes = [ct.c_void_p]
+        L.or_n_channels.argtypes = [ct.c_void_p]
+        L.or_last_error.restype = ct.c_char_p
+        L.or_forward.argtypes = [ct.c_void_p, ct.POINTER(OrBatch), _dp, _dp, _dp, ct.c_int]
+        L.or_k_matrix.argtypes = [ct.c_void_p, ct.POINTER(OrBatch), _dp, _dp, _dp, _dp, _dp, _dp,
+                                  _dp, ct.c_int]
+        L.or_adjoint.argtypes = [ct.c_void_p, ct.POINTER(OrBatch), _dp, _dp, _dp, _dp, _dp, _dp,
+                                 ct.c_int]
+        L.or_tangent_fd.argtypes = [ct.c_void_p, ct.POINTER(OrBatch), _dp, _dp, _dp, ct.c_double,
+                                    _dp, ct.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a, t=_dp):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+class Oracle:
+    """One sensor's coefficients, loaded by the oracle from the binary files."""
+
+    def __init__(self, coeff_dir: str, sensor_id: str):
+        L = lib()
+        self.h = L.or_init(coeff_dir.encode(), sensor_id.encode())
+        if not self.h:
+            raise IOError(L.or_last_error().decode())
+        self.n_channels = L.or_n_channels(self.h)
+
+    def close(self):
+        if self.h:
+            lib().or_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def _batch(self, atm, sfc, geo, opt):
+        keep = []
+
+        def c(a, dt=np.float64):
+            a = np.ascontiguousarray(a, dtype=dt)
+            keep.append(a)
+            return a
+        b = OrBatch()
+        b.n_profiles = atm.n_profiles
+        b.max_layers = atm.max_layers
+        b.n_layers = _p(c(atm.n_layers, np.int32), _ip)
+        b.n_absorbers = atm.n_absorbers
+        b.absorber_id = _p(c(atm.absorber_id, np.int32), _ip)
+        b.level_pressure = _p(c(atm.level_pressure))
+        b.pressure = _p(c(atm.pressure))
+        b.temperature = _p(c(atm.temperature))
+        b.absorber = _p(c(atm.absorber))
+        for f in ("land_coverage", "water_coverage", "snow_coverage", "ice_coverage",
+                  "land_temperature", "water_temperature", "snow_temperature", "ice_temperature"):
+            setattr(b, "surface_" + f, _p(c(getattr(sfc, f))))
+        b.sensor_zenith_angle = _p(c(geo.sensor_zenith_angle))
+        b.source_zenith_angle = _p(c(geo.source_zenith_angle))
+        b.surface_altitude = _p(c(geo.surface_altitude))
+        b.emissivity = _p(c(opt.emissivity))
+        return b, keep
+
+    def forward(self, atm, sfc, geo, opt, n_threads: int = 1, layer_od: bool = False):
+        P, L, K = atm.n_profiles, self.n_channels, atm.max_layers
+        b, keep = self._batch(atm, sfc, geo, opt)
+        rad = np.zeros((P, L))
+        bt = np.zeros((P, L))
+        od = np.zeros((P, L, K)) if layer_od else None
+        st = lib().or_forward(self.h, ct.byref(b), _p(rad), _p(bt), _p(od), n_threads)
+        if st:
+            raise RuntimeError(lib().or_last_error().decode())
+        return (rad, bt, od) if layer_od else (rad, bt)
+
+    def k_matrix(self, atm, sfc, geo, opt, bt_k=None, n_threads: int = 1):
+        P, L, K, J = atm.n_profiles, self.n_channels, atm.max_layers, atm.n_absorbers
+        b, keep = self._batch(atm, sfc, geo, opt)
+        seed = None if bt_k is None else np.ascontiguousarray(bt_k, np.float64)
+        rad, bt = np.zeros((P, L)), np.zeros((P, L))
+        tk, ak = np.zeros((P, L, K)), np.zeros((P, L, J, K))
+        tsk, ek = np.zeros((P, L)), np.zeros((P, L))
+        st = lib().or_k_matrix(self.h, ct.byref(b), _p(seed), _p(rad), _p(bt), _p(tk), _p(ak),
+                               _p(tsk), _p(ek), n_threads)
+        if st:
+            raise RuntimeError(lib().or_last_error().decode())
+        return dict(radiance=rad, bt=bt, temperature_k=tk, absorber_k=ak,
+                    water_temperature_k=tsk, surface_emissivity_k=ek)
+
+    def adjoint(self, atm, sfc, geo, opt, bt_ad, n_threads: int = 1):
+        P, L, K, J = atm.n_profiles, self.n_channels, atm.max_layers, atm.n_absorbers
+        b, keep = self._batch(atm, sfc, geo, opt)
+        seed = np.ascontiguousarray(bt_ad, np.float64)
+        rad, bt = np.zeros((P, L)), np.zeros((P, L))
+        ta, aa, wa = np.zeros((P, K)), np.zeros((P, J, K)), np.zeros(P)
+        st = lib().or_adjoint(self.h, ct.byref(b), _p(seed), _p(rad), _p(bt), _p(ta), _p(aa),
+                              _p(wa), n_threads)
+        if st:
+            raise RuntimeError(lib().or_last_error().decode())
+        return dict(radiance=rad, bt=bt, temperature_ad=ta, absorber_ad=aa, water_temperature_ad=wa)
+
+    def tangent_fd(self, atm, sfc, geo, opt, t_tl, a_tl, ts_tl, step=1e-4, n_threads: int = 1):
+        P, L = atm.n_profiles, self.n_channels
+        b, keep = self._batch(atm, sfc, geo, opt)
+        t_tl = np.ascontiguousarray(t_tl, np.float64)
+        a_tl = np.ascontiguousarray(a_tl, np.float64)
+        ts_tl = np.ascontiguousarray(ts_tl, np.float64)
+        out = np.zeros((P, L))
+        st = lib().or_tangent_fd(self.h, ct.byref(b), _p(t_tl), _p(a_tl), _p(ts_tl), step, _p(out),
+                                 n_threads)
+        if st:
+            raise RuntimeError(lib().or_last_error().decode())
+        return out
