@@ -1,0 +1,375 @@
+"""Python host API over the C-ABI (include/crtm_gpu.h).
+
+Mirrors the reference's public interface for this path:
+
+* ``CRTM_Init`` / ``CRTM_Destroy``          (src/CRTM_LifeCycle.f90:520, :1131)
+* ``CRTM_Forward``                          (src/CRTM_Forward_Module.f90:229-245)
+* ``CRTM_K_Matrix``                         (src/CRTM_K_Matrix_Module.f90:300-322)
+* ``CRTM_Adjoint``                          (src/CRTM_Adjoint_Module.f90:299-309)
+
+Each call returns the reference's integer status (SUCCESS=0, FAILURE=3) and
+fills caller-provided output objects, as the Fortran routines do.  The
+``CRTM`` class underneath offers the same calls on numpy arrays (host
+buffers, copies inside the call) and on torch CUDA tensors (device-resident,
+no copies).
+
+The GPU library is required: importing succeeds without it, but every call
+raises if ``libcrtm_gb300.so`` is missing or no CUDA device is present.
+There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import dataclasses
+import os
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from .structures import (AtmosphereBatch, GeometryBatch, KMatrixBatch, OptionsBatch,
+                         RTSolutionBatch, SurfaceBatch)
+
+SUCCESS, INFORMATION, WARNING, FAILURE = 0, 1, 2, 3
+FP64, MIXED = 0, 1
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libcrtm_gb300.so")
+
+_dp = ct.POINTER(ct.c_double)
+_ip = ct.POINTER(ct.c_int)
+
+
+class CBatch(ct.Structure):
+    _fields_ = [("n_profiles", ct.c_int), ("max_layers", ct.c_int), ("n_layers", ct.c_void_p),
+                ("n_absorbers", ct.c_int), ("absorber_id", ct.c_void_p),
+                ("level_pressure", ct.c_void_p), ("pressure", ct.c_void_p),
+                ("temperature", ct.c_void_p), ("absorber", ct.c_void_p),
+                ("land_coverage", ct.c_void_p), ("water_coverage", ct.c_void_p),
+                ("snow_coverage", ct.c_void_p), ("ice_coverage", ct.c_void_p),
+                ("land_temperature", ct.c_void_p), ("water_temperature", ct.c_void_p),
+                ("snow_temperature", ct.c_void_p), ("ice_temperature", ct.c_void_p),
+                ("sensor_zenith_angle", ct.c_void_p), ("source_zenith_angle", ct.c_void_p),
+                ("surface_altitude", ct.c_void_p), ("emissivity", ct.c_void_p)]
+
+
+class CRTSolution(ct.Structure):
+    _fields_ = [("radiance", ct.c_void_p), ("brightness_temperature", ct.c_void_p),
+                ("status", ct.c_void_p)]
+
+
+class CKMatrix(ct.Structure):
+    _fields_ = [("temperature", ct.c_void_p), ("absorber", ct.c_void_p),
+                ("water_temperature", ct.c_void_p), ("surface_emissivity", ct.c_void_p)]
+
+
+class CAdjoint(ct.Structure):
+    _fields_ = [("temperature", ct.c_void_p), ("absorber", ct.c_void_p),
+                ("water_temperature", ct.c_void_p)]
+
+
+_lib = None
+
+
+def library() -> ct.CDLL:
+    """Load the GPU library; raises if it is missing (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"GPU library not built: {LIB_PATH} (run crtmv3_gb300.build.build())")
+    L = ct.CDLL(LIB_PATH)
+    L.crtm_gpu_init.argtypes = [ct.c_char_p, ct.c_int, ct.POINTER(ct.c_char_p), ct.POINTER(ct.c_void_p)]
+    L.crtm_gpu_destroy.argtypes = [ct.c_void_p]
+    L.crtm_gpu_n_channels.argtypes = [ct.c_void_p, ct.c_int]
+    L.crtm_gpu_set_precision.argtypes = [ct.c_void_p, ct.c_int]
+    L.crtm_gpu_forward.argtypes = [ct.c_void_p, ct.c_int, ct.POINTER(CBatch), ct.POINTER(CRTSolution)]
+    L.crtm_gpu_k_matrix.argtypes = [ct.c_void_p, ct.c_int, ct.POINTER(CBatch), ct.c_void_p,
+                                    ct.POINTER(CKMatrix), ct.POINTER(CRTSolution)]
+    L.crtm_gpu_adjoint.argtypes = [ct.c_void_p, ct.c_int, ct.POINTER(CBatch), ct.c_void_p,
+                                   ct.POINTER(CAdjoint), ct.POINTER(CRTSolution)]
+    L.crtm_gpu_forward_device.argtypes = [ct.c_void_p, ct.c_int, ct.POINTER(CBatch),
+                                          ct.POINTER(CRTSolution), ct.c_void_p]
+    L.crtm_gpu_k_matrix_device.argtypes = [ct.c_void_p, ct.c_int, ct.POINTER(CBatch), ct.c_void_p,
+                                           ct.POINTER(CKMatrix), ct.POINTER(CRTSolution), ct.c_void_p]
+    L.crtm_gpu_adjoint_device.argtypes = [ct.c_void_p, ct.c_int, ct.POINTER(CBatch), ct.c_void_p,
+                                          ct.POINTER(CAdjoint), ct.POINTER(CRTSolution), ct.c_void_p]
+    L.crtm_gpu_last_error.argtypes = [ct.c_void_p, ct.c_char_p, ct.c_int]
+    L.crtm_gpu_launch_count.argtypes = [ct.c_void_p]
+    L.crtm_gpu_launch_count.restype = ct.c_longlong
+    _lib = L
+    return L
+
+
+def _addr(a) -> Optional[int]:
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()   # torch tensor
+
+
+class CRTM:
+    """One library handle: the coefficient tables of a list of sensors."""
+
+    def __init__(self, sensor_ids: Sequence[str], coeff_path: str, precision: int = FP64):
+        L = library()
+        h = ct.c_void_p()
+        ids = (ct.c_char_p * len(sensor_ids))(*[s.encode() for s in sensor_ids])
+        rc = L.crtm_gpu_init(coeff_path.encode(), len(sensor_ids), ids, ct.byref(h))
+        if rc != SUCCESS:
+            raise RuntimeError("crtm_gpu_init: " + self._err(None))
+        self.h = h
+        self.sensor_ids = list(sensor_ids)
+        self.n_channels = [L.crtm_gpu_n_channels(h, i) for i in range(len(sensor_ids))]
+        self.set_precision(precision)
+
+    @staticmethod
+    def _err(h) -> str:
+        L = library()
+        buf = ct.create_string_buffer(2048)
+        L.crtm_gpu_last_error(h, buf, 2048)
+        return buf.value.decode(errors="replace")
+
+    def error(self) -> str:
+        return self._err(self.h)
+
+    def set_precision(self, precision: int) -> None:
+        if library().crtm_gpu_set_precision(self.h, precision) != SUCCESS:
+            raise ValueError(self.error())
+        self.precision = precision
+
+    def launch_count(self) -> int:
+        return int(library().crtm_gpu_launch_count(self.h))
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            library().crtm_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------------
+    # host (numpy) calls
+    # ------------------------------------------------------------------
+    def _cbatch(self, atm: AtmosphereBatch, sfc: SurfaceBatch, geo: GeometryBatch,
+                opt: OptionsBatch, keep: list) -> CBatch:
+        def c(a, dt=np.float64):
+            a = np.ascontiguousarray(a, dtype=dt)
+            keep.append(a)
+            return a.ctypes.data
+        b = CBatch()
+        b.n_profiles = atm.n_profiles
+        b.max_layers = atm.max_layers
+        b.n_layers = c(atm.n_layers, np.int32)
+        b.n_absorbers = atm.n_absorbers
+        b.absorber_id = c(atm.absorber_id, np.int32)
+        b.level_pressure = c(atm.level_pressure)
+        b.pressure = c(atm.pressure)
+        b.temperature = c(atm.temperature)
+        b.absorber = c(atm.absorber)
+        for f in ("land_coverage", "water_coverage", "snow_coverage", "ice_coverage",
+                  "land_temperature", "water_temperature", "snow_temperature", "ice_temperature"):
+            setattr(b, f, c(getattr(sfc, f)))
+        b.sensor_zenith_angle = c(geo.sensor_zenith_angle)
+        b.source_zenith_angle = c(geo.source_zenith_angle)
+        b.surface_altitude = c(geo.surface_altitude)
+        if opt is None or opt.emissivity is None:
+            raise ValueError("Options.emissivity is required (Use_Emissivity path)")
+        b.emissivity = c(opt.emissivity)
+        return b
+
+    def _check(self, rc: int) -> None:
+        if rc != SUCCESS:
+            raise RuntimeError(self.error())
+
+    def forward(self, atm, sfc, geo, opt, sensor: int = 0) -> RTSolutionBatch:
+        P, L = atm.n_profiles, self.n_channels[sensor]
+        keep: list = []
+        b = self._cbatch(atm, sfc, geo, opt, keep)
+        rts = RTSolutionBatch(np.zeros((P, L)), np.zeros((P, L)), status=np.zeros(P, np.int32))
+        cr = CRTSolution(rts.radiance.ctypes.data, rts.brightness_temperature.ctypes.data,
+                         rts.status.ctypes.data)
+        self._check(library().crtm_gpu_forward(self.h, sensor, ct.byref(b), ct.byref(cr)))
+        return rts
+
+    def k_matrix(self, atm, sfc, geo, opt, bt_k=None, sensor: int = 0):
+        P, L, K, J = atm.n_profiles, self.n_channels[sensor], atm.max_layers, atm.n_absorbers
+        keep: list = []
+        b = self._cbatch(atm, sfc, geo, opt, keep)
+        seed = None if bt_k is None else np.ascontiguousarray(bt_k, np.float64)
+        rts = RTSolutionBatch(np.zeros((P, L)), np.zeros((P, L)), status=np.zeros(P, np.int32))
+        km = KMatrixBatch(np.zeros((P, L, K)), np.zeros((P, L, J, K)), np.zeros((P, L)), np.zeros((P, L)))
+        cr = CRTSolution(rts.radiance.ctypes.data, rts.brightness_temperature.ctypes.data,
+                         rts.status.ctypes.data)
+        ck = CKMatrix(km.temperature.ctypes.data, km.absorber.ctypes.data,
+                      km.water_temperature.ctypes.data, km.surface_emissivity.ctypes.data)
+        self._check(library().crtm_gpu_k_matrix(self.h, sensor, ct.byref(b), _addr(seed),
+                                                ct.byref(ck), ct.byref(cr)))
+        return km, rts
+
+    def adjoint(self, atm, sfc, geo, opt, bt_ad, sensor: int = 0):
+        P, L, K, J = atm.n_profiles, self.n_channels[sensor], atm.max_layers, atm.n_absorbers
+        keep: list = []
+        b = self._cbatch(atm, sfc, geo, opt, keep)
+        seed = np.ascontiguousarray(bt_ad, np.float64)
+        rts = RTSolutionBatch(np.zeros((P, L)), np.zeros((P, L)), status=np.zeros(P, np.int32))
+        out = dict(temperature=np.zeros((P, K)), absorber=np.zeros((P, J, K)), water_temperature=np.zeros(P))
+        cr = CRTSolution(rts.radiance.ctypes.data, rts.brightness_temperature.ctypes.data,
+                         rts.status.ctypes.data)
+        ca = CAdjoint(out["temperature"].ctypes.data, out["absorber"].ctypes.data,
+                      out["water_temperature"].ctypes.data)
+        self._check(library().crtm_gpu_adjoint(self.h, sensor, ct.byref(b), seed.ctypes.data,
+                                               ct.byref(ca), ct.byref(cr)))
+        return out, rts
+
+    # ------------------------------------------------------------------
+    # device-resident (torch CUDA tensors) calls
+    # ------------------------------------------------------------------
+    def device_batch(self, dev: dict, absorber_id: np.ndarray) -> tuple:
+        """``dev``: dict of torch CUDA tensors with the batch fields (float64 /
+        int32 n_layers).  absorber_id stays on the host."""
+        keep = [np.ascontiguousarray(absorber_id, np.int32)]
+        b = CBatch()
+        P, K = dev["temperature"].shape
+        b.n_profiles = P
+        b.max_layers = K
+        b.n_layers = dev["n_layers"].data_ptr()
+        b.n_absorbers = int(keep[0].shape[0])
+        b.absorber_id = keep[0].ctypes.data
+        for f in ("level_pressure", "pressure", "temperature", "absorber", "land_coverage",
+                  "water_coverage", "snow_coverage", "ice_coverage", "land_temperature",
+                  "water_temperature", "snow_temperature", "ice_temperature",
+                  "sensor_zenith_angle", "source_zenith_angle", "surface_altitude", "emissivity"):
+            t = dev.get(f)
+            setattr(b, f, None if t is None else t.data_ptr())
+        return b, keep
+
+    def k_matrix_device(self, b: CBatch, out: dict, seed=None, sensor: int = 0, stream=None) -> None:
+        cr = CRTSolution(out["radiance"].data_ptr(), out["bt"].data_ptr(),
+                         _addr(out.get("status")))
+        ck = CKMatrix(out["temperature_k"].data_ptr(), out["absorber_k"].data_ptr(),
+                      out["water_temperature_k"].data_ptr(), out["surface_emissivity_k"].data_ptr())
+        self._check(library().crtm_gpu_k_matrix_device(self.h, sensor, ct.byref(b), _addr(seed),
+                                                       ct.byref(ck), ct.byref(cr), stream))
+
+    def forward_device(self, b: CBatch, out: dict, sensor: int = 0, stream=None) -> None:
+        cr = CRTSolution(out["radiance"].data_ptr(), out["bt"].data_ptr(), _addr(out.get("status")))
+        self._check(library().crtm_gpu_forward_device(self.h, sensor, ct.byref(b), ct.byref(cr), stream))
+
+    def adjoint_device(self, b: CBatch, seed, out: dict, sensor: int = 0, stream=None) -> None:
+        cr = CRTSolution(out["radiance"].data_ptr(), out["bt"].data_ptr(), _addr(out.get("status")))
+        ca = CAdjoint(out["temperature_ad"].data_ptr(), out["absorber_ad"].data_ptr(),
+                      out["water_temperature_ad"].data_ptr())
+        self._check(library().crtm_gpu_adjoint_device(self.h, sensor, ct.byref(b), seed.data_ptr(),
+                                                      ct.byref(ca), ct.byref(cr), stream))
+
+
+# ---------------------------------------------------------------------------
+# Reference-named entry points
+# ---------------------------------------------------------------------------
+
+@dataclasses.dataclass
+class ChannelInfo:
+    """CRTM_ChannelInfo_type (src/ChannelInfo/CRTM_ChannelInfo_Define.f90:70-85), reduced to
+    what this path needs: the sensor, its index in the handle and its channel count."""
+    sensor_id: str
+    sensor_index: int
+    n_channels: int
+    handle: CRTM
+
+
+def CRTM_Init(sensor_ids: Sequence[str], channel_info: List[ChannelInfo], file_path: str = ".",
+              precision: int = FP64) -> int:
+    """CRTM_Init: load the coefficients of ``sensor_ids`` and fill ``channel_info``."""
+    try:
+        h = CRTM(sensor_ids, file_path, precision)
+    except RuntimeError as e:
+        print(f"CRTM_Init(FAILURE): {e}")
+        return FAILURE
+    channel_info.clear()
+    for i, s in enumerate(sensor_ids):
+        channel_info.append(ChannelInfo(s, i, h.n_channels[i], h))
+    return SUCCESS
+
+
+def CRTM_Destroy(channel_info: List[ChannelInfo]) -> int:
+    handles = {id(ci.handle): ci.handle for ci in channel_info}
+    for h in handles.values():
+        h.close()
+    channel_info.clear()
+    return SUCCESS
+
+
+def CRTM_Forward(atmosphere: AtmosphereBatch, surface: SurfaceBatch, geometry: GeometryBatch,
+                 channel_info: List[ChannelInfo], rts: List[RTSolutionBatch],
+                 options: Optional[OptionsBatch] = None) -> int:
+    """CRTM_Forward.  ``rts`` receives one RTSolutionBatch per sensor in ChannelInfo order.
+    ``options.emissivity`` is (P, total channels) over all sensors."""
+    rts.clear()
+    off = 0
+    for ci in channel_info:
+        opt = _sensor_options(options, off, ci.n_channels)
+        try:
+            rts.append(ci.handle.forward(atmosphere, surface, geometry, opt, ci.sensor_index))
+        except RuntimeError as e:
+            print(f"CRTM_Forward(FAILURE): {e}")
+            return FAILURE
+        off += ci.n_channels
+    return SUCCESS
+
+
+def CRTM_K_Matrix(atmosphere, surface, rts_k: Optional[Sequence[np.ndarray]], geometry,
+                  channel_info: List[ChannelInfo], atmosphere_k: List[KMatrixBatch],
+                  rts: List[RTSolutionBatch], options: Optional[OptionsBatch] = None) -> int:
+    """CRTM_K_Matrix.  ``rts_k[i]`` is the (P, L_i) brightness-temperature seed of sensor i
+    (None: 1); ``atmosphere_k`` receives the K-matrix per sensor (the surface Jacobians
+    are in its water_temperature / surface_emissivity fields)."""
+    atmosphere_k.clear()
+    rts.clear()
+    off = 0
+    for i, ci in enumerate(channel_info):
+        opt = _sensor_options(options, off, ci.n_channels)
+        seed = None if rts_k is None else rts_k[i]
+        try:
+            km, r = ci.handle.k_matrix(atmosphere, surface, geometry, opt, seed, ci.sensor_index)
+        except RuntimeError as e:
+            print(f"CRTM_K_Matrix(FAILURE): {e}")
+            return FAILURE
+        atmosphere_k.append(km)
+        rts.append(r)
+        off += ci.n_channels
+    return SUCCESS
+
+
+def CRTM_Adjoint(atmosphere, surface, rts_ad: Sequence[np.ndarray], geometry,
+                 channel_info: List[ChannelInfo], atmosphere_ad: dict, rts: List[RTSolutionBatch],
+                 options: Optional[OptionsBatch] = None) -> int:
+    """CRTM_Adjoint: adjoints summed over the channels of all sensors into ``atmosphere_ad``."""
+    rts.clear()
+    off = 0
+    P, K, J = atmosphere.n_profiles, atmosphere.max_layers, atmosphere.n_absorbers
+    tot = dict(temperature=np.zeros((P, K)), absorber=np.zeros((P, J, K)), water_temperature=np.zeros(P))
+    for i, ci in enumerate(channel_info):
+        opt = _sensor_options(options, off, ci.n_channels)
+        try:
+            out, r = ci.handle.adjoint(atmosphere, surface, geometry, opt, rts_ad[i], ci.sensor_index)
+        except RuntimeError as e:
+            print(f"CRTM_Adjoint(FAILURE): {e}")
+            return FAILURE
+        for k in tot:
+            tot[k] += out[k]
+        rts.append(r)
+        off += ci.n_channels
+    atmosphere_ad.clear()
+    atmosphere_ad.update(tot)
+    return SUCCESS
+
+
+def _sensor_options(options: Optional[OptionsBatch], off: int, n: int) -> OptionsBatch:
+    if options is None or options.emissivity is None:
+        raise ValueError("Options%Emissivity is required for this path (Use_Emissivity)")
+    return OptionsBatch(emissivity=np.ascontiguousarray(options.emissivity[:, off:off + n]))

@@ -1,0 +1,696 @@
+// Host runtime and C-ABI of the GB300 CRTM forward / K-matrix / adjoint library.
+//
+// crtm_gpu_init reads each sensor's SpcCoeff and ODPS TauCoeff binary files
+// (the reference's record layouts: SpcCoeff_Binary_IO.f90:660-711,
+// ODPS_Binary_IO.f90:586-900), builds the device tables once and keeps them
+// for the life of the handle (the reference keeps them in module globals
+// SC/TC after CRTM_Init, src/Coefficients/CRTM_SharedData.f90).  Each call
+// then runs the chunked kernel pipeline of odps_kernels.cuh on the handle's
+// stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/crtm_gpu.h"
+#include "odps_kernels.cuh"
+
+using namespace crtm;
+
+namespace {
+
+thread_local std::string g_init_error;
+
+// ---------------------------------------------------------------------------
+// Fortran sequential record files
+// ---------------------------------------------------------------------------
+struct Records {
+  std::vector<unsigned char> buf;
+  size_t off = 0;
+  bool swap = false;
+
+  static uint32_t bswap(uint32_t v) {
+    return (v >> 24) | ((v >> 8) & 0xff00u) | ((v << 8) & 0xff0000u) | (v << 24);
+  }
+  uint32_t u32(size_t at) const {
+    uint32_t v;
+    memcpy(&v, buf.data() + at, 4);
+    return swap ? bswap(v) : v;
+  }
+  bool open(const std::string& path, std::string& err) {
+    FILE* f = fopen(path.c_str(), "rb");
+    if (!f) { err = "cannot open " + path; return false; }
+    fseek(f, 0, SEEK_END);
+    long n = ftell(f);
+    fseek(f, 0, SEEK_SET);
+    buf.resize(n > 0 ? (size_t)n : 0);
+    bool ok = n > 0 && fread(buf.data(), 1, buf.size(), f) == buf.size();
+    fclose(f);
+    if (!ok || buf.size() < 12) { err = "cannot read " + path; return false; }
+    for (int s = 0; s < 2; s++) {
+      swap = s == 1;
+      if (u32(0) == 4 && u32(4) == 123456789u && u32(8) == 4) { off = 12; return true; }
+    }
+    err = path + ": not a CRTM binary file (magic number)";
+    return false;
+  }
+  // next record; returns false on corruption
+  bool next(const unsigned char*& data, size_t& len) {
+    if (off + 4 > buf.size()) return false;
+    uint32_t a = u32(off);
+    if (off + 8 + (size_t)a > buf.size() || u32(off + 4 + a) != a) return false;
+    data = buf.data() + off + 4;
+    len = a;
+    off += 8 + (size_t)a;
+    return true;
+  }
+  int i32(const unsigned char* p) const {
+    uint32_t v;
+    memcpy(&v, p, 4);
+    return (int)(swap ? bswap(v) : v);
+  }
+  double f64(const unsigned char* p) const {
+    unsigned char b[8];
+    memcpy(b, p, 8);
+    if (swap) std::reverse(b, b + 8);
+    double d;
+    memcpy(&d, b, 8);
+    return d;
+  }
+  float f32(const unsigned char* p) const {
+    uint32_t v;
+    memcpy(&v, p, 4);
+    if (swap) v = bswap(v);
+    float f;
+    memcpy(&f, &v, 4);
+    return f;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Sensor coefficients: host copies and device tables
+// ---------------------------------------------------------------------------
+struct Sensor {
+  std::string id;
+  int group = 0, K = 0, J = 0, Jm = 0, L = 0, sensor_type = 0, h2o_idx = 0, NS = 0;
+  std::vector<int> absorber_id;
+  std::vector<double> ref_lev, ref_p, ref_t, ref_a, min_a, max_a;  // [Jm][K] for absorbers
+  std::vector<double> c1, c2, b1, b2, cbr;
+  // device
+  float* d_C = nullptr;          // [K][NS][L]
+  unsigned* d_cmask = nullptr;   // [L]
+  double* d_tab = nullptr;       // concatenated tables
+  double* d_spec = nullptr;      // c1,c2,b1,b2,cbr [5][L]
+  SensorTables tables{};
+  SpecView spec{};
+};
+
+bool load_sensor(const std::string& dir, const std::string& id, Sensor& s, std::string& err) {
+  s.id = id;
+  Records r;
+  const unsigned char* d;
+  size_t len;
+  std::string tau = dir + "/" + id + ".TauCoeff.bin";
+  if (!r.open(tau, err)) return false;
+  auto bad = [&](const char* what) { err = tau + ": " + what; return false; };
+  if (!r.next(d, len) || len != 8) return bad("corrupt Release/Version record");
+  if (r.i32(d) != 2) return bad("unsupported ODPS release");
+  if (!r.next(d, len) || len != 4) return bad("corrupt Algorithm record");
+  if (r.i32(d) != 2) return bad("TauCoeff algorithm is not ODPS");
+  if (!r.next(d, len) || len != 28) return bad("corrupt dimension record");
+  int dims[7];
+  for (int i = 0; i < 7; i++) dims[i] = r.i32(d + 4 * i);
+  s.K = dims[0]; s.J = dims[1]; s.Jm = dims[2]; s.L = dims[3];
+  const long long n_coeffs = dims[4];
+  if (dims[6] > 0) return bad("ODPS OPTRAN coefficients are not supported by this build");
+  if (s.K < 2 || s.K > MAX_LAYERS || s.L < 1) return bad("dimensions out of range");
+  if (!r.next(d, len) || len != 4) return bad("corrupt Group record");
+  s.group = r.i32(d);
+  if (s.group < 1 || s.group > 3 || group_j(s.group) != s.J || group_jm(s.group) != s.Jm)
+    return bad("unsupported ODPS predictor group");
+  s.NS = group_ns(s.group);
+  if (!r.next(d, len) || len != 32) return bad("corrupt sensor-id record");
+  s.sensor_type = r.i32(d + 28);
+  if (!r.next(d, len) || len != 4u * s.L) return bad("corrupt channel record");
+  if (!r.next(d, len) || len != 4u * s.J) return bad("corrupt component record");
+  if (!r.next(d, len) || len != 4u * s.Jm) return bad("corrupt absorber record");
+  s.absorber_id.resize(s.Jm);
+  for (int j = 0; j < s.Jm; j++) s.absorber_id[j] = r.i32(d + 4 * j);
+  const size_t nref = (size_t)(s.K + 1) + 2 * s.K + 3 * (size_t)s.K * s.Jm;
+  if (!r.next(d, len) || len != 8 * nref) return bad("corrupt reference-profile record");
+  size_t o = 0;
+  auto take = [&](std::vector<double>& v, size_t n) {
+    v.resize(n);
+    for (size_t i = 0; i < n; i++) v[i] = r.f64(d + 8 * (o + i));
+    o += n;
+  };
+  take(s.ref_lev, s.K + 1);
+  take(s.ref_p, s.K);
+  take(s.ref_t, s.K);
+  take(s.ref_a, (size_t)s.K * s.Jm);
+  take(s.min_a, (size_t)s.K * s.Jm);
+  take(s.max_a, (size_t)s.K * s.Jm);
+  for (int k = 0; k < s.K; k++)
+    if (!(s.ref_lev[k + 1] > s.ref_lev[k]) || !(s.ref_p[k] > 0.0) || !(s.ref_t[k] > 0.0))
+      return bad("reference profile is not monotone / positive");
+  if (!r.next(d, len) || len != 8u * s.J * s.L) return bad("corrupt n_Predictors record");
+  std::vector<int> npred((size_t)s.J * s.L), pos((size_t)s.J * s.L);
+  for (size_t i = 0; i < npred.size(); i++) {
+    npred[i] = r.i32(d + 4 * i);
+    pos[i] = r.i32(d + 4 * (npred.size() + i));
+  }
+  std::vector<float> C(n_coeffs > 0 ? (size_t)n_coeffs : 0);
+  if (n_coeffs > 0) {
+    if (!r.next(d, len) || len != 4u * (size_t)n_coeffs) return bad("corrupt coefficient record");
+    for (long long i = 0; i < n_coeffs; i++) C[i] = r.f32(d + 4 * i);
+  }
+  // dense coefficient array [K][NS][L] and component masks
+  const int K = s.K, L = s.L, NS = s.NS;
+  std::vector<float> Cd((size_t)K * NS * L, 0.0f);
+  std::vector<unsigned> cmask(L, 0u);
+  static const int npmax[3][8] = {{7, 18, 7, 11, 11, 14, 10, 11}, {7, 15, 7, 11, 10}, {7, 14}};
+  for (int l = 0; l < L; l++) {
+    int off = 0;
+    for (int j = 0; j < s.J; j++) {
+      const int np = npred[(size_t)l * s.J + j];
+      const int mx = npmax[s.group - 1][j];
+      if (np > mx) return bad("n_Predictors exceeds the group's predictor count");
+      if (np > 0) {
+        const long long p0 = (long long)pos[(size_t)l * s.J + j] - 1;
+        if (p0 < 0 || p0 + (long long)np * K > n_coeffs) return bad("Pos_Index out of range");
+        cmask[l] |= 1u << j;
+        for (int i = 0; i < np; i++)
+          for (int k = 0; k < K; k++)
+            Cd[((size_t)k * NS + off + i) * L + l] = C[p0 + (size_t)i * K + k];
+      }
+      off += mx;
+    }
+  }
+  // SpcCoeff
+  Records sr;
+  std::string spc = dir + "/" + id + ".SpcCoeff.bin";
+  if (!sr.open(spc, err)) return false;
+  auto sbad = [&](const char* what) { err = spc + ": " + what; return false; };
+  if (!sr.next(d, len) || len != 8) return sbad("corrupt Release/Version record");
+  if (sr.i32(d + 4) < 3) return sbad("SpcCoeff version < 3 is not supported");
+  if (!sr.next(d, len) || len != 4) return sbad("corrupt dimension record");
+  if (sr.i32(d) != L) return sbad("channel count differs from the TauCoeff file");
+  if (!sr.next(d, len) || len != 32) return sbad("corrupt sensor-id record");
+  if (!sr.next(d, len) || len != (size_t)L * (4 + 4 + 8 + 4 + 8 * 8)) return sbad("corrupt channel record");
+  const size_t base = (size_t)L * 20;  // after channel, polarization, pol angle, flag
+  auto col = [&](int f, std::vector<double>& v) {
+    v.resize(L);
+    for (int l = 0; l < L; l++) v[l] = sr.f64(d + base + 8 * ((size_t)f * L + l));
+  };
+  // fields after the integer/polangle block: Frequency(0) Wavenumber(1) C1(2) C2(3) B1(4) B2(5) CBR(6) Solar(7)
+  col(2, s.c1); col(3, s.c2); col(4, s.b1); col(5, s.b2); col(6, s.cbr);
+  s.h2o_idx = (s.absorber_id[s.Jm - 1] == 1) ? s.Jm - 1 : 0;
+  // derived tables
+  std::vector<double> lev_lnp(K + 1), lnp(K), pdp(K), z(K + 1);
+  for (int k = 0; k <= K; k++) lev_lnp[k] = std::log(s.ref_lev[k]);
+  for (int k = 0; k < K; k++) lnp[k] = std::log(s.ref_p[k]);
+  for (int k = 0; k < K; k++)  // ODPS_Predictor.f90:690-700
+    pdp[k] = (k == 0) ? s.ref_lev[0] * (s.ref_lev[1] - s.ref_lev[0])
+                      : s.ref_lev[k + 1] * (s.ref_lev[k + 1] - s.ref_lev[k]);
+  z[K] = 0.0;  // Geopotential_Height, ODPS_CoordinateMapping.f90:607-634
+  for (int k = K; k >= 1; k--)
+    z[k - 1] = z[k] + CC_H * s.ref_t[k - 1] * (1.0 + C_TV * s.ref_a[(size_t)s.h2o_idx * K + k - 1]) *
+                          std::log(s.ref_lev[k] / s.ref_lev[k - 1]);
+  std::vector<double> tab;
+  auto put = [&](const std::vector<double>& v) { size_t at = tab.size(); tab.insert(tab.end(), v.begin(), v.end()); return at; };
+  size_t o_lev = put(s.ref_lev), o_levl = put(lev_lnp), o_lnp = put(lnp), o_t = put(s.ref_t);
+  size_t o_a = put(s.ref_a), o_mn = put(s.min_a), o_mx = put(s.max_a), o_pdp = put(pdp), o_z = put(z);
+  std::vector<double> spec;
+  for (auto* v : {&s.c1, &s.c2, &s.b1, &s.b2, &s.cbr}) spec.insert(spec.end(), v->begin(), v->end());
+  cudaError_t ce;
+  if ((ce = cudaMalloc(&s.d_C, Cd.size() * sizeof(float))) != cudaSuccess ||
+      (ce = cudaMalloc(&s.d_cmask, cmask.size() * sizeof(unsigned))) != cudaSuccess ||
+      (ce = cudaMalloc(&s.d_tab, tab.size() * sizeof(double))) != cudaSuccess ||
+      (ce = cudaMalloc(&s.d_spec, spec.size() * sizeof(double))) != cudaSuccess ||
+      (ce = cudaMemcpy(s.d_C, Cd.data(), Cd.size() * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (ce = cudaMemcpy(s.d_cmask, cmask.data(), cmask.size() * sizeof(unsigned), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (ce = cudaMemcpy(s.d_tab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (ce = cudaMemcpy(s.d_spec, spec.data(), spec.size() * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess) {
+    err = std::string("device upload of ") + id + " coefficients failed: " + cudaGetErrorString(ce);
+    return false;
+  }
+  SensorTables& t = s.tables;
+  t.group = s.group; t.K = K; t.J = s.J; t.Jm = s.Jm; t.L = L; t.sensor_type = s.sensor_type;
+  t.h2o_idx = s.h2o_idx;
+  t.ref_lev = s.d_tab + o_lev; t.ref_lev_lnp = s.d_tab + o_levl; t.ref_lnp = s.d_tab + o_lnp;
+  t.ref_t = s.d_tab + o_t; t.ref_a = s.d_tab + o_a; t.min_a = s.d_tab + o_mn; t.max_a = s.d_tab + o_mx;
+  t.pdp = s.d_tab + o_pdp; t.zgeo = s.d_tab + o_z;
+  s.spec.c1 = s.d_spec; s.spec.c2 = s.d_spec + L; s.spec.b1 = s.d_spec + 2 * L;
+  s.spec.b2 = s.d_spec + 3 * L; s.spec.cbr = s.d_spec + 4 * L;
+  return true;
+}
+
+void free_sensor(Sensor& s) {
+  cudaFree(s.d_C); cudaFree(s.d_cmask); cudaFree(s.d_tab); cudaFree(s.d_spec);
+  s.d_C = nullptr; s.d_cmask = nullptr; s.d_tab = nullptr; s.d_spec = nullptr;
+}
+
+// Grow-only device buffer
+struct DevBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  bool ensure(size_t bytes) {
+    if (bytes <= n) return true;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return false;
+    n = bytes;
+    return true;
+  }
+  void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
+};
+
+}  // namespace
+
+struct crtm_gpu_context {
+  std::vector<Sensor> sensors;
+  int precision = CRTM_GPU_FP64;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string error;
+  long long launches = 0;
+  size_t workspace_budget = (size_t)8 << 30;
+  DevBuf ws;        // chunk workspace
+  DevBuf io_in, io_out;  // device copies for the host entry points
+  DevBuf small;     // idx maps
+};
+
+namespace {
+
+int fail(crtm_gpu_handle h, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (h) h->error = buf; else g_init_error = buf;
+  return CRTM_GPU_FAILURE;
+}
+
+#define CK_LAUNCH(h)                                                                    \
+  do {                                                                                  \
+    (h)->launches++;                                                                    \
+    cudaError_t _e = cudaGetLastError();                                                \
+    if (_e != cudaSuccess) return fail(h, "kernel launch failed: %s", cudaGetErrorString(_e)); \
+  } while (0)
+
+size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Workspace carving for one chunk
+template <class R>
+struct Work {
+  PrepView<R> pv;
+  R* OD;
+  R *TAU, *RD, *RU, *TODAD, *BAD;
+  R* RA;
+  double* PT;     // adjoint: Planck part [n][Kmax][L]
+  double* TSS;    // adjoint: ts scratch [n][L]
+  double* ras;    // adjoint sums [n][1+Jm][K]
+  double* pts;    // [n][Kmax]
+  double* tss;    // [n]
+  int* idx_map;   // [Jm]
+  int* abs_of_user;  // [n_abs]
+};
+
+template <class R>
+size_t work_bytes(const Sensor& s, int n, int Kmax, int n_abs, int mode, Work<R>* w, char* base) {
+  const int K = s.K, L = s.L, NS = s.NS, Jm = s.Jm;
+  const int NNZ = s.group == 1 ? PD_NNZ_G1 : (s.group == 2 ? PD_NNZ_G2 : PD_NNZ_G3);
+  size_t off = 0;
+  auto carve = [&](size_t bytes) -> char* { char* p = base ? base + off : nullptr; off += align_up(bytes); return p; };
+  const size_t nn = (size_t)n;
+  PrepView<R> pv;
+  pv.X = (R*)carve(nn * K * NS * sizeof(R));
+  pv.D = mode ? (R*)carve(nn * K * NNZ * sizeof(R)) : nullptr;
+  pv.T = (double*)carve(nn * K * sizeof(double));
+  pv.A = (double*)carve(nn * Jm * K * sizeof(double));
+  pv.amask = (unsigned char*)carve(nn * Jm * K);
+  pv.band_i0 = (int*)carve(nn * K * sizeof(int));
+  pv.band_n = (int*)carve(nn * K * sizeof(int));
+  pv.band_w = (double*)carve(nn * K * MAX_BAND * sizeof(double));
+  pv.ulev_k1 = (int*)carve(nn * (Kmax + 1) * sizeof(int));
+  pv.ulev_k2 = (int*)carve(nn * (Kmax + 1) * sizeof(int));
+  pv.ulev_fac = (double*)carve(nn * (Kmax + 1) * sizeof(double));
+  pv.ulay_k0 = (int*)carve(nn * Kmax * sizeof(int));
+  pv.ulay_k1 = (int*)carve(nn * Kmax * sizeof(int));
+  pv.scal = (double*)carve(nn * 4 * sizeof(double));
+  pv.status = (int*)carve(nn * sizeof(int));
+  pv.K = K; pv.NS = NS; pv.NNZ = NNZ; pv.Jm = Jm; pv.Kmax = Kmax;
+  Work<R> wk{};
+  wk.pv = pv;
+  wk.OD = (R*)carve(nn * K * L * sizeof(R));
+  if (mode) {
+    const size_t col = nn * Kmax * L * sizeof(R);
+    wk.TAU = (R*)carve(col); wk.RD = (R*)carve(col); wk.RU = (R*)carve(col);
+    wk.TODAD = (R*)carve(col); wk.BAD = (R*)carve(col);
+    wk.RA = (R*)carve(nn * (1 + Jm) * K * L * sizeof(R));
+  }
+  if (mode == 2) {
+    wk.PT = (double*)carve(nn * Kmax * L * sizeof(double));
+    wk.TSS = (double*)carve(nn * L * sizeof(double));
+    wk.ras = (double*)carve(nn * (1 + Jm) * K * sizeof(double));
+    wk.pts = (double*)carve(nn * Kmax * sizeof(double));
+    wk.tss = (double*)carve(nn * sizeof(double));
+  }
+  wk.idx_map = (int*)carve(MAX_ABS * sizeof(int));
+  wk.abs_of_user = (int*)carve((size_t)(n_abs > 0 ? n_abs : 1) * sizeof(int));
+  if (w) *w = wk;
+  return off;
+}
+
+BatchView make_view(const crtm_gpu_batch* b) {
+  BatchView v;
+  v.n_profiles = b->n_profiles; v.max_layers = b->max_layers; v.n_abs = b->n_absorbers;
+  v.n_layers = b->n_layers; v.level_pressure = b->level_pressure; v.pressure = b->pressure;
+  v.temperature = b->temperature; v.absorber = b->absorber;
+  v.land_cov = b->land_coverage; v.water_cov = b->water_coverage;
+  v.snow_cov = b->snow_coverage; v.ice_cov = b->ice_coverage;
+  v.land_t = b->land_temperature; v.water_t = b->water_temperature;
+  v.snow_t = b->snow_temperature; v.ice_t = b->ice_temperature;
+  v.zenith = b->sensor_zenith_angle; v.altitude = b->surface_altitude;
+  v.emissivity = b->emissivity;
+  return v;
+}
+
+template <int G, class R> struct Tune;
+template <> struct Tune<1, double> { static constexpr int FWD = 4, AD = 2; };
+template <> struct Tune<1, float> { static constexpr int FWD = 8, AD = 2; };
+template <> struct Tune<2, double> { static constexpr int FWD = 4, AD = 2; };
+template <> struct Tune<2, float> { static constexpr int FWD = 8, AD = 4; };
+template <> struct Tune<3, double> { static constexpr int FWD = 4, AD = 4; };
+template <> struct Tune<3, float> { static constexpr int FWD = 8, AD = 4; };
+
+// mode 0 forward, 1 K-matrix, 2 adjoint
+template <int G, class R>
+int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, int mode,
+                 const double* seed, crtm_gpu_rtsolution* rts, crtm_gpu_kmatrix* kk,
+                 crtm_gpu_adjoint_out* ad, cudaStream_t st) {
+  const int P = b->n_profiles, Kmax = b->max_layers, L = s.L, K = s.K, n_abs = b->n_absorbers;
+  if (P <= 0) return CRTM_GPU_SUCCESS;
+  if (Kmax < 2 || Kmax > MAX_LAYERS) return fail(h, "max_layers %d out of range [2, %d]", Kmax, MAX_LAYERS);
+  if (n_abs < 0 || (n_abs > 0 && !b->absorber_id)) return fail(h, "absorber ids missing");
+  // absorber maps (host): ODPS absorber -> first user absorber with the same id
+  int idx_map[MAX_ABS];
+  std::vector<int> abs_of_user(n_abs > 0 ? n_abs : 1, -1);
+  for (int j = 0; j < s.Jm; j++) {
+    idx_map[j] = -1;
+    for (int jj = 0; jj < n_abs; jj++)
+      if (b->absorber_id[jj] == s.absorber_id[j]) { idx_map[j] = jj; break; }
+    if (idx_map[j] >= 0) abs_of_user[idx_map[j]] = j;
+  }
+  // chunk size from the workspace budget
+  const size_t per = work_bytes<R>(s, 2, Kmax, n_abs, mode, nullptr, nullptr) -
+                     work_bytes<R>(s, 1, Kmax, n_abs, mode, nullptr, nullptr);
+  int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)P, h->workspace_budget / std::max<size_t>(per, 1)));
+  const size_t need = work_bytes<R>(s, chunk, Kmax, n_abs, mode, nullptr, nullptr);
+  if (!h->ws.ensure(need)) return fail(h, "cannot allocate %zu bytes of workspace", need);
+  Work<R> w;
+  work_bytes<R>(s, chunk, Kmax, n_abs, mode, &w, (char*)h->ws.p);
+  if (cudaMemcpyAsync(w.idx_map, idx_map, sizeof(int) * s.Jm, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(w.abs_of_user, abs_of_user.data(), sizeof(int) * abs_of_user.size(),
+                      cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return fail(h, "absorber map upload failed");
+  const BatchView bv = make_view(b);
+  constexpr int NPF = Tune<G, R>::FWD, NPA = Tune<G, R>::AD;
+  for (int p0 = 0; p0 < P; p0 += chunk) {
+    const int n = std::min(chunk, P - p0);
+    prep_kernel<G, R><<<(n + 63) / 64, 64, 0, st>>>(s.tables, bv, w.pv, w.idx_map, p0, n);
+    CK_LAUNCH(h);
+    dim3 gf((L + 127) / 128, (n + NPF - 1) / NPF);
+    absorb_fwd_kernel<G, R, NPF><<<gf, 128, 0, st>>>(K, L, n, s.d_C, s.d_cmask, w.pv.X, w.OD);
+    CK_LAUNCH(h);
+    ColumnArgs<R> ca;
+    ca.K = K; ca.L = L; ca.Kmax = Kmax; ca.p_begin = p0; ca.n_chunk = n; ca.mode = mode;
+    ca.b = bv; ca.sp = s.spec; ca.pv = w.pv; ca.OD = w.OD;
+    ca.TAU = w.TAU; ca.RD = w.RD; ca.RU = w.RU; ca.TODAD = w.TODAD; ca.BAD = w.BAD;
+    ca.seed = seed; ca.radiance = rts->radiance; ca.bt = rts->brightness_temperature;
+    ca.kt = mode == 1 ? kk->temperature : (mode == 2 ? w.PT : nullptr);
+    ca.tsk = mode == 1 ? kk->water_temperature : (mode == 2 ? w.TSS : nullptr);
+    ca.ek = mode == 1 ? kk->surface_emissivity : nullptr;
+    ca.status = rts->status;
+    const long long nt = (long long)n * L;
+    column_kernel<R><<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(ca);
+    CK_LAUNCH(h);
+    if (mode == 0) continue;
+    dim3 ga((L + 127) / 128, (n + NPA - 1) / NPA);
+    absorb_ad_kernel<G, R, NPA><<<ga, 128, 0, st>>>(K, L, n, s.d_C, s.d_cmask, w.pv.D, w.OD,
+                                                      w.pv.T, w.pv.A, w.pv.amask, s.tables.pdp, w.RA);
+    CK_LAUNCH(h);
+    if (mode == 1) {
+      MapArgs<R> ma;
+      ma.K = K; ma.L = L; ma.Kmax = Kmax; ma.Jm = s.Jm; ma.n_abs = n_abs; ma.p_begin = p0;
+      ma.n_chunk = n; ma.b = bv; ma.pv = w.pv; ma.RA = w.RA; ma.abs_of_user = w.abs_of_user;
+      ma.kt = kk->temperature; ma.ka = kk->absorber;
+      map_kernel<R><<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(ma);
+      CK_LAUNCH(h);
+    } else {
+      const long long rows_ra = (long long)n * (1 + s.Jm) * K;
+      sum_channels_kernel<R><<<(unsigned)((rows_ra * 32 + 255) / 256), 256, 0, st>>>(w.RA, w.ras, rows_ra, L);
+      CK_LAUNCH(h);
+      const long long rows_pt = (long long)n * Kmax;
+      sum_channels_kernel<double><<<(unsigned)((rows_pt * 32 + 255) / 256), 256, 0, st>>>(w.PT, w.pts, rows_pt, L);
+      CK_LAUNCH(h);
+      sum_channels_kernel<double><<<(unsigned)(((long long)n * 32 + 255) / 256), 256, 0, st>>>(w.TSS, w.tss, n, L);
+      CK_LAUNCH(h);
+      AdjMapArgs<R> am;
+      am.K = K; am.Kmax = Kmax; am.Jm = s.Jm; am.n_abs = n_abs; am.p_begin = p0; am.n_chunk = n;
+      am.b = bv; am.pv = w.pv; am.ras = w.ras; am.pts = w.pts; am.tss = w.tss;
+      am.abs_of_user = w.abs_of_user; am.t_ad = ad->temperature; am.a_ad = ad->absorber;
+      am.ts_ad = ad->water_temperature;
+      const long long na = (long long)n * Kmax;
+      adjoint_map_kernel<R><<<(unsigned)((na + 255) / 256), 256, 0, st>>>(am);
+      CK_LAUNCH(h);
+    }
+  }
+  return CRTM_GPU_SUCCESS;
+}
+
+int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, const double* seed,
+             crtm_gpu_rtsolution* rts, crtm_gpu_kmatrix* kk, crtm_gpu_adjoint_out* ad,
+             cudaStream_t st) {
+  if (!h) return CRTM_GPU_FAILURE;
+  if (sensor < 0 || sensor >= (int)h->sensors.size()) return fail(h, "sensor index %d out of range", sensor);
+  if (!b || !rts || !rts->radiance || !rts->brightness_temperature) return fail(h, "missing batch or RTSolution buffers");
+  if (!b->n_layers || !b->level_pressure || !b->pressure || !b->temperature || !b->emissivity ||
+      !b->land_coverage || !b->water_coverage || !b->snow_coverage || !b->ice_coverage ||
+      !b->land_temperature || !b->water_temperature || !b->snow_temperature ||
+      !b->ice_temperature || !b->sensor_zenith_angle || (b->n_absorbers > 0 && !b->absorber))
+    return fail(h, "missing batch input arrays");
+  if (mode == 1 && (!kk || !kk->temperature || !kk->absorber || !kk->water_temperature || !kk->surface_emissivity))
+    return fail(h, "missing K-matrix output buffers");
+  if (mode == 2 && (!ad || !ad->temperature || !ad->absorber || !ad->water_temperature))
+    return fail(h, "missing adjoint output buffers");
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
+  const Sensor& s = h->sensors[sensor];
+  const bool fp64 = h->precision == CRTM_GPU_FP64;
+  switch (s.group) {
+    case 1: return fp64 ? run_pipeline<1, double>(h, s, b, mode, seed, rts, kk, ad, st)
+                        : run_pipeline<1, float>(h, s, b, mode, seed, rts, kk, ad, st);
+    case 2: return fp64 ? run_pipeline<2, double>(h, s, b, mode, seed, rts, kk, ad, st)
+                        : run_pipeline<2, float>(h, s, b, mode, seed, rts, kk, ad, st);
+    default: return fp64 ? run_pipeline<3, double>(h, s, b, mode, seed, rts, kk, ad, st)
+                         : run_pipeline<3, float>(h, s, b, mode, seed, rts, kk, ad, st);
+  }
+}
+
+// Host entry points: copy inputs to the device, run, copy outputs back.
+int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, const double* seed,
+              crtm_gpu_kmatrix* kk, crtm_gpu_adjoint_out* ad, crtm_gpu_rtsolution* rts) {
+  if (!h) return CRTM_GPU_FAILURE;
+  if (sensor < 0 || sensor >= (int)h->sensors.size()) return fail(h, "sensor index %d out of range", sensor);
+  if (!b || b->n_profiles < 0 || b->max_layers < 1 || b->n_absorbers < 0) return fail(h, "bad batch dimensions");
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
+  const int P = b->n_profiles, Km = b->max_layers, J = b->n_absorbers, L = h->sensors[sensor].L;
+  if (P == 0) return CRTM_GPU_SUCCESS;
+  for (int m = 0; m < P; m++)
+    if (b->n_layers[m] < 2 || b->n_layers[m] > Km)
+      return fail(h, "profile %d: n_layers %d outside [2, max_layers=%d]", m, b->n_layers[m], Km);
+  // input layout: doubles then ints
+  struct Item { const void* src; size_t bytes; };
+  const size_t PD = (size_t)P * sizeof(double);
+  std::vector<Item> items = {
+      {b->level_pressure, (size_t)P * (Km + 1) * 8}, {b->pressure, (size_t)P * Km * 8},
+      {b->temperature, (size_t)P * Km * 8},           {b->absorber, (size_t)P * J * Km * 8},
+      {b->land_coverage, PD}, {b->water_coverage, PD}, {b->snow_coverage, PD}, {b->ice_coverage, PD},
+      {b->land_temperature, PD}, {b->water_temperature, PD}, {b->snow_temperature, PD},
+      {b->ice_temperature, PD}, {b->sensor_zenith_angle, PD}, {b->surface_altitude, PD},
+      {b->emissivity, (size_t)P * L * 8}, {seed, (size_t)P * L * 8}, {b->n_layers, (size_t)P * 4}};
+  size_t tot = 0;
+  for (auto& it : items) tot += align_up(it.bytes);
+  if (!h->io_in.ensure(tot)) return fail(h, "cannot allocate %zu bytes for inputs", tot);
+  std::vector<void*> dptr(items.size(), nullptr);
+  size_t off = 0;
+  cudaStream_t st = h->stream;
+  for (size_t i = 0; i < items.size(); i++) {
+    if (items[i].src && items[i].bytes) {
+      dptr[i] = (char*)h->io_in.p + off;
+      if (cudaMemcpyAsync(dptr[i], items[i].src, items[i].bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return fail(h, "host-to-device copy failed");
+    }
+    off += align_up(items[i].bytes);
+  }
+  crtm_gpu_batch db = *b;
+  db.level_pressure = (const double*)dptr[0]; db.pressure = (const double*)dptr[1];
+  db.temperature = (const double*)dptr[2]; db.absorber = (const double*)dptr[3];
+  db.land_coverage = (const double*)dptr[4]; db.water_coverage = (const double*)dptr[5];
+  db.snow_coverage = (const double*)dptr[6]; db.ice_coverage = (const double*)dptr[7];
+  db.land_temperature = (const double*)dptr[8]; db.water_temperature = (const double*)dptr[9];
+  db.snow_temperature = (const double*)dptr[10]; db.ice_temperature = (const double*)dptr[11];
+  db.sensor_zenith_angle = (const double*)dptr[12]; db.surface_altitude = (const double*)dptr[13];
+  db.emissivity = (const double*)dptr[14];
+  const double* dseed = (const double*)dptr[15];
+  db.n_layers = (const int*)dptr[16];
+  // outputs
+  const size_t PL = (size_t)P * L;
+  std::vector<std::pair<void*, size_t>> outs = {{rts->radiance, PL * 8}, {rts->brightness_temperature, PL * 8},
+                                                {rts->status, rts->status ? (size_t)P * 4 : 0}};
+  if (mode == 1)
+    outs.insert(outs.end(), {{kk->temperature, PL * Km * 8}, {kk->absorber, PL * J * Km * 8},
+                             {kk->water_temperature, PL * 8}, {kk->surface_emissivity, PL * 8}});
+  if (mode == 2)
+    outs.insert(outs.end(), {{ad->temperature, (size_t)P * Km * 8}, {ad->absorber, (size_t)P * J * Km * 8},
+                             {ad->water_temperature, PD}});
+  size_t tout = 0;
+  for (auto& o : outs) tout += align_up(o.second);
+  if (!h->io_out.ensure(tout)) return fail(h, "cannot allocate %zu bytes for outputs", tout);
+  std::vector<void*> dout(outs.size(), nullptr);
+  off = 0;
+  for (size_t i = 0; i < outs.size(); i++) {
+    if (outs[i].first && outs[i].second) dout[i] = (char*)h->io_out.p + off;
+    off += align_up(outs[i].second);
+  }
+  crtm_gpu_rtsolution drts{(double*)dout[0], (double*)dout[1], (int*)dout[2]};
+  crtm_gpu_kmatrix dk{};
+  crtm_gpu_adjoint_out dad{};
+  if (mode == 1) dk = {(double*)dout[3], (double*)dout[4], (double*)dout[5], (double*)dout[6]};
+  if (mode == 2) dad = {(double*)dout[3], (double*)dout[4], (double*)dout[5]};
+  int rc = dispatch(h, sensor, &db, mode, dseed, &drts, mode == 1 ? &dk : nullptr,
+                    mode == 2 ? &dad : nullptr, st);
+  if (rc != CRTM_GPU_SUCCESS) return rc;
+  for (size_t i = 0; i < outs.size(); i++)
+    if (dout[i] && cudaMemcpyAsync(outs[i].first, dout[i], outs[i].second, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      return fail(h, "device-to-host copy failed");
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail(h, "CUDA error: %s", cudaGetErrorString(e));
+  if (rts->status)
+    for (int m = 0; m < P; m++)
+      if (rts->status[m] != 0) return fail(h, "profile %d failed (status bits 0x%x)", m, rts->status[m]);
+  return CRTM_GPU_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+int crtm_gpu_init(const char* coeff_path, int n_sensors, const char* const* sensor_ids,
+                  crtm_gpu_handle* handle) {
+  if (!handle) return fail(nullptr, "null handle pointer");
+  *handle = nullptr;
+  if (!coeff_path || n_sensors < 1 || !sensor_ids) return fail(nullptr, "bad init arguments");
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return fail(nullptr, "no CUDA device");
+  crtm_gpu_context* h = new crtm_gpu_context();
+  h->device = dev;
+  if (const char* e = getenv("CRTM_GPU_WORKSPACE_MB")) h->workspace_budget = (size_t)atoll(e) << 20;
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return fail(nullptr, "cudaStreamCreate failed");
+  }
+  h->sensors.resize(n_sensors);
+  for (int i = 0; i < n_sensors; i++) {
+    std::string err;
+    if (!sensor_ids[i] || !load_sensor(coeff_path, sensor_ids[i], h->sensors[i], err)) {
+      g_init_error = err.empty() ? "bad sensor id" : err;
+      crtm_gpu_destroy(h);
+      return CRTM_GPU_FAILURE;
+    }
+  }
+  *handle = h;
+  return CRTM_GPU_SUCCESS;
+}
+
+int crtm_gpu_destroy(crtm_gpu_handle h) {
+  if (!h) return CRTM_GPU_SUCCESS;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (auto& s : h->sensors) free_sensor(s);
+  h->ws.release(); h->io_in.release(); h->io_out.release(); h->small.release();
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return CRTM_GPU_SUCCESS;
+}
+
+int crtm_gpu_n_channels(crtm_gpu_handle h, int sensor) {
+  if (!h || sensor < 0 || sensor >= (int)h->sensors.size()) return -1;
+  return h->sensors[sensor].L;
+}
+
+int crtm_gpu_set_precision(crtm_gpu_handle h, int precision) {
+  if (!h) return CRTM_GPU_FAILURE;
+  if (precision != CRTM_GPU_FP64 && precision != CRTM_GPU_MIXED) return fail(h, "unknown precision %d", precision);
+  h->precision = precision;
+  return CRTM_GPU_SUCCESS;
+}
+
+int crtm_gpu_forward(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, crtm_gpu_rtsolution* rts) {
+  if (!rts) return fail(h, "missing RTSolution");
+  return host_call(h, sensor, b, 0, nullptr, nullptr, nullptr, rts);
+}
+
+int crtm_gpu_k_matrix(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const double* bt_k,
+                      crtm_gpu_kmatrix* k, crtm_gpu_rtsolution* rts) {
+  if (!rts || !k) return fail(h, "missing K-matrix or RTSolution outputs");
+  return host_call(h, sensor, b, 1, bt_k, k, nullptr, rts);
+}
+
+int crtm_gpu_adjoint(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const double* bt_ad,
+                     crtm_gpu_adjoint_out* ad, crtm_gpu_rtsolution* rts) {
+  if (!rts || !ad || !bt_ad) return fail(h, "missing adjoint seed or outputs");
+  return host_call(h, sensor, b, 2, bt_ad, nullptr, ad, rts);
+}
+
+int crtm_gpu_forward_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b,
+                            crtm_gpu_rtsolution* rts, void* stream) {
+  return dispatch(h, sensor, b, 0, nullptr, rts, nullptr, nullptr,
+                  stream ? (cudaStream_t)stream : (h ? h->stream : nullptr));
+}
+
+int crtm_gpu_k_matrix_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b,
+                             const double* bt_k, crtm_gpu_kmatrix* k, crtm_gpu_rtsolution* rts,
+                             void* stream) {
+  return dispatch(h, sensor, b, 1, bt_k, rts, k, nullptr,
+                  stream ? (cudaStream_t)stream : (h ? h->stream : nullptr));
+}
+
+int crtm_gpu_adjoint_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b,
+                            const double* bt_ad, crtm_gpu_adjoint_out* ad, crtm_gpu_rtsolution* rts,
+                            void* stream) {
+  if (!bt_ad) return fail(h, "missing adjoint seed");
+  return dispatch(h, sensor, b, 2, bt_ad, rts, nullptr, ad,
+                  stream ? (cudaStream_t)stream : (h ? h->stream : nullptr));
+}
+
+int crtm_gpu_last_error(crtm_gpu_handle h, char* buf, int n) {
+  const std::string& e = h ? h->error : g_init_error;
+  if (buf && n > 0) {
+    snprintf(buf, (size_t)n, "%s", e.c_str());
+  }
+  return (int)e.size();
+}
+
+long long crtm_gpu_launch_count(crtm_gpu_handle h) { return h ? h->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,155 @@
+/*
+ * crtm_gpu.h - C-ABI of the GB300 library for CRTM's per-profile x channel
+ * forward, K-matrix and adjoint path (ODPS absorption + Emission solver).
+ *
+ * Each entry point stands in for one reference interface (paths relative to
+ * the JCSDA/CRTMv3 source tree):
+ *
+ *   crtm_gpu_init        CRTM_Init        src/CRTM_LifeCycle.f90:520-576
+ *   crtm_gpu_destroy     CRTM_Destroy     src/CRTM_LifeCycle.f90:1131
+ *   crtm_gpu_forward     CRTM_Forward     src/CRTM_Forward_Module.f90:229-245
+ *   crtm_gpu_k_matrix    CRTM_K_Matrix    src/CRTM_K_Matrix_Module.f90:300-322
+ *   crtm_gpu_adjoint     CRTM_Adjoint     src/CRTM_Adjoint_Module.f90:299-309
+ *   crtm_gpu_last_error  Display_Message  src/Utility/Message_Handler.f90:114
+ *
+ * Status codes are the reference's (Message_Handler.f90:27-31).  A call fails
+ * as a whole when any profile fails (CRTM_Forward_Module.f90:415-421); the
+ * per-profile status words say which.
+ *
+ * Data layout (structure of arrays, C order, profiles outermost).  Layer 0
+ * is the top layer.  Every array is indexed with the batch's max_layers
+ * stride; layers past a profile's n_layers are ignored on input and written
+ * as zero on output.
+ *
+ *   level_pressure [P][max_layers+1] hPa     pressure, temperature [P][max_layers]
+ *   absorber       [P][n_absorbers][max_layers]  (units as the reference's Absorber_Units)
+ *   surface / geometry fields [P]; emissivity [P][n_channels] (Options%Emissivity)
+ *   radiance, brightness_temperature [P][n_channels]
+ *   K-matrix: temperature [P][n_channels][max_layers],
+ *             absorber [P][n_channels][n_absorbers][max_layers],
+ *             water_temperature, surface_emissivity [P][n_channels]
+ *   adjoint:  temperature [P][max_layers], absorber [P][n_absorbers][max_layers],
+ *             water_temperature [P]
+ *
+ * Outputs are overwritten (the reference accumulates into caller-zeroed
+ * K/AD structures; a caller that wants accumulation adds the result).
+ *
+ * Threading: calls on one handle are serialised on the handle's CUDA stream;
+ * separate handles may be used from separate host threads.
+ */
+#ifndef CRTM_GPU_H
+#define CRTM_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CRTM_GPU_SUCCESS 0
+#define CRTM_GPU_INFORMATION 1
+#define CRTM_GPU_WARNING 2
+#define CRTM_GPU_FAILURE 3
+
+/* Arithmetic forms.  FP64: every stage in double precision.  MIXED: predictors,
+ * regression and layer optics in single precision; Planck inversion (radiance
+ * to brightness temperature) and the surface terms in double precision. */
+#define CRTM_GPU_FP64 0
+#define CRTM_GPU_MIXED 1
+
+typedef struct crtm_gpu_context* crtm_gpu_handle;
+
+typedef struct {
+  int n_profiles;
+  int max_layers;
+  const int* n_layers;            /* [P] */
+  int n_absorbers;
+  const int* absorber_id;         /* [n_absorbers] HITRAN ids (H2O=1, CO2=2, O3=3, ...) */
+  const double* level_pressure;   /* [P][max_layers+1] */
+  const double* pressure;         /* [P][max_layers] */
+  const double* temperature;      /* [P][max_layers] */
+  const double* absorber;         /* [P][n_absorbers][max_layers] */
+  /* surface (CRTM_Surface_type) [P] */
+  const double* land_coverage;
+  const double* water_coverage;
+  const double* snow_coverage;
+  const double* ice_coverage;
+  const double* land_temperature;
+  const double* water_temperature;
+  const double* snow_temperature;
+  const double* ice_temperature;
+  /* geometry (CRTM_Geometry_type) [P], degrees */
+  const double* sensor_zenith_angle;
+  const double* source_zenith_angle;
+  const double* surface_altitude; /* may be NULL (0) */
+  /* options (CRTM_Options_type): Use_Emissivity is required in this build */
+  const double* emissivity;       /* [P][n_channels] */
+} crtm_gpu_batch;
+
+typedef struct {
+  double* radiance;                /* [P][L] */
+  double* brightness_temperature;  /* [P][L] */
+  int* status;                     /* [P] per-profile status bits, or NULL */
+} crtm_gpu_rtsolution;
+
+typedef struct {
+  double* temperature;        /* [P][L][max_layers] */
+  double* absorber;           /* [P][L][n_absorbers][max_layers] */
+  double* water_temperature;  /* [P][L] Surface_K%Water_Temperature */
+  double* surface_emissivity; /* [P][L] RTSolution_K%Surface_Emissivity */
+} crtm_gpu_kmatrix;
+
+typedef struct {
+  double* temperature;        /* [P][max_layers] */
+  double* absorber;           /* [P][n_absorbers][max_layers] */
+  double* water_temperature;  /* [P] */
+} crtm_gpu_adjoint_out;
+
+/* CRTM_Init: loads <coeff_path>/<sensor_id>.SpcCoeff.bin and .TauCoeff.bin
+ * (ODPS) for each sensor, uploads them to the current CUDA device. */
+int crtm_gpu_init(const char* coeff_path, int n_sensors, const char* const* sensor_ids,
+                  crtm_gpu_handle* handle);
+
+/* CRTM_Destroy */
+int crtm_gpu_destroy(crtm_gpu_handle handle);
+
+/* Number of channels of sensor index `sensor` (0-based, init order), or -1. */
+int crtm_gpu_n_channels(crtm_gpu_handle handle, int sensor);
+
+/* Select the arithmetic form for later calls (CRTM_GPU_FP64 or CRTM_GPU_MIXED). */
+int crtm_gpu_set_precision(crtm_gpu_handle handle, int precision);
+
+/* CRTM_Forward for one sensor: host buffers. */
+int crtm_gpu_forward(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* batch,
+                     crtm_gpu_rtsolution* rts);
+
+/* CRTM_K_Matrix for one sensor: host buffers.  bt_k [P][L] is the
+ * RTSolution_K%Brightness_Temperature seed (NULL means 1 everywhere). */
+int crtm_gpu_k_matrix(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* batch,
+                      const double* bt_k, crtm_gpu_kmatrix* k, crtm_gpu_rtsolution* rts);
+
+/* CRTM_Adjoint for one sensor: host buffers; bt_ad [P][L] seeds. */
+int crtm_gpu_adjoint(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* batch,
+                     const double* bt_ad, crtm_gpu_adjoint_out* ad, crtm_gpu_rtsolution* rts);
+
+/* Device-resident variants: every pointer in batch / outputs is a device
+ * pointer of the handle's device; `stream` is a cudaStream_t (NULL: the
+ * handle's stream).  They return after enqueueing the work. */
+int crtm_gpu_forward_device(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* batch,
+                            crtm_gpu_rtsolution* rts, void* stream);
+int crtm_gpu_k_matrix_device(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* batch,
+                             const double* bt_k, crtm_gpu_kmatrix* k, crtm_gpu_rtsolution* rts,
+                             void* stream);
+int crtm_gpu_adjoint_device(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* batch,
+                            const double* bt_ad, crtm_gpu_adjoint_out* ad,
+                            crtm_gpu_rtsolution* rts, void* stream);
+
+/* Copy the last error message of the handle (or of the last failed init when
+ * handle is NULL) into buf; returns its length. */
+int crtm_gpu_last_error(crtm_gpu_handle handle, char* buf, int n);
+
+/* Number of kernel launches the handle has issued since creation. */
+long long crtm_gpu_launch_count(crtm_gpu_handle handle);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

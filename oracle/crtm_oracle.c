@@ -1043,3 +1043,22 @@ int or_tangent_fd(const or_handle* hd, const or_batch* b, const double* temperat
   free(t2); free(a2); free(w2); free(bp); free(bm);
   return 0;
 }
+
+/* Test hook: the mapped profile and predictors of profile m (X as [K][J][18]). */
+int or_profile_state(const or_handle* h, const or_batch* b, int m, double* T, double* A,
+                     double* sec, double* X) {
+  pstate* s = (pstate*)malloc(sizeof(pstate));
+  geom g;
+  geometry_compute(b->sensor_zenith_angle[m], b->surface_altitude ? b->surface_altitude[m] : 0.0, &g);
+  map_input(h, b, m, &g, s);
+  compute_predictors(h, s);
+  for (int k = 0; k < h->K; k++) {
+    T[k] = s->T[k];
+    sec[k] = s->sec[k];
+    for (int j = 0; j < h->Jm; j++) A[j * h->K + k] = s->A[j][k];
+    for (int j = 0; j < h->J; j++)
+      for (int i = 0; i < MAXI; i++) X[(k * h->J + j) * MAXI + i] = s->X[k][j][i];
+  }
+  free(s);
+  return 0;
+}

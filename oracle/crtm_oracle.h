@@ -71,6 +71,11 @@ int or_adjoint(const or_handle* h, const or_batch* b, const double* bt_ad,
                double* radiance, double* bt, double* temperature_ad, double* absorber_ad,
                double* water_temperature_ad, int n_threads);
 
+/* Test hook: mapped temperature T[K], absorbers A[Jm][K], secants sec[K] and
+ * predictors X[K][J][18] of profile m. */
+int or_profile_state(const or_handle* h, const or_batch* b, int m, double* T, double* A,
+                     double* sec, double* X);
+
 /* Tangent-linear BT for perturbations of T and absorbers (used by symmetry tests):
  * temperature_tl [P][Kmax], absorber_tl [P][Jabs][Kmax], water_temperature_tl [P];
  * bt_tl [P][L] out.  Computed by central differences of the forward model with step h. */

@@ -1,0 +1,99 @@
+"""GPU library vs the CPU FP64 oracle, through the C-ABI (host entry points).
+
+Tolerances: the FP64 form must match the oracle within 1e-4 K in brightness
+temperature and 1e-6 relative (to the largest Jacobian of the case) in the
+K-matrix; the mixed form within 0.01 K and 1e-3 relative.
+"""
+import numpy as np
+import pytest
+
+from crtmv3_gb300 import synthetic as sy
+
+pytestmark = pytest.mark.gpu
+
+BT_TOL = {0: 1e-4, 1: 1e-2}
+JAC_TOL = {0: 1e-6, 1: 1e-3}
+
+
+def _case(sensor, P, nl, seed):
+    return sy.clear_sky_workload(sensor, P, nl, seed)
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("sensor,nl", [("mwsynth_c22", 100), ("irsynth_c616", 101),
+                                       ("mwsynth_c16", 90)])
+def test_forward_matches_oracle(gpu_lib, coeff_dir, sensor, nl, precision):
+    from oracle.pyoracle import Oracle
+    atm, sfc, geo, opt = _case(sensor, 5, nl, 1234)
+    h = gpu_lib.CRTM([sensor], coeff_dir, precision)
+    rts = h.forward(atm, sfc, geo, opt)
+    rad, bt = Oracle(coeff_dir, sensor).forward(atm, sfc, geo, opt)
+    assert np.abs(rts.brightness_temperature - bt).max() < BT_TOL[precision]
+    assert (rts.status == 0).all()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("sensor,nl", [("mwsynth_c22", 100), ("irsynth_c616", 101),
+                                       ("mwsynth_c16", 90)])
+def test_k_matrix_matches_oracle(gpu_lib, coeff_dir, sensor, nl, precision):
+    from oracle.pyoracle import Oracle
+    atm, sfc, geo, opt = _case(sensor, 4, nl, 99)
+    rng = np.random.default_rng(5)
+    h = gpu_lib.CRTM([sensor], coeff_dir, precision)
+    seed = rng.uniform(0.5, 1.5, (4, h.n_channels[0]))
+    km, rts = h.k_matrix(atm, sfc, geo, opt, seed)
+    ref = Oracle(coeff_dir, sensor).k_matrix(atm, sfc, geo, opt, seed)
+    assert np.abs(rts.brightness_temperature - ref["bt"]).max() < BT_TOL[precision]
+    assert _rel(km.temperature, ref["temperature_k"]) < JAC_TOL[precision]
+    assert _rel(km.absorber, ref["absorber_k"]) < JAC_TOL[precision] * 10
+    for j in range(atm.n_absorbers):
+        assert _rel(km.absorber[:, :, j], ref["absorber_k"][:, :, j]) < JAC_TOL[precision] * 10
+    assert _rel(km.water_temperature, ref["water_temperature_k"]) < JAC_TOL[precision]
+    assert _rel(km.surface_emissivity, ref["surface_emissivity_k"]) < JAC_TOL[precision]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_adjoint_matches_oracle(gpu_lib, coeff_dir, precision):
+    from oracle.pyoracle import Oracle
+    sensor = "irsynth_c616"
+    atm, sfc, geo, opt = _case(sensor, 3, 101, 7)
+    h = gpu_lib.CRTM([sensor], coeff_dir, precision)
+    seed = np.random.default_rng(1).normal(size=(3, h.n_channels[0]))
+    out, rts = h.adjoint(atm, sfc, geo, opt, seed)
+    ref = Oracle(coeff_dir, sensor).adjoint(atm, sfc, geo, opt, seed)
+    assert _rel(out["temperature"], ref["temperature_ad"]) < JAC_TOL[precision] * 10
+    assert _rel(out["absorber"], ref["absorber_ad"]) < JAC_TOL[precision] * 10
+    assert _rel(out["water_temperature"], ref["water_temperature_ad"]) < JAC_TOL[precision] * 10
+
+
+def test_ragged_layers_and_surface_pressure(gpu_lib, coeff_dir):
+    """Uneven layer counts in one batch and a surface above the ODPS surface level."""
+    from oracle.pyoracle import Oracle
+    sensor = "irsynth_c616"
+    nl = np.array([60, 137, 101, 75, 120])
+    atm, sfc, geo = sy.generate_profiles(5, nl, sy.absorber_set(1), 77, p_sfc=1013.0)
+    opt = sy.OptionsBatch(emissivity=sy.emissivity_for(2, 5, 616, 3))
+    h = gpu_lib.CRTM([sensor], coeff_dir, 0)
+    km, rts = h.k_matrix(atm, sfc, geo, opt)
+    ref = Oracle(coeff_dir, sensor).k_matrix(atm, sfc, geo, opt)
+    assert np.abs(rts.brightness_temperature - ref["bt"]).max() < 1e-4
+    assert _rel(km.temperature, ref["temperature_k"]) < 1e-6
+    # padding layers are zero
+    for m, n in enumerate(nl):
+        assert np.all(km.temperature[m, :, n:] == 0.0)
+
+
+def test_odd_sizes(gpu_lib, coeff_dir):
+    """One profile, and channel counts that are not multiples of the block size."""
+    from oracle.pyoracle import Oracle
+    for sensor in ("mwsynth_c22", "mwsynth_c16"):
+        atm, sfc, geo, opt = _case(sensor, 1, 100, 3)
+        h = gpu_lib.CRTM([sensor], coeff_dir, 0)
+        km, rts = h.k_matrix(atm, sfc, geo, opt)
+        ref = Oracle(coeff_dir, sensor).k_matrix(atm, sfc, geo, opt)
+        assert np.abs(rts.brightness_temperature - ref["bt"]).max() < 1e-4
+        assert _rel(km.temperature, ref["temperature_k"]) < 1e-6
