@@ -1,0 +1,353 @@
+"""Benchmark: clear-sky hyperspectral IR K-matrix, mixed precision vs all-FP64, on one GB300.
+
+Workload (one step): 2000 profiles x 101 layers x 2211 channels, ODPS group-1
+predictors (6 absorbers), Emission solver, forward + K-matrix with Jacobians
+w.r.t. temperature, H2O and O3 per layer plus skin temperature.  Synthetic
+seeded inputs and coefficient files (crtmv3_gb300.synthetic) stand in for real
+sensor data.
+
+Reported value: profile*channels per second of the mixed-precision form with
+inputs resident in HBM; the all-FP64 GPU form, the accuracy of the mixed form
+against it, the end-to-end rate through the C-ABI with host buffers, per-stage
+kernel times and the CPU baseline (the FP64 oracle on the host cores) are in
+the same JSON line.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--profiles P]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from crtmv3_gb300 import synthetic as sy  # noqa: E402
+
+SENSOR = "irsynth_c2211"
+N_LAYERS = 101
+METRIC = "K-matrix profile*channels/s (mixed precision, inputs in HBM)"
+UNIT = "profile*channels/s"
+COEFF_DIR = os.path.join(ROOT, "coeffs")
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    except OSError:
+        return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (1 GPU: the one we run on)."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(P: int, seed: int):
+    atm, sfc, geo, opt = sy.clear_sky_workload(SENSOR, P, N_LAYERS, seed)
+    return atm, sfc, geo, opt
+
+
+def device_batch(torch, h, atm, sfc, geo, opt, dev):
+    t = {}
+    for k in ("level_pressure", "pressure", "temperature", "absorber"):
+        t[k] = torch.from_numpy(np.ascontiguousarray(getattr(atm, k))).to(dev)
+    t["n_layers"] = torch.from_numpy(atm.n_layers.astype(np.int32)).to(dev)
+    for f in ("land_coverage", "water_coverage", "snow_coverage", "ice_coverage", "land_temperature",
+              "water_temperature", "snow_temperature", "ice_temperature"):
+        t[f] = torch.from_numpy(np.ascontiguousarray(getattr(sfc, f))).to(dev)
+    t["sensor_zenith_angle"] = torch.from_numpy(geo.sensor_zenith_angle).to(dev)
+    t["source_zenith_angle"] = torch.from_numpy(geo.source_zenith_angle).to(dev)
+    t["surface_altitude"] = torch.from_numpy(geo.surface_altitude).to(dev)
+    t["emissivity"] = torch.from_numpy(np.ascontiguousarray(opt.emissivity)).to(dev)
+    b, keep = h.device_batch(t, atm.absorber_id)
+    return b, keep, t
+
+
+def k_outputs(torch, P, L, K, JK, dev):
+    f = dict(dtype=torch.float64, device=dev)
+    return dict(radiance=torch.empty((P, L), **f), bt=torch.empty((P, L), **f),
+                temperature_k=torch.empty((P, L, K), **f), absorber_k=torch.empty((P, L, JK, K), **f),
+                water_temperature_k=torch.empty((P, L), **f), surface_emissivity_k=torch.empty((P, L), **f),
+                status=torch.empty((P,), dtype=torch.int32, device=dev))
+
+
+def cpu_baseline(P_sample: int, threads: int):
+    """FP64 oracle (restatement of the reference's CPU path) on the host cores."""
+    from oracle.pyoracle import Oracle
+    atm, sfc, geo, opt = make_workload(P_sample, 2024)
+    o = Oracle(COEFF_DIR, SENSOR)
+    o.k_matrix(atm.subset(slice(0, min(2, P_sample))), sfc.subset(slice(0, min(2, P_sample))),
+               geo.subset(slice(0, min(2, P_sample))), opt.subset(slice(0, min(2, P_sample))),
+               n_threads=threads)
+    t0 = time.perf_counter()
+    o.k_matrix(atm, sfc, geo, opt, n_threads=threads)
+    dt = time.perf_counter() - t0
+    return P_sample * o.n_channels / dt, dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    sy.write_sensor_files(COEFF_DIR, SENSOR)
+    threads = os.cpu_count() or 1
+    P_sample = args.cpu_profiles
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(max(threads // 2, 1), threads)
+    for _ in range(args.steps):
+        v, dt = cpu_baseline(P_sample, threads)
+        vals.append((v, dt))
+    value = statistics.median(v for v, _ in vals)
+    ms = statistics.median(dt for _, dt in vals) * 1e3
+    line = {"impl": "reference", "metric": METRIC.replace("mixed precision, inputs in HBM", "FP64 CPU"),
+            "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"clear-sky IR K-matrix, {P_sample} of 2000 profiles x {N_LAYERS} "
+                                   f"layers x 2211 channels per step", "profiles": P_sample,
+                       "layers": N_LAYERS, "channels": 2211},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{P_sample} profiles x 2211 channels K-matrix per step "
+                                       f"(FP64 C oracle, OpenMP over profiles)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--profiles", type=int, default=2000)
+    ap.add_argument("--cpu-profiles", type=int, default=128)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from crtmv3_gb300 import api, build
+    build.build()
+    if rank == 0:
+        sy.write_sensor_files(COEFF_DIR, SENSOR)
+    if dist:
+        dist.barrier()
+
+    P, K, L = args.profiles, N_LAYERS, 2211
+    atm, sfc, geo, opt = make_workload(P, 3000 + rank)
+    ids = list(atm.absorber_id)
+    sel = [ids.index(1), ids.index(3)]     # H2O, O3 Jacobians
+    JK = len(sel)
+    h = api.CRTM([SENSOR], COEFF_DIR, api.FP64)
+    b, keep, dev_in = device_batch(torch, h, atm, sfc, geo, opt, dev)
+    # a dedicated stream: the library enqueues on it and the CUDA events below time it
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    sptr = stream.cuda_stream
+    out = {0: k_outputs(torch, P, L, K, JK, dev), 1: k_outputs(torch, P, L, K, JK, dev)}
+
+    def step(prec):
+        h.set_precision(prec)
+        h.k_matrix_device(b, out[prec], None, 0, sptr, k_absorbers=sel)
+
+    def timed(prec, n):
+        torch.cuda.synchronize(dev)
+        if dist:
+            dist.barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            step(prec)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1)
+        if dist:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    for _ in range(args.warmup):
+        step(1)
+    for _ in range(max(1, min(args.warmup, 2))):
+        step(0)
+    torch.cuda.synchronize(dev)
+    launches0 = h.launch_count()
+    with ClockSampler(local) as clk:
+        ms_mixed = timed(1, args.steps)
+    launches_mixed = (h.launch_count() - launches0) // args.steps
+    fp64_steps = max(1, min(args.steps, 3))
+    ms_fp64 = timed(0, fp64_steps)
+    per_mixed = ms_mixed / args.steps
+    per_fp64 = ms_fp64 / fp64_steps
+    pc = P * L * world
+    value = pc / (per_mixed * 1e-3)
+    fp64_value = pc / (per_fp64 * 1e-3)
+
+    # accuracy of the mixed form against the all-FP64 form (same inputs, full workload)
+    a, r = out[1], out[0]
+    bt_err = float((a["bt"] - r["bt"]).abs().max())
+
+    def rel(x, y):
+        return float((x - y).abs().max() / y.abs().max().clamp_min(1e-300))
+    jac_err = max(rel(a["temperature_k"], r["temperature_k"]), rel(a["absorber_k"], r["absorber_k"]),
+                  rel(a["water_temperature_k"], r["water_temperature_k"]))
+
+    # per-stage kernel times (live CUDA events inside the library, one more mixed step)
+    h.set_profiling(True)
+    h.stage_times(reset=True)
+    step(1)
+    st = h.stage_times(reset=True)
+    h.set_profiling(False)
+    stage_ms = {k: v[0] for k, v in st.items() if v[1] > 0}
+    stage_launch = {k: v[1] for k, v in st.items() if v[1] > 0}
+    dom = max(stage_ms, key=stage_ms.get)
+    hbm, bf16, peak_kind = peaks()
+    # algorithmic bytes of the dominant stage per launch (map_out writes the
+    # Jacobians and reads the reference-layer adjoints; column reads/writes the OD columns)
+    n_chunks = stage_launch[dom]
+    algo = {
+        "map_out": P * L * ((1 + JK) * K * 8 + 3 * K * 4 + 2 * 8),
+        "column": P * L * (K * 4 * 2 + 5 * K * 4 * 2 + 8 * 4),
+        "absorb_ad": P * L * (K * 4 + 3 * K * 4),
+        "absorb_fwd": P * L * K * 4,
+        "prep": P * K * 8 * 200,
+    }
+    bytes_per_launch = algo.get(dom, 0) / n_chunks
+    t_launch = stage_ms[dom] / n_chunks * 1e-3
+    achieved = bytes_per_launch / t_launch / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": None, "kernel": dom,
+                "peak_source": peak_kind}
+
+    # end to end through the C-ABI with host (pinned) buffers, mixed form
+    e2e = None
+    if not args.no_e2e:
+        from crtmv3_gb300.structures import KMatrixBatch
+
+        def pin(shape):
+            return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+        kout = KMatrixBatch(pin((P, L, K)), pin((P, L, JK, K)), pin((P, L)), pin((P, L)))
+        h.set_precision(1)
+        h.k_matrix(atm, sfc, geo, opt, None, 0, k_absorbers=sel, out=kout)
+        n_e2e = max(1, min(args.steps, 3))
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            h.k_matrix(atm, sfc, geo, opt, None, 0, k_absorbers=sel, out=kout)
+        dt = (time.perf_counter() - t0) / n_e2e
+        h2d = sum(x.nbytes for x in (atm.level_pressure, atm.pressure, atm.temperature, atm.absorber,
+                                     opt.emissivity)) + 10 * P * 8 + P * 4
+        d2h = P * L * 8 * (2 + K + JK * K + 2) + P * 4
+        e2e = {"value": pc / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": dt * 1e3}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, dt = cpu_baseline(args.cpu_profiles, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_profiles} profiles x 2211 channels x {N_LAYERS} layers K-matrix, "
+                         f"FP64 C oracle with OpenMP over profiles ({dt:.1f} s)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": per_mixed, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "mixed f32/f64", "data": "synthetic",
+            "config": {"workload": f"clear-sky IR forward+K-matrix, {P} profiles x {N_LAYERS} layers x "
+                                   f"{L} channels (ODPS group 1, Emission), Jacobians T/H2O/O3 + Tskin",
+                       "profiles": P, "layers": N_LAYERS, "channels": L, "parallelism": f"replicas x{world}",
+                       "l2": "per-step working set > L2 (10.7 GB of K-matrix output per step)"},
+            "fp64_gpu": {"value": fp64_value, "ms_per_step": per_fp64, "steps": fp64_steps},
+            "speedup_mixed_vs_fp64": value / fp64_value,
+            "accuracy_mixed_vs_fp64": {"max_abs_bt_K": bt_err, "max_rel_jacobian": jac_err},
+            "stages_ms_per_step": stage_ms, "stage_launches_per_step": stage_launch,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(launches_mixed * args.steps),
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

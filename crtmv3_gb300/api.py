@@ -59,7 +59,8 @@ class CRTSolution(ct.Structure):
 
 class CKMatrix(ct.Structure):
     _fields_ = [("temperature", ct.c_void_p), ("absorber", ct.c_void_p),
-                ("water_temperature", ct.c_void_p), ("surface_emissivity", ct.c_void_p)]
+                ("water_temperature", ct.c_void_p), ("surface_emissivity", ct.c_void_p),
+                ("n_k_absorbers", ct.c_int), ("k_absorber_index", ct.c_void_p)]
 
 
 class CAdjoint(ct.Structure):
@@ -96,6 +97,8 @@ def library() -> ct.CDLL:
     L.crtm_gpu_last_error.argtypes = [ct.c_void_p, ct.c_char_p, ct.c_int]
     L.crtm_gpu_launch_count.argtypes = [ct.c_void_p]
     L.crtm_gpu_launch_count.restype = ct.c_longlong
+    L.crtm_gpu_set_profiling.argtypes = [ct.c_void_p, ct.c_int]
+    L.crtm_gpu_stage_times.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int]
     _lib = L
     return L
 
@@ -140,6 +143,18 @@ class CRTM:
 
     def launch_count(self) -> int:
         return int(library().crtm_gpu_launch_count(self.h))
+
+    STAGES = ("prep", "absorb_fwd", "column", "absorb_ad", "map_out", "adjoint_sum")
+
+    def set_profiling(self, enable: bool) -> None:
+        library().crtm_gpu_set_profiling(self.h, int(enable))
+
+    def stage_times(self, reset: bool = True) -> dict:
+        """{stage: (milliseconds, launches)} accumulated while profiling was enabled."""
+        ms = np.zeros(8)
+        n = np.zeros(8, np.int64)
+        k = library().crtm_gpu_stage_times(self.h, ms.ctypes.data, n.ctypes.data, 8, int(reset))
+        return {self.STAGES[i]: (float(ms[i]), int(n[i])) for i in range(min(k, len(self.STAGES)))}
 
     def close(self) -> None:
         if getattr(self, "h", None):
@@ -196,17 +211,24 @@ class CRTM:
         self._check(library().crtm_gpu_forward(self.h, sensor, ct.byref(b), ct.byref(cr)))
         return rts
 
-    def k_matrix(self, atm, sfc, geo, opt, bt_k=None, sensor: int = 0):
+    def k_matrix(self, atm, sfc, geo, opt, bt_k=None, sensor: int = 0, k_absorbers=None, out=None):
+        """K-matrix with host buffers.  ``k_absorbers``: optional list of user absorber
+        indices whose Jacobians are returned (default: all).  ``out``: optional
+        preallocated KMatrixBatch (e.g. in pinned memory)."""
         P, L, K, J = atm.n_profiles, self.n_channels[sensor], atm.max_layers, atm.n_absorbers
         keep: list = []
         b = self._cbatch(atm, sfc, geo, opt, keep)
         seed = None if bt_k is None else np.ascontiguousarray(bt_k, np.float64)
+        sel = None if k_absorbers is None else np.ascontiguousarray(k_absorbers, np.int32)
+        JK = J if sel is None else int(sel.shape[0])
         rts = RTSolutionBatch(np.zeros((P, L)), np.zeros((P, L)), status=np.zeros(P, np.int32))
-        km = KMatrixBatch(np.zeros((P, L, K)), np.zeros((P, L, J, K)), np.zeros((P, L)), np.zeros((P, L)))
+        km = out if out is not None else KMatrixBatch(np.zeros((P, L, K)), np.zeros((P, L, JK, K)),
+                                                      np.zeros((P, L)), np.zeros((P, L)))
         cr = CRTSolution(rts.radiance.ctypes.data, rts.brightness_temperature.ctypes.data,
                          rts.status.ctypes.data)
         ck = CKMatrix(km.temperature.ctypes.data, km.absorber.ctypes.data,
-                      km.water_temperature.ctypes.data, km.surface_emissivity.ctypes.data)
+                      km.water_temperature.ctypes.data, km.surface_emissivity.ctypes.data,
+                      0 if sel is None else JK, None if sel is None else sel.ctypes.data)
         self._check(library().crtm_gpu_k_matrix(self.h, sensor, ct.byref(b), _addr(seed),
                                                 ct.byref(ck), ct.byref(cr)))
         return km, rts
@@ -248,11 +270,14 @@ class CRTM:
             setattr(b, f, None if t is None else t.data_ptr())
         return b, keep
 
-    def k_matrix_device(self, b: CBatch, out: dict, seed=None, sensor: int = 0, stream=None) -> None:
+    def k_matrix_device(self, b: CBatch, out: dict, seed=None, sensor: int = 0, stream=None,
+                        k_absorbers=None) -> None:
         cr = CRTSolution(out["radiance"].data_ptr(), out["bt"].data_ptr(),
                          _addr(out.get("status")))
+        sel = None if k_absorbers is None else np.ascontiguousarray(k_absorbers, np.int32)
         ck = CKMatrix(out["temperature_k"].data_ptr(), out["absorber_k"].data_ptr(),
-                      out["water_temperature_k"].data_ptr(), out["surface_emissivity_k"].data_ptr())
+                      out["water_temperature_k"].data_ptr(), out["surface_emissivity_k"].data_ptr(),
+                      0 if sel is None else int(sel.shape[0]), None if sel is None else sel.ctypes.data)
         self._check(library().crtm_gpu_k_matrix_device(self.h, sensor, ct.byref(b), _addr(seed),
                                                        ct.byref(ck), ct.byref(cr), stream))
 

@@ -109,6 +109,7 @@ struct Sensor {
   double* d_tab = nullptr;       // concatenated tables
   double* d_spec = nullptr;      // c1,c2,b1,b2,cbr [5][L]
   SensorTables tables{};
+  RefSums refsums{};
   SpecView spec{};
 };
 
@@ -227,6 +228,23 @@ bool load_sensor(const std::string& dir, const std::string& id, Sensor& s, std::
   auto put = [&](const std::vector<double>& v) { size_t at = tab.size(); tab.insert(tab.end(), v.begin(), v.end()); return at; };
   size_t o_lev = put(s.ref_lev), o_levl = put(lev_lnp), o_lnp = put(lnp), o_t = put(s.ref_t);
   size_t o_a = put(s.ref_a), o_mn = put(s.min_a), o_mx = put(s.max_a), o_pdp = put(pdp), o_z = put(z);
+  // running sums of the reference profile (ODPS_Predictor.f90:707-759, the *_ref terms)
+  std::vector<double> tzr(K), tzpr(K), gzr((size_t)s.Jm * K), gtr((size_t)s.Jm * K);
+  {
+    double a0 = 0, a1 = 0;
+    for (int k = 0; k < K; k++) { a0 += s.ref_t[k]; a1 += pdp[k] * s.ref_t[k]; tzr[k] = a0; tzpr[k] = a1; }
+    for (int j = 0; j < s.Jm; j++) {
+      double g0 = 0, g1 = 0;
+      for (int k = 0; k < K; k++) {
+        const double ra = s.ref_a[(size_t)j * K + k];
+        g0 += pdp[k] * ra;
+        g1 += pdp[k] * ra * s.ref_t[k];
+        gzr[(size_t)j * K + k] = g0;
+        gtr[(size_t)j * K + k] = g1;
+      }
+    }
+  }
+  size_t o_tzr = put(tzr), o_tzpr = put(tzpr), o_gzr = put(gzr), o_gtr = put(gtr);
   std::vector<double> spec;
   for (auto* v : {&s.c1, &s.c2, &s.b1, &s.b2, &s.cbr}) spec.insert(spec.end(), v->begin(), v->end());
   cudaError_t ce;
@@ -247,6 +265,8 @@ bool load_sensor(const std::string& dir, const std::string& id, Sensor& s, std::
   t.ref_lev = s.d_tab + o_lev; t.ref_lev_lnp = s.d_tab + o_levl; t.ref_lnp = s.d_tab + o_lnp;
   t.ref_t = s.d_tab + o_t; t.ref_a = s.d_tab + o_a; t.min_a = s.d_tab + o_mn; t.max_a = s.d_tab + o_mx;
   t.pdp = s.d_tab + o_pdp; t.zgeo = s.d_tab + o_z;
+  s.refsums.tz_ref = s.d_tab + o_tzr; s.refsums.tzp_ref = s.d_tab + o_tzpr;
+  s.refsums.gazp_ref = s.d_tab + o_gzr; s.refsums.gatzp_ref = s.d_tab + o_gtr;
   s.spec.c1 = s.d_spec; s.spec.c2 = s.d_spec + L; s.spec.b1 = s.d_spec + 2 * L;
   s.spec.b2 = s.d_spec + 3 * L; s.spec.cbr = s.d_spec + 4 * L;
   return true;
@@ -286,6 +306,13 @@ struct crtm_gpu_context {
   DevBuf ws;        // chunk workspace
   DevBuf io_in, io_out;  // device copies for the host entry points
   DevBuf small;     // idx maps
+  // stage profiling
+  bool profiling = false;
+  struct Pending { int stage; cudaEvent_t a, b; };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> event_pool;
+  double stage_ms[8] = {0};
+  long long stage_n[8] = {0};
 };
 
 namespace {
@@ -307,66 +334,119 @@ int fail(crtm_gpu_handle h, const char* fmt, ...) {
     if (_e != cudaSuccess) return fail(h, "kernel launch failed: %s", cudaGetErrorString(_e)); \
   } while (0)
 
+cudaEvent_t take_event(crtm_gpu_handle h) {
+  if (!h->event_pool.empty()) {
+    cudaEvent_t e = h->event_pool.back();
+    h->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Brackets one kernel launch with events when profiling is enabled.
+struct StageScope {
+  crtm_gpu_handle h;
+  int stage;
+  cudaStream_t st;
+  cudaEvent_t a = nullptr;
+  StageScope(crtm_gpu_handle h_, int s_, cudaStream_t st_) : h(h_), stage(s_), st(st_) {
+    if (h->profiling) { a = take_event(h); cudaEventRecord(a, st); }
+  }
+  ~StageScope() {
+    if (a) {
+      cudaEvent_t b = take_event(h);
+      cudaEventRecord(b, st);
+      h->pending.push_back({stage, a, b});
+    }
+  }
+};
+
+void collect_stage_times(crtm_gpu_handle h) {
+  for (auto& p : h->pending) {
+    float ms = 0.0f;
+    if (cudaEventSynchronize(p.b) == cudaSuccess && cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      h->stage_ms[p.stage] += ms;
+      h->stage_n[p.stage] += 1;
+    }
+    h->event_pool.push_back(p.a);
+    h->event_pool.push_back(p.b);
+  }
+  h->pending.clear();
+}
+
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // Workspace carving for one chunk
 template <class R>
 struct Work {
   PrepView<R> pv;
-  R* OD;
-  R *TAU, *RD, *RU, *TODAD, *BAD;
-  R* RA;
-  double* PT;     // adjoint: Planck part [n][Kmax][L]
-  double* TSS;    // adjoint: ts scratch [n][L]
-  double* ras;    // adjoint sums [n][1+Jm][K]
-  double* pts;    // [n][Kmax]
-  double* tss;    // [n]
-  int* idx_map;   // [Jm]
-  int* abs_of_user;  // [n_abs]
+  R* OD;            // [n][K][L]
+  R* TAU, *DTOP;    // [n][Kmax][L]
+  R* PT;            // [n][Kmax][L]
+  R* SC;            // [n][L]
+  double* TSK;      // adjoint: [n][L]
+  R* RA;            // [n][nv][K][L]
+  double* ras;      // adjoint: [n][nv][K]
+  double* pts;      // adjoint: [n][Kmax]
+  double* tss;      // adjoint: [n]
+  int* idx_map;     // [Jm]
 };
 
-template <class R>
-size_t work_bytes(const Sensor& s, int n, int Kmax, int n_abs, int mode, Work<R>* w, char* base) {
-  const int K = s.K, L = s.L, NS = s.NS, Jm = s.Jm;
-  const int NNZ = s.group == 1 ? PD_NNZ_G1 : (s.group == 2 ? PD_NNZ_G2 : PD_NNZ_G3);
+template <int G, class R> struct Tune;
+template <> struct Tune<1, double> { static constexpr int FWD = 4, AD = 2; };
+template <> struct Tune<1, float> { static constexpr int FWD = 8, AD = 4; };
+template <> struct Tune<2, double> { static constexpr int FWD = 4, AD = 2; };
+template <> struct Tune<2, float> { static constexpr int FWD = 8, AD = 4; };
+template <> struct Tune<3, double> { static constexpr int FWD = 4, AD = 4; };
+template <> struct Tune<3, float> { static constexpr int FWD = 8, AD = 8; };
+// profiles per absorb_ad CTA
+template <int G, class R> constexpr int ad_profiles() { return Tune<G, R>::AD * AD_WARPS; }
+
+template <int G, class R>
+size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w, char* base) {
+  const int K = s.K, L = s.L, NS = s.NS, NX = DLayout<G>::NX;
+  const int npf = Tune<G, R>::FWD, npa = Tune<G, R>::AD;
   size_t off = 0;
   auto carve = [&](size_t bytes) -> char* { char* p = base ? base + off : nullptr; off += align_up(bytes); return p; };
   const size_t nn = (size_t)n;
+  const size_t ngf = (nn + npf - 1) / npf;
+  const size_t nga = ((nn + ad_profiles<G, R>() - 1) / ad_profiles<G, R>()) * AD_WARPS;
   PrepView<R> pv;
-  pv.X = (R*)carve(nn * K * NS * sizeof(R));
-  pv.D = mode ? (R*)carve(nn * K * NNZ * sizeof(R)) : nullptr;
-  pv.T = (double*)carve(nn * K * sizeof(double));
-  pv.A = (double*)carve(nn * Jm * K * sizeof(double));
-  pv.amask = (unsigned char*)carve(nn * Jm * K);
+  pv.Xg = (R*)carve(ngf * npf * K * NS * sizeof(R));
+  pv.Dg = mode ? (R*)carve(nga * npa * K * NX * sizeof(R)) : nullptr;
   pv.band_i0 = (int*)carve(nn * K * sizeof(int));
   pv.band_n = (int*)carve(nn * K * sizeof(int));
   pv.band_w = (double*)carve(nn * K * MAX_BAND * sizeof(double));
   pv.ulev_k1 = (int*)carve(nn * (Kmax + 1) * sizeof(int));
   pv.ulev_k2 = (int*)carve(nn * (Kmax + 1) * sizeof(int));
   pv.ulev_fac = (double*)carve(nn * (Kmax + 1) * sizeof(double));
-  pv.ulay_k0 = (int*)carve(nn * Kmax * sizeof(int));
-  pv.ulay_k1 = (int*)carve(nn * Kmax * sizeof(int));
+  pv.rlev_ilo = (int*)carve(nn * (K + 1) * sizeof(int));
+  pv.rlev_ihi = (int*)carve(nn * (K + 1) * sizeof(int));
+  pv.ub_k0 = (int*)carve(nn * Kmax * sizeof(int));
+  pv.ub_n = (int*)carve(nn * Kmax * sizeof(int));
+  pv.ub_w = (double*)carve(nn * Kmax * MAX_UBAND * sizeof(double));
   pv.scal = (double*)carve(nn * 4 * sizeof(double));
   pv.status = (int*)carve(nn * sizeof(int));
-  pv.K = K; pv.NS = NS; pv.NNZ = NNZ; pv.Jm = Jm; pv.Kmax = Kmax;
+  pv.K = K; pv.Kmax = Kmax; pv.npf = npf; pv.npa = mode ? npa : 0;
   Work<R> wk{};
   wk.pv = pv;
   wk.OD = (R*)carve(nn * K * L * sizeof(R));
   if (mode) {
-    const size_t col = nn * Kmax * L * sizeof(R);
-    wk.TAU = (R*)carve(col); wk.RD = (R*)carve(col); wk.RU = (R*)carve(col);
-    wk.TODAD = (R*)carve(col); wk.BAD = (R*)carve(col);
-    wk.RA = (R*)carve(nn * (1 + Jm) * K * L * sizeof(R));
+    wk.TAU = (R*)carve(nn * Kmax * L * sizeof(R));
+    wk.DTOP = (R*)carve(nn * Kmax * L * sizeof(R));
+    wk.PT = (R*)carve(nn * Kmax * L * sizeof(R));
+    wk.SC = (R*)carve(nn * L * sizeof(R));
+    wk.RA = (R*)carve(nn * nv * K * L * sizeof(R));
   }
   if (mode == 2) {
-    wk.PT = (double*)carve(nn * Kmax * L * sizeof(double));
-    wk.TSS = (double*)carve(nn * L * sizeof(double));
-    wk.ras = (double*)carve(nn * (1 + Jm) * K * sizeof(double));
+    wk.TSK = (double*)carve(nn * L * sizeof(double));
+    wk.ras = (double*)carve(nn * nv * K * sizeof(double));
     wk.pts = (double*)carve(nn * Kmax * sizeof(double));
     wk.tss = (double*)carve(nn * sizeof(double));
   }
   wk.idx_map = (int*)carve(MAX_ABS * sizeof(int));
-  wk.abs_of_user = (int*)carve((size_t)(n_abs > 0 ? n_abs : 1) * sizeof(int));
   if (w) *w = wk;
   return off;
 }
@@ -385,13 +465,13 @@ BatchView make_view(const crtm_gpu_batch* b) {
   return v;
 }
 
-template <int G, class R> struct Tune;
-template <> struct Tune<1, double> { static constexpr int FWD = 4, AD = 2; };
-template <> struct Tune<1, float> { static constexpr int FWD = 8, AD = 2; };
-template <> struct Tune<2, double> { static constexpr int FWD = 4, AD = 2; };
-template <> struct Tune<2, float> { static constexpr int FWD = 8, AD = 4; };
-template <> struct Tune<3, double> { static constexpr int FWD = 4, AD = 4; };
-template <> struct Tune<3, float> { static constexpr int FWD = 8, AD = 4; };
+template <class F>
+int reserve_smem(crtm_gpu_handle h, F kernel, size_t bytes, const char* what) {
+  if (bytes > 48 * 1024 &&
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+    return fail(h, "cannot reserve %zu bytes of shared memory for the %s kernel", bytes, what);
+  return CRTM_GPU_SUCCESS;
+}
 
 // mode 0 forward, 1 K-matrix, 2 adjoint
 template <int G, class R>
@@ -401,7 +481,8 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
   const int P = b->n_profiles, Kmax = b->max_layers, L = s.L, K = s.K, n_abs = b->n_absorbers;
   if (P <= 0) return CRTM_GPU_SUCCESS;
   if (Kmax < 2 || Kmax > MAX_LAYERS) return fail(h, "max_layers %d out of range [2, %d]", Kmax, MAX_LAYERS);
-  if (n_abs < 0 || (n_abs > 0 && !b->absorber_id)) return fail(h, "absorber ids missing");
+  if (n_abs < 0 || n_abs > MAX_OUT_ABS || (n_abs > 0 && !b->absorber_id))
+    return fail(h, "absorber count %d out of range [0, %d] or ids missing", n_abs, MAX_OUT_ABS);
   // absorber maps (host): ODPS absorber -> first user absorber with the same id
   int idx_map[MAX_ABS];
   std::vector<int> abs_of_user(n_abs > 0 ? n_abs : 1, -1);
@@ -411,65 +492,110 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       if (b->absorber_id[jj] == s.absorber_id[j]) { idx_map[j] = jj; break; }
     if (idx_map[j] >= 0) abs_of_user[idx_map[j]] = j;
   }
+  // requested absorber adjoints: K-matrix selection (default all) or, for the adjoint, all
+  OutAbs oa{};
+  if (mode == 1 && kk->n_k_absorbers > 0) {
+    if (kk->n_k_absorbers > n_abs || !kk->k_absorber_index) return fail(h, "bad K-matrix absorber selection");
+    oa.n = kk->n_k_absorbers;
+    for (int j = 0; j < oa.n; j++) {
+      const int ja = kk->k_absorber_index[j];
+      if (ja < 0 || ja >= n_abs) return fail(h, "K-matrix absorber index %d out of range", ja);
+      oa.odps[j] = abs_of_user[ja];
+    }
+  } else {
+    oa.n = n_abs;
+    for (int j = 0; j < n_abs; j++) oa.odps[j] = abs_of_user[j];
+  }
+  const int nv = 1 + oa.n;
   // chunk size from the workspace budget
-  const size_t per = work_bytes<R>(s, 2, Kmax, n_abs, mode, nullptr, nullptr) -
-                     work_bytes<R>(s, 1, Kmax, n_abs, mode, nullptr, nullptr);
-  int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)P, h->workspace_budget / std::max<size_t>(per, 1)));
-  const size_t need = work_bytes<R>(s, chunk, Kmax, n_abs, mode, nullptr, nullptr);
+  const size_t per = work_bytes<G, R>(s, 64, Kmax, nv, mode, nullptr, nullptr) / 64 + 1;
+  int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)P, h->workspace_budget / per));
+  const size_t need = work_bytes<G, R>(s, chunk, Kmax, nv, mode, nullptr, nullptr);
   if (!h->ws.ensure(need)) return fail(h, "cannot allocate %zu bytes of workspace", need);
   Work<R> w;
-  work_bytes<R>(s, chunk, Kmax, n_abs, mode, &w, (char*)h->ws.p);
-  if (cudaMemcpyAsync(w.idx_map, idx_map, sizeof(int) * s.Jm, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-      cudaMemcpyAsync(w.abs_of_user, abs_of_user.data(), sizeof(int) * abs_of_user.size(),
-                      cudaMemcpyHostToDevice, st) != cudaSuccess)
+  work_bytes<G, R>(s, chunk, Kmax, nv, mode, &w, (char*)h->ws.p);
+  if (cudaMemcpyAsync(w.idx_map, idx_map, sizeof(int) * s.Jm, cudaMemcpyHostToDevice, st) != cudaSuccess)
     return fail(h, "absorber map upload failed");
   const BatchView bv = make_view(b);
   constexpr int NPF = Tune<G, R>::FWD, NPA = Tune<G, R>::AD;
+  const size_t prep_smem = prep_smem_bytes<G>(K);
+  const size_t col_smem = column_smem_bytes<R>(K, Kmax);
+  int map_ct = 32;
+  while (map_ct > 8 && map_smem_bytes<R>(K, Kmax, nv, map_ct) > 200 * 1024) map_ct >>= 1;
+  const size_t map_smem = map_smem_bytes<R>(K, Kmax, nv, map_ct);
+  if (reserve_smem(h, column_kernel<R>, col_smem, "column") ||
+      reserve_smem(h, map_kernel<R>, map_smem, "map"))
+    return CRTM_GPU_FAILURE;
+  const bool ho_only = [&] {
+    for (int j = 0; j < oa.n; j++)
+      if (oa.odps[j] >= 2) return false;
+    return true;
+  }();
   for (int p0 = 0; p0 < P; p0 += chunk) {
     const int n = std::min(chunk, P - p0);
-    prep_kernel<G, R><<<(n + 63) / 64, 64, 0, st>>>(s.tables, bv, w.pv, w.idx_map, p0, n);
-    CK_LAUNCH(h);
-    dim3 gf((L + 127) / 128, (n + NPF - 1) / NPF);
-    absorb_fwd_kernel<G, R, NPF><<<gf, 128, 0, st>>>(K, L, n, s.d_C, s.d_cmask, w.pv.X, w.OD);
-    CK_LAUNCH(h);
-    ColumnArgs<R> ca;
+    {
+      StageScope sc(h, 0, st);
+      prep_kernel<G, R><<<n, 32, prep_smem, st>>>(s.tables, s.refsums, bv, w.pv, w.idx_map, p0, n);
+      CK_LAUNCH(h);
+    }
+    {
+      StageScope sc(h, 1, st);
+      dim3 gf((L + 127) / 128, (n + NPF - 1) / NPF);
+      absorb_fwd_kernel<G, R, NPF><<<gf, 128, 0, st>>>(K, L, n, s.d_C, s.d_cmask, w.pv.Xg, w.OD);
+      CK_LAUNCH(h);
+    }
+    ColumnArgs<R> ca{};
     ca.K = K; ca.L = L; ca.Kmax = Kmax; ca.p_begin = p0; ca.n_chunk = n; ca.mode = mode;
     ca.b = bv; ca.sp = s.spec; ca.pv = w.pv; ca.OD = w.OD;
-    ca.TAU = w.TAU; ca.RD = w.RD; ca.RU = w.RU; ca.TODAD = w.TODAD; ca.BAD = w.BAD;
+    ca.TAU = w.TAU; ca.DTOP = w.DTOP; ca.PT = w.PT; ca.SC = w.SC;
     ca.seed = seed; ca.radiance = rts->radiance; ca.bt = rts->brightness_temperature;
-    ca.kt = mode == 1 ? kk->temperature : (mode == 2 ? w.PT : nullptr);
-    ca.tsk = mode == 1 ? kk->water_temperature : (mode == 2 ? w.TSS : nullptr);
+    ca.tsk = mode == 1 ? kk->water_temperature : (mode == 2 ? w.TSK : nullptr);
     ca.ek = mode == 1 ? kk->surface_emissivity : nullptr;
     ca.status = rts->status;
-    const long long nt = (long long)n * L;
-    column_kernel<R><<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(ca);
-    CK_LAUNCH(h);
+    {
+      StageScope sc(h, 2, st);
+      dim3 gc((L + 127) / 128, n);
+      column_kernel<R><<<gc, 128, col_smem, st>>>(ca);
+      CK_LAUNCH(h);
+    }
     if (mode == 0) continue;
-    dim3 ga((L + 127) / 128, (n + NPA - 1) / NPA);
-    absorb_ad_kernel<G, R, NPA><<<ga, 128, 0, st>>>(K, L, n, s.d_C, s.d_cmask, w.pv.D, w.OD,
-                                                      w.pv.T, w.pv.A, w.pv.amask, s.tables.pdp, w.RA);
-    CK_LAUNCH(h);
+    {
+      StageScope sc(h, 3, st);
+      dim3 ga((L + 31) / 32, (n + ad_profiles<G, R>() - 1) / ad_profiles<G, R>());
+      if (ho_only)
+        absorb_ad_kernel<G, R, NPA, 1><<<ga, 32 * AD_WARPS, 0, st>>>(
+            K, L, n, s.d_C, s.d_cmask, w.pv.Dg, s.tables.pdp, w.OD, w.SC, oa, w.RA);
+      else
+        absorb_ad_kernel<G, R, NPA, 0><<<ga, 32 * AD_WARPS, 0, st>>>(
+            K, L, n, s.d_C, s.d_cmask, w.pv.Dg, s.tables.pdp, w.OD, w.SC, oa, w.RA);
+      CK_LAUNCH(h);
+    }
     if (mode == 1) {
-      MapArgs<R> ma;
-      ma.K = K; ma.L = L; ma.Kmax = Kmax; ma.Jm = s.Jm; ma.n_abs = n_abs; ma.p_begin = p0;
-      ma.n_chunk = n; ma.b = bv; ma.pv = w.pv; ma.RA = w.RA; ma.abs_of_user = w.abs_of_user;
+      MapArgs<R> ma{};
+      ma.K = K; ma.L = L; ma.Kmax = Kmax; ma.p_begin = p0; ma.n_chunk = n; ma.nv = nv; ma.ct = map_ct;
+      ma.b = bv; ma.pv = w.pv; ma.RA = w.RA; ma.PT = w.PT; ma.SC = w.SC;
       ma.kt = kk->temperature; ma.ka = kk->absorber;
-      map_kernel<R><<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(ma);
+      StageScope sc(h, 4, st);
+      dim3 gm((L + map_ct - 1) / map_ct, n);
+      map_kernel<R><<<gm, 256, map_smem, st>>>(ma);
       CK_LAUNCH(h);
     } else {
-      const long long rows_ra = (long long)n * (1 + s.Jm) * K;
-      sum_channels_kernel<R><<<(unsigned)((rows_ra * 32 + 255) / 256), 256, 0, st>>>(w.RA, w.ras, rows_ra, L);
+      StageScope sc(h, 5, st);
+      const long long rows_ra = (long long)n * nv * K;
+      channel_sum_kernel<R><<<(unsigned)((rows_ra * 32 + 255) / 256), 256, 0, st>>>(
+          w.RA, nullptr, 1, rows_ra, L, w.ras);
       CK_LAUNCH(h);
       const long long rows_pt = (long long)n * Kmax;
-      sum_channels_kernel<double><<<(unsigned)((rows_pt * 32 + 255) / 256), 256, 0, st>>>(w.PT, w.pts, rows_pt, L);
+      channel_sum_kernel<R><<<(unsigned)((rows_pt * 32 + 255) / 256), 256, 0, st>>>(
+          w.PT, w.SC, Kmax, rows_pt, L, w.pts);
       CK_LAUNCH(h);
-      sum_channels_kernel<double><<<(unsigned)(((long long)n * 32 + 255) / 256), 256, 0, st>>>(w.TSS, w.tss, n, L);
+      channel_sum_kernel<double><<<(unsigned)(((long long)n * 32 + 255) / 256), 256, 0, st>>>(
+          w.TSK, nullptr, 1, n, L, w.tss);
       CK_LAUNCH(h);
-      AdjMapArgs<R> am;
-      am.K = K; am.Kmax = Kmax; am.Jm = s.Jm; am.n_abs = n_abs; am.p_begin = p0; am.n_chunk = n;
+      AdjMapArgs<R> am{};
+      am.K = K; am.Kmax = Kmax; am.nv = nv; am.p_begin = p0; am.n_chunk = n;
       am.b = bv; am.pv = w.pv; am.ras = w.ras; am.pts = w.pts; am.tss = w.tss;
-      am.abs_of_user = w.abs_of_user; am.t_ad = ad->temperature; am.a_ad = ad->absorber;
-      am.ts_ad = ad->water_temperature;
+      am.t_ad = ad->temperature; am.a_ad = ad->absorber; am.ts_ad = ad->water_temperature;
       const long long na = (long long)n * Kmax;
       adjoint_map_kernel<R><<<(unsigned)((na + 255) / 256), 256, 0, st>>>(am);
       CK_LAUNCH(h);
@@ -557,8 +683,9 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
   const size_t PL = (size_t)P * L;
   std::vector<std::pair<void*, size_t>> outs = {{rts->radiance, PL * 8}, {rts->brightness_temperature, PL * 8},
                                                 {rts->status, rts->status ? (size_t)P * 4 : 0}};
+  const int JK = (mode == 1 && kk->n_k_absorbers > 0) ? kk->n_k_absorbers : J;
   if (mode == 1)
-    outs.insert(outs.end(), {{kk->temperature, PL * Km * 8}, {kk->absorber, PL * J * Km * 8},
+    outs.insert(outs.end(), {{kk->temperature, PL * Km * 8}, {kk->absorber, PL * JK * Km * 8},
                              {kk->water_temperature, PL * 8}, {kk->surface_emissivity, PL * 8}});
   if (mode == 2)
     outs.insert(outs.end(), {{ad->temperature, (size_t)P * Km * 8}, {ad->absorber, (size_t)P * J * Km * 8},
@@ -575,7 +702,9 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
   crtm_gpu_rtsolution drts{(double*)dout[0], (double*)dout[1], (int*)dout[2]};
   crtm_gpu_kmatrix dk{};
   crtm_gpu_adjoint_out dad{};
-  if (mode == 1) dk = {(double*)dout[3], (double*)dout[4], (double*)dout[5], (double*)dout[6]};
+  if (mode == 1)
+    dk = {(double*)dout[3], (double*)dout[4], (double*)dout[5], (double*)dout[6], kk->n_k_absorbers,
+          kk->k_absorber_index};
   if (mode == 2) dad = {(double*)dout[3], (double*)dout[4], (double*)dout[5]};
   int rc = dispatch(h, sensor, &db, mode, dseed, &drts, mode == 1 ? &dk : nullptr,
                     mode == 2 ? &dad : nullptr, st);
@@ -585,6 +714,7 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
       return fail(h, "device-to-host copy failed");
   cudaError_t e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail(h, "CUDA error: %s", cudaGetErrorString(e));
+  if (h->profiling) collect_stage_times(h);
   if (rts->status)
     for (int m = 0; m < P; m++)
       if (rts->status[m] != 0) return fail(h, "profile %d failed (status bits 0x%x)", m, rts->status[m]);
@@ -628,6 +758,8 @@ int crtm_gpu_destroy(crtm_gpu_handle h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (auto& s : h->sensors) free_sensor(s);
   h->ws.release(); h->io_in.release(); h->io_out.release(); h->small.release();
+  collect_stage_times(h);
+  for (auto e : h->event_pool) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return CRTM_GPU_SUCCESS;
@@ -692,5 +824,24 @@ int crtm_gpu_last_error(crtm_gpu_handle h, char* buf, int n) {
 }
 
 long long crtm_gpu_launch_count(crtm_gpu_handle h) { return h ? h->launches : 0; }
+
+int crtm_gpu_set_profiling(crtm_gpu_handle h, int enable) {
+  if (!h) return CRTM_GPU_FAILURE;
+  h->profiling = enable != 0;
+  return CRTM_GPU_SUCCESS;
+}
+
+int crtm_gpu_stage_times(crtm_gpu_handle h, double* ms, long long* launches, int n, int reset) {
+  if (!h) return 0;
+  cudaSetDevice(h->device);
+  collect_stage_times(h);
+  for (int i = 0; i < n && i < 8; i++) {
+    if (ms) ms[i] = h->stage_ms[i];
+    if (launches) launches[i] = h->stage_n[i];
+  }
+  if (reset)
+    for (int i = 0; i < 8; i++) { h->stage_ms[i] = 0.0; h->stage_n[i] = 0; }
+  return 6;
+}
 
 }  // extern "C"

@@ -1,20 +1,25 @@
 // CUDA kernels of the clear-sky ODPS + Emission forward / K-matrix / adjoint path.
 //
 // A batch is processed in chunks of profiles.  Per chunk:
-//   prep_kernel        one thread per profile: Map_Input, predictors X, partials D
-//   absorb_fwd_kernel  one thread per (channel, NP profiles): OD(k) = sum C*X
-//                      (ODPS_AtmAbsorption.f90:169-208), reference-layer ODs
-//   column_kernel      one thread per (profile, channel): clamp, path, level
-//                      interpolation (ODPS_AtmAbsorption.f90:213-254), Planck,
-//                      Emission forward (Emission_Module.f90:54-174), Planck
-//                      inversion, and for K/AD the Emission adjoint
-//                      (Emission_Module.f90:280-395) and the optical-depth
-//                      path adjoint (ODPS_AtmAbsorption.f90:487-540)
-//   absorb_ad_kernel   one thread per (channel, NP profiles): contraction of
-//                      the coefficients with the predictor partials and the
-//                      reverse running sums (ODPS_AtmAbsorption.f90:543-598 +
-//                      ODPS_Predictor.f90:1783-2643)
-//   map_kernel         Map_Input adjoint to user layers (ODPS_CoordinateMapping.f90:480-547)
+//   prep_kernel        one warp per profile: Map_Input (ODPS_CoordinateMapping.f90:151-319),
+//                      running sums by warp scans, predictors X
+//                      (ODPS_Predictor.f90:645-1095) and the predictor
+//                      partial-derivative table D; mapping bands for the adjoint
+//   absorb_fwd_kernel  one thread per (channel, NPF profiles): reference-layer
+//                      OD = sum C*X (ODPS_AtmAbsorption.f90:169-208)
+//   column_kernel      one CTA per (profile, 32 channels), one warp per channel,
+//                      layers across lanes: clamp + path + level interpolation
+//                      (ODPS_AtmAbsorption.f90:213-254), Planck, Emission
+//                      (Emission_Module.f90:54-174) as affine warp scans, Planck
+//                      inversion; for K/AD the Emission adjoint
+//                      (Emission_Module.f90:280-395) and the optical-depth path
+//                      adjoint (ODPS_AtmAbsorption.f90:487-540), also as scans
+//   absorb_ad_kernel   one thread per (channel, NPA profiles): coefficient x
+//                      predictor-partial contraction and reverse running sums
+//                      (ODPS_AtmAbsorption.f90:543-598, ODPS_Predictor.f90:1783-2643)
+//   map_kernel         one warp per (profile, channel): Map_Input adjoint to
+//                      user layers (ODPS_CoordinateMapping.f90:480-547), K output
+//   adjoint_*          CRTM_Adjoint: sums over channels, then the Map_Input adjoint
 #pragma once
 
 #include <cuda_runtime.h>
@@ -27,7 +32,10 @@
 
 namespace crtm {
 
-// (slot, variable) pattern of the partial-derivative table as device constants.
+constexpr int MAX_OUT_ABS = 8;   // absorber Jacobians per K-matrix call
+constexpr unsigned FULL = 0xffffffffu;
+
+// (slot, variable) pattern of the partial-derivative table.
 #define CRTM_PD_QCODES_MEMBERS(G)                                                       \
   static constexpr int QA0 = qA<G>(0), QA1 = qA<G>(1), QA2 = qA<G>(2), QA3 = qA<G>(3),  \
                        QA4 = qA<G>(4), QA5 = qA<G>(5);                                  \
@@ -42,21 +50,25 @@ namespace crtm {
 template <int G> struct PdTab;
 template <> struct PdTab<1> {
   CRTM_PD_QCODES_MEMBERS(1)
-  static constexpr int n = PD_NNZ_G1;
   static constexpr int slot[PD_NNZ_G1] = {PD_ENTRIES_G1(CRTM_PD_SLOT)};
   static constexpr int q[PD_NNZ_G1] = {PD_ENTRIES_G1(CRTM_PD_VAR)};
 };
 template <> struct PdTab<2> {
   CRTM_PD_QCODES_MEMBERS(2)
-  static constexpr int n = PD_NNZ_G2;
   static constexpr int slot[PD_NNZ_G2] = {PD_ENTRIES_G2(CRTM_PD_SLOT)};
   static constexpr int q[PD_NNZ_G2] = {PD_ENTRIES_G2(CRTM_PD_VAR)};
 };
 template <> struct PdTab<3> {
   CRTM_PD_QCODES_MEMBERS(3)
-  static constexpr int n = PD_NNZ_G3;
   static constexpr int slot[PD_NNZ_G3] = {PD_ENTRIES_G3(CRTM_PD_SLOT)};
   static constexpr int q[PD_NNZ_G3] = {PD_ENTRIES_G3(CRTM_PD_VAR)};
+};
+
+// Entries of D per layer: the partials, then pdp*A_a (a < JM), pdp*T and the
+// Map_Input adjoint pass mask (bit a set: absorber a passes).
+template <int G> struct DLayout {
+  static constexpr int NNZ = PdNnz<G>::value;
+  static constexpr int NX = NNZ + Group<G>::JM + 2;
 };
 
 // Component of slot s (evaluated at compile time only).
@@ -75,6 +87,100 @@ __device__ __forceinline__ void static_for_impl(F&& f, std::integer_sequence<int
 template <int N, class F>
 __device__ __forceinline__ void static_for(F&& f) {
   static_for_impl(f, std::make_integer_sequence<int, N>{});
+}
+
+// ---------------------------------------------------------------------------
+// Warp scans (lanes own consecutive blocks of elements)
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ T warp_excl_sum(T v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T n = __shfl_up_sync(FULL, v, o);
+    if (lane >= o) v += n;
+  }
+  const T e = __shfl_up_sync(FULL, v, 1);
+  return lane == 0 ? T(0) : e;
+}
+template <class T>
+__device__ __forceinline__ T warp_rexcl_sum(T v) {   // sum over lanes > lane
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T n = __shfl_down_sync(FULL, v, o);
+    if (lane + o < 32) v += n;
+  }
+  const T e = __shfl_down_sync(FULL, v, 1);
+  return lane == 31 ? T(0) : e;
+}
+template <class T>
+__device__ __forceinline__ T warp_excl_prod(T v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T n = __shfl_up_sync(FULL, v, o);
+    if (lane >= o) v *= n;
+  }
+  const T e = __shfl_up_sync(FULL, v, 1);
+  return lane == 0 ? T(1) : e;
+}
+template <class T>
+__device__ __forceinline__ T warp_rexcl_prod(T v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T n = __shfl_down_sync(FULL, v, o);
+    if (lane + o < 32) v *= n;
+  }
+  const T e = __shfl_down_sync(FULL, v, 1);
+  return lane == 31 ? T(1) : e;
+}
+// Affine maps x -> a*x + b.  Forward: lower lanes applied first; on return
+// (a, b) is the composition of the maps of lanes < lane.
+template <class T>
+__device__ __forceinline__ void warp_affine_excl(T& a, T& b) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T an = __shfl_up_sync(FULL, a, o), bn = __shfl_up_sync(FULL, b, o);
+    if (lane >= o) { b = a * bn + b; a = an * a; }
+  }
+  const T ae = __shfl_up_sync(FULL, a, 1), be = __shfl_up_sync(FULL, b, 1);
+  a = lane == 0 ? T(1) : ae;
+  b = lane == 0 ? T(0) : be;
+}
+// Reverse: higher lanes applied first; composition of the maps of lanes > lane.
+template <class T>
+__device__ __forceinline__ void warp_affine_rexcl(T& a, T& b) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T an = __shfl_down_sync(FULL, a, o), bn = __shfl_down_sync(FULL, b, o);
+    if (lane + o < 32) { b = a * bn + b; a = an * a; }
+  }
+  const T ae = __shfl_down_sync(FULL, a, 1), be = __shfl_down_sync(FULL, b, 1);
+  a = lane == 31 ? T(1) : ae;
+  b = lane == 31 ? T(0) : be;
+}
+
+// Vector loads of N consecutive values (N a multiple of 4 floats / 2 doubles,
+// source 16-byte aligned).
+template <class R, int N>
+__device__ __forceinline__ void load_group(const R* __restrict__ src, R* dst) {
+  if constexpr (sizeof(R) == 4) {
+#pragma unroll
+    for (int i = 0; i < N; i += 4) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(src + i));
+      dst[i] = v.x; dst[i + 1] = v.y; dst[i + 2] = v.z; dst[i + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; i += 2) {
+      const double2 v = __ldg(reinterpret_cast<const double2*>(src + i));
+      dst[i] = v.x; dst[i + 1] = v.y;
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -98,71 +204,264 @@ struct SpecView {
   const double* c1, *c2, *b1, *b2, *cbr;
 };
 
-template <class R>
-struct PrepView {
-  R* X;
-  R* D;
-  double* T;
-  double* A;
-  unsigned char* amask;
-  int* band_i0;
-  int* band_n;
-  double* band_w;
-  int* ulev_k1;
-  int* ulev_k2;
-  double* ulev_fac;
-  int* ulay_k0;
-  int* ulay_k1;
-  double* scal;
-  int* status;
-  int K, NS, NNZ, Jm, Kmax;
-
-  __device__ ProfileOut<R> profile(int p) const {
-    ProfileOut<R> o;
-    o.X = X + (size_t)p * K * NS;
-    o.D = D ? D + (size_t)p * K * NNZ : nullptr;
-    o.T = T + (size_t)p * K;
-    o.A = A + (size_t)p * Jm * K;
-    o.amask = amask + (size_t)p * Jm * K;
-    o.band_i0 = band_i0 + (size_t)p * K;
-    o.band_n = band_n + (size_t)p * K;
-    o.band_w = band_w + (size_t)p * K * MAX_BAND;
-    o.ulev_k1 = ulev_k1 + (size_t)p * (Kmax + 1);
-    o.ulev_k2 = ulev_k2 + (size_t)p * (Kmax + 1);
-    o.ulev_fac = ulev_fac + (size_t)p * (Kmax + 1);
-    o.ulay_k0 = ulay_k0 + (size_t)p * Kmax;
-    o.ulay_k1 = ulay_k1 + (size_t)p * Kmax;
-    o.scal = scal + (size_t)p * 4;
-    o.status = status + p;
-    return o;
-  }
+// Running sums of the reference profile (the *_ref terms of ODPS_Predictor.f90:707-759).
+struct RefSums {
+  const double* tz_ref;     // [K]
+  const double* tzp_ref;    // [K]
+  const double* gazp_ref;   // [Jm][K]
+  const double* gatzp_ref;  // [Jm][K]
 };
 
+template <class R>
+struct PrepView {
+  R* Xg;               // [ceil(n/npf)][K][NS][npf]
+  R* Dg;               // [ceil(n/npa)][K][NX][npa] (K/AD only)
+  int* band_i0;        // [n][K]
+  int* band_n;         // [n][K]
+  double* band_w;      // [n][K][MAX_BAND]
+  int* ulev_k1;        // [n][Kmax+1]  0-based reference level bracket of user level i
+  int* ulev_k2;        // [n][Kmax+1]
+  double* ulev_fac;    // [n][Kmax+1]
+  int* rlev_ilo;       // [n][K+1] user levels whose bracket touches reference level j
+  int* rlev_ihi;       // [n][K+1]
+  int* ub_k0;          // [n][Kmax] first reference layer mapping to user layer ku
+  int* ub_n;           // [n][Kmax]
+  double* ub_w;        // [n][Kmax][MAX_UBAND]
+  double* scal;        // [n][4]: sec_surface, u = cos(sensor zenith)
+  int* status;         // [n]
+  int K, Kmax, npf, npa;
+};
+
+template <int G>
+inline size_t prep_smem_bytes(int K) {
+  return sizeof(double) * ((size_t)(4 + 3 * Group<G>::JM) * K + 2 * MAX_LAYERS + 1) +
+         sizeof(int) * (size_t)K;
+}
+
 // ---------------------------------------------------------------------------
-// 1. prep
+// 1. prep: one warp (= one CTA) per profile
 // ---------------------------------------------------------------------------
 template <int G, class R>
-__global__ void prep_kernel(SensorTables S, BatchView b, PrepView<R> pv, const int* idx_map,
-                            int p_begin, int n_chunk) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(32) prep_kernel(SensorTables S, RefSums RS, BatchView b,
+                                                  PrepView<R> pv, const int* __restrict__ idx_map,
+                                                  int p_begin, int n_chunk) {
+  constexpr int JM = Group<G>::JM, NS = Group<G>::NS, NNZ = DLayout<G>::NNZ, NX = DLayout<G>::NX;
+  extern __shared__ double psm[];
+  const int lane = threadIdx.x;
+  const int p = blockIdx.x;
   if (p >= n_chunk) return;
   const int gp = p_begin + p;
-  ProfileIn in;
-  in.n_layers = b.n_layers[gp];
-  in.n_abs = b.n_abs;
-  in.level_pressure = b.level_pressure + (size_t)gp * (b.max_layers + 1);
-  in.pressure = b.pressure + (size_t)gp * b.max_layers;
-  in.temperature = b.temperature + (size_t)gp * b.max_layers;
-  in.absorber = b.absorber + (size_t)gp * b.n_abs * b.max_layers;
-  in.abs_stride = b.max_layers;
-  in.idx_map = idx_map;
-  in.zenith_deg = b.zenith[gp];
-  in.surface_altitude = b.altitude ? b.altitude[gp] : 0.0;
-  if (in.n_layers > b.max_layers) {
-    pv.status[p] = ST_BAD_LAYERS;
+  const int K = S.K, Kmax = pv.Kmax;
+  const int Ku = b.n_layers[gp];
+  if (Ku < 2 || Ku > Kmax || Ku > MAX_LAYERS) {
+    if (lane == 0) pv.status[p] = ST_BAD_LAYERS;
     return;
   }
-  prep_profile<G, R>(S, in, pv.profile(p));
+  double* sT = psm;                      // [K]     mapped temperature
+  double* sA = sT + K;                   // [JM][K] mapped absorber amounts
+  double* sTz = sA + (size_t)JM * K;     // [K]     running sum of T
+  double* sTzp = sTz + K;                // [K]     running sum of pdp*T
+  double* sGz = sTzp + K;                // [JM][K] running sum of pdp*A
+  double* sGt = sGz + (size_t)JM * K;    // [JM][K] running sum of pdp*A*T
+  double* ulnp = sGt + (size_t)JM * K;   // [MAX_LAYERS]
+  double* ulev = ulnp + MAX_LAYERS;      // [MAX_LAYERS+1]
+  int* sPass = reinterpret_cast<int*>(ulev + MAX_LAYERS + 1);  // [K]
+  const double* lev = b.level_pressure + (size_t)gp * (Kmax + 1);
+  const double* lay = b.pressure + (size_t)gp * Kmax;
+  const double* tu = b.temperature + (size_t)gp * Kmax;
+  for (int k = lane; k < Ku; k += 32) ulnp[k] = log(lay[k]);
+  for (int k = lane; k <= Ku; k += 32)
+    ulev[k] = (k == 0) ? ((lev[0] <= 0.0) ? log(lev[1] / 2.0) : log(lev[0])) : log(lev[k]);
+  __syncwarp();
+  int status = ST_OK;
+  int* bi0 = pv.band_i0 + (size_t)p * K;
+  int* bn = pv.band_n + (size_t)p * K;
+  double* bw = pv.band_w + (size_t)p * K * MAX_BAND;
+  // ---- mapping of T and absorbers to the reference layers (lanes stride over layers)
+  for (int k = lane; k < K; k += 32) {
+    const int st = layer_avg_start(S.ref_lnp, K, ulnp, Ku, k);
+    int i0, n;
+    double* w = bw + (size_t)k * MAX_BAND;
+    status |= layer_avg_column(S.ref_lnp, K, ulnp, Ku, k, st, &i0, &n, w);
+    bi0[k] = i0;
+    bn[k] = n;
+    double acc = 0.0;
+    for (int i = 0; i < n; i++) acc += w[i] * tu[i0 + i];
+    sT[k] = acc;
+    int pass = 0;
+#pragma unroll
+    for (int a = 0; a < JM; a++) {
+      const int map = idx_map[a];
+      double v;
+      if (map >= 0) {
+        const double* au = b.absorber + ((size_t)gp * b.n_abs + map) * Kmax;
+        v = 0.0;
+        for (int i = 0; i < n; i++) v += w[i] * au[i0 + i];
+        if (v <= EPS_FP) v = EPS_FP;
+        if (v < S.min_a[a * K + k]) v = S.min_a[a * K + k];
+        if (v > S.max_a[a * K + k]) v = S.max_a[a * K + k];
+        if (v > EPS_FP) pass |= 1 << a;   // ODPS_CoordinateMapping.f90:521-523
+      } else {
+        v = S.ref_a[a * K + k];
+      }
+      sA[a * K + k] = v;
+    }
+    sPass[k] = pass;
+  }
+  __syncwarp();
+  // ---- running sums: contiguous block per lane, warp scan of the block totals
+  {
+    const int per = (K + 31) / 32, k0 = min(K, lane * per), k1 = min(K, k0 + per);
+    for (int qn = 0; qn < 2 + 2 * JM; qn++) {
+      // qn: 0 T, 1 pdp*T, 2+a pdp*A_a, 2+JM+a pdp*A_a*T
+      const int a = (qn < 2) ? 0 : (qn - 2) % JM;
+      double* out = qn == 0 ? sTz : (qn == 1 ? sTzp : (qn < 2 + JM ? sGz + a * K : sGt + a * K));
+      double c = 0.0;
+      for (int k = k0; k < k1; k++) {
+        const double v = qn == 0 ? sT[k] : (qn == 1 ? S.pdp[k] * sT[k]
+                         : (qn < 2 + JM ? S.pdp[k] * sA[a * K + k] : S.pdp[k] * sA[a * K + k] * sT[k]));
+        c += v;
+      }
+      double run = warp_excl_sum(c);
+      for (int k = k0; k < k1; k++) {
+        const double v = qn == 0 ? sT[k] : (qn == 1 ? S.pdp[k] * sT[k]
+                         : (qn < 2 + JM ? S.pdp[k] * sA[a * K + k] : S.pdp[k] * sA[a * K + k] * sT[k]));
+        run += v;
+        out[k] = run;
+      }
+    }
+  }
+  __syncwarp();
+  // ---- height-dependent secants (ODPS_CoordinateMapping.f90:285-306)
+  const Geom g = geometry(b.zenith[gp]);
+  const double alt = b.altitude ? b.altitude[gp] : 0.0;
+  const double psfc = lev[Ku];
+  int sfc_idx = K;
+  double sfc_frac = 0.0;
+  if (S.ref_lev[K] > psfc) {
+    for (int k = K; k >= 0; k--)
+      if (S.ref_lev[k] < psfc) {
+        sfc_idx = k + 1;
+        sfc_frac = (S.ref_lev_lnp[sfc_idx] - ulev[Ku]) / (S.ref_lev_lnp[sfc_idx] - S.ref_lev_lnp[k]);
+        break;
+      }
+  }
+  double zoff;
+  if (S.ref_lev[K] >= psfc)
+    zoff = -(S.zgeo[sfc_idx] + sfc_frac * (S.zgeo[sfc_idx - 1] - S.zgeo[sfc_idx])) + alt;
+  else
+    zoff = CC_H * S.ref_t[K - 1] * log(1013.0 / S.ref_lev[K]);
+  const double sv = (EARTH_RADIUS + alt) * sin(g.trans_zenith_radian);
+  // ---- predictors and partials (lanes stride over layers)
+  const int pgf = p / pv.npf, pof = p % pv.npf;
+  const int pga = pv.npa ? p / pv.npa : 0, poa = pv.npa ? p % pv.npa : 0;
+  for (int k = lane; k < K; k += 32) {
+    LayerState Ls;
+    const double sa = sv / (EARTH_RADIUS + (S.zgeo[k + 1] + zoff));
+    Ls.sec = 1.0 / sqrt(1.0 - sa * sa);
+    Ls.T = sT[k];
+    Ls.Tref = S.ref_t[k];
+    Ls.pdp = S.pdp[k];
+    Ls.tz_ref = RS.tz_ref[k];
+    Ls.tz = sTz[k] / Ls.tz_ref;
+    Ls.tzp_ref = RS.tzp_ref[k];
+    Ls.tzp = sTzp[k] / Ls.tzp_ref;
+#pragma unroll
+    for (int a = 0; a < MAX_ABS; a++) {
+      if (a < JM) {
+        Ls.A[a] = sA[a * K + k];
+        Ls.Aref[a] = S.ref_a[a * K + k];
+        Ls.gazp_ref[a] = RS.gazp_ref[a * K + k];
+        Ls.gatzp_ref[a] = RS.gatzp_ref[a * K + k];
+        Ls.gazp[a] = sGz[a * K + k] / Ls.gazp_ref[a];
+        Ls.gatzp[a] = sGt[a * K + k] / Ls.gatzp_ref[a];
+      } else {
+        Ls.A[a] = Ls.Aref[a] = Ls.gazp[a] = Ls.gatzp[a] = Ls.gazp_ref[a] = Ls.gatzp_ref[a] = 1.0;
+      }
+    }
+    R X[NS];
+    layer_predictors<G, R>(Ls, X);
+    R* xo = pv.Xg + ((size_t)pgf * K + k) * NS * pv.npf + pof;
+#pragma unroll
+    for (int s = 0; s < NS; s++) xo[(size_t)s * pv.npf] = X[s];
+    if (pv.Dg) {
+      R D[NNZ];
+      layer_partials<G, R>(Ls, D);
+      R* dO = pv.Dg + ((size_t)pga * K + k) * NX * pv.npa + poa;
+#pragma unroll
+      for (int e = 0; e < NNZ; e++) dO[(size_t)e * pv.npa] = D[e];
+#pragma unroll
+      for (int a = 0; a < JM; a++) dO[(size_t)(NNZ + a) * pv.npa] = R(Ls.pdp * Ls.A[a]);
+      dO[(size_t)(NNZ + JM) * pv.npa] = R(Ls.pdp * Ls.T);
+      dO[(size_t)(NNZ + JM + 1) * pv.npa] = R(float(sPass[k]));
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) status |= __shfl_xor_sync(FULL, status, o);
+  // ---- reference -> user level brackets (Compute_Interp_Index, sequential on lane 0)
+  int* k1o = pv.ulev_k1 + (size_t)p * (Kmax + 1);
+  int* k2o = pv.ulev_k2 + (size_t)p * (Kmax + 1);
+  double* fo = pv.ulev_fac + (size_t)p * (Kmax + 1);
+  for (int i = lane; i <= Ku; i += 32) { k1o[i] = 0; k2o[i] = 0; }   // every entry a valid level
+  __syncwarp();
+  if (lane == 0) {
+    const double* x = S.ref_lev_lnp;
+    const int nx = K + 1, nu = Ku + 1;
+    int k1 = nu + 1, k2 = 0;
+    for (int iu = 1; iu <= nu; iu++) {
+      if (ulev[iu - 1] < x[0]) { k1o[iu - 1] = 0; k2o[iu - 1] = 0; }
+      else { k1 = iu; break; }
+    }
+    for (int iu = nu; iu >= k1; iu--) {
+      if (ulev[iu - 1] > x[nx - 1]) { k1o[iu - 1] = nx - 1; k2o[iu - 1] = nx - 1; }
+      else { k2 = iu; break; }
+    }
+    int jj = 1;
+    for (int iu = k1; iu <= k2; iu++)
+      for (int ix = jj; ix <= nx - 1; ix++)
+        if (ulev[iu - 1] >= x[ix - 1] && ulev[iu - 1] <= x[ix]) {
+          k1o[iu - 1] = ix - 1; k2o[iu - 1] = ix; jj = ix;
+          break;
+        }
+    for (int i = 0; i < nu; i++) {
+      const int a = k1o[i], c = k2o[i];
+      fo[i] = (a == c) ? 0.0 : (ulev[i] - x[a]) / (x[c] - x[a]);
+    }
+    pv.scal[(size_t)p * 4 + 0] = g.sec_trans_zenith;
+    pv.scal[(size_t)p * 4 + 1] = 1.0 / g.sec_sensor_zenith;  // Common_RTSolution.f90:227
+  }
+  __syncwarp();
+  // ---- reference level j <- user levels whose bracket touches it (path adjoint)
+  int* ilo = pv.rlev_ilo + (size_t)p * (K + 1);
+  int* ihi = pv.rlev_ihi + (size_t)p * (K + 1);
+  for (int jl = lane; jl <= K; jl += 32) {
+    int lo = Ku + 1, hi = -1;
+    for (int i = 0; i <= Ku; i++)
+      if (k1o[i] == jl || k2o[i] == jl) { if (i < lo) lo = i; hi = i; }
+    ilo[jl] = lo;
+    ihi[jl] = hi;
+  }
+  // ---- user layer ku <- reference layers mapping to it (Map_Input adjoint)
+  int* uk0 = pv.ub_k0 + (size_t)p * Kmax;
+  int* un = pv.ub_n + (size_t)p * Kmax;
+  double* uw = pv.ub_w + (size_t)p * Kmax * MAX_UBAND;
+  int ust = 0;
+  for (int ku = lane; ku < Ku; ku += 32) {
+    int k0 = -1, k1 = -1;
+    for (int k = 0; k < K; k++)
+      if (ku >= bi0[k] && ku < bi0[k] + bn[k]) { if (k0 < 0) k0 = k; k1 = k; }
+    int n = (k0 < 0) ? 0 : k1 - k0 + 1;
+    if (n > MAX_UBAND) { ust |= ST_UBAND_OVERFLOW; n = MAX_UBAND; }
+    uk0[ku] = k0 < 0 ? 0 : k0;
+    un[ku] = n;
+    for (int i = 0; i < n; i++) {
+      const int k = k0 + i, r = ku - bi0[k];
+      uw[(size_t)ku * MAX_UBAND + i] = (r >= 0 && r < bn[k]) ? bw[(size_t)k * MAX_BAND + r] : 0.0;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) ust |= __shfl_xor_sync(FULL, ust, o);
+  if (lane == 0) pv.status[p] = status | ust;
 }
 
 // ---------------------------------------------------------------------------
@@ -172,22 +471,22 @@ template <int G, class R, int NP>
 __global__ void __launch_bounds__(128) absorb_fwd_kernel(int K, int L, int n_chunk,
                                                          const float* __restrict__ C,
                                                          const unsigned* __restrict__ cmask,
-                                                         const R* __restrict__ X,
+                                                         const R* __restrict__ Xg,
                                                          R* __restrict__ OD) {
   constexpr int NS = Group<G>::NS, J = Group<G>::J;
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
-  const int p0 = blockIdx.y * NP;
+  const int pg = blockIdx.y;
+  const int p0 = pg * NP;
   const bool active = l < L;
-  const unsigned wmask = __reduce_or_sync(0xffffffffu, active ? cmask[l] : 0u);
+  const unsigned wmask = __reduce_or_sync(FULL, active ? cmask[l] : 0u);
   const int lc = active ? l : 0;
-  const R* Xp[NP];
-#pragma unroll
-  for (int p = 0; p < NP; p++) Xp[p] = X + (size_t)min(p0 + p, n_chunk - 1) * K * NS;
+  const R* Xb = Xg + (size_t)pg * K * NS * NP;
   for (int k = 0; k < K; k++) {
     R acc[NP];
 #pragma unroll
     for (int p = 0; p < NP; p++) acc[p] = R(0);
     const float* Ck = C + (size_t)k * NS * L + lc;
+    const R* Xk = Xb + (size_t)k * NS * NP;
     static_for<J>([&](auto jc) {
       constexpr int j = decltype(jc)::value;
       constexpr int s0 = Group<G>::OFF[j], s1 = Group<G>::OFF[j + 1];
@@ -195,8 +494,10 @@ __global__ void __launch_bounds__(128) absorb_fwd_kernel(int K, int L, int n_chu
 #pragma unroll
       for (int s = s0; s < s1; s++) {
         const R c = R(__ldg(Ck + (size_t)s * L));
+        R x[NP];
+        load_group<R, NP>(Xk + (size_t)s * NP, x);
 #pragma unroll
-        for (int p = 0; p < NP; p++) acc[p] += c * __ldg(Xp[p] + (size_t)k * NS + s);
+        for (int p = 0; p < NP; p++) acc[p] += c * x[p];
       }
     });
     if (active) {
@@ -208,8 +509,17 @@ __global__ void __launch_bounds__(128) absorb_fwd_kernel(int K, int L, int n_chu
 }
 
 // ---------------------------------------------------------------------------
-// 3. per-(profile, channel) column: path, interpolation, Emission, Planck.
-// mode 0: forward; 1: K-matrix; 2: adjoint.
+// 3. column: one thread per (profile, channel), two passes over the user layers.
+//    mode 0 forward, 1 K-matrix, 2 adjoint.
+//
+//    Pass 1 (top down) follows the forward model: OD path and its interpolation
+//    to the user levels, layer transmittance, Planck radiance and the
+//    downwelling recursion.  Pass 2 (bottom up) runs the upwelling recursion
+//    and, alongside it, the Emission adjoint and the OD-path adjoint for a
+//    unit radiance seed.  The Planck-inversion adjoint seed dBT/dR * seed is
+//    known only once the TOA radiance is, so it is written per (profile,
+//    channel) and applied by the kernels that consume the adjoints (the
+//    adjoint is linear in it).
 // ---------------------------------------------------------------------------
 template <class R>
 struct ColumnArgs {
@@ -217,12 +527,13 @@ struct ColumnArgs {
   BatchView b;
   SpecView sp;
   PrepView<R> pv;
-  R* OD;                  // [n_chunk][K][L] in: reference ODs, out (K/AD): OD adjoint
-  R* TAU, *RD, *RU, *TODAD, *BAD;  // [n_chunk][Kmax][L] scratch
+  R* OD;                  // [n][K][L]: in reference ODs, out (K/AD) unit-seed OD adjoint
+  R* TAU, *DTOP;          // [n][Kmax][L] scratch: layer OD and downwelling at the layer top
+  R* PT;                  // [n][Kmax][L] unit-seed Planck part of the temperature adjoint
+  R* SC;                  // [n][L] adjoint seed dBT/dR * seed
   const double* seed;     // [P][L] or null (=1)
   double* radiance, *bt;  // [P][L]
-  double* kt;             // K-matrix: [P][L][Kmax] (Planck part); adjoint: PT scratch [n_chunk][Kmax][L]
-  double* tsk, *ek;       // [P][L] (adjoint: [n_chunk][L] scratch for tsk)
+  double* tsk, *ek;       // K-matrix: [P][L]; adjoint: tsk is [n][L] scratch
   int* status;            // [P] or null
 };
 
@@ -232,120 +543,113 @@ __device__ __forceinline__ R clamp_od(R v) {
 }
 
 template <class R>
-__global__ void __launch_bounds__(256) column_kernel(ColumnArgs<R> a) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)a.n_chunk * a.L) return;
-  const int p = (int)(idx / a.L), l = (int)(idx % a.L);
-  const int gp = a.p_begin + p;
+inline size_t column_smem_bytes(int K, int Kmax) {
+  return sizeof(double) * (size_t)(Kmax + 1) + sizeof(R) * (size_t)Kmax +
+         sizeof(int) * (2 * (size_t)(Kmax + 1) + 2 * (size_t)(K + 1)) + 16;
+}
+
+template <class R>
+__global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int K = a.K, L = a.L, Kmax = a.Kmax;
+  const int p = blockIdx.y, gp = a.p_begin + p;
+  const int tid = threadIdx.x;
+  const int l = blockIdx.x * blockDim.x + tid;
+  double* facd = reinterpret_cast<double*>(smem_raw);   // [Kmax+1]
+  R* tus = reinterpret_cast<R*>(facd + Kmax + 1);        // [Kmax]
+  int* k1s = reinterpret_cast<int*>(tus + Kmax);         // [Kmax+1]
+  int* k2s = k1s + (Kmax + 1);
+  int* ilos = k2s + (Kmax + 1);                          // [K+1]
+  int* ihis = ilos + (K + 1);
   const int st = a.pv.status[p];
-  if (a.status && l == 0) a.status[gp] = st;
   const int Ku = a.b.n_layers[gp];
-  const size_t pl = (size_t)gp * L + l;
+  if (blockIdx.x == 0 && tid == 0 && a.status) a.status[gp] = st;
   if (st != 0) {
-    a.radiance[pl] = 0.0;
-    a.bt[pl] = 0.0;
+    if (l < L) {
+      const size_t pl = (size_t)gp * L + l;
+      a.radiance[pl] = 0.0;
+      a.bt[pl] = 0.0;
+      if (a.mode == 1) { a.tsk[pl] = 0.0; a.ek[pl] = 0.0; }
+      if (a.mode) a.SC[(size_t)p * L + l] = R(0);
+      if (a.mode == 2) a.tsk[(size_t)p * L + l] = 0.0;
+    }
     return;
   }
+  const double* tug = a.b.temperature + (size_t)gp * Kmax;
+  for (int i = tid; i < Kmax; i += blockDim.x) tus[i] = R(i < Ku ? tug[i] : 0.0);
+  const int* k1g = a.pv.ulev_k1 + (size_t)p * (Kmax + 1);
+  const int* k2g = a.pv.ulev_k2 + (size_t)p * (Kmax + 1);
+  const double* fg = a.pv.ulev_fac + (size_t)p * (Kmax + 1);
+  for (int i = tid; i <= Ku; i += blockDim.x) { k1s[i] = k1g[i]; k2s[i] = k2g[i]; facd[i] = fg[i]; }
+  if (a.mode) {
+    const int* ilg = a.pv.rlev_ilo + (size_t)p * (K + 1);
+    const int* ihg = a.pv.rlev_ihi + (size_t)p * (K + 1);
+    for (int i = tid; i <= K; i += blockDim.x) { ilos[i] = ilg[i]; ihis[i] = ihg[i]; }
+  }
+  __syncthreads();
+  if (l >= L) return;
+  const size_t pl = (size_t)gp * L + l;
   const double* sc = a.pv.scal + (size_t)p * 4;
-  const double sec_sfc = sc[0], u = sc[1];
-  const R ru = R(u), rsd = R(1.0 / u);
-  const R rsec = R(sec_sfc);
-  const R c1 = R(a.sp.c1[l]), c2 = R(a.sp.c2[l]), b1 = R(a.sp.b1[l]), b2 = R(a.sp.b2[l]);
-  const double* tu = a.b.temperature + (size_t)gp * Kmax;
-  const double ts = a.b.land_cov[gp] * a.b.land_t[gp] + a.b.water_cov[gp] * a.b.water_t[gp] +
-                    a.b.snow_cov[gp] * a.b.snow_t[gp] + a.b.ice_cov[gp] * a.b.ice_t[gp];
+  const R inv_sec = R(1.0 / sc[0]);
+  const R inv_u = R(1.0 / sc[1]);
+  const double c1d = a.sp.c1[l], c2d = a.sp.c2[l], b1d = a.sp.b1[l], b2d = a.sp.b2[l];
+  const R c1 = R(c1d), c2 = R(c2d), b1 = R(b1d), b2 = R(b2d);
   const double e = a.b.emissivity[pl];
   const R re = R(e), rr = R(1.0 - e);
-  const R Bs = planck_radiance<R>(c1, c2, b1, b2, R(ts));
-  const int* k1 = a.pv.ulev_k1 + (size_t)p * (Kmax + 1);
-  const int* k2 = a.pv.ulev_k2 + (size_t)p * (Kmax + 1);
-  const double* fac = a.pv.ulev_fac + (size_t)p * (Kmax + 1);
+  const double tsd = a.b.land_cov[gp] * a.b.land_t[gp] + a.b.water_cov[gp] * a.b.water_t[gp] +
+                     a.b.snow_cov[gp] * a.b.snow_t[gp] + a.b.ice_cov[gp] * a.b.ice_t[gp];
+  const double ted = b1d + b2d * tsd;
+  const double eed = exp(c2d / ted);
+  const R Bs = R(c1d / (eed - 1.0));
   R* od = a.OD + (size_t)p * K * L + l;
-  const size_t cs = (size_t)p * Kmax * L + l;   // column scratch base, stride L
+  const size_t cs = (size_t)p * Kmax * L + l;   // scratch base, stride L
 
-  // sweep 1 (top -> surface): user-level OD path, layer ODs, downwelling
+  // ---- pass 1 (top down): OD path, user-level interpolation, downwelling
   R cur = R(0), up_prev = R(0), rad_down = R(a.sp.cbr[l]);
-  R src = R(0), tr = R(1);   // forward-only accumulation of the TOA radiance
+  R src = R(0), tr = R(1);   // forward mode: TOA radiance accumulated top down
   int lvl = 0;
   for (int i = 0; i <= Ku; i++) {
-    const int ka = k1[i], kb = k2[i];
+    const int ka = k1s[i], kb = k2s[i];
     while (lvl < ka) { cur += clamp_od(od[(size_t)lvl * L]); lvl++; }
     R upi = cur;
     if (kb != ka) {
       const R yb = cur + clamp_od(od[(size_t)ka * L]);
-      upi = cur + (yb - cur) * R(fac[i]);
+      upi = cur + (yb - cur) * R(facd[i]);
     }
     if (i > 0) {
       const int ku = i - 1;
-      const R tau = (upi - up_prev) / rsec;
-      const R B = planck_radiance<R>(c1, c2, b1, b2, R(tu[ku]));
-      const R d = exp(-tau * rsd);
+      const R tau = (upi - up_prev) * inv_sec;
+      const R t = exp(-tau * inv_u);
+      const R te = b1 + b2 * tus[ku];
+      const R B = c1 / (exp(c2 / te) - R(1));
       if (a.mode == 0) {
-        const R t = exp(-tau / ru);
         src += tr * B * (R(1) - t);
-        tr *= t;
       } else {
         a.TAU[cs + (size_t)ku * L] = tau;
-        a.RD[cs + (size_t)ku * L] = rad_down;
+        a.DTOP[cs + (size_t)ku * L] = rad_down;
       }
-      rad_down = rad_down * d + B * (R(1) - d);
+      tr *= t;
+      rad_down = rad_down * t + B * (R(1) - t);
     }
     up_prev = upi;
   }
-  R rad_toa;
+  const R Dn = rad_down, Tn = tr;
   if (a.mode == 0) {
-    rad_toa = src + tr * (re * Bs + rr * rad_down);
-  } else {
-    // sweep 2 (surface -> top): upwelling radiance
-    R rad_up = re * Bs + rr * rad_down;
-    for (int ku = Ku - 1; ku >= 0; ku--) {
-      const R tau = a.TAU[cs + (size_t)ku * L];
-      const R t = exp(-tau / ru);
-      const R B = planck_radiance<R>(c1, c2, b1, b2, R(tu[ku]));
-      a.RU[cs + (size_t)ku * L] = rad_up;
-      rad_up = rad_up * t + B * (R(1) - t);
-    }
-    rad_toa = rad_up;
+    const double Rd = double(src + Tn * (re * Bs + rr * Dn));
+    a.radiance[pl] = Rd;
+    a.bt[pl] = planck_temperature(c1d, c2d, b1d, b2d, Rd);
+    return;
   }
-  const double Rd = double(rad_toa);
-  const double Td = planck_temperature(a.sp.c1[l], a.sp.c2[l], a.sp.b1[l], a.sp.b2[l], Rd);
-  a.radiance[pl] = Rd;
-  a.bt[pl] = Td;
-  if (a.mode == 0) return;
-
-  // Adjoint: Pre_Process_RTSolution_K (Planck inversion adjoint), then Emission_AD
-  const double seed = a.seed ? a.seed[pl] : 1.0;
-  R up_ad = R(planck_temperature_dR(a.sp.c1[l], a.sp.c2[l], a.sp.b1[l], a.sp.b2[l], Rd) * seed);
-  // sweep 3 (top -> surface): upwelling part
-  for (int ku = 0; ku < Ku; ku++) {
-    const R tau = a.TAU[cs + (size_t)ku * L];
-    const R t = exp(-tau / ru);
-    const R B = planck_radiance<R>(c1, c2, b1, b2, R(tu[ku]));
-    R a_ad = a.RU[cs + (size_t)ku * L] * t * up_ad;
-    const R src_ad = up_ad;
-    up_ad = up_ad * t;
-    a_ad -= B * t * src_ad;
-    a.TODAD[cs + (size_t)ku * L] = -a_ad / ru;
-    a.BAD[cs + (size_t)ku * L] = src_ad * (R(1) - t);
-  }
-  const R e_ad = up_ad * Bs;
-  const R bs_ad = re * up_ad;
-  const R refl_ad = up_ad * rad_down;
-  R down_ad = rr * up_ad;
-  const double ts_ad =
-      a.b.water_cov[gp] * planck_radiance_dT<double>(a.sp.c1[l], a.sp.c2[l], a.sp.b1[l],
-                                                     a.sp.b2[l], ts) * double(bs_ad);
-  if (a.mode == 1) {
-    a.tsk[pl] = ts_ad;
-    a.ek[pl] = double(e_ad - refl_ad);
-  } else {
-    a.tsk[(size_t)p * L + l] = ts_ad;
-  }
-  // sweep 4 (surface -> top): downwelling part, Planck adjoint, OD path adjoint
+  // ---- pass 2 (bottom up): upwelling, Emission adjoint, OD path adjoint (unit seed)
+  R U = re * Bs + rr * Dn;
+  R P = R(1);                 // transmittance of the layers below the current one
+  const R down0 = rr * Tn;    // downwelling adjoint at the surface (unit seed)
+  R cum = R(0);               // OD of the layers below the current one
+  R total = R(0);
+  for (int ku = 0; ku < Ku; ku++) total += a.TAU[cs + (size_t)ku * L];
   R pa_lo = R(0), pa_hi = R(0), suffix = R(0), ua_hi = R(0);
   int plvl = K - 1;
-  auto flush = [&](void) {
+  auto flush = [&]() {
     suffix += pa_hi;
     const R odr = od[(size_t)plvl * L];
     od[(size_t)plvl * L] = (odr < R(0) || odr > R(MAX_OD)) ? R(0) : suffix;
@@ -354,66 +658,111 @@ __global__ void __launch_bounds__(256) column_kernel(ColumnArgs<R> a) {
     plvl--;
   };
   auto scatter = [&](int i, R v) {
-    const int ka = k1[i], kb = k2[i];
+    const int ka = k1s[i], kb = k2s[i];
     while (ka < plvl) flush();
     if (ka == kb) {
       if (ka == plvl) pa_lo += v; else pa_hi += v;
     } else {
-      const R f = R(fac[i]);
-      if (ka == plvl) { pa_lo += (R(1) - f) * v; pa_hi += f * v; }
-      else { pa_hi += (R(1) - f) * v; }   // ka == plvl+1 implies kb > K: unreachable
+      const R f = R(facd[i]);
+      pa_lo += (R(1) - f) * v;
+      pa_hi += f * v;
     }
   };
-  double* kt_row = (a.mode == 1) ? a.kt + pl * Kmax : nullptr;
   for (int ku = Ku - 1; ku >= 0; ku--) {
     const R tau = a.TAU[cs + (size_t)ku * L];
-    const R d = exp(-tau * rsd);
-    const R B = planck_radiance<R>(c1, c2, b1, b2, R(tu[ku]));
-    R a_ad = a.RD[cs + (size_t)ku * L] * d * down_ad;
-    const R src_ad = down_ad;
-    down_ad = down_ad * d;
-    const R bad = a.BAD[cs + (size_t)ku * L] + src_ad * (R(1) - d);
-    a_ad -= B * d * src_ad;
-    const R tod = a.TODAD[cs + (size_t)ku * L] - a_ad * rsd;
-    const R pterm = planck_radiance_dT<R>(c1, c2, b1, b2, R(tu[ku])) * bad;
-    if (a.mode == 1) kt_row[ku] = double(pterm);
-    else a.kt[cs + (size_t)ku * L] = double(pterm);
-    // user-level path adjoint (ODPS_AtmAbsorption.f90:519-530)
-    ua_hi += tod / rsec;
+    const R Dtop = a.DTOP[cs + (size_t)ku * L];
+    const R t = exp(-tau * inv_u);
+    const R te = b1 + b2 * tus[ku];
+    const R ee = exp(c2 / te);
+    const R em1 = ee - R(1);
+    const R B = c1 / em1;
+    const R den = te * em1;
+    const R dB = c1 * c2 * ee * b2 / (den * den);
+    const R Tprev = exp(-(total - cum - tau) * inv_u);   // TOA to the top of this layer
+    // upwelling part (Emission_AD first loop)
+    R tod = -(Tprev * (U - B) * t) * inv_u;
+    R Bad = Tprev * (R(1) - t);
+    // downwelling part (Emission_AD second loop)
+    const R dad = down0 * P;
+    Bad += dad * (R(1) - t);
+    tod -= ((Dtop - B) * t * dad) * inv_u;
+    a.PT[cs + (size_t)ku * L] = dB * Bad;
+    U = t * U + B * (R(1) - t);
+    P *= t;
+    cum += tau;
+    // user-level path adjoint (ODPS_AtmAbsorption.f90:519-530) and its scatter to
+    // the reference levels (Interpolate_Profile_F1_AD), flushing finished layers
+    ua_hi += tod * inv_sec;
     scatter(ku + 1, ua_hi);
-    ua_hi = -tod / rsec;
+    ua_hi = -tod * inv_sec;
   }
   scatter(0, ua_hi);
   while (plvl >= 0) flush();
-  if (a.mode == 1)
-    for (int ku = Ku; ku < Kmax; ku++) kt_row[ku] = 0.0;
+  for (int ku = Ku; ku < Kmax; ku++) a.PT[cs + (size_t)ku * L] = R(0);
+  // ---- TOA radiance, brightness temperature and the adjoint seed
+  const double Rd = double(U);
+  a.radiance[pl] = Rd;
+  a.bt[pl] = planck_temperature(c1d, c2d, b1d, b2d, Rd);
+  const double seed = a.seed ? a.seed[pl] : 1.0;
+  const double scale = planck_temperature_dR(c1d, c2d, b1d, b2d, Rd) * seed;
+  a.SC[(size_t)p * L + l] = R(scale);
+  const double dBs = c1d * c2d * eed * b2d / ((ted * (eed - 1.0)) * (ted * (eed - 1.0)));
+  const double up_final = scale * double(Tn);
+  const double ts_ad = a.b.water_cov[gp] * dBs * e * up_final;
+  if (a.mode == 1) {
+    a.tsk[pl] = ts_ad;
+    a.ek[pl] = up_final * (double(Bs) - double(Dn));   // emissivity_AD - reflectivity_AD
+  } else {
+    a.tsk[(size_t)p * L + l] = ts_ad;
+  }
 }
 
 // ---------------------------------------------------------------------------
-// 4. absorption adjoint: reference-layer adjoints of T and the ODPS absorbers
-//    RA[p][v][k][l], v = 0 temperature, 1+a absorber a.
+// 4. absorption adjoint: reference-layer adjoints RA[p][v][k][l], v = 0 the
+//    temperature, v = 1+j the j-th requested absorber.  CTA = 32 channels
+//    (lanes) x 4 warps, each warp NP profiles; the coefficient slice of layer k
+//    for the CTA's channels is staged in shared memory and used by all warps.
 // ---------------------------------------------------------------------------
-template <int G, class R, int NP>
-__global__ void __launch_bounds__(128) absorb_ad_kernel(int K, int L, int n_chunk,
-                                                        const float* __restrict__ C,
-                                                        const unsigned* __restrict__ cmask,
-                                                        const R* __restrict__ D,
-                                                        const R* __restrict__ ODAD,
-                                                        const double* __restrict__ Tm,
-                                                        const double* __restrict__ Am,
-                                                        const unsigned char* __restrict__ amask,
-                                                        const double* __restrict__ pdp,
-                                                        R* __restrict__ RA) {
+struct OutAbs {
+  int n;                  // requested absorber adjoints
+  int odps[MAX_OUT_ABS];  // ODPS absorber of each, or -1 (absorber unknown to the sensor)
+};
+
+constexpr int AD_WARPS = 4;
+
+// OUTSET 0: adjoints of every ODPS absorber; 1: only absorbers 0 and 1 (H2O and,
+// for groups 1-2, O3), which skips the partials the other absorbers' own
+// adjoints need (their GATzp terms still feed the temperature adjoint).
+template <int G, int OUTSET>
+__host__ __device__ constexpr bool q_needed(int q) {
+  constexpr int JM = Group<G>::JM;
+  if (OUTSET == 0) return true;
+  if (q >= 1 && q <= JM) return (q - 1) < 2;                          // local absorber
+  if (q >= 3 + JM && q < 3 + 2 * JM) return (q - 3 - JM) < 2;          // GAzp
+  return true;
+}
+
+template <int G, class R, int NP, int OUTSET>
+__global__ void __launch_bounds__(32 * AD_WARPS) absorb_ad_kernel(
+    int K, int L, int n_chunk, const float* __restrict__ C, const unsigned* __restrict__ cmask,
+    const R* __restrict__ Dg, const double* __restrict__ pdp_tab, const R* __restrict__ ODAD,
+    const R* __restrict__ SC, OutAbs oa, R* __restrict__ RA) {
   constexpr int NS = Group<G>::NS, JM = Group<G>::JM, NV = Group<G>::NV;
-  constexpr int NNZ = PdNnz<G>::value;
-  const int l = blockIdx.x * blockDim.x + threadIdx.x;
-  const int p0 = blockIdx.y * NP;
+  constexpr int NNZ = DLayout<G>::NNZ, NX = DLayout<G>::NX;
+  __shared__ float cs[NS][32];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int l0 = blockIdx.x * 32, l = l0 + lane;
+  const int pg = blockIdx.y * AD_WARPS + wib;
+  const int p0 = pg * NP;
   const bool active = l < L;
-  const unsigned wmask = __reduce_or_sync(0xffffffffu, active ? cmask[l] : 0u);
-  const int lc = active ? l : 0;
-  int pp[NP];
+  const unsigned wmask = __reduce_or_sync(FULL, active ? cmask[l] : 0u);
+  const int nv = 1 + oa.n;
+  const R* Db = Dg + (size_t)pg * K * NX * NP;
+  const bool group_ok = p0 < n_chunk;
+  R scl[NP];
 #pragma unroll
-  for (int p = 0; p < NP; p++) pp[p] = min(p0 + p, n_chunk - 1);
+  for (int p = 0; p < NP; p++)
+    scl[p] = (active && p0 + p < n_chunk) ? SC[(size_t)(p0 + p) * L + l] : R(0);
   R Stz[NP], Stzp[NP], Sgazp[NP][JM], Sgatzp[NP][JM];
 #pragma unroll
   for (int p = 0; p < NP; p++) {
@@ -422,140 +771,178 @@ __global__ void __launch_bounds__(128) absorb_ad_kernel(int K, int L, int n_chun
     for (int a = 0; a < JM; a++) Sgazp[p][a] = Sgatzp[p][a] = R(0);
   }
   for (int k = K - 1; k >= 0; k--) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < NS * 32; i += 32 * AD_WARPS) {
+      const int s = i >> 5, c = i & 31;
+      cs[s][c] = (l0 + c < L) ? __ldg(C + ((size_t)k * NS + s) * L + l0 + c) : 0.0f;
+    }
+    __syncthreads();
+    if (!group_ok) continue;
     R E[NP][NV];
 #pragma unroll
     for (int p = 0; p < NP; p++)
 #pragma unroll
       for (int q = 0; q < NV; q++) E[p][q] = R(0);
-    const float* Ck = C + (size_t)k * NS * L + lc;
+    const R* Dk = Db + (size_t)k * NX * NP;
     static_for<NNZ>([&](auto ec) {
       constexpr int e = decltype(ec)::value;
       constexpr int s = PdTab<G>::slot[e], q = PdTab<G>::q[e];
       constexpr int j = slot_component<G>(s);
+      if constexpr (!q_needed<G, OUTSET>(q)) return;
       if (!(wmask & (1u << j))) return;
-      const R c = R(__ldg(Ck + (size_t)s * L));
+      const R c = R(cs[s][lane]);
+      R dv[NP];
+      load_group<R, NP>(Dk + (size_t)e * NP, dv);
 #pragma unroll
-      for (int p = 0; p < NP; p++) E[p][q] += c * __ldg(D + ((size_t)pp[p] * K + k) * NNZ + e);
+      for (int p = 0; p < NP; p++) E[p][q] += c * dv[p];
     });
-    const R pd = R(pdp[k]);
+    const R pdp = R(pdp_tab[k]);
 #pragma unroll
     for (int p = 0; p < NP; p++) {
-      const R oda = active ? ODAD[((size_t)pp[p] * K + k) * L + l] : R(0);
+      const bool valid = active && (p0 + p < n_chunk);
+      const R oda = valid ? ODAD[((size_t)(p0 + p) * K + k) * L + l] * scl[p] : R(0);
+      const R pT = __ldg(Dk + (size_t)(NNZ + JM) * NP + p);
+      const unsigned mask = (unsigned)__ldg(Dk + (size_t)(NNZ + JM + 1) * NP + p);
       Stz[p] += oda * E[p][qTz<G>()];
       Stzp[p] += oda * E[p][qTzp<G>()];
-      const R Tk = R(Tm[(size_t)pp[p] * K + k]);
-      R tad = oda * E[p][0] + Stz[p] + pd * Stzp[p];
+      // T_ad(k) = local + S_Tz + pdp*S_Tzp + sum_a (pdp*A_a)*S_GATzp_a
+      R tad = oda * E[p][0] + Stz[p] + pdp * Stzp[p];
       R aad[JM];
 #pragma unroll
       for (int a = 0; a < JM; a++) {
-        Sgazp[p][a] += oda * E[p][qGazp<G>(a)];
         Sgatzp[p][a] += oda * E[p][qGatzp<G>(a)];
-        const R Ak = R(Am[((size_t)pp[p] * JM + a) * K + k]);
-        tad += pd * Ak * Sgatzp[p][a];
-        aad[a] = oda * E[p][qA<G>(a)] + pd * Sgazp[p][a] + pd * Tk * Sgatzp[p][a];
-        if (!amask[((size_t)pp[p] * JM + a) * K + k]) aad[a] = R(0);
+        const R pA = __ldg(Dk + (size_t)(NNZ + a) * NP + p);
+        tad += pA * Sgatzp[p][a];
+        if (OUTSET == 0 || a < 2) {
+          Sgazp[p][a] += oda * E[p][qGazp<G>(a)];
+          // A_ad(k,a) = local + pdp*S_GAzp_a + (pdp*T)*S_GATzp_a, zero where Map_Input's
+          // adjoint blocks it (ODPS_CoordinateMapping.f90:521-523)
+          aad[a] = ((mask >> a) & 1u)
+                       ? oda * E[p][qA<G>(a)] + pdp * Sgazp[p][a] + pT * Sgatzp[p][a]
+                       : R(0);
+        } else {
+          aad[a] = R(0);
+        }
       }
-      if (active && p0 + p < n_chunk) {
-        R* out = RA + (((size_t)(p0 + p) * (1 + JM)) * K + k) * L + l;
+      if (valid) {
+        R* out = RA + ((size_t)(p0 + p) * nv * K + k) * L + l;
         out[0] = tad;
+        for (int jo = 0; jo < oa.n; jo++) {
+          const int aj = oa.odps[jo];
+          R vout = R(0);
 #pragma unroll
-        for (int a = 0; a < JM; a++) out[(size_t)(1 + a) * K * L] = aad[a];
+          for (int a = 0; a < JM; a++)
+            if (a == aj) vout = aad[a];
+          out[(size_t)(1 + jo) * K * L] = vout;
+        }
       }
     }
   }
 }
 
 // ---------------------------------------------------------------------------
-// 5. Map_Input adjoint to user layers: K-matrix outputs.
+// 5. Map_Input adjoint to user layers and the K-matrix outputs.  CTA = one
+//    profile x CT channels: the reference-layer adjoint tiles RA[v][k][CT] and
+//    the Planck part PT[ku][CT] are staged in shared memory, then each warp
+//    writes whole output rows (lanes across user layers).
 // ---------------------------------------------------------------------------
 template <class R>
 struct MapArgs {
-  int K, L, Kmax, Jm, n_abs, p_begin, n_chunk;
+  int K, L, Kmax, p_begin, n_chunk, nv, ct;
   BatchView b;
   PrepView<R> pv;
-  const R* RA;            // [n_chunk][1+Jm][K][L]
-  const int* abs_of_user; // [n_abs]: ODPS absorber index of each user absorber, or -1
-  double* kt;             // [P][L][Kmax] holds the Planck part on entry
-  double* ka;             // [P][L][n_abs][Kmax]
+  const R* RA;   // [n][nv][K][L]
+  const R* PT;   // [n][Kmax][L]
+  const R* SC;   // [n][L]
+  double* kt;    // [P][L][Kmax]
+  double* ka;    // [P][L][nv-1][Kmax]
 };
 
 template <class R>
+inline size_t map_smem_bytes(int K, int Kmax, int nv, int ct) {
+  return sizeof(R) * ((size_t)nv * K * (ct + 1) + (size_t)Kmax * (ct + 1) + ct +
+                      (size_t)Kmax * MAX_UBAND) +
+         sizeof(int) * 2 * (size_t)Kmax + 16;
+}
+
+template <class R>
 __global__ void __launch_bounds__(256) map_kernel(MapArgs<R> m) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)m.n_chunk * m.L) return;
-  const int p = (int)(idx / m.L), l = (int)(idx % m.L);
-  const int gp = m.p_begin + p;
-  const int K = m.K, L = m.L, Kmax = m.Kmax;
-  const size_t pl = (size_t)gp * L + l;
-  double* kt = m.kt + pl * Kmax;
-  double* ka = m.ka + pl * m.n_abs * Kmax;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int K = m.K, L = m.L, Kmax = m.Kmax, nv = m.nv, CT = m.ct, CS = m.ct + 1;
+  const int p = blockIdx.y, gp = m.p_begin + p;
+  const int l0 = blockIdx.x * CT;
+  const int tid = threadIdx.x, wib = tid >> 5, lane = tid & 31;
+  R* rat = reinterpret_cast<R*>(smem_raw);        // [nv][K][CS]
+  R* ptt = rat + (size_t)nv * K * CS;             // [Kmax][CS]
+  R* sct = ptt + (size_t)Kmax * CS;               // [CT]
+  R* uws = sct + CT;                              // [Kmax][MAX_UBAND]
+  int* uk0 = reinterpret_cast<int*>(uws + (size_t)Kmax * MAX_UBAND);
+  int* un = uk0 + Kmax;
   const int Ku = m.pv.status[p] ? 0 : m.b.n_layers[gp];
-  const int* i0 = m.pv.band_i0 + (size_t)p * K;
-  const int* nb = m.pv.band_n + (size_t)p * K;
-  const double* w = m.pv.band_w + (size_t)p * K * MAX_BAND;
-  const int* uk0 = m.pv.ulay_k0 + (size_t)p * Kmax;
-  const int* uk1 = m.pv.ulay_k1 + (size_t)p * Kmax;
-  const R* ra = m.RA + (size_t)p * (1 + m.Jm) * K * L + l;
-  for (int ku = 0; ku < Kmax; ku++) {
-    if (ku >= Ku) {
-      kt[ku] = 0.0;
-      for (int j = 0; j < m.n_abs; j++) ka[(size_t)j * Kmax + ku] = 0.0;
-      continue;
-    }
-    const int ka0 = uk0[ku], ka1 = uk1[ku];
-    double acc = 0.0;
-    for (int k = ka1; k >= ka0; k--) {
-      const int i = ku - i0[k];
-      if (i < 0 || i >= nb[k]) continue;
-      acc += w[k * MAX_BAND + i] * double(ra[(size_t)k * L]);
-    }
-    kt[ku] += acc;
-    for (int j = 0; j < m.n_abs; j++) {
-      const int a = m.abs_of_user[j];
-      double acc_a = 0.0;
-      if (a >= 0) {
-        const R* rav = ra + (size_t)(1 + a) * K * L;
-        for (int k = ka1; k >= ka0; k--) {
-          const int i = ku - i0[k];
-          if (i < 0 || i >= nb[k]) continue;
-          acc_a += w[k * MAX_BAND + i] * double(rav[(size_t)k * L]);
-        }
+  const int ncl = min(CT, L - l0);
+  for (int i = tid; i < nv * K * CT; i += 256) {
+    const int row = i / CT, c = i % CT;
+    rat[(size_t)row * CS + c] = c < ncl ? m.RA[((size_t)p * nv * K + row) * L + l0 + c] : R(0);
+  }
+  for (int i = tid; i < Kmax * CT; i += 256) {
+    const int ku = i / CT, c = i % CT;
+    ptt[(size_t)ku * CS + c] = (c < ncl && ku < Ku) ? m.PT[((size_t)p * Kmax + ku) * L + l0 + c] : R(0);
+  }
+  for (int c = tid; c < CT; c += 256) sct[c] = c < ncl ? m.SC[(size_t)p * L + l0 + c] : R(0);
+  for (int i = tid; i < Kmax; i += 256) {
+    uk0[i] = i < Ku ? m.pv.ub_k0[(size_t)p * Kmax + i] : 0;
+    un[i] = i < Ku ? m.pv.ub_n[(size_t)p * Kmax + i] : 0;
+  }
+  for (int i = tid; i < Kmax * MAX_UBAND; i += 256)
+    uws[i] = R(m.pv.ub_w[(size_t)p * Kmax * MAX_UBAND + i]);
+  __syncthreads();
+  for (int c = wib; c < ncl; c += 8) {
+    const size_t pl = (size_t)gp * L + l0 + c;
+    const R scl = sct[c];
+    for (int v = 0; v < nv; v++) {
+      double* out = v == 0 ? m.kt + pl * Kmax : m.ka + (pl * (nv - 1) + (v - 1)) * Kmax;
+      const R* rav = rat + (size_t)v * K * CS + c;
+      for (int ku = lane; ku < Kmax; ku += 32) {
+        if (ku >= Ku) { out[ku] = 0.0; continue; }
+        R acc = (v == 0) ? ptt[(size_t)ku * CS + c] * scl : R(0);
+        const int k0 = uk0[ku], n = un[ku];
+        for (int i = n - 1; i >= 0; i--) acc += uws[ku * MAX_UBAND + i] * rav[(size_t)(k0 + i) * CS];
+        out[ku] = double(acc);
       }
-      ka[(size_t)j * Kmax + ku] = acc_a;
     }
   }
 }
 
 // ---------------------------------------------------------------------------
-// Adjoint mode: sums over channels, then the Map_Input adjoint per profile.
+// 6. CRTM_Adjoint: sums over channels in a fixed order, then the Map_Input adjoint.
 // ---------------------------------------------------------------------------
-// rows [n_chunk][nrow][L] -> out [n_chunk][nrow]; one warp per row.
+// out[row] = sum_l in[row][l] * (w ? w[row / rows_per_w][l] : 1); one warp per row.
 template <class T>
-__global__ void sum_channels_kernel(const T* __restrict__ in, double* __restrict__ out,
-                                    long long n_rows, int L) {
+__global__ void channel_sum_kernel(const T* __restrict__ in, const T* __restrict__ w,
+                                   int rows_per_w, long long n_rows, int L, double* __restrict__ out) {
   const long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (row >= n_rows) return;
   const T* r = in + row * L;
+  const T* wr = w ? w + (row / rows_per_w) * L : nullptr;
   double acc = 0.0;
-  for (int l = lane; l < L; l += 32) acc += double(r[l]);
+  for (int l = lane; l < L; l += 32) acc += double(r[l]) * (wr ? double(wr[l]) : 1.0);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL, acc, o);
   if (lane == 0) out[row] = acc;
 }
 
 template <class R>
 struct AdjMapArgs {
-  int K, Kmax, Jm, n_abs, p_begin, n_chunk;
+  int K, Kmax, nv, p_begin, n_chunk;
   BatchView b;
   PrepView<R> pv;
-  const double* ras;      // [n_chunk][1+Jm][K] channel sums of RA
-  const double* pts;      // [n_chunk][Kmax] channel sums of the Planck part
-  const double* tss;      // [n_chunk] channel sums of the skin temperature adjoint
-  const int* abs_of_user;
-  double* t_ad;           // [P][Kmax]
-  double* a_ad;           // [P][n_abs][Kmax]
-  double* ts_ad;          // [P]
+  const double* ras;   // [n][nv][K] channel sums of RA
+  const double* pts;   // [n][Kmax] channel sums of SC * PT
+  const double* tss;   // [n] channel sums of the skin temperature adjoint
+  double* t_ad;        // [P][Kmax]
+  double* a_ad;        // [P][nv-1][Kmax]
+  double* ts_ad;       // [P]
 };
 
 template <class R>
@@ -564,38 +951,18 @@ __global__ void adjoint_map_kernel(AdjMapArgs<R> m) {
   if (idx >= (long long)m.n_chunk * m.Kmax) return;
   const int p = (int)(idx / m.Kmax), ku = (int)(idx % m.Kmax);
   const int gp = m.p_begin + p;
-  const int K = m.K, Kmax = m.Kmax;
+  const int K = m.K, Kmax = m.Kmax, nv = m.nv;
   const int Ku = m.pv.status[p] ? 0 : m.b.n_layers[gp];
   if (ku == 0) m.ts_ad[gp] = m.tss[p];
-  double* to = m.t_ad + (size_t)gp * Kmax;
-  double* ao = m.a_ad + (size_t)gp * m.n_abs * Kmax;
-  if (ku >= Ku) {
-    to[ku] = 0.0;
-    for (int j = 0; j < m.n_abs; j++) ao[(size_t)j * Kmax + ku] = 0.0;
-    return;
-  }
-  const int* i0 = m.pv.band_i0 + (size_t)p * K;
-  const int* nb = m.pv.band_n + (size_t)p * K;
-  const double* w = m.pv.band_w + (size_t)p * K * MAX_BAND;
-  const int k0 = m.pv.ulay_k0[(size_t)p * Kmax + ku], k1 = m.pv.ulay_k1[(size_t)p * Kmax + ku];
-  const double* ras = m.ras + (size_t)p * (1 + m.Jm) * K;
-  double acc = m.pts[(size_t)p * Kmax + ku];
-  for (int k = k1; k >= k0; k--) {
-    const int i = ku - i0[k];
-    if (i < 0 || i >= nb[k]) continue;
-    acc += w[k * MAX_BAND + i] * ras[k];
-  }
-  to[ku] = acc;
-  for (int j = 0; j < m.n_abs; j++) {
-    const int a = m.abs_of_user[j];
-    double acc_a = 0.0;
-    if (a >= 0)
-      for (int k = k1; k >= k0; k--) {
-        const int i = ku - i0[k];
-        if (i < 0 || i >= nb[k]) continue;
-        acc_a += w[k * MAX_BAND + i] * ras[(size_t)(1 + a) * K + k];
-      }
-    ao[(size_t)j * Kmax + ku] = acc_a;
+  for (int v = 0; v < nv; v++) {
+    double* out = v == 0 ? m.t_ad + (size_t)gp * Kmax : m.a_ad + ((size_t)gp * (nv - 1) + (v - 1)) * Kmax;
+    if (ku >= Ku) { out[ku] = 0.0; continue; }
+    double acc = (v == 0) ? m.pts[(size_t)p * Kmax + ku] : 0.0;
+    const int k0 = m.pv.ub_k0[(size_t)p * Kmax + ku], n = m.pv.ub_n[(size_t)p * Kmax + ku];
+    const double* uw = m.pv.ub_w + ((size_t)p * Kmax + ku) * MAX_UBAND;
+    const double* row = m.ras + ((size_t)p * nv + v) * K;
+    for (int i = n - 1; i >= 0; i--) acc += uw[i] * row[k0 + i];
+    out[ku] = acc;
   }
 }
 

@@ -20,7 +20,8 @@ namespace crtm {
 
 constexpr int MAX_LAYERS = 200;     // MAX_N_LAYERS (src/CRTM_Parameters.f90:64)
 constexpr int MAX_ABS = 6;          // ODPS absorbers of group 1
-constexpr int MAX_BAND = 24;        // user layers per reference layer in the mapping weights
+constexpr int MAX_BAND = 32;        // user layers per reference layer in the mapping weights
+constexpr int MAX_UBAND = 16;       // reference layers per user layer (transposed band)
 constexpr double PI_D = 3.141592653589793238462643383279;
 constexpr double DEG2RAD = PI_D / 180.0;
 constexpr double MAX_TRANS_ZENITH_ANGLE = 63.6122;   // CRTM_Parameters.f90:205
@@ -39,6 +40,7 @@ enum : int {
   ST_BAD_LAYERS = 1,      // layer count out of range
   ST_BAND_OVERFLOW = 2,   // mapping band wider than MAX_BAND
   ST_LAYERAVG_FAIL = 4,   // degenerate pressure grid in the layer averaging
+  ST_UBAND_OVERFLOW = 8,  // more than MAX_UBAND reference layers map to one user layer
 };
 
 // ---------------------------------------------------------------------------
@@ -430,89 +432,123 @@ CRTM_HD Geom geometry(double zenith_deg) {
 }
 
 // ---------------------------------------------------------------------------
-// Layer-averaging weights of user layers for each reference layer
+// Layer-averaging weights of user layers for one reference layer ki
 // (LayerAvg, ODPS_CoordinateMapping.f90:1108-1320).  px1: reference layer
-// ln p (n1), px2: user layer ln p (n2).  Writes band start i0[k], width
-// nw[k] and normalised weights w[k*MAX_BAND + i].  Returns status bits.
+// ln p (kn1 of them), px2: user layer ln p (kn2).  Writes the band start i0,
+// width nw and normalised weights w[0..nw).  `istart` is where the search
+// over user layers begins: the reference passes the previous column's first
+// weight index; any index not after the column's first contributing user
+// layer gives the same weights (user layers below it cannot contribute), so
+// columns can also be computed independently from a binary-search bound
+// (layer_avg_start).  Returns status bits.
 // ---------------------------------------------------------------------------
+CRTM_HD void layer_avg_edges(const double* px1, int kn1, const double* px2, int kn2, int ki,
+                             double& z1, double& z2, double& z3, int& iskip) {
+  z2 = px1[ki];
+  z1 = (ki == 0) ? 2.0 * z2 - px1[ki + 1] : px1[ki - 1];
+  z3 = (ki == kn1 - 1) ? 2.0 * z2 - z1 : px1[ki + 1];
+  if (z3 > px2[kn2 - 1]) z3 = px2[kn2 - 1];
+  iskip = 0;
+  if (z2 >= px2[kn2 - 1]) { z3 = px2[kn2 - 1]; z2 = px2[kn2 - 1]; iskip = 1; }
+}
+
+// First user layer j (0-based) with px2[j+1] > min(z1,z2,z3): no user layer
+// before it contributes to column ki.
+CRTM_HD int layer_avg_start(const double* px1, int kn1, const double* px2, int kn2, int ki) {
+  double z1, z2, z3;
+  int iskip;
+  layer_avg_edges(px1, kn1, px2, kn2, ki, z1, z2, z3, iskip);
+  double zmin = z1 < z2 ? z1 : z2;
+  if (z3 < zmin) zmin = z3;
+  int lo = 0, hi = kn2 - 1;  // answer in [0, kn2-1]
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (px2[mid + 1] > zmin) hi = mid; else lo = mid + 1;
+  }
+  return lo;
+}
+
+CRTM_HD int layer_avg_column(const double* px1, int kn1, const double* px2, int kn2, int ki,
+                             int istart, int* i0, int* nw, double* w) {
+  const double SMALLDIFF = 1.0e-20;
+  double z1, z2, z3;
+  int iskip;
+  layer_avg_edges(px1, kn1, px2, kn2, ki, z1, z2, z3, iskip);
+  double pz[MAX_BAND + 2];
+  for (int i = 0; i < MAX_BAND + 2; i++) pz[i] = 0.0;
+  int ic = 0, jend = kn2 - 1, j, bad = 0;
+  for (j = istart; j < kn2 - 1; j++) {
+    if (px2[j] > z3) { jend = j; break; }
+    for (int pass = 0; pass < 2; pass++) {
+      const double za = pass == 0 ? z1 : z3;  // the edge used by this half-layer
+      const bool hit = pass == 0 ? (px2[j] <= z2 && px2[j + 1] > z1)
+                                 : (px2[j] < z3 && px2[j + 1] >= z2 && iskip == 0);
+      if (!hit) continue;
+      const double zb = pass == 0 ? z3 : z1;  // the opposite edge
+      int itop = 0, ibot = 0;
+      double y1, y2;
+      if (za < zb) {
+        y1 = za; if (px2[j] > za) { y1 = px2[j]; itop = 1; }
+        y2 = z2; if (px2[j + 1] < z2) { y2 = px2[j + 1]; ibot = 1; }
+      } else {
+        y1 = z2; if (px2[j] > z2) { y1 = px2[j]; itop = 1; }
+        y2 = za; if (px2[j + 1] < za) { y2 = px2[j + 1]; ibot = 1; }
+      }
+      const double dy = y2 - y1, dz = za - z2;
+      if (fabs(dz) < SMALLDIFF) { bad = 1; break; }
+      const double dzd = 1.0 / dz;
+      double zw1 = (za - y1) * dzd * dy, zw2 = (za - y2) * dzd * dy;
+      const double dx = px2[j + 1] - px2[j];
+      if (fabs(dx) < SMALLDIFF) { bad = 1; break; }
+      const double d = (px2[j + 1] - z2) * (1.0 / dx);
+      if (za < zb && ibot == 0) { zw1 = zw1 + zw2 * d; zw2 = zw2 * (1.0 - d); }
+      else if (za > zb && itop == 0) { zw2 = zw2 + zw1 * (1.0 - d); zw1 = zw1 * d; }
+      const int r = j - istart;
+      if (r + 1 >= MAX_BAND + 2) { bad = 2; break; }
+      pz[r] += zw1; pz[r + 1] += zw2; ic = 1;
+    }
+    if (bad) break;
+  }
+  if (bad) {
+    *i0 = istart < kn2 ? istart : kn2 - 1; *nw = 1; w[0] = 1.0;
+    return (bad == 2) ? ST_BAND_OVERFLOW : ST_LAYERAVG_FAIL;
+  }
+  if (j >= kn2 - 1) jend = kn2 - 1;
+  if (ic == 0) {
+    const int r = jend - istart;
+    if (r < 0 || r >= MAX_BAND + 2) { *i0 = jend; *nw = 1; w[0] = 1.0; return ST_OK; }
+    pz[r] = 1.0;
+  }
+  int f = -1;
+  for (int r = 0; r < MAX_BAND + 2 && istart + r < kn2; r++)
+    if (pz[r] != 0.0) { f = r; break; }
+  if (f < 0) f = 0;
+  int n = 0;
+  for (int r = f; r < MAX_BAND + 2 && istart + r < kn2; r++) {
+    if (pz[r] == 0.0) break;
+    n++;
+  }
+  int status = ST_OK;
+  if (n > MAX_BAND) { status = ST_BAND_OVERFLOW; n = MAX_BAND; }
+  double zsum = 0.0;
+  for (int r = f; r < f + n; r++) zsum += pz[r];
+  *i0 = istart + f;
+  *nw = n;
+  for (int r = 0; r < n; r++) w[r] = pz[f + r] / zsum;
+  return status;
+}
+
+// All columns in the reference's order.  Each search starts at the later of
+// the previous column's first weight index (the reference's start) and the
+// column's binary-search bound, which keeps the band inside the fixed window.
 CRTM_HD int layer_avg_weights(const double* px1, int kn1, const double* px2, int kn2, int* i0,
                               int* nw, double* w) {
   int status = ST_OK, istart = 0;
-  const double SMALLDIFF = 1.0e-20;
   for (int ki = 0; ki < kn1; ki++) {
-    double z2 = px1[ki];
-    double z1 = (ki == 0) ? 2.0 * z2 - px1[ki + 1] : px1[ki - 1];
-    double z3 = (ki == kn1 - 1) ? 2.0 * z2 - z1 : px1[ki + 1];
-    if (z3 > px2[kn2 - 1]) z3 = px2[kn2 - 1];
-    int iskip = 0;
-    if (z2 >= px2[kn2 - 1]) { z3 = px2[kn2 - 1]; z2 = px2[kn2 - 1]; iskip = 1; }
-    // band-local accumulation: user layers istart .. istart+MAX_BAND+1
-    double pz[MAX_BAND + 2];
-    for (int i = 0; i < MAX_BAND + 2; i++) pz[i] = 0.0;
-    int ic = 0, jend = kn2 - 1, j, bad = 0;
-    for (j = istart; j < kn2 - 1; j++) {
-      if (px2[j] > z3) { jend = j; break; }
-      for (int pass = 0; pass < 2; pass++) {
-        double za = pass == 0 ? z1 : z3;  // the outer edge used by this half
-        bool hit = pass == 0 ? (px2[j] <= z2 && px2[j + 1] > z1)
-                             : (px2[j] < z3 && px2[j + 1] >= z2 && iskip == 0);
-        if (!hit) continue;
-        double zb = pass == 0 ? z3 : z1;  // the opposite edge
-        int itop = 0, ibot = 0;
-        double y1, y2;
-        if (za < zb) {
-          y1 = za; if (px2[j] > za) { y1 = px2[j]; itop = 1; }
-          y2 = z2; if (px2[j + 1] < z2) { y2 = px2[j + 1]; ibot = 1; }
-        } else {
-          y1 = z2; if (px2[j] > z2) { y1 = px2[j]; itop = 1; }
-          y2 = za; if (px2[j + 1] < za) { y2 = px2[j + 1]; ibot = 1; }
-        }
-        double dy = y2 - y1, dz = za - z2;
-        if (fabs(dz) < SMALLDIFF) { bad = 1; break; }
-        double dzd = 1.0 / dz;
-        double zw1 = (za - y1) * dzd * dy, zw2 = (za - y2) * dzd * dy;
-        double dx = px2[j + 1] - px2[j];
-        if (fabs(dx) < SMALLDIFF) { bad = 1; break; }
-        double d = (px2[j + 1] - z2) * (1.0 / dx);
-        if (za < zb && ibot == 0) { zw1 = zw1 + zw2 * d; zw2 = zw2 * (1.0 - d); }
-        else if (za > zb && itop == 0) { zw2 = zw2 + zw1 * (1.0 - d); zw1 = zw1 * d; }
-        const int r = j - istart;
-        if (r + 1 >= MAX_BAND + 2) { bad = 2; break; }
-        pz[r] += zw1; pz[r + 1] += zw2; ic = 1;
-      }
-      if (bad) break;
-    }
-    if (bad) {
-      status |= (bad == 2) ? ST_BAND_OVERFLOW : ST_LAYERAVG_FAIL;
-      i0[ki] = istart; nw[ki] = 1; w[ki * MAX_BAND] = 1.0;
-      continue;
-    }
-    if (j >= kn2 - 1) jend = kn2 - 1;
-    if (ic == 0) {
-      const int r = jend - istart;
-      if (r < 0 || r >= MAX_BAND + 2) {
-        status |= ST_BAND_OVERFLOW;
-        i0[ki] = istart; nw[ki] = 1; w[ki * MAX_BAND] = 1.0;
-        continue;
-      }
-      pz[r] = 1.0;
-    }
-    int f = -1;
-    for (int r = 0; r < MAX_BAND + 2 && istart + r < kn2; r++)
-      if (pz[r] != 0.0) { f = r; break; }
-    if (f < 0) f = 0;
-    int n = 0;
-    for (int r = f; r < MAX_BAND + 2 && istart + r < kn2; r++) {
-      if (pz[r] == 0.0) break;
-      n++;
-    }
-    if (n > MAX_BAND) { status |= ST_BAND_OVERFLOW; n = MAX_BAND; }
-    double zsum = 0.0;
-    for (int r = f; r < f + n; r++) zsum += pz[r];
-    i0[ki] = istart + f;
-    nw[ki] = n;
-    for (int r = 0; r < n; r++) w[ki * MAX_BAND + r] = pz[f + r] / zsum;
-    istart = istart + f;
+    const int lb = layer_avg_start(px1, kn1, px2, kn2, ki);
+    status |= layer_avg_column(px1, kn1, px2, kn2, ki, istart > lb ? istart : lb, i0 + ki, nw + ki,
+                               w + ki * MAX_BAND);
+    istart = i0[ki];
   }
   return status;
 }

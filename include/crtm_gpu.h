@@ -92,9 +92,16 @@ typedef struct {
 
 typedef struct {
   double* temperature;        /* [P][L][max_layers] */
-  double* absorber;           /* [P][L][n_absorbers][max_layers] */
+  double* absorber;           /* [P][L][n_k][max_layers], n_k = n_k_absorbers or n_absorbers */
   double* water_temperature;  /* [P][L] Surface_K%Water_Temperature */
   double* surface_emissivity; /* [P][L] RTSolution_K%Surface_Emissivity */
+  /* Optional selection of absorber Jacobians: when n_k_absorbers > 0 only the
+   * user absorbers k_absorber_index[0..n_k_absorbers-1] (host pointer, 0-based
+   * indices into the batch's absorbers) are written, in that order.  The
+   * reference always fills Atmosphere_K%Absorber for every absorber; callers
+   * that use only some of them save the rest of the output traffic. */
+  int n_k_absorbers;
+  const int* k_absorber_index;
 } crtm_gpu_kmatrix;
 
 typedef struct {
@@ -148,6 +155,16 @@ int crtm_gpu_last_error(crtm_gpu_handle handle, char* buf, int n);
 
 /* Number of kernel launches the handle has issued since creation. */
 long long crtm_gpu_launch_count(crtm_gpu_handle handle);
+
+/* Stage timing (no reference counterpart; the reference's only timing hook is
+ * the compile-time enable_timing flag, CRTM_Forward_Module.f90:265).  When
+ * enabled, every kernel launch is bracketed by CUDA events on the launch
+ * stream.  crtm_gpu_stage_times synchronises the handle's pending work and
+ * returns, per stage, the accumulated milliseconds and launch counts since the
+ * last reset: stages 0 prep, 1 absorb_fwd, 2 column, 3 absorb_ad, 4 map_out,
+ * 5 adjoint_sum.  Returns the number of stages. */
+int crtm_gpu_set_profiling(crtm_gpu_handle handle, int enable);
+int crtm_gpu_stage_times(crtm_gpu_handle handle, double* ms, long long* launches, int n, int reset);
 
 #ifdef __cplusplus
 }

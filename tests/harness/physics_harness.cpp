@@ -67,3 +67,41 @@ int hx_prep(int group, int K, const double* ref_lev, const double* ref_p, const 
   return status;
 }
 }
+
+extern "C" {
+// Layer-averaging bands computed in the reference's sequential order and
+// column by column from the binary-search start; returns 1 if they differ.
+int hx_layer_avg_compare(const double* px1, int kn1, const double* px2, int kn2, int* max_band) {
+  std::vector<int> a0(kn1), an(kn1), b0(kn1), bn(kn1);
+  std::vector<double> aw((size_t)kn1 * MAX_BAND), bw((size_t)kn1 * MAX_BAND);
+  int sa = layer_avg_weights(px1, kn1, px2, kn2, a0.data(), an.data(), aw.data());
+  int sb = 0;
+  for (int ki = 0; ki < kn1; ki++) {
+    int st = layer_avg_start(px1, kn1, px2, kn2, ki);
+    sb |= layer_avg_column(px1, kn1, px2, kn2, ki, st, &b0[ki], &bn[ki], &bw[(size_t)ki * MAX_BAND]);
+  }
+  int mb = 0;
+  for (int ki = 0; ki < kn1; ki++) {
+    if (an[ki] > mb) mb = an[ki];
+    if (a0[ki] != b0[ki] || an[ki] != bn[ki]) return 1;
+    for (int r = 0; r < an[ki]; r++)
+      if (aw[(size_t)ki * MAX_BAND + r] != bw[(size_t)ki * MAX_BAND + r]) return 1;
+  }
+  *max_band = mb;
+  return (sa != sb) ? 2 : 0;
+}
+}
+extern "C" int hx_layer_avg_debug(const double* px1, int kn1, const double* px2, int kn2, int* out) {
+  std::vector<int> a0(kn1), an(kn1);
+  std::vector<double> aw((size_t)kn1 * MAX_BAND);
+  layer_avg_weights(px1, kn1, px2, kn2, a0.data(), an.data(), aw.data());
+  for (int ki = 0; ki < kn1; ki++) {
+    int b0, bn; double bw[MAX_BAND];
+    int st = layer_avg_start(px1, kn1, px2, kn2, ki);
+    layer_avg_column(px1, kn1, px2, kn2, ki, st, &b0, &bn, bw);
+    int prev = ki ? a0[ki-1] : 0;
+    if (a0[ki] != b0 || an[ki] != bn) { out[0]=ki; out[1]=a0[ki]; out[2]=an[ki]; out[3]=b0; out[4]=bn; out[5]=st; out[6]=prev; return 1; }
+    for (int r = 0; r < bn; r++) if (aw[(size_t)ki*MAX_BAND+r] != bw[r]) { out[0]=ki; out[1]=-r; out[5]=st; out[6]=prev; return 2; }
+  }
+  return 0;
+}

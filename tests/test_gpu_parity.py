@@ -97,3 +97,38 @@ def test_odd_sizes(gpu_lib, coeff_dir):
         ref = Oracle(coeff_dir, sensor).k_matrix(atm, sfc, geo, opt)
         assert np.abs(rts.brightness_temperature - ref["bt"]).max() < 1e-4
         assert _rel(km.temperature, ref["temperature_k"]) < 1e-6
+
+
+def test_k_matrix_absorber_selection(gpu_lib, coeff_dir):
+    """Only the selected absorber Jacobians are written, in the selected order."""
+    from oracle.pyoracle import Oracle
+    sensor = "irsynth_c616"
+    atm, sfc, geo, opt = _case(sensor, 2, 101, 11)
+    h = gpu_lib.CRTM([sensor], coeff_dir, 0)
+    ids = list(atm.absorber_id)
+    sel = [ids.index(3), ids.index(1)]
+    km, rts = h.k_matrix(atm, sfc, geo, opt, k_absorbers=sel)
+    ref = Oracle(coeff_dir, sensor).k_matrix(atm, sfc, geo, opt)
+    assert km.absorber.shape[2] == 2
+    for j, ja in enumerate(sel):
+        assert _rel(km.absorber[:, :, j], ref["absorber_k"][:, :, ja]) < 1e-5
+
+
+def test_device_entry_points_and_stage_times(gpu_lib, coeff_dir):
+    """The device-resident K-matrix equals the host call; stage timing covers every stage."""
+    import torch
+    sensor = "irsynth_c616"
+    atm, sfc, geo, opt = _case(sensor, 3, 101, 21)
+    h = gpu_lib.CRTM([sensor], coeff_dir, 1)
+    km, rts = h.k_matrix(atm, sfc, geo, opt)
+    import bench
+    b, keep, t = bench.device_batch(torch, h, atm, sfc, geo, opt, torch.device("cuda"))
+    out = bench.k_outputs(torch, 3, h.n_channels[0], atm.max_layers, atm.n_absorbers, torch.device("cuda"))
+    h.set_profiling(True)
+    h.k_matrix_device(b, out, None, 0, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    st = h.stage_times()
+    assert np.array_equal(out["bt"].cpu().numpy(), rts.brightness_temperature)
+    assert np.array_equal(out["temperature_k"].cpu().numpy(), km.temperature)
+    for s in ("prep", "absorb_fwd", "column", "absorb_ad", "map_out"):
+        assert st[s][1] >= 1 and st[s][0] > 0.0
