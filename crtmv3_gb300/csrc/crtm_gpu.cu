@@ -99,12 +99,12 @@ struct Records {
 // ---------------------------------------------------------------------------
 struct Sensor {
   std::string id;
-  int group = 0, K = 0, J = 0, Jm = 0, L = 0, sensor_type = 0, h2o_idx = 0, NS = 0;
+  int group = 0, K = 0, J = 0, Jm = 0, L = 0, Lp = 0, sensor_type = 0, h2o_idx = 0, NS = 0;
   std::vector<int> absorber_id;
   std::vector<double> ref_lev, ref_p, ref_t, ref_a, min_a, max_a;  // [Jm][K] for absorbers
   std::vector<double> c1, c2, b1, b2, cbr;
   // device
-  float* d_C = nullptr;          // [K][NS][L]
+  float* d_C = nullptr;          // [K][NS][Lp]
   unsigned* d_cmask = nullptr;   // [L]
   double* d_tab = nullptr;       // concatenated tables
   double* d_spec = nullptr;      // c1,c2,b1,b2,cbr [5][L]
@@ -174,7 +174,9 @@ bool load_sensor(const std::string& dir, const std::string& id, Sensor& s, std::
   }
   // dense coefficient array [K][NS][L] and component masks
   const int K = s.K, L = s.L, NS = s.NS;
-  std::vector<float> Cd((size_t)K * NS * L, 0.0f);
+  s.Lp = (L + 31) / 32 * 32;   // 128-byte aligned coefficient rows
+  const int Lp = s.Lp;
+  std::vector<float> Cd((size_t)K * NS * Lp, 0.0f);
   std::vector<unsigned> cmask(L, 0u);
   static const int npmax[3][8] = {{7, 18, 7, 11, 11, 14, 10, 11}, {7, 15, 7, 11, 10}, {7, 14}};
   for (int l = 0; l < L; l++) {
@@ -189,7 +191,7 @@ bool load_sensor(const std::string& dir, const std::string& id, Sensor& s, std::
         cmask[l] |= 1u << j;
         for (int i = 0; i < np; i++)
           for (int k = 0; k < K; k++)
-            Cd[((size_t)k * NS + off + i) * L + l] = C[p0 + (size_t)i * K + k];
+            Cd[((size_t)k * NS + off + i) * Lp + l] = C[p0 + (size_t)i * K + k];
       }
       off += mx;
     }
@@ -306,6 +308,8 @@ struct crtm_gpu_context {
   DevBuf ws;        // chunk workspace
   DevBuf io_in, io_out;  // device copies for the host entry points
   DevBuf small;     // idx maps
+  cudaStream_t copy_stream = nullptr;   // device-to-host copies of finished chunks
+  std::vector<cudaEvent_t> chunk_events;
   // stage profiling
   bool profiling = false;
   struct Pending { int stage; cudaEvent_t a, b; };
@@ -411,7 +415,7 @@ size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w
   size_t off = 0;
   auto carve = [&](size_t bytes) -> char* { char* p = base ? base + off : nullptr; off += align_up(bytes); return p; };
   const size_t nn = (size_t)n;
-  const size_t ngf = (nn + npf - 1) / npf;
+  const size_t ngf = ((nn + npf * FWD_WARPS - 1) / (npf * FWD_WARPS)) * FWD_WARPS;
   const size_t nga = ((nn + ad_profiles<G, R>() - 1) / ad_profiles<G, R>()) * AD_WARPS;
   PrepView<R> pv;
   pv.Xg = (R*)carve(ngf * npf * K * NS * sizeof(R));
@@ -473,11 +477,40 @@ int reserve_smem(crtm_gpu_handle h, F kernel, size_t bytes, const char* what) {
   return CRTM_GPU_SUCCESS;
 }
 
+// Per-profile output slabs copied to host buffers as each chunk finishes
+// (host entry points only): element i covers bytes [p*per[i], (p+n)*per[i]).
+struct HostCopy {
+  int n = 0;
+  void* dst[8];
+  const void* src[8];
+  size_t per[8];
+  int max_chunk = 0;   // cap on the chunk size so that copies overlap compute
+};
+
+int copy_chunk(crtm_gpu_handle h, const HostCopy* hc, int p0, int n, cudaStream_t st) {
+  if (!h->copy_stream && cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(h, "cannot create the copy stream");
+  cudaEvent_t ev = nullptr;
+  if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess)
+    return fail(h, "cannot create a chunk event");
+  h->chunk_events.push_back(ev);
+  if (cudaEventRecord(ev, st) != cudaSuccess || cudaStreamWaitEvent(h->copy_stream, ev, 0) != cudaSuccess)
+    return fail(h, "chunk event failed");
+  for (int i = 0; i < hc->n; i++) {
+    if (!hc->dst[i] || !hc->per[i]) continue;
+    if (cudaMemcpyAsync((char*)hc->dst[i] + (size_t)p0 * hc->per[i],
+                        (const char*)hc->src[i] + (size_t)p0 * hc->per[i], (size_t)n * hc->per[i],
+                        cudaMemcpyDeviceToHost, h->copy_stream) != cudaSuccess)
+      return fail(h, "device-to-host copy failed");
+  }
+  return CRTM_GPU_SUCCESS;
+}
+
 // mode 0 forward, 1 K-matrix, 2 adjoint
 template <int G, class R>
 int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, int mode,
                  const double* seed, crtm_gpu_rtsolution* rts, crtm_gpu_kmatrix* kk,
-                 crtm_gpu_adjoint_out* ad, cudaStream_t st) {
+                 crtm_gpu_adjoint_out* ad, cudaStream_t st, const HostCopy* hc) {
   const int P = b->n_profiles, Kmax = b->max_layers, L = s.L, K = s.K, n_abs = b->n_absorbers;
   if (P <= 0) return CRTM_GPU_SUCCESS;
   if (Kmax < 2 || Kmax > MAX_LAYERS) return fail(h, "max_layers %d out of range [2, %d]", Kmax, MAX_LAYERS);
@@ -510,6 +543,7 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
   // chunk size from the workspace budget
   const size_t per = work_bytes<G, R>(s, 64, Kmax, nv, mode, nullptr, nullptr) / 64 + 1;
   int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)P, h->workspace_budget / per));
+  if (hc && hc->max_chunk > 0) chunk = std::min(chunk, hc->max_chunk);
   const size_t need = work_bytes<G, R>(s, chunk, Kmax, nv, mode, nullptr, nullptr);
   if (!h->ws.ensure(need)) return fail(h, "cannot allocate %zu bytes of workspace", need);
   Work<R> w;
@@ -523,7 +557,9 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
   int map_ct = 32;
   while (map_ct > 8 && map_smem_bytes<R>(K, Kmax, nv, map_ct) > 200 * 1024) map_ct >>= 1;
   const size_t map_smem = map_smem_bytes<R>(K, Kmax, nv, map_ct);
-  if (reserve_smem(h, column_kernel<R>, col_smem, "column") ||
+  constexpr size_t fwd_smem = fwd_smem_bytes<G, R, NPF>();
+  if (reserve_smem(h, absorb_fwd_kernel<G, R, NPF>, fwd_smem, "absorb_fwd") ||
+      reserve_smem(h, column_kernel<R>, col_smem, "column") ||
       reserve_smem(h, map_kernel<R>, map_smem, "map"))
     return CRTM_GPU_FAILURE;
   const bool ho_only = [&] {
@@ -540,8 +576,9 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
     }
     {
       StageScope sc(h, 1, st);
-      dim3 gf((L + 127) / 128, (n + NPF - 1) / NPF);
-      absorb_fwd_kernel<G, R, NPF><<<gf, 128, 0, st>>>(K, L, n, s.d_C, s.d_cmask, w.pv.Xg, w.OD);
+      dim3 gf((L + FWD_CH - 1) / FWD_CH, (n + NPF * FWD_WARPS - 1) / (NPF * FWD_WARPS));
+      absorb_fwd_kernel<G, R, NPF><<<gf, 32 * FWD_WARPS, fwd_smem, st>>>(K, L, s.Lp, n, s.d_C, s.d_cmask,
+                                                                   w.pv.Xg, w.OD);
       CK_LAUNCH(h);
     }
     ColumnArgs<R> ca{};
@@ -558,16 +595,21 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       column_kernel<R><<<gc, 128, col_smem, st>>>(ca);
       CK_LAUNCH(h);
     }
-    if (mode == 0) continue;
+    if (mode == 0) {
+      if (hc && hc->n) {
+        if (int rc = copy_chunk(h, hc, p0, n, st)) return rc;
+      }
+      continue;
+    }
     {
       StageScope sc(h, 3, st);
       dim3 ga((L + 31) / 32, (n + ad_profiles<G, R>() - 1) / ad_profiles<G, R>());
       if (ho_only)
         absorb_ad_kernel<G, R, NPA, 1><<<ga, 32 * AD_WARPS, 0, st>>>(
-            K, L, n, s.d_C, s.d_cmask, w.pv.Dg, s.tables.pdp, w.OD, w.SC, oa, w.RA);
+            K, L, s.Lp, n, s.d_C, s.d_cmask, w.pv.Dg, s.tables.pdp, w.OD, w.SC, oa, w.RA);
       else
         absorb_ad_kernel<G, R, NPA, 0><<<ga, 32 * AD_WARPS, 0, st>>>(
-            K, L, n, s.d_C, s.d_cmask, w.pv.Dg, s.tables.pdp, w.OD, w.SC, oa, w.RA);
+            K, L, s.Lp, n, s.d_C, s.d_cmask, w.pv.Dg, s.tables.pdp, w.OD, w.SC, oa, w.RA);
       CK_LAUNCH(h);
     }
     if (mode == 1) {
@@ -600,13 +642,16 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       adjoint_map_kernel<R><<<(unsigned)((na + 255) / 256), 256, 0, st>>>(am);
       CK_LAUNCH(h);
     }
+    if (hc && hc->n) {
+      if (int rc = copy_chunk(h, hc, p0, n, st)) return rc;
+    }
   }
   return CRTM_GPU_SUCCESS;
 }
 
 int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, const double* seed,
              crtm_gpu_rtsolution* rts, crtm_gpu_kmatrix* kk, crtm_gpu_adjoint_out* ad,
-             cudaStream_t st) {
+             cudaStream_t st, const HostCopy* hc = nullptr) {
   if (!h) return CRTM_GPU_FAILURE;
   if (sensor < 0 || sensor >= (int)h->sensors.size()) return fail(h, "sensor index %d out of range", sensor);
   if (!b || !rts || !rts->radiance || !rts->brightness_temperature) return fail(h, "missing batch or RTSolution buffers");
@@ -623,12 +668,12 @@ int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, c
   const Sensor& s = h->sensors[sensor];
   const bool fp64 = h->precision == CRTM_GPU_FP64;
   switch (s.group) {
-    case 1: return fp64 ? run_pipeline<1, double>(h, s, b, mode, seed, rts, kk, ad, st)
-                        : run_pipeline<1, float>(h, s, b, mode, seed, rts, kk, ad, st);
-    case 2: return fp64 ? run_pipeline<2, double>(h, s, b, mode, seed, rts, kk, ad, st)
-                        : run_pipeline<2, float>(h, s, b, mode, seed, rts, kk, ad, st);
-    default: return fp64 ? run_pipeline<3, double>(h, s, b, mode, seed, rts, kk, ad, st)
-                         : run_pipeline<3, float>(h, s, b, mode, seed, rts, kk, ad, st);
+    case 1: return fp64 ? run_pipeline<1, double>(h, s, b, mode, seed, rts, kk, ad, st, hc)
+                        : run_pipeline<1, float>(h, s, b, mode, seed, rts, kk, ad, st, hc);
+    case 2: return fp64 ? run_pipeline<2, double>(h, s, b, mode, seed, rts, kk, ad, st, hc)
+                        : run_pipeline<2, float>(h, s, b, mode, seed, rts, kk, ad, st, hc);
+    default: return fp64 ? run_pipeline<3, double>(h, s, b, mode, seed, rts, kk, ad, st, hc)
+                         : run_pipeline<3, float>(h, s, b, mode, seed, rts, kk, ad, st, hc);
   }
 }
 
@@ -706,14 +751,24 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
     dk = {(double*)dout[3], (double*)dout[4], (double*)dout[5], (double*)dout[6], kk->n_k_absorbers,
           kk->k_absorber_index};
   if (mode == 2) dad = {(double*)dout[3], (double*)dout[4], (double*)dout[5]};
+  HostCopy hc;
+  hc.n = (int)outs.size();
+  for (size_t i = 0; i < outs.size(); i++) {
+    hc.dst[i] = dout[i] ? outs[i].first : nullptr;
+    hc.src[i] = dout[i];
+    hc.per[i] = outs[i].second / (size_t)P;
+  }
+  // several chunks so that the copies of finished chunks overlap the next ones
+  hc.max_chunk = std::max(32, (P + 5) / 6);
   int rc = dispatch(h, sensor, &db, mode, dseed, &drts, mode == 1 ? &dk : nullptr,
-                    mode == 2 ? &dad : nullptr, st);
-  if (rc != CRTM_GPU_SUCCESS) return rc;
-  for (size_t i = 0; i < outs.size(); i++)
-    if (dout[i] && cudaMemcpyAsync(outs[i].first, dout[i], outs[i].second, cudaMemcpyDeviceToHost, st) != cudaSuccess)
-      return fail(h, "device-to-host copy failed");
+                    mode == 2 ? &dad : nullptr, st, &hc);
   cudaError_t e = cudaStreamSynchronize(st);
-  if (e != cudaSuccess) return fail(h, "CUDA error: %s", cudaGetErrorString(e));
+  cudaError_t e2 = h->copy_stream ? cudaStreamSynchronize(h->copy_stream) : cudaSuccess;
+  for (auto ev : h->chunk_events) cudaEventDestroy(ev);
+  h->chunk_events.clear();
+  if (rc != CRTM_GPU_SUCCESS) return rc;
+  if (e != cudaSuccess || e2 != cudaSuccess)
+    return fail(h, "CUDA error: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
   if (h->profiling) collect_stage_times(h);
   if (rts->status)
     for (int m = 0; m < P; m++)
@@ -760,7 +815,9 @@ int crtm_gpu_destroy(crtm_gpu_handle h) {
   h->ws.release(); h->io_in.release(); h->io_out.release(); h->small.release();
   collect_stage_times(h);
   for (auto e : h->event_pool) cudaEventDestroy(e);
+  if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
   if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   delete h;
   return CRTM_GPU_SUCCESS;
 }

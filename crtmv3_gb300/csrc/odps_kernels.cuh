@@ -183,6 +183,25 @@ __device__ __forceinline__ void load_group(const R* __restrict__ src, R* dst) {
   }
 }
 
+// Asynchronous global->shared copies (16 bytes; src_bytes 0 zero-fills).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, int src_bytes) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Coefficient tile of one reference layer: NS slots x 32 channels starting at
+// channel l0 of C[k][s][Lp] (Lp a multiple of 32, rows 128-byte aligned).
+template <int NS>
+__device__ __forceinline__ void load_c_tile(float (*dst)[32], const float* __restrict__ C, int k,
+                                            int Lp, int l0, int tid, int nthreads) {
+  for (int i = tid; i < NS * 8; i += nthreads) {
+    const int s = i >> 3, q = i & 7;
+    cp_async16(&dst[s][q * 4], C + ((size_t)k * NS + s) * Lp + l0 + q * 4, 16);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Device views
 // ---------------------------------------------------------------------------
@@ -465,45 +484,90 @@ __global__ void __launch_bounds__(32) prep_kernel(SensorTables S, RefSums RS, Ba
 }
 
 // ---------------------------------------------------------------------------
-// 2. absorption forward: OD[p][k][l] = sum_s C[k][s][l] * X[p][k][s]
+// 2. absorption forward: OD[p][k][l] = sum_s C[k][s][l] * X[p][k][s].
+//    CTA = 32 channels (lanes) x FWD_WARPS warps, each warp NP profiles; the
+//    coefficient slice of each layer is staged in shared memory (double
+//    buffered, cp.async) and used by all warps.
 // ---------------------------------------------------------------------------
+constexpr int FWD_WARPS = 4;
+constexpr int FWD_CH = 64;   // channels per CTA: 2 per lane
+
+// Coefficient tile of one reference layer: NS slots x FWD_CH channels from l0.
+template <int NS>
+__device__ __forceinline__ void load_c_tile64(float (*dst)[FWD_CH], const float* __restrict__ C,
+                                              int k, int Lp, int l0, int tid, int nthreads) {
+  for (int i = tid; i < NS * (FWD_CH / 4); i += nthreads) {
+    const int s = i / (FWD_CH / 4), q = i % (FWD_CH / 4);
+    const int l = l0 + q * 4;
+    // rows are padded to a multiple of 32 channels; a half tile past the end reads zeros
+    cp_async16(&dst[s][q * 4], C + ((size_t)k * NS + s) * Lp + (l < Lp ? l : 0), l < Lp ? 16 : 0);
+  }
+}
+
 template <int G, class R, int NP>
-__global__ void __launch_bounds__(128) absorb_fwd_kernel(int K, int L, int n_chunk,
-                                                         const float* __restrict__ C,
-                                                         const unsigned* __restrict__ cmask,
-                                                         const R* __restrict__ Xg,
-                                                         R* __restrict__ OD) {
+constexpr size_t fwd_smem_bytes() {
+  return sizeof(float) * 2 * Group<G>::NS * FWD_CH + sizeof(R) * 2 * FWD_WARPS * Group<G>::NS * NP;
+}
+
+template <int G, class R, int NP>
+__global__ void __launch_bounds__(32 * FWD_WARPS) absorb_fwd_kernel(int K, int L, int Lp, int n_chunk,
+                                                                    const float* __restrict__ C,
+                                                                    const unsigned* __restrict__ cmask,
+                                                                    const R* __restrict__ Xg,
+                                                                    R* __restrict__ OD) {
   constexpr int NS = Group<G>::NS, J = Group<G>::J;
-  const int l = blockIdx.x * blockDim.x + threadIdx.x;
-  const int pg = blockIdx.y;
+  constexpr int XCH = NS * NP * (int)sizeof(R) / 16;   // 16-byte chunks of one warp's X slice
+  extern __shared__ __align__(16) unsigned char fwd_smem[];
+  auto cs = reinterpret_cast<float (*)[NS][FWD_CH]>(fwd_smem);                       // [2][NS][FWD_CH]
+  auto xs = reinterpret_cast<R (*)[FWD_WARPS][NS * NP]>(fwd_smem + sizeof(float) * 2 * NS * FWD_CH);
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int l0 = blockIdx.x * FWD_CH;
+  const int la = l0 + lane, lb = l0 + 32 + lane;
+  const int pg = blockIdx.y * FWD_WARPS + wib;
   const int p0 = pg * NP;
-  const bool active = l < L;
-  const unsigned wmask = __reduce_or_sync(FULL, active ? cmask[l] : 0u);
-  const int lc = active ? l : 0;
+  const unsigned wmask = __reduce_or_sync(FULL, (la < L ? cmask[la] : 0u) | (lb < L ? cmask[lb] : 0u));
   const R* Xb = Xg + (size_t)pg * K * NS * NP;
+  const bool group_ok = p0 < n_chunk;
+  auto stage = [&](int k, int buf) {
+    load_c_tile64<NS>(cs[buf], C, k, Lp, l0, threadIdx.x, 32 * FWD_WARPS);
+    if (group_ok) {
+      const R* src = Xb + (size_t)k * NS * NP;
+      for (int i = lane; i < XCH; i += 32)
+        cp_async16(&xs[buf][wib][i * (16 / sizeof(R))], src + i * (16 / sizeof(R)), 16);
+    }
+    cp_async_commit();
+  };
+  stage(0, 0);
   for (int k = 0; k < K; k++) {
-    R acc[NP];
+    cp_async_wait_all();
+    __syncthreads();
+    if (k + 1 < K) stage(k + 1, (k + 1) & 1);
+    if (!group_ok) continue;
+    const float (*ct)[FWD_CH] = cs[k & 1];
+    const R* xk = xs[k & 1][wib];
+    R acc0[NP], acc1[NP];
 #pragma unroll
-    for (int p = 0; p < NP; p++) acc[p] = R(0);
-    const float* Ck = C + (size_t)k * NS * L + lc;
-    const R* Xk = Xb + (size_t)k * NS * NP;
+    for (int p = 0; p < NP; p++) acc0[p] = acc1[p] = R(0);
     static_for<J>([&](auto jc) {
       constexpr int j = decltype(jc)::value;
       constexpr int s0 = Group<G>::OFF[j], s1 = Group<G>::OFF[j + 1];
       if (!(wmask & (1u << j))) return;
 #pragma unroll
       for (int s = s0; s < s1; s++) {
-        const R c = R(__ldg(Ck + (size_t)s * L));
+        const R ca = R(ct[s][lane]), cb = R(ct[s][32 + lane]);
         R x[NP];
-        load_group<R, NP>(Xk + (size_t)s * NP, x);
 #pragma unroll
-        for (int p = 0; p < NP; p++) acc[p] += c * x[p];
+        for (int p = 0; p < NP; p++) x[p] = xk[s * NP + p];
+#pragma unroll
+        for (int p = 0; p < NP; p++) { acc0[p] += ca * x[p]; acc1[p] += cb * x[p]; }
       }
     });
-    if (active) {
 #pragma unroll
-      for (int p = 0; p < NP; p++)
-        if (p0 + p < n_chunk) OD[((size_t)(p0 + p) * K + k) * L + l] = acc[p];
+    for (int p = 0; p < NP; p++) {
+      if (p0 + p >= n_chunk) break;
+      R* o = OD + ((size_t)(p0 + p) * K + k) * L;
+      if (la < L) o[la] = acc0[p];
+      if (lb < L) o[lb] = acc1[p];
     }
   }
 }
@@ -744,12 +808,15 @@ __host__ __device__ constexpr bool q_needed(int q) {
 
 template <int G, class R, int NP, int OUTSET>
 __global__ void __launch_bounds__(32 * AD_WARPS) absorb_ad_kernel(
-    int K, int L, int n_chunk, const float* __restrict__ C, const unsigned* __restrict__ cmask,
-    const R* __restrict__ Dg, const double* __restrict__ pdp_tab, const R* __restrict__ ODAD,
-    const R* __restrict__ SC, OutAbs oa, R* __restrict__ RA) {
+    int K, int L, int Lp, int n_chunk, const float* __restrict__ C,
+    const unsigned* __restrict__ cmask, const R* __restrict__ Dg,
+    const double* __restrict__ pdp_tab, const R* __restrict__ ODAD, const R* __restrict__ SC,
+    OutAbs oa, R* __restrict__ RA) {
   constexpr int NS = Group<G>::NS, JM = Group<G>::JM, NV = Group<G>::NV;
   constexpr int NNZ = DLayout<G>::NNZ, NX = DLayout<G>::NX;
-  __shared__ float cs[NS][32];
+  constexpr int DCH = NX * NP * (int)sizeof(R) / 16;   // 16-byte chunks of one warp's D slice
+  __shared__ __align__(16) float cs[2][NS][32];
+  __shared__ __align__(16) R ds[2][AD_WARPS][NX * NP];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int l0 = blockIdx.x * 32, l = l0 + lane;
   const int pg = blockIdx.y * AD_WARPS + wib;
@@ -770,39 +837,44 @@ __global__ void __launch_bounds__(32 * AD_WARPS) absorb_ad_kernel(
 #pragma unroll
     for (int a = 0; a < JM; a++) Sgazp[p][a] = Sgatzp[p][a] = R(0);
   }
-  for (int k = K - 1; k >= 0; k--) {
-    __syncthreads();
-    for (int i = threadIdx.x; i < NS * 32; i += 32 * AD_WARPS) {
-      const int s = i >> 5, c = i & 31;
-      cs[s][c] = (l0 + c < L) ? __ldg(C + ((size_t)k * NS + s) * L + l0 + c) : 0.0f;
+  auto stage = [&](int k, int buf) {
+    load_c_tile<NS>(cs[buf], C, k, Lp, l0, threadIdx.x, 32 * AD_WARPS);
+    if (group_ok) {
+      const R* src = Db + (size_t)k * NX * NP;
+      for (int i = lane; i < DCH; i += 32) cp_async16(&ds[buf][wib][i * (16 / sizeof(R))], src + i * (16 / sizeof(R)), 16);
     }
+    cp_async_commit();
+  };
+  stage(K - 1, (K - 1) & 1);
+  for (int k = K - 1; k >= 0; k--) {
+    cp_async_wait_all();
     __syncthreads();
+    if (k > 0) stage(k - 1, (k - 1) & 1);
     if (!group_ok) continue;
+    const float (*ct)[32] = cs[k & 1];
+    const R* Dk = ds[k & 1][wib];
     R E[NP][NV];
 #pragma unroll
     for (int p = 0; p < NP; p++)
 #pragma unroll
       for (int q = 0; q < NV; q++) E[p][q] = R(0);
-    const R* Dk = Db + (size_t)k * NX * NP;
     static_for<NNZ>([&](auto ec) {
       constexpr int e = decltype(ec)::value;
       constexpr int s = PdTab<G>::slot[e], q = PdTab<G>::q[e];
       constexpr int j = slot_component<G>(s);
       if constexpr (!q_needed<G, OUTSET>(q)) return;
       if (!(wmask & (1u << j))) return;
-      const R c = R(cs[s][lane]);
-      R dv[NP];
-      load_group<R, NP>(Dk + (size_t)e * NP, dv);
+      const R c = R(ct[s][lane]);
 #pragma unroll
-      for (int p = 0; p < NP; p++) E[p][q] += c * dv[p];
+      for (int p = 0; p < NP; p++) E[p][q] += c * Dk[e * NP + p];
     });
     const R pdp = R(pdp_tab[k]);
 #pragma unroll
     for (int p = 0; p < NP; p++) {
       const bool valid = active && (p0 + p < n_chunk);
       const R oda = valid ? ODAD[((size_t)(p0 + p) * K + k) * L + l] * scl[p] : R(0);
-      const R pT = __ldg(Dk + (size_t)(NNZ + JM) * NP + p);
-      const unsigned mask = (unsigned)__ldg(Dk + (size_t)(NNZ + JM + 1) * NP + p);
+      const R pT = Dk[(NNZ + JM) * NP + p];
+      const unsigned mask = (unsigned)Dk[(NNZ + JM + 1) * NP + p];
       Stz[p] += oda * E[p][qTz<G>()];
       Stzp[p] += oda * E[p][qTzp<G>()];
       // T_ad(k) = local + S_Tz + pdp*S_Tzp + sum_a (pdp*A_a)*S_GATzp_a
@@ -811,7 +883,7 @@ __global__ void __launch_bounds__(32 * AD_WARPS) absorb_ad_kernel(
 #pragma unroll
       for (int a = 0; a < JM; a++) {
         Sgatzp[p][a] += oda * E[p][qGatzp<G>(a)];
-        const R pA = __ldg(Dk + (size_t)(NNZ + a) * NP + p);
+        const R pA = Dk[(NNZ + a) * NP + p];
         tad += pA * Sgatzp[p][a];
         if (OUTSET == 0 || a < 2) {
           Sgazp[p][a] += oda * E[p][qGazp<G>(a)];
@@ -869,44 +941,66 @@ template <class R>
 __global__ void __launch_bounds__(256) map_kernel(MapArgs<R> m) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int K = m.K, L = m.L, Kmax = m.Kmax, nv = m.nv, CT = m.ct, CS = m.ct + 1;
+  const int cshift = __ffs(CT) - 1;   // CT is a power of two
   const int p = blockIdx.y, gp = m.p_begin + p;
   const int l0 = blockIdx.x * CT;
   const int tid = threadIdx.x, wib = tid >> 5, lane = tid & 31;
   R* rat = reinterpret_cast<R*>(smem_raw);        // [nv][K][CS]
   R* ptt = rat + (size_t)nv * K * CS;             // [Kmax][CS]
   R* sct = ptt + (size_t)Kmax * CS;               // [CT]
-  R* uws = sct + CT;                              // [Kmax][MAX_UBAND]
+  R* uws = sct + CT;                              // [MAX_UBAND][Kmax]
   int* uk0 = reinterpret_cast<int*>(uws + (size_t)Kmax * MAX_UBAND);
   int* un = uk0 + Kmax;
   const int Ku = m.pv.status[p] ? 0 : m.b.n_layers[gp];
   const int ncl = min(CT, L - l0);
-  for (int i = tid; i < nv * K * CT; i += 256) {
-    const int row = i / CT, c = i % CT;
-    rat[(size_t)row * CS + c] = c < ncl ? m.RA[((size_t)p * nv * K + row) * L + l0 + c] : R(0);
+  {
+    const R* src = m.RA + (size_t)p * nv * K * L + l0;
+    const int total = nv * K << cshift;
+    for (int i = tid; i < total; i += 256) {
+      const int row = i >> cshift, c = i & (CT - 1);
+      rat[row * CS + c] = c < ncl ? src[(size_t)row * L + c] : R(0);
+    }
+    const R* pts = m.PT + (size_t)p * Kmax * L + l0;
+    const int tp = Ku << cshift;
+    for (int i = tid; i < tp; i += 256) {
+      const int ku = i >> cshift, c = i & (CT - 1);
+      ptt[ku * CS + c] = c < ncl ? pts[(size_t)ku * L + c] : R(0);
+    }
   }
-  for (int i = tid; i < Kmax * CT; i += 256) {
-    const int ku = i / CT, c = i % CT;
-    ptt[(size_t)ku * CS + c] = (c < ncl && ku < Ku) ? m.PT[((size_t)p * Kmax + ku) * L + l0 + c] : R(0);
+  if (tid < CT) sct[tid] = tid < ncl ? m.SC[(size_t)p * L + l0 + tid] : R(0);
+  for (int i = tid; i < Ku; i += 256) {
+    uk0[i] = m.pv.ub_k0[(size_t)p * Kmax + i];
+    un[i] = m.pv.ub_n[(size_t)p * Kmax + i];
   }
-  for (int c = tid; c < CT; c += 256) sct[c] = c < ncl ? m.SC[(size_t)p * L + l0 + c] : R(0);
-  for (int i = tid; i < Kmax; i += 256) {
-    uk0[i] = i < Ku ? m.pv.ub_k0[(size_t)p * Kmax + i] : 0;
-    un[i] = i < Ku ? m.pv.ub_n[(size_t)p * Kmax + i] : 0;
+  {
+    const double* uwg = m.pv.ub_w + (size_t)p * Kmax * MAX_UBAND;
+    for (int i = tid; i < Ku * MAX_UBAND; i += 256) {
+      const int ku = i / MAX_UBAND, j = i % MAX_UBAND;   // stored [j][ku]: conflict-free reads
+      uws[j * Kmax + ku] = R(uwg[i]);
+    }
   }
-  for (int i = tid; i < Kmax * MAX_UBAND; i += 256)
-    uws[i] = R(m.pv.ub_w[(size_t)p * Kmax * MAX_UBAND + i]);
   __syncthreads();
-  for (int c = wib; c < ncl; c += 8) {
-    const size_t pl = (size_t)gp * L + l0 + c;
-    const R scl = sct[c];
-    for (int v = 0; v < nv; v++) {
-      double* out = v == 0 ? m.kt + pl * Kmax : m.ka + (pl * (nv - 1) + (v - 1)) * Kmax;
-      const R* rav = rat + (size_t)v * K * CS + c;
-      for (int ku = lane; ku < Kmax; ku += 32) {
-        if (ku >= Ku) { out[ku] = 0.0; continue; }
-        R acc = (v == 0) ? ptt[(size_t)ku * CS + c] * scl : R(0);
-        const int k0 = uk0[ku], n = un[ku];
-        for (int i = n - 1; i >= 0; i--) acc += uws[ku * MAX_UBAND + i] * rav[(size_t)(k0 + i) * CS];
+  // each lane owns user layers ku = lane + 32*t; weights are read once per layer
+  for (int ku0 = 0; ku0 < Kmax; ku0 += 32) {
+    const int ku = ku0 + lane;
+    const bool live = ku < Ku;
+    const int k0 = live ? uk0[ku] : 0, n = live ? un[ku] : 0;
+    R w[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) w[i] = i < n ? uws[i * Kmax + ku] : R(0);
+    for (int c = wib; c < ncl; c += 8) {
+      const size_t pl = (size_t)gp * L + l0 + c;
+      const R scl = sct[c];
+      for (int v = 0; v < nv; v++) {
+        double* out = v == 0 ? m.kt + pl * Kmax : m.ka + (pl * (nv - 1) + (v - 1)) * Kmax;
+        if (ku >= Kmax) continue;
+        if (!live) { out[ku] = 0.0; continue; }
+        const R* rav = rat + (size_t)(v * K + k0) * CS + c;
+        R acc = (v == 0) ? ptt[ku * CS + c] * scl : R(0);
+#pragma unroll
+        for (int i = 3; i >= 0; i--)
+          if (i < n) acc += w[i] * rav[i * CS];
+        for (int i = 4; i < n; i++) acc += uws[i * Kmax + ku] * rav[i * CS];
         out[ku] = double(acc);
       }
     }
