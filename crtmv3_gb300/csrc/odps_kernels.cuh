@@ -375,43 +375,45 @@ __global__ void __launch_bounds__(32) prep_kernel(SensorTables S, RefSums RS, Ba
   const int pgf = p / pv.npf, pof = p % pv.npf;
   const int pga = pv.npa ? p / pv.npa : 0, poa = pv.npa ? p % pv.npa : 0;
   for (int k = lane; k < K; k += 32) {
-    LayerState Ls;
+    // the predictors and partials are evaluated in R: FP32 in the mixed form
+    LayerStateT<R> Ls;
     const double sa = sv / (EARTH_RADIUS + (S.zgeo[k + 1] + zoff));
-    Ls.sec = 1.0 / sqrt(1.0 - sa * sa);
-    Ls.T = sT[k];
-    Ls.Tref = S.ref_t[k];
-    Ls.pdp = S.pdp[k];
-    Ls.tz_ref = RS.tz_ref[k];
-    Ls.tz = sTz[k] / Ls.tz_ref;
-    Ls.tzp_ref = RS.tzp_ref[k];
-    Ls.tzp = sTzp[k] / Ls.tzp_ref;
+    Ls.sec = R(1.0 / sqrt(1.0 - sa * sa));
+    Ls.T_ = R(sT[k]);
+    Ls.Tref = R(S.ref_t[k]);
+    Ls.dT = R(sT[k] - S.ref_t[k]);
+    Ls.pdp = R(S.pdp[k]);
+    Ls.tz_ref = R(RS.tz_ref[k]);
+    Ls.tz = R(sTz[k] / RS.tz_ref[k]);
+    Ls.tzp_ref = R(RS.tzp_ref[k]);
+    Ls.tzp = R(sTzp[k] / RS.tzp_ref[k]);
 #pragma unroll
     for (int a = 0; a < MAX_ABS; a++) {
       if (a < JM) {
-        Ls.A[a] = sA[a * K + k];
-        Ls.Aref[a] = S.ref_a[a * K + k];
-        Ls.gazp_ref[a] = RS.gazp_ref[a * K + k];
-        Ls.gatzp_ref[a] = RS.gatzp_ref[a * K + k];
-        Ls.gazp[a] = sGz[a * K + k] / Ls.gazp_ref[a];
-        Ls.gatzp[a] = sGt[a * K + k] / Ls.gatzp_ref[a];
+        Ls.A[a] = R(sA[a * K + k]);
+        Ls.Aref[a] = R(S.ref_a[a * K + k]);
+        Ls.gazp_ref[a] = R(RS.gazp_ref[a * K + k]);
+        Ls.gatzp_ref[a] = R(RS.gatzp_ref[a * K + k]);
+        Ls.gazp[a] = R(sGz[a * K + k] / RS.gazp_ref[a * K + k]);
+        Ls.gatzp[a] = R(sGt[a * K + k] / RS.gatzp_ref[a * K + k]);
       } else {
-        Ls.A[a] = Ls.Aref[a] = Ls.gazp[a] = Ls.gatzp[a] = Ls.gazp_ref[a] = Ls.gatzp_ref[a] = 1.0;
+        Ls.A[a] = Ls.Aref[a] = Ls.gazp[a] = Ls.gatzp[a] = Ls.gazp_ref[a] = Ls.gatzp_ref[a] = R(1);
       }
     }
     R X[NS];
-    layer_predictors<G, R>(Ls, X);
+    layer_predictors<G, R, R>(Ls, X);
     R* xo = pv.Xg + ((size_t)pgf * K + k) * NS * pv.npf + pof;
 #pragma unroll
     for (int s = 0; s < NS; s++) xo[(size_t)s * pv.npf] = X[s];
     if (pv.Dg) {
       R D[NNZ];
-      layer_partials<G, R>(Ls, D);
+      layer_partials<G, R, R>(Ls, D);
       R* dO = pv.Dg + ((size_t)pga * K + k) * NX * pv.npa + poa;
 #pragma unroll
       for (int e = 0; e < NNZ; e++) dO[(size_t)e * pv.npa] = D[e];
 #pragma unroll
-      for (int a = 0; a < JM; a++) dO[(size_t)(NNZ + a) * pv.npa] = R(Ls.pdp * Ls.A[a]);
-      dO[(size_t)(NNZ + JM) * pv.npa] = R(Ls.pdp * Ls.T);
+      for (int a = 0; a < JM; a++) dO[(size_t)(NNZ + a) * pv.npa] = R(S.pdp[k] * sA[a * K + k]);
+      dO[(size_t)(NNZ + JM) * pv.npa] = R(S.pdp[k] * sT[k]);
       dO[(size_t)(NNZ + JM + 1) * pv.npa] = R(float(sPass[k]));
     }
   }
@@ -668,34 +670,44 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   R* od = a.OD + (size_t)p * K * L + l;
   const size_t cs = (size_t)p * Kmax * L + l;   // scratch base, stride L
 
-  // ---- pass 1 (top down): OD path, user-level interpolation, downwelling
-  R cur = R(0), up_prev = R(0), rad_down = R(a.sp.cbr[l]);
-  R src = R(0), tr = R(1);   // forward mode: TOA radiance accumulated top down
-  int lvl = 0;
-  for (int i = 0; i <= Ku; i++) {
-    const int ka = k1s[i], kb = k2s[i];
-    while (lvl < ka) { cur += clamp_od(od[(size_t)lvl * L]); lvl++; }
-    R upi = cur;
-    if (kb != ka) {
-      const R yb = cur + clamp_od(od[(size_t)ka * L]);
-      upi = cur + (yb - cur) * R(facd[i]);
-    }
-    if (i > 0) {
-      const int ku = i - 1;
-      const R tau = (upi - up_prev) * inv_sec;
-      const R t = exp(-tau * inv_u);
-      const R te = b1 + b2 * tus[ku];
-      const R B = c1 / (exp(c2 / te) - R(1));
-      if (a.mode == 0) {
-        src += tr * B * (R(1) - t);
-      } else {
-        a.TAU[cs + (size_t)ku * L] = tau;
-        a.DTOP[cs + (size_t)ku * L] = rad_down;
+  // ---- pass 1 (top down): OD path, user-level interpolation, downwelling.
+  // Reference levels are walked in order (OD loads prefetched two levels
+  // ahead); each user level is emitted once the upper level of its bracket
+  // is reached.
+  R rad_down = R(a.sp.cbr[l]);
+  R src = R(0), tr = R(1), total = R(0);   // forward: TOA radiance accumulated top down
+  R path_prev = R(0), path_cur = R(0), up_prev = R(0);
+  R od1 = K > 0 ? od[0] : R(0), od2 = K > 1 ? od[L] : R(0);
+  int i = 0;
+  for (int k = 0; k <= K; k++) {
+    while (i <= Ku && k2s[i] == k) {
+      const int ka = k1s[i];
+      const R upi = (ka == k) ? path_cur : path_prev + (path_cur - path_prev) * R(facd[i]);
+      if (i > 0) {
+        const int ku = i - 1;
+        const R tau = (upi - up_prev) * inv_sec;
+        const R t = exp(-tau * inv_u);
+        const R te = b1 + b2 * tus[ku];
+        const R B = c1 / (exp(c2 / te) - R(1));
+        if (a.mode == 0) {
+          src += tr * B * (R(1) - t);
+        } else {
+          a.TAU[cs + (size_t)ku * L] = tau;
+          a.DTOP[cs + (size_t)ku * L] = rad_down;
+        }
+        tr *= t;
+        total += tau;
+        rad_down = rad_down * t + B * (R(1) - t);
       }
-      tr *= t;
-      rad_down = rad_down * t + B * (R(1) - t);
+      up_prev = upi;
+      i++;
     }
-    up_prev = upi;
+    if (k == K) break;
+    const R v = clamp_od(od1);
+    od1 = od2;
+    if (k + 2 < K) od2 = od[(size_t)(k + 2) * L];
+    path_prev = path_cur;
+    path_cur += v;
   }
   const R Dn = rad_down, Tn = tr;
   if (a.mode == 0) {
@@ -709,32 +721,32 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   R P = R(1);                 // transmittance of the layers below the current one
   const R down0 = rr * Tn;    // downwelling adjoint at the surface (unit seed)
   R cum = R(0);               // OD of the layers below the current one
-  R total = R(0);
-  for (int ku = 0; ku < Ku; ku++) total += a.TAU[cs + (size_t)ku * L];
   R pa_lo = R(0), pa_hi = R(0), suffix = R(0), ua_hi = R(0);
   int plvl = K - 1;
+  R odm = od[(size_t)plvl * L];   // reference OD of layer plvl (clamp test), prefetched
   auto flush = [&]() {
     suffix += pa_hi;
-    const R odr = od[(size_t)plvl * L];
-    od[(size_t)plvl * L] = (odr < R(0) || odr > R(MAX_OD)) ? R(0) : suffix;
+    od[(size_t)plvl * L] = (odm < R(0) || odm > R(MAX_OD)) ? R(0) : suffix;
     pa_hi = pa_lo;
     pa_lo = R(0);
     plvl--;
+    if (plvl >= 0) odm = od[(size_t)plvl * L];
   };
-  auto scatter = [&](int i, R v) {
-    const int ka = k1s[i], kb = k2s[i];
+  auto scatter = [&](int iu, R v) {
+    const int ka = k1s[iu], kb = k2s[iu];
     while (ka < plvl) flush();
     if (ka == kb) {
       if (ka == plvl) pa_lo += v; else pa_hi += v;
     } else {
-      const R f = R(facd[i]);
+      const R f = R(facd[iu]);
       pa_lo += (R(1) - f) * v;
       pa_hi += f * v;
     }
   };
+  R tau_n = a.TAU[cs + (size_t)(Ku - 1) * L], dt_n = a.DTOP[cs + (size_t)(Ku - 1) * L];
   for (int ku = Ku - 1; ku >= 0; ku--) {
-    const R tau = a.TAU[cs + (size_t)ku * L];
-    const R Dtop = a.DTOP[cs + (size_t)ku * L];
+    const R tau = tau_n, Dtop = dt_n;
+    if (ku > 0) { tau_n = a.TAU[cs + (size_t)(ku - 1) * L]; dt_n = a.DTOP[cs + (size_t)(ku - 1) * L]; }
     const R t = exp(-tau * inv_u);
     const R te = b1 + b2 * tus[ku];
     const R ee = exp(c2 / te);

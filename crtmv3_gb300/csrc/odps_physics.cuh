@@ -75,12 +75,16 @@ CRTM_HD int group_j(int g) { return g == 1 ? 8 : (g == 2 ? 5 : 2); }
 // ---------------------------------------------------------------------------
 // Per-layer state handed to the predictor and partial-derivative functions.
 // ---------------------------------------------------------------------------
-struct LayerState {
-  double sec, T, Tref, pdp;
-  double A[MAX_ABS], Aref[MAX_ABS];
-  double tz, tzp, tz_ref, tzp_ref;
-  double gazp[MAX_ABS], gatzp[MAX_ABS], gazp_ref[MAX_ABS], gatzp_ref[MAX_ABS];
+// T is the arithmetic type of the predictor and partial-derivative evaluation.
+template <class T>
+struct LayerStateT {
+  T sec, T_, Tref, pdp;
+  T dT;   // T_ - Tref, formed in FP64 before any rounding to T (it cancels)
+  T A[MAX_ABS], Aref[MAX_ABS];
+  T tz, tzp, tz_ref, tzp_ref;
+  T gazp[MAX_ABS], gatzp[MAX_ABS], gazp_ref[MAX_ABS], gatzp_ref[MAX_ABS];
 };
+using LayerState = LayerStateT<double>;
 
 // Variable index helpers
 template <int G> CRTM_HD constexpr int qT() { return 0; }
@@ -93,18 +97,18 @@ template <int G> CRTM_HD constexpr int qGatzp(int a) { return 3 + 2 * Group<G>::
 // ---------------------------------------------------------------------------
 // Predictors X[s] of one layer (ODPS_Compute_Predictor, ODPS_Predictor.f90:775-1093).
 // ---------------------------------------------------------------------------
-template <int G, class R>
-CRTM_HD void layer_predictors(const LayerState& L, R* X) {
-  const double s = L.sec, t = L.T / L.Tref, t2 = t * t, dT = L.T - L.Tref;
-  const double dT2 = dT * fabs(dT);
-  const double H = L.A[0] / L.Aref[0], Ha = s * H, Hr = sqrt(Ha), Hs = Ha * Ha;
-  const double Hd = H / L.gatzp[0];
+template <int G, class R, class T = double>
+CRTM_HD void layer_predictors(const LayerStateT<T>& L, R* X) {
+  const T s = L.sec, t = L.T_ / L.Tref, t2 = t * t, dT = L.dT;
+  const T dT2 = dT * fabs(dT);
+  const T H = L.A[0] / L.Aref[0], Ha = s * H, Hr = sqrt(Ha), Hs = Ha * Ha;
+  const T Hd = H / L.gatzp[0];
   // dry component (slots 0..6)
   X[0] = R(s); X[1] = R(s * t); X[2] = R(s * t2); X[3] = R(t); X[4] = R(s * s); X[5] = R(t2);
   X[6] = R(L.tz);
   if (G == 3) {
     R* w = X + 7;
-    const double g = L.gazp[0];
+    const T g = L.gazp[0];
     w[0] = R(Ha / t); w[1] = R(Ha / t * H); w[2] = R(Ha / t2 * H / t2); w[3] = R(Ha / t2);
     w[4] = R(Ha / t2 * H); w[5] = R(Ha / (t2 * t2)); w[6] = R(Ha); w[7] = R(Ha * dT);
     w[8] = R((s * g) * (s * g)); w[9] = R(s * g); w[10] = R(s); w[11] = R(Hs * Ha);
@@ -113,8 +117,8 @@ CRTM_HD void layer_predictors(const LayerState& L, R* X) {
   }
   constexpr int oWLO = 7, oWCO = (G == 1 ? 25 : 22), oOZO = (G == 1 ? 32 : 29),
                 oCO2 = (G == 1 ? 43 : 40);
-  const double O = L.A[1] / L.Aref[1], Oa = s * O, Or = sqrt(Oa), go = L.gazp[1];
-  const double C2 = L.A[2] / L.Aref[2], gc = L.gazp[2], tzp = L.tzp, gh = L.gazp[0];
+  const T O = L.A[1] / L.Aref[1], Oa = s * O, Or = sqrt(Oa), go = L.gazp[1];
+  const T C2 = L.A[2] / L.Aref[2], gc = L.gazp[2], tzp = L.tzp, gh = L.gazp[0];
   R* wl = X + oWLO;
   wl[0] = R(Ha); wl[1] = R(Ha * dT); wl[2] = R(Hs); wl[3] = R(Ha * dT2); wl[4] = R(sqrt(Hr));
   wl[5] = R(Hs * Ha); wl[6] = R(Hr); wl[7] = R(Hr * dT); wl[8] = R(Hs * Hs); wl[9] = R(Hd);
@@ -132,14 +136,14 @@ CRTM_HD void layer_predictors(const LayerState& L, R* X) {
   c2[6] = R(s * tzp); c2[7] = R((s * gc) * (s * gc)); c2[8] = R(tzp * tzp * tzp);
   c2[9] = R(s * tzp * sqrt(t));
   if (G == 1) {
-    const double N = L.A[3] / L.Aref[3], Na = s * N, Nr = sqrt(Na), gn = L.gazp[3];
-    const double Cr = L.A[4] / L.Aref[4], COa = s * Cr, COr = sqrt(COa), gco = L.gazp[4];
-    const double COc = COa * Cr / gco;
-    const double M = L.A[5] / L.Aref[5], Ma = s * M, Mr = sqrt(Ma), gm = L.gazp[5], Mz = s * gm;
+    const T N = L.A[3] / L.Aref[3], Na = s * N, Nr = sqrt(Na), gn = L.gazp[3];
+    const T Cr = L.A[4] / L.Aref[4], COa = s * Cr, COr = sqrt(COa), gco = L.gazp[4];
+    const T COc = COa * Cr / gco;
+    const T M = L.A[5] / L.Aref[5], Ma = s * M, Mr = sqrt(Ma), gm = L.gazp[5], Mz = s * gm;
     c2[10] = R(COa);
     wl[15] = R(Ma); wl[16] = R(Ma * Ma * dT); wl[17] = R(COa);
     R* np = X + 54;
-    np[0] = R(Na * dT); np[1] = R(Nr); np[2] = R(N * dT); np[3] = R(pow(Na, 0.25)); np[4] = R(Na);
+    np[0] = R(Na * dT); np[1] = R(Nr); np[2] = R(N * dT); np[3] = R(pow(Na, T(0.25))); np[4] = R(Na);
     np[5] = R(s * gn); np[6] = R(s * L.gatzp[3]); np[7] = R(Na * Na); np[8] = R(L.gatzp[3]);
     np[9] = R(Nr * N / gn); np[10] = R(Ma); np[11] = R(Ma * gm); np[12] = R(COa);
     np[13] = R(COa * s * gco);
@@ -167,11 +171,11 @@ CRTM_HD void layer_predictors(const LayerState& L, R* X) {
 
 // Shared locals available to the entry expressions.
 #define CRTM_PD_LOCALS(G)                                                         \
-  const double s = L.sec, iT = 1.0 / L.Tref, t = L.T * iT, t2 = t * t;            \
-  const double dT = L.T - L.Tref, adT = fabs(dT), dT2 = dT * adT;                 \
-  const double iA0 = 1.0 / L.Aref[0], H = L.A[0] * iA0, Ha = s * H, Hr = sqrt(Ha); \
-  const double gt0 = L.gatzp[0];                                                  \
-  const double dt2 = 2.0 * t * iT; /* d(t^2)/dT */                                \
+  const T s = L.sec, iT = T(1.0) / L.Tref, t = L.T_ * iT, t2 = t * t;            \
+  const T dT = L.dT, adT = fabs(dT), dT2 = dT * adT;                          \
+  const T iA0 = T(1.0) / L.Aref[0], H = L.A[0] * iA0, Ha = s * H, Hr = sqrt(Ha); \
+  const T gt0 = L.gatzp[0];                                                  \
+  const T dt2 = T(2.0) * t * iT; /* d(t^2)/dT */                                \
   (void)dt2; (void)dT2; (void)Hr; (void)gt0;
 
 #define PD_DRY(E)                                       \
@@ -179,32 +183,32 @@ CRTM_HD void layer_predictors(const LayerState& L, R* X) {
   E(2, 0, s * dt2)                                      \
   E(3, 0, iT)                                           \
   E(5, 0, dt2)                                          \
-  E(6, QTZ, 1.0 / L.tz_ref)
+  E(6, QTZ, T(1.0) / L.tz_ref)
 
 // water vapour continuum (group 1/2) or first seven wet predictors (group 3)
 #define PD_WCO(E, o)                                                        \
   E(o + 0, QA0, s * iA0 / t)                                                \
   E(o + 0, 0, -Ha / (t * t) * iT)                                           \
-  E(o + 1, QA0, 2.0 * Ha * iA0 / t)                                         \
+  E(o + 1, QA0, T(2.0) * Ha * iA0 / t)                                         \
   E(o + 1, 0, -Ha * H / (t * t) * iT)                                       \
-  E(o + 2, QA0, 2.0 * Ha * iA0 / (t2 * t2))                                 \
-  E(o + 2, 0, -2.0 * Ha * H / (t2 * t2 * t2) * dt2)                         \
+  E(o + 2, QA0, T(2.0) * Ha * iA0 / (t2 * t2))                                 \
+  E(o + 2, 0, -T(2.0) * Ha * H / (t2 * t2 * t2) * dt2)                         \
   E(o + 3, QA0, s * iA0 / t2)                                               \
   E(o + 3, 0, -Ha / (t2 * t2) * dt2)                                        \
-  E(o + 4, QA0, 2.0 * Ha * iA0 / t2)                                        \
+  E(o + 4, QA0, T(2.0) * Ha * iA0 / t2)                                        \
   E(o + 4, 0, -Ha * H / (t2 * t2) * dt2)                                    \
   E(o + 5, QA0, s * iA0 / (t2 * t2))                                        \
-  E(o + 5, 0, -2.0 * Ha / (t2 * t2 * t2) * dt2)                             \
+  E(o + 5, 0, -T(2.0) * Ha / (t2 * t2 * t2) * dt2)                             \
   E(o + 6, QA0, s * iA0)
 
 // group 3 wet predictors 8..14
 #define PD_WET_TAIL(E)                                                      \
   E(14, QA0, s * iA0 * dT)                                                  \
   E(14, 0, Ha)                                                              \
-  E(15, QGAZP0, 2.0 * s * s * L.gazp[0] / L.gazp_ref[0])                    \
+  E(15, QGAZP0, T(2.0) * s * s * L.gazp[0] / L.gazp_ref[0])                    \
   E(16, QGAZP0, s / L.gazp_ref[0])                                          \
-  E(18, QA0, 3.0 * Ha * Ha * s * iA0)                                       \
-  E(19, QA0, 4.0 * Ha * Ha * Ha * s * iA0)                                  \
+  E(18, QA0, T(3.0) * Ha * Ha * s * iA0)                                       \
+  E(19, QA0, T(4.0) * Ha * Ha * Ha * s * iA0)                                  \
   E(20, QA0, iA0 / gt0)                                                     \
   E(20, QGATZP0, -H / (gt0 * gt0) / L.gatzp_ref[0])
 
@@ -213,26 +217,26 @@ CRTM_HD void layer_predictors(const LayerState& L, R* X) {
   E(7, QA0, s * iA0)                                                        \
   E(8, QA0, s * iA0 * dT)                                                   \
   E(8, 0, Ha)                                                               \
-  E(9, QA0, 2.0 * Ha * s * iA0)                                             \
+  E(9, QA0, T(2.0) * Ha * s * iA0)                                             \
   E(10, QA0, s * iA0 * dT2)                                                 \
-  E(10, 0, Ha * 2.0 * adT)                                                  \
-  E(11, QA0, 0.25 * sqrt(Hr) / Ha * s * iA0)                                \
-  E(12, QA0, 3.0 * Ha * Ha * s * iA0)                                       \
-  E(13, QA0, 0.5 / Hr * s * iA0)                                            \
-  E(14, QA0, 0.5 / Hr * s * iA0 * dT)                                       \
+  E(10, 0, Ha * T(2.0) * adT)                                                  \
+  E(11, QA0, T(0.25) * sqrt(Hr) / Ha * s * iA0)                                \
+  E(12, QA0, T(3.0) * Ha * Ha * s * iA0)                                       \
+  E(13, QA0, T(0.5) / Hr * s * iA0)                                            \
+  E(14, QA0, T(0.5) / Hr * s * iA0 * dT)                                       \
   E(14, 0, Hr)                                                              \
-  E(15, QA0, 4.0 * Ha * Ha * Ha * s * iA0)                                  \
+  E(15, QA0, T(4.0) * Ha * Ha * Ha * s * iA0)                                  \
   E(16, QA0, iA0 / gt0)                                                     \
   E(16, QGATZP0, -H / (gt0 * gt0) / L.gatzp_ref[0])                         \
-  E(17, QA0, (0.5 / Hr * s * (H / gt0) + Hr / gt0) * iA0)                   \
+  E(17, QA0, (T(0.5) / Hr * s * (H / gt0) + Hr / gt0) * iA0)                   \
   E(17, QGATZP0, -Hr * H / (gt0 * gt0) / L.gatzp_ref[0])                    \
-  E(18, QGAZP0, 2.0 * s * s * L.gazp[0] / L.gazp_ref[0])                    \
+  E(18, QGAZP0, T(2.0) * s * s * L.gazp[0] / L.gazp_ref[0])                    \
   E(19, QGAZP0, s / L.gazp_ref[0])                                          \
   E(21, QA2, s / L.Aref[2])
 
 #define PD_WLO_G1(E)                                                        \
   E(22, QA5, s / L.Aref[5])                                                 \
-  E(23, QA5, 2.0 * (s * L.A[5] / L.Aref[5]) * s / L.Aref[5] * dT)           \
+  E(23, QA5, T(2.0) * (s * L.A[5] / L.Aref[5]) * s / L.Aref[5] * dT)           \
   E(23, 0, (s * L.A[5] / L.Aref[5]) * (s * L.A[5] / L.Aref[5]))             \
   E(24, QA4, s / L.Aref[4])
 
@@ -241,24 +245,24 @@ CRTM_HD void layer_predictors(const LayerState& L, R* X) {
   E(o + 0, QA1, s / L.Aref[1])                                                           \
   E(o + 1, QA1, s / L.Aref[1] * dT)                                                      \
   E(o + 1, 0, s * L.A[1] / L.Aref[1])                                                    \
-  E(o + 2, QA1, 2.0 * (s * L.A[1] / L.Aref[1]) * L.gazp[1] / L.Aref[1])                  \
+  E(o + 2, QA1, T(2.0) * (s * L.A[1] / L.Aref[1]) * L.gazp[1] / L.Aref[1])                  \
   E(o + 2, QGAZP1, (s * L.A[1] / L.Aref[1]) * (L.A[1] / L.Aref[1]) / L.gazp_ref[1])      \
-  E(o + 3, QA1, 2.0 * (s * L.A[1] / L.Aref[1]) * s / L.Aref[1])                          \
+  E(o + 3, QA1, T(2.0) * (s * L.A[1] / L.Aref[1]) * s / L.Aref[1])                          \
   E(o + 4, QA1, s / L.Aref[1] * L.gazp[1])                                               \
   E(o + 4, QGAZP1, (s * L.A[1] / L.Aref[1]) / L.gazp_ref[1])                             \
   E(o + 5, QA1, s / L.Aref[1] * sqrt(s * L.gazp[1]))                                     \
-  E(o + 5, QGAZP1, 0.5 * (s * L.A[1] / L.Aref[1]) * sqrt(s / L.gazp[1]) / L.gazp_ref[1]) \
-  E(o + 6, QA1, 0.5 / sqrt(s * L.A[1] / L.Aref[1]) * s / L.Aref[1] * dT)                 \
+  E(o + 5, QGAZP1, T(0.5) * (s * L.A[1] / L.Aref[1]) * sqrt(s / L.gazp[1]) / L.gazp_ref[1]) \
+  E(o + 6, QA1, T(0.5) / sqrt(s * L.A[1] / L.Aref[1]) * s / L.Aref[1] * dT)                 \
   E(o + 6, 0, sqrt(s * L.A[1] / L.Aref[1]))                                              \
-  E(o + 7, QA1, 0.5 / sqrt(s * L.A[1] / L.Aref[1]) * s / L.Aref[1])                      \
+  E(o + 7, QA1, T(0.5) / sqrt(s * L.A[1] / L.Aref[1]) * s / L.Aref[1])                      \
   E(o + 8, QA1,                                                                          \
-    (0.5 / sqrt(s * L.A[1] / L.Aref[1]) * s * (L.A[1] / L.Aref[1]) +                     \
+    (T(0.5) / sqrt(s * L.A[1] / L.Aref[1]) * s * (L.A[1] / L.Aref[1]) +                     \
      sqrt(s * L.A[1] / L.Aref[1])) / L.gazp[1] / L.Aref[1])                              \
   E(o + 8, QGAZP1,                                                                       \
     -sqrt(s * L.A[1] / L.Aref[1]) * (L.A[1] / L.Aref[1]) / (L.gazp[1] * L.gazp[1]) /     \
         L.gazp_ref[1])                                                                   \
   E(o + 9, QGAZP1, s / L.gazp_ref[1])                                                    \
-  E(o + 10, QGAZP1, 2.0 * s * s * L.gazp[1] / L.gazp_ref[1])
+  E(o + 10, QGAZP1, T(2.0) * s * s * L.gazp[1] / L.gazp_ref[1])
 
 // carbon dioxide, offset o (slot o+10 only in group 1)
 #define PD_CO2(E, o)                                                                  \
@@ -268,10 +272,10 @@ CRTM_HD void layer_predictors(const LayerState& L, R* X) {
   E(o + 3, 0, dt2)                                                                    \
   E(o + 5, QA2, s / L.Aref[2])                                                        \
   E(o + 6, QTZP, s / L.tzp_ref)                                                       \
-  E(o + 7, QGAZP2, 2.0 * s * s * L.gazp[2] / L.gazp_ref[2])                           \
-  E(o + 8, QTZP, 3.0 * L.tzp * L.tzp / L.tzp_ref)                                     \
+  E(o + 7, QGAZP2, T(2.0) * s * s * L.gazp[2] / L.gazp_ref[2])                           \
+  E(o + 8, QTZP, T(3.0) * L.tzp * L.tzp / L.tzp_ref)                                     \
   E(o + 9, QTZP, s * sqrt(t) / L.tzp_ref)                                             \
-  E(o + 9, 0, s * L.tzp * 0.5 / sqrt(t) * iT)
+  E(o + 9, 0, s * L.tzp * T(0.5) / sqrt(t) * iT)
 
 #define PD_CO2_G1(E) E(53, QA4, s / L.Aref[4])
 
@@ -279,17 +283,17 @@ CRTM_HD void layer_predictors(const LayerState& L, R* X) {
 #define PD_N2O(E)                                                                        \
   E(54, QA3, s / L.Aref[3] * dT)                                                         \
   E(54, 0, s * L.A[3] / L.Aref[3])                                                       \
-  E(55, QA3, 0.5 / sqrt(s * L.A[3] / L.Aref[3]) * s / L.Aref[3])                         \
+  E(55, QA3, T(0.5) / sqrt(s * L.A[3] / L.Aref[3]) * s / L.Aref[3])                         \
   E(56, QA3, dT / L.Aref[3])                                                             \
   E(56, 0, L.A[3] / L.Aref[3])                                                           \
-  E(57, QA3, 0.25 * pow(s * L.A[3] / L.Aref[3], -0.75) * s / L.Aref[3])                  \
+  E(57, QA3, T(0.25) * pow(s * L.A[3] / L.Aref[3], -T(0.75)) * s / L.Aref[3])                  \
   E(58, QA3, s / L.Aref[3])                                                              \
   E(59, QGAZP3, s / L.gazp_ref[3])                                                       \
   E(60, QGATZP3, s / L.gatzp_ref[3])                                                     \
-  E(61, QA3, 2.0 * (s * L.A[3] / L.Aref[3]) * s / L.Aref[3])                             \
-  E(62, QGATZP3, 1.0 / L.gatzp_ref[3])                                                   \
+  E(61, QA3, T(2.0) * (s * L.A[3] / L.Aref[3]) * s / L.Aref[3])                             \
+  E(62, QGATZP3, T(1.0) / L.gatzp_ref[3])                                                   \
   E(63, QA3,                                                                             \
-    (0.5 / sqrt(s * L.A[3] / L.Aref[3]) * s * (L.A[3] / L.Aref[3]) +                     \
+    (T(0.5) / sqrt(s * L.A[3] / L.Aref[3]) * s * (L.A[3] / L.Aref[3]) +                     \
      sqrt(s * L.A[3] / L.Aref[3])) / L.gazp[3] / L.Aref[3])                              \
   E(63, QGAZP3,                                                                          \
     -sqrt(s * L.A[3] / L.Aref[3]) * (L.A[3] / L.Aref[3]) / (L.gazp[3] * L.gazp[3]) /     \
@@ -306,41 +310,41 @@ CRTM_HD void layer_predictors(const LayerState& L, R* X) {
   E(68, QA4, s / L.Aref[4])                                                              \
   E(69, QA4, s / L.Aref[4] * dT)                                                         \
   E(69, 0, s * L.A[4] / L.Aref[4])                                                       \
-  E(70, QA4, 0.25 * sqrt(sqrt(s * L.A[4] / L.Aref[4])) / (s * L.A[4] / L.Aref[4]) * s /  \
+  E(70, QA4, T(0.25) * sqrt(sqrt(s * L.A[4] / L.Aref[4])) / (s * L.A[4] / L.Aref[4]) * s /  \
                  L.Aref[4])                                                              \
-  E(71, QA4, 0.5 / sqrt(s * L.A[4] / L.Aref[4]) * s / L.Aref[4] * dT)                    \
+  E(71, QA4, T(0.5) / sqrt(s * L.A[4] / L.Aref[4]) * s / L.Aref[4] * dT)                    \
   E(71, 0, sqrt(s * L.A[4] / L.Aref[4]))                                                 \
-  E(72, QA4, 2.0 * (s * L.A[4] / L.Aref[4]) * s / L.Aref[4])                             \
-  E(73, QA4, 0.5 / sqrt(s * L.A[4] / L.Aref[4]) * s / L.Aref[4])                         \
+  E(72, QA4, T(2.0) * (s * L.A[4] / L.Aref[4]) * s / L.Aref[4])                             \
+  E(73, QA4, T(0.5) / sqrt(s * L.A[4] / L.Aref[4]) * s / L.Aref[4])                         \
   E(74, QA4, s / L.Aref[4] * dT2)                                                        \
-  E(74, 0, (s * L.A[4] / L.Aref[4]) * 2.0 * adT)                                         \
-  E(75, QA4, 2.0 * s * (L.A[4] / L.Aref[4]) / L.gazp[4] / L.Aref[4])                     \
+  E(74, 0, (s * L.A[4] / L.Aref[4]) * T(2.0) * adT)                                         \
+  E(75, QA4, T(2.0) * s * (L.A[4] / L.Aref[4]) / L.gazp[4] / L.Aref[4])                     \
   E(75, QGAZP4, -COc / L.gazp[4] / L.gazp_ref[4])                                        \
   E(76, QA4,                                                                             \
-    ((2.0 * s * (L.A[4] / L.Aref[4]) / L.gazp[4]) / sqrt(s * L.A[4] / L.Aref[4]) -       \
-     COc * 0.5 * s / (sqrt(s * L.A[4] / L.Aref[4]) * (s * L.A[4] / L.Aref[4]))) /        \
+    ((T(2.0) * s * (L.A[4] / L.Aref[4]) / L.gazp[4]) / sqrt(s * L.A[4] / L.Aref[4]) -       \
+     COc * T(0.5) * s / (sqrt(s * L.A[4] / L.Aref[4]) * (s * L.A[4] / L.Aref[4]))) /        \
         L.Aref[4])                                                                       \
   E(76, QGAZP4, -COc / sqrt(s * L.A[4] / L.Aref[4]) / L.gazp[4] / L.gazp_ref[4])         \
-  E(77, QA4, 2.0 * s * (L.A[4] / L.Aref[4]) / L.gazp[4] * sqrt(L.gazp[4]) / L.Aref[4])   \
-  E(77, QGAZP4, -0.5 * COc / sqrt(L.gazp[4]) / L.gazp_ref[4])
+  E(77, QA4, T(2.0) * s * (L.A[4] / L.Aref[4]) / L.gazp[4] * sqrt(L.gazp[4]) / L.Aref[4])   \
+  E(77, QGAZP4, -T(0.5) * COc / sqrt(L.gazp[4]) / L.gazp_ref[4])
 
 // CH4 (group 1, slots 78..88)
 #define PD_CH4(E)                                                                        \
   E(78, QA5, s / L.Aref[5] * dT)                                                         \
   E(78, 0, s * L.A[5] / L.Aref[5])                                                       \
-  E(79, QA5, 0.5 / sqrt(s * L.A[5] / L.Aref[5]) * s / L.Aref[5])                         \
-  E(80, QA5, 2.0 * (s * L.A[5] / L.Aref[5]) * s / L.Aref[5])                             \
+  E(79, QA5, T(0.5) / sqrt(s * L.A[5] / L.Aref[5]) * s / L.Aref[5])                         \
+  E(80, QA5, T(2.0) * (s * L.A[5] / L.Aref[5]) * s / L.Aref[5])                             \
   E(81, QA5, s / L.Aref[5])                                                              \
   E(82, QA5, dT / L.Aref[5])                                                             \
   E(82, 0, L.A[5] / L.Aref[5])                                                           \
   E(83, QGAZP5, s / L.gazp_ref[5])                                                       \
-  E(84, QGAZP5, 2.0 * s * L.gazp[5] * s / L.gazp_ref[5])                                 \
-  E(85, QA5, 0.25 * sqrt(sqrt(s * L.A[5] / L.Aref[5])) / (s * L.A[5] / L.Aref[5]) * s /  \
+  E(84, QGAZP5, T(2.0) * s * L.gazp[5] * s / L.gazp_ref[5])                                 \
+  E(85, QA5, T(0.25) * sqrt(sqrt(s * L.A[5] / L.Aref[5])) / (s * L.A[5] / L.Aref[5]) * s /  \
                  L.Aref[5])                                                              \
-  E(86, QGATZP5, 1.0 / L.gatzp_ref[5])                                                   \
+  E(86, QGATZP5, T(1.0) / L.gatzp_ref[5])                                                   \
   E(87, QGATZP5, s / L.gatzp_ref[5])                                                     \
   E(88, QA5,                                                                             \
-    (0.5 / sqrt(s * L.A[5] / L.Aref[5]) * s * (L.A[5] / L.Aref[5]) +                     \
+    (T(0.5) / sqrt(s * L.A[5] / L.Aref[5]) * s * (L.A[5] / L.Aref[5]) +                     \
      sqrt(s * L.A[5] / L.Aref[5])) / L.gazp[5] / L.Aref[5])                              \
   E(88, QGAZP5,                                                                          \
     -sqrt(s * L.A[5] / L.Aref[5]) * (L.A[5] / L.Aref[5]) / (L.gazp[5] * L.gazp[5]) /     \
@@ -378,13 +382,13 @@ template <> struct PdNnz<3> { static constexpr int value = PD_NNZ_G3; };
 // Value writer: D[e] for the e-th entry, in list order.
 #define CRTM_PD_VALUE(slot, q, expr) D[e++] = R(expr);
 
-template <int G, class R>
-CRTM_HD void layer_partials(const LayerState& L, R* D) {
+template <int G, class R, class T = double>
+CRTM_HD void layer_partials(const LayerStateT<T>& L, R* D) {
   CRTM_PD_LOCALS(G)
   CRTM_PD_QCODES(G)
   int e = 0;
   if (G == 1) {
-    const double COc = (s * L.A[4] / L.Aref[4]) * (L.A[4] / L.Aref[4]) / L.gazp[4];
+    const T COc = (s * L.A[4] / L.Aref[4]) * (L.A[4] / L.Aref[4]) / L.gazp[4];
     (void)COc;
     PD_ENTRIES_G1(CRTM_PD_VALUE)
   } else if (G == 2) {

@@ -137,20 +137,21 @@ CRTM_HD void prep_profile(const SensorTables& S, const ProfileIn& P, const Profi
   for (int k = 0; k < K; k++) {
     const double sa = sv / (EARTH_RADIUS + (S.zgeo[k + 1] + zoff));
     L.sec = 1.0 / sqrt(1.0 - sa * sa);
-    L.T = O.T[k];
+    L.T_ = O.T[k];
     L.Tref = S.ref_t[k];
+    L.dT = O.T[k] - S.ref_t[k];
     const double pdp = S.pdp[k];
     L.pdp = pdp;
-    tz_r += S.ref_t[k]; tz_s += L.T;
+    tz_r += S.ref_t[k]; tz_s += L.T_;
     L.tz_ref = tz_r; L.tz = tz_s / tz_r;
-    tzp_r += pdp * S.ref_t[k]; tzp_s += pdp * L.T;
+    tzp_r += pdp * S.ref_t[k]; tzp_s += pdp * L.T_;
     L.tzp_ref = tzp_r; L.tzp = tzp_s / tzp_r;
     for (int j = 0; j < Jm; j++) {
       const double a = O.A[j * K + k], ar = S.ref_a[j * K + k];
       L.A[j] = a; L.Aref[j] = ar;
       gazp_r[j] += pdp * ar; gazp_s[j] += pdp * a;
       L.gazp_ref[j] = gazp_r[j]; L.gazp[j] = gazp_s[j] / gazp_r[j];
-      gatzp_r[j] += pdp * ar * S.ref_t[k]; gatzp_s[j] += pdp * a * L.T;
+      gatzp_r[j] += pdp * ar * S.ref_t[k]; gatzp_s[j] += pdp * a * L.T_;
       L.gatzp_ref[j] = gatzp_r[j]; L.gatzp[j] = gatzp_s[j] / gatzp_r[j];
     }
     layer_predictors<G, R>(L, O.X + (size_t)k * NS);

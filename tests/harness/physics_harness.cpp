@@ -25,7 +25,7 @@ void hx_pattern(int group, int* slot, int* q) {
 // Layer predictors and partials for an explicit layer state (arrays of MAX_ABS).
 void hx_layer(int group, const double* st, double* X, double* D) {
   LayerState L;
-  L.sec = st[0]; L.T = st[1]; L.Tref = st[2]; L.pdp = st[3];
+  L.sec = st[0]; L.T_ = st[1]; L.Tref = st[2]; L.pdp = st[3]; L.dT = st[1] - st[2];
   L.tz = st[4]; L.tzp = st[5]; L.tz_ref = st[6]; L.tzp_ref = st[7];
   for (int a = 0; a < MAX_ABS; a++) {
     L.A[a] = st[8 + a]; L.Aref[a] = st[14 + a];

@@ -132,3 +132,16 @@ def test_device_entry_points_and_stage_times(gpu_lib, coeff_dir):
     assert np.array_equal(out["temperature_k"].cpu().numpy(), km.temperature)
     for s in ("prep", "absorb_fwd", "column", "absorb_ad", "map_out"):
         assert st[s][1] >= 1 and st[s][0] > 0.0
+
+
+def test_mixed_against_fp64_on_many_profiles(gpu_lib, coeff_dir):
+    """The mixed form against the FP64 form on 300 profiles (rare layer states,
+    e.g. T within a few mK of the reference temperature, show up only in
+    larger batches): 0.01 K in BT, 1e-3 relative in the Jacobians."""
+    sensor = "irsynth_c616"
+    atm, sfc, geo, opt = _case(sensor, 300, 101, 23)
+    ref = gpu_lib.CRTM([sensor], coeff_dir, 0).k_matrix(atm, sfc, geo, opt)
+    mix = gpu_lib.CRTM([sensor], coeff_dir, 1).k_matrix(atm, sfc, geo, opt)
+    assert np.abs(mix[1].brightness_temperature - ref[1].brightness_temperature).max() <= BT_TOL[1]
+    for f in ("temperature", "absorber", "water_temperature"):
+        assert _rel(getattr(mix[0], f), getattr(ref[0], f)) <= JAC_TOL[1], f
