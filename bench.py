@@ -32,6 +32,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 from crtmv3_gb300 import synthetic as sy  # noqa: E402
+from crtmv3_gb300.replicas import max_over_ranks  # noqa: E402
 
 SENSOR = "irsynth_c2211"
 N_LAYERS = 101
@@ -133,18 +134,30 @@ def k_outputs(torch, P, L, K, JK, dev):
                 status=torch.empty((P,), dtype=torch.int32, device=dev))
 
 
-def cpu_baseline(P_sample: int, threads: int):
-    """FP64 oracle (restatement of the reference's CPU path) on the host cores."""
+def cpu_baseline(P_sample: int, threads: int, min_seconds: float = 10.0):
+    """FP64 oracle (restatement of the reference's CPU path) on the host cores:
+    K-matrix calls on batches of ``P_sample`` profiles of the workload, repeated
+    until at least ``min_seconds`` of CPU work; returns (p*c/s, seconds, calls)."""
     from oracle.pyoracle import Oracle
     atm, sfc, geo, opt = make_workload(P_sample, 2024)
     o = Oracle(COEFF_DIR, SENSOR)
-    o.k_matrix(atm.subset(slice(0, min(2, P_sample))), sfc.subset(slice(0, min(2, P_sample))),
-               geo.subset(slice(0, min(2, P_sample))), opt.subset(slice(0, min(2, P_sample))),
-               n_threads=threads)
-    t0 = time.perf_counter()
-    o.k_matrix(atm, sfc, geo, opt, n_threads=threads)
-    dt = time.perf_counter() - t0
-    return P_sample * o.n_channels / dt, dt
+    w = slice(0, min(2, P_sample))
+    o.k_matrix(atm.subset(w), sfc.subset(w), geo.subset(w), opt.subset(w), n_threads=threads)
+    calls, t0 = 0, time.perf_counter()
+    while True:
+        o.k_matrix(atm, sfc, geo, opt, n_threads=threads)
+        calls += 1
+        dt = time.perf_counter() - t0
+        if dt >= min_seconds:
+            break
+    return calls * P_sample * o.n_channels / dt, dt, calls
+
+
+def workload_config(P: int, world: int) -> dict:
+    return {"workload": f"clear-sky IR forward+K-matrix, {P} profiles x {N_LAYERS} layers x 2211 "
+                        f"channels (ODPS group 1, Emission), Jacobians T/H2O/O3 + Tskin",
+            "profiles": P, "layers": N_LAYERS, "channels": 2211, "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2: 10.7 GB of K-matrix output per step, no flush"}
 
 
 def run_reference(args):
@@ -156,19 +169,18 @@ def run_reference(args):
     P_sample = args.cpu_profiles
     vals = []
     for _ in range(args.warmup):
-        cpu_baseline(max(threads // 2, 1), threads)
+        cpu_baseline(max(threads // 2, 1), threads, min_seconds=0.0)
     for _ in range(args.steps):
-        v, dt = cpu_baseline(P_sample, threads)
+        v, dt, calls = cpu_baseline(P_sample, threads, min_seconds=0.0)
         vals.append((v, dt))
     value = statistics.median(v for v, _ in vals)
     ms = statistics.median(dt for _, dt in vals) * 1e3
-    line = {"impl": "reference", "metric": METRIC.replace("mixed precision, inputs in HBM", "FP64 CPU"),
+    cfg = workload_config(args.profiles, 1)
+    cfg["sample_profiles_per_step"] = P_sample
+    line = {"impl": "reference", "metric": METRIC,
             "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"clear-sky IR K-matrix, {P_sample} of 2000 profiles x {N_LAYERS} "
-                                   f"layers x 2211 channels per step", "profiles": P_sample,
-                       "layers": N_LAYERS, "channels": 2211},
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{P_sample} profiles x 2211 channels K-matrix per step "
                                        f"(FP64 C oracle, OpenMP over profiles)"},
@@ -184,7 +196,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--profiles", type=int, default=2000)
-    ap.add_argument("--cpu-profiles", type=int, default=128)
+    ap.add_argument("--cpu-profiles", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -236,12 +248,7 @@ def main():
             step(prec)
         e1.record(stream)
         torch.cuda.synchronize(dev)
-        ms = e0.elapsed_time(e1)
-        if dist:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return max_over_ranks(e0.elapsed_time(e1), dist, dev)
 
     for _ in range(args.warmup):
         step(1)
@@ -249,8 +256,14 @@ def main():
         step(0)
     torch.cuda.synchronize(dev)
     launches0 = h.launch_count()
+    # per-stage kernel times: CUDA events around every launch on the launching
+    # stream, recorded by the library during the timed steps themselves
+    h.set_profiling(True)
+    h.stage_times(reset=True)
     with ClockSampler(local) as clk:
         ms_mixed = timed(1, args.steps)
+    st = h.stage_times(reset=True)
+    h.set_profiling(False)
     launches_mixed = (h.launch_count() - launches0) // args.steps
     fp64_steps = max(1, min(args.steps, 3))
     ms_fp64 = timed(0, fp64_steps)
@@ -269,32 +282,37 @@ def main():
     jac_err = max(rel(a["temperature_k"], r["temperature_k"]), rel(a["absorber_k"], r["absorber_k"]),
                   rel(a["water_temperature_k"], r["water_temperature_k"]))
 
-    # per-stage kernel times (live CUDA events inside the library, one more mixed step)
-    h.set_profiling(True)
-    h.stage_times(reset=True)
-    step(1)
-    st = h.stage_times(reset=True)
-    h.set_profiling(False)
-    stage_ms = {k: v[0] for k, v in st.items() if v[1] > 0}
-    stage_launch = {k: v[1] for k, v in st.items() if v[1] > 0}
-    dom = max(stage_ms, key=stage_ms.get)
+    stage_ms = {k: v[0] / args.steps for k, v in st.items() if v[1] > 0}
+    stage_launch = {k: v[1] // args.steps for k, v in st.items() if v[1] > 0}
     hbm, bf16, peak_kind = peaks()
-    # algorithmic bytes of the dominant stage per launch (map_out writes the
-    # Jacobians and reads the reference-layer adjoints; column reads/writes the OD columns)
-    n_chunks = stage_launch[dom]
-    algo = {
-        "map_out": P * L * ((1 + JK) * K * 8 + 3 * K * 4 + 2 * 8),
-        "column": P * L * (K * 4 * 2 + 5 * K * 4 * 2 + 8 * 4),
-        "absorb_ad": P * L * (K * 4 + 3 * K * 4),
-        "absorb_fwd": P * L * K * 4,
-        "prep": P * K * 8 * 200,
+    # Algorithmic bytes per profile*channel of each stage in the mixed form (FP32
+    # intermediates, FP64 outputs; K_r = 100 reference layers, K_u = 101 user
+    # layers, 2 absorber Jacobians), and the DRAM bytes per profile*channel that
+    # ncu measured for the same kernels on a 192-profile case of this workload
+    # (profiles/kmatrix_c2_kernels.md).
+    kr, ku = 100, K
+    algo_pc = {
+        "map_out": (1 + JK) * kr * 4 + ku * 4 + 4 + (1 + JK) * ku * 8,
+        "column": kr * 4 + 2 * 2 * ku * 4 + kr * 4 + kr * 4 + ku * 4 + 36,
+        "absorb_ad": kr * 4 + 4 + (1 + JK) * kr * 4,
+        "absorb_fwd": kr * 4,
     }
-    bytes_per_launch = algo.get(dom, 0) / n_chunks
-    t_launch = stage_ms[dom] / n_chunks * 1e-3
-    achieved = bytes_per_launch / t_launch / 1e9
+    ncu_pc = {"map_out": 3915.0, "column": 2501.0, "absorb_ad": 1917.0, "absorb_fwd": 495.0}
+    kernels = {}
+    for st_name, ms in stage_ms.items():
+        if st_name not in algo_pc:
+            continue
+        kernels[st_name] = {"ms_per_step": ms,
+                            "achieved_gbs": algo_pc[st_name] * P * L / (ms * 1e-3) / 1e9,
+                            "algorithmic_bytes_per_pc": algo_pc[st_name]}
+    dom = max(kernels, key=lambda k: kernels[k]["ms_per_step"])
+    n_launch = stage_launch[dom]
+    pc_launch = P * L / n_launch
+    achieved = kernels[dom]["achieved_gbs"]
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": None, "kernel": dom,
-                "peak_source": peak_kind}
+                "frac": achieved / hbm, "traffic": ncu_pc[dom] * pc_launch,
+                "algorithmic_bytes": algo_pc[dom] * pc_launch, "kernel": dom,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"}
 
     # end to end through the C-ABI with host (pinned) buffers, mixed form
     e2e = None
@@ -315,31 +333,42 @@ def main():
         h2d = sum(x.nbytes for x in (atm.level_pressure, atm.pressure, atm.temperature, atm.absorber,
                                      opt.emissivity)) + 10 * P * 8 + P * 4
         d2h = P * L * 8 * (2 + K + JK * K + 2) + P * 4
+        # the host link bounds this figure: plain pinned device-to-host copy rate
+        nb = 1 << 28
+        dsrc = torch.empty(nb, dtype=torch.float64, device=dev)
+        hdst = torch.empty(nb, dtype=torch.float64, pin_memory=True)
+        hdst.copy_(dsrc)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(3):
+            hdst.copy_(dsrc, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        d2h_gbs = 3 * nb * 8 / (time.perf_counter() - t0) / 1e9
+        del dsrc, hdst
         e2e = {"value": pc / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "ms_per_step": dt * 1e3}
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": dt * 1e3,
+               "d2h_copy_gbs": d2h_gbs, "d2h_bound_ms": d2h / d2h_gbs / 1e6}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, dt = cpu_baseline(args.cpu_profiles, threads)
+        v, dt, calls = cpu_baseline(args.cpu_profiles, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{args.cpu_profiles} profiles x 2211 channels x {N_LAYERS} layers K-matrix, "
-                         f"FP64 C oracle with OpenMP over profiles ({dt:.1f} s)"}
+               "sample": f"{calls} K-matrix calls of {args.cpu_profiles} profiles x 2211 channels x "
+                         f"{N_LAYERS} layers (all absorber Jacobians), FP64 C oracle with OpenMP "
+                         f"over profiles, {dt:.1f} s"}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": per_mixed, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "mixed f32/f64", "data": "synthetic",
-            "config": {"workload": f"clear-sky IR forward+K-matrix, {P} profiles x {N_LAYERS} layers x "
-                                   f"{L} channels (ODPS group 1, Emission), Jacobians T/H2O/O3 + Tskin",
-                       "profiles": P, "layers": N_LAYERS, "channels": L, "parallelism": f"replicas x{world}",
-                       "l2": "per-step working set > L2 (10.7 GB of K-matrix output per step)"},
+            "config": workload_config(P, world),
             "fp64_gpu": {"value": fp64_value, "ms_per_step": per_fp64, "steps": fp64_steps},
             "speedup_mixed_vs_fp64": value / fp64_value,
             "accuracy_mixed_vs_fp64": {"max_abs_bt_K": bt_err, "max_rel_jacobian": jac_err},
             "stages_ms_per_step": stage_ms, "stage_launches_per_step": stage_launch,
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "kernels": kernels, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(launches_mixed * args.steps),
             "clocks": clk.summary(),
         }

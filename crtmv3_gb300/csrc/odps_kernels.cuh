@@ -621,8 +621,9 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   const int p = blockIdx.y, gp = a.p_begin + p;
   const int tid = threadIdx.x;
   const int l = blockIdx.x * blockDim.x + tid;
-  double* facd = reinterpret_cast<double*>(smem_raw);   // [Kmax+1]
-  R* tus = reinterpret_cast<R*>(facd + Kmax + 1);        // [Kmax]
+  // interpolation factors in R, converted once per CTA (the slot is sized for doubles)
+  R* facd = reinterpret_cast<R*>(smem_raw);              // [Kmax+1]
+  R* tus = reinterpret_cast<R*>(reinterpret_cast<double*>(smem_raw) + Kmax + 1);   // [Kmax]
   int* k1s = reinterpret_cast<int*>(tus + Kmax);         // [Kmax+1]
   int* k2s = k1s + (Kmax + 1);
   int* ilos = k2s + (Kmax + 1);                          // [K+1]
@@ -646,7 +647,7 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   const int* k1g = a.pv.ulev_k1 + (size_t)p * (Kmax + 1);
   const int* k2g = a.pv.ulev_k2 + (size_t)p * (Kmax + 1);
   const double* fg = a.pv.ulev_fac + (size_t)p * (Kmax + 1);
-  for (int i = tid; i <= Ku; i += blockDim.x) { k1s[i] = k1g[i]; k2s[i] = k2g[i]; facd[i] = fg[i]; }
+  for (int i = tid; i <= Ku; i += blockDim.x) { k1s[i] = k1g[i]; k2s[i] = k2g[i]; facd[i] = R(fg[i]); }
   if (a.mode) {
     const int* ilg = a.pv.rlev_ilo + (size_t)p * (K + 1);
     const int* ihg = a.pv.rlev_ihi + (size_t)p * (K + 1);
@@ -664,9 +665,11 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   const R re = R(e), rr = R(1.0 - e);
   const double tsd = a.b.land_cov[gp] * a.b.land_t[gp] + a.b.water_cov[gp] * a.b.water_t[gp] +
                      a.b.snow_cov[gp] * a.b.snow_t[gp] + a.b.ice_cov[gp] * a.b.ice_t[gp];
-  const double ted = b1d + b2d * tsd;
-  const double eed = exp(c2d / ted);
-  const R Bs = R(c1d / (eed - 1.0));
+  // surface Planck radiance and its temperature derivative in R (the Planck
+  // inversion at the end stays in FP64)
+  const R ted = b1 + b2 * R(tsd);
+  const R eed = exp(c2 / ted);
+  const R Bs = c1 / (eed - R(1));
   R* od = a.OD + (size_t)p * K * L + l;
   const size_t cs = (size_t)p * Kmax * L + l;   // scratch base, stride L
 
@@ -682,7 +685,7 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   for (int k = 0; k <= K; k++) {
     while (i <= Ku && k2s[i] == k) {
       const int ka = k1s[i];
-      const R upi = (ka == k) ? path_cur : path_prev + (path_cur - path_prev) * R(facd[i]);
+      const R upi = (ka == k) ? path_cur : path_prev + (path_cur - path_prev) * facd[i];
       if (i > 0) {
         const int ku = i - 1;
         const R tau = (upi - up_prev) * inv_sec;
@@ -738,7 +741,7 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
     if (ka == kb) {
       if (ka == plvl) pa_lo += v; else pa_hi += v;
     } else {
-      const R f = R(facd[iu]);
+      const R f = facd[iu];
       pa_lo += (R(1) - f) * v;
       pa_hi += f * v;
     }
@@ -778,13 +781,16 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   // ---- TOA radiance, brightness temperature and the adjoint seed
   const double Rd = double(U);
   a.radiance[pl] = Rd;
-  a.bt[pl] = planck_temperature(c1d, c2d, b1d, b2d, Rd);
+  double btv, dtdr;
+  planck_temperature_with_dR(c1d, c2d, b1d, b2d, Rd, &btv, &dtdr);
+  a.bt[pl] = btv;
   const double seed = a.seed ? a.seed[pl] : 1.0;
-  const double scale = planck_temperature_dR(c1d, c2d, b1d, b2d, Rd) * seed;
+  const double scale = dtdr * seed;
   a.SC[(size_t)p * L + l] = R(scale);
-  const double dBs = c1d * c2d * eed * b2d / ((ted * (eed - 1.0)) * (ted * (eed - 1.0)));
+  const R dden = ted * (eed - R(1));
+  const R dBs = c1 * c2 * eed * b2 / (dden * dden);
   const double up_final = scale * double(Tn);
-  const double ts_ad = a.b.water_cov[gp] * dBs * e * up_final;
+  const double ts_ad = a.b.water_cov[gp] * double(dBs) * e * up_final;
   if (a.mode == 1) {
     a.tsk[pl] = ts_ad;
     a.ek[pl] = up_final * (double(Bs) - double(Dn));   // emissivity_AD - reflectivity_AD
@@ -857,12 +863,23 @@ __global__ void __launch_bounds__(32 * AD_WARPS) absorb_ad_kernel(
     }
     cp_async_commit();
   };
+  // OD adjoints of the next layer are loaded one iteration ahead
+  R odn[NP];
+#pragma unroll
+  for (int p = 0; p < NP; p++)
+    odn[p] = (active && p0 + p < n_chunk) ? ODAD[((size_t)(p0 + p) * K + (K - 1)) * L + l] : R(0);
   stage(K - 1, (K - 1) & 1);
   for (int k = K - 1; k >= 0; k--) {
     cp_async_wait_all();
     __syncthreads();
     if (k > 0) stage(k - 1, (k - 1) & 1);
     if (!group_ok) continue;
+    R odc[NP];
+#pragma unroll
+    for (int p = 0; p < NP; p++) {
+      odc[p] = odn[p];
+      if (k > 0 && active && p0 + p < n_chunk) odn[p] = ODAD[((size_t)(p0 + p) * K + (k - 1)) * L + l];
+    }
     const float (*ct)[32] = cs[k & 1];
     const R* Dk = ds[k & 1][wib];
     R E[NP][NV];
@@ -884,7 +901,7 @@ __global__ void __launch_bounds__(32 * AD_WARPS) absorb_ad_kernel(
 #pragma unroll
     for (int p = 0; p < NP; p++) {
       const bool valid = active && (p0 + p < n_chunk);
-      const R oda = valid ? ODAD[((size_t)(p0 + p) * K + k) * L + l] * scl[p] : R(0);
+      const R oda = valid ? odc[p] * scl[p] : R(0);
       const R pT = Dk[(NNZ + JM) * NP + p];
       const unsigned mask = (unsigned)Dk[(NNZ + JM + 1) * NP + p];
       Stz[p] += oda * E[p][qTz<G>()];

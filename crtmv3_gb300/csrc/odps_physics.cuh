@@ -9,6 +9,8 @@
 #pragma once
 
 #include <math.h>
+#include <stdint.h>
+#include <string.h>
 
 #ifdef __CUDACC__
 #define CRTM_HD __host__ __device__ __forceinline__
@@ -591,6 +593,38 @@ CRTM_HD R planck_radiance_dT(R c1, R c2, R b1, R b2, R T) {
   R d = te * (e - R(1));
   return c1 * c2 * e * b2 / (d * d);
 }
+// Exact float -> double conversion with integer operations.  On GB300 the
+// hardware conversion runs on the narrow FP64 pipe; kernels that store FP64
+// results of FP32 arithmetic (one conversion per output element) use this
+// instead.  Handles zeros, subnormals, infinities and NaNs.
+CRTM_HD double f32_to_f64_exact(float f) {
+  uint32_t u;
+  memcpy(&u, &f, 4);
+  const uint32_t sign = u & 0x80000000u;
+  uint32_t e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  uint32_t hi;
+  if (e == 0xffu) {
+    hi = sign | 0x7ff00000u | (m >> 3);
+  } else if (e == 0) {
+    if (m == 0) {
+      hi = sign;
+    } else {   // subnormal float: normalise (the double is normal)
+      int sh = 0;
+      while (!(m & 0x800000u)) { m <<= 1; sh++; }
+      m &= 0x7fffffu;
+      hi = sign | ((uint32_t)(1 - sh + 896) << 20) | (m >> 3);
+    }
+  } else {
+    hi = sign | ((e + 896u) << 20) | (m >> 3);
+  }
+  const uint64_t bits = ((uint64_t)hi << 32) | ((uint64_t)(m & 7u) << 29);
+  double d;
+  memcpy(&d, &bits, 8);
+  return d;
+}
+CRTM_HD double to_f64(float f) { return f32_to_f64_exact(f); }
+CRTM_HD double to_f64(double d) { return d; }
+
 CRTM_HD double planck_temperature(double c1, double c2, double b1, double b2, double R) {
   double te = c2 / log(c1 / R + 1.0);
   return (te - b1) / b2;
@@ -599,6 +633,16 @@ CRTM_HD double planck_temperature_dR(double c1, double c2, double b1, double b2,
   double arg = c1 / R + 1.0;
   double d = R * log(arg);
   return c1 * c2 / (b2 * arg * d * d);
+}
+// Both of the above from one logarithm (CRTM_Planck_Temperature and its adjoint,
+// CRTM_Planck_Functions.f90:470-492,697-723).
+CRTM_HD void planck_temperature_with_dR(double c1, double c2, double b1, double b2, double R,
+                                        double* T, double* dTdR) {
+  const double arg = c1 / R + 1.0;
+  const double lg = log(arg);
+  *T = (c2 / lg - b1) / b2;
+  const double d = R * lg;
+  *dTdR = c1 * c2 / (b2 * arg * d * d);
 }
 
 }  // namespace crtm

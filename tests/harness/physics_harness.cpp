@@ -105,3 +105,5 @@ extern "C" int hx_layer_avg_debug(const double* px1, int kn1, const double* px2,
   }
   return 0;
 }
+
+extern "C" double hx_f32_to_f64(float f) { return f32_to_f64_exact(f); }

@@ -132,3 +132,20 @@ def test_layer_average_columns_are_independent(hx):
         mb = ct.c_int(0)
         assert hx.hx_layer_avg_compare(_ptr(ref), 100, _ptr(lay), n, ct.byref(mb)) == 0
         assert mb.value <= MAX_BAND
+
+
+def test_exact_float_to_double_conversion(hx):
+    """The integer-pipe float->double conversion used for FP64 stores of FP32
+    results equals the hardware conversion, including zeros, subnormals,
+    infinities and the largest finite values."""
+    hx.hx_f32_to_f64.argtypes = [ct.c_float]
+    hx.hx_f32_to_f64.restype = ct.c_double
+    rng = np.random.default_rng(7)
+    bits = np.concatenate([rng.integers(0, 2**32, 200000, dtype=np.uint64).astype(np.uint32),
+                           np.arange(0, 70000, dtype=np.uint32),                    # subnormals
+                           np.arange(0x7f7f0000, 0x7f800001, 97, dtype=np.uint32),  # large, inf
+                           np.array([0x80000000, 0x80000001, 0xff800000], np.uint32)])
+    f = bits.view(np.float32)
+    f = f[~np.isnan(f)]
+    got = np.array([hx.hx_f32_to_f64(float(x)) for x in f])
+    assert np.array_equal(got.view(np.uint64), f.astype(np.float64).view(np.uint64))
