@@ -94,6 +94,7 @@ def library() -> ct.CDLL:
                                            ct.POINTER(CKMatrix), ct.POINTER(CRTSolution), ct.c_void_p]
     L.crtm_gpu_adjoint_device.argtypes = [ct.c_void_p, ct.c_int, ct.POINTER(CBatch), ct.c_void_p,
                                           ct.POINTER(CAdjoint), ct.POINTER(CRTSolution), ct.c_void_p]
+    L.crtm_gpu_k_matrix_device_static.argtypes = L.crtm_gpu_k_matrix_device.argtypes
     L.crtm_gpu_last_error.argtypes = [ct.c_void_p, ct.c_char_p, ct.c_int]
     L.crtm_gpu_launch_count.argtypes = [ct.c_void_p]
     L.crtm_gpu_launch_count.restype = ct.c_longlong
@@ -271,15 +272,19 @@ class CRTM:
         return b, keep
 
     def k_matrix_device(self, b: CBatch, out: dict, seed=None, sensor: int = 0, stream=None,
-                        k_absorbers=None) -> None:
+                        k_absorbers=None, static_scratch: bool = False) -> None:
+        """K-matrix on device tensors.  ``static_scratch``: use the entry point that
+        keeps its intermediates in the library's fixed per-device scratch and
+        allocates no device memory (calls must not overlap in time)."""
         cr = CRTSolution(out["radiance"].data_ptr(), out["bt"].data_ptr(),
                          _addr(out.get("status")))
         sel = None if k_absorbers is None else np.ascontiguousarray(k_absorbers, np.int32)
         ck = CKMatrix(out["temperature_k"].data_ptr(), out["absorber_k"].data_ptr(),
                       out["water_temperature_k"].data_ptr(), out["surface_emissivity_k"].data_ptr(),
                       0 if sel is None else int(sel.shape[0]), None if sel is None else sel.ctypes.data)
-        self._check(library().crtm_gpu_k_matrix_device(self.h, sensor, ct.byref(b), _addr(seed),
-                                                       ct.byref(ck), ct.byref(cr), stream))
+        fn = (library().crtm_gpu_k_matrix_device_static if static_scratch
+              else library().crtm_gpu_k_matrix_device)
+        self._check(fn(self.h, sensor, ct.byref(b), _addr(seed), ct.byref(ck), ct.byref(cr), stream))
 
     def forward_device(self, b: CBatch, out: dict, sensor: int = 0, stream=None) -> None:
         cr = CRTSolution(out["radiance"].data_ptr(), out["bt"].data_ptr(), _addr(out.get("status")))

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
@@ -24,9 +25,26 @@
 
 using namespace crtm;
 
+// Scratch of crtm_gpu_k_matrix_device_static: one fixed block per device,
+// reserved when the module loads, so that the call itself allocates nothing.
+// 128 MiB holds the intermediates of at least one profile for up to ~8500
+// channels at 200 layers with 8 absorber Jacobians in FP64; larger batches
+// are processed in chunks that fit.
+static constexpr size_t STATIC_SCRATCH_BYTES = (size_t)CRTM_GPU_STATIC_SCRATCH_MIB << 20;
+static __device__ __align__(256) unsigned char g_static_scratch[STATIC_SCRATCH_BYTES];
+
 namespace {
 
 thread_local std::string g_init_error;
+
+// Device address of g_static_scratch, looked up once per device.
+constexpr int MAX_STATIC_DEVICES = 64;
+struct StaticScratchSlot {
+  std::once_flag once;
+  void* ptr = nullptr;
+  cudaError_t err = cudaSuccess;
+};
+StaticScratchSlot g_static_slots[MAX_STATIC_DEVICES];
 
 // ---------------------------------------------------------------------------
 // Fortran sequential record files
@@ -487,6 +505,13 @@ struct HostCopy {
   int max_chunk = 0;   // cap on the chunk size so that copies overlap compute
 };
 
+// Caller-owned scratch of fixed size used instead of the handle's workspace
+// (crtm_gpu_k_matrix_device_static).
+struct FixedScratch {
+  char* base;
+  size_t bytes;
+};
+
 int copy_chunk(crtm_gpu_handle h, const HostCopy* hc, int p0, int n, cudaStream_t st) {
   if (!h->copy_stream && cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
     return fail(h, "cannot create the copy stream");
@@ -510,7 +535,8 @@ int copy_chunk(crtm_gpu_handle h, const HostCopy* hc, int p0, int n, cudaStream_
 template <int G, class R>
 int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, int mode,
                  const double* seed, crtm_gpu_rtsolution* rts, crtm_gpu_kmatrix* kk,
-                 crtm_gpu_adjoint_out* ad, cudaStream_t st, const HostCopy* hc) {
+                 crtm_gpu_adjoint_out* ad, cudaStream_t st, const HostCopy* hc,
+                 const FixedScratch* fixed) {
   const int P = b->n_profiles, Kmax = b->max_layers, L = s.L, K = s.K, n_abs = b->n_absorbers;
   if (P <= 0) return CRTM_GPU_SUCCESS;
   if (Kmax < 2 || Kmax > MAX_LAYERS) return fail(h, "max_layers %d out of range [2, %d]", Kmax, MAX_LAYERS);
@@ -544,10 +570,24 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
   const size_t per = work_bytes<G, R>(s, 64, Kmax, nv, mode, nullptr, nullptr) / 64 + 1;
   int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)P, h->workspace_budget / per));
   if (hc && hc->max_chunk > 0) chunk = std::min(chunk, hc->max_chunk);
-  const size_t need = work_bytes<G, R>(s, chunk, Kmax, nv, mode, nullptr, nullptr);
-  if (!h->ws.ensure(need)) return fail(h, "cannot allocate %zu bytes of workspace", need);
+  char* ws_base;
+  if (fixed) {
+    // largest chunk whose workspace fits the fixed scratch
+    chunk = (int)std::min<size_t>((size_t)chunk, fixed->bytes / per);
+    while (chunk > 1 && work_bytes<G, R>(s, chunk, Kmax, nv, mode, nullptr, nullptr) > fixed->bytes) chunk--;
+    const size_t one = work_bytes<G, R>(s, 1, Kmax, nv, mode, nullptr, nullptr);
+    if (chunk < 1 || one > fixed->bytes)
+      return fail(h, "one profile of this call needs %zu bytes of scratch (%d channels, max_layers %d, "
+                     "%d absorber Jacobians); the static scratch holds %zu bytes",
+                  one, L, Kmax, nv - 1, fixed->bytes);
+    ws_base = fixed->base;
+  } else {
+    const size_t need = work_bytes<G, R>(s, chunk, Kmax, nv, mode, nullptr, nullptr);
+    if (!h->ws.ensure(need)) return fail(h, "cannot allocate %zu bytes of workspace", need);
+    ws_base = (char*)h->ws.p;
+  }
   Work<R> w;
-  work_bytes<G, R>(s, chunk, Kmax, nv, mode, &w, (char*)h->ws.p);
+  work_bytes<G, R>(s, chunk, Kmax, nv, mode, &w, ws_base);
   if (cudaMemcpyAsync(w.idx_map, idx_map, sizeof(int) * s.Jm, cudaMemcpyHostToDevice, st) != cudaSuccess)
     return fail(h, "absorber map upload failed");
   const BatchView bv = make_view(b);
@@ -651,7 +691,7 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
 
 int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, const double* seed,
              crtm_gpu_rtsolution* rts, crtm_gpu_kmatrix* kk, crtm_gpu_adjoint_out* ad,
-             cudaStream_t st, const HostCopy* hc = nullptr) {
+             cudaStream_t st, const HostCopy* hc = nullptr, const FixedScratch* fixed = nullptr) {
   if (!h) return CRTM_GPU_FAILURE;
   if (sensor < 0 || sensor >= (int)h->sensors.size()) return fail(h, "sensor index %d out of range", sensor);
   if (!b || !rts || !rts->radiance || !rts->brightness_temperature) return fail(h, "missing batch or RTSolution buffers");
@@ -668,12 +708,12 @@ int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, c
   const Sensor& s = h->sensors[sensor];
   const bool fp64 = h->precision == CRTM_GPU_FP64;
   switch (s.group) {
-    case 1: return fp64 ? run_pipeline<1, double>(h, s, b, mode, seed, rts, kk, ad, st, hc)
-                        : run_pipeline<1, float>(h, s, b, mode, seed, rts, kk, ad, st, hc);
-    case 2: return fp64 ? run_pipeline<2, double>(h, s, b, mode, seed, rts, kk, ad, st, hc)
-                        : run_pipeline<2, float>(h, s, b, mode, seed, rts, kk, ad, st, hc);
-    default: return fp64 ? run_pipeline<3, double>(h, s, b, mode, seed, rts, kk, ad, st, hc)
-                         : run_pipeline<3, float>(h, s, b, mode, seed, rts, kk, ad, st, hc);
+    case 1: return fp64 ? run_pipeline<1, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed)
+                        : run_pipeline<1, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed);
+    case 2: return fp64 ? run_pipeline<2, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed)
+                        : run_pipeline<2, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed);
+    default: return fp64 ? run_pipeline<3, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed)
+                         : run_pipeline<3, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed);
   }
 }
 
@@ -870,6 +910,38 @@ int crtm_gpu_adjoint_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch*
   if (!bt_ad) return fail(h, "missing adjoint seed");
   return dispatch(h, sensor, b, 2, bt_ad, rts, nullptr, ad,
                   stream ? (cudaStream_t)stream : (h ? h->stream : nullptr));
+}
+
+// The K-matrix of crtm_gpu_k_matrix_device with its intermediates in
+// g_static_scratch instead of the handle's grow-on-demand workspace.  Some
+// callers cannot let a call allocate: a host model whose device memory is
+// already held by its own caching allocator (a cudaMalloc here would fail or
+// force that cache to be released), or an assimilation loop that calls the
+// operator every iteration on a few profiles, where cudaMalloc and cudaFree
+// would synchronise the whole device and stall its other streams.
+//
+// The first call on a device looks up the scratch address with that device
+// current (cudaGetSymbolAddress); make that first call before any stream
+// capture begins.  Later calls only enqueue kernels and one small copy of
+// the absorber map.  No part of the scratch is read before the same call's
+// kernels write it, so nothing needs clearing between calls.  The scratch is
+// shared by every handle on the device: two calls that overlap in time (on
+// different streams, handles or host threads) overwrite each other's
+// intermediates, so callers must order them (one stream, or events).
+int crtm_gpu_k_matrix_device_static(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b,
+                                    const double* bt_k, crtm_gpu_kmatrix* k,
+                                    crtm_gpu_rtsolution* rts, void* stream) {
+  if (!h) return CRTM_GPU_FAILURE;
+  if (h->device < 0 || h->device >= MAX_STATIC_DEVICES)
+    return fail(h, "device %d has no static scratch slot", h->device);
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
+  StaticScratchSlot& slot = g_static_slots[h->device];
+  std::call_once(slot.once, [&slot] { slot.err = cudaGetSymbolAddress(&slot.ptr, g_static_scratch); });
+  if (slot.err != cudaSuccess || !slot.ptr)
+    return fail(h, "static scratch lookup failed: %s", cudaGetErrorString(slot.err));
+  const FixedScratch fx{(char*)slot.ptr, STATIC_SCRATCH_BYTES};
+  return dispatch(h, sensor, b, 1, bt_k, rts, k, nullptr,
+                  stream ? (cudaStream_t)stream : h->stream, nullptr, &fx);
 }
 
 int crtm_gpu_last_error(crtm_gpu_handle h, char* buf, int n) {

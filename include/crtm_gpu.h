@@ -149,6 +149,22 @@ int crtm_gpu_adjoint_device(crtm_gpu_handle handle, int sensor, const crtm_gpu_b
                             const double* bt_ad, crtm_gpu_adjoint_out* ad,
                             crtm_gpu_rtsolution* rts, void* stream);
 
+/* No counterpart in the reference (CRTM_K_Matrix allocates its work arrays on
+ * every call).  crtm_gpu_k_matrix_device without device-memory allocation:
+ * the intermediates live in a static per-device scratch of
+ * CRTM_GPU_STATIC_SCRATCH_MIB MiB, for callers whose device memory is held by
+ * another allocator or who cannot afford the device-wide synchronisation of
+ * cudaMalloc/cudaFree inside a call.  Batches are processed in chunks that fit
+ * the scratch; a call fails (CRTM_GPU_FAILURE, message from
+ * crtm_gpu_last_error) when one profile's intermediates do not fit.  The first
+ * call on a device looks up the scratch address and should come before any
+ * stream capture.  The scratch is shared by all handles on a device: calls
+ * that overlap in time race and must be ordered by the caller. */
+#define CRTM_GPU_STATIC_SCRATCH_MIB 128
+int crtm_gpu_k_matrix_device_static(crtm_gpu_handle handle, int sensor,
+                                    const crtm_gpu_batch* batch, const double* bt_k,
+                                    crtm_gpu_kmatrix* k, crtm_gpu_rtsolution* rts, void* stream);
+
 /* Copy the last error message of the handle (or of the last failed init when
  * handle is NULL) into buf; returns its length. */
 int crtm_gpu_last_error(crtm_gpu_handle handle, char* buf, int n);
