@@ -214,3 +214,90 @@ def read_spccoeff(path: str) -> SpcCoeff:
     ch, pol, pang, flag, freq, wn, c1, c2, b1, b2, cb, si = fields
     return SpcCoeff(sid, int(ids[0]), ch, freq, wn, c1, c2, b1, b2, cb, si, pol, pang, flag,
                     int(ids[1]), int(ids[2]))
+
+
+# ---------------------------------------------------------------------------
+# CloudCoeff (cloud optical property LUT)
+# ---------------------------------------------------------------------------
+
+CLOUDCOEFF_RELEASE = 3          # ``CloudCoeff_Define.f90:72``
+MIE_TAMU_CLOUDCOEFF = 1         # Version of a LUT indexed by effective radius
+
+# Cloud types (``src/Atmosphere/Cloud/CRTM_Cloud_Define.f90:150-155``)
+WATER_CLOUD, ICE_CLOUD, RAIN_CLOUD, SNOW_CLOUD, GRAUPEL_CLOUD, HAIL_CLOUD = 1, 2, 3, 4, 5, 6
+
+
+@dataclasses.dataclass
+class CloudCoeff:
+    """Cloud optical property LUT (``CloudCoeff_Define.f90:87-131``).
+
+    Arrays are shaped in the reference's Fortran index order (first index
+    fastest on disk): ``ke_l_mw[f, r, t]``, ``pcoeff_l_mw[f, r, t, l, m]`` with
+    l = 0..n_legendre_terms, ``ke_s_mw[f, r, d]``, ``ke_ir[f, r, d]`` with
+    d = 1..n_mw_densities+1 and ``pcoeff_ir[f, r, d, l, m]`` with
+    l = 1..n_legendre_terms.
+    """
+    frequency_mw: np.ndarray      # GHz
+    frequency_ir: np.ndarray      # cm^-1
+    reff_mw: np.ndarray           # microns
+    reff_ir: np.ndarray
+    temperature: np.ndarray       # K
+    density_mw: np.ndarray
+    ke_l_mw: np.ndarray
+    w_l_mw: np.ndarray
+    g_l_mw: np.ndarray
+    pcoeff_l_mw: np.ndarray
+    ke_s_mw: np.ndarray
+    w_s_mw: np.ndarray
+    g_s_mw: np.ndarray
+    pcoeff_s_mw: np.ndarray
+    ke_ir: np.ndarray
+    w_ir: np.ndarray
+    g_ir: np.ndarray
+    pcoeff_ir: np.ndarray
+    version: int = MIE_TAMU_CLOUDCOEFF
+
+    @property
+    def n_legendre_terms(self) -> int:
+        return int(self.pcoeff_l_mw.shape[3]) - 1
+
+    @property
+    def n_phase_elements(self) -> int:
+        return int(self.pcoeff_l_mw.shape[4])
+
+
+def write_cloudcoeff(path: str, cc: CloudCoeff, byteorder: str = "<") -> None:
+    """Record order of ``CloudCoeff_Binary_IO.f90:597-660`` (the kb arrays are
+    not part of the binary file)."""
+    with open(path, "wb") as f:
+        w = RecordWriter(f, byteorder)
+        w.record(np.array([CLOUDCOEFF_RELEASE, cc.version], np.int32))
+        w.record(np.array([cc.frequency_mw.size, cc.reff_mw.size, cc.frequency_ir.size,
+                           cc.reff_ir.size, cc.temperature.size, cc.density_mw.size,
+                           cc.n_legendre_terms, cc.n_phase_elements], np.int32))
+        w.record(cc.frequency_mw, cc.frequency_ir, cc.reff_mw, cc.reff_ir, cc.temperature,
+                 cc.density_mw)
+        w.record(cc.ke_l_mw, cc.w_l_mw, cc.g_l_mw, cc.pcoeff_l_mw)
+        w.record(cc.ke_s_mw, cc.w_s_mw, cc.g_s_mw, cc.pcoeff_s_mw)
+        w.record(cc.ke_ir, cc.w_ir, cc.g_ir, cc.pcoeff_ir)
+
+
+def read_cloudcoeff(path: str) -> CloudCoeff:
+    with open(path, "rb") as f:
+        r = RecordReader(f)
+        rel, ver = r.split(r.record(), [("i4", (2,))])[0]
+        if rel != CLOUDCOEFF_RELEASE:
+            raise IOError(f"CloudCoeff release {rel} not supported")
+        dims = r.split(r.record(), [("i4", (8,))])[0]
+        nfm, nrm, nfi, nri, nt, nd, nl, nph = (int(x) for x in dims)
+        axes = r.split(r.record(), [("f8", (nfm,)), ("f8", (nfi,)), ("f8", (nrm,)),
+                                    ("f8", (nri,)), ("f8", (nt,)), ("f8", (nd,))])
+
+        def block(shape3, pshape):
+            n3 = int(np.prod(shape3))
+            parts = r.split(r.record(), [("f8", (n3,))] * 3 + [("f8", (int(np.prod(pshape)),))])
+            return [p.reshape(shape3, order="F") for p in parts[:3]] + [parts[3].reshape(pshape, order="F")]
+        lmw = block((nfm, nrm, nt), (nfm, nrm, nt, nl + 1, nph))
+        smw = block((nfm, nrm, nd), (nfm, nrm, nd, nl + 1, nph))
+        ir = block((nfi, nri, nd + 1), (nfi, nri, nd + 1, nl, nph))
+    return CloudCoeff(*axes, *lmw, *smw, *ir, version=int(ver))

@@ -395,3 +395,117 @@ def clear_sky_workload(sensor_id: str, n_profiles: int, n_layers, seed: int):
                                       else (co.H2O_ID, co.O3_ID), seed)
     opt = OptionsBatch(emissivity=emissivity_for(stype, n_profiles, L, seed + 1))
     return atm, sfc, geo, opt
+
+
+# ---------------------------------------------------------------------------
+# Clouds: synthetic CloudCoeff LUT and cloudy profiles
+# ---------------------------------------------------------------------------
+
+CLOUD_N_LEGENDRE = 38       # >= 21 + 16 + 1: the 16-stream offset plus 16 terms fit
+
+
+def _phase_terms(g: np.ndarray, n_leg: int) -> np.ndarray:
+    """Legendre terms 0.5*g**l of a Henyey-Greenstein phase function in the
+    reference's normalisation (term 0 is 1/2), shape g.shape + (n_leg+1,)."""
+    return 0.5 * g[..., None] ** np.arange(n_leg + 1)
+
+
+def generate_cloudcoeff(seed: int = 7) -> co.CloudCoeff:
+    """Smooth synthetic cloud optical properties on the reference's LUT axes:
+    8 MW frequencies x 30 radii x 6 temperatures (liquid) or 3 densities
+    (frozen), 20 IR wavenumbers x 30 radii x 4 densities, 38 Legendre terms."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    f_mw = np.array([10.0, 19.0, 23.8, 31.4, 50.3, 89.0, 150.0, 190.0])
+    r_mw = np.geomspace(5.0, 1000.0, 30)
+    temp = np.array([233.0, 248.0, 263.0, 278.0, 293.0, 308.0])
+    dens = np.array([100.0, 400.0, 900.0])
+    f_ir = np.linspace(500.0, 3000.0, 20)
+    r_ir = np.geomspace(2.0, 1000.0, 30)
+    nl = CLOUD_N_LEGENDRE
+    jit = lambda shape: 1.0 + 0.02 * rng.standard_normal(shape)   # noqa: E731
+    # microwave liquid: size parameter x = 2 pi r f / c
+    x = 2.0 * np.pi * r_mw[None, :, None] * f_mw[:, None, None] / 3.0e5
+    tfac = 1.0 + 0.004 * (300.0 - temp[None, None, :])
+    ke_l = 0.08 * (f_mw[:, None, None] / 10.0) ** 1.8 * (1.0 + 3.0 * x ** 2 / (1.0 + x ** 2)) * tfac
+    w_l = np.clip(0.9 * x ** 2 / (1.0 + x ** 2) * np.ones_like(tfac), 0.0, 0.99)
+    g_l = 0.8 * x / (1.0 + x) * np.ones_like(tfac)
+    ke_l, w_l = ke_l * jit(ke_l.shape), w_l * jit(w_l.shape).clip(0.0, 1.0)
+    pc_l = _phase_terms(g_l, nl)[..., None]
+    # microwave frozen: density axis
+    xs = 2.0 * np.pi * r_mw[None, :, None] * f_mw[:, None, None] / 3.0e5 * np.ones((1, 1, dens.size))
+    dfac = 1.0 + 0.2 * np.arange(dens.size)[None, None, :]
+    ke_s = 0.03 * (f_mw[:, None, None] / 10.0) ** 1.5 * (1.0 + 2.0 * xs ** 2 / (1.0 + xs ** 2)) * dfac
+    w_s = np.clip(0.97 * xs ** 2 / (1.0 + xs ** 2), 0.0, 0.99)
+    g_s = 0.75 * xs / (1.0 + xs)
+    ke_s = ke_s * jit(ke_s.shape)
+    pc_s = _phase_terms(g_s, nl)[..., None]
+    # infrared: density axis 1..4 (1 liquid, 2-4 frozen)
+    xi = 2.0 * np.pi * r_ir[None, :, None] * f_ir[:, None, None] / 1.0e4 * np.ones((1, 1, dens.size + 1))
+    q = 2.0 - 1.5 / (1.0 + xi)
+    ke_ir = 1.5e3 / r_ir[None, :, None] * q * (1.0 + 0.1 * np.arange(dens.size + 1)[None, None, :])
+    band = 0.1 * np.sin(f_ir / 300.0)[:, None, None]
+    w_ir = np.clip(0.5 + 0.45 * xi / (1.0 + xi) - band, 0.05, 0.999)
+    g_ir = 0.85 * xi / (1.0 + xi)
+    ke_ir = ke_ir * jit(ke_ir.shape)
+    pc_ir = _phase_terms(g_ir, nl)[..., 1:, None]
+    return co.CloudCoeff(f_mw, f_ir, r_mw, r_ir, temp, dens, ke_l, w_l, g_l, pc_l, ke_s, w_s, g_s,
+                         pc_s, ke_ir, w_ir, g_ir, pc_ir)
+
+
+def write_cloud_files(coeff_dir: str) -> str:
+    """Write ``CloudCoeff.bin`` (the reference's default file name) if missing."""
+    os.makedirs(coeff_dir, exist_ok=True)
+    path = os.path.join(coeff_dir, "CloudCoeff.bin")
+    if not os.path.exists(path):
+        co.write_cloudcoeff(path + ".tmp", generate_cloudcoeff())
+        os.replace(path + ".tmp", path)
+    return path
+
+
+# effective radius ranges (microns) by cloud type
+REFF_RANGE = {co.WATER_CLOUD: (5.0, 20.0), co.ICE_CLOUD: (20.0, 200.0), co.RAIN_CLOUD: (100.0, 1000.0),
+              co.SNOW_CLOUD: (100.0, 1000.0), co.GRAUPEL_CLOUD: (200.0, 1000.0),
+              co.HAIL_CLOUD: (300.0, 1000.0)}
+
+
+def add_clouds(atm: AtmosphereBatch, cloud_types: Sequence[int], seed: int, max_fraction: float = 0.3,
+               wc_scale: float = 1.0) -> AtmosphereBatch:
+    """Give every profile the clouds ``cloud_types``: each active in a random
+    0-``max_fraction`` of the layers, water content lognormal with geometric
+    mean 0.05 g/m^2 x ``wc_scale`` and sigma_ln 1.2 (stored in kg/m^2, the
+    reference's unit), effective radius uniform in the type's range.
+    Cloud_Fraction stays 0, so the reference treats the profile as one
+    cloudy column (coverage flag CLEAR, no clear/cloudy mixing)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    P, K = atm.n_profiles, atm.max_layers
+    NC = len(cloud_types)
+    wc = np.zeros((P, NC, K))
+    reff = np.zeros((P, NC, K))
+    for m in range(P):
+        n = int(atm.n_layers[m])
+        for c, t in enumerate(cloud_types):
+            frac = rng.uniform(0.0, max_fraction)
+            mask = rng.uniform(size=n) < frac
+            wc[m, c, :n][mask] = 5.0e-5 * wc_scale * np.exp(1.2 * rng.standard_normal(mask.sum()))
+            lo, hi = REFF_RANGE[t]
+            reff[m, c, :n][mask] = rng.uniform(lo, hi, mask.sum())
+    atm.n_clouds = np.full(P, NC, np.int32)
+    atm.cloud_type = np.tile(np.asarray(cloud_types, np.int32), (P, 1))
+    atm.cloud_water_content = wc
+    atm.cloud_effective_radius = reff
+    atm.cloud_fraction = np.zeros((P, K))
+    return atm
+
+
+def cloudy_workload(sensor_id: str, n_profiles: int, n_layers, seed: int,
+                    cloud_types=(co.WATER_CLOUD, co.ICE_CLOUD, co.RAIN_CLOUD, co.SNOW_CLOUD,
+                                 co.GRAUPEL_CLOUD), wc_scale: float = 1.0, n_streams=None):
+    """A cloudy run of one synthetic sensor (``n_streams``: None for the
+    reference's stream rule, or a per-profile array for Options%Use_N_Streams)."""
+    atm, sfc, geo, opt = clear_sky_workload(sensor_id, n_profiles, n_layers, seed)
+    add_clouds(atm, cloud_types, seed + 17, wc_scale=wc_scale)
+    if n_streams is not None:
+        ns = np.broadcast_to(np.asarray(n_streams, np.int32), (n_profiles,)).copy()
+        opt.use_n_streams = ns > 0
+        opt.n_streams = ns
+    return atm, sfc, geo, opt

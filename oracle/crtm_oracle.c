@@ -55,7 +55,7 @@ struct or_handle_s {
   int* n_pred; /* [L][J] */
   int* pos;    /* [L][J], 1-based */
   float* c;
-  double *wn, *c1, *c2, *b1, *b2, *cbr, *solar;
+  double *wn, *c1, *c2, *b1, *b2, *cbr, *solar, *freq;
 };
 
 /* ---------------- Fortran sequential record reader ------------------------ */
@@ -227,7 +227,8 @@ static int load_spccoeff(or_handle* h, const char* path) {
   {
     double* tmp = (double*)malloc(sizeof(double) * 8 * L);
     copy_f64(tmp, d + (size_t)L * 20, (size_t)8 * L, r.swap);
-    h->wn = (double*)malloc(sizeof(double) * 7 * L);
+    h->wn = (double*)malloc(sizeof(double) * 8 * L);
+    h->freq = h->wn + 7 * L; memcpy(h->freq, tmp, sizeof(double) * L);
     memcpy(h->wn, tmp + 1 * L, sizeof(double) * L);
     h->c1 = h->wn + L; memcpy(h->c1, tmp + 2 * L, sizeof(double) * L);
     h->c2 = h->wn + 2 * L; memcpy(h->c2, tmp + 3 * L, sizeof(double) * L);
@@ -1062,3 +1063,6 @@ int or_profile_state(const or_handle* h, const or_batch* b, int m, double* T, do
   free(s);
   return 0;
 }
+
+/* ---- scattering (clouds, ADA) ------------------------------------------- */
+#include "oracle_scatter.inc"

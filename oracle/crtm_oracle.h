@@ -83,6 +83,33 @@ int or_tangent_fd(const or_handle* hd, const or_batch* b, const double* temperat
                   const double* absorber_tl, const double* water_temperature_tl, double step,
                   double* bt_tl, int n_threads);
 
+/* ---- clouds and the ADA solver ------------------------------------------- */
+typedef struct or_cloud_s or_cloud;
+
+/* Load a CloudCoeff binary file (Release 3). */
+or_cloud* or_cloud_init(const char* path);
+void or_cloud_destroy(or_cloud* c);
+
+typedef struct {
+  int max_clouds;                  /* NC: stride of the cloud arrays            */
+  const int* n_clouds;             /* [P] clouds used by each profile (<= NC)   */
+  const int* cloud_type;           /* [P][NC] WATER=1 ICE=2 RAIN=3 SNOW=4 GRAUPEL=5 HAIL=6 */
+  const double* water_content;     /* [P][NC][max_layers] kg/m^2                */
+  const double* effective_radius;  /* [P][NC][max_layers] microns               */
+  const int* n_streams;            /* [P] Options%n_Streams, 0 = stream rule; may be NULL */
+} or_clouds;
+
+/* Forward with clouds: ADA for profiles with clouds, Emission otherwise. */
+int or_forward_scatter(const or_handle* h, const or_cloud* cc, const or_batch* b, const or_clouds* cl,
+                       double* radiance, double* bt, int n_threads);
+
+/* Test hooks: one ADA layer (row-major nZ x nZ blocks) and the angle/phase setup. */
+int or_amom_layer(int nS, int nZ, double w, double tau, const double* mu, const double* wt,
+                  const double* ff, const double* bb, double B, double* trans, double* refl,
+                  double* src);
+int or_phase_setup(int nleg, double mu_sensor, const double* pc, double* mu, double* wt, double* ff,
+                   double* bb, int* nZ_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -32,9 +32,14 @@ class OrBatch(ct.Structure):
                 ("surface_altitude", _dp), ("emissivity", _dp)]
 
 
+class OrClouds(ct.Structure):
+    _fields_ = [("max_clouds", ct.c_int), ("n_clouds", _ip), ("cloud_type", _ip),
+                ("water_content", _dp), ("effective_radius", _dp), ("n_streams", _ip)]
+
+
 def build(force: bool = False) -> str:
-    src = os.path.join(HERE, "crtm_oracle.c")
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in ("crtm_oracle.c", "crtm_oracle.h", "oracle_scatter.inc")]
+    if force or not os.path.exists(LIB) or any(os.path.getmtime(LIB) < os.path.getmtime(f) for f in srcs):
         subprocess.run(["make", "-C", HERE, "-B", "liboracle.so"], check=True,
                        stdout=subprocess.DEVNULL)
     return LIB
@@ -60,6 +65,14 @@ def lib():
                                  ct.c_int]
         L.or_tangent_fd.argtypes = [ct.c_void_p, ct.POINTER(OrBatch), _dp, _dp, _dp, ct.c_double,
                                     _dp, ct.c_int]
+        L.or_cloud_init.restype = ct.c_void_p
+        L.or_cloud_init.argtypes = [ct.c_char_p]
+        L.or_cloud_destroy.argtypes = [ct.c_void_p]
+        L.or_forward_scatter.argtypes = [ct.c_void_p, ct.c_void_p, ct.POINTER(OrBatch),
+                                         ct.POINTER(OrClouds), _dp, _dp, ct.c_int]
+        L.or_amom_layer.argtypes = [ct.c_int, ct.c_int, ct.c_double, ct.c_double, _dp, _dp, _dp, _dp,
+                                    ct.c_double, _dp, _dp, _dp]
+        L.or_phase_setup.argtypes = [ct.c_int, ct.c_double, _dp, _dp, _dp, _dp, _dp, _ip]
         _lib = L
     return _lib
 
@@ -147,6 +160,37 @@ class Oracle:
         if st:
             raise RuntimeError(lib().or_last_error().decode())
         return dict(radiance=rad, bt=bt, temperature_ad=ta, absorber_ad=aa, water_temperature_ad=wa)
+
+    def forward_scatter(self, atm, sfc, geo, opt, cloudcoeff_path: str, n_threads: int = 1):
+        """Forward with clouds (ADA); profiles without clouds take the Emission solver."""
+        L = lib()
+        ch = L.or_cloud_init(cloudcoeff_path.encode())
+        if not ch:
+            raise IOError(L.or_last_error().decode())
+        try:
+            P, nL = atm.n_profiles, self.n_channels
+            b, keep = self._batch(atm, sfc, geo, opt)
+            NC = int(atm.cloud_type.shape[1]) if atm.cloud_type is not None else 0
+            c = OrClouds()
+            c.max_clouds = NC
+            arrs = [np.ascontiguousarray(atm.n_clouds if atm.n_clouds is not None else np.zeros(P), np.int32),
+                    np.ascontiguousarray(atm.cloud_type if NC else np.zeros((P, 1)), np.int32),
+                    np.ascontiguousarray(atm.cloud_water_content if NC else np.zeros((P, 1, atm.max_layers))),
+                    np.ascontiguousarray(atm.cloud_effective_radius if NC else np.zeros((P, 1, atm.max_layers)))]
+            keep += arrs
+            c.n_clouds, c.cloud_type = _p(arrs[0], _ip), _p(arrs[1], _ip)
+            c.water_content, c.effective_radius = _p(arrs[2]), _p(arrs[3])
+            if opt.n_streams is not None:
+                ns = np.ascontiguousarray(np.where(opt.use_n_streams, opt.n_streams, 0), np.int32)
+                keep.append(ns)
+                c.n_streams = _p(ns, _ip)
+            rad, bt = np.zeros((P, nL)), np.zeros((P, nL))
+            st = L.or_forward_scatter(self.h, ch, ct.byref(b), ct.byref(c), _p(rad), _p(bt), n_threads)
+            if st:
+                raise RuntimeError(L.or_last_error().decode())
+            return rad, bt
+        finally:
+            L.or_cloud_destroy(ch)
 
     def tangent_fd(self, atm, sfc, geo, opt, t_tl, a_tl, ts_tl, step=1e-4, n_threads: int = 1):
         P, L = atm.n_profiles, self.n_channels

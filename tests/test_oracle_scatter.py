@@ -1,0 +1,159 @@
+"""The oracle's cloud / ADA path (CPU).
+
+The reference publishes no outputs for this path either.  These tests pin the
+oracle by an independent eigensolver, by known answers and by limits:
+
+* one ADA layer (MOM, ADA_Module.f90:262-354) against the same formulas
+  evaluated with numpy's general eigensolver (the reference uses a general
+  real eigensolver, ASYMTX);
+* Kirchhoff: an isothermal atmosphere over a black surface at the same
+  temperature gives BT = T for any cloud, any scattering and any stream count;
+* clouds below the water-content threshold: the ADA path with no scattering
+  layer equals the Emission solver;
+* stream-count convergence.
+"""
+import ctypes as ct
+
+import numpy as np
+import pytest
+
+from crtmv3_gb300 import coefficients as co, synthetic as sy
+
+_dp = ct.POINTER(ct.c_double)
+
+
+def _p(a):
+    return a.ctypes.data_as(_dp)
+
+
+@pytest.fixture(scope="module")
+def cloud_path(coeff_dir):
+    return sy.write_cloud_files(coeff_dir)
+
+
+def _setup(nleg, mu_sensor, g):
+    from oracle.pyoracle import lib
+    pc = 0.5 * g ** np.arange(nleg + 1)
+    n = 20
+    mu, wt = np.zeros(n), np.zeros(n)
+    ff, bb = np.zeros(n * n), np.zeros(n * n)
+    nz = ct.c_int(0)
+    lib().or_phase_setup(nleg, mu_sensor, _p(pc), _p(mu), _p(wt), _p(ff), _p(bb), ct.byref(nz))
+    nZ = nz.value
+    return mu[:nZ].copy(), wt[:nZ].copy(), ff[:nZ * nZ].reshape(nZ, nZ), bb[:nZ * nZ].reshape(nZ, nZ)
+
+
+def _mom_numpy(mu, wt, ff, bb, w, tau):
+    """MOM (ADA_Module.f90:262-354) with numpy's general eigensolver."""
+    s = min(w, 0.999999)
+    c = s / mu
+    PM = c[:, None] * bb * wt[None, :]
+    PP = c[:, None] * ff * wt[None, :] - np.diag(1.0 / mu)
+    PPM, PPP = PP - PM, PP + PM
+    HH = PPM @ PPP
+    ev, E = np.linalg.eig(HH)
+    assert np.abs(ev.imag).max() < 1e-9 * np.abs(ev).max()
+    ev, E = ev.real, E.real
+    lam = np.where(ev > 0, np.sqrt(np.maximum(ev, 0)), 0.0)
+    EF = np.linalg.inv(PPM) @ (E * lam[None, :])
+    Gp, Gm = (E + EF) / 2, (E - EF) / 2
+    ex = np.exp(-lam * tau)
+    A1, A4 = Gp * ex[None, :], Gm * ex[None, :]
+    A2 = np.linalg.inv(Gm) @ A1
+    A3, A5, A6 = Gp @ A2, A1 @ A2, A4 @ A2
+    iGA = np.linalg.inv(Gm - A5)
+    return (A4 - A3) @ iGA, (Gp - A6) @ iGA
+
+
+@pytest.mark.parametrize("nleg,mu_sensor", [(2, 0.83), (4, 0.6), (6, 0.97), (8, 0.5), (16, 0.71)])
+@pytest.mark.parametrize("w,tau,g", [(0.5, 0.3, 0.6), (0.95, 4.0, 0.85), (0.2, 0.01, 0.3)])
+def test_mom_layer_matches_general_eigensolver(nleg, mu_sensor, w, tau, g):
+    from oracle.pyoracle import lib
+    mu, wt, ff, bb = _setup(nleg, mu_sensor, g)
+    nZ = mu.size
+    nS = (nleg + 2) // 2
+    T, R, S = np.zeros(nZ * nZ), np.zeros(nZ * nZ), np.zeros(nZ)
+    rc = lib().or_amom_layer(nS, nZ, w, tau, _p(mu), _p(wt), _p(np.ascontiguousarray(ff)),
+                             _p(np.ascontiguousarray(bb)), 1.0, _p(T), _p(R), _p(S))
+    assert rc == 0
+    Tn, Rn = _mom_numpy(mu, wt, ff, bb, w, tau)
+    assert np.abs(T.reshape(nZ, nZ) - Tn).max() < 1e-11
+    assert np.abs(R.reshape(nZ, nZ) - Rn).max() < 1e-11
+
+
+def test_normalised_phase_conserves_energy():
+    """After Normalize_Phase the scattering out of each quadrature stream sums to 1."""
+    for nleg in (2, 4, 6, 8, 16):
+        mu, wt, ff, bb = _setup(nleg, 0.77, 0.7)
+        nS = (nleg + 2) // 2
+        rows = ((ff + bb)[:nS, :nS] * wt[None, :nS]).sum(axis=1)
+        assert np.abs(rows - 1.0).max() < 1e-12
+        assert np.allclose(ff, ff.T) and np.allclose(bb, bb.T)
+
+
+def _isothermal(atm, sfc, opt, T=265.0):
+    for m in range(atm.n_profiles):
+        atm.temperature[m, :atm.n_layers[m]] = T
+    sfc.water_temperature[:] = T
+    opt.emissivity[:] = 1.0
+
+
+def _isothermal_sensor(coeff_dir, tmp_path, sensor, T):
+    """A copy of ``sensor`` whose cosmic background is B(T): with it the scene is
+    an isothermal enclosure."""
+    import shutil
+    sc = co.read_spccoeff(f"{coeff_dir}/{sensor}.SpcCoeff.bin")
+    te = sc.band_c1 + sc.band_c2 * T
+    sc.cosmic_background_radiance = sc.planck_c1 / (np.exp(sc.planck_c2 / te) - 1.0)
+    co.write_spccoeff(str(tmp_path / f"{sensor}.SpcCoeff.bin"), sc)
+    shutil.copy(f"{coeff_dir}/{sensor}.TauCoeff.bin", tmp_path / f"{sensor}.TauCoeff.bin")
+    return str(tmp_path)
+
+
+@pytest.mark.parametrize("sensor,nl", [("mwsynth_c16", 100), ("irsynth_c616", 101)])
+@pytest.mark.parametrize("n_streams", [None, 8, 16])
+def test_kirchhoff_isothermal_enclosure(coeff_dir, cloud_path, tmp_path, sensor, nl, n_streams):
+    """Isothermal atmosphere, black surface and a cosmic background all at the
+    same temperature: BT = T for any cloud, scattering and stream count."""
+    from oracle.pyoracle import Oracle
+    d = _isothermal_sensor(coeff_dir, tmp_path, sensor, 265.0)
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 3, nl, 41, wc_scale=300.0, n_streams=n_streams)
+    _isothermal(atm, sfc, opt)
+    _, bt = Oracle(d, sensor).forward_scatter(atm, sfc, geo, opt, cloud_path)
+    assert np.abs(bt - 265.0).max() < 1e-8
+
+
+@pytest.mark.parametrize("sensor,nl", [("mwsynth_c16", 100), ("irsynth_c616", 101)])
+def test_sub_threshold_clouds_equal_emission(coeff_dir, cloud_path, sensor, nl):
+    """Water content below WATER_CONTENT_THRESHOLD: ADA runs (the profile has
+    clouds) but no layer scatters, and the result equals the Emission solver."""
+    from oracle.pyoracle import Oracle
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 3, nl, 42)
+    atm.cloud_water_content[:] = np.where(atm.cloud_water_content > 0, 5e-7, 0.0)
+    o = Oracle(coeff_dir, sensor)
+    _, bt = o.forward_scatter(atm, sfc, geo, opt, cloud_path)
+    _, bt0 = o.forward(atm, sfc, geo, opt)
+    assert np.abs(bt - bt0).max() < 1e-9
+
+
+def test_clear_profiles_in_a_cloudy_batch(coeff_dir, cloud_path):
+    from oracle.pyoracle import Oracle
+    sensor = "mwsynth_c16"
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 4, 100, 43, wc_scale=100.0)
+    atm.n_clouds[1] = 0
+    o = Oracle(coeff_dir, sensor)
+    _, bt = o.forward_scatter(atm, sfc, geo, opt, cloud_path)
+    _, bt0 = o.forward(atm, sfc, geo, opt)
+    assert np.array_equal(bt[1], bt0[1])
+    assert np.abs(bt[0] - bt0[0]).max() > 0.1
+
+
+def test_stream_count_convergence(coeff_dir, cloud_path):
+    from oracle.pyoracle import Oracle
+    sensor = "mwsynth_c16"
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 3, 100, 44, wc_scale=100.0, n_streams=16)
+    o = Oracle(coeff_dir, sensor)
+    _, b16 = o.forward_scatter(atm, sfc, geo, opt, cloud_path)
+    opt.n_streams[:] = 8
+    _, b8 = o.forward_scatter(atm, sfc, geo, opt, cloud_path)
+    assert np.abs(b16 - b8).max() < 1.0
