@@ -49,7 +49,10 @@ class CBatch(ct.Structure):
                 ("land_temperature", ct.c_void_p), ("water_temperature", ct.c_void_p),
                 ("snow_temperature", ct.c_void_p), ("ice_temperature", ct.c_void_p),
                 ("sensor_zenith_angle", ct.c_void_p), ("source_zenith_angle", ct.c_void_p),
-                ("surface_altitude", ct.c_void_p), ("emissivity", ct.c_void_p)]
+                ("surface_altitude", ct.c_void_p), ("emissivity", ct.c_void_p),
+                ("max_clouds", ct.c_int), ("n_clouds", ct.c_void_p), ("cloud_type", ct.c_void_p),
+                ("cloud_water_content", ct.c_void_p), ("cloud_effective_radius", ct.c_void_p),
+                ("n_streams", ct.c_void_p)]
 
 
 class CRTSolution(ct.Structure):
@@ -145,7 +148,7 @@ class CRTM:
     def launch_count(self) -> int:
         return int(library().crtm_gpu_launch_count(self.h))
 
-    STAGES = ("prep", "absorb_fwd", "column", "absorb_ad", "map_out", "adjoint_sum")
+    STAGES = ("prep", "absorb_fwd", "column", "absorb_ad", "map_out", "adjoint_sum", "scatter")
 
     def set_profiling(self, enable: bool) -> None:
         library().crtm_gpu_set_profiling(self.h, int(enable))
@@ -196,6 +199,15 @@ class CRTM:
         if opt is None or opt.emissivity is None:
             raise ValueError("Options.emissivity is required (Use_Emissivity path)")
         b.emissivity = c(opt.emissivity)
+        if atm.n_clouds is not None and atm.cloud_type is not None and atm.cloud_type.shape[1] > 0:
+            b.max_clouds = int(atm.cloud_type.shape[1])
+            b.n_clouds = c(atm.n_clouds, np.int32)
+            b.cloud_type = c(atm.cloud_type, np.int32)
+            b.cloud_water_content = c(atm.cloud_water_content)
+            b.cloud_effective_radius = c(atm.cloud_effective_radius)
+        if opt.n_streams is not None:
+            use = opt.use_n_streams if opt.use_n_streams is not None else np.ones(atm.n_profiles, bool)
+            b.n_streams = c(np.where(use, opt.n_streams, 0), np.int32)
         return b
 
     def _check(self, rc: int) -> None:
@@ -266,9 +278,13 @@ class CRTM:
         for f in ("level_pressure", "pressure", "temperature", "absorber", "land_coverage",
                   "water_coverage", "snow_coverage", "ice_coverage", "land_temperature",
                   "water_temperature", "snow_temperature", "ice_temperature",
-                  "sensor_zenith_angle", "source_zenith_angle", "surface_altitude", "emissivity"):
+                  "sensor_zenith_angle", "source_zenith_angle", "surface_altitude", "emissivity",
+                  "n_clouds", "cloud_type", "cloud_water_content", "cloud_effective_radius",
+                  "n_streams"):
             t = dev.get(f)
             setattr(b, f, None if t is None else t.data_ptr())
+        if dev.get("cloud_type") is not None:
+            b.max_clouds = int(dev["cloud_type"].shape[1])
         return b, keep
 
     def k_matrix_device(self, b: CBatch, out: dict, seed=None, sensor: int = 0, stream=None,

@@ -22,6 +22,7 @@
 
 #include "../../include/crtm_gpu.h"
 #include "odps_kernels.cuh"
+#include "scatter_kernels.cuh"
 
 using namespace crtm;
 
@@ -120,12 +121,12 @@ struct Sensor {
   int group = 0, K = 0, J = 0, Jm = 0, L = 0, Lp = 0, sensor_type = 0, h2o_idx = 0, NS = 0;
   std::vector<int> absorber_id;
   std::vector<double> ref_lev, ref_p, ref_t, ref_a, min_a, max_a;  // [Jm][K] for absorbers
-  std::vector<double> c1, c2, b1, b2, cbr;
+  std::vector<double> c1, c2, b1, b2, cbr, freq, wn;
   // device
   float* d_C = nullptr;          // [K][NS][Lp]
   unsigned* d_cmask = nullptr;   // [L]
   double* d_tab = nullptr;       // concatenated tables
-  double* d_spec = nullptr;      // c1,c2,b1,b2,cbr [5][L]
+  double* d_spec = nullptr;      // c1,c2,b1,b2,cbr,frequency,wavenumber [7][L]
   SensorTables tables{};
   RefSums refsums{};
   SpecView spec{};
@@ -231,7 +232,7 @@ bool load_sensor(const std::string& dir, const std::string& id, Sensor& s, std::
     for (int l = 0; l < L; l++) v[l] = sr.f64(d + base + 8 * ((size_t)f * L + l));
   };
   // fields after the integer/polangle block: Frequency(0) Wavenumber(1) C1(2) C2(3) B1(4) B2(5) CBR(6) Solar(7)
-  col(2, s.c1); col(3, s.c2); col(4, s.b1); col(5, s.b2); col(6, s.cbr);
+  col(0, s.freq); col(1, s.wn); col(2, s.c1); col(3, s.c2); col(4, s.b1); col(5, s.b2); col(6, s.cbr);
   s.h2o_idx = (s.absorber_id[s.Jm - 1] == 1) ? s.Jm - 1 : 0;
   // derived tables
   std::vector<double> lev_lnp(K + 1), lnp(K), pdp(K), z(K + 1);
@@ -266,7 +267,7 @@ bool load_sensor(const std::string& dir, const std::string& id, Sensor& s, std::
   }
   size_t o_tzr = put(tzr), o_tzpr = put(tzpr), o_gzr = put(gzr), o_gtr = put(gtr);
   std::vector<double> spec;
-  for (auto* v : {&s.c1, &s.c2, &s.b1, &s.b2, &s.cbr}) spec.insert(spec.end(), v->begin(), v->end());
+  for (auto* v : {&s.c1, &s.c2, &s.b1, &s.b2, &s.cbr, &s.freq, &s.wn}) spec.insert(spec.end(), v->begin(), v->end());
   cudaError_t ce;
   if ((ce = cudaMalloc(&s.d_C, Cd.size() * sizeof(float))) != cudaSuccess ||
       (ce = cudaMalloc(&s.d_cmask, cmask.size() * sizeof(unsigned))) != cudaSuccess ||
@@ -289,12 +290,59 @@ bool load_sensor(const std::string& dir, const std::string& id, Sensor& s, std::
   s.refsums.gazp_ref = s.d_tab + o_gzr; s.refsums.gatzp_ref = s.d_tab + o_gtr;
   s.spec.c1 = s.d_spec; s.spec.c2 = s.d_spec + L; s.spec.b1 = s.d_spec + 2 * L;
   s.spec.b2 = s.d_spec + 3 * L; s.spec.cbr = s.d_spec + 4 * L;
+  s.spec.freq = s.d_spec + 5 * L; s.spec.wn = s.d_spec + 6 * L;
   return true;
 }
 
 void free_sensor(Sensor& s) {
   cudaFree(s.d_C); cudaFree(s.d_cmask); cudaFree(s.d_tab); cudaFree(s.d_spec);
   s.d_C = nullptr; s.d_cmask = nullptr; s.d_tab = nullptr; s.d_spec = nullptr;
+}
+
+// CloudCoeff.bin (CloudCoeff_Binary_IO.f90:360-460): Release/Version, 8
+// dimensions, the axis vectors, then (ke, w, g, pcoeff) for the MW liquid,
+// MW solid and IR tables.  Only phase element 1 of pcoeff is kept; g is not
+// used by this path.
+bool load_cloudcoeff(const std::string& path, std::vector<double>& buf, int* dims, size_t* off,
+                     std::string& err) {
+  Records r;
+  if (!r.open(path, err)) return false;
+  const unsigned char* d;
+  size_t len;
+  auto bad = [&](const char* what) { err = path + ": " + what; return false; };
+  if (!r.next(d, len) || len != 8) return bad("corrupt Release/Version record");
+  if (r.i32(d) != 3) return bad("unsupported CloudCoeff release");
+  if (!r.next(d, len) || len != 32) return bad("corrupt dimension record");
+  int nd8[8];
+  for (int i = 0; i < 8; i++) nd8[i] = r.i32(d + 4 * i);
+  const int nfm = nd8[0], nrm = nd8[1], nfi = nd8[2], nri = nd8[3], nt = nd8[4], nd = nd8[5],
+            nleg = nd8[6], nph = nd8[7];
+  if (nfm < 4 || nrm < 4 || nfi < 4 || nri < 4 || nt < 4 || nd < 1 || nleg < 1 || nleg > 64 || nph < 1)
+    return bad("dimensions out of range");
+  buf.clear();
+  auto take = [&](const unsigned char* src, size_t n) {
+    size_t at = buf.size();
+    for (size_t i = 0; i < n; i++) buf.push_back(r.f64(src + 8 * i));
+    return at;
+  };
+  const size_t na = (size_t)nfm + nfi + nrm + nri + nt + nd;
+  if (!r.next(d, len) || len != 8 * na) return bad("corrupt axis record");
+  off[0] = take(d, nfm);                                   // frequency MW
+  off[1] = take(d + 8 * nfm, nfi);                         // frequency IR
+  off[2] = take(d + 8 * ((size_t)nfm + nfi), nrm);         // radius MW
+  off[3] = take(d + 8 * ((size_t)nfm + nfi + nrm), nri);   // radius IR
+  off[4] = take(d + 8 * ((size_t)nfm + nfi + nrm + nri), nt);   // temperature
+  const size_t n3[3] = {(size_t)nfm * nrm * nt, (size_t)nfm * nrm * nd, (size_t)nfi * nri * (nd + 1)};
+  const size_t nl[3] = {(size_t)nleg + 1, (size_t)nleg + 1, (size_t)nleg};
+  for (int bk = 0; bk < 3; bk++) {
+    const size_t np = n3[bk] * nl[bk] * nph;
+    if (!r.next(d, len) || len != 8 * (3 * n3[bk] + np)) return bad("corrupt LUT record");
+    off[5 + 3 * bk] = take(d, n3[bk]);                          // ke
+    off[6 + 3 * bk] = take(d + 8 * n3[bk], n3[bk]);             // w
+    off[7 + 3 * bk] = take(d + 8 * 3 * n3[bk], n3[bk] * nl[bk]); // pcoeff, phase element 1
+  }
+  dims[0] = nfm; dims[1] = nrm; dims[2] = nt; dims[3] = nd; dims[4] = nfi; dims[5] = nri; dims[6] = nleg;
+  return true;
 }
 
 // Grow-only device buffer
@@ -326,6 +374,11 @@ struct crtm_gpu_context {
   DevBuf ws;        // chunk workspace
   DevBuf io_in, io_out;  // device copies for the host entry points
   DevBuf small;     // idx maps
+  // cloud LUT (CloudCoeff.bin), when present
+  bool has_clouds = false;
+  double* d_cloud = nullptr;
+  CloudLut lut{};
+  int* d_error = nullptr;   // first failure code of the scattering kernel
   cudaStream_t copy_stream = nullptr;   // device-to-host copies of finished chunks
   std::vector<cudaEvent_t> chunk_events;
   // stage profiling
@@ -437,7 +490,8 @@ size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w
   const size_t nga = ((nn + ad_profiles<G, R>() - 1) / ad_profiles<G, R>()) * AD_WARPS;
   PrepView<R> pv;
   pv.Xg = (R*)carve(ngf * npf * K * NS * sizeof(R));
-  pv.Dg = mode ? (R*)carve(nga * npa * K * NX * sizeof(R)) : nullptr;
+  const bool adj = mode == 1 || mode == 2;
+  pv.Dg = adj ? (R*)carve(nga * npa * K * NX * sizeof(R)) : nullptr;
   pv.band_i0 = (int*)carve(nn * K * sizeof(int));
   pv.band_n = (int*)carve(nn * K * sizeof(int));
   pv.band_w = (double*)carve(nn * K * MAX_BAND * sizeof(double));
@@ -451,11 +505,12 @@ size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w
   pv.ub_w = (double*)carve(nn * Kmax * MAX_UBAND * sizeof(double));
   pv.scal = (double*)carve(nn * 4 * sizeof(double));
   pv.status = (int*)carve(nn * sizeof(int));
-  pv.K = K; pv.Kmax = Kmax; pv.npf = npf; pv.npa = mode ? npa : 0;
+  pv.K = K; pv.Kmax = Kmax; pv.npf = npf; pv.npa = adj ? npa : 0;
   Work<R> wk{};
   wk.pv = pv;
   wk.OD = (R*)carve(nn * K * L * sizeof(R));
-  if (mode) {
+  if (mode == 3) wk.TAU = (R*)carve(nn * Kmax * L * sizeof(R));
+  if (adj) {
     wk.TAU = (R*)carve(nn * Kmax * L * sizeof(R));
     wk.DTOP = (R*)carve(nn * Kmax * L * sizeof(R));
     wk.PT = (R*)carve(nn * Kmax * L * sizeof(R));
@@ -635,7 +690,24 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       column_kernel<R><<<gc, 128, col_smem, st>>>(ca);
       CK_LAUNCH(h);
     }
-    if (mode == 0) {
+    if (mode == 3) {   // cloudy forward: ADA over the gas layer optical depths
+      ScatterArgs<R> sa{};
+      sa.K = K; sa.L = L; sa.Kmax = Kmax; sa.p_begin = p0; sa.n_chunk = n;
+      sa.microwave = s.sensor_type == 1;
+      sa.b = bv; sa.sp = s.spec; sa.pv = w.pv; sa.lut = h->lut;
+      sa.max_clouds = b->max_clouds; sa.n_clouds = b->n_clouds; sa.cloud_type = b->cloud_type;
+      sa.wc = b->cloud_water_content; sa.reff = b->cloud_effective_radius; sa.n_streams = b->n_streams;
+      sa.TAU = w.TAU; sa.radiance = rts->radiance; sa.bt = rts->brightness_temperature;
+      sa.status = rts->status; sa.error = h->d_error;
+      StageScope sc(h, 6, st);
+      dim3 gs((L + SCATTER_THREADS - 1) / SCATTER_THREADS, n);
+      if (b->n_streams)
+        scatter_kernel<SC_NZ_MAX, R><<<gs, SCATTER_THREADS, 0, st>>>(sa);
+      else
+        scatter_kernel<5, R><<<gs, SCATTER_THREADS, 0, st>>>(sa);
+      CK_LAUNCH(h);
+    }
+    if (mode == 0 || mode == 3) {
       if (hc && hc->n) {
         if (int rc = copy_chunk(h, hc, p0, n, st)) return rc;
       }
@@ -707,6 +779,14 @@ int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, c
   if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
   const Sensor& s = h->sensors[sensor];
   const bool fp64 = h->precision == CRTM_GPU_FP64;
+  if (b->max_clouds > 0) {
+    if (mode != 0) return fail(h, "the K-matrix and adjoint are not available for batches with clouds");
+    if (!h->has_clouds) return fail(h, "batch has clouds but no CloudCoeff.bin was loaded at init");
+    if (!b->n_clouds || !b->cloud_type || !b->cloud_water_content || !b->cloud_effective_radius)
+      return fail(h, "cloud arrays missing for max_clouds = %d", b->max_clouds);
+    if (cudaMemsetAsync(h->d_error, 0, sizeof(int), st) != cudaSuccess) return fail(h, "error flag reset failed");
+    mode = 3;
+  }
   switch (s.group) {
     case 1: return fp64 ? run_pipeline<1, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed)
                         : run_pipeline<1, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed);
@@ -739,6 +819,18 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
       {b->land_temperature, PD}, {b->water_temperature, PD}, {b->snow_temperature, PD},
       {b->ice_temperature, PD}, {b->sensor_zenith_angle, PD}, {b->surface_altitude, PD},
       {b->emissivity, (size_t)P * L * 8}, {seed, (size_t)P * L * 8}, {b->n_layers, (size_t)P * 4}};
+  const int NC = b->max_clouds > 0 ? b->max_clouds : 0;
+  if (NC > 0) {
+    if (!b->n_clouds || !b->cloud_type || !b->cloud_water_content || !b->cloud_effective_radius)
+      return fail(h, "cloud arrays missing for max_clouds = %d", NC);
+    for (int m = 0; m < P; m++)
+      if (b->n_clouds[m] < 0 || b->n_clouds[m] > NC)
+        return fail(h, "profile %d: n_clouds %d outside [0, max_clouds=%d]", m, b->n_clouds[m], NC);
+    items.insert(items.end(), {{b->cloud_water_content, (size_t)P * NC * Km * 8},
+                               {b->cloud_effective_radius, (size_t)P * NC * Km * 8},
+                               {b->n_clouds, (size_t)P * 4}, {b->cloud_type, (size_t)P * NC * 4},
+                               {b->n_streams, b->n_streams ? (size_t)P * 4 : 0}});
+  }
   size_t tot = 0;
   for (auto& it : items) tot += align_up(it.bytes);
   if (!h->io_in.ensure(tot)) return fail(h, "cannot allocate %zu bytes for inputs", tot);
@@ -764,6 +856,13 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
   db.emissivity = (const double*)dptr[14];
   const double* dseed = (const double*)dptr[15];
   db.n_layers = (const int*)dptr[16];
+  if (NC > 0) {
+    db.cloud_water_content = (const double*)dptr[17];
+    db.cloud_effective_radius = (const double*)dptr[18];
+    db.n_clouds = (const int*)dptr[19];
+    db.cloud_type = (const int*)dptr[20];
+    db.n_streams = (const int*)dptr[21];
+  }
   // outputs
   const size_t PL = (size_t)P * L;
   std::vector<std::pair<void*, size_t>> outs = {{rts->radiance, PL * 8}, {rts->brightness_temperature, PL * 8},
@@ -810,6 +909,12 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
   if (e != cudaSuccess || e2 != cudaSuccess)
     return fail(h, "CUDA error: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
   if (h->profiling) collect_stage_times(h);
+  if (NC > 0) {
+    int code = 0;
+    if (cudaMemcpy(&code, h->d_error, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return fail(h, "cannot read the scattering error flag");
+    if (code) return fail(h, "cloudy radiative transfer failed (code %d: 1-3 stream set, 4 cloud type, 5-6 singular matrix)", code);
+  }
   if (rts->status)
     for (int m = 0; m < P; m++)
       if (rts->status[m] != 0) return fail(h, "profile %d failed (status bits 0x%x)", m, rts->status[m]);
@@ -843,6 +948,46 @@ int crtm_gpu_init(const char* coeff_path, int n_sensors, const char* const* sens
       return CRTM_GPU_FAILURE;
     }
   }
+  {
+    // the cloud LUT is optional: without it, batches with clouds are refused
+    const std::string cpath = std::string(coeff_path) + "/CloudCoeff.bin";
+    FILE* f = fopen(cpath.c_str(), "rb");
+    if (f) {
+      fclose(f);
+      std::vector<double> buf;
+      int dims[7];
+      size_t off[14];
+      std::string err;
+      if (!load_cloudcoeff(cpath, buf, dims, off, err)) {
+        g_init_error = err;
+        crtm_gpu_destroy(h);
+        return CRTM_GPU_FAILURE;
+      }
+      if (cudaMalloc(&h->d_cloud, buf.size() * sizeof(double)) != cudaSuccess ||
+          cudaMemcpy(h->d_cloud, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+        g_init_error = "device upload of CloudCoeff.bin failed";
+        crtm_gpu_destroy(h);
+        return CRTM_GPU_FAILURE;
+      }
+      CloudLut& L = h->lut;
+      L.nfm = dims[0]; L.nrm = dims[1]; L.nt = dims[2]; L.nd = dims[3]; L.nfi = dims[4]; L.nri = dims[5];
+      L.nleg = dims[6];
+      const double* b0 = h->d_cloud;
+      L.f_mw = b0 + off[0]; L.f_ir = b0 + off[1]; L.r_mw = b0 + off[2]; L.r_ir = b0 + off[3]; L.t = b0 + off[4];
+      L.ke_l = b0 + off[5]; L.w_l = b0 + off[6]; L.pc_l = b0 + off[7];
+      L.ke_s = b0 + off[8]; L.w_s = b0 + off[9]; L.pc_s = b0 + off[10];
+      L.ke_ir = b0 + off[11]; L.w_ir = b0 + off[12]; L.pc_ir = b0 + off[13];
+      h->has_clouds = true;
+    }
+    GaussTable gt{};
+    for (int n = 1; n <= 9; n++) double_gauss_host(n, gt.mu[n], gt.w[n]);
+    if (cudaMemcpyToSymbol(c_gauss, &gt, sizeof gt) != cudaSuccess ||
+        cudaMalloc(&h->d_error, sizeof(int)) != cudaSuccess) {
+      g_init_error = "device set-up of the scattering tables failed";
+      crtm_gpu_destroy(h);
+      return CRTM_GPU_FAILURE;
+    }
+  }
   *handle = h;
   return CRTM_GPU_SUCCESS;
 }
@@ -853,6 +998,8 @@ int crtm_gpu_destroy(crtm_gpu_handle h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (auto& s : h->sensors) free_sensor(s);
   h->ws.release(); h->io_in.release(); h->io_out.release(); h->small.release();
+  cudaFree(h->d_cloud);
+  cudaFree(h->d_error);
   collect_stage_times(h);
   for (auto e : h->event_pool) cudaEventDestroy(e);
   if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
@@ -970,7 +1117,7 @@ int crtm_gpu_stage_times(crtm_gpu_handle h, double* ms, long long* launches, int
   }
   if (reset)
     for (int i = 0; i < 8; i++) { h->stage_ms[i] = 0.0; h->stage_n[i] = 0; }
-  return 6;
+  return 7;
 }
 
 }  // extern "C"

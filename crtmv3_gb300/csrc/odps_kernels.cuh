@@ -221,6 +221,7 @@ struct BatchView {
 
 struct SpecView {
   const double* c1, *c2, *b1, *b2, *cbr;
+  const double* freq, *wn;   // GHz, cm^-1
 };
 
 // Running sums of the reference profile (the *_ref terms of ODPS_Predictor.f90:707-759).
@@ -576,7 +577,7 @@ __global__ void __launch_bounds__(32 * FWD_WARPS) absorb_fwd_kernel(int K, int L
 
 // ---------------------------------------------------------------------------
 // 3. column: one thread per (profile, channel), two passes over the user layers.
-//    mode 0 forward, 1 K-matrix, 2 adjoint.
+//    mode 0 forward, 1 K-matrix, 2 adjoint, 3 layer optical depths only.
 //
 //    Pass 1 (top down) follows the forward model: OD path and its interpolation
 //    to the user levels, layer transmittance, Planck radiance and the
@@ -637,7 +638,7 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
       a.radiance[pl] = 0.0;
       a.bt[pl] = 0.0;
       if (a.mode == 1) { a.tsk[pl] = 0.0; a.ek[pl] = 0.0; }
-      if (a.mode) a.SC[(size_t)p * L + l] = R(0);
+      if (a.mode == 1 || a.mode == 2) a.SC[(size_t)p * L + l] = R(0);
       if (a.mode == 2) a.tsk[(size_t)p * L + l] = 0.0;
     }
     return;
@@ -696,7 +697,7 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
           src += tr * B * (R(1) - t);
         } else {
           a.TAU[cs + (size_t)ku * L] = tau;
-          a.DTOP[cs + (size_t)ku * L] = rad_down;
+          if (a.mode != 3) a.DTOP[cs + (size_t)ku * L] = rad_down;
         }
         tr *= t;
         total += tau;
@@ -719,6 +720,7 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
     a.bt[pl] = planck_temperature(c1d, c2d, b1d, b2d, Rd);
     return;
   }
+  if (a.mode == 3) return;   // gas layer optical depths only (the cloudy solver follows)
   // ---- pass 2 (bottom up): upwelling, Emission adjoint, OD path adjoint (unit seed)
   R U = re * Bs + rr * Dn;
   R P = R(1);                 // transmittance of the layers below the current one

@@ -1,0 +1,607 @@
+// Cloud scattering and the ADA solver for one (profile, channel): the physics
+// of the cloudy forward path, written for one GPU thread per pair and
+// compiled for the CPU as well (tests/harness).
+//
+// Reference behaviour followed (JCSDA/CRTMv3):
+//   LUT interpolation   src/Interpolation/CRTM_Interpolation.f90 (Find_Random_Index
+//                       :769-788, LPoly :832-860, Interp_1D/2D/3D :226-275)
+//   cloud optics        src/AtmScatter/CRTM_CloudScatter.f90:221-399, :927-1009, :1269-1416
+//   stream count        src/RTSolution/CRTM_RTSolution.f90:1204-1260
+//   combine             src/AtmOptics/CRTM_AtmOptics.f90:369-432
+//   angles and phase    src/RTSolution/Common_RTSolution.f90:189-458, 1857-1943, 2885-2940
+//   ADA                 src/RTSolution/ADA/ADA_Module.f90:97-258, 262-354, 552-743
+//
+// Differences of form (same numbers):
+//   - Layer optics are computed inside the adding loop, one layer at a time
+//     from the surface up, so no per-layer phase arrays are kept.
+//   - MOM's eigenproblem HH = (PP-PM)(PP+PM) is solved in its symmetric form
+//     (Cholesky of the PD matrix D^-1/2 (I - s W^1/2 (F+B) W^1/2) D^-1/2 and
+//     Jacobi rotations).  Only the eigenvalues and the eigenvectors' span
+//     enter the layer transmission and reflection; their scaling and order
+//     cancel in MOM's formulas.
+#pragma once
+
+#include <math.h>
+
+#include "odps_physics.cuh"
+
+namespace crtm {
+
+constexpr int SC_NLEG_MAX = 16;          // MAX_N_LEGENDRE_TERMS
+constexpr int SC_NZ_MAX = 10;            // 9 streams (16-stream option) + the sensor angle
+constexpr double WATER_CONTENT_THRESHOLD = 1.0e-6;   // CRTM_Parameters.f90:256
+constexpr double BS_THRESHOLD = 1.0e-10;             // CRTM_Parameters.f90:260
+constexpr double MAX_ALBEDO = 0.999999;              // RTV_Define.f90:77
+constexpr double PHASE_THRESHOLD = 1.0e-7;           // RTV_Define.f90:74
+constexpr double DELTA_OPTICAL_DEPTH = 1.0e-8;       // RTV_Define.f90:76
+constexpr double ANGLE_THRESHOLD = 1.0e-7;           // RTV_Define.f90:70
+
+// Device copy of the CloudCoeff LUT (phase element 1 only).  Tables keep the
+// file's Fortran order (frequency fastest).
+struct CloudLut {
+  int nfm, nrm, nt, nd, nfi, nri, nleg;
+  const double* f_mw, *r_mw, *t, *f_ir, *r_ir;
+  const double* ke_l, *w_l, *pc_l;   // [nt][nrm][nfm], pc: [nleg+1][nt][nrm][nfm]
+  const double* ke_s, *w_s, *pc_s;   // [nd][nrm][nfm],  pc: [nleg+1][nd][nrm][nfm]
+  const double* ke_ir, *w_ir, *pc_ir; // [nd+1][nri][nfi], pc: [nleg][nd+1][nri][nfi]
+};
+
+// Gauss-Legendre angles/weights on (0,1) for 1..9 streams (Double_Gauss_Quadrature).
+struct GaussTable {
+  double mu[10][SC_NZ_MAX];
+  double w[10][SC_NZ_MAX];
+};
+
+// ---- interpolation ----------------------------------------------------------
+struct Lagrange4 {
+  int i0;              // first of the 4 points
+  double wl[3], wr[3]; // left and right quadratic weights, already blended
+};
+
+// Clamp x into the axis, bracket it with 4 points and form the blended
+// quadratic weights (the reference's LPoly applied to a 4-point window).
+CRTM_HD Lagrange4 lagrange4(const double* ax, int n, double x) {
+  x = x < ax[0] ? ax[0] : (x > ax[n - 1] ? ax[n - 1] : x);
+  int k = 0;
+  while (k < n && x > ax[k]) k++;     // first node >= x
+  int i0 = k - 2;
+  i0 = i0 < 0 ? 0 : (i0 > n - 4 ? n - 4 : i0);
+  const double* p = ax + i0;
+  const double a0 = x - p[0], a1 = x - p[1], a2 = x - p[2], a3 = x - p[3];
+  const double d01 = p[0] - p[1], d02 = p[0] - p[2], d12 = p[1] - p[2], d13 = p[1] - p[3],
+               d23 = p[2] - p[3];
+  double wr = (x < p[1]) ? 0.0 : ((x > p[2]) ? 1.0 : a1 / (-d12));
+  const double wl = 1.0 - wr;
+  Lagrange4 L;
+  L.i0 = i0;
+  L.wl[0] = wl * (a1 * a2 / (d01 * d02));
+  L.wl[1] = wl * (a0 * a2 / (-d01 * d12));
+  L.wl[2] = wl * (a0 * a1 / (d02 * d12));
+  L.wr[0] = wr * (a2 * a3 / (d12 * d13));
+  L.wr[1] = wr * (a1 * a3 / (-d12 * d23));
+  L.wr[2] = wr * (a1 * a2 / (d13 * d23));
+  return L;
+}
+
+CRTM_HD double lerp4(const double* z, size_t stride, const Lagrange4& L) {
+  const double z0 = z[0], z1 = z[stride], z2 = z[2 * stride], z3 = z[3 * stride];
+  return (L.wl[0] * z0 + L.wl[1] * z1 + L.wl[2] * z2) + (L.wr[0] * z1 + L.wr[1] * z2 + L.wr[2] * z3);
+}
+
+// 2-D: dimension u fastest (stride 1), v with stride nu.
+CRTM_HD double lerp4x4(const double* z, int nu, const Lagrange4& U, const Lagrange4& V) {
+  double a[4];
+  const double* b = z + (size_t)V.i0 * nu + U.i0;
+  for (int j = 0; j < 4; j++) a[j] = lerp4(b + (size_t)j * nu, 1, U);
+  return lerp4(a, 1, V);
+}
+
+CRTM_HD double lerp4x4x4(const double* z, int nu, int nv, const Lagrange4& U,
+                                const Lagrange4& V, const Lagrange4& W) {
+  double a[4];
+  for (int k = 0; k < 4; k++) a[k] = lerp4x4(z + (size_t)(W.i0 + k) * nu * nv, nu, U, V);
+  return lerp4(a, 1, W);
+}
+
+// Legendre offset of the stream set (CloudCoeff_Define.f90:83-84).
+CRTM_HD int legendre_offset(int nleg) {
+  return nleg == 2 || nleg == 4 ? 0 : (nleg == 6 ? 5 : (nleg == 8 ? 12 : (nleg == 16 ? 21 : -1)));
+}
+
+// Optical properties of one cloud layer: ke (m^2/kg), w and the phase terms
+// pc[0..nleg].  Returns false for an unknown cloud type.
+CRTM_HD bool cloud_layer_optics(const CloudLut& C, bool microwave, double freq, int type,
+                                       double reff, double temp, int nleg, int loff, double* ke,
+                                       double* w, double* pc) {
+  for (int l = 0; l <= nleg; l++) pc[l] = 0.0;
+  *w = 0.0;
+  if (!microwave) {
+    // density slot of Get_Cloud_Opt_IR: liquid 1, snow 2, graupel 3, ice/hail 4
+    const int kd = (type == 1 || type == 3) ? 0 : (type == 4 ? 1 : (type == 5 ? 2 : (type == 2 || type == 6 ? 3 : -1)));
+    if (kd < 0) return false;
+    const Lagrange4 F = lagrange4(C.f_ir, C.nfi, freq), R = lagrange4(C.r_ir, C.nri, reff);
+    const size_t plane = (size_t)C.nfi * C.nri, vol = plane * (C.nd + 1);
+    *ke = lerp4x4(C.ke_ir + kd * plane, C.nfi, F, R);
+    *w = lerp4x4(C.w_ir + kd * plane, C.nfi, F, R);
+    pc[0] = 0.5;
+    for (int l = 1; l <= nleg; l++) pc[l] = lerp4x4(C.pc_ir + (l + loff - 1) * vol + kd * plane, C.nfi, F, R);
+    return true;
+  }
+  const Lagrange4 F = lagrange4(C.f_mw, C.nfm, freq);
+  const size_t plane = (size_t)C.nfm * C.nrm;
+  if (type == 1 || type == 3) {   // liquid: temperature axis
+    const Lagrange4 T = lagrange4(C.t, C.nt, temp);
+    if (type == 1) {              // cloud water: (frequency, temperature) at the first radius
+      double a[4];
+      for (int k = 0; k < 4; k++) a[k] = lerp4(C.ke_l + (size_t)(T.i0 + k) * plane + F.i0, 1, F);
+      *ke = lerp4(a, 1, T);
+      return true;
+    }
+    const Lagrange4 R = lagrange4(C.r_mw, C.nrm, reff);
+    const size_t vol = plane * C.nt;
+    *ke = lerp4x4x4(C.ke_l, C.nfm, C.nrm, F, R, T);
+    *w = lerp4x4x4(C.w_l, C.nfm, C.nrm, F, R, T);
+    pc[0] = 0.5;
+    for (int l = 1; l <= nleg; l++) pc[l] = lerp4x4x4(C.pc_l + (l + loff) * vol, C.nfm, C.nrm, F, R, T);
+    return true;
+  }
+  const int kd = type == 4 ? 0 : (type == 5 ? 1 : (type == 2 || type == 6 ? 2 : -1));
+  if (kd < 0) return false;
+  if (type == 2) {                // cloud ice: frequency only, first radius
+    *ke = lerp4(C.ke_s + kd * plane + F.i0, 1, F);
+    return true;
+  }
+  const Lagrange4 R = lagrange4(C.r_mw, C.nrm, reff);
+  const size_t vol = plane * C.nd;
+  *ke = lerp4x4(C.ke_s + kd * plane, C.nfm, F, R);
+  *w = lerp4x4(C.w_s + kd * plane, C.nfm, F, R);
+  pc[0] = 0.5;
+  for (int l = 1; l <= nleg; l++) pc[l] = lerp4x4(C.pc_s + (l + loff) * vol + kd * plane, C.nfm, F, R);
+  return true;
+}
+
+// ---- small dense matrices (row-major, fixed capacity NZ x NZ) --------------
+template <int NZ>
+struct Mat {
+  double a[NZ][NZ];
+};
+
+template <int NZ>
+CRTM_HD void mat_mul(int n, const Mat<NZ>& A, const Mat<NZ>& B, Mat<NZ>& C) {
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) {
+      double s = 0.0;
+      for (int k = 0; k < n; k++) s += A.a[i][k] * B.a[k][j];
+      C.a[i][j] = s;
+    }
+}
+
+// In-place inverse by Gauss-Jordan elimination with partial pivoting.
+template <int NZ>
+CRTM_HD bool mat_invert(int n, Mat<NZ>& A) {
+  int perm[NZ];
+  for (int i = 0; i < n; i++) perm[i] = i;
+  for (int k = 0; k < n; k++) {
+    int p = k;
+    double best = fabs(A.a[k][k]);
+    for (int i = k + 1; i < n; i++)
+      if (fabs(A.a[i][k]) > best) { best = fabs(A.a[i][k]); p = i; }
+    if (!(best > 1.0e-40)) return false;
+    if (p != k) {
+      for (int j = 0; j < n; j++) { const double t = A.a[p][j]; A.a[p][j] = A.a[k][j]; A.a[k][j] = t; }
+      const int t = perm[p]; perm[p] = perm[k]; perm[k] = t;
+    }
+    const double d = 1.0 / A.a[k][k];
+    for (int j = 0; j < n; j++) A.a[k][j] *= d;
+    A.a[k][k] = d;
+    for (int i = 0; i < n; i++) {
+      if (i == k) continue;
+      const double f = A.a[i][k];
+      if (f == 0.0) continue;
+      for (int j = 0; j < n; j++) A.a[i][j] -= f * A.a[k][j];
+      A.a[i][k] = -f * d;
+    }
+  }
+  // undo the row interchanges as column interchanges of the inverse
+  double tmp[NZ];
+  for (int i = 0; i < n; i++) {
+    for (int j = 0; j < n; j++) tmp[perm[j]] = A.a[i][j];
+    for (int j = 0; j < n; j++) A.a[i][j] = tmp[j];
+  }
+  return true;
+}
+
+// Symmetric eigenproblem S = V diag(lam) V^T by cyclic Jacobi rotations.
+template <int NZ>
+CRTM_HD void jacobi(int n, Mat<NZ>& S, double* lam, Mat<NZ>& V) {
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) V.a[i][j] = (i == j) ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 60; sweep++) {
+    double off = 0.0, diag = 0.0;
+    for (int i = 0; i < n; i++) {
+      diag += S.a[i][i] * S.a[i][i];
+      for (int j = i + 1; j < n; j++) off += S.a[i][j] * S.a[i][j];
+    }
+    if (off <= 1.0e-32 * diag) break;
+    for (int p = 0; p < n - 1; p++)
+      for (int q = p + 1; q < n; q++) {
+        const double apq = S.a[p][q];
+        if (apq == 0.0) continue;
+        const double th = (S.a[q][q] - S.a[p][p]) / (2.0 * apq);
+        const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < n; k++) {
+          const double kp = S.a[k][p], kq = S.a[k][q];
+          S.a[k][p] = c * kp - s * kq;
+          S.a[k][q] = s * kp + c * kq;
+        }
+        for (int k = 0; k < n; k++) {
+          const double pk = S.a[p][k], qk = S.a[q][k];
+          S.a[p][k] = c * pk - s * qk;
+          S.a[q][k] = s * pk + c * qk;
+        }
+        for (int k = 0; k < n; k++) {
+          const double kp = V.a[k][p], kq = V.a[k][q];
+          V.a[k][p] = c * kp - s * kq;
+          V.a[k][q] = s * kp + c * kq;
+        }
+      }
+  }
+  for (int i = 0; i < n; i++) lam[i] = S.a[i][i];
+}
+
+// Layer optics of a scattering layer for the adding method (CRTM_AMOM_layer +
+// MOM, azimuth order 0, no solar source): transmission T, reflection R and
+// the thermal source (identical up and down).  ff/bb are the normalised
+// forward/backward phase blocks.  Returns false on a failed factorisation.
+template <int NZ>
+CRTM_HD bool ada_layer(int nS, int nZ, double w, double tau, const double* mu,
+                              const double* wt, const Mat<NZ>& ff, const Mat<NZ>& bb, double B,
+                              Mat<NZ>& T, Mat<NZ>& R, double* src) {
+  if (tau < DELTA_OPTICAL_DEPTH) {   // thin layer: first-order scattering
+    const double s = tau * w;
+    for (int i = 0; i < nZ; i++) {
+      const double c = s / mu[i];
+      double th = 0.0;
+      for (int j = 0; j < nZ; j++) {
+        R.a[i][j] = c * bb.a[i][j] * wt[j];
+        T.a[i][j] = c * ff.a[i][j] * wt[j] + (i == j ? 1.0 - tau / mu[i] : 0.0);
+        th += R.a[i][j] + T.a[i][j];
+      }
+      src[i] = (1.0 - th) * B;
+    }
+    return true;
+  }
+  const double s = w < MAX_ALBEDO ? w : MAX_ALBEDO;
+  // symmetric form of the quadrature block
+  Mat<NZ> X, Y, V;
+  double lam[NZ], sq[NZ];
+  for (int i = 0; i < nS; i++) sq[i] = sqrt(wt[i]);
+  for (int i = 0; i < nS; i++)
+    for (int j = 0; j < nS; j++) {
+      const double sw = s * sq[i] * sq[j], dd = 1.0 / sqrt(mu[i] * mu[j]);
+      const double id = (i == j) ? 1.0 : 0.0;
+      X.a[i][j] = (id - sw * (ff.a[i][j] - bb.a[i][j])) * dd;
+      Y.a[i][j] = (id - sw * (ff.a[i][j] + bb.a[i][j])) * dd;
+    }
+  // Cholesky Y = L L^T (lower triangle of Y overwritten by L)
+  for (int j = 0; j < nS; j++) {
+    double d = Y.a[j][j];
+    for (int k = 0; k < j; k++) d -= Y.a[j][k] * Y.a[j][k];
+    if (!(d > 0.0)) return false;
+    d = sqrt(d);
+    Y.a[j][j] = d;
+    for (int i = j + 1; i < nS; i++) {
+      double v = Y.a[i][j];
+      for (int k = 0; k < j; k++) v -= Y.a[i][k] * Y.a[j][k];
+      Y.a[i][j] = v / d;
+    }
+  }
+  // S = L^T X L in V (temporary X L in T)
+  for (int i = 0; i < nS; i++)
+    for (int j = 0; j < nS; j++) {
+      double v = 0.0;
+      for (int k = j; k < nS; k++) v += X.a[i][k] * Y.a[k][j];
+      T.a[i][j] = v;
+    }
+  for (int i = 0; i < nS; i++)
+    for (int j = i; j < nS; j++) {
+      double v = 0.0;
+      for (int k = i; k < nS; k++) v += Y.a[k][i] * T.a[k][j];
+      V.a[i][j] = v;
+    }
+  for (int i = 0; i < nS; i++)
+    for (int j = 0; j < i; j++) V.a[i][j] = V.a[j][i];
+  jacobi(nS, V, lam, X);   // eigenvectors u in the columns of X
+  // E = W^-1/2 D^-1/2 L^-T u: eigenvectors of HH, in R
+  for (int c = 0; c < nS; c++) {
+    for (int i = nS - 1; i >= 0; i--) {
+      double v = X.a[i][c];
+      for (int k = i + 1; k < nS; k++) v -= Y.a[k][i] * R.a[k][c];
+      R.a[i][c] = v / Y.a[i][i];
+    }
+    for (int i = 0; i < nS; i++) R.a[i][c] /= sqrt(wt[i] * mu[i]);
+  }
+  // PP, PM for the full set of angles: PPM = PP - PM kept in X, PPP in Y
+  for (int i = 0; i < nZ; i++) {
+    const double c = s / mu[i];
+    for (int j = 0; j < nZ; j++) {
+      const double f = c * ff.a[i][j] * wt[j] - (i == j ? 1.0 / mu[i] : 0.0), b = c * bb.a[i][j] * wt[j];
+      X.a[i][j] = f - b;
+      Y.a[i][j] = f + b;
+    }
+  }
+  if (nZ > nS) {   // sensor angle (weight 0): HH is block lower triangular
+    const int z = nZ - 1;
+    double hz[NZ];
+    for (int k = 0; k < nZ; k++) {
+      double v = 0.0;
+      for (int m = 0; m < nZ; m++) v += X.a[z][m] * Y.a[m][k];
+      hz[k] = v;   // row z of HH
+    }
+    for (int c = 0; c < nS; c++) {
+      double v = 0.0;
+      for (int k = 0; k < nS; k++) v += hz[k] * R.a[k][c];
+      R.a[z][c] = v / (lam[c] - hz[z]);
+    }
+    for (int i = 0; i < nS; i++) R.a[i][z] = 0.0;
+    R.a[z][z] = 1.0;
+    lam[z] = hz[z];
+  }
+  // MOM with the eigenpairs (E in R, eigenvalues lam)
+  if (!mat_invert(nZ, X)) return false;   // inverse of PP - PM
+  double ex[NZ];
+  for (int i = 0; i < nZ; i++) {
+    lam[i] = lam[i] > 0.0 ? sqrt(lam[i]) : 0.0;
+    ex[i] = exp(-lam[i] * tau);
+  }
+  // EF = (PP-PM)^-1 E diag(lam);  Gp = (E + EF)/2 in Y, Gm = (E - EF)/2 in V
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) {
+      double v = 0.0;
+      for (int k = 0; k < nZ; k++) v += X.a[i][k] * R.a[k][j];
+      v *= lam[j];
+      Y.a[i][j] = 0.5 * (R.a[i][j] + v);
+      V.a[i][j] = 0.5 * (R.a[i][j] - v);
+    }
+  // A2 = Gm^-1 A1 with A1 = Gp diag(ex)
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) X.a[i][j] = V.a[i][j];
+  if (!mat_invert(nZ, X)) return false;    // Gm^-1
+  Mat<NZ> A2;
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) {
+      double v = 0.0;
+      for (int k = 0; k < nZ; k++) v += X.a[i][k] * Y.a[k][j];
+      A2.a[i][j] = v * ex[j];
+    }
+  // Gm - A1 A2 in X;  T <- (Gm diag(ex) - Gp A2), R <- (Gp - Gm diag(ex) A2)
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) {
+      double a5 = 0.0, a3 = 0.0, a6 = 0.0;
+      for (int k = 0; k < nZ; k++) {
+        a5 += Y.a[i][k] * ex[k] * A2.a[k][j];
+        a3 += Y.a[i][k] * A2.a[k][j];
+        a6 += V.a[i][k] * ex[k] * A2.a[k][j];
+      }
+      X.a[i][j] = V.a[i][j] - a5;
+      T.a[i][j] = V.a[i][j] * ex[j] - a3;
+      R.a[i][j] = Y.a[i][j] - a6;
+    }
+  if (!mat_invert(nZ, X)) return false;    // (Gm - A5)^-1
+  Mat<NZ> tmp;
+  mat_mul(nZ, T, X, tmp);
+  mat_mul(nZ, R, X, V);
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) { T.a[i][j] = tmp.a[i][j]; R.a[i][j] = V.a[i][j]; }
+  for (int i = 0; i < nZ; i++) {
+    double th = 0.0;
+    for (int j = 0; j < nS; j++) th += T.a[i][j] + R.a[i][j];
+    if (i == nZ - 1 && nZ == nS + 1) th += T.a[i][i];
+    src[i] = (1.0 - th) * B;
+  }
+  return true;
+}
+
+// Forward/backward phase blocks of one layer from its Legendre terms
+// (CRTM_Phase_Matrix, m = 0) and their normalisation (Normalize_Phase).
+template <int NZ>
+CRTM_HD void phase_blocks(int nS, int nZ, int nleg, const double* pc, const double (*P)[SC_NLEG_MAX + 1],
+                                 const double* wt, Mat<NZ>& ff, Mat<NZ>& bb) {
+  for (int i = 0; i < nZ; i++)
+    for (int j = i; j < nZ; j++) {
+      double f = 0.0, b = 0.0;
+      for (int l = 0; l < nleg; l++) {
+        const double t = pc[l] * P[i][l] * P[j][l];
+        f += t;
+        b += (l & 1) ? -t : t;
+      }
+      ff.a[i][j] = ff.a[j][i] = f < 0.0 ? PHASE_THRESHOLD : f;
+      bb.a[i][j] = bb.a[j][i] = b < 0.0 ? PHASE_THRESHOLD : b;
+    }
+  double carried = 0.0;
+  for (int i = 0; i < nS; i++) {
+    double nf = 0.0;
+    for (int j = i; j < nZ; j++) nf += (ff.a[i][j] + bb.a[i][j]) * wt[j];
+    const double sc = (1.0 - carried) / nf;
+    for (int j = i; j < nZ; j++) {
+      ff.a[i][j] *= sc; bb.a[i][j] *= sc;
+      ff.a[j][i] = ff.a[i][j]; bb.a[j][i] = bb.a[i][j];
+    }
+    carried = 0.0;
+    if (i + 1 < nZ)
+      for (int j = 0; j <= i; j++) carried += (ff.a[i + 1][j] + bb.a[i + 1][j]) * wt[j];
+  }
+  if (nS < nZ) {
+    const int z = nZ - 1;
+    for (int j = 0; j < nZ; j++) {
+      ff.a[j][z] /= carried; bb.a[j][z] /= carried;
+      if (j < z) { ff.a[z][j] = ff.a[j][z]; bb.a[z][j] = bb.a[j][z]; }
+    }
+  }
+}
+
+// Inputs of one (profile, channel) for the cloudy solver.
+struct CloudyColumn {
+  int Ku, n_clouds, nleg;                // nleg: Legendre terms of the stream set
+  bool microwave;
+  double freq;                           // GHz (MW) or cm^-1 (IR): LUT axis
+  double mu_sensor, emissivity, planck_surface, cosmic;
+  double c1, c2, b1, b2;                 // Planck constants of the channel
+  const double* temperature;             // [Ku]
+  const int* cloud_type;                 // [n_clouds]
+  const double* wc;                      // [n_clouds] rows of stride cstride
+  const double* reff;
+  size_t cstride;
+};
+
+// TOA radiance at the sensor angle of one cloudy (profile, channel) by the
+// adding method from the surface; gas layer ODs come from od(k).  Returns 0
+// or an error code.
+template <int NZ, class OdFn>
+CRTM_HD int cloudy_radiance(const CloudyColumn& in, const CloudLut& lut, const GaussTable& gt,
+                                   OdFn od_of, double* radiance) {
+  const int nleg = in.nleg, loff = legendre_offset(nleg);
+  if (loff < 0 || nleg > SC_NLEG_MAX) return 1;
+  if (lut.nleg < nleg + loff) return 2;
+  const int nS = (nleg + 2) / 2;
+  if (nS + 1 > NZ || nS > 9) return 3;
+  double mu[NZ], wt[NZ];
+  for (int i = 0; i < nS; i++) { mu[i] = gt.mu[nS][i]; wt[i] = gt.w[nS][i]; }
+  int nZ = nS, isat = -1;
+  for (int i = 0; i < nS; i++)
+    if (fabs(mu[i] - in.mu_sensor) < ANGLE_THRESHOLD) { isat = i; break; }
+  if (isat < 0) { nZ = nS + 1; isat = nS; mu[nS] = in.mu_sensor; wt[nS] = 0.0; }
+  double P[NZ][SC_NLEG_MAX + 1];
+  for (int i = 0; i < nZ; i++) {   // Legendre_M, m = 0
+    P[i][0] = 1.0;
+    if (nleg > 0) P[i][1] = mu[i];
+    for (int j = 1; j < nleg; j++) P[i][j + 1] = ((2 * j + 1) * mu[i] * P[i][j] - j * P[i][j - 1]) / (j + 1);
+  }
+  Mat<NZ> Rup, T, R, ff, bb;
+  double rad[NZ], src[NZ], tmp[NZ];
+  for (int i = 0; i < nZ; i++) {
+    for (int j = 0; j < nZ; j++) Rup.a[i][j] = 0.0;
+    Rup.a[i][i] = 1.0 - in.emissivity;
+    rad[i] = in.emissivity * in.planck_surface;
+  }
+  double pc[SC_NLEG_MAX + 1], pcs[SC_NLEG_MAX + 1];
+  for (int k = in.Ku - 1; k >= 0; k--) {
+    // layer optics: gas OD plus every cloud's OD, scattering and phase sums
+    double od = od_of(k), bs_sum = 0.0;
+    for (int l = 0; l <= nleg; l++) pcs[l] = 0.0;
+    const double tk = in.temperature[k];
+    for (int c = 0; c < in.n_clouds; c++) {
+      const double wc = in.wc[c * in.cstride + k];
+      if (!(wc > WATER_CONTENT_THRESHOLD)) continue;
+      double ke, w;
+      if (!cloud_layer_optics(lut, in.microwave, in.freq, in.cloud_type[c], in.reff[c * in.cstride + k], tk,
+                              nleg, loff, &ke, &w, pc))
+        return 4;
+      if (ke <= 0.0) { ke = 0.0; w = 0.0; }
+      if (w <= 0.0) { w = 0.0; for (int l = 0; l <= nleg; l++) pc[l] = 0.0; }
+      if (w >= 1.0) w = 1.0;
+      od += ke * wc;
+      const double bs = wc * ke * w;
+      bs_sum += bs;
+      for (int l = 1; l <= nleg; l++) pcs[l] += pc[l] * bs;
+    }
+    double ssa = bs_sum;
+    if (bs_sum > BS_THRESHOLD) {   // combine and delta truncation
+      const double w = bs_sum / od;
+      for (int l = 1; l <= nleg; l++) pcs[l] /= bs_sum;
+      pcs[0] = 0.5;
+      const double f = pcs[nleg];
+      od = (1.0 - f * w) * od;
+      ssa = (1.0 - f) * w / (1.0 - f * w);
+    }
+    const double te = in.b1 + in.b2 * tk;
+    const double B = in.c1 / (exp(in.c2 / te) - 1.0);
+    bool scat = false;
+    if (ssa > BS_THRESHOLD) {
+      phase_blocks<NZ>(nS, nZ, nleg, pcs, P, wt, ff, bb);
+      double mx = 0.0;
+      for (int i = 0; i < nZ; i++)
+        for (int j = 0; j < nZ; j++) mx = fabs(ff.a[i][j]) > mx ? fabs(ff.a[i][j]) : mx;
+      scat = mx > 0.0;
+    }
+    if (scat) {
+      if (!ada_layer<NZ>(nS, nZ, ssa, od, mu, wt, ff, bb, B, T, R, src)) return 5;
+      // Gamma = (I - Rup R)^-1 in ff; IGT = T Gamma in bb
+      for (int i = 0; i < nZ; i++)
+        for (int j = 0; j < nZ; j++) {
+          double v = 0.0;
+          for (int m = 0; m < nZ; m++) v += Rup.a[i][m] * R.a[m][j];
+          ff.a[i][j] = (i == j ? 1.0 : 0.0) - v;
+        }
+      if (!mat_invert(nZ, ff)) return 6;
+      mat_mul(nZ, T, ff, bb);
+      for (int i = 0; i < nZ; i++) {
+        double v = rad[i];
+        for (int j = 0; j < nZ; j++) v += Rup.a[i][j] * src[j];
+        tmp[i] = v;
+      }
+      for (int i = 0; i < nZ; i++) {
+        double v = src[i];
+        for (int j = 0; j < nZ; j++) v += bb.a[i][j] * tmp[j];
+        rad[i] = v;
+      }
+      mat_mul(nZ, Rup, T, ff);       // Rup T
+      mat_mul(nZ, bb, ff, Rup);      // IGT Rup T
+      for (int i = 0; i < nZ; i++)
+        for (int j = 0; j < nZ; j++) Rup.a[i][j] += R.a[i][j];
+    } else {
+      double tr[NZ];
+      for (int i = 0; i < nZ; i++) {
+        tr[i] = exp(-od / mu[i]);
+        src[i] = B * (1.0 - tr[i]);
+      }
+      for (int i = 0; i < nZ; i++) {
+        double v = rad[i];
+        for (int j = 0; j < nZ; j++) v += Rup.a[i][j] * src[j];
+        tmp[i] = src[i] + tr[i] * v;
+      }
+      for (int i = 0; i < nZ; i++) {
+        rad[i] = tmp[i];
+        for (int j = 0; j < nZ; j++) Rup.a[i][j] *= tr[i] * tr[j];
+      }
+    }
+  }
+  double s = 0.0;
+  for (int j = 0; j < nZ; j++) s += Rup.a[isat][j];
+  *radiance = rad[isat] + s * in.cosmic;
+  return 0;
+}
+
+// Stream rule (CRTM_Compute_nStreams): Legendre terms 2/4/6 from the Mie
+// parameter of the largest effective radius in the profile.
+CRTM_HD int stream_rule_nleg(double max_reff, double wavenumber) {
+  const double mie = 2.0 * PI_D * max_reff * wavenumber / 10000.0;
+  return mie < 0.01 ? 2 : (mie < 1.0 ? 4 : 6);
+}
+
+// Double_Gauss_Quadrature for n points on (0,1).
+inline void double_gauss_host(int n, double* x, double* w) {
+  const int k = (n + 1) / 2;
+  for (int j = 1; j <= k; j++) {
+    double X = cos(PI_D * (j - 0.25) / (n + 0.5)), XP, PL = 0, PL1, PL2, DPL = 1;
+    for (int it = 0; it < 10; it++) {
+      PL1 = 1.0;
+      PL = X;
+      for (int l = 2; l <= n; l++) {
+        PL2 = PL1;
+        PL1 = PL;
+        PL = ((2 * l - 1) * X * PL1 - (l - 1) * PL2) / l;
+      }
+      DPL = n * (X * PL - PL1) / (X * X - 1.0);
+      XP = X;
+      X = XP - PL / DPL;
+      if (!(fabs(X - XP) > 3.0e-14)) break;
+    }
+    x[j - 1] = (1.0 - X) / 2.0;
+    x[n - j] = (1.0 + X) / 2.0;
+    w[j - 1] = w[n - j] = 1.0 / ((1.0 - X * X) * DPL * DPL);
+  }
+}
+
+}  // namespace crtm

@@ -82,6 +82,18 @@ typedef struct {
   const double* surface_altitude; /* may be NULL (0) */
   /* options (CRTM_Options_type): Use_Emissivity is required in this build */
   const double* emissivity;       /* [P][n_channels] */
+  /* clouds (CRTM_Cloud_type, Atmosphere%Cloud(:)).  max_clouds = 0: clear-sky
+   * batch, the cloud pointers are not read.  A profile with n_clouds > 0 is
+   * solved with the scattering solver (ADA) as one cloudy column (the
+   * reference's coverage flag CLEAR: Cloud_Fraction not used). */
+  int max_clouds;                 /* NC: stride of the cloud arrays */
+  const int* n_clouds;            /* [P] clouds of each profile, <= NC */
+  const int* cloud_type;          /* [P][NC] WATER=1 ICE=2 RAIN=3 SNOW=4 GRAUPEL=5 HAIL=6 */
+  const double* cloud_water_content;    /* [P][NC][max_layers] kg/m^2 */
+  const double* cloud_effective_radius; /* [P][NC][max_layers] microns */
+  /* Options%n_Streams for profiles with Options%Use_N_Streams (2, 4, 6, 8 or
+   * 16), 0 for the reference's stream rule; NULL: the rule everywhere. */
+  const int* n_streams;           /* [P] */
 } crtm_gpu_batch;
 
 typedef struct {
@@ -111,7 +123,9 @@ typedef struct {
 } crtm_gpu_adjoint_out;
 
 /* CRTM_Init: loads <coeff_path>/<sensor_id>.SpcCoeff.bin and .TauCoeff.bin
- * (ODPS) for each sensor, uploads them to the current CUDA device. */
+ * (ODPS) for each sensor, and <coeff_path>/CloudCoeff.bin when that file
+ * exists (the reference's default cloud LUT name), and uploads them to the
+ * current CUDA device.  Batches with clouds need the cloud LUT. */
 int crtm_gpu_init(const char* coeff_path, int n_sensors, const char* const* sensor_ids,
                   crtm_gpu_handle* handle);
 
@@ -124,7 +138,9 @@ int crtm_gpu_n_channels(crtm_gpu_handle handle, int sensor);
 /* Select the arithmetic form for later calls (CRTM_GPU_FP64 or CRTM_GPU_MIXED). */
 int crtm_gpu_set_precision(crtm_gpu_handle handle, int precision);
 
-/* CRTM_Forward for one sensor: host buffers. */
+/* CRTM_Forward for one sensor: host buffers.  Profiles with clouds use the
+ * ADA scattering solver (in FP64 in both arithmetic forms); the K-matrix and
+ * adjoint entry points return CRTM_GPU_FAILURE for batches with clouds. */
 int crtm_gpu_forward(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* batch,
                      crtm_gpu_rtsolution* rts);
 

@@ -1,0 +1,79 @@
+"""Cloudy forward (cloud LUT, combine, ADA) on the GPU against the oracle.
+
+Tolerances: 1e-4 K in brightness temperature in the FP64 form.  In the mixed
+form the gas layer optical depths come from the FP32 regression (the
+scattering solver is FP64 in both forms), so 0.01 K as for clear sky.
+"""
+import numpy as np
+import pytest
+
+from crtmv3_gb300 import coefficients as co, synthetic as sy
+
+pytestmark = pytest.mark.gpu
+
+BT_TOL = {0: 1e-4, 1: 1e-2}
+
+
+@pytest.fixture(scope="module")
+def cloud_dir(coeff_dir):
+    sy.write_cloud_files(coeff_dir)
+    return coeff_dir
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("sensor,nl,n_streams,wc_scale", [
+    ("mwsynth_c16", 100, None, 1.0),      # config C3 distributions, stream rule
+    ("mwsynth_c16", 100, None, 300.0),    # thick clouds
+    ("mwsynth_c16", 100, 8, 100.0),
+    ("mwsynth_c16", 100, 16, 100.0),
+    ("irsynth_c616", 101, None, 100.0),
+    ("mwsynth_c22", 100, None, 100.0)])
+def test_cloudy_forward_matches_oracle(gpu_lib, cloud_dir, precision, sensor, nl, n_streams, wc_scale):
+    from oracle.pyoracle import Oracle
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 6, nl, 61, wc_scale=wc_scale, n_streams=n_streams)
+    atm.n_clouds[2] = 0   # one clear profile in the batch
+    _, ref = Oracle(cloud_dir, sensor).forward_scatter(atm, sfc, geo, opt, f"{cloud_dir}/CloudCoeff.bin")
+    h = gpu_lib.CRTM([sensor], cloud_dir, precision)
+    rts = h.forward(atm, sfc, geo, opt)
+    assert np.abs(rts.brightness_temperature - ref).max() <= BT_TOL[precision]
+    assert (rts.status == 0).all()
+
+
+def test_ragged_cloudy_batch(gpu_lib, cloud_dir):
+    from oracle.pyoracle import Oracle
+    sensor = "mwsynth_c16"
+    nl = np.array([60, 137, 101, 75, 120])
+    atm, sfc, geo = sy.generate_profiles(5, nl, (co.H2O_ID,), 62, p_sfc=1013.0)
+    opt = sy.OptionsBatch(emissivity=sy.emissivity_for(co.MICROWAVE_SENSOR, 5, 16, 63))
+    sy.add_clouds(atm, (co.RAIN_CLOUD, co.SNOW_CLOUD, co.GRAUPEL_CLOUD), 64, wc_scale=200.0)
+    _, ref = Oracle(cloud_dir, sensor).forward_scatter(atm, sfc, geo, opt, f"{cloud_dir}/CloudCoeff.bin")
+    rts = gpu_lib.CRTM([sensor], cloud_dir, 0).forward(atm, sfc, geo, opt)
+    assert np.abs(rts.brightness_temperature - ref).max() <= BT_TOL[0]
+
+
+def test_cloudy_k_matrix_is_refused(gpu_lib, cloud_dir):
+    atm, sfc, geo, opt = sy.cloudy_workload("mwsynth_c16", 2, 100, 65)
+    h = gpu_lib.CRTM(["mwsynth_c16"], cloud_dir, 0)
+    with pytest.raises(RuntimeError, match="not available for batches with clouds"):
+        h.k_matrix(atm, sfc, geo, opt)
+
+
+def test_isothermal_enclosure_on_gpu(gpu_lib, cloud_dir, tmp_path):
+    """Kirchhoff check of the GPU solver itself: an isothermal scene whose
+    cosmic background is B(T) gives BT = T for any cloud and stream count."""
+    import shutil
+    sensor = "mwsynth_c16"
+    sc = co.read_spccoeff(f"{cloud_dir}/{sensor}.SpcCoeff.bin")
+    te = sc.band_c1 + sc.band_c2 * 250.0
+    sc.cosmic_background_radiance = sc.planck_c1 / (np.exp(sc.planck_c2 / te) - 1.0)
+    co.write_spccoeff(str(tmp_path / f"{sensor}.SpcCoeff.bin"), sc)
+    shutil.copy(f"{cloud_dir}/{sensor}.TauCoeff.bin", tmp_path / f"{sensor}.TauCoeff.bin")
+    shutil.copy(f"{cloud_dir}/CloudCoeff.bin", tmp_path / "CloudCoeff.bin")
+    for ns in (None, 16):
+        atm, sfc, geo, opt = sy.cloudy_workload(sensor, 4, 100, 66, wc_scale=300.0, n_streams=ns)
+        for m in range(4):
+            atm.temperature[m, :atm.n_layers[m]] = 250.0
+        sfc.water_temperature[:] = 250.0
+        opt.emissivity[:] = 1.0
+        rts = gpu_lib.CRTM([sensor], str(tmp_path), 0).forward(atm, sfc, geo, opt)
+        assert np.abs(rts.brightness_temperature - 250.0).max() < 1e-8

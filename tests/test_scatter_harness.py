@@ -1,0 +1,105 @@
+"""The GPU library's cloud/ADA physics header (scatter_physics.cuh), compiled
+for the CPU, against the oracle: one ADA layer, and whole cloudy
+(profile, channel) radiances given the oracle's gas layer optical depths."""
+import ctypes as ct
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from crtmv3_gb300 import coefficients as co, synthetic as sy
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+_dp = ct.POINTER(ct.c_double)
+_ip = ct.POINTER(ct.c_int)
+
+
+def _p(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+@pytest.fixture(scope="module")
+def sx(tmp_path_factory):
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    out = str(tmp_path_factory.mktemp("sx") / "libsx.so")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-I",
+                    os.path.join(ROOT, "crtmv3_gb300", "csrc"), "-o", out,
+                    os.path.join(HERE, "harness", "scatter_harness.cpp")], check=True)
+    return ct.CDLL(out)
+
+
+@pytest.mark.parametrize("nleg,mu_s", [(2, 0.9), (4, 0.55), (6, 0.8), (8, 0.66), (16, 0.93)])
+@pytest.mark.parametrize("w,tau", [(0.6, 0.5), (0.98, 6.0), (0.3, 5e-9), (0.05, 0.02)])
+def test_ada_layer_matches_oracle(sx, nleg, mu_s, w, tau):
+    from oracle.pyoracle import lib
+    pc = 0.5 * 0.8 ** np.arange(nleg + 1)
+    mu, wt = np.zeros(20), np.zeros(20)
+    ff, bb = np.zeros(400), np.zeros(400)
+    nz = ct.c_int(0)
+    lib().or_phase_setup(nleg, mu_s, _p(pc), _p(mu), _p(wt), _p(ff), _p(bb), ct.byref(nz))
+    nZ, nS = nz.value, (nleg + 2) // 2
+    outs = [[np.zeros(nZ * nZ), np.zeros(nZ * nZ), np.zeros(nZ)] for _ in range(2)]
+    assert lib().or_amom_layer(nS, nZ, w, tau, _p(mu), _p(wt), _p(ff), _p(bb), 1.7,
+                               *[_p(x) for x in outs[0]]) == 0
+    assert sx.sx_ada_layer(nS, nZ, ct.c_double(w), ct.c_double(tau), _p(mu), _p(wt), _p(ff), _p(bb),
+                           ct.c_double(1.7), *[_p(x) for x in outs[1]]) == 0
+    for a, b in zip(*outs):
+        assert np.abs(a - b).max() < 1e-12
+
+
+@pytest.mark.parametrize("sensor,nl,n_streams", [("mwsynth_c16", 100, None), ("mwsynth_c16", 100, 16),
+                                                 ("irsynth_c616", 101, None), ("mwsynth_c22", 100, 8)])
+def test_cloudy_radiance_matches_oracle(sx, coeff_dir, sensor, nl, n_streams):
+    from oracle.pyoracle import Oracle
+    path = sy.write_cloud_files(coeff_dir)
+    cc = co.read_cloudcoeff(path)
+    sc = co.read_spccoeff(f"{coeff_dir}/{sensor}.SpcCoeff.bin")
+    o = Oracle(coeff_dir, sensor)
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 3, nl, 51, wc_scale=200.0, n_streams=n_streams)
+    if sensor == "irsynth_c616":   # only a channel subset for time
+        pass
+    rad_ref, _ = o.forward_scatter(atm, sfc, geo, opt, path)
+    _, _, lod = o.forward(atm, sfc, geo, opt, layer_od=True)
+    f = lambda a: np.ascontiguousarray(np.ravel(a, order="F"))   # noqa: E731
+    arrs = [f(x) for x in (cc.frequency_mw, cc.reff_mw, cc.temperature, cc.frequency_ir, cc.reff_ir,
+                           cc.ke_l_mw, cc.w_l_mw, cc.pcoeff_l_mw, cc.ke_s_mw, cc.w_s_mw, cc.pcoeff_s_mw,
+                           cc.ke_ir, cc.w_ir, cc.pcoeff_ir)]
+    dims = np.array([cc.frequency_mw.size, cc.reff_mw.size, cc.temperature.size, cc.density_mw.size,
+                     cc.frequency_ir.size, cc.reff_ir.size, cc.n_legendre_terms], np.int32)
+    mw = sc.sensor_type == co.MICROWAVE_SENSOR
+    L = sc.n_channels
+    chans = range(0, L, max(1, L // 40))
+    worst = 0.0
+    for m in range(atm.n_profiles):
+        Ku = int(atm.n_layers[m])
+        ts = sfc.water_temperature[m]
+        mu = np.cos(np.deg2rad(geo.sensor_zenith_angle[m]))
+        temp = np.ascontiguousarray(atm.temperature[m, :Ku])
+        NC = atm.cloud_type.shape[1]
+        wc = np.ascontiguousarray(atm.cloud_water_content[m])
+        re = np.ascontiguousarray(atm.cloud_effective_radius[m])
+        ctype = np.ascontiguousarray(atm.cloud_type[m], np.int32)
+        for l in chans:
+            planck = np.array([sc.planck_c1[l], sc.planck_c2[l], sc.band_c1[l], sc.band_c2[l]])
+            te = sc.band_c1[l] + sc.band_c2[l] * ts
+            bs = sc.planck_c1[l] / (np.exp(sc.planck_c2[l] / te) - 1.0)
+            if n_streams:
+                nleg = n_streams
+            else:
+                nleg = sx.sx_stream_rule(ct.c_double(re[:, :Ku].max()), ct.c_double(sc.wavenumber[l]))
+            od = np.ascontiguousarray(lod[m, l, :Ku])
+            r = ct.c_double(0.0)
+            rc = sx.sx_cloudy_radiance(
+                _p(dims, _ip), *[_p(a) for a in arrs], Ku, NC, nleg, int(mw),
+                ct.c_double(sc.frequency[l] if mw else sc.wavenumber[l]), ct.c_double(mu),
+                ct.c_double(opt.emissivity[m, l]), ct.c_double(bs),
+                ct.c_double(sc.cosmic_background_radiance[l]), _p(planck), _p(temp), _p(ctype, _ip),
+                _p(wc), _p(re), atm.max_layers, _p(od), ct.byref(r))
+            assert rc == 0
+            worst = max(worst, abs(r.value - rad_ref[m, l]) / abs(rad_ref[m, l]))
+    assert worst < 1e-11
