@@ -148,7 +148,8 @@ class CRTM:
     def launch_count(self) -> int:
         return int(library().crtm_gpu_launch_count(self.h))
 
-    STAGES = ("prep", "absorb_fwd", "column", "absorb_ad", "map_out", "adjoint_sum", "scatter")
+    STAGES = ("prep", "absorb_fwd", "column", "absorb_ad", "map_out", "adjoint_sum", "scatter_layers",
+              "scatter_adding")
 
     def set_profiling(self, enable: bool) -> None:
         library().crtm_gpu_set_profiling(self.h, int(enable))

@@ -463,6 +463,8 @@ struct Work {
   R* SC;            // [n][L]
   double* TSK;      // adjoint: [n][L]
   R* RA;            // [n][nv][K][L]
+  R* LB;            // cloudy forward: [n][Kmax][NE][L] layer records
+  double* maxreff;  // cloudy forward: [n]
   double* ras;      // adjoint: [n][nv][K]
   double* pts;      // adjoint: [n][Kmax]
   double* tss;      // adjoint: [n]
@@ -509,7 +511,11 @@ size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w
   Work<R> wk{};
   wk.pv = pv;
   wk.OD = (R*)carve(nn * K * L * sizeof(R));
-  if (mode == 3) wk.TAU = (R*)carve(nn * Kmax * L * sizeof(R));
+  if (mode == 3) {   // nv carries the layer record length here
+    wk.TAU = (R*)carve(nn * Kmax * L * sizeof(R));
+    wk.LB = (R*)carve(nn * Kmax * (size_t)nv * L * sizeof(R));
+    wk.maxreff = (double*)carve(nn * sizeof(double));
+  }
   if (adj) {
     wk.TAU = (R*)carve(nn * Kmax * L * sizeof(R));
     wk.DTOP = (R*)carve(nn * Kmax * L * sizeof(R));
@@ -621,28 +627,31 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
     for (int j = 0; j < n_abs; j++) oa.odps[j] = abs_of_user[j];
   }
   const int nv = 1 + oa.n;
+  // cloudy forward: NZ angles of the kernels (16-stream option or the stream rule)
+  const bool nz_max = mode == 3 && b->n_streams != nullptr;
+  const int wnv = mode == 3 ? (nz_max ? layer_record<SC_NZ_MAX>() : layer_record<5>()) : nv;
   // chunk size from the workspace budget
-  const size_t per = work_bytes<G, R>(s, 64, Kmax, nv, mode, nullptr, nullptr) / 64 + 1;
+  const size_t per = work_bytes<G, R>(s, 64, Kmax, wnv, mode, nullptr, nullptr) / 64 + 1;
   int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)P, h->workspace_budget / per));
   if (hc && hc->max_chunk > 0) chunk = std::min(chunk, hc->max_chunk);
   char* ws_base;
   if (fixed) {
     // largest chunk whose workspace fits the fixed scratch
     chunk = (int)std::min<size_t>((size_t)chunk, fixed->bytes / per);
-    while (chunk > 1 && work_bytes<G, R>(s, chunk, Kmax, nv, mode, nullptr, nullptr) > fixed->bytes) chunk--;
-    const size_t one = work_bytes<G, R>(s, 1, Kmax, nv, mode, nullptr, nullptr);
+    while (chunk > 1 && work_bytes<G, R>(s, chunk, Kmax, wnv, mode, nullptr, nullptr) > fixed->bytes) chunk--;
+    const size_t one = work_bytes<G, R>(s, 1, Kmax, wnv, mode, nullptr, nullptr);
     if (chunk < 1 || one > fixed->bytes)
       return fail(h, "one profile of this call needs %zu bytes of scratch (%d channels, max_layers %d, "
                      "%d absorber Jacobians); the static scratch holds %zu bytes",
                   one, L, Kmax, nv - 1, fixed->bytes);
     ws_base = fixed->base;
   } else {
-    const size_t need = work_bytes<G, R>(s, chunk, Kmax, nv, mode, nullptr, nullptr);
+    const size_t need = work_bytes<G, R>(s, chunk, Kmax, wnv, mode, nullptr, nullptr);
     if (!h->ws.ensure(need)) return fail(h, "cannot allocate %zu bytes of workspace", need);
     ws_base = (char*)h->ws.p;
   }
   Work<R> w;
-  work_bytes<G, R>(s, chunk, Kmax, nv, mode, &w, ws_base);
+  work_bytes<G, R>(s, chunk, Kmax, wnv, mode, &w, ws_base);
   if (cudaMemcpyAsync(w.idx_map, idx_map, sizeof(int) * s.Jm, cudaMemcpyHostToDevice, st) != cudaSuccess)
     return fail(h, "absorber map upload failed");
   const BatchView bv = make_view(b);
@@ -690,22 +699,37 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       column_kernel<R><<<gc, 128, col_smem, st>>>(ca);
       CK_LAUNCH(h);
     }
-    if (mode == 3) {   // cloudy forward: ADA over the gas layer optical depths
+    if (mode == 3) {   // cloudy forward: layer optics, then the adding from the surface
       ScatterArgs<R> sa{};
       sa.K = K; sa.L = L; sa.Kmax = Kmax; sa.p_begin = p0; sa.n_chunk = n;
       sa.microwave = s.sensor_type == 1;
       sa.b = bv; sa.sp = s.spec; sa.pv = w.pv; sa.lut = h->lut;
       sa.max_clouds = b->max_clouds; sa.n_clouds = b->n_clouds; sa.cloud_type = b->cloud_type;
       sa.wc = b->cloud_water_content; sa.reff = b->cloud_effective_radius; sa.n_streams = b->n_streams;
-      sa.TAU = w.TAU; sa.radiance = rts->radiance; sa.bt = rts->brightness_temperature;
+      sa.TAU = w.TAU; sa.LB = w.LB; sa.maxreff = w.maxreff;
+      sa.radiance = rts->radiance; sa.bt = rts->brightness_temperature;
       sa.status = rts->status; sa.error = h->d_error;
-      StageScope sc(h, 6, st);
-      dim3 gs((L + SCATTER_THREADS - 1) / SCATTER_THREADS, n);
-      if (b->n_streams)
-        scatter_kernel<SC_NZ_MAX, R><<<gs, SCATTER_THREADS, 0, st>>>(sa);
-      else
-        scatter_kernel<5, R><<<gs, SCATTER_THREADS, 0, st>>>(sa);
-      CK_LAUNCH(h);
+      const long long nlay = (long long)n * Kmax * L;
+      const unsigned gl = (unsigned)((nlay + SCATTER_THREADS - 1) / SCATTER_THREADS);
+      dim3 ga((L + SCATTER_THREADS - 1) / SCATTER_THREADS, n);
+      {
+        StageScope sc(h, 6, st);
+        scatter_maxreff_kernel<R><<<(n + 3) / 4, 128, 0, st>>>(sa);
+        CK_LAUNCH(h);
+        if (nz_max)
+          scatter_layers_kernel<SC_NZ_MAX, R><<<gl, SCATTER_THREADS, 0, st>>>(sa);
+        else
+          scatter_layers_kernel<5, R><<<gl, SCATTER_THREADS, 0, st>>>(sa);
+        CK_LAUNCH(h);
+      }
+      {
+        StageScope sc(h, 7, st);
+        if (nz_max)
+          scatter_adding_kernel<SC_NZ_MAX, R><<<ga, SCATTER_THREADS, 0, st>>>(sa);
+        else
+          scatter_adding_kernel<5, R><<<ga, SCATTER_THREADS, 0, st>>>(sa);
+        CK_LAUNCH(h);
+      }
     }
     if (mode == 0 || mode == 3) {
       if (hc && hc->n) {
@@ -1117,7 +1141,7 @@ int crtm_gpu_stage_times(crtm_gpu_handle h, double* ms, long long* launches, int
   }
   if (reset)
     for (int i = 0; i < 8; i++) { h->stage_ms[i] = 0.0; h->stage_n[i] = 0; }
-  return 7;
+  return 8;
 }
 
 }  // extern "C"

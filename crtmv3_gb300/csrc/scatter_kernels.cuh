@@ -1,9 +1,19 @@
-// Cloudy forward kernel: one thread per (profile, channel) runs the cloud
-// optics, the combine, the phase matrices and the ADA adding method
-// (scatter_physics.cuh) over the profile's layers, from the gas layer optical
-// depths the column kernel stored.  The scattering arithmetic is FP64 in
-// every form: the reference keeps its matrix inversions and thin-layer
-// initialisation in FP64.
+// Cloudy forward kernels, after the column kernel has stored the gas layer
+// optical depths:
+//
+//   scatter_layers_kernel  one thread per (profile, layer, channel): cloud
+//                          optics, combine, phase blocks and, for scattering
+//                          layers, the layer transmission/reflection/source
+//                          (MOM), in the working precision R.  Layers are
+//                          independent, so this is where the parallelism is.
+//   scatter_adding_kernel  one thread per (profile, channel): the adding
+//                          recursion from the surface to the top, FP64 in
+//                          every form (the (I - R R)^-1 inversions), then the
+//                          FP64 Planck inversion.
+//
+// Per-layer results go through HBM with channels fastest:
+// LB[p][k][e][l], e = 0 kind (0 clear, 1 scattering, <0 error), 1 optical
+// depth, then T (NZ*NZ), R (NZ*NZ) and the source (NZ).
 #pragma once
 
 #include "odps_kernels.cuh"
@@ -12,6 +22,9 @@
 namespace crtm {
 
 __constant__ GaussTable c_gauss;
+
+template <int NZ>
+constexpr int layer_record() { return 2 + 2 * NZ * NZ + NZ; }
 
 template <class R>
 struct ScatterArgs {
@@ -26,6 +39,8 @@ struct ScatterArgs {
   const double* wc, *reff;      // [P][NC][Kmax]
   const int* n_streams;         // [P] or null
   const R* TAU;                 // [n][Kmax][L] gas layer optical depths
+  R* LB;                        // [n][Kmax][NE][L] layer records
+  double* maxreff;              // [n]
   double* radiance, *bt;        // [P][L]
   int* status;                  // [P] or null
   int* error;                   // first failing code (device), 0 if none
@@ -33,82 +48,141 @@ struct ScatterArgs {
 
 constexpr int SCATTER_THREADS = 128;
 
+// Largest effective radius of each profile's clouds (stream rule input).
+template <class R>
+__global__ void scatter_maxreff_kernel(ScatterArgs<R> a) {
+  const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (p >= a.n_chunk) return;
+  const int gp = a.p_begin + p, Ku = a.b.n_layers[gp], nc = a.n_clouds[gp];
+  const double* rp = a.reff + (size_t)gp * a.max_clouds * a.Kmax;
+  double mr = 0.0;
+  for (int i = lane; i < nc * Ku; i += 32) {
+    const double r = rp[(size_t)(i / Ku) * a.Kmax + (i % Ku)];
+    mr = r > mr ? r : mr;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v = __shfl_xor_sync(FULL, mr, o);
+    mr = v > mr ? v : mr;
+  }
+  if (lane == 0) a.maxreff[p] = mr;
+}
+
+template <class R>
+__device__ __forceinline__ CloudyColumn column_inputs(const ScatterArgs<R>& a, int p, int gp, int l) {
+  CloudyColumn c;
+  c.Ku = a.b.n_layers[gp];
+  c.n_clouds = a.n_clouds[gp];
+  const int ns = a.n_streams ? a.n_streams[gp] : 0;
+  c.nleg = ns > 0 ? ns : stream_rule_nleg(a.maxreff[p], a.sp.wn[l]);
+  c.microwave = a.microwave != 0;
+  c.freq = a.microwave ? a.sp.freq[l] : a.sp.wn[l];
+  c.mu_sensor = a.pv.scal[(size_t)p * 4 + 1];
+  const size_t pl = (size_t)gp * a.L + l;
+  c.emissivity = a.b.emissivity[pl];
+  c.c1 = a.sp.c1[l]; c.c2 = a.sp.c2[l]; c.b1 = a.sp.b1[l]; c.b2 = a.sp.b2[l];
+  const double ts = a.b.land_cov[gp] * a.b.land_t[gp] + a.b.water_cov[gp] * a.b.water_t[gp] +
+                    a.b.snow_cov[gp] * a.b.snow_t[gp] + a.b.ice_cov[gp] * a.b.ice_t[gp];
+  c.planck_surface = c.c1 / (exp(c.c2 / (c.b1 + c.b2 * ts)) - 1.0);
+  c.cosmic = a.sp.cbr[l];
+  c.temperature = a.b.temperature + (size_t)gp * a.Kmax;
+  c.cloud_type = a.cloud_type + (size_t)gp * a.max_clouds;
+  c.wc = a.wc + (size_t)gp * a.max_clouds * a.Kmax;
+  c.reff = a.reff + (size_t)gp * a.max_clouds * a.Kmax;
+  c.cstride = (size_t)a.Kmax;
+  return c;
+}
+
 template <int NZ, class R>
-__global__ void __launch_bounds__(SCATTER_THREADS) scatter_kernel(ScatterArgs<R> a) {
-  __shared__ double s_maxreff;
+__global__ void __launch_bounds__(SCATTER_THREADS) scatter_layers_kernel(ScatterArgs<R> a) {
+  constexpr int NE = layer_record<NZ>();
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int L = a.L, Kmax = a.Kmax;
+  if (idx >= (long long)a.n_chunk * Kmax * L) return;
+  const int l = (int)(idx % L);
+  const int k = (int)((idx / L) % Kmax);
+  const int p = (int)(idx / ((long long)L * Kmax));
+  const int gp = a.p_begin + p;
+  if (a.pv.status[p] != 0 || a.n_clouds[gp] == 0 || k >= a.b.n_layers[gp]) return;
+  R* rec = a.LB + ((size_t)p * Kmax + k) * NE * L + l;
+  const CloudyColumn c = column_inputs(a, p, gp, l);
+  StreamSet<NZ, double> S;
+  if (int rc = stream_set<NZ, double>(c.nleg, c.mu_sensor, a.lut.nleg, c_gauss, S)) {
+    rec[0] = R(-rc);
+    return;
+  }
+  Mat<NZ, R> Tm, Rm;
+  R src[NZ], od;
+  const double gas = double(a.TAU[((size_t)p * Kmax + k) * L + l]);
+  const int kind = layer_optics<NZ, R>(c, a.lut, S, k, gas, &od, Tm, Rm, src);
+  rec[0] = R(kind);
+  rec[(size_t)L] = od;
+  if (kind != 1) return;
+  const int nZ = S.nZ;
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) {
+      rec[(size_t)(2 + i * NZ + j) * L] = Tm.a[i][j];
+      rec[(size_t)(2 + NZ * NZ + i * NZ + j) * L] = Rm.a[i][j];
+    }
+  for (int i = 0; i < nZ; i++) rec[(size_t)(2 + 2 * NZ * NZ + i) * L] = src[i];
+}
+
+template <int NZ, class R>
+__global__ void __launch_bounds__(SCATTER_THREADS) scatter_adding_kernel(ScatterArgs<R> a) {
+  constexpr int NE = layer_record<NZ>();
   const int L = a.L, Kmax = a.Kmax;
   const int p = blockIdx.y, gp = a.p_begin + p;
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
-  const int st = a.pv.status[p];
-  const int Ku = a.b.n_layers[gp];
-  const int nc = a.n_clouds[gp];
-  // largest effective radius of the profile's clouds (stream rule input)
-  if (threadIdx.x == 0) s_maxreff = 0.0;
-  __syncthreads();
-  if (st == 0 && nc > 0) {
-    double mr = 0.0;
-    const double* rp = a.reff + (size_t)gp * a.max_clouds * Kmax;
-    for (int i = threadIdx.x; i < nc * Ku; i += blockDim.x) {
-      const double r = rp[(size_t)(i / Ku) * Kmax + (i % Ku)];
-      mr = r > mr ? r : mr;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      const double v = __shfl_xor_sync(FULL, mr, o);
-      mr = v > mr ? v : mr;
-    }
-    if ((threadIdx.x & 31) == 0 && mr > 0.0) {
-      // non-negative doubles order like their bit patterns
-      atomicMax(reinterpret_cast<unsigned long long*>(&s_maxreff), (unsigned long long)__double_as_longlong(mr));
-    }
-  }
-  __syncthreads();
   if (l >= L) return;
   const size_t pl = (size_t)gp * L + l;
-  if (st != 0) {
+  if (a.pv.status[p] != 0) {
     a.radiance[pl] = 0.0;
     a.bt[pl] = 0.0;
     return;
   }
-  const double c1 = a.sp.c1[l], c2 = a.sp.c2[l], b1 = a.sp.b1[l], b2 = a.sp.b2[l];
-  const double e = a.b.emissivity[pl];
-  const double ts = a.b.land_cov[gp] * a.b.land_t[gp] + a.b.water_cov[gp] * a.b.water_t[gp] +
-                    a.b.snow_cov[gp] * a.b.snow_t[gp] + a.b.ice_cov[gp] * a.b.ice_t[gp];
-  const double Bs = c1 / (exp(c2 / (b1 + b2 * ts)) - 1.0);
-  const double mu = a.pv.scal[(size_t)p * 4 + 1];
-  const double* tu = a.b.temperature + (size_t)gp * Kmax;
+  const CloudyColumn c = column_inputs(a, p, gp, l);
   const R* tau = a.TAU + (size_t)p * Kmax * L + l;
   double rad = 0.0;
   int code = 0;
-  if (nc == 0) {   // clear profile: Emission solver, in FP64 here
-    const double inv_u = 1.0 / mu;
-    double down = a.sp.cbr[l], tr_tot = 1.0, src = 0.0;
-    for (int k = 0; k < Ku; k++) {
+  if (c.n_clouds == 0) {   // clear profile: Emission solver, FP64 here
+    const double inv_u = 1.0 / c.mu_sensor;
+    double down = c.cosmic, tr_tot = 1.0, src = 0.0;
+    for (int k = 0; k < c.Ku; k++) {
       const double t = exp(-double(tau[(size_t)k * L]) * inv_u);
-      const double B = c1 / (exp(c2 / (b1 + b2 * tu[k])) - 1.0);
+      const double B = c.c1 / (exp(c.c2 / (c.b1 + c.b2 * c.temperature[k])) - 1.0);
       src += tr_tot * B * (1.0 - t);
       down = down * t + B * (1.0 - t);
       tr_tot *= t;
     }
-    rad = src + tr_tot * (e * Bs + (1.0 - e) * down);
+    rad = src + tr_tot * (c.emissivity * c.planck_surface + (1.0 - c.emissivity) * down);
   } else {
-    CloudyColumn c;
-    c.Ku = Ku;
-    c.n_clouds = nc;
-    const int ns = a.n_streams ? a.n_streams[gp] : 0;
-    c.nleg = ns > 0 ? ns : stream_rule_nleg(s_maxreff, a.sp.wn[l]);
-    c.microwave = a.microwave != 0;
-    c.freq = a.microwave ? a.sp.freq[l] : a.sp.wn[l];
-    c.mu_sensor = mu;
-    c.emissivity = e;
-    c.planck_surface = Bs;
-    c.cosmic = a.sp.cbr[l];
-    c.c1 = c1; c.c2 = c2; c.b1 = b1; c.b2 = b2;
-    c.temperature = tu;
-    c.cloud_type = a.cloud_type + (size_t)gp * a.max_clouds;
-    c.wc = a.wc + (size_t)gp * a.max_clouds * Kmax;
-    c.reff = a.reff + (size_t)gp * a.max_clouds * Kmax;
-    c.cstride = (size_t)Kmax;
-    code = cloudy_radiance<NZ>(c, a.lut, c_gauss, [&](int k) { return double(tau[(size_t)k * L]); }, &rad);
+    StreamSet<NZ, double> S;
+    code = stream_set<NZ, double>(c.nleg, c.mu_sensor, a.lut.nleg, c_gauss, S);
+    if (!code) {
+      const int nZ = S.nZ;
+      AddingState<NZ> A;
+      adding_init<NZ>(A, nZ, c.emissivity, c.planck_surface);
+      Mat<NZ, double> Tm, Rm;
+      double src[NZ];
+      for (int k = c.Ku - 1; k >= 0 && !code; k--) {
+        const R* rec = a.LB + ((size_t)p * Kmax + k) * NE * L + l;
+        const int kind = (int)rec[0];
+        const double od = double(rec[(size_t)L]);
+        if (kind < 0) { code = -kind; break; }
+        if (kind == 1) {
+          for (int i = 0; i < nZ; i++)
+            for (int j = 0; j < nZ; j++) {
+              Tm.a[i][j] = double(rec[(size_t)(2 + i * NZ + j) * L]);
+              Rm.a[i][j] = double(rec[(size_t)(2 + NZ * NZ + i * NZ + j) * L]);
+            }
+          for (int i = 0; i < nZ; i++) src[i] = double(rec[(size_t)(2 + 2 * NZ * NZ + i) * L]);
+          if (!adding_scatter<NZ>(A, nZ, Tm, Rm, src)) code = 6;
+        } else {
+          const double tk = c.temperature[k];
+          adding_clear<NZ>(A, nZ, S.mu, od, c.c1 / (exp(c.c2 / (c.b1 + c.b2 * tk)) - 1.0));
+        }
+      }
+      if (!code) rad = adding_toa<NZ>(A, nZ, S.isat, c.cosmic);
+    }
   }
   if (code) {
     atomicCAS(a.error, 0, code);
@@ -116,7 +190,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_kernel(ScatterArgs<R>
     rad = 0.0;
   }
   a.radiance[pl] = rad;
-  a.bt[pl] = code ? 0.0 : planck_temperature(c1, c2, b1, b2, rad);
+  a.bt[pl] = code ? 0.0 : planck_temperature(c.c1, c.c2, c.b1, c.b2, rad);
 }
 
 }  // namespace crtm

@@ -161,49 +161,49 @@ CRTM_HD bool cloud_layer_optics(const CloudLut& C, bool microwave, double freq, 
 }
 
 // ---- small dense matrices (row-major, fixed capacity NZ x NZ) --------------
-template <int NZ>
+template <int NZ, class T>
 struct Mat {
-  double a[NZ][NZ];
+  T a[NZ][NZ];
 };
 
-template <int NZ>
-CRTM_HD void mat_mul(int n, const Mat<NZ>& A, const Mat<NZ>& B, Mat<NZ>& C) {
+template <int NZ, class T>
+CRTM_HD void mat_mul(int n, const Mat<NZ, T>& A, const Mat<NZ, T>& B, Mat<NZ, T>& C) {
   for (int i = 0; i < n; i++)
     for (int j = 0; j < n; j++) {
-      double s = 0.0;
+      T s = T(0.0);
       for (int k = 0; k < n; k++) s += A.a[i][k] * B.a[k][j];
       C.a[i][j] = s;
     }
 }
 
 // In-place inverse by Gauss-Jordan elimination with partial pivoting.
-template <int NZ>
-CRTM_HD bool mat_invert(int n, Mat<NZ>& A) {
+template <int NZ, class T>
+CRTM_HD bool mat_invert(int n, Mat<NZ, T>& A) {
   int perm[NZ];
   for (int i = 0; i < n; i++) perm[i] = i;
   for (int k = 0; k < n; k++) {
     int p = k;
-    double best = fabs(A.a[k][k]);
+    T best = fabs(A.a[k][k]);
     for (int i = k + 1; i < n; i++)
       if (fabs(A.a[i][k]) > best) { best = fabs(A.a[i][k]); p = i; }
-    if (!(best > 1.0e-40)) return false;
+    if (!(best > T(1.0e-40))) return false;
     if (p != k) {
-      for (int j = 0; j < n; j++) { const double t = A.a[p][j]; A.a[p][j] = A.a[k][j]; A.a[k][j] = t; }
+      for (int j = 0; j < n; j++) { const T t = A.a[p][j]; A.a[p][j] = A.a[k][j]; A.a[k][j] = t; }
       const int t = perm[p]; perm[p] = perm[k]; perm[k] = t;
     }
-    const double d = 1.0 / A.a[k][k];
+    const T d = T(1.0) / A.a[k][k];
     for (int j = 0; j < n; j++) A.a[k][j] *= d;
     A.a[k][k] = d;
     for (int i = 0; i < n; i++) {
       if (i == k) continue;
-      const double f = A.a[i][k];
-      if (f == 0.0) continue;
+      const T f = A.a[i][k];
+      if (f == T(0.0)) continue;
       for (int j = 0; j < n; j++) A.a[i][j] -= f * A.a[k][j];
       A.a[i][k] = -f * d;
     }
   }
   // undo the row interchanges as column interchanges of the inverse
-  double tmp[NZ];
+  T tmp[NZ];
   for (int i = 0; i < n; i++) {
     for (int j = 0; j < n; j++) tmp[perm[j]] = A.a[i][j];
     for (int j = 0; j < n; j++) A.a[i][j] = tmp[j];
@@ -212,36 +212,36 @@ CRTM_HD bool mat_invert(int n, Mat<NZ>& A) {
 }
 
 // Symmetric eigenproblem S = V diag(lam) V^T by cyclic Jacobi rotations.
-template <int NZ>
-CRTM_HD void jacobi(int n, Mat<NZ>& S, double* lam, Mat<NZ>& V) {
+template <int NZ, class T>
+CRTM_HD void jacobi(int n, Mat<NZ, T>& S, T* lam, Mat<NZ, T>& V) {
   for (int i = 0; i < n; i++)
-    for (int j = 0; j < n; j++) V.a[i][j] = (i == j) ? 1.0 : 0.0;
+    for (int j = 0; j < n; j++) V.a[i][j] = (i == j) ? T(1.0) : T(0.0);
   for (int sweep = 0; sweep < 60; sweep++) {
-    double off = 0.0, diag = 0.0;
+    T off = T(0.0), diag = T(0.0);
     for (int i = 0; i < n; i++) {
       diag += S.a[i][i] * S.a[i][i];
       for (int j = i + 1; j < n; j++) off += S.a[i][j] * S.a[i][j];
     }
-    if (off <= 1.0e-32 * diag) break;
+    if (off <= T(1.0e-32) * diag) break;
     for (int p = 0; p < n - 1; p++)
       for (int q = p + 1; q < n; q++) {
-        const double apq = S.a[p][q];
-        if (apq == 0.0) continue;
-        const double th = (S.a[q][q] - S.a[p][p]) / (2.0 * apq);
-        const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        const T apq = S.a[p][q];
+        if (apq == T(0.0)) continue;
+        const T th = (S.a[q][q] - S.a[p][p]) / (T(2.0) * apq);
+        const T t = (th >= T(0.0) ? T(1.0) : -T(1.0)) / (fabs(th) + sqrt(th * th + T(1.0)));
+        const T c = T(1.0) / sqrt(t * t + T(1.0)), s = t * c;
         for (int k = 0; k < n; k++) {
-          const double kp = S.a[k][p], kq = S.a[k][q];
+          const T kp = S.a[k][p], kq = S.a[k][q];
           S.a[k][p] = c * kp - s * kq;
           S.a[k][q] = s * kp + c * kq;
         }
         for (int k = 0; k < n; k++) {
-          const double pk = S.a[p][k], qk = S.a[q][k];
+          const T pk = S.a[p][k], qk = S.a[q][k];
           S.a[p][k] = c * pk - s * qk;
           S.a[q][k] = s * pk + c * qk;
         }
         for (int k = 0; k < n; k++) {
-          const double kp = V.a[k][p], kq = V.a[k][q];
+          const T kp = V.a[k][p], kq = V.a[k][q];
           V.a[k][p] = c * kp - s * kq;
           V.a[k][q] = s * kp + c * kq;
         }
@@ -254,45 +254,45 @@ CRTM_HD void jacobi(int n, Mat<NZ>& S, double* lam, Mat<NZ>& V) {
 // MOM, azimuth order 0, no solar source): transmission T, reflection R and
 // the thermal source (identical up and down).  ff/bb are the normalised
 // forward/backward phase blocks.  Returns false on a failed factorisation.
-template <int NZ>
-CRTM_HD bool ada_layer(int nS, int nZ, double w, double tau, const double* mu,
-                              const double* wt, const Mat<NZ>& ff, const Mat<NZ>& bb, double B,
-                              Mat<NZ>& T, Mat<NZ>& R, double* src) {
-  if (tau < DELTA_OPTICAL_DEPTH) {   // thin layer: first-order scattering
-    const double s = tau * w;
+template <int NZ, class T>
+CRTM_HD bool ada_layer(int nS, int nZ, T w, T tau, const T* mu,
+                              const T* wt, const Mat<NZ, T>& ff, const Mat<NZ, T>& bb, T B,
+                              Mat<NZ, T>& Tm, Mat<NZ, T>& Rm, T* src) {
+  if (tau < T(DELTA_OPTICAL_DEPTH)) {   // thin layer: first-order scattering
+    const T s = tau * w;
     for (int i = 0; i < nZ; i++) {
-      const double c = s / mu[i];
-      double th = 0.0;
+      const T c = s / mu[i];
+      T th = T(0.0);
       for (int j = 0; j < nZ; j++) {
-        R.a[i][j] = c * bb.a[i][j] * wt[j];
-        T.a[i][j] = c * ff.a[i][j] * wt[j] + (i == j ? 1.0 - tau / mu[i] : 0.0);
-        th += R.a[i][j] + T.a[i][j];
+        Rm.a[i][j] = c * bb.a[i][j] * wt[j];
+        Tm.a[i][j] = c * ff.a[i][j] * wt[j] + (i == j ? T(1.0) - tau / mu[i] : T(0.0));
+        th += Rm.a[i][j] + Tm.a[i][j];
       }
-      src[i] = (1.0 - th) * B;
+      src[i] = (T(1.0) - th) * B;
     }
     return true;
   }
-  const double s = w < MAX_ALBEDO ? w : MAX_ALBEDO;
+  const T s = w < T(MAX_ALBEDO) ? w : T(MAX_ALBEDO);
   // symmetric form of the quadrature block
-  Mat<NZ> X, Y, V;
-  double lam[NZ], sq[NZ];
+  Mat<NZ, T> X, Y, V;
+  T lam[NZ], sq[NZ];
   for (int i = 0; i < nS; i++) sq[i] = sqrt(wt[i]);
   for (int i = 0; i < nS; i++)
     for (int j = 0; j < nS; j++) {
-      const double sw = s * sq[i] * sq[j], dd = 1.0 / sqrt(mu[i] * mu[j]);
-      const double id = (i == j) ? 1.0 : 0.0;
+      const T sw = s * sq[i] * sq[j], dd = T(1.0) / sqrt(mu[i] * mu[j]);
+      const T id = (i == j) ? T(1.0) : T(0.0);
       X.a[i][j] = (id - sw * (ff.a[i][j] - bb.a[i][j])) * dd;
       Y.a[i][j] = (id - sw * (ff.a[i][j] + bb.a[i][j])) * dd;
     }
   // Cholesky Y = L L^T (lower triangle of Y overwritten by L)
   for (int j = 0; j < nS; j++) {
-    double d = Y.a[j][j];
+    T d = Y.a[j][j];
     for (int k = 0; k < j; k++) d -= Y.a[j][k] * Y.a[j][k];
-    if (!(d > 0.0)) return false;
+    if (!(d > T(0.0))) return false;
     d = sqrt(d);
     Y.a[j][j] = d;
     for (int i = j + 1; i < nS; i++) {
-      double v = Y.a[i][j];
+      T v = Y.a[i][j];
       for (int k = 0; k < j; k++) v -= Y.a[i][k] * Y.a[j][k];
       Y.a[i][j] = v / d;
     }
@@ -300,14 +300,14 @@ CRTM_HD bool ada_layer(int nS, int nZ, double w, double tau, const double* mu,
   // S = L^T X L in V (temporary X L in T)
   for (int i = 0; i < nS; i++)
     for (int j = 0; j < nS; j++) {
-      double v = 0.0;
+      T v = T(0.0);
       for (int k = j; k < nS; k++) v += X.a[i][k] * Y.a[k][j];
-      T.a[i][j] = v;
+      Tm.a[i][j] = v;
     }
   for (int i = 0; i < nS; i++)
     for (int j = i; j < nS; j++) {
-      double v = 0.0;
-      for (int k = i; k < nS; k++) v += Y.a[k][i] * T.a[k][j];
+      T v = T(0.0);
+      for (int k = i; k < nS; k++) v += Y.a[k][i] * Tm.a[k][j];
       V.a[i][j] = v;
     }
   for (int i = 0; i < nS; i++)
@@ -316,119 +316,119 @@ CRTM_HD bool ada_layer(int nS, int nZ, double w, double tau, const double* mu,
   // E = W^-1/2 D^-1/2 L^-T u: eigenvectors of HH, in R
   for (int c = 0; c < nS; c++) {
     for (int i = nS - 1; i >= 0; i--) {
-      double v = X.a[i][c];
-      for (int k = i + 1; k < nS; k++) v -= Y.a[k][i] * R.a[k][c];
-      R.a[i][c] = v / Y.a[i][i];
+      T v = X.a[i][c];
+      for (int k = i + 1; k < nS; k++) v -= Y.a[k][i] * Rm.a[k][c];
+      Rm.a[i][c] = v / Y.a[i][i];
     }
-    for (int i = 0; i < nS; i++) R.a[i][c] /= sqrt(wt[i] * mu[i]);
+    for (int i = 0; i < nS; i++) Rm.a[i][c] /= sqrt(wt[i] * mu[i]);
   }
   // PP, PM for the full set of angles: PPM = PP - PM kept in X, PPP in Y
   for (int i = 0; i < nZ; i++) {
-    const double c = s / mu[i];
+    const T c = s / mu[i];
     for (int j = 0; j < nZ; j++) {
-      const double f = c * ff.a[i][j] * wt[j] - (i == j ? 1.0 / mu[i] : 0.0), b = c * bb.a[i][j] * wt[j];
+      const T f = c * ff.a[i][j] * wt[j] - (i == j ? T(1.0) / mu[i] : T(0.0)), b = c * bb.a[i][j] * wt[j];
       X.a[i][j] = f - b;
       Y.a[i][j] = f + b;
     }
   }
   if (nZ > nS) {   // sensor angle (weight 0): HH is block lower triangular
     const int z = nZ - 1;
-    double hz[NZ];
+    T hz[NZ];
     for (int k = 0; k < nZ; k++) {
-      double v = 0.0;
+      T v = T(0.0);
       for (int m = 0; m < nZ; m++) v += X.a[z][m] * Y.a[m][k];
       hz[k] = v;   // row z of HH
     }
     for (int c = 0; c < nS; c++) {
-      double v = 0.0;
-      for (int k = 0; k < nS; k++) v += hz[k] * R.a[k][c];
-      R.a[z][c] = v / (lam[c] - hz[z]);
+      T v = T(0.0);
+      for (int k = 0; k < nS; k++) v += hz[k] * Rm.a[k][c];
+      Rm.a[z][c] = v / (lam[c] - hz[z]);
     }
-    for (int i = 0; i < nS; i++) R.a[i][z] = 0.0;
-    R.a[z][z] = 1.0;
+    for (int i = 0; i < nS; i++) Rm.a[i][z] = T(0.0);
+    Rm.a[z][z] = T(1.0);
     lam[z] = hz[z];
   }
   // MOM with the eigenpairs (E in R, eigenvalues lam)
   if (!mat_invert(nZ, X)) return false;   // inverse of PP - PM
-  double ex[NZ];
+  T ex[NZ];
   for (int i = 0; i < nZ; i++) {
-    lam[i] = lam[i] > 0.0 ? sqrt(lam[i]) : 0.0;
+    lam[i] = lam[i] > T(0.0) ? sqrt(lam[i]) : T(0.0);
     ex[i] = exp(-lam[i] * tau);
   }
   // EF = (PP-PM)^-1 E diag(lam);  Gp = (E + EF)/2 in Y, Gm = (E - EF)/2 in V
   for (int i = 0; i < nZ; i++)
     for (int j = 0; j < nZ; j++) {
-      double v = 0.0;
-      for (int k = 0; k < nZ; k++) v += X.a[i][k] * R.a[k][j];
+      T v = T(0.0);
+      for (int k = 0; k < nZ; k++) v += X.a[i][k] * Rm.a[k][j];
       v *= lam[j];
-      Y.a[i][j] = 0.5 * (R.a[i][j] + v);
-      V.a[i][j] = 0.5 * (R.a[i][j] - v);
+      Y.a[i][j] = T(0.5) * (Rm.a[i][j] + v);
+      V.a[i][j] = T(0.5) * (Rm.a[i][j] - v);
     }
   // A2 = Gm^-1 A1 with A1 = Gp diag(ex)
   for (int i = 0; i < nZ; i++)
     for (int j = 0; j < nZ; j++) X.a[i][j] = V.a[i][j];
   if (!mat_invert(nZ, X)) return false;    // Gm^-1
-  Mat<NZ> A2;
+  Mat<NZ, T> A2;
   for (int i = 0; i < nZ; i++)
     for (int j = 0; j < nZ; j++) {
-      double v = 0.0;
+      T v = T(0.0);
       for (int k = 0; k < nZ; k++) v += X.a[i][k] * Y.a[k][j];
       A2.a[i][j] = v * ex[j];
     }
   // Gm - A1 A2 in X;  T <- (Gm diag(ex) - Gp A2), R <- (Gp - Gm diag(ex) A2)
   for (int i = 0; i < nZ; i++)
     for (int j = 0; j < nZ; j++) {
-      double a5 = 0.0, a3 = 0.0, a6 = 0.0;
+      T a5 = T(0.0), a3 = T(0.0), a6 = T(0.0);
       for (int k = 0; k < nZ; k++) {
         a5 += Y.a[i][k] * ex[k] * A2.a[k][j];
         a3 += Y.a[i][k] * A2.a[k][j];
         a6 += V.a[i][k] * ex[k] * A2.a[k][j];
       }
       X.a[i][j] = V.a[i][j] - a5;
-      T.a[i][j] = V.a[i][j] * ex[j] - a3;
-      R.a[i][j] = Y.a[i][j] - a6;
+      Tm.a[i][j] = V.a[i][j] * ex[j] - a3;
+      Rm.a[i][j] = Y.a[i][j] - a6;
     }
   if (!mat_invert(nZ, X)) return false;    // (Gm - A5)^-1
-  Mat<NZ> tmp;
-  mat_mul(nZ, T, X, tmp);
-  mat_mul(nZ, R, X, V);
+  Mat<NZ, T> tmp;
+  mat_mul(nZ, Tm, X, tmp);
+  mat_mul(nZ, Rm, X, V);
   for (int i = 0; i < nZ; i++)
-    for (int j = 0; j < nZ; j++) { T.a[i][j] = tmp.a[i][j]; R.a[i][j] = V.a[i][j]; }
+    for (int j = 0; j < nZ; j++) { Tm.a[i][j] = tmp.a[i][j]; Rm.a[i][j] = V.a[i][j]; }
   for (int i = 0; i < nZ; i++) {
-    double th = 0.0;
-    for (int j = 0; j < nS; j++) th += T.a[i][j] + R.a[i][j];
-    if (i == nZ - 1 && nZ == nS + 1) th += T.a[i][i];
-    src[i] = (1.0 - th) * B;
+    T th = T(0.0);
+    for (int j = 0; j < nS; j++) th += Tm.a[i][j] + Rm.a[i][j];
+    if (i == nZ - 1 && nZ == nS + 1) th += Tm.a[i][i];
+    src[i] = (T(1.0) - th) * B;
   }
   return true;
 }
 
 // Forward/backward phase blocks of one layer from its Legendre terms
 // (CRTM_Phase_Matrix, m = 0) and their normalisation (Normalize_Phase).
-template <int NZ>
-CRTM_HD void phase_blocks(int nS, int nZ, int nleg, const double* pc, const double (*P)[SC_NLEG_MAX + 1],
-                                 const double* wt, Mat<NZ>& ff, Mat<NZ>& bb) {
+template <int NZ, class T>
+CRTM_HD void phase_blocks(int nS, int nZ, int nleg, const T* pc, const T (*P)[SC_NLEG_MAX + 1],
+                                 const T* wt, Mat<NZ, T>& ff, Mat<NZ, T>& bb) {
   for (int i = 0; i < nZ; i++)
     for (int j = i; j < nZ; j++) {
-      double f = 0.0, b = 0.0;
+      T f = T(0.0), b = T(0.0);
       for (int l = 0; l < nleg; l++) {
-        const double t = pc[l] * P[i][l] * P[j][l];
+        const T t = pc[l] * P[i][l] * P[j][l];
         f += t;
         b += (l & 1) ? -t : t;
       }
-      ff.a[i][j] = ff.a[j][i] = f < 0.0 ? PHASE_THRESHOLD : f;
-      bb.a[i][j] = bb.a[j][i] = b < 0.0 ? PHASE_THRESHOLD : b;
+      ff.a[i][j] = ff.a[j][i] = f < T(0.0) ? T(PHASE_THRESHOLD) : f;
+      bb.a[i][j] = bb.a[j][i] = b < T(0.0) ? T(PHASE_THRESHOLD) : b;
     }
-  double carried = 0.0;
+  T carried = T(0.0);
   for (int i = 0; i < nS; i++) {
-    double nf = 0.0;
+    T nf = T(0.0);
     for (int j = i; j < nZ; j++) nf += (ff.a[i][j] + bb.a[i][j]) * wt[j];
-    const double sc = (1.0 - carried) / nf;
+    const T sc = (T(1.0) - carried) / nf;
     for (int j = i; j < nZ; j++) {
       ff.a[i][j] *= sc; bb.a[i][j] *= sc;
       ff.a[j][i] = ff.a[i][j]; bb.a[j][i] = bb.a[i][j];
     }
-    carried = 0.0;
+    carried = T(0.0);
     if (i + 1 < nZ)
       for (int j = 0; j <= i; j++) carried += (ff.a[i + 1][j] + bb.a[i + 1][j]) * wt[j];
   }
@@ -455,121 +455,203 @@ struct CloudyColumn {
   size_t cstride;
 };
 
-// TOA radiance at the sensor angle of one cloudy (profile, channel) by the
-// adding method from the surface; gas layer ODs come from od(k).  Returns 0
-// or an error code.
+// Stream angles of a (profile, channel): Gauss angles of the stream set plus
+// the sensor angle with weight 0 unless it is one of them (Assign_Common_Input),
+// and Legendre polynomials P_l(mu_i), l = 0..nleg (Legendre_M, m = 0).
+template <int NZ, class T>
+struct StreamSet {
+  int nleg, loff, nS, nZ, isat;
+  T mu[NZ], wt[NZ];
+  T P[NZ][SC_NLEG_MAX + 1];
+};
+
+// Returns 0 or an error code (1-3: stream set does not fit).
+template <int NZ, class T>
+CRTM_HD int stream_set(int nleg, double mu_sensor, int lut_nleg, const GaussTable& gt, StreamSet<NZ, T>& S) {
+  S.nleg = nleg;
+  S.loff = legendre_offset(nleg);
+  if (S.loff < 0 || nleg > SC_NLEG_MAX) return 1;
+  if (lut_nleg < nleg + S.loff) return 2;
+  S.nS = (nleg + 2) / 2;
+  if (S.nS + 1 > NZ || S.nS > 9) return 3;
+  S.nZ = S.nS;
+  S.isat = -1;
+  for (int i = 0; i < S.nS; i++) {
+    S.mu[i] = T(gt.mu[S.nS][i]);
+    S.wt[i] = T(gt.w[S.nS][i]);
+    if (S.isat < 0 && fabs(gt.mu[S.nS][i] - mu_sensor) < ANGLE_THRESHOLD) S.isat = i;
+  }
+  if (S.isat < 0) { S.nZ = S.nS + 1; S.isat = S.nS; S.mu[S.nS] = T(mu_sensor); S.wt[S.nS] = T(0); }
+  for (int i = 0; i < S.nZ; i++) {
+    S.P[i][0] = T(1);
+    if (nleg > 0) S.P[i][1] = S.mu[i];
+    for (int j = 1; j < nleg; j++)
+      S.P[i][j + 1] = (T(2 * j + 1) * S.mu[i] * S.P[i][j] - T(j) * S.P[i][j - 1]) / T(j + 1);
+  }
+  return 0;
+}
+
+// Optics of layer k for the adding method: cloud optics summed over the
+// clouds, combine and delta truncation, and for a scattering layer the
+// phase blocks and the layer's transmission, reflection and source
+// (ada_layer).  Returns 1 for a scattering layer, 0 for a clear one (od is
+// then the layer optical depth), negative on failure.
+template <int NZ, class T>
+CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const StreamSet<NZ, double>& S, int k,
+                         double gas_od, T* od_out, Mat<NZ, T>& Tm, Mat<NZ, T>& Rm, T* src) {
+  const int nleg = S.nleg;
+  double od = gas_od, bs_sum = 0.0;
+  double pc[SC_NLEG_MAX + 1], pcs[SC_NLEG_MAX + 1];
+  for (int l = 0; l <= nleg; l++) pcs[l] = 0.0;
+  const double tk = in.temperature[k];
+  for (int c = 0; c < in.n_clouds; c++) {
+    const double wc = in.wc[c * in.cstride + k];
+    if (!(wc > WATER_CONTENT_THRESHOLD)) continue;
+    double ke, w;
+    if (!cloud_layer_optics(lut, in.microwave, in.freq, in.cloud_type[c], in.reff[c * in.cstride + k], tk,
+                            nleg, S.loff, &ke, &w, pc))
+      return -4;
+    if (ke <= 0.0) { ke = 0.0; w = 0.0; }
+    if (w <= 0.0) { w = 0.0; for (int l = 0; l <= nleg; l++) pc[l] = 0.0; }
+    if (w >= 1.0) w = 1.0;
+    od += ke * wc;
+    const double bs = wc * ke * w;
+    bs_sum += bs;
+    for (int l = 1; l <= nleg; l++) pcs[l] += pc[l] * bs;
+  }
+  double ssa = bs_sum;
+  if (bs_sum > BS_THRESHOLD) {   // CRTM_AtmOptics_Combine
+    const double w = bs_sum / od;
+    for (int l = 1; l <= nleg; l++) pcs[l] /= bs_sum;
+    pcs[0] = 0.5;
+    const double f = pcs[nleg];
+    od = (1.0 - f * w) * od;
+    ssa = (1.0 - f) * w / (1.0 - f * w);
+  }
+  *od_out = T(od);
+  if (!(ssa > BS_THRESHOLD)) return 0;
+  // Phase blocks and MOM in FP64 in every form: MOM's three inversions and
+  // its eigenvectors lose accuracy in FP32 for thick, highly scattering
+  // layers.  Only the stored layer record is in T.
+  Mat<NZ, double> ff, bb, Td, Rd;
+  double mu[NZ], wt[NZ], P[NZ][SC_NLEG_MAX + 1], srcd[NZ];
+  for (int i = 0; i < S.nZ; i++) {
+    mu[i] = double(S.mu[i]);
+    wt[i] = double(S.wt[i]);
+    for (int l = 0; l <= nleg; l++) P[i][l] = double(S.P[i][l]);
+  }
+  phase_blocks<NZ, double>(S.nS, S.nZ, nleg, pcs, P, wt, ff, bb);
+  double mx = 0.0;
+  for (int i = 0; i < S.nZ; i++)
+    for (int j = 0; j < S.nZ; j++) mx = fabs(ff.a[i][j]) > mx ? fabs(ff.a[i][j]) : mx;
+  if (!(mx > 0.0)) return 0;
+  const double B = in.c1 / (exp(in.c2 / (in.b1 + in.b2 * tk)) - 1.0);
+  if (!ada_layer<NZ, double>(S.nS, S.nZ, ssa, od, mu, wt, ff, bb, B, Td, Rd, srcd)) return -5;
+  for (int i = 0; i < S.nZ; i++) {
+    src[i] = T(srcd[i]);
+    for (int j = 0; j < S.nZ; j++) { Tm.a[i][j] = T(Td.a[i][j]); Rm.a[i][j] = T(Rd.a[i][j]); }
+  }
+  return 1;
+}
+
+// Adding state: reflectivity of everything below the current level (Rup) and
+// upwelling radiance there (rad), FP64 in every form.
+template <int NZ>
+struct AddingState {
+  Mat<NZ, double> Rup;
+  double rad[NZ];
+};
+
+template <int NZ>
+CRTM_HD void adding_init(AddingState<NZ>& A, int nZ, double emissivity, double planck_surface) {
+  for (int i = 0; i < nZ; i++) {
+    for (int j = 0; j < nZ; j++) A.Rup.a[i][j] = 0.0;
+    A.Rup.a[i][i] = 1.0 - emissivity;
+    A.rad[i] = emissivity * planck_surface;
+  }
+}
+
+// Clear layer: diagonal transmission exp(-od/mu_i), source B (1 - t_i).
+template <int NZ>
+CRTM_HD void adding_clear(AddingState<NZ>& A, int nZ, const double* mu, double od, double B) {
+  double tr[NZ], src[NZ], tmp[NZ];
+  for (int i = 0; i < nZ; i++) {
+    tr[i] = exp(-od / mu[i]);
+    src[i] = B * (1.0 - tr[i]);
+  }
+  for (int i = 0; i < nZ; i++) {
+    double v = A.rad[i];
+    for (int j = 0; j < nZ; j++) v += A.Rup.a[i][j] * src[j];
+    tmp[i] = src[i] + tr[i] * v;
+  }
+  for (int i = 0; i < nZ; i++) {
+    A.rad[i] = tmp[i];
+    for (int j = 0; j < nZ; j++) A.Rup.a[i][j] *= tr[i] * tr[j];
+  }
+}
+
+// Scattering layer (ADA_Module.f90:169-190): Gamma = (I - Rup R)^-1,
+// rad <- src + T Gamma (Rup src + rad),  Rup <- R + T Gamma Rup T.
+template <int NZ>
+CRTM_HD bool adding_scatter(AddingState<NZ>& A, int nZ, const Mat<NZ, double>& Tm, const Mat<NZ, double>& Rm,
+                            const double* src) {
+  Mat<NZ, double> G, IGT;
+  double tmp[NZ];
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) {
+      double v = 0.0;
+      for (int m = 0; m < nZ; m++) v += A.Rup.a[i][m] * Rm.a[m][j];
+      G.a[i][j] = (i == j ? 1.0 : 0.0) - v;
+    }
+  if (!mat_invert<NZ, double>(nZ, G)) return false;
+  mat_mul<NZ, double>(nZ, Tm, G, IGT);
+  for (int i = 0; i < nZ; i++) {
+    double v = A.rad[i];
+    for (int j = 0; j < nZ; j++) v += A.Rup.a[i][j] * src[j];
+    tmp[i] = v;
+  }
+  for (int i = 0; i < nZ; i++) {
+    double v = src[i];
+    for (int j = 0; j < nZ; j++) v += IGT.a[i][j] * tmp[j];
+    A.rad[i] = v;
+  }
+  mat_mul<NZ, double>(nZ, A.Rup, Tm, G);    // Rup T
+  mat_mul<NZ, double>(nZ, IGT, G, A.Rup);   // T Gamma Rup T
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) A.Rup.a[i][j] += Rm.a[i][j];
+  return true;
+}
+
+template <int NZ>
+CRTM_HD double adding_toa(const AddingState<NZ>& A, int nZ, int isat, double cosmic) {
+  double s = 0.0;
+  for (int j = 0; j < nZ; j++) s += A.Rup.a[isat][j];
+  return A.rad[isat] + s * cosmic;
+}
+
+// The whole (profile, channel) in one pass, FP64 (the layer-parallel GPU
+// kernels split it into layer_optics for every layer, then the adding).
 template <int NZ, class OdFn>
 CRTM_HD int cloudy_radiance(const CloudyColumn& in, const CloudLut& lut, const GaussTable& gt,
-                                   OdFn od_of, double* radiance) {
-  const int nleg = in.nleg, loff = legendre_offset(nleg);
-  if (loff < 0 || nleg > SC_NLEG_MAX) return 1;
-  if (lut.nleg < nleg + loff) return 2;
-  const int nS = (nleg + 2) / 2;
-  if (nS + 1 > NZ || nS > 9) return 3;
-  double mu[NZ], wt[NZ];
-  for (int i = 0; i < nS; i++) { mu[i] = gt.mu[nS][i]; wt[i] = gt.w[nS][i]; }
-  int nZ = nS, isat = -1;
-  for (int i = 0; i < nS; i++)
-    if (fabs(mu[i] - in.mu_sensor) < ANGLE_THRESHOLD) { isat = i; break; }
-  if (isat < 0) { nZ = nS + 1; isat = nS; mu[nS] = in.mu_sensor; wt[nS] = 0.0; }
-  double P[NZ][SC_NLEG_MAX + 1];
-  for (int i = 0; i < nZ; i++) {   // Legendre_M, m = 0
-    P[i][0] = 1.0;
-    if (nleg > 0) P[i][1] = mu[i];
-    for (int j = 1; j < nleg; j++) P[i][j + 1] = ((2 * j + 1) * mu[i] * P[i][j] - j * P[i][j - 1]) / (j + 1);
-  }
-  Mat<NZ> Rup, T, R, ff, bb;
-  double rad[NZ], src[NZ], tmp[NZ];
-  for (int i = 0; i < nZ; i++) {
-    for (int j = 0; j < nZ; j++) Rup.a[i][j] = 0.0;
-    Rup.a[i][i] = 1.0 - in.emissivity;
-    rad[i] = in.emissivity * in.planck_surface;
-  }
-  double pc[SC_NLEG_MAX + 1], pcs[SC_NLEG_MAX + 1];
+                            OdFn od_of, double* radiance) {
+  StreamSet<NZ, double> S;
+  if (int rc = stream_set<NZ, double>(in.nleg, in.mu_sensor, lut.nleg, gt, S)) return rc;
+  AddingState<NZ> A;
+  adding_init<NZ>(A, S.nZ, in.emissivity, in.planck_surface);
+  Mat<NZ, double> Tm, Rm;
+  double src[NZ];
   for (int k = in.Ku - 1; k >= 0; k--) {
-    // layer optics: gas OD plus every cloud's OD, scattering and phase sums
-    double od = od_of(k), bs_sum = 0.0;
-    for (int l = 0; l <= nleg; l++) pcs[l] = 0.0;
-    const double tk = in.temperature[k];
-    for (int c = 0; c < in.n_clouds; c++) {
-      const double wc = in.wc[c * in.cstride + k];
-      if (!(wc > WATER_CONTENT_THRESHOLD)) continue;
-      double ke, w;
-      if (!cloud_layer_optics(lut, in.microwave, in.freq, in.cloud_type[c], in.reff[c * in.cstride + k], tk,
-                              nleg, loff, &ke, &w, pc))
-        return 4;
-      if (ke <= 0.0) { ke = 0.0; w = 0.0; }
-      if (w <= 0.0) { w = 0.0; for (int l = 0; l <= nleg; l++) pc[l] = 0.0; }
-      if (w >= 1.0) w = 1.0;
-      od += ke * wc;
-      const double bs = wc * ke * w;
-      bs_sum += bs;
-      for (int l = 1; l <= nleg; l++) pcs[l] += pc[l] * bs;
-    }
-    double ssa = bs_sum;
-    if (bs_sum > BS_THRESHOLD) {   // combine and delta truncation
-      const double w = bs_sum / od;
-      for (int l = 1; l <= nleg; l++) pcs[l] /= bs_sum;
-      pcs[0] = 0.5;
-      const double f = pcs[nleg];
-      od = (1.0 - f * w) * od;
-      ssa = (1.0 - f) * w / (1.0 - f * w);
-    }
-    const double te = in.b1 + in.b2 * tk;
-    const double B = in.c1 / (exp(in.c2 / te) - 1.0);
-    bool scat = false;
-    if (ssa > BS_THRESHOLD) {
-      phase_blocks<NZ>(nS, nZ, nleg, pcs, P, wt, ff, bb);
-      double mx = 0.0;
-      for (int i = 0; i < nZ; i++)
-        for (int j = 0; j < nZ; j++) mx = fabs(ff.a[i][j]) > mx ? fabs(ff.a[i][j]) : mx;
-      scat = mx > 0.0;
-    }
-    if (scat) {
-      if (!ada_layer<NZ>(nS, nZ, ssa, od, mu, wt, ff, bb, B, T, R, src)) return 5;
-      // Gamma = (I - Rup R)^-1 in ff; IGT = T Gamma in bb
-      for (int i = 0; i < nZ; i++)
-        for (int j = 0; j < nZ; j++) {
-          double v = 0.0;
-          for (int m = 0; m < nZ; m++) v += Rup.a[i][m] * R.a[m][j];
-          ff.a[i][j] = (i == j ? 1.0 : 0.0) - v;
-        }
-      if (!mat_invert(nZ, ff)) return 6;
-      mat_mul(nZ, T, ff, bb);
-      for (int i = 0; i < nZ; i++) {
-        double v = rad[i];
-        for (int j = 0; j < nZ; j++) v += Rup.a[i][j] * src[j];
-        tmp[i] = v;
-      }
-      for (int i = 0; i < nZ; i++) {
-        double v = src[i];
-        for (int j = 0; j < nZ; j++) v += bb.a[i][j] * tmp[j];
-        rad[i] = v;
-      }
-      mat_mul(nZ, Rup, T, ff);       // Rup T
-      mat_mul(nZ, bb, ff, Rup);      // IGT Rup T
-      for (int i = 0; i < nZ; i++)
-        for (int j = 0; j < nZ; j++) Rup.a[i][j] += R.a[i][j];
+    double od;
+    const int kind = layer_optics<NZ, double>(in, lut, S, k, od_of(k), &od, Tm, Rm, src);
+    if (kind < 0) return -kind;
+    if (kind == 1) {
+      if (!adding_scatter<NZ>(A, S.nZ, Tm, Rm, src)) return 6;
     } else {
-      double tr[NZ];
-      for (int i = 0; i < nZ; i++) {
-        tr[i] = exp(-od / mu[i]);
-        src[i] = B * (1.0 - tr[i]);
-      }
-      for (int i = 0; i < nZ; i++) {
-        double v = rad[i];
-        for (int j = 0; j < nZ; j++) v += Rup.a[i][j] * src[j];
-        tmp[i] = src[i] + tr[i] * v;
-      }
-      for (int i = 0; i < nZ; i++) {
-        rad[i] = tmp[i];
-        for (int j = 0; j < nZ; j++) Rup.a[i][j] *= tr[i] * tr[j];
-      }
+      const double tk = in.temperature[k];
+      adding_clear<NZ>(A, S.nZ, S.mu, od, in.c1 / (exp(in.c2 / (in.b1 + in.b2 * tk)) - 1.0));
     }
   }
-  double s = 0.0;
-  for (int j = 0; j < nZ; j++) s += Rup.a[isat][j];
-  *radiance = rad[isat] + s * in.cosmic;
+  *radiance = adding_toa<NZ>(A, S.nZ, S.isat, in.cosmic);
   return 0;
 }
 

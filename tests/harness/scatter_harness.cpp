@@ -18,10 +18,10 @@ extern "C" {
 
 int sx_ada_layer(int nS, int nZ, double w, double tau, const double* mu, const double* wt,
                  const double* ff, const double* bb, double B, double* T, double* R, double* src) {
-  Mat<SC_NZ_MAX> F, Bm, Tm, Rm;
+  Mat<SC_NZ_MAX, double> F, Bm, Tm, Rm;
   for (int i = 0; i < nZ; i++)
     for (int j = 0; j < nZ; j++) { F.a[i][j] = ff[i * nZ + j]; Bm.a[i][j] = bb[i * nZ + j]; }
-  if (!ada_layer<SC_NZ_MAX>(nS, nZ, w, tau, mu, wt, F, Bm, B, Tm, Rm, src)) return 1;
+  if (!ada_layer<SC_NZ_MAX, double>(nS, nZ, w, tau, mu, wt, F, Bm, B, Tm, Rm, src)) return 1;
   for (int i = 0; i < nZ; i++)
     for (int j = 0; j < nZ; j++) { T[i * nZ + j] = Tm.a[i][j]; R[i * nZ + j] = Rm.a[i][j]; }
   return 0;
