@@ -52,7 +52,7 @@ class CBatch(ct.Structure):
                 ("surface_altitude", ct.c_void_p), ("emissivity", ct.c_void_p),
                 ("max_clouds", ct.c_int), ("n_clouds", ct.c_void_p), ("cloud_type", ct.c_void_p),
                 ("cloud_water_content", ct.c_void_p), ("cloud_effective_radius", ct.c_void_p),
-                ("n_streams", ct.c_void_p)]
+                ("n_streams", ct.c_void_p), ("rt_algorithm_id", ct.c_void_p)]
 
 
 class CRTSolution(ct.Structure):
@@ -209,6 +209,8 @@ class CRTM:
         if opt.n_streams is not None:
             use = opt.use_n_streams if opt.use_n_streams is not None else np.ones(atm.n_profiles, bool)
             b.n_streams = c(np.where(use, opt.n_streams, 0), np.int32)
+        if opt.rt_algorithm_id is not None:
+            b.rt_algorithm_id = c(opt.rt_algorithm_id, np.int32)
         return b
 
     def _check(self, rc: int) -> None:
@@ -281,7 +283,7 @@ class CRTM:
                   "water_temperature", "snow_temperature", "ice_temperature",
                   "sensor_zenith_angle", "source_zenith_angle", "surface_altitude", "emissivity",
                   "n_clouds", "cloud_type", "cloud_water_content", "cloud_effective_radius",
-                  "n_streams"):
+                  "n_streams", "rt_algorithm_id"):
             t = dev.get(f)
             setattr(b, f, None if t is None else t.data_ptr())
         if dev.get("cloud_type") is not None:

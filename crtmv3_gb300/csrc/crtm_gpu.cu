@@ -464,6 +464,7 @@ struct Work {
   double* TSK;      // adjoint: [n][L]
   R* RA;            // [n][nv][K][L]
   R* LB;            // cloudy forward: [n][Kmax][NE][L] layer records
+  double* FB;       // cloudy forward with SOI: [n][2][2][Kmax+1][NZ][L] fields
   double* maxreff;  // cloudy forward: [n]
   double* ras;      // adjoint: [n][nv][K]
   double* pts;      // adjoint: [n][Kmax]
@@ -482,7 +483,8 @@ template <> struct Tune<3, float> { static constexpr int FWD = 8, AD = 8; };
 template <int G, class R> constexpr int ad_profiles() { return Tune<G, R>::AD * AD_WARPS; }
 
 template <int G, class R>
-size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w, char* base) {
+size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w, char* base,
+                  bool soi_fields = false) {
   const int K = s.K, L = s.L, NS = s.NS, NX = DLayout<G>::NX;
   const int npf = Tune<G, R>::FWD, npa = Tune<G, R>::AD;
   size_t off = 0;
@@ -515,6 +517,9 @@ size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w
     wk.TAU = (R*)carve(nn * Kmax * L * sizeof(R));
     wk.LB = (R*)carve(nn * Kmax * (size_t)nv * L * sizeof(R));
     wk.maxreff = (double*)carve(nn * sizeof(double));
+    // SOI fields: 2 fields x 2 buffers x levels x angles (angles <= NZ <= record length)
+    const size_t nz = nv == 2 + 2 * SC_NZ_MAX * SC_NZ_MAX + SC_NZ_MAX ? SC_NZ_MAX : 5;
+    wk.FB = soi_fields ? (double*)carve(nn * 4 * (size_t)(Kmax + 1) * nz * L * sizeof(double)) : nullptr;
   }
   if (adj) {
     wk.TAU = (R*)carve(nn * Kmax * L * sizeof(R));
@@ -630,28 +635,29 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
   // cloudy forward: NZ angles of the kernels (16-stream option or the stream rule)
   const bool nz_max = mode == 3 && b->n_streams != nullptr;
   const int wnv = mode == 3 ? (nz_max ? layer_record<SC_NZ_MAX>() : layer_record<5>()) : nv;
+  const bool soi = mode == 3 && b->rt_algorithm_id != nullptr;
   // chunk size from the workspace budget
-  const size_t per = work_bytes<G, R>(s, 64, Kmax, wnv, mode, nullptr, nullptr) / 64 + 1;
+  const size_t per = work_bytes<G, R>(s, 64, Kmax, wnv, mode, nullptr, nullptr, soi) / 64 + 1;
   int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)P, h->workspace_budget / per));
   if (hc && hc->max_chunk > 0) chunk = std::min(chunk, hc->max_chunk);
   char* ws_base;
   if (fixed) {
     // largest chunk whose workspace fits the fixed scratch
     chunk = (int)std::min<size_t>((size_t)chunk, fixed->bytes / per);
-    while (chunk > 1 && work_bytes<G, R>(s, chunk, Kmax, wnv, mode, nullptr, nullptr) > fixed->bytes) chunk--;
-    const size_t one = work_bytes<G, R>(s, 1, Kmax, wnv, mode, nullptr, nullptr);
+    while (chunk > 1 && work_bytes<G, R>(s, chunk, Kmax, wnv, mode, nullptr, nullptr, soi) > fixed->bytes) chunk--;
+    const size_t one = work_bytes<G, R>(s, 1, Kmax, wnv, mode, nullptr, nullptr, soi);
     if (chunk < 1 || one > fixed->bytes)
       return fail(h, "one profile of this call needs %zu bytes of scratch (%d channels, max_layers %d, "
                      "%d absorber Jacobians); the static scratch holds %zu bytes",
                   one, L, Kmax, nv - 1, fixed->bytes);
     ws_base = fixed->base;
   } else {
-    const size_t need = work_bytes<G, R>(s, chunk, Kmax, wnv, mode, nullptr, nullptr);
+    const size_t need = work_bytes<G, R>(s, chunk, Kmax, wnv, mode, nullptr, nullptr, soi);
     if (!h->ws.ensure(need)) return fail(h, "cannot allocate %zu bytes of workspace", need);
     ws_base = (char*)h->ws.p;
   }
   Work<R> w;
-  work_bytes<G, R>(s, chunk, Kmax, wnv, mode, &w, ws_base);
+  work_bytes<G, R>(s, chunk, Kmax, wnv, mode, &w, ws_base, soi);
   if (cudaMemcpyAsync(w.idx_map, idx_map, sizeof(int) * s.Jm, cudaMemcpyHostToDevice, st) != cudaSuccess)
     return fail(h, "absorber map upload failed");
   const BatchView bv = make_view(b);
@@ -706,6 +712,7 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       sa.b = bv; sa.sp = s.spec; sa.pv = w.pv; sa.lut = h->lut;
       sa.max_clouds = b->max_clouds; sa.n_clouds = b->n_clouds; sa.cloud_type = b->cloud_type;
       sa.wc = b->cloud_water_content; sa.reff = b->cloud_effective_radius; sa.n_streams = b->n_streams;
+      sa.rt_algorithm = b->rt_algorithm_id; sa.FB = w.FB;
       sa.TAU = w.TAU; sa.LB = w.LB; sa.maxreff = w.maxreff;
       sa.radiance = rts->radiance; sa.bt = rts->brightness_temperature;
       sa.status = rts->status; sa.error = h->d_error;
@@ -729,6 +736,13 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
         else
           scatter_adding_kernel<5, R><<<ga, SCATTER_THREADS, 0, st>>>(sa);
         CK_LAUNCH(h);
+        if (soi) {
+          if (nz_max)
+            scatter_soi_kernel<SC_NZ_MAX, R><<<ga, SCATTER_THREADS, 0, st>>>(sa);
+          else
+            scatter_soi_kernel<5, R><<<ga, SCATTER_THREADS, 0, st>>>(sa);
+          CK_LAUNCH(h);
+        }
       }
     }
     if (mode == 0 || mode == 3) {
@@ -853,7 +867,8 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
     items.insert(items.end(), {{b->cloud_water_content, (size_t)P * NC * Km * 8},
                                {b->cloud_effective_radius, (size_t)P * NC * Km * 8},
                                {b->n_clouds, (size_t)P * 4}, {b->cloud_type, (size_t)P * NC * 4},
-                               {b->n_streams, b->n_streams ? (size_t)P * 4 : 0}});
+                               {b->n_streams, b->n_streams ? (size_t)P * 4 : 0},
+                               {b->rt_algorithm_id, b->rt_algorithm_id ? (size_t)P * 4 : 0}});
   }
   size_t tot = 0;
   for (auto& it : items) tot += align_up(it.bytes);
@@ -886,6 +901,7 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
     db.n_clouds = (const int*)dptr[19];
     db.cloud_type = (const int*)dptr[20];
     db.n_streams = (const int*)dptr[21];
+    db.rt_algorithm_id = (const int*)dptr[22];
   }
   // outputs
   const size_t PL = (size_t)P * L;

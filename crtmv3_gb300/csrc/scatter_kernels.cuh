@@ -7,9 +7,9 @@
 //                          (MOM), in the working precision R.  Layers are
 //                          independent, so this is where the parallelism is.
 //   scatter_adding_kernel  one thread per (profile, channel): the adding
-//                          recursion from the surface to the top, FP64 in
-//                          every form (the (I - R R)^-1 inversions), then the
-//                          FP64 Planck inversion.
+//                          recursion from the surface to the top (ADA) or the
+//                          successive orders of interaction (SOI), FP64 in
+//                          every form, then the FP64 Planck inversion.
 //
 // Per-layer results go through HBM with channels fastest:
 // LB[p][k][e][l], e = 0 kind (0 clear, 1 scattering, <0 error), 1 optical
@@ -38,6 +38,8 @@ struct ScatterArgs {
   const int* cloud_type;        // [P][NC]
   const double* wc, *reff;      // [P][NC][Kmax]
   const int* n_streams;         // [P] or null
+  const int* rt_algorithm;      // [P] or null (ADA)
+  double* FB;                   // SOI fields [n][2][2][Kmax+1][NZ][L], or null
   const R* TAU;                 // [n][Kmax][L] gas layer optical depths
   R* LB;                        // [n][Kmax][NE][L] layer records
   double* maxreff;              // [n]
@@ -89,6 +91,7 @@ __device__ __forceinline__ CloudyColumn column_inputs(const ScatterArgs<R>& a, i
   c.wc = a.wc + (size_t)gp * a.max_clouds * a.Kmax;
   c.reff = a.reff + (size_t)gp * a.max_clouds * a.Kmax;
   c.cstride = (size_t)a.Kmax;
+  c.soi = a.rt_algorithm && a.rt_algorithm[gp] == 168;   // RT_SOI
   return c;
 }
 
@@ -154,6 +157,8 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_adding_kernel(Scatter
       tr_tot *= t;
     }
     rad = src + tr_tot * (c.emissivity * c.planck_surface + (1.0 - c.emissivity) * down);
+  } else if (c.soi) {
+    return;   // SOI profiles: scatter_soi_kernel
   } else {
     StreamSet<NZ, double> S;
     code = stream_set<NZ, double>(c.nleg, c.mu_sensor, a.lut.nleg, c_gauss, S);
@@ -183,6 +188,58 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_adding_kernel(Scatter
       }
       if (!code) rad = adding_toa<NZ>(A, nZ, S.isat, c.cosmic);
     }
+  }
+  if (code) {
+    atomicCAS(a.error, 0, code);
+    if (a.status) atomicOr(a.status + gp, 1 << 4);
+    rad = 0.0;
+  }
+  a.radiance[pl] = rad;
+  a.bt[pl] = code ? 0.0 : planck_temperature(c.c1, c.c2, c.b1, c.b2, rad);
+}
+
+
+// SOI profiles (Options%RT_Algorithm_Id = RT_SOI): successive orders of
+// interaction over the layer records, fields in FB.
+template <int NZ, class R>
+__global__ void __launch_bounds__(SCATTER_THREADS) scatter_soi_kernel(ScatterArgs<R> a) {
+  constexpr int NE = layer_record<NZ>();
+  const int L = a.L, Kmax = a.Kmax;
+  const int p = blockIdx.y, gp = a.p_begin + p;
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= L || a.pv.status[p] != 0) return;
+  const CloudyColumn c = column_inputs(a, p, gp, l);
+  if (c.n_clouds == 0 || !c.soi) return;
+  const size_t pl = (size_t)gp * L + l;
+  double rad = 0.0;
+  int code = 0;
+  StreamSet<NZ, double> S;
+  code = stream_set<NZ, double>(c.nleg, c.mu_sensor, a.lut.nleg, c_gauss, S);
+  if (!code) {
+    const int nZ = S.nZ;
+    auto layer = [&](int k, int* kind, double* od, double* B, Mat<NZ, double>& Tm, Mat<NZ, double>& Rm,
+                     double* src) {
+      const R* rec = a.LB + ((size_t)p * Kmax + k) * NE * L + l;
+      *kind = (int)rec[0];
+      *od = double(rec[(size_t)L]);
+      const double tk = c.temperature[k];
+      *B = c.c1 / (exp(c.c2 / (c.b1 + c.b2 * tk)) - 1.0);
+      if (*kind != 1) return;
+      for (int i = 0; i < nZ; i++) {
+        for (int j = 0; j < nZ; j++) {
+          Tm.a[i][j] = double(rec[(size_t)(2 + i * NZ + j) * L]);
+          Rm.a[i][j] = double(rec[(size_t)(2 + NZ * NZ + i * NZ + j) * L]);
+        }
+        src[i] = double(rec[(size_t)(2 + 2 * NZ * NZ + i) * L]);
+      }
+    };
+    double* fb = a.FB + (size_t)p * 4 * (Kmax + 1) * NZ * L + l;
+    const size_t lev = (size_t)NZ * L, buf = (size_t)(Kmax + 1) * lev;
+    auto dn = [&](int k, int i, int b) -> double& { return fb[b * buf + k * lev + (size_t)i * L]; };
+    auto up = [&](int k, int i, int b) -> double& { return fb[(2 + b) * buf + k * lev + (size_t)i * L]; };
+    for (int k = 0; k < c.Ku && !code; k++)
+      if ((int)a.LB[((size_t)p * Kmax + k) * NE * L + l] < 0) code = -(int)a.LB[((size_t)p * Kmax + k) * NE * L + l];
+    if (!code) soi_solve<NZ>(nZ, c.Ku, S.isat, S.mu, c.emissivity, c.planck_surface, c.cosmic, layer, dn, up, &rad);
   }
   if (code) {
     atomicCAS(a.error, 0, code);

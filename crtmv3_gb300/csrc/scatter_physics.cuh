@@ -441,6 +441,69 @@ CRTM_HD void phase_blocks(int nS, int nZ, int nleg, const T* pc, const T (*P)[SC
   }
 }
 
+// SOI layer doubling (SOI_Module.f90: CRTM_Truncated_Doubling :697-827 uses
+// I + R R in place of (I - R R)^-1; CRTM_Doubling_layer :1091-1234 inverts):
+// from a first-order layer of optical depth tau / 2^n, n doublings give the
+// layer's transmission T, reflection R and thermal source.
+template <int NZ>
+CRTM_HD bool soi_doubling(bool trunc, int nS, int nZ, double w, double tau, const double* mu, const double* wt,
+                          const Mat<NZ, double>& ff, const Mat<NZ, double>& bb, double B, Mat<NZ, double>& Tm,
+                          Mat<NZ, double>& Rm, double* src) {
+  if (tau < 1.0e-6) {   // OPTICAL_DEPTH_THRESHOLD: transparent, no source
+    for (int i = 0; i < nZ; i++) {
+      src[i] = 0.0;
+      for (int j = 0; j < nZ; j++) { Tm.a[i][j] = (i == j) ? 1.0 : 0.0; Rm.a[i][j] = 0.0; }
+    }
+    return true;
+  }
+  int nd = (int)(log(tau / DELTA_OPTICAL_DEPTH) / log(2.0)) + 1;
+  if (nd < 1) nd = 1;
+  double dt;
+  if (nd <= 55) {                      // MAX_N_DOUBLING
+    dt = tau;
+    for (int i = 0; i < nd; i++) dt *= 0.5;
+  } else {
+    nd = 55;
+    dt = DELTA_OPTICAL_DEPTH;
+  }
+  const double s = dt * w;
+  for (int i = 0; i < nZ; i++) {
+    const double c = s / mu[i];
+    for (int j = 0; j < nZ; j++) {
+      Rm.a[i][j] = c * bb.a[i][j] * wt[j];
+      Tm.a[i][j] = c * ff.a[i][j] * wt[j] + (i == j ? 1.0 - dt / mu[i] : 0.0);
+    }
+  }
+  Mat<NZ, double> G, A, Bq;
+  for (int L = 0; L < nd; L++) {
+    mat_mul<NZ, double>(nZ, Rm, Rm, G);
+    for (int i = 0; i < nZ; i++)
+      for (int j = 0; j < nZ; j++) G.a[i][j] = (trunc ? G.a[i][j] : -G.a[i][j]) + (i == j ? 1.0 : 0.0);
+    if (!trunc && !mat_invert<NZ, double>(nZ, G)) {
+      // the reference falls back to the clear layer
+      for (int i = 0; i < nZ; i++) {
+        src[i] = 0.0;
+        for (int j = 0; j < nZ; j++) { Tm.a[i][j] = (i == j) ? exp(-tau / mu[i]) : 0.0; Rm.a[i][j] = 0.0; }
+      }
+      return true;
+    }
+    mat_mul<NZ, double>(nZ, Tm, G, A);    // term2 = T (I -/+ R R)^(-1 or +1)
+    mat_mul<NZ, double>(nZ, A, Rm, G);    // term2 R
+    mat_mul<NZ, double>(nZ, G, Tm, Bq);   // term2 R T
+    for (int i = 0; i < nZ; i++)
+      for (int j = 0; j < nZ; j++) Rm.a[i][j] += Bq.a[i][j];
+    mat_mul<NZ, double>(nZ, A, Tm, G);
+    Tm = G;
+  }
+  for (int i = 0; i < nZ; i++) {
+    double c1 = 0.0, c2 = 0.0;
+    for (int j = 0; j < nS; j++) { c1 += Tm.a[i][j]; c2 += Rm.a[i][j]; }
+    if (i == nZ - 1 && nZ == nS + 1) c1 += Tm.a[i][i];
+    src[i] = (1.0 - c1 - c2) * B;
+  }
+  return true;
+}
+
 // Inputs of one (profile, channel) for the cloudy solver.
 struct CloudyColumn {
   int Ku, n_clouds, nleg;                // nleg: Legendre terms of the stream set
@@ -453,6 +516,7 @@ struct CloudyColumn {
   const double* wc;                      // [n_clouds] rows of stride cstride
   const double* reff;
   size_t cstride;
+  bool soi;                              // Options%RT_Algorithm_Id == RT_SOI
 };
 
 // Stream angles of a (profile, channel): Gauss angles of the stream set plus
@@ -541,12 +605,17 @@ CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const Stre
     for (int l = 0; l <= nleg; l++) P[i][l] = double(S.P[i][l]);
   }
   phase_blocks<NZ, double>(S.nS, S.nZ, nleg, pcs, P, wt, ff, bb);
-  double mx = 0.0;
-  for (int i = 0; i < S.nZ; i++)
-    for (int j = 0; j < S.nZ; j++) mx = fabs(ff.a[i][j]) > mx ? fabs(ff.a[i][j]) : mx;
-  if (!(mx > 0.0)) return 0;
   const double B = in.c1 / (exp(in.c2 / (in.b1 + in.b2 * tk)) - 1.0);
-  if (!ada_layer<NZ, double>(S.nS, S.nZ, ssa, od, mu, wt, ff, bb, B, Td, Rd, srcd)) return -5;
+  if (in.soi) {   // SOI: doubling, then the direct beam taken out of the diagonal
+    soi_doubling<NZ>(ssa < 0.8 && od < 4.0, S.nS, S.nZ, ssa, od, mu, wt, ff, bb, B, Td, Rd, srcd);
+    for (int i = 0; i < S.nZ; i++) Td.a[i][i] -= exp(-od / mu[i]);
+  } else {
+    double mx = 0.0;
+    for (int i = 0; i < S.nZ; i++)
+      for (int j = 0; j < S.nZ; j++) mx = fabs(ff.a[i][j]) > mx ? fabs(ff.a[i][j]) : mx;
+    if (!(mx > 0.0)) return 0;
+    if (!ada_layer<NZ, double>(S.nS, S.nZ, ssa, od, mu, wt, ff, bb, B, Td, Rd, srcd)) return -5;
+  }
   for (int i = 0; i < S.nZ; i++) {
     src[i] = T(srcd[i]);
     for (int j = 0; j < S.nZ; j++) { Tm.a[i][j] = T(Td.a[i][j]); Rm.a[i][j] = T(Rd.a[i][j]); }
@@ -629,11 +698,68 @@ CRTM_HD double adding_toa(const AddingState<NZ>& A, int nZ, int isat, double cos
   return A.rad[isat] + s * cosmic;
 }
 
+// CRTM_SOI (SOI_Module.f90:63-283): successive orders of interaction.  Order
+// 1 carries the thermal sources, the surface emission and the cosmic
+// background; each later order scatters the previous order's diffuse fields
+// through the layers' T and R.  Stops when the newest order adds less than
+// 1e-4 of the radiance (at least 2 orders, at most 75).  Field storage is the
+// caller's: dn(k, i, b) / up(k, i, b) give level k, angle i, buffer b (0/1).
+template <int NZ, class LayerFn, class DnFn, class UpFn>
+CRTM_HD int soi_solve(int nZ, int Ku, int isat, const double* mu, double emissivity, double planck_surface,
+                      double cosmic, LayerFn layer, DnFn dn, UpFn up, double* radiance) {
+  // layer(k, &kind, &od, &B, T, R, src): kind 0 clear, 1 scattering
+  double total = 0.0, change = 1.0e10;
+  int niter = 0, cur = 0;
+  Mat<NZ, double> Tm, Rm;
+  double src[NZ], etr[NZ];
+  while ((change > 1.0e-4 && niter + 1 <= 75) || niter < 2) {
+    niter++;
+    const int prev = cur ^ 1;
+    if (niter == 1) cur = 0;
+    for (int i = 0; i < nZ; i++) dn(0, i, cur) = niter == 1 ? cosmic : 0.0;
+    for (int k = 0; k < Ku; k++) {
+      int kind;
+      double od, B;
+      layer(k, &kind, &od, &B, Tm, Rm, src);
+      for (int i = 0; i < nZ; i++) etr[i] = exp(-od / mu[i]);
+      for (int i = 0; i < nZ; i++) {
+        double sv = 0.0;
+        if (niter == 1) sv = kind == 1 ? src[i] : B * (1.0 - etr[i]);
+        else if (kind == 1 && od >= 1.0e-6)
+          for (int j = 0; j < nZ; j++) sv += Tm.a[i][j] * dn(k, j, prev) + Rm.a[i][j] * up(k + 1, j, prev);
+        dn(k + 1, i, cur) = dn(k, i, cur) * etr[i] + sv;
+      }
+    }
+    for (int i = 0; i < nZ; i++)
+      up(Ku, i, cur) = (1.0 - emissivity) * dn(Ku, i, cur) + (niter == 1 ? emissivity * planck_surface : 0.0);
+    for (int k = Ku - 1; k >= 0; k--) {
+      int kind;
+      double od, B;
+      layer(k, &kind, &od, &B, Tm, Rm, src);
+      for (int i = 0; i < nZ; i++) etr[i] = exp(-od / mu[i]);
+      for (int i = 0; i < nZ; i++) {
+        double sv = 0.0;
+        if (niter == 1) sv = kind == 1 ? src[i] : B * (1.0 - etr[i]);
+        else if (kind == 1 && od >= 1.0e-6)
+          for (int j = 0; j < nZ; j++) sv += Rm.a[i][j] * dn(k, j, prev) + Tm.a[i][j] * up(k + 1, j, prev);
+        up(k, i, cur) = up(k + 1, i, cur) * etr[i] + sv;
+      }
+    }
+    const double rad = up(0, isat, cur);
+    total += rad;
+    change = rad / total;
+    cur ^= 1;
+  }
+  *radiance = total;
+  return 0;
+}
+
 // The whole (profile, channel) in one pass, FP64 (the layer-parallel GPU
 // kernels split it into layer_optics for every layer, then the adding).
 template <int NZ, class OdFn>
 CRTM_HD int cloudy_radiance(const CloudyColumn& in, const CloudLut& lut, const GaussTable& gt,
                             OdFn od_of, double* radiance) {
+  if (in.soi) return 7;   // SOI needs every layer's record: the layered form
   StreamSet<NZ, double> S;
   if (int rc = stream_set<NZ, double>(in.nleg, in.mu_sensor, lut.nleg, gt, S)) return rc;
   AddingState<NZ> A;

@@ -94,6 +94,9 @@ typedef struct {
   /* Options%n_Streams for profiles with Options%Use_N_Streams (2, 4, 6, 8 or
    * 16), 0 for the reference's stream rule; NULL: the rule everywhere. */
   const int* n_streams;           /* [P] */
+  /* Options%RT_Algorithm_Id for cloudy profiles: 56 ADA, 168 SOI
+   * (src/CRTM_Parameters.f90:247-248); NULL: ADA everywhere. */
+  const int* rt_algorithm_id;     /* [P] */
 } crtm_gpu_batch;
 
 typedef struct {
@@ -139,8 +142,8 @@ int crtm_gpu_n_channels(crtm_gpu_handle handle, int sensor);
 int crtm_gpu_set_precision(crtm_gpu_handle handle, int precision);
 
 /* CRTM_Forward for one sensor: host buffers.  Profiles with clouds use the
- * ADA scattering solver (in FP64 in both arithmetic forms); the K-matrix and
- * adjoint entry points return CRTM_GPU_FAILURE for batches with clouds. */
+ * ADA or SOI scattering solver (FP64 in both arithmetic forms); the K-matrix
+ * and adjoint entry points return CRTM_GPU_FAILURE for batches with clouds. */
 int crtm_gpu_forward(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* batch,
                      crtm_gpu_rtsolution* rts);
 

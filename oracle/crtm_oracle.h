@@ -97,9 +97,10 @@ typedef struct {
   const double* water_content;     /* [P][NC][max_layers] kg/m^2                */
   const double* effective_radius;  /* [P][NC][max_layers] microns               */
   const int* n_streams;            /* [P] Options%n_Streams, 0 = stream rule; may be NULL */
+  const int* rt_algorithm;         /* [P] Options%RT_Algorithm_Id: 56 ADA, 168 SOI; may be NULL (ADA) */
 } or_clouds;
 
-/* Forward with clouds: ADA for profiles with clouds, Emission otherwise. */
+/* Forward with clouds: ADA or SOI for profiles with clouds, Emission otherwise. */
 int or_forward_scatter(const or_handle* h, const or_cloud* cc, const or_batch* b, const or_clouds* cl,
                        double* radiance, double* bt, int n_threads);
 

@@ -34,7 +34,8 @@ class OrBatch(ct.Structure):
 
 class OrClouds(ct.Structure):
     _fields_ = [("max_clouds", ct.c_int), ("n_clouds", _ip), ("cloud_type", _ip),
-                ("water_content", _dp), ("effective_radius", _dp), ("n_streams", _ip)]
+                ("water_content", _dp), ("effective_radius", _dp), ("n_streams", _ip),
+                ("rt_algorithm", _ip)]
 
 
 def build(force: bool = False) -> str:
@@ -184,6 +185,10 @@ class Oracle:
                 ns = np.ascontiguousarray(np.where(opt.use_n_streams, opt.n_streams, 0), np.int32)
                 keep.append(ns)
                 c.n_streams = _p(ns, _ip)
+            if opt.rt_algorithm_id is not None:
+                ra = np.ascontiguousarray(opt.rt_algorithm_id, np.int32)
+                keep.append(ra)
+                c.rt_algorithm = _p(ra, _ip)
             rad, bt = np.zeros((P, nL)), np.zeros((P, nL))
             st = L.or_forward_scatter(self.h, ch, ct.byref(b), ct.byref(c), _p(rad), _p(bt), n_threads)
             if st:

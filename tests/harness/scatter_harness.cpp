@@ -35,7 +35,7 @@ int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, 
                        int nleg, int microwave, double freq, double mu_sensor, double emissivity,
                        double planck_surface, double cosmic, const double* planck, const double* temp,
                        const int* cloud_type, const double* wc, const double* reff, int cstride,
-                       const double* od, double* radiance) {
+                       const double* od, int soi, double* radiance) {
   CloudLut L{dims[0], dims[1], dims[2], dims[3], dims[4], dims[5], dims[6], f_mw, r_mw, t, f_ir, r_ir,
              ke_l, w_l, pc_l, ke_s, w_s, pc_s, ke_ir, w_ir, pc_ir};
   static const GaussTable gt = make_gauss();
@@ -44,7 +44,72 @@ int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, 
   c.mu_sensor = mu_sensor; c.emissivity = emissivity; c.planck_surface = planck_surface; c.cosmic = cosmic;
   c.c1 = planck[0]; c.c2 = planck[1]; c.b1 = planck[2]; c.b2 = planck[3];
   c.temperature = temp; c.cloud_type = cloud_type; c.wc = wc; c.reff = reff; c.cstride = (size_t)cstride;
-  return cloudy_radiance<SC_NZ_MAX>(c, L, gt, [&](int k) { return od[k]; }, radiance);
+  c.soi = soi != 0;
+  if (soi == 2) {   // layered ADA as the GPU kernels run it (records with NZ = 5)
+    c.soi = false;
+    constexpr int NZ = 5, NE = 2 + 2 * NZ * NZ + NZ;
+    StreamSet<NZ, double> S;
+    if (int rc = stream_set<NZ, double>(nleg, mu_sensor, L.nleg, gt, S)) return rc;
+    std::vector<double> rec((size_t)Ku * NE);
+    for (int k = 0; k < Ku; k++) {
+      Mat<NZ, double> Tm, Rm;
+      double srcv[NZ], o;
+      const int kind = layer_optics<NZ, double>(c, L, S, k, od[k], &o, Tm, Rm, srcv);
+      double* r = &rec[(size_t)k * NE];
+      r[0] = kind;
+      r[1] = o;
+      if (kind != 1) continue;
+      for (int i = 0; i < S.nZ; i++) {
+        for (int j = 0; j < S.nZ; j++) { r[2 + i * NZ + j] = Tm.a[i][j]; r[2 + NZ * NZ + i * NZ + j] = Rm.a[i][j]; }
+        r[2 + 2 * NZ * NZ + i] = srcv[i];
+      }
+    }
+    AddingState<NZ> A;
+    adding_init<NZ>(A, S.nZ, emissivity, planck_surface);
+    for (int k = Ku - 1; k >= 0; k--) {
+      const double* r = &rec[(size_t)k * NE];
+      const int kind = (int)r[0];
+      if (kind < 0) return -kind;
+      if (kind == 1) {
+        Mat<NZ, double> Tm, Rm;
+        double srcv[NZ];
+        for (int i = 0; i < S.nZ; i++) {
+          for (int j = 0; j < S.nZ; j++) { Tm.a[i][j] = r[2 + i * NZ + j]; Rm.a[i][j] = r[2 + NZ * NZ + i * NZ + j]; }
+          srcv[i] = r[2 + 2 * NZ * NZ + i];
+        }
+        if (!adding_scatter<NZ>(A, S.nZ, Tm, Rm, srcv)) return 6;
+      } else {
+        adding_clear<NZ>(A, S.nZ, S.mu, r[1], c.c1 / (exp(c.c2 / (c.b1 + c.b2 * temp[k])) - 1.0));
+      }
+    }
+    *radiance = adding_toa<NZ>(A, S.nZ, S.isat, cosmic);
+    return 0;
+  }
+  if (!c.soi) return cloudy_radiance<SC_NZ_MAX>(c, L, gt, [&](int k) { return od[k]; }, radiance);
+  // SOI: every layer's record first, then the orders of interaction
+  constexpr int NZ = SC_NZ_MAX;
+  StreamSet<NZ, double> S;
+  if (int rc = stream_set<NZ, double>(nleg, mu_sensor, L.nleg, gt, S)) return rc;
+  std::vector<int> kind(Ku);
+  std::vector<double> ods(Ku);
+  std::vector<Mat<NZ, double>> T(Ku), R(Ku);
+  std::vector<double> src((size_t)Ku * NZ);
+  for (int k = 0; k < Ku; k++) {
+    kind[k] = layer_optics<NZ, double>(c, L, S, k, od[k], &ods[k], T[k], R[k], &src[(size_t)k * NZ]);
+    if (kind[k] < 0) return -kind[k];
+  }
+  auto layer = [&](int k, int* kd, double* o, double* B, Mat<NZ, double>& Tm, Mat<NZ, double>& Rm, double* sv) {
+    *kd = kind[k];
+    *o = ods[k];
+    *B = c.c1 / (exp(c.c2 / (c.b1 + c.b2 * temp[k])) - 1.0);
+    Tm = T[k];
+    Rm = R[k];
+    for (int i = 0; i < NZ; i++) sv[i] = src[(size_t)k * NZ + i];
+  };
+  std::vector<double> f((size_t)4 * (Ku + 1) * NZ);
+  auto dn = [&](int k, int i, int b) -> double& { return f[((size_t)b * (Ku + 1) + k) * NZ + i]; };
+  auto up = [&](int k, int i, int b) -> double& { return f[((size_t)(2 + b) * (Ku + 1) + k) * NZ + i]; };
+  return soi_solve<NZ>(S.nZ, Ku, S.isat, S.mu, emissivity, planck_surface, cosmic, layer, dn, up, radiance);
 }
 
 int sx_stream_rule(double max_reff, double wavenumber) { return stream_rule_nleg(max_reff, wavenumber); }

@@ -39,6 +39,20 @@ def test_cloudy_forward_matches_oracle(gpu_lib, cloud_dir, precision, sensor, nl
     assert (rts.status == 0).all()
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("sensor,nl,n_streams", [("mwsynth_c16", 100, None), ("mwsynth_c16", 100, 16),
+                                                 ("irsynth_c616", 101, None)])
+def test_soi_forward_matches_oracle(gpu_lib, cloud_dir, precision, sensor, nl, n_streams):
+    """Options%RT_Algorithm_Id = RT_SOI for half of the profiles, ADA for the rest."""
+    from oracle.pyoracle import Oracle
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 6, nl, 67, wc_scale=100.0, n_streams=n_streams)
+    opt.rt_algorithm_id = np.array([168, 56, 168, 56, 168, 168], np.int32)
+    atm.n_clouds[4] = 0
+    _, ref = Oracle(cloud_dir, sensor).forward_scatter(atm, sfc, geo, opt, f"{cloud_dir}/CloudCoeff.bin")
+    rts = gpu_lib.CRTM([sensor], cloud_dir, precision).forward(atm, sfc, geo, opt)
+    assert np.abs(rts.brightness_temperature - ref).max() <= BT_TOL[precision]
+
+
 def test_ragged_cloudy_batch(gpu_lib, cloud_dir):
     from oracle.pyoracle import Oracle
     sensor = "mwsynth_c16"

@@ -157,3 +157,17 @@ def test_stream_count_convergence(coeff_dir, cloud_path):
     opt.n_streams[:] = 8
     _, b8 = o.forward_scatter(atm, sfc, geo, opt, cloud_path)
     assert np.abs(b16 - b8).max() < 1.0
+
+
+@pytest.mark.parametrize("sensor,nl", [("mwsynth_c16", 100), ("irsynth_c616", 101)])
+def test_soi_agrees_with_ada(coeff_dir, cloud_path, sensor, nl):
+    """Two different solvers of the same scattering problem: at the config's
+    cloud amounts SOI (successive orders, 1e-4 stopping rule, truncated
+    doubling) and ADA (eigen-solution + adding) agree to 0.02 K."""
+    from oracle.pyoracle import Oracle
+    o = Oracle(coeff_dir, sensor)
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 4, nl, 45)
+    _, ba = o.forward_scatter(atm, sfc, geo, opt, cloud_path)
+    opt.rt_algorithm_id = np.full(4, 168, np.int32)
+    _, bs = o.forward_scatter(atm, sfc, geo, opt, cloud_path)
+    assert np.abs(bs - ba).max() < 0.02

@@ -52,17 +52,20 @@ def test_ada_layer_matches_oracle(sx, nleg, mu_s, w, tau):
         assert np.abs(a - b).max() < 1e-12
 
 
-@pytest.mark.parametrize("sensor,nl,n_streams", [("mwsynth_c16", 100, None), ("mwsynth_c16", 100, 16),
-                                                 ("irsynth_c616", 101, None), ("mwsynth_c22", 100, 8)])
-def test_cloudy_radiance_matches_oracle(sx, coeff_dir, sensor, nl, n_streams):
+@pytest.mark.parametrize("sensor,nl,n_streams,soi", [("mwsynth_c16", 100, None, 0), ("mwsynth_c16", 100, 16, 0),
+                                                     ("irsynth_c616", 101, None, 0), ("mwsynth_c22", 100, 8, 0),
+                                                     ("mwsynth_c16", 100, None, 1), ("mwsynth_c16", 100, 16, 1),
+                                                     ("irsynth_c616", 101, None, 1),
+                                                     ("mwsynth_c16", 100, None, 2), ("irsynth_c616", 101, None, 2)])
+def test_cloudy_radiance_matches_oracle(sx, coeff_dir, sensor, nl, n_streams, soi):
     from oracle.pyoracle import Oracle
     path = sy.write_cloud_files(coeff_dir)
     cc = co.read_cloudcoeff(path)
     sc = co.read_spccoeff(f"{coeff_dir}/{sensor}.SpcCoeff.bin")
     o = Oracle(coeff_dir, sensor)
     atm, sfc, geo, opt = sy.cloudy_workload(sensor, 3, nl, 51, wc_scale=200.0, n_streams=n_streams)
-    if sensor == "irsynth_c616":   # only a channel subset for time
-        pass
+    if soi == 1:
+        opt.rt_algorithm_id = np.full(atm.n_profiles, 168, np.int32)
     rad_ref, _ = o.forward_scatter(atm, sfc, geo, opt, path)
     _, _, lod = o.forward(atm, sfc, geo, opt, layer_od=True)
     f = lambda a: np.ascontiguousarray(np.ravel(a, order="F"))   # noqa: E731
@@ -99,7 +102,7 @@ def test_cloudy_radiance_matches_oracle(sx, coeff_dir, sensor, nl, n_streams):
                 ct.c_double(sc.frequency[l] if mw else sc.wavenumber[l]), ct.c_double(mu),
                 ct.c_double(opt.emissivity[m, l]), ct.c_double(bs),
                 ct.c_double(sc.cosmic_background_radiance[l]), _p(planck), _p(temp), _p(ctype, _ip),
-                _p(wc), _p(re), atm.max_layers, _p(od), ct.byref(r))
+                _p(wc), _p(re), atm.max_layers, _p(od), soi, ct.byref(r))
             assert rc == 0
             worst = max(worst, abs(r.value - rad_ref[m, l]) / abs(rad_ref[m, l]))
     assert worst < 1e-11
