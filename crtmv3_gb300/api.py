@@ -52,7 +52,9 @@ class CBatch(ct.Structure):
                 ("surface_altitude", ct.c_void_p), ("emissivity", ct.c_void_p),
                 ("max_clouds", ct.c_int), ("n_clouds", ct.c_void_p), ("cloud_type", ct.c_void_p),
                 ("cloud_water_content", ct.c_void_p), ("cloud_effective_radius", ct.c_void_p),
-                ("n_streams", ct.c_void_p), ("rt_algorithm_id", ct.c_void_p)]
+                ("n_streams", ct.c_void_p), ("rt_algorithm_id", ct.c_void_p),
+                ("max_aerosols", ct.c_int), ("n_aerosols", ct.c_void_p), ("aerosol_type", ct.c_void_p),
+                ("aerosol_concentration", ct.c_void_p), ("aerosol_effective_radius", ct.c_void_p)]
 
 
 class CRTSolution(ct.Structure):
@@ -211,6 +213,12 @@ class CRTM:
             b.n_streams = c(np.where(use, opt.n_streams, 0), np.int32)
         if opt.rt_algorithm_id is not None:
             b.rt_algorithm_id = c(opt.rt_algorithm_id, np.int32)
+        if atm.n_aerosols is not None and atm.aerosol_type is not None and atm.aerosol_type.shape[1] > 0:
+            b.max_aerosols = int(atm.aerosol_type.shape[1])
+            b.n_aerosols = c(atm.n_aerosols, np.int32)
+            b.aerosol_type = c(atm.aerosol_type, np.int32)
+            b.aerosol_concentration = c(atm.aerosol_concentration)
+            b.aerosol_effective_radius = c(atm.aerosol_effective_radius)
         return b
 
     def _check(self, rc: int) -> None:
@@ -283,11 +291,14 @@ class CRTM:
                   "water_temperature", "snow_temperature", "ice_temperature",
                   "sensor_zenith_angle", "source_zenith_angle", "surface_altitude", "emissivity",
                   "n_clouds", "cloud_type", "cloud_water_content", "cloud_effective_radius",
-                  "n_streams", "rt_algorithm_id"):
+                  "n_streams", "rt_algorithm_id", "n_aerosols", "aerosol_type", "aerosol_concentration",
+                  "aerosol_effective_radius"):
             t = dev.get(f)
             setattr(b, f, None if t is None else t.data_ptr())
         if dev.get("cloud_type") is not None:
             b.max_clouds = int(dev["cloud_type"].shape[1])
+        if dev.get("aerosol_type") is not None:
+            b.max_aerosols = int(dev["aerosol_type"].shape[1])
         return b, keep
 
     def k_matrix_device(self, b: CBatch, out: dict, seed=None, sensor: int = 0, stream=None,

@@ -301,3 +301,74 @@ def read_cloudcoeff(path: str) -> CloudCoeff:
         smw = block((nfm, nrm, nd), (nfm, nrm, nd, nl + 1, nph))
         ir = block((nfi, nri, nd + 1), (nfi, nri, nd + 1, nl, nph))
     return CloudCoeff(*axes, *lmw, *smw, *ir, version=int(ver))
+
+
+# ---------------------------------------------------------------------------
+# AerosolCoeff (aerosol optical property LUT), scheme 'CRTM'
+# ---------------------------------------------------------------------------
+
+AEROSOLCOEFF_RELEASE = 4        # ``AerosolCoeff_Define.f90:75``
+AEROSOL_SL = 80                 # character length of the names (``AerosolCoeff_Define.f90:82``)
+
+
+@dataclasses.dataclass
+class AerosolCoeff:
+    """Aerosol LUT (``AerosolCoeff_Define.f90:94-125``).  Arrays in the
+    reference's Fortran index order: ``ke[w, rh, r, sigma, type]``,
+    ``pcoeff[w, rh, r, sigma, type, l, m]`` with l = 0..n_legendre_terms;
+    ``reff[r, type]``, ``rsig[sigma, type]``, ``rh[n_rh_radii]``.
+    Wavelengths in microns; the reference converts them to frequencies
+    10^4/wavelength (cm^-1), which must increase along the axis."""
+    type_id: np.ndarray
+    type_name: list
+    wavelength: np.ndarray
+    reff: np.ndarray
+    rsig: np.ndarray
+    rh: np.ndarray
+    ke: np.ndarray
+    w: np.ndarray
+    g: np.ndarray
+    pcoeff: np.ndarray
+    data_source: str = "synthetic"
+    version: int = 1
+
+
+def write_aerosolcoeff(path: str, ac: AerosolCoeff, byteorder: str = "<") -> None:
+    """Record order of ``AerosolCoeff_Binary_IO.f90:396-530`` for the 'CRTM'
+    scheme (which carries n_RH_Radii) and a Version <= 300 file (no kb)."""
+    nw, nrh, nr, ns, nt = ac.ke.shape
+    nl = ac.pcoeff.shape[5] - 1
+    with open(path, "wb") as f:
+        wr = RecordWriter(f, byteorder)
+        wr.record(np.array([AEROSOLCOEFF_RELEASE, ac.version], np.int32))
+        wr.record(np.array([nw, nr, ns, nt, nrh, nl, ac.pcoeff.shape[6]], np.int32))
+        wr.record(np.array([ac.rh.size], np.int32))
+        wr.record(np.array([AEROSOL_SL], np.int32))
+        wr.record(ac.data_source.ljust(AEROSOL_SL)[:AEROSOL_SL].encode("ascii"))
+        wr.record(np.asarray(ac.type_id, np.int32))
+        wr.record(np.array([AEROSOL_SL], np.int32))
+        wr.record(b"".join(n.ljust(AEROSOL_SL)[:AEROSOL_SL].encode("ascii") for n in ac.type_name))
+        wr.record(ac.wavelength, ac.reff, ac.rsig, ac.rh)
+        wr.record(ac.ke, ac.w, ac.g, ac.pcoeff)
+
+
+def read_aerosolcoeff(path: str) -> AerosolCoeff:
+    with open(path, "rb") as f:
+        r = RecordReader(f)
+        rel, ver = r.split(r.record(), [("i4", (2,))])[0]
+        if rel != AEROSOLCOEFF_RELEASE:
+            raise IOError(f"AerosolCoeff release {rel} not supported")
+        nw, nr, ns, nt, nrh, nl, nph = (int(x) for x in r.split(r.record(), [("i4", (7,))])[0])
+        (nrr,) = r.split(r.record(), [("i4", ())])
+        r.record()
+        src = r.split(r.record(), [("S", AEROSOL_SL)])[0]
+        tid = r.split(r.record(), [("i4", (nt,))])[0]
+        r.record()
+        names = r.split(r.record(), [("S", AEROSOL_SL)] * nt)
+        wl, reff, rsig, rh = r.split(r.record(), [("f8", (nw,)), ("f8", (nr, nt)), ("f8", (ns, nt)),
+                                                  ("f8", (int(nrr),))])
+        shp = (nw, nrh, nr, ns, nt)
+        n5 = int(np.prod(shp))
+        parts = r.split(r.record(), [("f8", (n5,))] * 3 + [("f8", (n5 * (nl + 1) * nph,))])
+    return AerosolCoeff(tid, names, wl, reff, rsig, rh, *[p.reshape(shp, order="F") for p in parts[:3]],
+                        parts[3].reshape(shp + (nl + 1, nph), order="F"), src, int(ver))

@@ -345,6 +345,56 @@ bool load_cloudcoeff(const std::string& path, std::vector<double>& buf, int* dim
   return true;
 }
 
+// AerosolCoeff.bin, scheme 'CRTM' (AerosolCoeff_Binary_IO.f90:396-530):
+// Release/Version, 7 dimensions, n_RH_Radii, the data-source string, type
+// ids, type names, (wavelength, Reff, Rsig, RH), then (ke, w, g, pcoeff).
+// Version > 300 files carry kb as well and are refused here.
+bool load_aerosolcoeff(const std::string& path, std::vector<double>& buf, std::vector<int>& types, int* dims,
+                       size_t* off, std::string& err) {
+  Records r;
+  if (!r.open(path, err)) return false;
+  const unsigned char* d;
+  size_t len;
+  auto bad = [&](const char* what) { err = path + ": " + what; return false; };
+  if (!r.next(d, len) || len != 8) return bad("corrupt Release/Version record");
+  if (r.i32(d) != 4) return bad("unsupported AerosolCoeff release");
+  if (r.i32(d + 4) > 300) return bad("AerosolCoeff files with kb (Version > 300) are not supported");
+  if (!r.next(d, len) || len != 28) return bad("corrupt dimension record");
+  int dm[7];
+  for (int i = 0; i < 7; i++) dm[i] = r.i32(d + 4 * i);
+  const int nw = dm[0], nr = dm[1], ns = dm[2], nt = dm[3], nrh = dm[4], nleg = dm[5], nph = dm[6];
+  if (nw < 4 || nr < 4 || ns < 1 || nt < 1 || nrh < 1 || nleg < 1 || nleg > 64 || nph < 1)
+    return bad("dimensions out of range");
+  if (!r.next(d, len) || len != 4) return bad("corrupt n_RH_Radii record");
+  const int nrr = r.i32(d);
+  if (!r.next(d, len) || len != 4) return bad("corrupt string-length record");
+  if (!r.next(d, len)) return bad("corrupt data-source record");
+  if (!r.next(d, len) || len != 4u * nt) return bad("corrupt type record");
+  types.resize(nt);
+  for (int t = 0; t < nt; t++) types[t] = r.i32(d + 4 * t);
+  if (!r.next(d, len) || len != 4) return bad("corrupt string-length record");
+  if (!r.next(d, len)) return bad("corrupt type-name record");
+  const size_t nax = (size_t)nw + (size_t)nr * nt + (size_t)ns * nt + nrr;
+  if (!r.next(d, len) || len != 8 * nax) return bad("corrupt axis record");
+  buf.clear();
+  off[0] = 0;
+  for (int i = 0; i < nw; i++) buf.push_back(1.0e4 / r.f64(d + 8 * i));   // micron_to_inverse_cm
+  for (int i = 1; i < nw; i++)
+    if (!(buf[i] > buf[i - 1])) return bad("frequencies (10^4/wavelength) must increase");
+  off[1] = buf.size();
+  for (size_t i = 0; i < (size_t)nr * nt; i++) buf.push_back(r.f64(d + 8 * (nw + i)));
+  const size_t n5 = (size_t)nw * nrh * nr * ns * nt;
+  if (!r.next(d, len) || len != 8 * (3 * n5 + n5 * (nleg + 1) * nph)) return bad("corrupt LUT record");
+  off[2] = buf.size();
+  for (size_t i = 0; i < n5; i++) buf.push_back(r.f64(d + 8 * i));
+  off[3] = buf.size();
+  for (size_t i = 0; i < n5; i++) buf.push_back(r.f64(d + 8 * (n5 + i)));
+  off[4] = buf.size();
+  for (size_t i = 0; i < n5 * (nleg + 1); i++) buf.push_back(r.f64(d + 8 * (3 * n5 + i)));
+  dims[0] = nw; dims[1] = nrh; dims[2] = nr; dims[3] = ns; dims[4] = nt; dims[5] = nleg;
+  return true;
+}
+
 // Grow-only device buffer
 struct DevBuf {
   void* p = nullptr;
@@ -378,6 +428,11 @@ struct crtm_gpu_context {
   bool has_clouds = false;
   double* d_cloud = nullptr;
   CloudLut lut{};
+  // aerosol LUT (AerosolCoeff.bin, scheme 'CRTM'), when present
+  bool has_aerosols = false;
+  double* d_aero = nullptr;
+  int* d_aero_type = nullptr;
+  AerosolLut alut{};
   int* d_error = nullptr;   // first failure code of the scattering kernel
   cudaStream_t copy_stream = nullptr;   // device-to-host copies of finished chunks
   std::vector<cudaEvent_t> chunk_events;
@@ -713,6 +768,10 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       sa.max_clouds = b->max_clouds; sa.n_clouds = b->n_clouds; sa.cloud_type = b->cloud_type;
       sa.wc = b->cloud_water_content; sa.reff = b->cloud_effective_radius; sa.n_streams = b->n_streams;
       sa.rt_algorithm = b->rt_algorithm_id; sa.FB = w.FB;
+      sa.alut = h->alut; sa.max_aerosols = b->max_aerosols > 0 ? b->max_aerosols : 0;
+      sa.n_aerosols = b->n_aerosols; sa.aerosol_type = b->aerosol_type;
+      sa.conc = b->aerosol_concentration; sa.aer_reff = b->aerosol_effective_radius;
+      if (b->max_clouds <= 0) sa.max_clouds = 0;
       sa.TAU = w.TAU; sa.LB = w.LB; sa.maxreff = w.maxreff;
       sa.radiance = rts->radiance; sa.bt = rts->brightness_temperature;
       sa.status = rts->status; sa.error = h->d_error;
@@ -817,11 +876,16 @@ int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, c
   if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
   const Sensor& s = h->sensors[sensor];
   const bool fp64 = h->precision == CRTM_GPU_FP64;
-  if (b->max_clouds > 0) {
-    if (mode != 0) return fail(h, "the K-matrix and adjoint are not available for batches with clouds");
-    if (!h->has_clouds) return fail(h, "batch has clouds but no CloudCoeff.bin was loaded at init");
-    if (!b->n_clouds || !b->cloud_type || !b->cloud_water_content || !b->cloud_effective_radius)
+  if (b->max_clouds > 0 || b->max_aerosols > 0) {
+    if (mode != 0) return fail(h, "the K-matrix and adjoint are not available for batches with clouds or aerosols");
+    if (b->max_clouds > 0 && !h->has_clouds) return fail(h, "batch has clouds but no CloudCoeff.bin was loaded at init");
+    if (b->max_aerosols > 0 && !h->has_aerosols && s.sensor_type != 1)
+      return fail(h, "batch has aerosols but no AerosolCoeff.bin was loaded at init");
+    if (b->max_clouds > 0 && (!b->n_clouds || !b->cloud_type || !b->cloud_water_content || !b->cloud_effective_radius))
       return fail(h, "cloud arrays missing for max_clouds = %d", b->max_clouds);
+    if (b->max_aerosols > 0 && (!b->n_aerosols || !b->aerosol_type || !b->aerosol_concentration ||
+                                !b->aerosol_effective_radius))
+      return fail(h, "aerosol arrays missing for max_aerosols = %d", b->max_aerosols);
     if (cudaMemsetAsync(h->d_error, 0, sizeof(int), st) != cudaSuccess) return fail(h, "error flag reset failed");
     mode = 3;
   }
@@ -858,6 +922,14 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
       {b->ice_temperature, PD}, {b->sensor_zenith_angle, PD}, {b->surface_altitude, PD},
       {b->emissivity, (size_t)P * L * 8}, {seed, (size_t)P * L * 8}, {b->n_layers, (size_t)P * 4}};
   const int NC = b->max_clouds > 0 ? b->max_clouds : 0;
+  const int NA = b->max_aerosols > 0 ? b->max_aerosols : 0;
+  if (NA > 0) {
+    if (!b->n_aerosols || !b->aerosol_type || !b->aerosol_concentration || !b->aerosol_effective_radius)
+      return fail(h, "aerosol arrays missing for max_aerosols = %d", NA);
+    for (int m = 0; m < P; m++)
+      if (b->n_aerosols[m] < 0 || b->n_aerosols[m] > NA)
+        return fail(h, "profile %d: n_aerosols %d outside [0, max_aerosols=%d]", m, b->n_aerosols[m], NA);
+  }
   if (NC > 0) {
     if (!b->n_clouds || !b->cloud_type || !b->cloud_water_content || !b->cloud_effective_radius)
       return fail(h, "cloud arrays missing for max_clouds = %d", NC);
@@ -868,6 +940,16 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
                                {b->cloud_effective_radius, (size_t)P * NC * Km * 8},
                                {b->n_clouds, (size_t)P * 4}, {b->cloud_type, (size_t)P * NC * 4},
                                {b->n_streams, b->n_streams ? (size_t)P * 4 : 0},
+                               {b->rt_algorithm_id, b->rt_algorithm_id ? (size_t)P * 4 : 0}});
+  }
+  const size_t aer0 = items.size();
+  if (NA > 0)
+    items.insert(items.end(), {{b->aerosol_concentration, (size_t)P * NA * Km * 8},
+                               {b->aerosol_effective_radius, (size_t)P * NA * Km * 8},
+                               {b->n_aerosols, (size_t)P * 4}, {b->aerosol_type, (size_t)P * NA * 4}});
+  if (NC == 0 && b->max_clouds <= 0 && (b->n_streams || b->rt_algorithm_id) && NA > 0) {
+    // options without clouds (aerosol-only batch)
+    items.insert(items.end(), {{b->n_streams, b->n_streams ? (size_t)P * 4 : 0},
                                {b->rt_algorithm_id, b->rt_algorithm_id ? (size_t)P * 4 : 0}});
   }
   size_t tot = 0;
@@ -902,6 +984,16 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
     db.cloud_type = (const int*)dptr[20];
     db.n_streams = (const int*)dptr[21];
     db.rt_algorithm_id = (const int*)dptr[22];
+  }
+  if (NA > 0) {
+    db.aerosol_concentration = (const double*)dptr[aer0];
+    db.aerosol_effective_radius = (const double*)dptr[aer0 + 1];
+    db.n_aerosols = (const int*)dptr[aer0 + 2];
+    db.aerosol_type = (const int*)dptr[aer0 + 3];
+    if (NC == 0) {
+      db.n_streams = b->n_streams ? (const int*)dptr[aer0 + 4] : nullptr;
+      db.rt_algorithm_id = b->rt_algorithm_id ? (const int*)dptr[aer0 + 5] : nullptr;
+    }
   }
   // outputs
   const size_t PL = (size_t)P * L;
@@ -949,11 +1041,12 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
   if (e != cudaSuccess || e2 != cudaSuccess)
     return fail(h, "CUDA error: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
   if (h->profiling) collect_stage_times(h);
-  if (NC > 0) {
+  if (NC > 0 || NA > 0) {
     int code = 0;
     if (cudaMemcpy(&code, h->d_error, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
       return fail(h, "cannot read the scattering error flag");
-    if (code) return fail(h, "cloudy radiative transfer failed (code %d: 1-3 stream set, 4 cloud type, 5-6 singular matrix)", code);
+    if (code) return fail(h, "scattering radiative transfer failed (code %d: 1-3 stream set, 4 cloud type, "
+                             "5-6 singular matrix, 8 aerosol stream set or LUT, 9 aerosol type)", code);
   }
   if (rts->status)
     for (int m = 0; m < P; m++)
@@ -1019,6 +1112,34 @@ int crtm_gpu_init(const char* coeff_path, int n_sensors, const char* const* sens
       L.ke_ir = b0 + off[11]; L.w_ir = b0 + off[12]; L.pc_ir = b0 + off[13];
       h->has_clouds = true;
     }
+    const std::string apath = std::string(coeff_path) + "/AerosolCoeff.bin";
+    if (FILE* fa = fopen(apath.c_str(), "rb")) {
+      fclose(fa);
+      std::vector<double> abuf;
+      std::vector<int> types;
+      int adims[6];
+      size_t aoff[5];
+      std::string err;
+      if (!load_aerosolcoeff(apath, abuf, types, adims, aoff, err)) {
+        g_init_error = err;
+        crtm_gpu_destroy(h);
+        return CRTM_GPU_FAILURE;
+      }
+      if (cudaMalloc(&h->d_aero, abuf.size() * sizeof(double)) != cudaSuccess ||
+          cudaMalloc(&h->d_aero_type, types.size() * sizeof(int)) != cudaSuccess ||
+          cudaMemcpy(h->d_aero, abuf.data(), abuf.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+          cudaMemcpy(h->d_aero_type, types.data(), types.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+        g_init_error = "device upload of AerosolCoeff.bin failed";
+        crtm_gpu_destroy(h);
+        return CRTM_GPU_FAILURE;
+      }
+      AerosolLut& A = h->alut;
+      A.nw = adims[0]; A.nrh = adims[1]; A.nr = adims[2]; A.ns = adims[3]; A.nt = adims[4]; A.nleg = adims[5];
+      A.type_id = h->d_aero_type;
+      A.freq = h->d_aero + aoff[0]; A.reff = h->d_aero + aoff[1]; A.ke = h->d_aero + aoff[2];
+      A.w = h->d_aero + aoff[3]; A.pc = h->d_aero + aoff[4];
+      h->has_aerosols = true;
+    }
     GaussTable gt{};
     for (int n = 1; n <= 9; n++) double_gauss_host(n, gt.mu[n], gt.w[n]);
     if (cudaMemcpyToSymbol(c_gauss, &gt, sizeof gt) != cudaSuccess ||
@@ -1039,6 +1160,8 @@ int crtm_gpu_destroy(crtm_gpu_handle h) {
   for (auto& s : h->sensors) free_sensor(s);
   h->ws.release(); h->io_in.release(); h->io_out.release(); h->small.release();
   cudaFree(h->d_cloud);
+  cudaFree(h->d_aero);
+  cudaFree(h->d_aero_type);
   cudaFree(h->d_error);
   collect_stage_times(h);
   for (auto e : h->event_pool) cudaEventDestroy(e);

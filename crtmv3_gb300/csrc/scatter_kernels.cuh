@@ -39,6 +39,11 @@ struct ScatterArgs {
   const double* wc, *reff;      // [P][NC][Kmax]
   const int* n_streams;         // [P] or null
   const int* rt_algorithm;      // [P] or null (ADA)
+  AerosolLut alut;
+  int max_aerosols;
+  const int* n_aerosols;        // [P] (null when max_aerosols = 0)
+  const int* aerosol_type;      // [P][NA]
+  const double* conc, *aer_reff;   // [P][NA][Kmax]
   double* FB;                   // SOI fields [n][2][2][Kmax+1][NZ][L], or null
   const R* TAU;                 // [n][Kmax][L] gas layer optical depths
   R* LB;                        // [n][Kmax][NE][L] layer records
@@ -55,11 +60,15 @@ template <class R>
 __global__ void scatter_maxreff_kernel(ScatterArgs<R> a) {
   const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (p >= a.n_chunk) return;
-  const int gp = a.p_begin + p, Ku = a.b.n_layers[gp], nc = a.n_clouds[gp];
-  const double* rp = a.reff + (size_t)gp * a.max_clouds * a.Kmax;
+  const int gp = a.p_begin + p, Ku = a.b.n_layers[gp];
+  const int nc = a.max_clouds > 0 ? a.n_clouds[gp] : 0, na = a.max_aerosols > 0 ? a.n_aerosols[gp] : 0;
   double mr = 0.0;
   for (int i = lane; i < nc * Ku; i += 32) {
-    const double r = rp[(size_t)(i / Ku) * a.Kmax + (i % Ku)];
+    const double r = a.reff[((size_t)gp * a.max_clouds + i / Ku) * a.Kmax + (i % Ku)];
+    mr = r > mr ? r : mr;
+  }
+  for (int i = lane; i < na * Ku; i += 32) {
+    const double r = a.aer_reff[((size_t)gp * a.max_aerosols + i / Ku) * a.Kmax + (i % Ku)];
     mr = r > mr ? r : mr;
   }
   for (int o = 16; o > 0; o >>= 1) {
@@ -73,7 +82,7 @@ template <class R>
 __device__ __forceinline__ CloudyColumn column_inputs(const ScatterArgs<R>& a, int p, int gp, int l) {
   CloudyColumn c;
   c.Ku = a.b.n_layers[gp];
-  c.n_clouds = a.n_clouds[gp];
+  c.n_clouds = a.max_clouds > 0 ? a.n_clouds[gp] : 0;
   const int ns = a.n_streams ? a.n_streams[gp] : 0;
   c.nleg = ns > 0 ? ns : stream_rule_nleg(a.maxreff[p], a.sp.wn[l]);
   c.microwave = a.microwave != 0;
@@ -87,11 +96,17 @@ __device__ __forceinline__ CloudyColumn column_inputs(const ScatterArgs<R>& a, i
   c.planck_surface = c.c1 / (exp(c.c2 / (c.b1 + c.b2 * ts)) - 1.0);
   c.cosmic = a.sp.cbr[l];
   c.temperature = a.b.temperature + (size_t)gp * a.Kmax;
-  c.cloud_type = a.cloud_type + (size_t)gp * a.max_clouds;
-  c.wc = a.wc + (size_t)gp * a.max_clouds * a.Kmax;
-  c.reff = a.reff + (size_t)gp * a.max_clouds * a.Kmax;
+  c.cloud_type = a.max_clouds > 0 ? a.cloud_type + (size_t)gp * a.max_clouds : nullptr;
+  c.wc = a.max_clouds > 0 ? a.wc + (size_t)gp * a.max_clouds * a.Kmax : nullptr;
+  c.reff = a.max_clouds > 0 ? a.reff + (size_t)gp * a.max_clouds * a.Kmax : nullptr;
   c.cstride = (size_t)a.Kmax;
   c.soi = a.rt_algorithm && a.rt_algorithm[gp] == 168;   // RT_SOI
+  c.n_aerosols = a.max_aerosols > 0 ? a.n_aerosols[gp] : 0;
+  c.wavenumber = a.sp.wn[l];
+  c.aerosol_type = a.max_aerosols > 0 ? a.aerosol_type + (size_t)gp * a.max_aerosols : nullptr;
+  c.conc = a.max_aerosols > 0 ? a.conc + (size_t)gp * a.max_aerosols * a.Kmax : nullptr;
+  c.aer_reff = a.max_aerosols > 0 ? a.aer_reff + (size_t)gp * a.max_aerosols * a.Kmax : nullptr;
+  c.alut = &a.alut;
   return c;
 }
 
@@ -105,11 +120,12 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_layers_kernel(Scatter
   const int k = (int)((idx / L) % Kmax);
   const int p = (int)(idx / ((long long)L * Kmax));
   const int gp = a.p_begin + p;
-  if (a.pv.status[p] != 0 || a.n_clouds[gp] == 0 || k >= a.b.n_layers[gp]) return;
+  if (a.pv.status[p] != 0 || k >= a.b.n_layers[gp]) return;
   R* rec = a.LB + ((size_t)p * Kmax + k) * NE * L + l;
   const CloudyColumn c = column_inputs(a, p, gp, l);
+  if (c.n_clouds == 0 && c.n_aerosols == 0) return;
   StreamSet<NZ, double> S;
-  if (int rc = stream_set<NZ, double>(c.nleg, c.mu_sensor, a.lut.nleg, c_gauss, S)) {
+  if (int rc = stream_set<NZ, double>(c.nleg, c.mu_sensor, c.n_clouds > 0 ? a.lut.nleg : -1, c_gauss, S)) {
     rec[0] = R(-rc);
     return;
   }
@@ -146,7 +162,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_adding_kernel(Scatter
   const R* tau = a.TAU + (size_t)p * Kmax * L + l;
   double rad = 0.0;
   int code = 0;
-  if (c.n_clouds == 0) {   // clear profile: Emission solver, FP64 here
+  if (c.n_clouds == 0 && c.n_aerosols == 0) {   // clear profile: Emission solver, FP64 here
     const double inv_u = 1.0 / c.mu_sensor;
     double down = c.cosmic, tr_tot = 1.0, src = 0.0;
     for (int k = 0; k < c.Ku; k++) {
@@ -161,7 +177,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_adding_kernel(Scatter
     return;   // SOI profiles: scatter_soi_kernel
   } else {
     StreamSet<NZ, double> S;
-    code = stream_set<NZ, double>(c.nleg, c.mu_sensor, a.lut.nleg, c_gauss, S);
+    code = stream_set<NZ, double>(c.nleg, c.mu_sensor, c.n_clouds > 0 ? a.lut.nleg : -1, c_gauss, S);
     if (!code) {
       const int nZ = S.nZ;
       AddingState<NZ> A;
@@ -209,12 +225,12 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_soi_kernel(ScatterArg
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (l >= L || a.pv.status[p] != 0) return;
   const CloudyColumn c = column_inputs(a, p, gp, l);
-  if (c.n_clouds == 0 || !c.soi) return;
+  if ((c.n_clouds == 0 && c.n_aerosols == 0) || !c.soi) return;
   const size_t pl = (size_t)gp * L + l;
   double rad = 0.0;
   int code = 0;
   StreamSet<NZ, double> S;
-  code = stream_set<NZ, double>(c.nleg, c.mu_sensor, a.lut.nleg, c_gauss, S);
+  code = stream_set<NZ, double>(c.nleg, c.mu_sensor, c.n_clouds > 0 ? a.lut.nleg : -1, c_gauss, S);
   if (!code) {
     const int nZ = S.nZ;
     auto layer = [&](int k, int* kind, double* od, double* B, Mat<NZ, double>& Tm, Mat<NZ, double>& Rm,

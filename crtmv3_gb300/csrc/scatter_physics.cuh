@@ -160,6 +160,36 @@ CRTM_HD bool cloud_layer_optics(const CloudLut& C, bool microwave, double freq, 
   return true;
 }
 
+// Device copy of the AerosolCoeff LUT, scheme 'CRTM' (first RH and sigma of
+// each type; phase element 1).  Tables in the file's Fortran order.
+struct AerosolLut {
+  int nw, nrh, nr, ns, nt, nleg;
+  const int* type_id;       // [nt]
+  const double* freq;       // [nw] cm^-1, increasing
+  const double* reff;       // [nt][nr]
+  const double* ke, *w;     // [nt][ns][nr][nrh][nw]
+  const double* pc;         // [nleg+1][nt][ns][nr][nrh][nw]
+};
+
+// Get_Aerosol_Opt, scheme 'CRTM' (CRTM_AerosolScatter.f90:772-855).
+CRTM_HD bool aerosol_layer_optics(const AerosolLut& A, double wavenumber, int type, double reff, int nleg,
+                                  int loff, double* ke, double* w, double* pc) {
+  int k = -1;
+  for (int t = 0; t < A.nt; t++)
+    if (A.type_id[t] == type) { k = t; break; }
+  if (k < 0) return false;
+  const Lagrange4 F = lagrange4(A.freq, A.nw, wavenumber);
+  const Lagrange4 Rr = lagrange4(A.reff + (size_t)k * A.nr, A.nr, reff);
+  const int nu = A.nw * A.nrh;                     // radius stride
+  const size_t base = (size_t)k * A.nw * A.nrh * A.nr * A.ns;
+  const size_t n5 = (size_t)A.nw * A.nrh * A.nr * A.ns * A.nt;
+  *ke = lerp4x4(A.ke + base, nu, F, Rr);
+  *w = lerp4x4(A.w + base, nu, F, Rr);
+  pc[0] = 0.5;
+  for (int l = 1; l <= nleg; l++) pc[l] = lerp4x4(A.pc + n5 * (l + loff) + base, nu, F, Rr);
+  return true;
+}
+
 // ---- small dense matrices (row-major, fixed capacity NZ x NZ) --------------
 template <int NZ, class T>
 struct Mat {
@@ -517,6 +547,12 @@ struct CloudyColumn {
   const double* reff;
   size_t cstride;
   bool soi;                              // Options%RT_Algorithm_Id == RT_SOI
+  int n_aerosols;                        // used for non-microwave sensors only
+  double wavenumber;                     // aerosol LUT axis, cm^-1
+  const int* aerosol_type;               // [n_aerosols]
+  const double* conc;                    // [n_aerosols] rows of stride cstride, kg/m^2
+  const double* aer_reff;
+  const AerosolLut* alut;
 };
 
 // Stream angles of a (profile, channel): Gauss angles of the stream set plus
@@ -535,7 +571,7 @@ CRTM_HD int stream_set(int nleg, double mu_sensor, int lut_nleg, const GaussTabl
   S.nleg = nleg;
   S.loff = legendre_offset(nleg);
   if (S.loff < 0 || nleg > SC_NLEG_MAX) return 1;
-  if (lut_nleg < nleg + S.loff) return 2;
+  if (lut_nleg >= 0 && lut_nleg < nleg + S.loff) return 2;   // lut_nleg < 0: no clouds
   S.nS = (nleg + 2) / 2;
   if (S.nS + 1 > NZ || S.nS > 9) return 3;
   S.nZ = S.nS;
@@ -582,6 +618,24 @@ CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const Stre
     const double bs = wc * ke * w;
     bs_sum += bs;
     for (int l = 1; l <= nleg; l++) pcs[l] += pc[l] * bs;
+  }
+  if (in.n_aerosols > 0 && !in.microwave) {   // CRTM_Compute_AerosolScatter (:170-317)
+    if (nleg == 2 || !in.alut || in.alut->nleg < nleg + S.loff) return -8;
+    for (int c = 0; c < in.n_aerosols; c++) {
+      const double conc = in.conc[c * in.cstride + k];
+      if (!(conc > 1.0e-9)) continue;   // AEROSOL_CONTENT_THRESHOLD
+      double ke, w;
+      if (!aerosol_layer_optics(*in.alut, in.wavenumber, in.aerosol_type[c], in.aer_reff[c * in.cstride + k],
+                                nleg, S.loff, &ke, &w, pc))
+        return -9;
+      if (ke <= 0.0) { ke = 0.0; w = 0.0; }
+      if (w <= 0.0) { w = 0.0; for (int l = 0; l <= nleg; l++) pc[l] = 0.0; }
+      if (w >= 1.0) w = 1.0;
+      od += ke * conc;
+      const double bs = conc * ke * w;
+      bs_sum += bs;
+      for (int l = 0; l <= nleg; l++) pcs[l] += pc[l] * bs;
+    }
   }
   double ssa = bs_sum;
   if (bs_sum > BS_THRESHOLD) {   // CRTM_AtmOptics_Combine
@@ -761,7 +815,7 @@ CRTM_HD int cloudy_radiance(const CloudyColumn& in, const CloudLut& lut, const G
                             OdFn od_of, double* radiance) {
   if (in.soi) return 7;   // SOI needs every layer's record: the layered form
   StreamSet<NZ, double> S;
-  if (int rc = stream_set<NZ, double>(in.nleg, in.mu_sensor, lut.nleg, gt, S)) return rc;
+  if (int rc = stream_set<NZ, double>(in.nleg, in.mu_sensor, in.n_clouds > 0 ? lut.nleg : -1, gt, S)) return rc;
   AddingState<NZ> A;
   adding_init<NZ>(A, S.nZ, in.emissivity, in.planck_surface);
   Mat<NZ, double> Tm, Rm;

@@ -509,3 +509,76 @@ def cloudy_workload(sensor_id: str, n_profiles: int, n_layers, seed: int,
         opt.use_n_streams = ns > 0
         opt.n_streams = ns
     return atm, sfc, geo, opt
+
+
+# ---------------------------------------------------------------------------
+# Aerosols: synthetic AerosolCoeff LUT (scheme 'CRTM') and aerosol profiles
+# ---------------------------------------------------------------------------
+
+DUST_AEROSOL, SEASALT_AEROSOL, SULFATE_AEROSOL = 1, 2, 5
+AEROSOL_TYPES = (DUST_AEROSOL, SEASALT_AEROSOL, SULFATE_AEROSOL)
+AEROSOL_REFF = {DUST_AEROSOL: (0.5, 5.0), SEASALT_AEROSOL: (0.3, 3.0), SULFATE_AEROSOL: (0.05, 0.5)}
+
+
+def generate_aerosolcoeff(seed: int = 9) -> co.AerosolCoeff:
+    """20 wavelengths (frequencies increasing) x 10 RH x 40 radii x 1 sigma x 3
+    types, 38 Legendre terms; scheme 'CRTM' uses the first RH and sigma."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    wl = np.geomspace(25.0, 0.3, 20)                      # microns, decreasing
+    nu = 1.0e4 / wl                                        # cm^-1, increasing
+    nrh, nr, nt, nl = 10, 40, len(AEROSOL_TYPES), CLOUD_N_LEGENDRE
+    reff = np.stack([np.geomspace(0.01, 20.0, nr)] * nt, axis=1)
+    rsig = np.ones((1, nt))
+    rh = np.linspace(0.0, 0.99, nrh)
+    x = 2.0 * np.pi * reff[None, :, :] * nu[:, None, None] / 1.0e4          # (w, r, type)
+    q = 2.0 * x ** 2 / (1.0 + x ** 2)
+    dens = np.array([2.6, 2.2, 1.7])[None, None, :]        # g/cm^3
+    ke = 0.75 * q / (dens * 1.0e3 * reff[None, :, :] * 1.0e-6)            # m^2/kg
+    w = np.clip(np.array([0.75, 0.98, 0.95])[None, None, :] * x / (1.0 + x) + 0.02, 0.01, 0.995)
+    g = 0.7 * x / (1.0 + x)
+    jit = 1.0 + 0.02 * rng.standard_normal(ke.shape)
+    ke = ke * jit
+    ke5 = np.repeat(ke[:, None, :, None, :], nrh, axis=1)
+    w5 = np.repeat(w[:, None, :, None, :], nrh, axis=1)
+    g5 = np.repeat(g[:, None, :, None, :], nrh, axis=1)
+    pc = 0.5 * g5[..., None] ** np.arange(nl + 1)
+    return co.AerosolCoeff(np.array(AEROSOL_TYPES, np.int32), ["Dust", "SeaSalt", "Sulfate"], wl, reff,
+                           rsig, rh, ke5, w5, g5, pc[..., None])
+
+
+def write_aerosol_files(coeff_dir: str) -> str:
+    """Write ``AerosolCoeff.bin`` (the reference's default file name) if missing."""
+    os.makedirs(coeff_dir, exist_ok=True)
+    path = os.path.join(coeff_dir, "AerosolCoeff.bin")
+    if not os.path.exists(path):
+        co.write_aerosolcoeff(path + ".tmp", generate_aerosolcoeff())
+        os.replace(path + ".tmp", path)
+    return path
+
+
+def add_aerosols(atm: AtmosphereBatch, aerosol_types: Sequence[int], seed: int,
+                 load_scale: float = 1.0) -> AtmosphereBatch:
+    """Aerosols of ``aerosol_types`` in every profile: lognormal column loading
+    in 0.01-1 g/m^2 (x ``load_scale``), exponential vertical profile with a
+    1-3 km scale height, effective radius uniform in the type's range
+    (concentration stored in kg/m^2 per layer)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    P, K = atm.n_profiles, atm.max_layers
+    NA = len(aerosol_types)
+    conc = np.zeros((P, NA, K))
+    reff = np.zeros((P, NA, K))
+    for m in range(P):
+        n = int(atm.n_layers[m])
+        z = height_km(np.maximum(atm.pressure[m, :n], 1e-3))
+        dz = np.abs(np.gradient(z))
+        for a, t in enumerate(aerosol_types):
+            col = np.exp(rng.uniform(np.log(0.01), np.log(1.0))) * 1.0e-3 * load_scale   # kg/m^2
+            prof = np.exp(-z / rng.uniform(1.0, 3.0)) * dz
+            conc[m, a, :n] = col * prof / prof.sum()
+            lo, hi = AEROSOL_REFF[t]
+            reff[m, a, :n] = rng.uniform(lo, hi)
+    atm.n_aerosols = np.full(P, NA, np.int32)
+    atm.aerosol_type = np.tile(np.asarray(aerosol_types, np.int32), (P, 1))
+    atm.aerosol_concentration = conc
+    atm.aerosol_effective_radius = reff
+    return atm

@@ -97,6 +97,14 @@ typedef struct {
   /* Options%RT_Algorithm_Id for cloudy profiles: 56 ADA, 168 SOI
    * (src/CRTM_Parameters.f90:247-248); NULL: ADA everywhere. */
   const int* rt_algorithm_id;     /* [P] */
+  /* aerosols (CRTM_Aerosol_type, Atmosphere%Aerosol(:)), AerosolCoeff scheme
+   * 'CRTM'; max_aerosols = 0: none.  Aerosols scatter for infrared, visible
+   * and ultraviolet sensors only (the reference skips them for microwave). */
+  int max_aerosols;               /* NA: stride of the aerosol arrays */
+  const int* n_aerosols;          /* [P] aerosols of each profile, <= NA */
+  const int* aerosol_type;        /* [P][NA] AerosolCoeff Type ids */
+  const double* aerosol_concentration;    /* [P][NA][max_layers] kg/m^2 */
+  const double* aerosol_effective_radius; /* [P][NA][max_layers] microns */
 } crtm_gpu_batch;
 
 typedef struct {
@@ -126,9 +134,10 @@ typedef struct {
 } crtm_gpu_adjoint_out;
 
 /* CRTM_Init: loads <coeff_path>/<sensor_id>.SpcCoeff.bin and .TauCoeff.bin
- * (ODPS) for each sensor, and <coeff_path>/CloudCoeff.bin when that file
- * exists (the reference's default cloud LUT name), and uploads them to the
- * current CUDA device.  Batches with clouds need the cloud LUT. */
+ * (ODPS) for each sensor, and <coeff_path>/CloudCoeff.bin and
+ * AerosolCoeff.bin when those files exist (the reference's default LUT
+ * names), and uploads them to the current CUDA device.  Batches with clouds
+ * or aerosols need the matching LUT. */
 int crtm_gpu_init(const char* coeff_path, int n_sensors, const char* const* sensor_ids,
                   crtm_gpu_handle* handle);
 

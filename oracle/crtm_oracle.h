@@ -98,11 +98,22 @@ typedef struct {
   const double* effective_radius;  /* [P][NC][max_layers] microns               */
   const int* n_streams;            /* [P] Options%n_Streams, 0 = stream rule; may be NULL */
   const int* rt_algorithm;         /* [P] Options%RT_Algorithm_Id: 56 ADA, 168 SOI; may be NULL (ADA) */
+  int max_aerosols;                /* NA: stride of the aerosol arrays (0: none) */
+  const int* n_aerosols;           /* [P] */
+  const int* aerosol_type;         /* [P][NA] AerosolCoeff Type ids */
+  const double* aerosol_concentration;     /* [P][NA][max_layers] kg/m^2 */
+  const double* aerosol_effective_radius;  /* [P][NA][max_layers] microns */
 } or_clouds;
 
-/* Forward with clouds: ADA or SOI for profiles with clouds, Emission otherwise. */
-int or_forward_scatter(const or_handle* h, const or_cloud* cc, const or_batch* b, const or_clouds* cl,
-                       double* radiance, double* bt, int n_threads);
+typedef struct or_aerosol_s or_aerosol;
+/* Load an AerosolCoeff binary file (Release 4, scheme 'CRTM'). */
+or_aerosol* or_aerosol_init(const char* path);
+void or_aerosol_destroy(or_aerosol* a);
+
+/* Forward with clouds and aerosols: ADA or SOI for profiles with clouds or
+ * aerosols, Emission otherwise.  cc / ca may be NULL when unused. */
+int or_forward_scatter(const or_handle* h, const or_cloud* cc, const or_aerosol* ca, const or_batch* b,
+                       const or_clouds* cl, double* radiance, double* bt, int n_threads);
 
 /* Test hooks: one ADA layer (row-major nZ x nZ blocks) and the angle/phase setup. */
 int or_amom_layer(int nS, int nZ, double w, double tau, const double* mu, const double* wt,

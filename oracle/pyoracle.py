@@ -11,6 +11,7 @@ import os
 import subprocess
 
 import numpy as np
+from typing import Optional
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
@@ -35,7 +36,8 @@ class OrBatch(ct.Structure):
 class OrClouds(ct.Structure):
     _fields_ = [("max_clouds", ct.c_int), ("n_clouds", _ip), ("cloud_type", _ip),
                 ("water_content", _dp), ("effective_radius", _dp), ("n_streams", _ip),
-                ("rt_algorithm", _ip)]
+                ("rt_algorithm", _ip), ("max_aerosols", ct.c_int), ("n_aerosols", _ip),
+                ("aerosol_type", _ip), ("aerosol_concentration", _dp), ("aerosol_effective_radius", _dp)]
 
 
 def build(force: bool = False) -> str:
@@ -69,8 +71,11 @@ def lib():
         L.or_cloud_init.restype = ct.c_void_p
         L.or_cloud_init.argtypes = [ct.c_char_p]
         L.or_cloud_destroy.argtypes = [ct.c_void_p]
-        L.or_forward_scatter.argtypes = [ct.c_void_p, ct.c_void_p, ct.POINTER(OrBatch),
+        L.or_forward_scatter.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.POINTER(OrBatch),
                                          ct.POINTER(OrClouds), _dp, _dp, ct.c_int]
+        L.or_aerosol_init.restype = ct.c_void_p
+        L.or_aerosol_init.argtypes = [ct.c_char_p]
+        L.or_aerosol_destroy.argtypes = [ct.c_void_p]
         L.or_amom_layer.argtypes = [ct.c_int, ct.c_int, ct.c_double, ct.c_double, _dp, _dp, _dp, _dp,
                                     ct.c_double, _dp, _dp, _dp]
         L.or_phase_setup.argtypes = [ct.c_int, ct.c_double, _dp, _dp, _dp, _dp, _dp, _ip]
@@ -162,40 +167,56 @@ class Oracle:
             raise RuntimeError(lib().or_last_error().decode())
         return dict(radiance=rad, bt=bt, temperature_ad=ta, absorber_ad=aa, water_temperature_ad=wa)
 
-    def forward_scatter(self, atm, sfc, geo, opt, cloudcoeff_path: str, n_threads: int = 1):
-        """Forward with clouds (ADA); profiles without clouds take the Emission solver."""
+    def forward_scatter(self, atm, sfc, geo, opt, cloudcoeff_path: Optional[str] = None,
+                        aerosolcoeff_path: Optional[str] = None, n_threads: int = 1):
+        """Forward with clouds and aerosols (ADA or SOI per Options%RT_Algorithm_Id);
+        profiles without either take the Emission solver."""
         L = lib()
-        ch = L.or_cloud_init(cloudcoeff_path.encode())
-        if not ch:
-            raise IOError(L.or_last_error().decode())
+        ch = ah = None
         try:
+            if cloudcoeff_path:
+                ch = L.or_cloud_init(cloudcoeff_path.encode())
+                if not ch:
+                    raise IOError(L.or_last_error().decode())
+            if aerosolcoeff_path:
+                ah = L.or_aerosol_init(aerosolcoeff_path.encode())
+                if not ah:
+                    raise IOError(L.or_last_error().decode())
             P, nL = atm.n_profiles, self.n_channels
             b, keep = self._batch(atm, sfc, geo, opt)
-            NC = int(atm.cloud_type.shape[1]) if atm.cloud_type is not None else 0
             c = OrClouds()
-            c.max_clouds = NC
-            arrs = [np.ascontiguousarray(atm.n_clouds if atm.n_clouds is not None else np.zeros(P), np.int32),
-                    np.ascontiguousarray(atm.cloud_type if NC else np.zeros((P, 1)), np.int32),
-                    np.ascontiguousarray(atm.cloud_water_content if NC else np.zeros((P, 1, atm.max_layers))),
-                    np.ascontiguousarray(atm.cloud_effective_radius if NC else np.zeros((P, 1, atm.max_layers)))]
-            keep += arrs
-            c.n_clouds, c.cloud_type = _p(arrs[0], _ip), _p(arrs[1], _ip)
-            c.water_content, c.effective_radius = _p(arrs[2]), _p(arrs[3])
+
+            def arr(a, dt=np.float64):
+                a = np.ascontiguousarray(a, dt)
+                keep.append(a)
+                return a
+            if atm.cloud_type is not None and atm.cloud_type.shape[1] > 0:
+                c.max_clouds = int(atm.cloud_type.shape[1])
+                c.n_clouds = _p(arr(atm.n_clouds, np.int32), _ip)
+                c.cloud_type = _p(arr(atm.cloud_type, np.int32), _ip)
+                c.water_content = _p(arr(atm.cloud_water_content))
+                c.effective_radius = _p(arr(atm.cloud_effective_radius))
+            if atm.aerosol_type is not None and atm.aerosol_type.shape[1] > 0:
+                c.max_aerosols = int(atm.aerosol_type.shape[1])
+                c.n_aerosols = _p(arr(atm.n_aerosols, np.int32), _ip)
+                c.aerosol_type = _p(arr(atm.aerosol_type, np.int32), _ip)
+                c.aerosol_concentration = _p(arr(atm.aerosol_concentration))
+                c.aerosol_effective_radius = _p(arr(atm.aerosol_effective_radius))
             if opt.n_streams is not None:
-                ns = np.ascontiguousarray(np.where(opt.use_n_streams, opt.n_streams, 0), np.int32)
-                keep.append(ns)
-                c.n_streams = _p(ns, _ip)
+                use = opt.use_n_streams if opt.use_n_streams is not None else np.ones(P, bool)
+                c.n_streams = _p(arr(np.where(use, opt.n_streams, 0), np.int32), _ip)
             if opt.rt_algorithm_id is not None:
-                ra = np.ascontiguousarray(opt.rt_algorithm_id, np.int32)
-                keep.append(ra)
-                c.rt_algorithm = _p(ra, _ip)
+                c.rt_algorithm = _p(arr(opt.rt_algorithm_id, np.int32), _ip)
             rad, bt = np.zeros((P, nL)), np.zeros((P, nL))
-            st = L.or_forward_scatter(self.h, ch, ct.byref(b), ct.byref(c), _p(rad), _p(bt), n_threads)
+            st = L.or_forward_scatter(self.h, ch, ah, ct.byref(b), ct.byref(c), _p(rad), _p(bt), n_threads)
             if st:
                 raise RuntimeError(L.or_last_error().decode())
             return rad, bt
         finally:
-            L.or_cloud_destroy(ch)
+            if ch:
+                L.or_cloud_destroy(ch)
+            if ah:
+                L.or_aerosol_destroy(ah)
 
     def tangent_fd(self, atm, sfc, geo, opt, t_tl, a_tl, ts_tl, step=1e-4, n_threads: int = 1):
         P, L = atm.n_profiles, self.n_channels

@@ -35,7 +35,15 @@ int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, 
                        int nleg, int microwave, double freq, double mu_sensor, double emissivity,
                        double planck_surface, double cosmic, const double* planck, const double* temp,
                        const int* cloud_type, const double* wc, const double* reff, int cstride,
-                       const double* od, int soi, double* radiance) {
+                       const double* od, int soi, int n_aer, const int* aer_type, const double* conc,
+                       const double* aer_reff, const int* adims, const int* atypes, const double* afreq,
+                       const double* areff, const double* ake, const double* aw, const double* apc,
+                       double wavenumber, double* radiance) {
+  AerosolLut A{};
+  if (n_aer > 0) {
+    A.nw = adims[0]; A.nrh = adims[1]; A.nr = adims[2]; A.ns = adims[3]; A.nt = adims[4]; A.nleg = adims[5];
+    A.type_id = atypes; A.freq = afreq; A.reff = areff; A.ke = ake; A.w = aw; A.pc = apc;
+  }
   CloudLut L{dims[0], dims[1], dims[2], dims[3], dims[4], dims[5], dims[6], f_mw, r_mw, t, f_ir, r_ir,
              ke_l, w_l, pc_l, ke_s, w_s, pc_s, ke_ir, w_ir, pc_ir};
   static const GaussTable gt = make_gauss();
@@ -44,12 +52,14 @@ int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, 
   c.mu_sensor = mu_sensor; c.emissivity = emissivity; c.planck_surface = planck_surface; c.cosmic = cosmic;
   c.c1 = planck[0]; c.c2 = planck[1]; c.b1 = planck[2]; c.b2 = planck[3];
   c.temperature = temp; c.cloud_type = cloud_type; c.wc = wc; c.reff = reff; c.cstride = (size_t)cstride;
+  c.n_aerosols = n_aer; c.wavenumber = wavenumber; c.aerosol_type = aer_type; c.conc = conc;
+  c.aer_reff = aer_reff; c.alut = &A;
   c.soi = soi != 0;
   if (soi == 2) {   // layered ADA as the GPU kernels run it (records with NZ = 5)
     c.soi = false;
     constexpr int NZ = 5, NE = 2 + 2 * NZ * NZ + NZ;
     StreamSet<NZ, double> S;
-    if (int rc = stream_set<NZ, double>(nleg, mu_sensor, L.nleg, gt, S)) return rc;
+    if (int rc = stream_set<NZ, double>(nleg, mu_sensor, n_clouds > 0 ? L.nleg : -1, gt, S)) return rc;
     std::vector<double> rec((size_t)Ku * NE);
     for (int k = 0; k < Ku; k++) {
       Mat<NZ, double> Tm, Rm;
@@ -89,7 +99,7 @@ int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, 
   // SOI: every layer's record first, then the orders of interaction
   constexpr int NZ = SC_NZ_MAX;
   StreamSet<NZ, double> S;
-  if (int rc = stream_set<NZ, double>(nleg, mu_sensor, L.nleg, gt, S)) return rc;
+  if (int rc = stream_set<NZ, double>(nleg, mu_sensor, n_clouds > 0 ? L.nleg : -1, gt, S)) return rc;
   std::vector<int> kind(Ku);
   std::vector<double> ods(Ku);
   std::vector<Mat<NZ, double>> T(Ku), R(Ku);

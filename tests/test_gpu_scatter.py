@@ -91,3 +91,24 @@ def test_isothermal_enclosure_on_gpu(gpu_lib, cloud_dir, tmp_path):
         opt.emissivity[:] = 1.0
         rts = gpu_lib.CRTM([sensor], str(tmp_path), 0).forward(atm, sfc, geo, opt)
         assert np.abs(rts.brightness_temperature - 250.0).max() < 1e-8
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("clouds,soi", [(True, False), (False, False), (True, True)])
+def test_aerosols_match_oracle(gpu_lib, cloud_dir, precision, clouds, soi):
+    """Config C4 shape: IR sensor, liquid and ice clouds plus dust, sea salt and
+    sulfate (AerosolCoeff scheme 'CRTM'); aerosol-only profiles too."""
+    from oracle.pyoracle import Oracle
+    sensor = "irsynth_c616"
+    apath = sy.write_aerosol_files(cloud_dir)
+    atm, sfc, geo, opt = sy.clear_sky_workload(sensor, 5, 101, 68)
+    if clouds:
+        sy.add_clouds(atm, (co.WATER_CLOUD, co.ICE_CLOUD), 69, wc_scale=50.0)
+    sy.add_aerosols(atm, sy.AEROSOL_TYPES, 70, load_scale=20.0)
+    atm.n_aerosols[3] = 0
+    if soi:
+        opt.rt_algorithm_id = np.array([168, 56, 168, 168, 56], np.int32)
+    _, ref = Oracle(cloud_dir, sensor).forward_scatter(atm, sfc, geo, opt,
+                                                       f"{cloud_dir}/CloudCoeff.bin" if clouds else None, apath)
+    rts = gpu_lib.CRTM([sensor], cloud_dir, precision).forward(atm, sfc, geo, opt)
+    assert np.abs(rts.brightness_temperature - ref).max() <= BT_TOL[precision]

@@ -52,21 +52,29 @@ def test_ada_layer_matches_oracle(sx, nleg, mu_s, w, tau):
         assert np.abs(a - b).max() < 1e-12
 
 
-@pytest.mark.parametrize("sensor,nl,n_streams,soi", [("mwsynth_c16", 100, None, 0), ("mwsynth_c16", 100, 16, 0),
-                                                     ("irsynth_c616", 101, None, 0), ("mwsynth_c22", 100, 8, 0),
-                                                     ("mwsynth_c16", 100, None, 1), ("mwsynth_c16", 100, 16, 1),
-                                                     ("irsynth_c616", 101, None, 1),
-                                                     ("mwsynth_c16", 100, None, 2), ("irsynth_c616", 101, None, 2)])
-def test_cloudy_radiance_matches_oracle(sx, coeff_dir, sensor, nl, n_streams, soi):
+@pytest.mark.parametrize("sensor,nl,n_streams,soi,aer", [
+    ("mwsynth_c16", 100, None, 0, 0), ("mwsynth_c16", 100, 16, 0, 0), ("irsynth_c616", 101, None, 0, 0),
+    ("mwsynth_c22", 100, 8, 0, 0), ("mwsynth_c16", 100, None, 1, 0), ("mwsynth_c16", 100, 16, 1, 0),
+    ("irsynth_c616", 101, None, 1, 0), ("mwsynth_c16", 100, None, 2, 0), ("irsynth_c616", 101, None, 2, 0),
+    ("irsynth_c616", 101, None, 0, 1), ("irsynth_c616", 101, 8, 1, 1), ("irsynth_c616", 101, None, 0, 2),
+    ("mwsynth_c16", 100, None, 0, 1)])
+def test_cloudy_radiance_matches_oracle(sx, coeff_dir, sensor, nl, n_streams, soi, aer):
+    """aer 1: clouds and aerosols; aer 2: aerosols only."""
     from oracle.pyoracle import Oracle
     path = sy.write_cloud_files(coeff_dir)
+    apath = sy.write_aerosol_files(coeff_dir)
     cc = co.read_cloudcoeff(path)
+    ac = co.read_aerosolcoeff(apath)
     sc = co.read_spccoeff(f"{coeff_dir}/{sensor}.SpcCoeff.bin")
     o = Oracle(coeff_dir, sensor)
     atm, sfc, geo, opt = sy.cloudy_workload(sensor, 3, nl, 51, wc_scale=200.0, n_streams=n_streams)
     if soi == 1:
         opt.rt_algorithm_id = np.full(atm.n_profiles, 168, np.int32)
-    rad_ref, _ = o.forward_scatter(atm, sfc, geo, opt, path)
+    if aer:
+        sy.add_aerosols(atm, sy.AEROSOL_TYPES, 52, load_scale=30.0)
+    if aer == 2:
+        atm.n_clouds[:] = 0
+    rad_ref, _ = o.forward_scatter(atm, sfc, geo, opt, path, apath if aer else None)
     _, _, lod = o.forward(atm, sfc, geo, opt, layer_od=True)
     f = lambda a: np.ascontiguousarray(np.ravel(a, order="F"))   # noqa: E731
     arrs = [f(x) for x in (cc.frequency_mw, cc.reff_mw, cc.temperature, cc.frequency_ir, cc.reff_ir,
@@ -75,6 +83,10 @@ def test_cloudy_radiance_matches_oracle(sx, coeff_dir, sensor, nl, n_streams, so
     dims = np.array([cc.frequency_mw.size, cc.reff_mw.size, cc.temperature.size, cc.density_mw.size,
                      cc.frequency_ir.size, cc.reff_ir.size, cc.n_legendre_terms], np.int32)
     mw = sc.sensor_type == co.MICROWAVE_SENSOR
+    adims = np.array([ac.wavelength.size, ac.ke.shape[1], ac.ke.shape[2], ac.ke.shape[3], ac.ke.shape[4],
+                      ac.pcoeff.shape[5] - 1], np.int32)
+    aarrs = [np.ascontiguousarray(ac.type_id, np.int32)] + [f(x) for x in (
+        1.0e4 / ac.wavelength, ac.reff, ac.ke, ac.w, ac.pcoeff[..., 0])]
     L = sc.n_channels
     chans = range(0, L, max(1, L // 40))
     worst = 0.0
@@ -87,6 +99,11 @@ def test_cloudy_radiance_matches_oracle(sx, coeff_dir, sensor, nl, n_streams, so
         wc = np.ascontiguousarray(atm.cloud_water_content[m])
         re = np.ascontiguousarray(atm.cloud_effective_radius[m])
         ctype = np.ascontiguousarray(atm.cloud_type[m], np.int32)
+        nc = int(atm.n_clouds[m])
+        na = int(atm.n_aerosols[m]) if aer else 0
+        atype = np.ascontiguousarray(atm.aerosol_type[m] if aer else np.zeros(1), np.int32)
+        conc = np.ascontiguousarray(atm.aerosol_concentration[m] if aer else np.zeros((1, atm.max_layers)))
+        areff = np.ascontiguousarray(atm.aerosol_effective_radius[m] if aer else np.zeros((1, atm.max_layers)))
         for l in chans:
             planck = np.array([sc.planck_c1[l], sc.planck_c2[l], sc.band_c1[l], sc.band_c2[l]])
             te = sc.band_c1[l] + sc.band_c2[l] * ts
@@ -94,15 +111,18 @@ def test_cloudy_radiance_matches_oracle(sx, coeff_dir, sensor, nl, n_streams, so
             if n_streams:
                 nleg = n_streams
             else:
-                nleg = sx.sx_stream_rule(ct.c_double(re[:, :Ku].max()), ct.c_double(sc.wavenumber[l]))
+                mr = max(re[:nc, :Ku].max() if nc else 0.0, areff[:na, :Ku].max() if na else 0.0)
+                nleg = sx.sx_stream_rule(ct.c_double(mr), ct.c_double(sc.wavenumber[l]))
             od = np.ascontiguousarray(lod[m, l, :Ku])
             r = ct.c_double(0.0)
             rc = sx.sx_cloudy_radiance(
-                _p(dims, _ip), *[_p(a) for a in arrs], Ku, NC, nleg, int(mw),
+                _p(dims, _ip), *[_p(a) for a in arrs], Ku, nc, nleg, int(mw),
                 ct.c_double(sc.frequency[l] if mw else sc.wavenumber[l]), ct.c_double(mu),
                 ct.c_double(opt.emissivity[m, l]), ct.c_double(bs),
                 ct.c_double(sc.cosmic_background_radiance[l]), _p(planck), _p(temp), _p(ctype, _ip),
-                _p(wc), _p(re), atm.max_layers, _p(od), soi, ct.byref(r))
+                _p(wc), _p(re), atm.max_layers, _p(od), soi, na, _p(atype, _ip), _p(conc), _p(areff),
+                _p(adims, _ip), _p(aarrs[0], _ip), *[_p(a) for a in aarrs[1:]],
+                ct.c_double(sc.wavenumber[l]), ct.byref(r))
             assert rc == 0
             worst = max(worst, abs(r.value - rad_ref[m, l]) / abs(rad_ref[m, l]))
     assert worst < 1e-11
