@@ -9,7 +9,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libcrtm_gb300.so")
 SOURCES = ["crtm_gpu.cu"]
-HEADERS = ["odps_physics.cuh", "odps_prep.cuh", "odps_kernels.cuh"]
+HEADERS = ["odps_physics.cuh", "odps_prep.cuh", "odps_kernels.cuh", "scatter_physics.cuh",
+           "scatter_kernels.cuh", "dual.cuh"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
               "--expt-relaxed-constexpr", "-lineinfo", "-Xcompiler", "-fPIC", "-shared"]
 

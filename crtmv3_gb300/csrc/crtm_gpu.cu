@@ -518,9 +518,10 @@ struct Work {
   R* SC;            // [n][L]
   double* TSK;      // adjoint: [n][L]
   R* RA;            // [n][nv][K][L]
-  R* LB;            // cloudy forward: [n][Kmax][NE][L] layer records
+  R* LB;            // scattering: [n][Kmax][NE][L] layer records
   double* FB;       // cloudy forward with SOI: [n][2][2][Kmax+1][NZ][L] fields
-  double* maxreff;  // cloudy forward: [n]
+  double* maxreff;  // scattering: [n]
+  double* AS;       // scattering K-matrix/adjoint: [n][Kmax+1][NZ*NZ+NZ][L] adding states
   double* ras;      // adjoint: [n][nv][K]
   double* pts;      // adjoint: [n][Kmax]
   double* tss;      // adjoint: [n]
@@ -537,9 +538,16 @@ template <> struct Tune<3, float> { static constexpr int FWD = 8, AD = 8; };
 // profiles per absorb_ad CTA
 template <int G, class R> constexpr int ad_profiles() { return Tune<G, R>::AD * AD_WARPS; }
 
+// Scattering part of a chunk's workspace: layer record length (0: none),
+// angles of the kernels, SOI fields, adding states of the K-matrix.
+struct ScatterWork {
+  int rec = 0, nz = 0;
+  bool soi = false, kstate = false;
+};
+
 template <int G, class R>
 size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w, char* base,
-                  bool soi_fields = false) {
+                  const ScatterWork& sw = ScatterWork()) {
   const int K = s.K, L = s.L, NS = s.NS, NX = DLayout<G>::NX;
   const int npf = Tune<G, R>::FWD, npa = Tune<G, R>::AD;
   size_t off = 0;
@@ -568,13 +576,14 @@ size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w
   Work<R> wk{};
   wk.pv = pv;
   wk.OD = (R*)carve(nn * K * L * sizeof(R));
-  if (mode == 3) {   // nv carries the layer record length here
-    wk.TAU = (R*)carve(nn * Kmax * L * sizeof(R));
-    wk.LB = (R*)carve(nn * Kmax * (size_t)nv * L * sizeof(R));
+  if (mode == 3) wk.TAU = (R*)carve(nn * Kmax * L * sizeof(R));
+  if (sw.rec > 0) {
+    wk.LB = (R*)carve(nn * Kmax * (size_t)sw.rec * L * sizeof(R));
     wk.maxreff = (double*)carve(nn * sizeof(double));
-    // SOI fields: 2 fields x 2 buffers x levels x angles (angles <= NZ <= record length)
-    const size_t nz = nv == 2 + 2 * SC_NZ_MAX * SC_NZ_MAX + SC_NZ_MAX ? SC_NZ_MAX : 5;
-    wk.FB = soi_fields ? (double*)carve(nn * 4 * (size_t)(Kmax + 1) * nz * L * sizeof(double)) : nullptr;
+    // SOI fields: 2 fields x 2 buffers x levels x angles
+    wk.FB = sw.soi ? (double*)carve(nn * 4 * (size_t)(Kmax + 1) * sw.nz * L * sizeof(double)) : nullptr;
+    wk.AS = sw.kstate ? (double*)carve(nn * (size_t)(Kmax + 1) * (sw.nz * sw.nz + sw.nz) * L * sizeof(double))
+                      : nullptr;
   }
   if (adj) {
     wk.TAU = (R*)carve(nn * Kmax * L * sizeof(R));
@@ -657,7 +666,7 @@ template <int G, class R>
 int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, int mode,
                  const double* seed, crtm_gpu_rtsolution* rts, crtm_gpu_kmatrix* kk,
                  crtm_gpu_adjoint_out* ad, cudaStream_t st, const HostCopy* hc,
-                 const FixedScratch* fixed) {
+                 const FixedScratch* fixed, bool scat) {
   const int P = b->n_profiles, Kmax = b->max_layers, L = s.L, K = s.K, n_abs = b->n_absorbers;
   if (P <= 0) return CRTM_GPU_SUCCESS;
   if (Kmax < 2 || Kmax > MAX_LAYERS) return fail(h, "max_layers %d out of range [2, %d]", Kmax, MAX_LAYERS);
@@ -687,32 +696,39 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
     for (int j = 0; j < n_abs; j++) oa.odps[j] = abs_of_user[j];
   }
   const int nv = 1 + oa.n;
-  // cloudy forward: NZ angles of the kernels (16-stream option or the stream rule)
-  const bool nz_max = mode == 3 && b->n_streams != nullptr;
-  const int wnv = mode == 3 ? (nz_max ? layer_record<SC_NZ_MAX>() : layer_record<5>()) : nv;
+  // scattering: NZ angles of the kernels (16-stream option or the stream rule)
+  const bool nz_max = scat && b->n_streams != nullptr;
   const bool soi = mode == 3 && b->rt_algorithm_id != nullptr;
+  ScatterWork sw;
+  if (scat) {
+    sw.nz = nz_max ? SC_NZ_MAX : 5;
+    sw.soi = soi;
+    sw.kstate = mode != 3;
+    sw.rec = mode == 3 ? (nz_max ? layer_record<SC_NZ_MAX>() : layer_record<5>())
+                       : (nz_max ? layer_record_k<SC_NZ_MAX>() : layer_record_k<5>());
+  }
   // chunk size from the workspace budget
-  const size_t per = work_bytes<G, R>(s, 64, Kmax, wnv, mode, nullptr, nullptr, soi) / 64 + 1;
+  const size_t per = work_bytes<G, R>(s, 64, Kmax, nv, mode, nullptr, nullptr, sw) / 64 + 1;
   int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)P, h->workspace_budget / per));
   if (hc && hc->max_chunk > 0) chunk = std::min(chunk, hc->max_chunk);
   char* ws_base;
   if (fixed) {
     // largest chunk whose workspace fits the fixed scratch
     chunk = (int)std::min<size_t>((size_t)chunk, fixed->bytes / per);
-    while (chunk > 1 && work_bytes<G, R>(s, chunk, Kmax, wnv, mode, nullptr, nullptr, soi) > fixed->bytes) chunk--;
-    const size_t one = work_bytes<G, R>(s, 1, Kmax, wnv, mode, nullptr, nullptr, soi);
+    while (chunk > 1 && work_bytes<G, R>(s, chunk, Kmax, nv, mode, nullptr, nullptr, sw) > fixed->bytes) chunk--;
+    const size_t one = work_bytes<G, R>(s, 1, Kmax, nv, mode, nullptr, nullptr, sw);
     if (chunk < 1 || one > fixed->bytes)
       return fail(h, "one profile of this call needs %zu bytes of scratch (%d channels, max_layers %d, "
                      "%d absorber Jacobians); the static scratch holds %zu bytes",
                   one, L, Kmax, nv - 1, fixed->bytes);
     ws_base = fixed->base;
   } else {
-    const size_t need = work_bytes<G, R>(s, chunk, Kmax, wnv, mode, nullptr, nullptr, soi);
+    const size_t need = work_bytes<G, R>(s, chunk, Kmax, nv, mode, nullptr, nullptr, sw);
     if (!h->ws.ensure(need)) return fail(h, "cannot allocate %zu bytes of workspace", need);
     ws_base = (char*)h->ws.p;
   }
   Work<R> w;
-  work_bytes<G, R>(s, chunk, Kmax, wnv, mode, &w, ws_base, soi);
+  work_bytes<G, R>(s, chunk, Kmax, nv, mode, &w, ws_base, sw);
   if (cudaMemcpyAsync(w.idx_map, idx_map, sizeof(int) * s.Jm, cudaMemcpyHostToDevice, st) != cudaSuccess)
     return fail(h, "absorber map upload failed");
   const BatchView bv = make_view(b);
@@ -754,13 +770,20 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
     ca.tsk = mode == 1 ? kk->water_temperature : (mode == 2 ? w.TSK : nullptr);
     ca.ek = mode == 1 ? kk->surface_emissivity : nullptr;
     ca.status = rts->status;
+    // scattering K-matrix/adjoint: the column runs twice around the scattering kernels
+    const bool split = scat && mode != 3;
+    if (split) {
+      ca.pass = 1;
+      ca.n_clouds = b->max_clouds > 0 ? b->n_clouds : nullptr;
+      ca.n_aerosols = b->max_aerosols > 0 ? b->n_aerosols : nullptr;
+    }
+    dim3 gc((L + 127) / 128, n);
     {
       StageScope sc(h, 2, st);
-      dim3 gc((L + 127) / 128, n);
       column_kernel<R><<<gc, 128, col_smem, st>>>(ca);
       CK_LAUNCH(h);
     }
-    if (mode == 3) {   // cloudy forward: layer optics, then the adding from the surface
+    if (scat) {   // layer optics, then the adding from the surface (and its adjoint)
       ScatterArgs<R> sa{};
       sa.K = K; sa.L = L; sa.Kmax = Kmax; sa.p_begin = p0; sa.n_chunk = n;
       sa.microwave = s.sensor_type == 1;
@@ -775,6 +798,8 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       sa.TAU = w.TAU; sa.LB = w.LB; sa.maxreff = w.maxreff;
       sa.radiance = rts->radiance; sa.bt = rts->brightness_temperature;
       sa.status = rts->status; sa.error = h->d_error;
+      sa.mode = mode; sa.TOD = w.TAU; sa.PT = w.PT; sa.SC = w.SC; sa.seed = seed;
+      sa.tsk = ca.tsk; sa.ek = ca.ek; sa.AS = w.AS;
       const long long nlay = (long long)n * Kmax * L;
       const unsigned gl = (unsigned)((nlay + SCATTER_THREADS - 1) / SCATTER_THREADS);
       dim3 ga((L + SCATTER_THREADS - 1) / SCATTER_THREADS, n);
@@ -782,13 +807,32 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
         StageScope sc(h, 6, st);
         scatter_maxreff_kernel<R><<<(n + 3) / 4, 128, 0, st>>>(sa);
         CK_LAUNCH(h);
-        if (nz_max)
+        if (split) {
+          if (nz_max)
+            scatter_layers_k_kernel<SC_NZ_MAX, R><<<gl, SCATTER_THREADS, 0, st>>>(sa);
+          else
+            scatter_layers_k_kernel<5, R><<<gl, SCATTER_THREADS, 0, st>>>(sa);
+        } else if (nz_max) {
           scatter_layers_kernel<SC_NZ_MAX, R><<<gl, SCATTER_THREADS, 0, st>>>(sa);
-        else
+        } else {
           scatter_layers_kernel<5, R><<<gl, SCATTER_THREADS, 0, st>>>(sa);
+        }
         CK_LAUNCH(h);
       }
-      {
+      if (split) {
+        {
+          StageScope sc(h, 7, st);
+          if (nz_max)
+            scatter_kmatrix_kernel<SC_NZ_MAX, R><<<ga, SCATTER_THREADS, 0, st>>>(sa);
+          else
+            scatter_kmatrix_kernel<5, R><<<ga, SCATTER_THREADS, 0, st>>>(sa);
+          CK_LAUNCH(h);
+        }
+        ca.pass = 2;
+        StageScope sc(h, 2, st);
+        column_kernel<R><<<gc, 128, col_smem, st>>>(ca);
+        CK_LAUNCH(h);
+      } else {
         StageScope sc(h, 7, st);
         if (nz_max)
           scatter_adding_kernel<SC_NZ_MAX, R><<<ga, SCATTER_THREADS, 0, st>>>(sa);
@@ -876,8 +920,8 @@ int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, c
   if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
   const Sensor& s = h->sensors[sensor];
   const bool fp64 = h->precision == CRTM_GPU_FP64;
-  if (b->max_clouds > 0 || b->max_aerosols > 0) {
-    if (mode != 0) return fail(h, "the K-matrix and adjoint are not available for batches with clouds or aerosols");
+  const bool scat = b->max_clouds > 0 || b->max_aerosols > 0;
+  if (scat) {
     if (b->max_clouds > 0 && !h->has_clouds) return fail(h, "batch has clouds but no CloudCoeff.bin was loaded at init");
     if (b->max_aerosols > 0 && !h->has_aerosols && s.sensor_type != 1)
       return fail(h, "batch has aerosols but no AerosolCoeff.bin was loaded at init");
@@ -887,15 +931,15 @@ int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, c
                                 !b->aerosol_effective_radius))
       return fail(h, "aerosol arrays missing for max_aerosols = %d", b->max_aerosols);
     if (cudaMemsetAsync(h->d_error, 0, sizeof(int), st) != cudaSuccess) return fail(h, "error flag reset failed");
-    mode = 3;
+    if (mode == 0) mode = 3;
   }
   switch (s.group) {
-    case 1: return fp64 ? run_pipeline<1, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed)
-                        : run_pipeline<1, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed);
-    case 2: return fp64 ? run_pipeline<2, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed)
-                        : run_pipeline<2, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed);
-    default: return fp64 ? run_pipeline<3, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed)
-                         : run_pipeline<3, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed);
+    case 1: return fp64 ? run_pipeline<1, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat)
+                        : run_pipeline<1, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat);
+    case 2: return fp64 ? run_pipeline<2, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat)
+                        : run_pipeline<2, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat);
+    default: return fp64 ? run_pipeline<3, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat)
+                         : run_pipeline<3, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat);
   }
 }
 
@@ -1046,7 +1090,8 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
     if (cudaMemcpy(&code, h->d_error, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
       return fail(h, "cannot read the scattering error flag");
     if (code) return fail(h, "scattering radiative transfer failed (code %d: 1-3 stream set, 4 cloud type, "
-                             "5-6 singular matrix, 8 aerosol stream set or LUT, 9 aerosol type)", code);
+                             "5-6 singular matrix, 8 aerosol stream set or LUT, 9 aerosol type, 10 K-matrix or adjoint "
+                             "requested with RT_SOI)", code);
   }
   if (rts->status)
     for (int m = 0; m < P; m++)

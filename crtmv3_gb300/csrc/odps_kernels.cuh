@@ -602,6 +602,12 @@ struct ColumnArgs {
   double* radiance, *bt;  // [P][L]
   double* tsk, *ek;       // K-matrix: [P][L]; adjoint: tsk is [n][L] scratch
   int* status;            // [P] or null
+  // Scattering profiles in a K-matrix/adjoint call: launched twice.  pass 1
+  // stores TAU/DTOP and stops; the scattering K kernel then overwrites TAU of
+  // scattering profiles with dR/dtau; pass 2 finishes clear profiles as usual
+  // and, for scattering profiles, maps dR/dtau onto the reference levels.
+  int pass;                      // 0: one launch (no scattering profiles)
+  const int* n_clouds, *n_aerosols;   // [P] or null
 };
 
 template <class R>
@@ -696,8 +702,10 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
         if (a.mode == 0) {
           src += tr * B * (R(1) - t);
         } else {
-          a.TAU[cs + (size_t)ku * L] = tau;
-          if (a.mode != 3) a.DTOP[cs + (size_t)ku * L] = rad_down;
+          if (a.pass != 2) {
+            a.TAU[cs + (size_t)ku * L] = tau;
+            if (a.mode != 3) a.DTOP[cs + (size_t)ku * L] = rad_down;
+          }
         }
         tr *= t;
         total += tau;
@@ -721,6 +729,7 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
     return;
   }
   if (a.mode == 3) return;   // gas layer optical depths only (the cloudy solver follows)
+  if (a.pass == 1) return;   // TAU/DTOP stored; the scattering K kernel runs next
   // ---- pass 2 (bottom up): upwelling, Emission adjoint, OD path adjoint (unit seed)
   R U = re * Bs + rr * Dn;
   R P = R(1);                 // transmittance of the layers below the current one
@@ -748,6 +757,19 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
       pa_hi += f * v;
     }
   };
+  if (a.pass == 2 && ((a.n_clouds && a.n_clouds[gp] > 0) || (a.n_aerosols && a.n_aerosols[gp] > 0))) {
+    // scattering profile: TAU holds dR/dtau from the scattering K kernel, which
+    // also wrote PT, SC and the surface and radiance outputs
+    for (int ku = Ku - 1; ku >= 0; ku--) {
+      const R tod = a.TAU[cs + (size_t)ku * L];
+      ua_hi += tod * inv_sec;
+      scatter(ku + 1, ua_hi);
+      ua_hi = -tod * inv_sec;
+    }
+    scatter(0, ua_hi);
+    while (plvl >= 0) flush();
+    return;
+  }
   R tau_n = a.TAU[cs + (size_t)(Ku - 1) * L], dt_n = a.DTOP[cs + (size_t)(Ku - 1) * L];
   for (int ku = Ku - 1; ku >= 0; ku--) {
     const R tau = tau_n, Dtop = dt_n;

@@ -14,6 +14,24 @@
 // Per-layer results go through HBM with channels fastest:
 // LB[p][k][e][l], e = 0 kind (0 clear, 1 scattering, <0 error), 1 optical
 // depth, then T (NZ*NZ), R (NZ*NZ) and the source (NZ).
+//
+// K-matrix and adjoint of scattering profiles (ADA), between the two column
+// launches:
+//
+//   scatter_layers_k_kernel  one thread per (profile, layer, channel): the
+//                            layer optics on derivative numbers (directions:
+//                            gas optical depth, temperature); the record adds
+//                            the derivatives of T, R, the source and the
+//                            optical depth (layer_record_k).
+//   scatter_kmatrix_kernel   one thread per (profile, channel): the adding
+//                            from the surface with the level states kept in
+//                            AS, then the adding adjoint from the top down,
+//                            contracted with the layer derivatives.  Writes
+//                            dR/dtau of each user layer over TAU (the second
+//                            column launch maps it onto the reference
+//                            levels), the Planck part of the temperature
+//                            adjoint into PT, the adjoint seed into SC, and
+//                            the surface adjoints.
 #pragma once
 
 #include "odps_kernels.cuh"
@@ -25,6 +43,14 @@ __constant__ GaussTable c_gauss;
 
 template <int NZ>
 constexpr int layer_record() { return 2 + 2 * NZ * NZ + NZ; }
+// K-matrix layer record: kind, optical depth, the values of T, R and the
+// source (NV = 2 NZ^2 + NZ), their derivatives with respect to the gas optical
+// depth and to the temperature (NV each), then the optical depth's two.
+template <int NZ>
+constexpr int layer_record_k() { return 4 + 3 * (2 * NZ * NZ + NZ); }
+// adding state per level: Rup (NZ*NZ) and the upwelling radiance (NZ)
+template <int NZ>
+constexpr int adding_state_size() { return NZ * NZ + NZ; }
 
 template <class R>
 struct ScatterArgs {
@@ -51,6 +77,14 @@ struct ScatterArgs {
   double* radiance, *bt;        // [P][L]
   int* status;                  // [P] or null
   int* error;                   // first failing code (device), 0 if none
+  // K-matrix (mode 1) and adjoint (mode 2)
+  int mode;
+  R* TOD;                       // [n][Kmax][L] out: dR/dtau of the user layers (aliases TAU)
+  R* PT;                        // [n][Kmax][L] out: dR/dT at fixed gas optical depth
+  R* SC;                        // [n][L] out: dBT/dR * seed
+  const double* seed;           // [P][L] or null (=1)
+  double* tsk, *ek;             // K-matrix: [P][L]; adjoint: tsk is [n][L]
+  double* AS;                   // [n][Kmax+1][NS][L] adding states
 };
 
 constexpr int SCATTER_THREADS = 128;
@@ -132,7 +166,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_layers_kernel(Scatter
   Mat<NZ, R> Tm, Rm;
   R src[NZ], od;
   const double gas = double(a.TAU[((size_t)p * Kmax + k) * L + l]);
-  const int kind = layer_optics<NZ, R>(c, a.lut, S, k, gas, &od, Tm, Rm, src);
+  const int kind = layer_optics<NZ, R>(c, a.lut, S, k, gas, c.temperature[k], &od, Tm, Rm, src);
   rec[0] = R(kind);
   rec[(size_t)L] = od;
   if (kind != 1) return;
@@ -264,6 +298,146 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_soi_kernel(ScatterArg
   }
   a.radiance[pl] = rad;
   a.bt[pl] = code ? 0.0 : planck_temperature(c.c1, c.c2, c.b1, c.b2, rad);
+}
+
+template <int NZ, class R>
+__global__ void __launch_bounds__(SCATTER_THREADS) scatter_layers_k_kernel(ScatterArgs<R> a) {
+  constexpr int NE = layer_record_k<NZ>(), NV = 2 * NZ * NZ + NZ;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int L = a.L, Kmax = a.Kmax;
+  if (idx >= (long long)a.n_chunk * Kmax * L) return;
+  const int l = (int)(idx % L);
+  const int k = (int)((idx / L) % Kmax);
+  const int p = (int)(idx / ((long long)L * Kmax));
+  const int gp = a.p_begin + p;
+  if (a.pv.status[p] != 0 || k >= a.b.n_layers[gp]) return;
+  R* rec = a.LB + ((size_t)p * Kmax + k) * NE * L + l;
+  const CloudyColumn c = column_inputs(a, p, gp, l);
+  if (c.n_clouds == 0 && c.n_aerosols == 0) return;
+  if (c.soi) { rec[0] = R(-10); return; }   // SOI K-matrix: not available
+  StreamSet<NZ, double> S;
+  if (int rc = stream_set<NZ, double>(c.nleg, c.mu_sensor, c.n_clouds > 0 ? a.lut.nleg : -1, c_gauss, S)) {
+    rec[0] = R(-rc);
+    return;
+  }
+  using D = Dual<2>;
+  D gd(double(a.TAU[((size_t)p * Kmax + k) * L + l])), tt(c.temperature[k]);
+  gd.d[0] = 1.0;
+  tt.d[1] = 1.0;
+  Mat<NZ, D> Tm, Rm;
+  D src[NZ], od;
+  const int kind = layer_optics<NZ, D, D>(c, a.lut, S, k, gd, tt, &od, Tm, Rm, src);
+  rec[0] = R(kind);
+  rec[(size_t)L] = R(od.v);
+  rec[(size_t)(2 + 3 * NV) * L] = R(od.d[0]);
+  rec[(size_t)(3 + 3 * NV) * L] = R(od.d[1]);
+  if (kind != 1) return;
+  const int nZ = S.nZ;
+  for (int i = 0; i < nZ; i++) {
+    for (int j = 0; j < nZ; j++) {
+      const size_t et = (size_t)(2 + i * NZ + j), er = et + NZ * NZ;
+      rec[et * L] = R(Tm.a[i][j].v);
+      rec[(et + NV) * L] = R(Tm.a[i][j].d[0]);
+      rec[(et + 2 * NV) * L] = R(Tm.a[i][j].d[1]);
+      rec[er * L] = R(Rm.a[i][j].v);
+      rec[(er + NV) * L] = R(Rm.a[i][j].d[0]);
+      rec[(er + 2 * NV) * L] = R(Rm.a[i][j].d[1]);
+    }
+    const size_t es = (size_t)(2 + 2 * NZ * NZ + i);
+    rec[es * L] = R(src[i].v);
+    rec[(es + NV) * L] = R(src[i].d[0]);
+    rec[(es + 2 * NV) * L] = R(src[i].d[1]);
+  }
+}
+
+template <int NZ, class R>
+__global__ void __launch_bounds__(SCATTER_THREADS) scatter_kmatrix_kernel(ScatterArgs<R> a) {
+  constexpr int NE = layer_record_k<NZ>(), NV = 2 * NZ * NZ + NZ, NS = adding_state_size<NZ>();
+  const int L = a.L, Kmax = a.Kmax;
+  const int p = blockIdx.y, gp = a.p_begin + p;
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= L || a.pv.status[p] != 0) return;
+  const CloudyColumn c = column_inputs(a, p, gp, l);
+  if (c.n_clouds == 0 && c.n_aerosols == 0) return;   // clear: the column kernel's Emission adjoint
+  const size_t pl = (size_t)gp * L + l;
+  R* tod = a.TOD + (size_t)p * Kmax * L + l;
+  R* pt = a.PT + (size_t)p * Kmax * L + l;
+  double rad = 0.0, e_b = 0.0, Bs_b = 0.0;
+  StreamSet<NZ, double> S;
+  int code = stream_set<NZ, double>(c.nleg, c.mu_sensor, c.n_clouds > 0 ? a.lut.nleg : -1, c_gauss, S);
+  if (!code) {
+    const int nZ = S.nZ;
+    auto rec_of = [&](int k) { return a.LB + ((size_t)p * Kmax + k) * NE * L + l; };
+    auto layer = [&](int k, int* kind, double* od, Mat<NZ, double>& Tm, Mat<NZ, double>& Rm, double* src) {
+      const R* rec = rec_of(k);
+      *kind = (int)rec[0];
+      *od = double(rec[(size_t)L]);
+      if (*kind != 1) return;
+      for (int i = 0; i < nZ; i++) {
+        for (int j = 0; j < nZ; j++) {
+          Tm.a[i][j] = double(rec[(size_t)(2 + i * NZ + j) * L]);
+          Rm.a[i][j] = double(rec[(size_t)(2 + NZ * NZ + i * NZ + j) * L]);
+        }
+        src[i] = double(rec[(size_t)(2 + 2 * NZ * NZ + i) * L]);
+      }
+    };
+    double* as = a.AS + (size_t)p * (Kmax + 1) * NS * L + l;
+    auto state = [&](int lev, int i) -> double& { return as[((size_t)lev * NS + i) * L]; };
+    auto contract = [&](int k, int kind, const Mat<NZ, double>& T_b, const Mat<NZ, double>& R_b,
+                        const double* src_b, double od_b, double* g) {
+      const R* rec = rec_of(k);
+      if (kind != 1) {
+        g[0] = od_b * double(rec[(size_t)(2 + 3 * NV) * L]);
+        g[1] = od_b * double(rec[(size_t)(3 + 3 * NV) * L]);
+        return true;
+      }
+      for (int d = 0; d < 2; d++) {
+        const R* r = rec + (size_t)(2 + (1 + d) * NV) * L;
+        double acc = 0.0;
+        for (int i = 0; i < nZ; i++) {
+          for (int j = 0; j < nZ; j++)
+            acc += T_b.a[i][j] * double(r[(size_t)(i * NZ + j) * L]) +
+                   R_b.a[i][j] * double(r[(size_t)(NZ * NZ + i * NZ + j) * L]);
+          acc += src_b[i] * double(r[(size_t)(2 * NZ * NZ + i) * L]);
+        }
+        g[d] = acc;
+      }
+      return true;
+    };
+    auto out = [&](int k, double g, double t) {
+      tod[(size_t)k * L] = R(g);
+      pt[(size_t)k * L] = R(t);
+    };
+    code = cloudy_kmatrix<NZ>(c, S, layer, state, contract, out, &rad, &e_b, &Bs_b);
+  }
+  double scale = 0.0, ts_ad = 0.0, btv = 0.0;
+  if (code) {
+    atomicCAS(a.error, 0, code);
+    if (a.status) atomicOr(a.status + gp, 1 << 4);
+    rad = 0.0;
+    e_b = 0.0;
+    for (int k = 0; k < Kmax; k++) { tod[(size_t)k * L] = R(0); pt[(size_t)k * L] = R(0); }
+  } else {
+    for (int k = c.Ku; k < Kmax; k++) pt[(size_t)k * L] = R(0);
+    double dtdr;
+    planck_temperature_with_dR(c.c1, c.c2, c.b1, c.b2, rad, &btv, &dtdr);
+    scale = dtdr * (a.seed ? a.seed[pl] : 1.0);
+    // surface temperature: d(Planck)/dTs of the water surface
+    const double ts = a.b.land_cov[gp] * a.b.land_t[gp] + a.b.water_cov[gp] * a.b.water_t[gp] +
+                      a.b.snow_cov[gp] * a.b.snow_t[gp] + a.b.ice_cov[gp] * a.b.ice_t[gp];
+    const double te = c.b1 + c.b2 * ts, ee = exp(c.c2 / te);
+    const double dBs = c.c1 * c.c2 * ee * c.b2 / (te * te * (ee - 1.0) * (ee - 1.0));
+    ts_ad = a.b.water_cov[gp] * dBs * Bs_b * scale;
+  }
+  a.radiance[pl] = rad;
+  a.bt[pl] = btv;
+  a.SC[(size_t)p * L + l] = R(scale);
+  if (a.mode == 1) {
+    a.tsk[pl] = ts_ad;
+    a.ek[pl] = scale * e_b;
+  } else {
+    a.tsk[(size_t)p * L + l] = ts_ad;
+  }
 }
 
 }  // namespace crtm

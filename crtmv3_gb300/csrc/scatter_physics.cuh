@@ -23,6 +23,7 @@
 
 #include <math.h>
 
+#include "dual.cuh"
 #include "odps_physics.cuh"
 
 namespace crtm {
@@ -53,26 +54,32 @@ struct GaussTable {
 };
 
 // ---- interpolation ----------------------------------------------------------
-struct Lagrange4 {
-  int i0;              // first of the 4 points
-  double wl[3], wr[3]; // left and right quadratic weights, already blended
+// Weights in S: the temperature axis of the liquid-cloud tables carries
+// derivatives in the cloudy K-matrix; the other axes are plain doubles.
+template <class S>
+struct Lagrange4T {
+  int i0;          // first of the 4 points
+  S wl[3], wr[3];  // left and right quadratic weights, already blended
 };
+using Lagrange4 = Lagrange4T<double>;
 
 // Clamp x into the axis, bracket it with 4 points and form the blended
 // quadratic weights (the reference's LPoly applied to a 4-point window).
-CRTM_HD Lagrange4 lagrange4(const double* ax, int n, double x) {
-  x = x < ax[0] ? ax[0] : (x > ax[n - 1] ? ax[n - 1] : x);
+template <class S>
+CRTM_HD Lagrange4T<S> lagrange4(const double* ax, int n, S x) {
+  if (x < ax[0]) x = S(ax[0]);
+  if (x > ax[n - 1]) x = S(ax[n - 1]);
   int k = 0;
   while (k < n && x > ax[k]) k++;     // first node >= x
   int i0 = k - 2;
   i0 = i0 < 0 ? 0 : (i0 > n - 4 ? n - 4 : i0);
   const double* p = ax + i0;
-  const double a0 = x - p[0], a1 = x - p[1], a2 = x - p[2], a3 = x - p[3];
+  const S a0 = x - p[0], a1 = x - p[1], a2 = x - p[2], a3 = x - p[3];
   const double d01 = p[0] - p[1], d02 = p[0] - p[2], d12 = p[1] - p[2], d13 = p[1] - p[3],
                d23 = p[2] - p[3];
-  double wr = (x < p[1]) ? 0.0 : ((x > p[2]) ? 1.0 : a1 / (-d12));
-  const double wl = 1.0 - wr;
-  Lagrange4 L;
+  S wr = (x < p[1]) ? S(0.0) : ((x > p[2]) ? S(1.0) : a1 / (-d12));
+  const S wl = 1.0 - wr;
+  Lagrange4T<S> L;
   L.i0 = i0;
   L.wl[0] = wl * (a1 * a2 / (d01 * d02));
   L.wl[1] = wl * (a0 * a2 / (-d01 * d12));
@@ -83,8 +90,9 @@ CRTM_HD Lagrange4 lagrange4(const double* ax, int n, double x) {
   return L;
 }
 
-CRTM_HD double lerp4(const double* z, size_t stride, const Lagrange4& L) {
-  const double z0 = z[0], z1 = z[stride], z2 = z[2 * stride], z3 = z[3 * stride];
+template <class S, class Z>
+CRTM_HD S lerp4(const Z* z, size_t stride, const Lagrange4T<S>& L) {
+  const Z z0 = z[0], z1 = z[stride], z2 = z[2 * stride], z3 = z[3 * stride];
   return (L.wl[0] * z0 + L.wl[1] * z1 + L.wl[2] * z2) + (L.wr[0] * z1 + L.wr[1] * z2 + L.wr[2] * z3);
 }
 
@@ -96,8 +104,10 @@ CRTM_HD double lerp4x4(const double* z, int nu, const Lagrange4& U, const Lagran
   return lerp4(a, 1, V);
 }
 
-CRTM_HD double lerp4x4x4(const double* z, int nu, int nv, const Lagrange4& U,
-                                const Lagrange4& V, const Lagrange4& W) {
+// 3-D with the third axis (temperature) in S.
+template <class S>
+CRTM_HD S lerp4x4x4(const double* z, int nu, int nv, const Lagrange4& U, const Lagrange4& V,
+                    const Lagrange4T<S>& W) {
   double a[4];
   for (int k = 0; k < 4; k++) a[k] = lerp4x4(z + (size_t)(W.i0 + k) * nu * nv, nu, U, V);
   return lerp4(a, 1, W);
@@ -109,28 +119,29 @@ CRTM_HD int legendre_offset(int nleg) {
 }
 
 // Optical properties of one cloud layer: ke (m^2/kg), w and the phase terms
-// pc[0..nleg].  Returns false for an unknown cloud type.
-CRTM_HD bool cloud_layer_optics(const CloudLut& C, bool microwave, double freq, int type,
-                                       double reff, double temp, int nleg, int loff, double* ke,
-                                       double* w, double* pc) {
-  for (int l = 0; l <= nleg; l++) pc[l] = 0.0;
-  *w = 0.0;
+// pc[0..nleg].  Only the liquid microwave tables depend on temperature, so
+// only they carry S's derivatives.  Returns false for an unknown cloud type.
+template <class S>
+CRTM_HD bool cloud_layer_optics(const CloudLut& C, bool microwave, double freq, int type, double reff,
+                                S temp, int nleg, int loff, S* ke, S* w, S* pc) {
+  for (int l = 0; l <= nleg; l++) pc[l] = S(0.0);
+  *w = S(0.0);
   if (!microwave) {
     // density slot of Get_Cloud_Opt_IR: liquid 1, snow 2, graupel 3, ice/hail 4
     const int kd = (type == 1 || type == 3) ? 0 : (type == 4 ? 1 : (type == 5 ? 2 : (type == 2 || type == 6 ? 3 : -1)));
     if (kd < 0) return false;
     const Lagrange4 F = lagrange4(C.f_ir, C.nfi, freq), R = lagrange4(C.r_ir, C.nri, reff);
     const size_t plane = (size_t)C.nfi * C.nri, vol = plane * (C.nd + 1);
-    *ke = lerp4x4(C.ke_ir + kd * plane, C.nfi, F, R);
-    *w = lerp4x4(C.w_ir + kd * plane, C.nfi, F, R);
-    pc[0] = 0.5;
-    for (int l = 1; l <= nleg; l++) pc[l] = lerp4x4(C.pc_ir + (l + loff - 1) * vol + kd * plane, C.nfi, F, R);
+    *ke = S(lerp4x4(C.ke_ir + kd * plane, C.nfi, F, R));
+    *w = S(lerp4x4(C.w_ir + kd * plane, C.nfi, F, R));
+    pc[0] = S(0.5);
+    for (int l = 1; l <= nleg; l++) pc[l] = S(lerp4x4(C.pc_ir + (l + loff - 1) * vol + kd * plane, C.nfi, F, R));
     return true;
   }
   const Lagrange4 F = lagrange4(C.f_mw, C.nfm, freq);
   const size_t plane = (size_t)C.nfm * C.nrm;
   if (type == 1 || type == 3) {   // liquid: temperature axis
-    const Lagrange4 T = lagrange4(C.t, C.nt, temp);
+    const Lagrange4T<S> T = lagrange4(C.t, C.nt, temp);
     if (type == 1) {              // cloud water: (frequency, temperature) at the first radius
       double a[4];
       for (int k = 0; k < 4; k++) a[k] = lerp4(C.ke_l + (size_t)(T.i0 + k) * plane + F.i0, 1, F);
@@ -141,22 +152,22 @@ CRTM_HD bool cloud_layer_optics(const CloudLut& C, bool microwave, double freq, 
     const size_t vol = plane * C.nt;
     *ke = lerp4x4x4(C.ke_l, C.nfm, C.nrm, F, R, T);
     *w = lerp4x4x4(C.w_l, C.nfm, C.nrm, F, R, T);
-    pc[0] = 0.5;
+    pc[0] = S(0.5);
     for (int l = 1; l <= nleg; l++) pc[l] = lerp4x4x4(C.pc_l + (l + loff) * vol, C.nfm, C.nrm, F, R, T);
     return true;
   }
   const int kd = type == 4 ? 0 : (type == 5 ? 1 : (type == 2 || type == 6 ? 2 : -1));
   if (kd < 0) return false;
   if (type == 2) {                // cloud ice: frequency only, first radius
-    *ke = lerp4(C.ke_s + kd * plane + F.i0, 1, F);
+    *ke = S(lerp4(C.ke_s + kd * plane + F.i0, 1, F));
     return true;
   }
   const Lagrange4 R = lagrange4(C.r_mw, C.nrm, reff);
   const size_t vol = plane * C.nd;
-  *ke = lerp4x4(C.ke_s + kd * plane, C.nfm, F, R);
-  *w = lerp4x4(C.w_s + kd * plane, C.nfm, F, R);
-  pc[0] = 0.5;
-  for (int l = 1; l <= nleg; l++) pc[l] = lerp4x4(C.pc_s + (l + loff) * vol + kd * plane, C.nfm, F, R);
+  *ke = S(lerp4x4(C.ke_s + kd * plane, C.nfm, F, R));
+  *w = S(lerp4x4(C.w_s + kd * plane, C.nfm, F, R));
+  pc[0] = S(0.5);
+  for (int l = 1; l <= nleg; l++) pc[l] = S(lerp4x4(C.pc_s + (l + loff) * vol + kd * plane, C.nfm, F, R));
   return true;
 }
 
@@ -227,7 +238,7 @@ CRTM_HD bool mat_invert(int n, Mat<NZ, T>& A) {
     for (int i = 0; i < n; i++) {
       if (i == k) continue;
       const T f = A.a[i][k];
-      if (f == T(0.0)) continue;
+      if (is_zero(f)) continue;
       for (int j = 0; j < n; j++) A.a[i][j] -= f * A.a[k][j];
       A.a[i][k] = -f * d;
     }
@@ -278,6 +289,46 @@ CRTM_HD void jacobi(int n, Mat<NZ, T>& S, T* lam, Mat<NZ, T>& V) {
       }
   }
   for (int i = 0; i < n; i++) lam[i] = S.a[i][i];
+}
+
+// Symmetric eigenproblem on derivative numbers: eigenpairs of the value
+// part by Jacobi, then their derivatives by first-order perturbation:
+// d(lambda_i) = v_i' dS v_i and dv_i = sum_{j != i} v_j (v_j' dS v_i) / (lambda_i - lambda_j).
+template <int NZ, int N>
+CRTM_HD void jacobi(int n, Mat<NZ, Dual<N>>& S, Dual<N>* lam, Mat<NZ, Dual<N>>& V) {
+  Mat<NZ, double> S0, V0;
+  double l0[NZ];
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) S0.a[i][j] = S.a[i][j].v;
+  jacobi<NZ, double>(n, S0, l0, V0);
+  for (int i = 0; i < n; i++) {
+    lam[i] = Dual<N>(l0[i]);
+    for (int j = 0; j < n; j++) V.a[i][j] = Dual<N>(V0.a[i][j]);
+  }
+  for (int q = 0; q < N; q++) {
+    // M = V0' dS V0
+    double M[NZ][NZ], T1[NZ][NZ];
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++) {
+        double v = 0.0;
+        for (int k = 0; k < n; k++) v += S.a[i][k].d[q] * V0.a[k][j];
+        T1[i][j] = v;
+      }
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++) {
+        double v = 0.0;
+        for (int k = 0; k < n; k++) v += V0.a[k][i] * T1[k][j];
+        M[i][j] = v;
+      }
+    for (int i = 0; i < n; i++) lam[i].d[q] = M[i][i];
+    for (int r = 0; r < n; r++)     // row r of dV = V0 C, C_ji = M_ji / (l_i - l_j)
+      for (int i = 0; i < n; i++) {
+        double v = 0.0;
+        for (int j = 0; j < n; j++)
+          if (j != i) v += V0.a[r][j] * M[j][i] / (l0[i] - l0[j]);
+        V.a[r][i].d[q] = v;
+      }
+  }
 }
 
 // Layer optics of a scattering layer for the adding method (CRTM_AMOM_layer +
@@ -591,88 +642,102 @@ CRTM_HD int stream_set(int nleg, double mu_sensor, int lut_nleg, const GaussTabl
   return 0;
 }
 
-// Optics of layer k for the adding method: cloud optics summed over the
-// clouds, combine and delta truncation, and for a scattering layer the
-// phase blocks and the layer's transmission, reflection and source
-// (ada_layer).  Returns 1 for a scattering layer, 0 for a clear one (od is
-// then the layer optical depth), negative on failure.
-template <int NZ, class T>
-CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const StreamSet<NZ, double>& S, int k,
-                         double gas_od, T* od_out, Mat<NZ, T>& Tm, Mat<NZ, T>& Rm, T* src) {
-  const int nleg = S.nleg;
-  double od = gas_od, bs_sum = 0.0;
-  double pc[SC_NLEG_MAX + 1], pcs[SC_NLEG_MAX + 1];
-  for (int l = 0; l <= nleg; l++) pcs[l] = 0.0;
-  const double tk = in.temperature[k];
+// Optics of layer k for the adding method: cloud and aerosol optics summed
+// over the species, combine and delta truncation, and for a scattering layer
+// the phase blocks and the layer's transmission, reflection and source
+// (ada_layer, or SOI doubling).  Computed in S (FP64 in every form, or
+// derivative numbers for the K-matrix), stored in T.  Returns 1 for a
+// scattering layer, 0 for a clear one (od is then the layer optical depth),
+// negative on failure.
+template <int NZ, class T, class S = double>
+CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const StreamSet<NZ, double>& St, int k,
+                         S gas_od, S tk, T* od_out, Mat<NZ, T>& Tm, Mat<NZ, T>& Rm, T* src) {
+  const int nleg = St.nleg;
+  S od = gas_od, bs_sum = S(0.0);
+  S pc[SC_NLEG_MAX + 1], pcs[SC_NLEG_MAX + 1];
+  for (int l = 0; l <= nleg; l++) pcs[l] = S(0.0);
   for (int c = 0; c < in.n_clouds; c++) {
     const double wc = in.wc[c * in.cstride + k];
     if (!(wc > WATER_CONTENT_THRESHOLD)) continue;
-    double ke, w;
-    if (!cloud_layer_optics(lut, in.microwave, in.freq, in.cloud_type[c], in.reff[c * in.cstride + k], tk,
-                            nleg, S.loff, &ke, &w, pc))
+    S ke, w;
+    if (!cloud_layer_optics<S>(lut, in.microwave, in.freq, in.cloud_type[c], in.reff[c * in.cstride + k], tk,
+                               nleg, St.loff, &ke, &w, pc))
       return -4;
-    if (ke <= 0.0) { ke = 0.0; w = 0.0; }
-    if (w <= 0.0) { w = 0.0; for (int l = 0; l <= nleg; l++) pc[l] = 0.0; }
-    if (w >= 1.0) w = 1.0;
+    if (ke <= 0.0) { ke = S(0.0); w = S(0.0); }
+    if (w <= 0.0) { w = S(0.0); for (int l = 0; l <= nleg; l++) pc[l] = S(0.0); }
+    if (w >= 1.0) w = S(1.0);
     od += ke * wc;
-    const double bs = wc * ke * w;
+    const S bs = ke * w * wc;
     bs_sum += bs;
     for (int l = 1; l <= nleg; l++) pcs[l] += pc[l] * bs;
   }
   if (in.n_aerosols > 0 && !in.microwave) {   // CRTM_Compute_AerosolScatter (:170-317)
-    if (nleg == 2 || !in.alut || in.alut->nleg < nleg + S.loff) return -8;
+    if (nleg == 2 || !in.alut || in.alut->nleg < nleg + St.loff) return -8;
+    double pa[SC_NLEG_MAX + 1];
     for (int c = 0; c < in.n_aerosols; c++) {
       const double conc = in.conc[c * in.cstride + k];
       if (!(conc > 1.0e-9)) continue;   // AEROSOL_CONTENT_THRESHOLD
       double ke, w;
       if (!aerosol_layer_optics(*in.alut, in.wavenumber, in.aerosol_type[c], in.aer_reff[c * in.cstride + k],
-                                nleg, S.loff, &ke, &w, pc))
+                                nleg, St.loff, &ke, &w, pa))
         return -9;
       if (ke <= 0.0) { ke = 0.0; w = 0.0; }
-      if (w <= 0.0) { w = 0.0; for (int l = 0; l <= nleg; l++) pc[l] = 0.0; }
+      if (w <= 0.0) { w = 0.0; for (int l = 0; l <= nleg; l++) pa[l] = 0.0; }
       if (w >= 1.0) w = 1.0;
       od += ke * conc;
       const double bs = conc * ke * w;
       bs_sum += bs;
-      for (int l = 0; l <= nleg; l++) pcs[l] += pc[l] * bs;
+      for (int l = 0; l <= nleg; l++) pcs[l] += pa[l] * bs;
     }
   }
-  double ssa = bs_sum;
+  S ssa = bs_sum;
   if (bs_sum > BS_THRESHOLD) {   // CRTM_AtmOptics_Combine
-    const double w = bs_sum / od;
+    const S w = bs_sum / od;
     for (int l = 1; l <= nleg; l++) pcs[l] /= bs_sum;
-    pcs[0] = 0.5;
-    const double f = pcs[nleg];
+    pcs[0] = S(0.5);
+    const S f = pcs[nleg];
     od = (1.0 - f * w) * od;
     ssa = (1.0 - f) * w / (1.0 - f * w);
   }
   *od_out = T(od);
   if (!(ssa > BS_THRESHOLD)) return 0;
-  // Phase blocks and MOM in FP64 in every form: MOM's three inversions and
-  // its eigenvectors lose accuracy in FP32 for thick, highly scattering
-  // layers.  Only the stored layer record is in T.
-  Mat<NZ, double> ff, bb, Td, Rd;
-  double mu[NZ], wt[NZ], P[NZ][SC_NLEG_MAX + 1], srcd[NZ];
-  for (int i = 0; i < S.nZ; i++) {
-    mu[i] = double(S.mu[i]);
-    wt[i] = double(S.wt[i]);
-    for (int l = 0; l <= nleg; l++) P[i][l] = double(S.P[i][l]);
+  // Phase blocks and MOM in S (FP64 values in every form: MOM's inversions
+  // and eigenvectors lose accuracy in FP32 for thick, highly scattering
+  // layers).  Only the stored layer record is in T.
+  Mat<NZ, S> ff, bb, Td, Rd;
+  S mu[NZ], wt[NZ], P[NZ][SC_NLEG_MAX + 1], srcd[NZ];
+  for (int i = 0; i < St.nZ; i++) {
+    mu[i] = S(St.mu[i]);
+    wt[i] = S(St.wt[i]);
+    for (int l = 0; l <= nleg; l++) P[i][l] = S(St.P[i][l]);
   }
-  phase_blocks<NZ, double>(S.nS, S.nZ, nleg, pcs, P, wt, ff, bb);
-  const double B = in.c1 / (exp(in.c2 / (in.b1 + in.b2 * tk)) - 1.0);
+  phase_blocks<NZ, S>(St.nS, St.nZ, nleg, pcs, P, wt, ff, bb);
+  const S B = in.c1 / (exp(in.c2 / (in.b1 + in.b2 * tk)) - 1.0);
   if (in.soi) {   // SOI: doubling, then the direct beam taken out of the diagonal
-    soi_doubling<NZ>(ssa < 0.8 && od < 4.0, S.nS, S.nZ, ssa, od, mu, wt, ff, bb, B, Td, Rd, srcd);
-    for (int i = 0; i < S.nZ; i++) Td.a[i][i] -= exp(-od / mu[i]);
+    Mat<NZ, double> ffd, bbd, Tdd, Rdd;
+    double mud[NZ], wtd[NZ], srd[NZ];
+    for (int i = 0; i < St.nZ; i++) {
+      mud[i] = St.mu[i];
+      wtd[i] = St.wt[i];
+      for (int j = 0; j < St.nZ; j++) { ffd.a[i][j] = value_of(ff.a[i][j]); bbd.a[i][j] = value_of(bb.a[i][j]); }
+    }
+    const double odv = value_of(od), ssav = value_of(ssa);
+    soi_doubling<NZ>(ssav < 0.8 && odv < 4.0, St.nS, St.nZ, ssav, odv, mud, wtd, ffd, bbd, value_of(B), Tdd, Rdd, srd);
+    for (int i = 0; i < St.nZ; i++) {
+      Tdd.a[i][i] -= ::exp(-odv / mud[i]);
+      srcd[i] = S(srd[i]);
+      for (int j = 0; j < St.nZ; j++) { Td.a[i][j] = S(Tdd.a[i][j]); Rd.a[i][j] = S(Rdd.a[i][j]); }
+    }
   } else {
-    double mx = 0.0;
-    for (int i = 0; i < S.nZ; i++)
-      for (int j = 0; j < S.nZ; j++) mx = fabs(ff.a[i][j]) > mx ? fabs(ff.a[i][j]) : mx;
+    S mx = S(0.0);
+    for (int i = 0; i < St.nZ; i++)
+      for (int j = 0; j < St.nZ; j++) mx = fabs(ff.a[i][j]) > mx ? fabs(ff.a[i][j]) : mx;
     if (!(mx > 0.0)) return 0;
-    if (!ada_layer<NZ, double>(S.nS, S.nZ, ssa, od, mu, wt, ff, bb, B, Td, Rd, srcd)) return -5;
+    if (!ada_layer<NZ, S>(St.nS, St.nZ, ssa, od, mu, wt, ff, bb, B, Td, Rd, srcd)) return -5;
   }
-  for (int i = 0; i < S.nZ; i++) {
+  for (int i = 0; i < St.nZ; i++) {
     src[i] = T(srcd[i]);
-    for (int j = 0; j < S.nZ; j++) { Tm.a[i][j] = T(Td.a[i][j]); Rm.a[i][j] = T(Rd.a[i][j]); }
+    for (int j = 0; j < St.nZ; j++) { Tm.a[i][j] = T(Td.a[i][j]); Rm.a[i][j] = T(Rd.a[i][j]); }
   }
   return 1;
 }
@@ -752,6 +817,161 @@ CRTM_HD double adding_toa(const AddingState<NZ>& A, int nZ, int isat, double cos
   return A.rad[isat] + s * cosmic;
 }
 
+// ---- adjoint of the adding (reverse mode), unit TOA radiance seed ----------
+// The forward adding maps (Rup, rad) below a layer to (Rup', rad') above it.
+// Given the adjoints of (Rup', rad'), these give the adjoints of (Rup, rad)
+// and of the layer's inputs.  The forward state below the layer is passed in.
+
+// Clear layer (diagonal transmission t_i = exp(-od/mu_i), source B (1 - t_i)):
+// returns d/d(od) and d/dB.
+template <int NZ>
+CRTM_HD void adding_clear_adjoint(int nZ, const double* mu, double od, double B, const Mat<NZ, double>& Rup,
+                                  const double* rad, Mat<NZ, double>& Rup_b, double* rad_b, double* od_b,
+                                  double* B_b) {
+  double tr[NZ], src[NZ], t[NZ], tr_b[NZ], src_b[NZ], t_b[NZ];
+  for (int i = 0; i < nZ; i++) {
+    tr[i] = exp(-od / mu[i]);
+    src[i] = B * (1.0 - tr[i]);
+  }
+  for (int i = 0; i < nZ; i++) {
+    double v = rad[i];
+    for (int j = 0; j < nZ; j++) v += Rup.a[i][j] * src[j];
+    t[i] = v;
+  }
+  // rad'_i = src_i + tr_i t_i ;  Rup'_ij = tr_i Rup_ij tr_j
+  for (int i = 0; i < nZ; i++) {
+    src_b[i] = rad_b[i];
+    tr_b[i] = rad_b[i] * t[i];
+    t_b[i] = rad_b[i] * tr[i];
+  }
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) {
+      const double g = Rup_b.a[i][j];
+      tr_b[i] += g * Rup.a[i][j] * tr[j];
+      tr_b[j] += g * tr[i] * Rup.a[i][j];
+      Rup_b.a[i][j] = g * tr[i] * tr[j];
+    }
+  // t_i = rad_i + sum_j Rup_ij src_j
+  for (int i = 0; i < nZ; i++) {
+    rad_b[i] = t_b[i];
+    for (int j = 0; j < nZ; j++) {
+      Rup_b.a[i][j] += t_b[i] * src[j];
+      src_b[j] += t_b[i] * Rup.a[i][j];
+    }
+  }
+  double ob = 0.0, bb = 0.0;
+  for (int i = 0; i < nZ; i++) {
+    bb += src_b[i] * (1.0 - tr[i]);
+    tr_b[i] -= src_b[i] * B;
+    ob -= tr_b[i] * tr[i] / mu[i];
+  }
+  *od_b = ob;
+  *B_b = bb;
+}
+
+// Scattering layer (transmission T, reflection R, source src): adjoints of the
+// layer's T, R and src.  Returns false on a singular (I - Rup R).
+template <int NZ>
+CRTM_HD bool adding_scatter_adjoint(int nZ, const Mat<NZ, double>& Tm, const Mat<NZ, double>& Rm,
+                                    const double* src, const Mat<NZ, double>& Rup, const double* rad,
+                                    Mat<NZ, double>& Rup_b, double* rad_b, Mat<NZ, double>& T_b,
+                                    Mat<NZ, double>& R_b, double* src_b) {
+  Mat<NZ, double> G, IGT, RT, M1, M2;
+  double t[NZ], t_b[NZ];
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) {
+      double v = 0.0;
+      for (int m = 0; m < nZ; m++) v += Rup.a[i][m] * Rm.a[m][j];
+      G.a[i][j] = (i == j ? 1.0 : 0.0) - v;
+    }
+  if (!mat_invert<NZ, double>(nZ, G)) return false;     // G now holds Gamma
+  mat_mul<NZ, double>(nZ, Tm, G, IGT);
+  mat_mul<NZ, double>(nZ, Rup, Tm, RT);
+  for (int i = 0; i < nZ; i++) {
+    double v = rad[i];
+    for (int j = 0; j < nZ; j++) v += Rup.a[i][j] * src[j];
+    t[i] = v;
+  }
+  // IGT_b = rad'_b t^T + Rup'_b RT^T  (in M1);  t_b = IGT^T rad'_b;  RT_b = IGT^T Rup'_b (in M2)
+  for (int i = 0; i < nZ; i++) {
+    src_b[i] = rad_b[i];
+    for (int j = 0; j < nZ; j++) {
+      double v = rad_b[i] * t[j];
+      for (int m = 0; m < nZ; m++) v += Rup_b.a[i][m] * RT.a[j][m];
+      M1.a[i][j] = v;
+    }
+  }
+  for (int j = 0; j < nZ; j++) {
+    double v = 0.0;
+    for (int i = 0; i < nZ; i++) v += IGT.a[i][j] * rad_b[i];
+    t_b[j] = v;
+  }
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) {
+      double v = 0.0;
+      for (int m = 0; m < nZ; m++) v += IGT.a[m][i] * Rup_b.a[m][j];
+      M2.a[i][j] = v;
+      R_b.a[i][j] = Rup_b.a[i][j];
+    }
+  // RT = Rup T:  Rup_b = RT_b T^T ;  T_b = Rup^T RT_b
+  Mat<NZ, double> Rb_new;
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) {
+      double a = 0.0, b = 0.0;
+      for (int m = 0; m < nZ; m++) {
+        a += M2.a[i][m] * Tm.a[j][m];
+        b += Rup.a[m][i] * M2.a[m][j];
+      }
+      Rb_new.a[i][j] = a;
+      T_b.a[i][j] = b;
+    }
+  // t = rad + Rup src
+  for (int i = 0; i < nZ; i++) {
+    rad_b[i] = t_b[i];
+    for (int j = 0; j < nZ; j++) {
+      Rb_new.a[i][j] += t_b[i] * src[j];
+      src_b[j] += t_b[i] * Rup.a[i][j];
+    }
+  }
+  // IGT = T Gamma:  T_b += IGT_b Gamma^T ;  Gamma_b = T^T IGT_b (in M2)
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) {
+      double a = 0.0, b = 0.0;
+      for (int m = 0; m < nZ; m++) {
+        a += M1.a[i][m] * G.a[j][m];
+        b += Tm.a[m][i] * M1.a[m][j];
+      }
+      T_b.a[i][j] += a;
+      M2.a[i][j] = b;
+    }
+  // Gamma = G^-1:  G_b = -Gamma^T Gamma_b Gamma^T (in M1)
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) {
+      double v = 0.0;
+      for (int m = 0; m < nZ; m++) v += M2.a[i][m] * G.a[j][m];
+      IGT.a[i][j] = v;   // Gamma_b Gamma^T
+    }
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) {
+      double v = 0.0;
+      for (int m = 0; m < nZ; m++) v += G.a[m][i] * IGT.a[m][j];
+      M1.a[i][j] = -v;
+    }
+  // G = I - Rup R:  Rup_b -= G_b R^T ;  R_b -= Rup^T G_b
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) {
+      double a = 0.0, b = 0.0;
+      for (int m = 0; m < nZ; m++) {
+        a += M1.a[i][m] * Rm.a[j][m];
+        b += Rup.a[m][i] * M1.a[m][j];
+      }
+      Rb_new.a[i][j] -= a;
+      R_b.a[i][j] -= b;
+    }
+  Rup_b = Rb_new;
+  return true;
+}
+
 // CRTM_SOI (SOI_Module.f90:63-283): successive orders of interaction.  Order
 // 1 carries the thermal sources, the surface emission and the cosmic
 // background; each later order scatters the previous order's diffuse fields
@@ -822,7 +1042,7 @@ CRTM_HD int cloudy_radiance(const CloudyColumn& in, const CloudLut& lut, const G
   double src[NZ];
   for (int k = in.Ku - 1; k >= 0; k--) {
     double od;
-    const int kind = layer_optics<NZ, double>(in, lut, S, k, od_of(k), &od, Tm, Rm, src);
+    const int kind = layer_optics<NZ, double>(in, lut, S, k, od_of(k), in.temperature[k], &od, Tm, Rm, src);
     if (kind < 0) return -kind;
     if (kind == 1) {
       if (!adding_scatter<NZ>(A, S.nZ, Tm, Rm, src)) return 6;
@@ -832,6 +1052,120 @@ CRTM_HD int cloudy_radiance(const CloudyColumn& in, const CloudLut& lut, const G
     }
   }
   *radiance = adding_toa<NZ>(A, S.nZ, S.isat, in.cosmic);
+  return 0;
+}
+
+// Derivatives of one layer's optics with respect to its gas optical depth
+// (direction 0) and temperature (direction 1), contracted with the adjoints of
+// the layer's T, R and source (scattering layer) or of its optical depth
+// (clear layer): g[d] = sum(T_b dT/dd) + sum(R_b dR/dd) + sum(src_b dsrc/dd),
+// or od_b dod/dd.  The layer's optics are evaluated on derivative numbers;
+// returns the layer kind, which must match the forward pass.
+template <int NZ>
+CRTM_HD int layer_contract(const CloudyColumn& in, const CloudLut& lut, const StreamSet<NZ, double>& S, int k,
+                           double gas_od, const Mat<NZ, double>& T_b, const Mat<NZ, double>& R_b,
+                           const double* src_b, double od_b, double* g) {
+  using D = Dual<2>;
+  D gd(gas_od), tt(in.temperature[k]);
+  gd.d[0] = 1.0;
+  tt.d[1] = 1.0;
+  Mat<NZ, D> Td, Rd;
+  D srcd[NZ], odd;
+  const int kind = layer_optics<NZ, D, D>(in, lut, S, k, gd, tt, &odd, Td, Rd, srcd);
+  g[0] = g[1] = 0.0;
+  if (kind == 1) {
+    for (int i = 0; i < S.nZ; i++) {
+      g[0] += src_b[i] * srcd[i].d[0];
+      g[1] += src_b[i] * srcd[i].d[1];
+      for (int j = 0; j < S.nZ; j++) {
+        g[0] += T_b.a[i][j] * Td.a[i][j].d[0] + R_b.a[i][j] * Rd.a[i][j].d[0];
+        g[1] += T_b.a[i][j] * Td.a[i][j].d[1] + R_b.a[i][j] * Rd.a[i][j].d[1];
+      }
+    }
+  } else if (kind == 0) {
+    g[0] = od_b * odd.d[0];
+    g[1] = od_b * odd.d[1];
+  }
+  return kind;
+}
+
+// K-matrix of one (profile, channel) through ADA, for a unit TOA radiance
+// seed: the radiance, and for every layer k the derivatives with respect to
+// the layer's gas optical depth (dgas) and its temperature (dT: Planck source
+// and the temperature axis of the liquid-cloud tables), plus those with
+// respect to the surface emissivity and the surface Planck radiance.
+// Forward adding with every level's (Rup, rad) kept in state(level, i) (nZ*nZ
+// + nZ values per level, level Ku = surface), then the adding adjoint from the
+// top down.  layer(k, kind, od, T, R, src) gives the layer records of the
+// forward pass; contract(k, kind, T_b, R_b, src_b, od_b, g) the contraction
+// of the layer's optics derivatives with the adjoints of its record (see
+// layer_contract), returning false when the layer's kind does not match.
+template <int NZ, class LayerFn, class StateFn, class ContractFn, class OutFn>
+CRTM_HD int cloudy_kmatrix(const CloudyColumn& in, const StreamSet<NZ, double>& S, LayerFn layer,
+                           StateFn state, ContractFn contract, OutFn out, double* radiance, double* e_b,
+                           double* Bs_b) {
+  const int nZ = S.nZ, Ku = in.Ku;
+  AddingState<NZ> A;
+  adding_init<NZ>(A, nZ, in.emissivity, in.planck_surface);
+  auto save = [&](int lev) {
+    for (int i = 0; i < nZ; i++) {
+      for (int j = 0; j < nZ; j++) state(lev, i * NZ + j) = A.Rup.a[i][j];
+      state(lev, NZ * NZ + i) = A.rad[i];
+    }
+  };
+  auto load = [&](int lev, Mat<NZ, double>& Rup, double* rad) {
+    for (int i = 0; i < nZ; i++) {
+      for (int j = 0; j < nZ; j++) Rup.a[i][j] = state(lev, i * NZ + j);
+      rad[i] = state(lev, NZ * NZ + i);
+    }
+  };
+  save(Ku);
+  Mat<NZ, double> Tm, Rm;
+  double src[NZ];
+  for (int k = Ku - 1; k >= 0; k--) {
+    int kind;
+    double od;
+    layer(k, &kind, &od, Tm, Rm, src);
+    if (kind < 0) return -kind;
+    if (kind == 1) {
+      if (!adding_scatter<NZ>(A, nZ, Tm, Rm, src)) return 6;
+    } else {
+      adding_clear<NZ>(A, nZ, S.mu, od, in.c1 / (exp(in.c2 / (in.b1 + in.b2 * in.temperature[k])) - 1.0));
+    }
+    save(k);
+  }
+  *radiance = adding_toa<NZ>(A, nZ, S.isat, in.cosmic);
+  // adjoint of the TOA radiance
+  Mat<NZ, double> Rup_b, Rup, T_b, R_b;
+  double rad_b[NZ], rad[NZ], src_b[NZ];
+  for (int i = 0; i < nZ; i++) {
+    rad_b[i] = (i == S.isat) ? 1.0 : 0.0;
+    for (int j = 0; j < nZ; j++) Rup_b.a[i][j] = (i == S.isat) ? in.cosmic : 0.0;
+  }
+  for (int k = 0; k < Ku; k++) {
+    load(k + 1, Rup, rad);
+    int kind;
+    double od, g[2];
+    layer(k, &kind, &od, Tm, Rm, src);
+    if (kind == 1) {
+      if (!adding_scatter_adjoint<NZ>(nZ, Tm, Rm, src, Rup, rad, Rup_b, rad_b, T_b, R_b, src_b)) return 6;
+      if (!contract(k, kind, T_b, R_b, src_b, 0.0, g)) return 7;
+    } else {
+      // Planck source of a clear layer and its temperature derivative
+      const double te = in.b1 + in.b2 * in.temperature[k];
+      const double ee = exp(in.c2 / te), B = in.c1 / (ee - 1.0);
+      const double dB = in.c1 * in.c2 * ee * in.b2 / (te * te * (ee - 1.0) * (ee - 1.0));
+      double od_b, B_b;
+      adding_clear_adjoint<NZ>(nZ, S.mu, od, B, Rup, rad, Rup_b, rad_b, &od_b, &B_b);
+      if (!contract(k, kind, T_b, R_b, src_b, od_b, g)) return 7;
+      g[1] += B_b * dB;
+    }
+    out(k, g[0], g[1]);
+  }
+  double tr = 0.0, sr = 0.0;
+  for (int i = 0; i < nZ; i++) { tr += Rup_b.a[i][i]; sr += rad_b[i]; }
+  *e_b = -tr + in.planck_surface * sr;
+  *Bs_b = in.emissivity * sr;
   return 0;
 }
 

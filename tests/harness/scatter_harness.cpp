@@ -64,7 +64,7 @@ int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, 
     for (int k = 0; k < Ku; k++) {
       Mat<NZ, double> Tm, Rm;
       double srcv[NZ], o;
-      const int kind = layer_optics<NZ, double>(c, L, S, k, od[k], &o, Tm, Rm, srcv);
+      const int kind = layer_optics<NZ, double>(c, L, S, k, od[k], temp[k], &o, Tm, Rm, srcv);
       double* r = &rec[(size_t)k * NE];
       r[0] = kind;
       r[1] = o;
@@ -105,7 +105,7 @@ int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, 
   std::vector<Mat<NZ, double>> T(Ku), R(Ku);
   std::vector<double> src((size_t)Ku * NZ);
   for (int k = 0; k < Ku; k++) {
-    kind[k] = layer_optics<NZ, double>(c, L, S, k, od[k], &ods[k], T[k], R[k], &src[(size_t)k * NZ]);
+    kind[k] = layer_optics<NZ, double>(c, L, S, k, od[k], temp[k], &ods[k], T[k], R[k], &src[(size_t)k * NZ]);
     if (kind[k] < 0) return -kind[k];
   }
   auto layer = [&](int k, int* kd, double* o, double* B, Mat<NZ, double>& Tm, Mat<NZ, double>& Rm, double* sv) {
@@ -123,4 +123,79 @@ int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, 
 }
 
 int sx_stream_rule(double max_reff, double wavenumber) { return stream_rule_nleg(max_reff, wavenumber); }
+}
+
+
+// One layer's record (od, T, R, src: 1 + 2 nZ^2 + nZ values) for gas optical
+// depth gas and temperature tk, with its derivatives d/dgas and d/dtk from the
+// derivative-number evaluation.  Same LUT and column arguments as above.
+extern "C" int sx_layer_record(const int* dims, const double* f_mw, const double* r_mw, const double* t,
+                               const double* f_ir, const double* r_ir, const double* ke_l, const double* w_l,
+                               const double* pc_l, const double* ke_s, const double* w_s, const double* pc_s,
+                               const double* ke_ir, const double* w_ir, const double* pc_ir, int n_clouds,
+                               int nleg, int microwave, double freq, double mu_sensor, const double* planck,
+                               const int* cloud_type, const double* wc, const double* reff, int cstride, int k,
+                               double gas, double tk, double* val, double* dgas, double* dtk, int* nz_out) {
+  CloudLut L{dims[0], dims[1], dims[2], dims[3], dims[4], dims[5], dims[6], f_mw, r_mw, t, f_ir, r_ir,
+             ke_l, w_l, pc_l, ke_s, w_s, pc_s, ke_ir, w_ir, pc_ir};
+  static const GaussTable gt = make_gauss();
+  CloudyColumn c{};
+  c.Ku = k + 1; c.n_clouds = n_clouds; c.nleg = nleg; c.microwave = microwave != 0; c.freq = freq;
+  c.mu_sensor = mu_sensor;
+  c.c1 = planck[0]; c.c2 = planck[1]; c.b1 = planck[2]; c.b2 = planck[3];
+  c.cloud_type = cloud_type; c.wc = wc; c.reff = reff; c.cstride = (size_t)cstride;
+  constexpr int NZ = SC_NZ_MAX;
+  StreamSet<NZ, double> S;
+  if (int rc = stream_set<NZ, double>(nleg, mu_sensor, L.nleg, gt, S)) return -100 - rc;
+  using D = Dual<2>;
+  D g(gas), tt(tk);
+  g.d[0] = 1.0;
+  tt.d[1] = 1.0;
+  Mat<NZ, D> Tm, Rm;
+  D src[NZ], od;
+  const int kind = layer_optics<NZ, D, D>(c, L, S, k, g, tt, &od, Tm, Rm, src);
+  const int nZ = S.nZ;
+  *nz_out = nZ;
+  auto put = [&](const D& x, int i) { val[i] = x.v; dgas[i] = x.d[0]; dtk[i] = x.d[1]; };
+  put(od, 0);
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) { put(Tm.a[i][j], 1 + i * nZ + j); put(Rm.a[i][j], 1 + nZ * nZ + i * nZ + j); }
+  for (int i = 0; i < nZ; i++) put(src[i], 1 + 2 * nZ * nZ + i);
+  return kind;
+}
+
+
+// K-matrix of one cloudy (profile, channel) through ADA for a unit radiance
+// seed: radiance, dR/d(gas OD_k), dR/dT_k, dR/de and dR/dB_surface.
+extern "C" int sx_cloudy_kmatrix(const int* dims, const double* f_mw, const double* r_mw, const double* t,
+                                 const double* f_ir, const double* r_ir, const double* ke_l, const double* w_l,
+                                 const double* pc_l, const double* ke_s, const double* w_s, const double* pc_s,
+                                 const double* ke_ir, const double* w_ir, const double* pc_ir, int Ku,
+                                 int n_clouds, int nleg, int microwave, double freq, double mu_sensor,
+                                 double emissivity, double planck_surface, double cosmic, const double* planck,
+                                 const double* temp, const int* cloud_type, const double* wc, const double* reff,
+                                 int cstride, const double* od, double* radiance, double* dgas, double* dT,
+                                 double* e_b, double* Bs_b) {
+  CloudLut L{dims[0], dims[1], dims[2], dims[3], dims[4], dims[5], dims[6], f_mw, r_mw, t, f_ir, r_ir,
+             ke_l, w_l, pc_l, ke_s, w_s, pc_s, ke_ir, w_ir, pc_ir};
+  static const GaussTable gt = make_gauss();
+  CloudyColumn c{};
+  c.Ku = Ku; c.n_clouds = n_clouds; c.nleg = nleg; c.microwave = microwave != 0; c.freq = freq;
+  c.mu_sensor = mu_sensor; c.emissivity = emissivity; c.planck_surface = planck_surface; c.cosmic = cosmic;
+  c.c1 = planck[0]; c.c2 = planck[1]; c.b1 = planck[2]; c.b2 = planck[3];
+  c.temperature = temp; c.cloud_type = cloud_type; c.wc = wc; c.reff = reff; c.cstride = (size_t)cstride;
+  constexpr int NZ = SC_NZ_MAX;
+  StreamSet<NZ, double> S;
+  if (int rc = stream_set<NZ, double>(nleg, mu_sensor, L.nleg, gt, S)) return rc;
+  auto layer = [&](int k, int* kind, double* o, Mat<NZ, double>& Tm, Mat<NZ, double>& Rm, double* src) {
+    *kind = layer_optics<NZ, double>(c, L, S, k, od[k], temp[k], o, Tm, Rm, src);
+  };
+  std::vector<double> st((size_t)(Ku + 1) * (NZ * NZ + NZ));
+  auto state = [&](int lev, int i) -> double& { return st[(size_t)lev * (NZ * NZ + NZ) + i]; };
+  auto contract = [&](int k, int kind, const Mat<NZ, double>& T_b, const Mat<NZ, double>& R_b,
+                      const double* src_b, double od_b, double* g) {
+    return layer_contract<NZ>(c, L, S, k, od[k], T_b, R_b, src_b, od_b, g) == kind;
+  };
+  auto out = [&](int k, double g, double tt) { dgas[k] = g; dT[k] = tt; };
+  return cloudy_kmatrix<NZ>(c, S, layer, state, contract, out, radiance, e_b, Bs_b);
 }

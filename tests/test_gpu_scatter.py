@@ -65,13 +65,6 @@ def test_ragged_cloudy_batch(gpu_lib, cloud_dir):
     assert np.abs(rts.brightness_temperature - ref).max() <= BT_TOL[0]
 
 
-def test_cloudy_k_matrix_is_refused(gpu_lib, cloud_dir):
-    atm, sfc, geo, opt = sy.cloudy_workload("mwsynth_c16", 2, 100, 65)
-    h = gpu_lib.CRTM(["mwsynth_c16"], cloud_dir, 0)
-    with pytest.raises(RuntimeError, match="not available for batches with clouds"):
-        h.k_matrix(atm, sfc, geo, opt)
-
-
 def test_isothermal_enclosure_on_gpu(gpu_lib, cloud_dir, tmp_path):
     """Kirchhoff check of the GPU solver itself: an isothermal scene whose
     cosmic background is B(T) gives BT = T for any cloud and stream count."""

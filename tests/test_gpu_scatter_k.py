@@ -1,0 +1,226 @@
+"""K-matrix and adjoint of scattering profiles (clouds, aerosols; ADA) on the GPU.
+
+The oracle's cloudy forward is the checker: central finite differences of it
+(FP64) give the Jacobians of one layer in every profile at a time, for the
+temperature (step 1e-3 K) and each absorber (step 1e-4 of the amount), and of
+the surface temperature and emissivity.  Central differences of a smooth FP64
+forward carry about 1e-7 of the largest Jacobian, so the FP64 form must agree
+within 2e-5 relative to the largest Jacobian of the variable (layer by layer);
+the mixed form must agree with the FP64 form within 1e-3, as for clear sky.
+"""
+import copy
+
+import numpy as np
+import pytest
+
+from crtmv3_gb300 import coefficients as co, synthetic as sy
+
+pytestmark = pytest.mark.gpu
+
+FD_TOL = 2e-5
+MIX_TOL = 1e-3
+RT_SOI = 168
+
+
+@pytest.fixture(scope="module")
+def cloud_dir(coeff_dir):
+    sy.write_cloud_files(coeff_dir)
+    sy.write_aerosol_files(coeff_dir)
+    return coeff_dir
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def _paths(d, atm):
+    cp = f"{d}/CloudCoeff.bin" if atm.cloud_type is not None else None
+    ap = f"{d}/AerosolCoeff.bin" if atm.aerosol_type is not None else None
+    return cp, ap
+
+
+def _fd_bt(orc, d, atm, sfc, geo, opt, perturb, step):
+    """Central difference of the oracle's cloudy brightness temperatures:
+    perturb(atm, sfc, opt, s) applies a signed step s (scalar or per profile)."""
+    cp, ap = _paths(d, atm)
+    out = []
+    for sgn in (1.0, -1.0):
+        a, s, o = copy.deepcopy(atm), copy.deepcopy(sfc), copy.deepcopy(opt)
+        perturb(a, s, o, sgn * step)
+        out.append(orc.forward_scatter(a, s, geo, o, cp, ap, n_threads=8)[1])
+    st = np.asarray(step, np.float64)
+    return (out[0] - out[1]) / (2.0 * (st[:, None] if st.ndim else st))
+
+
+def _check_layers(km, orc, d, atm, sfc, geo, opt, layers):
+    for k in layers:
+        def pt(a, s, o, h, k=k):
+            a.temperature[:, k] += h
+        fd = _fd_bt(orc, d, atm, sfc, geo, opt, pt, 1e-3)
+        got = km.temperature[:, :, k]
+        assert np.abs(got - fd).max() <= FD_TOL * max(np.abs(km.temperature).max(), 1e-12), (k, _rel(got, fd))
+        for j in range(atm.n_absorbers):
+            step = 1e-4 * atm.absorber[:, j, k]
+
+            def pa(a, s, o, h, k=k, j=j):
+                a.absorber[:, j, k] += h
+            fd = _fd_bt(orc, d, atm, sfc, geo, opt, pa, step)
+            got = km.absorber[:, :, j, k]
+            scale = max(np.abs(km.absorber[:, :, j]).max(), 1e-12)
+            assert np.abs(got - fd).max() <= FD_TOL * scale, (k, j, _rel(got, fd))
+
+
+def _check_surface(km, orc, d, atm, sfc, geo, opt):
+    def pw(a, s, o, h):
+        s.water_temperature += h
+    fd = _fd_bt(orc, d, atm, sfc, geo, opt, pw, 1e-3)
+    assert np.abs(km.water_temperature - fd).max() <= FD_TOL * np.abs(fd).max()
+
+    def pe(a, s, o, h):
+        o.emissivity = o.emissivity + h
+    fd = _fd_bt(orc, d, atm, sfc, geo, opt, pe, 1e-5)
+    assert np.abs(km.surface_emissivity - fd).max() <= FD_TOL * np.abs(fd).max()
+
+
+def _layers(atm, extra=(3, 30, 60, 90)):
+    """Layers to difference: a few fixed ones plus the cloudy layers of profile 0."""
+    ks = set(k for k in extra if k < int(atm.n_layers.min()))
+    if atm.cloud_water_content is not None:
+        ks |= set(np.nonzero(atm.cloud_water_content[0].max(axis=0) > 0)[0][:4].tolist())
+    return sorted(ks)
+
+
+@pytest.mark.parametrize("sensor,nl,n_streams,wc_scale", [
+    ("mwsynth_c16", 100, None, 100.0),     # stream rule
+    ("mwsynth_c16", 100, 16, 100.0),       # Options%n_Streams = 16
+    ("irsynth_c616", 101, None, 30.0)])
+def test_cloudy_k_matrix_matches_oracle_differences(gpu_lib, cloud_dir, sensor, nl, n_streams, wc_scale):
+    from oracle.pyoracle import Oracle
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 4, nl, 81, wc_scale=wc_scale, n_streams=n_streams)
+    atm.n_clouds[2] = 0   # one clear profile in the batch
+    h = gpu_lib.CRTM([sensor], cloud_dir, 0)
+    km, rts = h.k_matrix(atm, sfc, geo, opt)
+    orc = Oracle(cloud_dir, sensor)
+    _, bt = orc.forward_scatter(atm, sfc, geo, opt, f"{cloud_dir}/CloudCoeff.bin", n_threads=8)
+    assert np.abs(rts.brightness_temperature - bt).max() <= 1e-4
+    _check_layers(km, orc, cloud_dir, atm, sfc, geo, opt, _layers(atm))
+    _check_surface(km, orc, cloud_dir, atm, sfc, geo, opt)
+
+
+def test_aerosol_k_matrix_matches_oracle_differences(gpu_lib, cloud_dir):
+    """IR sensor, liquid and ice clouds plus dust, sea salt and sulfate; one
+    profile with aerosols only, one clear."""
+    from oracle.pyoracle import Oracle
+    sensor = "irsynth_c616"
+    atm, sfc, geo, opt = sy.clear_sky_workload(sensor, 4, 101, 82)
+    sy.add_clouds(atm, (co.WATER_CLOUD, co.ICE_CLOUD), 83, wc_scale=30.0)
+    sy.add_aerosols(atm, sy.AEROSOL_TYPES, 84, load_scale=20.0)
+    atm.n_clouds[1] = 0
+    atm.n_clouds[3] = 0
+    atm.n_aerosols[3] = 0
+    km, rts = gpu_lib.CRTM([sensor], cloud_dir, 0).k_matrix(atm, sfc, geo, opt)
+    orc = Oracle(cloud_dir, sensor)
+    _check_layers(km, orc, cloud_dir, atm, sfc, geo, opt, _layers(atm, (10, 50, 80, 100)))
+    _check_surface(km, orc, cloud_dir, atm, sfc, geo, opt)
+
+
+@pytest.mark.parametrize("sensor,n_streams", [("mwsynth_c16", None), ("irsynth_c616", None),
+                                              ("mwsynth_c16", 8)])
+def test_mixed_cloudy_k_matrix_matches_fp64(gpu_lib, cloud_dir, sensor, n_streams):
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 24, 100, 85, wc_scale=100.0, n_streams=n_streams)
+    atm.n_clouds[::5] = 0
+    ref = gpu_lib.CRTM([sensor], cloud_dir, 0).k_matrix(atm, sfc, geo, opt)
+    mix = gpu_lib.CRTM([sensor], cloud_dir, 1).k_matrix(atm, sfc, geo, opt)
+    assert np.abs(mix[1].brightness_temperature - ref[1].brightness_temperature).max() <= 1e-2
+    for f in ("temperature", "absorber", "water_temperature", "surface_emissivity"):
+        assert _rel(getattr(mix[0], f), getattr(ref[0], f)) <= MIX_TOL, f
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_cloudy_k_matrix_radiance_matches_forward(gpu_lib, cloud_dir, precision):
+    atm, sfc, geo, opt = sy.cloudy_workload("mwsynth_c16", 12, 100, 86, wc_scale=300.0)
+    h = gpu_lib.CRTM(["mwsynth_c16"], cloud_dir, precision)
+    fw = h.forward(atm, sfc, geo, opt)
+    _, rts = h.k_matrix(atm, sfc, geo, opt)
+    assert np.abs(rts.brightness_temperature - fw.brightness_temperature).max() <= 1e-6
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_cloudy_adjoint_is_seeded_k_matrix_sum(gpu_lib, cloud_dir, precision):
+    """Adjoint of a BT seed = sum over channels of seed x K (CRTM_Adjoint vs
+    CRTM_K_Matrix with the same seed)."""
+    sensor = "irsynth_c616"
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 9, 101, 87, wc_scale=30.0)
+    sy.add_aerosols(atm, sy.AEROSOL_TYPES, 88, load_scale=20.0)
+    atm.n_clouds[4] = 0
+    atm.n_aerosols[7] = 0
+    seed = np.random.Generator(np.random.PCG64(89)).standard_normal((9, 616))
+    h = gpu_lib.CRTM([sensor], cloud_dir, precision)
+    km, _ = h.k_matrix(atm, sfc, geo, opt, seed)
+    ad, _ = h.adjoint(atm, sfc, geo, opt, seed)
+    tol = 1e-10 if precision == 0 else 1e-5
+    assert _rel(ad["temperature"], km.temperature.sum(axis=1)) <= tol
+    assert _rel(ad["absorber"], km.absorber.sum(axis=1)) <= tol
+    assert _rel(ad["water_temperature"], km.water_temperature.sum(axis=1)) <= tol
+
+
+def test_clear_profile_in_cloudy_batch_keeps_clear_k_matrix(gpu_lib, cloud_dir):
+    sensor = "mwsynth_c16"
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 5, 100, 90, wc_scale=100.0)
+    atm.n_clouds[1] = 0
+    h = gpu_lib.CRTM([sensor], cloud_dir, 0)
+    km, _ = h.k_matrix(atm, sfc, geo, opt)
+    clear = copy.deepcopy(atm)
+    clear.n_clouds = clear.cloud_type = clear.cloud_water_content = None
+    clear.cloud_effective_radius = clear.cloud_fraction = None
+    kc, _ = h.k_matrix(clear, sfc, geo, opt)
+    assert _rel(km.temperature[1], kc.temperature[1]) <= 1e-12
+    assert _rel(km.absorber[1], kc.absorber[1]) <= 1e-12
+    assert np.abs(km.temperature[0] - kc.temperature[0]).max() > 1e-6   # the clouds do matter
+
+
+def test_isothermal_enclosure_k_matrix_sum_rule(gpu_lib, cloud_dir, tmp_path):
+    """Isothermal scene at 250 K with cosmic background c = B(250 K): BT = 250 K
+    whatever the clouds and absorbers.  Raising every temperature and c together
+    by dT raises BT by dT, so sum_k K_T(k) + K_Ts + dR/dc = 1 for every channel
+    (dBT/dR . dB/dT = 1 with the same band correction).  R is linear in c, so
+    dR/dc comes exactly from a second forward run with c scaled by 1 + 1e-3."""
+    import os
+    import shutil
+    sensor = "mwsynth_c16"
+    sc = co.read_spccoeff(f"{cloud_dir}/{sensor}.SpcCoeff.bin")
+    te = sc.band_c1 + sc.band_c2 * 250.0
+    cosmic = sc.planck_c1 / (np.exp(sc.planck_c2 / te) - 1.0)
+    dirs = []
+    for i, c in enumerate((cosmic, cosmic * (1.0 + 1e-3))):
+        d = tmp_path / f"c{i}"
+        os.makedirs(d)
+        sc.cosmic_background_radiance = c
+        co.write_spccoeff(str(d / f"{sensor}.SpcCoeff.bin"), sc)
+        shutil.copy(f"{cloud_dir}/{sensor}.TauCoeff.bin", d / f"{sensor}.TauCoeff.bin")
+        shutil.copy(f"{cloud_dir}/CloudCoeff.bin", d / "CloudCoeff.bin")
+        dirs.append(str(d))
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 64, 100, 91, wc_scale=300.0)
+    for m in range(64):
+        atm.temperature[m, :atm.n_layers[m]] = 250.0
+    sfc.land_coverage[:] = sfc.snow_coverage[:] = sfc.ice_coverage[:] = 0.0
+    sfc.water_coverage[:] = 1.0
+    sfc.water_temperature[:] = 250.0
+    km, rts = gpu_lib.CRTM([sensor], dirs[0], 0).k_matrix(atm, sfc, geo, opt)
+    assert np.abs(rts.brightness_temperature - 250.0).max() < 1e-8
+    r2 = gpu_lib.CRTM([sensor], dirs[1], 0).forward(atm, sfc, geo, opt).radiance
+    dr_dc = (r2 - rts.radiance) / (cosmic * 1e-3)[None, :]
+    total = km.temperature.sum(axis=2) + km.water_temperature + dr_dc
+    assert np.abs(total - 1.0).max() < 1e-8
+    assert dr_dc.max() > 1e-3   # the clouds reflect part of the cosmic background
+
+
+def test_soi_k_matrix_is_refused(gpu_lib, cloud_dir):
+    atm, sfc, geo, opt = sy.cloudy_workload("mwsynth_c16", 3, 100, 92, wc_scale=100.0)
+    opt.rt_algorithm_id = np.array([56, 168, 56], np.int32)
+    h = gpu_lib.CRTM(["mwsynth_c16"], cloud_dir, 0)
+    with pytest.raises(RuntimeError, match="RT_SOI"):
+        h.k_matrix(atm, sfc, geo, opt)
+    # the handle stays usable
+    km, rts = h.k_matrix(atm, sfc, geo, sy.OptionsBatch(emissivity=opt.emissivity))
+    assert (rts.status == 0).all()

@@ -126,3 +126,128 @@ def test_cloudy_radiance_matches_oracle(sx, coeff_dir, sensor, nl, n_streams, so
             assert rc == 0
             worst = max(worst, abs(r.value - rad_ref[m, l]) / abs(rad_ref[m, l]))
     assert worst < 1e-11
+
+
+@pytest.mark.parametrize("sensor,nleg,wc_scale", [("mwsynth_c16", 6, 300.0), ("mwsynth_c16", 16, 100.0),
+                                                  ("irsynth_c616", 6, 100.0), ("mwsynth_c16", 2, 50.0)])
+def test_layer_derivatives_match_finite_differences(sx, coeff_dir, sensor, nleg, wc_scale):
+    """d(layer T, R, source, optical depth) / d(gas optical depth) and / d(temperature)
+    from derivative numbers through the cloud LUT, combine, phase blocks and
+    MOM (eigen-perturbation), against central differences of the FP64 forward."""
+    path = sy.write_cloud_files(coeff_dir)
+    cc = co.read_cloudcoeff(path)
+    sc = co.read_spccoeff(f"{coeff_dir}/{sensor}.SpcCoeff.bin")
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 2, 100, 53, wc_scale=wc_scale,
+                                            cloud_types=(co.WATER_CLOUD, co.RAIN_CLOUD, co.SNOW_CLOUD))
+    f = lambda a: np.ascontiguousarray(np.ravel(a, order="F"))   # noqa: E731
+    arrs = [f(x) for x in (cc.frequency_mw, cc.reff_mw, cc.temperature, cc.frequency_ir, cc.reff_ir,
+                           cc.ke_l_mw, cc.w_l_mw, cc.pcoeff_l_mw, cc.ke_s_mw, cc.w_s_mw, cc.pcoeff_s_mw,
+                           cc.ke_ir, cc.w_ir, cc.pcoeff_ir)]
+    dims = np.array([cc.frequency_mw.size, cc.reff_mw.size, cc.temperature.size, cc.density_mw.size,
+                     cc.frequency_ir.size, cc.reff_ir.size, cc.n_legendre_terms], np.int32)
+    mw = sc.sensor_type == co.MICROWAVE_SENSOR
+    m = 0
+    wc = np.ascontiguousarray(atm.cloud_water_content[m])
+    re = np.ascontiguousarray(atm.cloud_effective_radius[m])
+    ctype = np.ascontiguousarray(atm.cloud_type[m], np.int32)
+    NC = ctype.size
+    cloudy = np.where((wc > 1e-6).any(axis=0))[0]
+    n = 30 * 30
+    checked = 0
+    for k in cloudy[:6]:
+        for l in (0, sc.n_channels // 2):
+            planck = np.array([sc.planck_c1[l], sc.planck_c2[l], sc.band_c1[l], sc.band_c2[l]])
+            fr = sc.frequency[l] if mw else sc.wavenumber[l]
+
+            def rec(gas, tk):
+                outs = [np.zeros(2 * 20 * 20 + 40) for _ in range(3)]
+                nz = ct.c_int(0)
+                kind = sx.sx_layer_record(_p(dims, _ip), *[_p(a) for a in arrs], NC, nleg, int(mw),
+                                          ct.c_double(fr), ct.c_double(0.83), _p(planck), _p(ctype, _ip),
+                                          _p(wc), _p(re), atm.max_layers, int(k), ct.c_double(gas),
+                                          ct.c_double(tk), *[_p(o) for o in outs], ct.byref(nz))
+                nZ = nz.value
+                ne = 1 + 2 * nZ * nZ + nZ
+                return kind, [o[:ne] for o in outs]
+            gas, tk = 0.05, float(atm.temperature[m, k])
+            kind, (v, dg, dt) = rec(gas, tk)
+            if kind != 1:
+                continue
+            for h, d, which in ((1e-6, dg, 0), (1e-4, dt, 1)):
+                args_p = (gas + h, tk) if which == 0 else (gas, tk + h)
+                args_m = (gas - h, tk) if which == 0 else (gas, tk - h)
+                fd = (rec(*args_p)[1][0] - rec(*args_m)[1][0]) / (2 * h)
+                scale = np.abs(fd).max() + 1e-12
+                assert np.abs(fd - d).max() <= 1e-6 * scale + 1e-10, (k, l, which)
+            checked += 1
+    assert checked > 0
+
+
+@pytest.mark.parametrize("sensor,nl,n_streams,wc_scale", [("mwsynth_c16", 100, None, 300.0),
+                                                          ("mwsynth_c16", 100, 16, 100.0),
+                                                          ("irsynth_c616", 101, None, 100.0)])
+def test_cloudy_kmatrix_matches_finite_differences(sx, coeff_dir, sensor, nl, n_streams, wc_scale):
+    """ADA K-matrix (adjoint of the adding, derivative numbers through the
+    layer optics) against central differences of the FP64 cloudy radiance
+    with respect to each layer's gas optical depth and temperature, the
+    surface emissivity and the surface Planck radiance."""
+    path = sy.write_cloud_files(coeff_dir)
+    cc = co.read_cloudcoeff(path)
+    sc = co.read_spccoeff(f"{coeff_dir}/{sensor}.SpcCoeff.bin")
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 1, nl, 54, wc_scale=wc_scale, n_streams=n_streams)
+    f = lambda a: np.ascontiguousarray(np.ravel(a, order="F"))   # noqa: E731
+    arrs = [f(x) for x in (cc.frequency_mw, cc.reff_mw, cc.temperature, cc.frequency_ir, cc.reff_ir,
+                           cc.ke_l_mw, cc.w_l_mw, cc.pcoeff_l_mw, cc.ke_s_mw, cc.w_s_mw, cc.pcoeff_s_mw,
+                           cc.ke_ir, cc.w_ir, cc.pcoeff_ir)]
+    dims = np.array([cc.frequency_mw.size, cc.reff_mw.size, cc.temperature.size, cc.density_mw.size,
+                     cc.frequency_ir.size, cc.reff_ir.size, cc.n_legendre_terms], np.int32)
+    mw = sc.sensor_type == co.MICROWAVE_SENSOR
+    m, Ku = 0, int(atm.n_layers[0])
+    temp0 = np.ascontiguousarray(atm.temperature[m, :Ku])
+    wc = np.ascontiguousarray(atm.cloud_water_content[m])
+    re = np.ascontiguousarray(atm.cloud_effective_radius[m])
+    ctype = np.ascontiguousarray(atm.cloud_type[m], np.int32)
+    od0 = np.full(Ku, 0.02) * (1.0 + 0.5 * np.sin(np.arange(Ku)))
+    mu = np.cos(np.deg2rad(geo.sensor_zenith_angle[m]))
+    for l in (0, sc.n_channels // 3):
+        planck = np.array([sc.planck_c1[l], sc.planck_c2[l], sc.band_c1[l], sc.band_c2[l]])
+        nleg = n_streams or sx.sx_stream_rule(ct.c_double(re[:, :Ku].max()), ct.c_double(sc.wavenumber[l]))
+        fr = sc.frequency[l] if mw else sc.wavenumber[l]
+        e, bs, cbr = float(opt.emissivity[m, l]), 1.5 * planck[0], float(sc.cosmic_background_radiance[l])
+
+        def fwd(od, temp, e=e, bs=bs):
+            r = ct.c_double()
+            assert sx.sx_cloudy_radiance(_p(dims, _ip), *[_p(a) for a in arrs], Ku, ctype.size, nleg, int(mw),
+                                         ct.c_double(fr), ct.c_double(mu), ct.c_double(e), ct.c_double(bs),
+                                         ct.c_double(cbr), _p(planck), _p(temp), _p(ctype, _ip), _p(wc), _p(re),
+                                         atm.max_layers, _p(od), 0, 0, None, None, None, None, None, None,
+                                         None, None, None, None, ct.c_double(sc.wavenumber[l]), ct.byref(r)) == 0
+            return r.value
+        dg, dT = np.zeros(Ku), np.zeros(Ku)
+        rad, eb, bb = ct.c_double(), ct.c_double(), ct.c_double()
+        assert sx.sx_cloudy_kmatrix(_p(dims, _ip), *[_p(a) for a in arrs], Ku, ctype.size, nleg, int(mw),
+                                    ct.c_double(fr), ct.c_double(mu), ct.c_double(e), ct.c_double(bs),
+                                    ct.c_double(cbr), _p(planck), _p(temp0), _p(ctype, _ip), _p(wc), _p(re),
+                                    atm.max_layers, _p(od0), ct.byref(rad), _p(dg), _p(dT), ct.byref(eb),
+                                    ct.byref(bb)) == 0
+        assert abs(rad.value - fwd(od0, temp0)) <= 1e-13 * abs(rad.value)
+        cloudy = np.where((wc[:, :Ku] > 1e-6).any(axis=0))[0]
+        for k in list(cloudy[:5]) + [0, Ku - 1]:
+            h = 1e-7
+            o1, o2 = od0.copy(), od0.copy()
+            o1[k] += h
+            o2[k] -= h
+            fd = (fwd(o1, temp0) - fwd(o2, temp0)) / (2 * h)
+            assert abs(fd - dg[k]) <= 1e-6 * np.abs(dg).max(), (l, k, fd, dg[k])
+            h = 1e-4
+            t1, t2 = temp0.copy(), temp0.copy()
+            t1[k] += h
+            t2[k] -= h
+            fd = (fwd(od0, t1) - fwd(od0, t2)) / (2 * h)
+            assert abs(fd - dT[k]) <= 1e-6 * np.abs(dT).max(), (l, k, fd, dT[k])
+        he = 1e-3
+        fd = (fwd(od0, temp0, e=e + he) - fwd(od0, temp0, e=e - he)) / (2 * he)
+        assert abs(fd - eb.value) <= 1e-5 * abs(eb.value) + 1e-15 * abs(rad.value) / he
+        # the radiance is linear in the surface Planck radiance: a large step is exact
+        fd = (fwd(od0, temp0, bs=bs * 1.1) - fwd(od0, temp0, bs=bs * 0.9)) / (0.2 * bs)
+        assert abs(fd - bb.value) <= 1e-6 * abs(bb.value) + 1e-12
