@@ -54,7 +54,8 @@ class CBatch(ct.Structure):
                 ("cloud_water_content", ct.c_void_p), ("cloud_effective_radius", ct.c_void_p),
                 ("n_streams", ct.c_void_p), ("rt_algorithm_id", ct.c_void_p),
                 ("max_aerosols", ct.c_int), ("n_aerosols", ct.c_void_p), ("aerosol_type", ct.c_void_p),
-                ("aerosol_concentration", ct.c_void_p), ("aerosol_effective_radius", ct.c_void_p)]
+                ("aerosol_concentration", ct.c_void_p), ("aerosol_effective_radius", ct.c_void_p),
+                ("cloud_fraction", ct.c_void_p), ("overlap_id", ct.c_void_p)]
 
 
 class CRTSolution(ct.Structure):
@@ -208,6 +209,10 @@ class CRTM:
             b.cloud_type = c(atm.cloud_type, np.int32)
             b.cloud_water_content = c(atm.cloud_water_content)
             b.cloud_effective_radius = c(atm.cloud_effective_radius)
+            if atm.cloud_fraction is not None:
+                b.cloud_fraction = c(atm.cloud_fraction)
+        if getattr(opt, "overlap_id", None) is not None:
+            b.overlap_id = c(opt.overlap_id, np.int32)
         if opt.n_streams is not None:
             use = opt.use_n_streams if opt.use_n_streams is not None else np.ones(atm.n_profiles, bool)
             b.n_streams = c(np.where(use, opt.n_streams, 0), np.int32)
@@ -292,7 +297,7 @@ class CRTM:
                   "sensor_zenith_angle", "source_zenith_angle", "surface_altitude", "emissivity",
                   "n_clouds", "cloud_type", "cloud_water_content", "cloud_effective_radius",
                   "n_streams", "rt_algorithm_id", "n_aerosols", "aerosol_type", "aerosol_concentration",
-                  "aerosol_effective_radius"):
+                  "aerosol_effective_radius", "cloud_fraction", "overlap_id"):
             t = dev.get(f)
             setattr(b, f, None if t is None else t.data_ptr())
         if dev.get("cloud_type") is not None:

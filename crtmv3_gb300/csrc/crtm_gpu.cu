@@ -521,7 +521,10 @@ struct Work {
   R* LB;            // scattering: [n][Kmax][NE][L] layer records
   double* FB;       // cloudy forward with SOI: [n][2][2][Kmax+1][NZ][L] fields
   double* maxreff;  // scattering: [n]
+  double* cover;    // scattering: [n] total cloud cover
   double* AS;       // scattering K-matrix/adjoint: [n][Kmax+1][NZ*NZ+NZ][L] adding states
+  R* TODc;          // scattering K-matrix/adjoint: [n][Kmax][L] cloudy dR/dtau
+  double* CB;       // scattering K-matrix/adjoint: [n][3][L] cloudy radiance and surface terms
   double* ras;      // adjoint: [n][nv][K]
   double* pts;      // adjoint: [n][Kmax]
   double* tss;      // adjoint: [n]
@@ -580,10 +583,13 @@ size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w
   if (sw.rec > 0) {
     wk.LB = (R*)carve(nn * Kmax * (size_t)sw.rec * L * sizeof(R));
     wk.maxreff = (double*)carve(nn * sizeof(double));
+    wk.cover = (double*)carve(nn * sizeof(double));
     // SOI fields: 2 fields x 2 buffers x levels x angles
     wk.FB = sw.soi ? (double*)carve(nn * 4 * (size_t)(Kmax + 1) * sw.nz * L * sizeof(double)) : nullptr;
     wk.AS = sw.kstate ? (double*)carve(nn * (size_t)(Kmax + 1) * (sw.nz * sw.nz + sw.nz) * L * sizeof(double))
                       : nullptr;
+    wk.TODc = sw.kstate ? (R*)carve(nn * Kmax * L * sizeof(R)) : nullptr;
+    wk.CB = sw.kstate ? (double*)carve(nn * 3 * L * sizeof(double)) : nullptr;
   }
   if (adj) {
     wk.TAU = (R*)carve(nn * Kmax * L * sizeof(R));
@@ -776,6 +782,7 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       ca.pass = 1;
       ca.n_clouds = b->max_clouds > 0 ? b->n_clouds : nullptr;
       ca.n_aerosols = b->max_aerosols > 0 ? b->n_aerosols : nullptr;
+      ca.TODc = w.TODc; ca.CB = w.CB; ca.cover = w.cover;
     }
     dim3 gc((L + 127) / 128, n);
     {
@@ -795,17 +802,18 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       sa.n_aerosols = b->n_aerosols; sa.aerosol_type = b->aerosol_type;
       sa.conc = b->aerosol_concentration; sa.aer_reff = b->aerosol_effective_radius;
       if (b->max_clouds <= 0) sa.max_clouds = 0;
-      sa.TAU = w.TAU; sa.LB = w.LB; sa.maxreff = w.maxreff;
+      sa.TAU = w.TAU; sa.LB = w.LB; sa.maxreff = w.maxreff; sa.cover = w.cover;
+      sa.cloud_fraction = sa.max_clouds > 0 ? b->cloud_fraction : nullptr;
+      sa.overlap = sa.max_clouds > 0 ? b->overlap_id : nullptr;
       sa.radiance = rts->radiance; sa.bt = rts->brightness_temperature;
       sa.status = rts->status; sa.error = h->d_error;
-      sa.mode = mode; sa.TOD = w.TAU; sa.PT = w.PT; sa.SC = w.SC; sa.seed = seed;
-      sa.tsk = ca.tsk; sa.ek = ca.ek; sa.AS = w.AS;
+      sa.TODc = w.TODc; sa.PT = w.PT; sa.CB = w.CB; sa.AS = w.AS;
       const long long nlay = (long long)n * Kmax * L;
       const unsigned gl = (unsigned)((nlay + SCATTER_THREADS - 1) / SCATTER_THREADS);
       dim3 ga((L + SCATTER_THREADS - 1) / SCATTER_THREADS, n);
       {
         StageScope sc(h, 6, st);
-        scatter_maxreff_kernel<R><<<(n + 3) / 4, 128, 0, st>>>(sa);
+        scatter_profile_kernel<R><<<(n + 3) / 4, 128, 0, st>>>(sa);
         CK_LAUNCH(h);
         if (split) {
           if (nz_max)
@@ -984,7 +992,9 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
                                {b->cloud_effective_radius, (size_t)P * NC * Km * 8},
                                {b->n_clouds, (size_t)P * 4}, {b->cloud_type, (size_t)P * NC * 4},
                                {b->n_streams, b->n_streams ? (size_t)P * 4 : 0},
-                               {b->rt_algorithm_id, b->rt_algorithm_id ? (size_t)P * 4 : 0}});
+                               {b->rt_algorithm_id, b->rt_algorithm_id ? (size_t)P * 4 : 0},
+                               {b->cloud_fraction, b->cloud_fraction ? (size_t)P * Km * 8 : 0},
+                               {b->overlap_id, b->overlap_id ? (size_t)P * 4 : 0}});
   }
   const size_t aer0 = items.size();
   if (NA > 0)
@@ -1028,6 +1038,11 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
     db.cloud_type = (const int*)dptr[20];
     db.n_streams = (const int*)dptr[21];
     db.rt_algorithm_id = (const int*)dptr[22];
+    db.cloud_fraction = (const double*)dptr[23];
+    db.overlap_id = (const int*)dptr[24];
+  } else {
+    db.cloud_fraction = nullptr;
+    db.overlap_id = nullptr;
   }
   if (NA > 0) {
     db.aerosol_concentration = (const double*)dptr[aer0];
@@ -1091,7 +1106,7 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
       return fail(h, "cannot read the scattering error flag");
     if (code) return fail(h, "scattering radiative transfer failed (code %d: 1-3 stream set, 4 cloud type, "
                              "5-6 singular matrix, 8 aerosol stream set or LUT, 9 aerosol type, 10 K-matrix or adjoint "
-                             "requested with RT_SOI)", code);
+                             "requested with RT_SOI, 11 invalid Options%Overlap_Id)", code);
   }
   if (rts->status)
     for (int m = 0; m < P; m++)

@@ -603,11 +603,15 @@ struct ColumnArgs {
   double* tsk, *ek;       // K-matrix: [P][L]; adjoint: tsk is [n][L] scratch
   int* status;            // [P] or null
   // Scattering profiles in a K-matrix/adjoint call: launched twice.  pass 1
-  // stores TAU/DTOP and stops; the scattering K kernel then overwrites TAU of
-  // scattering profiles with dR/dtau; pass 2 finishes clear profiles as usual
-  // and, for scattering profiles, maps dR/dtau onto the reference levels.
+  // stores TAU/DTOP and stops; the scattering K kernel then writes the cloudy
+  // column's unit-seed derivatives; pass 2 finishes clear profiles as usual
+  // and, for scattering profiles, mixes the cloudy column with the clear one
+  // (weights tcc and 1 - tcc of a fractional profile; 1 and 0 otherwise).
   int pass;                      // 0: one launch (no scattering profiles)
   const int* n_clouds, *n_aerosols;   // [P] or null
+  const R* TODc;                 // [n][Kmax][L] cloudy dR/dtau (PT holds the cloudy dR/dT)
+  const double* CB;              // [n][3][L] cloudy radiance, dR/de, dR/dBs
+  const double* cover;           // [n] total cloud cover, -1: no clear part
 };
 
 template <class R>
@@ -757,19 +761,10 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
       pa_hi += f * v;
     }
   };
-  if (a.pass == 2 && ((a.n_clouds && a.n_clouds[gp] > 0) || (a.n_aerosols && a.n_aerosols[gp] > 0))) {
-    // scattering profile: TAU holds dR/dtau from the scattering K kernel, which
-    // also wrote PT, SC and the surface and radiance outputs
-    for (int ku = Ku - 1; ku >= 0; ku--) {
-      const R tod = a.TAU[cs + (size_t)ku * L];
-      ua_hi += tod * inv_sec;
-      scatter(ku + 1, ua_hi);
-      ua_hi = -tod * inv_sec;
-    }
-    scatter(0, ua_hi);
-    while (plvl >= 0) flush();
-    return;
-  }
+  const bool scat = a.pass == 2 && ((a.n_clouds && a.n_clouds[gp] > 0) || (a.n_aerosols && a.n_aerosols[gp] > 0));
+  double wcloud = 0.0;   // weight of the cloudy column
+  if (scat) wcloud = a.cover[p] < 0.0 ? 1.0 : a.cover[p];
+  const R wclr = R(1.0 - wcloud), wcl = R(wcloud);
   R tau_n = a.TAU[cs + (size_t)(Ku - 1) * L], dt_n = a.DTOP[cs + (size_t)(Ku - 1) * L];
   for (int ku = Ku - 1; ku >= 0; ku--) {
     const R tau = tau_n, Dtop = dt_n;
@@ -789,7 +784,12 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
     const R dad = down0 * P;
     Bad += dad * (R(1) - t);
     tod -= ((Dtop - B) * t * dad) * inv_u;
-    a.PT[cs + (size_t)ku * L] = dB * Bad;
+    R ptv = dB * Bad;
+    if (scat) {
+      ptv = wclr * ptv + wcl * a.PT[cs + (size_t)ku * L];
+      tod = wclr * tod + wcl * a.TODc[cs + (size_t)ku * L];
+    }
+    a.PT[cs + (size_t)ku * L] = ptv;
     U = t * U + B * (R(1) - t);
     P *= t;
     cum += tau;
@@ -802,8 +802,18 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   scatter(0, ua_hi);
   while (plvl >= 0) flush();
   for (int ku = Ku; ku < Kmax; ku++) a.PT[cs + (size_t)ku * L] = R(0);
-  // ---- TOA radiance, brightness temperature and the adjoint seed
-  const double Rd = double(U);
+  // ---- TOA radiance, brightness temperature and the adjoint seed; the
+  // surface derivatives for a unit radiance seed (emissivity with the
+  // reflectivity 1 - e, and the surface Planck radiance)
+  double Rd = double(U);
+  double e_b = double(Tn) * (double(Bs) - double(Dn));
+  double Bs_b = e * double(Tn);
+  if (scat) {
+    const double* cb = a.CB + (size_t)p * 3 * L + l;
+    Rd = (1.0 - wcloud) * Rd + wcloud * cb[0];
+    e_b = (1.0 - wcloud) * e_b + wcloud * cb[(size_t)L];
+    Bs_b = (1.0 - wcloud) * Bs_b + wcloud * cb[2 * (size_t)L];
+  }
   a.radiance[pl] = Rd;
   double btv, dtdr;
   planck_temperature_with_dR(c1d, c2d, b1d, b2d, Rd, &btv, &dtdr);
@@ -813,11 +823,10 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   a.SC[(size_t)p * L + l] = R(scale);
   const R dden = ted * (eed - R(1));
   const R dBs = c1 * c2 * eed * b2 / (dden * dden);
-  const double up_final = scale * double(Tn);
-  const double ts_ad = a.b.water_cov[gp] * double(dBs) * e * up_final;
+  const double ts_ad = a.b.water_cov[gp] * double(dBs) * Bs_b * scale;
   if (a.mode == 1) {
     a.tsk[pl] = ts_ad;
-    a.ek[pl] = up_final * (double(Bs) - double(Dn));   // emissivity_AD - reflectivity_AD
+    a.ek[pl] = scale * e_b;   // emissivity_AD - reflectivity_AD
   } else {
     a.tsk[(size_t)p * L + l] = ts_ad;
   }

@@ -26,12 +26,14 @@
 //   scatter_kmatrix_kernel   one thread per (profile, channel): the adding
 //                            from the surface with the level states kept in
 //                            AS, then the adding adjoint from the top down,
-//                            contracted with the layer derivatives.  Writes
-//                            dR/dtau of each user layer over TAU (the second
-//                            column launch maps it onto the reference
-//                            levels), the Planck part of the temperature
-//                            adjoint into PT, the adjoint seed into SC, and
-//                            the surface adjoints.
+//                            contracted with the layer derivatives.  Writes,
+//                            for a unit radiance seed, dR/dtau of each user
+//                            layer (TODc), the Planck part of the temperature
+//                            derivative (PT), and the radiance and surface
+//                            derivatives (CB).  The second column launch
+//                            mixes them with the clear column of a
+//                            fractional profile, applies the Planck-inversion
+//                            seed and maps dR/dtau onto the reference levels.
 #pragma once
 
 #include "odps_kernels.cuh"
@@ -73,31 +75,36 @@ struct ScatterArgs {
   double* FB;                   // SOI fields [n][2][2][Kmax+1][NZ][L], or null
   const R* TAU;                 // [n][Kmax][L] gas layer optical depths
   R* LB;                        // [n][Kmax][NE][L] layer records
+  const double* cloud_fraction; // [P][Kmax] or null (1)
+  const int* overlap;           // [P] Options%Overlap_Id or null (4, average)
   double* maxreff;              // [n]
+  double* cover;                // [n] total cloud cover, -1: no clear part
   double* radiance, *bt;        // [P][L]
   int* status;                  // [P] or null
   int* error;                   // first failing code (device), 0 if none
-  // K-matrix (mode 1) and adjoint (mode 2)
-  int mode;
-  R* TOD;                       // [n][Kmax][L] out: dR/dtau of the user layers (aliases TAU)
-  R* PT;                        // [n][Kmax][L] out: dR/dT at fixed gas optical depth
-  R* SC;                        // [n][L] out: dBT/dR * seed
-  const double* seed;           // [P][L] or null (=1)
-  double* tsk, *ek;             // K-matrix: [P][L]; adjoint: tsk is [n][L]
+  // K-matrix and adjoint: the cloudy column's derivatives for a unit
+  // radiance seed, combined with the clear column by the second column launch
+  R* TODc;                      // [n][Kmax][L] dR/dtau of the user layers
+  R* PT;                        // [n][Kmax][L] dR/dT at fixed gas optical depth
+  double* CB;                   // [n][3][L] radiance, dR/d(emissivity), dR/d(surface Planck)
   double* AS;                   // [n][Kmax+1][NS][L] adding states
 };
 
 constexpr int SCATTER_THREADS = 128;
 
-// Largest effective radius of each profile's clouds (stream rule input).
+// Per profile, one warp each: the largest effective radius of its clouds and
+// aerosols (stream rule input; clouds dropped by a fraction below 1e-12 do
+// not count) and the total cloud cover of a fractional profile.
 template <class R>
-__global__ void scatter_maxreff_kernel(ScatterArgs<R> a) {
+__global__ void scatter_profile_kernel(ScatterArgs<R> a) {
   const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (p >= a.n_chunk) return;
   const int gp = a.p_begin + p, Ku = a.b.n_layers[gp];
   const int nc = a.max_clouds > 0 ? a.n_clouds[gp] : 0, na = a.max_aerosols > 0 ? a.n_aerosols[gp] : 0;
+  const double* cf = a.cloud_fraction ? a.cloud_fraction + (size_t)gp * a.Kmax : nullptr;
   double mr = 0.0;
   for (int i = lane; i < nc * Ku; i += 32) {
+    if (cf && cf[i % Ku] < MIN_COVERAGE) continue;
     const double r = a.reff[((size_t)gp * a.max_clouds + i / Ku) * a.Kmax + (i % Ku)];
     mr = r > mr ? r : mr;
   }
@@ -109,7 +116,36 @@ __global__ void scatter_maxreff_kernel(ScatterArgs<R> a) {
     const double v = __shfl_xor_sync(FULL, mr, o);
     mr = v > mr ? v : mr;
   }
-  if (lane == 0) a.maxreff[p] = mr;
+  if (lane == 0) {
+    a.maxreff[p] = mr;
+    double tcc = -1.0;
+    if (nc > 0) {
+      tcc = total_cloud_cover(Ku, nc, cf, a.wc + (size_t)gp * a.max_clouds * a.Kmax, (size_t)a.Kmax,
+                              a.overlap ? a.overlap[gp] : 4);
+      if (tcc < -1.5) {
+        atomicCAS(a.error, 0, 11);
+        if (a.status) atomicOr(a.status + gp, 1 << 4);
+        tcc = -1.0;
+      }
+    }
+    a.cover[p] = tcc;
+  }
+}
+
+// Radiance of the clear column (gas optical depths tau, stride L; Emission
+// solver in FP64), the clear part of a fractional profile.
+template <class R>
+__device__ double clear_column_radiance(const CloudyColumn& c, const R* tau, int L) {
+  const double inv_u = 1.0 / c.mu_sensor;
+  double down = c.cosmic, tr_tot = 1.0, src = 0.0;
+  for (int k = 0; k < c.Ku; k++) {
+    const double t = exp(-double(tau[(size_t)k * L]) * inv_u);
+    const double B = c.c1 / (exp(c.c2 / (c.b1 + c.b2 * c.temperature[k])) - 1.0);
+    src += tr_tot * B * (1.0 - t);
+    down = down * t + B * (1.0 - t);
+    tr_tot *= t;
+  }
+  return src + tr_tot * (c.emissivity * c.planck_surface + (1.0 - c.emissivity) * down);
 }
 
 template <class R>
@@ -141,6 +177,9 @@ __device__ __forceinline__ CloudyColumn column_inputs(const ScatterArgs<R>& a, i
   c.conc = a.max_aerosols > 0 ? a.conc + (size_t)gp * a.max_aerosols * a.Kmax : nullptr;
   c.aer_reff = a.max_aerosols > 0 ? a.aer_reff + (size_t)gp * a.max_aerosols * a.Kmax : nullptr;
   c.alut = &a.alut;
+  c.cf = a.cloud_fraction && c.n_clouds > 0 ? a.cloud_fraction + (size_t)gp * a.Kmax : nullptr;
+  const double tcc = a.cover[p];
+  c.wc_div = tcc > MIN_COVERAGE ? tcc : 1.0;
   return c;
 }
 
@@ -197,16 +236,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_adding_kernel(Scatter
   double rad = 0.0;
   int code = 0;
   if (c.n_clouds == 0 && c.n_aerosols == 0) {   // clear profile: Emission solver, FP64 here
-    const double inv_u = 1.0 / c.mu_sensor;
-    double down = c.cosmic, tr_tot = 1.0, src = 0.0;
-    for (int k = 0; k < c.Ku; k++) {
-      const double t = exp(-double(tau[(size_t)k * L]) * inv_u);
-      const double B = c.c1 / (exp(c.c2 / (c.b1 + c.b2 * c.temperature[k])) - 1.0);
-      src += tr_tot * B * (1.0 - t);
-      down = down * t + B * (1.0 - t);
-      tr_tot *= t;
-    }
-    rad = src + tr_tot * (c.emissivity * c.planck_surface + (1.0 - c.emissivity) * down);
+    rad = clear_column_radiance(c, tau, L);
   } else if (c.soi) {
     return;   // SOI profiles: scatter_soi_kernel
   } else {
@@ -237,6 +267,8 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_adding_kernel(Scatter
         }
       }
       if (!code) rad = adding_toa<NZ>(A, nZ, S.isat, c.cosmic);
+      const double tcc = a.cover[p];
+      if (!code && tcc >= 0.0) rad = (1.0 - tcc) * clear_column_radiance(c, tau, L) + tcc * rad;
     }
   }
   if (code) {
@@ -290,6 +322,9 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_soi_kernel(ScatterArg
     for (int k = 0; k < c.Ku && !code; k++)
       if ((int)a.LB[((size_t)p * Kmax + k) * NE * L + l] < 0) code = -(int)a.LB[((size_t)p * Kmax + k) * NE * L + l];
     if (!code) soi_solve<NZ>(nZ, c.Ku, S.isat, S.mu, c.emissivity, c.planck_surface, c.cosmic, layer, dn, up, &rad);
+    const double tcc = a.cover[p];
+    if (!code && tcc >= 0.0)
+      rad = (1.0 - tcc) * clear_column_radiance(c, a.TAU + (size_t)p * Kmax * L + l, L) + tcc * rad;
   }
   if (code) {
     atomicCAS(a.error, 0, code);
@@ -359,8 +394,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_kmatrix_kernel(Scatte
   if (l >= L || a.pv.status[p] != 0) return;
   const CloudyColumn c = column_inputs(a, p, gp, l);
   if (c.n_clouds == 0 && c.n_aerosols == 0) return;   // clear: the column kernel's Emission adjoint
-  const size_t pl = (size_t)gp * L + l;
-  R* tod = a.TOD + (size_t)p * Kmax * L + l;
+  R* tod = a.TODc + (size_t)p * Kmax * L + l;
   R* pt = a.PT + (size_t)p * Kmax * L + l;
   double rad = 0.0, e_b = 0.0, Bs_b = 0.0;
   StreamSet<NZ, double> S;
@@ -410,34 +444,16 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_kmatrix_kernel(Scatte
     };
     code = cloudy_kmatrix<NZ>(c, S, layer, state, contract, out, &rad, &e_b, &Bs_b);
   }
-  double scale = 0.0, ts_ad = 0.0, btv = 0.0;
   if (code) {
     atomicCAS(a.error, 0, code);
     if (a.status) atomicOr(a.status + gp, 1 << 4);
-    rad = 0.0;
-    e_b = 0.0;
-    for (int k = 0; k < Kmax; k++) { tod[(size_t)k * L] = R(0); pt[(size_t)k * L] = R(0); }
-  } else {
-    for (int k = c.Ku; k < Kmax; k++) pt[(size_t)k * L] = R(0);
-    double dtdr;
-    planck_temperature_with_dR(c.c1, c.c2, c.b1, c.b2, rad, &btv, &dtdr);
-    scale = dtdr * (a.seed ? a.seed[pl] : 1.0);
-    // surface temperature: d(Planck)/dTs of the water surface
-    const double ts = a.b.land_cov[gp] * a.b.land_t[gp] + a.b.water_cov[gp] * a.b.water_t[gp] +
-                      a.b.snow_cov[gp] * a.b.snow_t[gp] + a.b.ice_cov[gp] * a.b.ice_t[gp];
-    const double te = c.b1 + c.b2 * ts, ee = exp(c.c2 / te);
-    const double dBs = c.c1 * c.c2 * ee * c.b2 / (te * te * (ee - 1.0) * (ee - 1.0));
-    ts_ad = a.b.water_cov[gp] * dBs * Bs_b * scale;
+    rad = e_b = Bs_b = 0.0;
+    for (int k = 0; k < c.Ku; k++) { tod[(size_t)k * L] = R(0); pt[(size_t)k * L] = R(0); }
   }
-  a.radiance[pl] = rad;
-  a.bt[pl] = btv;
-  a.SC[(size_t)p * L + l] = R(scale);
-  if (a.mode == 1) {
-    a.tsk[pl] = ts_ad;
-    a.ek[pl] = scale * e_b;
-  } else {
-    a.tsk[(size_t)p * L + l] = ts_ad;
-  }
+  double* cb = a.CB + (size_t)p * 3 * L + l;
+  cb[0] = rad;
+  cb[(size_t)L] = e_b;
+  cb[2 * (size_t)L] = Bs_b;
 }
 
 }  // namespace crtm

@@ -31,6 +31,8 @@ namespace crtm {
 constexpr int SC_NLEG_MAX = 16;          // MAX_N_LEGENDRE_TERMS
 constexpr int SC_NZ_MAX = 10;            // 9 streams (16-stream option) + the sensor angle
 constexpr double WATER_CONTENT_THRESHOLD = 1.0e-6;   // CRTM_Parameters.f90:256
+constexpr double MIN_COVERAGE = 1.0e-12;             // CRTM_Parameters.f90:257
+constexpr double FRACTIONAL_COVERAGE = 1.0e-6;       // CRTM_Atmosphere.f90:164
 constexpr double BS_THRESHOLD = 1.0e-10;             // CRTM_Parameters.f90:260
 constexpr double MAX_ALBEDO = 0.999999;              // RTV_Define.f90:77
 constexpr double PHASE_THRESHOLD = 1.0e-7;           // RTV_Define.f90:74
@@ -585,6 +587,73 @@ CRTM_HD bool soi_doubling(bool trunc, int nS, int nZ, double w, double tau, cons
   return true;
 }
 
+// Total cloud cover of a profile (Compute_CloudCover,
+// CRTM_CloudCover_Define.f90:447-642) after its coverage flag
+// (CRTM_Atmosphere_Coverage, CRTM_Atmosphere.f90:158-203).  cf: the layers'
+// Cloud_Fraction (null: 1), values below 1e-12 count as 0 and drop the
+// layer's clouds; wc: n_clouds rows of stride cstride.  Returns the total
+// cover of a FRACTIONAL profile (a cloudy layer with a fraction above 1e-6),
+// -1 for a profile whose clouds fill the column, -2 for an invalid overlap id
+// (1 maximum, 2 random, 3 maximum-random, 4 average, 5 overcast).
+CRTM_HD double total_cloud_cover(int Ku, int n_clouds, const double* cf, const double* wc, size_t cstride,
+                                 int overlap) {
+  auto frac = [&](int k) {
+    const double f = cf ? cf[k] : 1.0;
+    return f < MIN_COVERAGE ? 0.0 : f;
+  };
+  auto lwc = [&](int k) {   // cloud water of the layer above the threshold
+    double s = 0.0;
+    if (frac(k) == 0.0) return s;
+    for (int c = 0; c < n_clouds; c++) {
+      const double w = wc[c * cstride + k];
+      if (w > WATER_CONTENT_THRESHOLD) s += w;
+    }
+    return s;
+  };
+  bool fractional = false;
+  for (int k = 0; k < Ku && !fractional; k++) fractional = frac(k) > FRACTIONAL_COVERAGE && lwc(k) > 0.0;
+  if (!fractional) return -1.0;
+  double tcc = 0.0;
+  switch (overlap) {
+    case 1:   // maximum
+      for (int k = 0; k < Ku; k++) tcc = frac(k) > tcc ? frac(k) : tcc;
+      break;
+    case 2: {   // random
+      double prod = 1.0;
+      for (int k = 0; k < Ku; k++)
+        if (frac(k) > MIN_COVERAGE) prod *= 1.0 - frac(k);
+      tcc = 1.0 - prod;
+      break;
+    }
+    case 3: {   // maximum-random
+      double prod = 1.0 - frac(0);
+      for (int k = 1; k < Ku; k++) {
+        const double a = frac(k - 1), b = frac(k);
+        const double mc = 1.0 - (a > b ? a : b);
+        prod = (prod == 0.0 && 1.0 - a == 0.0) ? mc : prod * (mc / (1.0 - a));
+      }
+      tcc = 1.0 - prod;
+      break;
+    }
+    case 4: {   // average, weighted by the layers' cloud water
+      double ws = 0.0, cws = 0.0;
+      for (int k = 0; k < Ku; k++) {
+        const double w = lwc(k);
+        ws += w;
+        cws += frac(k) * w;
+      }
+      tcc = ws > 0.0 ? cws / ws : 0.0;
+      break;
+    }
+    case 5:   // overcast
+      tcc = 1.0;
+      break;
+    default:
+      return -2.0;
+  }
+  return tcc;
+}
+
 // Inputs of one (profile, channel) for the cloudy solver.
 struct CloudyColumn {
   int Ku, n_clouds, nleg;                // nleg: Legendre terms of the stream set
@@ -604,6 +673,12 @@ struct CloudyColumn {
   const double* conc;                    // [n_aerosols] rows of stride cstride, kg/m^2
   const double* aer_reff;
   const AerosolLut* alut;
+  // Cloud_Fraction of the profile's layers (null: 1): clouds are dropped
+  // where it is below 1e-12 (CRTM_Forward_Module.f90:367-376); water content
+  // divided by the total cloud cover of a fractional profile (Compute_CloudCover,
+  // CRTM_CloudCover_Define.f90:512-519), 1 otherwise.
+  const double* cf = nullptr;
+  double wc_div = 1.0;
 };
 
 // Stream angles of a (profile, channel): Gauss angles of the stream set plus
@@ -656,8 +731,9 @@ CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const Stre
   S od = gas_od, bs_sum = S(0.0);
   S pc[SC_NLEG_MAX + 1], pcs[SC_NLEG_MAX + 1];
   for (int l = 0; l <= nleg; l++) pcs[l] = S(0.0);
-  for (int c = 0; c < in.n_clouds; c++) {
-    const double wc = in.wc[c * in.cstride + k];
+  const bool dropped = in.cf && in.cf[k] < MIN_COVERAGE;
+  for (int c = 0; c < in.n_clouds && !dropped; c++) {
+    const double wc = in.wc[c * in.cstride + k] / in.wc_div;
     if (!(wc > WATER_CONTENT_THRESHOLD)) continue;
     S ke, w;
     if (!cloud_layer_optics<S>(lut, in.microwave, in.freq, in.cloud_type[c], in.reff[c * in.cstride + k], tk,

@@ -131,12 +131,13 @@ class OptionsBatch:
     n_streams: Optional[np.ndarray] = None       # (P,) int
     rt_algorithm_id: Optional[np.ndarray] = None  # (P,) RT_ADA / RT_SOI
     include_scattering: bool = True
+    overlap_id: Optional[np.ndarray] = None      # (P,) cloud-cover overlap 1-5 (None: 4, average)
 
     def subset(self, idx) -> "OptionsBatch":
         def take(a):
             return None if a is None else np.ascontiguousarray(a[idx])
         return OptionsBatch(take(self.emissivity), take(self.use_n_streams), take(self.n_streams),
-                            take(self.rt_algorithm_id), self.include_scattering)
+                            take(self.rt_algorithm_id), self.include_scattering, take(self.overlap_id))
 
 
 @dataclasses.dataclass

@@ -469,13 +469,16 @@ REFF_RANGE = {co.WATER_CLOUD: (5.0, 20.0), co.ICE_CLOUD: (20.0, 200.0), co.RAIN_
 
 
 def add_clouds(atm: AtmosphereBatch, cloud_types: Sequence[int], seed: int, max_fraction: float = 0.3,
-               wc_scale: float = 1.0) -> AtmosphereBatch:
+               wc_scale: float = 1.0, cover=None) -> AtmosphereBatch:
     """Give every profile the clouds ``cloud_types``: each active in a random
     0-``max_fraction`` of the layers, water content lognormal with geometric
     mean 0.05 g/m^2 x ``wc_scale`` and sigma_ln 1.2 (stored in kg/m^2, the
     reference's unit), effective radius uniform in the type's range.
-    Cloud_Fraction stays 0, so the reference treats the profile as one
-    cloudy column (coverage flag CLEAR, no clear/cloudy mixing)."""
+    Cloud_Fraction is 1 in the cloudy layers (``cover`` None), or uniform in
+    ``cover`` = (lo, hi) there; 0 elsewhere.  The reference drops clouds
+    where the fraction is below 1e-12, and mixes a clear and a cloudy column
+    by the overlap scheme's total cover when a cloudy layer's fraction is
+    above 1e-6 (with fraction 1 the total cover is 1: one cloudy column)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     P, K = atm.n_profiles, atm.max_layers
     NC = len(cloud_types)
@@ -493,7 +496,12 @@ def add_clouds(atm: AtmosphereBatch, cloud_types: Sequence[int], seed: int, max_
     atm.cloud_type = np.tile(np.asarray(cloud_types, np.int32), (P, 1))
     atm.cloud_water_content = wc
     atm.cloud_effective_radius = reff
-    atm.cloud_fraction = np.zeros((P, K))
+    cloudy = (wc > 0).any(axis=1)
+    if cover is None:
+        atm.cloud_fraction = np.where(cloudy, 1.0, 0.0)
+    else:
+        rc = np.random.Generator(np.random.PCG64(seed + 1000003))
+        atm.cloud_fraction = np.where(cloudy, rc.uniform(cover[0], cover[1], (P, K)), 0.0)
     return atm
 
 

@@ -84,8 +84,8 @@ typedef struct {
   const double* emissivity;       /* [P][n_channels] */
   /* clouds (CRTM_Cloud_type, Atmosphere%Cloud(:)).  max_clouds = 0: clear-sky
    * batch, the cloud pointers are not read.  A profile with n_clouds > 0 is
-   * solved with the scattering solver (ADA) as one cloudy column (the
-   * reference's coverage flag CLEAR: Cloud_Fraction not used). */
+   * solved with the scattering solver (ADA or SOI); its cloud coverage
+   * follows cloud_fraction below. */
   int max_clouds;                 /* NC: stride of the cloud arrays */
   const int* n_clouds;            /* [P] clouds of each profile, <= NC */
   const int* cloud_type;          /* [P][NC] WATER=1 ICE=2 RAIN=3 SNOW=4 GRAUPEL=5 HAIL=6 */
@@ -105,6 +105,18 @@ typedef struct {
   const int* aerosol_type;        /* [P][NA] AerosolCoeff Type ids */
   const double* aerosol_concentration;    /* [P][NA][max_layers] kg/m^2 */
   const double* aerosol_effective_radius; /* [P][NA][max_layers] microns */
+  /* Atmosphere%Cloud_Fraction (CRTM_Atmosphere_Define.f90).  Where it is
+   * below 1e-12 the layer's clouds are dropped (CRTM_Forward_Module.f90:367-376);
+   * a profile with a cloudy layer whose fraction is above 1e-6 is FRACTIONAL
+   * (CRTM_Atmosphere.f90:158-203): its radiance is (1 - tcc) x the clear
+   * column (gas only, Emission) + tcc x the cloudy column with the water
+   * content divided by tcc, tcc the total cloud cover of the overlap scheme
+   * (CRTM_CloudCover_Define.f90:447-642).  NULL: 1 in every layer (one cloudy
+   * column: tcc = 1 for every overlap scheme). */
+  const double* cloud_fraction;   /* [P][max_layers] */
+  /* Options%Overlap_Id: 1 maximum, 2 random, 3 maximum-random, 4 average,
+   * 5 overcast; NULL: 4 (the reference's default). */
+  const int* overlap_id;          /* [P] */
 } crtm_gpu_batch;
 
 typedef struct {

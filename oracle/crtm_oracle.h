@@ -103,6 +103,8 @@ typedef struct {
   const int* aerosol_type;         /* [P][NA] AerosolCoeff Type ids */
   const double* aerosol_concentration;     /* [P][NA][max_layers] kg/m^2 */
   const double* aerosol_effective_radius;  /* [P][NA][max_layers] microns */
+  const double* cloud_fraction;    /* [P][max_layers] Cloud_Fraction; NULL: 1 in every layer */
+  const int* overlap;              /* [P] Options%Overlap_Id 1-5; NULL: 4 (average) */
 } or_clouds;
 
 typedef struct or_aerosol_s or_aerosol;

@@ -37,7 +37,8 @@ class OrClouds(ct.Structure):
     _fields_ = [("max_clouds", ct.c_int), ("n_clouds", _ip), ("cloud_type", _ip),
                 ("water_content", _dp), ("effective_radius", _dp), ("n_streams", _ip),
                 ("rt_algorithm", _ip), ("max_aerosols", ct.c_int), ("n_aerosols", _ip),
-                ("aerosol_type", _ip), ("aerosol_concentration", _dp), ("aerosol_effective_radius", _dp)]
+                ("aerosol_type", _ip), ("aerosol_concentration", _dp), ("aerosol_effective_radius", _dp),
+                ("cloud_fraction", _dp), ("overlap", _ip)]
 
 
 def build(force: bool = False) -> str:
@@ -207,6 +208,10 @@ class Oracle:
                 c.n_streams = _p(arr(np.where(use, opt.n_streams, 0), np.int32), _ip)
             if opt.rt_algorithm_id is not None:
                 c.rt_algorithm = _p(arr(opt.rt_algorithm_id, np.int32), _ip)
+            if c.max_clouds > 0 and atm.cloud_fraction is not None:
+                c.cloud_fraction = _p(arr(atm.cloud_fraction))
+            if getattr(opt, "overlap_id", None) is not None:
+                c.overlap = _p(arr(opt.overlap_id, np.int32), _ip)
             rad, bt = np.zeros((P, nL)), np.zeros((P, nL))
             st = L.or_forward_scatter(self.h, ch, ah, ct.byref(b), ct.byref(c), _p(rad), _p(bt), n_threads)
             if st:

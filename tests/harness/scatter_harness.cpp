@@ -123,6 +123,9 @@ int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, 
 }
 
 int sx_stream_rule(double max_reff, double wavenumber) { return stream_rule_nleg(max_reff, wavenumber); }
+double sx_total_cloud_cover(int Ku, int n_clouds, const double* cf, const double* wc, int cstride, int overlap) {
+  return total_cloud_cover(Ku, n_clouds, cf, wc, (size_t)cstride, overlap);
+}
 }
 
 

@@ -105,3 +105,46 @@ def test_aerosols_match_oracle(gpu_lib, cloud_dir, precision, clouds, soi):
                                                        f"{cloud_dir}/CloudCoeff.bin" if clouds else None, apath)
     rts = gpu_lib.CRTM([sensor], cloud_dir, precision).forward(atm, sfc, geo, opt)
     assert np.abs(rts.brightness_temperature - ref).max() <= BT_TOL[precision]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("overlap", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("sensor", ["mwsynth_c16", "irsynth_c616"])
+def test_fractional_cloud_cover_matches_oracle(gpu_lib, cloud_dir, precision, overlap, sensor):
+    """Cloud_Fraction in (0.05, 0.95) in cloudy layers: the clear and the
+    scaled cloudy column mixed by the overlap scheme's total cover; ADA and
+    SOI profiles, one profile with fraction 1, one whose clouds are dropped
+    (fraction below 1e-12), one clear."""
+    from oracle.pyoracle import Oracle
+    nl = 100 if sensor.startswith("mw") else 101
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 8, nl, 71, cloud_types=(co.WATER_CLOUD, co.ICE_CLOUD, co.RAIN_CLOUD),
+                                            wc_scale=60.0)
+    sy.add_clouds(atm, (co.WATER_CLOUD, co.ICE_CLOUD, co.RAIN_CLOUD), 72, wc_scale=60.0, cover=(0.05, 0.95))
+    atm.cloud_fraction[1] = np.where(atm.cloud_fraction[1] > 0, 1.0, 0.0)
+    atm.cloud_fraction[2] *= 1e-13
+    atm.n_clouds[3] = 0
+    opt.overlap_id = np.full(8, overlap, np.int32)
+    opt.rt_algorithm_id = np.array([56, 56, 56, 56, 168, 168, 56, 168], np.int32)
+    _, ref = Oracle(cloud_dir, sensor).forward_scatter(atm, sfc, geo, opt, f"{cloud_dir}/CloudCoeff.bin")
+    rts = gpu_lib.CRTM([sensor], cloud_dir, precision).forward(atm, sfc, geo, opt)
+    assert np.abs(rts.brightness_temperature - ref).max() <= BT_TOL[precision]
+
+
+def test_null_cloud_fraction_is_one_cloudy_column(gpu_lib, cloud_dir):
+    atm, sfc, geo, opt = sy.cloudy_workload("mwsynth_c16", 4, 100, 73, wc_scale=100.0)
+    h = gpu_lib.CRTM(["mwsynth_c16"], cloud_dir, 0)
+    bt1 = h.forward(atm, sfc, geo, opt).brightness_temperature
+    atm.cloud_fraction = None
+    bt0 = h.forward(atm, sfc, geo, opt).brightness_temperature
+    assert np.abs(bt1 - bt0).max() == 0.0
+
+
+def test_invalid_overlap_id_fails(gpu_lib, cloud_dir):
+    atm, sfc, geo, opt = sy.cloudy_workload("mwsynth_c16", 3, 100, 74, wc_scale=100.0)
+    sy.add_clouds(atm, (co.WATER_CLOUD,), 75, wc_scale=100.0, cover=(0.2, 0.8))
+    opt.overlap_id = np.array([4, 0, 4], np.int32)
+    h = gpu_lib.CRTM(["mwsynth_c16"], cloud_dir, 0)
+    with pytest.raises(RuntimeError, match="Overlap_Id"):
+        h.forward(atm, sfc, geo, opt)
+    opt.overlap_id = None
+    assert (h.forward(atm, sfc, geo, opt).status == 0).all()

@@ -90,13 +90,19 @@ def _layers(atm, extra=(3, 30, 60, 90)):
     return sorted(ks)
 
 
-@pytest.mark.parametrize("sensor,nl,n_streams,wc_scale", [
-    ("mwsynth_c16", 100, None, 100.0),     # stream rule
-    ("mwsynth_c16", 100, 16, 100.0),       # Options%n_Streams = 16
-    ("irsynth_c616", 101, None, 30.0)])
-def test_cloudy_k_matrix_matches_oracle_differences(gpu_lib, cloud_dir, sensor, nl, n_streams, wc_scale):
+@pytest.mark.parametrize("sensor,nl,n_streams,wc_scale,cover", [
+    ("mwsynth_c16", 100, None, 100.0, None),     # stream rule
+    ("mwsynth_c16", 100, 16, 100.0, None),       # Options%n_Streams = 16
+    ("irsynth_c616", 101, None, 30.0, None),
+    ("mwsynth_c16", 100, None, 100.0, (0.1, 0.9)),    # fractional cover, average overlap
+    ("irsynth_c616", 101, 8, 30.0, (0.1, 0.9))])
+def test_cloudy_k_matrix_matches_oracle_differences(gpu_lib, cloud_dir, sensor, nl, n_streams, wc_scale, cover):
     from oracle.pyoracle import Oracle
     atm, sfc, geo, opt = sy.cloudy_workload(sensor, 4, nl, 81, wc_scale=wc_scale, n_streams=n_streams)
+    if cover is not None:
+        sy.add_clouds(atm, (co.WATER_CLOUD, co.ICE_CLOUD, co.RAIN_CLOUD, co.SNOW_CLOUD), 80, wc_scale=wc_scale,
+                      cover=cover)
+        opt.overlap_id = np.array([4, 3, 4, 1], np.int32)
     atm.n_clouds[2] = 0   # one clear profile in the batch
     h = gpu_lib.CRTM([sensor], cloud_dir, 0)
     km, rts = h.k_matrix(atm, sfc, geo, opt)
@@ -151,6 +157,8 @@ def test_cloudy_adjoint_is_seeded_k_matrix_sum(gpu_lib, cloud_dir, precision):
     CRTM_K_Matrix with the same seed)."""
     sensor = "irsynth_c616"
     atm, sfc, geo, opt = sy.cloudy_workload(sensor, 9, 101, 87, wc_scale=30.0)
+    sy.add_clouds(atm, (co.WATER_CLOUD, co.ICE_CLOUD), 86, wc_scale=30.0, cover=(0.1, 1.0))
+    opt.overlap_id = np.array([1, 2, 3, 4, 5, 4, 4, 3, 2], np.int32)
     sy.add_aerosols(atm, sy.AEROSOL_TYPES, 88, load_scale=20.0)
     atm.n_clouds[4] = 0
     atm.n_aerosols[7] = 0

@@ -171,3 +171,84 @@ def test_soi_agrees_with_ada(coeff_dir, cloud_path, sensor, nl):
     opt.rt_algorithm_id = np.full(4, 168, np.int32)
     _, bs = o.forward_scatter(atm, sfc, geo, opt, cloud_path)
     assert np.abs(bs - ba).max() < 0.02
+
+
+# ---------------------------------------------------------------------------
+# Cloud coverage (CRTM_Atmosphere_Coverage, Compute_CloudCover)
+# ---------------------------------------------------------------------------
+
+def _tcc(cf, lwc, overlap):
+    """Total cloud cover of one profile (CRTM_CloudCover_Define.f90:522-638),
+    restated for the test: cf and the summed cloud water per layer."""
+    cf = np.where(cf < 1e-12, 0.0, cf)
+    if overlap == 1:
+        return cf.max()
+    if overlap == 2:
+        return 1.0 - np.prod(np.where(cf > 1e-12, 1.0 - cf, 1.0))
+    if overlap == 3:
+        prod = 1.0 - cf[0]
+        for k in range(1, cf.size):
+            mc = 1.0 - max(cf[k - 1], cf[k])
+            prod = mc if (prod == 0.0 and cf[k - 1] == 1.0) else prod * mc / (1.0 - cf[k - 1])
+        return 1.0 - prod
+    if overlap == 4:
+        w = np.where(lwc > 1e-6, lwc, 0.0)
+        return (cf * w).sum() / w.sum()
+    return 1.0
+
+
+@pytest.mark.parametrize("overlap", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("sensor,nl", [("mwsynth_c16", 100), ("irsynth_c616", 101)])
+def test_fractional_cover_mixes_clear_and_scaled_cloudy_columns(coeff_dir, cloud_path, sensor, nl, overlap):
+    """FRACTIONAL profile = (1 - tcc) x the clear column (gas only) + tcc x the
+    cloudy column with water content / tcc (CRTM_Forward_Module.f90:1086-1093,
+    CRTM_CloudCover_Define.f90:512-519), tcc from the overlap scheme."""
+    import copy
+    from oracle.pyoracle import Oracle
+    P = 4
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, P, nl, 301, cloud_types=(co.WATER_CLOUD, co.ICE_CLOUD),
+                                            wc_scale=50.0)
+    sy.add_clouds(atm, (co.WATER_CLOUD, co.ICE_CLOUD), 302, wc_scale=50.0, cover=(0.05, 0.95))
+    opt.overlap_id = np.full(P, overlap, np.int32)
+    orc = Oracle(coeff_dir, sensor)
+    _, bt = orc.forward_scatter(atm, sfc, geo, opt, cloud_path)
+    clear = copy.deepcopy(atm)
+    clear.n_clouds = np.zeros(P, np.int32)
+    r_clear, _ = orc.forward_scatter(clear, sfc, geo, opt, cloud_path)
+    tcc = np.array([_tcc(atm.cloud_fraction[m, :nl], atm.cloud_water_content[m, :, :nl].sum(axis=0), overlap)
+                    for m in range(P)])
+    assert ((tcc > 0.04) & (tcc <= 1.0)).all()
+    full = copy.deepcopy(atm)
+    full.cloud_water_content = atm.cloud_water_content / tcc[:, None, None]
+    full.cloud_fraction = np.where(atm.cloud_fraction > 0, 1.0, 0.0)
+    r_cloudy, _ = orc.forward_scatter(full, sfc, geo, opt, cloud_path)
+    mix = (1.0 - tcc[:, None]) * r_clear + tcc[:, None] * r_cloudy
+    sc = co.read_spccoeff(f"{coeff_dir}/{sensor}.SpcCoeff.bin")
+    te_inv = sc.planck_c2 / np.log(sc.planck_c1 / mix + 1.0)
+    bt_mix = (te_inv - sc.band_c1) / sc.band_c2
+    assert np.abs(bt - bt_mix).max() < 1e-9
+
+
+def test_cloud_fraction_thresholds(coeff_dir, cloud_path):
+    """Fraction below 1e-12 drops the cloud (CRTM_Forward_Module.f90:367-376);
+    between 1e-12 and 1e-6 the profile is one cloudy column, as with fraction 1;
+    an invalid overlap id fails."""
+    import copy
+    from oracle.pyoracle import Oracle
+    sensor = "mwsynth_c16"
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 3, 100, 303, wc_scale=100.0)
+    orc = Oracle(coeff_dir, sensor)
+    _, bt1 = orc.forward_scatter(atm, sfc, geo, opt, cloud_path)
+    small = copy.deepcopy(atm)
+    small.cloud_fraction = atm.cloud_fraction * 1e-9
+    _, bts = orc.forward_scatter(small, sfc, geo, opt, cloud_path)
+    assert np.abs(bts - bt1).max() == 0.0
+    gone = copy.deepcopy(atm)
+    gone.cloud_fraction = atm.cloud_fraction * 1e-13
+    _, btg = orc.forward_scatter(gone, sfc, geo, opt, cloud_path)
+    _, btc = orc.forward(atm, sfc, geo, opt)
+    assert np.abs(btg - btc).max() < 1e-9
+    assert np.abs(bt1 - btc).max() > 1.0
+    opt.overlap_id = np.array([4, 9, 4], np.int32)
+    with pytest.raises(RuntimeError, match="Overlap"):
+        orc.forward_scatter(atm, sfc, geo, opt, cloud_path)

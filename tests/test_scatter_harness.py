@@ -251,3 +251,27 @@ def test_cloudy_kmatrix_matches_finite_differences(sx, coeff_dir, sensor, nl, n_
         # the radiance is linear in the surface Planck radiance: a large step is exact
         fd = (fwd(od0, temp0, bs=bs * 1.1) - fwd(od0, temp0, bs=bs * 0.9)) / (0.2 * bs)
         assert abs(fd - bb.value) <= 1e-6 * abs(bb.value) + 1e-12
+
+
+@pytest.mark.parametrize("overlap", [1, 2, 3, 4, 5])
+def test_total_cloud_cover_matches_overlap_schemes(sx, overlap):
+    """total_cloud_cover (the GPU's per-profile cloud cover) against the
+    overlap formulas of CRTM_CloudCover_Define.f90:522-638 restated in the
+    oracle tests, on random fractions with tiny, zero and unit values mixed in."""
+    from test_oracle_scatter import _tcc
+    sx.sx_total_cloud_cover.restype = ct.c_double
+    rng = np.random.Generator(np.random.PCG64(400 + overlap))
+    for trial in range(200):
+        K, NC = 60, 3
+        wc = np.where(rng.uniform(size=(NC, K)) < 0.3, 10.0 ** rng.uniform(-7, -2, (NC, K)), 0.0)
+        special = rng.choice([0.0, 1e-13, 1e-9, 1.0, -0.1], size=K)
+        cf = np.where(rng.uniform(size=K) < (0.5 if trial % 2 else 0.05), special, rng.uniform(0.0, 1.0, K))
+        wcz = np.where(cf[None, :] < 1e-12, 0.0, wc)
+        lwc = np.where(wcz > 1e-6, wcz, 0.0).sum(axis=0)
+        frac = ((np.where(cf < 1e-12, 0.0, cf) > 1e-6) & (lwc > 0)).any()
+        got = sx.sx_total_cloud_cover(K, NC, _p(cf), _p(np.ascontiguousarray(wc)), K, overlap)
+        if not frac:
+            assert got == -1.0
+        else:
+            assert abs(got - _tcc(cf, lwc, overlap)) < 1e-14
+    assert sx.sx_total_cloud_cover(3, 1, _p(np.ones(3)), _p(np.full(3, 1e-3)), 3, 7) == -2.0
