@@ -189,6 +189,218 @@ def run_reference(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# Scattering workloads (optional: --workload C3 | C4 | C5)
+# ---------------------------------------------------------------------------
+
+SCATTER_METRIC = {
+    "C3": "forward+adjoint profile*channels/s (cloudy MW, ADA, mixed precision, inputs in HBM)",
+    "C4": "forward+K-matrix profile*channels/s (all-sky IR with aerosols, ADA, mixed precision, inputs in HBM)",
+    "C5": "forward+K-matrix profile*channels/s (ragged 3-sensor batch, 30% cloudy, mixed precision, "
+          "inputs in HBM)",
+}
+
+
+def scatter_groups(name: str, rank: int):
+    """Per-sensor sub-batches [(sensor, atm, sfc, geo, opt)] of a scattering workload."""
+    from crtmv3_gb300 import coefficients as co
+    if name == "C3":
+        # 5000 x 100 x 16 MW, 5 cloud types (Cloud_Fraction 1 in cloudy layers),
+        # stream rule with Options%n_Streams 8 / 16 on a tenth of the profiles each
+        atm, sfc, geo, opt = sy.cloudy_workload("mwsynth_c16", 5000, 100, 3100 + rank)
+        rng = np.random.Generator(np.random.PCG64(3200 + rank))
+        ns = rng.choice(np.array([0, 8, 16], np.int32), size=5000, p=[0.8, 0.1, 0.1])
+        opt.use_n_streams, opt.n_streams = ns > 0, ns
+        return [("mwsynth_c16", atm, sfc, geo, opt)]
+    if name == "C4":
+        # 1000 x 100 x 616 IR, liquid + ice clouds, dust + sea salt + sulfate
+        atm, sfc, geo, opt = sy.clear_sky_workload("irsynth_c616", 1000, 100, 3300 + rank)
+        sy.add_clouds(atm, (co.WATER_CLOUD, co.ICE_CLOUD), 3301 + rank)
+        sy.add_aerosols(atm, sy.AEROSOL_TYPES, 3302 + rank)
+        return [("irsynth_c616", atm, sfc, geo, opt)]
+    # C5: 20000 profiles, layers U[60,137], one of 3 sensors each, 30 % cloudy
+    # with the stream rule or Options%n_Streams 8 / 16
+    P = 20000
+    rng = np.random.Generator(np.random.PCG64(3400 + rank))
+    sensors = ("mwsynth_c22", "irsynth_c616", "irsynth_c2211")
+    which = rng.integers(0, 3, P)
+    nl = rng.integers(60, 138, P)
+    groups = []
+    for i, sid in enumerate(sensors):
+        idx = np.nonzero(which == i)[0]
+        atm, sfc, geo, opt = sy.clear_sky_workload(sid, idx.size, nl[idx], 3500 + 10 * rank + i)
+        types = ((co.WATER_CLOUD, co.ICE_CLOUD, co.RAIN_CLOUD, co.SNOW_CLOUD, co.GRAUPEL_CLOUD)
+                 if sid.startswith("mw") else (co.WATER_CLOUD, co.ICE_CLOUD))
+        sy.add_clouds(atm, types, 3600 + 10 * rank + i)
+        cloudy = rng.uniform(size=idx.size) < 0.3
+        atm.n_clouds[~cloudy] = 0
+        ns = np.where(cloudy, rng.choice(np.array([0, 8, 16], np.int32), size=idx.size, p=[0.6, 0.2, 0.2]), 0)
+        opt.use_n_streams, opt.n_streams = ns > 0, ns.astype(np.int32)
+        groups.append((sid, atm, sfc, geo, opt))
+    return groups
+
+
+def scatter_device_inputs(torch, h, atm, sfc, geo, opt, dev):
+    t = {}
+    for k in ("level_pressure", "pressure", "temperature", "absorber", "cloud_water_content",
+              "cloud_effective_radius", "cloud_fraction", "aerosol_concentration", "aerosol_effective_radius"):
+        v = getattr(atm, k)
+        if v is not None:
+            t[k] = torch.from_numpy(np.ascontiguousarray(v, np.float64)).to(dev)
+    for k in ("n_layers", "n_clouds", "cloud_type", "n_aerosols", "aerosol_type"):
+        v = getattr(atm, k)
+        if v is not None:
+            t[k] = torch.from_numpy(np.ascontiguousarray(v, np.int32)).to(dev)
+    for f in ("land_coverage", "water_coverage", "snow_coverage", "ice_coverage", "land_temperature",
+              "water_temperature", "snow_temperature", "ice_temperature"):
+        t[f] = torch.from_numpy(np.ascontiguousarray(getattr(sfc, f))).to(dev)
+    for f in ("sensor_zenith_angle", "source_zenith_angle", "surface_altitude"):
+        t[f] = torch.from_numpy(np.ascontiguousarray(getattr(geo, f))).to(dev)
+    t["emissivity"] = torch.from_numpy(np.ascontiguousarray(opt.emissivity)).to(dev)
+    if opt.n_streams is not None:
+        t["n_streams"] = torch.from_numpy(np.where(opt.use_n_streams, opt.n_streams, 0).astype(np.int32)).to(dev)
+    if opt.rt_algorithm_id is not None:
+        t["rt_algorithm_id"] = torch.from_numpy(opt.rt_algorithm_id.astype(np.int32)).to(dev)
+    b, keep = h.device_batch(t, atm.absorber_id)
+    return b, keep, t
+
+
+def run_scattering(args, torch, dev, rank, world, dist):
+    from crtmv3_gb300 import api
+    name = args.workload
+    # cloudy K-matrix intermediates take ~0.3 GB per IR profile: a larger
+    # chunk workspace keeps the scattering kernels' grids full
+    os.environ.setdefault("CRTM_GPU_WORKSPACE_MB", "32768")
+    groups = scatter_groups(name, rank)
+    if rank == 0:
+        for sid, *_ in groups:
+            sy.write_sensor_files(COEFF_DIR, sid)
+        sy.write_cloud_files(COEFF_DIR)
+        sy.write_aerosol_files(COEFF_DIR)
+    if dist:
+        dist.barrier()
+    sids = [g[0] for g in groups]
+    h = api.CRTM(sids, COEFF_DIR, api.FP64)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    sptr = stream.cuda_stream
+    f64 = dict(dtype=torch.float64, device=dev)
+    calls = []
+    for si, (sid, atm, sfc, geo, opt) in enumerate(groups):
+        b, keep, t = scatter_device_inputs(torch, h, atm, sfc, geo, opt, dev)
+        P, K, L = atm.n_profiles, atm.max_layers, h.n_channels[si]
+        ids = list(atm.absorber_id)
+        sel = [ids.index(j) for j in (1, 3) if j in ids]
+        outs = {}
+        for prec in (0, 1):
+            o = dict(radiance=torch.empty((P, L), **f64), bt=torch.empty((P, L), **f64),
+                     status=torch.empty((P,), dtype=torch.int32, device=dev))
+            if name == "C3":
+                o.update(temperature_ad=torch.empty((P, K), **f64),
+                         absorber_ad=torch.empty((P, atm.n_absorbers, K), **f64),
+                         water_temperature_ad=torch.empty((P,), **f64))
+            else:
+                o.update(temperature_k=torch.empty((P, L, K), **f64),
+                         absorber_k=torch.empty((P, L, len(sel), K), **f64),
+                         water_temperature_k=torch.empty((P, L), **f64),
+                         surface_emissivity_k=torch.empty((P, L), **f64))
+            outs[prec] = o
+        seed = torch.ones((P, L), **f64)
+        calls.append(dict(si=si, b=b, keep=(keep, t), sel=sel, outs=outs, seed=seed, pc=P * L))
+
+    def step(prec):
+        h.set_precision(prec)
+        for c in calls:
+            if name == "C3":
+                h.adjoint_device(c["b"], c["seed"], c["outs"][prec], c["si"], sptr)
+            else:
+                h.k_matrix_device(c["b"], c["outs"][prec], None, c["si"], sptr, k_absorbers=c["sel"])
+
+    def timed(prec, n):
+        torch.cuda.synchronize(dev)
+        if dist:
+            dist.barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            step(prec)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return max_over_ranks(e0.elapsed_time(e1), dist, dev)
+
+    for _ in range(args.warmup):
+        step(1)
+    step(0)
+    torch.cuda.synchronize(dev)
+    launches0 = h.launch_count()
+    h.set_profiling(True)
+    h.stage_times(reset=True)
+    with ClockSampler(local_rank()) as clk:
+        ms_mixed = timed(1, args.steps)
+    st = h.stage_times(reset=True)
+    h.set_profiling(False)
+    launches = h.launch_count() - launches0
+    fp64_steps = max(1, min(args.steps, 2))
+    ms_fp64 = timed(0, fp64_steps)
+    pc = sum(c["pc"] for c in calls) * world
+    per_mixed, per_fp64 = ms_mixed / args.steps, ms_fp64 / fp64_steps
+    value, fp64_value = pc / (per_mixed * 1e-3), pc / (per_fp64 * 1e-3)
+    bt_err, jac_err = 0.0, 0.0
+    for c in calls:
+        a, r = c["outs"][1], c["outs"][0]
+        bt_err = max(bt_err, float((a["bt"] - r["bt"]).abs().max()))
+        for f in (("temperature_ad", "absorber_ad", "water_temperature_ad") if name == "C3" else
+                  ("temperature_k", "absorber_k", "water_temperature_k", "surface_emissivity_k")):
+            jac_err = max(jac_err, float((a[f] - r[f]).abs().max() / r[f].abs().max().clamp_min(1e-300)))
+    extra = {}
+    if name == "C4":   # SOI forward on the same inputs (K-matrix with RT_SOI is not built)
+        sid, atm, sfc, geo, opt = groups[0]
+        opt.rt_algorithm_id = np.full(atm.n_profiles, 168, np.int32)
+        b, keep, t = scatter_device_inputs(torch, h, atm, sfc, geo, opt, dev)
+        fo = calls[0]["outs"][1]
+        h.set_precision(1)
+        h.forward_device(b, fo, 0, sptr)
+        opt.rt_algorithm_id = np.full(atm.n_profiles, 56, np.int32)
+        b2, keep2, t2 = scatter_device_inputs(torch, h, atm, sfc, geo, opt, dev)
+        fo2 = {k: torch.empty_like(v) for k, v in fo.items() if k in ("radiance", "bt", "status")}
+        for lab, bb, oo in (("soi", b, fo), ("ada", b2, fo2)):
+            h.forward_device(bb, oo, 0, sptr)
+            torch.cuda.synchronize(dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                h.forward_device(bb, oo, 0, sptr)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            ms = e0.elapsed_time(e1) / args.steps
+            extra[f"{lab}_forward_mixed"] = {"ms_per_step": ms, "value": calls[0]["pc"] / (ms * 1e-3)}
+        extra["soi_vs_ada_max_abs_bt_K"] = float((fo["bt"] - fo2["bt"]).abs().max())
+    if rank == 0:
+        cfg = {"workload": name, "groups": [{"sensor": c_[0], "profiles": int(c_[1].n_profiles),
+                                              "layers_max": int(c_[1].max_layers),
+                                              "cloudy_profiles": int((c_[1].n_clouds > 0).sum())}
+                                             for c_ in groups],
+               "parallelism": f"replicas x{world}",
+               "l2": "inputs and per-step intermediates far larger than L2, no flush"}
+        line = {"metric": SCATTER_METRIC[name], "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_mixed,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "mixed f32/f64",
+                "data": "synthetic", "config": cfg,
+                "fp64_gpu": {"value": fp64_value, "ms_per_step": per_fp64, "steps": fp64_steps},
+                "speedup_mixed_vs_fp64": value / fp64_value,
+                "accuracy_mixed_vs_fp64": {"max_abs_bt_K": bt_err, "max_rel_jacobian": jac_err},
+                "stages_ms_per_step": {k: v[0] / args.steps for k, v in st.items() if v[1] > 0},
+                "stage_launches_per_step": {k: v[1] // args.steps for k, v in st.items() if v[1] > 0},
+                "gpu_launches": int(launches), "roofline": None, "cpu_baseline": None, "e2e": None,
+                "clocks": clk.summary(), **extra}
+        print(json.dumps(line))
+    return 0
+
+
+def local_rank() -> int:
+    return int(os.environ.get("LOCAL_RANK", "0"))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -199,6 +411,8 @@ def main():
     ap.add_argument("--cpu-profiles", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="C2", choices=["C2", "C3", "C4", "C5"],
+                    help="C2 (default): the headline clear-sky IR K-matrix; C3-C5: scattering workloads")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -215,6 +429,11 @@ def main():
     dev = torch.device("cuda", local)
     from crtmv3_gb300 import api, build
     build.build()
+    if args.workload != "C2":
+        rc = run_scattering(args, torch, dev, rank, world, dist)
+        if dist:
+            dist.destroy_process_group()
+        return rc
     if rank == 0:
         sy.write_sensor_files(COEFF_DIR, SENSOR)
     if dist:
