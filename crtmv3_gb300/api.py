@@ -63,15 +63,35 @@ class CRTSolution(ct.Structure):
                 ("status", ct.c_void_p)]
 
 
+SCATTER_JACOBIANS = ("cloud_water_content", "cloud_effective_radius", "cloud_fraction",
+                     "aerosol_concentration", "aerosol_effective_radius")
+
+
 class CKMatrix(ct.Structure):
     _fields_ = [("temperature", ct.c_void_p), ("absorber", ct.c_void_p),
                 ("water_temperature", ct.c_void_p), ("surface_emissivity", ct.c_void_p),
-                ("n_k_absorbers", ct.c_int), ("k_absorber_index", ct.c_void_p)]
+                ("n_k_absorbers", ct.c_int), ("k_absorber_index", ct.c_void_p)] + \
+               [(f, ct.c_void_p) for f in SCATTER_JACOBIANS]
 
 
 class CAdjoint(ct.Structure):
     _fields_ = [("temperature", ct.c_void_p), ("absorber", ct.c_void_p),
-                ("water_temperature", ct.c_void_p)]
+                ("water_temperature", ct.c_void_p)] + [(f, ct.c_void_p) for f in SCATTER_JACOBIANS]
+
+
+def _scatter_shapes(atm) -> dict:
+    """Per-profile shapes (after the profile axis) of the scattering Jacobians
+    that a batch has: clouds (NC, Kmax) and the cloud fraction (Kmax,), aerosols
+    (NA, Kmax)."""
+    K = atm.max_layers
+    out = {}
+    if atm.cloud_type is not None and atm.cloud_type.shape[1] > 0:
+        NC = atm.cloud_type.shape[1]
+        out.update(cloud_water_content=(NC, K), cloud_effective_radius=(NC, K), cloud_fraction=(K,))
+    if atm.aerosol_type is not None and atm.aerosol_type.shape[1] > 0:
+        NA = atm.aerosol_type.shape[1]
+        out.update(aerosol_concentration=(NA, K), aerosol_effective_radius=(NA, K))
+    return out
 
 
 _lib = None
@@ -240,10 +260,14 @@ class CRTM:
         self._check(library().crtm_gpu_forward(self.h, sensor, ct.byref(b), ct.byref(cr)))
         return rts
 
-    def k_matrix(self, atm, sfc, geo, opt, bt_k=None, sensor: int = 0, k_absorbers=None, out=None):
+    def k_matrix(self, atm, sfc, geo, opt, bt_k=None, sensor: int = 0, k_absorbers=None, out=None,
+                 scattering_jacobians: bool = True):
         """K-matrix with host buffers.  ``k_absorbers``: optional list of user absorber
         indices whose Jacobians are returned (default: all).  ``out``: optional
-        preallocated KMatrixBatch (e.g. in pinned memory)."""
+        preallocated KMatrixBatch (e.g. in pinned memory).  ``scattering_jacobians``:
+        also return the cloud water content / effective radius / fraction and
+        aerosol concentration / effective radius Jacobians of a batch with clouds
+        or aerosols."""
         P, L, K, J = atm.n_profiles, self.n_channels[sensor], atm.max_layers, atm.n_absorbers
         keep: list = []
         b = self._cbatch(atm, sfc, geo, opt, keep)
@@ -253,11 +277,15 @@ class CRTM:
         rts = RTSolutionBatch(np.zeros((P, L)), np.zeros((P, L)), status=np.zeros(P, np.int32))
         km = out if out is not None else KMatrixBatch(np.zeros((P, L, K)), np.zeros((P, L, JK, K)),
                                                       np.zeros((P, L)), np.zeros((P, L)))
+        if out is None and scattering_jacobians:
+            for f, shp in _scatter_shapes(atm).items():
+                setattr(km, f, np.zeros((P, L) + shp))
         cr = CRTSolution(rts.radiance.ctypes.data, rts.brightness_temperature.ctypes.data,
                          rts.status.ctypes.data)
         ck = CKMatrix(km.temperature.ctypes.data, km.absorber.ctypes.data,
                       km.water_temperature.ctypes.data, km.surface_emissivity.ctypes.data,
-                      0 if sel is None else JK, None if sel is None else sel.ctypes.data)
+                      0 if sel is None else JK, None if sel is None else sel.ctypes.data,
+                      *[_addr(getattr(km, f, None)) for f in SCATTER_JACOBIANS])
         self._check(library().crtm_gpu_k_matrix(self.h, sensor, ct.byref(b), _addr(seed),
                                                 ct.byref(ck), ct.byref(cr)))
         return km, rts
@@ -269,10 +297,12 @@ class CRTM:
         seed = np.ascontiguousarray(bt_ad, np.float64)
         rts = RTSolutionBatch(np.zeros((P, L)), np.zeros((P, L)), status=np.zeros(P, np.int32))
         out = dict(temperature=np.zeros((P, K)), absorber=np.zeros((P, J, K)), water_temperature=np.zeros(P))
+        for f, shp in _scatter_shapes(atm).items():
+            out[f] = np.zeros((P,) + shp)
         cr = CRTSolution(rts.radiance.ctypes.data, rts.brightness_temperature.ctypes.data,
                          rts.status.ctypes.data)
         ca = CAdjoint(out["temperature"].ctypes.data, out["absorber"].ctypes.data,
-                      out["water_temperature"].ctypes.data)
+                      out["water_temperature"].ctypes.data, *[_addr(out.get(f)) for f in SCATTER_JACOBIANS])
         self._check(library().crtm_gpu_adjoint(self.h, sensor, ct.byref(b), seed.ctypes.data,
                                                ct.byref(ca), ct.byref(cr)))
         return out, rts
@@ -316,7 +346,8 @@ class CRTM:
         sel = None if k_absorbers is None else np.ascontiguousarray(k_absorbers, np.int32)
         ck = CKMatrix(out["temperature_k"].data_ptr(), out["absorber_k"].data_ptr(),
                       out["water_temperature_k"].data_ptr(), out["surface_emissivity_k"].data_ptr(),
-                      0 if sel is None else int(sel.shape[0]), None if sel is None else sel.ctypes.data)
+                      0 if sel is None else int(sel.shape[0]), None if sel is None else sel.ctypes.data,
+                      *[_addr(out.get(f + "_k")) for f in SCATTER_JACOBIANS])
         fn = (library().crtm_gpu_k_matrix_device_static if static_scratch
               else library().crtm_gpu_k_matrix_device)
         self._check(fn(self.h, sensor, ct.byref(b), _addr(seed), ct.byref(ck), ct.byref(cr), stream))
@@ -328,7 +359,7 @@ class CRTM:
     def adjoint_device(self, b: CBatch, seed, out: dict, sensor: int = 0, stream=None) -> None:
         cr = CRTSolution(out["radiance"].data_ptr(), out["bt"].data_ptr(), _addr(out.get("status")))
         ca = CAdjoint(out["temperature_ad"].data_ptr(), out["absorber_ad"].data_ptr(),
-                      out["water_temperature_ad"].data_ptr())
+                      out["water_temperature_ad"].data_ptr(), *[_addr(out.get(f + "_ad")) for f in SCATTER_JACOBIANS])
         self._check(library().crtm_gpu_adjoint_device(self.h, sensor, ct.byref(b), seed.data_ptr(),
                                                       ct.byref(ca), ct.byref(cr), stream))
 

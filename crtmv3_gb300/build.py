@@ -8,11 +8,14 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libcrtm_gb300.so")
-SOURCES = ["crtm_gpu.cu"]
+# Translation units, compiled in parallel: the host runtime with the ODPS and
+# forward scattering kernels, and one unit per (angle capacity, precision) of
+# the scattering K-matrix kernels.
+SOURCES = ["crtm_gpu.cu", "scatter_k_f5.cu", "scatter_k_d5.cu", "scatter_k_f10.cu", "scatter_k_d10.cu"]
 HEADERS = ["odps_physics.cuh", "odps_prep.cuh", "odps_kernels.cuh", "scatter_physics.cuh",
-           "scatter_kernels.cuh", "dual.cuh"]
-NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
-              "--expt-relaxed-constexpr", "-lineinfo", "-Xcompiler", "-fPIC", "-shared"]
+           "scatter_kernels.cuh", "scatter_launch.h", "dual.cuh"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "--expt-relaxed-constexpr", "-lineinfo", "-Xcompiler", "-fPIC"]
 
 
 def nvcc() -> str:
@@ -34,15 +37,26 @@ def _stale() -> bool:
 def build(force: bool = False, verbose: bool = False) -> str:
     if not force and not _stale():
         return LIB
-    cmd = [nvcc()] + NVCC_FLAGS + ["-o", LIB + ".tmp"] + [os.path.join(CSRC, s) for s in SOURCES]
-    if verbose:
-        print(" ".join(cmd), file=sys.stderr)
+    objdir = os.path.join(HERE, "_build")
+    os.makedirs(objdir, exist_ok=True)
+    procs = []
+    for src in SOURCES:
+        obj = os.path.join(objdir, os.path.splitext(src)[0] + ".o")
+        cmd = [nvcc()] + NVCC_FLAGS + ["-c", "-o", obj, os.path.join(CSRC, src)]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        procs.append((obj, subprocess.Popen(cmd, cwd=CSRC, stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                                            text=True)))
+    errors = []
+    for obj, pr in procs:
+        out, _ = pr.communicate()
+        if pr.returncode != 0:
+            errors.append(out)
+    if errors:
+        raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + [o for o, _ in procs]
     res = subprocess.run(cmd, cwd=CSRC, capture_output=True, text=True)
     if res.returncode != 0:
-        raise RuntimeError("nvcc failed:\n" + res.stdout + res.stderr)
+        raise RuntimeError("link failed:\n" + res.stdout + res.stderr)
     os.replace(LIB + ".tmp", LIB)
     return LIB
-
-
-if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose=True))

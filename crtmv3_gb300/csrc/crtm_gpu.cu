@@ -23,6 +23,7 @@
 #include "../../include/crtm_gpu.h"
 #include "odps_kernels.cuh"
 #include "scatter_kernels.cuh"
+#include "scatter_launch.h"
 
 using namespace crtm;
 
@@ -524,7 +525,11 @@ struct Work {
   double* cover;    // scattering: [n] total cloud cover
   double* AS;       // scattering K-matrix/adjoint: [n][Kmax+1][NZ*NZ+NZ][L] adding states
   R* TODc;          // scattering K-matrix/adjoint: [n][Kmax][L] cloudy dR/dtau
-  double* CB;       // scattering K-matrix/adjoint: [n][3][L] cloudy radiance and surface terms
+  double* CB;       // scattering K-matrix/adjoint: [n][4][L] cloudy radiance, surface terms, clear radiance
+  double* LBA;      // scattering K-matrix/adjoint: [n][Kmax][NE][L] layer record adjoints
+  double* CJ, *CR;  // species Jacobians: [n][slots][Kmax][L]
+  double* CF;       // cloud-fraction Jacobian: [n][Kmax][L]
+  double* TD;       // cloud-cover derivatives: [n][2][Kmax]
   double* ras;      // adjoint: [n][nv][K]
   double* pts;      // adjoint: [n][Kmax]
   double* tss;      // adjoint: [n]
@@ -546,6 +551,8 @@ template <int G, class R> constexpr int ad_profiles() { return Tune<G, R>::AD * 
 struct ScatterWork {
   int rec = 0, nz = 0;
   bool soi = false, kstate = false;
+  int slots = 0;         // species Jacobian slots (max_clouds + max_aerosols), 0: none
+  bool cf = false;       // cloud-fraction Jacobian
 };
 
 template <int G, class R>
@@ -589,7 +596,13 @@ size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w
     wk.AS = sw.kstate ? (double*)carve(nn * (size_t)(Kmax + 1) * (sw.nz * sw.nz + sw.nz) * L * sizeof(double))
                       : nullptr;
     wk.TODc = sw.kstate ? (R*)carve(nn * Kmax * L * sizeof(R)) : nullptr;
-    wk.CB = sw.kstate ? (double*)carve(nn * 3 * L * sizeof(double)) : nullptr;
+    wk.CB = sw.kstate ? (double*)carve(nn * 4 * L * sizeof(double)) : nullptr;
+    wk.LBA = sw.kstate ? (double*)carve(nn * Kmax * (size_t)sw.rec * L * sizeof(double)) : nullptr;
+    const size_t sj = nn * (size_t)sw.slots * Kmax * L * sizeof(double);
+    wk.CJ = sw.slots ? (double*)carve(sj) : nullptr;
+    wk.CR = sw.slots ? (double*)carve(sj) : nullptr;
+    wk.CF = sw.cf ? (double*)carve(nn * Kmax * L * sizeof(double)) : nullptr;
+    wk.TD = sw.kstate && (sw.slots || sw.cf) ? (double*)carve(nn * 2 * Kmax * sizeof(double)) : nullptr;
   }
   if (adj) {
     wk.TAU = (R*)carve(nn * Kmax * L * sizeof(R));
@@ -635,9 +648,9 @@ int reserve_smem(crtm_gpu_handle h, F kernel, size_t bytes, const char* what) {
 // (host entry points only): element i covers bytes [p*per[i], (p+n)*per[i]).
 struct HostCopy {
   int n = 0;
-  void* dst[8];
-  const void* src[8];
-  size_t per[8];
+  void* dst[16];
+  const void* src[16];
+  size_t per[16];
   int max_chunk = 0;   // cap on the chunk size so that copies overlap compute
 };
 
@@ -705,13 +718,26 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
   // scattering: NZ angles of the kernels (16-stream option or the stream rule)
   const bool nz_max = scat && b->n_streams != nullptr;
   const bool soi = mode == 3 && b->rt_algorithm_id != nullptr;
+  // scattering Jacobian outputs that the caller asked for
+  double* o_wc = nullptr, *o_re = nullptr, *o_cf = nullptr, *o_ac = nullptr, *o_ar = nullptr;
+  if (mode == 1) {
+    o_wc = kk->cloud_water_content; o_re = kk->cloud_effective_radius; o_cf = kk->cloud_fraction;
+    o_ac = kk->aerosol_concentration; o_ar = kk->aerosol_effective_radius;
+  } else if (mode == 2) {
+    o_wc = ad->cloud_water_content; o_re = ad->cloud_effective_radius; o_cf = ad->cloud_fraction;
+    o_ac = ad->aerosol_concentration; o_ar = ad->aerosol_effective_radius;
+  }
+  const int NCb = b->max_clouds > 0 ? b->max_clouds : 0, NAb = b->max_aerosols > 0 ? b->max_aerosols : 0;
+  if (NCb == 0) o_wc = o_re = o_cf = nullptr;
+  if (NAb == 0) o_ac = o_ar = nullptr;
   ScatterWork sw;
   if (scat) {
     sw.nz = nz_max ? SC_NZ_MAX : 5;
     sw.soi = soi;
     sw.kstate = mode != 3;
-    sw.rec = mode == 3 ? (nz_max ? layer_record<SC_NZ_MAX>() : layer_record<5>())
-                       : (nz_max ? layer_record_k<SC_NZ_MAX>() : layer_record_k<5>());
+    sw.rec = nz_max ? layer_record<SC_NZ_MAX>() : layer_record<5>();
+    if (sw.kstate && (o_wc || o_re || o_cf || o_ac || o_ar)) sw.slots = NCb + NAb;
+    sw.cf = sw.kstate && o_cf != nullptr;
   }
   // chunk size from the workspace budget
   const size_t per = work_bytes<G, R>(s, 64, Kmax, nv, mode, nullptr, nullptr, sw) / 64 + 1;
@@ -807,7 +833,8 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       sa.overlap = sa.max_clouds > 0 ? b->overlap_id : nullptr;
       sa.radiance = rts->radiance; sa.bt = rts->brightness_temperature;
       sa.status = rts->status; sa.error = h->d_error;
-      sa.TODc = w.TODc; sa.PT = w.PT; sa.CB = w.CB; sa.AS = w.AS;
+      sa.TODc = w.TODc; sa.PT = w.PT; sa.CB = w.CB; sa.AS = w.AS; sa.LBA = w.LBA;
+      sa.n_slots = sw.slots; sa.CJ = w.CJ; sa.CR = w.CR; sa.CF = w.CF; sa.TD = w.TD; sa.SC = w.SC;
       const long long nlay = (long long)n * Kmax * L;
       const unsigned gl = (unsigned)((nlay + SCATTER_THREADS - 1) / SCATTER_THREADS);
       dim3 ga((L + SCATTER_THREADS - 1) / SCATTER_THREADS, n);
@@ -815,31 +842,56 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
         StageScope sc(h, 6, st);
         scatter_profile_kernel<R><<<(n + 3) / 4, 128, 0, st>>>(sa);
         CK_LAUNCH(h);
-        if (split) {
-          if (nz_max)
-            scatter_layers_k_kernel<SC_NZ_MAX, R><<<gl, SCATTER_THREADS, 0, st>>>(sa);
-          else
-            scatter_layers_k_kernel<5, R><<<gl, SCATTER_THREADS, 0, st>>>(sa);
-        } else if (nz_max) {
+        if (nz_max)
           scatter_layers_kernel<SC_NZ_MAX, R><<<gl, SCATTER_THREADS, 0, st>>>(sa);
-        } else {
+        else
           scatter_layers_kernel<5, R><<<gl, SCATTER_THREADS, 0, st>>>(sa);
-        }
         CK_LAUNCH(h);
       }
       if (split) {
         {
           StageScope sc(h, 7, st);
           if (nz_max)
-            scatter_kmatrix_kernel<SC_NZ_MAX, R><<<ga, SCATTER_THREADS, 0, st>>>(sa);
+            launch_scatter_kmatrix<SC_NZ_MAX, R>(sa, ga, st);
           else
-            scatter_kmatrix_kernel<5, R><<<ga, SCATTER_THREADS, 0, st>>>(sa);
+            launch_scatter_kmatrix<5, R>(sa, ga, st);
           CK_LAUNCH(h);
         }
-        ca.pass = 2;
-        StageScope sc(h, 2, st);
-        column_kernel<R><<<gc, 128, col_smem, st>>>(ca);
-        CK_LAUNCH(h);
+        {
+          StageScope sc(h, 6, st);
+          if (nz_max)
+            launch_scatter_contract<SC_NZ_MAX, R>(sa, gl, st);
+          else
+            launch_scatter_contract<5, R>(sa, gl, st);
+          CK_LAUNCH(h);
+        }
+        {
+          ca.pass = 2;
+          StageScope sc(h, 2, st);
+          column_kernel<R><<<gc, 128, col_smem, st>>>(ca);
+          CK_LAUNCH(h);
+        }
+        if (sw.slots || sw.cf) {   // species and cloud-fraction Jacobians: cover chain rule, seed, outputs
+          StageScope sc(h, 7, st);
+          scatter_species_kernel<R><<<ga, SCATTER_THREADS, 0, st>>>(sa);
+          CK_LAUNCH(h);
+          struct Out { double* o; const double* X; int S, s0, ns; };
+          const Out outs[5] = {{o_wc, w.CJ, sw.slots, 0, NCb}, {o_re, w.CR, sw.slots, 0, NCb},
+                               {o_ac, w.CJ, sw.slots, NCb, NAb}, {o_ar, w.CR, sw.slots, NCb, NAb},
+                               {o_cf, w.CF, 1, 0, 1}};
+          for (const Out& o : outs) {
+            if (!o.o || !o.X || o.ns == 0) continue;
+            if (mode == 1) {
+              dim3 gt((L + 31) / 32, (Kmax + 31) / 32, std::min(n * o.ns, 65535));
+              species_k_out_kernel<<<gt, dim3(32, 8), 0, st>>>(o.X, o.S, o.s0, o.ns, Kmax, L, p0, n, o.o);
+            } else {
+              const long long rows = (long long)n * o.ns * Kmax;
+              species_ad_out_kernel<<<(unsigned)((rows + 7) / 8), 256, 0, st>>>(o.X, o.S, o.s0, o.ns, Kmax, L,
+                                                                              p0, n, o.o);
+            }
+            CK_LAUNCH(h);
+          }
+        }
       } else {
         StageScope sc(h, 7, st);
         if (nz_max)
@@ -930,6 +982,9 @@ int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, c
   const bool fp64 = h->precision == CRTM_GPU_FP64;
   const bool scat = b->max_clouds > 0 || b->max_aerosols > 0;
   if (scat) {
+    if (b->max_clouds > SC_NC_MAX || b->max_aerosols > SC_NC_MAX)
+      return fail(h, "at most %d clouds and %d aerosols per profile", SC_NC_MAX, SC_NC_MAX);
+    if (b->max_layers > SC_KMAX) return fail(h, "at most %d layers in a batch with clouds or aerosols", SC_KMAX);
     if (b->max_clouds > 0 && !h->has_clouds) return fail(h, "batch has clouds but no CloudCoeff.bin was loaded at init");
     if (b->max_aerosols > 0 && !h->has_aerosols && s.sensor_type != 1)
       return fail(h, "batch has aerosols but no AerosolCoeff.bin was loaded at init");
@@ -1059,12 +1114,23 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
   std::vector<std::pair<void*, size_t>> outs = {{rts->radiance, PL * 8}, {rts->brightness_temperature, PL * 8},
                                                 {rts->status, rts->status ? (size_t)P * 4 : 0}};
   const int JK = (mode == 1 && kk->n_k_absorbers > 0) ? kk->n_k_absorbers : J;
+  const size_t NCo = NC, NAo = NA;
   if (mode == 1)
     outs.insert(outs.end(), {{kk->temperature, PL * Km * 8}, {kk->absorber, PL * JK * Km * 8},
-                             {kk->water_temperature, PL * 8}, {kk->surface_emissivity, PL * 8}});
+                             {kk->water_temperature, PL * 8}, {kk->surface_emissivity, PL * 8},
+                             {kk->cloud_water_content, NCo ? PL * NCo * Km * 8 : 0},
+                             {kk->cloud_effective_radius, NCo ? PL * NCo * Km * 8 : 0},
+                             {kk->cloud_fraction, NCo ? PL * Km * 8 : 0},
+                             {kk->aerosol_concentration, NAo ? PL * NAo * Km * 8 : 0},
+                             {kk->aerosol_effective_radius, NAo ? PL * NAo * Km * 8 : 0}});
   if (mode == 2)
     outs.insert(outs.end(), {{ad->temperature, (size_t)P * Km * 8}, {ad->absorber, (size_t)P * J * Km * 8},
-                             {ad->water_temperature, PD}});
+                             {ad->water_temperature, PD},
+                             {ad->cloud_water_content, NCo ? (size_t)P * NCo * Km * 8 : 0},
+                             {ad->cloud_effective_radius, NCo ? (size_t)P * NCo * Km * 8 : 0},
+                             {ad->cloud_fraction, NCo ? (size_t)P * Km * 8 : 0},
+                             {ad->aerosol_concentration, NAo ? (size_t)P * NAo * Km * 8 : 0},
+                             {ad->aerosol_effective_radius, NAo ? (size_t)P * NAo * Km * 8 : 0}});
   size_t tout = 0;
   for (auto& o : outs) tout += align_up(o.second);
   if (!h->io_out.ensure(tout)) return fail(h, "cannot allocate %zu bytes for outputs", tout);
@@ -1079,8 +1145,11 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
   crtm_gpu_adjoint_out dad{};
   if (mode == 1)
     dk = {(double*)dout[3], (double*)dout[4], (double*)dout[5], (double*)dout[6], kk->n_k_absorbers,
-          kk->k_absorber_index};
-  if (mode == 2) dad = {(double*)dout[3], (double*)dout[4], (double*)dout[5]};
+          kk->k_absorber_index, (double*)dout[7], (double*)dout[8], (double*)dout[9], (double*)dout[10],
+          (double*)dout[11]};
+  if (mode == 2)
+    dad = {(double*)dout[3], (double*)dout[4], (double*)dout[5], (double*)dout[6], (double*)dout[7],
+           (double*)dout[8], (double*)dout[9], (double*)dout[10]};
   HostCopy hc;
   hc.n = (int)outs.size();
   for (size_t i = 0; i < outs.size(); i++) {
@@ -1202,7 +1271,7 @@ int crtm_gpu_init(const char* coeff_path, int n_sensors, const char* const* sens
     }
     GaussTable gt{};
     for (int n = 1; n <= 9; n++) double_gauss_host(n, gt.mu[n], gt.w[n]);
-    if (cudaMemcpyToSymbol(c_gauss, &gt, sizeof gt) != cudaSuccess ||
+    if (cudaMemcpyToSymbol(c_gauss, &gt, sizeof gt) != cudaSuccess || scatter_k_set_gauss(gt) ||
         cudaMalloc(&h->d_error, sizeof(int)) != cudaSuccess) {
       g_init_error = "device set-up of the scattering tables failed";
       crtm_gpu_destroy(h);

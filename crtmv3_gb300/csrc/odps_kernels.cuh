@@ -610,7 +610,7 @@ struct ColumnArgs {
   int pass;                      // 0: one launch (no scattering profiles)
   const int* n_clouds, *n_aerosols;   // [P] or null
   const R* TODc;                 // [n][Kmax][L] cloudy dR/dtau (PT holds the cloudy dR/dT)
-  const double* CB;              // [n][3][L] cloudy radiance, dR/de, dR/dBs
+  const double* CB;              // [n][4][L] cloudy radiance, dR/de, dR/dBs, clear radiance
   const double* cover;           // [n] total cloud cover, -1: no clear part
 };
 
@@ -809,7 +809,7 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   double e_b = double(Tn) * (double(Bs) - double(Dn));
   double Bs_b = e * double(Tn);
   if (scat) {
-    const double* cb = a.CB + (size_t)p * 3 * L + l;
+    const double* cb = a.CB + (size_t)p * 4 * L + l;
     Rd = (1.0 - wcloud) * Rd + wcloud * cb[0];
     e_b = (1.0 - wcloud) * e_b + wcloud * cb[(size_t)L];
     Bs_b = (1.0 - wcloud) * Bs_b + wcloud * cb[2 * (size_t)L];

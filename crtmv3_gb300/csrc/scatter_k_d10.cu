@@ -1,0 +1,27 @@
+// Scattering K-matrix/adjoint kernels for NZ = 10 angles (Options%n_Streams up to 16),
+// FP64 records; one translation unit so that the library compiles in parallel.
+#include "scatter_kernels.cuh"
+#include "scatter_launch.h"
+
+namespace crtm {
+
+static_assert(SC_NZ_MAX == 10, "angle capacity of this unit");
+
+int scatter_k_d10_set_gauss(const GaussTable& g) {
+  return cudaMemcpyToSymbol(c_gauss, &g, sizeof g) == cudaSuccess ? 0 : 1;
+}
+
+template <int NZ, class R>
+void launch_scatter_kmatrix(const ScatterArgs<R>& a, dim3 grid, cudaStream_t st) {
+  scatter_kmatrix_kernel<NZ, R><<<grid, SCATTER_THREADS, 0, st>>>(a);
+}
+
+template <int NZ, class R>
+void launch_scatter_contract(const ScatterArgs<R>& a, unsigned grid, cudaStream_t st) {
+  scatter_contract_kernel<NZ, R><<<grid, SCATTER_THREADS, 0, st>>>(a);
+}
+
+template void launch_scatter_kmatrix<10, double>(const ScatterArgs<double>&, dim3, cudaStream_t);
+template void launch_scatter_contract<10, double>(const ScatterArgs<double>&, unsigned, cudaStream_t);
+
+}  // namespace crtm

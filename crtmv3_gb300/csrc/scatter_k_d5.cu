@@ -1,0 +1,27 @@
+// Scattering K-matrix/adjoint kernels for NZ = 5 angles (the stream rule's 2-6 streams),
+// FP64 records; one translation unit so that the library compiles in parallel.
+#include "scatter_kernels.cuh"
+#include "scatter_launch.h"
+
+namespace crtm {
+
+static_assert(5 == 5, "angle capacity of this unit");
+
+int scatter_k_d5_set_gauss(const GaussTable& g) {
+  return cudaMemcpyToSymbol(c_gauss, &g, sizeof g) == cudaSuccess ? 0 : 1;
+}
+
+template <int NZ, class R>
+void launch_scatter_kmatrix(const ScatterArgs<R>& a, dim3 grid, cudaStream_t st) {
+  scatter_kmatrix_kernel<NZ, R><<<grid, SCATTER_THREADS, 0, st>>>(a);
+}
+
+template <int NZ, class R>
+void launch_scatter_contract(const ScatterArgs<R>& a, unsigned grid, cudaStream_t st) {
+  scatter_contract_kernel<NZ, R><<<grid, SCATTER_THREADS, 0, st>>>(a);
+}
+
+template void launch_scatter_kmatrix<5, double>(const ScatterArgs<double>&, dim3, cudaStream_t);
+template void launch_scatter_contract<5, double>(const ScatterArgs<double>&, unsigned, cudaStream_t);
+
+}  // namespace crtm

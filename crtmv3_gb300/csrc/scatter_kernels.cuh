@@ -15,25 +15,29 @@
 // LB[p][k][e][l], e = 0 kind (0 clear, 1 scattering, <0 error), 1 optical
 // depth, then T (NZ*NZ), R (NZ*NZ) and the source (NZ).
 //
-// K-matrix and adjoint of scattering profiles (ADA), between the two column
-// launches:
+// K-matrix and adjoint of scattering profiles (ADA).  After the first column
+// launch and scatter_layers_kernel (the forward layer records):
 //
-//   scatter_layers_k_kernel  one thread per (profile, layer, channel): the
-//                            layer optics on derivative numbers (directions:
-//                            gas optical depth, temperature); the record adds
-//                            the derivatives of T, R, the source and the
-//                            optical depth (layer_record_k).
 //   scatter_kmatrix_kernel   one thread per (profile, channel): the adding
 //                            from the surface with the level states kept in
-//                            AS, then the adding adjoint from the top down,
-//                            contracted with the layer derivatives.  Writes,
-//                            for a unit radiance seed, dR/dtau of each user
-//                            layer (TODc), the Planck part of the temperature
-//                            derivative (PT), and the radiance and surface
-//                            derivatives (CB).  The second column launch
-//                            mixes them with the clear column of a
-//                            fractional profile, applies the Planck-inversion
-//                            seed and maps dR/dtau onto the reference levels.
+//                            AS, then the adding adjoint from the top down.
+//                            Writes each layer's record adjoints (LBA, FP64:
+//                            kind, od_b, B_b, then T_b, R_b, src_b) and the
+//                            cloudy radiance, its surface derivatives and the
+//                            clear-column radiance of a fractional profile (CB).
+//   scatter_contract_kernel  one thread per (profile, layer, channel): the
+//                            layer optics on derivative numbers (gas optical
+//                            depth, temperature, and each active cloud or
+//                            aerosol's amount and radius), contracted with
+//                            the record adjoints: dR/dtau (TODc), dR/dT at
+//                            fixed gas optical depth (PT) and the species
+//                            Jacobians (CJ, CR), all for a unit radiance seed.
+//
+// The second column launch mixes TODc, PT and CB with the clear column of a
+// fractional profile, applies the Planck-inversion seed (SC) and maps dR/dtau
+// onto the reference levels; scatter_species_kernel then applies the cover
+// chain rule and SC to the species and cloud-fraction Jacobians, and
+// species_k_out_kernel / species_ad_out_kernel write them out.
 #pragma once
 
 #include "odps_kernels.cuh"
@@ -41,15 +45,12 @@
 
 namespace crtm {
 
-__constant__ GaussTable c_gauss;
+// Gauss angles and weights.  Internal linkage: every translation unit that
+// launches scattering kernels holds its own copy, uploaded at init.
+static __constant__ GaussTable c_gauss;
 
 template <int NZ>
 constexpr int layer_record() { return 2 + 2 * NZ * NZ + NZ; }
-// K-matrix layer record: kind, optical depth, the values of T, R and the
-// source (NV = 2 NZ^2 + NZ), their derivatives with respect to the gas optical
-// depth and to the temperature (NV each), then the optical depth's two.
-template <int NZ>
-constexpr int layer_record_k() { return 4 + 3 * (2 * NZ * NZ + NZ); }
 // adding state per level: Rup (NZ*NZ) and the upwelling radiance (NZ)
 template <int NZ>
 constexpr int adding_state_size() { return NZ * NZ + NZ; }
@@ -86,8 +87,15 @@ struct ScatterArgs {
   // radiance seed, combined with the clear column by the second column launch
   R* TODc;                      // [n][Kmax][L] dR/dtau of the user layers
   R* PT;                        // [n][Kmax][L] dR/dT at fixed gas optical depth
-  double* CB;                   // [n][3][L] radiance, dR/d(emissivity), dR/d(surface Planck)
+  double* CB;                   // [n][4][L] radiance, dR/de, dR/d(surface Planck), clear radiance
   double* AS;                   // [n][Kmax+1][NS][L] adding states
+  double* LBA;                  // [n][Kmax][NE][L] record adjoints
+  // species Jacobians: slots 0..max_clouds-1 clouds, then aerosols
+  int n_slots;                  // max_clouds + max_aerosols when requested, else 0
+  double* CJ, *CR;              // [n][n_slots][Kmax][L] amount and radius
+  double* CF;                   // [n][Kmax][L] cloud fraction, or null
+  double* TD;                   // [n][2][Kmax] d tcc / d cf, d tcc / d wc (fractional profiles)
+  const R* SC;                  // [n][L] dBT/dR x seed (after the second column launch)
 };
 
 constexpr int SCATTER_THREADS = 128;
@@ -119,9 +127,10 @@ __global__ void scatter_profile_kernel(ScatterArgs<R> a) {
   if (lane == 0) {
     a.maxreff[p] = mr;
     double tcc = -1.0;
+    const int ov = a.overlap ? a.overlap[gp] : 4;
+    const double* wc = nc > 0 ? a.wc + (size_t)gp * a.max_clouds * a.Kmax : nullptr;
     if (nc > 0) {
-      tcc = total_cloud_cover(Ku, nc, cf, a.wc + (size_t)gp * a.max_clouds * a.Kmax, (size_t)a.Kmax,
-                              a.overlap ? a.overlap[gp] : 4);
+      tcc = total_cloud_cover(Ku, nc, cf, wc, (size_t)a.Kmax, ov);
       if (tcc < -1.5) {
         atomicCAS(a.error, 0, 11);
         if (a.status) atomicOr(a.status + gp, 1 << 4);
@@ -129,6 +138,9 @@ __global__ void scatter_profile_kernel(ScatterArgs<R> a) {
       }
     }
     a.cover[p] = tcc;
+    if (a.TD && tcc >= 0.0)
+      cloud_cover_derivatives(Ku, nc, cf, wc, (size_t)a.Kmax, ov, tcc, a.TD + (size_t)p * 2 * a.Kmax,
+                              a.TD + (size_t)p * 2 * a.Kmax + a.Kmax);
   }
 }
 
@@ -336,74 +348,26 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_soi_kernel(ScatterArg
 }
 
 template <int NZ, class R>
-__global__ void __launch_bounds__(SCATTER_THREADS) scatter_layers_k_kernel(ScatterArgs<R> a) {
-  constexpr int NE = layer_record_k<NZ>(), NV = 2 * NZ * NZ + NZ;
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int L = a.L, Kmax = a.Kmax;
-  if (idx >= (long long)a.n_chunk * Kmax * L) return;
-  const int l = (int)(idx % L);
-  const int k = (int)((idx / L) % Kmax);
-  const int p = (int)(idx / ((long long)L * Kmax));
-  const int gp = a.p_begin + p;
-  if (a.pv.status[p] != 0 || k >= a.b.n_layers[gp]) return;
-  R* rec = a.LB + ((size_t)p * Kmax + k) * NE * L + l;
-  const CloudyColumn c = column_inputs(a, p, gp, l);
-  if (c.n_clouds == 0 && c.n_aerosols == 0) return;
-  if (c.soi) { rec[0] = R(-10); return; }   // SOI K-matrix: not available
-  StreamSet<NZ, double> S;
-  if (int rc = stream_set<NZ, double>(c.nleg, c.mu_sensor, c.n_clouds > 0 ? a.lut.nleg : -1, c_gauss, S)) {
-    rec[0] = R(-rc);
-    return;
-  }
-  using D = Dual<2>;
-  D gd(double(a.TAU[((size_t)p * Kmax + k) * L + l])), tt(c.temperature[k]);
-  gd.d[0] = 1.0;
-  tt.d[1] = 1.0;
-  Mat<NZ, D> Tm, Rm;
-  D src[NZ], od;
-  const int kind = layer_optics<NZ, D, D>(c, a.lut, S, k, gd, tt, &od, Tm, Rm, src);
-  rec[0] = R(kind);
-  rec[(size_t)L] = R(od.v);
-  rec[(size_t)(2 + 3 * NV) * L] = R(od.d[0]);
-  rec[(size_t)(3 + 3 * NV) * L] = R(od.d[1]);
-  if (kind != 1) return;
-  const int nZ = S.nZ;
-  for (int i = 0; i < nZ; i++) {
-    for (int j = 0; j < nZ; j++) {
-      const size_t et = (size_t)(2 + i * NZ + j), er = et + NZ * NZ;
-      rec[et * L] = R(Tm.a[i][j].v);
-      rec[(et + NV) * L] = R(Tm.a[i][j].d[0]);
-      rec[(et + 2 * NV) * L] = R(Tm.a[i][j].d[1]);
-      rec[er * L] = R(Rm.a[i][j].v);
-      rec[(er + NV) * L] = R(Rm.a[i][j].d[0]);
-      rec[(er + 2 * NV) * L] = R(Rm.a[i][j].d[1]);
-    }
-    const size_t es = (size_t)(2 + 2 * NZ * NZ + i);
-    rec[es * L] = R(src[i].v);
-    rec[(es + NV) * L] = R(src[i].d[0]);
-    rec[(es + 2 * NV) * L] = R(src[i].d[1]);
-  }
-}
-
-template <int NZ, class R>
 __global__ void __launch_bounds__(SCATTER_THREADS) scatter_kmatrix_kernel(ScatterArgs<R> a) {
-  constexpr int NE = layer_record_k<NZ>(), NV = 2 * NZ * NZ + NZ, NS = adding_state_size<NZ>();
+  constexpr int NE = layer_record<NZ>(), NS = adding_state_size<NZ>();
   const int L = a.L, Kmax = a.Kmax;
   const int p = blockIdx.y, gp = a.p_begin + p;
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (l >= L || a.pv.status[p] != 0) return;
   const CloudyColumn c = column_inputs(a, p, gp, l);
   if (c.n_clouds == 0 && c.n_aerosols == 0) return;   // clear: the column kernel's Emission adjoint
-  R* tod = a.TODc + (size_t)p * Kmax * L + l;
-  R* pt = a.PT + (size_t)p * Kmax * L + l;
+  if (c.soi) {   // the SOI K-matrix is not built
+    atomicCAS(a.error, 0, 10);
+    if (a.status) atomicOr(a.status + gp, 1 << 4);
+    return;
+  }
   double rad = 0.0, e_b = 0.0, Bs_b = 0.0;
   StreamSet<NZ, double> S;
   int code = stream_set<NZ, double>(c.nleg, c.mu_sensor, c.n_clouds > 0 ? a.lut.nleg : -1, c_gauss, S);
   if (!code) {
     const int nZ = S.nZ;
-    auto rec_of = [&](int k) { return a.LB + ((size_t)p * Kmax + k) * NE * L + l; };
     auto layer = [&](int k, int* kind, double* od, Mat<NZ, double>& Tm, Mat<NZ, double>& Rm, double* src) {
-      const R* rec = rec_of(k);
+      const R* rec = a.LB + ((size_t)p * Kmax + k) * NE * L + l;
       *kind = (int)rec[0];
       *od = double(rec[(size_t)L]);
       if (*kind != 1) return;
@@ -417,43 +381,216 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_kmatrix_kernel(Scatte
     };
     double* as = a.AS + (size_t)p * (Kmax + 1) * NS * L + l;
     auto state = [&](int lev, int i) -> double& { return as[((size_t)lev * NS + i) * L]; };
-    auto contract = [&](int k, int kind, const Mat<NZ, double>& T_b, const Mat<NZ, double>& R_b,
-                        const double* src_b, double od_b, double* g) {
-      const R* rec = rec_of(k);
+    auto adj = [&](int k, int kind, const Mat<NZ, double>& T_b, const Mat<NZ, double>& R_b, const double* src_b,
+                   double od_b, double B_b) {
+      double* rb = a.LBA + ((size_t)p * Kmax + k) * NE * L + l;
+      rb[0] = kind;
+      rb[(size_t)L] = od_b;
       if (kind != 1) {
-        g[0] = od_b * double(rec[(size_t)(2 + 3 * NV) * L]);
-        g[1] = od_b * double(rec[(size_t)(3 + 3 * NV) * L]);
-        return true;
+        rb[2 * (size_t)L] = B_b;
+        return;
       }
-      for (int d = 0; d < 2; d++) {
-        const R* r = rec + (size_t)(2 + (1 + d) * NV) * L;
-        double acc = 0.0;
-        for (int i = 0; i < nZ; i++) {
-          for (int j = 0; j < nZ; j++)
-            acc += T_b.a[i][j] * double(r[(size_t)(i * NZ + j) * L]) +
-                   R_b.a[i][j] * double(r[(size_t)(NZ * NZ + i * NZ + j) * L]);
-          acc += src_b[i] * double(r[(size_t)(2 * NZ * NZ + i) * L]);
+      for (int i = 0; i < nZ; i++) {
+        for (int j = 0; j < nZ; j++) {
+          rb[(size_t)(2 + i * NZ + j) * L] = T_b.a[i][j];
+          rb[(size_t)(2 + NZ * NZ + i * NZ + j) * L] = R_b.a[i][j];
         }
-        g[d] = acc;
+        rb[(size_t)(2 + 2 * NZ * NZ + i) * L] = src_b[i];
       }
-      return true;
     };
-    auto out = [&](int k, double g, double t) {
-      tod[(size_t)k * L] = R(g);
-      pt[(size_t)k * L] = R(t);
-    };
-    code = cloudy_kmatrix<NZ>(c, S, layer, state, contract, out, &rad, &e_b, &Bs_b);
+    code = cloudy_adjoint<NZ>(c, S, layer, state, adj, &rad, &e_b, &Bs_b);
   }
   if (code) {
     atomicCAS(a.error, 0, code);
     if (a.status) atomicOr(a.status + gp, 1 << 4);
     rad = e_b = Bs_b = 0.0;
-    for (int k = 0; k < c.Ku; k++) { tod[(size_t)k * L] = R(0); pt[(size_t)k * L] = R(0); }
+    for (int k = 0; k < c.Ku; k++) a.LBA[((size_t)p * Kmax + k) * NE * L + l] = -1.0;
   }
-  double* cb = a.CB + (size_t)p * 3 * L + l;
+  double* cb = a.CB + (size_t)p * 4 * L + l;
   cb[0] = rad;
   cb[(size_t)L] = e_b;
   cb[2 * (size_t)L] = Bs_b;
+  cb[3 * (size_t)L] = a.cover[p] >= 0.0 ? clear_column_radiance(c, a.TAU + (size_t)p * Kmax * L + l, L) : 0.0;
+}
+
+// Active species of layer k (clouds above the water-content threshold after
+// the cover scaling and not dropped, aerosols above theirs for non-microwave
+// sensors), as seed indices of layer_optics.
+CRTM_HD int active_species(const CloudyColumn& c, int k, int* sp) {
+  int n = 0;
+  if (!(c.cf && c.cf[k] < MIN_COVERAGE))
+    for (int i = 0; i < c.n_clouds; i++)
+      if (c.wc[i * c.cstride + k] / c.wc_div > WATER_CONTENT_THRESHOLD) sp[n++] = i;
+  if (!c.microwave)
+    for (int i = 0; i < c.n_aerosols; i++)
+      if (c.conc[i * c.cstride + k] > AEROSOL_CONTENT_THRESHOLD) sp[n++] = c.n_clouds + i;
+  return n;
+}
+
+template <int NZ, class R>
+__global__ void __launch_bounds__(SCATTER_THREADS) scatter_contract_kernel(ScatterArgs<R> a) {
+  constexpr int NE = layer_record<NZ>();
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int L = a.L, Kmax = a.Kmax;
+  if (idx >= (long long)a.n_chunk * Kmax * L) return;
+  const int l = (int)(idx % L);
+  const int k = (int)((idx / L) % Kmax);
+  const int p = (int)(idx / ((long long)L * Kmax));
+  const int gp = a.p_begin + p;
+  if (a.pv.status[p] != 0 || k >= a.b.n_layers[gp]) return;
+  const CloudyColumn c = column_inputs(a, p, gp, l);
+  if (c.n_clouds == 0 && c.n_aerosols == 0) return;
+  const size_t kl = ((size_t)p * Kmax + k) * L + l;
+  auto slot = [&](int s) { return s < c.n_clouds ? s : a.max_clouds + (s - c.n_clouds); };
+  if (a.n_slots > 0)
+    for (int s = 0; s < a.n_slots; s++) {
+      a.CJ[((size_t)p * a.n_slots + s) * Kmax * L + (size_t)k * L + l] = 0.0;
+      a.CR[((size_t)p * a.n_slots + s) * Kmax * L + (size_t)k * L + l] = 0.0;
+    }
+  const double* rb = a.LBA + ((size_t)p * Kmax + k) * NE * L + l;
+  const int kind = (int)rb[0];
+  if (kind < 0 || c.soi) {
+    a.TODc[kl] = R(0);
+    a.PT[kl] = R(0);
+    return;
+  }
+  StreamSet<NZ, double> S;
+  if (stream_set<NZ, double>(c.nleg, c.mu_sensor, c.n_clouds > 0 ? a.lut.nleg : -1, c_gauss, S)) return;
+  const int nZ = S.nZ;
+  Mat<NZ, double> T_b, R_b;
+  double src_b[NZ];
+  const double od_b = rb[(size_t)L], B_b = kind == 1 ? 0.0 : rb[2 * (size_t)L];
+  if (kind == 1)
+    for (int i = 0; i < nZ; i++) {
+      for (int j = 0; j < nZ; j++) {
+        T_b.a[i][j] = rb[(size_t)(2 + i * NZ + j) * L];
+        R_b.a[i][j] = rb[(size_t)(2 + NZ * NZ + i * NZ + j) * L];
+      }
+      src_b[i] = rb[(size_t)(2 + 2 * NZ * NZ + i) * L];
+    }
+  const double gas = double(a.TAU[kl]);
+  int sp[2 * SC_NC_MAX];
+  const int nsp = a.n_slots > 0 ? active_species(c, k, sp) : 0;
+  double g[4];
+  int done = 0;
+  if (nsp == 0) {
+    const LayerDirections d{true, 0, {0, 0, 0, 0}};
+    layer_contract<NZ, 2>(c, a.lut, S, k, gas, d, T_b, R_b, src_b, od_b, B_b, g);
+  } else {   // gas, temperature and the first species in one pass
+    const LayerDirections d{true, 1, {sp[0], 0, 0, 0}};
+    layer_contract<NZ, 4>(c, a.lut, S, k, gas, d, T_b, R_b, src_b, od_b, B_b, g);
+    const size_t o = ((size_t)p * a.n_slots + slot(sp[0])) * Kmax * L + (size_t)k * L + l;
+    a.CJ[o] = g[2];
+    a.CR[o] = g[3];
+    done = 1;
+  }
+  a.TODc[kl] = R(g[0]);
+  a.PT[kl] = R(g[1]);
+  while (done < nsp) {   // two more species per pass
+    const int m = nsp - done >= 2 ? 2 : 1;
+    const LayerDirections d{false, m, {sp[done], m == 2 ? sp[done + 1] : 0, 0, 0}};
+    layer_contract<NZ, 4>(c, a.lut, S, k, gas, d, T_b, R_b, src_b, od_b, B_b, g);
+    for (int i = 0; i < m; i++) {
+      const size_t o = ((size_t)p * a.n_slots + slot(sp[done + i])) * Kmax * L + (size_t)k * L + l;
+      a.CJ[o] = g[2 * i];
+      a.CR[o] = g[2 * i + 1];
+    }
+    done += m;
+  }
+}
+
+// Species and cloud-fraction Jacobians of one (profile, channel), in place:
+// a fractional profile's radiance is (1 - tcc) R_clear + tcc R_cloudy(wc / tcc),
+// so d/dwc = dRc/dwc' + dR/dtcc dtcc/dwc, d/dradius and the aerosols' = tcc dRc,
+// d/dcf = dR/dtcc dtcc/dcf with dR/dtcc = Rc - R_clear - sum(wc dRc/dwc') / tcc;
+// then x SC (dBT/dR x seed).
+template <class R>
+__global__ void scatter_species_kernel(ScatterArgs<R> a) {
+  const int L = a.L, Kmax = a.Kmax;
+  const int p = blockIdx.y, gp = a.p_begin + p;
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= L) return;
+  const int Ku = a.b.n_layers[gp];
+  const int nc = a.max_clouds > 0 ? a.n_clouds[gp] : 0, na = a.max_aerosols > 0 ? a.n_aerosols[gp] : 0;
+  const bool live = a.pv.status[p] == 0 && (nc > 0 || na > 0);
+  const double sc = live ? double(a.SC[(size_t)p * L + l]) : 0.0;
+  const double tcc = live ? a.cover[p] : -1.0;
+  const double w = tcc < 0.0 ? 1.0 : tcc;
+  const double* wc = nc > 0 ? a.wc + (size_t)gp * a.max_clouds * Kmax : nullptr;
+  const double* cf = a.cloud_fraction && nc > 0 ? a.cloud_fraction + (size_t)gp * Kmax : nullptr;
+  auto J = [&](double* X, int s, int k) -> double& {
+    return X[((size_t)p * a.n_slots + s) * Kmax * L + (size_t)k * L + l];
+  };
+  double dtcc = 0.0;   // dR/dtcc
+  if (tcc >= 0.0) {
+    const double* cb = a.CB + (size_t)p * 4 * L + l;
+    dtcc = cb[0] - cb[3 * (size_t)L];
+    if (tcc > MIN_COVERAGE) {
+      double sum = 0.0;
+      for (int c = 0; c < nc; c++)
+        for (int k = 0; k < Ku; k++) sum += wc[(size_t)c * Kmax + k] * J(a.CJ, c, k);
+      dtcc -= sum / tcc;
+    }
+  }
+  const double* dcf = tcc >= 0.0 && a.TD ? a.TD + (size_t)p * 2 * Kmax : nullptr;
+  for (int s = 0; s < a.n_slots; s++) {
+    const bool cloud = s < a.max_clouds;
+    for (int k = 0; k < Kmax; k++) {
+      double& x = J(a.CJ, s, k);
+      double& r = J(a.CR, s, k);
+      if (k >= Ku || !live) { x = r = 0.0; continue; }
+      if (cloud) {
+        double v = x;
+        const double wk = s < nc ? wc[(size_t)s * Kmax + k] : 0.0;
+        if (dcf && wk > WATER_CONTENT_THRESHOLD && !(cf && cf[k] < MIN_COVERAGE)) v += dtcc * dcf[Kmax + k];
+        x = sc * v;
+        r = sc * w * r;
+      } else {
+        x = sc * w * x;
+        r = sc * w * r;
+      }
+    }
+  }
+  if (a.CF)
+    for (int k = 0; k < Kmax; k++)
+      a.CF[((size_t)p * Kmax + k) * L + l] = (live && dcf && k < Ku) ? sc * dtcc * dcf[k] : 0.0;
+}
+
+// K-matrix outputs of the species Jacobians: X[n][S][Kmax][L] slots s0..s0+ns-1
+// to out[P][L][ns][Kmax] (a shared-memory transpose of 32 x 32 tiles).
+static __global__ void species_k_out_kernel(const double* X, int S, int s0, int ns, int Kmax, int L, int p_begin,
+                                     int n, double* out) {
+  __shared__ double tile[32][33];
+  const int k0 = blockIdx.y * 32, l0 = blockIdx.x * 32;
+  for (int ps = blockIdx.z; ps < n * ns; ps += gridDim.z) {
+    const int p = ps / ns, s = ps % ns;
+    const double* in = X + ((size_t)p * S + s0 + s) * Kmax * L;
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+      const int k = k0 + i, l = l0 + threadIdx.x;
+      tile[i][threadIdx.x] = (k < Kmax && l < L) ? in[(size_t)k * L + l] : 0.0;
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+      const int l = l0 + i, k = k0 + threadIdx.x;
+      if (l < L && k < Kmax) out[(((size_t)(p_begin + p) * L + l) * ns + s) * Kmax + k] = tile[threadIdx.x][i];
+    }
+  }
+}
+
+// Adjoint outputs: out[P][ns][Kmax] = sum over channels of slots s0..s0+ns-1
+// (one warp per row, lanes over channels).
+static __global__ void species_ad_out_kernel(const double* X, int S, int s0, int ns, int Kmax, int L, int p_begin,
+                                      int n, double* out) {
+  const long long row = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= (long long)n * ns * Kmax) return;
+  const int k = (int)(row % Kmax), s = (int)((row / Kmax) % ns), p = (int)(row / ((long long)Kmax * ns));
+  const double* in = X + (((size_t)p * S + s0 + s) * Kmax + k) * L;
+  double acc = 0.0;
+  for (int l = lane; l < L; l += 32) acc += in[l];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL, acc, o);
+  if (lane == 0) out[((size_t)(p_begin + p) * ns + s) * Kmax + k] = acc;
 }
 
 }  // namespace crtm

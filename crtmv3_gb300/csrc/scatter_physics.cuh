@@ -30,7 +30,10 @@ namespace crtm {
 
 constexpr int SC_NLEG_MAX = 16;          // MAX_N_LEGENDRE_TERMS
 constexpr int SC_NZ_MAX = 10;            // 9 streams (16-stream option) + the sensor angle
+constexpr int SC_KMAX = 1024;            // layers of a profile with clouds or aerosols
+constexpr int SC_NC_MAX = 8;             // clouds (and aerosols) of a profile
 constexpr double WATER_CONTENT_THRESHOLD = 1.0e-6;   // CRTM_Parameters.f90:256
+constexpr double AEROSOL_CONTENT_THRESHOLD = 1.0e-9; // CRTM_Parameters.f90:255
 constexpr double MIN_COVERAGE = 1.0e-12;             // CRTM_Parameters.f90:257
 constexpr double FRACTIONAL_COVERAGE = 1.0e-6;       // CRTM_Atmosphere.f90:164
 constexpr double BS_THRESHOLD = 1.0e-10;             // CRTM_Parameters.f90:260
@@ -56,8 +59,8 @@ struct GaussTable {
 };
 
 // ---- interpolation ----------------------------------------------------------
-// Weights in S: the temperature axis of the liquid-cloud tables carries
-// derivatives in the cloudy K-matrix; the other axes are plain doubles.
+// Weights in S: the radius axis and the temperature axis of the liquid-cloud
+// tables carry derivatives in the cloudy K-matrix; frequency is a plain double.
 template <class S>
 struct Lagrange4T {
   int i0;          // first of the 4 points
@@ -98,19 +101,20 @@ CRTM_HD S lerp4(const Z* z, size_t stride, const Lagrange4T<S>& L) {
   return (L.wl[0] * z0 + L.wl[1] * z1 + L.wl[2] * z2) + (L.wr[0] * z1 + L.wr[1] * z2 + L.wr[2] * z3);
 }
 
-// 2-D: dimension u fastest (stride 1), v with stride nu.
-CRTM_HD double lerp4x4(const double* z, int nu, const Lagrange4& U, const Lagrange4& V) {
+// 2-D: dimension u (frequency, plain) fastest, v with stride nu.
+template <class S>
+CRTM_HD S lerp4x4(const double* z, int nu, const Lagrange4& U, const Lagrange4T<S>& V) {
   double a[4];
   const double* b = z + (size_t)V.i0 * nu + U.i0;
   for (int j = 0; j < 4; j++) a[j] = lerp4(b + (size_t)j * nu, 1, U);
   return lerp4(a, 1, V);
 }
 
-// 3-D with the third axis (temperature) in S.
+// 3-D: frequency (plain), radius and temperature in S.
 template <class S>
-CRTM_HD S lerp4x4x4(const double* z, int nu, int nv, const Lagrange4& U, const Lagrange4& V,
+CRTM_HD S lerp4x4x4(const double* z, int nu, int nv, const Lagrange4& U, const Lagrange4T<S>& V,
                     const Lagrange4T<S>& W) {
-  double a[4];
+  S a[4];
   for (int k = 0; k < 4; k++) a[k] = lerp4x4(z + (size_t)(W.i0 + k) * nu * nv, nu, U, V);
   return lerp4(a, 1, W);
 }
@@ -121,10 +125,11 @@ CRTM_HD int legendre_offset(int nleg) {
 }
 
 // Optical properties of one cloud layer: ke (m^2/kg), w and the phase terms
-// pc[0..nleg].  Only the liquid microwave tables depend on temperature, so
-// only they carry S's derivatives.  Returns false for an unknown cloud type.
+// pc[0..nleg].  Only the liquid microwave tables depend on temperature; the
+// effective radius and the temperature carry S's derivatives.  Returns false
+// for an unknown cloud type.
 template <class S>
-CRTM_HD bool cloud_layer_optics(const CloudLut& C, bool microwave, double freq, int type, double reff,
+CRTM_HD bool cloud_layer_optics(const CloudLut& C, bool microwave, double freq, int type, S reff,
                                 S temp, int nleg, int loff, S* ke, S* w, S* pc) {
   for (int l = 0; l <= nleg; l++) pc[l] = S(0.0);
   *w = S(0.0);
@@ -132,12 +137,13 @@ CRTM_HD bool cloud_layer_optics(const CloudLut& C, bool microwave, double freq, 
     // density slot of Get_Cloud_Opt_IR: liquid 1, snow 2, graupel 3, ice/hail 4
     const int kd = (type == 1 || type == 3) ? 0 : (type == 4 ? 1 : (type == 5 ? 2 : (type == 2 || type == 6 ? 3 : -1)));
     if (kd < 0) return false;
-    const Lagrange4 F = lagrange4(C.f_ir, C.nfi, freq), R = lagrange4(C.r_ir, C.nri, reff);
+    const Lagrange4 F = lagrange4(C.f_ir, C.nfi, freq);
+    const Lagrange4T<S> R = lagrange4(C.r_ir, C.nri, reff);
     const size_t plane = (size_t)C.nfi * C.nri, vol = plane * (C.nd + 1);
-    *ke = S(lerp4x4(C.ke_ir + kd * plane, C.nfi, F, R));
-    *w = S(lerp4x4(C.w_ir + kd * plane, C.nfi, F, R));
+    *ke = lerp4x4(C.ke_ir + kd * plane, C.nfi, F, R);
+    *w = lerp4x4(C.w_ir + kd * plane, C.nfi, F, R);
     pc[0] = S(0.5);
-    for (int l = 1; l <= nleg; l++) pc[l] = S(lerp4x4(C.pc_ir + (l + loff - 1) * vol + kd * plane, C.nfi, F, R));
+    for (int l = 1; l <= nleg; l++) pc[l] = lerp4x4(C.pc_ir + (l + loff - 1) * vol + kd * plane, C.nfi, F, R);
     return true;
   }
   const Lagrange4 F = lagrange4(C.f_mw, C.nfm, freq);
@@ -150,7 +156,7 @@ CRTM_HD bool cloud_layer_optics(const CloudLut& C, bool microwave, double freq, 
       *ke = lerp4(a, 1, T);
       return true;
     }
-    const Lagrange4 R = lagrange4(C.r_mw, C.nrm, reff);
+    const Lagrange4T<S> R = lagrange4(C.r_mw, C.nrm, reff);
     const size_t vol = plane * C.nt;
     *ke = lerp4x4x4(C.ke_l, C.nfm, C.nrm, F, R, T);
     *w = lerp4x4x4(C.w_l, C.nfm, C.nrm, F, R, T);
@@ -164,12 +170,12 @@ CRTM_HD bool cloud_layer_optics(const CloudLut& C, bool microwave, double freq, 
     *ke = S(lerp4(C.ke_s + kd * plane + F.i0, 1, F));
     return true;
   }
-  const Lagrange4 R = lagrange4(C.r_mw, C.nrm, reff);
+  const Lagrange4T<S> R = lagrange4(C.r_mw, C.nrm, reff);
   const size_t vol = plane * C.nd;
-  *ke = S(lerp4x4(C.ke_s + kd * plane, C.nfm, F, R));
-  *w = S(lerp4x4(C.w_s + kd * plane, C.nfm, F, R));
+  *ke = lerp4x4(C.ke_s + kd * plane, C.nfm, F, R);
+  *w = lerp4x4(C.w_s + kd * plane, C.nfm, F, R);
   pc[0] = S(0.5);
-  for (int l = 1; l <= nleg; l++) pc[l] = S(lerp4x4(C.pc_s + (l + loff) * vol + kd * plane, C.nfm, F, R));
+  for (int l = 1; l <= nleg; l++) pc[l] = lerp4x4(C.pc_s + (l + loff) * vol + kd * plane, C.nfm, F, R);
   return true;
 }
 
@@ -184,21 +190,23 @@ struct AerosolLut {
   const double* pc;         // [nleg+1][nt][ns][nr][nrh][nw]
 };
 
-// Get_Aerosol_Opt, scheme 'CRTM' (CRTM_AerosolScatter.f90:772-855).
-CRTM_HD bool aerosol_layer_optics(const AerosolLut& A, double wavenumber, int type, double reff, int nleg,
-                                  int loff, double* ke, double* w, double* pc) {
+// Get_Aerosol_Opt, scheme 'CRTM' (CRTM_AerosolScatter.f90:772-855); the
+// effective radius carries S's derivatives.
+template <class S>
+CRTM_HD bool aerosol_layer_optics(const AerosolLut& A, double wavenumber, int type, S reff, int nleg,
+                                  int loff, S* ke, S* w, S* pc) {
   int k = -1;
   for (int t = 0; t < A.nt; t++)
     if (A.type_id[t] == type) { k = t; break; }
   if (k < 0) return false;
   const Lagrange4 F = lagrange4(A.freq, A.nw, wavenumber);
-  const Lagrange4 Rr = lagrange4(A.reff + (size_t)k * A.nr, A.nr, reff);
+  const Lagrange4T<S> Rr = lagrange4(A.reff + (size_t)k * A.nr, A.nr, reff);
   const int nu = A.nw * A.nrh;                     // radius stride
   const size_t base = (size_t)k * A.nw * A.nrh * A.nr * A.ns;
   const size_t n5 = (size_t)A.nw * A.nrh * A.nr * A.ns * A.nt;
   *ke = lerp4x4(A.ke + base, nu, F, Rr);
   *w = lerp4x4(A.w + base, nu, F, Rr);
-  pc[0] = 0.5;
+  pc[0] = S(0.5);
   for (int l = 1; l <= nleg; l++) pc[l] = lerp4x4(A.pc + n5 * (l + loff) + base, nu, F, Rr);
   return true;
 }
@@ -717,6 +725,15 @@ CRTM_HD int stream_set(int nleg, double mu_sensor, int lut_nleg, const GaussTabl
   return 0;
 }
 
+// Species seeds of a derivative evaluation: seed(s, amount, radius) may set
+// the derivative parts of species s's layer amount (cloud water content after
+// the cover scaling, or aerosol concentration) and effective radius; species
+// are the clouds 0..n_clouds-1, then the aerosols.
+struct NoSeed {
+  template <class S>
+  CRTM_HD void operator()(int, S&, S&) const {}
+};
+
 // Optics of layer k for the adding method: cloud and aerosol optics summed
 // over the species, combine and delta truncation, and for a scattering layer
 // the phase blocks and the layer's transmission, reflection and source
@@ -724,20 +741,22 @@ CRTM_HD int stream_set(int nleg, double mu_sensor, int lut_nleg, const GaussTabl
 // derivative numbers for the K-matrix), stored in T.  Returns 1 for a
 // scattering layer, 0 for a clear one (od is then the layer optical depth),
 // negative on failure.
-template <int NZ, class T, class S = double>
+template <int NZ, class T, class S = double, class Seed = NoSeed>
 CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const StreamSet<NZ, double>& St, int k,
-                         S gas_od, S tk, T* od_out, Mat<NZ, T>& Tm, Mat<NZ, T>& Rm, T* src) {
+                         S gas_od, S tk, T* od_out, Mat<NZ, T>& Tm, Mat<NZ, T>& Rm, T* src,
+                         Seed seed = Seed()) {
   const int nleg = St.nleg;
   S od = gas_od, bs_sum = S(0.0);
   S pc[SC_NLEG_MAX + 1], pcs[SC_NLEG_MAX + 1];
   for (int l = 0; l <= nleg; l++) pcs[l] = S(0.0);
   const bool dropped = in.cf && in.cf[k] < MIN_COVERAGE;
   for (int c = 0; c < in.n_clouds && !dropped; c++) {
-    const double wc = in.wc[c * in.cstride + k] / in.wc_div;
-    if (!(wc > WATER_CONTENT_THRESHOLD)) continue;
+    const double wcv = in.wc[c * in.cstride + k] / in.wc_div;
+    if (!(wcv > WATER_CONTENT_THRESHOLD)) continue;
+    S wc(wcv), re(in.reff[c * in.cstride + k]);
+    seed(c, wc, re);
     S ke, w;
-    if (!cloud_layer_optics<S>(lut, in.microwave, in.freq, in.cloud_type[c], in.reff[c * in.cstride + k], tk,
-                               nleg, St.loff, &ke, &w, pc))
+    if (!cloud_layer_optics<S>(lut, in.microwave, in.freq, in.cloud_type[c], re, tk, nleg, St.loff, &ke, &w, pc))
       return -4;
     if (ke <= 0.0) { ke = S(0.0); w = S(0.0); }
     if (w <= 0.0) { w = S(0.0); for (int l = 0; l <= nleg; l++) pc[l] = S(0.0); }
@@ -749,19 +768,20 @@ CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const Stre
   }
   if (in.n_aerosols > 0 && !in.microwave) {   // CRTM_Compute_AerosolScatter (:170-317)
     if (nleg == 2 || !in.alut || in.alut->nleg < nleg + St.loff) return -8;
-    double pa[SC_NLEG_MAX + 1];
+    S pa[SC_NLEG_MAX + 1];
     for (int c = 0; c < in.n_aerosols; c++) {
-      const double conc = in.conc[c * in.cstride + k];
-      if (!(conc > 1.0e-9)) continue;   // AEROSOL_CONTENT_THRESHOLD
-      double ke, w;
-      if (!aerosol_layer_optics(*in.alut, in.wavenumber, in.aerosol_type[c], in.aer_reff[c * in.cstride + k],
-                                nleg, St.loff, &ke, &w, pa))
+      const double concv = in.conc[c * in.cstride + k];
+      if (!(concv > AEROSOL_CONTENT_THRESHOLD)) continue;
+      S conc(concv), re(in.aer_reff[c * in.cstride + k]);
+      seed(in.n_clouds + c, conc, re);
+      S ke, w;
+      if (!aerosol_layer_optics<S>(*in.alut, in.wavenumber, in.aerosol_type[c], re, nleg, St.loff, &ke, &w, pa))
         return -9;
-      if (ke <= 0.0) { ke = 0.0; w = 0.0; }
-      if (w <= 0.0) { w = 0.0; for (int l = 0; l <= nleg; l++) pa[l] = 0.0; }
-      if (w >= 1.0) w = 1.0;
+      if (ke <= 0.0) { ke = S(0.0); w = S(0.0); }
+      if (w <= 0.0) { w = S(0.0); for (int l = 0; l <= nleg; l++) pa[l] = S(0.0); }
+      if (w >= 1.0) w = S(1.0);
       od += ke * conc;
-      const double bs = conc * ke * w;
+      const S bs = conc * ke * w;
       bs_sum += bs;
       for (int l = 0; l <= nleg; l++) pcs[l] += pa[l] * bs;
     }
@@ -1131,55 +1151,75 @@ CRTM_HD int cloudy_radiance(const CloudyColumn& in, const CloudLut& lut, const G
   return 0;
 }
 
-// Derivatives of one layer's optics with respect to its gas optical depth
-// (direction 0) and temperature (direction 1), contracted with the adjoints of
-// the layer's T, R and source (scattering layer) or of its optical depth
-// (clear layer): g[d] = sum(T_b dT/dd) + sum(R_b dR/dd) + sum(src_b dsrc/dd),
-// or od_b dod/dd.  The layer's optics are evaluated on derivative numbers;
-// returns the layer kind, which must match the forward pass.
-template <int NZ>
+// Directions of one derivative evaluation of a layer's optics: the gas
+// optical depth and the temperature (when gas_t; directions 0 and 1), then
+// for each listed species its amount and its effective radius (directions
+// base + 2i and base + 2i + 1, base = 2 or 0).  Species index: clouds
+// 0..n_clouds-1, then aerosols.
+struct LayerDirections {
+  bool gas_t;
+  int nsp;
+  int sp[4];
+};
+
+// Contraction of one layer's optics derivatives with the adjoints of its
+// record: for a scattering layer g[d] = sum(T_b dT/dd) + sum(R_b dR/dd) +
+// sum(src_b dsrc/dd); for a clear one g[d] = od_b dod/dd, plus B_b dB/dT in
+// the temperature direction (its Planck radiance enters the adding outside
+// the layer optics).  The optics are evaluated on derivative numbers with N
+// directions.  Returns the layer kind of that evaluation.
+template <int NZ, int N>
 CRTM_HD int layer_contract(const CloudyColumn& in, const CloudLut& lut, const StreamSet<NZ, double>& S, int k,
-                           double gas_od, const Mat<NZ, double>& T_b, const Mat<NZ, double>& R_b,
-                           const double* src_b, double od_b, double* g) {
-  using D = Dual<2>;
+                           double gas_od, const LayerDirections& dir, const Mat<NZ, double>& T_b,
+                           const Mat<NZ, double>& R_b, const double* src_b, double od_b, double B_b, double* g) {
+  using D = Dual<N>;
   D gd(gas_od), tt(in.temperature[k]);
-  gd.d[0] = 1.0;
-  tt.d[1] = 1.0;
+  const int base = dir.gas_t ? 2 : 0;
+  if (dir.gas_t) {
+    gd.d[0] = 1.0;
+    tt.d[1] = 1.0;
+  }
+  auto seed = [&](int s, D& amount, D& radius) {
+    for (int i = 0; i < dir.nsp; i++)
+      if (dir.sp[i] == s) {
+        amount.d[base + 2 * i] = 1.0;
+        radius.d[base + 2 * i + 1] = 1.0;
+      }
+  };
   Mat<NZ, D> Td, Rd;
   D srcd[NZ], odd;
-  const int kind = layer_optics<NZ, D, D>(in, lut, S, k, gd, tt, &odd, Td, Rd, srcd);
-  g[0] = g[1] = 0.0;
+  const int kind = layer_optics<NZ, D, D>(in, lut, S, k, gd, tt, &odd, Td, Rd, srcd, seed);
+  for (int d = 0; d < N; d++) g[d] = 0.0;
   if (kind == 1) {
-    for (int i = 0; i < S.nZ; i++) {
-      g[0] += src_b[i] * srcd[i].d[0];
-      g[1] += src_b[i] * srcd[i].d[1];
-      for (int j = 0; j < S.nZ; j++) {
-        g[0] += T_b.a[i][j] * Td.a[i][j].d[0] + R_b.a[i][j] * Rd.a[i][j].d[0];
-        g[1] += T_b.a[i][j] * Td.a[i][j].d[1] + R_b.a[i][j] * Rd.a[i][j].d[1];
+    for (int i = 0; i < S.nZ; i++)
+      for (int d = 0; d < N; d++) {
+        double acc = src_b[i] * srcd[i].d[d];
+        for (int j = 0; j < S.nZ; j++) acc += T_b.a[i][j] * Td.a[i][j].d[d] + R_b.a[i][j] * Rd.a[i][j].d[d];
+        g[d] += acc;
       }
-    }
   } else if (kind == 0) {
-    g[0] = od_b * odd.d[0];
-    g[1] = od_b * odd.d[1];
+    for (int d = 0; d < N; d++) g[d] = od_b * odd.d[d];
+    if (dir.gas_t) {
+      const double te = in.b1 + in.b2 * in.temperature[k];
+      const double ee = exp(in.c2 / te);
+      g[1] += B_b * in.c1 * in.c2 * ee * in.b2 / (te * te * (ee - 1.0) * (ee - 1.0));
+    }
   }
   return kind;
 }
 
-// K-matrix of one (profile, channel) through ADA, for a unit TOA radiance
-// seed: the radiance, and for every layer k the derivatives with respect to
-// the layer's gas optical depth (dgas) and its temperature (dT: Planck source
-// and the temperature axis of the liquid-cloud tables), plus those with
-// respect to the surface emissivity and the surface Planck radiance.
-// Forward adding with every level's (Rup, rad) kept in state(level, i) (nZ*nZ
-// + nZ values per level, level Ku = surface), then the adding adjoint from the
-// top down.  layer(k, kind, od, T, R, src) gives the layer records of the
-// forward pass; contract(k, kind, T_b, R_b, src_b, od_b, g) the contraction
-// of the layer's optics derivatives with the adjoints of its record (see
-// layer_contract), returning false when the layer's kind does not match.
-template <int NZ, class LayerFn, class StateFn, class ContractFn, class OutFn>
-CRTM_HD int cloudy_kmatrix(const CloudyColumn& in, const StreamSet<NZ, double>& S, LayerFn layer,
-                           StateFn state, ContractFn contract, OutFn out, double* radiance, double* e_b,
-                           double* Bs_b) {
+// Adjoint of the adding for one (profile, channel) through ADA, for a unit
+// TOA radiance seed.  Forward adding with every level's (Rup, rad) kept in
+// state(level, i) (nZ*nZ + nZ values per level, level Ku = surface), then the
+// adding adjoint from the top down.  layer(k, kind, od, T, R, src) gives the
+// layer records of the forward pass; adj(k, kind, T_b, R_b, src_b, od_b, B_b)
+// receives each layer's record adjoints (scattering layer: T_b, R_b, src_b;
+// clear layer: od_b and the Planck radiance's B_b).  Returns the radiance and
+// the derivatives with respect to the surface emissivity (reflectivity 1 - e)
+// and the surface Planck radiance.
+template <int NZ, class LayerFn, class StateFn, class AdjFn>
+CRTM_HD int cloudy_adjoint(const CloudyColumn& in, const StreamSet<NZ, double>& S, LayerFn layer,
+                           StateFn state, AdjFn adj, double* radiance, double* e_b, double* Bs_b) {
   const int nZ = S.nZ, Ku = in.Ku;
   AddingState<NZ> A;
   adding_init<NZ>(A, nZ, in.emissivity, in.planck_surface);
@@ -1221,28 +1261,100 @@ CRTM_HD int cloudy_kmatrix(const CloudyColumn& in, const StreamSet<NZ, double>& 
   for (int k = 0; k < Ku; k++) {
     load(k + 1, Rup, rad);
     int kind;
-    double od, g[2];
+    double od;
     layer(k, &kind, &od, Tm, Rm, src);
     if (kind == 1) {
       if (!adding_scatter_adjoint<NZ>(nZ, Tm, Rm, src, Rup, rad, Rup_b, rad_b, T_b, R_b, src_b)) return 6;
-      if (!contract(k, kind, T_b, R_b, src_b, 0.0, g)) return 7;
+      adj(k, kind, T_b, R_b, src_b, 0.0, 0.0);
     } else {
-      // Planck source of a clear layer and its temperature derivative
-      const double te = in.b1 + in.b2 * in.temperature[k];
-      const double ee = exp(in.c2 / te), B = in.c1 / (ee - 1.0);
-      const double dB = in.c1 * in.c2 * ee * in.b2 / (te * te * (ee - 1.0) * (ee - 1.0));
+      const double B = in.c1 / (exp(in.c2 / (in.b1 + in.b2 * in.temperature[k])) - 1.0);
       double od_b, B_b;
       adding_clear_adjoint<NZ>(nZ, S.mu, od, B, Rup, rad, Rup_b, rad_b, &od_b, &B_b);
-      if (!contract(k, kind, T_b, R_b, src_b, od_b, g)) return 7;
-      g[1] += B_b * dB;
+      adj(k, kind, T_b, R_b, src_b, od_b, B_b);
     }
-    out(k, g[0], g[1]);
   }
   double tr = 0.0, sr = 0.0;
   for (int i = 0; i < nZ; i++) { tr += Rup_b.a[i][i]; sr += rad_b[i]; }
   *e_b = -tr + in.planck_surface * sr;
   *Bs_b = in.emissivity * sr;
   return 0;
+}
+
+// Derivatives of the total cloud cover (total_cloud_cover) with respect to
+// each layer's cloud fraction (dcf) and, for the average overlap, to the
+// water content of a cloud whose content is above the threshold in that layer
+// (dwc; 0 for the other schemes): the reverse of Compute_CloudCover
+// (CRTM_CloudCover_Define.f90:522-638).  tcc >= 0 (a fractional profile).
+CRTM_HD void cloud_cover_derivatives(int Ku, int n_clouds, const double* cf, const double* wc, size_t cstride,
+                                     int overlap, double tcc, double* dcf, double* dwc) {
+  auto frac = [&](int k) {
+    const double f = cf ? cf[k] : 1.0;
+    return f < MIN_COVERAGE ? 0.0 : f;
+  };
+  for (int k = 0; k < Ku; k++) dcf[k] = dwc[k] = 0.0;
+  if (overlap == 1) {          // running maximum: the first layer that reaches it
+    int km = 0;
+    for (int k = 1; k < Ku; k++)
+      if (frac(k) > frac(km)) km = k;
+    if (cf && cf[km] >= MIN_COVERAGE) dcf[km] = 1.0;
+  } else if (overlap == 2) {   // 1 - prod(1 - cf) over the layers above the threshold
+    double pre = 1.0;
+    for (int k = 0; k < Ku; k++) {
+      dcf[k] = pre;            // product over the layers above k
+      if (frac(k) > MIN_COVERAGE) pre *= 1.0 - frac(k);
+    }
+    double suf = 1.0;
+    for (int k = Ku - 1; k >= 0; k--) {
+      const bool on = frac(k) > MIN_COVERAGE;
+      dcf[k] = on ? dcf[k] * suf : 0.0;
+      if (on) suf *= 1.0 - frac(k);
+    }
+  } else if (overlap == 3) {   // maximum-random: reverse of the product recursion
+    double prod[SC_KMAX];
+    const int n = Ku < SC_KMAX ? Ku : SC_KMAX;
+    prod[0] = 1.0 - frac(0);
+    for (int k = 1; k < n; k++) {
+      const double a = frac(k - 1), b = frac(k), mc = 1.0 - (a > b ? a : b);
+      prod[k] = (prod[k - 1] == 0.0 && 1.0 - a == 0.0) ? mc : prod[k - 1] * (mc / (1.0 - a));
+    }
+    double pb = -1.0;          // d tcc / d prod(n-1)
+    for (int k = n - 1; k >= 1; k--) {
+      const double a = frac(k - 1), b = frac(k), mc = 1.0 - (a > b ? a : b);
+      double mcb;
+      if (prod[k - 1] == 0.0 && 1.0 - a == 0.0) {
+        mcb = pb;
+        pb = 0.0;
+      } else {
+        const double r = 1.0 / (1.0 - a);
+        mcb = pb * prod[k - 1] * r;
+        dcf[k - 1] += pb * prod[k - 1] * mc * r * r;
+        pb = pb * mc * r;
+      }
+      if (a > b) dcf[k - 1] -= mcb; else dcf[k] -= mcb;
+    }
+    dcf[0] -= pb;
+    for (int k = 0; k < n; k++)
+      if (cf && cf[k] < MIN_COVERAGE) dcf[k] = 0.0;
+  } else if (overlap == 4) {   // water-content weighted average
+    double ws = 0.0;
+    for (int k = 0; k < Ku; k++) {
+      if (frac(k) == 0.0) continue;
+      for (int c = 0; c < n_clouds; c++) {
+        const double w = wc[c * cstride + k];
+        if (w > WATER_CONTENT_THRESHOLD) ws += w;
+      }
+    }
+    for (int k = 0; k < Ku && ws > 0.0; k++) {
+      if (frac(k) == 0.0) continue;
+      double lwc = 0.0;
+      for (int c = 0; c < n_clouds; c++) {
+        const double w = wc[c * cstride + k];
+        if (w > WATER_CONTENT_THRESHOLD) lwc += w;
+      }
+      dcf[k] = lwc / ws;
+      dwc[k] = (frac(k) - tcc) / ws;
+    }
+  }
 }
 
 // Stream rule (CRTM_Compute_nStreams): Legendre terms 2/4/6 from the Mie

@@ -164,5 +164,8 @@ class KMatrixBatch:
     absorber: np.ndarray
     water_temperature: np.ndarray
     surface_emissivity: np.ndarray
-    cloud_water_content: Optional[np.ndarray] = None
-    cloud_effective_radius: Optional[np.ndarray] = None
+    cloud_water_content: Optional[np.ndarray] = None     # (P, L, NC, Kmax)
+    cloud_effective_radius: Optional[np.ndarray] = None  # (P, L, NC, Kmax)
+    cloud_fraction: Optional[np.ndarray] = None          # (P, L, Kmax)
+    aerosol_concentration: Optional[np.ndarray] = None   # (P, L, NA, Kmax)
+    aerosol_effective_radius: Optional[np.ndarray] = None  # (P, L, NA, Kmax)

@@ -137,12 +137,31 @@ typedef struct {
    * that use only some of them save the rest of the output traffic. */
   int n_k_absorbers;
   const int* k_absorber_index;
+  /* Jacobians of scattering profiles (Atmosphere_K%Cloud(n)%Water_Content,
+   * %Effective_Radius, Atmosphere_K%Cloud_Fraction, Atmosphere_K%Aerosol(n)%
+   * Concentration, %Effective_Radius); each may be NULL (not computed).  Cloud
+   * arrays [P][L][max_clouds][max_layers], cloud_fraction [P][L][max_layers],
+   * aerosol arrays [P][L][max_aerosols][max_layers]; zero outside each
+   * profile's clouds, aerosols and layers. */
+  double* cloud_water_content;
+  double* cloud_effective_radius;
+  double* cloud_fraction;
+  double* aerosol_concentration;
+  double* aerosol_effective_radius;
 } crtm_gpu_kmatrix;
 
 typedef struct {
   double* temperature;        /* [P][max_layers] */
   double* absorber;           /* [P][n_absorbers][max_layers] */
   double* water_temperature;  /* [P] */
+  /* adjoints of the scattering inputs (Atmosphere_AD%Cloud(n)%..., %Cloud_Fraction,
+   * %Aerosol(n)%...), each may be NULL: [P][max_clouds][max_layers],
+   * [P][max_layers], [P][max_aerosols][max_layers] */
+  double* cloud_water_content;
+  double* cloud_effective_radius;
+  double* cloud_fraction;
+  double* aerosol_concentration;
+  double* aerosol_effective_radius;
 } crtm_gpu_adjoint_out;
 
 /* CRTM_Init: loads <coeff_path>/<sensor_id>.SpcCoeff.bin and .TauCoeff.bin

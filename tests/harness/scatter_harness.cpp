@@ -126,6 +126,10 @@ int sx_stream_rule(double max_reff, double wavenumber) { return stream_rule_nleg
 double sx_total_cloud_cover(int Ku, int n_clouds, const double* cf, const double* wc, int cstride, int overlap) {
   return total_cloud_cover(Ku, n_clouds, cf, wc, (size_t)cstride, overlap);
 }
+void sx_cloud_cover_derivatives(int Ku, int n_clouds, const double* cf, const double* wc, int cstride, int overlap,
+                                double tcc, double* dcf, double* dwc) {
+  cloud_cover_derivatives(Ku, n_clouds, cf, wc, (size_t)cstride, overlap, tcc, dcf, dwc);
+}
 }
 
 
@@ -178,7 +182,7 @@ extern "C" int sx_cloudy_kmatrix(const int* dims, const double* f_mw, const doub
                                  double emissivity, double planck_surface, double cosmic, const double* planck,
                                  const double* temp, const int* cloud_type, const double* wc, const double* reff,
                                  int cstride, const double* od, double* radiance, double* dgas, double* dT,
-                                 double* e_b, double* Bs_b) {
+                                 double* e_b, double* Bs_b, double* dwc, double* dre) {
   CloudLut L{dims[0], dims[1], dims[2], dims[3], dims[4], dims[5], dims[6], f_mw, r_mw, t, f_ir, r_ir,
              ke_l, w_l, pc_l, ke_s, w_s, pc_s, ke_ir, w_ir, pc_ir};
   static const GaussTable gt = make_gauss();
@@ -195,10 +199,22 @@ extern "C" int sx_cloudy_kmatrix(const int* dims, const double* f_mw, const doub
   };
   std::vector<double> st((size_t)(Ku + 1) * (NZ * NZ + NZ));
   auto state = [&](int lev, int i) -> double& { return st[(size_t)lev * (NZ * NZ + NZ) + i]; };
-  auto contract = [&](int k, int kind, const Mat<NZ, double>& T_b, const Mat<NZ, double>& R_b,
-                      const double* src_b, double od_b, double* g) {
-    return layer_contract<NZ>(c, L, S, k, od[k], T_b, R_b, src_b, od_b, g) == kind;
+  int bad = 0;
+  auto adj = [&](int k, int kind, const Mat<NZ, double>& T_b, const Mat<NZ, double>& R_b, const double* src_b,
+                 double od_b, double B_b) {
+    // gas and temperature, then each cloud's (water content, radius), one cloud per pass
+    LayerDirections d{true, 0, {0, 0, 0, 0}};
+    double g[4];
+    if (layer_contract<NZ, 2>(c, L, S, k, od[k], d, T_b, R_b, src_b, od_b, B_b, g) != kind) bad = 7;
+    dgas[k] = g[0];
+    dT[k] = g[1];
+    for (int cc = 0; cc < n_clouds; cc++) {
+      d = LayerDirections{false, 1, {cc, 0, 0, 0}};
+      if (layer_contract<NZ, 2>(c, L, S, k, od[k], d, T_b, R_b, src_b, od_b, B_b, g) != kind) bad = 7;
+      if (dwc) dwc[(size_t)cc * cstride + k] = g[0];
+      if (dre) dre[(size_t)cc * cstride + k] = g[1];
+    }
   };
-  auto out = [&](int k, double g, double tt) { dgas[k] = g; dT[k] = tt; };
-  return cloudy_kmatrix<NZ>(c, S, layer, state, contract, out, radiance, e_b, Bs_b);
+  const int rc = cloudy_adjoint<NZ>(c, S, layer, state, adj, radiance, e_b, Bs_b);
+  return rc ? rc : bad;
 }

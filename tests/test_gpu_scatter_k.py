@@ -41,7 +41,8 @@ def _paths(d, atm):
 
 def _fd_bt(orc, d, atm, sfc, geo, opt, perturb, step):
     """Central difference of the oracle's cloudy brightness temperatures:
-    perturb(atm, sfc, opt, s) applies a signed step s (scalar or per profile)."""
+    perturb(atm, sfc, opt, s) applies a signed step s (scalar or per profile;
+    profiles with a zero step come out as zero)."""
     cp, ap = _paths(d, atm)
     out = []
     for sgn in (1.0, -1.0):
@@ -49,7 +50,8 @@ def _fd_bt(orc, d, atm, sfc, geo, opt, perturb, step):
         perturb(a, s, o, sgn * step)
         out.append(orc.forward_scatter(a, s, geo, o, cp, ap, n_threads=8)[1])
     st = np.asarray(step, np.float64)
-    return (out[0] - out[1]) / (2.0 * (st[:, None] if st.ndim else st))
+    den = 2.0 * (st[:, None] if st.ndim else st)
+    return (out[0] - out[1]) / np.where(den == 0.0, 1.0, den)
 
 
 def _check_layers(km, orc, d, atm, sfc, geo, opt, layers):
@@ -68,6 +70,52 @@ def _check_layers(km, orc, d, atm, sfc, geo, opt, layers):
             got = km.absorber[:, :, j, k]
             scale = max(np.abs(km.absorber[:, :, j]).max(), 1e-12)
             assert np.abs(got - fd).max() <= FD_TOL * scale, (k, j, _rel(got, fd))
+
+
+def _check_species(km, orc, d, atm, sfc, geo, opt, layers, fraction=False):
+    """Cloud water content / effective radius (and, for fractional profiles,
+    cloud fraction) and aerosol concentration / effective radius Jacobians of
+    the listed layers against central differences (steps 1e-4 of the value,
+    1e-6 in the fraction), profile by profile where the species is present."""
+    groups = []
+    if atm.cloud_type is not None:
+        groups += [("cloud_water_content", "cloud_water_content", c) for c in range(atm.cloud_type.shape[1])]
+        groups += [("cloud_effective_radius", "cloud_effective_radius", c) for c in range(atm.cloud_type.shape[1])]
+    if atm.aerosol_type is not None:
+        groups += [("aerosol_concentration", "aerosol_concentration", a) for a in range(atm.aerosol_type.shape[1])]
+        groups += [("aerosol_effective_radius", "aerosol_effective_radius", a)
+                   for a in range(atm.aerosol_type.shape[1])]
+    checked = 0
+    for k in layers:
+        for kname, aname, c in groups:
+            amount = getattr(atm, "cloud_water_content" if kname.startswith("cloud") else "aerosol_concentration")
+            on = amount[:, c, k] > (1e-6 if kname.startswith("cloud") else 1e-9)
+            if kname.startswith("cloud") and atm.cloud_fraction is not None:
+                on &= atm.cloud_fraction[:, k] >= 1e-12
+            if not on.any():
+                continue
+            val = getattr(atm, aname)[:, c, k]
+            step = np.where(on, 1e-4 * val, 0.0)
+
+            def pert(a, s_, o, h, aname=aname, c=c, k=k):
+                getattr(a, aname)[:, c, k] += h
+            fd = _fd_bt(orc, d, atm, sfc, geo, opt, pert, step)
+            got = getattr(km, kname)[:, :, c, k]
+            scale = max(np.abs(getattr(km, kname)[:, :, c] * getattr(atm, aname)[:, None, c]).max(), 1e-12)
+            err = np.abs((got - fd)[on] * val[on, None]).max()
+            assert err <= FD_TOL * scale, (kname, c, k, err / scale)
+            checked += 1
+        if fraction:
+            on = atm.cloud_fraction[:, k] > 0.0
+            if on.any():
+                def pf(a, s_, o, h, k=k):
+                    a.cloud_fraction[:, k] += h
+                fd = _fd_bt(orc, d, atm, sfc, geo, opt, pf, np.where(on, 1e-6, 0.0))
+                got = km.cloud_fraction[:, :, k]
+                scale = max(np.abs(km.cloud_fraction).max(), 1e-12)
+                assert np.abs((got - fd)[on]).max() <= 1e-4 * scale, ("cloud_fraction", k)
+                checked += 1
+    assert checked > 0
 
 
 def _check_surface(km, orc, d, atm, sfc, geo, opt):
@@ -111,6 +159,7 @@ def test_cloudy_k_matrix_matches_oracle_differences(gpu_lib, cloud_dir, sensor, 
     assert np.abs(rts.brightness_temperature - bt).max() <= 1e-4
     _check_layers(km, orc, cloud_dir, atm, sfc, geo, opt, _layers(atm))
     _check_surface(km, orc, cloud_dir, atm, sfc, geo, opt)
+    _check_species(km, orc, cloud_dir, atm, sfc, geo, opt, _layers(atm, ())[:4], fraction=cover is not None)
 
 
 def test_aerosol_k_matrix_matches_oracle_differences(gpu_lib, cloud_dir):
@@ -128,6 +177,7 @@ def test_aerosol_k_matrix_matches_oracle_differences(gpu_lib, cloud_dir):
     orc = Oracle(cloud_dir, sensor)
     _check_layers(km, orc, cloud_dir, atm, sfc, geo, opt, _layers(atm, (10, 50, 80, 100)))
     _check_surface(km, orc, cloud_dir, atm, sfc, geo, opt)
+    _check_species(km, orc, cloud_dir, atm, sfc, geo, opt, _layers(atm, (30, 90))[:4])
 
 
 @pytest.mark.parametrize("sensor,n_streams", [("mwsynth_c16", None), ("irsynth_c616", None),
@@ -138,7 +188,8 @@ def test_mixed_cloudy_k_matrix_matches_fp64(gpu_lib, cloud_dir, sensor, n_stream
     ref = gpu_lib.CRTM([sensor], cloud_dir, 0).k_matrix(atm, sfc, geo, opt)
     mix = gpu_lib.CRTM([sensor], cloud_dir, 1).k_matrix(atm, sfc, geo, opt)
     assert np.abs(mix[1].brightness_temperature - ref[1].brightness_temperature).max() <= 1e-2
-    for f in ("temperature", "absorber", "water_temperature", "surface_emissivity"):
+    for f in ("temperature", "absorber", "water_temperature", "surface_emissivity", "cloud_water_content",
+              "cloud_effective_radius"):
         assert _rel(getattr(mix[0], f), getattr(ref[0], f)) <= MIX_TOL, f
 
 
@@ -170,6 +221,9 @@ def test_cloudy_adjoint_is_seeded_k_matrix_sum(gpu_lib, cloud_dir, precision):
     assert _rel(ad["temperature"], km.temperature.sum(axis=1)) <= tol
     assert _rel(ad["absorber"], km.absorber.sum(axis=1)) <= tol
     assert _rel(ad["water_temperature"], km.water_temperature.sum(axis=1)) <= tol
+    for f in ("cloud_water_content", "cloud_effective_radius", "cloud_fraction", "aerosol_concentration",
+              "aerosol_effective_radius"):
+        assert _rel(ad[f], getattr(km, f).sum(axis=1)) <= tol, f
 
 
 def test_clear_profile_in_cloudy_batch_keeps_clear_k_matrix(gpu_lib, cloud_dir):

@@ -189,8 +189,9 @@ def test_layer_derivatives_match_finite_differences(sx, coeff_dir, sensor, nleg,
 def test_cloudy_kmatrix_matches_finite_differences(sx, coeff_dir, sensor, nl, n_streams, wc_scale):
     """ADA K-matrix (adjoint of the adding, derivative numbers through the
     layer optics) against central differences of the FP64 cloudy radiance
-    with respect to each layer's gas optical depth and temperature, the
-    surface emissivity and the surface Planck radiance."""
+    with respect to each layer's gas optical depth and temperature, each
+    cloud's water content and effective radius, the surface emissivity and
+    the surface Planck radiance."""
     path = sy.write_cloud_files(coeff_dir)
     cc = co.read_cloudcoeff(path)
     sc = co.read_spccoeff(f"{coeff_dir}/{sensor}.SpcCoeff.bin")
@@ -215,7 +216,7 @@ def test_cloudy_kmatrix_matches_finite_differences(sx, coeff_dir, sensor, nl, n_
         fr = sc.frequency[l] if mw else sc.wavenumber[l]
         e, bs, cbr = float(opt.emissivity[m, l]), 1.5 * planck[0], float(sc.cosmic_background_radiance[l])
 
-        def fwd(od, temp, e=e, bs=bs):
+        def fwd(od, temp, e=e, bs=bs, wc=wc, re=re):
             r = ct.c_double()
             assert sx.sx_cloudy_radiance(_p(dims, _ip), *[_p(a) for a in arrs], Ku, ctype.size, nleg, int(mw),
                                          ct.c_double(fr), ct.c_double(mu), ct.c_double(e), ct.c_double(bs),
@@ -224,12 +225,13 @@ def test_cloudy_kmatrix_matches_finite_differences(sx, coeff_dir, sensor, nl, n_
                                          None, None, None, None, ct.c_double(sc.wavenumber[l]), ct.byref(r)) == 0
             return r.value
         dg, dT = np.zeros(Ku), np.zeros(Ku)
+        dwc, dre = np.zeros_like(wc), np.zeros_like(re)
         rad, eb, bb = ct.c_double(), ct.c_double(), ct.c_double()
         assert sx.sx_cloudy_kmatrix(_p(dims, _ip), *[_p(a) for a in arrs], Ku, ctype.size, nleg, int(mw),
                                     ct.c_double(fr), ct.c_double(mu), ct.c_double(e), ct.c_double(bs),
                                     ct.c_double(cbr), _p(planck), _p(temp0), _p(ctype, _ip), _p(wc), _p(re),
                                     atm.max_layers, _p(od0), ct.byref(rad), _p(dg), _p(dT), ct.byref(eb),
-                                    ct.byref(bb)) == 0
+                                    ct.byref(bb), _p(dwc), _p(dre)) == 0
         assert abs(rad.value - fwd(od0, temp0)) <= 1e-13 * abs(rad.value)
         cloudy = np.where((wc[:, :Ku] > 1e-6).any(axis=0))[0]
         for k in list(cloudy[:5]) + [0, Ku - 1]:
@@ -245,6 +247,22 @@ def test_cloudy_kmatrix_matches_finite_differences(sx, coeff_dir, sensor, nl, n_
             t2[k] -= h
             fd = (fwd(od0, t1) - fwd(od0, t2)) / (2 * h)
             assert abs(fd - dT[k]) <= 1e-6 * np.abs(dT).max(), (l, k, fd, dT[k])
+            for c in range(ctype.size):
+                if not wc[c, k] > 1e-6:
+                    assert dwc[c, k] == 0.0 and dre[c, k] == 0.0
+                    continue
+                hw = 1e-4 * wc[c, k]
+                w1, w2 = wc.copy(), wc.copy()
+                w1[c, k] += hw
+                w2[c, k] -= hw
+                fd = (fwd(od0, temp0, wc=w1) - fwd(od0, temp0, wc=w2)) / (2 * hw)
+                assert abs(fd - dwc[c, k]) <= 1e-6 * np.abs(dwc * wc).max() / wc[c, k] + 1e-12, (l, k, c)
+                hr = 1e-4 * re[c, k]
+                r1, r2 = re.copy(), re.copy()
+                r1[c, k] += hr
+                r2[c, k] -= hr
+                fd = (fwd(od0, temp0, re=r1) - fwd(od0, temp0, re=r2)) / (2 * hr)
+                assert abs(fd - dre[c, k]) <= 1e-6 * np.abs(dre * re).max() / re[c, k] + 1e-12, (l, k, c)
         he = 1e-3
         fd = (fwd(od0, temp0, e=e + he) - fwd(od0, temp0, e=e - he)) / (2 * he)
         assert abs(fd - eb.value) <= 1e-5 * abs(eb.value) + 1e-15 * abs(rad.value) / he
@@ -275,3 +293,42 @@ def test_total_cloud_cover_matches_overlap_schemes(sx, overlap):
         else:
             assert abs(got - _tcc(cf, lwc, overlap)) < 1e-14
     assert sx.sx_total_cloud_cover(3, 1, _p(np.ones(3)), _p(np.full(3, 1e-3)), 3, 7) == -2.0
+
+
+@pytest.mark.parametrize("overlap", [1, 2, 3, 4, 5])
+def test_cloud_cover_derivatives_match_differences(sx, overlap):
+    """cloud_cover_derivatives against central differences of total_cloud_cover
+    in each layer's cloud fraction and (average overlap) each cloud's water
+    content."""
+    sx.sx_total_cloud_cover.restype = ct.c_double
+    rng = np.random.Generator(np.random.PCG64(500 + overlap))
+    for trial in range(20):
+        K, NC = 40, 2
+        wc = np.where(rng.uniform(size=(NC, K)) < 0.4, 10.0 ** rng.uniform(-5, -2, (NC, K)), 0.0)
+        cf = np.where((wc > 0).any(axis=0), rng.uniform(0.05, 0.95, K), 0.0)
+
+        def tcc(cf_, wc_):
+            return sx.sx_total_cloud_cover(K, NC, _p(np.ascontiguousarray(cf_)), _p(np.ascontiguousarray(wc_)),
+                                           K, overlap)
+        t0 = tcc(cf, wc)
+        assert t0 >= 0.0
+        dcf, dwc = np.zeros(K), np.zeros(K)
+        sx.sx_cloud_cover_derivatives(K, NC, _p(cf), _p(wc), K, overlap, ct.c_double(t0), _p(dcf), _p(dwc))
+        h = 1e-7
+        for k in range(K):
+            if cf[k] == 0.0:
+                continue
+            c1, c2 = cf.copy(), cf.copy()
+            c1[k] += h
+            c2[k] -= h
+            fd = (tcc(c1, wc) - tcc(c2, wc)) / (2 * h)
+            assert abs(fd - dcf[k]) < 1e-6, (k, fd, dcf[k])
+            for c in range(NC):
+                if wc[c, k] <= 1e-6:
+                    continue
+                hw = 1e-4 * wc[c, k]
+                w1, w2 = wc.copy(), wc.copy()
+                w1[c, k] += hw
+                w2[c, k] -= hw
+                fd = (tcc(cf, w1) - tcc(cf, w2)) / (2 * hw)
+                assert abs(fd - dwc[k]) <= 1e-6 * (abs(fd) + 1.0), (k, c, fd, dwc[k])
