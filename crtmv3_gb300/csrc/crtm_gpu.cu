@@ -519,7 +519,8 @@ struct Work {
   R* SC;            // [n][L]
   double* TSK;      // adjoint: [n][L]
   R* RA;            // [n][nv][K][L]
-  R* LB;            // scattering: [n][Kmax][NE][L] layer records
+  R* LB;            // cloudy forward: [n][Kmax][NE][L] layer records
+  double* LBK;      // scattering K-matrix/adjoint: [n][Kmax][NE][L] layer records, FP64
   double* FB;       // cloudy forward with SOI: [n][2][2][Kmax+1][NZ][L] fields
   double* maxreff;  // scattering: [n]
   double* cover;    // scattering: [n] total cloud cover
@@ -588,7 +589,10 @@ size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w
   wk.OD = (R*)carve(nn * K * L * sizeof(R));
   if (mode == 3) wk.TAU = (R*)carve(nn * Kmax * L * sizeof(R));
   if (sw.rec > 0) {
-    wk.LB = (R*)carve(nn * Kmax * (size_t)sw.rec * L * sizeof(R));
+    if (sw.kstate)
+      wk.LBK = (double*)carve(nn * Kmax * (size_t)sw.rec * L * sizeof(double));
+    else
+      wk.LB = (R*)carve(nn * Kmax * (size_t)sw.rec * L * sizeof(R));
     wk.maxreff = (double*)carve(nn * sizeof(double));
     wk.cover = (double*)carve(nn * sizeof(double));
     // SOI fields: 2 fields x 2 buffers x levels x angles
@@ -828,7 +832,7 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       sa.n_aerosols = b->n_aerosols; sa.aerosol_type = b->aerosol_type;
       sa.conc = b->aerosol_concentration; sa.aer_reff = b->aerosol_effective_radius;
       if (b->max_clouds <= 0) sa.max_clouds = 0;
-      sa.TAU = w.TAU; sa.LB = w.LB; sa.maxreff = w.maxreff; sa.cover = w.cover;
+      sa.TAU = w.TAU; sa.LB = w.LB; sa.LBK = w.LBK; sa.maxreff = w.maxreff; sa.cover = w.cover;
       sa.cloud_fraction = sa.max_clouds > 0 ? b->cloud_fraction : nullptr;
       sa.overlap = sa.max_clouds > 0 ? b->overlap_id : nullptr;
       sa.radiance = rts->radiance; sa.bt = rts->brightness_temperature;
@@ -842,10 +846,14 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
         StageScope sc(h, 6, st);
         scatter_profile_kernel<R><<<(n + 3) / 4, 128, 0, st>>>(sa);
         CK_LAUNCH(h);
-        if (nz_max)
-          scatter_layers_kernel<SC_NZ_MAX, R><<<gl, SCATTER_THREADS, 0, st>>>(sa);
+        if (split && nz_max)
+          launch_scatter_layers_k<SC_NZ_MAX, R>(sa, gl, st);
+        else if (split)
+          launch_scatter_layers_k<5, R>(sa, gl, st);
+        else if (nz_max)
+          scatter_layers_kernel<SC_NZ_MAX, R, R><<<gl, SCATTER_THREADS, 0, st>>>(sa, w.LB);
         else
-          scatter_layers_kernel<5, R><<<gl, SCATTER_THREADS, 0, st>>>(sa);
+          scatter_layers_kernel<5, R, R><<<gl, SCATTER_THREADS, 0, st>>>(sa, w.LB);
         CK_LAUNCH(h);
       }
       if (split) {
@@ -979,8 +987,13 @@ int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, c
     return fail(h, "missing adjoint output buffers");
   if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
   const Sensor& s = h->sensors[sensor];
-  const bool fp64 = h->precision == CRTM_GPU_FP64;
   const bool scat = b->max_clouds > 0 || b->max_aerosols > 0;
+  // The K-matrix and adjoint of a batch with clouds or aerosols run the gas
+  // optics in FP64 in both forms: the cloud Jacobians are small differences
+  // of large terms, and the FP32 regression's optical-depth rounding moves
+  // them by more than 1e-3 of their largest value.  The scattering work is
+  // FP64 in both forms anyway and the gas optics is under 1 % of such a call.
+  const bool fp64 = h->precision == CRTM_GPU_FP64 || (scat && (mode == 1 || mode == 2));
   if (scat) {
     if (b->max_clouds > SC_NC_MAX || b->max_aerosols > SC_NC_MAX)
       return fail(h, "at most %d clouds and %d aerosols per profile", SC_NC_MAX, SC_NC_MAX);

@@ -12,6 +12,11 @@ int scatter_k_d10_set_gauss(const GaussTable& g) {
 }
 
 template <int NZ, class R>
+void launch_scatter_layers_k(const ScatterArgs<R>& a, unsigned grid, cudaStream_t st) {
+  scatter_layers_kernel<NZ, R, double><<<grid, SCATTER_THREADS, 0, st>>>(a, a.LBK);
+}
+
+template <int NZ, class R>
 void launch_scatter_kmatrix(const ScatterArgs<R>& a, dim3 grid, cudaStream_t st) {
   scatter_kmatrix_kernel<NZ, R><<<grid, SCATTER_THREADS, 0, st>>>(a);
 }
@@ -21,6 +26,7 @@ void launch_scatter_contract(const ScatterArgs<R>& a, unsigned grid, cudaStream_
   scatter_contract_kernel<NZ, R><<<grid, SCATTER_THREADS, 0, st>>>(a);
 }
 
+template void launch_scatter_layers_k<10, double>(const ScatterArgs<double>&, unsigned, cudaStream_t);
 template void launch_scatter_kmatrix<10, double>(const ScatterArgs<double>&, dim3, cudaStream_t);
 template void launch_scatter_contract<10, double>(const ScatterArgs<double>&, unsigned, cudaStream_t);
 

@@ -75,7 +75,9 @@ struct ScatterArgs {
   const double* conc, *aer_reff;   // [P][NA][Kmax]
   double* FB;                   // SOI fields [n][2][2][Kmax+1][NZ][L], or null
   const R* TAU;                 // [n][Kmax][L] gas layer optical depths
-  R* LB;                        // [n][Kmax][NE][L] layer records
+  R* LB;                        // [n][Kmax][NE][L] layer records (forward)
+  double* LBK;                  // [n][Kmax][NE][L] layer records of the K-matrix / adjoint, FP64 in
+                                // both forms: the species contractions cancel strongly
   const double* cloud_fraction; // [P][Kmax] or null (1)
   const int* overlap;           // [P] Options%Overlap_Id or null (4, average)
   double* maxreff;              // [n]
@@ -195,8 +197,8 @@ __device__ __forceinline__ CloudyColumn column_inputs(const ScatterArgs<R>& a, i
   return c;
 }
 
-template <int NZ, class R>
-__global__ void __launch_bounds__(SCATTER_THREADS) scatter_layers_kernel(ScatterArgs<R> a) {
+template <int NZ, class R, class Rec>
+__global__ void __launch_bounds__(SCATTER_THREADS) scatter_layers_kernel(ScatterArgs<R> a, Rec* LBr) {
   constexpr int NE = layer_record<NZ>();
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int L = a.L, Kmax = a.Kmax;
@@ -206,19 +208,19 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_layers_kernel(Scatter
   const int p = (int)(idx / ((long long)L * Kmax));
   const int gp = a.p_begin + p;
   if (a.pv.status[p] != 0 || k >= a.b.n_layers[gp]) return;
-  R* rec = a.LB + ((size_t)p * Kmax + k) * NE * L + l;
+  Rec* rec = LBr + ((size_t)p * Kmax + k) * NE * L + l;
   const CloudyColumn c = column_inputs(a, p, gp, l);
   if (c.n_clouds == 0 && c.n_aerosols == 0) return;
   StreamSet<NZ, double> S;
   if (int rc = stream_set<NZ, double>(c.nleg, c.mu_sensor, c.n_clouds > 0 ? a.lut.nleg : -1, c_gauss, S)) {
-    rec[0] = R(-rc);
+    rec[0] = Rec(-rc);
     return;
   }
-  Mat<NZ, R> Tm, Rm;
-  R src[NZ], od;
+  Mat<NZ, Rec> Tm, Rm;
+  Rec src[NZ], od;
   const double gas = double(a.TAU[((size_t)p * Kmax + k) * L + l]);
-  const int kind = layer_optics<NZ, R>(c, a.lut, S, k, gas, c.temperature[k], &od, Tm, Rm, src);
-  rec[0] = R(kind);
+  const int kind = layer_optics<NZ, Rec>(c, a.lut, S, k, gas, c.temperature[k], &od, Tm, Rm, src);
+  rec[0] = Rec(kind);
   rec[(size_t)L] = od;
   if (kind != 1) return;
   const int nZ = S.nZ;
@@ -367,16 +369,16 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_kmatrix_kernel(Scatte
   if (!code) {
     const int nZ = S.nZ;
     auto layer = [&](int k, int* kind, double* od, Mat<NZ, double>& Tm, Mat<NZ, double>& Rm, double* src) {
-      const R* rec = a.LB + ((size_t)p * Kmax + k) * NE * L + l;
+      const double* rec = a.LBK + ((size_t)p * Kmax + k) * NE * L + l;
       *kind = (int)rec[0];
-      *od = double(rec[(size_t)L]);
+      *od = rec[(size_t)L];
       if (*kind != 1) return;
       for (int i = 0; i < nZ; i++) {
         for (int j = 0; j < nZ; j++) {
-          Tm.a[i][j] = double(rec[(size_t)(2 + i * NZ + j) * L]);
-          Rm.a[i][j] = double(rec[(size_t)(2 + NZ * NZ + i * NZ + j) * L]);
+          Tm.a[i][j] = rec[(size_t)(2 + i * NZ + j) * L];
+          Rm.a[i][j] = rec[(size_t)(2 + NZ * NZ + i * NZ + j) * L];
         }
-        src[i] = double(rec[(size_t)(2 + 2 * NZ * NZ + i) * L]);
+        src[i] = rec[(size_t)(2 + 2 * NZ * NZ + i) * L];
       }
     };
     double* as = a.AS + (size_t)p * (Kmax + 1) * NS * L + l;

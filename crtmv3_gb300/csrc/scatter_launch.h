@@ -23,6 +23,8 @@ inline int scatter_k_set_gauss(const GaussTable& g) {
 }
 
 template <int NZ, class R>
+void launch_scatter_layers_k(const ScatterArgs<R>& a, unsigned grid, cudaStream_t st);
+template <int NZ, class R>
 void launch_scatter_kmatrix(const ScatterArgs<R>& a, dim3 grid, cudaStream_t st);
 template <int NZ, class R>
 void launch_scatter_contract(const ScatterArgs<R>& a, unsigned grid, cudaStream_t st);

@@ -195,11 +195,15 @@ def test_mixed_cloudy_k_matrix_matches_fp64(gpu_lib, cloud_dir, sensor, n_stream
 
 @pytest.mark.parametrize("precision", [0, 1])
 def test_cloudy_k_matrix_radiance_matches_forward(gpu_lib, cloud_dir, precision):
+    """The K-matrix returns the forward radiance.  The mixed form's forward
+    keeps its layer records in FP32 and the K-matrix in FP64, so they agree to
+    1e-3 K there (both within 0.01 K of the FP64 form); exactly otherwise."""
     atm, sfc, geo, opt = sy.cloudy_workload("mwsynth_c16", 12, 100, 86, wc_scale=300.0)
     h = gpu_lib.CRTM(["mwsynth_c16"], cloud_dir, precision)
     fw = h.forward(atm, sfc, geo, opt)
     _, rts = h.k_matrix(atm, sfc, geo, opt)
-    assert np.abs(rts.brightness_temperature - fw.brightness_temperature).max() <= 1e-6
+    assert np.abs(rts.brightness_temperature - fw.brightness_temperature).max() <= (1e-6 if precision == 0
+                                                                                   else 1e-3)
 
 
 @pytest.mark.parametrize("precision", [0, 1])
