@@ -17,6 +17,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -846,32 +847,42 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
         StageScope sc(h, 6, st);
         scatter_profile_kernel<R><<<(n + 3) / 4, 128, 0, st>>>(sa);
         CK_LAUNCH(h);
-        if (split && nz_max)
-          launch_scatter_layers_k<SC_NZ_MAX, R>(sa, gl, st);
-        else if (split)
-          launch_scatter_layers_k<5, R>(sa, gl, st);
-        else if (nz_max)
-          scatter_layers_kernel<SC_NZ_MAX, R, R><<<gl, SCATTER_THREADS, 0, st>>>(sa, w.LB);
-        else
-          scatter_layers_kernel<5, R, R><<<gl, SCATTER_THREADS, 0, st>>>(sa, w.LB);
+        if (split) {   // K-matrix / adjoint: R is double here (FP64 gas optics)
+          if constexpr (std::is_same<R, double>::value) {
+            if (nz_max)
+              launch_scatter_layers_k<SC_NZ_MAX, double>(sa, gl, st);
+            else
+              launch_scatter_layers_k<5, double>(sa, gl, st);
+          }
+        } else {   // forward: FP64 layer solver in both forms (records in R)
+          using C = double;
+          if (nz_max)
+            scatter_layers_kernel<SC_NZ_MAX, R, R, C><<<gl, SCATTER_THREADS, 0, st>>>(sa, w.LB);
+          else
+            scatter_layers_kernel<5, R, R, C><<<gl, SCATTER_THREADS, 0, st>>>(sa, w.LB);
+        }
         CK_LAUNCH(h);
       }
       if (split) {
-        {
-          StageScope sc(h, 7, st);
-          if (nz_max)
-            launch_scatter_kmatrix<SC_NZ_MAX, R>(sa, ga, st);
-          else
-            launch_scatter_kmatrix<5, R>(sa, ga, st);
-          CK_LAUNCH(h);
-        }
-        {
-          StageScope sc(h, 6, st);
-          if (nz_max)
-            launch_scatter_contract<SC_NZ_MAX, R>(sa, gl, st);
-          else
-            launch_scatter_contract<5, R>(sa, gl, st);
-          CK_LAUNCH(h);
+        if constexpr (std::is_same<R, double>::value) {
+          {
+            StageScope sc(h, 7, st);
+            if (nz_max)
+              launch_scatter_kmatrix<SC_NZ_MAX>(sa, ga, st);
+            else
+              launch_scatter_kmatrix<5>(sa, ga, st);
+            CK_LAUNCH(h);
+          }
+          {
+            StageScope sc(h, 6, st);
+            if (nz_max)
+              launch_scatter_contract<SC_NZ_MAX, double>(sa, gl, st);
+            else
+              launch_scatter_contract<5, double>(sa, gl, st);
+            CK_LAUNCH(h);
+          }
+        } else {
+          return fail(h, "internal: scattering K-matrix with FP32 gas optics");
         }
         {
           ca.pass = 2;

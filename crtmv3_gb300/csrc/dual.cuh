@@ -1,11 +1,14 @@
-// Forward-mode derivative numbers: a value and N directional derivatives.
-// The cloudy K-matrix evaluates each layer's optics (cloud/aerosol LUT,
-// combine, phase, MOM) on these to get the layer's transmission, reflection
-// and source together with their derivatives with respect to the layer's gas
-// optical depth and temperature.
+// Forward-mode derivative numbers: a value and N directional derivatives, in
+// the scalar S (double, or double-float in the mixed form).  The cloudy
+// K-matrix evaluates each layer's optics (cloud/aerosol LUT, combine, phase,
+// MOM) on these to get the derivatives of the layer's transmission,
+// reflection and source with respect to its gas optical depth, temperature
+// and the clouds' and aerosols' amounts and radii.
 #pragma once
 
 #include <math.h>
+
+#include "dd.cuh"
 
 #ifndef CRTM_HD
 #ifdef __CUDACC__
@@ -17,18 +20,19 @@
 
 namespace crtm {
 
-// keep the plain overloads visible next to the Dual ones below
+// keep the plain overloads visible next to the Dual and DD ones
 using ::exp;
 using ::fabs;
 using ::sqrt;
 
-template <int N>
+template <int N, class S = double>
 struct Dual {
-  double v;
-  double d[N];
-  CRTM_HD Dual() : v(0.0) { for (int i = 0; i < N; i++) d[i] = 0.0; }
-  CRTM_HD Dual(double x) : v(x) { for (int i = 0; i < N; i++) d[i] = 0.0; }   // NOLINT: implicit from double
-  CRTM_HD explicit operator double() const { return v; }
+  S v;
+  S d[N];
+  CRTM_HD Dual() : v(0.0) { for (int i = 0; i < N; i++) d[i] = S(0.0); }
+  CRTM_HD Dual(double x) : v(x) { for (int i = 0; i < N; i++) d[i] = S(0.0); }   // NOLINT: implicit
+  CRTM_HD Dual(const S& x, int) : v(x) { for (int i = 0; i < N; i++) d[i] = S(0.0); }
+  CRTM_HD explicit operator double() const { return (double)v; }
   CRTM_HD Dual& operator+=(const Dual& b) { v += b.v; for (int i = 0; i < N; i++) d[i] += b.d[i]; return *this; }
   CRTM_HD Dual& operator-=(const Dual& b) { v -= b.v; for (int i = 0; i < N; i++) d[i] -= b.d[i]; return *this; }
   CRTM_HD Dual& operator*=(const Dual& b) {
@@ -37,66 +41,74 @@ struct Dual {
     return *this;
   }
   CRTM_HD Dual& operator/=(const Dual& b) {
-    const double r = 1.0 / b.v, q = v * r;
+    const S r = S(1.0) / b.v, q = v * r;
     for (int i = 0; i < N; i++) d[i] = (d[i] - q * b.d[i]) * r;
     v = q;
     return *this;
   }
 };
 
-template <int N> CRTM_HD Dual<N> operator+(Dual<N> a, const Dual<N>& b) { return a += b; }
-template <int N> CRTM_HD Dual<N> operator-(Dual<N> a, const Dual<N>& b) { return a -= b; }
-template <int N> CRTM_HD Dual<N> operator*(Dual<N> a, const Dual<N>& b) { return a *= b; }
-template <int N> CRTM_HD Dual<N> operator/(Dual<N> a, const Dual<N>& b) { return a /= b; }
-template <int N> CRTM_HD Dual<N> operator+(Dual<N> a, double b) { a.v += b; return a; }
-template <int N> CRTM_HD Dual<N> operator+(double b, Dual<N> a) { a.v += b; return a; }
-template <int N> CRTM_HD Dual<N> operator-(Dual<N> a, double b) { a.v -= b; return a; }
-template <int N> CRTM_HD Dual<N> operator-(double b, const Dual<N>& a) {
-  Dual<N> r;
-  r.v = b - a.v;
+template <int N, class S> CRTM_HD Dual<N, S> operator+(Dual<N, S> a, const Dual<N, S>& b) { return a += b; }
+template <int N, class S> CRTM_HD Dual<N, S> operator-(Dual<N, S> a, const Dual<N, S>& b) { return a -= b; }
+template <int N, class S> CRTM_HD Dual<N, S> operator*(Dual<N, S> a, const Dual<N, S>& b) { return a *= b; }
+template <int N, class S> CRTM_HD Dual<N, S> operator/(Dual<N, S> a, const Dual<N, S>& b) { return a /= b; }
+template <int N, class S> CRTM_HD Dual<N, S> operator+(Dual<N, S> a, double b) { a.v += S(b); return a; }
+template <int N, class S> CRTM_HD Dual<N, S> operator+(double b, Dual<N, S> a) { a.v += S(b); return a; }
+template <int N, class S> CRTM_HD Dual<N, S> operator-(Dual<N, S> a, double b) { a.v -= S(b); return a; }
+template <int N, class S> CRTM_HD Dual<N, S> operator-(double b, const Dual<N, S>& a) {
+  Dual<N, S> r;
+  r.v = S(b) - a.v;
   for (int i = 0; i < N; i++) r.d[i] = -a.d[i];
   return r;
 }
-template <int N> CRTM_HD Dual<N> operator*(Dual<N> a, double b) { a.v *= b; for (int i = 0; i < N; i++) a.d[i] *= b; return a; }
-template <int N> CRTM_HD Dual<N> operator*(double b, Dual<N> a) { return a * b; }
-template <int N> CRTM_HD Dual<N> operator/(Dual<N> a, double b) { return a * (1.0 / b); }
-template <int N> CRTM_HD Dual<N> operator/(double b, const Dual<N>& a) { return Dual<N>(b) / a; }
-template <int N> CRTM_HD Dual<N> operator-(const Dual<N>& a) { return 0.0 - a; }
+template <int N, class S> CRTM_HD Dual<N, S> operator*(Dual<N, S> a, double b) {
+  const S bs(b);
+  a.v *= bs;
+  for (int i = 0; i < N; i++) a.d[i] *= bs;
+  return a;
+}
+template <int N, class S> CRTM_HD Dual<N, S> operator*(double b, Dual<N, S> a) { return a * b; }
+template <int N, class S> CRTM_HD Dual<N, S> operator/(Dual<N, S> a, double b) { return a * (1.0 / b); }
+template <int N, class S> CRTM_HD Dual<N, S> operator/(double b, const Dual<N, S>& a) { return Dual<N, S>(b) / a; }
+template <int N, class S> CRTM_HD Dual<N, S> operator-(const Dual<N, S>& a) { return 0.0 - a; }
 
-template <int N> CRTM_HD bool operator<(const Dual<N>& a, const Dual<N>& b) { return a.v < b.v; }
-template <int N> CRTM_HD bool operator>(const Dual<N>& a, const Dual<N>& b) { return a.v > b.v; }
-template <int N> CRTM_HD bool operator<=(const Dual<N>& a, const Dual<N>& b) { return a.v <= b.v; }
-template <int N> CRTM_HD bool operator>=(const Dual<N>& a, const Dual<N>& b) { return a.v >= b.v; }
-template <int N> CRTM_HD bool operator<(const Dual<N>& a, double b) { return a.v < b; }
-template <int N> CRTM_HD bool operator>(const Dual<N>& a, double b) { return a.v > b; }
-template <int N> CRTM_HD bool operator<=(const Dual<N>& a, double b) { return a.v <= b; }
-template <int N> CRTM_HD bool operator>=(const Dual<N>& a, double b) { return a.v >= b; }
-template <int N> CRTM_HD bool operator==(const Dual<N>& a, double b) { return a.v == b; }
+template <int N, class S> CRTM_HD bool operator<(const Dual<N, S>& a, const Dual<N, S>& b) { return a.v < b.v; }
+template <int N, class S> CRTM_HD bool operator>(const Dual<N, S>& a, const Dual<N, S>& b) { return a.v > b.v; }
+template <int N, class S> CRTM_HD bool operator<=(const Dual<N, S>& a, const Dual<N, S>& b) { return a.v <= b.v; }
+template <int N, class S> CRTM_HD bool operator>=(const Dual<N, S>& a, const Dual<N, S>& b) { return a.v >= b.v; }
+template <int N, class S> CRTM_HD bool operator<(const Dual<N, S>& a, double b) { return a.v < b; }
+template <int N, class S> CRTM_HD bool operator>(const Dual<N, S>& a, double b) { return a.v > b; }
+template <int N, class S> CRTM_HD bool operator<=(const Dual<N, S>& a, double b) { return a.v <= b; }
+template <int N, class S> CRTM_HD bool operator>=(const Dual<N, S>& a, double b) { return a.v >= b; }
+template <int N, class S> CRTM_HD bool operator==(const Dual<N, S>& a, double b) { return a.v == b; }
 
-template <int N> CRTM_HD Dual<N> sqrt(const Dual<N>& a) {
-  Dual<N> r;
-  r.v = ::sqrt(a.v);
-  const double g = 0.5 / r.v;
+template <int N, class S> CRTM_HD Dual<N, S> sqrt(const Dual<N, S>& a) {
+  Dual<N, S> r;
+  r.v = sqrt(a.v);
+  const S g = S(0.5) / r.v;
   for (int i = 0; i < N; i++) r.d[i] = a.d[i] * g;
   return r;
 }
-template <int N> CRTM_HD Dual<N> exp(const Dual<N>& a) {
-  Dual<N> r;
-  r.v = ::exp(a.v);
+template <int N, class S> CRTM_HD Dual<N, S> exp(const Dual<N, S>& a) {
+  Dual<N, S> r;
+  r.v = exp(a.v);
   for (int i = 0; i < N; i++) r.d[i] = a.d[i] * r.v;
   return r;
 }
-template <int N> CRTM_HD Dual<N> fabs(const Dual<N>& a) { return a.v < 0.0 ? -a : a; }
+template <int N, class S> CRTM_HD Dual<N, S> fabs(const Dual<N, S>& a) { return a.v < 0.0 ? -a : a; }
 
 CRTM_HD double value_of(double x) { return x; }
 CRTM_HD bool is_zero(double x) { return x == 0.0; }
 CRTM_HD bool is_zero(float x) { return x == 0.0f; }
-template <int N> CRTM_HD bool is_zero(const Dual<N>& x) {
-  if (x.v != 0.0) return false;
+template <int N, class S> CRTM_HD bool is_zero(const Dual<N, S>& x) {
+  if (!is_zero(x.v)) return false;
   for (int i = 0; i < N; i++)
-    if (x.d[i] != 0.0) return false;
+    if (!is_zero(x.d[i])) return false;
   return true;
 }
-template <int N> CRTM_HD double value_of(const Dual<N>& x) { return x.v; }
+template <int N, class S> CRTM_HD double value_of(const Dual<N, S>& x) { return value_of(x.v); }
+// derivative part i as a double
+CRTM_HD double part(double x) { return x; }
+CRTM_HD double part(const DD& x) { return (double)x; }
 
 }  // namespace crtm

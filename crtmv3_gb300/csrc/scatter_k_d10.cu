@@ -1,5 +1,6 @@
 // Scattering K-matrix/adjoint kernels for NZ = 10 angles (Options%n_Streams up to 16),
-// FP64 records; one translation unit so that the library compiles in parallel.
+// layer solver in FP64 (the all-FP64 form); one translation unit so that the
+// library compiles in parallel.
 #include "scatter_kernels.cuh"
 #include "scatter_launch.h"
 
@@ -11,23 +12,23 @@ int scatter_k_d10_set_gauss(const GaussTable& g) {
   return cudaMemcpyToSymbol(c_gauss, &g, sizeof g) == cudaSuccess ? 0 : 1;
 }
 
-template <int NZ, class R>
-void launch_scatter_layers_k(const ScatterArgs<R>& a, unsigned grid, cudaStream_t st) {
-  scatter_layers_kernel<NZ, R, double><<<grid, SCATTER_THREADS, 0, st>>>(a, a.LBK);
+template <int NZ, class C>
+void launch_scatter_layers_k(const ScatterArgs<double>& a, unsigned grid, cudaStream_t st) {
+  scatter_layers_kernel<NZ, double, double, C><<<grid, SCATTER_THREADS, 0, st>>>(a, a.LBK);
 }
 
-template <int NZ, class R>
-void launch_scatter_kmatrix(const ScatterArgs<R>& a, dim3 grid, cudaStream_t st) {
-  scatter_kmatrix_kernel<NZ, R><<<grid, SCATTER_THREADS, 0, st>>>(a);
+template <int NZ>
+void launch_scatter_kmatrix(const ScatterArgs<double>& a, dim3 grid, cudaStream_t st) {
+  scatter_kmatrix_kernel<NZ, double><<<grid, SCATTER_THREADS, 0, st>>>(a);
 }
 
-template <int NZ, class R>
-void launch_scatter_contract(const ScatterArgs<R>& a, unsigned grid, cudaStream_t st) {
-  scatter_contract_kernel<NZ, R><<<grid, SCATTER_THREADS, 0, st>>>(a);
+template <int NZ, class C>
+void launch_scatter_contract(const ScatterArgs<double>& a, unsigned grid, cudaStream_t st) {
+  scatter_contract_kernel<NZ, double, C><<<grid, SCATTER_THREADS, 0, st>>>(a);
 }
 
 template void launch_scatter_layers_k<10, double>(const ScatterArgs<double>&, unsigned, cudaStream_t);
-template void launch_scatter_kmatrix<10, double>(const ScatterArgs<double>&, dim3, cudaStream_t);
+template void launch_scatter_kmatrix<10>(const ScatterArgs<double>&, dim3, cudaStream_t);
 template void launch_scatter_contract<10, double>(const ScatterArgs<double>&, unsigned, cudaStream_t);
 
 }  // namespace crtm

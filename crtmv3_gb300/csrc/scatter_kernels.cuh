@@ -102,6 +102,11 @@ struct ScatterArgs {
 
 constexpr int SCATTER_THREADS = 128;
 
+// The layer solver's arithmetic C is a template parameter of the layer and
+// contraction kernels: double in the all-FP64 form, DD (double-float on the
+// FP32 pipe: about 48 bits at a quarter of the cost of GB300's FP64) in the
+// mixed form.
+
 // Per profile, one warp each: the largest effective radius of its clouds and
 // aerosols (stream rule input; clouds dropped by a fraction below 1e-12 do
 // not count) and the total cloud cover of a fractional profile.
@@ -197,7 +202,7 @@ __device__ __forceinline__ CloudyColumn column_inputs(const ScatterArgs<R>& a, i
   return c;
 }
 
-template <int NZ, class R, class Rec>
+template <int NZ, class R, class Rec, class C>
 __global__ void __launch_bounds__(SCATTER_THREADS) scatter_layers_kernel(ScatterArgs<R> a, Rec* LBr) {
   constexpr int NE = layer_record<NZ>();
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -219,7 +224,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_layers_kernel(Scatter
   Mat<NZ, Rec> Tm, Rm;
   Rec src[NZ], od;
   const double gas = double(a.TAU[((size_t)p * Kmax + k) * L + l]);
-  const int kind = layer_optics<NZ, Rec>(c, a.lut, S, k, gas, c.temperature[k], &od, Tm, Rm, src);
+  const int kind = layer_optics<NZ, Rec, C>(c, a.lut, S, k, C(gas), C(c.temperature[k]), &od, Tm, Rm, src);
   rec[0] = Rec(kind);
   rec[(size_t)L] = od;
   if (kind != 1) return;
@@ -429,7 +434,7 @@ CRTM_HD int active_species(const CloudyColumn& c, int k, int* sp) {
   return n;
 }
 
-template <int NZ, class R>
+template <int NZ, class R, class C>
 __global__ void __launch_bounds__(SCATTER_THREADS) scatter_contract_kernel(ScatterArgs<R> a) {
   constexpr int NE = layer_record<NZ>();
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -477,10 +482,10 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_contract_kernel(Scatt
   int done = 0;
   if (nsp == 0) {
     const LayerDirections d{true, 0, {0, 0, 0, 0}};
-    layer_contract<NZ, 2>(c, a.lut, S, k, gas, d, T_b, R_b, src_b, od_b, B_b, g);
+    layer_contract<NZ, 2, C>(c, a.lut, S, k, gas, d, T_b, R_b, src_b, od_b, B_b, g);
   } else {   // gas, temperature and the first species in one pass
     const LayerDirections d{true, 1, {sp[0], 0, 0, 0}};
-    layer_contract<NZ, 4>(c, a.lut, S, k, gas, d, T_b, R_b, src_b, od_b, B_b, g);
+    layer_contract<NZ, 4, C>(c, a.lut, S, k, gas, d, T_b, R_b, src_b, od_b, B_b, g);
     const size_t o = ((size_t)p * a.n_slots + slot(sp[0])) * Kmax * L + (size_t)k * L + l;
     a.CJ[o] = g[2];
     a.CR[o] = g[3];
@@ -491,7 +496,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_contract_kernel(Scatt
   while (done < nsp) {   // two more species per pass
     const int m = nsp - done >= 2 ? 2 : 1;
     const LayerDirections d{false, m, {sp[done], m == 2 ? sp[done + 1] : 0, 0, 0}};
-    layer_contract<NZ, 4>(c, a.lut, S, k, gas, d, T_b, R_b, src_b, od_b, B_b, g);
+    layer_contract<NZ, 4, C>(c, a.lut, S, k, gas, d, T_b, R_b, src_b, od_b, B_b, g);
     for (int i = 0; i < m; i++) {
       const size_t o = ((size_t)p * a.n_slots + slot(sp[done + i])) * Kmax * L + (size_t)k * L + l;
       a.CJ[o] = g[2 * i];

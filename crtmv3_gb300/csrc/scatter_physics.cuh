@@ -273,7 +273,7 @@ CRTM_HD void jacobi(int n, Mat<NZ, T>& S, T* lam, Mat<NZ, T>& V) {
       diag += S.a[i][i] * S.a[i][i];
       for (int j = i + 1; j < n; j++) off += S.a[i][j] * S.a[i][j];
     }
-    if (off <= T(1.0e-32) * diag) break;
+    if (off <= T(JacobiEps<T>::value) * diag) break;
     for (int p = 0; p < n - 1; p++)
       for (int q = p + 1; q < n; q++) {
         const T apq = S.a[p][q];
@@ -304,36 +304,36 @@ CRTM_HD void jacobi(int n, Mat<NZ, T>& S, T* lam, Mat<NZ, T>& V) {
 // Symmetric eigenproblem on derivative numbers: eigenpairs of the value
 // part by Jacobi, then their derivatives by first-order perturbation:
 // d(lambda_i) = v_i' dS v_i and dv_i = sum_{j != i} v_j (v_j' dS v_i) / (lambda_i - lambda_j).
-template <int NZ, int N>
-CRTM_HD void jacobi(int n, Mat<NZ, Dual<N>>& S, Dual<N>* lam, Mat<NZ, Dual<N>>& V) {
-  Mat<NZ, double> S0, V0;
-  double l0[NZ];
+template <int NZ, int N, class Q>
+CRTM_HD void jacobi(int n, Mat<NZ, Dual<N, Q>>& S, Dual<N, Q>* lam, Mat<NZ, Dual<N, Q>>& V) {
+  Mat<NZ, Q> S0, V0;
+  Q l0[NZ];
   for (int i = 0; i < n; i++)
     for (int j = 0; j < n; j++) S0.a[i][j] = S.a[i][j].v;
-  jacobi<NZ, double>(n, S0, l0, V0);
+  jacobi<NZ, Q>(n, S0, l0, V0);
   for (int i = 0; i < n; i++) {
-    lam[i] = Dual<N>(l0[i]);
-    for (int j = 0; j < n; j++) V.a[i][j] = Dual<N>(V0.a[i][j]);
+    lam[i] = Dual<N, Q>(l0[i], 0);
+    for (int j = 0; j < n; j++) V.a[i][j] = Dual<N, Q>(V0.a[i][j], 0);
   }
   for (int q = 0; q < N; q++) {
     // M = V0' dS V0
-    double M[NZ][NZ], T1[NZ][NZ];
+    Q M[NZ][NZ], T1[NZ][NZ];
     for (int i = 0; i < n; i++)
       for (int j = 0; j < n; j++) {
-        double v = 0.0;
+        Q v = Q(0.0);
         for (int k = 0; k < n; k++) v += S.a[i][k].d[q] * V0.a[k][j];
         T1[i][j] = v;
       }
     for (int i = 0; i < n; i++)
       for (int j = 0; j < n; j++) {
-        double v = 0.0;
+        Q v = Q(0.0);
         for (int k = 0; k < n; k++) v += V0.a[k][i] * T1[k][j];
         M[i][j] = v;
       }
     for (int i = 0; i < n; i++) lam[i].d[q] = M[i][i];
     for (int r = 0; r < n; r++)     // row r of dV = V0 C, C_ji = M_ji / (l_i - l_j)
       for (int i = 0; i < n; i++) {
-        double v = 0.0;
+        Q v = Q(0.0);
         for (int j = 0; j < n; j++)
           if (j != i) v += V0.a[r][j] * M[j][i] / (l0[i] - l0[j]);
         V.a[r][i].d[q] = v;
@@ -1168,11 +1168,11 @@ struct LayerDirections {
 // the temperature direction (its Planck radiance enters the adding outside
 // the layer optics).  The optics are evaluated on derivative numbers with N
 // directions.  Returns the layer kind of that evaluation.
-template <int NZ, int N>
+template <int NZ, int N, class Q = double>
 CRTM_HD int layer_contract(const CloudyColumn& in, const CloudLut& lut, const StreamSet<NZ, double>& S, int k,
                            double gas_od, const LayerDirections& dir, const Mat<NZ, double>& T_b,
                            const Mat<NZ, double>& R_b, const double* src_b, double od_b, double B_b, double* g) {
-  using D = Dual<N>;
+  using D = Dual<N, Q>;
   D gd(gas_od), tt(in.temperature[k]);
   const int base = dir.gas_t ? 2 : 0;
   if (dir.gas_t) {
@@ -1193,12 +1193,13 @@ CRTM_HD int layer_contract(const CloudyColumn& in, const CloudLut& lut, const St
   if (kind == 1) {
     for (int i = 0; i < S.nZ; i++)
       for (int d = 0; d < N; d++) {
-        double acc = src_b[i] * srcd[i].d[d];
-        for (int j = 0; j < S.nZ; j++) acc += T_b.a[i][j] * Td.a[i][j].d[d] + R_b.a[i][j] * Rd.a[i][j].d[d];
+        double acc = src_b[i] * part(srcd[i].d[d]);
+        for (int j = 0; j < S.nZ; j++)
+          acc += T_b.a[i][j] * part(Td.a[i][j].d[d]) + R_b.a[i][j] * part(Rd.a[i][j].d[d]);
         g[d] += acc;
       }
   } else if (kind == 0) {
-    for (int d = 0; d < N; d++) g[d] = od_b * odd.d[d];
+    for (int d = 0; d < N; d++) g[d] = od_b * part(odd.d[d]);
     if (dir.gas_t) {
       const double te = in.b1 + in.b2 * in.temperature[k];
       const double ee = exp(in.c2 / te);

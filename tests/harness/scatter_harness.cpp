@@ -27,6 +27,37 @@ int sx_ada_layer(int nS, int nZ, double w, double tau, const double* mu, const d
   return 0;
 }
 
+// One ADA layer in double-float (the mixed form's layer solver).
+int sx_ada_layer_dd(int nS, int nZ, double w, double tau, const double* mu, const double* wt,
+                    const double* ff, const double* bb, double B, double* T, double* R, double* src) {
+  Mat<SC_NZ_MAX, DD> F, Bm, Tm, Rm;
+  DD mud[SC_NZ_MAX], wtd[SC_NZ_MAX], s[SC_NZ_MAX];
+  for (int i = 0; i < nZ; i++) {
+    mud[i] = DD(mu[i]);
+    wtd[i] = DD(wt[i]);
+    for (int j = 0; j < nZ; j++) { F.a[i][j] = DD(ff[i * nZ + j]); Bm.a[i][j] = DD(bb[i * nZ + j]); }
+  }
+  if (!ada_layer<SC_NZ_MAX, DD>(nS, nZ, DD(w), DD(tau), mud, wtd, F, Bm, DD(B), Tm, Rm, s)) return 1;
+  for (int i = 0; i < nZ; i++) {
+    src[i] = (double)s[i];
+    for (int j = 0; j < nZ; j++) { T[i * nZ + j] = (double)Tm.a[i][j]; R[i * nZ + j] = (double)Rm.a[i][j]; }
+  }
+  return 0;
+}
+
+// Double-float arithmetic checks: a op b for op = 0 +, 1 -, 2 *, 3 /, 4 sqrt(a), 5 exp(a).
+double sx_dd_op(int op, double a, double b) {
+  const DD x(a), y(b);
+  switch (op) {
+    case 0: return (double)(x + y);
+    case 1: return (double)(x - y);
+    case 2: return (double)(x * y);
+    case 3: return (double)(x / y);
+    case 4: return (double)sqrt(x);
+    default: return (double)exp(x);
+  }
+}
+
 // dims: nfm nrm nt nd nfi nri nleg; arrays in the file's Fortran order.
 int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, const double* t,
                        const double* f_ir, const double* r_ir, const double* ke_l, const double* w_l,
@@ -55,8 +86,8 @@ int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, 
   c.n_aerosols = n_aer; c.wavenumber = wavenumber; c.aerosol_type = aer_type; c.conc = conc;
   c.aer_reff = aer_reff; c.alut = &A;
   c.soi = soi != 0;
-  if (soi == 2) {   // layered ADA as the GPU kernels run it (records with NZ = 5)
-    c.soi = false;
+  if (soi == 2 || soi == 3) {   // layered ADA as the GPU kernels run it (records with NZ = 5);
+    c.soi = false;              // soi = 3: layer optics in double-float (the mixed form)
     constexpr int NZ = 5, NE = 2 + 2 * NZ * NZ + NZ;
     StreamSet<NZ, double> S;
     if (int rc = stream_set<NZ, double>(nleg, mu_sensor, n_clouds > 0 ? L.nleg : -1, gt, S)) return rc;
@@ -64,7 +95,8 @@ int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, 
     for (int k = 0; k < Ku; k++) {
       Mat<NZ, double> Tm, Rm;
       double srcv[NZ], o;
-      const int kind = layer_optics<NZ, double>(c, L, S, k, od[k], temp[k], &o, Tm, Rm, srcv);
+      const int kind = soi == 3 ? layer_optics<NZ, double, DD>(c, L, S, k, DD(od[k]), DD(temp[k]), &o, Tm, Rm, srcv)
+                                : layer_optics<NZ, double>(c, L, S, k, od[k], temp[k], &o, Tm, Rm, srcv);
       double* r = &rec[(size_t)k * NE];
       r[0] = kind;
       r[1] = o;
@@ -182,7 +214,7 @@ extern "C" int sx_cloudy_kmatrix(const int* dims, const double* f_mw, const doub
                                  double emissivity, double planck_surface, double cosmic, const double* planck,
                                  const double* temp, const int* cloud_type, const double* wc, const double* reff,
                                  int cstride, const double* od, double* radiance, double* dgas, double* dT,
-                                 double* e_b, double* Bs_b, double* dwc, double* dre) {
+                                 double* e_b, double* Bs_b, double* dwc, double* dre, int dd) {
   CloudLut L{dims[0], dims[1], dims[2], dims[3], dims[4], dims[5], dims[6], f_mw, r_mw, t, f_ir, r_ir,
              ke_l, w_l, pc_l, ke_s, w_s, pc_s, ke_ir, w_ir, pc_ir};
   static const GaussTable gt = make_gauss();
@@ -205,12 +237,16 @@ extern "C" int sx_cloudy_kmatrix(const int* dims, const double* f_mw, const doub
     // gas and temperature, then each cloud's (water content, radius), one cloud per pass
     LayerDirections d{true, 0, {0, 0, 0, 0}};
     double g[4];
-    if (layer_contract<NZ, 2>(c, L, S, k, od[k], d, T_b, R_b, src_b, od_b, B_b, g) != kind) bad = 7;
+    auto contract = [&](const LayerDirections& dir) {
+      return dd ? layer_contract<NZ, 2, DD>(c, L, S, k, od[k], dir, T_b, R_b, src_b, od_b, B_b, g)
+                : layer_contract<NZ, 2>(c, L, S, k, od[k], dir, T_b, R_b, src_b, od_b, B_b, g);
+    };
+    if (contract(d) != kind) bad = 7;
     dgas[k] = g[0];
     dT[k] = g[1];
     for (int cc = 0; cc < n_clouds; cc++) {
       d = LayerDirections{false, 1, {cc, 0, 0, 0}};
-      if (layer_contract<NZ, 2>(c, L, S, k, od[k], d, T_b, R_b, src_b, od_b, B_b, g) != kind) bad = 7;
+      if (contract(d) != kind) bad = 7;
       if (dwc) dwc[(size_t)cc * cstride + k] = g[0];
       if (dre) dre[(size_t)cc * cstride + k] = g[1];
     }

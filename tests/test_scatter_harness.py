@@ -57,9 +57,12 @@ def test_ada_layer_matches_oracle(sx, nleg, mu_s, w, tau):
     ("mwsynth_c22", 100, 8, 0, 0), ("mwsynth_c16", 100, None, 1, 0), ("mwsynth_c16", 100, 16, 1, 0),
     ("irsynth_c616", 101, None, 1, 0), ("mwsynth_c16", 100, None, 2, 0), ("irsynth_c616", 101, None, 2, 0),
     ("irsynth_c616", 101, None, 0, 1), ("irsynth_c616", 101, 8, 1, 1), ("irsynth_c616", 101, None, 0, 2),
-    ("mwsynth_c16", 100, None, 0, 1)])
+    ("mwsynth_c16", 100, None, 0, 1), ("mwsynth_c16", 100, None, 3, 0), ("irsynth_c616", 101, None, 3, 1),
+    ("irsynth_c616", 101, None, 3, 2)])
 def test_cloudy_radiance_matches_oracle(sx, coeff_dir, sensor, nl, n_streams, soi, aer):
-    """aer 1: clouds and aerosols; aer 2: aerosols only."""
+    """aer 1: clouds and aerosols; aer 2: aerosols only.  soi 2 / 3: layered
+    ADA as the GPU kernels run it, with the layer optics in FP64 / in
+    double-float (the mixed form)."""
     from oracle.pyoracle import Oracle
     path = sy.write_cloud_files(coeff_dir)
     apath = sy.write_aerosol_files(coeff_dir)
@@ -227,11 +230,19 @@ def test_cloudy_kmatrix_matches_finite_differences(sx, coeff_dir, sensor, nl, n_
         dg, dT = np.zeros(Ku), np.zeros(Ku)
         dwc, dre = np.zeros_like(wc), np.zeros_like(re)
         rad, eb, bb = ct.c_double(), ct.c_double(), ct.c_double()
-        assert sx.sx_cloudy_kmatrix(_p(dims, _ip), *[_p(a) for a in arrs], Ku, ctype.size, nleg, int(mw),
-                                    ct.c_double(fr), ct.c_double(mu), ct.c_double(e), ct.c_double(bs),
-                                    ct.c_double(cbr), _p(planck), _p(temp0), _p(ctype, _ip), _p(wc), _p(re),
-                                    atm.max_layers, _p(od0), ct.byref(rad), _p(dg), _p(dT), ct.byref(eb),
-                                    ct.byref(bb), _p(dwc), _p(dre)) == 0
+        kargs = (_p(dims, _ip), *[_p(a) for a in arrs], Ku, ctype.size, nleg, int(mw), ct.c_double(fr),
+                 ct.c_double(mu), ct.c_double(e), ct.c_double(bs), ct.c_double(cbr), _p(planck), _p(temp0),
+                 _p(ctype, _ip), _p(wc), _p(re), atm.max_layers, _p(od0), ct.byref(rad))
+        assert sx.sx_cloudy_kmatrix(*kargs, _p(dg), _p(dT), ct.byref(eb), ct.byref(bb), _p(dwc), _p(dre), 0) == 0
+        # the contraction on double-float derivative numbers (the mixed form) agrees to 1e-6 of
+        # the largest Jacobian (eigenvector derivatives divide by eigenvalue gaps, which
+        # double-float resolves to ~1e-15 instead of FP64's 1e-16)
+        d2 = [np.zeros(Ku), np.zeros(Ku), np.zeros_like(wc), np.zeros_like(re)]
+        eb2, bb2 = ct.c_double(), ct.c_double()
+        assert sx.sx_cloudy_kmatrix(*kargs, _p(d2[0]), _p(d2[1]), ct.byref(eb2), ct.byref(bb2), _p(d2[2]),
+                                    _p(d2[3]), 1) == 0
+        for x, y in zip((dg, dT, dwc * wc, dre * re), (d2[0], d2[1], d2[2] * wc, d2[3] * re)):
+            assert np.abs(x - y).max() <= 1e-6 * max(np.abs(x).max(), 1e-30)
         assert abs(rad.value - fwd(od0, temp0)) <= 1e-13 * abs(rad.value)
         cloudy = np.where((wc[:, :Ku] > 1e-6).any(axis=0))[0]
         for k in list(cloudy[:5]) + [0, Ku - 1]:
@@ -332,3 +343,49 @@ def test_cloud_cover_derivatives_match_differences(sx, overlap):
                 w2[c, k] -= hw
                 fd = (tcc(cf, w1) - tcc(cf, w2)) / (2 * hw)
                 assert abs(fd - dwc[k]) <= 1e-6 * (abs(fd) + 1.0), (k, c, fd, dwc[k])
+
+
+def test_double_float_arithmetic(sx):
+    """Double-float (two FP32 words) arithmetic against FP64: about 2^-46
+    relative for products, quotients and roots; sums to 2^-46 of the larger
+    operand (cancellation is exact).  Magnitudes 1e-12..1e12 (the layer
+    solver's range): below ~1e-30 the low word leaves FP32's normal range."""
+    sx.sx_dd_op.restype = ct.c_double
+    rng = np.random.Generator(np.random.PCG64(700))
+    a = rng.uniform(-1, 1, 2000) * 10.0 ** rng.uniform(-12, 12, 2000)
+    b = rng.uniform(-1, 1, 2000) * 10.0 ** rng.uniform(-12, 12, 2000)
+    tol = 2.0 ** -45
+    for x, y in zip(a, b):
+        s = sx.sx_dd_op(0, ct.c_double(x), ct.c_double(y))
+        assert abs(s - (x + y)) <= tol * max(abs(x), abs(y))
+        s = sx.sx_dd_op(1, ct.c_double(x), ct.c_double(x * (1 + 1e-9)))
+        assert abs(s - (x - x * (1 + 1e-9))) <= tol * abs(x)
+        assert abs(sx.sx_dd_op(2, ct.c_double(x), ct.c_double(y)) - x * y) <= tol * abs(x * y)
+        assert abs(sx.sx_dd_op(3, ct.c_double(x), ct.c_double(y)) - x / y) <= tol * abs(x / y)
+        assert abs(sx.sx_dd_op(4, ct.c_double(abs(x)), ct.c_double(0)) - np.sqrt(abs(x))) <= tol * np.sqrt(abs(x))
+    for x in rng.uniform(-60, 60, 200):   # the input's rounding, amplified by |x|
+        assert abs(sx.sx_dd_op(5, ct.c_double(x), ct.c_double(0)) - np.exp(x)) <= tol * max(abs(x), 1) * np.exp(x)
+
+
+@pytest.mark.parametrize("nleg,mu_s", [(2, 0.9), (4, 0.55), (6, 0.8), (16, 0.93)])
+@pytest.mark.parametrize("w,tau", [(0.6, 0.5), (0.98, 6.0), (0.999999, 40.0), (0.3, 5e-9), (0.05, 0.02)])
+def test_ada_layer_in_double_float_matches_fp64(sx, nleg, mu_s, w, tau):
+    """The mixed form's layer solver (MOM in double-float on the FP32 pipe)
+    against the FP64 solver, including near-conservative thick layers where
+    plain FP32 fails."""
+    from oracle.pyoracle import lib
+    pc = 0.5 * 0.85 ** np.arange(nleg + 1)
+    mu, wt = np.zeros(20), np.zeros(20)
+    ff, bb = np.zeros(400), np.zeros(400)
+    nz = ct.c_int(0)
+    lib().or_phase_setup(nleg, mu_s, _p(pc), _p(mu), _p(wt), _p(ff), _p(bb), ct.byref(nz))
+    nZ, nS = nz.value, (nleg + 2) // 2
+    outs = [[np.zeros(nZ * nZ), np.zeros(nZ * nZ), np.zeros(nZ)] for _ in range(2)]
+    args = (nS, nZ, ct.c_double(w), ct.c_double(tau), _p(mu), _p(wt), _p(ff), _p(bb), ct.c_double(1.7))
+    assert sx.sx_ada_layer(*args, *[_p(x) for x in outs[0]]) == 0
+    assert sx.sx_ada_layer_dd(*args, *[_p(x) for x in outs[1]]) == 0
+    # T and R are at most 1; the source (1 - sum T - sum R) B cancels for
+    # near-conservative layers, so it is held to 1e-10 of B
+    assert np.abs(outs[0][0] - outs[1][0]).max() <= 1e-11
+    assert np.abs(outs[0][1] - outs[1][1]).max() <= 1e-11
+    assert np.abs(outs[0][2] - outs[1][2]).max() <= 1e-10 * 1.7
