@@ -39,3 +39,34 @@ def test_api_fails_loudly_without_library(monkeypatch, tmp_path):
     monkeypatch.setattr(api, "_lib", None)
     with pytest.raises(RuntimeError):
         api.library()
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="no C compiler")
+def test_ctypes_structs_match_the_header_layout(tmp_path):
+    """Every field of the ctypes mirrors in crtmv3_gb300/api.py sits at the
+    offset the C header gives it, and the structs have the same size."""
+    import subprocess
+    from crtmv3_gb300 import api
+    structs = {"crtm_gpu_batch": api.CBatch, "crtm_gpu_rtsolution": api.CRTSolution,
+               "crtm_gpu_kmatrix": api.CKMatrix, "crtm_gpu_adjoint_out": api.CAdjoint}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "crtm_gpu.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'  printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), "-o", str(exe), str(src)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    seen = 0
+    for line in out:
+        if not line:
+            continue
+        cname, field, value = line.split()
+        py = structs[cname]
+        got = ct.sizeof(py) if field == "size" else getattr(py, field).offset
+        assert got == int(value), (cname, field, got, value)
+        seen += 1
+    assert seen == sum(len(p._fields_) + 1 for p in structs.values())
