@@ -67,16 +67,28 @@ SCATTER_JACOBIANS = ("cloud_water_content", "cloud_effective_radius", "cloud_fra
                      "aerosol_concentration", "aerosol_effective_radius")
 
 
+SURFACE_COVERS = ("land_temperature", "snow_temperature", "ice_temperature")
+
+
 class CKMatrix(ct.Structure):
     _fields_ = [("temperature", ct.c_void_p), ("absorber", ct.c_void_p),
                 ("water_temperature", ct.c_void_p), ("surface_emissivity", ct.c_void_p),
                 ("n_k_absorbers", ct.c_int), ("k_absorber_index", ct.c_void_p)] + \
-               [(f, ct.c_void_p) for f in SCATTER_JACOBIANS]
+               [(f, ct.c_void_p) for f in SCATTER_JACOBIANS + SURFACE_COVERS]
 
 
 class CAdjoint(ct.Structure):
     _fields_ = [("temperature", ct.c_void_p), ("absorber", ct.c_void_p),
-                ("water_temperature", ct.c_void_p)] + [(f, ct.c_void_p) for f in SCATTER_JACOBIANS]
+                ("water_temperature", ct.c_void_p)] + [(f, ct.c_void_p) for f in SCATTER_JACOBIANS + SURFACE_COVERS]
+
+
+TL_FIELDS = ("temperature", "absorber", "land_temperature", "water_temperature", "snow_temperature",
+             "ice_temperature", "emissivity", "cloud_water_content", "cloud_effective_radius", "cloud_fraction",
+             "aerosol_concentration", "aerosol_effective_radius")
+
+
+class CTLIn(ct.Structure):
+    _fields_ = [(f, ct.c_void_p) for f in TL_FIELDS]
 
 
 def _scatter_shapes(atm) -> dict:
@@ -280,12 +292,15 @@ class CRTM:
         if out is None and scattering_jacobians:
             for f, shp in _scatter_shapes(atm).items():
                 setattr(km, f, np.zeros((P, L) + shp))
+        if out is None:
+            for f in SURFACE_COVERS:
+                setattr(km, f, np.zeros((P, L)))
         cr = CRTSolution(rts.radiance.ctypes.data, rts.brightness_temperature.ctypes.data,
                          rts.status.ctypes.data)
         ck = CKMatrix(km.temperature.ctypes.data, km.absorber.ctypes.data,
                       km.water_temperature.ctypes.data, km.surface_emissivity.ctypes.data,
                       0 if sel is None else JK, None if sel is None else sel.ctypes.data,
-                      *[_addr(getattr(km, f, None)) for f in SCATTER_JACOBIANS])
+                      *[_addr(getattr(km, f, None)) for f in SCATTER_JACOBIANS + SURFACE_COVERS])
         self._check(library().crtm_gpu_k_matrix(self.h, sensor, ct.byref(b), _addr(seed),
                                                 ct.byref(ck), ct.byref(cr)))
         return km, rts
@@ -299,13 +314,53 @@ class CRTM:
         out = dict(temperature=np.zeros((P, K)), absorber=np.zeros((P, J, K)), water_temperature=np.zeros(P))
         for f, shp in _scatter_shapes(atm).items():
             out[f] = np.zeros((P,) + shp)
+        for f in SURFACE_COVERS:
+            out[f] = np.zeros(P)
         cr = CRTSolution(rts.radiance.ctypes.data, rts.brightness_temperature.ctypes.data,
                          rts.status.ctypes.data)
         ca = CAdjoint(out["temperature"].ctypes.data, out["absorber"].ctypes.data,
-                      out["water_temperature"].ctypes.data, *[_addr(out.get(f)) for f in SCATTER_JACOBIANS])
+                      out["water_temperature"].ctypes.data,
+                      *[_addr(out.get(f)) for f in SCATTER_JACOBIANS + SURFACE_COVERS])
         self._check(library().crtm_gpu_adjoint(self.h, sensor, ct.byref(b), seed.ctypes.data,
                                                ct.byref(ca), ct.byref(cr)))
         return out, rts
+
+    def tangent_linear(self, atm, sfc, geo, opt, atm_tl=None, sfc_tl=None, emissivity_tl=None,
+                       sensor: int = 0):
+        """CRTM_Tangent_Linear: the brightness-temperature perturbation (P, L)
+        from perturbations of the atmosphere (``atm_tl``: an object with any of
+        temperature, absorber, cloud_water_content, cloud_effective_radius,
+        cloud_fraction, aerosol_concentration, aerosol_effective_radius shaped
+        like ``atm``'s), the surface (``sfc_tl``: cover temperatures) and the
+        emissivity (P, L).  Returns (bt_tl, rts)."""
+        P, L = atm.n_profiles, self.n_channels[sensor]
+        keep: list = []
+        b = self._cbatch(atm, sfc, geo, opt, keep)
+
+        def arr(obj, name):
+            v = getattr(obj, name, None) if obj is not None else None
+            if v is None:
+                return None
+            a = np.ascontiguousarray(v, np.float64)
+            keep.append(a)
+            return a.ctypes.data
+        vals = {f: arr(atm_tl, f) for f in ("temperature", "absorber", "cloud_water_content",
+                                             "cloud_effective_radius", "cloud_fraction", "aerosol_concentration",
+                                             "aerosol_effective_radius")}
+        vals.update({f: arr(sfc_tl, f) for f in ("land_temperature", "water_temperature", "snow_temperature",
+                                                  "ice_temperature")})
+        if emissivity_tl is not None:
+            e = np.ascontiguousarray(emissivity_tl, np.float64)
+            keep.append(e)
+            vals["emissivity"] = e.ctypes.data
+        tl = CTLIn(*[vals.get(f) for f in TL_FIELDS])
+        rts = RTSolutionBatch(np.zeros((P, L)), np.zeros((P, L)), status=np.zeros(P, np.int32))
+        cr = CRTSolution(rts.radiance.ctypes.data, rts.brightness_temperature.ctypes.data,
+                         rts.status.ctypes.data)
+        bt_tl = np.zeros((P, L))
+        self._check(library().crtm_gpu_tangent_linear(self.h, sensor, ct.byref(b), ct.byref(tl), ct.byref(cr),
+                                                      bt_tl.ctypes.data))
+        return bt_tl, rts
 
     # ------------------------------------------------------------------
     # device-resident (torch CUDA tensors) calls
@@ -447,8 +502,7 @@ def CRTM_Adjoint(atmosphere, surface, rts_ad: Sequence[np.ndarray], geometry,
     """CRTM_Adjoint: adjoints summed over the channels of all sensors into ``atmosphere_ad``."""
     rts.clear()
     off = 0
-    P, K, J = atmosphere.n_profiles, atmosphere.max_layers, atmosphere.n_absorbers
-    tot = dict(temperature=np.zeros((P, K)), absorber=np.zeros((P, J, K)), water_temperature=np.zeros(P))
+    tot: dict = {}
     for i, ci in enumerate(channel_info):
         opt = _sensor_options(options, off, ci.n_channels)
         try:
@@ -456,12 +510,35 @@ def CRTM_Adjoint(atmosphere, surface, rts_ad: Sequence[np.ndarray], geometry,
         except RuntimeError as e:
             print(f"CRTM_Adjoint(FAILURE): {e}")
             return FAILURE
-        for k in tot:
-            tot[k] += out[k]
+        for k, v in out.items():
+            tot[k] = tot[k] + v if k in tot else v.copy()
         rts.append(r)
         off += ci.n_channels
     atmosphere_ad.clear()
     atmosphere_ad.update(tot)
+    return SUCCESS
+
+
+def CRTM_Tangent_Linear(atmosphere, surface, atmosphere_tl, surface_tl, geometry,
+                        channel_info: List[ChannelInfo], rts: List[RTSolutionBatch], rts_tl: List[np.ndarray],
+                        options: Optional[OptionsBatch] = None) -> int:
+    """CRTM_Tangent_Linear (src/CRTM_Tangent_Linear_Module.f90:271): forward
+    RTSolution and the brightness-temperature perturbations, one (P, L) array
+    per sensor, from the atmosphere and surface perturbations."""
+    rts.clear()
+    rts_tl.clear()
+    off = 0
+    for ci in channel_info:
+        opt = _sensor_options(options, off, ci.n_channels)
+        try:
+            bt_tl, r = ci.handle.tangent_linear(atmosphere, surface, geometry, opt, atmosphere_tl, surface_tl,
+                                                sensor=ci.sensor_index)
+        except RuntimeError as e:
+            print(f"CRTM_Tangent_Linear(FAILURE): {e}")
+            return FAILURE
+        rts.append(r)
+        rts_tl.append(bt_tl)
+        off += ci.n_channels
     return SUCCESS
 
 

@@ -426,6 +426,8 @@ struct crtm_gpu_context {
   int map_channels = 16;   // channels per map_kernel CTA (power of two, 8..32; 16 measured fastest on C2)
   DevBuf ws;        // chunk workspace
   DevBuf io_in, io_out;  // device copies for the host entry points
+  DevBuf io_tl;          // tangent-linear inputs of the host entry point
+  DevBuf tl_k;           // tangent linear: the K-matrix it contracts
   DevBuf small;     // idx maps
   // cloud LUT (CloudCoeff.bin), when present
   bool has_clouds = false;
@@ -810,6 +812,7 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
     ca.seed = seed; ca.radiance = rts->radiance; ca.bt = rts->brightness_temperature;
     ca.tsk = mode == 1 ? kk->water_temperature : (mode == 2 ? w.TSK : nullptr);
     ca.ek = mode == 1 ? kk->surface_emissivity : nullptr;
+    if (mode == 1) { ca.tsk_land = kk->land_temperature; ca.tsk_snow = kk->snow_temperature; ca.tsk_ice = kk->ice_temperature; }
     ca.status = rts->status;
     // scattering K-matrix/adjoint: the column runs twice around the scattering kernels
     const bool split = scat && mode != 3;
@@ -974,6 +977,7 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       am.K = K; am.Kmax = Kmax; am.nv = nv; am.p_begin = p0; am.n_chunk = n;
       am.b = bv; am.pv = w.pv; am.ras = w.ras; am.pts = w.pts; am.tss = w.tss;
       am.t_ad = ad->temperature; am.a_ad = ad->absorber; am.ts_ad = ad->water_temperature;
+      am.ts_land = ad->land_temperature; am.ts_snow = ad->snow_temperature; am.ts_ice = ad->ice_temperature;
       const long long na = (long long)n * Kmax;
       adjoint_map_kernel<R><<<(unsigned)((na + 255) / 256), 256, 0, st>>>(am);
       CK_LAUNCH(h);
@@ -1034,18 +1038,14 @@ int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, c
   }
 }
 
+int check_call(crtm_gpu_handle h, const crtm_gpu_batch* b, const crtm_gpu_rtsolution* rts);
+
 // Host entry points: copy inputs to the device, run, copy outputs back.
-int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, const double* seed,
-              crtm_gpu_kmatrix* kk, crtm_gpu_adjoint_out* ad, crtm_gpu_rtsolution* rts) {
-  if (!h) return CRTM_GPU_FAILURE;
-  if (sensor < 0 || sensor >= (int)h->sensors.size()) return fail(h, "sensor index %d out of range", sensor);
-  if (!b || b->n_profiles < 0 || b->max_layers < 1 || b->n_absorbers < 0) return fail(h, "bad batch dimensions");
-  if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
-  const int P = b->n_profiles, Km = b->max_layers, J = b->n_absorbers, L = h->sensors[sensor].L;
-  if (P == 0) return CRTM_GPU_SUCCESS;
-  for (int m = 0; m < P; m++)
-    if (b->n_layers[m] < 2 || b->n_layers[m] > Km)
-      return fail(h, "profile %d: n_layers %d outside [2, max_layers=%d]", m, b->n_layers[m], Km);
+// Copy a host batch (and an optional [P][L] seed) into the handle's input
+// buffer; db receives the batch with device pointers.
+int stage_batch(crtm_gpu_handle h, const crtm_gpu_batch* b, int L, const double* seed, crtm_gpu_batch* db_out,
+                const double** dseed_out) {
+  const int P = b->n_profiles, Km = b->max_layers, J = b->n_absorbers;
   // input layout: doubles then ints
   struct Item { const void* src; size_t bytes; };
   const size_t PD = (size_t)P * sizeof(double);
@@ -1103,7 +1103,8 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
     }
     off += align_up(items[i].bytes);
   }
-  crtm_gpu_batch db = *b;
+  crtm_gpu_batch& db = *db_out;
+  db = *b;
   db.level_pressure = (const double*)dptr[0]; db.pressure = (const double*)dptr[1];
   db.temperature = (const double*)dptr[2]; db.absorber = (const double*)dptr[3];
   db.land_coverage = (const double*)dptr[4]; db.water_coverage = (const double*)dptr[5];
@@ -1137,6 +1138,29 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
       db.rt_algorithm_id = b->rt_algorithm_id ? (const int*)dptr[aer0 + 5] : nullptr;
     }
   }
+  *dseed_out = dseed;
+  return CRTM_GPU_SUCCESS;
+}
+
+int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, const double* seed,
+              crtm_gpu_kmatrix* kk, crtm_gpu_adjoint_out* ad, crtm_gpu_rtsolution* rts) {
+  if (!h) return CRTM_GPU_FAILURE;
+  if (sensor < 0 || sensor >= (int)h->sensors.size()) return fail(h, "sensor index %d out of range", sensor);
+  if (!b || b->n_profiles < 0 || b->max_layers < 1 || b->n_absorbers < 0) return fail(h, "bad batch dimensions");
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
+  const int P = b->n_profiles, Km = b->max_layers, J = b->n_absorbers, L = h->sensors[sensor].L;
+  if (P == 0) return CRTM_GPU_SUCCESS;
+  for (int m = 0; m < P; m++)
+    if (b->n_layers[m] < 2 || b->n_layers[m] > Km)
+      return fail(h, "profile %d: n_layers %d outside [2, max_layers=%d]", m, b->n_layers[m], Km);
+  crtm_gpu_batch db;
+  const double* dseed = nullptr;
+  if (int rc = stage_batch(h, b, L, seed, &db, &dseed)) return rc;
+  const int NC = b->max_clouds > 0 ? b->max_clouds : 0;
+  const int NA = b->max_aerosols > 0 ? b->max_aerosols : 0;
+  const size_t PD = (size_t)P * sizeof(double);
+  cudaStream_t st = h->stream;
+  size_t off = 0;
   // outputs
   const size_t PL = (size_t)P * L;
   std::vector<std::pair<void*, size_t>> outs = {{rts->radiance, PL * 8}, {rts->brightness_temperature, PL * 8},
@@ -1150,7 +1174,9 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
                              {kk->cloud_effective_radius, NCo ? PL * NCo * Km * 8 : 0},
                              {kk->cloud_fraction, NCo ? PL * Km * 8 : 0},
                              {kk->aerosol_concentration, NAo ? PL * NAo * Km * 8 : 0},
-                             {kk->aerosol_effective_radius, NAo ? PL * NAo * Km * 8 : 0}});
+                             {kk->aerosol_effective_radius, NAo ? PL * NAo * Km * 8 : 0},
+                             {kk->land_temperature, PL * 8}, {kk->snow_temperature, PL * 8},
+                             {kk->ice_temperature, PL * 8}});
   if (mode == 2)
     outs.insert(outs.end(), {{ad->temperature, (size_t)P * Km * 8}, {ad->absorber, (size_t)P * J * Km * 8},
                              {ad->water_temperature, PD},
@@ -1158,7 +1184,8 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
                              {ad->cloud_effective_radius, NCo ? (size_t)P * NCo * Km * 8 : 0},
                              {ad->cloud_fraction, NCo ? (size_t)P * Km * 8 : 0},
                              {ad->aerosol_concentration, NAo ? (size_t)P * NAo * Km * 8 : 0},
-                             {ad->aerosol_effective_radius, NAo ? (size_t)P * NAo * Km * 8 : 0}});
+                             {ad->aerosol_effective_radius, NAo ? (size_t)P * NAo * Km * 8 : 0},
+                             {ad->land_temperature, PD}, {ad->snow_temperature, PD}, {ad->ice_temperature, PD}});
   size_t tout = 0;
   for (auto& o : outs) tout += align_up(o.second);
   if (!h->io_out.ensure(tout)) return fail(h, "cannot allocate %zu bytes for outputs", tout);
@@ -1174,10 +1201,11 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
   if (mode == 1)
     dk = {(double*)dout[3], (double*)dout[4], (double*)dout[5], (double*)dout[6], kk->n_k_absorbers,
           kk->k_absorber_index, (double*)dout[7], (double*)dout[8], (double*)dout[9], (double*)dout[10],
-          (double*)dout[11]};
+          (double*)dout[11], (double*)dout[12], (double*)dout[13], (double*)dout[14]};
   if (mode == 2)
     dad = {(double*)dout[3], (double*)dout[4], (double*)dout[5], (double*)dout[6], (double*)dout[7],
-           (double*)dout[8], (double*)dout[9], (double*)dout[10]};
+           (double*)dout[8], (double*)dout[9], (double*)dout[10], (double*)dout[11], (double*)dout[12],
+           (double*)dout[13]};
   HostCopy hc;
   hc.n = (int)outs.size();
   for (size_t i = 0; i < outs.size(); i++) {
@@ -1197,7 +1225,13 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
   if (e != cudaSuccess || e2 != cudaSuccess)
     return fail(h, "CUDA error: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
   if (h->profiling) collect_stage_times(h);
-  if (NC > 0 || NA > 0) {
+  return check_call(h, b, rts);
+}
+
+// After a host entry point's work has finished: the scattering error flag and
+// the per-profile status words.
+int check_call(crtm_gpu_handle h, const crtm_gpu_batch* b, const crtm_gpu_rtsolution* rts) {
+  if (b->max_clouds > 0 || b->max_aerosols > 0) {
     int code = 0;
     if (cudaMemcpy(&code, h->d_error, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
       return fail(h, "cannot read the scattering error flag");
@@ -1206,9 +1240,159 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
                              "requested with RT_SOI, 11 invalid Options%Overlap_Id)", code);
   }
   if (rts->status)
-    for (int m = 0; m < P; m++)
+    for (int m = 0; m < b->n_profiles; m++)
       if (rts->status[m] != 0) return fail(h, "profile %d failed (status bits 0x%x)", m, rts->status[m]);
   return CRTM_GPU_SUCCESS;
+}
+
+// Tangent linear as the K-matrix contracted with the perturbations: one warp
+// per (profile, channel), lanes over the layers.
+struct TLArgs {
+  int P, L, Km, J, NC, NA;
+  const int* n_layers;
+  const int* status;
+  const double* kt, *ka, *kw, *kl, *ks, *ki, *ke, *kwc, *kre, *kcf, *kac, *kar;
+  crtm_gpu_tl_in d;
+  double* bt_tl;
+};
+
+__global__ void tl_kernel(TLArgs a) {
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= (long long)a.P * a.L) return;
+  const int p = (int)(w / a.L), l = (int)(w % a.L);
+  const int Ku = a.n_layers[p];
+  const size_t pl = (size_t)p * a.L + l;
+  double s = 0.0;
+  auto rows = [&](const double* K, const double* D, int nrow) {
+    if (!K || !D) return;
+    for (int r = 0; r < nrow; r++) {
+      const double* kr = K + (pl * nrow + r) * a.Km;
+      const double* dr = D + ((size_t)p * nrow + r) * a.Km;
+      for (int k = lane; k < Ku; k += 32) s += kr[k] * dr[k];
+    }
+  };
+  rows(a.kt, a.d.temperature, 1);
+  rows(a.ka, a.d.absorber, a.J);
+  rows(a.kwc, a.d.cloud_water_content, a.NC);
+  rows(a.kre, a.d.cloud_effective_radius, a.NC);
+  rows(a.kcf, a.d.cloud_fraction, 1);
+  rows(a.kac, a.d.aerosol_concentration, a.NA);
+  rows(a.kar, a.d.aerosol_effective_radius, a.NA);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane) return;
+  if (a.d.water_temperature) s += a.kw[pl] * a.d.water_temperature[p];
+  if (a.d.land_temperature) s += a.kl[pl] * a.d.land_temperature[p];
+  if (a.d.snow_temperature) s += a.ks[pl] * a.d.snow_temperature[p];
+  if (a.d.ice_temperature) s += a.ki[pl] * a.d.ice_temperature[p];
+  if (a.d.emissivity) s += a.ke[pl] * a.d.emissivity[pl];
+  a.bt_tl[pl] = (a.status && a.status[p]) ? 0.0 : s;
+}
+
+int tl_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm_gpu_tl_in* tl,
+              crtm_gpu_rtsolution* rts, double* bt_tl, cudaStream_t st) {
+  if (!h) return CRTM_GPU_FAILURE;
+  if (!tl || !bt_tl) return fail(h, "missing tangent-linear inputs or output");
+  if (sensor < 0 || sensor >= (int)h->sensors.size()) return fail(h, "sensor index %d out of range", sensor);
+  if (!b || b->n_profiles < 0 || b->max_layers < 1) return fail(h, "bad batch dimensions");
+  const size_t P = b->n_profiles, L = h->sensors[sensor].L, Km = b->max_layers, J = b->n_absorbers;
+  const size_t NC = b->max_clouds > 0 ? b->max_clouds : 0, NA = b->max_aerosols > 0 ? b->max_aerosols : 0;
+  if (P == 0) return CRTM_GPU_SUCCESS;
+  const bool wc = NC && (tl->cloud_water_content || tl->cloud_effective_radius);
+  const bool cf = NC && tl->cloud_fraction;
+  const bool aer = NA && (tl->aerosol_concentration || tl->aerosol_effective_radius);
+  const size_t PL = P * L;
+  const size_t n_el = PL * Km * (1 + J) + 5 * PL + (wc ? 2 * PL * NC * Km : 0) + (cf ? PL * Km : 0) +
+                      (aer ? 2 * PL * NA * Km : 0);
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
+  if (!h->tl_k.ensure(n_el * sizeof(double)))
+    return fail(h, "cannot allocate %zu bytes for the tangent linear's K-matrix", n_el * sizeof(double));
+  double* q = (double*)h->tl_k.p;
+  auto take = [&](size_t n) { double* r = q; q += n; return r; };
+  crtm_gpu_kmatrix kk{};
+  kk.temperature = take(PL * Km);
+  kk.absorber = take(PL * J * Km);
+  kk.water_temperature = take(PL);
+  kk.land_temperature = take(PL);
+  kk.snow_temperature = take(PL);
+  kk.ice_temperature = take(PL);
+  kk.surface_emissivity = take(PL);
+  if (wc) { kk.cloud_water_content = take(PL * NC * Km); kk.cloud_effective_radius = take(PL * NC * Km); }
+  if (cf) kk.cloud_fraction = take(PL * Km);
+  if (aer) { kk.aerosol_concentration = take(PL * NA * Km); kk.aerosol_effective_radius = take(PL * NA * Km); }
+  if (int rc = dispatch(h, sensor, b, 1, nullptr, rts, &kk, nullptr, st)) return rc;
+  TLArgs ta{};
+  ta.P = (int)P; ta.L = (int)L; ta.Km = (int)Km; ta.J = (int)J; ta.NC = (int)NC; ta.NA = (int)NA;
+  ta.n_layers = b->n_layers; ta.status = rts->status; ta.d = *tl; ta.bt_tl = bt_tl;
+  ta.kt = kk.temperature; ta.ka = kk.absorber; ta.kw = kk.water_temperature; ta.kl = kk.land_temperature;
+  ta.ks = kk.snow_temperature; ta.ki = kk.ice_temperature; ta.ke = kk.surface_emissivity;
+  ta.kwc = kk.cloud_water_content; ta.kre = kk.cloud_effective_radius; ta.kcf = kk.cloud_fraction;
+  ta.kac = kk.aerosol_concentration; ta.kar = kk.aerosol_effective_radius;
+  const long long threads = (long long)PL * 32;
+  tl_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(ta);
+  CK_LAUNCH(h);
+  return CRTM_GPU_SUCCESS;
+}
+
+int tl_host(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm_gpu_tl_in* tl,
+            crtm_gpu_rtsolution* rts, double* bt_tl) {
+  if (!h) return CRTM_GPU_FAILURE;
+  if (!tl || !bt_tl || !rts || !rts->radiance || !rts->brightness_temperature)
+    return fail(h, "missing tangent-linear inputs or outputs");
+  if (sensor < 0 || sensor >= (int)h->sensors.size()) return fail(h, "sensor index %d out of range", sensor);
+  if (!b || b->n_profiles < 0 || b->max_layers < 1 || b->n_absorbers < 0) return fail(h, "bad batch dimensions");
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
+  const size_t P = b->n_profiles, L = h->sensors[sensor].L, Km = b->max_layers, J = b->n_absorbers;
+  const size_t NC = b->max_clouds > 0 ? b->max_clouds : 0, NA = b->max_aerosols > 0 ? b->max_aerosols : 0;
+  if (P == 0) return CRTM_GPU_SUCCESS;
+  for (size_t m = 0; m < P; m++)
+    if (b->n_layers[m] < 2 || b->n_layers[m] > (int)Km)
+      return fail(h, "profile %zu: n_layers %d outside [2, max_layers=%zu]", m, b->n_layers[m], Km);
+  crtm_gpu_batch db;
+  const double* dseed = nullptr;
+  if (int rc = stage_batch(h, b, (int)L, nullptr, &db, &dseed)) return rc;
+  cudaStream_t st = h->stream;
+  // perturbations
+  const double* srcs[12] = {tl->temperature, tl->absorber, tl->land_temperature, tl->water_temperature,
+                            tl->snow_temperature, tl->ice_temperature, tl->emissivity, tl->cloud_water_content,
+                            tl->cloud_effective_radius, tl->cloud_fraction, tl->aerosol_concentration,
+                            tl->aerosol_effective_radius};
+  const size_t sz[12] = {P * Km, P * J * Km, P, P, P, P, P * L, P * NC * Km, P * NC * Km, NC ? P * Km : 0,
+                         P * NA * Km, P * NA * Km};
+  size_t tot = 0;
+  for (int i = 0; i < 12; i++) tot += srcs[i] && sz[i] ? align_up(sz[i] * 8) : 0;
+  if (!h->io_tl.ensure(tot + 256)) return fail(h, "cannot allocate %zu bytes for the perturbations", tot);
+  const double* dsrc[12] = {};
+  size_t off = 0;
+  for (int i = 0; i < 12; i++) {
+    if (!srcs[i] || !sz[i]) continue;
+    dsrc[i] = (const double*)((char*)h->io_tl.p + off);
+    if (cudaMemcpyAsync((void*)dsrc[i], srcs[i], sz[i] * 8, cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return fail(h, "host-to-device copy failed");
+    off += align_up(sz[i] * 8);
+  }
+  const crtm_gpu_tl_in dtl = {dsrc[0], dsrc[1], dsrc[2], dsrc[3], dsrc[4], dsrc[5],
+                              dsrc[6], dsrc[7], dsrc[8], dsrc[9], dsrc[10], dsrc[11]};
+  // outputs
+  const size_t PL = P * L;
+  const size_t o_bt = align_up(PL * 8), o_tl = o_bt + align_up(PL * 8), o_st = o_tl + align_up(PL * 8);
+  if (!h->io_out.ensure(o_st + align_up(P * 4))) return fail(h, "cannot allocate the outputs");
+  char* ob = (char*)h->io_out.p;
+  crtm_gpu_rtsolution drts{(double*)ob, (double*)(ob + o_bt), rts->status ? (int*)(ob + o_st) : nullptr};
+  int rc = tl_device(h, sensor, &db, &dtl, &drts, (double*)(ob + o_tl), st);
+  if (rc == CRTM_GPU_SUCCESS) {
+    if (cudaMemcpyAsync(rts->radiance, drts.radiance, PL * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(rts->brightness_temperature, drts.brightness_temperature, PL * 8, cudaMemcpyDeviceToHost,
+                        st) != cudaSuccess ||
+        cudaMemcpyAsync(bt_tl, ob + o_tl, PL * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        (rts->status && cudaMemcpyAsync(rts->status, drts.status, P * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess))
+      rc = fail(h, "device-to-host copy failed");
+  }
+  const cudaError_t e = cudaStreamSynchronize(st);
+  if (rc != CRTM_GPU_SUCCESS) return rc;
+  if (e != cudaSuccess) return fail(h, "CUDA error: %s", cudaGetErrorString(e));
+  if (h->profiling) collect_stage_times(h);
+  return check_call(h, b, rts);
 }
 
 }  // namespace
@@ -1360,6 +1544,18 @@ int crtm_gpu_adjoint(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, con
                      crtm_gpu_adjoint_out* ad, crtm_gpu_rtsolution* rts) {
   if (!rts || !ad || !bt_ad) return fail(h, "missing adjoint seed or outputs");
   return host_call(h, sensor, b, 2, bt_ad, nullptr, ad, rts);
+}
+
+int crtm_gpu_tangent_linear(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm_gpu_tl_in* tl,
+                            crtm_gpu_rtsolution* rts, double* bt_tl) {
+  return tl_host(h, sensor, b, tl, rts, bt_tl);
+}
+
+int crtm_gpu_tangent_linear_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b,
+                                   const crtm_gpu_tl_in* tl, crtm_gpu_rtsolution* rts, double* bt_tl,
+                                   void* stream) {
+  if (!rts || !rts->radiance || !rts->brightness_temperature) return fail(h, "missing RTSolution buffers");
+  return tl_device(h, sensor, b, tl, rts, bt_tl, stream ? (cudaStream_t)stream : (h ? h->stream : nullptr));
 }
 
 int crtm_gpu_forward_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b,

@@ -600,7 +600,9 @@ struct ColumnArgs {
   R* SC;                  // [n][L] adjoint seed dBT/dR * seed
   const double* seed;     // [P][L] or null (=1)
   double* radiance, *bt;  // [P][L]
-  double* tsk, *ek;       // K-matrix: [P][L]; adjoint: tsk is [n][L] scratch
+  double* tsk, *ek;       // K-matrix: [P][L] water temperature, emissivity; adjoint: tsk is [n][L]
+                          // scratch of dBT/dTs x seed
+  double* tsk_land, *tsk_snow, *tsk_ice;   // K-matrix: [P][L] or null
   int* status;            // [P] or null
   // Scattering profiles in a K-matrix/adjoint call: launched twice.  pass 1
   // stores TAU/DTOP and stops; the scattering K kernel then writes the cloudy
@@ -823,9 +825,14 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   a.SC[(size_t)p * L + l] = R(scale);
   const R dden = ted * (eed - R(1));
   const R dBs = c1 * c2 * eed * b2 / (dden * dden);
-  const double ts_ad = a.b.water_cov[gp] * double(dBs) * Bs_b * scale;
+  // surface temperature: Ts = sum of the coverage-weighted cover temperatures
+  // (CRTM_Compute_SurfaceT), so each cover's adjoint is its coverage x dBT/dTs
+  const double ts_ad = double(dBs) * Bs_b * scale;
   if (a.mode == 1) {
-    a.tsk[pl] = ts_ad;
+    a.tsk[pl] = a.b.water_cov[gp] * ts_ad;
+    if (a.tsk_land) a.tsk_land[pl] = a.b.land_cov[gp] * ts_ad;
+    if (a.tsk_snow) a.tsk_snow[pl] = a.b.snow_cov[gp] * ts_ad;
+    if (a.tsk_ice) a.tsk_ice[pl] = a.b.ice_cov[gp] * ts_ad;
     a.ek[pl] = scale * e_b;   // emissivity_AD - reflectivity_AD
   } else {
     a.tsk[(size_t)p * L + l] = ts_ad;
@@ -1098,7 +1105,8 @@ struct AdjMapArgs {
   const double* tss;   // [n] channel sums of the skin temperature adjoint
   double* t_ad;        // [P][Kmax]
   double* a_ad;        // [P][nv-1][Kmax]
-  double* ts_ad;       // [P]
+  double* ts_ad;       // [P] water temperature
+  double* ts_land, *ts_snow, *ts_ice;   // [P] or null
 };
 
 template <class R>
@@ -1109,7 +1117,12 @@ __global__ void adjoint_map_kernel(AdjMapArgs<R> m) {
   const int gp = m.p_begin + p;
   const int K = m.K, Kmax = m.Kmax, nv = m.nv;
   const int Ku = m.pv.status[p] ? 0 : m.b.n_layers[gp];
-  if (ku == 0) m.ts_ad[gp] = m.tss[p];
+  if (ku == 0) {
+    m.ts_ad[gp] = m.b.water_cov[gp] * m.tss[p];
+    if (m.ts_land) m.ts_land[gp] = m.b.land_cov[gp] * m.tss[p];
+    if (m.ts_snow) m.ts_snow[gp] = m.b.snow_cov[gp] * m.tss[p];
+    if (m.ts_ice) m.ts_ice[gp] = m.b.ice_cov[gp] * m.tss[p];
+  }
   for (int v = 0; v < nv; v++) {
     double* out = v == 0 ? m.t_ad + (size_t)gp * Kmax : m.a_ad + ((size_t)gp * (nv - 1) + (v - 1)) * Kmax;
     if (ku >= Ku) { out[ku] = 0.0; continue; }

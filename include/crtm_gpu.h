@@ -1,6 +1,7 @@
 /*
  * crtm_gpu.h - C-ABI of the GB300 library for CRTM's per-profile x channel
- * forward, K-matrix and adjoint path (ODPS absorption + Emission solver).
+ * forward, K-matrix, adjoint and tangent-linear path (ODPS absorption, cloud
+ * and aerosol scattering, Emission / ADA / SOI solvers).
  *
  * Each entry point stands in for one reference interface (paths relative to
  * the JCSDA/CRTMv3 source tree):
@@ -10,6 +11,7 @@
  *   crtm_gpu_forward     CRTM_Forward     src/CRTM_Forward_Module.f90:229-245
  *   crtm_gpu_k_matrix    CRTM_K_Matrix    src/CRTM_K_Matrix_Module.f90:300-322
  *   crtm_gpu_adjoint     CRTM_Adjoint     src/CRTM_Adjoint_Module.f90:299-309
+ *   crtm_gpu_tangent_linear  CRTM_Tangent_Linear  src/CRTM_Tangent_Linear_Module.f90:271
  *   crtm_gpu_last_error  Display_Message  src/Utility/Message_Handler.f90:114
  *
  * Status codes are the reference's (Message_Handler.f90:27-31).  A call fails
@@ -148,6 +150,11 @@ typedef struct {
   double* cloud_fraction;
   double* aerosol_concentration;
   double* aerosol_effective_radius;
+  /* Surface_K%Land_Temperature, %Snow_Temperature, %Ice_Temperature [P][L]
+   * (each cover's coverage x dBT/dTs, CRTM_Compute_SurfaceT_AD), or NULL */
+  double* land_temperature;
+  double* snow_temperature;
+  double* ice_temperature;
 } crtm_gpu_kmatrix;
 
 typedef struct {
@@ -162,7 +169,31 @@ typedef struct {
   double* cloud_fraction;
   double* aerosol_concentration;
   double* aerosol_effective_radius;
+  double* land_temperature;   /* [P] Surface_AD%Land_Temperature, or NULL */
+  double* snow_temperature;   /* [P] */
+  double* ice_temperature;    /* [P] */
 } crtm_gpu_adjoint_out;
+
+/* Tangent-linear inputs (Atmosphere_TL, Surface_TL and the emissivity
+ * perturbation): each array may be NULL (no perturbation of that input).
+ * Shapes as the batch's: temperature [P][max_layers], absorber
+ * [P][n_absorbers][max_layers], cover temperatures [P], emissivity [P][L],
+ * cloud arrays [P][max_clouds][max_layers], cloud_fraction [P][max_layers],
+ * aerosol arrays [P][max_aerosols][max_layers]. */
+typedef struct {
+  const double* temperature;
+  const double* absorber;
+  const double* land_temperature;
+  const double* water_temperature;
+  const double* snow_temperature;
+  const double* ice_temperature;
+  const double* emissivity;
+  const double* cloud_water_content;
+  const double* cloud_effective_radius;
+  const double* cloud_fraction;
+  const double* aerosol_concentration;
+  const double* aerosol_effective_radius;
+} crtm_gpu_tl_in;
 
 /* CRTM_Init: loads <coeff_path>/<sensor_id>.SpcCoeff.bin and .TauCoeff.bin
  * (ODPS) for each sensor, and <coeff_path>/CloudCoeff.bin and
@@ -196,6 +227,14 @@ int crtm_gpu_k_matrix(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* 
 int crtm_gpu_adjoint(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* batch,
                      const double* bt_ad, crtm_gpu_adjoint_out* ad, crtm_gpu_rtsolution* rts);
 
+/* CRTM_Tangent_Linear: the forward radiances and brightness temperatures
+ * (rts) and the brightness-temperature perturbation bt_tl [P][L] produced by
+ * the input perturbations tl.  Computed as the K-matrix contracted with the
+ * perturbations (exact to rounding; it costs about one K-matrix call and keeps
+ * the K-matrix in device scratch owned by the handle). */
+int crtm_gpu_tangent_linear(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* batch,
+                            const crtm_gpu_tl_in* tl, crtm_gpu_rtsolution* rts, double* bt_tl);
+
 /* Device-resident variants: every pointer in batch / outputs is a device
  * pointer of the handle's device; `stream` is a cudaStream_t (NULL: the
  * handle's stream).  They return after enqueueing the work. */
@@ -207,6 +246,9 @@ int crtm_gpu_k_matrix_device(crtm_gpu_handle handle, int sensor, const crtm_gpu_
 int crtm_gpu_adjoint_device(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* batch,
                             const double* bt_ad, crtm_gpu_adjoint_out* ad,
                             crtm_gpu_rtsolution* rts, void* stream);
+int crtm_gpu_tangent_linear_device(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* batch,
+                                   const crtm_gpu_tl_in* tl, crtm_gpu_rtsolution* rts, double* bt_tl,
+                                   void* stream);
 
 /* No counterpart in the reference (CRTM_K_Matrix allocates its work arrays on
  * every call).  crtm_gpu_k_matrix_device without device-memory allocation:
