@@ -441,6 +441,11 @@ struct crtm_gpu_context {
   int* d_error = nullptr;   // first failure code of the scattering kernel
   cudaStream_t copy_stream = nullptr;   // device-to-host copies of finished chunks
   std::vector<cudaEvent_t> chunk_events;
+  // Calls on a handle share its workspace and buffers, whatever stream each
+  // call uses: every call waits for this event, recorded at the end of the
+  // previous call's work on that call's stream.
+  cudaEvent_t order_event = nullptr;
+  bool order_pending = false;
   // stage profiling
   bool profiling = false;
   struct Pending { int stage; cudaEvent_t a, b; };
@@ -989,6 +994,15 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
   return CRTM_GPU_SUCCESS;
 }
 
+// Order this call's work on st after the previous call's, and mark the end
+// of this call's work (see order_event).
+void order_after_previous(crtm_gpu_handle h, cudaStream_t st) {
+  if (h->order_pending && h->order_event) cudaStreamWaitEvent(st, h->order_event, 0);
+}
+void mark_done(crtm_gpu_handle h, cudaStream_t st) {
+  if (h->order_event && cudaEventRecord(h->order_event, st) == cudaSuccess) h->order_pending = true;
+}
+
 int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, const double* seed,
              crtm_gpu_rtsolution* rts, crtm_gpu_kmatrix* kk, crtm_gpu_adjoint_out* ad,
              cudaStream_t st, const HostCopy* hc = nullptr, const FixedScratch* fixed = nullptr) {
@@ -1028,14 +1042,20 @@ int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, c
     if (cudaMemsetAsync(h->d_error, 0, sizeof(int), st) != cudaSuccess) return fail(h, "error flag reset failed");
     if (mode == 0) mode = 3;
   }
+  order_after_previous(h, st);
+  int rc;
   switch (s.group) {
-    case 1: return fp64 ? run_pipeline<1, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat)
-                        : run_pipeline<1, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat);
-    case 2: return fp64 ? run_pipeline<2, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat)
-                        : run_pipeline<2, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat);
-    default: return fp64 ? run_pipeline<3, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat)
-                         : run_pipeline<3, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat);
+    case 1: rc = fp64 ? run_pipeline<1, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat)
+                      : run_pipeline<1, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat);
+            break;
+    case 2: rc = fp64 ? run_pipeline<2, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat)
+                      : run_pipeline<2, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat);
+            break;
+    default: rc = fp64 ? run_pipeline<3, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat)
+                       : run_pipeline<3, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat);
   }
+  mark_done(h, st);
+  return rc;
 }
 
 int check_call(crtm_gpu_handle h, const crtm_gpu_batch* b, const crtm_gpu_rtsolution* rts);
@@ -1046,6 +1066,7 @@ int check_call(crtm_gpu_handle h, const crtm_gpu_batch* b, const crtm_gpu_rtsolu
 int stage_batch(crtm_gpu_handle h, const crtm_gpu_batch* b, int L, const double* seed, crtm_gpu_batch* db_out,
                 const double** dseed_out) {
   const int P = b->n_profiles, Km = b->max_layers, J = b->n_absorbers;
+  order_after_previous(h, h->stream);
   // input layout: doubles then ints
   struct Item { const void* src; size_t bytes; };
   const size_t PD = (size_t)P * sizeof(double);
@@ -1331,6 +1352,7 @@ int tl_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm
   const long long threads = (long long)PL * 32;
   tl_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(ta);
   CK_LAUNCH(h);
+  mark_done(h, st);
   return CRTM_GPU_SUCCESS;
 }
 
@@ -1413,7 +1435,8 @@ int crtm_gpu_init(const char* coeff_path, int n_sensors, const char* const* sens
     const int v = atoi(e);
     if (v == 8 || v == 16 || v == 32) h->map_channels = v;
   }
-  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->order_event, cudaEventDisableTiming) != cudaSuccess) {
     delete h;
     return fail(nullptr, "cudaStreamCreate failed");
   }
@@ -1509,6 +1532,10 @@ int crtm_gpu_destroy(crtm_gpu_handle h) {
   cudaFree(h->d_aero_type);
   cudaFree(h->d_error);
   collect_stage_times(h);
+  if (h->order_event) {   // the last call's work, whatever stream it ran on
+    cudaEventSynchronize(h->order_event);
+    cudaEventDestroy(h->order_event);
+  }
   for (auto e : h->event_pool) cudaEventDestroy(e);
   if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -1555,20 +1582,20 @@ int crtm_gpu_tangent_linear_device(crtm_gpu_handle h, int sensor, const crtm_gpu
                                    const crtm_gpu_tl_in* tl, crtm_gpu_rtsolution* rts, double* bt_tl,
                                    void* stream) {
   if (!rts || !rts->radiance || !rts->brightness_temperature) return fail(h, "missing RTSolution buffers");
-  return tl_device(h, sensor, b, tl, rts, bt_tl, stream ? (cudaStream_t)stream : (h ? h->stream : nullptr));
+  return tl_device(h, sensor, b, tl, rts, bt_tl, (cudaStream_t)stream);
 }
 
 int crtm_gpu_forward_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b,
                             crtm_gpu_rtsolution* rts, void* stream) {
   return dispatch(h, sensor, b, 0, nullptr, rts, nullptr, nullptr,
-                  stream ? (cudaStream_t)stream : (h ? h->stream : nullptr));
+                  (cudaStream_t)stream);
 }
 
 int crtm_gpu_k_matrix_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b,
                              const double* bt_k, crtm_gpu_kmatrix* k, crtm_gpu_rtsolution* rts,
                              void* stream) {
   return dispatch(h, sensor, b, 1, bt_k, rts, k, nullptr,
-                  stream ? (cudaStream_t)stream : (h ? h->stream : nullptr));
+                  (cudaStream_t)stream);
 }
 
 int crtm_gpu_adjoint_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b,
@@ -1576,7 +1603,7 @@ int crtm_gpu_adjoint_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch*
                             void* stream) {
   if (!bt_ad) return fail(h, "missing adjoint seed");
   return dispatch(h, sensor, b, 2, bt_ad, rts, nullptr, ad,
-                  stream ? (cudaStream_t)stream : (h ? h->stream : nullptr));
+                  (cudaStream_t)stream);
 }
 
 // The K-matrix of crtm_gpu_k_matrix_device with its intermediates in
@@ -1608,7 +1635,7 @@ int crtm_gpu_k_matrix_device_static(crtm_gpu_handle h, int sensor, const crtm_gp
     return fail(h, "static scratch lookup failed: %s", cudaGetErrorString(slot.err));
   const FixedScratch fx{(char*)slot.ptr, STATIC_SCRATCH_BYTES};
   return dispatch(h, sensor, b, 1, bt_k, rts, k, nullptr,
-                  stream ? (cudaStream_t)stream : h->stream, nullptr, &fx);
+                  (cudaStream_t)stream, nullptr, &fx);
 }
 
 int crtm_gpu_last_error(crtm_gpu_handle h, char* buf, int n) {

@@ -236,8 +236,9 @@ int crtm_gpu_tangent_linear(crtm_gpu_handle handle, int sensor, const crtm_gpu_b
                             const crtm_gpu_tl_in* tl, crtm_gpu_rtsolution* rts, double* bt_tl);
 
 /* Device-resident variants: every pointer in batch / outputs is a device
- * pointer of the handle's device; `stream` is a cudaStream_t (NULL: the
- * handle's stream).  They return after enqueueing the work. */
+ * pointer of the handle's device; `stream` is the cudaStream_t the work is
+ * enqueued on (NULL: CUDA's default stream, so the work is ordered with the
+ * caller's default-stream work).  They return after enqueueing the work. */
 int crtm_gpu_forward_device(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* batch,
                             crtm_gpu_rtsolution* rts, void* stream);
 int crtm_gpu_k_matrix_device(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* batch,
