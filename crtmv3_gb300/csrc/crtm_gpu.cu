@@ -424,6 +424,7 @@ struct crtm_gpu_context {
   long long launches = 0;
   size_t workspace_budget = (size_t)8 << 30;
   int map_channels = 16;   // channels per map_kernel CTA (power of two, 8..32; 16 measured fastest on C2)
+  int soi_slots = 20;      // SOI K-matrix/adjoint: order fields kept per (profile, channel), 17..75
   DevBuf ws;        // chunk workspace
   DevBuf io_in, io_out;  // device copies for the host entry points
   DevBuf io_tl;          // tangent-linear inputs of the host entry point
@@ -530,7 +531,8 @@ struct Work {
   R* RA;            // [n][nv][K][L]
   R* LB;            // cloudy forward: [n][Kmax][NE][L] layer records
   double* LBK;      // scattering K-matrix/adjoint: [n][Kmax][NE][L] layer records, FP64
-  double* FB;       // cloudy forward with SOI: [n][2][2][Kmax+1][NZ][L] fields
+  double* FB;       // SOI: [n][2][2][Kmax+1][NZ][L] fields (forward), adjoint fields (K-matrix/adjoint)
+  double* FS;       // SOI K-matrix/adjoint: [n][slots][2][Kmax+1][NZ][L] order fields
   double* maxreff;  // scattering: [n]
   double* cover;    // scattering: [n] total cloud cover
   double* AS;       // scattering K-matrix/adjoint: [n][Kmax+1][NZ*NZ+NZ][L] adding states
@@ -561,6 +563,7 @@ template <int G, class R> constexpr int ad_profiles() { return Tune<G, R>::AD * 
 struct ScatterWork {
   int rec = 0, nz = 0;
   bool soi = false, kstate = false;
+  int soi_slots = 0;     // SOI order-field slots of the K-matrix/adjoint
   int slots = 0;         // species Jacobian slots (max_clouds + max_aerosols), 0: none
   bool cf = false;       // cloud-fraction Jacobian
 };
@@ -606,6 +609,9 @@ size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w
     wk.cover = (double*)carve(nn * sizeof(double));
     // SOI fields: 2 fields x 2 buffers x levels x angles
     wk.FB = sw.soi ? (double*)carve(nn * 4 * (size_t)(Kmax + 1) * sw.nz * L * sizeof(double)) : nullptr;
+    wk.FS = sw.soi && sw.kstate
+                ? (double*)carve(nn * (size_t)sw.soi_slots * 2 * (Kmax + 1) * sw.nz * L * sizeof(double))
+                : nullptr;
     wk.AS = sw.kstate ? (double*)carve(nn * (size_t)(Kmax + 1) * (sw.nz * sw.nz + sw.nz) * L * sizeof(double))
                       : nullptr;
     wk.TODc = sw.kstate ? (R*)carve(nn * Kmax * L * sizeof(R)) : nullptr;
@@ -730,7 +736,7 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
   const int nv = 1 + oa.n;
   // scattering: NZ angles of the kernels (16-stream option or the stream rule)
   const bool nz_max = scat && b->n_streams != nullptr;
-  const bool soi = mode == 3 && b->rt_algorithm_id != nullptr;
+  const bool soi = scat && b->rt_algorithm_id != nullptr;
   // scattering Jacobian outputs that the caller asked for
   double* o_wc = nullptr, *o_re = nullptr, *o_cf = nullptr, *o_ac = nullptr, *o_ar = nullptr;
   if (mode == 1) {
@@ -748,6 +754,7 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
     sw.nz = nz_max ? SC_NZ_MAX : 5;
     sw.soi = soi;
     sw.kstate = mode != 3;
+    sw.soi_slots = soi && sw.kstate ? h->soi_slots : 0;
     sw.rec = nz_max ? layer_record<SC_NZ_MAX>() : layer_record<5>();
     if (sw.kstate && (o_wc || o_re || o_cf || o_ac || o_ar)) sw.slots = NCb + NAb;
     sw.cf = sw.kstate && o_cf != nullptr;
@@ -840,7 +847,7 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       sa.b = bv; sa.sp = s.spec; sa.pv = w.pv; sa.lut = h->lut;
       sa.max_clouds = b->max_clouds; sa.n_clouds = b->n_clouds; sa.cloud_type = b->cloud_type;
       sa.wc = b->cloud_water_content; sa.reff = b->cloud_effective_radius; sa.n_streams = b->n_streams;
-      sa.rt_algorithm = b->rt_algorithm_id; sa.FB = w.FB;
+      sa.rt_algorithm = b->rt_algorithm_id; sa.FB = w.FB; sa.FS = w.FS; sa.soi_slots = sw.soi_slots;
       sa.alut = h->alut; sa.max_aerosols = b->max_aerosols > 0 ? b->max_aerosols : 0;
       sa.n_aerosols = b->n_aerosols; sa.aerosol_type = b->aerosol_type;
       sa.conc = b->aerosol_concentration; sa.aer_reff = b->aerosol_effective_radius;
@@ -880,9 +887,9 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
           {
             StageScope sc(h, 7, st);
             if (nz_max)
-              launch_scatter_kmatrix<SC_NZ_MAX>(sa, ga, st);
+              launch_scatter_kmatrix<SC_NZ_MAX>(sa, ga, st, soi);
             else
-              launch_scatter_kmatrix<5>(sa, ga, st);
+              launch_scatter_kmatrix<5>(sa, ga, st, soi);
             CK_LAUNCH(h);
           }
           {
@@ -1257,8 +1264,8 @@ int check_call(crtm_gpu_handle h, const crtm_gpu_batch* b, const crtm_gpu_rtsolu
     if (cudaMemcpy(&code, h->d_error, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
       return fail(h, "cannot read the scattering error flag");
     if (code) return fail(h, "scattering radiative transfer failed (code %d: 1-3 stream set, 4 cloud type, "
-                             "5-6 singular matrix, 8 aerosol stream set or LUT, 9 aerosol type, 10 K-matrix or adjoint "
-                             "requested with RT_SOI, 11 invalid Options%Overlap_Id)", code);
+                             "5-6 singular matrix, 8 aerosol stream set or LUT, 9 aerosol type, 11 invalid "
+                             "Options%Overlap_Id, 12 SOI order-field slots below 17)", code);
   }
   if (rts->status)
     for (int m = 0; m < b->n_profiles; m++)
@@ -1435,6 +1442,11 @@ int crtm_gpu_init(const char* coeff_path, int n_sensors, const char* const* sens
     const int v = atoi(e);
     if (v == 8 || v == 16 || v == 32) h->map_channels = v;
   }
+  if (const char* e = getenv("CRTM_GPU_SOI_SLOTS")) {
+    const int v = atoi(e);
+    if (v >= 17 && v <= 75) h->soi_slots = v;
+  }
+
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&h->order_event, cudaEventDisableTiming) != cudaSuccess) {
     delete h;

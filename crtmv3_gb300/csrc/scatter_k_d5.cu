@@ -18,8 +18,9 @@ void launch_scatter_layers_k(const ScatterArgs<double>& a, unsigned grid, cudaSt
 }
 
 template <int NZ>
-void launch_scatter_kmatrix(const ScatterArgs<double>& a, dim3 grid, cudaStream_t st) {
+void launch_scatter_kmatrix(const ScatterArgs<double>& a, dim3 grid, cudaStream_t st, bool soi) {
   scatter_kmatrix_kernel<NZ, double><<<grid, SCATTER_THREADS, 0, st>>>(a);
+  if (soi) scatter_soi_k_kernel<NZ><<<grid, SCATTER_THREADS, 0, st>>>(a);
 }
 
 template <int NZ, class C>
@@ -28,7 +29,7 @@ void launch_scatter_contract(const ScatterArgs<double>& a, unsigned grid, cudaSt
 }
 
 template void launch_scatter_layers_k<5, double>(const ScatterArgs<double>&, unsigned, cudaStream_t);
-template void launch_scatter_kmatrix<5>(const ScatterArgs<double>&, dim3, cudaStream_t);
+template void launch_scatter_kmatrix<5>(const ScatterArgs<double>&, dim3, cudaStream_t, bool);
 template void launch_scatter_contract<5, double>(const ScatterArgs<double>&, unsigned, cudaStream_t);
 
 }  // namespace crtm

@@ -15,8 +15,8 @@
 // LB[p][k][e][l], e = 0 kind (0 clear, 1 scattering, <0 error), 1 optical
 // depth, then T (NZ*NZ), R (NZ*NZ) and the source (NZ).
 //
-// K-matrix and adjoint of scattering profiles (ADA).  After the first column
-// launch and scatter_layers_kernel (the forward layer records):
+// K-matrix and adjoint of scattering profiles.  After the first column launch
+// and scatter_layers_kernel (the forward layer records):
 //
 //   scatter_kmatrix_kernel   one thread per (profile, channel): the adding
 //                            from the surface with the level states kept in
@@ -25,6 +25,9 @@
 //                            kind, od_b, B_b, then T_b, R_b, src_b) and the
 //                            cloudy radiance, its surface derivatives and the
 //                            clear-column radiance of a fractional profile (CB).
+//   scatter_soi_k_kernel     the same for the SOI profiles: the orders of
+//                            interaction with their fields kept (FS), then
+//                            their adjoint from the last order down.
 //   scatter_contract_kernel  one thread per (profile, layer, channel): the
 //                            layer optics on derivative numbers (gas optical
 //                            depth, temperature, and each active cloud or
@@ -73,7 +76,10 @@ struct ScatterArgs {
   const int* n_aerosols;        // [P] (null when max_aerosols = 0)
   const int* aerosol_type;      // [P][NA]
   const double* conc, *aer_reff;   // [P][NA][Kmax]
-  double* FB;                   // SOI fields [n][2][2][Kmax+1][NZ][L], or null
+  double* FB;                   // SOI fields [n][2][2][Kmax+1][NZ][L], or null (K-matrix/adjoint:
+                                // the orders' adjoint fields)
+  double* FS;                   // SOI K-matrix/adjoint: [n][soi_slots][2][Kmax+1][NZ][L] order fields
+  int soi_slots;
   const R* TAU;                 // [n][Kmax][L] gas layer optical depths
   R* LB;                        // [n][Kmax][NE][L] layer records (forward)
   double* LBK;                  // [n][Kmax][NE][L] layer records of the K-matrix / adjoint, FP64 in
@@ -318,29 +324,31 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_soi_kernel(ScatterArg
   code = stream_set<NZ, double>(c.nleg, c.mu_sensor, c.n_clouds > 0 ? a.lut.nleg : -1, c_gauss, S);
   if (!code) {
     const int nZ = S.nZ;
-    auto layer = [&](int k, int* kind, double* od, double* B, Mat<NZ, double>& Tm, Mat<NZ, double>& Rm,
-                     double* src) {
-      const R* rec = a.LB + ((size_t)p * Kmax + k) * NE * L + l;
-      *kind = (int)rec[0];
-      *od = double(rec[(size_t)L]);
-      const double tk = c.temperature[k];
-      *B = c.c1 / (exp(c.c2 / (c.b1 + c.b2 * tk)) - 1.0);
-      if (*kind != 1) return;
-      for (int i = 0; i < nZ; i++) {
+    const R* rec0 = a.LB + (size_t)p * Kmax * NE * L + l;
+    auto rec = [&](int k, int e) { return double(rec0[((size_t)k * NE + e) * L]); };
+    auto lod = [&](int k, int* kind, double* od, double* B) {
+      *kind = (int)rec(k, 0);
+      *od = rec(k, 1);
+      *B = c.c1 / (exp(c.c2 / (c.b1 + c.b2 * c.temperature[k])) - 1.0);
+    };
+    auto lsrc = [&](int k, double* src) {
+      for (int i = 0; i < nZ; i++) src[i] = rec(k, 2 + 2 * NZ * NZ + i);
+    };
+    auto ltr = [&](int k, Mat<NZ, double>& Tm, Mat<NZ, double>& Rm) {
+      for (int i = 0; i < nZ; i++)
         for (int j = 0; j < nZ; j++) {
-          Tm.a[i][j] = double(rec[(size_t)(2 + i * NZ + j) * L]);
-          Rm.a[i][j] = double(rec[(size_t)(2 + NZ * NZ + i * NZ + j) * L]);
+          Tm.a[i][j] = rec(k, 2 + i * NZ + j);
+          Rm.a[i][j] = rec(k, 2 + NZ * NZ + i * NZ + j);
         }
-        src[i] = double(rec[(size_t)(2 + 2 * NZ * NZ + i) * L]);
-      }
     };
     double* fb = a.FB + (size_t)p * 4 * (Kmax + 1) * NZ * L + l;
-    const size_t lev = (size_t)NZ * L, buf = (size_t)(Kmax + 1) * lev;
-    auto dn = [&](int k, int i, int b) -> double& { return fb[b * buf + k * lev + (size_t)i * L]; };
-    auto up = [&](int k, int i, int b) -> double& { return fb[(2 + b) * buf + k * lev + (size_t)i * L]; };
+    auto fld = [&](int b, int f, int k, int i) -> double& {
+      return fb[(((size_t)(2 * f + b) * (Kmax + 1) + k) * NZ + i) * L];
+    };
     for (int k = 0; k < c.Ku && !code; k++)
-      if ((int)a.LB[((size_t)p * Kmax + k) * NE * L + l] < 0) code = -(int)a.LB[((size_t)p * Kmax + k) * NE * L + l];
-    if (!code) soi_solve<NZ>(nZ, c.Ku, S.isat, S.mu, c.emissivity, c.planck_surface, c.cosmic, layer, dn, up, &rad);
+      if ((int)rec(k, 0) < 0) code = -(int)rec(k, 0);
+    if (!code)
+      soi_solve<NZ>(nZ, c.Ku, S.isat, S.mu, c.emissivity, c.planck_surface, c.cosmic, lod, lsrc, ltr, fld, &rad);
     const double tcc = a.cover[p];
     if (!code && tcc >= 0.0)
       rad = (1.0 - tcc) * clear_column_radiance(c, a.TAU + (size_t)p * Kmax * L + l, L) + tcc * rad;
@@ -363,11 +371,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_kmatrix_kernel(Scatte
   if (l >= L || a.pv.status[p] != 0) return;
   const CloudyColumn c = column_inputs(a, p, gp, l);
   if (c.n_clouds == 0 && c.n_aerosols == 0) return;   // clear: the column kernel's Emission adjoint
-  if (c.soi) {   // the SOI K-matrix is not built
-    atomicCAS(a.error, 0, 10);
-    if (a.status) atomicOr(a.status + gp, 1 << 4);
-    return;
-  }
+  if (c.soi) return;                                   // scatter_soi_k_kernel
   double rad = 0.0, e_b = 0.0, Bs_b = 0.0;
   StreamSet<NZ, double> S;
   int code = stream_set<NZ, double>(c.nleg, c.mu_sensor, c.n_clouds > 0 ? a.lut.nleg : -1, c_gauss, S);
@@ -420,6 +424,72 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_kmatrix_kernel(Scatte
   cb[3 * (size_t)L] = a.cover[p] >= 0.0 ? clear_column_radiance(c, a.TAU + (size_t)p * Kmax * L + l, L) : 0.0;
 }
 
+// K-matrix / adjoint of the SOI profiles (Options%RT_Algorithm_Id = RT_SOI),
+// one thread per (profile, channel): the orders of interaction over the FP64
+// layer records with every order's fields kept in FS (checkpoints and
+// recomputation beyond soi_slots orders), then their adjoint from the last
+// order down into the record adjoints (LBA) and CB, as scatter_kmatrix_kernel
+// does for ADA.
+template <int NZ>
+__global__ void __launch_bounds__(SCATTER_THREADS) scatter_soi_k_kernel(ScatterArgs<double> a) {
+  constexpr int NE = layer_record<NZ>();
+  const int L = a.L, Kmax = a.Kmax;
+  const int p = blockIdx.y, gp = a.p_begin + p;
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= L || a.pv.status[p] != 0) return;
+  const CloudyColumn c = column_inputs(a, p, gp, l);
+  if ((c.n_clouds == 0 && c.n_aerosols == 0) || !c.soi) return;
+  double rad = 0.0, e_b = 0.0, Bs_b = 0.0;
+  StreamSet<NZ, double> S;
+  int code = stream_set<NZ, double>(c.nleg, c.mu_sensor, c.n_clouds > 0 ? a.lut.nleg : -1, c_gauss, S);
+  const double* rec0 = a.LBK + (size_t)p * Kmax * NE * L + l;
+  auto rec = [&](int k, int e) { return rec0[((size_t)k * NE + e) * L]; };
+  for (int k = 0; k < c.Ku && !code; k++)
+    if ((int)rec(k, 0) < 0) code = -(int)rec(k, 0);
+  if (!code) {
+    const int nZ = S.nZ;
+    auto lod = [&](int k, int* kind, double* od, double* B) {
+      *kind = (int)rec(k, 0);
+      *od = rec(k, 1);
+      *B = c.c1 / (exp(c.c2 / (c.b1 + c.b2 * c.temperature[k])) - 1.0);
+    };
+    auto lsrc = [&](int k, double* src) {
+      for (int i = 0; i < nZ; i++) src[i] = rec(k, 2 + 2 * NZ * NZ + i);
+    };
+    auto ltr = [&](int k, Mat<NZ, double>& Tm, Mat<NZ, double>& Rm) {
+      for (int i = 0; i < nZ; i++)
+        for (int j = 0; j < nZ; j++) {
+          Tm.a[i][j] = rec(k, 2 + i * NZ + j);
+          Rm.a[i][j] = rec(k, 2 + NZ * NZ + i * NZ + j);
+        }
+    };
+    const size_t lev = (size_t)NZ * L, fsz = (size_t)(Kmax + 1) * lev;
+    double* fs = a.FS + (size_t)p * a.soi_slots * 2 * fsz + l;
+    double* fb = a.FB + (size_t)p * 4 * fsz + l;
+    auto fld = [&](int sl, int f, int k, int i) -> double& {
+      return fs[(size_t)(2 * sl + f) * fsz + k * lev + (size_t)i * L];
+    };
+    auto lam = [&](int b, int f, int k, int i) -> double& {
+      return fb[(size_t)(2 * b + f) * fsz + k * lev + (size_t)i * L];
+    };
+    double* rb = a.LBA + (size_t)p * Kmax * NE * L + l;
+    auto ab = [&](int k, int e) -> double& { return rb[((size_t)k * NE + e) * L]; };
+    code = soi_adjoint<NZ>(nZ, c.Ku, S.isat, S.mu, c.emissivity, c.planck_surface, c.cosmic, a.soi_slots, lod, lsrc,
+                           ltr, fld, lam, ab, &rad, &e_b, &Bs_b);
+  }
+  if (code) {
+    atomicCAS(a.error, 0, code);
+    if (a.status) atomicOr(a.status + gp, 1 << 4);
+    rad = e_b = Bs_b = 0.0;
+    for (int k = 0; k < c.Ku; k++) a.LBA[((size_t)p * Kmax + k) * NE * L + l] = -1.0;
+  }
+  double* cb = a.CB + (size_t)p * 4 * L + l;
+  cb[0] = rad;
+  cb[(size_t)L] = e_b;
+  cb[2 * (size_t)L] = Bs_b;
+  cb[3 * (size_t)L] = a.cover[p] >= 0.0 ? clear_column_radiance(c, a.TAU + (size_t)p * Kmax * L + l, L) : 0.0;
+}
+
 // Active species of layer k (clouds above the water-content threshold after
 // the cover scaling and not dropped, aerosols above theirs for non-microwave
 // sensors), as seed indices of layer_optics.
@@ -456,7 +526,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_contract_kernel(Scatt
     }
   const double* rb = a.LBA + ((size_t)p * Kmax + k) * NE * L + l;
   const int kind = (int)rb[0];
-  if (kind < 0 || c.soi) {
+  if (kind < 0) {
     a.TODc[kl] = R(0);
     a.PT[kl] = R(0);
     return;

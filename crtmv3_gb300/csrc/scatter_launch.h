@@ -22,8 +22,9 @@ inline int scatter_k_set_gauss(const GaussTable& g) {
 
 template <int NZ, class C>
 void launch_scatter_layers_k(const ScatterArgs<double>& a, unsigned grid, cudaStream_t st);
+// the ADA adding adjoint, then (soi) the SOI orders' adjoint of the SOI profiles
 template <int NZ>
-void launch_scatter_kmatrix(const ScatterArgs<double>& a, dim3 grid, cudaStream_t st);
+void launch_scatter_kmatrix(const ScatterArgs<double>& a, dim3 grid, cudaStream_t st, bool soi);
 template <int NZ, class C>
 void launch_scatter_contract(const ScatterArgs<double>& a, unsigned grid, cudaStream_t st);
 

@@ -536,58 +536,58 @@ CRTM_HD void phase_blocks(int nS, int nZ, int nleg, const T* pc, const T (*P)[SC
 // I + R R in place of (I - R R)^-1; CRTM_Doubling_layer :1091-1234 inverts):
 // from a first-order layer of optical depth tau / 2^n, n doublings give the
 // layer's transmission T, reflection R and thermal source.
-template <int NZ>
-CRTM_HD bool soi_doubling(bool trunc, int nS, int nZ, double w, double tau, const double* mu, const double* wt,
-                          const Mat<NZ, double>& ff, const Mat<NZ, double>& bb, double B, Mat<NZ, double>& Tm,
-                          Mat<NZ, double>& Rm, double* src) {
+template <int NZ, class T>
+CRTM_HD bool soi_doubling(bool trunc, int nS, int nZ, T w, T tau, const T* mu, const T* wt,
+                          const Mat<NZ, T>& ff, const Mat<NZ, T>& bb, T B, Mat<NZ, T>& Tm,
+                          Mat<NZ, T>& Rm, T* src) {
   if (tau < 1.0e-6) {   // OPTICAL_DEPTH_THRESHOLD: transparent, no source
     for (int i = 0; i < nZ; i++) {
-      src[i] = 0.0;
-      for (int j = 0; j < nZ; j++) { Tm.a[i][j] = (i == j) ? 1.0 : 0.0; Rm.a[i][j] = 0.0; }
+      src[i] = T(0.0);
+      for (int j = 0; j < nZ; j++) { Tm.a[i][j] = T((i == j) ? 1.0 : 0.0); Rm.a[i][j] = T(0.0); }
     }
     return true;
   }
-  int nd = (int)(log(tau / DELTA_OPTICAL_DEPTH) / log(2.0)) + 1;
+  int nd = (int)(log(value_of(tau) / DELTA_OPTICAL_DEPTH) / log(2.0)) + 1;
   if (nd < 1) nd = 1;
-  double dt;
+  T dt;
   if (nd <= 55) {                      // MAX_N_DOUBLING
     dt = tau;
-    for (int i = 0; i < nd; i++) dt *= 0.5;
+    for (int i = 0; i < nd; i++) dt = dt * 0.5;
   } else {
     nd = 55;
-    dt = DELTA_OPTICAL_DEPTH;
+    dt = T(DELTA_OPTICAL_DEPTH);
   }
-  const double s = dt * w;
+  const T s = dt * w;
   for (int i = 0; i < nZ; i++) {
-    const double c = s / mu[i];
+    const T c = s / mu[i];
     for (int j = 0; j < nZ; j++) {
       Rm.a[i][j] = c * bb.a[i][j] * wt[j];
-      Tm.a[i][j] = c * ff.a[i][j] * wt[j] + (i == j ? 1.0 - dt / mu[i] : 0.0);
+      Tm.a[i][j] = c * ff.a[i][j] * wt[j] + (i == j ? 1.0 - dt / mu[i] : T(0.0));
     }
   }
-  Mat<NZ, double> G, A, Bq;
+  Mat<NZ, T> G, A, Bq;
   for (int L = 0; L < nd; L++) {
-    mat_mul<NZ, double>(nZ, Rm, Rm, G);
+    mat_mul<NZ, T>(nZ, Rm, Rm, G);
     for (int i = 0; i < nZ; i++)
-      for (int j = 0; j < nZ; j++) G.a[i][j] = (trunc ? G.a[i][j] : -G.a[i][j]) + (i == j ? 1.0 : 0.0);
-    if (!trunc && !mat_invert<NZ, double>(nZ, G)) {
+      for (int j = 0; j < nZ; j++) G.a[i][j] = (trunc ? G.a[i][j] : -G.a[i][j]) + T(i == j ? 1.0 : 0.0);
+    if (!trunc && !mat_invert<NZ, T>(nZ, G)) {
       // the reference falls back to the clear layer
       for (int i = 0; i < nZ; i++) {
-        src[i] = 0.0;
-        for (int j = 0; j < nZ; j++) { Tm.a[i][j] = (i == j) ? exp(-tau / mu[i]) : 0.0; Rm.a[i][j] = 0.0; }
+        src[i] = T(0.0);
+        for (int j = 0; j < nZ; j++) { Tm.a[i][j] = (i == j) ? exp(-tau / mu[i]) : T(0.0); Rm.a[i][j] = T(0.0); }
       }
       return true;
     }
-    mat_mul<NZ, double>(nZ, Tm, G, A);    // term2 = T (I -/+ R R)^(-1 or +1)
-    mat_mul<NZ, double>(nZ, A, Rm, G);    // term2 R
-    mat_mul<NZ, double>(nZ, G, Tm, Bq);   // term2 R T
+    mat_mul<NZ, T>(nZ, Tm, G, A);    // term2 = T (I -/+ R R)^(-1 or +1)
+    mat_mul<NZ, T>(nZ, A, Rm, G);    // term2 R
+    mat_mul<NZ, T>(nZ, G, Tm, Bq);   // term2 R T
     for (int i = 0; i < nZ; i++)
       for (int j = 0; j < nZ; j++) Rm.a[i][j] += Bq.a[i][j];
-    mat_mul<NZ, double>(nZ, A, Tm, G);
+    mat_mul<NZ, T>(nZ, A, Tm, G);
     Tm = G;
   }
   for (int i = 0; i < nZ; i++) {
-    double c1 = 0.0, c2 = 0.0;
+    T c1 = T(0.0), c2 = T(0.0);
     for (int j = 0; j < nS; j++) { c1 += Tm.a[i][j]; c2 += Rm.a[i][j]; }
     if (i == nZ - 1 && nZ == nS + 1) c1 += Tm.a[i][i];
     src[i] = (1.0 - c1 - c2) * B;
@@ -810,20 +810,8 @@ CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const Stre
   phase_blocks<NZ, S>(St.nS, St.nZ, nleg, pcs, P, wt, ff, bb);
   const S B = in.c1 / (exp(in.c2 / (in.b1 + in.b2 * tk)) - 1.0);
   if (in.soi) {   // SOI: doubling, then the direct beam taken out of the diagonal
-    Mat<NZ, double> ffd, bbd, Tdd, Rdd;
-    double mud[NZ], wtd[NZ], srd[NZ];
-    for (int i = 0; i < St.nZ; i++) {
-      mud[i] = St.mu[i];
-      wtd[i] = St.wt[i];
-      for (int j = 0; j < St.nZ; j++) { ffd.a[i][j] = value_of(ff.a[i][j]); bbd.a[i][j] = value_of(bb.a[i][j]); }
-    }
-    const double odv = value_of(od), ssav = value_of(ssa);
-    soi_doubling<NZ>(ssav < 0.8 && odv < 4.0, St.nS, St.nZ, ssav, odv, mud, wtd, ffd, bbd, value_of(B), Tdd, Rdd, srd);
-    for (int i = 0; i < St.nZ; i++) {
-      Tdd.a[i][i] -= ::exp(-odv / mud[i]);
-      srcd[i] = S(srd[i]);
-      for (int j = 0; j < St.nZ; j++) { Td.a[i][j] = S(Tdd.a[i][j]); Rd.a[i][j] = S(Rdd.a[i][j]); }
-    }
+    soi_doubling<NZ, S>(ssa < 0.8 && od < 4.0, St.nS, St.nZ, ssa, od, mu, wt, ff, bb, B, Td, Rd, srcd);
+    for (int i = 0; i < St.nZ; i++) Td.a[i][i] -= exp(-od / mu[i]);
   } else {
     S mx = S(0.0);
     for (int i = 0; i < St.nZ; i++)
@@ -1068,59 +1056,235 @@ CRTM_HD bool adding_scatter_adjoint(int nZ, const Mat<NZ, double>& Tm, const Mat
   return true;
 }
 
-// CRTM_SOI (SOI_Module.f90:63-283): successive orders of interaction.  Order
-// 1 carries the thermal sources, the surface emission and the cosmic
+// One order of interaction n (1-based) of CRTM_SOI (SOI_Module.f90:63-283):
+// the order's downwelling and upwelling fields go to field slot cur, computed
+// from the previous order's in slot prev (not read for n = 1).  Order 1
+// carries the thermal sources, the surface emission and the cosmic
 // background; each later order scatters the previous order's diffuse fields
-// through the layers' T and R.  Stops when the newest order adds less than
-// 1e-4 of the radiance (at least 2 orders, at most 75).  Field storage is the
-// caller's: dn(k, i, b) / up(k, i, b) give level k, angle i, buffer b (0/1).
-template <int NZ, class LayerFn, class DnFn, class UpFn>
-CRTM_HD int soi_solve(int nZ, int Ku, int isat, const double* mu, double emissivity, double planck_surface,
-                      double cosmic, LayerFn layer, DnFn dn, UpFn up, double* radiance) {
-  // layer(k, &kind, &od, &B, T, R, src): kind 0 clear, 1 scattering
-  double total = 0.0, change = 1.0e10;
-  int niter = 0, cur = 0;
+// through the layers' T (direct beam removed) and R; between scattering events
+// the fields propagate with the direct transmission exp(-od / mu).
+// lod(k, &kind, &od, &B) gives layer k's kind (0 clear, 1 scattering), optical
+// depth and Planck radiance; lsrc(k, src) and ltr(k, T, R) its source and
+// matrices (scattering layers).  fld(slot, f, k, i): field f (0 down, 1 up) at
+// level k (0 top, Ku surface), angle i.  Returns the order's upwelling
+// radiance at the top in the sensor angle.
+template <int NZ, class LodFn, class SrcFn, class TrFn, class FldFn>
+CRTM_HD double soi_order(int n, int cur, int prev, int nZ, int Ku, int isat, const double* mu,
+                         double emissivity, double planck_surface, double cosmic, LodFn lod, SrcFn lsrc,
+                         TrFn ltr, FldFn fld) {
   Mat<NZ, double> Tm, Rm;
-  double src[NZ], etr[NZ];
-  while ((change > 1.0e-4 && niter + 1 <= 75) || niter < 2) {
-    niter++;
-    const int prev = cur ^ 1;
-    if (niter == 1) cur = 0;
-    for (int i = 0; i < nZ; i++) dn(0, i, cur) = niter == 1 ? cosmic : 0.0;
-    for (int k = 0; k < Ku; k++) {
+  double sv[NZ], etr[NZ];
+  for (int i = 0; i < nZ; i++) fld(cur, 0, 0, i) = n == 1 ? cosmic : 0.0;
+  for (int dir = 0; dir < 2; dir++) {   // down from the top, then up from the surface
+    if (dir == 1)
+      for (int i = 0; i < nZ; i++)
+        fld(cur, 1, Ku, i) = (1.0 - emissivity) * fld(cur, 0, Ku, i) + (n == 1 ? emissivity * planck_surface : 0.0);
+    for (int m = 0; m < Ku; m++) {
+      const int k = dir == 0 ? m : Ku - 1 - m;
       int kind;
       double od, B;
-      layer(k, &kind, &od, &B, Tm, Rm, src);
+      lod(k, &kind, &od, &B);
       for (int i = 0; i < nZ; i++) etr[i] = exp(-od / mu[i]);
-      for (int i = 0; i < nZ; i++) {
-        double sv = 0.0;
-        if (niter == 1) sv = kind == 1 ? src[i] : B * (1.0 - etr[i]);
-        else if (kind == 1 && od >= 1.0e-6)
-          for (int j = 0; j < nZ; j++) sv += Tm.a[i][j] * dn(k, j, prev) + Rm.a[i][j] * up(k + 1, j, prev);
-        dn(k + 1, i, cur) = dn(k, i, cur) * etr[i] + sv;
+      if (n == 1) {
+        if (kind == 1)
+          lsrc(k, sv);
+        else
+          for (int i = 0; i < nZ; i++) sv[i] = B * (1.0 - etr[i]);
+      } else if (kind == 1 && od >= 1.0e-6) {
+        ltr(k, Tm, Rm);
+        const Mat<NZ, double>& A = dir == 0 ? Tm : Rm;   // acts on the downwelling field above
+        const Mat<NZ, double>& C = dir == 0 ? Rm : Tm;   // acts on the upwelling field below
+        for (int i = 0; i < nZ; i++) {
+          double v = 0.0;
+          for (int j = 0; j < nZ; j++) v += A.a[i][j] * fld(prev, 0, k, j) + C.a[i][j] * fld(prev, 1, k + 1, j);
+          sv[i] = v;
+        }
+      } else {
+        for (int i = 0; i < nZ; i++) sv[i] = 0.0;
       }
+      if (dir == 0)
+        for (int i = 0; i < nZ; i++) fld(cur, 0, k + 1, i) = fld(cur, 0, k, i) * etr[i] + sv[i];
+      else
+        for (int i = 0; i < nZ; i++) fld(cur, 1, k, i) = fld(cur, 1, k + 1, i) * etr[i] + sv[i];
     }
-    for (int i = 0; i < nZ; i++)
-      up(Ku, i, cur) = (1.0 - emissivity) * dn(Ku, i, cur) + (niter == 1 ? emissivity * planck_surface : 0.0);
-    for (int k = Ku - 1; k >= 0; k--) {
-      int kind;
-      double od, B;
-      layer(k, &kind, &od, &B, Tm, Rm, src);
-      for (int i = 0; i < nZ; i++) etr[i] = exp(-od / mu[i]);
-      for (int i = 0; i < nZ; i++) {
-        double sv = 0.0;
-        if (niter == 1) sv = kind == 1 ? src[i] : B * (1.0 - etr[i]);
-        else if (kind == 1 && od >= 1.0e-6)
-          for (int j = 0; j < nZ; j++) sv += Rm.a[i][j] * dn(k, j, prev) + Tm.a[i][j] * up(k + 1, j, prev);
-        up(k, i, cur) = up(k + 1, i, cur) * etr[i] + sv;
-      }
-    }
-    const double rad = up(0, isat, cur);
+  }
+  return fld(cur, 1, 0, isat);
+}
+
+// CRTM_SOI: orders until the newest adds less than 1e-4 of the radiance (at
+// least 2, at most 75: MAX_N_SOI_ITERATIONS), fields in two slots.
+constexpr int SOI_MAX_ORDERS = 75;
+template <int NZ, class LodFn, class SrcFn, class TrFn, class FldFn>
+CRTM_HD int soi_solve(int nZ, int Ku, int isat, const double* mu, double emissivity, double planck_surface,
+                      double cosmic, LodFn lod, SrcFn lsrc, TrFn ltr, FldFn fld, double* radiance) {
+  double total = 0.0, change = 1.0e10;
+  int n = 0;
+  while ((change > 1.0e-4 && n + 1 <= SOI_MAX_ORDERS) || n < 2) {
+    n++;
+    const double rad = soi_order<NZ>(n, (n - 1) & 1, n & 1, nZ, Ku, isat, mu, emissivity, planck_surface, cosmic,
+                                     lod, lsrc, ltr, fld);
     total += rad;
     change = rad / total;
-    cur ^= 1;
   }
   *radiance = total;
+  return 0;
+}
+
+// Adjoint of the SOI for a unit radiance seed (CRTM_SOI_AD,
+// SOI_Module.f90:477-): every order of interaction is linear in the previous
+// order's fields, so the reverse runs from the last order down, each order's
+// fields' adjoints collecting the seed (its share of the radiance), the next
+// order's scattering sources and the propagation.  Accumulates into
+// ab(k, e) layer k's record adjoints in the record layout (e = 0 kind, 1 od_b,
+// then T_b, R_b, src_b for a scattering layer, 2 the Planck radiance's B_b for
+// a clear one) and returns the radiance, dR/de and dR/d(surface Planck).
+//
+// Field storage: n_slots order fields fld(slot, ...) (at least 17) and two
+// adjoint fields lam(b, f, k, i), b = 0, 1.  With the orders' count N at most
+// n_slots every order is kept; beyond, orders c, 2c, ... are kept as
+// checkpoints (c the smallest with (N-1)/c + c <= n_slots) and each segment
+// of c orders is recomputed from its checkpoint before its reverse.
+template <int NZ, class LodFn, class SrcFn, class TrFn, class FldFn, class LamFn, class AbFn>
+CRTM_HD int soi_adjoint(int nZ, int Ku, int isat, const double* mu, double emissivity, double planck_surface,
+                        double cosmic, int n_slots, LodFn lod, SrcFn lsrc, TrFn ltr, FldFn fld, LamFn lam,
+                        AbFn ab, double* radiance, double* e_b, double* Bs_b, int* n_orders = nullptr) {
+  constexpr int NE_T = 2, NE_R = 2 + NZ * NZ, NE_S = 2 + 2 * NZ * NZ;
+  if (n_slots < 17) return 12;
+  // forward: orders into slots 0..n_slots-1, beyond that alternately into the last two
+  const int M = n_slots;
+  auto slot1 = [&](int n) { return n <= M ? n - 1 : M - 1 - ((n - M) & 1); };
+  double total = 0.0, change = 1.0e10;
+  int N = 0;
+  while ((change > 1.0e-4 && N + 1 <= SOI_MAX_ORDERS) || N < 2) {
+    N++;
+    const double rad = soi_order<NZ>(N, slot1(N), N > 1 ? slot1(N - 1) : 0, nZ, Ku, isat, mu, emissivity,
+                                     planck_surface, cosmic, lod, lsrc, ltr, fld);
+    total += rad;
+    change = rad / total;
+  }
+  *radiance = total;
+  if (n_orders) *n_orders = N;
+  // segments: c orders each, checkpoints at orders c, 2c, ..., nck c
+  int c = N, nck = 0;
+  if (N > M) {
+    for (c = 2; c <= N; c++)
+      if ((N - 1) / c + c <= M) break;
+    nck = (N - 1) / c;
+  }
+  auto slot2 = [&](int n) { return (n % c == 0 && n / c <= nck) ? n / c - 1 : nck + (n - 1) % c; };
+  auto slot = [&](int n) { return N <= M ? n - 1 : slot2(n); };
+  auto order_into = [&](int n) {
+    soi_order<NZ>(n, slot(n), n > 1 ? slot(n - 1) : 0, nZ, Ku, isat, mu, emissivity, planck_surface, cosmic, lod,
+                  lsrc, ltr, fld);
+  };
+  if (N > M)
+    for (int n = 1; n <= nck * c; n++) order_into(n);   // the checkpoints
+  // record adjoints and adjoint fields start at zero
+  for (int k = 0; k < Ku; k++) {
+    int kind;
+    double od, B;
+    lod(k, &kind, &od, &B);
+    ab(k, 0) = kind;
+    ab(k, 1) = 0.0;
+    if (kind == 1) {
+      for (int i = 0; i < nZ; i++) {
+        for (int j = 0; j < nZ; j++) { ab(k, NE_T + i * NZ + j) = 0.0; ab(k, NE_R + i * NZ + j) = 0.0; }
+        ab(k, NE_S + i) = 0.0;
+      }
+    } else {
+      ab(k, 2) = 0.0;
+    }
+  }
+  for (int b = 0; b < 2; b++)
+    for (int f = 0; f < 2; f++)
+      for (int k = 0; k <= Ku; k++)
+        for (int i = 0; i < nZ; i++) lam(b, f, k, i) = 0.0;
+  double eb = 0.0, bsb = 0.0;
+  Mat<NZ, double> Tm, Rm;
+  double etr[NZ], sd[NZ], su[NZ];
+  for (int s = nck; s >= 0; s--) {
+    const int a0 = s * c + 1, b0 = s == nck ? N : (s + 1) * c;
+    if (N > M)
+      for (int n = a0; n <= b0; n++) order_into(n);
+    for (int n = b0; n >= a0; n--) {
+      const int cur = slot(n), prv = n > 1 ? slot(n - 1) : 0, lc = n & 1, lp = lc ^ 1;
+      lam(lc, 1, 0, isat) += 1.0;
+      // up(k) = up(k+1) etr + sv_up(k), k = Ku-1 .. 0
+      for (int k = 0; k < Ku; k++) {
+        int kind;
+        double od, B;
+        lod(k, &kind, &od, &B);
+        double g = 0.0;
+        for (int i = 0; i < nZ; i++) {
+          const double e = exp(-od / mu[i]), lu = lam(lc, 1, k, i);
+          lam(lc, 1, k + 1, i) += lu * e;
+          g += lu * fld(cur, 1, k + 1, i) * e / mu[i];
+        }
+        ab(k, 1) -= g;
+      }
+      // surface: up(Ku) = (1 - e) dn(Ku) + [n = 1] e Bs
+      for (int i = 0; i < nZ; i++) {
+        const double lu = lam(lc, 1, Ku, i);
+        lam(lc, 0, Ku, i) += (1.0 - emissivity) * lu;
+        eb += lu * ((n == 1 ? planck_surface : 0.0) - fld(cur, 0, Ku, i));
+        if (n == 1) bsb += emissivity * lu;
+      }
+      // dn(k+1) = dn(k) etr + sv_dn(k), k = 0 .. Ku-1; then the sources of layer k
+      for (int k = Ku - 1; k >= 0; k--) {
+        int kind;
+        double od, B;
+        lod(k, &kind, &od, &B);
+        double g = 0.0;
+        for (int i = 0; i < nZ; i++) {
+          etr[i] = exp(-od / mu[i]);
+          const double ld = lam(lc, 0, k + 1, i);
+          lam(lc, 0, k, i) += ld * etr[i];
+          g += ld * fld(cur, 0, k, i) * etr[i] / mu[i];
+          sd[i] = ld;
+          su[i] = lam(lc, 1, k, i);
+        }
+        ab(k, 1) -= g;
+        if (n == 1) {
+          if (kind == 1) {
+            for (int i = 0; i < nZ; i++) ab(k, NE_S + i) += sd[i] + su[i];
+          } else {
+            double gb = 0.0, go = 0.0;
+            for (int i = 0; i < nZ; i++) {
+              const double w = sd[i] + su[i];
+              gb += w * (1.0 - etr[i]);
+              go += w * B * etr[i] / mu[i];
+            }
+            ab(k, 2) += gb;
+            ab(k, 1) += go;
+          }
+        } else if (kind == 1 && od >= 1.0e-6) {
+          // sv_dn = T dn'(k) + R up'(k+1), sv_up = R dn'(k) + T up'(k+1) (' order n-1)
+          ltr(k, Tm, Rm);
+          for (int i = 0; i < nZ; i++)
+            for (int j = 0; j < nZ; j++) {
+              const double dj = fld(prv, 0, k, j), uj = fld(prv, 1, k + 1, j);
+              ab(k, NE_T + i * NZ + j) += sd[i] * dj + su[i] * uj;
+              ab(k, NE_R + i * NZ + j) += sd[i] * uj + su[i] * dj;
+            }
+          for (int j = 0; j < nZ; j++) {
+            double ad = 0.0, au = 0.0;
+            for (int i = 0; i < nZ; i++) {
+              ad += Tm.a[i][j] * sd[i] + Rm.a[i][j] * su[i];
+              au += Rm.a[i][j] * sd[i] + Tm.a[i][j] * su[i];
+            }
+            lam(lp, 0, k, j) += ad;
+            lam(lp, 1, k + 1, j) += au;
+          }
+        }
+      }
+      // order n's adjoints are spent: the buffer becomes order n-2's
+      for (int f = 0; f < 2; f++)
+        for (int k = 0; k <= Ku; k++)
+          for (int i = 0; i < nZ; i++) lam(lc, f, k, i) = 0.0;
+    }
+  }
+  *e_b = eb;
+  *Bs_b = bsb;
   return 0;
 }
 
@@ -1164,7 +1328,9 @@ struct LayerDirections {
 
 // Contraction of one layer's optics derivatives with the adjoints of its
 // record: for a scattering layer g[d] = sum(T_b dT/dd) + sum(R_b dR/dd) +
-// sum(src_b dsrc/dd); for a clear one g[d] = od_b dod/dd, plus B_b dB/dT in
+// sum(src_b dsrc/dd) + od_b dod/dd (od_b is 0 for ADA, whose adding takes
+// the layer's optical depth only through T, R and the source; SOI propagates
+// between layers with exp(-od / mu)); for a clear one g[d] = od_b dod/dd, plus B_b dB/dT in
 // the temperature direction (its Planck radiance enters the adding outside
 // the layer optics).  The optics are evaluated on derivative numbers with N
 // directions.  Returns the layer kind of that evaluation.
@@ -1191,6 +1357,7 @@ CRTM_HD int layer_contract(const CloudyColumn& in, const CloudLut& lut, const St
   const int kind = layer_optics<NZ, D, D>(in, lut, S, k, gd, tt, &odd, Td, Rd, srcd, seed);
   for (int d = 0; d < N; d++) g[d] = 0.0;
   if (kind == 1) {
+    for (int d = 0; d < N; d++) g[d] = od_b * part(odd.d[d]);   // SOI's direct transmission
     for (int i = 0; i < S.nZ; i++)
       for (int d = 0; d < N; d++) {
         double acc = src_b[i] * part(srcd[i].d[d]);

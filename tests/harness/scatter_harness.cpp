@@ -140,18 +140,16 @@ int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, 
     kind[k] = layer_optics<NZ, double>(c, L, S, k, od[k], temp[k], &ods[k], T[k], R[k], &src[(size_t)k * NZ]);
     if (kind[k] < 0) return -kind[k];
   }
-  auto layer = [&](int k, int* kd, double* o, double* B, Mat<NZ, double>& Tm, Mat<NZ, double>& Rm, double* sv) {
+  auto lod = [&](int k, int* kd, double* o, double* B) {
     *kd = kind[k];
     *o = ods[k];
     *B = c.c1 / (exp(c.c2 / (c.b1 + c.b2 * temp[k])) - 1.0);
-    Tm = T[k];
-    Rm = R[k];
-    for (int i = 0; i < NZ; i++) sv[i] = src[(size_t)k * NZ + i];
   };
+  auto lsrc = [&](int k, double* sv) { for (int i = 0; i < NZ; i++) sv[i] = src[(size_t)k * NZ + i]; };
+  auto ltr = [&](int k, Mat<NZ, double>& Tm, Mat<NZ, double>& Rm) { Tm = T[k]; Rm = R[k]; };
   std::vector<double> f((size_t)4 * (Ku + 1) * NZ);
-  auto dn = [&](int k, int i, int b) -> double& { return f[((size_t)b * (Ku + 1) + k) * NZ + i]; };
-  auto up = [&](int k, int i, int b) -> double& { return f[((size_t)(2 + b) * (Ku + 1) + k) * NZ + i]; };
-  return soi_solve<NZ>(S.nZ, Ku, S.isat, S.mu, emissivity, planck_surface, cosmic, layer, dn, up, radiance);
+  auto fld = [&](int b, int fi, int k, int i) -> double& { return f[((size_t)(2 * fi + b) * (Ku + 1) + k) * NZ + i]; };
+  return soi_solve<NZ>(S.nZ, Ku, S.isat, S.mu, emissivity, planck_surface, cosmic, lod, lsrc, ltr, fld, radiance);
 }
 
 int sx_stream_rule(double max_reff, double wavenumber) { return stream_rule_nleg(max_reff, wavenumber); }
@@ -214,7 +212,8 @@ extern "C" int sx_cloudy_kmatrix(const int* dims, const double* f_mw, const doub
                                  double emissivity, double planck_surface, double cosmic, const double* planck,
                                  const double* temp, const int* cloud_type, const double* wc, const double* reff,
                                  int cstride, const double* od, double* radiance, double* dgas, double* dT,
-                                 double* e_b, double* Bs_b, double* dwc, double* dre, int dd) {
+                                 double* e_b, double* Bs_b, double* dwc, double* dre, int dd, int soi_slots,
+                                 int* n_orders) {
   CloudLut L{dims[0], dims[1], dims[2], dims[3], dims[4], dims[5], dims[6], f_mw, r_mw, t, f_ir, r_ir,
              ke_l, w_l, pc_l, ke_s, w_s, pc_s, ke_ir, w_ir, pc_ir};
   static const GaussTable gt = make_gauss();
@@ -251,6 +250,63 @@ extern "C" int sx_cloudy_kmatrix(const int* dims, const double* f_mw, const doub
       if (dre) dre[(size_t)cc * cstride + k] = g[1];
     }
   };
-  const int rc = cloudy_adjoint<NZ>(c, S, layer, state, adj, radiance, e_b, Bs_b);
-  return rc ? rc : bad;
+  if (soi_slots <= 0) {
+    const int rc = cloudy_adjoint<NZ>(c, S, layer, state, adj, radiance, e_b, Bs_b);
+    return rc ? rc : bad;
+  }
+  // SOI (soi_slots order-field slots): records first, the orders' adjoint,
+  // then the same contraction of every layer's record adjoints
+  c.soi = true;
+  constexpr int NE = 2 + 2 * NZ * NZ + NZ;
+  std::vector<double> rec((size_t)Ku * NE), rab((size_t)Ku * NE);
+  for (int k = 0; k < Ku; k++) {
+    Mat<NZ, double> Tm, Rm;
+    double sv[NZ], o;
+    const int kind = layer_optics<NZ, double>(c, L, S, k, od[k], temp[k], &o, Tm, Rm, sv);
+    if (kind < 0) return -kind;
+    double* r = &rec[(size_t)k * NE];
+    r[0] = kind;
+    r[1] = o;
+    for (int i = 0; i < NZ; i++) {
+      for (int j = 0; j < NZ; j++) { r[2 + i * NZ + j] = Tm.a[i][j]; r[2 + NZ * NZ + i * NZ + j] = Rm.a[i][j]; }
+      r[2 + 2 * NZ * NZ + i] = sv[i];
+    }
+  }
+  const int nZ = S.nZ;
+  auto lod = [&](int k, int* kd, double* o, double* B) {
+    *kd = (int)rec[(size_t)k * NE];
+    *o = rec[(size_t)k * NE + 1];
+    *B = c.c1 / (exp(c.c2 / (c.b1 + c.b2 * temp[k])) - 1.0);
+  };
+  auto lsrc = [&](int k, double* sv) { for (int i = 0; i < nZ; i++) sv[i] = rec[(size_t)k * NE + 2 + 2 * NZ * NZ + i]; };
+  auto ltr = [&](int k, Mat<NZ, double>& Tm, Mat<NZ, double>& Rm) {
+    for (int i = 0; i < nZ; i++)
+      for (int j = 0; j < nZ; j++) {
+        Tm.a[i][j] = rec[(size_t)k * NE + 2 + i * NZ + j];
+        Rm.a[i][j] = rec[(size_t)k * NE + 2 + NZ * NZ + i * NZ + j];
+      }
+  };
+  std::vector<double> fs((size_t)soi_slots * 2 * (Ku + 1) * NZ, 0.0), lm((size_t)4 * (Ku + 1) * NZ, 0.0);
+  auto fld = [&](int sl, int f, int k, int i) -> double& { return fs[(((size_t)sl * 2 + f) * (Ku + 1) + k) * NZ + i]; };
+  auto lam = [&](int b, int f, int k, int i) -> double& { return lm[(((size_t)b * 2 + f) * (Ku + 1) + k) * NZ + i]; };
+  auto ab = [&](int k, int e) -> double& { return rab[(size_t)k * NE + e]; };
+  const int rc = soi_adjoint<NZ>(nZ, Ku, S.isat, S.mu, emissivity, planck_surface, cosmic, soi_slots, lod, lsrc, ltr,
+                                 fld, lam, ab, radiance, e_b, Bs_b, n_orders);
+  if (rc) return rc;
+  for (int k = 0; k < Ku; k++) {
+    const double* r = &rab[(size_t)k * NE];
+    Mat<NZ, double> T_b, R_b;
+    double src_b[NZ];
+    const int kind = (int)r[0];
+    for (int i = 0; i < NZ; i++) {
+      for (int j = 0; j < NZ; j++) {
+        T_b.a[i][j] = kind == 1 ? r[2 + i * NZ + j] : 0.0;
+        R_b.a[i][j] = kind == 1 ? r[2 + NZ * NZ + i * NZ + j] : 0.0;
+      }
+      src_b[i] = kind == 1 ? r[2 + 2 * NZ * NZ + i] : 0.0;
+    }
+    adj(k, kind, T_b, R_b, src_b, r[1], kind == 1 ? 0.0 : r[2]);
+  }
+  return bad;
 }
+
