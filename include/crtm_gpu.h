@@ -212,9 +212,9 @@ int crtm_gpu_n_channels(crtm_gpu_handle handle, int sensor);
 /* Select the arithmetic form for later calls (CRTM_GPU_FP64 or CRTM_GPU_MIXED). */
 int crtm_gpu_set_precision(crtm_gpu_handle handle, int precision);
 
-/* CRTM_Forward for one sensor: host buffers.  Profiles with clouds use the
- * ADA or SOI scattering solver (FP64 in both arithmetic forms); the K-matrix
- * and adjoint entry points return CRTM_GPU_FAILURE for batches with clouds. */
+/* CRTM_Forward for one sensor: host buffers.  Profiles with clouds or
+ * aerosols use the ADA or SOI scattering solver (FP64 in both arithmetic
+ * forms), as do the K-matrix, adjoint and tangent-linear entry points. */
 int crtm_gpu_forward(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* batch,
                      crtm_gpu_rtsolution* rts);
 
