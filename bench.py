@@ -201,20 +201,22 @@ SCATTER_METRIC = {
 }
 
 
-def scatter_groups(name: str, rank: int):
-    """Per-sensor sub-batches [(sensor, atm, sfc, geo, opt)] of a scattering workload."""
+def scatter_groups(name: str, rank: int, profiles: int = 0):
+    """Per-sensor sub-batches [(sensor, atm, sfc, geo, opt)] of a scattering
+    workload; ``profiles`` > 0 scales C3 / C4 down (profiling captures)."""
     from crtmv3_gb300 import coefficients as co
     if name == "C3":
         # 5000 x 100 x 16 MW, 5 cloud types (Cloud_Fraction 1 in cloudy layers),
         # stream rule with Options%n_Streams 8 / 16 on a tenth of the profiles each
-        atm, sfc, geo, opt = sy.cloudy_workload("mwsynth_c16", 5000, 100, 3100 + rank)
+        P = profiles or 5000
+        atm, sfc, geo, opt = sy.cloudy_workload("mwsynth_c16", P, 100, 3100 + rank)
         rng = np.random.Generator(np.random.PCG64(3200 + rank))
-        ns = rng.choice(np.array([0, 8, 16], np.int32), size=5000, p=[0.8, 0.1, 0.1])
+        ns = rng.choice(np.array([0, 8, 16], np.int32), size=P, p=[0.8, 0.1, 0.1])
         opt.use_n_streams, opt.n_streams = ns > 0, ns
         return [("mwsynth_c16", atm, sfc, geo, opt)]
     if name == "C4":
         # 1000 x 100 x 616 IR, liquid + ice clouds, dust + sea salt + sulfate
-        atm, sfc, geo, opt = sy.clear_sky_workload("irsynth_c616", 1000, 100, 3300 + rank)
+        atm, sfc, geo, opt = sy.clear_sky_workload("irsynth_c616", profiles or 1000, 100, 3300 + rank)
         sy.add_clouds(atm, (co.WATER_CLOUD, co.ICE_CLOUD), 3301 + rank)
         sy.add_aerosols(atm, sy.AEROSOL_TYPES, 3302 + rank)
         return [("irsynth_c616", atm, sfc, geo, opt)]
@@ -271,7 +273,7 @@ def run_scattering(args, torch, dev, rank, world, dist):
     # cloudy K-matrix intermediates take ~0.3 GB per IR profile: a larger
     # chunk workspace keeps the scattering kernels' grids full
     os.environ.setdefault("CRTM_GPU_WORKSPACE_MB", "32768")
-    groups = scatter_groups(name, rank)
+    groups = scatter_groups(name, rank, args.profiles if args.profiles != 2000 else 0)
     if rank == 0:
         for sid, *_ in groups:
             sy.write_sensor_files(COEFF_DIR, sid)
@@ -370,7 +372,7 @@ def run_scattering(args, torch, dev, rank, world, dist):
     per_mixed, per_fp64 = ms_mixed / args.steps, ms_fp64 / fp64_steps
     value, fp64_value = pc / (per_mixed * 1e-3), pc / (per_fp64 * 1e-3)
     extra = {}
-    if name == "C4":   # SOI forward on the same inputs (K-matrix with RT_SOI is not built)
+    if name == "C4":   # SOI forward and K-matrix on the same inputs, ADA forward beside them
         sid, atm, sfc, geo, opt = groups[0]
         opt.rt_algorithm_id = np.full(atm.n_profiles, 168, np.int32)
         b, keep, t = scatter_device_inputs(torch, h, atm, sfc, geo, opt, dev)
@@ -392,6 +394,19 @@ def run_scattering(args, torch, dev, rank, world, dist):
             ms = e0.elapsed_time(e1) / args.steps
             extra[f"{lab}_forward_mixed"] = {"ms_per_step": ms, "value": calls[0]["pc"] / (ms * 1e-3)}
         extra["soi_vs_ada_max_abs_bt_K"] = float((fo["bt"] - fo2["bt"]).abs().max())
+        # SOI K-matrix (the orders' adjoint) into the main call's outputs
+        c0 = calls[0]
+        h.k_matrix_device(b, c0["out"], None, 0, sptr, k_absorbers=c0["sel"])
+        torch.cuda.synchronize(dev)
+        ks = max(1, min(args.steps, 2))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(ks):
+            h.k_matrix_device(b, c0["out"], None, 0, sptr, k_absorbers=c0["sel"])
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / ks
+        extra["soi_kmatrix"] = {"ms_per_step": ms, "value": c0["pc"] / (ms * 1e-3), "steps": ks}
     if rank == 0:
         cfg = {"workload": name, "groups": [{"sensor": c_[0], "profiles": int(c_[1].n_profiles),
                                               "layers_max": int(c_[1].max_layers),
