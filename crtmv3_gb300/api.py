@@ -55,7 +55,8 @@ class CBatch(ct.Structure):
                 ("n_streams", ct.c_void_p), ("rt_algorithm_id", ct.c_void_p),
                 ("max_aerosols", ct.c_int), ("n_aerosols", ct.c_void_p), ("aerosol_type", ct.c_void_p),
                 ("aerosol_concentration", ct.c_void_p), ("aerosol_effective_radius", ct.c_void_p),
-                ("cloud_fraction", ct.c_void_p), ("overlap_id", ct.c_void_p)]
+                ("cloud_fraction", ct.c_void_p), ("overlap_id", ct.c_void_p),
+                ("aerosol_effective_variance", ct.c_void_p), ("relative_humidity", ct.c_void_p)]
 
 
 class CRTSolution(ct.Structure):
@@ -69,32 +70,40 @@ SCATTER_JACOBIANS = ("cloud_water_content", "cloud_effective_radius", "cloud_fra
 
 SURFACE_COVERS = ("land_temperature", "snow_temperature", "ice_temperature")
 
+# the aerosol schemes' second LUT coordinate: Effective_Variance ('CMAQ'),
+# Relative_Humidity ('GOCART-GEOS5', 'NAAPS')
+SCHEME_JACOBIANS = ("aerosol_effective_variance", "relative_humidity")
+AEROSOL_MODELS = ("CRTM", "CMAQ", "GOCART-GEOS5", "NAAPS")
+
 
 class CKMatrix(ct.Structure):
     _fields_ = [("temperature", ct.c_void_p), ("absorber", ct.c_void_p),
                 ("water_temperature", ct.c_void_p), ("surface_emissivity", ct.c_void_p),
                 ("n_k_absorbers", ct.c_int), ("k_absorber_index", ct.c_void_p)] + \
-               [(f, ct.c_void_p) for f in SCATTER_JACOBIANS + SURFACE_COVERS]
+               [(f, ct.c_void_p) for f in SCATTER_JACOBIANS + SURFACE_COVERS + SCHEME_JACOBIANS]
 
 
 class CAdjoint(ct.Structure):
     _fields_ = [("temperature", ct.c_void_p), ("absorber", ct.c_void_p),
-                ("water_temperature", ct.c_void_p)] + [(f, ct.c_void_p) for f in SCATTER_JACOBIANS + SURFACE_COVERS]
+                ("water_temperature", ct.c_void_p)] + \
+               [(f, ct.c_void_p) for f in SCATTER_JACOBIANS + SURFACE_COVERS + SCHEME_JACOBIANS]
 
 
 TL_FIELDS = ("temperature", "absorber", "land_temperature", "water_temperature", "snow_temperature",
              "ice_temperature", "emissivity", "cloud_water_content", "cloud_effective_radius", "cloud_fraction",
-             "aerosol_concentration", "aerosol_effective_radius")
+             "aerosol_concentration", "aerosol_effective_radius", "aerosol_effective_variance",
+             "relative_humidity")
 
 
 class CTLIn(ct.Structure):
     _fields_ = [(f, ct.c_void_p) for f in TL_FIELDS]
 
 
-def _scatter_shapes(atm) -> dict:
+def _scatter_shapes(atm, aerosol_model: str = "CRTM") -> dict:
     """Per-profile shapes (after the profile axis) of the scattering Jacobians
     that a batch has: clouds (NC, Kmax) and the cloud fraction (Kmax,), aerosols
-    (NA, Kmax)."""
+    (NA, Kmax), and the aerosol scheme's effective variance (NA, Kmax; 'CMAQ')
+    or relative humidity (Kmax,; 'GOCART-GEOS5', 'NAAPS')."""
     K = atm.max_layers
     out = {}
     if atm.cloud_type is not None and atm.cloud_type.shape[1] > 0:
@@ -103,6 +112,10 @@ def _scatter_shapes(atm) -> dict:
     if atm.aerosol_type is not None and atm.aerosol_type.shape[1] > 0:
         NA = atm.aerosol_type.shape[1]
         out.update(aerosol_concentration=(NA, K), aerosol_effective_radius=(NA, K))
+        if aerosol_model == "CMAQ":
+            out["aerosol_effective_variance"] = (NA, K)
+        if aerosol_model in ("GOCART-GEOS5", "NAAPS"):
+            out["relative_humidity"] = (K,)
     return out
 
 
@@ -118,6 +131,8 @@ def library() -> ct.CDLL:
         raise RuntimeError(f"GPU library not built: {LIB_PATH} (run crtmv3_gb300.build.build())")
     L = ct.CDLL(LIB_PATH)
     L.crtm_gpu_init.argtypes = [ct.c_char_p, ct.c_int, ct.POINTER(ct.c_char_p), ct.POINTER(ct.c_void_p)]
+    L.crtm_gpu_init_aerosol.argtypes = [ct.c_char_p, ct.c_int, ct.POINTER(ct.c_char_p), ct.c_char_p, ct.c_char_p,
+                                        ct.POINTER(ct.c_void_p)]
     L.crtm_gpu_destroy.argtypes = [ct.c_void_p]
     L.crtm_gpu_n_channels.argtypes = [ct.c_void_p, ct.c_int]
     L.crtm_gpu_set_precision.argtypes = [ct.c_void_p, ct.c_int]
@@ -153,14 +168,25 @@ def _addr(a) -> Optional[int]:
 class CRTM:
     """One library handle: the coefficient tables of a list of sensors."""
 
-    def __init__(self, sensor_ids: Sequence[str], coeff_path: str, precision: int = FP64):
+    def __init__(self, sensor_ids: Sequence[str], coeff_path: str, precision: int = FP64,
+                 aerosol_model: Optional[str] = None, aerosol_coeff_file: Optional[str] = None):
+        """``aerosol_model`` / ``aerosol_coeff_file``: CRTM_Init's Aerosol_Model
+        ('CRTM' by default, 'CMAQ', 'GOCART-GEOS5', 'NAAPS') and the AerosolCoeff
+        file name under ``coeff_path`` (default AerosolCoeff.bin)."""
         L = library()
         h = ct.c_void_p()
         ids = (ct.c_char_p * len(sensor_ids))(*[s.encode() for s in sensor_ids])
-        rc = L.crtm_gpu_init(coeff_path.encode(), len(sensor_ids), ids, ct.byref(h))
+        if aerosol_model is None and aerosol_coeff_file is None:
+            rc = L.crtm_gpu_init(coeff_path.encode(), len(sensor_ids), ids, ct.byref(h))
+        else:
+            rc = L.crtm_gpu_init_aerosol(coeff_path.encode(), len(sensor_ids), ids,
+                                         None if aerosol_model is None else aerosol_model.encode(),
+                                         None if aerosol_coeff_file is None else aerosol_coeff_file.encode(),
+                                         ct.byref(h))
         if rc != SUCCESS:
             raise RuntimeError("crtm_gpu_init: " + self._err(None))
         self.h = h
+        self.aerosol_model = aerosol_model or "CRTM"
         self.sensor_ids = list(sensor_ids)
         self.n_channels = [L.crtm_gpu_n_channels(h, i) for i in range(len(sensor_ids))]
         self.set_precision(precision)
@@ -256,6 +282,10 @@ class CRTM:
             b.aerosol_type = c(atm.aerosol_type, np.int32)
             b.aerosol_concentration = c(atm.aerosol_concentration)
             b.aerosol_effective_radius = c(atm.aerosol_effective_radius)
+            if getattr(atm, "aerosol_effective_variance", None) is not None:
+                b.aerosol_effective_variance = c(atm.aerosol_effective_variance)
+            if getattr(atm, "relative_humidity", None) is not None:
+                b.relative_humidity = c(atm.relative_humidity)
         return b
 
     def _check(self, rc: int) -> None:
@@ -290,7 +320,7 @@ class CRTM:
         km = out if out is not None else KMatrixBatch(np.zeros((P, L, K)), np.zeros((P, L, JK, K)),
                                                       np.zeros((P, L)), np.zeros((P, L)))
         if out is None and scattering_jacobians:
-            for f, shp in _scatter_shapes(atm).items():
+            for f, shp in _scatter_shapes(atm, self.aerosol_model).items():
                 setattr(km, f, np.zeros((P, L) + shp))
         if out is None:
             for f in SURFACE_COVERS:
@@ -300,7 +330,7 @@ class CRTM:
         ck = CKMatrix(km.temperature.ctypes.data, km.absorber.ctypes.data,
                       km.water_temperature.ctypes.data, km.surface_emissivity.ctypes.data,
                       0 if sel is None else JK, None if sel is None else sel.ctypes.data,
-                      *[_addr(getattr(km, f, None)) for f in SCATTER_JACOBIANS + SURFACE_COVERS])
+                      *[_addr(getattr(km, f, None)) for f in SCATTER_JACOBIANS + SURFACE_COVERS + SCHEME_JACOBIANS])
         self._check(library().crtm_gpu_k_matrix(self.h, sensor, ct.byref(b), _addr(seed),
                                                 ct.byref(ck), ct.byref(cr)))
         return km, rts
@@ -312,7 +342,7 @@ class CRTM:
         seed = np.ascontiguousarray(bt_ad, np.float64)
         rts = RTSolutionBatch(np.zeros((P, L)), np.zeros((P, L)), status=np.zeros(P, np.int32))
         out = dict(temperature=np.zeros((P, K)), absorber=np.zeros((P, J, K)), water_temperature=np.zeros(P))
-        for f, shp in _scatter_shapes(atm).items():
+        for f, shp in _scatter_shapes(atm, self.aerosol_model).items():
             out[f] = np.zeros((P,) + shp)
         for f in SURFACE_COVERS:
             out[f] = np.zeros(P)
@@ -320,7 +350,7 @@ class CRTM:
                          rts.status.ctypes.data)
         ca = CAdjoint(out["temperature"].ctypes.data, out["absorber"].ctypes.data,
                       out["water_temperature"].ctypes.data,
-                      *[_addr(out.get(f)) for f in SCATTER_JACOBIANS + SURFACE_COVERS])
+                      *[_addr(out.get(f)) for f in SCATTER_JACOBIANS + SURFACE_COVERS + SCHEME_JACOBIANS])
         self._check(library().crtm_gpu_adjoint(self.h, sensor, ct.byref(b), seed.ctypes.data,
                                                ct.byref(ca), ct.byref(cr)))
         return out, rts
@@ -346,7 +376,8 @@ class CRTM:
             return a.ctypes.data
         vals = {f: arr(atm_tl, f) for f in ("temperature", "absorber", "cloud_water_content",
                                              "cloud_effective_radius", "cloud_fraction", "aerosol_concentration",
-                                             "aerosol_effective_radius")}
+                                             "aerosol_effective_radius", "aerosol_effective_variance",
+                                             "relative_humidity")}
         vals.update({f: arr(sfc_tl, f) for f in ("land_temperature", "water_temperature", "snow_temperature",
                                                   "ice_temperature")})
         if emissivity_tl is not None:
@@ -382,7 +413,8 @@ class CRTM:
                   "sensor_zenith_angle", "source_zenith_angle", "surface_altitude", "emissivity",
                   "n_clouds", "cloud_type", "cloud_water_content", "cloud_effective_radius",
                   "n_streams", "rt_algorithm_id", "n_aerosols", "aerosol_type", "aerosol_concentration",
-                  "aerosol_effective_radius", "cloud_fraction", "overlap_id"):
+                  "aerosol_effective_radius", "cloud_fraction", "overlap_id", "aerosol_effective_variance",
+                  "relative_humidity"):
             t = dev.get(f)
             setattr(b, f, None if t is None else t.data_ptr())
         if dev.get("cloud_type") is not None:
@@ -403,6 +435,8 @@ class CRTM:
                       out["water_temperature_k"].data_ptr(), out["surface_emissivity_k"].data_ptr(),
                       0 if sel is None else int(sel.shape[0]), None if sel is None else sel.ctypes.data,
                       *[_addr(out.get(f + "_k")) for f in SCATTER_JACOBIANS])
+        for f in SCHEME_JACOBIANS:
+            setattr(ck, f, _addr(out.get(f + "_k")))
         fn = (library().crtm_gpu_k_matrix_device_static if static_scratch
               else library().crtm_gpu_k_matrix_device)
         self._check(fn(self.h, sensor, ct.byref(b), _addr(seed), ct.byref(ck), ct.byref(cr), stream))
@@ -415,6 +449,8 @@ class CRTM:
         cr = CRTSolution(out["radiance"].data_ptr(), out["bt"].data_ptr(), _addr(out.get("status")))
         ca = CAdjoint(out["temperature_ad"].data_ptr(), out["absorber_ad"].data_ptr(),
                       out["water_temperature_ad"].data_ptr(), *[_addr(out.get(f + "_ad")) for f in SCATTER_JACOBIANS])
+        for f in SCHEME_JACOBIANS:
+            setattr(ca, f, _addr(out.get(f + "_ad")))
         self._check(library().crtm_gpu_adjoint_device(self.h, sensor, ct.byref(b), seed.data_ptr(),
                                                       ct.byref(ca), ct.byref(cr), stream))
 
@@ -434,10 +470,13 @@ class ChannelInfo:
 
 
 def CRTM_Init(sensor_ids: Sequence[str], channel_info: List[ChannelInfo], file_path: str = ".",
-              precision: int = FP64) -> int:
-    """CRTM_Init: load the coefficients of ``sensor_ids`` and fill ``channel_info``."""
+              precision: int = FP64, aerosol_model: Optional[str] = None,
+              aerosolcoeff_file: Optional[str] = None) -> int:
+    """CRTM_Init: load the coefficients of ``sensor_ids`` and fill ``channel_info``
+    (Aerosol_Model and AerosolCoeff_File as the reference's optional arguments,
+    src/CRTM_LifeCycle.f90:523-561)."""
     try:
-        h = CRTM(sensor_ids, file_path, precision)
+        h = CRTM(sensor_ids, file_path, precision, aerosol_model, aerosolcoeff_file)
     except RuntimeError as e:
         print(f"CRTM_Init(FAILURE): {e}")
         return FAILURE
@@ -543,6 +582,8 @@ def CRTM_Tangent_Linear(atmosphere, surface, atmosphere_tl, surface_tl, geometry
 
 
 def _sensor_options(options: Optional[OptionsBatch], off: int, n: int) -> OptionsBatch:
+    """One sensor's options: its columns of Options%Emissivity and every
+    per-profile option."""
     if options is None or options.emissivity is None:
         raise ValueError("Options%Emissivity is required for this path (Use_Emissivity)")
-    return OptionsBatch(emissivity=np.ascontiguousarray(options.emissivity[:, off:off + n]))
+    return dataclasses.replace(options, emissivity=np.ascontiguousarray(options.emissivity[:, off:off + n]))

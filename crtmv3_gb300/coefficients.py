@@ -304,7 +304,8 @@ def read_cloudcoeff(path: str) -> CloudCoeff:
 
 
 # ---------------------------------------------------------------------------
-# AerosolCoeff (aerosol optical property LUT), scheme 'CRTM'
+# AerosolCoeff (aerosol optical property LUT), schemes 'CRTM', 'CMAQ',
+# 'GOCART-GEOS5', 'NAAPS'
 # ---------------------------------------------------------------------------
 
 AEROSOLCOEFF_RELEASE = 4        # ``AerosolCoeff_Define.f90:75``
@@ -333,16 +334,31 @@ class AerosolCoeff:
     version: int = 1
 
 
-def write_aerosolcoeff(path: str, ac: AerosolCoeff, byteorder: str = "<") -> None:
-    """Record order of ``AerosolCoeff_Binary_IO.f90:396-530`` for the 'CRTM'
-    scheme (which carries n_RH_Radii) and a Version <= 300 file (no kb)."""
+AEROSOL_SCHEMES = ("CRTM", "CMAQ", "GOCART-GEOS5", "NAAPS")
+
+
+def _rh_radii_record(scheme: str) -> bool:
+    """'CRTM' and 'CMAQ' files carry the n_RH_Radii record and an RH axis of
+    that length; 'GOCART-GEOS5' / 'NAAPS' an RH axis of n_RH entries
+    (``AerosolCoeff_Binary_IO.f90:421-424``, ``AerosolCoeff_Define.f90:342-354``)."""
+    if scheme not in AEROSOL_SCHEMES:
+        raise ValueError(f"unknown aerosol scheme {scheme!r}")
+    return scheme in ("CRTM", "CMAQ")
+
+
+def write_aerosolcoeff(path: str, ac: AerosolCoeff, byteorder: str = "<", scheme: str = "CRTM") -> None:
+    """Record order of ``AerosolCoeff_Binary_IO.f90:396-530`` for a Version
+    <= 300 file (no kb); the scheme decides the n_RH_Radii record."""
     nw, nrh, nr, ns, nt = ac.ke.shape
     nl = ac.pcoeff.shape[5] - 1
+    if not _rh_radii_record(scheme) and ac.rh.size != nrh:
+        raise ValueError("the RH axis of a GOCART-GEOS5 / NAAPS table has n_RH entries")
     with open(path, "wb") as f:
         wr = RecordWriter(f, byteorder)
         wr.record(np.array([AEROSOLCOEFF_RELEASE, ac.version], np.int32))
         wr.record(np.array([nw, nr, ns, nt, nrh, nl, ac.pcoeff.shape[6]], np.int32))
-        wr.record(np.array([ac.rh.size], np.int32))
+        if _rh_radii_record(scheme):
+            wr.record(np.array([ac.rh.size], np.int32))
         wr.record(np.array([AEROSOL_SL], np.int32))
         wr.record(ac.data_source.ljust(AEROSOL_SL)[:AEROSOL_SL].encode("ascii"))
         wr.record(np.asarray(ac.type_id, np.int32))
@@ -352,14 +368,17 @@ def write_aerosolcoeff(path: str, ac: AerosolCoeff, byteorder: str = "<") -> Non
         wr.record(ac.ke, ac.w, ac.g, ac.pcoeff)
 
 
-def read_aerosolcoeff(path: str) -> AerosolCoeff:
+def read_aerosolcoeff(path: str, scheme: str = "CRTM") -> AerosolCoeff:
     with open(path, "rb") as f:
         r = RecordReader(f)
         rel, ver = r.split(r.record(), [("i4", (2,))])[0]
         if rel != AEROSOLCOEFF_RELEASE:
             raise IOError(f"AerosolCoeff release {rel} not supported")
         nw, nr, ns, nt, nrh, nl, nph = (int(x) for x in r.split(r.record(), [("i4", (7,))])[0])
-        (nrr,) = r.split(r.record(), [("i4", ())])
+        if _rh_radii_record(scheme):
+            (nrr,) = r.split(r.record(), [("i4", ())])
+        else:
+            nrr = nrh
         r.record()
         src = r.split(r.record(), [("S", AEROSOL_SL)])[0]
         tid = r.split(r.record(), [("i4", (nt,))])[0]

@@ -347,12 +347,15 @@ bool load_cloudcoeff(const std::string& path, std::vector<double>& buf, int* dim
   return true;
 }
 
-// AerosolCoeff.bin, scheme 'CRTM' (AerosolCoeff_Binary_IO.f90:396-530):
-// Release/Version, 7 dimensions, n_RH_Radii, the data-source string, type
-// ids, type names, (wavelength, Reff, Rsig, RH), then (ke, w, g, pcoeff).
-// Version > 300 files carry kb as well and are refused here.
-bool load_aerosolcoeff(const std::string& path, std::vector<double>& buf, std::vector<int>& types, int* dims,
-                       size_t* off, std::string& err) {
+// AerosolCoeff file (AerosolCoeff_Binary_IO.f90:396-530): Release/Version,
+// 7 dimensions, n_RH_Radii ('CRTM' and 'CMAQ' files only), the data-source
+// string, type ids, type names, (wavelength, Reff, Rsig, RH), then (ke, w, g,
+// pcoeff).  The RH axis has n_RH_Radii entries in 'CRTM' / 'CMAQ' files and
+// n_RH in 'GOCART-GEOS5' / 'NAAPS' ones (AerosolCoeff_Define.f90:342-354).
+// Version > 300 files carry kb as well and are refused here.  dims: nw nrh nr
+// ns nt nleg n_rh_axis; off: freq reff ke w pc rsig rh.
+bool load_aerosolcoeff(const std::string& path, int scheme, std::vector<double>& buf, std::vector<int>& types,
+                       int* dims, size_t* off, std::string& err) {
   Records r;
   if (!r.open(path, err)) return false;
   const unsigned char* d;
@@ -365,10 +368,18 @@ bool load_aerosolcoeff(const std::string& path, std::vector<double>& buf, std::v
   int dm[7];
   for (int i = 0; i < 7; i++) dm[i] = r.i32(d + 4 * i);
   const int nw = dm[0], nr = dm[1], ns = dm[2], nt = dm[3], nrh = dm[4], nleg = dm[5], nph = dm[6];
-  if (nw < 4 || nr < 4 || ns < 1 || nt < 1 || nrh < 1 || nleg < 1 || nleg > 64 || nph < 1)
+  if (nw < 4 || nr < 1 || ns < 1 || nt < 1 || nrh < 1 || nleg < 1 || nleg > 64 || nph < 1)
     return bad("dimensions out of range");
-  if (!r.next(d, len) || len != 4) return bad("corrupt n_RH_Radii record");
-  const int nrr = r.i32(d);
+  // the interpolated axes need the 4-point window
+  if ((scheme <= AEROSOL_CMAQ && nr < 4) || (scheme == AEROSOL_CMAQ && ns < 4) ||
+      (scheme >= AEROSOL_GOCART && nrh < 4))
+    return bad("an axis that the aerosol scheme interpolates has fewer than 4 entries");
+  int nrr = nrh;
+  if (scheme <= AEROSOL_CMAQ) {
+    if (!r.next(d, len) || len != 4) return bad("corrupt n_RH_Radii record");
+    nrr = r.i32(d);
+    if (nrr < 1) return bad("n_RH_Radii out of range");
+  }
   if (!r.next(d, len) || len != 4) return bad("corrupt string-length record");
   if (!r.next(d, len)) return bad("corrupt data-source record");
   if (!r.next(d, len) || len != 4u * nt) return bad("corrupt type record");
@@ -385,6 +396,10 @@ bool load_aerosolcoeff(const std::string& path, std::vector<double>& buf, std::v
     if (!(buf[i] > buf[i - 1])) return bad("frequencies (10^4/wavelength) must increase");
   off[1] = buf.size();
   for (size_t i = 0; i < (size_t)nr * nt; i++) buf.push_back(r.f64(d + 8 * (nw + i)));
+  off[5] = buf.size();
+  for (size_t i = 0; i < (size_t)ns * nt; i++) buf.push_back(r.f64(d + 8 * (nw + (size_t)nr * nt + i)));
+  off[6] = buf.size();
+  for (size_t i = 0; i < (size_t)nrr; i++) buf.push_back(r.f64(d + 8 * (nw + (size_t)(nr + ns) * nt + i)));
   const size_t n5 = (size_t)nw * nrh * nr * ns * nt;
   if (!r.next(d, len) || len != 8 * (3 * n5 + n5 * (nleg + 1) * nph)) return bad("corrupt LUT record");
   off[2] = buf.size();
@@ -393,7 +408,7 @@ bool load_aerosolcoeff(const std::string& path, std::vector<double>& buf, std::v
   for (size_t i = 0; i < n5; i++) buf.push_back(r.f64(d + 8 * (n5 + i)));
   off[4] = buf.size();
   for (size_t i = 0; i < n5 * (nleg + 1); i++) buf.push_back(r.f64(d + 8 * (3 * n5 + i)));
-  dims[0] = nw; dims[1] = nrh; dims[2] = nr; dims[3] = ns; dims[4] = nt; dims[5] = nleg;
+  dims[0] = nw; dims[1] = nrh; dims[2] = nr; dims[3] = ns; dims[4] = nt; dims[5] = nleg; dims[6] = nrr;
   return true;
 }
 
@@ -541,6 +556,8 @@ struct Work {
   double* LBA;      // scattering K-matrix/adjoint: [n][Kmax][NE][L] layer record adjoints
   double* CJ, *CR;  // species Jacobians: [n][slots][Kmax][L]
   double* CF;       // cloud-fraction Jacobian: [n][Kmax][L]
+  double* CV;       // aerosol effective-variance Jacobians ('CMAQ'): [n][slots][Kmax][L]
+  double* CH;       // relative-humidity Jacobian ('GOCART-GEOS5', 'NAAPS'): [n][Kmax][L]
   double* TD;       // cloud-cover derivatives: [n][2][Kmax]
   double* ras;      // adjoint: [n][nv][K]
   double* pts;      // adjoint: [n][Kmax]
@@ -566,6 +583,7 @@ struct ScatterWork {
   int soi_slots = 0;     // SOI order-field slots of the K-matrix/adjoint
   int slots = 0;         // species Jacobian slots (max_clouds + max_aerosols), 0: none
   bool cf = false;       // cloud-fraction Jacobian
+  bool cv = false, ch = false;   // aerosol effective-variance / relative-humidity Jacobians
 };
 
 template <int G, class R>
@@ -621,6 +639,8 @@ size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w
     wk.CJ = sw.slots ? (double*)carve(sj) : nullptr;
     wk.CR = sw.slots ? (double*)carve(sj) : nullptr;
     wk.CF = sw.cf ? (double*)carve(nn * Kmax * L * sizeof(double)) : nullptr;
+    wk.CV = sw.cv ? (double*)carve(sj) : nullptr;
+    wk.CH = sw.ch ? (double*)carve(nn * Kmax * L * sizeof(double)) : nullptr;
     wk.TD = sw.kstate && (sw.slots || sw.cf) ? (double*)carve(nn * 2 * Kmax * sizeof(double)) : nullptr;
   }
   if (adj) {
@@ -667,9 +687,9 @@ int reserve_smem(crtm_gpu_handle h, F kernel, size_t bytes, const char* what) {
 // (host entry points only): element i covers bytes [p*per[i], (p+n)*per[i]).
 struct HostCopy {
   int n = 0;
-  void* dst[16];
-  const void* src[16];
-  size_t per[16];
+  void* dst[24];
+  const void* src[24];
+  size_t per[24];
   int max_chunk = 0;   // cap on the chunk size so that copies overlap compute
 };
 
@@ -739,16 +759,23 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
   const bool soi = scat && b->rt_algorithm_id != nullptr;
   // scattering Jacobian outputs that the caller asked for
   double* o_wc = nullptr, *o_re = nullptr, *o_cf = nullptr, *o_ac = nullptr, *o_ar = nullptr;
+  double* o_av = nullptr, *o_rh = nullptr;
   if (mode == 1) {
     o_wc = kk->cloud_water_content; o_re = kk->cloud_effective_radius; o_cf = kk->cloud_fraction;
     o_ac = kk->aerosol_concentration; o_ar = kk->aerosol_effective_radius;
+    o_av = kk->aerosol_effective_variance; o_rh = kk->relative_humidity;
   } else if (mode == 2) {
     o_wc = ad->cloud_water_content; o_re = ad->cloud_effective_radius; o_cf = ad->cloud_fraction;
     o_ac = ad->aerosol_concentration; o_ar = ad->aerosol_effective_radius;
+    o_av = ad->aerosol_effective_variance; o_rh = ad->relative_humidity;
   }
   const int NCb = b->max_clouds > 0 ? b->max_clouds : 0, NAb = b->max_aerosols > 0 ? b->max_aerosols : 0;
   if (NCb == 0) o_wc = o_re = o_cf = nullptr;
-  if (NAb == 0) o_ac = o_ar = nullptr;
+  if (NAb == 0) o_ac = o_ar = o_av = o_rh = nullptr;
+  // the scheme's second aerosol coordinate: effective variance ('CMAQ') or
+  // relative humidity ('GOCART-GEOS5', 'NAAPS'); the other output stays zero
+  const int ascheme = h->has_aerosols ? h->alut.scheme : AEROSOL_CRTM;
+  const bool want_av = o_av && ascheme == AEROSOL_CMAQ, want_rh = o_rh && ascheme >= AEROSOL_GOCART;
   ScatterWork sw;
   if (scat) {
     sw.nz = nz_max ? SC_NZ_MAX : 5;
@@ -756,8 +783,10 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
     sw.kstate = mode != 3;
     sw.soi_slots = soi && sw.kstate ? h->soi_slots : 0;
     sw.rec = nz_max ? layer_record<SC_NZ_MAX>() : layer_record<5>();
-    if (sw.kstate && (o_wc || o_re || o_cf || o_ac || o_ar)) sw.slots = NCb + NAb;
+    if (sw.kstate && (o_wc || o_re || o_cf || o_ac || o_ar || o_av || o_rh)) sw.slots = NCb + NAb;
     sw.cf = sw.kstate && o_cf != nullptr;
+    sw.cv = sw.kstate && want_av;
+    sw.ch = sw.kstate && want_rh;
   }
   // chunk size from the workspace budget
   const size_t per = work_bytes<G, R>(s, 64, Kmax, nv, mode, nullptr, nullptr, sw) / 64 + 1;
@@ -851,6 +880,9 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       sa.alut = h->alut; sa.max_aerosols = b->max_aerosols > 0 ? b->max_aerosols : 0;
       sa.n_aerosols = b->n_aerosols; sa.aerosol_type = b->aerosol_type;
       sa.conc = b->aerosol_concentration; sa.aer_reff = b->aerosol_effective_radius;
+      sa.aer_var = sa.max_aerosols > 0 ? b->aerosol_effective_variance : nullptr;
+      sa.rh = sa.max_aerosols > 0 ? b->relative_humidity : nullptr;
+      sa.CV = w.CV; sa.CH = w.CH;
       if (b->max_clouds <= 0) sa.max_clouds = 0;
       sa.TAU = w.TAU; sa.LB = w.LB; sa.LBK = w.LBK; sa.maxreff = w.maxreff; sa.cover = w.cover;
       sa.cloud_fraction = sa.max_clouds > 0 ? b->cloud_fraction : nullptr;
@@ -914,9 +946,10 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
           scatter_species_kernel<R><<<ga, SCATTER_THREADS, 0, st>>>(sa);
           CK_LAUNCH(h);
           struct Out { double* o; const double* X; int S, s0, ns; };
-          const Out outs[5] = {{o_wc, w.CJ, sw.slots, 0, NCb}, {o_re, w.CR, sw.slots, 0, NCb},
+          const Out outs[7] = {{o_wc, w.CJ, sw.slots, 0, NCb}, {o_re, w.CR, sw.slots, 0, NCb},
                                {o_ac, w.CJ, sw.slots, NCb, NAb}, {o_ar, w.CR, sw.slots, NCb, NAb},
-                               {o_cf, w.CF, 1, 0, 1}};
+                               {o_cf, w.CF, 1, 0, 1}, {o_av, w.CV, sw.slots, NCb, NAb},
+                               {o_rh, w.CH, 1, 0, 1}};
           for (const Out& o : outs) {
             if (!o.o || !o.X || o.ns == 0) continue;
             if (mode == 1) {
@@ -930,6 +963,15 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
             CK_LAUNCH(h);
           }
         }
+        // outputs of a coordinate that the handle's aerosol scheme does not have: zero
+        const size_t rows_k = mode == 1 ? (size_t)L * Kmax : (size_t)Kmax;
+        if (o_av && !sw.cv &&
+            cudaMemsetAsync(o_av + (size_t)p0 * NAb * rows_k, 0, (size_t)n * NAb * rows_k * sizeof(double), st) !=
+                cudaSuccess)
+          return fail(h, "output clear failed");
+        if (o_rh && !sw.ch &&
+            cudaMemsetAsync(o_rh + (size_t)p0 * rows_k, 0, (size_t)n * rows_k * sizeof(double), st) != cudaSuccess)
+          return fail(h, "output clear failed");
       } else {
         StageScope sc(h, 7, st);
         if (nz_max)
@@ -1112,6 +1154,11 @@ int stage_batch(crtm_gpu_handle h, const crtm_gpu_batch* b, int L, const double*
     items.insert(items.end(), {{b->aerosol_concentration, (size_t)P * NA * Km * 8},
                                {b->aerosol_effective_radius, (size_t)P * NA * Km * 8},
                                {b->n_aerosols, (size_t)P * 4}, {b->aerosol_type, (size_t)P * NA * 4}});
+  const size_t aer1 = items.size();
+  if (NA > 0)
+    items.insert(items.end(),
+                 {{b->aerosol_effective_variance, b->aerosol_effective_variance ? (size_t)P * NA * Km * 8 : 0},
+                  {b->relative_humidity, b->relative_humidity ? (size_t)P * Km * 8 : 0}});
   if (NC == 0 && b->max_clouds <= 0 && (b->n_streams || b->rt_algorithm_id) && NA > 0) {
     // options without clouds (aerosol-only batch)
     items.insert(items.end(), {{b->n_streams, b->n_streams ? (size_t)P * 4 : 0},
@@ -1162,9 +1209,14 @@ int stage_batch(crtm_gpu_handle h, const crtm_gpu_batch* b, int L, const double*
     db.n_aerosols = (const int*)dptr[aer0 + 2];
     db.aerosol_type = (const int*)dptr[aer0 + 3];
     if (NC == 0) {
-      db.n_streams = b->n_streams ? (const int*)dptr[aer0 + 4] : nullptr;
-      db.rt_algorithm_id = b->rt_algorithm_id ? (const int*)dptr[aer0 + 5] : nullptr;
+      db.n_streams = b->n_streams ? (const int*)dptr[aer1 + 2] : nullptr;
+      db.rt_algorithm_id = b->rt_algorithm_id ? (const int*)dptr[aer1 + 3] : nullptr;
     }
+    db.aerosol_effective_variance = (const double*)dptr[aer1];
+    db.relative_humidity = (const double*)dptr[aer1 + 1];
+  } else {
+    db.aerosol_effective_variance = nullptr;
+    db.relative_humidity = nullptr;
   }
   *dseed_out = dseed;
   return CRTM_GPU_SUCCESS;
@@ -1204,7 +1256,9 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
                              {kk->aerosol_concentration, NAo ? PL * NAo * Km * 8 : 0},
                              {kk->aerosol_effective_radius, NAo ? PL * NAo * Km * 8 : 0},
                              {kk->land_temperature, PL * 8}, {kk->snow_temperature, PL * 8},
-                             {kk->ice_temperature, PL * 8}});
+                             {kk->ice_temperature, PL * 8},
+                             {kk->aerosol_effective_variance, NAo ? PL * NAo * Km * 8 : 0},
+                             {kk->relative_humidity, NAo ? PL * Km * 8 : 0}});
   if (mode == 2)
     outs.insert(outs.end(), {{ad->temperature, (size_t)P * Km * 8}, {ad->absorber, (size_t)P * J * Km * 8},
                              {ad->water_temperature, PD},
@@ -1213,7 +1267,9 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
                              {ad->cloud_fraction, NCo ? (size_t)P * Km * 8 : 0},
                              {ad->aerosol_concentration, NAo ? (size_t)P * NAo * Km * 8 : 0},
                              {ad->aerosol_effective_radius, NAo ? (size_t)P * NAo * Km * 8 : 0},
-                             {ad->land_temperature, PD}, {ad->snow_temperature, PD}, {ad->ice_temperature, PD}});
+                             {ad->land_temperature, PD}, {ad->snow_temperature, PD}, {ad->ice_temperature, PD},
+                             {ad->aerosol_effective_variance, NAo ? (size_t)P * NAo * Km * 8 : 0},
+                             {ad->relative_humidity, NAo ? (size_t)P * Km * 8 : 0}});
   size_t tout = 0;
   for (auto& o : outs) tout += align_up(o.second);
   if (!h->io_out.ensure(tout)) return fail(h, "cannot allocate %zu bytes for outputs", tout);
@@ -1229,11 +1285,12 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
   if (mode == 1)
     dk = {(double*)dout[3], (double*)dout[4], (double*)dout[5], (double*)dout[6], kk->n_k_absorbers,
           kk->k_absorber_index, (double*)dout[7], (double*)dout[8], (double*)dout[9], (double*)dout[10],
-          (double*)dout[11], (double*)dout[12], (double*)dout[13], (double*)dout[14]};
+          (double*)dout[11], (double*)dout[12], (double*)dout[13], (double*)dout[14], (double*)dout[15],
+          (double*)dout[16]};
   if (mode == 2)
     dad = {(double*)dout[3], (double*)dout[4], (double*)dout[5], (double*)dout[6], (double*)dout[7],
            (double*)dout[8], (double*)dout[9], (double*)dout[10], (double*)dout[11], (double*)dout[12],
-           (double*)dout[13]};
+           (double*)dout[13], (double*)dout[14], (double*)dout[15]};
   HostCopy hc;
   hc.n = (int)outs.size();
   for (size_t i = 0; i < outs.size(); i++) {
@@ -1279,7 +1336,7 @@ struct TLArgs {
   int P, L, Km, J, NC, NA;
   const int* n_layers;
   const int* status;
-  const double* kt, *ka, *kw, *kl, *ks, *ki, *ke, *kwc, *kre, *kcf, *kac, *kar;
+  const double* kt, *ka, *kw, *kl, *ks, *ki, *ke, *kwc, *kre, *kcf, *kac, *kar, *kav, *krh;
   crtm_gpu_tl_in d;
   double* bt_tl;
 };
@@ -1307,6 +1364,8 @@ __global__ void tl_kernel(TLArgs a) {
   rows(a.kcf, a.d.cloud_fraction, 1);
   rows(a.kac, a.d.aerosol_concentration, a.NA);
   rows(a.kar, a.d.aerosol_effective_radius, a.NA);
+  rows(a.kav, a.d.aerosol_effective_variance, a.NA);
+  rows(a.krh, a.d.relative_humidity, 1);
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane) return;
   if (a.d.water_temperature) s += a.kw[pl] * a.d.water_temperature[p];
@@ -1329,9 +1388,10 @@ int tl_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm
   const bool wc = NC && (tl->cloud_water_content || tl->cloud_effective_radius);
   const bool cf = NC && tl->cloud_fraction;
   const bool aer = NA && (tl->aerosol_concentration || tl->aerosol_effective_radius);
+  const bool av = NA && tl->aerosol_effective_variance, rh = NA && tl->relative_humidity;
   const size_t PL = P * L;
   const size_t n_el = PL * Km * (1 + J) + 5 * PL + (wc ? 2 * PL * NC * Km : 0) + (cf ? PL * Km : 0) +
-                      (aer ? 2 * PL * NA * Km : 0);
+                      (aer ? 2 * PL * NA * Km : 0) + (av ? PL * NA * Km : 0) + (rh ? PL * Km : 0);
   if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
   if (!h->tl_k.ensure(n_el * sizeof(double)))
     return fail(h, "cannot allocate %zu bytes for the tangent linear's K-matrix", n_el * sizeof(double));
@@ -1348,6 +1408,8 @@ int tl_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm
   if (wc) { kk.cloud_water_content = take(PL * NC * Km); kk.cloud_effective_radius = take(PL * NC * Km); }
   if (cf) kk.cloud_fraction = take(PL * Km);
   if (aer) { kk.aerosol_concentration = take(PL * NA * Km); kk.aerosol_effective_radius = take(PL * NA * Km); }
+  if (av) kk.aerosol_effective_variance = take(PL * NA * Km);
+  if (rh) kk.relative_humidity = take(PL * Km);
   if (int rc = dispatch(h, sensor, b, 1, nullptr, rts, &kk, nullptr, st)) return rc;
   TLArgs ta{};
   ta.P = (int)P; ta.L = (int)L; ta.Km = (int)Km; ta.J = (int)J; ta.NC = (int)NC; ta.NA = (int)NA;
@@ -1356,6 +1418,7 @@ int tl_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm
   ta.ks = kk.snow_temperature; ta.ki = kk.ice_temperature; ta.ke = kk.surface_emissivity;
   ta.kwc = kk.cloud_water_content; ta.kre = kk.cloud_effective_radius; ta.kcf = kk.cloud_fraction;
   ta.kac = kk.aerosol_concentration; ta.kar = kk.aerosol_effective_radius;
+  ta.kav = kk.aerosol_effective_variance; ta.krh = kk.relative_humidity;
   const long long threads = (long long)PL * 32;
   tl_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(ta);
   CK_LAUNCH(h);
@@ -1382,26 +1445,27 @@ int tl_host(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm_g
   if (int rc = stage_batch(h, b, (int)L, nullptr, &db, &dseed)) return rc;
   cudaStream_t st = h->stream;
   // perturbations
-  const double* srcs[12] = {tl->temperature, tl->absorber, tl->land_temperature, tl->water_temperature,
-                            tl->snow_temperature, tl->ice_temperature, tl->emissivity, tl->cloud_water_content,
-                            tl->cloud_effective_radius, tl->cloud_fraction, tl->aerosol_concentration,
-                            tl->aerosol_effective_radius};
-  const size_t sz[12] = {P * Km, P * J * Km, P, P, P, P, P * L, P * NC * Km, P * NC * Km, NC ? P * Km : 0,
-                         P * NA * Km, P * NA * Km};
+  constexpr int NTL = 14;
+  const double* srcs[NTL] = {tl->temperature, tl->absorber, tl->land_temperature, tl->water_temperature,
+                             tl->snow_temperature, tl->ice_temperature, tl->emissivity, tl->cloud_water_content,
+                             tl->cloud_effective_radius, tl->cloud_fraction, tl->aerosol_concentration,
+                             tl->aerosol_effective_radius, tl->aerosol_effective_variance, tl->relative_humidity};
+  const size_t sz[NTL] = {P * Km, P * J * Km, P, P, P, P, P * L, P * NC * Km, P * NC * Km, NC ? P * Km : 0,
+                          P * NA * Km, P * NA * Km, P * NA * Km, NA ? P * Km : 0};
   size_t tot = 0;
-  for (int i = 0; i < 12; i++) tot += srcs[i] && sz[i] ? align_up(sz[i] * 8) : 0;
+  for (int i = 0; i < NTL; i++) tot += srcs[i] && sz[i] ? align_up(sz[i] * 8) : 0;
   if (!h->io_tl.ensure(tot + 256)) return fail(h, "cannot allocate %zu bytes for the perturbations", tot);
-  const double* dsrc[12] = {};
+  const double* dsrc[NTL] = {};
   size_t off = 0;
-  for (int i = 0; i < 12; i++) {
+  for (int i = 0; i < NTL; i++) {
     if (!srcs[i] || !sz[i]) continue;
     dsrc[i] = (const double*)((char*)h->io_tl.p + off);
     if (cudaMemcpyAsync((void*)dsrc[i], srcs[i], sz[i] * 8, cudaMemcpyHostToDevice, st) != cudaSuccess)
       return fail(h, "host-to-device copy failed");
     off += align_up(sz[i] * 8);
   }
-  const crtm_gpu_tl_in dtl = {dsrc[0], dsrc[1], dsrc[2], dsrc[3], dsrc[4], dsrc[5],
-                              dsrc[6], dsrc[7], dsrc[8], dsrc[9], dsrc[10], dsrc[11]};
+  const crtm_gpu_tl_in dtl = {dsrc[0], dsrc[1], dsrc[2], dsrc[3],  dsrc[4],  dsrc[5],  dsrc[6],
+                              dsrc[7], dsrc[8], dsrc[9], dsrc[10], dsrc[11], dsrc[12], dsrc[13]};
   // outputs
   const size_t PL = P * L;
   const size_t o_bt = align_up(PL * 8), o_tl = o_bt + align_up(PL * 8), o_st = o_tl + align_up(PL * 8);
@@ -1430,9 +1494,23 @@ extern "C" {
 
 int crtm_gpu_init(const char* coeff_path, int n_sensors, const char* const* sensor_ids,
                   crtm_gpu_handle* handle) {
+  return crtm_gpu_init_aerosol(coeff_path, n_sensors, sensor_ids, nullptr, nullptr, handle);
+}
+
+int crtm_gpu_init_aerosol(const char* coeff_path, int n_sensors, const char* const* sensor_ids,
+                          const char* aerosol_model, const char* aerosol_coeff_file, crtm_gpu_handle* handle) {
   if (!handle) return fail(nullptr, "null handle pointer");
   *handle = nullptr;
   if (!coeff_path || n_sensors < 1 || !sensor_ids) return fail(nullptr, "bad init arguments");
+  int scheme = AEROSOL_CRTM;
+  if (aerosol_model) {
+    const std::string m = aerosol_model;
+    if (m == "CRTM") scheme = AEROSOL_CRTM;
+    else if (m == "CMAQ") scheme = AEROSOL_CMAQ;
+    else if (m == "GOCART-GEOS5") scheme = AEROSOL_GOCART;
+    else if (m == "NAAPS") scheme = AEROSOL_NAAPS;
+    else return fail(nullptr, "unknown Aerosol_Model '%s' (CRTM, CMAQ, GOCART-GEOS5 or NAAPS)", aerosol_model);
+  }
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(nullptr, "no CUDA device");
   crtm_gpu_context* h = new crtm_gpu_context();
@@ -1492,15 +1570,22 @@ int crtm_gpu_init(const char* coeff_path, int n_sensors, const char* const* sens
       L.ke_ir = b0 + off[11]; L.w_ir = b0 + off[12]; L.pc_ir = b0 + off[13];
       h->has_clouds = true;
     }
-    const std::string apath = std::string(coeff_path) + "/AerosolCoeff.bin";
-    if (FILE* fa = fopen(apath.c_str(), "rb")) {
+    const std::string apath =
+        std::string(coeff_path) + "/" + (aerosol_coeff_file ? aerosol_coeff_file : "AerosolCoeff.bin");
+    FILE* fa = fopen(apath.c_str(), "rb");
+    if (!fa && aerosol_coeff_file) {   // a named LUT must exist
+      g_init_error = apath + ": cannot open";
+      crtm_gpu_destroy(h);
+      return CRTM_GPU_FAILURE;
+    }
+    if (fa) {
       fclose(fa);
       std::vector<double> abuf;
       std::vector<int> types;
-      int adims[6];
-      size_t aoff[5];
+      int adims[7];
+      size_t aoff[7];
       std::string err;
-      if (!load_aerosolcoeff(apath, abuf, types, adims, aoff, err)) {
+      if (!load_aerosolcoeff(apath, scheme, abuf, types, adims, aoff, err)) {
         g_init_error = err;
         crtm_gpu_destroy(h);
         return CRTM_GPU_FAILURE;
@@ -1515,9 +1600,12 @@ int crtm_gpu_init(const char* coeff_path, int n_sensors, const char* const* sens
       }
       AerosolLut& A = h->alut;
       A.nw = adims[0]; A.nrh = adims[1]; A.nr = adims[2]; A.ns = adims[3]; A.nt = adims[4]; A.nleg = adims[5];
+      A.nrh_axis = adims[6];
+      A.scheme = scheme;
       A.type_id = h->d_aero_type;
       A.freq = h->d_aero + aoff[0]; A.reff = h->d_aero + aoff[1]; A.ke = h->d_aero + aoff[2];
-      A.w = h->d_aero + aoff[3]; A.pc = h->d_aero + aoff[4];
+      A.w = h->d_aero + aoff[3]; A.pc = h->d_aero + aoff[4]; A.rsig = h->d_aero + aoff[5];
+      A.rh = h->d_aero + aoff[6];
       h->has_aerosols = true;
     }
     GaussTable gt{};

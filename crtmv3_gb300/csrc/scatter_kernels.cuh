@@ -76,6 +76,8 @@ struct ScatterArgs {
   const int* n_aerosols;        // [P] (null when max_aerosols = 0)
   const int* aerosol_type;      // [P][NA]
   const double* conc, *aer_reff;   // [P][NA][Kmax]
+  const double* aer_var;        // [P][NA][Kmax] Effective_Variance ('CMAQ'), or null (0)
+  const double* rh;             // [P][Kmax] Relative_Humidity ('GOCART-GEOS5', 'NAAPS'), or null (0)
   double* FB;                   // SOI fields [n][2][2][Kmax+1][NZ][L], or null (K-matrix/adjoint:
                                 // the orders' adjoint fields)
   double* FS;                   // SOI K-matrix/adjoint: [n][soi_slots][2][Kmax+1][NZ][L] order fields
@@ -102,6 +104,8 @@ struct ScatterArgs {
   int n_slots;                  // max_clouds + max_aerosols when requested, else 0
   double* CJ, *CR;              // [n][n_slots][Kmax][L] amount and radius
   double* CF;                   // [n][Kmax][L] cloud fraction, or null
+  double* CV;                   // [n][n_slots][Kmax][L] aerosol effective variance ('CMAQ'), or null
+  double* CH;                   // [n][Kmax][L] relative humidity ('GOCART-GEOS5', 'NAAPS'), or null
   double* TD;                   // [n][2][Kmax] d tcc / d cf, d tcc / d wc (fractional profiles)
   const R* SC;                  // [n][L] dBT/dR x seed (after the second column launch)
 };
@@ -201,6 +205,8 @@ __device__ __forceinline__ CloudyColumn column_inputs(const ScatterArgs<R>& a, i
   c.aerosol_type = a.max_aerosols > 0 ? a.aerosol_type + (size_t)gp * a.max_aerosols : nullptr;
   c.conc = a.max_aerosols > 0 ? a.conc + (size_t)gp * a.max_aerosols * a.Kmax : nullptr;
   c.aer_reff = a.max_aerosols > 0 ? a.aer_reff + (size_t)gp * a.max_aerosols * a.Kmax : nullptr;
+  c.aer_var = a.max_aerosols > 0 && a.aer_var ? a.aer_var + (size_t)gp * a.max_aerosols * a.Kmax : nullptr;
+  c.rh = a.max_aerosols > 0 && a.rh ? a.rh + (size_t)gp * a.Kmax : nullptr;
   c.alut = &a.alut;
   c.cf = a.cloud_fraction && c.n_clouds > 0 ? a.cloud_fraction + (size_t)gp * a.Kmax : nullptr;
   const double tcc = a.cover[p];
@@ -523,6 +529,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_contract_kernel(Scatt
     for (int s = 0; s < a.n_slots; s++) {
       a.CJ[((size_t)p * a.n_slots + s) * Kmax * L + (size_t)k * L + l] = 0.0;
       a.CR[((size_t)p * a.n_slots + s) * Kmax * L + (size_t)k * L + l] = 0.0;
+      if (a.CV) a.CV[((size_t)p * a.n_slots + s) * Kmax * L + (size_t)k * L + l] = 0.0;
     }
   const double* rb = a.LBA + ((size_t)p * Kmax + k) * NE * L + l;
   const int kind = (int)rb[0];
@@ -574,6 +581,19 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_contract_kernel(Scatt
     }
     done += m;
   }
+  if (a.CV && a.alut.scheme == AEROSOL_CMAQ) {   // the aerosols' effective variance, four per pass
+    int av[2 * SC_NC_MAX], nav = 0;
+    for (int i = 0; i < nsp; i++)
+      if (sp[i] >= c.n_clouds) av[nav++] = sp[i];
+    for (int i0 = 0; i0 < nav; i0 += 4) {
+      const int m = nav - i0 < 4 ? nav - i0 : 4;
+      LayerDirections d{false, m, {av[i0], m > 1 ? av[i0 + 1] : 0, m > 2 ? av[i0 + 2] : 0, m > 3 ? av[i0 + 3] : 0}};
+      d.second = true;
+      layer_contract<NZ, 4, C>(c, a.lut, S, k, gas, d, T_b, R_b, src_b, od_b, B_b, g);
+      for (int i = 0; i < m; i++)
+        a.CV[((size_t)p * a.n_slots + slot(av[i0 + i])) * Kmax * L + (size_t)k * L + l] = g[i];
+    }
+  }
 }
 
 // Species and cloud-fraction Jacobians of one (profile, channel), in place:
@@ -610,12 +630,20 @@ __global__ void scatter_species_kernel(ScatterArgs<R> a) {
     }
   }
   const double* dcf = tcc >= 0.0 && a.TD ? a.TD + (size_t)p * 2 * Kmax : nullptr;
+  // GOCART-GEOS5 / NAAPS: an aerosol's second slot holds its lookup's RH
+  // derivative; the layer's RH Jacobian is their sum, the radius one is zero
+  const bool rh_slots = a.max_aerosols > 0 && a.alut.scheme >= AEROSOL_GOCART;
   for (int s = 0; s < a.n_slots; s++) {
     const bool cloud = s < a.max_clouds;
     for (int k = 0; k < Kmax; k++) {
       double& x = J(a.CJ, s, k);
       double& r = J(a.CR, s, k);
-      if (k >= Ku || !live) { x = r = 0.0; continue; }
+      double* v2 = a.CV ? &J(a.CV, s, k) : nullptr;
+      if (k >= Ku || !live) {
+        x = r = 0.0;
+        if (v2) *v2 = 0.0;
+        continue;
+      }
       if (cloud) {
         double v = x;
         const double wk = s < nc ? wc[(size_t)s * Kmax + k] : 0.0;
@@ -625,9 +653,19 @@ __global__ void scatter_species_kernel(ScatterArgs<R> a) {
       } else {
         x = sc * w * x;
         r = sc * w * r;
+        if (v2) *v2 = sc * w * *v2;
       }
     }
   }
+  if (a.CH)
+    for (int k = 0; k < Kmax; k++) {
+      double h = 0.0;
+      for (int s = a.max_clouds; s < a.n_slots && rh_slots; s++) h += J(a.CR, s, k);
+      a.CH[((size_t)p * Kmax + k) * L + l] = h;
+    }
+  if (rh_slots)
+    for (int s = a.max_clouds; s < a.n_slots; s++)
+      for (int k = 0; k < Kmax; k++) J(a.CR, s, k) = 0.0;
   if (a.CF)
     for (int k = 0; k < Kmax; k++)
       a.CF[((size_t)p * Kmax + k) * L + l] = (live && dcf && k < Ku) ? sc * dtcc * dcf[k] : 0.0;

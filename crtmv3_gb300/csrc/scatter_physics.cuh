@@ -41,6 +41,11 @@ constexpr double MAX_ALBEDO = 0.999999;              // RTV_Define.f90:77
 constexpr double PHASE_THRESHOLD = 1.0e-7;           // RTV_Define.f90:74
 constexpr double DELTA_OPTICAL_DEPTH = 1.0e-8;       // RTV_Define.f90:76
 constexpr double ANGLE_THRESHOLD = 1.0e-7;           // RTV_Define.f90:70
+// K-matrix contraction: relative gap between a MOM quadrature eigenvalue and
+// the sensor angle's below which the derivatives are taken at shifted sensor
+// angles mu (1 +- SENSOR_SHIFT)
+constexpr double SENSOR_GAP_MIN = 1.0e-3;
+constexpr double SENSOR_SHIFT = 1.0e-3;
 
 // Device copy of the CloudCoeff LUT (phase element 1 only).  Tables keep the
 // file's Fortran order (frequency fastest).
@@ -181,33 +186,55 @@ CRTM_HD bool cloud_layer_optics(const CloudLut& C, bool microwave, double freq, 
 
 // Device copy of the AerosolCoeff LUT, scheme 'CRTM' (first RH and sigma of
 // each type; phase element 1).  Tables in the file's Fortran order.
+// CRTM_Init's Aerosol_Model: the LUT's layout and interpolation axes
+constexpr int AEROSOL_CRTM = 0, AEROSOL_CMAQ = 1, AEROSOL_GOCART = 2, AEROSOL_NAAPS = 3;
+
 struct AerosolLut {
   int nw, nrh, nr, ns, nt, nleg;
+  int scheme;               // AEROSOL_CRTM .. AEROSOL_NAAPS
+  int nrh_axis;             // entries of the RH axis (n_RH_Radii or n_RH)
   const int* type_id;       // [nt]
   const double* freq;       // [nw] cm^-1, increasing
   const double* reff;       // [nt][nr]
+  const double* rsig;       // [nt][ns]
+  const double* rh;         // [nrh_axis]
   const double* ke, *w;     // [nt][ns][nr][nrh][nw]
   const double* pc;         // [nleg+1][nt][ns][nr][nrh][nw]
 };
 
-// Get_Aerosol_Opt, scheme 'CRTM' (CRTM_AerosolScatter.f90:772-855); the
-// effective radius carries S's derivatives.
+// Get_Aerosol_Opt (CRTM_AerosolScatter.f90:772-918).  'CRTM': frequency x
+// radius at the first RH and sigma; 'CMAQ': frequency x radius x sigma at the
+// first RH; 'GOCART-GEOS5' / 'NAAPS': frequency x RH at the first radius and
+// sigma.  Radius, sigma (Effective_Variance) and RH carry S's derivatives.
 template <class S>
-CRTM_HD bool aerosol_layer_optics(const AerosolLut& A, double wavenumber, int type, S reff, int nleg,
-                                  int loff, S* ke, S* w, S* pc) {
+CRTM_HD bool aerosol_layer_optics(const AerosolLut& A, double wavenumber, int type, S reff, S rsig, S rh,
+                                  int nleg, int loff, S* ke, S* w, S* pc) {
   int k = -1;
   for (int t = 0; t < A.nt; t++)
     if (A.type_id[t] == type) { k = t; break; }
   if (k < 0) return false;
   const Lagrange4 F = lagrange4(A.freq, A.nw, wavenumber);
-  const Lagrange4T<S> Rr = lagrange4(A.reff + (size_t)k * A.nr, A.nr, reff);
   const int nu = A.nw * A.nrh;                     // radius stride
   const size_t base = (size_t)k * A.nw * A.nrh * A.nr * A.ns;
   const size_t n5 = (size_t)A.nw * A.nrh * A.nr * A.ns * A.nt;
-  *ke = lerp4x4(A.ke + base, nu, F, Rr);
-  *w = lerp4x4(A.w + base, nu, F, Rr);
   pc[0] = S(0.5);
-  for (int l = 1; l <= nleg; l++) pc[l] = lerp4x4(A.pc + n5 * (l + loff) + base, nu, F, Rr);
+  if (A.scheme == AEROSOL_CRTM) {
+    const Lagrange4T<S> Rr = lagrange4(A.reff + (size_t)k * A.nr, A.nr, reff);
+    *ke = lerp4x4(A.ke + base, nu, F, Rr);
+    *w = lerp4x4(A.w + base, nu, F, Rr);
+    for (int l = 1; l <= nleg; l++) pc[l] = lerp4x4(A.pc + n5 * (l + loff) + base, nu, F, Rr);
+  } else if (A.scheme == AEROSOL_CMAQ) {
+    const Lagrange4T<S> Rr = lagrange4(A.reff + (size_t)k * A.nr, A.nr, reff);
+    const Lagrange4T<S> Sg = lagrange4(A.rsig + (size_t)k * A.ns, A.ns, rsig);
+    *ke = lerp4x4x4(A.ke + base, nu, A.nr, F, Rr, Sg);
+    *w = lerp4x4x4(A.w + base, nu, A.nr, F, Rr, Sg);
+    for (int l = 1; l <= nleg; l++) pc[l] = lerp4x4x4(A.pc + n5 * (l + loff) + base, nu, A.nr, F, Rr, Sg);
+  } else {
+    const Lagrange4T<S> H = lagrange4(A.rh, A.nrh, rh);
+    *ke = lerp4x4(A.ke + base, A.nw, F, H);
+    *w = lerp4x4(A.w + base, A.nw, F, H);
+    for (int l = 1; l <= nleg; l++) pc[l] = lerp4x4(A.pc + n5 * (l + loff) + base, A.nw, F, H);
+  }
   return true;
 }
 
@@ -345,10 +372,16 @@ CRTM_HD void jacobi(int n, Mat<NZ, Dual<N, Q>>& S, Dual<N, Q>* lam, Mat<NZ, Dual
 // MOM, azimuth order 0, no solar source): transmission T, reflection R and
 // the thermal source (identical up and down).  ff/bb are the normalised
 // forward/backward phase blocks.  Returns false on a failed factorisation.
+// gap (optional): the smallest |lambda_c - h_zz| / |lambda_c| between the
+// quadrature eigenvalues and the sensor angle's diagonal term of HH (1 when
+// there is no separate sensor angle).  Near 0 the eigenbasis is nearly
+// defective: the layer's T and R stay smooth, but their derivatives through
+// the eigenvectors lose about eps / gap^2 of their accuracy.
 template <int NZ, class T>
 CRTM_HD bool ada_layer(int nS, int nZ, T w, T tau, const T* mu,
                               const T* wt, const Mat<NZ, T>& ff, const Mat<NZ, T>& bb, T B,
-                              Mat<NZ, T>& Tm, Mat<NZ, T>& Rm, T* src) {
+                              Mat<NZ, T>& Tm, Mat<NZ, T>& Rm, T* src, double* gap = nullptr) {
+  if (gap) *gap = 1.0;
   if (tau < T(DELTA_OPTICAL_DEPTH)) {   // thin layer: first-order scattering
     const T s = tau * w;
     for (int i = 0; i < nZ; i++) {
@@ -434,6 +467,10 @@ CRTM_HD bool ada_layer(int nS, int nZ, T w, T tau, const T* mu,
       T v = T(0.0);
       for (int k = 0; k < nS; k++) v += hz[k] * Rm.a[k][c];
       Rm.a[z][c] = v / (lam[c] - hz[z]);
+      if (gap) {
+        const double g = fabs(value_of(lam[c]) - value_of(hz[z])) / fabs(value_of(lam[c]));
+        if (g < *gap) *gap = g;
+      }
     }
     for (int i = 0; i < nS; i++) Rm.a[i][z] = T(0.0);
     Rm.a[z][z] = T(1.0);
@@ -680,6 +717,8 @@ struct CloudyColumn {
   const int* aerosol_type;               // [n_aerosols]
   const double* conc;                    // [n_aerosols] rows of stride cstride, kg/m^2
   const double* aer_reff;
+  const double* aer_var = nullptr;       // Effective_Variance rows ('CMAQ'), null: 0
+  const double* rh = nullptr;            // [Ku] Relative_Humidity ('GOCART-GEOS5', 'NAAPS'), null: 0
   const AerosolLut* alut;
   // Cloud_Fraction of the profile's layers (null: 1): clouds are dropped
   // where it is below 1e-12 (CRTM_Forward_Module.f90:367-376); water content
@@ -725,13 +764,16 @@ CRTM_HD int stream_set(int nleg, double mu_sensor, int lut_nleg, const GaussTabl
   return 0;
 }
 
-// Species seeds of a derivative evaluation: seed(s, amount, radius) may set
+// Species seeds of a derivative evaluation: seed(s, amount, c1, c2) may set
 // the derivative parts of species s's layer amount (cloud water content after
-// the cover scaling, or aerosol concentration) and effective radius; species
-// are the clouds 0..n_clouds-1, then the aerosols.
+// the cover scaling, or aerosol concentration) and of its LUT coordinates:
+// c1 the effective radius (clouds; aerosols of the 'CRTM' and 'CMAQ' schemes)
+// or the layer's relative humidity as this aerosol's lookup sees it
+// ('GOCART-GEOS5', 'NAAPS'); c2 the effective variance ('CMAQ'; unused
+// otherwise).  Species are the clouds 0..n_clouds-1, then the aerosols.
 struct NoSeed {
   template <class S>
-  CRTM_HD void operator()(int, S&, S&) const {}
+  CRTM_HD void operator()(int, S&, S&, S&) const {}
 };
 
 // Optics of layer k for the adding method: cloud and aerosol optics summed
@@ -744,7 +786,7 @@ struct NoSeed {
 template <int NZ, class T, class S = double, class Seed = NoSeed>
 CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const StreamSet<NZ, double>& St, int k,
                          S gas_od, S tk, T* od_out, Mat<NZ, T>& Tm, Mat<NZ, T>& Rm, T* src,
-                         Seed seed = Seed()) {
+                         Seed seed = Seed(), double* gap = nullptr) {
   const int nleg = St.nleg;
   S od = gas_od, bs_sum = S(0.0);
   S pc[SC_NLEG_MAX + 1], pcs[SC_NLEG_MAX + 1];
@@ -753,8 +795,8 @@ CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const Stre
   for (int c = 0; c < in.n_clouds && !dropped; c++) {
     const double wcv = in.wc[c * in.cstride + k] / in.wc_div;
     if (!(wcv > WATER_CONTENT_THRESHOLD)) continue;
-    S wc(wcv), re(in.reff[c * in.cstride + k]);
-    seed(c, wc, re);
+    S wc(wcv), re(in.reff[c * in.cstride + k]), unused(0.0);
+    seed(c, wc, re, unused);
     S ke, w;
     if (!cloud_layer_optics<S>(lut, in.microwave, in.freq, in.cloud_type[c], re, tk, nleg, St.loff, &ke, &w, pc))
       return -4;
@@ -773,9 +815,11 @@ CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const Stre
       const double concv = in.conc[c * in.cstride + k];
       if (!(concv > AEROSOL_CONTENT_THRESHOLD)) continue;
       S conc(concv), re(in.aer_reff[c * in.cstride + k]);
-      seed(in.n_clouds + c, conc, re);
+      S sg(in.aer_var ? in.aer_var[c * in.cstride + k] : 0.0), rh(in.rh ? in.rh[k] : 0.0);
+      seed(in.n_clouds + c, conc, in.alut->scheme >= AEROSOL_GOCART ? rh : re, sg);
       S ke, w;
-      if (!aerosol_layer_optics<S>(*in.alut, in.wavenumber, in.aerosol_type[c], re, nleg, St.loff, &ke, &w, pa))
+      if (!aerosol_layer_optics<S>(*in.alut, in.wavenumber, in.aerosol_type[c], re, sg, rh, nleg, St.loff, &ke,
+                                   &w, pa))
         return -9;
       if (ke <= 0.0) { ke = S(0.0); w = S(0.0); }
       if (w <= 0.0) { w = S(0.0); for (int l = 0; l <= nleg; l++) pa[l] = S(0.0); }
@@ -817,7 +861,7 @@ CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const Stre
     for (int i = 0; i < St.nZ; i++)
       for (int j = 0; j < St.nZ; j++) mx = fabs(ff.a[i][j]) > mx ? fabs(ff.a[i][j]) : mx;
     if (!(mx > 0.0)) return 0;
-    if (!ada_layer<NZ, S>(St.nS, St.nZ, ssa, od, mu, wt, ff, bb, B, Td, Rd, srcd)) return -5;
+    if (!ada_layer<NZ, S>(St.nS, St.nZ, ssa, od, mu, wt, ff, bb, B, Td, Rd, srcd, gap)) return -5;
   }
   for (int i = 0; i < St.nZ; i++) {
     src[i] = T(srcd[i]);
@@ -1315,15 +1359,74 @@ CRTM_HD int cloudy_radiance(const CloudyColumn& in, const CloudLut& lut, const G
   return 0;
 }
 
+// A layer's optics on derivative numbers (layer_optics with S = T = D), with
+// the derivatives of a nearly defective MOM eigenbasis taken at shifted
+// sensor angles.
+template <int NZ, int N, class Q, class Seed>
+CRTM_HD int layer_optics_dual(const CloudyColumn& in, const CloudLut& lut, const StreamSet<NZ, double>& S, int k,
+                              Dual<N, Q> gd, Dual<N, Q> tt, Dual<N, Q>* odd, Mat<NZ, Dual<N, Q>>& Td,
+                              Mat<NZ, Dual<N, Q>>& Rd, Dual<N, Q>* srcd, Seed seed) {
+  using D = Dual<N, Q>;
+  double gap = 1.0;
+  const int kind = layer_optics<NZ, D, D>(in, lut, S, k, gd, tt, odd, Td, Rd, srcd, seed, &gap);
+  if (kind == 1 && gap < SENSOR_GAP_MIN && S.nZ == S.nS + 1) {
+    // A quadrature eigenvalue of MOM nearly meets the sensor angle's: the
+    // eigenbasis is nearly defective and the derivatives through it lose
+    // about eps / gap^2.  T, R and the source are smooth in the sensor angle:
+    // their derivatives come from sensor angles mu (1 +- h), h = 1e-3 and
+    // 2e-3 (gaps >= 1e-3 there), as the Richardson extrapolation
+    // (4 D(h) - D(2h)) / 3 of the symmetric means, accurate to O(h^4).
+    Mat<NZ, D> T2, R2;
+    D s2[NZ], o2;
+    Mat<NZ, D> Ta, Ra;
+    D sa[NZ], oa;
+    int n_ok = 0;
+    for (int side = 0; side < 4; side++) {
+      const double f = (side & 1 ? -1.0 : 1.0) * (side < 2 ? SENSOR_SHIFT : 2.0 * SENSOR_SHIFT);
+      const double wgt = (side < 2 ? 4.0 : -1.0) / 6.0;   // (4 mean(h) - mean(2h)) / 3
+      StreamSet<NZ, double> S2 = S;
+      const int z = S.nZ - 1;
+      S2.mu[z] = S.mu[z] * (1.0 + f);
+      S2.P[z][0] = 1.0;
+      if (S2.nleg > 0) S2.P[z][1] = S2.mu[z];
+      for (int j = 1; j < S2.nleg; j++)
+        S2.P[z][j + 1] = ((2 * j + 1) * S2.mu[z] * S2.P[z][j] - j * S2.P[z][j - 1]) / (j + 1);
+      if (layer_optics<NZ, D, D>(in, lut, S2, k, gd, tt, &o2, T2, R2, s2, seed) != 1) break;
+      for (int i = 0; i < S.nZ; i++) {
+        for (int j = 0; j < S.nZ; j++)
+          for (int q = 0; q < N; q++) {
+            const Q t = T2.a[i][j].d[q] * wgt, r = R2.a[i][j].d[q] * wgt;
+            Ta.a[i][j].d[q] = n_ok ? Ta.a[i][j].d[q] + t : t;
+            Ra.a[i][j].d[q] = n_ok ? Ra.a[i][j].d[q] + r : r;
+          }
+        for (int q = 0; q < N; q++) sa[i].d[q] = n_ok ? sa[i].d[q] + s2[i].d[q] * wgt : s2[i].d[q] * wgt;
+      }
+      for (int q = 0; q < N; q++) oa.d[q] = n_ok ? oa.d[q] + o2.d[q] * wgt : o2.d[q] * wgt;
+      n_ok++;
+    }
+    if (n_ok == 4) {   // else (a shifted angle changed the layer's kind) keep the direct derivatives
+      for (int i = 0; i < S.nZ; i++) {
+        for (int j = 0; j < S.nZ; j++)
+          for (int q = 0; q < N; q++) { Td.a[i][j].d[q] = Ta.a[i][j].d[q]; Rd.a[i][j].d[q] = Ra.a[i][j].d[q]; }
+        for (int q = 0; q < N; q++) srcd[i].d[q] = sa[i].d[q];
+      }
+      for (int q = 0; q < N; q++) odd->d[q] = oa.d[q];
+    }
+  }
+  return kind;
+}
+
 // Directions of one derivative evaluation of a layer's optics: the gas
 // optical depth and the temperature (when gas_t; directions 0 and 1), then
-// for each listed species its amount and its effective radius (directions
-// base + 2i and base + 2i + 1, base = 2 or 0).  Species index: clouds
-// 0..n_clouds-1, then aerosols.
+// for each listed species its amount and its first LUT coordinate c1
+// (directions base + 2i and base + 2i + 1, base = 2 or 0), or with second
+// set its second coordinate c2 only (direction base + i).  Species index:
+// clouds 0..n_clouds-1, then aerosols.
 struct LayerDirections {
   bool gas_t;
   int nsp;
   int sp[4];
+  bool second = false;   // the listed species' second LUT coordinate (c2), direction i each
 };
 
 // Contraction of one layer's optics derivatives with the adjoints of its
@@ -1345,16 +1448,20 @@ CRTM_HD int layer_contract(const CloudyColumn& in, const CloudLut& lut, const St
     gd.d[0] = 1.0;
     tt.d[1] = 1.0;
   }
-  auto seed = [&](int s, D& amount, D& radius) {
+  auto seed = [&](int s, D& amount, D& c1, D& c2) {
     for (int i = 0; i < dir.nsp; i++)
       if (dir.sp[i] == s) {
-        amount.d[base + 2 * i] = 1.0;
-        radius.d[base + 2 * i + 1] = 1.0;
+        if (dir.second) {
+          c2.d[base + i] = 1.0;
+        } else {
+          amount.d[base + 2 * i] = 1.0;
+          c1.d[base + 2 * i + 1] = 1.0;
+        }
       }
   };
   Mat<NZ, D> Td, Rd;
   D srcd[NZ], odd;
-  const int kind = layer_optics<NZ, D, D>(in, lut, S, k, gd, tt, &odd, Td, Rd, srcd, seed);
+  const int kind = layer_optics_dual<NZ>(in, lut, S, k, gd, tt, &odd, Td, Rd, srcd, seed);
   for (int d = 0; d < N; d++) g[d] = 0.0;
   if (kind == 1) {
     for (int d = 0; d < N; d++) g[d] = od_b * part(odd.d[d]);   // SOI's direct transmission

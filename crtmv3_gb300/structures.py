@@ -53,6 +53,11 @@ class AtmosphereBatch:
     aerosol_type: Optional[np.ndarray] = None     # (P, NA)
     aerosol_concentration: Optional[np.ndarray] = None   # (P, NA, Kmax) kg/m^2
     aerosol_effective_radius: Optional[np.ndarray] = None  # (P, NA, Kmax) microns
+    # aerosol scheme inputs: Effective_Variance ('CMAQ') and the layers'
+    # Relative_Humidity ('GOCART-GEOS5', 'NAAPS'); None means zero, as the
+    # reference's structures are initialised (the LUT lookup clamps them)
+    aerosol_effective_variance: Optional[np.ndarray] = None  # (P, NA, Kmax)
+    relative_humidity: Optional[np.ndarray] = None  # (P, Kmax), 0..1
 
     @property
     def n_profiles(self) -> int:
@@ -75,7 +80,8 @@ class AtmosphereBatch:
             take(self.n_clouds), take(self.cloud_type), take(self.cloud_water_content),
             take(self.cloud_effective_radius), take(self.cloud_fraction),
             take(self.n_aerosols), take(self.aerosol_type), take(self.aerosol_concentration),
-            take(self.aerosol_effective_radius))
+            take(self.aerosol_effective_radius), take(self.aerosol_effective_variance),
+            take(self.relative_humidity))
 
 
 @dataclasses.dataclass
@@ -169,3 +175,5 @@ class KMatrixBatch:
     cloud_fraction: Optional[np.ndarray] = None          # (P, L, Kmax)
     aerosol_concentration: Optional[np.ndarray] = None   # (P, L, NA, Kmax)
     aerosol_effective_radius: Optional[np.ndarray] = None  # (P, L, NA, Kmax)
+    aerosol_effective_variance: Optional[np.ndarray] = None  # (P, L, NA, Kmax) ('CMAQ')
+    relative_humidity: Optional[np.ndarray] = None         # (P, L, Kmax) ('GOCART-GEOS5', 'NAAPS')

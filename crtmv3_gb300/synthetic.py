@@ -528,40 +528,92 @@ AEROSOL_TYPES = (DUST_AEROSOL, SEASALT_AEROSOL, SULFATE_AEROSOL)
 AEROSOL_REFF = {DUST_AEROSOL: (0.5, 5.0), SEASALT_AEROSOL: (0.3, 3.0), SULFATE_AEROSOL: (0.05, 0.5)}
 
 
-def generate_aerosolcoeff(seed: int = 9) -> co.AerosolCoeff:
-    """20 wavelengths (frequencies increasing) x 10 RH x 40 radii x 1 sigma x 3
-    types, 38 Legendre terms; scheme 'CRTM' uses the first RH and sigma."""
+def generate_aerosolcoeff(seed: int = 9, scheme: str = "CRTM") -> co.AerosolCoeff:
+    """Synthetic AerosolCoeff table for one scheme, 20 wavelengths
+    (frequencies increasing) x 3 types, 38 Legendre terms, smooth Mie-like
+    optics (extinction efficiency 2x^2/(1+x^2) of the size parameter x):
+
+    - 'CRTM': 10 RH x 40 radii x 1 sigma; the scheme reads the first RH;
+    - 'CMAQ': 1 RH x 40 radii x 6 log-normal widths sigma; broader size
+      distributions act as larger particles;
+    - 'GOCART-GEOS5' / 'NAAPS': 8 RH x 1 radius x 1 sigma; hygroscopic growth
+      (kappa per type) swells the dry radius with relative humidity."""
     rng = np.random.Generator(np.random.PCG64(seed))
     wl = np.geomspace(25.0, 0.3, 20)                      # microns, decreasing
     nu = 1.0e4 / wl                                        # cm^-1, increasing
-    nrh, nr, nt, nl = 10, 40, len(AEROSOL_TYPES), CLOUD_N_LEGENDRE
-    reff = np.stack([np.geomspace(0.01, 20.0, nr)] * nt, axis=1)
-    rsig = np.ones((1, nt))
-    rh = np.linspace(0.0, 0.99, nrh)
-    x = 2.0 * np.pi * reff[None, :, :] * nu[:, None, None] / 1.0e4          # (w, r, type)
-    q = 2.0 * x ** 2 / (1.0 + x ** 2)
-    dens = np.array([2.6, 2.2, 1.7])[None, None, :]        # g/cm^3
-    ke = 0.75 * q / (dens * 1.0e3 * reff[None, :, :] * 1.0e-6)            # m^2/kg
-    w = np.clip(np.array([0.75, 0.98, 0.95])[None, None, :] * x / (1.0 + x) + 0.02, 0.01, 0.995)
-    g = 0.7 * x / (1.0 + x)
-    jit = 1.0 + 0.02 * rng.standard_normal(ke.shape)
-    ke = ke * jit
-    ke5 = np.repeat(ke[:, None, :, None, :], nrh, axis=1)
-    w5 = np.repeat(w[:, None, :, None, :], nrh, axis=1)
-    g5 = np.repeat(g[:, None, :, None, :], nrh, axis=1)
+    nt, nl = len(AEROSOL_TYPES), CLOUD_N_LEGENDRE
+    dens = np.array([2.6, 2.2, 1.7])                       # g/cm^3
+    w0 = np.array([0.75, 0.98, 0.95])
+
+    def optics(r_eff, r_mass):
+        """r_eff (..., type) optical radius, r_mass the radius of the dry mass:
+        ke [m^2/kg], w, g with the wavelength axis first."""
+        x = 2.0 * np.pi * r_eff[None] * nu.reshape((-1,) + (1,) * r_eff.ndim) / 1.0e4
+        q = 2.0 * x ** 2 / (1.0 + x ** 2)
+        ke = 0.75 * q * (r_eff / r_mass)[None] ** 2 / (dens * 1.0e3 * r_mass[None] * 1.0e-6)
+        w = np.clip(w0 * x / (1.0 + x) + 0.02, 0.01, 0.995)
+        g = 0.7 * x / (1.0 + x)
+        return ke * (1.0 + 0.02 * rng.standard_normal(ke.shape)), w, g
+
+    if scheme in ("CRTM", "CMAQ"):
+        nrh, nr = (10, 40) if scheme == "CRTM" else (1, 40)
+        reff = np.stack([np.geomspace(0.01, 20.0, nr)] * nt, axis=1)            # (r, type)
+        rh = np.linspace(0.0, 0.99, nrh) if scheme == "CRTM" else np.zeros(1)
+        if scheme == "CRTM":
+            rsig = np.ones((1, nt))
+            ke, w, g = optics(reff, reff)                                        # (w, r, type)
+            ke5, w5, g5 = (np.repeat(a[:, None, :, None, :], nrh, axis=1) for a in (ke, w, g))
+        else:
+            ns = 6
+            rsig = np.stack([np.linspace(1.1, 2.6, ns)] * nt, axis=1)            # (sigma, type)
+            broad = np.exp(0.5 * np.log(rsig) ** 2)                              # (sigma, type)
+            r_opt = reff[:, None, :] * broad[None, :, :]                         # (r, sigma, type)
+            ke, w, g = optics(r_opt, np.broadcast_to(reff[:, None, :], r_opt.shape))
+            ke5, w5, g5 = (a[:, None] for a in (ke, w, g))                       # (w, 1, r, sigma, type)
+    else:
+        nrh = 8
+        rh = np.array([0.0, 0.5, 0.7, 0.8, 0.9, 0.95, 0.98, 0.99])
+        rdry = np.array([1.5, 1.0, 0.15])
+        kappa = np.array([0.05, 1.0, 0.6])
+        gf = (1.0 + kappa[None, :] * rh[:, None] / (1.0 - rh[:, None])) ** (1.0 / 3.0)   # (rh, type)
+        r_wet = rdry[None, :] * gf
+        ke, w, g = optics(r_wet, np.broadcast_to(rdry[None, :], r_wet.shape))           # (w, rh, type)
+        reff = rdry[None, :].copy()
+        rsig = np.ones((1, nt))
+        ke5, w5, g5 = (a[:, :, None, None, :] for a in (ke, w, g))                      # (w, rh, 1, 1, type)
     pc = 0.5 * g5[..., None] ** np.arange(nl + 1)
     return co.AerosolCoeff(np.array(AEROSOL_TYPES, np.int32), ["Dust", "SeaSalt", "Sulfate"], wl, reff,
-                           rsig, rh, ke5, w5, g5, pc[..., None])
+                           rsig, rh, np.ascontiguousarray(ke5), np.ascontiguousarray(w5),
+                           np.ascontiguousarray(g5), pc[..., None])
 
 
-def write_aerosol_files(coeff_dir: str) -> str:
-    """Write ``AerosolCoeff.bin`` (the reference's default file name) if missing."""
+def aerosol_file_name(scheme: str = "CRTM") -> str:
+    """``AerosolCoeff.bin`` (the reference's default name) for 'CRTM', else
+    ``AerosolCoeff.<scheme>.bin``."""
+    return "AerosolCoeff.bin" if scheme == "CRTM" else f"AerosolCoeff.{scheme}.bin"
+
+
+def write_aerosol_files(coeff_dir: str, scheme: str = "CRTM") -> str:
+    """Write the scheme's synthetic AerosolCoeff file if missing."""
     os.makedirs(coeff_dir, exist_ok=True)
-    path = os.path.join(coeff_dir, "AerosolCoeff.bin")
+    path = os.path.join(coeff_dir, aerosol_file_name(scheme))
     if not os.path.exists(path):
-        co.write_aerosolcoeff(path + ".tmp", generate_aerosolcoeff())
+        co.write_aerosolcoeff(path + ".tmp", generate_aerosolcoeff(scheme=scheme), scheme=scheme)
         os.replace(path + ".tmp", path)
     return path
+
+
+def add_aerosol_scheme_inputs(atm: AtmosphereBatch, seed: int) -> AtmosphereBatch:
+    """Effective_Variance (the 'CMAQ' table's sigma, uniform in [1.2, 2.4] per
+    aerosol and profile) and Relative_Humidity (0.3-0.95 at the surface,
+    falling with height) for the aerosol schemes that read them."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    P, K = atm.n_profiles, atm.max_layers
+    NA = atm.aerosol_type.shape[1]
+    atm.aerosol_effective_variance = np.repeat(rng.uniform(1.2, 2.4, (P, NA))[:, :, None], K, axis=2)
+    z = height_km(np.maximum(atm.pressure, 1e-3))
+    atm.relative_humidity = np.clip(rng.uniform(0.3, 0.95, (P, 1)) * np.exp(-z / 8.0), 0.0, 0.99)
+    return atm
 
 
 def add_aerosols(atm: AtmosphereBatch, aerosol_types: Sequence[int], seed: int,

@@ -99,9 +99,10 @@ typedef struct {
   /* Options%RT_Algorithm_Id for cloudy profiles: 56 ADA, 168 SOI
    * (src/CRTM_Parameters.f90:247-248); NULL: ADA everywhere. */
   const int* rt_algorithm_id;     /* [P] */
-  /* aerosols (CRTM_Aerosol_type, Atmosphere%Aerosol(:)), AerosolCoeff scheme
-   * 'CRTM'; max_aerosols = 0: none.  Aerosols scatter for infrared, visible
-   * and ultraviolet sensors only (the reference skips them for microwave). */
+  /* aerosols (CRTM_Aerosol_type, Atmosphere%Aerosol(:)), in the handle's
+   * AerosolCoeff scheme (crtm_gpu_init_aerosol); max_aerosols = 0: none.
+   * Aerosols scatter for infrared, visible and ultraviolet sensors only (the
+   * reference skips them for microwave). */
   int max_aerosols;               /* NA: stride of the aerosol arrays */
   const int* n_aerosols;          /* [P] aerosols of each profile, <= NA */
   const int* aerosol_type;        /* [P][NA] AerosolCoeff Type ids */
@@ -119,6 +120,13 @@ typedef struct {
   /* Options%Overlap_Id: 1 maximum, 2 random, 3 maximum-random, 4 average,
    * 5 overcast; NULL: 4 (the reference's default). */
   const int* overlap_id;          /* [P] */
+  /* Atmosphere%Aerosol(n)%Effective_Variance (the 'CMAQ' table's sigma axis)
+   * and Atmosphere%Relative_Humidity (0-1, the 'GOCART-GEOS5' / 'NAAPS' RH
+   * axis), read by those schemes only (CRTM_AerosolScatter.f90:245-252).
+   * NULL: zero, as the reference initialises them; the LUT lookup clamps
+   * each to its axis. */
+  const double* aerosol_effective_variance; /* [P][NA][max_layers] */
+  const double* relative_humidity;          /* [P][max_layers] */
 } crtm_gpu_batch;
 
 typedef struct {
@@ -155,6 +163,11 @@ typedef struct {
   double* land_temperature;
   double* snow_temperature;
   double* ice_temperature;
+  /* Atmosphere_K%Aerosol(n)%Effective_Variance [P][L][max_aerosols][max_layers]
+   * ('CMAQ') and Atmosphere_K%Relative_Humidity [P][L][max_layers]
+   * ('GOCART-GEOS5', 'NAAPS'), or NULL; zero under the other schemes. */
+  double* aerosol_effective_variance;
+  double* relative_humidity;
 } crtm_gpu_kmatrix;
 
 typedef struct {
@@ -172,6 +185,8 @@ typedef struct {
   double* land_temperature;   /* [P] Surface_AD%Land_Temperature, or NULL */
   double* snow_temperature;   /* [P] */
   double* ice_temperature;    /* [P] */
+  double* aerosol_effective_variance; /* [P][max_aerosols][max_layers], or NULL */
+  double* relative_humidity;          /* [P][max_layers], or NULL */
 } crtm_gpu_adjoint_out;
 
 /* Tangent-linear inputs (Atmosphere_TL, Surface_TL and the emissivity
@@ -193,6 +208,8 @@ typedef struct {
   const double* cloud_fraction;
   const double* aerosol_concentration;
   const double* aerosol_effective_radius;
+  const double* aerosol_effective_variance; /* [P][max_aerosols][max_layers] */
+  const double* relative_humidity;          /* [P][max_layers] */
 } crtm_gpu_tl_in;
 
 /* CRTM_Init: loads <coeff_path>/<sensor_id>.SpcCoeff.bin and .TauCoeff.bin
@@ -202,6 +219,16 @@ typedef struct {
  * or aerosols need the matching LUT. */
 int crtm_gpu_init(const char* coeff_path, int n_sensors, const char* const* sensor_ids,
                   crtm_gpu_handle* handle);
+
+/* CRTM_Init with its Aerosol_Model and AerosolCoeff_File arguments
+ * (src/CRTM_LifeCycle.f90:523-561,678,706): aerosol_model 'CRTM' (the
+ * default), 'CMAQ', 'GOCART-GEOS5' or 'NAAPS' selects the LUT layout and
+ * interpolation (CRTM_AerosolScatter.f90:822-918); aerosol_coeff_file is the
+ * LUT's file name under coeff_path (NULL: AerosolCoeff.bin).  NULL
+ * aerosol_model means 'CRTM'. */
+int crtm_gpu_init_aerosol(const char* coeff_path, int n_sensors, const char* const* sensor_ids,
+                          const char* aerosol_model, const char* aerosol_coeff_file,
+                          crtm_gpu_handle* handle);
 
 /* CRTM_Destroy */
 int crtm_gpu_destroy(crtm_gpu_handle handle);

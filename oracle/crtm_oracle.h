@@ -105,10 +105,17 @@ typedef struct {
   const double* aerosol_effective_radius;  /* [P][NA][max_layers] microns */
   const double* cloud_fraction;    /* [P][max_layers] Cloud_Fraction; NULL: 1 in every layer */
   const int* overlap;              /* [P] Options%Overlap_Id 1-5; NULL: 4 (average) */
+  const double* aerosol_effective_variance;  /* [P][NA][max_layers] ('CMAQ'); NULL: 0 */
+  const double* relative_humidity; /* [P][max_layers] Atmosphere%Relative_Humidity ('GOCART-GEOS5',
+                                      'NAAPS'); NULL: 0 */
 } or_clouds;
 
 typedef struct or_aerosol_s or_aerosol;
-/* Load an AerosolCoeff binary file (Release 4, scheme 'CRTM'). */
+enum { OR_AEROSOL_CRTM = 0, OR_AEROSOL_CMAQ = 1, OR_AEROSOL_GOCART = 2, OR_AEROSOL_NAAPS = 3 };
+/* Load an AerosolCoeff binary file (Release 4) for the scheme 'CRTM',
+ * 'CMAQ', 'GOCART-GEOS5' or 'NAAPS' (CRTM_Init's Aerosol_Model). */
+or_aerosol* or_aerosol_init_scheme(const char* path, const char* scheme);
+/* scheme 'CRTM' */
 or_aerosol* or_aerosol_init(const char* path);
 void or_aerosol_destroy(or_aerosol* a);
 

@@ -38,7 +38,8 @@ class OrClouds(ct.Structure):
                 ("water_content", _dp), ("effective_radius", _dp), ("n_streams", _ip),
                 ("rt_algorithm", _ip), ("max_aerosols", ct.c_int), ("n_aerosols", _ip),
                 ("aerosol_type", _ip), ("aerosol_concentration", _dp), ("aerosol_effective_radius", _dp),
-                ("cloud_fraction", _dp), ("overlap", _ip)]
+                ("cloud_fraction", _dp), ("overlap", _ip), ("aerosol_effective_variance", _dp),
+                ("relative_humidity", _dp)]
 
 
 def build(force: bool = False) -> str:
@@ -76,6 +77,8 @@ def lib():
                                          ct.POINTER(OrClouds), _dp, _dp, ct.c_int]
         L.or_aerosol_init.restype = ct.c_void_p
         L.or_aerosol_init.argtypes = [ct.c_char_p]
+        L.or_aerosol_init_scheme.restype = ct.c_void_p
+        L.or_aerosol_init_scheme.argtypes = [ct.c_char_p, ct.c_char_p]
         L.or_aerosol_destroy.argtypes = [ct.c_void_p]
         L.or_amom_layer.argtypes = [ct.c_int, ct.c_int, ct.c_double, ct.c_double, _dp, _dp, _dp, _dp,
                                     ct.c_double, _dp, _dp, _dp]
@@ -169,9 +172,11 @@ class Oracle:
         return dict(radiance=rad, bt=bt, temperature_ad=ta, absorber_ad=aa, water_temperature_ad=wa)
 
     def forward_scatter(self, atm, sfc, geo, opt, cloudcoeff_path: Optional[str] = None,
-                        aerosolcoeff_path: Optional[str] = None, n_threads: int = 1):
+                        aerosolcoeff_path: Optional[str] = None, n_threads: int = 1,
+                        aerosol_scheme: str = "CRTM"):
         """Forward with clouds and aerosols (ADA or SOI per Options%RT_Algorithm_Id);
-        profiles without either take the Emission solver."""
+        profiles without either take the Emission solver.  aerosol_scheme is
+        CRTM_Init's Aerosol_Model for the AerosolCoeff file."""
         L = lib()
         ch = ah = None
         try:
@@ -180,7 +185,7 @@ class Oracle:
                 if not ch:
                     raise IOError(L.or_last_error().decode())
             if aerosolcoeff_path:
-                ah = L.or_aerosol_init(aerosolcoeff_path.encode())
+                ah = L.or_aerosol_init_scheme(aerosolcoeff_path.encode(), aerosol_scheme.encode())
                 if not ah:
                     raise IOError(L.or_last_error().decode())
             P, nL = atm.n_profiles, self.n_channels
@@ -203,6 +208,10 @@ class Oracle:
                 c.aerosol_type = _p(arr(atm.aerosol_type, np.int32), _ip)
                 c.aerosol_concentration = _p(arr(atm.aerosol_concentration))
                 c.aerosol_effective_radius = _p(arr(atm.aerosol_effective_radius))
+                if getattr(atm, "aerosol_effective_variance", None) is not None:
+                    c.aerosol_effective_variance = _p(arr(atm.aerosol_effective_variance))
+                if getattr(atm, "relative_humidity", None) is not None:
+                    c.relative_humidity = _p(arr(atm.relative_humidity))
             if opt.n_streams is not None:
                 use = opt.use_n_streams if opt.use_n_streams is not None else np.ones(P, bool)
                 c.n_streams = _p(arr(np.where(use, opt.n_streams, 0), np.int32), _ip)

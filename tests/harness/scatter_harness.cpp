@@ -67,13 +67,17 @@ int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, 
                        double planck_surface, double cosmic, const double* planck, const double* temp,
                        const int* cloud_type, const double* wc, const double* reff, int cstride,
                        const double* od, int soi, int n_aer, const int* aer_type, const double* conc,
-                       const double* aer_reff, const int* adims, const int* atypes, const double* afreq,
-                       const double* areff, const double* ake, const double* aw, const double* apc,
-                       double wavenumber, double* radiance) {
+                       const double* aer_reff, const double* aer_var, const double* rh_layers,
+                       const int* adims, const int* atypes, const double* afreq, const double* areff,
+                       const double* arsig, const double* arh, const double* ake, const double* aw,
+                       const double* apc, double wavenumber, double* radiance) {
+  // adims: nw nrh nr ns nt nleg scheme n_rh_axis
   AerosolLut A{};
   if (n_aer > 0) {
     A.nw = adims[0]; A.nrh = adims[1]; A.nr = adims[2]; A.ns = adims[3]; A.nt = adims[4]; A.nleg = adims[5];
-    A.type_id = atypes; A.freq = afreq; A.reff = areff; A.ke = ake; A.w = aw; A.pc = apc;
+    A.scheme = adims[6]; A.nrh_axis = adims[7];
+    A.type_id = atypes; A.freq = afreq; A.reff = areff; A.rsig = arsig; A.rh = arh; A.ke = ake; A.w = aw;
+    A.pc = apc;
   }
   CloudLut L{dims[0], dims[1], dims[2], dims[3], dims[4], dims[5], dims[6], f_mw, r_mw, t, f_ir, r_ir,
              ke_l, w_l, pc_l, ke_s, w_s, pc_s, ke_ir, w_ir, pc_ir};
@@ -84,7 +88,7 @@ int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, 
   c.c1 = planck[0]; c.c2 = planck[1]; c.b1 = planck[2]; c.b2 = planck[3];
   c.temperature = temp; c.cloud_type = cloud_type; c.wc = wc; c.reff = reff; c.cstride = (size_t)cstride;
   c.n_aerosols = n_aer; c.wavenumber = wavenumber; c.aerosol_type = aer_type; c.conc = conc;
-  c.aer_reff = aer_reff; c.alut = &A;
+  c.aer_reff = aer_reff; c.aer_var = aer_var; c.rh = rh_layers; c.alut = &A;
   c.soi = soi != 0;
   if (soi == 2 || soi == 3) {   // layered ADA as the GPU kernels run it (records with NZ = 5);
     c.soi = false;              // soi = 3: layer optics in double-float (the mixed form)
@@ -310,3 +314,55 @@ extern "C" int sx_cloudy_kmatrix(const int* dims, const double* f_mw, const doub
   return bad;
 }
 
+
+
+// One aerosol-only layer's record (od, T, R, src) and its derivatives with
+// respect to aerosol a's concentration and first LUT coordinate (radius, or
+// the layer's relative humidity for 'GOCART-GEOS5' / 'NAAPS'), from the
+// derivative-number evaluation the K-matrix contraction uses
+// (layer_optics_dual), and the MOM eigenvalue gap at the sensor angle.
+// adims as sx_cloudy_radiance's.
+extern "C" int sx_aerosol_layer_record(const int* adims, const int* atypes, const double* afreq,
+                                       const double* areff, const double* arsig, const double* arh,
+                                       const double* ake, const double* aw, const double* apc, int n_aer,
+                                       const int* aer_type, const double* conc, const double* aer_reff,
+                                       const double* aer_var, double rh_layer, int nleg, double mu_sensor,
+                                       const double* planck, double wavenumber, double gas, double tk, int a,
+                                       double* val, double* dconc, double* dc1, int* nz_out, double* gap_out) {
+  AerosolLut A{};
+  A.nw = adims[0]; A.nrh = adims[1]; A.nr = adims[2]; A.ns = adims[3]; A.nt = adims[4]; A.nleg = adims[5];
+  A.scheme = adims[6]; A.nrh_axis = adims[7];
+  A.type_id = atypes; A.freq = afreq; A.reff = areff; A.rsig = arsig; A.rh = arh; A.ke = ake; A.w = aw;
+  A.pc = apc;
+  CloudLut L{};
+  static const GaussTable gt = make_gauss();
+  CloudyColumn c{};
+  c.Ku = 1; c.n_clouds = 0; c.nleg = nleg; c.microwave = false; c.freq = wavenumber; c.mu_sensor = mu_sensor;
+  c.c1 = planck[0]; c.c2 = planck[1]; c.b1 = planck[2]; c.b2 = planck[3];
+  c.n_aerosols = n_aer; c.wavenumber = wavenumber; c.aerosol_type = aer_type; c.conc = conc;
+  c.aer_reff = aer_reff; c.aer_var = aer_var; c.rh = &rh_layer; c.cstride = 1; c.alut = &A;
+  constexpr int NZ = SC_NZ_MAX;
+  StreamSet<NZ, double> S;
+  if (int rc = stream_set<NZ, double>(nleg, mu_sensor, -1, gt, S)) return -100 - rc;
+  using D = Dual<2>;
+  auto seed = [&](int s, D& amount, D& c1, D&) {
+    if (s == a) { amount.d[0] = 1.0; c1.d[1] = 1.0; }
+  };
+  Mat<NZ, D> Tm, Rm;
+  D src[NZ], od;
+  const int kind = layer_optics_dual<NZ>(c, L, S, 0, D(gas), D(tk), &od, Tm, Rm, src, seed);
+  const int nZ = S.nZ;
+  *nz_out = nZ;
+  if (gap_out) {   // the MOM eigenvalue gap at the sensor angle (plain evaluation)
+    Mat<NZ, double> T0, R0;
+    double s0[NZ], o0;
+    *gap_out = 1.0;
+    layer_optics<NZ, double>(c, L, S, 0, gas, tk, &o0, T0, R0, s0, NoSeed(), gap_out);
+  }
+  auto put = [&](const D& x, int i) { val[i] = x.v; dconc[i] = x.d[0]; dc1[i] = x.d[1]; };
+  put(od, 0);
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) { put(Tm.a[i][j], 1 + i * nZ + j); put(Rm.a[i][j], 1 + nZ * nZ + i * nZ + j); }
+  for (int i = 0; i < nZ; i++) put(src[i], 1 + 2 * nZ * nZ + i);
+  return kind;
+}

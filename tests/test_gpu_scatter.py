@@ -4,6 +4,8 @@ Tolerances: 1e-4 K in brightness temperature in the FP64 form.  In the mixed
 form the gas layer optical depths come from the FP32 regression (the
 scattering solver is FP64 in both forms), so 0.01 K as for clear sky.
 """
+import copy
+
 import numpy as np
 import pytest
 
@@ -105,6 +107,42 @@ def test_aerosols_match_oracle(gpu_lib, cloud_dir, precision, clouds, soi):
                                                        f"{cloud_dir}/CloudCoeff.bin" if clouds else None, apath)
     rts = gpu_lib.CRTM([sensor], cloud_dir, precision).forward(atm, sfc, geo, opt)
     assert np.abs(rts.brightness_temperature - ref).max() <= BT_TOL[precision]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("scheme,soi", [("CMAQ", False), ("GOCART-GEOS5", False), ("NAAPS", True),
+                                        ("CMAQ", True)])
+def test_aerosol_schemes_match_oracle(gpu_lib, cloud_dir, precision, scheme, soi):
+    """CRTM_Init's Aerosol_Model: 'CMAQ' interpolates the LUT in (frequency,
+    radius, sigma) with Effective_Variance as sigma, 'GOCART-GEOS5' / 'NAAPS' in
+    (frequency, RH) with the layers' Relative_Humidity; liquid and ice clouds
+    beside the aerosols, one aerosol-only and one clear profile."""
+    from oracle.pyoracle import Oracle
+    sensor = "irsynth_c616"
+    apath = sy.write_aerosol_files(cloud_dir, scheme)
+    atm, sfc, geo, opt = sy.clear_sky_workload(sensor, 5, 101, 71)
+    sy.add_clouds(atm, (co.WATER_CLOUD, co.ICE_CLOUD), 72, wc_scale=50.0)
+    sy.add_aerosols(atm, sy.AEROSOL_TYPES, 73, load_scale=20.0)
+    sy.add_aerosol_scheme_inputs(atm, 74)
+    atm.n_clouds[1] = 0
+    atm.n_aerosols[3] = atm.n_clouds[3] = 0
+    if soi:
+        opt.rt_algorithm_id = np.array([168, 56, 168, 168, 56], np.int32)
+    _, ref = Oracle(cloud_dir, sensor).forward_scatter(atm, sfc, geo, opt, f"{cloud_dir}/CloudCoeff.bin", apath,
+                                                       aerosol_scheme=scheme)
+    h = gpu_lib.CRTM([sensor], cloud_dir, precision, aerosol_model=scheme,
+                     aerosol_coeff_file=sy.aerosol_file_name(scheme))
+    rts = h.forward(atm, sfc, geo, opt)
+    assert np.abs(rts.brightness_temperature - ref).max() <= BT_TOL[precision]
+    # the scheme's coordinate matters: without it the radiances move
+    bare = copy.deepcopy(atm)
+    bare.aerosol_effective_variance = bare.relative_humidity = None
+    assert np.abs(h.forward(bare, sfc, geo, opt).brightness_temperature - rts.brightness_temperature).max() > 1e-3
+
+
+def test_unknown_aerosol_model_is_refused(gpu_lib, cloud_dir):
+    with pytest.raises(RuntimeError, match="Aerosol_Model"):
+        gpu_lib.CRTM(["irsynth_c616"], cloud_dir, 0, aerosol_model="OPAC")
 
 
 @pytest.mark.parametrize("precision", [0, 1])

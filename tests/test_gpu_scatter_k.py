@@ -192,6 +192,89 @@ def test_aerosol_k_matrix_matches_oracle_differences(gpu_lib, cloud_dir):
     _check_species(km, orc, cloud_dir, atm, sfc, geo, opt, _layers(atm, (30, 90))[:4])
 
 
+@pytest.mark.parametrize("scheme", ["CMAQ", "GOCART-GEOS5", "NAAPS"])
+def test_aerosol_scheme_k_matrix_matches_oracle_differences(gpu_lib, cloud_dir, scheme):
+    """K-matrix under CRTM_Init's other aerosol models: concentration (and, for
+    'CMAQ', radius and Effective_Variance; for 'GOCART-GEOS5' / 'NAAPS' the
+    layers' Relative_Humidity, summed over the aerosols that read it) against
+    central differences of the oracle's forward in the same scheme; the
+    coordinates a scheme does not read have zero Jacobians.  The adjoint is
+    the seeded K-matrix summed over channels."""
+    from oracle.pyoracle import Oracle
+    sensor = "irsynth_c616"
+    apath = sy.write_aerosol_files(cloud_dir, scheme)
+    atm, sfc, geo, opt = sy.clear_sky_workload(sensor, 4, 101, 97)
+    sy.add_clouds(atm, (co.WATER_CLOUD, co.ICE_CLOUD), 98, wc_scale=30.0)
+    sy.add_aerosols(atm, sy.AEROSOL_TYPES, 99, load_scale=20.0)
+    sy.add_aerosol_scheme_inputs(atm, 100)
+    atm.n_clouds[1] = 0
+    atm.n_aerosols[3] = 0
+    h = gpu_lib.CRTM([sensor], cloud_dir, 0, aerosol_model=scheme, aerosol_coeff_file=sy.aerosol_file_name(scheme))
+    km, rts = h.k_matrix(atm, sfc, geo, opt)
+    orc = Oracle(cloud_dir, sensor)
+    _, bt = orc.forward_scatter(atm, sfc, geo, opt, f"{cloud_dir}/CloudCoeff.bin", apath, n_threads=8,
+                                aerosol_scheme=scheme)
+    assert np.abs(rts.brightness_temperature - bt).max() <= 1e-4
+
+    def fd(perturb, step):
+        out = []
+        for sgn in (1.0, -1.0):
+            a = copy.deepcopy(atm)
+            perturb(a, sgn * step)
+            out.append(orc.forward_scatter(a, sfc, geo, opt, f"{cloud_dir}/CloudCoeff.bin", apath, n_threads=8,
+                                           aerosol_scheme=scheme)[1])
+        st = np.asarray(step, np.float64)
+        den = 2.0 * (st[:, None] if st.ndim else st)
+        return (out[0] - out[1]) / np.where(den == 0.0, 1.0, den)
+    layers = sorted(set([5, 40, 80, 95]) | set(np.nonzero(atm.aerosol_concentration[0].max(axis=0) > 1e-7)[0][-3:]))
+    fields = [("aerosol_concentration", "aerosol_concentration")]
+    if scheme == "CMAQ":
+        fields += [("aerosol_effective_radius", "aerosol_effective_radius"),
+                   ("aerosol_effective_variance", "aerosol_effective_variance")]
+    checked = 0
+    for k in layers:
+        for kname, aname in fields:
+            for c in range(atm.aerosol_type.shape[1]):
+                val = getattr(atm, aname)[:, c, k]
+                on = atm.aerosol_concentration[:, c, k] > 1e-9
+                if not on.any():
+                    continue
+
+                def pert(a, hh, aname=aname, c=c, k=k):
+                    getattr(a, aname)[:, c, k] += hh
+                d = fd(pert, np.where(on, 1e-4 * val, 0.0))
+                got = getattr(km, kname)[:, :, c, k]
+                scale = max(np.abs(getattr(km, kname)[:, :, c] * getattr(atm, aname)[:, None, c]).max(), 1e-12)
+                err = np.abs((got - d)[on] * val[on, None]).max()
+                assert err <= FD_TOL * scale, (kname, c, k, err / scale)
+                checked += 1
+        if scheme != "CMAQ":
+            on = (atm.aerosol_concentration[:, :, k] > 1e-9).any(axis=1) & (atm.relative_humidity[:, k] > 0.0)
+            if on.any():
+                def prh(a, hh, k=k):
+                    a.relative_humidity[:, k] += hh
+                d = fd(prh, np.where(on, 1e-4 * atm.relative_humidity[:, k], 0.0))
+                got = km.relative_humidity[:, :, k]
+                scale = max(np.abs(km.relative_humidity * atm.relative_humidity[:, None, :]).max(), 1e-12)
+                err = np.abs((got - d)[on] * atm.relative_humidity[on, k][:, None]).max()
+                assert err <= FD_TOL * scale, ("relative_humidity", k, err / scale)
+                checked += 1
+    assert checked > 0
+    if scheme == "CMAQ":
+        assert np.abs(km.aerosol_effective_variance).max() > 0
+        assert getattr(km, "relative_humidity", None) is None
+    else:
+        assert np.abs(km.relative_humidity).max() > 0
+        assert np.abs(km.aerosol_effective_radius).max() == 0.0
+    # adjoint = seeded K-matrix summed over the channels
+    seed = np.random.Generator(np.random.PCG64(101)).standard_normal((4, 616))
+    km2, _ = h.k_matrix(atm, sfc, geo, opt, seed)
+    ad, _ = h.adjoint(atm, sfc, geo, opt, seed)
+    for f in ("aerosol_concentration", "aerosol_effective_radius",
+              "aerosol_effective_variance" if scheme == "CMAQ" else "relative_humidity"):
+        assert _rel(ad[f], getattr(km2, f).sum(axis=1)) <= 1e-10, f
+
+
 @pytest.mark.parametrize("sensor,n_streams", [("mwsynth_c16", None), ("irsynth_c616", None),
                                               ("mwsynth_c16", 8)])
 def test_mixed_cloudy_k_matrix_matches_fp64(gpu_lib, cloud_dir, sensor, n_streams):

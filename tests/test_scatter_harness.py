@@ -52,22 +52,28 @@ def test_ada_layer_matches_oracle(sx, nleg, mu_s, w, tau):
         assert np.abs(a - b).max() < 1e-12
 
 
-@pytest.mark.parametrize("sensor,nl,n_streams,soi,aer", [
-    ("mwsynth_c16", 100, None, 0, 0), ("mwsynth_c16", 100, 16, 0, 0), ("irsynth_c616", 101, None, 0, 0),
-    ("mwsynth_c22", 100, 8, 0, 0), ("mwsynth_c16", 100, None, 1, 0), ("mwsynth_c16", 100, 16, 1, 0),
-    ("irsynth_c616", 101, None, 1, 0), ("mwsynth_c16", 100, None, 2, 0), ("irsynth_c616", 101, None, 2, 0),
-    ("irsynth_c616", 101, None, 0, 1), ("irsynth_c616", 101, 8, 1, 1), ("irsynth_c616", 101, None, 0, 2),
-    ("mwsynth_c16", 100, None, 0, 1), ("mwsynth_c16", 100, None, 3, 0), ("irsynth_c616", 101, None, 3, 1),
-    ("irsynth_c616", 101, None, 3, 2)])
-def test_cloudy_radiance_matches_oracle(sx, coeff_dir, sensor, nl, n_streams, soi, aer):
+@pytest.mark.parametrize("sensor,nl,n_streams,soi,aer,scheme", [
+    ("mwsynth_c16", 100, None, 0, 0, "CRTM"), ("mwsynth_c16", 100, 16, 0, 0, "CRTM"),
+    ("irsynth_c616", 101, None, 0, 0, "CRTM"), ("mwsynth_c22", 100, 8, 0, 0, "CRTM"),
+    ("mwsynth_c16", 100, None, 1, 0, "CRTM"), ("mwsynth_c16", 100, 16, 1, 0, "CRTM"),
+    ("irsynth_c616", 101, None, 1, 0, "CRTM"), ("mwsynth_c16", 100, None, 2, 0, "CRTM"),
+    ("irsynth_c616", 101, None, 2, 0, "CRTM"), ("irsynth_c616", 101, None, 0, 1, "CRTM"),
+    ("irsynth_c616", 101, 8, 1, 1, "CRTM"), ("irsynth_c616", 101, None, 0, 2, "CRTM"),
+    ("mwsynth_c16", 100, None, 0, 1, "CRTM"), ("mwsynth_c16", 100, None, 3, 0, "CRTM"),
+    ("irsynth_c616", 101, None, 3, 1, "CRTM"), ("irsynth_c616", 101, None, 3, 2, "CRTM"),
+    ("irsynth_c616", 101, None, 0, 1, "CMAQ"), ("irsynth_c616", 101, 8, 1, 2, "CMAQ"),
+    ("irsynth_c616", 101, None, 0, 1, "GOCART-GEOS5"), ("irsynth_c616", 101, None, 1, 2, "NAAPS")])
+def test_cloudy_radiance_matches_oracle(sx, coeff_dir, sensor, nl, n_streams, soi, aer, scheme):
     """aer 1: clouds and aerosols; aer 2: aerosols only.  soi 2 / 3: layered
     ADA as the GPU kernels run it, with the layer optics in FP64 / in
-    double-float (the mixed form)."""
+    double-float (the mixed form).  scheme: the AerosolCoeff scheme
+    (CRTM_Init's Aerosol_Model) with its effective variance and relative
+    humidity inputs."""
     from oracle.pyoracle import Oracle
     path = sy.write_cloud_files(coeff_dir)
-    apath = sy.write_aerosol_files(coeff_dir)
+    apath = sy.write_aerosol_files(coeff_dir, scheme)
     cc = co.read_cloudcoeff(path)
-    ac = co.read_aerosolcoeff(apath)
+    ac = co.read_aerosolcoeff(apath, scheme)
     sc = co.read_spccoeff(f"{coeff_dir}/{sensor}.SpcCoeff.bin")
     o = Oracle(coeff_dir, sensor)
     atm, sfc, geo, opt = sy.cloudy_workload(sensor, 3, nl, 51, wc_scale=200.0, n_streams=n_streams)
@@ -75,9 +81,10 @@ def test_cloudy_radiance_matches_oracle(sx, coeff_dir, sensor, nl, n_streams, so
         opt.rt_algorithm_id = np.full(atm.n_profiles, 168, np.int32)
     if aer:
         sy.add_aerosols(atm, sy.AEROSOL_TYPES, 52, load_scale=30.0)
+        sy.add_aerosol_scheme_inputs(atm, 53)
     if aer == 2:
         atm.n_clouds[:] = 0
-    rad_ref, _ = o.forward_scatter(atm, sfc, geo, opt, path, apath if aer else None)
+    rad_ref, _ = o.forward_scatter(atm, sfc, geo, opt, path, apath if aer else None, aerosol_scheme=scheme)
     _, _, lod = o.forward(atm, sfc, geo, opt, layer_od=True)
     f = lambda a: np.ascontiguousarray(np.ravel(a, order="F"))   # noqa: E731
     arrs = [f(x) for x in (cc.frequency_mw, cc.reff_mw, cc.temperature, cc.frequency_ir, cc.reff_ir,
@@ -87,9 +94,9 @@ def test_cloudy_radiance_matches_oracle(sx, coeff_dir, sensor, nl, n_streams, so
                      cc.frequency_ir.size, cc.reff_ir.size, cc.n_legendre_terms], np.int32)
     mw = sc.sensor_type == co.MICROWAVE_SENSOR
     adims = np.array([ac.wavelength.size, ac.ke.shape[1], ac.ke.shape[2], ac.ke.shape[3], ac.ke.shape[4],
-                      ac.pcoeff.shape[5] - 1], np.int32)
+                      ac.pcoeff.shape[5] - 1, co.AEROSOL_SCHEMES.index(scheme), ac.rh.size], np.int32)
     aarrs = [np.ascontiguousarray(ac.type_id, np.int32)] + [f(x) for x in (
-        1.0e4 / ac.wavelength, ac.reff, ac.ke, ac.w, ac.pcoeff[..., 0])]
+        1.0e4 / ac.wavelength, ac.reff, ac.rsig, ac.rh, ac.ke, ac.w, ac.pcoeff[..., 0])]
     L = sc.n_channels
     chans = range(0, L, max(1, L // 40))
     worst = 0.0
@@ -107,6 +114,8 @@ def test_cloudy_radiance_matches_oracle(sx, coeff_dir, sensor, nl, n_streams, so
         atype = np.ascontiguousarray(atm.aerosol_type[m] if aer else np.zeros(1), np.int32)
         conc = np.ascontiguousarray(atm.aerosol_concentration[m] if aer else np.zeros((1, atm.max_layers)))
         areff = np.ascontiguousarray(atm.aerosol_effective_radius[m] if aer else np.zeros((1, atm.max_layers)))
+        avar = np.ascontiguousarray(atm.aerosol_effective_variance[m] if aer else np.zeros((1, atm.max_layers)))
+        rhl = np.ascontiguousarray(atm.relative_humidity[m] if aer else np.zeros(atm.max_layers))
         for l in chans:
             planck = np.array([sc.planck_c1[l], sc.planck_c2[l], sc.band_c1[l], sc.band_c2[l]])
             te = sc.band_c1[l] + sc.band_c2[l] * ts
@@ -124,7 +133,7 @@ def test_cloudy_radiance_matches_oracle(sx, coeff_dir, sensor, nl, n_streams, so
                 ct.c_double(opt.emissivity[m, l]), ct.c_double(bs),
                 ct.c_double(sc.cosmic_background_radiance[l]), _p(planck), _p(temp), _p(ctype, _ip),
                 _p(wc), _p(re), atm.max_layers, _p(od), soi, na, _p(atype, _ip), _p(conc), _p(areff),
-                _p(adims, _ip), _p(aarrs[0], _ip), *[_p(a) for a in aarrs[1:]],
+                _p(avar), _p(rhl), _p(adims, _ip), _p(aarrs[0], _ip), *[_p(a) for a in aarrs[1:]],
                 ct.c_double(sc.wavenumber[l]), ct.byref(r))
             assert rc == 0
             worst = max(worst, abs(r.value - rad_ref[m, l]) / abs(rad_ref[m, l]))
@@ -232,9 +241,8 @@ def test_cloudy_kmatrix_matches_finite_differences(sx, coeff_dir, sensor, nl, n_
             assert sx.sx_cloudy_radiance(_p(dims, _ip), *[_p(a) for a in arrs], Ku, ctype.size, nleg, int(mw),
                                          ct.c_double(fr), ct.c_double(mu), ct.c_double(e), ct.c_double(bs),
                                          ct.c_double(cbr), _p(planck), _p(temp), _p(ctype, _ip), _p(wc), _p(re),
-                                         atm.max_layers, _p(od), 1 if soi else 0, 0, None, None, None, None,
-                                         None, None,
-                                         None, None, None, None, ct.c_double(sc.wavenumber[l]), ct.byref(r)) == 0
+                                         atm.max_layers, _p(od), 1 if soi else 0, 0, *([None] * 14),
+                                         ct.c_double(sc.wavenumber[l]), ct.byref(r)) == 0
             return r.value
         dg, dT = np.zeros(Ku), np.zeros(Ku)
         dwc, dre = np.zeros_like(wc), np.zeros_like(re)
@@ -415,3 +423,61 @@ def test_ada_layer_in_double_float_matches_fp64(sx, nleg, mu_s, w, tau):
     assert np.abs(outs[0][0] - outs[1][0]).max() <= 1e-11
     assert np.abs(outs[0][1] - outs[1][1]).max() <= 1e-11
     assert np.abs(outs[0][2] - outs[1][2]).max() <= 1e-10 * 1.7
+
+
+def test_nearly_defective_eigenbasis_derivatives(sx, coeff_dir):
+    """A layer whose MOM quadrature eigenvalue nearly meets the sensor angle's
+    (relative gap ~2e-6; an aerosol-only IR layer under the 'GOCART-GEOS5'
+    table): the eigenbasis is nearly defective and derivatives through it lose
+    ~eps/gap^2, while the layer's T, R and source stay smooth.  The K-matrix
+    contraction's evaluation (derivatives at sensor angles mu (1 +- 1e-3))
+    matches central differences of the record with a 1e-2 relative step
+    (smaller steps drown in the ~1e-10 rounding of the record's values there)
+    to 2e-5 of the largest derivative, for each aerosol's concentration."""
+    from oracle.pyoracle import Oracle
+    scheme = "GOCART-GEOS5"
+    sensor = "irsynth_c616"
+    sy.write_cloud_files(coeff_dir)
+    apath = sy.write_aerosol_files(coeff_dir, scheme)
+    ac = co.read_aerosolcoeff(apath, scheme)
+    sc = co.read_spccoeff(f"{coeff_dir}/{sensor}.SpcCoeff.bin")
+    atm, sfc, geo, opt = sy.clear_sky_workload(sensor, 4, 101, 97)
+    sy.add_clouds(atm, (co.WATER_CLOUD, co.ICE_CLOUD), 98, wc_scale=30.0)
+    sy.add_aerosols(atm, sy.AEROSOL_TYPES, 99, load_scale=20.0)
+    sy.add_aerosol_scheme_inputs(atm, 100)
+    _, _, lod = Oracle(coeff_dir, sensor).forward(atm, sfc, geo, opt, layer_od=True)
+    p, l, k = 1, 107, 80
+    f = lambda a: np.ascontiguousarray(np.ravel(a, order="F"))   # noqa: E731
+    adims = np.array([ac.wavelength.size, ac.ke.shape[1], ac.ke.shape[2], ac.ke.shape[3], ac.ke.shape[4],
+                      ac.pcoeff.shape[5] - 1, co.AEROSOL_SCHEMES.index(scheme), ac.rh.size], np.int32)
+    aarrs = [f(x) for x in (1.0e4 / ac.wavelength, ac.reff, ac.rsig, ac.rh, ac.ke, ac.w, ac.pcoeff[..., 0])]
+    atypes = np.ascontiguousarray(ac.type_id, np.int32)
+    planck = np.array([sc.planck_c1[l], sc.planck_c2[l], sc.band_c1[l], sc.band_c2[l]])
+    mu = float(np.cos(np.deg2rad(geo.sensor_zenith_angle[p])))
+    nleg = sx.sx_stream_rule(ct.c_double(atm.aerosol_effective_radius[p].max()), ct.c_double(sc.wavenumber[l]))
+    at = np.ascontiguousarray(atm.aerosol_type[p], np.int32)
+    reff = np.ascontiguousarray(atm.aerosol_effective_radius[p, :, k])
+    var = np.ascontiguousarray(atm.aerosol_effective_variance[p, :, k])
+    rh, gas, tk = float(atm.relative_humidity[p, k]), float(lod[p, l, k]), float(atm.temperature[p, k])
+
+    def rec(conc, a):
+        outs = [np.zeros(2 * 100 + 20) for _ in range(3)]
+        nz, gap = ct.c_int(), ct.c_double()
+        kind = sx.sx_aerosol_layer_record(_p(adims, _ip), _p(atypes, _ip), *[_p(x) for x in aarrs], 3, _p(at, _ip),
+                                          _p(conc), _p(reff), _p(var), ct.c_double(rh), nleg, ct.c_double(mu),
+                                          _p(planck), ct.c_double(sc.wavenumber[l]), ct.c_double(gas),
+                                          ct.c_double(tk), a, *[_p(o) for o in outs], ct.byref(nz), ct.byref(gap))
+        assert kind == 1
+        ne = 1 + 2 * nz.value ** 2 + nz.value
+        return gap.value, [o[:ne] for o in outs]
+    conc0 = np.ascontiguousarray(atm.aerosol_concentration[p, :, k])
+    gap, _ = rec(conc0, 0)
+    assert gap < 1e-5   # the configuration is the nearly defective one
+    for a in range(3):
+        _, (v, dc, _) = rec(conc0, a)
+        h = 1e-2 * conc0[a]
+        c1, c2 = conc0.copy(), conc0.copy()
+        c1[a] += h
+        c2[a] -= h
+        fd = (rec(c1, a)[1][0] - rec(c2, a)[1][0]) / (2 * h)
+        assert np.abs(fd - dc).max() <= 2e-5 * np.abs(fd).max(), a
