@@ -549,7 +549,7 @@ def main():
         "absorb_ad": kr * 4 + 4 + (1 + JK) * kr * 4,
         "absorb_fwd": kr * 4,
     }
-    ncu_pc = {"map_out": 3915.0, "column": 2501.0, "absorb_ad": 1917.0, "absorb_fwd": 495.0}
+    ncu_pc = {"map_out": 3908.0, "column": 2568.0, "absorb_ad": 1934.0, "absorb_fwd": 495.0}
     kernels = {}
     for st_name, ms in stage_ms.items():
         if st_name not in algo_pc:

@@ -210,16 +210,16 @@ class CRTM:
         return int(library().crtm_gpu_launch_count(self.h))
 
     STAGES = ("prep", "absorb_fwd", "column", "absorb_ad", "map_out", "adjoint_sum", "scatter_layers",
-              "scatter_adding")
+              "scatter_adding", "scatter_contract", "scatter_species")
 
     def set_profiling(self, enable: bool) -> None:
         library().crtm_gpu_set_profiling(self.h, int(enable))
 
     def stage_times(self, reset: bool = True) -> dict:
         """{stage: (milliseconds, launches)} accumulated while profiling was enabled."""
-        ms = np.zeros(8)
-        n = np.zeros(8, np.int64)
-        k = library().crtm_gpu_stage_times(self.h, ms.ctypes.data, n.ctypes.data, 8, int(reset))
+        ms = np.zeros(len(self.STAGES))
+        n = np.zeros(len(self.STAGES), np.int64)
+        k = library().crtm_gpu_stage_times(self.h, ms.ctypes.data, n.ctypes.data, len(self.STAGES), int(reset))
         return {self.STAGES[i]: (float(ms[i]), int(n[i])) for i in range(min(k, len(self.STAGES)))}
 
     def close(self) -> None:

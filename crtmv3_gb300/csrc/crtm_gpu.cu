@@ -467,8 +467,9 @@ struct crtm_gpu_context {
   struct Pending { int stage; cudaEvent_t a, b; };
   std::vector<Pending> pending;
   std::vector<cudaEvent_t> event_pool;
-  double stage_ms[8] = {0};
-  long long stage_n[8] = {0};
+  static constexpr int N_STAGES = 10;
+  double stage_ms[N_STAGES] = {0};
+  long long stage_n[N_STAGES] = {0};
 };
 
 namespace {
@@ -925,7 +926,7 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
             CK_LAUNCH(h);
           }
           {
-            StageScope sc(h, 6, st);
+            StageScope sc(h, 8, st);
             if (nz_max)
               launch_scatter_contract<SC_NZ_MAX, double>(sa, gl, st);
             else
@@ -942,7 +943,7 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
           CK_LAUNCH(h);
         }
         if (sw.slots || sw.cf) {   // species and cloud-fraction Jacobians: cover chain rule, seed, outputs
-          StageScope sc(h, 7, st);
+          StageScope sc(h, 9, st);
           scatter_species_kernel<R><<<ga, SCATTER_THREADS, 0, st>>>(sa);
           CK_LAUNCH(h);
           struct Out { double* o; const double* X; int S, s0, ns; };
@@ -1758,13 +1759,14 @@ int crtm_gpu_stage_times(crtm_gpu_handle h, double* ms, long long* launches, int
   if (!h) return 0;
   cudaSetDevice(h->device);
   collect_stage_times(h);
-  for (int i = 0; i < n && i < 8; i++) {
+  const int N = crtm_gpu_context::N_STAGES;
+  for (int i = 0; i < n && i < N; i++) {
     if (ms) ms[i] = h->stage_ms[i];
     if (launches) launches[i] = h->stage_n[i];
   }
   if (reset)
-    for (int i = 0; i < 8; i++) { h->stage_ms[i] = 0.0; h->stage_n[i] = 0; }
-  return 8;
+    for (int i = 0; i < N; i++) { h->stage_ms[i] = 0.0; h->stage_n[i] = 0; }
+  return N;
 }
 
 }  // extern "C"

@@ -307,8 +307,10 @@ long long crtm_gpu_launch_count(crtm_gpu_handle handle);
  * stream.  crtm_gpu_stage_times synchronises the handle's pending work and
  * returns, per stage, the accumulated milliseconds and launch counts since the
  * last reset: stages 0 prep, 1 absorb_fwd, 2 column, 3 absorb_ad, 4 map_out,
- * 5 adjoint_sum, 6 scatter_layers, 7 scatter_adding.  Returns the number of
- * stages. */
+ * 5 adjoint_sum, 6 scatter_layers (layer records), 7 scatter_adding (adding or
+ * orders of interaction and their adjoints), 8 scatter_contract (record
+ * adjoints contracted with the layer optics' derivatives), 9 scatter_species
+ * (cover chain rule and the species outputs).  Returns the number of stages. */
 int crtm_gpu_set_profiling(crtm_gpu_handle handle, int enable);
 int crtm_gpu_stage_times(crtm_gpu_handle handle, double* ms, long long* launches, int n, int reset);
 
