@@ -56,7 +56,8 @@ class CBatch(ct.Structure):
                 ("max_aerosols", ct.c_int), ("n_aerosols", ct.c_void_p), ("aerosol_type", ct.c_void_p),
                 ("aerosol_concentration", ct.c_void_p), ("aerosol_effective_radius", ct.c_void_p),
                 ("cloud_fraction", ct.c_void_p), ("overlap_id", ct.c_void_p),
-                ("aerosol_effective_variance", ct.c_void_p), ("relative_humidity", ct.c_void_p)]
+                ("aerosol_effective_variance", ct.c_void_p), ("relative_humidity", ct.c_void_p),
+                ("wind_speed", ct.c_void_p)]
 
 
 class CRTSolution(ct.Structure):
@@ -72,7 +73,7 @@ SURFACE_COVERS = ("land_temperature", "snow_temperature", "ice_temperature")
 
 # the aerosol schemes' second LUT coordinate: Effective_Variance ('CMAQ'),
 # Relative_Humidity ('GOCART-GEOS5', 'NAAPS')
-SCHEME_JACOBIANS = ("aerosol_effective_variance", "relative_humidity")
+SCHEME_JACOBIANS = ("aerosol_effective_variance", "relative_humidity", "wind_speed")
 AEROSOL_MODELS = ("CRTM", "CMAQ", "GOCART-GEOS5", "NAAPS")
 
 
@@ -92,7 +93,7 @@ class CAdjoint(ct.Structure):
 TL_FIELDS = ("temperature", "absorber", "land_temperature", "water_temperature", "snow_temperature",
              "ice_temperature", "emissivity", "cloud_water_content", "cloud_effective_radius", "cloud_fraction",
              "aerosol_concentration", "aerosol_effective_radius", "aerosol_effective_variance",
-             "relative_humidity")
+             "relative_humidity", "wind_speed")
 
 
 class CTLIn(ct.Structure):
@@ -258,9 +259,11 @@ class CRTM:
         b.sensor_zenith_angle = c(geo.sensor_zenith_angle)
         b.source_zenith_angle = c(geo.source_zenith_angle)
         b.surface_altitude = c(geo.surface_altitude)
-        if opt is None or opt.emissivity is None:
-            raise ValueError("Options.emissivity is required (Use_Emissivity path)")
-        b.emissivity = c(opt.emissivity)
+        # no emissivity: the IR sea-surface emissivity model (clear-sky IR batches over water)
+        if opt is not None and opt.emissivity is not None:
+            b.emissivity = c(opt.emissivity)
+        if getattr(sfc, "wind_speed", None) is not None:
+            b.wind_speed = c(sfc.wind_speed)
         if atm.n_clouds is not None and atm.cloud_type is not None and atm.cloud_type.shape[1] > 0:
             b.max_clouds = int(atm.cloud_type.shape[1])
             b.n_clouds = c(atm.n_clouds, np.int32)
@@ -325,6 +328,8 @@ class CRTM:
         if out is None:
             for f in SURFACE_COVERS:
                 setattr(km, f, np.zeros((P, L)))
+            if opt is None or opt.emissivity is None:
+                km.wind_speed = np.zeros((P, L))
         cr = CRTSolution(rts.radiance.ctypes.data, rts.brightness_temperature.ctypes.data,
                          rts.status.ctypes.data)
         ck = CKMatrix(km.temperature.ctypes.data, km.absorber.ctypes.data,
@@ -346,6 +351,8 @@ class CRTM:
             out[f] = np.zeros((P,) + shp)
         for f in SURFACE_COVERS:
             out[f] = np.zeros(P)
+        if opt is None or opt.emissivity is None:
+            out["wind_speed"] = np.zeros(P)
         cr = CRTSolution(rts.radiance.ctypes.data, rts.brightness_temperature.ctypes.data,
                          rts.status.ctypes.data)
         ca = CAdjoint(out["temperature"].ctypes.data, out["absorber"].ctypes.data,
@@ -379,7 +386,7 @@ class CRTM:
                                              "aerosol_effective_radius", "aerosol_effective_variance",
                                              "relative_humidity")}
         vals.update({f: arr(sfc_tl, f) for f in ("land_temperature", "water_temperature", "snow_temperature",
-                                                  "ice_temperature")})
+                                                  "ice_temperature", "wind_speed")})
         if emissivity_tl is not None:
             e = np.ascontiguousarray(emissivity_tl, np.float64)
             keep.append(e)
@@ -414,7 +421,7 @@ class CRTM:
                   "n_clouds", "cloud_type", "cloud_water_content", "cloud_effective_radius",
                   "n_streams", "rt_algorithm_id", "n_aerosols", "aerosol_type", "aerosol_concentration",
                   "aerosol_effective_radius", "cloud_fraction", "overlap_id", "aerosol_effective_variance",
-                  "relative_humidity"):
+                  "relative_humidity", "wind_speed"):
             t = dev.get(f)
             setattr(b, f, None if t is None else t.data_ptr())
         if dev.get("cloud_type") is not None:
@@ -583,7 +590,10 @@ def CRTM_Tangent_Linear(atmosphere, surface, atmosphere_tl, surface_tl, geometry
 
 def _sensor_options(options: Optional[OptionsBatch], off: int, n: int) -> OptionsBatch:
     """One sensor's options: its columns of Options%Emissivity and every
-    per-profile option."""
-    if options is None or options.emissivity is None:
-        raise ValueError("Options%Emissivity is required for this path (Use_Emissivity)")
+    per-profile option.  Without an emissivity the library's surface model
+    supplies it (the IR sea-surface model)."""
+    if options is None:
+        return OptionsBatch()
+    if options.emissivity is None:
+        return options
     return dataclasses.replace(options, emissivity=np.ascontiguousarray(options.emissivity[:, off:off + n]))

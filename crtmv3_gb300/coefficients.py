@@ -391,3 +391,63 @@ def read_aerosolcoeff(path: str, scheme: str = "CRTM") -> AerosolCoeff:
         parts = r.split(r.record(), [("f8", (n5,))] * 3 + [("f8", (n5 * (nl + 1) * nph,))])
     return AerosolCoeff(tid, names, wl, reff, rsig, rh, *[p.reshape(shp, order="F") for p in parts[:3]],
                         parts[3].reshape(shp + (nl + 1, nph), order="F"), src, int(ver))
+
+
+# ---------------------------------------------------------------------------
+# IRwaterCoeff (IR sea-surface emissivity LUT, CRTM_IRSSEM)
+# ---------------------------------------------------------------------------
+
+IRWATERCOEFF_RELEASE = 4        # ``IRwaterCoeff_Define.f90:65``
+IRWATER_SL = 80                 # Classification_Name length (``IRwaterCoeff_Define.f90:77``)
+
+
+@dataclasses.dataclass
+class IRwaterCoeff:
+    """IR water emissivity table (``IRwaterCoeff_Define.f90:86-106``):
+    ``emissivity[angle, frequency, wind speed, temperature]`` (Fortran order),
+    angles in degrees, frequencies in cm^-1, wind speeds in m/s, temperatures
+    in K.  A 'Nalli2' classification interpolates in temperature as well
+    (``CRTM_IRSSEM.f90:252-301``); other tables use the first temperature."""
+    classification: str
+    angle: np.ndarray
+    frequency: np.ndarray
+    wind_speed: np.ndarray
+    temperature: np.ndarray
+    emissivity: np.ndarray
+    version: int = 2
+
+
+def write_irwatercoeff(path: str, wc: IRwaterCoeff, byteorder: str = "<") -> None:
+    """Record order of ``IRwaterCoeff_Define.f90:1147-1210`` (IRwaterCoeff_WriteFile):
+    Release/Version, the 4 dimensions, 5 global attributes (length, then the
+    text when the length is not 0), the classification name, the 4 axes, the
+    emissivity."""
+    with open(path, "wb") as f:
+        wr = RecordWriter(f, byteorder)
+        wr.record(np.array([IRWATERCOEFF_RELEASE, wc.version], np.int32))
+        wr.record(np.array([wc.angle.size, wc.frequency.size, wc.wind_speed.size, wc.temperature.size], np.int32))
+        for text in ("write_module: crtmv3_gb300.coefficients", "", "title: synthetic IR water emissivity",
+                     "", ""):
+            wr.record(np.array([len(text)], np.int32))
+            if text:
+                wr.record(text.encode("ascii"))
+        wr.record(wc.classification.ljust(IRWATER_SL)[:IRWATER_SL].encode("ascii"))
+        wr.record(wc.angle, wc.frequency, wc.wind_speed, wc.temperature)
+        wr.record(np.asfortranarray(wc.emissivity))
+
+
+def read_irwatercoeff(path: str) -> IRwaterCoeff:
+    with open(path, "rb") as f:
+        r = RecordReader(f)
+        rel, ver = r.split(r.record(), [("i4", (2,))])[0]
+        if rel != IRWATERCOEFF_RELEASE:
+            raise IOError(f"IRwaterCoeff release {rel} not supported")
+        na, nf, nv, nt = (int(x) for x in r.split(r.record(), [("i4", (4,))])[0])
+        for _ in range(5):
+            (n,) = r.split(r.record(), [("i4", ())])
+            if n:
+                r.record()
+        name = r.split(r.record(), [("S", IRWATER_SL)])[0].strip()
+        a, fr, v, t = r.split(r.record(), [("f8", (na,)), ("f8", (nf,)), ("f8", (nv,)), ("f8", (nt,))])
+        (e,) = r.split(r.record(), [("f8", (na * nf * nv * nt,))])
+    return IRwaterCoeff(name, a, fr, v, t, e.reshape((na, nf, nv, nt), order="F"), int(ver))

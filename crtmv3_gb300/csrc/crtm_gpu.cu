@@ -412,6 +412,42 @@ bool load_aerosolcoeff(const std::string& path, int scheme, std::vector<double>&
   return true;
 }
 
+// IRwaterCoeff file (IRwaterCoeff_Define.f90:805-984): Release/Version, the
+// 4 dimensions, 5 global attributes (a length record, then the text when the
+// length is not 0), the classification name, the axes (angle, frequency,
+// wind speed, temperature), the emissivity.  dims: na nf nv nt nalli2;
+// off: angle freq wind temp e.
+bool load_irwatercoeff(const std::string& path, std::vector<double>& buf, int* dims, size_t* off,
+                       std::string& err) {
+  Records r;
+  if (!r.open(path, err)) return false;
+  const unsigned char* d;
+  size_t len;
+  auto bad = [&](const char* what) { err = path + ": " + what; return false; };
+  if (!r.next(d, len) || len != 8) return bad("corrupt Release/Version record");
+  if (r.i32(d) != 4) return bad("unsupported IRwaterCoeff release");
+  if (!r.next(d, len) || len != 16) return bad("corrupt dimension record");
+  const int na = r.i32(d), nf = r.i32(d + 4), nv = r.i32(d + 8), nt = r.i32(d + 12);
+  if (na < 4 || nf < 4 || nv < 4 || nt < 1) return bad("dimensions out of range");
+  for (int g = 0; g < 5; g++) {
+    if (!r.next(d, len) || len != 4) return bad("corrupt global attribute");
+    if (r.i32(d) > 0 && !r.next(d, len)) return bad("corrupt global attribute");
+  }
+  if (!r.next(d, len) || len != 80) return bad("corrupt classification record");
+  const std::string name(reinterpret_cast<const char*>(d), 80);
+  const bool nalli2 = name.compare(0, 6, "Nalli2") == 0 && (name.size() == 6 || name[6] == ' ');
+  if (nalli2 && nt < 4) return bad("a Nalli2 table needs at least 4 temperatures");
+  const size_t nax = (size_t)na + nf + nv + nt, ne = (size_t)na * nf * nv * nt;
+  if (!r.next(d, len) || len != 8 * nax) return bad("corrupt axis record");
+  buf.clear();
+  for (size_t i = 0; i < nax; i++) buf.push_back(r.f64(d + 8 * i));
+  off[0] = 0; off[1] = na; off[2] = na + nf; off[3] = na + nf + nv; off[4] = nax;
+  if (!r.next(d, len) || len != 8 * ne) return bad("corrupt emissivity record");
+  for (size_t i = 0; i < ne; i++) buf.push_back(r.f64(d + 8 * i));
+  dims[0] = na; dims[1] = nf; dims[2] = nv; dims[3] = nt; dims[4] = nalli2 ? 1 : 0;
+  return true;
+}
+
 // Grow-only device buffer
 struct DevBuf {
   void* p = nullptr;
@@ -454,6 +490,12 @@ struct crtm_gpu_context {
   double* d_aero = nullptr;
   int* d_aero_type = nullptr;
   AerosolLut alut{};
+  // IR sea-surface emissivity table (Nalli.IRwater.EmisCoeff.bin), when present
+  bool has_irwater = false;
+  double* d_irw = nullptr;
+  IRWaterLut irw{};
+  DevBuf sfc;               // emissivity model: e, de/dv, de/dT [P][L]
+  bool model_call = false;  // the last call used the emissivity model
   int* d_error = nullptr;   // first failure code of the scattering kernel
   cudaStream_t copy_stream = nullptr;   // device-to-host copies of finished chunks
   std::vector<cudaEvent_t> chunk_events;
@@ -559,6 +601,7 @@ struct Work {
   double* CF;       // cloud-fraction Jacobian: [n][Kmax][L]
   double* CV;       // aerosol effective-variance Jacobians ('CMAQ'): [n][slots][Kmax][L]
   double* CH;       // relative-humidity Jacobian ('GOCART-GEOS5', 'NAAPS'): [n][Kmax][L]
+  double* WS;       // adjoint with the emissivity model: [n][L] wind-speed adjoints
   double* TD;       // cloud-cover derivatives: [n][2][Kmax]
   double* ras;      // adjoint: [n][nv][K]
   double* pts;      // adjoint: [n][Kmax]
@@ -585,6 +628,7 @@ struct ScatterWork {
   int slots = 0;         // species Jacobian slots (max_clouds + max_aerosols), 0: none
   bool cf = false;       // cloud-fraction Jacobian
   bool cv = false, ch = false;   // aerosol effective-variance / relative-humidity Jacobians
+  bool wind = false;     // adjoint through the emissivity model: per-(profile, channel) wind-speed adjoints
 };
 
 template <int G, class R>
@@ -651,6 +695,7 @@ size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w
     wk.SC = (R*)carve(nn * L * sizeof(R));
     wk.RA = (R*)carve(nn * nv * K * L * sizeof(R));
   }
+  if (mode == 2 && sw.wind) wk.WS = (double*)carve(nn * L * sizeof(double));
   if (mode == 2) {
     wk.TSK = (double*)carve(nn * L * sizeof(double));
     wk.ras = (double*)carve(nn * nv * K * sizeof(double));
@@ -701,6 +746,36 @@ struct FixedScratch {
   size_t bytes;
 };
 
+// IR sea-surface emissivity model of a call (batch emissivity NULL):
+// de/d(wind speed) and de/d(water temperature) [P][L] (the latter null unless
+// the table is 'Nalli2').
+struct SfcModel {
+  const double* ev = nullptr;
+  const double* et = nullptr;
+};
+
+// CRTM_Compute_IR_Water_SfcOptics (CRTM_IR_Water_SfcOptics.f90:179-254) for
+// the Emission solver: the emissivity at the sensor zenith angle (the one
+// angle of a clear-sky column; specular, reflectivity 1 - e) and its wind
+// speed / water temperature derivatives, one thread per (profile, channel).
+// Profiles whose water coverage is not 1 raise error 13 (the land, snow and
+// ice models are not built).
+__global__ void irwater_kernel(IRWaterLut W, int P, int L, const double* wn, const double* zenith,
+                               const double* t_water, const double* water_cov, const double* wind, double* E,
+                               double* EV, double* ET, int* error) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)P * L) return;
+  const int p = (int)(i / L), l = (int)(i % L);
+  if (fabs(water_cov[p] - 1.0) > 1.0e-12) atomicCAS(error, 0, 13);
+  Dual<2> t(t_water[p]), v(wind ? wind[p] : 5.0);   // DEFAULT_WIND_SPEED
+  v.d[0] = 1.0;
+  t.d[1] = 1.0;
+  const Dual<2> e = irssem<Dual<2>>(W, t, v, wn[l], zenith[p]);
+  E[i] = e.v;
+  EV[i] = e.d[0];
+  ET[i] = e.d[1];
+}
+
 int copy_chunk(crtm_gpu_handle h, const HostCopy* hc, int p0, int n, cudaStream_t st) {
   if (!h->copy_stream && cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
     return fail(h, "cannot create the copy stream");
@@ -725,7 +800,7 @@ template <int G, class R>
 int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, int mode,
                  const double* seed, crtm_gpu_rtsolution* rts, crtm_gpu_kmatrix* kk,
                  crtm_gpu_adjoint_out* ad, cudaStream_t st, const HostCopy* hc,
-                 const FixedScratch* fixed, bool scat) {
+                 const FixedScratch* fixed, bool scat, const SfcModel* sm) {
   const int P = b->n_profiles, Kmax = b->max_layers, L = s.L, K = s.K, n_abs = b->n_absorbers;
   if (P <= 0) return CRTM_GPU_SUCCESS;
   if (Kmax < 2 || Kmax > MAX_LAYERS) return fail(h, "max_layers %d out of range [2, %d]", Kmax, MAX_LAYERS);
@@ -789,6 +864,7 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
     sw.cv = sw.kstate && want_av;
     sw.ch = sw.kstate && want_rh;
   }
+  sw.wind = mode == 2 && sm && sm->ev && ad->wind_speed;
   // chunk size from the workspace budget
   const size_t per = work_bytes<G, R>(s, 64, Kmax, nv, mode, nullptr, nullptr, sw) / 64 + 1;
   int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)P, h->workspace_budget / per));
@@ -855,6 +931,11 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
     ca.tsk = mode == 1 ? kk->water_temperature : (mode == 2 ? w.TSK : nullptr);
     ca.ek = mode == 1 ? kk->surface_emissivity : nullptr;
     if (mode == 1) { ca.tsk_land = kk->land_temperature; ca.tsk_snow = kk->snow_temperature; ca.tsk_ice = kk->ice_temperature; }
+    if (sm && sm->ev) {   // emissivity model
+      ca.sfc_ev = sm->ev;
+      ca.sfc_et = sm->et;
+      ca.wind_k = mode == 1 ? kk->wind_speed : (mode == 2 ? w.WS : nullptr);
+    }
     ca.status = rts->status;
     // scattering K-matrix/adjoint: the column runs twice around the scattering kernels
     const bool split = scat && mode != 3;
@@ -1028,6 +1109,11 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       channel_sum_kernel<double><<<(unsigned)(((long long)n * 32 + 255) / 256), 256, 0, st>>>(
           w.TSK, nullptr, 1, n, L, w.tss);
       CK_LAUNCH(h);
+      if (w.WS) {   // Surface_AD%Wind_Speed through the emissivity model
+        channel_sum_kernel<double><<<(unsigned)(((long long)n * 32 + 255) / 256), 256, 0, st>>>(
+            w.WS, nullptr, 1, n, L, ad->wind_speed + p0);
+        CK_LAUNCH(h);
+      }
       AdjMapArgs<R> am{};
       am.K = K; am.Kmax = Kmax; am.nv = nv; am.p_begin = p0; am.n_chunk = n;
       am.b = bv; am.pv = w.pv; am.ras = w.ras; am.pts = w.pts; am.tss = w.tss;
@@ -1059,7 +1145,7 @@ int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, c
   if (!h) return CRTM_GPU_FAILURE;
   if (sensor < 0 || sensor >= (int)h->sensors.size()) return fail(h, "sensor index %d out of range", sensor);
   if (!b || !rts || !rts->radiance || !rts->brightness_temperature) return fail(h, "missing batch or RTSolution buffers");
-  if (!b->n_layers || !b->level_pressure || !b->pressure || !b->temperature || !b->emissivity ||
+  if (!b->n_layers || !b->level_pressure || !b->pressure || !b->temperature ||
       !b->land_coverage || !b->water_coverage || !b->snow_coverage || !b->ice_coverage ||
       !b->land_temperature || !b->water_temperature || !b->snow_temperature ||
       !b->ice_temperature || !b->sensor_zenith_angle || (b->n_absorbers > 0 && !b->absorber))
@@ -1092,17 +1178,47 @@ int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, c
     if (cudaMemsetAsync(h->d_error, 0, sizeof(int), st) != cudaSuccess) return fail(h, "error flag reset failed");
     if (mode == 0) mode = 3;
   }
+  // no emissivity given: the IR sea-surface emissivity model (clear sky, water)
+  const bool model = b->emissivity == nullptr;
+  h->model_call = model;
+  if (model) {
+    if (!h->has_irwater)
+      return fail(h, "no emissivity given and no Nalli.IRwater.EmisCoeff.bin was loaded at init");
+    if (s.sensor_type != 2)
+      return fail(h, "no emissivity given: the surface emissivity model is built for infrared sensors (IR water)");
+    if (scat)
+      return fail(h, "no emissivity given: the IR water emissivity model is built for clear-sky batches; "
+                     "supply Options%%Emissivity for batches with clouds or aerosols");
+  }
   order_after_previous(h, st);
+  crtm_gpu_batch bm;
+  SfcModel sm{};
+  if (model) {
+    const size_t PL = (size_t)b->n_profiles * s.L;
+    if (!h->sfc.ensure(3 * PL * sizeof(double))) return fail(h, "cannot allocate the emissivity model's buffers");
+    double* E = (double*)h->sfc.p;
+    if (cudaMemsetAsync(h->d_error, 0, sizeof(int), st) != cudaSuccess) return fail(h, "error flag reset failed");
+    irwater_kernel<<<(unsigned)((PL + 255) / 256), 256, 0, st>>>(h->irw, b->n_profiles, s.L, s.spec.wn,
+                                                                 b->sensor_zenith_angle, b->water_temperature,
+                                                                 b->water_coverage, b->wind_speed, E, E + PL,
+                                                                 E + 2 * PL, h->d_error);
+    CK_LAUNCH(h);
+    bm = *b;
+    bm.emissivity = E;
+    b = &bm;
+    sm.ev = E + PL;
+    sm.et = h->irw.nalli2 ? E + 2 * PL : nullptr;
+  }
   int rc;
   switch (s.group) {
-    case 1: rc = fp64 ? run_pipeline<1, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat)
-                      : run_pipeline<1, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat);
+    case 1: rc = fp64 ? run_pipeline<1, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat, &sm)
+                      : run_pipeline<1, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat, &sm);
             break;
-    case 2: rc = fp64 ? run_pipeline<2, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat)
-                      : run_pipeline<2, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat);
+    case 2: rc = fp64 ? run_pipeline<2, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat, &sm)
+                      : run_pipeline<2, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat, &sm);
             break;
-    default: rc = fp64 ? run_pipeline<3, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat)
-                       : run_pipeline<3, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat);
+    default: rc = fp64 ? run_pipeline<3, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat, &sm)
+                       : run_pipeline<3, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat, &sm);
   }
   mark_done(h, st);
   return rc;
@@ -1155,6 +1271,8 @@ int stage_batch(crtm_gpu_handle h, const crtm_gpu_batch* b, int L, const double*
     items.insert(items.end(), {{b->aerosol_concentration, (size_t)P * NA * Km * 8},
                                {b->aerosol_effective_radius, (size_t)P * NA * Km * 8},
                                {b->n_aerosols, (size_t)P * 4}, {b->aerosol_type, (size_t)P * NA * 4}});
+  const size_t wind0 = items.size();
+  items.push_back({b->wind_speed, b->wind_speed ? PD : 0});
   const size_t aer1 = items.size();
   if (NA > 0)
     items.insert(items.end(),
@@ -1204,6 +1322,7 @@ int stage_batch(crtm_gpu_handle h, const crtm_gpu_batch* b, int L, const double*
     db.cloud_fraction = nullptr;
     db.overlap_id = nullptr;
   }
+  db.wind_speed = (const double*)dptr[wind0];
   if (NA > 0) {
     db.aerosol_concentration = (const double*)dptr[aer0];
     db.aerosol_effective_radius = (const double*)dptr[aer0 + 1];
@@ -1259,7 +1378,7 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
                              {kk->land_temperature, PL * 8}, {kk->snow_temperature, PL * 8},
                              {kk->ice_temperature, PL * 8},
                              {kk->aerosol_effective_variance, NAo ? PL * NAo * Km * 8 : 0},
-                             {kk->relative_humidity, NAo ? PL * Km * 8 : 0}});
+                             {kk->relative_humidity, NAo ? PL * Km * 8 : 0}, {kk->wind_speed, PL * 8}});
   if (mode == 2)
     outs.insert(outs.end(), {{ad->temperature, (size_t)P * Km * 8}, {ad->absorber, (size_t)P * J * Km * 8},
                              {ad->water_temperature, PD},
@@ -1270,7 +1389,7 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
                              {ad->aerosol_effective_radius, NAo ? (size_t)P * NAo * Km * 8 : 0},
                              {ad->land_temperature, PD}, {ad->snow_temperature, PD}, {ad->ice_temperature, PD},
                              {ad->aerosol_effective_variance, NAo ? (size_t)P * NAo * Km * 8 : 0},
-                             {ad->relative_humidity, NAo ? (size_t)P * Km * 8 : 0}});
+                             {ad->relative_humidity, NAo ? (size_t)P * Km * 8 : 0}, {ad->wind_speed, PD}});
   size_t tout = 0;
   for (auto& o : outs) tout += align_up(o.second);
   if (!h->io_out.ensure(tout)) return fail(h, "cannot allocate %zu bytes for outputs", tout);
@@ -1287,11 +1406,11 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
     dk = {(double*)dout[3], (double*)dout[4], (double*)dout[5], (double*)dout[6], kk->n_k_absorbers,
           kk->k_absorber_index, (double*)dout[7], (double*)dout[8], (double*)dout[9], (double*)dout[10],
           (double*)dout[11], (double*)dout[12], (double*)dout[13], (double*)dout[14], (double*)dout[15],
-          (double*)dout[16]};
+          (double*)dout[16], (double*)dout[17]};
   if (mode == 2)
     dad = {(double*)dout[3], (double*)dout[4], (double*)dout[5], (double*)dout[6], (double*)dout[7],
            (double*)dout[8], (double*)dout[9], (double*)dout[10], (double*)dout[11], (double*)dout[12],
-           (double*)dout[13], (double*)dout[14], (double*)dout[15]};
+           (double*)dout[13], (double*)dout[14], (double*)dout[15], (double*)dout[16]};
   HostCopy hc;
   hc.n = (int)outs.size();
   for (size_t i = 0; i < outs.size(); i++) {
@@ -1317,13 +1436,14 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
 // After a host entry point's work has finished: the scattering error flag and
 // the per-profile status words.
 int check_call(crtm_gpu_handle h, const crtm_gpu_batch* b, const crtm_gpu_rtsolution* rts) {
-  if (b->max_clouds > 0 || b->max_aerosols > 0) {
+  if (b->max_clouds > 0 || b->max_aerosols > 0 || h->model_call) {
     int code = 0;
     if (cudaMemcpy(&code, h->d_error, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
       return fail(h, "cannot read the scattering error flag");
-    if (code) return fail(h, "scattering radiative transfer failed (code %d: 1-3 stream set, 4 cloud type, "
+    if (code) return fail(h, "radiative transfer failed (code %d: 1-3 stream set, 4 cloud type, "
                              "5-6 singular matrix, 8 aerosol stream set or LUT, 9 aerosol type, 11 invalid "
-                             "Options%Overlap_Id, 12 SOI order-field slots below 17)", code);
+                             "Options%Overlap_Id, 12 SOI order-field slots below 17, 13 emissivity model with a water "
+                             "coverage other than 1)", code);
   }
   if (rts->status)
     for (int m = 0; m < b->n_profiles; m++)
@@ -1337,7 +1457,7 @@ struct TLArgs {
   int P, L, Km, J, NC, NA;
   const int* n_layers;
   const int* status;
-  const double* kt, *ka, *kw, *kl, *ks, *ki, *ke, *kwc, *kre, *kcf, *kac, *kar, *kav, *krh;
+  const double* kt, *ka, *kw, *kl, *ks, *ki, *ke, *kwc, *kre, *kcf, *kac, *kar, *kav, *krh, *kws;
   crtm_gpu_tl_in d;
   double* bt_tl;
 };
@@ -1374,6 +1494,7 @@ __global__ void tl_kernel(TLArgs a) {
   if (a.d.snow_temperature) s += a.ks[pl] * a.d.snow_temperature[p];
   if (a.d.ice_temperature) s += a.ki[pl] * a.d.ice_temperature[p];
   if (a.d.emissivity) s += a.ke[pl] * a.d.emissivity[pl];
+  if (a.d.wind_speed && a.kws) s += a.kws[pl] * a.d.wind_speed[p];
   a.bt_tl[pl] = (a.status && a.status[p]) ? 0.0 : s;
 }
 
@@ -1390,9 +1511,11 @@ int tl_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm
   const bool cf = NC && tl->cloud_fraction;
   const bool aer = NA && (tl->aerosol_concentration || tl->aerosol_effective_radius);
   const bool av = NA && tl->aerosol_effective_variance, rh = NA && tl->relative_humidity;
+  const bool ws = tl->wind_speed && !b->emissivity;   // the emissivity model's wind speed
   const size_t PL = P * L;
   const size_t n_el = PL * Km * (1 + J) + 5 * PL + (wc ? 2 * PL * NC * Km : 0) + (cf ? PL * Km : 0) +
-                      (aer ? 2 * PL * NA * Km : 0) + (av ? PL * NA * Km : 0) + (rh ? PL * Km : 0);
+                      (aer ? 2 * PL * NA * Km : 0) + (av ? PL * NA * Km : 0) + (rh ? PL * Km : 0) +
+                      (ws ? PL : 0);
   if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
   if (!h->tl_k.ensure(n_el * sizeof(double)))
     return fail(h, "cannot allocate %zu bytes for the tangent linear's K-matrix", n_el * sizeof(double));
@@ -1411,6 +1534,7 @@ int tl_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm
   if (aer) { kk.aerosol_concentration = take(PL * NA * Km); kk.aerosol_effective_radius = take(PL * NA * Km); }
   if (av) kk.aerosol_effective_variance = take(PL * NA * Km);
   if (rh) kk.relative_humidity = take(PL * Km);
+  if (ws) kk.wind_speed = take(PL);
   if (int rc = dispatch(h, sensor, b, 1, nullptr, rts, &kk, nullptr, st)) return rc;
   TLArgs ta{};
   ta.P = (int)P; ta.L = (int)L; ta.Km = (int)Km; ta.J = (int)J; ta.NC = (int)NC; ta.NA = (int)NA;
@@ -1419,7 +1543,7 @@ int tl_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm
   ta.ks = kk.snow_temperature; ta.ki = kk.ice_temperature; ta.ke = kk.surface_emissivity;
   ta.kwc = kk.cloud_water_content; ta.kre = kk.cloud_effective_radius; ta.kcf = kk.cloud_fraction;
   ta.kac = kk.aerosol_concentration; ta.kar = kk.aerosol_effective_radius;
-  ta.kav = kk.aerosol_effective_variance; ta.krh = kk.relative_humidity;
+  ta.kav = kk.aerosol_effective_variance; ta.krh = kk.relative_humidity; ta.kws = kk.wind_speed;
   const long long threads = (long long)PL * 32;
   tl_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(ta);
   CK_LAUNCH(h);
@@ -1446,13 +1570,14 @@ int tl_host(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm_g
   if (int rc = stage_batch(h, b, (int)L, nullptr, &db, &dseed)) return rc;
   cudaStream_t st = h->stream;
   // perturbations
-  constexpr int NTL = 14;
+  constexpr int NTL = 15;
   const double* srcs[NTL] = {tl->temperature, tl->absorber, tl->land_temperature, tl->water_temperature,
                              tl->snow_temperature, tl->ice_temperature, tl->emissivity, tl->cloud_water_content,
                              tl->cloud_effective_radius, tl->cloud_fraction, tl->aerosol_concentration,
-                             tl->aerosol_effective_radius, tl->aerosol_effective_variance, tl->relative_humidity};
+                             tl->aerosol_effective_radius, tl->aerosol_effective_variance, tl->relative_humidity,
+                             tl->wind_speed};
   const size_t sz[NTL] = {P * Km, P * J * Km, P, P, P, P, P * L, P * NC * Km, P * NC * Km, NC ? P * Km : 0,
-                          P * NA * Km, P * NA * Km, P * NA * Km, NA ? P * Km : 0};
+                          P * NA * Km, P * NA * Km, P * NA * Km, NA ? P * Km : 0, P};
   size_t tot = 0;
   for (int i = 0; i < NTL; i++) tot += srcs[i] && sz[i] ? align_up(sz[i] * 8) : 0;
   if (!h->io_tl.ensure(tot + 256)) return fail(h, "cannot allocate %zu bytes for the perturbations", tot);
@@ -1465,8 +1590,8 @@ int tl_host(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm_g
       return fail(h, "host-to-device copy failed");
     off += align_up(sz[i] * 8);
   }
-  const crtm_gpu_tl_in dtl = {dsrc[0], dsrc[1], dsrc[2], dsrc[3],  dsrc[4],  dsrc[5],  dsrc[6],
-                              dsrc[7], dsrc[8], dsrc[9], dsrc[10], dsrc[11], dsrc[12], dsrc[13]};
+  const crtm_gpu_tl_in dtl = {dsrc[0], dsrc[1], dsrc[2],  dsrc[3],  dsrc[4],  dsrc[5],  dsrc[6], dsrc[7],
+                              dsrc[8], dsrc[9], dsrc[10], dsrc[11], dsrc[12], dsrc[13], dsrc[14]};
   // outputs
   const size_t PL = P * L;
   const size_t o_bt = align_up(PL * 8), o_tl = o_bt + align_up(PL * 8), o_st = o_tl + align_up(PL * 8);
@@ -1609,6 +1734,30 @@ int crtm_gpu_init_aerosol(const char* coeff_path, int n_sensors, const char* con
       A.rh = h->d_aero + aoff[6];
       h->has_aerosols = true;
     }
+    const std::string wpath = std::string(coeff_path) + "/Nalli.IRwater.EmisCoeff.bin";
+    if (FILE* fw = fopen(wpath.c_str(), "rb")) {   // the reference's default IRwaterCoeff_File
+      fclose(fw);
+      std::vector<double> wbuf;
+      int wd[5];
+      size_t wo[5];
+      std::string err;
+      if (!load_irwatercoeff(wpath, wbuf, wd, wo, err)) {
+        g_init_error = err;
+        crtm_gpu_destroy(h);
+        return CRTM_GPU_FAILURE;
+      }
+      if (cudaMalloc(&h->d_irw, wbuf.size() * sizeof(double)) != cudaSuccess ||
+          cudaMemcpy(h->d_irw, wbuf.data(), wbuf.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+        g_init_error = "device upload of Nalli.IRwater.EmisCoeff.bin failed";
+        crtm_gpu_destroy(h);
+        return CRTM_GPU_FAILURE;
+      }
+      IRWaterLut& W = h->irw;
+      W.na = wd[0]; W.nf = wd[1]; W.nv = wd[2]; W.nt = wd[3]; W.nalli2 = wd[4];
+      W.angle = h->d_irw + wo[0]; W.freq = h->d_irw + wo[1]; W.wind = h->d_irw + wo[2];
+      W.temp = h->d_irw + wo[3]; W.e = h->d_irw + wo[4];
+      h->has_irwater = true;
+    }
     GaussTable gt{};
     for (int n = 1; n <= 9; n++) double_gauss_host(n, gt.mu[n], gt.w[n]);
     if (cudaMemcpyToSymbol(c_gauss, &gt, sizeof gt) != cudaSuccess || scatter_k_set_gauss(gt) ||
@@ -1627,7 +1776,8 @@ int crtm_gpu_destroy(crtm_gpu_handle h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (auto& s : h->sensors) free_sensor(s);
-  h->ws.release(); h->io_in.release(); h->io_out.release(); h->small.release();
+  h->ws.release(); h->io_in.release(); h->io_out.release(); h->small.release(); h->sfc.release();
+  cudaFree(h->d_irw);
   cudaFree(h->d_cloud);
   cudaFree(h->d_aero);
   cudaFree(h->d_aero_type);

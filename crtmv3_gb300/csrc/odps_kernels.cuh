@@ -603,6 +603,11 @@ struct ColumnArgs {
   double* tsk, *ek;       // K-matrix: [P][L] water temperature, emissivity; adjoint: tsk is [n][L]
                           // scratch of dBT/dTs x seed
   double* tsk_land, *tsk_snow, *tsk_ice;   // K-matrix: [P][L] or null
+  // IR sea-surface emissivity model (batch emissivity from CRTM_IRSSEM): its
+  // derivatives de/d(wind speed), de/d(water temperature) [P][L], or null;
+  // wind_k receives dBT/d(wind speed): K-matrix [P][L], adjoint [n][L]
+  const double* sfc_ev, *sfc_et;
+  double* wind_k;
   int* status;            // [P] or null
   // Scattering profiles in a K-matrix/adjoint call: launched twice.  pass 1
   // stores TAU/DTOP and stops; the scattering K kernel then writes the cloudy
@@ -652,6 +657,7 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
       if (a.mode == 1) { a.tsk[pl] = 0.0; a.ek[pl] = 0.0; }
       if (a.mode == 1 || a.mode == 2) a.SC[(size_t)p * L + l] = R(0);
       if (a.mode == 2) a.tsk[(size_t)p * L + l] = 0.0;
+      if (a.wind_k) a.wind_k[a.mode == 1 ? pl : (size_t)p * L + l] = 0.0;
     }
     return;
   }
@@ -828,14 +834,20 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   // surface temperature: Ts = sum of the coverage-weighted cover temperatures
   // (CRTM_Compute_SurfaceT), so each cover's adjoint is its coverage x dBT/dTs
   const double ts_ad = double(dBs) * Bs_b * scale;
+  // emissivity model (water coverage 1): de/dT adds to the water temperature
+  // adjoint, de/dv gives the wind speed's (CRTM_Compute_IRSSEM_AD)
+  const double e_ad = scale * e_b;   // emissivity_AD - reflectivity_AD
+  const double ts_e = a.sfc_et ? e_ad * a.sfc_et[pl] : 0.0;
   if (a.mode == 1) {
-    a.tsk[pl] = a.b.water_cov[gp] * ts_ad;
+    a.tsk[pl] = a.b.water_cov[gp] * ts_ad + ts_e;
     if (a.tsk_land) a.tsk_land[pl] = a.b.land_cov[gp] * ts_ad;
     if (a.tsk_snow) a.tsk_snow[pl] = a.b.snow_cov[gp] * ts_ad;
     if (a.tsk_ice) a.tsk_ice[pl] = a.b.ice_cov[gp] * ts_ad;
-    a.ek[pl] = scale * e_b;   // emissivity_AD - reflectivity_AD
+    a.ek[pl] = e_ad;
+    if (a.wind_k) a.wind_k[pl] = e_ad * a.sfc_ev[pl];
   } else {
-    a.tsk[(size_t)p * L + l] = ts_ad;
+    a.tsk[(size_t)p * L + l] = ts_ad + ts_e;
+    if (a.wind_k) a.wind_k[(size_t)p * L + l] = e_ad * a.sfc_ev[pl];
   }
 }
 

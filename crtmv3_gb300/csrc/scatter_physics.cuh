@@ -238,6 +238,35 @@ CRTM_HD bool aerosol_layer_optics(const AerosolLut& A, double wavenumber, int ty
   return true;
 }
 
+// IR sea-surface emissivity table (IRwaterCoeff_Define.f90:86-106), Fortran
+// order (angle fastest, then frequency, wind speed, temperature).
+struct IRWaterLut {
+  int na, nf, nv, nt;
+  int nalli2;               // 'Nalli2' classification: temperature is an axis too
+  const double* angle;      // [na] degrees
+  const double* freq;       // [nf] cm^-1
+  const double* wind;       // [nv] m/s
+  const double* temp;       // [nt] K
+  const double* e;          // [nt][nv][nf][na]
+};
+
+// CRTM_Compute_IRSSEM (CRTM_IRSSEM.f90:204-334) at one angle (degrees): the
+// 4-point blended Lagrange interpolation in angle, frequency and wind speed,
+// and water temperature for a 'Nalli2' table, each clamped to its axis as
+// Find_Random_Index does.  Wind speed and temperature carry S's derivatives.
+template <class S>
+CRTM_HD S irssem(const IRWaterLut& W, S water_temperature, S wind_speed, double frequency, double angle) {
+  const Lagrange4 A = lagrange4(W.angle, W.na, fabs(angle));
+  const Lagrange4T<S> F = lagrange4(W.freq, W.nf, S(frequency));
+  const Lagrange4T<S> V = lagrange4(W.wind, W.nv, wind_speed);
+  if (!W.nalli2) return lerp4x4x4(W.e, W.na, W.nf, A, F, V);
+  const Lagrange4T<S> T = lagrange4(W.temp, W.nt, water_temperature);
+  const size_t n3 = (size_t)W.na * W.nf * W.nv;
+  S a[4];
+  for (int l = 0; l < 4; l++) a[l] = lerp4x4x4(W.e + (size_t)(T.i0 + l) * n3, W.na, W.nf, A, F, V);
+  return lerp4(a, 1, T);
+}
+
 // ---- small dense matrices (row-major, fixed capacity NZ x NZ) --------------
 template <int NZ, class T>
 struct Mat {

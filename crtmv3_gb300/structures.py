@@ -95,6 +95,9 @@ class SurfaceBatch:
     water_temperature: np.ndarray
     snow_temperature: np.ndarray
     ice_temperature: np.ndarray
+    # Surface%Wind_Speed (m/s), read by the IR water emissivity model when the
+    # emissivity is not supplied (CRTM_Surface_Define.f90:183 default 5 m/s)
+    wind_speed: Optional[np.ndarray] = None
 
     @staticmethod
     def ocean(water_temperature: np.ndarray) -> "SurfaceBatch":
@@ -105,8 +108,8 @@ class SurfaceBatch:
                             np.full(P, 260.0), np.full(P, 260.0))
 
     def subset(self, idx) -> "SurfaceBatch":
-        return SurfaceBatch(*[np.ascontiguousarray(getattr(self, f.name)[idx])
-                              for f in dataclasses.fields(self)])
+        return SurfaceBatch(*[None if getattr(self, f.name) is None else
+                              np.ascontiguousarray(getattr(self, f.name)[idx]) for f in dataclasses.fields(self)])
 
 
 @dataclasses.dataclass
@@ -177,3 +180,4 @@ class KMatrixBatch:
     aerosol_effective_radius: Optional[np.ndarray] = None  # (P, L, NA, Kmax)
     aerosol_effective_variance: Optional[np.ndarray] = None  # (P, L, NA, Kmax) ('CMAQ')
     relative_humidity: Optional[np.ndarray] = None         # (P, L, Kmax) ('GOCART-GEOS5', 'NAAPS')
+    wind_speed: Optional[np.ndarray] = None                # (P, L) through the IR water emissivity model

@@ -642,3 +642,38 @@ def add_aerosols(atm: AtmosphereBatch, aerosol_types: Sequence[int], seed: int,
     atm.aerosol_concentration = conc
     atm.aerosol_effective_radius = reff
     return atm
+
+
+IRWATER_FILE = "Nalli.IRwater.EmisCoeff.bin"   # the reference's default IRwaterCoeff_File
+
+
+def generate_irwatercoeff(classification: str = "Nalli") -> co.IRwaterCoeff:
+    """Synthetic IR sea-surface emissivity table: 18 angles (0-85 deg) x 61
+    frequencies (600-3000 cm^-1) x 16 wind speeds (0-15 m/s) x 1 temperature
+    (5, 270-310 K, for 'Nalli2').  Emissivity 1 - R with a Schlick-type
+    Fresnel reflectance R(theta) = R0 + (1 - R0)(1 - cos theta)^5 of a
+    frequency-dependent refractive index, reduced at slant angles by wind
+    roughness, and a weak temperature dependence."""
+    ang = np.arange(0.0, 86.0, 5.0)
+    nu = np.arange(600.0, 3001.0, 40.0)
+    wind = np.arange(0.0, 16.0, 1.0)
+    temp = np.array([270.0, 280.0, 290.0, 300.0, 310.0]) if classification == "Nalli2" else np.array([290.0])
+    n = 1.28 + 0.05 * np.sin(nu / 300.0)
+    r0 = ((n - 1.0) / (n + 1.0)) ** 2
+    c = np.cos(np.deg2rad(ang))
+    R = r0[None, :] + (1.0 - r0[None, :]) * (1.0 - c[:, None]) ** 5            # (angle, frequency)
+    s2 = (1.0 - c ** 2)[:, None, None]
+    Rv = R[:, :, None] * (1.0 - 0.02 * wind[None, None, :] * s2)              # (angle, frequency, wind)
+    e = 1.0 - Rv
+    e4 = e[..., None] * (1.0 + 1.0e-4 * (temp[None, None, None, :] - 290.0))
+    return co.IRwaterCoeff(classification, ang, nu, wind, temp, np.clip(e4, 0.0, 1.0))
+
+
+def write_irwater_file(coeff_dir: str, classification: str = "Nalli", name: str = IRWATER_FILE) -> str:
+    """Write the synthetic IR water emissivity table if missing."""
+    os.makedirs(coeff_dir, exist_ok=True)
+    path = os.path.join(coeff_dir, name)
+    if not os.path.exists(path):
+        co.write_irwatercoeff(path + ".tmp", generate_irwatercoeff(classification))
+        os.replace(path + ".tmp", path)
+    return path

@@ -83,7 +83,11 @@ typedef struct {
   const double* source_zenith_angle;
   const double* surface_altitude; /* may be NULL (0) */
   /* options (CRTM_Options_type): Use_Emissivity is required in this build */
-  const double* emissivity;       /* [P][n_channels] */
+  /* Options%Emissivity [P][n_channels] (Use_Emissivity), or NULL: the
+   * emissivity comes from the IR sea-surface model (CRTM_IRSSEM with the
+   * handle's Nalli.IRwater.EmisCoeff.bin) at the sensor zenith angle, for
+   * infrared sensors, clear-sky batches and water coverage 1 only. */
+  const double* emissivity;
   /* clouds (CRTM_Cloud_type, Atmosphere%Cloud(:)).  max_clouds = 0: clear-sky
    * batch, the cloud pointers are not read.  A profile with n_clouds > 0 is
    * solved with the scattering solver (ADA or SOI); its cloud coverage
@@ -127,6 +131,9 @@ typedef struct {
    * each to its axis. */
   const double* aerosol_effective_variance; /* [P][NA][max_layers] */
   const double* relative_humidity;          /* [P][max_layers] */
+  /* Surface%Wind_Speed [P] m/s, read by the IR sea-surface emissivity model
+   * (NULL: the reference's default 5 m/s, CRTM_Surface_Define.f90:183). */
+  const double* wind_speed;
 } crtm_gpu_batch;
 
 typedef struct {
@@ -168,6 +175,10 @@ typedef struct {
    * ('GOCART-GEOS5', 'NAAPS'), or NULL; zero under the other schemes. */
   double* aerosol_effective_variance;
   double* relative_humidity;
+  /* Surface_K%Wind_Speed [P][L] through the IR sea-surface emissivity model
+   * (batch emissivity NULL), or NULL; a 'Nalli2' table's temperature
+   * dependence is added into water_temperature. */
+  double* wind_speed;
 } crtm_gpu_kmatrix;
 
 typedef struct {
@@ -187,6 +198,7 @@ typedef struct {
   double* ice_temperature;    /* [P] */
   double* aerosol_effective_variance; /* [P][max_aerosols][max_layers], or NULL */
   double* relative_humidity;          /* [P][max_layers], or NULL */
+  double* wind_speed;                 /* [P] Surface_AD%Wind_Speed (emissivity model), or NULL */
 } crtm_gpu_adjoint_out;
 
 /* Tangent-linear inputs (Atmosphere_TL, Surface_TL and the emissivity
@@ -210,13 +222,15 @@ typedef struct {
   const double* aerosol_effective_radius;
   const double* aerosol_effective_variance; /* [P][max_aerosols][max_layers] */
   const double* relative_humidity;          /* [P][max_layers] */
+  const double* wind_speed;                 /* [P] (emissivity model) */
 } crtm_gpu_tl_in;
 
 /* CRTM_Init: loads <coeff_path>/<sensor_id>.SpcCoeff.bin and .TauCoeff.bin
- * (ODPS) for each sensor, and <coeff_path>/CloudCoeff.bin and
- * AerosolCoeff.bin when those files exist (the reference's default LUT
- * names), and uploads them to the current CUDA device.  Batches with clouds
- * or aerosols need the matching LUT. */
+ * (ODPS) for each sensor, and <coeff_path>/CloudCoeff.bin, AerosolCoeff.bin
+ * and Nalli.IRwater.EmisCoeff.bin when those files exist (the reference's
+ * default file names), and uploads them to the current CUDA device.  Batches
+ * with clouds or aerosols need the matching LUT; batches without an
+ * emissivity need the IR water table. */
 int crtm_gpu_init(const char* coeff_path, int n_sensors, const char* const* sensor_ids,
                   crtm_gpu_handle* handle);
 

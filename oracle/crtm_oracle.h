@@ -124,6 +124,17 @@ void or_aerosol_destroy(or_aerosol* a);
 int or_forward_scatter(const or_handle* h, const or_cloud* cc, const or_aerosol* ca, const or_batch* b,
                        const or_clouds* cl, double* radiance, double* bt, int n_threads);
 
+/* ---- IR sea-surface emissivity (CRTM_IRSSEM) ------------------------------ */
+typedef struct or_irwater_s or_irwater;
+/* Load an IRwaterCoeff binary file (Release 4). */
+or_irwater* or_irwater_init(const char* path);
+void or_irwater_destroy(or_irwater* w);
+/* CRTM_Compute_IRSSEM (CRTM_IRSSEM.f90:204-334) at one angle (degrees):
+ * Lagrange interpolation in angle, frequency (cm^-1) and wind speed (m/s),
+ * and water temperature (K) for a 'Nalli2' table; each clamped to its axis. */
+double or_irssem(const or_irwater* w, double water_temperature, double wind_speed, double frequency,
+                 double angle);
+
 /* Test hooks: one ADA layer (row-major nZ x nZ blocks) and the angle/phase setup. */
 int or_amom_layer(int nS, int nZ, double w, double tau, const double* mu, const double* wt,
                   const double* ff, const double* bb, double B, double* trans, double* refl,

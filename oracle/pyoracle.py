@@ -80,6 +80,11 @@ def lib():
         L.or_aerosol_init_scheme.restype = ct.c_void_p
         L.or_aerosol_init_scheme.argtypes = [ct.c_char_p, ct.c_char_p]
         L.or_aerosol_destroy.argtypes = [ct.c_void_p]
+        L.or_irwater_init.restype = ct.c_void_p
+        L.or_irwater_init.argtypes = [ct.c_char_p]
+        L.or_irwater_destroy.argtypes = [ct.c_void_p]
+        L.or_irssem.restype = ct.c_double
+        L.or_irssem.argtypes = [ct.c_void_p, ct.c_double, ct.c_double, ct.c_double, ct.c_double]
         L.or_amom_layer.argtypes = [ct.c_int, ct.c_int, ct.c_double, ct.c_double, _dp, _dp, _dp, _dp,
                                     ct.c_double, _dp, _dp, _dp]
         L.or_phase_setup.argtypes = [ct.c_int, ct.c_double, _dp, _dp, _dp, _dp, _dp, _ip]
@@ -244,3 +249,24 @@ class Oracle:
         if st:
             raise RuntimeError(lib().or_last_error().decode())
         return out
+
+
+def irwater_emissivity(path: str, sfc, geo, frequency) -> np.ndarray:
+    """(P, L) IR sea-surface emissivities at each profile's sensor zenith angle
+    (CRTM_IRSSEM through the oracle) from Surface%Water_Temperature and
+    %Wind_Speed (5 m/s when absent) and the channel frequencies (cm^-1)."""
+    L = lib()
+    h = L.or_irwater_init(path.encode())
+    if not h:
+        raise IOError(L.or_last_error().decode())
+    try:
+        P = sfc.water_temperature.shape[0]
+        wind = sfc.wind_speed if getattr(sfc, "wind_speed", None) is not None else np.full(P, 5.0)
+        out = np.zeros((P, len(frequency)))
+        for m in range(P):
+            for c, f in enumerate(frequency):
+                out[m, c] = L.or_irssem(h, float(sfc.water_temperature[m]), float(wind[m]), float(f),
+                                        float(geo.sensor_zenith_angle[m]))
+        return out
+    finally:
+        L.or_irwater_destroy(h)

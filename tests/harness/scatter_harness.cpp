@@ -366,3 +366,17 @@ extern "C" int sx_aerosol_layer_record(const int* adims, const int* atypes, cons
   for (int i = 0; i < nZ; i++) put(src[i], 1 + 2 * nZ * nZ + i);
   return kind;
 }
+
+// IR sea-surface emissivity (irssem) with its wind-speed and temperature derivatives.
+extern "C" double sx_irssem(const int* dims, int nalli2, const double* angle, const double* freq, const double* wind,
+                            const double* temp, const double* e, double water_temperature, double wind_speed,
+                            double frequency, double ang, double* de_dv, double* de_dt) {
+  const IRWaterLut W{dims[0], dims[1], dims[2], dims[3], nalli2, angle, freq, wind, temp, e};
+  Dual<2> t(water_temperature), v(wind_speed);
+  v.d[0] = 1.0;
+  t.d[1] = 1.0;
+  const Dual<2> r = irssem<Dual<2>>(W, t, v, frequency, ang);
+  *de_dv = r.d[0];
+  *de_dt = r.d[1];
+  return irssem<double>(W, water_temperature, wind_speed, frequency, ang);
+}

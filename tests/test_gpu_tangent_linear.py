@@ -1,7 +1,8 @@
 """CRTM_Tangent_Linear on the GPU: against central differences of the forward
 and, through the dot-product test, against the adjoint (<TL dx, y> = <dx, AD y>,
 the reference's test_AD.f90:216-377 method).  Clear sky, clouds with
-fractional cover, and aerosols; FP64 form."""
+fractional cover, and aerosols (schemes 'CRTM', 'CMAQ' with Effective_Variance
+and 'GOCART-GEOS5' with Relative_Humidity perturbed); FP64 form."""
 import copy
 import types
 
@@ -16,8 +17,19 @@ pytestmark = pytest.mark.gpu
 @pytest.fixture(scope="module")
 def cloud_dir(coeff_dir):
     sy.write_cloud_files(coeff_dir)
-    sy.write_aerosol_files(coeff_dir)
+    for scheme in co.AEROSOL_SCHEMES:
+        sy.write_aerosol_files(coeff_dir, scheme)
     return coeff_dir
+
+
+SCHEME = {"cmaq": "CMAQ", "gocart": "GOCART-GEOS5"}
+
+
+def _handle(gpu_lib, cloud_dir, sensor, kind):
+    scheme = SCHEME.get(kind)
+    if scheme is None:
+        return gpu_lib.CRTM([sensor], cloud_dir, 0)
+    return gpu_lib.CRTM([sensor], cloud_dir, 0, aerosol_model=scheme, aerosol_coeff_file=sy.aerosol_file_name(scheme))
 
 
 def _case(kind):
@@ -33,6 +45,8 @@ def _case(kind):
     atm, sfc, geo, opt = sy.clear_sky_workload(sensor, 4, 101, 404)
     sy.add_clouds(atm, (co.WATER_CLOUD, co.ICE_CLOUD), 405, wc_scale=30.0)
     sy.add_aerosols(atm, sy.AEROSOL_TYPES, 406, load_scale=20.0)
+    if kind in SCHEME:
+        sy.add_aerosol_scheme_inputs(atm, 410)
     return (sensor, atm, sfc, geo, opt)
 
 
@@ -42,7 +56,8 @@ def _direction(atm, sfc, P, L, seed):
     d = types.SimpleNamespace()
     d.temperature = rng.standard_normal(atm.temperature.shape)
     d.absorber = rng.standard_normal(atm.absorber.shape) * atm.absorber * 0.05
-    for f in ("cloud_water_content", "cloud_effective_radius", "aerosol_concentration", "aerosol_effective_radius"):
+    for f in ("cloud_water_content", "cloud_effective_radius", "aerosol_concentration", "aerosol_effective_radius",
+              "aerosol_effective_variance", "relative_humidity"):
         v = getattr(atm, f)
         setattr(d, f, None if v is None else rng.uniform(-0.05, 0.05, v.shape) * v)
     d.cloud_fraction = None if atm.cloud_fraction is None else \
@@ -56,7 +71,8 @@ def _direction(atm, sfc, P, L, seed):
 def _moved(atm, sfc, opt, d, s, e, h):
     a, f, o = copy.deepcopy(atm), copy.deepcopy(sfc), copy.deepcopy(opt)
     for name in ("temperature", "absorber", "cloud_water_content", "cloud_effective_radius", "cloud_fraction",
-                 "aerosol_concentration", "aerosol_effective_radius"):
+                 "aerosol_concentration", "aerosol_effective_radius", "aerosol_effective_variance",
+                 "relative_humidity"):
         dv = getattr(d, name)
         if dv is not None and getattr(a, name) is not None:
             setattr(a, name, getattr(a, name) + h * dv)
@@ -66,10 +82,10 @@ def _moved(atm, sfc, opt, d, s, e, h):
     return a, f, o
 
 
-@pytest.mark.parametrize("kind", ["clear", "clouds", "aerosols"])
+@pytest.mark.parametrize("kind", ["clear", "clouds", "aerosols", "cmaq", "gocart"])
 def test_tangent_linear_matches_central_differences(gpu_lib, cloud_dir, kind):
     sensor, atm, sfc, geo, opt = _case(kind)
-    h = gpu_lib.CRTM([sensor], cloud_dir, 0)
+    h = _handle(gpu_lib, cloud_dir, sensor, kind)
     P, L = atm.n_profiles, h.n_channels[0]
     sfc.land_coverage[:] = 0.2
     sfc.water_coverage[:] = 0.6
@@ -92,10 +108,10 @@ def test_tangent_linear_matches_central_differences(gpu_lib, cloud_dir, kind):
                                                       [x.max() / np.abs(bt_tl).max() for x in errs])
 
 
-@pytest.mark.parametrize("kind", ["clear", "clouds", "aerosols"])
+@pytest.mark.parametrize("kind", ["clear", "clouds", "aerosols", "cmaq", "gocart"])
 def test_tangent_linear_adjoint_dot_product(gpu_lib, cloud_dir, kind):
     sensor, atm, sfc, geo, opt = _case(kind)
-    h = gpu_lib.CRTM([sensor], cloud_dir, 0)
+    h = _handle(gpu_lib, cloud_dir, sensor, kind)
     P, L = atm.n_profiles, h.n_channels[0]
     d, s, e = _direction(atm, sfc, P, L, 408)
     d.cloud_fraction = None if atm.cloud_fraction is None else np.where(atm.cloud_fraction > 0, d.cloud_fraction, 0)
@@ -107,7 +123,7 @@ def test_tangent_linear_adjoint_dot_product(gpu_lib, cloud_dir, kind):
     rhs += float(sum((ad[f] * getattr(s, f)).sum() for f in ("land_temperature", "water_temperature",
                                                              "snow_temperature", "ice_temperature")))
     for f in ("cloud_water_content", "cloud_effective_radius", "cloud_fraction", "aerosol_concentration",
-              "aerosol_effective_radius"):
-        if f in ad and getattr(d, f) is not None:
+              "aerosol_effective_radius", "aerosol_effective_variance", "relative_humidity"):
+        if f in ad and getattr(d, f, None) is not None:
             rhs += float((ad[f] * getattr(d, f)).sum())
     assert abs(lhs - rhs) <= 1e-10 * max(abs(lhs), 1e-300), (lhs, rhs)

@@ -481,3 +481,48 @@ def test_nearly_defective_eigenbasis_derivatives(sx, coeff_dir):
         c2[a] -= h
         fd = (rec(c1, a)[1][0] - rec(c2, a)[1][0]) / (2 * h)
         assert np.abs(fd - dc).max() <= 2e-5 * np.abs(fd).max(), a
+
+
+@pytest.mark.parametrize("classification", ["Nalli", "Nalli2"])
+def test_irssem_matches_oracle(sx, tmp_path, classification):
+    """The GPU header's IR sea-surface emissivity (CRTM_IRSSEM) against the
+    oracle's on random angles, frequencies, wind speeds and temperatures,
+    inside and outside the table's axes, and its wind-speed / temperature
+    derivatives against central differences."""
+    from oracle.pyoracle import lib
+    path = sy.write_irwater_file(str(tmp_path), classification, "irw.bin")
+    w = co.read_irwatercoeff(path)
+    L = lib()
+    h = L.or_irwater_init(path.encode())
+    assert h
+    f = lambda a: np.ascontiguousarray(np.ravel(a, order="F"))   # noqa: E731
+    dims = np.array([w.angle.size, w.frequency.size, w.wind_speed.size, w.temperature.size], np.int32)
+    arrs = [f(x) for x in (w.angle, w.frequency, w.wind_speed, w.temperature, w.emissivity)]
+    sx.sx_irssem.restype = ct.c_double
+    rng = np.random.Generator(np.random.PCG64(11))
+    nalli2 = int(classification == "Nalli2")
+
+    def gpu(t, v, fr, a):
+        dv, dt = ct.c_double(), ct.c_double()
+        e = sx.sx_irssem(_p(dims, _ip), nalli2, *[_p(x) for x in arrs], ct.c_double(t), ct.c_double(v),
+                         ct.c_double(fr), ct.c_double(a), ct.byref(dv), ct.byref(dt))
+        return e, dv.value, dt.value
+    try:
+        for _ in range(300):
+            t, v = rng.uniform(265.0, 315.0), rng.uniform(-1.0, 18.0)
+            fr, a = rng.uniform(550.0, 3100.0), rng.uniform(-80.0, 88.0)
+            e, dv, dt = gpu(t, v, fr, a)
+            assert abs(e - L.or_irssem(h, t, v, fr, a)) <= 1e-14
+            hv = 1e-5
+            fd = (gpu(t, v + hv, fr, a)[0] - gpu(t, v - hv, fr, a)[0]) / (2 * hv)
+            assert abs(fd - dv) <= 1e-7, (v, fd, dv)
+            fd = (gpu(t + hv, v, fr, a)[0] - gpu(t - hv, v, fr, a)[0]) / (2 * hv)
+            assert abs(fd - dt) <= 1e-7
+            if not nalli2:
+                assert dt == 0.0
+        # at the table's nodes the interpolation returns the table
+        i, j, k = 3, 10, 5
+        assert abs(gpu(w.temperature[0], w.wind_speed[k], w.frequency[j], w.angle[i])[0] -
+                   w.emissivity[i, j, k, 0]) <= 1e-14
+    finally:
+        L.or_irwater_destroy(h)
