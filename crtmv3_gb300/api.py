@@ -100,6 +100,12 @@ class CTLIn(ct.Structure):
     _fields_ = [(f, ct.c_void_p) for f in TL_FIELDS]
 
 
+class CTuning(ct.Structure):
+    """crtm_gpu_tuning: channels per map CTA, profile cap per pipeline pass,
+    measured milliseconds per call."""
+    _fields_ = [("map_channels", ct.c_int), ("chunk_profiles", ct.c_int), ("ms_per_call", ct.c_double)]
+
+
 def _scatter_shapes(atm, aerosol_model: str = "CRTM") -> dict:
     """Per-profile shapes (after the profile axis) of the scattering Jacobians
     that a batch has: clouds (NC, Kmax) and the cloud fraction (Kmax,), aerosols
@@ -149,6 +155,10 @@ def library() -> ct.CDLL:
     L.crtm_gpu_adjoint_device.argtypes = [ct.c_void_p, ct.c_int, ct.POINTER(CBatch), ct.c_void_p,
                                           ct.POINTER(CAdjoint), ct.POINTER(CRTSolution), ct.c_void_p]
     L.crtm_gpu_k_matrix_device_static.argtypes = L.crtm_gpu_k_matrix_device.argtypes
+    L.crtm_gpu_get_tuning.argtypes = [ct.c_void_p, ct.c_int, ct.c_int, ct.POINTER(CTuning)]
+    L.crtm_gpu_set_tuning.argtypes = [ct.c_void_p, ct.c_int, ct.c_int, ct.POINTER(CTuning)]
+    L.crtm_gpu_autotune_k_matrix_device.argtypes = L.crtm_gpu_k_matrix_device.argtypes + [
+        ct.c_int, ct.POINTER(CTuning), ct.c_int, ct.POINTER(ct.c_int), ct.POINTER(CTuning)]
     L.crtm_gpu_last_error.argtypes = [ct.c_void_p, ct.c_char_p, ct.c_int]
     L.crtm_gpu_launch_count.argtypes = [ct.c_void_p]
     L.crtm_gpu_launch_count.restype = ct.c_longlong
@@ -435,6 +445,13 @@ class CRTM:
         """K-matrix on device tensors.  ``static_scratch``: use the entry point that
         keeps its intermediates in the library's fixed per-device scratch and
         allocates no device memory (calls must not overlap in time)."""
+        cr, ck, sel = self._kmatrix_structs(out, k_absorbers)
+        fn = (library().crtm_gpu_k_matrix_device_static if static_scratch
+              else library().crtm_gpu_k_matrix_device)
+        self._check(fn(self.h, sensor, ct.byref(b), _addr(seed), ct.byref(ck), ct.byref(cr), stream))
+
+    @staticmethod
+    def _kmatrix_structs(out: dict, k_absorbers=None):
         cr = CRTSolution(out["radiance"].data_ptr(), out["bt"].data_ptr(),
                          _addr(out.get("status")))
         sel = None if k_absorbers is None else np.ascontiguousarray(k_absorbers, np.int32)
@@ -444,9 +461,38 @@ class CRTM:
                       *[_addr(out.get(f + "_k")) for f in SCATTER_JACOBIANS])
         for f in SCHEME_JACOBIANS:
             setattr(ck, f, _addr(out.get(f + "_k")))
-        fn = (library().crtm_gpu_k_matrix_device_static if static_scratch
-              else library().crtm_gpu_k_matrix_device)
-        self._check(fn(self.h, sensor, ct.byref(b), _addr(seed), ct.byref(ck), ct.byref(cr), stream))
+        return cr, ck, sel   # sel keeps the absorber selection alive during the call
+
+    def tuning(self, sensor: int = 0, precision: Optional[int] = None) -> dict:
+        """The tuning in effect for a sensor and arithmetic form (default: the
+        handle's): map_channels, chunk_profiles, ms_per_call."""
+        t = CTuning()
+        pr = self.precision if precision is None else precision
+        self._check(library().crtm_gpu_get_tuning(self.h, sensor, pr, ct.byref(t)))
+        return dict(map_channels=t.map_channels, chunk_profiles=t.chunk_profiles, ms_per_call=t.ms_per_call)
+
+    def set_tuning(self, map_channels: int = 0, chunk_profiles: int = 0, sensor: int = 0,
+                   precision: Optional[int] = None) -> None:
+        pr = self.precision if precision is None else precision
+        t = CTuning(map_channels, chunk_profiles, 0.0)
+        self._check(library().crtm_gpu_set_tuning(self.h, sensor, pr, ct.byref(t)))
+
+    def autotune_k_matrix_device(self, b: CBatch, out: dict, seed=None, sensor: int = 0, stream=None,
+                                 reps: int = 3, k_absorbers=None) -> dict:
+        """Time the device K-matrix of this batch under each candidate tuning
+        and keep the fastest for the sensor (crtm_gpu_autotune_k_matrix_device).
+        Returns {"chosen": {...}, "trials": [{...}, ...]}; ``out`` holds the
+        batch's K-matrix afterwards."""
+        cr, ck, sel = self._kmatrix_structs(out, k_absorbers)
+        trials = (CTuning * 16)()
+        n = ct.c_int(0)
+        best = CTuning()
+        self._check(library().crtm_gpu_autotune_k_matrix_device(
+            self.h, sensor, ct.byref(b), _addr(seed), ct.byref(ck), ct.byref(cr), stream, reps,
+            trials, 16, ct.byref(n), ct.byref(best)))
+        conv = lambda t: dict(map_channels=t.map_channels, chunk_profiles=t.chunk_profiles,
+                              ms_per_call=t.ms_per_call)
+        return dict(chosen=conv(best), trials=[conv(trials[i]) for i in range(min(n.value, 16))])
 
     def forward_device(self, b: CBatch, out: dict, sensor: int = 0, stream=None) -> None:
         cr = CRTSolution(out["radiance"].data_ptr(), out["bt"].data_ptr(), _addr(out.get("status")))

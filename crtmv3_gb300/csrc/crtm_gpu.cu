@@ -132,6 +132,13 @@ struct Sensor {
   SensorTables tables{};
   RefSums refsums{};
   SpecView spec{};
+  // tuning per arithmetic form ([0] FP64, [1] mixed), set by
+  // crtm_gpu_set_tuning or crtm_gpu_autotune_k_matrix_device: channels per
+  // map_kernel CTA (0 = the handle default) and a cap on the profiles per
+  // pipeline pass (0 = as many as the workspace budget holds)
+  int tune_map[2] = {0, 0};
+  int tune_chunk[2] = {0, 0};
+  double tune_ms[2] = {0.0, 0.0};
 };
 
 bool load_sensor(const std::string& dir, const std::string& id, Sensor& s, std::string& err) {
@@ -869,6 +876,8 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
   const size_t per = work_bytes<G, R>(s, 64, Kmax, nv, mode, nullptr, nullptr, sw) / 64 + 1;
   int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)P, h->workspace_budget / per));
   if (hc && hc->max_chunk > 0) chunk = std::min(chunk, hc->max_chunk);
+  constexpr int form = sizeof(R) == sizeof(float) ? 1 : 0;
+  if (!fixed && s.tune_chunk[form] > 0) chunk = std::min(chunk, s.tune_chunk[form]);
   char* ws_base;
   if (fixed) {
     // largest chunk whose workspace fits the fixed scratch
@@ -895,8 +904,9 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
   const size_t col_smem = column_smem_bytes<R>(K, Kmax);
   // channels per map CTA: 16 (more resident CTAs hide the tile loads; C2:
   // 6.4 ms against 7.4 ms with 32 and 8.1 ms with 8), fewer if the tiles exceed
-  // the shared-memory budget (CRTM_GPU_MAP_CHANNELS: 8, 16 or 32 overrides)
-  int map_ct = h->map_channels;
+  // the shared-memory budget (CRTM_GPU_MAP_CHANNELS: 8, 16 or 32 overrides;
+  // a sensor's tuning overrides both)
+  int map_ct = s.tune_map[form] > 0 ? s.tune_map[form] : h->map_channels;
   while (map_ct > 8 && map_smem_bytes<R>(K, Kmax, nv, map_ct) > 200 * 1024) map_ct >>= 1;
   const size_t map_smem = map_smem_bytes<R>(K, Kmax, nv, map_ct);
   constexpr size_t fwd_smem = fwd_smem_bytes<G, R, NPF>();
@@ -1887,6 +1897,116 @@ int crtm_gpu_k_matrix_device_static(crtm_gpu_handle h, int sensor, const crtm_gp
   const FixedScratch fx{(char*)slot.ptr, STATIC_SCRATCH_BYTES};
   return dispatch(h, sensor, b, 1, bt_k, rts, k, nullptr,
                   (cudaStream_t)stream, nullptr, &fx);
+}
+
+int crtm_gpu_get_tuning(crtm_gpu_handle h, int sensor, int precision, crtm_gpu_tuning* out) {
+  if (!h) return CRTM_GPU_FAILURE;
+  if (sensor < 0 || sensor >= (int)h->sensors.size()) return fail(h, "sensor index %d out of range", sensor);
+  if (precision != CRTM_GPU_FP64 && precision != CRTM_GPU_MIXED) return fail(h, "unknown precision %d", precision);
+  if (!out) return fail(h, "missing tuning output");
+  const Sensor& s = h->sensors[sensor];
+  const int f = precision == CRTM_GPU_MIXED ? 1 : 0;
+  out->map_channels = s.tune_map[f] > 0 ? s.tune_map[f] : h->map_channels;
+  out->chunk_profiles = s.tune_chunk[f];
+  out->ms_per_call = s.tune_ms[f];
+  return CRTM_GPU_SUCCESS;
+}
+
+int crtm_gpu_set_tuning(crtm_gpu_handle h, int sensor, int precision, const crtm_gpu_tuning* t) {
+  if (!h) return CRTM_GPU_FAILURE;
+  if (sensor < 0 || sensor >= (int)h->sensors.size()) return fail(h, "sensor index %d out of range", sensor);
+  if (precision != CRTM_GPU_FP64 && precision != CRTM_GPU_MIXED) return fail(h, "unknown precision %d", precision);
+  if (!t) return fail(h, "missing tuning");
+  if (t->map_channels != 0 && t->map_channels != 8 && t->map_channels != 16 && t->map_channels != 32)
+    return fail(h, "map_channels must be 0, 8, 16 or 32 (got %d)", t->map_channels);
+  if (t->chunk_profiles < 0) return fail(h, "chunk_profiles must be >= 0 (got %d)", t->chunk_profiles);
+  Sensor& s = h->sensors[sensor];
+  const int f = precision == CRTM_GPU_MIXED ? 1 : 0;
+  s.tune_map[f] = t->map_channels;
+  s.tune_chunk[f] = t->chunk_profiles;
+  s.tune_ms[f] = 0.0;
+  return CRTM_GPU_SUCCESS;
+}
+
+// Times the K-matrix of this batch (device buffers, as
+// crtm_gpu_k_matrix_device) under each candidate tuning and keeps the
+// fastest for the sensor and the arithmetic form the call runs in.
+// Candidates: 16, 8 and 32 channels per map CTA, each with no cap on the
+// profiles per pipeline pass, with P/2 and with P/4.  Each candidate runs
+// once untimed (workspace growth, shared-memory attributes), then `reps`
+// times between two CUDA events on `stream`.  The per-output arithmetic of
+// the pipeline does not depend on either setting, so every trial writes the
+// same K-matrix and RTSolution; the outputs hold it when the call returns.
+int crtm_gpu_autotune_k_matrix_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b,
+                                      const double* bt_k, crtm_gpu_kmatrix* k,
+                                      crtm_gpu_rtsolution* rts, void* stream, int reps,
+                                      crtm_gpu_tuning* trials, int max_trials, int* n_trials,
+                                      crtm_gpu_tuning* chosen) {
+  if (!h) return CRTM_GPU_FAILURE;
+  if (sensor < 0 || sensor >= (int)h->sensors.size()) return fail(h, "sensor index %d out of range", sensor);
+  if (!b || b->n_profiles < 1) return fail(h, "autotune needs a batch of at least one profile");
+  if (reps < 1 || reps > 1000) return fail(h, "reps must be in 1..1000 (got %d)", reps);
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
+  const cudaStream_t st = (cudaStream_t)stream;
+  const bool scat = b->max_clouds > 0 || b->max_aerosols > 0;
+  // the form dispatch runs the K-matrix in (batches with clouds or aerosols: FP64)
+  const int f = (h->precision == CRTM_GPU_MIXED && !scat) ? 1 : 0;
+  Sensor& s = h->sensors[sensor];
+  const int old_map = s.tune_map[f], old_chunk = s.tune_chunk[f];
+  const double old_ms = s.tune_ms[f];
+  const int P = b->n_profiles;
+  std::vector<std::pair<int, int>> cand;
+  for (int mc : {16, 8, 32}) {
+    int last = -1;
+    for (int cap : {0, (P + 1) / 2, (P + 3) / 4}) {
+      if (cap >= P) cap = 0;   // a cap at or above the batch is no cap
+      if (cap == last) continue;
+      cand.emplace_back(mc, cap);
+      last = cap;
+    }
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    return fail(h, "cudaEventCreate failed");
+  }
+  int best = -1;
+  double best_ms = 0.0;
+  int rc = CRTM_GPU_SUCCESS;
+  int n = 0;
+  for (size_t i = 0; i < cand.size(); i++) {
+    s.tune_map[f] = cand[i].first;
+    s.tune_chunk[f] = cand[i].second;
+    rc = dispatch(h, sensor, b, 1, bt_k, rts, k, nullptr, st);
+    if (rc != CRTM_GPU_SUCCESS) break;
+    if (cudaEventRecord(e0, st) != cudaSuccess) { rc = fail(h, "cudaEventRecord failed"); break; }
+    for (int r = 0; r < reps && rc == CRTM_GPU_SUCCESS; r++) rc = dispatch(h, sensor, b, 1, bt_k, rts, k, nullptr, st);
+    if (rc != CRTM_GPU_SUCCESS) break;
+    float ms = 0.0f;
+    if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      rc = fail(h, "timing the trial failed: %s", cudaGetErrorString(cudaGetLastError()));
+      break;
+    }
+    const double per = (double)ms / reps;
+    if (trials && n < max_trials) trials[n] = crtm_gpu_tuning{cand[i].first, cand[i].second, per};
+    n++;
+    if (best < 0 || per < best_ms) { best = (int)i; best_ms = per; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (n_trials) *n_trials = n;
+  if (rc != CRTM_GPU_SUCCESS || best < 0) {
+    s.tune_map[f] = old_map;
+    s.tune_chunk[f] = old_chunk;
+    s.tune_ms[f] = old_ms;
+    return rc != CRTM_GPU_SUCCESS ? rc : fail(h, "autotune ran no trial");
+  }
+  s.tune_map[f] = cand[best].first;
+  s.tune_chunk[f] = cand[best].second;
+  s.tune_ms[f] = best_ms;
+  if (chosen) *chosen = crtm_gpu_tuning{cand[best].first, cand[best].second, best_ms};
+  return CRTM_GPU_SUCCESS;
 }
 
 int crtm_gpu_last_error(crtm_gpu_handle h, char* buf, int n) {

@@ -308,6 +308,45 @@ int crtm_gpu_k_matrix_device_static(crtm_gpu_handle handle, int sensor,
                                     const crtm_gpu_batch* batch, const double* bt_k,
                                     crtm_gpu_kmatrix* k, crtm_gpu_rtsolution* rts, void* stream);
 
+/* Tuning of the pipeline (no reference counterpart: the reference's only
+ * batching parameter is the OpenMP chunking of profiles and channels,
+ * CRTM_Forward_Module.f90:328-357).  Kept per sensor and per arithmetic form
+ * (CRTM_GPU_FP64 / CRTM_GPU_MIXED; the K-matrix of a batch with clouds or
+ * aerosols runs in the FP64 form).  Neither setting changes any output's
+ * arithmetic, only the work decomposition:
+ *   map_channels    channels per map_kernel CTA: 8, 16 or 32; 0 = the handle
+ *                   default (16, or the CRTM_GPU_MAP_CHANNELS environment
+ *                   variable); reduced automatically when the tiles exceed
+ *                   the shared-memory budget
+ *   chunk_profiles  at most this many profiles per pipeline pass; 0 = as many
+ *                   as the workspace budget holds (the static-scratch entry
+ *                   point sizes its own passes and ignores it)
+ *   ms_per_call     the autotuner's measured time of one call with this
+ *                   setting; 0 when set by crtm_gpu_set_tuning
+ * crtm_gpu_get_tuning reports the values in effect (map_channels resolved). */
+typedef struct {
+  int map_channels;
+  int chunk_profiles;
+  double ms_per_call;
+} crtm_gpu_tuning;
+int crtm_gpu_get_tuning(crtm_gpu_handle handle, int sensor, int precision, crtm_gpu_tuning* out);
+int crtm_gpu_set_tuning(crtm_gpu_handle handle, int sensor, int precision, const crtm_gpu_tuning* t);
+
+/* Autotuner (no reference counterpart).  Runs crtm_gpu_k_matrix_device on the
+ * given device buffers under each candidate tuning (map_channels 16, 8, 32,
+ * each with no chunk cap, P/2 and P/4; duplicates dropped), once untimed and
+ * then `reps` (1..1000) times between CUDA events on `stream`, and keeps the
+ * fastest for the sensor and the form the call runs in.  Up to max_trials
+ * measured candidates go to `trials` (may be NULL), their number to *n_trials
+ * and the winner to *chosen (either may be NULL).  On return the outputs hold
+ * the batch's K-matrix and RTSolution.  On failure the previous tuning is
+ * kept. */
+int crtm_gpu_autotune_k_matrix_device(crtm_gpu_handle handle, int sensor,
+                                      const crtm_gpu_batch* batch, const double* bt_k,
+                                      crtm_gpu_kmatrix* k, crtm_gpu_rtsolution* rts, void* stream,
+                                      int reps, crtm_gpu_tuning* trials, int max_trials,
+                                      int* n_trials, crtm_gpu_tuning* chosen);
+
 /* Copy the last error message of the handle (or of the last failed init when
  * handle is NULL) into buf; returns its length. */
 int crtm_gpu_last_error(crtm_gpu_handle handle, char* buf, int n);

@@ -49,7 +49,7 @@ def test_ctypes_structs_match_the_header_layout(tmp_path):
     from crtmv3_gb300 import api
     structs = {"crtm_gpu_batch": api.CBatch, "crtm_gpu_rtsolution": api.CRTSolution,
                "crtm_gpu_kmatrix": api.CKMatrix, "crtm_gpu_adjoint_out": api.CAdjoint,
-               "crtm_gpu_tl_in": api.CTLIn}
+               "crtm_gpu_tl_in": api.CTLIn, "crtm_gpu_tuning": api.CTuning}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "crtm_gpu.h"', "int main(void) {"]
     for cname, py in structs.items():
         lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
