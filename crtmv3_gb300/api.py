@@ -22,10 +22,12 @@ from __future__ import annotations
 import ctypes as ct
 import dataclasses
 import os
+import types
 from typing import List, Optional, Sequence
 
 import numpy as np
 
+from . import addlayers
 from .structures import (AtmosphereBatch, GeometryBatch, KMatrixBatch, OptionsBatch,
                          RTSolutionBatch, SurfaceBatch)
 
@@ -553,6 +555,9 @@ def CRTM_Forward(atmosphere: AtmosphereBatch, surface: SurfaceBatch, geometry: G
     """CRTM_Forward.  ``rts`` receives one RTSolutionBatch per sensor in ChannelInfo order.
     ``options.emissivity`` is (P, total channels) over all sensors."""
     rts.clear()
+    atmosphere, _ = _added_layers(atmosphere, "CRTM_Forward")
+    if atmosphere is None:
+        return FAILURE
     off = 0
     for ci in channel_info:
         opt = _sensor_options(options, off, ci.n_channels)
@@ -573,6 +578,9 @@ def CRTM_K_Matrix(atmosphere, surface, rts_k: Optional[Sequence[np.ndarray]], ge
     are in its water_temperature / surface_emissivity fields)."""
     atmosphere_k.clear()
     rts.clear()
+    atmosphere, added = _added_layers(atmosphere, "CRTM_K_Matrix")
+    if atmosphere is None:
+        return FAILURE
     off = 0
     for i, ci in enumerate(channel_info):
         opt = _sensor_options(options, off, ci.n_channels)
@@ -582,6 +590,9 @@ def CRTM_K_Matrix(atmosphere, surface, rts_k: Optional[Sequence[np.ndarray]], ge
         except RuntimeError as e:
             print(f"CRTM_K_Matrix(FAILURE): {e}")
             return FAILURE
+        if added.any:
+            km = dataclasses.replace(km, **{f: addlayers.user_layers(added, getattr(km, f))
+                                             for f in LAYER_FIELDS})
         atmosphere_k.append(km)
         rts.append(r)
         off += ci.n_channels
@@ -593,6 +604,9 @@ def CRTM_Adjoint(atmosphere, surface, rts_ad: Sequence[np.ndarray], geometry,
                  options: Optional[OptionsBatch] = None) -> int:
     """CRTM_Adjoint: adjoints summed over the channels of all sensors into ``atmosphere_ad``."""
     rts.clear()
+    atmosphere, added = _added_layers(atmosphere, "CRTM_Adjoint")
+    if atmosphere is None:
+        return FAILURE
     off = 0
     tot: dict = {}
     for i, ci in enumerate(channel_info):
@@ -602,6 +616,8 @@ def CRTM_Adjoint(atmosphere, surface, rts_ad: Sequence[np.ndarray], geometry,
         except RuntimeError as e:
             print(f"CRTM_Adjoint(FAILURE): {e}")
             return FAILURE
+        if added.any:
+            out = {k: addlayers.user_layers(added, v) if k in LAYER_FIELDS else v for k, v in out.items()}
         for k, v in out.items():
             tot[k] = tot[k] + v if k in tot else v.copy()
         rts.append(r)
@@ -619,6 +635,12 @@ def CRTM_Tangent_Linear(atmosphere, surface, atmosphere_tl, surface_tl, geometry
     per sensor, from the atmosphere and surface perturbations."""
     rts.clear()
     rts_tl.clear()
+    atmosphere, added = _added_layers(atmosphere, "CRTM_Tangent_Linear")
+    if atmosphere is None:
+        return FAILURE
+    if added.any and atmosphere_tl is not None:
+        atmosphere_tl = types.SimpleNamespace(**{
+            f: addlayers.extend_perturbation(added, getattr(atmosphere_tl, f, None)) for f in LAYER_FIELDS})
     off = 0
     for ci in channel_info:
         opt = _sensor_options(options, off, ci.n_channels)
@@ -632,6 +654,23 @@ def CRTM_Tangent_Linear(atmosphere, surface, atmosphere_tl, surface_tl, geometry
         rts_tl.append(bt_tl)
         off += ci.n_channels
     return SUCCESS
+
+
+# layer-indexed fields of the K-matrix, adjoint and tangent-linear structures
+LAYER_FIELDS = ("temperature", "absorber", "cloud_water_content", "cloud_effective_radius", "cloud_fraction",
+                "aerosol_concentration", "aerosol_effective_radius", "aerosol_effective_variance",
+                "relative_humidity")
+
+
+def _added_layers(atmosphere: AtmosphereBatch, routine: str):
+    """CRTM_Atmosphere_AddLayers before the call (CRTM_Forward_Module.f90:595,
+    CRTM_K_Matrix_Module.f90:693): (extended batch, AddedLayers), or (None,
+    None) after printing the failure."""
+    try:
+        return addlayers.add_layers(atmosphere)
+    except ValueError as e:
+        print(f"{routine}(FAILURE): {e}")
+        return None, None
 
 
 def _sensor_options(options: Optional[OptionsBatch], off: int, n: int) -> OptionsBatch:

@@ -58,6 +58,11 @@ class AtmosphereBatch:
     # reference's structures are initialised (the LUT lookup clamps them)
     aerosol_effective_variance: Optional[np.ndarray] = None  # (P, NA, Kmax)
     relative_humidity: Optional[np.ndarray] = None  # (P, Kmax), 0..1
+    # Atmosphere%Climatology (1-6, default 6 = US Standard Atmosphere) and
+    # %Add_Extra_Layers (default true): the model profile that supplies the
+    # layers above a top level below 0.005 hPa (CRTM_Atmosphere_Define.f90:436-448)
+    climatology: Optional[np.ndarray] = None        # (P,) int
+    add_extra_layers: Optional[np.ndarray] = None   # (P,) bool
 
     @property
     def n_profiles(self) -> int:
@@ -81,7 +86,7 @@ class AtmosphereBatch:
             take(self.cloud_effective_radius), take(self.cloud_fraction),
             take(self.n_aerosols), take(self.aerosol_type), take(self.aerosol_concentration),
             take(self.aerosol_effective_radius), take(self.aerosol_effective_variance),
-            take(self.relative_humidity))
+            take(self.relative_humidity), take(self.climatology), take(self.add_extra_layers))
 
 
 @dataclasses.dataclass

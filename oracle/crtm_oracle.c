@@ -1066,3 +1066,50 @@ int or_profile_state(const or_handle* h, const or_batch* b, int m, double* T, do
 
 /* ---- scattering (clouds, ADA) ------------------------------------------- */
 #include "oracle_scatter.inc"
+
+/* ---- CRTM_Atmosphere_AddLayers for one profile -----------------------------
+ * src/Atmosphere/CRTM_Atmosphere.f90:248-400 with Extra_Layers :1043-1050,
+ * Layer_P / Layer_X :1054-1066, Interp_LPoly / Interp_Linear :1070-1084 and
+ * Shift_Profile :1088-1098; the model rows come from CRTM_Get_Model_Profile
+ * (src/Atmosphere/CRTM_Model_Profiles.f90:1120-1141).
+ *
+ * mlp[nlev]: model level pressures; mlt[nlev]: the model's level
+ * temperatures; mla[J][nlev]: its level amounts of the profile's J absorbers.
+ * top: the profile's Level_Pressure(0); up, ut: its first two layer
+ * pressures / temperatures; ua[J][2]: its first two layers' absorber amounts.
+ * Writes the n added layers: pl[n+1] level pressures, p[n], t[n], a[J][n].
+ * Returns n, or 0 when no model level lies at or below the top. */
+int or_add_layers(int nlev, const double* mlp, const double* mlt, const double* mla, int J,
+                  double top, const double* up, const double* ut, const double* ua,
+                  double* pl, double* p, double* t, double* a) {
+  int n = 0;
+  for (int k = 1; k < nlev; k++) {   /* 1-based DO n = 1, SIZE(...) over the 0-based levels */
+    if (mlp[k] >= top) { n = k; break; }
+  }
+  if (n < 1) return 0;
+  double tl[128], al[128];
+  if (n + 1 > 128) return 0;
+  for (int k = 0; k <= n; k++) { pl[k] = mlp[k]; tl[k] = mlt[k]; }
+  const double w = (log(top) - log(pl[n - 1])) / (log(pl[n]) - log(pl[n - 1]));
+  pl[n] = top;
+  tl[n] = (tl[n] - tl[n - 1]) * w + tl[n - 1];
+  for (int k = 1; k <= n; k++) {
+    p[k - 1] = (pl[k] - pl[k - 1]) / log(pl[k] / pl[k - 1]);
+    t[k - 1] = 0.5 * (tl[k - 1] + tl[k]);
+  }
+  const double e = (log(p[n - 1]) - log(up[0])) / (log(up[1]) - log(up[0]));
+  const double dt = ((ut[1] - ut[0]) * e + ut[0]) - t[n - 1];
+  for (int k = 0; k < n; k++) t[k] += dt;
+  for (int j = 0; j < J; j++) {
+    for (int k = 0; k <= n; k++) al[k] = mla[(size_t)j * nlev + k];
+    al[n] = (al[n] - al[n - 1]) * w + al[n - 1];
+    double* aj = a + (size_t)j * n;
+    for (int k = 1; k <= n; k++) aj[k - 1] = 0.5 * (al[k - 1] + al[k]);
+    const double da = ((ua[2 * j + 1] - ua[2 * j]) * e + ua[2 * j]) - aj[n - 1];
+    for (int k = 0; k < n; k++) {
+      aj[k] += da;
+      if (aj[k] < 0.0) aj[k] = 1.0e-76;   /* MINIMUM_ABSORBER_AMOUNT, CRTM_Parameters.f90:140 */
+    }
+  }
+  return n;
+}

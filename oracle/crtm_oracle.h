@@ -142,6 +142,13 @@ int or_amom_layer(int nS, int nZ, double w, double tau, const double* mu, const 
 int or_phase_setup(int nleg, double mu_sensor, const double* pc, double* mu, double* wt, double* ff,
                    double* bb, int* nZ_out);
 
+/* ---- CRTM_Atmosphere_AddLayers ------------------------------------------- */
+/* The layers added above one profile whose top lies below the model's first
+ * level (0.005 hPa); returns their number n (0: none can be added). */
+int or_add_layers(int nlev, const double* mlp, const double* mlt, const double* mla, int J,
+                  double top, const double* up, const double* ut, const double* ua,
+                  double* pl, double* p, double* t, double* a);
+
 #ifdef __cplusplus
 }
 #endif

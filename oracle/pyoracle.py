@@ -88,6 +88,8 @@ def lib():
         L.or_amom_layer.argtypes = [ct.c_int, ct.c_int, ct.c_double, ct.c_double, _dp, _dp, _dp, _dp,
                                     ct.c_double, _dp, _dp, _dp]
         L.or_phase_setup.argtypes = [ct.c_int, ct.c_double, _dp, _dp, _dp, _dp, _dp, _ip]
+        L.or_add_layers.argtypes = [ct.c_int, _dp, _dp, _dp, ct.c_int, ct.c_double, _dp, _dp, _dp,
+                                    _dp, _dp, _dp, _dp]
         _lib = L
     return _lib
 
@@ -270,3 +272,25 @@ def irwater_emissivity(path: str, sfc, geo, frequency) -> np.ndarray:
         return out
     finally:
         L.or_irwater_destroy(h)
+
+
+def add_layers_profile(model_p, model_t, model_a, top, user_p, user_t, user_a):
+    """The oracle's CRTM_Atmosphere_AddLayers for one profile: (pl (n+1,),
+    p (n,), t (n,), a (J, n)); n = 0 gives empty arrays.  model_a (J, nlev):
+    the climatology's rows for the profile's absorbers; user_p, user_t (2,) and
+    user_a (J, 2): the profile's first two layers."""
+    L = lib()
+    mp = np.ascontiguousarray(model_p, np.float64)
+    mt = np.ascontiguousarray(model_t, np.float64)
+    ma = np.ascontiguousarray(model_a, np.float64)
+    J, nlev = ma.shape
+    up = np.ascontiguousarray(user_p[:2], np.float64)
+    ut = np.ascontiguousarray(user_t[:2], np.float64)
+    ua = np.ascontiguousarray(np.asarray(user_a, np.float64)[:, :2])
+    pl = np.zeros(nlev)
+    p = np.zeros(nlev)
+    t = np.zeros(nlev)
+    a = np.zeros(J * nlev)
+    n = L.or_add_layers(nlev, _p(mp), _p(mt), _p(ma), J, float(top), _p(up), _p(ut), _p(ua),
+                        _p(pl), _p(p), _p(t), _p(a))
+    return pl[:n + 1] if n else pl[:0], p[:n], t[:n], a[:J * n].reshape(J, n)
