@@ -182,6 +182,17 @@ class OracleHandle:
         km = KMatrixBatch(r["temperature_k"], r["absorber_k"], r["water_temperature_k"], r["surface_emissivity_k"])
         return km, RTSolutionBatch(r["radiance"], r["bt"], status=np.zeros(atm.n_profiles, np.int32))
 
+    def tangent_linear(self, atm, sfc, geo, opt, atm_tl=None, sfc_tl=None, sensor=0):
+        self.seen.append((atm, atm_tl))
+        P, K = atm.n_profiles, atm.max_layers
+        t_tl = np.ascontiguousarray(getattr(atm_tl, "temperature", None) if atm_tl is not None else None)
+        t_tl = np.zeros((P, K)) if t_tl.ndim == 0 else t_tl
+        a_tl = getattr(atm_tl, "absorber", None) if atm_tl is not None else None
+        a_tl = np.zeros((P, atm.n_absorbers, K)) if a_tl is None else np.ascontiguousarray(a_tl)
+        bt_tl = self.o.tangent_fd(atm, sfc, geo, opt, t_tl, a_tl, np.zeros(P), step=1e-4)
+        rad, bt = self.o.forward(atm, sfc, geo, opt)
+        return bt_tl, RTSolutionBatch(rad, bt, status=np.zeros(P, np.int32))
+
     def adjoint(self, atm, sfc, geo, opt, bt_ad, sensor=0):
         self.seen.append(atm)
         r = self.o.adjoint(atm, sfc, geo, opt, bt_ad)
@@ -246,3 +257,28 @@ def test_k_matrix_matches_differences_below_the_top_two_layers(coeff_dir):
             bts.append(r[0].brightness_temperature)
         fd = (bts[0] - bts[1]) / (2 * step)
         assert np.abs(fd - kt[:, :, k]).max() < 1e-5 * scale, k
+
+
+def test_tangent_linear_gives_the_added_layers_no_perturbation(coeff_dir):
+    import types
+    atm, sfc, geo, opt = _workload(P=2, cut=(8, 15))
+    h = OracleHandle(coeff_dir)
+    L = h.o.n_channels
+    ci = [api.ChannelInfo(SENSOR, 0, L, h)]
+    ext, info = al.add_layers(atm)
+    dT = np.random.default_rng(4).normal(0, 0.5, (2, atm.max_layers))
+    for p in range(2):
+        dT[p, atm.n_layers[p]:] = 0.0
+    rts, tl = [], []
+    assert api.CRTM_Tangent_Linear(atm, sfc, types.SimpleNamespace(temperature=dT), None, geo, ci, rts, tl,
+                                   opt) == api.SUCCESS
+    seen_atm, seen_tl = h.seen[-1]
+    assert seen_atm.max_layers == ext.max_layers
+    for p in range(2):
+        n, m = int(info.n_added[p]), int(atm.n_layers[p])
+        assert (seen_tl.temperature[p, :n] == 0).all()
+        np.testing.assert_array_equal(seen_tl.temperature[p, n:n + m], dT[p, :m])
+    ks, r2 = [], []
+    assert api.CRTM_K_Matrix(atm, sfc, None, geo, ci, ks, r2, opt) == api.SUCCESS
+    lin = np.einsum("plk,pk->pl", ks[0].temperature, dT)
+    assert np.abs(tl[0] - lin).max() < 1e-5 * np.abs(lin).max()
