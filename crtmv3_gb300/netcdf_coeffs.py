@@ -1,0 +1,204 @@
+"""netCDF (classic format) SpcCoeff and ODPS TauCoeff files: readers, writers
+and the conversion to the binary files that crtm_gpu_init loads.
+
+The reference writes both with NF90_CREATE(..., NF90_CLOBBER), i.e. netCDF
+classic (src/Coefficients/SpcCoeff/SpcCoeff_netCDF_IO.f90:1501,
+src/Coefficients/TauCoeff/ODPS/ODPS_netCDF_IO.f90:1471).  Names, types and
+dimensions follow SpcCoeff_netCDF_IO.f90:68-183 and ODPS_netCDF_IO.f90:63-240.
+A Fortran variable dimensioned (a, b) is stored in netCDF as (b, a), so the
+2-D arrays are transposed on the way in and out.
+
+CRTM_Init's SpcCoeff_Format / TauCoeff_Format = 'netCDF'
+(src/CRTM_LifeCycle.f90) reads <Sensor_Id>.SpcCoeff.nc and
+<Sensor_Id>.TauCoeff.nc.  crtmv3_gb300.api.CRTM_Init does the same through
+``convert_sensor``: the files become binary files in a private directory,
+which the library then loads.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import numpy as np
+from scipy.io import netcdf_file
+
+from . import coefficients as co
+
+N_COMPONENTS_G = co.N_COMPONENTS_G
+N_ABSORBERS_G = co.N_ABSORBERS_G
+
+
+def _attr(f, name, default=None):
+    v = getattr(f, name, default)
+    if isinstance(v, bytes):
+        return v.decode().strip()
+    if isinstance(v, np.ndarray) and v.size == 1:
+        return v.item()
+    return v
+
+
+def _var(f, name, dtype=None):
+    if name not in f.variables:
+        raise ValueError(f"netCDF coefficient file: variable {name} missing")
+    a = np.array(f.variables[name].data)
+    return a if dtype is None else a.astype(dtype)
+
+
+# ---------------------------------------------------------------------------
+# SpcCoeff
+# ---------------------------------------------------------------------------
+
+def write_spccoeff_nc(path: str, sc: co.SpcCoeff) -> None:
+    """SpcCoeff_netCDF_IO's layout (:68-183): dimension n_Channels, scalar
+    Sensor_Type, per-channel variables, Sensor_Id and WMO ids as global
+    attributes."""
+    L = sc.n_channels
+    with netcdf_file(path, "w", version=1) as f:
+        f.Release = np.int32(co.SPCCOEFF_RELEASE)
+        f.Version = np.int32(1)
+        f.Sensor_Id = sc.sensor_id
+        f.WMO_Satellite_Id = np.int32(sc.wmo_satellite_id)
+        f.WMO_Sensor_Id = np.int32(sc.wmo_sensor_id)
+        f.createDimension("n_Channels", L)
+        v = f.createVariable("Sensor_Type", "i4", ())
+        v[...] = np.int32(sc.sensor_type)
+        cols = [("Sensor_Channel", "i4", sc.sensor_channel),
+                ("Polarization", "i4", sc.polarization if sc.polarization is not None else np.zeros(L)),
+                ("Polarization_Angle", "f8", sc.pol_angle if sc.pol_angle is not None else np.zeros(L)),
+                ("Channel_Flag", "i4", sc.channel_flag if sc.channel_flag is not None else np.zeros(L)),
+                ("Frequency", "f8", sc.frequency), ("Wavenumber", "f8", sc.wavenumber),
+                ("Planck_C1", "f8", sc.planck_c1), ("Planck_C2", "f8", sc.planck_c2),
+                ("Band_C1", "f8", sc.band_c1), ("Band_C2", "f8", sc.band_c2),
+                ("Cosmic_Background_Radiance", "f8", sc.cosmic_background_radiance),
+                ("Solar_Irradiance", "f8", sc.solar_irradiance)]
+        for name, t, data in cols:
+            v = f.createVariable(name, t, ("n_Channels",))
+            v[:] = np.asarray(data).astype(t)
+
+
+def read_spccoeff_nc(path: str) -> co.SpcCoeff:
+    with netcdf_file(path, "r", mmap=False) as f:
+        return co.SpcCoeff(
+            sensor_id=str(_attr(f, "Sensor_Id", "")),
+            sensor_type=int(f.variables["Sensor_Type"].data[()]),
+            sensor_channel=_var(f, "Sensor_Channel", np.int32),
+            frequency=_var(f, "Frequency", np.float64), wavenumber=_var(f, "Wavenumber", np.float64),
+            planck_c1=_var(f, "Planck_C1", np.float64), planck_c2=_var(f, "Planck_C2", np.float64),
+            band_c1=_var(f, "Band_C1", np.float64), band_c2=_var(f, "Band_C2", np.float64),
+            cosmic_background_radiance=_var(f, "Cosmic_Background_Radiance", np.float64),
+            solar_irradiance=_var(f, "Solar_Irradiance", np.float64),
+            polarization=_var(f, "Polarization", np.int32),
+            pol_angle=_var(f, "Polarization_Angle", np.float64),
+            channel_flag=_var(f, "Channel_Flag", np.int32),
+            wmo_satellite_id=int(_attr(f, "WMO_Satellite_Id", 1023)),
+            wmo_sensor_id=int(_attr(f, "WMO_Sensor_Id", 2047)))
+
+
+# ---------------------------------------------------------------------------
+# ODPS TauCoeff
+# ---------------------------------------------------------------------------
+
+def write_odps_nc(path: str, tc: co.ODPSCoeff) -> None:
+    """ODPS_netCDF_IO's layout (:63-240) without the OPTRAN part
+    (n_OCoeffs = 0)."""
+    J, Jm, K, L = tc.n_components, tc.n_absorbers, tc.n_layers, int(tc.sensor_channel.shape[0])
+    with netcdf_file(path, "w", version=1) as f:
+        f.Release = np.int32(co.ODPS_RELEASE)
+        f.Version = np.int32(1)
+        f.Sensor_Id = tc.sensor_id
+        f.Algorithm = np.int32(2)
+        f.WMO_Satellite_Id = np.int32(tc.wmo_satellite_id)
+        f.WMO_Sensor_Id = np.int32(tc.wmo_sensor_id)
+        f.createDimension("n_Layers", K)
+        f.createDimension("n_Levels", K + 1)
+        f.createDimension("n_Components", J)
+        f.createDimension("n_Absorbers", Jm)
+        f.createDimension("n_Channels", L)
+        f.createDimension("n_Coeffs", max(int(tc.c.shape[0]), 1))
+        for name, val in (("Group_Index", tc.group_index), ("Sensor_Type", tc.sensor_type)):
+            v = f.createVariable(name, "i4", ())
+            v[...] = np.int32(val)
+        spec = [("Ref_Level_Pressure", "f8", ("n_Levels",), tc.ref_level_pressure),
+                ("Ref_Pressure", "f8", ("n_Layers",), tc.ref_pressure),
+                ("Ref_Temperature", "f8", ("n_Layers",), tc.ref_temperature),
+                ("Ref_Absorber", "f8", ("n_Absorbers", "n_Layers"), np.asarray(tc.ref_absorber).T),
+                ("Min_Absorber", "f8", ("n_Absorbers", "n_Layers"), np.asarray(tc.min_absorber).T),
+                ("Max_Absorber", "f8", ("n_Absorbers", "n_Layers"), np.asarray(tc.max_absorber).T),
+                ("Sensor_Channel", "i4", ("n_Channels",), tc.sensor_channel),
+                ("Component_ID", "i4", ("n_Components",), tc.component_id),
+                ("Absorber_ID", "i4", ("n_Absorbers",), tc.absorber_id),
+                ("n_Predictors", "i4", ("n_Channels", "n_Components"), np.asarray(tc.n_predictors).T),
+                ("Pos_Index", "i4", ("n_Channels", "n_Components"), np.asarray(tc.pos_index).T),
+                ("ODPS_Coefficients", "f4", ("n_Coeffs",),
+                 tc.c if tc.c.shape[0] else np.zeros(1, np.float32))]
+        for name, t, dims, data in spec:
+            v = f.createVariable(name, t, dims)
+            v[:] = np.asarray(data).astype(t)
+
+
+def read_odps_nc(path: str) -> co.ODPSCoeff:
+    with netcdf_file(path, "r", mmap=False) as f:
+        if "n_OCoeffs" in f.dimensions and int(f.dimensions["n_OCoeffs"] or 0) > 0:
+            raise ValueError(f"{path}: ODPS file with OPTRAN water-vapour-line coefficients (n_OCoeffs > 0) "
+                             f"is not supported")
+        group = int(f.variables["Group_Index"].data[()])
+        if group not in N_COMPONENTS_G:
+            raise ValueError(f"{path}: unknown ODPS group index {group}")
+        n_pred = _var(f, "n_Predictors", np.int32).T.copy()
+        pos = _var(f, "Pos_Index", np.int32).T.copy()
+        # a file without coefficients still has a one-element placeholder
+        c = _var(f, "ODPS_Coefficients", np.float32) if n_pred.sum() > 0 else np.zeros(0, np.float32)
+        if n_pred.shape[0] != N_COMPONENTS_G[group]:
+            raise ValueError(f"{path}: {n_pred.shape[0]} components for group {group}")
+        return co.ODPSCoeff(
+            group_index=group, sensor_id=str(_attr(f, "Sensor_Id", "")),
+            sensor_type=int(f.variables["Sensor_Type"].data[()]),
+            sensor_channel=_var(f, "Sensor_Channel", np.int32),
+            ref_level_pressure=_var(f, "Ref_Level_Pressure", np.float64),
+            ref_pressure=_var(f, "Ref_Pressure", np.float64),
+            ref_temperature=_var(f, "Ref_Temperature", np.float64),
+            ref_absorber=_var(f, "Ref_Absorber", np.float64).T.copy(),
+            min_absorber=_var(f, "Min_Absorber", np.float64).T.copy(),
+            max_absorber=_var(f, "Max_Absorber", np.float64).T.copy(),
+            n_predictors=n_pred, pos_index=pos, c=c,
+            wmo_satellite_id=int(_attr(f, "WMO_Satellite_Id", 1023)),
+            wmo_sensor_id=int(_attr(f, "WMO_Sensor_Id", 2047)))
+
+
+# ---------------------------------------------------------------------------
+# conversion for CRTM_Init
+# ---------------------------------------------------------------------------
+
+def convert_sensor(src_dir: str, sensor_id: str, out_dir: str, spc_format: str = "Binary",
+                   tau_format: str = "Binary") -> None:
+    """Put <sensor_id>.SpcCoeff.bin and .TauCoeff.bin into out_dir: converted
+    from the .nc files of src_dir for the formats given as 'netCDF', linked
+    to src_dir's binary files otherwise."""
+    for kind, fmt, read, write in (("SpcCoeff", spc_format, read_spccoeff_nc, co.write_spccoeff),
+                                   ("TauCoeff", tau_format, read_odps_nc, co.write_odps)):
+        dst = os.path.join(out_dir, f"{sensor_id}.{kind}.bin")
+        if fmt.lower() == "netcdf":
+            write(dst, read(os.path.join(src_dir, f"{sensor_id}.{kind}.nc")))
+        elif fmt.lower() == "binary":
+            _link(os.path.join(src_dir, f"{sensor_id}.{kind}.bin"), dst)
+        else:
+            raise ValueError(f"{kind}_Format must be 'Binary' or 'netCDF' (got {fmt!r})")
+
+
+def link_shared_files(src_dir: str, out_dir: str,
+                      names=("CloudCoeff.bin", "AerosolCoeff.bin", "AerosolCoeff.CMAQ.bin",
+                             "AerosolCoeff.GOCART-GEOS5.bin", "AerosolCoeff.NAAPS.bin",
+                             "Nalli.IRwater.EmisCoeff.bin"), extra=()) -> None:
+    """The coefficient files shared by all sensors, as src_dir has them."""
+    for n in tuple(names) + tuple(extra):
+        p = os.path.join(src_dir, n)
+        if os.path.exists(p):
+            _link(p, os.path.join(out_dir, n))
+
+
+def _link(src: str, dst: str) -> None:
+    if not os.path.exists(src):
+        raise FileNotFoundError(src)
+    try:
+        os.symlink(os.path.abspath(src), dst)
+    except OSError:
+        shutil.copyfile(src, dst)
