@@ -527,20 +527,27 @@ class ChannelInfo:
 def CRTM_Init(sensor_ids: Sequence[str], channel_info: List[ChannelInfo], file_path: str = ".",
               precision: int = FP64, aerosol_model: Optional[str] = None,
               aerosolcoeff_file: Optional[str] = None, spccoeff_format: str = "Binary",
-              taucoeff_format: str = "Binary") -> int:
+              taucoeff_format: str = "Binary", irwatercoeff_format: str = "Binary") -> int:
     """CRTM_Init: load the coefficients of ``sensor_ids`` and fill ``channel_info``
     (Aerosol_Model, AerosolCoeff_File, SpcCoeff_Format and TauCoeff_Format as
-    the reference's optional arguments, src/CRTM_LifeCycle.f90:523-561).  With
-    a format 'netCDF' the sensors' <id>.SpcCoeff.nc / <id>.TauCoeff.nc files
+    the reference's optional arguments, src/CRTM_LifeCycle.f90:523-561, and
+    IRwaterCoeff_Format).  With a format 'netCDF' the sensors'
+    <id>.SpcCoeff.nc / <id>.TauCoeff.nc files (and Nalli.IRwater.EmisCoeff.nc)
     are converted to binary files in a private directory, which is loaded."""
     path = file_path
     try:
-        if spccoeff_format.lower() != "binary" or taucoeff_format.lower() != "binary":
+        fmts = (spccoeff_format, taucoeff_format, irwatercoeff_format)
+        for fm in fmts:
+            if fm.lower() not in ("binary", "netcdf"):
+                raise ValueError(f"coefficient format must be 'Binary' or 'netCDF' (got {fm!r})")
+        if any(fm.lower() == "netcdf" for fm in fmts):
             import tempfile
             from . import netcdf_coeffs
             path = tempfile.mkdtemp(prefix="crtm_coeffs_")
             for s in sensor_ids:
                 netcdf_coeffs.convert_sensor(file_path, s, path, spccoeff_format, taucoeff_format)
+            if irwatercoeff_format.lower() == "netcdf":
+                netcdf_coeffs.convert_irwater(file_path, path)
             netcdf_coeffs.link_shared_files(file_path, path, extra=(aerosolcoeff_file,) if aerosolcoeff_file else ())
     except (OSError, ValueError, KeyError) as e:
         print(f"CRTM_Init(FAILURE): {e}")

@@ -165,6 +165,42 @@ def read_odps_nc(path: str) -> co.ODPSCoeff:
 
 
 # ---------------------------------------------------------------------------
+# IRwaterCoeff (IR sea-surface emissivity table)
+# ---------------------------------------------------------------------------
+
+IRWATER_FILE = "Nalli.IRwater.EmisCoeff"
+
+
+def write_irwater_nc(path: str, wc: co.IRwaterCoeff) -> None:
+    """IRwaterCoeff_netCDF_IO's layout (src/Coefficients/EmisCoeff/IR_Water/
+    IRwaterCoeff_netCDF_IO.f90:62-121, :1262-1338): the four axes and
+    Emissivity(n_Angles, n_Frequencies, n_Wind_Speeds, n_Temperature),
+    stored as (n_Temperature, n_Wind_Speeds, n_Frequencies, n_Angles)."""
+    with netcdf_file(path, "w", version=1) as f:
+        f.Release = np.int32(1)
+        f.Version = np.int32(wc.version)
+        f.Classification_Name = wc.classification
+        for dim, name, data in (("n_Angles", "Angle", wc.angle), ("n_Frequencies", "Frequency", wc.frequency),
+                                ("n_Wind_Speeds", "Wind_Speed", wc.wind_speed),
+                                ("n_Temperature", "Temperature", wc.temperature)):
+            f.createDimension(dim, int(np.asarray(data).shape[0]))
+            v = f.createVariable(name, "f8", (dim,))
+            v[:] = np.asarray(data, np.float64)
+        v = f.createVariable("Emissivity", "f8", ("n_Temperature", "n_Wind_Speeds", "n_Frequencies", "n_Angles"))
+        v[:] = np.asarray(wc.emissivity, np.float64).transpose(3, 2, 1, 0)
+
+
+def read_irwater_nc(path: str) -> co.IRwaterCoeff:
+    with netcdf_file(path, "r", mmap=False) as f:
+        return co.IRwaterCoeff(
+            classification=str(_attr(f, "Classification_Name", "")),
+            angle=_var(f, "Angle", np.float64), frequency=_var(f, "Frequency", np.float64),
+            wind_speed=_var(f, "Wind_Speed", np.float64), temperature=_var(f, "Temperature", np.float64),
+            emissivity=np.ascontiguousarray(_var(f, "Emissivity", np.float64).transpose(3, 2, 1, 0)),
+            version=int(_attr(f, "Version", 2)))
+
+
+# ---------------------------------------------------------------------------
 # conversion for CRTM_Init
 # ---------------------------------------------------------------------------
 
@@ -184,6 +220,12 @@ def convert_sensor(src_dir: str, sensor_id: str, out_dir: str, spc_format: str =
             raise ValueError(f"{kind}_Format must be 'Binary' or 'netCDF' (got {fmt!r})")
 
 
+def convert_irwater(src_dir: str, out_dir: str) -> None:
+    """Nalli.IRwater.EmisCoeff.nc of src_dir as the binary file in out_dir."""
+    co.write_irwatercoeff(os.path.join(out_dir, IRWATER_FILE + ".bin"),
+                          read_irwater_nc(os.path.join(src_dir, IRWATER_FILE + ".nc")))
+
+
 def link_shared_files(src_dir: str, out_dir: str,
                       names=("CloudCoeff.bin", "AerosolCoeff.bin", "AerosolCoeff.CMAQ.bin",
                              "AerosolCoeff.GOCART-GEOS5.bin", "AerosolCoeff.NAAPS.bin",
@@ -191,7 +233,7 @@ def link_shared_files(src_dir: str, out_dir: str,
     """The coefficient files shared by all sensors, as src_dir has them."""
     for n in tuple(names) + tuple(extra):
         p = os.path.join(src_dir, n)
-        if os.path.exists(p):
+        if os.path.exists(p) and not os.path.exists(os.path.join(out_dir, n)):
             _link(p, os.path.join(out_dir, n))
 
 

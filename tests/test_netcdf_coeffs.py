@@ -105,3 +105,29 @@ def test_crtm_init_formats(coeff_dir, tmp_path, monkeypatch):
     # a missing file or an unknown format fails the call
     assert api.CRTM_Init([sensor], ci, str(src), spccoeff_format="netCDF") == api.FAILURE
     assert api.CRTM_Init([sensor], ci, str(src), taucoeff_format="HDF") == api.FAILURE
+
+
+def test_irwater_round_trip_and_init(coeff_dir, tmp_path, monkeypatch):
+    from crtmv3_gb300 import synthetic as sy2
+    binp = sy2.write_irwater_file(str(tmp_path))
+    wc = co.read_irwatercoeff(binp)
+    src = tmp_path / "src"
+    src.mkdir()
+    nc.write_irwater_nc(str(src / (nc.IRWATER_FILE + ".nc")), wc)
+    with netcdf_file(str(src / (nc.IRWATER_FILE + ".nc")), "r", mmap=False) as f:
+        assert f.variables["Emissivity"].dimensions == ("n_Temperature", "n_Wind_Speeds", "n_Frequencies",
+                                                         "n_Angles")
+    _fields_equal(nc.read_irwater_nc(str(src / (nc.IRWATER_FILE + ".nc"))), wc)
+    sensor = "irsynth_c616"
+    for kind in ("TauCoeff", "SpcCoeff"):
+        os.symlink(os.path.join(coeff_dir, f"{sensor}.{kind}.bin"), str(src / f"{sensor}.{kind}.bin"))
+    seen = {}
+
+    class FakeCRTM:
+        def __init__(self, ids, path, *a):
+            seen["path"] = path
+            self.n_channels = [616]
+
+    monkeypatch.setattr(api, "CRTM", FakeCRTM)
+    assert api.CRTM_Init([sensor], [], str(src), irwatercoeff_format="netCDF") == api.SUCCESS
+    assert filecmp.cmp(os.path.join(seen["path"], nc.IRWATER_FILE + ".bin"), binp, shallow=False)
