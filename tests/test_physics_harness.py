@@ -36,8 +36,24 @@ def _ptr(a):
     return a.ctypes.data_as(ct.c_void_p)
 
 
-@pytest.mark.parametrize("sensor,nl", [("mwsynth_c22", 100), ("irsynth_c616", 101), ("mwsynth_c16", 77)])
-def test_prep_matches_oracle(hx, coeff_dir, sensor, nl):
+def _extended(atm, cut):
+    """The batch without its top `cut` layers, extended again by AddLayers."""
+    import dataclasses
+    from crtmv3_gb300 import addlayers as al
+    m = atm.n_layers - cut
+    cutb = dataclasses.replace(
+        atm, n_layers=m.astype(np.int32), level_pressure=np.ascontiguousarray(atm.level_pressure[:, cut:]),
+        pressure=np.ascontiguousarray(atm.pressure[:, cut:]), temperature=np.ascontiguousarray(atm.temperature[:, cut:]),
+        absorber=np.ascontiguousarray(atm.absorber[:, :, cut:]))
+    ext, info = al.add_layers(cutb)
+    assert info.any
+    return ext
+
+
+@pytest.mark.parametrize("sensor,nl,cut", [("mwsynth_c22", 100, 0), ("irsynth_c616", 101, 0), ("mwsynth_c16", 77, 0),
+                                           # profile tops below 0.005 hPa, extended by AddLayers
+                                           ("irsynth_c616", 101, 9), ("mwsynth_c22", 100, 25)])
+def test_prep_matches_oracle(hx, coeff_dir, sensor, nl, cut):
     from oracle import pyoracle as po
     o = po.Oracle(coeff_dir, sensor)
     tc = co.read_odps(f"{coeff_dir}/{sensor}.TauCoeff.bin")
@@ -45,6 +61,8 @@ def test_prep_matches_oracle(hx, coeff_dir, sensor, nl):
     NS = {1: 89, 2: 50, 3: 21}[G]
     nnz = hx.hx_nnz(G)
     atm, sfc, geo, opt = sy.clear_sky_workload(sensor, 2, nl, 40)
+    if cut:
+        atm = _extended(atm, cut)
     b, keep = o._batch(atm, sfc, geo, opt)
     L = po.lib()
     L.or_profile_state.argtypes = [ct.c_void_p, ct.POINTER(po.OrBatch), ct.c_int] + [po._dp] * 4
