@@ -134,23 +134,52 @@ def k_outputs(torch, P, L, K, JK, dev):
                 status=torch.empty((P,), dtype=torch.int32, device=dev))
 
 
+def jacobian_sel(atm):
+    """User absorber indices of the H2O and O3 Jacobians that the K-matrix returns."""
+    ids = list(atm.absorber_id)
+    return [ids.index(1), ids.index(3)]
+
+
 def cpu_baseline(P_sample: int, threads: int, min_seconds: float = 10.0):
     """FP64 oracle (restatement of the reference's CPU path) on the host cores:
-    K-matrix calls on batches of ``P_sample`` profiles of the workload, repeated
-    until at least ``min_seconds`` of CPU work; returns (p*c/s, seconds, calls)."""
+    K-matrix calls on batches of ``P_sample`` profiles of the workload with the
+    same two absorber Jacobians as the GPU arm, repeated until at least
+    ``min_seconds`` of CPU work; returns (p*c/s, seconds, calls, sample, oracle
+    outputs of the sample)."""
     from oracle.pyoracle import Oracle
     atm, sfc, geo, opt = make_workload(P_sample, 2024)
+    sel = jacobian_sel(atm)
     o = Oracle(COEFF_DIR, SENSOR)
     w = slice(0, min(2, P_sample))
-    o.k_matrix(atm.subset(w), sfc.subset(w), geo.subset(w), opt.subset(w), n_threads=threads)
+    o.k_matrix(atm.subset(w), sfc.subset(w), geo.subset(w), opt.subset(w), n_threads=threads, k_absorbers=sel)
     calls, t0 = 0, time.perf_counter()
     while True:
-        o.k_matrix(atm, sfc, geo, opt, n_threads=threads)
+        ref = o.k_matrix(atm, sfc, geo, opt, n_threads=threads, k_absorbers=sel)
         calls += 1
         dt = time.perf_counter() - t0
         if dt >= min_seconds:
             break
-    return calls * P_sample * o.n_channels / dt, dt, calls
+    return calls * P_sample * o.n_channels / dt, dt, calls, (atm, sfc, geo, opt), ref
+
+
+def oracle_errors(h, sample, ref, prec):
+    """Errors of one GPU form against the FP64 oracle on the CPU-baseline
+    sample: max |dBT| (K) and, per Jacobian output, max |dK| / max |K_oracle|."""
+    atm, sfc, geo, opt = sample
+    sel = jacobian_sel(atm)
+    h.set_precision(prec)
+    km, rts = h.k_matrix(atm, sfc, geo, opt, k_absorbers=sel)
+
+    def rel(x, y):
+        return float(np.abs(x - y).max() / max(np.abs(y).max(), 1e-300))
+    return {"max_abs_bt_K": float(np.abs(rts.brightness_temperature - ref["bt"]).max()),
+            "max_rel_jacobian": {
+                "temperature": rel(km.temperature, ref["temperature_k"]),
+                "h2o": rel(km.absorber[:, :, 0], ref["absorber_k"][:, :, sel[0]]),
+                "o3": rel(km.absorber[:, :, 1], ref["absorber_k"][:, :, sel[1]]),
+                "water_temperature": rel(km.water_temperature, ref["water_temperature_k"]),
+                "surface_emissivity": rel(km.surface_emissivity, ref["surface_emissivity_k"])},
+            "profiles": int(atm.n_profiles)}
 
 
 def workload_config(P: int, world: int) -> dict:
@@ -172,7 +201,7 @@ def run_reference(args):
     for _ in range(args.warmup):
         cpu_baseline(max(threads // 2, 1), threads, min_seconds=0.0)
     for _ in range(args.steps):
-        v, dt, calls = cpu_baseline(P_sample, threads, min_seconds=0.0)
+        v, dt, calls, _, _ = cpu_baseline(P_sample, threads, min_seconds=0.0)
         vals.append((v, dt))
     value = statistics.median(v for v, _ in vals)
     ms = statistics.median(dt for _, dt in vals) * 1e3
@@ -183,7 +212,8 @@ def run_reference(args):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{P_sample} profiles x 2211 channels K-matrix per step "
+                             "sample": f"{P_sample} profiles x 2211 channels K-matrix per step, "
+                                       f"H2O and O3 Jacobians as the GPU arm "
                                        f"(FP64 C oracle, OpenMP over profiles)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -479,8 +509,7 @@ def main():
 
     P, K, L = args.profiles, N_LAYERS, 2211
     atm, sfc, geo, opt = make_workload(P, 3000 + rank)
-    ids = list(atm.absorber_id)
-    sel = [ids.index(1), ids.index(3)]     # H2O, O3 Jacobians
+    sel = jacobian_sel(atm)     # H2O, O3 Jacobians
     JK = len(sel)
     h = api.CRTM([SENSOR], COEFF_DIR, api.FP64)
     b, keep, dev_in = device_batch(torch, h, atm, sfc, geo, opt, dev)
@@ -614,13 +643,16 @@ def main():
                "d2h_copy_gbs": d2h_gbs, "d2h_bound_ms": d2h / d2h_gbs / 1e6}
 
     cpu = None
+    vs_oracle = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, dt, calls = cpu_baseline(args.cpu_profiles, threads)
+        v, dt, calls, sample, ref = cpu_baseline(args.cpu_profiles, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{calls} K-matrix calls of {args.cpu_profiles} profiles x 2211 channels x "
-                         f"{N_LAYERS} layers (all absorber Jacobians), FP64 C oracle with OpenMP "
-                         f"over profiles, {dt:.1f} s"}
+                         f"{N_LAYERS} layers (H2O and O3 Jacobians, as the GPU arm), FP64 C oracle "
+                         f"with OpenMP over profiles, {dt:.1f} s"}
+        # both GPU forms against the oracle on the same sample (untimed)
+        vs_oracle = {"mixed": oracle_errors(h, sample, ref, 1), "fp64": oracle_errors(h, sample, ref, 0)}
 
     if rank == 0:
         line = {
@@ -632,6 +664,7 @@ def main():
             "fp64_gpu": {"value": fp64_value, "ms_per_step": per_fp64, "steps": fp64_steps},
             "speedup_mixed_vs_fp64": value / fp64_value,
             "accuracy_mixed_vs_fp64": {"max_abs_bt_K": bt_err, "max_rel_jacobian": jac_err},
+            "accuracy_vs_oracle": vs_oracle,
             "stages_ms_per_step": stage_ms, "stage_launches_per_step": stage_launch,
             "kernels": kernels, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(launches_mixed * args.steps),

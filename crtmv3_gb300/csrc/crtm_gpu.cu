@@ -29,8 +29,11 @@
 using namespace crtm;
 
 // Scratch of crtm_gpu_k_matrix_device_static: one fixed block per device,
-// reserved when the module loads, so that the call itself allocates nothing.
-// 128 MiB holds the intermediates of at least one profile for up to ~8500
+// reserved when this library's device code is loaded on that device, so that
+// the call itself allocates nothing.  With CUDA's lazy module loading (the
+// default) that load happens on the module's first use on the device:
+// crtm_gpu_init takes the block's address there (static_scratch_slot), which
+// loads it, so a later static call never triggers the load.  128 MiB holds the intermediates of at least one profile for up to ~8500
 // channels at 200 layers with 8 absorber Jacobians in FP64; larger batches
 // are processed in chunks that fit.
 static constexpr size_t STATIC_SCRATCH_BYTES = (size_t)CRTM_GPU_STATIC_SCRATCH_MIB << 20;
@@ -48,6 +51,14 @@ struct StaticScratchSlot {
   cudaError_t err = cudaSuccess;
 };
 StaticScratchSlot g_static_slots[MAX_STATIC_DEVICES];
+
+// The slot of device dev (current), its address looked up on first use.
+StaticScratchSlot* static_scratch_slot(int dev) {
+  if (dev < 0 || dev >= MAX_STATIC_DEVICES) return nullptr;
+  StaticScratchSlot& slot = g_static_slots[dev];
+  std::call_once(slot.once, [&slot] { slot.err = cudaGetSymbolAddress(&slot.ptr, g_static_scratch); });
+  return &slot;
+}
 
 // ---------------------------------------------------------------------------
 // Fortran sequential record files
@@ -1019,10 +1030,17 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
           {
             StageScope sc(h, 8, st);
             if (nz_max)
-              launch_scatter_contract<SC_NZ_MAX, double>(sa, gl, st);
+              launch_scatter_reverse<SC_NZ_MAX, double>(sa, gl, st);
             else
-              launch_scatter_contract<5, double>(sa, gl, st);
+              launch_scatter_reverse<5, double>(sa, gl, st);
             CK_LAUNCH(h);
+            if (soi) {   // the SOI profiles' layers
+              if (nz_max)
+                launch_scatter_contract<SC_NZ_MAX, double>(sa, gl, st);
+              else
+                launch_scatter_contract<5, double>(sa, gl, st);
+              CK_LAUNCH(h);
+            }
           }
         } else {
           return fail(h, "internal: scattering K-matrix with FP32 gas optics");
@@ -1200,13 +1218,31 @@ int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, c
       return fail(h, "no emissivity given: the IR water emissivity model is built for clear-sky batches; "
                      "supply Options%%Emissivity for batches with clouds or aerosols");
   }
-  order_after_previous(h, st);
   crtm_gpu_batch bm;
   SfcModel sm{};
+  FixedScratch fixed_rest{};
+  double* E = nullptr;
+  if (model) {
+    const size_t PL = (size_t)b->n_profiles * s.L, eb = 3 * PL * sizeof(double);
+    if (fixed) {
+      // a call that may not allocate takes the model's e, de/dv and de/dT
+      // from the front of its fixed scratch and runs the pipeline on the rest
+      const size_t take = (eb + 255) & ~(size_t)255;
+      if (take >= fixed->bytes)
+        return fail(h, "the emissivity model's %zu bytes (%d profiles x %d channels) do not fit the static "
+                       "scratch of %zu bytes: pass an emissivity or fewer profiles per call",
+                    eb, b->n_profiles, s.L, fixed->bytes);
+      E = (double*)fixed->base;
+      fixed_rest = FixedScratch{fixed->base + take, fixed->bytes - take};
+      fixed = &fixed_rest;
+    } else {
+      if (!h->sfc.ensure(eb)) return fail(h, "cannot allocate the emissivity model's buffers");
+      E = (double*)h->sfc.p;
+    }
+  }
+  order_after_previous(h, st);
   if (model) {
     const size_t PL = (size_t)b->n_profiles * s.L;
-    if (!h->sfc.ensure(3 * PL * sizeof(double))) return fail(h, "cannot allocate the emissivity model's buffers");
-    double* E = (double*)h->sfc.p;
     if (cudaMemsetAsync(h->d_error, 0, sizeof(int), st) != cudaSuccess) return fail(h, "error flag reset failed");
     irwater_kernel<<<(unsigned)((PL + 255) / 256), 256, 0, st>>>(h->irw, b->n_profiles, s.L, s.spec.wn,
                                                                  b->sensor_zenith_angle, b->water_temperature,
@@ -1666,6 +1702,8 @@ int crtm_gpu_init_aerosol(const char* coeff_path, int n_sensors, const char* con
     delete h;
     return fail(nullptr, "cudaStreamCreate failed");
   }
+  // load the device code (and with it the static scratch) on this device now
+  static_scratch_slot(dev);
   h->sensors.resize(n_sensors);
   for (int i = 0; i < n_sensors; i++) {
     std::string err;
@@ -1875,10 +1913,13 @@ int crtm_gpu_adjoint_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch*
 // operator every iteration on a few profiles, where cudaMalloc and cudaFree
 // would synchronise the whole device and stall its other streams.
 //
-// The first call on a device looks up the scratch address with that device
-// current (cudaGetSymbolAddress); make that first call before any stream
-// capture begins.  Later calls only enqueue kernels and one small copy of
-// the absorber map.  No part of the scratch is read before the same call's
+// crtm_gpu_init looks up the scratch address on its device with that device
+// current (cudaGetSymbolAddress); if that lookup has not happened on the
+// handle's device, the first call here does it, and that first call should
+// come before any stream capture.  Calls only enqueue kernels and one small
+// copy of the absorber map.  Without a batch emissivity the IR sea-surface
+// emissivity model's three [P][L] arrays are taken from the front of the
+// scratch as well.  No part of the scratch is read before the same call's
 // kernels write it, so nothing needs clearing between calls.  The scratch is
 // shared by every handle on the device: two calls that overlap in time (on
 // different streams, handles or host threads) overwrite each other's
@@ -1890,11 +1931,10 @@ int crtm_gpu_k_matrix_device_static(crtm_gpu_handle h, int sensor, const crtm_gp
   if (h->device < 0 || h->device >= MAX_STATIC_DEVICES)
     return fail(h, "device %d has no static scratch slot", h->device);
   if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
-  StaticScratchSlot& slot = g_static_slots[h->device];
-  std::call_once(slot.once, [&slot] { slot.err = cudaGetSymbolAddress(&slot.ptr, g_static_scratch); });
-  if (slot.err != cudaSuccess || !slot.ptr)
-    return fail(h, "static scratch lookup failed: %s", cudaGetErrorString(slot.err));
-  const FixedScratch fx{(char*)slot.ptr, STATIC_SCRATCH_BYTES};
+  const StaticScratchSlot* slot = static_scratch_slot(h->device);
+  if (slot->err != cudaSuccess || !slot->ptr)
+    return fail(h, "static scratch lookup failed: %s", cudaGetErrorString(slot->err));
+  const FixedScratch fx{(char*)slot->ptr, STATIC_SCRATCH_BYTES};
   return dispatch(h, sensor, b, 1, bt_k, rts, k, nullptr,
                   (cudaStream_t)stream, nullptr, &fx);
 }

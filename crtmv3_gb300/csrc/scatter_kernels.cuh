@@ -44,7 +44,7 @@
 #pragma once
 
 #include "odps_kernels.cuh"
-#include "scatter_physics.cuh"
+#include "scatter_adjoint.cuh"
 
 namespace crtm {
 
@@ -523,6 +523,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_contract_kernel(Scatt
   if (a.pv.status[p] != 0 || k >= a.b.n_layers[gp]) return;
   const CloudyColumn c = column_inputs(a, p, gp, l);
   if (c.n_clouds == 0 && c.n_aerosols == 0) return;
+  if (!c.soi) return;   // ADA profiles: scatter_reverse_kernel
   const size_t kl = ((size_t)p * Kmax + k) * L + l;
   auto slot = [&](int s) { return s < c.n_clouds ? s : a.max_clouds + (s - c.n_clouds); };
   if (a.n_slots > 0)
@@ -592,6 +593,78 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_contract_kernel(Scatt
       layer_contract<NZ, 4, C>(c, a.lut, S, k, gas, d, T_b, R_b, src_b, od_b, B_b, g);
       for (int i = 0; i < m; i++)
         a.CV[((size_t)p * a.n_slots + slot(av[i0 + i])) * Kmax * L + (size_t)k * L + l] = g[i];
+    }
+  }
+}
+
+// The same contraction for the ADA profiles (and the clear layers of any
+// profile not on SOI), one thread per (profile, layer, channel), by the
+// reverse sweep through the layer's optics (layer_adjoint): all of the
+// layer's inputs in one pass, in the arithmetic C.
+template <int NZ, class R, class C>
+__global__ void __launch_bounds__(SCATTER_THREADS) scatter_reverse_kernel(ScatterArgs<R> a) {
+  constexpr int NE = layer_record<NZ>();
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int L = a.L, Kmax = a.Kmax;
+  if (idx >= (long long)a.n_chunk * Kmax * L) return;
+  const int l = (int)(idx % L);
+  const int k = (int)((idx / L) % Kmax);
+  const int p = (int)(idx / ((long long)L * Kmax));
+  const int gp = a.p_begin + p;
+  if (a.pv.status[p] != 0 || k >= a.b.n_layers[gp]) return;
+  const CloudyColumn c = column_inputs(a, p, gp, l);
+  if (c.n_clouds == 0 && c.n_aerosols == 0) return;
+  if (c.soi) return;    // SOI profiles: scatter_contract_kernel
+  const size_t kl = ((size_t)p * Kmax + k) * L + l;
+  auto slot = [&](int s) { return s < c.n_clouds ? s : a.max_clouds + (s - c.n_clouds); };
+  auto jac = [&](double* X, int s) -> double& {
+    return X[((size_t)p * a.n_slots + s) * Kmax * L + (size_t)k * L + l];
+  };
+  if (a.n_slots > 0)
+    for (int s = 0; s < a.n_slots; s++) {
+      jac(a.CJ, s) = 0.0;
+      jac(a.CR, s) = 0.0;
+      if (a.CV) jac(a.CV, s) = 0.0;
+    }
+  const double* rb = a.LBA + ((size_t)p * Kmax + k) * NE * L + l;
+  const int kind = (int)rb[0];
+  if (kind < 0) {
+    a.TODc[kl] = R(0);
+    a.PT[kl] = R(0);
+    return;
+  }
+  StreamSet<NZ, double> S;
+  if (stream_set<NZ, double>(c.nleg, c.mu_sensor, c.n_clouds > 0 ? a.lut.nleg : -1, c_gauss, S)) return;
+  const int nZ = S.nZ;
+  Mat<NZ, double> T_b, R_b;
+  double src_b[NZ];
+  const double od_b = rb[(size_t)L], B_b = kind == 1 ? 0.0 : rb[2 * (size_t)L];
+  if (kind == 1)
+    for (int i = 0; i < nZ; i++) {
+      for (int j = 0; j < nZ; j++) {
+        T_b.a[i][j] = rb[(size_t)(2 + i * NZ + j) * L];
+        R_b.a[i][j] = rb[(size_t)(2 + NZ * NZ + i * NZ + j) * L];
+      }
+      src_b[i] = rb[(size_t)(2 + 2 * NZ * NZ + i) * L];
+    }
+  double g[2], gs[2 * SC_NC_MAX][3];
+  const int kr = layer_adjoint<NZ, C>(c, a.lut, S, k, double(a.TAU[kl]), kind, T_b, R_b, src_b,
+                                      kind == 1 ? 0.0 : od_b, B_b, g, gs);
+  if (kr < 0) {
+    atomicCAS(a.error, 0, -kr);
+    if (a.status) atomicOr(a.status + gp, 1 << 4);
+    a.TODc[kl] = R(0);
+    a.PT[kl] = R(0);
+    return;
+  }
+  a.TODc[kl] = R(g[0]);
+  a.PT[kl] = R(g[1]);
+  if (a.n_slots > 0) {
+    const int nsp = c.n_clouds + (c.microwave ? 0 : c.n_aerosols);
+    for (int s = 0; s < nsp; s++) {
+      jac(a.CJ, slot(s)) = gs[s][0];
+      jac(a.CR, slot(s)) = gs[s][1];
+      if (a.CV && a.alut.scheme == AEROSOL_CMAQ && s >= c.n_clouds) jac(a.CV, slot(s)) = gs[s][2];
     }
   }
 }

@@ -397,6 +397,98 @@ CRTM_HD void jacobi(int n, Mat<NZ, Dual<N, Q>>& S, Dual<N, Q>* lam, Mat<NZ, Dual
   }
 }
 
+// Eigenpairs of MOM's HH = (PP - PM)(PP + PM) for a layer of scaled albedo s
+// (CRTM_AMOM_layer / MOM, ADA_Module.f90:262-354 and :552-743): the
+// eigenvectors in the columns of E, the eigenvalues in lam.  The quadrature
+// block is solved in its symmetric form, the sensor angle's eigenpair from
+// the block-triangular structure.  On return X = PP - PM and Y = PP + PM over
+// all nZ angles; V and W are scratch.  Returns false on a failed
+// factorisation.  gap: see ada_layer.
+template <int NZ, class T>
+CRTM_HD bool mom_eigen(int nS, int nZ, T s, const T* mu, const T* wt, const Mat<NZ, T>& ff, const Mat<NZ, T>& bb,
+                       Mat<NZ, T>& E, T* lam, Mat<NZ, T>& X, Mat<NZ, T>& Y, Mat<NZ, T>& V, Mat<NZ, T>& W,
+                       double* gap) {
+  // symmetric form of the quadrature block
+  T sq[NZ];
+  for (int i = 0; i < nS; i++) sq[i] = sqrt(wt[i]);
+  for (int i = 0; i < nS; i++)
+    for (int j = 0; j < nS; j++) {
+      const T sw = s * sq[i] * sq[j], dd = T(1.0) / sqrt(mu[i] * mu[j]);
+      const T id = (i == j) ? T(1.0) : T(0.0);
+      X.a[i][j] = (id - sw * (ff.a[i][j] - bb.a[i][j])) * dd;
+      Y.a[i][j] = (id - sw * (ff.a[i][j] + bb.a[i][j])) * dd;
+    }
+  // Cholesky Y = L L^T (lower triangle of Y overwritten by L)
+  for (int j = 0; j < nS; j++) {
+    T d = Y.a[j][j];
+    for (int k = 0; k < j; k++) d -= Y.a[j][k] * Y.a[j][k];
+    if (!(d > T(0.0))) return false;
+    d = sqrt(d);
+    Y.a[j][j] = d;
+    for (int i = j + 1; i < nS; i++) {
+      T v = Y.a[i][j];
+      for (int k = 0; k < j; k++) v -= Y.a[i][k] * Y.a[j][k];
+      Y.a[i][j] = v / d;
+    }
+  }
+  // S = L^T X L in V (temporary X L in W)
+  for (int i = 0; i < nS; i++)
+    for (int j = 0; j < nS; j++) {
+      T v = T(0.0);
+      for (int k = j; k < nS; k++) v += X.a[i][k] * Y.a[k][j];
+      W.a[i][j] = v;
+    }
+  for (int i = 0; i < nS; i++)
+    for (int j = i; j < nS; j++) {
+      T v = T(0.0);
+      for (int k = i; k < nS; k++) v += Y.a[k][i] * W.a[k][j];
+      V.a[i][j] = v;
+    }
+  for (int i = 0; i < nS; i++)
+    for (int j = 0; j < i; j++) V.a[i][j] = V.a[j][i];
+  jacobi(nS, V, lam, X);   // eigenvectors u in the columns of X
+  // E = W^-1/2 D^-1/2 L^-T u: eigenvectors of HH, in E
+  for (int c = 0; c < nS; c++) {
+    for (int i = nS - 1; i >= 0; i--) {
+      T v = X.a[i][c];
+      for (int k = i + 1; k < nS; k++) v -= Y.a[k][i] * E.a[k][c];
+      E.a[i][c] = v / Y.a[i][i];
+    }
+    for (int i = 0; i < nS; i++) E.a[i][c] /= sqrt(wt[i] * mu[i]);
+  }
+  // PP, PM for the full set of angles: PPM = PP - PM kept in X, PPP in Y
+  for (int i = 0; i < nZ; i++) {
+    const T c = s / mu[i];
+    for (int j = 0; j < nZ; j++) {
+      const T f = c * ff.a[i][j] * wt[j] - (i == j ? T(1.0) / mu[i] : T(0.0)), b = c * bb.a[i][j] * wt[j];
+      X.a[i][j] = f - b;
+      Y.a[i][j] = f + b;
+    }
+  }
+  if (nZ > nS) {   // sensor angle (weight 0): HH is block lower triangular
+    const int z = nZ - 1;
+    T hz[NZ];
+    for (int k = 0; k < nZ; k++) {
+      T v = T(0.0);
+      for (int m = 0; m < nZ; m++) v += X.a[z][m] * Y.a[m][k];
+      hz[k] = v;   // row z of HH
+    }
+    for (int c = 0; c < nS; c++) {
+      T v = T(0.0);
+      for (int k = 0; k < nS; k++) v += hz[k] * E.a[k][c];
+      E.a[z][c] = v / (lam[c] - hz[z]);
+      if (gap) {
+        const double g = fabs(value_of(lam[c]) - value_of(hz[z])) / fabs(value_of(lam[c]));
+        if (g < *gap) *gap = g;
+      }
+    }
+    for (int i = 0; i < nS; i++) E.a[i][z] = T(0.0);
+    E.a[z][z] = T(1.0);
+    lam[z] = hz[z];
+  }
+  return true;
+}
+
 // Layer optics of a scattering layer for the adding method (CRTM_AMOM_layer +
 // MOM, azimuth order 0, no solar source): transmission T, reflection R and
 // the thermal source (identical up and down).  ff/bb are the normalised
@@ -426,85 +518,9 @@ CRTM_HD bool ada_layer(int nS, int nZ, T w, T tau, const T* mu,
     return true;
   }
   const T s = w < T(MAX_ALBEDO) ? w : T(MAX_ALBEDO);
-  // symmetric form of the quadrature block
   Mat<NZ, T> X, Y, V;
-  T lam[NZ], sq[NZ];
-  for (int i = 0; i < nS; i++) sq[i] = sqrt(wt[i]);
-  for (int i = 0; i < nS; i++)
-    for (int j = 0; j < nS; j++) {
-      const T sw = s * sq[i] * sq[j], dd = T(1.0) / sqrt(mu[i] * mu[j]);
-      const T id = (i == j) ? T(1.0) : T(0.0);
-      X.a[i][j] = (id - sw * (ff.a[i][j] - bb.a[i][j])) * dd;
-      Y.a[i][j] = (id - sw * (ff.a[i][j] + bb.a[i][j])) * dd;
-    }
-  // Cholesky Y = L L^T (lower triangle of Y overwritten by L)
-  for (int j = 0; j < nS; j++) {
-    T d = Y.a[j][j];
-    for (int k = 0; k < j; k++) d -= Y.a[j][k] * Y.a[j][k];
-    if (!(d > T(0.0))) return false;
-    d = sqrt(d);
-    Y.a[j][j] = d;
-    for (int i = j + 1; i < nS; i++) {
-      T v = Y.a[i][j];
-      for (int k = 0; k < j; k++) v -= Y.a[i][k] * Y.a[j][k];
-      Y.a[i][j] = v / d;
-    }
-  }
-  // S = L^T X L in V (temporary X L in T)
-  for (int i = 0; i < nS; i++)
-    for (int j = 0; j < nS; j++) {
-      T v = T(0.0);
-      for (int k = j; k < nS; k++) v += X.a[i][k] * Y.a[k][j];
-      Tm.a[i][j] = v;
-    }
-  for (int i = 0; i < nS; i++)
-    for (int j = i; j < nS; j++) {
-      T v = T(0.0);
-      for (int k = i; k < nS; k++) v += Y.a[k][i] * Tm.a[k][j];
-      V.a[i][j] = v;
-    }
-  for (int i = 0; i < nS; i++)
-    for (int j = 0; j < i; j++) V.a[i][j] = V.a[j][i];
-  jacobi(nS, V, lam, X);   // eigenvectors u in the columns of X
-  // E = W^-1/2 D^-1/2 L^-T u: eigenvectors of HH, in R
-  for (int c = 0; c < nS; c++) {
-    for (int i = nS - 1; i >= 0; i--) {
-      T v = X.a[i][c];
-      for (int k = i + 1; k < nS; k++) v -= Y.a[k][i] * Rm.a[k][c];
-      Rm.a[i][c] = v / Y.a[i][i];
-    }
-    for (int i = 0; i < nS; i++) Rm.a[i][c] /= sqrt(wt[i] * mu[i]);
-  }
-  // PP, PM for the full set of angles: PPM = PP - PM kept in X, PPP in Y
-  for (int i = 0; i < nZ; i++) {
-    const T c = s / mu[i];
-    for (int j = 0; j < nZ; j++) {
-      const T f = c * ff.a[i][j] * wt[j] - (i == j ? T(1.0) / mu[i] : T(0.0)), b = c * bb.a[i][j] * wt[j];
-      X.a[i][j] = f - b;
-      Y.a[i][j] = f + b;
-    }
-  }
-  if (nZ > nS) {   // sensor angle (weight 0): HH is block lower triangular
-    const int z = nZ - 1;
-    T hz[NZ];
-    for (int k = 0; k < nZ; k++) {
-      T v = T(0.0);
-      for (int m = 0; m < nZ; m++) v += X.a[z][m] * Y.a[m][k];
-      hz[k] = v;   // row z of HH
-    }
-    for (int c = 0; c < nS; c++) {
-      T v = T(0.0);
-      for (int k = 0; k < nS; k++) v += hz[k] * Rm.a[k][c];
-      Rm.a[z][c] = v / (lam[c] - hz[z]);
-      if (gap) {
-        const double g = fabs(value_of(lam[c]) - value_of(hz[z])) / fabs(value_of(lam[c]));
-        if (g < *gap) *gap = g;
-      }
-    }
-    for (int i = 0; i < nS; i++) Rm.a[i][z] = T(0.0);
-    Rm.a[z][z] = T(1.0);
-    lam[z] = hz[z];
-  }
+  T lam[NZ];
+  if (!mom_eigen<NZ, T>(nS, nZ, s, mu, wt, ff, bb, Rm, lam, X, Y, V, Tm, gap)) return false;
   // MOM with the eigenpairs (E in R, eigenvalues lam)
   if (!mat_invert(nZ, X)) return false;   // inverse of PP - PM
   T ex[NZ];
@@ -805,6 +821,79 @@ struct NoSeed {
   CRTM_HD void operator()(int, S&, S&, S&) const {}
 };
 
+// Species s's additive share of layer k's optics: the optical depth
+// ke * amount, the scattering bs = ke * w * amount and the phase sums
+// pc[l] * bs (l = 1..nleg for a cloud, 0..nleg for an aerosol) are added to
+// od, bs_sum and pcs.  Species 0..n_clouds-1 are the clouds
+// (CRTM_Compute_CloudScatter, CRTM_CloudScatter.f90:221-399), then the
+// aerosols (CRTM_Compute_AerosolScatter, CRTM_AerosolScatter.f90:170-317).
+// A species below its amount threshold (or a cloud in a layer whose
+// Cloud_Fraction drops it) adds nothing.  Returns 0 or a negative error.
+template <class S, class Seed>
+CRTM_HD int species_share(const CloudyColumn& in, const CloudLut& lut, int nleg, int loff, int k, int sp, S tk,
+                          Seed seed, S* od, S* bs_sum, S* pcs) {
+  S pc[SC_NLEG_MAX + 1];
+  if (sp < in.n_clouds) {
+    if (in.cf && in.cf[k] < MIN_COVERAGE) return 0;
+    const double wcv = in.wc[sp * in.cstride + k] / in.wc_div;
+    if (!(wcv > WATER_CONTENT_THRESHOLD)) return 0;
+    S wc(wcv), re(in.reff[sp * in.cstride + k]), unused(0.0);
+    seed(sp, wc, re, unused);
+    S ke, w;
+    if (!cloud_layer_optics<S>(lut, in.microwave, in.freq, in.cloud_type[sp], re, tk, nleg, loff, &ke, &w, pc))
+      return -4;
+    if (ke <= 0.0) { ke = S(0.0); w = S(0.0); }
+    if (w <= 0.0) { w = S(0.0); for (int l = 0; l <= nleg; l++) pc[l] = S(0.0); }
+    if (w >= 1.0) w = S(1.0);
+    *od += ke * wc;
+    const S bs = ke * w * wc;
+    *bs_sum += bs;
+    for (int l = 1; l <= nleg; l++) pcs[l] += pc[l] * bs;
+    return 0;
+  }
+  const int c = sp - in.n_clouds;
+  const double concv = in.conc[c * in.cstride + k];
+  if (!(concv > AEROSOL_CONTENT_THRESHOLD)) return 0;
+  S conc(concv), re(in.aer_reff[c * in.cstride + k]);
+  S sg(in.aer_var ? in.aer_var[c * in.cstride + k] : 0.0), rh(in.rh ? in.rh[k] : 0.0);
+  seed(sp, conc, in.alut->scheme >= AEROSOL_GOCART ? rh : re, sg);
+  S ke, w;
+  if (!aerosol_layer_optics<S>(*in.alut, in.wavenumber, in.aerosol_type[c], re, sg, rh, nleg, loff, &ke, &w, pc))
+    return -9;
+  if (ke <= 0.0) { ke = S(0.0); w = S(0.0); }
+  if (w <= 0.0) { w = S(0.0); for (int l = 0; l <= nleg; l++) pc[l] = S(0.0); }
+  if (w >= 1.0) w = S(1.0);
+  *od += ke * conc;
+  const S bs = conc * ke * w;
+  *bs_sum += bs;
+  for (int l = 0; l <= nleg; l++) pcs[l] += pc[l] * bs;
+  return 0;
+}
+
+// Number of species of a column whose optics enter the layers: its clouds,
+// and its aerosols for an infrared sensor.  Returns -8 when the aerosol table
+// cannot serve the stream set.
+CRTM_HD int scattering_species(const CloudyColumn& in, int nleg, int loff) {
+  if (in.n_aerosols > 0 && !in.microwave) {
+    if (nleg == 2 || !in.alut || in.alut->nleg < nleg + loff) return -8;
+    return in.n_clouds + in.n_aerosols;
+  }
+  return in.n_clouds;
+}
+
+// Sum of every species' share of layer k (species_share), clouds first.
+template <class S, class Seed>
+CRTM_HD int species_sums(const CloudyColumn& in, const CloudLut& lut, int nleg, int loff, int k, S tk, Seed seed,
+                         S* od, S* bs_sum, S* pcs) {
+  for (int c = 0; c < in.n_clouds; c++)
+    if (const int rc = species_share<S>(in, lut, nleg, loff, k, c, tk, seed, od, bs_sum, pcs)) return rc;
+  const int nsp = scattering_species(in, nleg, loff);
+  if (nsp < 0) return nsp;
+  for (int c = in.n_clouds; c < nsp; c++)
+    if (const int rc = species_share<S>(in, lut, nleg, loff, k, c, tk, seed, od, bs_sum, pcs)) return rc;
+  return 0;
+}
+
 // Optics of layer k for the adding method: cloud and aerosol optics summed
 // over the species, combine and delta truncation, and for a scattering layer
 // the phase blocks and the layer's transmission, reflection and source
@@ -818,47 +907,9 @@ CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const Stre
                          Seed seed = Seed(), double* gap = nullptr) {
   const int nleg = St.nleg;
   S od = gas_od, bs_sum = S(0.0);
-  S pc[SC_NLEG_MAX + 1], pcs[SC_NLEG_MAX + 1];
+  S pcs[SC_NLEG_MAX + 1];
   for (int l = 0; l <= nleg; l++) pcs[l] = S(0.0);
-  const bool dropped = in.cf && in.cf[k] < MIN_COVERAGE;
-  for (int c = 0; c < in.n_clouds && !dropped; c++) {
-    const double wcv = in.wc[c * in.cstride + k] / in.wc_div;
-    if (!(wcv > WATER_CONTENT_THRESHOLD)) continue;
-    S wc(wcv), re(in.reff[c * in.cstride + k]), unused(0.0);
-    seed(c, wc, re, unused);
-    S ke, w;
-    if (!cloud_layer_optics<S>(lut, in.microwave, in.freq, in.cloud_type[c], re, tk, nleg, St.loff, &ke, &w, pc))
-      return -4;
-    if (ke <= 0.0) { ke = S(0.0); w = S(0.0); }
-    if (w <= 0.0) { w = S(0.0); for (int l = 0; l <= nleg; l++) pc[l] = S(0.0); }
-    if (w >= 1.0) w = S(1.0);
-    od += ke * wc;
-    const S bs = ke * w * wc;
-    bs_sum += bs;
-    for (int l = 1; l <= nleg; l++) pcs[l] += pc[l] * bs;
-  }
-  if (in.n_aerosols > 0 && !in.microwave) {   // CRTM_Compute_AerosolScatter (:170-317)
-    if (nleg == 2 || !in.alut || in.alut->nleg < nleg + St.loff) return -8;
-    S pa[SC_NLEG_MAX + 1];
-    for (int c = 0; c < in.n_aerosols; c++) {
-      const double concv = in.conc[c * in.cstride + k];
-      if (!(concv > AEROSOL_CONTENT_THRESHOLD)) continue;
-      S conc(concv), re(in.aer_reff[c * in.cstride + k]);
-      S sg(in.aer_var ? in.aer_var[c * in.cstride + k] : 0.0), rh(in.rh ? in.rh[k] : 0.0);
-      seed(in.n_clouds + c, conc, in.alut->scheme >= AEROSOL_GOCART ? rh : re, sg);
-      S ke, w;
-      if (!aerosol_layer_optics<S>(*in.alut, in.wavenumber, in.aerosol_type[c], re, sg, rh, nleg, St.loff, &ke,
-                                   &w, pa))
-        return -9;
-      if (ke <= 0.0) { ke = S(0.0); w = S(0.0); }
-      if (w <= 0.0) { w = S(0.0); for (int l = 0; l <= nleg; l++) pa[l] = S(0.0); }
-      if (w >= 1.0) w = S(1.0);
-      od += ke * conc;
-      const S bs = conc * ke * w;
-      bs_sum += bs;
-      for (int l = 0; l <= nleg; l++) pcs[l] += pa[l] * bs;
-    }
-  }
+  if (const int rc = species_sums<S>(in, lut, nleg, St.loff, k, tk, seed, &od, &bs_sum, pcs)) return rc;
   S ssa = bs_sum;
   if (bs_sum > BS_THRESHOLD) {   // CRTM_AtmOptics_Combine
     const S w = bs_sum / od;

@@ -299,10 +299,14 @@ int crtm_gpu_tangent_linear_device(crtm_gpu_handle handle, int sensor, const crt
  * another allocator or who cannot afford the device-wide synchronisation of
  * cudaMalloc/cudaFree inside a call.  Batches are processed in chunks that fit
  * the scratch; a call fails (CRTM_GPU_FAILURE, message from
- * crtm_gpu_last_error) when one profile's intermediates do not fit.  The first
- * call on a device looks up the scratch address and should come before any
- * stream capture.  The scratch is shared by all handles on a device: calls
- * that overlap in time race and must be ordered by the caller. */
+ * crtm_gpu_last_error) when one profile's intermediates do not fit.  With no
+ * batch emissivity, the IR sea-surface emissivity model's 3 x P x L doubles
+ * also come from the scratch (the call fails when they leave no room for one
+ * profile).  crtm_gpu_init looks up the scratch address on its device; where
+ * it has not, the first call on a device does, and that call should come
+ * before any stream capture.  The scratch is shared by all handles on a
+ * device: calls that overlap in time race and must be ordered by the
+ * caller. */
 #define CRTM_GPU_STATIC_SCRATCH_MIB 128
 int crtm_gpu_k_matrix_device_static(crtm_gpu_handle handle, int sensor,
                                     const crtm_gpu_batch* batch, const double* bt_k,

@@ -815,7 +815,7 @@ static void map_input_ad(const or_handle* h, const or_batch* b, const pstate* s,
   const int K = h->K, Kmax = b->max_layers;
   for (int j = h->Jm - 1; j >= 0; j--) {
     int map = s->idx_map[j];
-    if (map < 0) continue;
+    if (map < 0 || (b->k_absorber_mask && !b->k_absorber_mask[map])) continue;
     double* out = Ak + (size_t)map * Kmax;
     for (int k = K - 1; k >= 0; k--) {
       double a = (s->A[j][k] <= tol) ? 0.0 : A_ad[j][k];

@@ -52,6 +52,8 @@ typedef struct {
   const double* source_zenith_angle;   /* [P] degrees */
   const double* surface_altitude;      /* [P] */
   const double* emissivity;            /* [P][L] */
+  const int* k_absorber_mask;          /* [Jabs] nonzero: return this absorber's K-matrix / adjoint
+                                          (NULL: all); the others stay zero */
 } or_batch;
 
 /* Forward: radiance and brightness temperature [P][L]; layer_od [P][L][max_layers] optional. */

@@ -30,7 +30,7 @@ class OrBatch(ct.Structure):
                 ("surface_land_temperature", _dp), ("surface_water_temperature", _dp),
                 ("surface_snow_temperature", _dp), ("surface_ice_temperature", _dp),
                 ("sensor_zenith_angle", _dp), ("source_zenith_angle", _dp),
-                ("surface_altitude", _dp), ("emissivity", _dp)]
+                ("surface_altitude", _dp), ("emissivity", _dp), ("k_absorber_mask", _ip)]
 
 
 class OrClouds(ct.Structure):
@@ -152,9 +152,16 @@ class Oracle:
             raise RuntimeError(lib().or_last_error().decode())
         return (rad, bt, od) if layer_od else (rad, bt)
 
-    def k_matrix(self, atm, sfc, geo, opt, bt_k=None, n_threads: int = 1):
+    def k_matrix(self, atm, sfc, geo, opt, bt_k=None, n_threads: int = 1, k_absorbers=None):
+        """``k_absorbers``: user absorber indices whose Jacobians are computed
+        (default all); the other absorbers' Jacobians are returned as zeros."""
         P, L, K, J = atm.n_profiles, self.n_channels, atm.max_layers, atm.n_absorbers
         b, keep = self._batch(atm, sfc, geo, opt)
+        if k_absorbers is not None:
+            mask = np.zeros(J, np.int32)
+            mask[np.asarray(k_absorbers, int)] = 1
+            keep.append(mask)
+            b.k_absorber_mask = _p(mask, _ip)
         seed = None if bt_k is None else np.ascontiguousarray(bt_k, np.float64)
         rad, bt = np.zeros((P, L)), np.zeros((P, L))
         tk, ak = np.zeros((P, L, K)), np.zeros((P, L, J, K))

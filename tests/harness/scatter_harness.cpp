@@ -2,7 +2,7 @@
 // infrastructure only): one ADA layer and one cloudy (profile, channel).
 #include <vector>
 
-#include "scatter_physics.cuh"
+#include "scatter_adjoint.cuh"
 
 using namespace crtm;
 
@@ -14,7 +14,15 @@ GaussTable make_gauss() {
 }
 }  // namespace
 
+// precision experiments: FP32 records with FP64 for layers whose smallest
+// row absorptance is below g_fp64_absorptance (0: none)
+static double g_fp64_absorptance = 0.0;
+static long g_fp64_layers = 0, g_all_layers = 0;
+
 extern "C" {
+
+void sx_set_fp64_absorptance(double a) { g_fp64_absorptance = a; g_fp64_layers = g_all_layers = 0; }
+double sx_fp64_fraction() { return g_all_layers ? (double)g_fp64_layers / g_all_layers : 0.0; }
 
 int sx_ada_layer(int nS, int nZ, double w, double tau, const double* mu, const double* wt,
                  const double* ff, const double* bb, double B, double* T, double* R, double* src) {
@@ -90,17 +98,37 @@ int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, 
   c.n_aerosols = n_aer; c.wavenumber = wavenumber; c.aerosol_type = aer_type; c.conc = conc;
   c.aer_reff = aer_reff; c.aer_var = aer_var; c.rh = rh_layers; c.alut = &A;
   c.soi = soi != 0;
-  if (soi == 2 || soi == 3) {   // layered ADA as the GPU kernels run it (records with NZ = 5);
-    c.soi = false;              // soi = 3: layer optics in double-float (the mixed form)
-    constexpr int NZ = 5, NE = 2 + 2 * NZ * NZ + NZ;
+  if (soi >= 2 && soi <= 4) {   // layered ADA as the GPU kernels run it (records with NZ = 10);
+    c.soi = false;               // layer optics in FP64 (2), double-float (3) or FP32 (4)
+    constexpr int NZ = SC_NZ_MAX, NE = 2 + 2 * NZ * NZ + NZ;
     StreamSet<NZ, double> S;
     if (int rc = stream_set<NZ, double>(nleg, mu_sensor, n_clouds > 0 ? L.nleg : -1, gt, S)) return rc;
     std::vector<double> rec((size_t)Ku * NE);
     for (int k = 0; k < Ku; k++) {
       Mat<NZ, double> Tm, Rm;
       double srcv[NZ], o;
-      const int kind = soi == 3 ? layer_optics<NZ, double, DD>(c, L, S, k, DD(od[k]), DD(temp[k]), &o, Tm, Rm, srcv)
-                                : layer_optics<NZ, double>(c, L, S, k, od[k], temp[k], &o, Tm, Rm, srcv);
+      int kind;
+      if (soi == 3)
+        kind = layer_optics<NZ, double, DD>(c, L, S, k, DD(od[k]), DD(temp[k]), &o, Tm, Rm, srcv);
+      else if (soi == 4) {
+        kind = layer_optics<NZ, double, float>(c, L, S, k, float(od[k]), float(temp[k]), &o, Tm, Rm, srcv);
+        if (kind == 1 && g_fp64_absorptance > 0.0) {
+          double amin = 1.0;
+          for (int i = 0; i < S.nZ; i++) {
+            double th = 0.0;
+            for (int j = 0; j < S.nS; j++) th += Tm.a[i][j] + Rm.a[i][j];
+            if (S.nZ == S.nS + 1 && i == S.nZ - 1) th += Tm.a[i][i];
+            amin = 1.0 - th < amin ? 1.0 - th : amin;
+          }
+          if (amin < g_fp64_absorptance) {
+            g_fp64_layers++;
+            kind = layer_optics<NZ, double>(c, L, S, k, od[k], temp[k], &o, Tm, Rm, srcv);
+          }
+        }
+        g_all_layers += kind == 1;
+      }
+      else
+        kind = layer_optics<NZ, double>(c, L, S, k, od[k], temp[k], &o, Tm, Rm, srcv);
       double* r = &rec[(size_t)k * NE];
       r[0] = kind;
       r[1] = o;
@@ -379,4 +407,83 @@ extern "C" double sx_irssem(const int* dims, int nalli2, const double* angle, co
   *de_dv = r.d[0];
   *de_dt = r.d[1];
   return irssem<double>(W, water_temperature, wind_speed, frequency, ang);
+}
+
+
+// One layer's optics adjoint two ways, for record adjoints T_b, R_b, src_b
+// (scattering layer) or od_b, B_b (clear layer): the reverse sweep
+// (layer_adjoint, FP64) and the contraction on derivative numbers
+// (layer_contract).  Outputs per method: g[0] gas optical depth, g[1]
+// temperature, then per species s (clouds, then aerosols) amount, c1, c2 at
+// g[2 + 3 s ..].  Column and LUT arguments as sx_cloudy_radiance's.  Returns
+// the layer kind of the reverse sweep (or its negative error), and
+// *kind_dual that of the derivative-number evaluation.
+extern "C" int sx_layer_adjoint_compare(
+    const int* dims, const double* f_mw, const double* r_mw, const double* t, const double* f_ir,
+    const double* r_ir, const double* ke_l, const double* w_l, const double* pc_l, const double* ke_s,
+    const double* w_s, const double* pc_s, const double* ke_ir, const double* w_ir, const double* pc_ir, int Ku,
+    int n_clouds, int nleg, int microwave, double freq, double mu_sensor, const double* planck, const double* temp,
+    const int* cloud_type, const double* wc, const double* reff, int cstride, int n_aer, const int* aer_type,
+    const double* conc, const double* aer_reff, const double* aer_var, const double* rh_layers, const int* adims,
+    const int* atypes, const double* afreq, const double* areff, const double* arsig, const double* arh,
+    const double* ake, const double* aw, const double* apc, double wavenumber, int k, double gas,
+    const double* tb, const double* rb, const double* sb, double od_b, double B_b, double* g_rev, double* g_dual,
+    int* kind_dual, int* nz_out) {
+  AerosolLut A{};
+  if (n_aer > 0) {
+    A.nw = adims[0]; A.nrh = adims[1]; A.nr = adims[2]; A.ns = adims[3]; A.nt = adims[4]; A.nleg = adims[5];
+    A.scheme = adims[6]; A.nrh_axis = adims[7];
+    A.type_id = atypes; A.freq = afreq; A.reff = areff; A.rsig = arsig; A.rh = arh; A.ke = ake; A.w = aw;
+    A.pc = apc;
+  }
+  CloudLut L{dims[0], dims[1], dims[2], dims[3], dims[4], dims[5], dims[6], f_mw, r_mw, t, f_ir, r_ir,
+             ke_l, w_l, pc_l, ke_s, w_s, pc_s, ke_ir, w_ir, pc_ir};
+  static const GaussTable gt = make_gauss();
+  CloudyColumn c{};
+  c.Ku = Ku; c.n_clouds = n_clouds; c.nleg = nleg; c.microwave = microwave != 0; c.freq = freq;
+  c.mu_sensor = mu_sensor;
+  c.c1 = planck[0]; c.c2 = planck[1]; c.b1 = planck[2]; c.b2 = planck[3];
+  c.temperature = temp; c.cloud_type = cloud_type; c.wc = wc; c.reff = reff; c.cstride = (size_t)cstride;
+  c.n_aerosols = n_aer; c.wavenumber = wavenumber; c.aerosol_type = aer_type; c.conc = conc;
+  c.aer_reff = aer_reff; c.aer_var = aer_var; c.rh = rh_layers; c.alut = &A;
+  constexpr int NZ = SC_NZ_MAX;
+  StreamSet<NZ, double> S;
+  if (int rc = stream_set<NZ, double>(nleg, mu_sensor, n_clouds > 0 ? L.nleg : -1, gt, S)) return -100 - rc;
+  const int nZ = S.nZ;
+  *nz_out = nZ;
+  Mat<NZ, double> T_b, R_b;
+  double src_b[NZ];
+  for (int i = 0; i < nZ; i++) {
+    src_b[i] = sb[i];
+    for (int j = 0; j < nZ; j++) { T_b.a[i][j] = tb[i * nZ + j]; R_b.a[i][j] = rb[i * nZ + j]; }
+  }
+  const int nsp = n_clouds + (microwave ? 0 : n_aer);
+  // the record's kind from the plain forward
+  Mat<NZ, double> T0, R0;
+  double s0[NZ], o0;
+  const int kind = layer_optics<NZ, double>(c, L, S, k, gas, temp[k], &o0, T0, R0, s0);
+  if (kind < 0) return kind;
+  double g[2], gs[2 * SC_NC_MAX][3];
+  const int kr = layer_adjoint<NZ, double>(c, L, S, k, gas, kind, T_b, R_b, src_b, kind == 1 ? 0.0 : od_b,
+                                           kind == 1 ? 0.0 : B_b, g, gs);
+  g_rev[0] = g[0];
+  g_rev[1] = g[1];
+  for (int s = 0; s < nsp; s++)
+    for (int q = 0; q < 3; q++) g_rev[2 + 3 * s + q] = gs[s][q];
+  double gd[4];
+  LayerDirections d{true, 0, {0, 0, 0, 0}};
+  *kind_dual = layer_contract<NZ, 2>(c, L, S, k, gas, d, T_b, R_b, src_b, kind == 1 ? 0.0 : od_b,
+                                     kind == 1 ? 0.0 : B_b, gd);
+  g_dual[0] = gd[0];
+  g_dual[1] = gd[1];
+  for (int s = 0; s < nsp; s++) {
+    d = LayerDirections{false, 1, {s, 0, 0, 0}};
+    layer_contract<NZ, 2>(c, L, S, k, gas, d, T_b, R_b, src_b, kind == 1 ? 0.0 : od_b, 0.0, gd);
+    g_dual[2 + 3 * s] = gd[0];
+    g_dual[3 + 3 * s] = gd[1];
+    d.second = true;
+    layer_contract<NZ, 2>(c, L, S, k, gas, d, T_b, R_b, src_b, kind == 1 ? 0.0 : od_b, 0.0, gd);
+    g_dual[4 + 3 * s] = gd[0];
+  }
+  return kr;
 }

@@ -145,3 +145,28 @@ def test_mixed_against_fp64_on_many_profiles(gpu_lib, coeff_dir):
     assert np.abs(mix[1].brightness_temperature - ref[1].brightness_temperature).max() <= BT_TOL[1]
     for f in ("temperature", "absorber", "water_temperature"):
         assert _rel(getattr(mix[0], f), getattr(ref[0], f)) <= JAC_TOL[1], f
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_k_matrix_c2211_bench_sensor_matches_oracle(gpu_lib, coeff_dir, precision):
+    """The clear-sky IR workload's own sensor (2211 channels, ODPS group 1, 6
+    absorbers, 101 layers) with the H2O and O3 Jacobians that its K-matrix
+    returns, against the oracle computing the same two."""
+    from crtmv3_gb300 import coefficients as co
+    from oracle.pyoracle import Oracle
+    sensor = "irsynth_c2211"
+    atm, sfc, geo, opt = _case(sensor, 4, 101, 2211)
+    ids = list(atm.absorber_id)
+    sel = [ids.index(co.H2O_ID), ids.index(co.O3_ID)]
+    h = gpu_lib.CRTM([sensor], coeff_dir, precision)
+    km, rts = h.k_matrix(atm, sfc, geo, opt, k_absorbers=sel)
+    ref = Oracle(coeff_dir, sensor).k_matrix(atm, sfc, geo, opt, n_threads=4, k_absorbers=sel)
+    assert np.abs(rts.brightness_temperature - ref["bt"]).max() < BT_TOL[precision]
+    assert (rts.status == 0).all()
+    assert _rel(km.temperature, ref["temperature_k"]) < JAC_TOL[precision]
+    for i, j in enumerate(sel):
+        assert _rel(km.absorber[:, :, i], ref["absorber_k"][:, :, j]) < JAC_TOL[precision]
+    others = [j for j in range(atm.n_absorbers) if j not in sel]
+    assert not ref["absorber_k"][:, :, others].any()
+    assert _rel(km.water_temperature, ref["water_temperature_k"]) < JAC_TOL[precision]
+    assert _rel(km.surface_emissivity, ref["surface_emissivity_k"]) < JAC_TOL[precision]

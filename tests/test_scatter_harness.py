@@ -526,3 +526,92 @@ def test_irssem_matches_oracle(sx, tmp_path, classification):
                    w.emissivity[i, j, k, 0]) <= 1e-14
     finally:
         L.or_irwater_destroy(h)
+
+
+def _lut_args(coeff_dir, scheme):
+    """CloudCoeff and AerosolCoeff arguments of the harness entry points."""
+    cc = co.read_cloudcoeff(sy.write_cloud_files(coeff_dir))
+    f = lambda a: np.ascontiguousarray(np.ravel(a, order="F"))   # noqa: E731
+    arrs = [f(x) for x in (cc.frequency_mw, cc.reff_mw, cc.temperature, cc.frequency_ir, cc.reff_ir,
+                           cc.ke_l_mw, cc.w_l_mw, cc.pcoeff_l_mw, cc.ke_s_mw, cc.w_s_mw, cc.pcoeff_s_mw,
+                           cc.ke_ir, cc.w_ir, cc.pcoeff_ir)]
+    dims = np.array([cc.frequency_mw.size, cc.reff_mw.size, cc.temperature.size, cc.density_mw.size,
+                     cc.frequency_ir.size, cc.reff_ir.size, cc.n_legendre_terms], np.int32)
+    ac = co.read_aerosolcoeff(sy.write_aerosol_files(coeff_dir, scheme), scheme)
+    adims = np.array([ac.wavelength.size, ac.ke.shape[1], ac.ke.shape[2], ac.ke.shape[3], ac.ke.shape[4],
+                      ac.pcoeff.shape[5] - 1, co.AEROSOL_SCHEMES.index(scheme), ac.rh.size], np.int32)
+    aarrs = [f(x) for x in (1.0e4 / ac.wavelength, ac.reff, ac.rsig, ac.rh, ac.ke, ac.w, ac.pcoeff[..., 0])]
+    atypes = np.ascontiguousarray(ac.type_id, np.int32)
+    return dims, arrs, adims, atypes, aarrs
+
+
+@pytest.mark.parametrize("sensor,n_streams,aer,scheme", [("mwsynth_c16", None, False, "CRTM"),
+                                                         ("mwsynth_c16", 16, False, "CRTM"),
+                                                         ("irsynth_c616", None, True, "CRTM"),
+                                                         ("irsynth_c616", 8, True, "CMAQ"),
+                                                         ("irsynth_c616", 16, True, "GOCART-GEOS5")])
+def test_layer_adjoint_matches_derivative_numbers(sx, coeff_dir, sensor, n_streams, aer, scheme):
+    """The reverse sweep through a layer's optics (MOM, phase normalisation,
+    combine, LUT) gives the same contraction of the record adjoints as the
+    forward-mode derivative numbers, for every input of the layer: gas
+    optical depth, temperature, and each cloud's and aerosol's amount and
+    LUT coordinates.  Agreement to 1e-9 of each group's largest value
+    (both are exact derivatives; the difference is rounding)."""
+    dims, arrs, adims, atypes, aarrs = _lut_args(coeff_dir, scheme)
+    sc = co.read_spccoeff(f"{coeff_dir}/{sensor}.SpcCoeff.bin")
+    mw = sc.sensor_type == co.MICROWAVE_SENSOR
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 2, 100, 61, wc_scale=30.0, n_streams=n_streams,
+                                            cloud_types=(co.WATER_CLOUD, co.ICE_CLOUD, co.RAIN_CLOUD)
+                                            if mw else (co.WATER_CLOUD, co.ICE_CLOUD))
+    NA = 0
+    if aer:
+        sy.add_aerosols(atm, sy.AEROSOL_TYPES, 62, load_scale=20.0)
+        sy.add_aerosol_scheme_inputs(atm, 63)
+        NA = 3
+    rng = np.random.default_rng(64)
+    n_checked = 0
+    for m in range(2):
+        Ku = int(atm.n_layers[m])
+        temp = np.ascontiguousarray(atm.temperature[m, :Ku])
+        wc = np.ascontiguousarray(atm.cloud_water_content[m])
+        re = np.ascontiguousarray(atm.cloud_effective_radius[m])
+        ctype = np.ascontiguousarray(atm.cloud_type[m], np.int32)
+        if aer:
+            conc = np.ascontiguousarray(atm.aerosol_concentration[m])
+            areff = np.ascontiguousarray(atm.aerosol_effective_radius[m])
+            avar = np.ascontiguousarray(atm.aerosol_effective_variance[m])
+            rh = np.ascontiguousarray(atm.relative_humidity[m])
+            at = np.ascontiguousarray(atm.aerosol_type[m], np.int32)
+            aptr = [_p(at, _ip), _p(conc), _p(areff), _p(avar), _p(rh), _p(adims, _ip), _p(atypes, _ip),
+                    *[_p(x) for x in aarrs]]
+        else:
+            aptr = [None] * 14
+        mu = float(np.cos(np.deg2rad(geo.sensor_zenith_angle[m])))
+        for l in (0, sc.n_channels // 2, sc.n_channels - 1):
+            planck = np.array([sc.planck_c1[l], sc.planck_c2[l], sc.band_c1[l], sc.band_c2[l]])
+            rmax = max(re[:, :Ku].max(), atm.aerosol_effective_radius[m].max() if aer else 0.0)
+            nleg = n_streams or sx.sx_stream_rule(ct.c_double(rmax), ct.c_double(sc.wavenumber[l]))
+            if aer and nleg == 2:
+                continue
+            fr = sc.frequency[l] if mw else sc.wavenumber[l]
+            cloudy = np.where((wc[:, :Ku] > 1e-6).any(axis=0))[0]
+            for k in list(cloudy[:4]) + [Ku - 1]:
+                nz = 10
+                tb, rb, sb = rng.normal(size=nz * nz), rng.normal(size=nz * nz), rng.normal(size=nz)
+                ns = 2 + 3 * (ctype.size + NA)
+                gr, gd = np.zeros(ns), np.zeros(ns)
+                kd, nzo = ct.c_int(), ct.c_int()
+                kind = sx.sx_layer_adjoint_compare(
+                    _p(dims, _ip), *[_p(a) for a in arrs], Ku, ctype.size, nleg, int(mw), ct.c_double(fr),
+                    ct.c_double(mu), _p(planck), _p(temp), _p(ctype, _ip), _p(wc), _p(re), atm.max_layers,
+                    NA, *aptr, ct.c_double(sc.wavenumber[l]), int(k), ct.c_double(0.01 + 0.02 * (k % 3)),
+                    _p(tb), _p(rb), _p(sb), ct.c_double(0.7), ct.c_double(-0.3), _p(gr), _p(gd),
+                    ct.byref(kd), ct.byref(nzo))
+                assert kind >= 0, kind
+                assert kind == kd.value
+                groups = [slice(0, 1), slice(1, 2)] + [slice(2 + q, ns, 3) for q in range(3)]
+                for gsl in groups:
+                    scale = max(np.abs(gd[gsl]).max(), 1e-300)
+                    assert np.abs(gr[gsl] - gd[gsl]).max() <= 1e-9 * scale, (m, l, k, gsl, gr[gsl], gd[gsl])
+                n_checked += kind
+    assert n_checked > 5

@@ -136,3 +136,109 @@ def test_static_scratch_rejects_oversized_profiles(gpu_lib, tmp_path):
     h.k_matrix_device(b, o, None, 0, stream, static_scratch=True)
     torch.cuda.synchronize()
     _close(o, ref)
+
+
+def test_static_scratch_with_emissivity_model(gpu_lib, coeff_dir, tmp_path):
+    """No batch emissivity: the IR sea-surface emissivity model's e, de/dv and
+    de/dT arrays come from the static scratch too, so the call still grows no
+    device memory, and its outputs (with the wind-speed Jacobian) match the
+    regular entry point's."""
+    import shutil
+
+    import torch
+    sensor = "irsynth_c616"
+    for f in os.listdir(coeff_dir):
+        if f.startswith(sensor):
+            shutil.copy(os.path.join(coeff_dir, f), tmp_path)
+    sy.write_irwater_file(str(tmp_path), "Nalli")
+    P = 6
+    atm, sfc, geo, opt = sy.clear_sky_workload(sensor, P, 101, 73)
+    sfc.land_coverage[:] = sfc.snow_coverage[:] = sfc.ice_coverage[:] = 0.0
+    sfc.water_coverage[:] = 1.0
+    ref_h = gpu_lib.CRTM([sensor], str(tmp_path), 0)
+    L, K, J = ref_h.n_channels[0], atm.max_layers, atm.n_absorbers
+    b, keep, t = _device_inputs(torch, ref_h, atm, sfc, geo, opt)
+    t["wind_speed"] = torch.from_numpy(np.linspace(1.0, 12.0, P)).cuda()
+    t.pop("emissivity")
+    b, keep = ref_h.device_batch(t, atm.absorber_id)
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def outs():
+        o = _outputs(torch, P, L, K, J)
+        o["wind_speed_k"] = torch.full((P, L), np.nan, dtype=torch.float64, device="cuda")
+        return o
+
+    ref = outs()
+    ref_h.k_matrix_device(b, ref, None, 0, stream)
+    torch.cuda.synchronize()
+    h = gpu_lib.CRTM([sensor], str(tmp_path), 0)
+    runs = [outs() for _ in range(2)]
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for o in runs:
+        h.k_matrix_device(b, o, None, 0, stream, static_scratch=True)
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    for o in runs:
+        _close(o, ref)
+        scale = float(ref["wind_speed_k"].abs().max())
+        assert scale > 0.0
+        assert float((o["wind_speed_k"] - ref["wind_speed_k"]).abs().max()) <= TOL * scale
+    assert free0 - free1 < (16 << 20)
+
+
+def test_static_scratch_cloudy_and_aerosol_batch(gpu_lib, coeff_dir, tmp_path):
+    """Clouds and aerosols: the scattering intermediates (FP64 layer records,
+    adding states, species slots) fit the static scratch chunk by chunk and
+    the species Jacobians match the regular entry point's."""
+    import shutil
+
+    import torch
+    sensor = "irsynth_c616"
+    for f in os.listdir(coeff_dir):
+        if f.startswith(sensor):
+            shutil.copy(os.path.join(coeff_dir, f), tmp_path)
+    sy.write_cloud_files(str(tmp_path))
+    sy.write_aerosol_files(str(tmp_path))
+    P = 4
+    atm, sfc, geo, opt = sy.clear_sky_workload(sensor, P, 100, 74)
+    sy.add_clouds(atm, (co.WATER_CLOUD, co.ICE_CLOUD), 75)
+    sy.add_aerosols(atm, sy.AEROSOL_TYPES, 76)
+    ref_h = gpu_lib.CRTM([sensor], str(tmp_path), 0)
+    L, K, J = ref_h.n_channels[0], atm.max_layers, atm.n_absorbers
+    b, keep, t = _device_inputs(torch, ref_h, atm, sfc, geo, opt)
+    for k in ("cloud_water_content", "cloud_effective_radius", "cloud_fraction", "aerosol_concentration",
+              "aerosol_effective_radius"):
+        t[k] = torch.from_numpy(np.ascontiguousarray(getattr(atm, k), np.float64)).cuda()
+    for k in ("n_clouds", "cloud_type", "n_aerosols", "aerosol_type"):
+        t[k] = torch.from_numpy(np.ascontiguousarray(getattr(atm, k), np.int32)).cuda()
+    b, keep = ref_h.device_batch(t, atm.absorber_id)
+    stream = torch.cuda.current_stream().cuda_stream
+    NC, NA = atm.cloud_type.shape[1], atm.aerosol_type.shape[1]
+    species = {"cloud_water_content_k": NC, "cloud_effective_radius_k": NC,
+               "aerosol_concentration_k": NA, "aerosol_effective_radius_k": NA}
+
+    def outs():
+        o = _outputs(torch, P, L, K, J)
+        for f, n in species.items():
+            o[f] = torch.full((P, L, n, K), np.nan, dtype=torch.float64, device="cuda")
+        return o
+
+    ref = outs()
+    ref_h.k_matrix_device(b, ref, None, 0, stream)
+    torch.cuda.synchronize()
+    h = gpu_lib.CRTM([sensor], str(tmp_path), 0)
+    runs = [outs() for _ in range(2)]
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for o in runs:
+        h.k_matrix_device(b, o, None, 0, stream, static_scratch=True)
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    for o in runs:
+        _close(o, ref)
+        for f in species:
+            scale = float(ref[f].abs().max())
+            assert scale > 0.0, f
+            assert float((o[f] - ref[f]).abs().max()) <= TOL * scale, f
+    assert free0 - free1 < (16 << 20)
