@@ -10,8 +10,10 @@ CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libcrtm_gb300.so")
 # Translation units, compiled in parallel: the host runtime with the ODPS and
 # forward scattering kernels, and per angle capacity one unit of the
-# scattering K-matrix kernels and one of the SOI layers' contraction.
-SOURCES = ["crtm_gpu.cu", "scatter_k_d5.cu", "scatter_k_d10.cu", "scatter_soi_d5.cu", "scatter_soi_d10.cu"]
+# scattering K-matrix kernels per arithmetic form and one of the SOI layers'
+# contraction.
+SOURCES = ["crtm_gpu.cu", "scatter_k_d5.cu", "scatter_k_d10.cu", "scatter_k_d5f.cu", "scatter_k_d10f.cu",
+           "scatter_soi_d5.cu", "scatter_soi_d10.cu"]
 HEADERS = ["odps_physics.cuh", "odps_prep.cuh", "odps_kernels.cuh", "scatter_physics.cuh",
            "scatter_kernels.cuh", "scatter_adjoint.cuh", "scatter_launch.h", "dual.cuh", "dd.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -1001,39 +1001,41 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
         StageScope sc(h, 6, st);
         scatter_profile_kernel<R><<<(n + 3) / 4, 128, 0, st>>>(sa);
         CK_LAUNCH(h);
-        if (split) {   // K-matrix / adjoint: R is double here (FP64 gas optics)
-          if constexpr (std::is_same<R, double>::value) {
-            if (nz_max)
-              launch_scatter_layers_k<SC_NZ_MAX, double>(sa, gl, st);
-            else
-              launch_scatter_layers_k<5, double>(sa, gl, st);
-          }
-        } else {   // forward: FP64 layer solver in both forms (records in R)
-          using C = double;
+        if (split) {   // K-matrix / adjoint: FP64 records, layer solver in R
           if (nz_max)
-            scatter_layers_kernel<SC_NZ_MAX, R, R, C><<<gl, SCATTER_THREADS, 0, st>>>(sa, w.LB);
+            launch_scatter_layers_k<SC_NZ_MAX, R, R>(sa, gl, st);
           else
-            scatter_layers_kernel<5, R, R, C><<<gl, SCATTER_THREADS, 0, st>>>(sa, w.LB);
+            launch_scatter_layers_k<5, R, R>(sa, gl, st);
+        } else if (soi) {   // forward with SOI profiles: FP64 layer solver (records in R)
+          if (nz_max)
+            scatter_layers_kernel<SC_NZ_MAX, R, R, double><<<gl, SCATTER_THREADS, 0, st>>>(sa, w.LB);
+          else
+            scatter_layers_kernel<5, R, R, double><<<gl, SCATTER_THREADS, 0, st>>>(sa, w.LB);
+        } else {   // forward: layer solver in R (records in R)
+          if (nz_max)
+            scatter_layers_kernel<SC_NZ_MAX, R, R, R><<<gl, SCATTER_THREADS, 0, st>>>(sa, w.LB);
+          else
+            scatter_layers_kernel<5, R, R, R><<<gl, SCATTER_THREADS, 0, st>>>(sa, w.LB);
         }
         CK_LAUNCH(h);
       }
       if (split) {
-        if constexpr (std::is_same<R, double>::value) {
-          {
-            StageScope sc(h, 7, st);
-            if (nz_max)
-              launch_scatter_kmatrix<SC_NZ_MAX>(sa, ga, st, soi);
-            else
-              launch_scatter_kmatrix<5>(sa, ga, st, soi);
-            CK_LAUNCH(h);
-          }
-          {
-            StageScope sc(h, 8, st);
-            if (nz_max)
-              launch_scatter_reverse<SC_NZ_MAX, double>(sa, gl, st);
-            else
-              launch_scatter_reverse<5, double>(sa, gl, st);
-            CK_LAUNCH(h);
+        {
+          StageScope sc(h, 7, st);
+          if (nz_max)
+            launch_scatter_kmatrix<SC_NZ_MAX, R>(sa, ga, st, soi);
+          else
+            launch_scatter_kmatrix<5, R>(sa, ga, st, soi);
+          CK_LAUNCH(h);
+        }
+        {
+          StageScope sc(h, 8, st);
+          if (nz_max)
+            launch_scatter_reverse<SC_NZ_MAX, R, R>(sa, gl, st);
+          else
+            launch_scatter_reverse<5, R, R>(sa, gl, st);
+          CK_LAUNCH(h);
+          if constexpr (std::is_same<R, double>::value) {
             if (soi) {   // the SOI profiles' layers
               if (nz_max)
                 launch_scatter_contract<SC_NZ_MAX, double>(sa, gl, st);
@@ -1041,9 +1043,9 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
                 launch_scatter_contract<5, double>(sa, gl, st);
               CK_LAUNCH(h);
             }
+          } else if (soi) {
+            return fail(h, "internal: SOI K-matrix in the mixed form");
           }
-        } else {
-          return fail(h, "internal: scattering K-matrix with FP32 gas optics");
         }
         {
           ca.pass = 2;
@@ -1185,12 +1187,12 @@ int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, c
   if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
   const Sensor& s = h->sensors[sensor];
   const bool scat = b->max_clouds > 0 || b->max_aerosols > 0;
-  // The K-matrix and adjoint of a batch with clouds or aerosols run the gas
-  // optics in FP64 in both forms: the cloud Jacobians are small differences
-  // of large terms, and the FP32 regression's optical-depth rounding moves
-  // them by more than 1e-3 of their largest value.  The scattering work is
-  // FP64 in both forms anyway and the gas optics is under 1 % of such a call.
-  const bool fp64 = h->precision == CRTM_GPU_FP64 || (scat && (mode == 1 || mode == 2));
+  // The mixed form runs the gas optics and the scattering layer solver in
+  // FP32 and the adding in FP64.  The K-matrix and adjoint of a batch with
+  // SOI profiles (Options%RT_Algorithm_Id given) run in the FP64 form: the SOI
+  // layers' doubling and its derivative-number contraction are FP64 only.
+  const bool fp64 = h->precision == CRTM_GPU_FP64 ||
+                    (scat && (mode == 1 || mode == 2) && b->rt_algorithm_id != nullptr);
   if (scat) {
     if (b->max_clouds > SC_NC_MAX || b->max_aerosols > SC_NC_MAX)
       return fail(h, "at most %d clouds and %d aerosols per profile", SC_NC_MAX, SC_NC_MAX);

@@ -106,13 +106,14 @@ CRTM_HD DD sqrt(const DD& a) {
   return dd_detail::fast_two_sum(s, r.hi / (2.0f * s));
 }
 CRTM_HD DD exp(const DD& a) { return DD(::exp((double)a)); }
+CRTM_HD DD expm1(const DD& a) { return DD(::expm1((double)a)); }
 
 CRTM_HD double value_of(const DD& x) { return (double)x; }
 CRTM_HD bool is_zero(const DD& x) { return x.hi == 0.0f && x.lo == 0.0f; }
 
 // Jacobi convergence threshold on (off-diagonal / diagonal) squared norms
 template <class T> struct JacobiEps { static constexpr double value = 1.0e-32; };
-template <> struct JacobiEps<float> { static constexpr double value = 1.0e-12; };
+template <> struct JacobiEps<float> { static constexpr double value = 1.0e-14; };
 template <> struct JacobiEps<DD> { static constexpr double value = 1.0e-27; };
 
 }  // namespace crtm

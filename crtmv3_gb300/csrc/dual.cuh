@@ -22,6 +22,7 @@ namespace crtm {
 
 // keep the plain overloads visible next to the Dual and DD ones
 using ::exp;
+using ::expm1;
 using ::fabs;
 using ::sqrt;
 
@@ -93,6 +94,13 @@ template <int N, class S> CRTM_HD Dual<N, S> exp(const Dual<N, S>& a) {
   Dual<N, S> r;
   r.v = exp(a.v);
   for (int i = 0; i < N; i++) r.d[i] = a.d[i] * r.v;
+  return r;
+}
+template <int N, class S> CRTM_HD Dual<N, S> expm1(const Dual<N, S>& a) {
+  Dual<N, S> r;
+  r.v = expm1(a.v);
+  const S e = r.v + S(1.0);
+  for (int i = 0; i < N; i++) r.d[i] = a.d[i] * e;
   return r;
 }
 template <int N, class S> CRTM_HD Dual<N, S> fabs(const Dual<N, S>& a) { return a.v < 0.0 ? -a : a; }

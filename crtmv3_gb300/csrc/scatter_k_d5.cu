@@ -1,7 +1,8 @@
-// Scattering K-matrix/adjoint kernels for NZ = 5 angles (the stream rule's 2-6 streams), FP64:
-// the layer records, the adding adjoint (and the SOI orders' adjoint), and
-// the reverse sweep through the ADA layers' optics.  One translation unit per
-// angle capacity so that the library compiles in parallel.
+// Scattering K-matrix/adjoint kernels for NZ = 5 angles (the stream rule's 2-6 streams), FP64 form:
+// the layer records, the adding adjoint (and, FP64 form, the SOI orders'
+// adjoint), and the reverse sweep through the ADA layers' optics.  One
+// translation unit per angle capacity and form so that the library compiles
+// in parallel.
 #include "scatter_kernels.cuh"
 #include "scatter_launch.h"
 
@@ -11,24 +12,25 @@ int scatter_k_d5_set_gauss(const GaussTable& g) {
   return cudaMemcpyToSymbol(c_gauss, &g, sizeof g) == cudaSuccess ? 0 : 1;
 }
 
-template <int NZ, class C>
-void launch_scatter_layers_k(const ScatterArgs<double>& a, unsigned grid, cudaStream_t st) {
-  scatter_layers_kernel<NZ, double, double, C><<<grid, SCATTER_THREADS, 0, st>>>(a, a.LBK);
+template <int NZ, class R, class C>
+void launch_scatter_layers_k(const ScatterArgs<R>& a, unsigned grid, cudaStream_t st) {
+  scatter_layers_kernel<NZ, R, double, C><<<grid, SCATTER_THREADS, 0, st>>>(a, a.LBK);
 }
 
-template <int NZ>
-void launch_scatter_kmatrix(const ScatterArgs<double>& a, dim3 grid, cudaStream_t st, bool soi) {
-  scatter_kmatrix_kernel<NZ, double><<<grid, SCATTER_THREADS, 0, st>>>(a);
-  if (soi) scatter_soi_k_kernel<NZ><<<grid, SCATTER_THREADS, 0, st>>>(a);
+template <int NZ, class R>
+void launch_scatter_kmatrix(const ScatterArgs<R>& a, dim3 grid, cudaStream_t st, bool soi) {
+  scatter_kmatrix_kernel<NZ, R><<<grid, SCATTER_THREADS, 0, st>>>(a);
+  if constexpr (std::is_same<R, double>::value)
+    if (soi) scatter_soi_k_kernel<NZ><<<grid, SCATTER_THREADS, 0, st>>>(a);
 }
 
-template <int NZ, class C>
-void launch_scatter_reverse(const ScatterArgs<double>& a, unsigned grid, cudaStream_t st) {
-  scatter_reverse_kernel<NZ, double, C><<<grid, SCATTER_THREADS, 0, st>>>(a);
+template <int NZ, class R, class C>
+void launch_scatter_reverse(const ScatterArgs<R>& a, unsigned grid, cudaStream_t st) {
+  scatter_reverse_kernel<NZ, R, C><<<grid, SCATTER_THREADS, 0, st>>>(a);
 }
 
-template void launch_scatter_layers_k<5, double>(const ScatterArgs<double>&, unsigned, cudaStream_t);
-template void launch_scatter_kmatrix<5>(const ScatterArgs<double>&, dim3, cudaStream_t, bool);
-template void launch_scatter_reverse<5, double>(const ScatterArgs<double>&, unsigned, cudaStream_t);
+template void launch_scatter_layers_k<5, double, double>(const ScatterArgs<double>&, unsigned, cudaStream_t);
+template void launch_scatter_kmatrix<5, double>(const ScatterArgs<double>&, dim3, cudaStream_t, bool);
+template void launch_scatter_reverse<5, double, double>(const ScatterArgs<double>&, unsigned, cudaStream_t);
 
 }  // namespace crtm

@@ -490,43 +490,56 @@ CRTM_HD bool mom_eigen(int nS, int nZ, T s, const T* mu, const T* wt, const Mat<
 }
 
 // Layer optics of a scattering layer for the adding method (CRTM_AMOM_layer +
-// MOM, azimuth order 0, no solar source): transmission T, reflection R and
-// the thermal source (identical up and down).  ff/bb are the normalised
-// forward/backward phase blocks.  Returns false on a failed factorisation.
+// MOM, azimuth order 0, no solar source), in loss form: U = I - T (T the
+// layer's transmission), the reflection R and the thermal source (identical
+// up and down).  ff/bb are the normalised forward/backward phase blocks.
+// Returns false on a failed factorisation.
+//
+// MOM gives T and R as ratios of differences that cancel as the layer thins
+// (T -> I, R -> 0 as tau -> 0): with D = I - diag(exp(-lambda tau)) from expm1,
+// P = Gm^-1 Gp, Q = Gm - Gp P and e = I - D, the reference's
+//   T = (Gm e - Gp A2)(Gm - Gp e A2)^-1,  R = (Gp - Gm e A2)(...)^-1,  A2 = P e
+// are rewritten with GA = Q + Gp (D P e + P D) as
+//   U = (Q D + Gp (D P e + P D)) GA^-1,  R = (Gp D + Gm D P e) GA^-1,
+// every term of which is O(D): U, R and the source (1 - row sums of T + R)
+// keep the arithmetic's relative precision for thin layers, which FP32
+// records need.
 // gap (optional): the smallest |lambda_c - h_zz| / |lambda_c| between the
 // quadrature eigenvalues and the sensor angle's diagonal term of HH (1 when
 // there is no separate sensor angle).  Near 0 the eigenbasis is nearly
 // defective: the layer's T and R stay smooth, but their derivatives through
 // the eigenvectors lose about eps / gap^2 of their accuracy.
 template <int NZ, class T>
-CRTM_HD bool ada_layer(int nS, int nZ, T w, T tau, const T* mu,
-                              const T* wt, const Mat<NZ, T>& ff, const Mat<NZ, T>& bb, T B,
-                              Mat<NZ, T>& Tm, Mat<NZ, T>& Rm, T* src, double* gap = nullptr) {
+CRTM_HD bool ada_layer_loss(int nS, int nZ, T w, T tau, const T* mu, const T* wt, const Mat<NZ, T>& ff,
+                            const Mat<NZ, T>& bb, T B, Mat<NZ, T>& Um, Mat<NZ, T>& Rm, T* src,
+                            double* gap = nullptr) {
   if (gap) *gap = 1.0;
+  const bool sensor_row = nZ == nS + 1;
   if (tau < T(DELTA_OPTICAL_DEPTH)) {   // thin layer: first-order scattering
     const T s = tau * w;
     for (int i = 0; i < nZ; i++) {
       const T c = s / mu[i];
-      T th = T(0.0);
+      T a = T(0.0);
       for (int j = 0; j < nZ; j++) {
         Rm.a[i][j] = c * bb.a[i][j] * wt[j];
-        Tm.a[i][j] = c * ff.a[i][j] * wt[j] + (i == j ? T(1.0) - tau / mu[i] : T(0.0));
-        th += Rm.a[i][j] + Tm.a[i][j];
+        Um.a[i][j] = (i == j ? tau / mu[i] : T(0.0)) - c * ff.a[i][j] * wt[j];
+        a += Um.a[i][j] - Rm.a[i][j];
       }
-      src[i] = (T(1.0) - th) * B;
+      src[i] = a * B;
     }
     return true;
   }
   const T s = w < T(MAX_ALBEDO) ? w : T(MAX_ALBEDO);
   Mat<NZ, T> X, Y, V;
   T lam[NZ];
-  if (!mom_eigen<NZ, T>(nS, nZ, s, mu, wt, ff, bb, Rm, lam, X, Y, V, Tm, gap)) return false;
+  if (!mom_eigen<NZ, T>(nS, nZ, s, mu, wt, ff, bb, Rm, lam, X, Y, V, Um, gap)) return false;
   // MOM with the eigenpairs (E in R, eigenvalues lam)
   if (!mat_invert(nZ, X)) return false;   // inverse of PP - PM
-  T ex[NZ];
+  T ex[NZ], dx[NZ];
   for (int i = 0; i < nZ; i++) {
     lam[i] = lam[i] > T(0.0) ? sqrt(lam[i]) : T(0.0);
     ex[i] = exp(-lam[i] * tau);
+    dx[i] = -expm1(-lam[i] * tau);
   }
   // EF = (PP-PM)^-1 E diag(lam);  Gp = (E + EF)/2 in Y, Gm = (E - EF)/2 in V
   for (int i = 0; i < nZ; i++)
@@ -537,42 +550,55 @@ CRTM_HD bool ada_layer(int nS, int nZ, T w, T tau, const T* mu,
       Y.a[i][j] = T(0.5) * (Rm.a[i][j] + v);
       V.a[i][j] = T(0.5) * (Rm.a[i][j] - v);
     }
-  // A2 = Gm^-1 A1 with A1 = Gp diag(ex)
+  // P = Gm^-1 Gp (in Rm)
   for (int i = 0; i < nZ; i++)
     for (int j = 0; j < nZ; j++) X.a[i][j] = V.a[i][j];
   if (!mat_invert(nZ, X)) return false;    // Gm^-1
-  Mat<NZ, T> A2;
+  mat_mul(nZ, X, Y, Rm);
+  // W = D P e + P D (in X);  Q = Gm - Gp P (in Um)
   for (int i = 0; i < nZ; i++)
     for (int j = 0; j < nZ; j++) {
+      X.a[i][j] = dx[i] * Rm.a[i][j] * ex[j] + Rm.a[i][j] * dx[j];
       T v = T(0.0);
-      for (int k = 0; k < nZ; k++) v += X.a[i][k] * Y.a[k][j];
-      A2.a[i][j] = v * ex[j];
+      for (int k = 0; k < nZ; k++) v += Y.a[i][k] * Rm.a[k][j];
+      Um.a[i][j] = V.a[i][j] - v;
     }
-  // Gm - A1 A2 in X;  T <- (Gm diag(ex) - Gp A2), R <- (Gp - Gm diag(ex) A2)
+  // GA = Q + Gp W (in A);  U numerator Q D + Gp W (in Um);  R numerator Gp D + Gm D P e (in Rn)
+  Mat<NZ, T> A, Rn;
   for (int i = 0; i < nZ; i++)
     for (int j = 0; j < nZ; j++) {
-      T a5 = T(0.0), a3 = T(0.0), a6 = T(0.0);
+      T gw = T(0.0), gd = T(0.0);
       for (int k = 0; k < nZ; k++) {
-        a5 += Y.a[i][k] * ex[k] * A2.a[k][j];
-        a3 += Y.a[i][k] * A2.a[k][j];
-        a6 += V.a[i][k] * ex[k] * A2.a[k][j];
+        gw += Y.a[i][k] * X.a[k][j];
+        gd += V.a[i][k] * dx[k] * Rm.a[k][j];
       }
-      X.a[i][j] = V.a[i][j] - a5;
-      Tm.a[i][j] = V.a[i][j] * ex[j] - a3;
-      Rm.a[i][j] = Y.a[i][j] - a6;
+      A.a[i][j] = Um.a[i][j] + gw;
+      Um.a[i][j] = Um.a[i][j] * dx[j] + gw;
+      Rn.a[i][j] = Y.a[i][j] * dx[j] + gd * ex[j];
     }
-  if (!mat_invert(nZ, X)) return false;    // (Gm - A5)^-1
-  Mat<NZ, T> tmp;
-  mat_mul(nZ, Tm, X, tmp);
-  mat_mul(nZ, Rm, X, V);
+  if (!mat_invert(nZ, A)) return false;    // GA^-1
+  mat_mul(nZ, Um, A, X);
+  mat_mul(nZ, Rn, A, V);
   for (int i = 0; i < nZ; i++)
-    for (int j = 0; j < nZ; j++) { Tm.a[i][j] = tmp.a[i][j]; Rm.a[i][j] = V.a[i][j]; }
+    for (int j = 0; j < nZ; j++) { Um.a[i][j] = X.a[i][j]; Rm.a[i][j] = V.a[i][j]; }
+  // source (1 - row sum of T + R) B over the quadrature columns (and T's
+  // diagonal on the sensor row) = (row sum of U - row sum of R) B
   for (int i = 0; i < nZ; i++) {
-    T th = T(0.0);
-    for (int j = 0; j < nS; j++) th += Tm.a[i][j] + Rm.a[i][j];
-    if (i == nZ - 1 && nZ == nS + 1) th += Tm.a[i][i];
-    src[i] = (T(1.0) - th) * B;
+    T a = T(0.0);
+    for (int j = 0; j < nS; j++) a += Um.a[i][j] - Rm.a[i][j];
+    if (sensor_row && i == nZ - 1) a += Um.a[i][i];
+    src[i] = a * B;
   }
+  return true;
+}
+
+// ada_layer_loss with the transmission T = I - U.
+template <int NZ, class T>
+CRTM_HD bool ada_layer(int nS, int nZ, T w, T tau, const T* mu, const T* wt, const Mat<NZ, T>& ff,
+                       const Mat<NZ, T>& bb, T B, Mat<NZ, T>& Tm, Mat<NZ, T>& Rm, T* src, double* gap = nullptr) {
+  if (!ada_layer_loss<NZ, T>(nS, nZ, w, tau, mu, wt, ff, bb, B, Tm, Rm, src, gap)) return false;
+  for (int i = 0; i < nZ; i++)
+    for (int j = 0; j < nZ; j++) Tm.a[i][j] = (i == j ? T(1.0) : T(0.0)) - Tm.a[i][j];
   return true;
 }
 
@@ -921,9 +947,7 @@ CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const Stre
   }
   *od_out = T(od);
   if (!(ssa > BS_THRESHOLD)) return 0;
-  // Phase blocks and MOM in S (FP64 values in every form: MOM's inversions
-  // and eigenvectors lose accuracy in FP32 for thick, highly scattering
-  // layers).  Only the stored layer record is in T.
+  // Phase blocks and MOM in S; the stored layer record is in T.
   Mat<NZ, S> ff, bb, Td, Rd;
   S mu[NZ], wt[NZ], P[NZ][SC_NLEG_MAX + 1], srcd[NZ];
   for (int i = 0; i < St.nZ; i++) {
@@ -941,7 +965,17 @@ CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const Stre
     for (int i = 0; i < St.nZ; i++)
       for (int j = 0; j < St.nZ; j++) mx = fabs(ff.a[i][j]) > mx ? fabs(ff.a[i][j]) : mx;
     if (!(mx > 0.0)) return 0;
-    if (!ada_layer<NZ, S>(St.nS, St.nZ, ssa, od, mu, wt, ff, bb, B, Td, Rd, srcd, gap)) return -5;
+    // loss form U = I - T: the record's T = I - U is formed in the record's
+    // type, so a layer solved in FP32 keeps its relative precision in FP64 records
+    if (!ada_layer_loss<NZ, S>(St.nS, St.nZ, ssa, od, mu, wt, ff, bb, B, Td, Rd, srcd, gap)) return -5;
+    for (int i = 0; i < St.nZ; i++) {
+      src[i] = T(srcd[i]);
+      for (int j = 0; j < St.nZ; j++) {
+        Tm.a[i][j] = (i == j ? T(1.0) : T(0.0)) - T(Td.a[i][j]);
+        Rm.a[i][j] = T(Rd.a[i][j]);
+      }
+    }
+    return 1;
   }
   for (int i = 0; i < St.nZ; i++) {
     src[i] = T(srcd[i]);

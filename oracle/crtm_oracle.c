@@ -1066,6 +1066,7 @@ int or_profile_state(const or_handle* h, const or_batch* b, int m, double* T, do
 
 /* ---- scattering (clouds, ADA) ------------------------------------------- */
 #include "oracle_scatter.inc"
+#include "oracle_scatter_k.inc"
 
 /* ---- CRTM_Atmosphere_AddLayers for one profile -----------------------------
  * src/Atmosphere/CRTM_Atmosphere.f90:248-400 with Extra_Layers :1043-1050,

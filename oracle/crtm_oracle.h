@@ -126,6 +126,19 @@ void or_aerosol_destroy(or_aerosol* a);
 int or_forward_scatter(const or_handle* h, const or_cloud* cc, const or_aerosol* ca, const or_batch* b,
                        const or_clouds* cl, double* radiance, double* bt, int n_threads);
 
+/* K-matrix of a batch with clouds and aerosols through ADA (reverse mode of
+ * CRTM_ADA_AD / MOM_AD and the scattering, combine and LUT adjoints), with the
+ * clear-sky gas chain; outputs as or_k_matrix plus the cloud water content
+ * and effective radius Jacobians [P][L][NC][Kmax] and the aerosol
+ * concentration and first-coordinate Jacobians [P][L][NA][Kmax] (NULL: not
+ * returned).  Profiles on SOI, or fractional ones whose total cloud cover is
+ * not 1, are refused. */
+int or_k_matrix_scatter(const or_handle* h, const or_cloud* cc, const or_aerosol* ca, const or_batch* b,
+                        const or_clouds* cl, const double* bt_k, double* radiance, double* bt,
+                        double* temperature_k, double* absorber_k, double* water_temperature_k,
+                        double* surface_emissivity_k, double* wc_k, double* re_k, double* ac_k, double* ar_k,
+                        int n_threads);
+
 /* ---- IR sea-surface emissivity (CRTM_IRSSEM) ------------------------------ */
 typedef struct or_irwater_s or_irwater;
 /* Load an IRwaterCoeff binary file (Release 4). */

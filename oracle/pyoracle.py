@@ -43,7 +43,8 @@ class OrClouds(ct.Structure):
 
 
 def build(force: bool = False) -> str:
-    srcs = [os.path.join(HERE, f) for f in ("crtm_oracle.c", "crtm_oracle.h", "oracle_scatter.inc")]
+    srcs = [os.path.join(HERE, f) for f in ("crtm_oracle.c", "crtm_oracle.h", "oracle_scatter.inc",
+                                             "oracle_scatter_k.inc")]
     if force or not os.path.exists(LIB) or any(os.path.getmtime(LIB) < os.path.getmtime(f) for f in srcs):
         subprocess.run(["make", "-C", HERE, "-B", "liboracle.so"], check=True,
                        stdout=subprocess.DEVNULL)
@@ -75,6 +76,8 @@ def lib():
         L.or_cloud_destroy.argtypes = [ct.c_void_p]
         L.or_forward_scatter.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.POINTER(OrBatch),
                                          ct.POINTER(OrClouds), _dp, _dp, ct.c_int]
+        L.or_k_matrix_scatter.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.POINTER(OrBatch),
+                                          ct.POINTER(OrClouds)] + [_dp] * 11 + [ct.c_int]
         L.or_aerosol_init.restype = ct.c_void_p
         L.or_aerosol_init.argtypes = [ct.c_char_p]
         L.or_aerosol_init_scheme.restype = ct.c_void_p
@@ -185,6 +188,59 @@ class Oracle:
             raise RuntimeError(lib().or_last_error().decode())
         return dict(radiance=rad, bt=bt, temperature_ad=ta, absorber_ad=aa, water_temperature_ad=wa)
 
+    @staticmethod
+    def _clouds(atm, opt, keep):
+        """The or_clouds structure of a batch (arrays kept alive in ``keep``)."""
+        P = atm.n_profiles
+        c = OrClouds()
+
+        def arr(a, dt=np.float64):
+            a = np.ascontiguousarray(a, dt)
+            keep.append(a)
+            return a
+        if atm.cloud_type is not None and atm.cloud_type.shape[1] > 0:
+            c.max_clouds = int(atm.cloud_type.shape[1])
+            c.n_clouds = _p(arr(atm.n_clouds, np.int32), _ip)
+            c.cloud_type = _p(arr(atm.cloud_type, np.int32), _ip)
+            c.water_content = _p(arr(atm.cloud_water_content))
+            c.effective_radius = _p(arr(atm.cloud_effective_radius))
+        if atm.aerosol_type is not None and atm.aerosol_type.shape[1] > 0:
+            c.max_aerosols = int(atm.aerosol_type.shape[1])
+            c.n_aerosols = _p(arr(atm.n_aerosols, np.int32), _ip)
+            c.aerosol_type = _p(arr(atm.aerosol_type, np.int32), _ip)
+            c.aerosol_concentration = _p(arr(atm.aerosol_concentration))
+            c.aerosol_effective_radius = _p(arr(atm.aerosol_effective_radius))
+            if getattr(atm, "aerosol_effective_variance", None) is not None:
+                c.aerosol_effective_variance = _p(arr(atm.aerosol_effective_variance))
+            if getattr(atm, "relative_humidity", None) is not None:
+                c.relative_humidity = _p(arr(atm.relative_humidity))
+        if opt.n_streams is not None:
+            use = opt.use_n_streams if opt.use_n_streams is not None else np.ones(P, bool)
+            c.n_streams = _p(arr(np.where(use, opt.n_streams, 0), np.int32), _ip)
+        if opt.rt_algorithm_id is not None:
+            c.rt_algorithm = _p(arr(opt.rt_algorithm_id, np.int32), _ip)
+        if c.max_clouds > 0 and atm.cloud_fraction is not None:
+            c.cloud_fraction = _p(arr(atm.cloud_fraction))
+        if getattr(opt, "overlap_id", None) is not None:
+            c.overlap = _p(arr(opt.overlap_id, np.int32), _ip)
+        return c
+
+    @staticmethod
+    def _luts(cloudcoeff_path, aerosolcoeff_path, aerosol_scheme):
+        L = lib()
+        ch = ah = None
+        if cloudcoeff_path:
+            ch = L.or_cloud_init(cloudcoeff_path.encode())
+            if not ch:
+                raise IOError(L.or_last_error().decode())
+        if aerosolcoeff_path:
+            ah = L.or_aerosol_init_scheme(aerosolcoeff_path.encode(), aerosol_scheme.encode())
+            if not ah:
+                if ch:
+                    L.or_cloud_destroy(ch)
+                raise IOError(L.or_last_error().decode())
+        return ch, ah
+
     def forward_scatter(self, atm, sfc, geo, opt, cloudcoeff_path: Optional[str] = None,
                         aerosolcoeff_path: Optional[str] = None, n_threads: int = 1,
                         aerosol_scheme: str = "CRTM"):
@@ -192,54 +248,60 @@ class Oracle:
         profiles without either take the Emission solver.  aerosol_scheme is
         CRTM_Init's Aerosol_Model for the AerosolCoeff file."""
         L = lib()
-        ch = ah = None
+        ch, ah = self._luts(cloudcoeff_path, aerosolcoeff_path, aerosol_scheme)
         try:
-            if cloudcoeff_path:
-                ch = L.or_cloud_init(cloudcoeff_path.encode())
-                if not ch:
-                    raise IOError(L.or_last_error().decode())
-            if aerosolcoeff_path:
-                ah = L.or_aerosol_init_scheme(aerosolcoeff_path.encode(), aerosol_scheme.encode())
-                if not ah:
-                    raise IOError(L.or_last_error().decode())
             P, nL = atm.n_profiles, self.n_channels
             b, keep = self._batch(atm, sfc, geo, opt)
-            c = OrClouds()
-
-            def arr(a, dt=np.float64):
-                a = np.ascontiguousarray(a, dt)
-                keep.append(a)
-                return a
-            if atm.cloud_type is not None and atm.cloud_type.shape[1] > 0:
-                c.max_clouds = int(atm.cloud_type.shape[1])
-                c.n_clouds = _p(arr(atm.n_clouds, np.int32), _ip)
-                c.cloud_type = _p(arr(atm.cloud_type, np.int32), _ip)
-                c.water_content = _p(arr(atm.cloud_water_content))
-                c.effective_radius = _p(arr(atm.cloud_effective_radius))
-            if atm.aerosol_type is not None and atm.aerosol_type.shape[1] > 0:
-                c.max_aerosols = int(atm.aerosol_type.shape[1])
-                c.n_aerosols = _p(arr(atm.n_aerosols, np.int32), _ip)
-                c.aerosol_type = _p(arr(atm.aerosol_type, np.int32), _ip)
-                c.aerosol_concentration = _p(arr(atm.aerosol_concentration))
-                c.aerosol_effective_radius = _p(arr(atm.aerosol_effective_radius))
-                if getattr(atm, "aerosol_effective_variance", None) is not None:
-                    c.aerosol_effective_variance = _p(arr(atm.aerosol_effective_variance))
-                if getattr(atm, "relative_humidity", None) is not None:
-                    c.relative_humidity = _p(arr(atm.relative_humidity))
-            if opt.n_streams is not None:
-                use = opt.use_n_streams if opt.use_n_streams is not None else np.ones(P, bool)
-                c.n_streams = _p(arr(np.where(use, opt.n_streams, 0), np.int32), _ip)
-            if opt.rt_algorithm_id is not None:
-                c.rt_algorithm = _p(arr(opt.rt_algorithm_id, np.int32), _ip)
-            if c.max_clouds > 0 and atm.cloud_fraction is not None:
-                c.cloud_fraction = _p(arr(atm.cloud_fraction))
-            if getattr(opt, "overlap_id", None) is not None:
-                c.overlap = _p(arr(opt.overlap_id, np.int32), _ip)
+            c = self._clouds(atm, opt, keep)
             rad, bt = np.zeros((P, nL)), np.zeros((P, nL))
             st = L.or_forward_scatter(self.h, ch, ah, ct.byref(b), ct.byref(c), _p(rad), _p(bt), n_threads)
             if st:
                 raise RuntimeError(L.or_last_error().decode())
             return rad, bt
+        finally:
+            if ch:
+                L.or_cloud_destroy(ch)
+            if ah:
+                L.or_aerosol_destroy(ah)
+
+    def k_matrix_scatter(self, atm, sfc, geo, opt, cloudcoeff_path: Optional[str] = None,
+                         aerosolcoeff_path: Optional[str] = None, bt_k=None, n_threads: int = 1,
+                         aerosol_scheme: str = "CRTM", k_absorbers=None):
+        """K-matrix of a batch with clouds and aerosols through ADA (the
+        oracle's reverse mode of the reference's ADA, MOM, phase, combine and
+        LUT adjoints), dict with the clear-sky K-matrix keys plus
+        cloud_water_content_k, cloud_effective_radius_k [P][L][NC][Kmax] and
+        aerosol_concentration_k, aerosol_effective_radius_k [P][L][NA][Kmax]
+        (the latter: relative humidity for 'GOCART-GEOS5' / 'NAAPS')."""
+        L = lib()
+        ch, ah = self._luts(cloudcoeff_path, aerosolcoeff_path, aerosol_scheme)
+        try:
+            P, nL, K, J = atm.n_profiles, self.n_channels, atm.max_layers, atm.n_absorbers
+            b, keep = self._batch(atm, sfc, geo, opt)
+            if k_absorbers is not None:
+                mask = np.zeros(J, np.int32)
+                mask[np.asarray(k_absorbers, int)] = 1
+                keep.append(mask)
+                b.k_absorber_mask = _p(mask, _ip)
+            c = self._clouds(atm, opt, keep)
+            NC, NA = max(c.max_clouds, 0), max(c.max_aerosols, 0)
+            seed = None if bt_k is None else np.ascontiguousarray(bt_k, np.float64)
+            o = dict(radiance=np.zeros((P, nL)), bt=np.zeros((P, nL)), temperature_k=np.zeros((P, nL, K)),
+                     absorber_k=np.zeros((P, nL, J, K)), water_temperature_k=np.zeros((P, nL)),
+                     surface_emissivity_k=np.zeros((P, nL)),
+                     cloud_water_content_k=np.zeros((P, nL, NC, K)), cloud_effective_radius_k=np.zeros((P, nL, NC, K)),
+                     aerosol_concentration_k=np.zeros((P, nL, NA, K)),
+                     aerosol_effective_radius_k=np.zeros((P, nL, NA, K)))
+            st = L.or_k_matrix_scatter(self.h, ch, ah, ct.byref(b), ct.byref(c), _p(seed), _p(o["radiance"]),
+                                       _p(o["bt"]), _p(o["temperature_k"]), _p(o["absorber_k"]),
+                                       _p(o["water_temperature_k"]), _p(o["surface_emissivity_k"]),
+                                       _p(o["cloud_water_content_k"]) if NC else None,
+                                       _p(o["cloud_effective_radius_k"]) if NC else None,
+                                       _p(o["aerosol_concentration_k"]) if NA else None,
+                                       _p(o["aerosol_effective_radius_k"]) if NA else None, n_threads)
+            if st:
+                raise RuntimeError(L.or_last_error().decode())
+            return o
         finally:
             if ch:
                 L.or_cloud_destroy(ch)

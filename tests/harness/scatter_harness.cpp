@@ -18,10 +18,12 @@ GaussTable make_gauss() {
 // row absorptance is below g_fp64_absorptance (0: none)
 static double g_fp64_absorptance = 0.0;
 static long g_fp64_layers = 0, g_all_layers = 0;
+static int g_fp32_layer = -1;   // >= 0: only that layer in FP32
 
 extern "C" {
 
 void sx_set_fp64_absorptance(double a) { g_fp64_absorptance = a; g_fp64_layers = g_all_layers = 0; }
+void sx_set_fp32_layer(int k) { g_fp32_layer = k; }
 double sx_fp64_fraction() { return g_all_layers ? (double)g_fp64_layers / g_all_layers : 0.0; }
 
 int sx_ada_layer(int nS, int nZ, double w, double tau, const double* mu, const double* wt,
@@ -110,7 +112,7 @@ int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, 
       int kind;
       if (soi == 3)
         kind = layer_optics<NZ, double, DD>(c, L, S, k, DD(od[k]), DD(temp[k]), &o, Tm, Rm, srcv);
-      else if (soi == 4) {
+      else if (soi == 4 && (g_fp32_layer < 0 || g_fp32_layer == k)) {
         kind = layer_optics<NZ, double, float>(c, L, S, k, float(od[k]), float(temp[k]), &o, Tm, Rm, srcv);
         if (kind == 1 && g_fp64_absorptance > 0.0) {
           double amin = 1.0;

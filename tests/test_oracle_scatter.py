@@ -252,3 +252,75 @@ def test_cloud_fraction_thresholds(coeff_dir, cloud_path):
     opt.overlap_id = np.array([4, 9, 4], np.int32)
     with pytest.raises(RuntimeError, match="Overlap"):
         orc.forward_scatter(atm, sfc, geo, opt, cloud_path)
+
+
+@pytest.mark.parametrize("sensor,n_streams,aer", [("irsynth_c616", None, True), ("mwsynth_c22", None, False),
+                                                  ("irsynth_c616", 16, True), ("mwsynth_c16", 8, False)])
+def test_oracle_cloudy_kmatrix_matches_central_differences(coeff_dir, sensor, n_streams, aer):
+    """The oracle's cloudy K-matrix (reverse mode of the ADA adding, MOM,
+    phase normalisation, combine and LUT interpolation) against central
+    differences of the oracle's own cloudy forward, for the temperature
+    (1e-3 K), every absorber, each cloud's water content and effective
+    radius, each aerosol's concentration and radius (1e-4 relative steps)
+    and the surface temperature: within 2e-6 of each variable's largest
+    Jacobian (the differences' truncation and rounding)."""
+    import copy
+
+    from oracle.pyoracle import Oracle
+    sy.write_sensor_files(coeff_dir, sensor)
+    cp, ap = sy.write_cloud_files(coeff_dir), sy.write_aerosol_files(coeff_dir)
+    mw = sensor.startswith("mw")
+    types = ((co.WATER_CLOUD, co.ICE_CLOUD, co.RAIN_CLOUD, co.SNOW_CLOUD, co.GRAUPEL_CLOUD) if mw
+             else (co.WATER_CLOUD, co.ICE_CLOUD))
+    atm, sfc, geo, opt = sy.cloudy_workload(sensor, 1, 60, 11, cloud_types=types, wc_scale=10.0,
+                                            n_streams=n_streams)
+    if aer:
+        sy.add_aerosols(atm, sy.AEROSOL_TYPES, 12, load_scale=10.0)
+    o = Oracle(coeff_dir, sensor)
+    K = o.k_matrix_scatter(atm, sfc, geo, opt, cp, ap if aer else None, n_threads=8)
+
+    def bt(a, s=sfc):
+        return o.forward_scatter(a, s, geo, opt, cp, ap if aer else None, n_threads=8)[1]
+    assert np.array_equal(bt(atm), K["bt"])
+
+    def fd(field, idx, h, rel=True):
+        a1, a2 = copy.deepcopy(atm), copy.deepcopy(atm)
+        hh = h * abs(getattr(a1, field)[idx]) if rel else h
+        getattr(a1, field)[idx] += hh
+        getattr(a2, field)[idx] -= hh
+        return (bt(a1) - bt(a2)) / (2 * hh)
+
+    def check(name, got, want, scale):
+        assert np.abs(got - want).max() <= 2e-6 * scale, (name, np.abs(got - want).max() / scale)
+    m, tol_checked = 0, 0
+    Ku = int(atm.n_layers[m])
+    wc = atm.cloud_water_content
+    cloudy = np.where((wc[m] > 1e-6).any(axis=0))[0]
+    for k in [cloudy[0], cloudy[len(cloudy) // 2], Ku - 1]:
+        check("T", fd("temperature", (m, k), 1e-3, rel=False)[m], K["temperature_k"][m, :, k],
+              np.abs(K["temperature_k"][m]).max())
+        for j in range(min(atm.n_absorbers, 2)):
+            check(f"absorber {j}", fd("absorber", (m, j, k), 1e-4)[m], K["absorber_k"][m, :, j, k],
+                  np.abs(K["absorber_k"][m, :, j]).max() * 3.0)
+        for c in range(wc.shape[1]):
+            if not wc[m, c, k] > 1e-6:
+                assert not K["cloud_water_content_k"][m, :, c, k].any()
+                continue
+            for f, kf in (("cloud_water_content", "cloud_water_content_k"),
+                          ("cloud_effective_radius", "cloud_effective_radius_k")):
+                x = getattr(atm, f)
+                check(f, fd(f, (m, c, k), 1e-4)[m] * x[m, c, k], K[kf][m, :, c, k] * x[m, c, k],
+                      np.abs(K[kf][m, :, c] * x[m, c]).max())
+                tol_checked += 1
+        for a in (range(3) if aer and k == cloudy[0] else ()):
+            for f, kf in (("aerosol_concentration", "aerosol_concentration_k"),
+                          ("aerosol_effective_radius", "aerosol_effective_radius_k")):
+                x = getattr(atm, f)
+                check(f, fd(f, (m, a, k), 1e-4)[m] * x[m, a, k], K[kf][m, :, a, k] * x[m, a, k],
+                      np.abs(K[kf][m, :, a] * x[m, a]).max())
+    s1, s2 = copy.deepcopy(sfc), copy.deepcopy(sfc)
+    s1.water_temperature[m] += 1e-3
+    s2.water_temperature[m] -= 1e-3
+    check("Ts", ((bt(atm, s1) - bt(atm, s2)) / 2e-3)[m], K["water_temperature_k"][m],
+          np.abs(K["water_temperature_k"][m]).max())
+    assert tol_checked >= 2
