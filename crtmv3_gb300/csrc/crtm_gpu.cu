@@ -814,11 +814,15 @@ int copy_chunk(crtm_gpu_handle h, const HostCopy* hc, int p0, int n, cudaStream_
 }
 
 // mode 0 forward, 1 K-matrix, 2 adjoint
+// perm: device array of the batch profiles the pipeline runs, in order
+// (b->n_profiles of them), or null for all of the batch's profiles in its
+// own order.  nz_max: scattering kernels for up to 16 streams (else the
+// stream rule's, up to 6).
 template <int G, class R>
 int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, int mode,
                  const double* seed, crtm_gpu_rtsolution* rts, crtm_gpu_kmatrix* kk,
                  crtm_gpu_adjoint_out* ad, cudaStream_t st, const HostCopy* hc,
-                 const FixedScratch* fixed, bool scat, const SfcModel* sm) {
+                 const FixedScratch* fixed, bool scat, const SfcModel* sm, const int* perm, bool nz_max) {
   const int P = b->n_profiles, Kmax = b->max_layers, L = s.L, K = s.K, n_abs = b->n_absorbers;
   if (P <= 0) return CRTM_GPU_SUCCESS;
   if (Kmax < 2 || Kmax > MAX_LAYERS) return fail(h, "max_layers %d out of range [2, %d]", Kmax, MAX_LAYERS);
@@ -848,8 +852,6 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
     for (int j = 0; j < n_abs; j++) oa.odps[j] = abs_of_user[j];
   }
   const int nv = 1 + oa.n;
-  // scattering: NZ angles of the kernels (16-stream option or the stream rule)
-  const bool nz_max = scat && b->n_streams != nullptr;
   const bool soi = scat && b->rt_algorithm_id != nullptr;
   // scattering Jacobian outputs that the caller asked for
   double* o_wc = nullptr, *o_re = nullptr, *o_cf = nullptr, *o_ac = nullptr, *o_ar = nullptr;
@@ -909,7 +911,8 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
   work_bytes<G, R>(s, chunk, Kmax, nv, mode, &w, ws_base, sw);
   if (cudaMemcpyAsync(w.idx_map, idx_map, sizeof(int) * s.Jm, cudaMemcpyHostToDevice, st) != cudaSuccess)
     return fail(h, "absorber map upload failed");
-  const BatchView bv = make_view(b);
+  BatchView bv = make_view(b);
+  bv.perm = perm;
   constexpr int NPF = Tune<G, R>::FWD, NPA = Tune<G, R>::AD;
   const size_t prep_smem = prep_smem_bytes<G>(K);
   const size_t col_smem = column_smem_bytes<R>(K, Kmax);
@@ -1066,24 +1069,28 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
             if (!o.o || !o.X || o.ns == 0) continue;
             if (mode == 1) {
               dim3 gt((L + 31) / 32, (Kmax + 31) / 32, std::min(n * o.ns, 65535));
-              species_k_out_kernel<<<gt, dim3(32, 8), 0, st>>>(o.X, o.S, o.s0, o.ns, Kmax, L, p0, n, o.o);
+              species_k_out_kernel<<<gt, dim3(32, 8), 0, st>>>(o.X, o.S, o.s0, o.ns, Kmax, L, p0, n, o.o,
+                                                               perm);
             } else {
               const long long rows = (long long)n * o.ns * Kmax;
               species_ad_out_kernel<<<(unsigned)((rows + 7) / 8), 256, 0, st>>>(o.X, o.S, o.s0, o.ns, Kmax, L,
-                                                                              p0, n, o.o);
+                                                                              p0, n, o.o, perm);
             }
             CK_LAUNCH(h);
           }
         }
         // outputs of a coordinate that the handle's aerosol scheme does not have: zero
         const size_t rows_k = mode == 1 ? (size_t)L * Kmax : (size_t)Kmax;
-        if (o_av && !sw.cv &&
-            cudaMemsetAsync(o_av + (size_t)p0 * NAb * rows_k, 0, (size_t)n * NAb * rows_k * sizeof(double), st) !=
-                cudaSuccess)
-          return fail(h, "output clear failed");
-        if (o_rh && !sw.ch &&
-            cudaMemsetAsync(o_rh + (size_t)p0 * rows_k, 0, (size_t)n * rows_k * sizeof(double), st) != cudaSuccess)
-          return fail(h, "output clear failed");
+        const auto clear_rows = [&](double* o, size_t row) {
+          if (perm) {
+            const size_t nel = (size_t)n * row;
+            zero_profile_rows_kernel<<<(unsigned)((nel + 255) / 256), 256, 0, st>>>(o, perm + p0, n, row);
+            return cudaGetLastError() == cudaSuccess;
+          }
+          return cudaMemsetAsync(o + (size_t)p0 * row, 0, (size_t)n * row * sizeof(double), st) == cudaSuccess;
+        };
+        if (o_av && !sw.cv && !clear_rows(o_av, NAb * rows_k)) return fail(h, "output clear failed");
+        if (o_rh && !sw.ch && !clear_rows(o_rh, rows_k)) return fail(h, "output clear failed");
       } else {
         StageScope sc(h, 7, st);
         if (nz_max)
@@ -1257,16 +1264,100 @@ int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, c
     sm.ev = E + PL;
     sm.et = h->irw.nalli2 ? E + 2 * PL : nullptr;
   }
-  int rc;
-  switch (s.group) {
-    case 1: rc = fp64 ? run_pipeline<1, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat, &sm)
-                      : run_pipeline<1, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat, &sm);
-            break;
-    case 2: rc = fp64 ? run_pipeline<2, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat, &sm)
-                      : run_pipeline<2, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat, &sm);
-            break;
-    default: rc = fp64 ? run_pipeline<3, double>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat, &sm)
-                       : run_pipeline<3, float>(h, s, b, mode, seed, rts, kk, ad, st, hc, fixed, scat, &sm);
+  auto run = [&](const crtm_gpu_batch* bb, int md, const HostCopy* hcc, const FixedScratch* fx, bool sc,
+                 const int* perm, bool nzm) {
+    switch (s.group) {
+      case 1: return fp64 ? run_pipeline<1, double>(h, s, bb, md, seed, rts, kk, ad, st, hcc, fx, sc, &sm, perm, nzm)
+                          : run_pipeline<1, float>(h, s, bb, md, seed, rts, kk, ad, st, hcc, fx, sc, &sm, perm, nzm);
+      case 2: return fp64 ? run_pipeline<2, double>(h, s, bb, md, seed, rts, kk, ad, st, hcc, fx, sc, &sm, perm, nzm)
+                          : run_pipeline<2, float>(h, s, bb, md, seed, rts, kk, ad, st, hcc, fx, sc, &sm, perm, nzm);
+      default: return fp64 ? run_pipeline<3, double>(h, s, bb, md, seed, rts, kk, ad, st, hcc, fx, sc, &sm, perm, nzm)
+                           : run_pipeline<3, float>(h, s, bb, md, seed, rts, kk, ad, st, hcc, fx, sc, &sm, perm, nzm);
+    }
+  };
+  int rc = CRTM_GPU_SUCCESS;
+  if (!scat || b->n_profiles <= 0) {
+    rc = run(b, mode, hc, fixed, scat, nullptr, scat && b->n_streams != nullptr);
+  } else {
+    // Buckets of a batch with clouds or aerosols: its clear profiles (the
+    // clear-sky pipeline), its cloudy ones on the stream rule or up to 6
+    // streams (kernels for 5 angles) and those with 8 or 16 streams (10
+    // angles), each run as its own pipeline, so that every chunk's
+    // scattering work space and grids hold only profiles that use them.  The
+    // profile counts, clouds and stream options are read back to the host
+    // first (the call waits for the stream to reach this point).
+    const int P = b->n_profiles;
+    std::vector<int> nc(P, 0), na(P, 0), ns(P, 0);
+    bool ok = true;
+    if (b->max_clouds > 0)
+      ok &= cudaMemcpyAsync(nc.data(), b->n_clouds, sizeof(int) * P, cudaMemcpyDeviceToHost, st) == cudaSuccess;
+    if (b->max_aerosols > 0)
+      ok &= cudaMemcpyAsync(na.data(), b->n_aerosols, sizeof(int) * P, cudaMemcpyDeviceToHost, st) == cudaSuccess;
+    if (b->n_streams)
+      ok &= cudaMemcpyAsync(ns.data(), b->n_streams, sizeof(int) * P, cudaMemcpyDeviceToHost, st) == cudaSuccess;
+    if (!ok || cudaStreamSynchronize(st) != cudaSuccess) return fail(h, "reading the batch's cloud counts failed");
+    int cnt[3] = {0, 0, 0};
+    std::vector<int> cls(P);
+    for (int p = 0; p < P; p++) {
+      cls[p] = (nc[p] > 0 || na[p] > 0) ? (ns[p] > 6 ? 2 : 1) : 0;
+      cnt[cls[p]]++;
+    }
+    const int start[3] = {0, cnt[0], cnt[0] + cnt[1]};
+    const int n_buckets = (cnt[0] > 0) + (cnt[1] > 0) + (cnt[2] > 0);
+    const int* dperm = nullptr;
+    FixedScratch fx_rest{};
+    if (n_buckets > 1) {   // the profiles in bucket order (stable)
+      std::vector<int> perm(P);
+      int pos[3] = {start[0], start[1], start[2]};
+      for (int p = 0; p < P; p++) perm[pos[cls[p]]++] = p;
+      const size_t pb = ((size_t)P * sizeof(int) + 255) & ~(size_t)255;
+      int* dp;
+      if (fixed) {
+        if (pb >= fixed->bytes) return fail(h, "the profile order of %d profiles does not fit the static scratch", P);
+        dp = (int*)fixed->base;
+        fx_rest = FixedScratch{fixed->base + pb, fixed->bytes - pb};
+        fixed = &fx_rest;
+      } else {
+        if (!h->small.ensure(pb)) return fail(h, "cannot allocate the profile order");
+        dp = (int*)h->small.p;
+      }
+      if (cudaMemcpyAsync(dp, perm.data(), sizeof(int) * P, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return fail(h, "profile order upload failed");
+      dperm = dp;
+    }
+    for (int c = 0; c < 3 && rc == CRTM_GPU_SUCCESS; c++) {
+      if (!cnt[c]) continue;
+      crtm_gpu_batch bc = *b;
+      bc.n_profiles = cnt[c];
+      rc = run(&bc, c == 0 && mode == 3 ? 0 : mode, dperm ? nullptr : hc, fixed, c != 0,
+               dperm ? dperm + start[c] : nullptr, c == 2);
+    }
+    // the scattering Jacobians of the clear profiles are zero
+    if (rc == CRTM_GPU_SUCCESS && cnt[0] > 0 && (mode == 1 || mode == 2)) {
+      const int NCb = b->max_clouds > 0 ? b->max_clouds : 0, NAb = b->max_aerosols > 0 ? b->max_aerosols : 0;
+      const size_t lead = mode == 1 ? (size_t)s.L * b->max_layers : (size_t)b->max_layers;
+      double* const outs[7] = {
+          mode == 1 ? kk->cloud_water_content : ad->cloud_water_content,
+          mode == 1 ? kk->cloud_effective_radius : ad->cloud_effective_radius,
+          mode == 1 ? kk->cloud_fraction : ad->cloud_fraction,
+          mode == 1 ? kk->aerosol_concentration : ad->aerosol_concentration,
+          mode == 1 ? kk->aerosol_effective_radius : ad->aerosol_effective_radius,
+          mode == 1 ? kk->aerosol_effective_variance : ad->aerosol_effective_variance,
+          mode == 1 ? kk->relative_humidity : ad->relative_humidity};
+      const size_t rows[7] = {lead * NCb, lead * NCb, NCb ? lead : 0, lead * NAb, lead * NAb, lead * NAb,
+                              NAb ? lead : 0};
+      for (int i = 0; i < 7; i++) {
+        if (!outs[i] || !rows[i]) continue;
+        if (dperm) {
+          const size_t nel = (size_t)cnt[0] * rows[i];
+          zero_profile_rows_kernel<<<(unsigned)((nel + 255) / 256), 256, 0, st>>>(outs[i], dperm, cnt[0], rows[i]);
+          CK_LAUNCH(h);
+        } else if (cudaMemsetAsync(outs[i], 0, (size_t)P * rows[i] * sizeof(double), st) != cudaSuccess) {
+          rc = fail(h, "output clear failed");
+        }
+      }
+    }
+    if (rc == CRTM_GPU_SUCCESS && dperm && hc && hc->n) rc = copy_chunk(h, hc, 0, P, st);
   }
   mark_done(h, st);
   return rc;

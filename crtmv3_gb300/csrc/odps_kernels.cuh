@@ -217,7 +217,15 @@ struct BatchView {
   const double* zenith;
   const double* altitude;
   const double* emissivity;
+  // Profile order of the pipeline: chunk position i (p_begin + p) is batch
+  // profile perm[i]; null for the batch's own order.  The pipeline runs the
+  // profiles of one bucket (clear, cloudy with up to 6 streams, cloudy with
+  // 8-16 streams) at a time.
+  const int* perm = nullptr;
 };
+
+// Batch profile of pipeline position i.
+CRTM_HD int batch_profile(const BatchView& b, int i) { return b.perm ? b.perm[i] : i; }
 
 struct SpecView {
   const double* c1, *c2, *b1, *b2, *cbr;
@@ -270,7 +278,7 @@ __global__ void __launch_bounds__(32) prep_kernel(SensorTables S, RefSums RS, Ba
   const int lane = threadIdx.x;
   const int p = blockIdx.x;
   if (p >= n_chunk) return;
-  const int gp = p_begin + p;
+  const int gp = batch_profile(b, p_begin + p);
   const int K = S.K, Kmax = pv.Kmax;
   const int Ku = b.n_layers[gp];
   if (Ku < 2 || Ku > Kmax || Ku > MAX_LAYERS) {
@@ -636,7 +644,7 @@ template <class R>
 __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int K = a.K, L = a.L, Kmax = a.Kmax;
-  const int p = blockIdx.y, gp = a.p_begin + p;
+  const int p = blockIdx.y, gp = batch_profile(a.b, a.p_begin + p);
   const int tid = threadIdx.x;
   const int l = blockIdx.x * blockDim.x + tid;
   // interpolation factors in R, converted once per CTA (the slot is sized for doubles)
@@ -1023,7 +1031,7 @@ __global__ void __launch_bounds__(256) map_kernel(MapArgs<R> m) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int K = m.K, L = m.L, Kmax = m.Kmax, nv = m.nv, CT = m.ct, CS = m.ct + 1;
   const int cshift = __ffs(CT) - 1;   // CT is a power of two
-  const int p = blockIdx.y, gp = m.p_begin + p;
+  const int p = blockIdx.y, gp = batch_profile(m.b, m.p_begin + p);
   const int l0 = blockIdx.x * CT;
   const int tid = threadIdx.x, wib = tid >> 5, lane = tid & 31;
   R* rat = reinterpret_cast<R*>(smem_raw);        // [nv][K][CS]
@@ -1126,7 +1134,7 @@ __global__ void adjoint_map_kernel(AdjMapArgs<R> m) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)m.n_chunk * m.Kmax) return;
   const int p = (int)(idx / m.Kmax), ku = (int)(idx % m.Kmax);
-  const int gp = m.p_begin + p;
+  const int gp = batch_profile(m.b, m.p_begin + p);
   const int K = m.K, Kmax = m.Kmax, nv = m.nv;
   const int Ku = m.pv.status[p] ? 0 : m.b.n_layers[gp];
   if (ku == 0) {

@@ -124,7 +124,7 @@ template <class R>
 __global__ void scatter_profile_kernel(ScatterArgs<R> a) {
   const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (p >= a.n_chunk) return;
-  const int gp = a.p_begin + p, Ku = a.b.n_layers[gp];
+  const int gp = batch_profile(a.b, a.p_begin + p), Ku = a.b.n_layers[gp];
   const int nc = a.max_clouds > 0 ? a.n_clouds[gp] : 0, na = a.max_aerosols > 0 ? a.n_aerosols[gp] : 0;
   const double* cf = a.cloud_fraction ? a.cloud_fraction + (size_t)gp * a.Kmax : nullptr;
   double mr = 0.0;
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_layers_kernel(Scatter
   const int l = (int)(idx % L);
   const int k = (int)((idx / L) % Kmax);
   const int p = (int)(idx / ((long long)L * Kmax));
-  const int gp = a.p_begin + p;
+  const int gp = batch_profile(a.b, a.p_begin + p);
   if (a.pv.status[p] != 0 || k >= a.b.n_layers[gp]) return;
   Rec* rec = LBr + ((size_t)p * Kmax + k) * NE * L + l;
   const CloudyColumn c = column_inputs(a, p, gp, l);
@@ -253,7 +253,7 @@ template <int NZ, class R>
 __global__ void __launch_bounds__(SCATTER_THREADS) scatter_adding_kernel(ScatterArgs<R> a) {
   constexpr int NE = layer_record<NZ>();
   const int L = a.L, Kmax = a.Kmax;
-  const int p = blockIdx.y, gp = a.p_begin + p;
+  const int p = blockIdx.y, gp = batch_profile(a.b, a.p_begin + p);
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (l >= L) return;
   const size_t pl = (size_t)gp * L + l;
@@ -318,7 +318,7 @@ template <int NZ, class R>
 __global__ void __launch_bounds__(SCATTER_THREADS) scatter_soi_kernel(ScatterArgs<R> a) {
   constexpr int NE = layer_record<NZ>();
   const int L = a.L, Kmax = a.Kmax;
-  const int p = blockIdx.y, gp = a.p_begin + p;
+  const int p = blockIdx.y, gp = batch_profile(a.b, a.p_begin + p);
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (l >= L || a.pv.status[p] != 0) return;
   const CloudyColumn c = column_inputs(a, p, gp, l);
@@ -372,7 +372,7 @@ template <int NZ, class R>
 __global__ void __launch_bounds__(SCATTER_THREADS) scatter_kmatrix_kernel(ScatterArgs<R> a) {
   constexpr int NE = layer_record<NZ>(), NS = adding_state_size<NZ>();
   const int L = a.L, Kmax = a.Kmax;
-  const int p = blockIdx.y, gp = a.p_begin + p;
+  const int p = blockIdx.y, gp = batch_profile(a.b, a.p_begin + p);
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (l >= L || a.pv.status[p] != 0) return;
   const CloudyColumn c = column_inputs(a, p, gp, l);
@@ -440,7 +440,7 @@ template <int NZ>
 __global__ void __launch_bounds__(SCATTER_THREADS) scatter_soi_k_kernel(ScatterArgs<double> a) {
   constexpr int NE = layer_record<NZ>();
   const int L = a.L, Kmax = a.Kmax;
-  const int p = blockIdx.y, gp = a.p_begin + p;
+  const int p = blockIdx.y, gp = batch_profile(a.b, a.p_begin + p);
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (l >= L || a.pv.status[p] != 0) return;
   const CloudyColumn c = column_inputs(a, p, gp, l);
@@ -519,7 +519,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_contract_kernel(Scatt
   const int l = (int)(idx % L);
   const int k = (int)((idx / L) % Kmax);
   const int p = (int)(idx / ((long long)L * Kmax));
-  const int gp = a.p_begin + p;
+  const int gp = batch_profile(a.b, a.p_begin + p);
   if (a.pv.status[p] != 0 || k >= a.b.n_layers[gp]) return;
   const CloudyColumn c = column_inputs(a, p, gp, l);
   if (c.n_clouds == 0 && c.n_aerosols == 0) return;
@@ -610,7 +610,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_reverse_kernel(Scatte
   const int l = (int)(idx % L);
   const int k = (int)((idx / L) % Kmax);
   const int p = (int)(idx / ((long long)L * Kmax));
-  const int gp = a.p_begin + p;
+  const int gp = batch_profile(a.b, a.p_begin + p);
   if (a.pv.status[p] != 0 || k >= a.b.n_layers[gp]) return;
   const CloudyColumn c = column_inputs(a, p, gp, l);
   if (c.n_clouds == 0 && c.n_aerosols == 0) return;
@@ -677,7 +677,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_reverse_kernel(Scatte
 template <class R>
 __global__ void scatter_species_kernel(ScatterArgs<R> a) {
   const int L = a.L, Kmax = a.Kmax;
-  const int p = blockIdx.y, gp = a.p_begin + p;
+  const int p = blockIdx.y, gp = batch_profile(a.b, a.p_begin + p);
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (l >= L) return;
   const int Ku = a.b.n_layers[gp];
@@ -747,7 +747,7 @@ __global__ void scatter_species_kernel(ScatterArgs<R> a) {
 // K-matrix outputs of the species Jacobians: X[n][S][Kmax][L] slots s0..s0+ns-1
 // to out[P][L][ns][Kmax] (a shared-memory transpose of 32 x 32 tiles).
 static __global__ void species_k_out_kernel(const double* X, int S, int s0, int ns, int Kmax, int L, int p_begin,
-                                     int n, double* out) {
+                                     int n, double* out, const int* perm) {
   __shared__ double tile[32][33];
   const int k0 = blockIdx.y * 32, l0 = blockIdx.x * 32;
   for (int ps = blockIdx.z; ps < n * ns; ps += gridDim.z) {
@@ -761,7 +761,8 @@ static __global__ void species_k_out_kernel(const double* X, int S, int s0, int 
     __syncthreads();
     for (int i = threadIdx.y; i < 32; i += blockDim.y) {
       const int l = l0 + i, k = k0 + threadIdx.x;
-      if (l < L && k < Kmax) out[(((size_t)(p_begin + p) * L + l) * ns + s) * Kmax + k] = tile[threadIdx.x][i];
+      const size_t gp = perm ? perm[p_begin + p] : p_begin + p;
+      if (l < L && k < Kmax) out[((gp * L + l) * ns + s) * Kmax + k] = tile[threadIdx.x][i];
     }
   }
 }
@@ -769,7 +770,7 @@ static __global__ void species_k_out_kernel(const double* X, int S, int s0, int 
 // Adjoint outputs: out[P][ns][Kmax] = sum over channels of slots s0..s0+ns-1
 // (one warp per row, lanes over channels).
 static __global__ void species_ad_out_kernel(const double* X, int S, int s0, int ns, int Kmax, int L, int p_begin,
-                                      int n, double* out) {
+                                      int n, double* out, const int* perm) {
   const long long row = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (row >= (long long)n * ns * Kmax) return;
@@ -778,7 +779,16 @@ static __global__ void species_ad_out_kernel(const double* X, int S, int s0, int
   double acc = 0.0;
   for (int l = lane; l < L; l += 32) acc += in[l];
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL, acc, o);
-  if (lane == 0) out[((size_t)(p_begin + p) * ns + s) * Kmax + k] = acc;
+  const size_t gp = perm ? perm[p_begin + p] : p_begin + p;
+  if (lane == 0) out[(gp * ns + s) * Kmax + k] = acc;
+}
+
+// Zero rows of `row` doubles of out for the batch profiles perm[0..n-1] (the
+// scattering Jacobians of a bucket's clear profiles).
+static __global__ void zero_profile_rows_kernel(double* out, const int* perm, int n, size_t row) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)n * row) return;
+  out[(size_t)perm[i / row] * row + i % row] = 0.0;
 }
 
 }  // namespace crtm

@@ -73,3 +73,69 @@ def test_cloudy_k_matrix_matches_oracle(gpu_lib, cloud_dir, sensor, n_streams, a
         x = getattr(atm, field)[:, None]
         scale = max(np.abs(ref[key] * x).max(), 1e-300)
         assert np.abs((got - ref[key]) * x).max() <= tol * scale, field
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_ragged_batch_buckets_match_oracle(gpu_lib, cloud_dir, precision):
+    """A batch whose profiles alternate between clear, cloudy on the stream
+    rule and cloudy with Options%n_Streams 16: the library runs each bucket as
+    its own pipeline (clear-sky, 5-angle and 10-angle scattering kernels) in
+    the batch's buffers.  Every profile's outputs match the oracle, the clear
+    profiles' cloud Jacobians are zero, and the host entry point (outputs
+    copied back after all buckets) agrees with the device one."""
+    import torch
+    from oracle.pyoracle import Oracle
+    sensor = "irsynth_c616"
+    P = 6
+    atm, sfc, geo, opt = _case(sensor, None, False, 411, P=P, nl=90)
+    atm.n_clouds[[0, 3]] = 0
+    ns = np.array([0, 0, 16, 0, 0, 16], np.int32)
+    opt.use_n_streams, opt.n_streams = ns > 0, ns
+    h = gpu_lib.CRTM([sensor], cloud_dir, precision)
+    km, rts = h.k_matrix(atm, sfc, geo, opt)
+    ref = Oracle(cloud_dir, sensor).k_matrix_scatter(atm, sfc, geo, opt, f"{cloud_dir}/CloudCoeff.bin", None,
+                                                     n_threads=8)
+    assert (rts.status == 0).all()
+    assert np.abs(rts.brightness_temperature - ref["bt"]).max() < BT_TOL[precision]
+    tol = JAC_TOL[precision]
+    assert _rel(km.temperature, ref["temperature_k"]) < tol
+    assert _rel(km.water_temperature, ref["water_temperature_k"]) < tol
+    x = atm.cloud_water_content[:, None]
+    assert np.abs((km.cloud_water_content - ref["cloud_water_content_k"]) * x).max() <= \
+        tol * np.abs(ref["cloud_water_content_k"] * x).max()
+    for p in (0, 3):
+        assert not km.cloud_water_content[p].any() and not km.cloud_effective_radius[p].any()
+        assert not km.cloud_fraction[p].any()
+    # the device entry point on the same batch
+    dev = torch.device("cuda")
+    t = {}
+    for k in ("level_pressure", "pressure", "temperature", "absorber", "cloud_water_content",
+              "cloud_effective_radius", "cloud_fraction"):
+        t[k] = torch.from_numpy(np.ascontiguousarray(getattr(atm, k), np.float64)).to(dev)
+    for k in ("n_layers", "n_clouds", "cloud_type"):
+        t[k] = torch.from_numpy(np.ascontiguousarray(getattr(atm, k), np.int32)).to(dev)
+    for f in ("land_coverage", "water_coverage", "snow_coverage", "ice_coverage", "land_temperature",
+              "water_temperature", "snow_temperature", "ice_temperature"):
+        t[f] = torch.from_numpy(np.ascontiguousarray(getattr(sfc, f))).to(dev)
+    for f in ("sensor_zenith_angle", "source_zenith_angle", "surface_altitude"):
+        t[f] = torch.from_numpy(np.ascontiguousarray(getattr(geo, f))).to(dev)
+    t["emissivity"] = torch.from_numpy(np.ascontiguousarray(opt.emissivity)).to(dev)
+    t["n_streams"] = torch.from_numpy(ns).to(dev)
+    b, keep = h.device_batch(t, atm.absorber_id)
+    L, K, NC = h.n_channels[0], atm.max_layers, atm.cloud_type.shape[1]
+    f64 = dict(dtype=torch.float64, device=dev)
+    o = dict(radiance=torch.full((P, L), np.nan, **f64), bt=torch.full((P, L), np.nan, **f64),
+             temperature_k=torch.full((P, L, K), np.nan, **f64),
+             absorber_k=torch.full((P, L, atm.n_absorbers, K), np.nan, **f64),
+             water_temperature_k=torch.full((P, L), np.nan, **f64),
+             surface_emissivity_k=torch.full((P, L), np.nan, **f64),
+             cloud_water_content_k=torch.full((P, L, NC, K), np.nan, **f64),
+             cloud_effective_radius_k=torch.full((P, L, NC, K), np.nan, **f64),
+             cloud_fraction_k=torch.full((P, L, K), np.nan, **f64),
+             status=torch.full((P,), -1, dtype=torch.int32, device=dev))
+    h.k_matrix_device(b, o, None, 0, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(o["bt"].cpu().numpy(), rts.brightness_temperature)
+    assert np.array_equal(o["temperature_k"].cpu().numpy(), km.temperature)
+    assert np.array_equal(o["cloud_water_content_k"].cpu().numpy(), km.cloud_water_content)
+    assert not o["cloud_fraction_k"].isnan().any()
