@@ -1,18 +1,24 @@
-"""Benchmark: clear-sky hyperspectral IR K-matrix, mixed precision vs all-FP64, on one GB300.
+"""Benchmark: the K-matrix of the ragged mixed-sensor batch, mixed precision vs all-FP64, on one GB300.
 
-Workload (one step): 2000 profiles x 101 layers x 2211 channels, ODPS group-1
-predictors (6 absorbers), Emission solver, forward + K-matrix with Jacobians
-w.r.t. temperature, H2O and O3 per layer plus skin temperature.  Synthetic
-seeded inputs and coefficient files (crtmv3_gb300.synthetic) stand in for real
-sensor data.
+Default workload (one step, --workload C5): 20000 profiles with layer counts
+uniform in 60-137, each seen by one of 3 synthetic sensors (22 microwave, 616
+and 2211 infrared channels), 30 % of them cloudy (liquid and ice clouds in the
+infrared, 5 cloud types in the microwave) with the stream rule or
+Options%n_Streams 8 / 16; forward + K-matrix through ADA with the Jacobians of
+temperature, H2O and O3 per layer, skin temperature, emissivity and each
+cloud's water content and effective radius.  Synthetic seeded inputs and
+coefficient files (crtmv3_gb300.synthetic) stand in for real sensor data.
 
 Reported value: profile*channels per second of the mixed-precision form with
-inputs resident in HBM; the all-FP64 GPU form, the accuracy of the mixed form
-against it, the end-to-end rate through the C-ABI with host buffers, per-stage
-kernel times and the CPU baseline (the FP64 oracle on the host cores) are in
-the same JSON line.
+inputs resident in HBM.  The same JSON line carries the all-FP64 GPU form,
+the accuracy of both forms against the FP64 oracle (and of the mixed form
+against the FP64 form), per-stage kernel times, the roofline of the dominant
+kernel stage, the end-to-end rate through the host entry point and the CPU
+baseline (the oracle on the host cores).  --workload C2 is the clear-sky IR
+K-matrix (2000 x 101 x 2211); C3 and C4 the cloudy microwave adjoint and the
+all-sky infrared K-matrix.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--profiles P]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload C5|C2|C3|C4]
 """
 from __future__ import annotations
 
@@ -191,30 +197,60 @@ def workload_config(P: int, world: int) -> dict:
 
 
 def run_reference(args):
+    """The reference's CPU path (the FP64 oracle, a restatement of it: the
+    Fortran reference cannot be built here) on the host cores: each step is
+    a bounded sample of the workload (C2: args.cpu_profiles profiles; C3-C5:
+    the first args.cpu_profiles profiles of each sensor group)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    sy.write_sensor_files(COEFF_DIR, SENSOR)
     threads = os.cpu_count() or 1
-    P_sample = args.cpu_profiles
-    vals = []
-    for _ in range(args.warmup):
-        cpu_baseline(max(threads // 2, 1), threads, min_seconds=0.0)
-    for _ in range(args.steps):
-        v, dt, calls, _, _ = cpu_baseline(P_sample, threads, min_seconds=0.0)
-        vals.append((v, dt))
+    if args.workload == "C2":
+        sy.write_sensor_files(COEFF_DIR, SENSOR)
+        P_sample = args.cpu_profiles
+        vals = []
+        for _ in range(args.warmup):
+            cpu_baseline(max(threads // 2, 1), threads, min_seconds=0.0)
+        for _ in range(args.steps):
+            v, dt, calls, _, _ = cpu_baseline(P_sample, threads, min_seconds=0.0)
+            vals.append((v, dt))
+        cfg = workload_config(args.profiles, 1)
+        cfg["sample_profiles_per_step"] = P_sample
+        metric = METRIC
+        sample = (f"{P_sample} profiles x 2211 channels K-matrix per step, H2O and O3 Jacobians as the GPU arm "
+                  f"(FP64 C oracle, OpenMP over profiles)")
+    else:
+        if args.workload == "C3":
+            print(json.dumps({"impl": "reference", "unavailable": "the oracle's cloudy path has a K-matrix, "
+                              "not the adjoint this workload times"}))
+            return 0
+        groups = scatter_groups(args.workload, 0, args.profiles if args.profiles != 2000 else 0)
+        for sid, *_ in groups:
+            sy.write_sensor_files(COEFF_DIR, sid)
+        sy.write_cloud_files(COEFF_DIR)
+        sy.write_aerosol_files(COEFF_DIR)
+        samp = sample_groups(groups, args.cpu_profiles)
+        small = sample_groups(groups, 2)
+        for _ in range(args.warmup):
+            oracle_scatter_k(small, threads)
+        vals = []
+        for _ in range(args.steps):
+            _, pc, dt = oracle_scatter_k(samp, threads)
+            vals.append((pc / dt, dt))
+        cfg = {"workload": args.workload + ": " + SCATTER_WORKLOAD[args.workload],
+               "groups": [{"sensor": g[0], "profiles": int(g[1].n_profiles)} for g in groups],
+               "parallelism": "replicas x1", "sample_profiles_per_group_per_step": args.cpu_profiles}
+        metric = SCATTER_METRIC[args.workload]
+        sample = (f"the first {args.cpu_profiles} profiles of each sensor group per step (the workload's mix of "
+                  f"clear and cloudy profiles and stream options), K-matrix with the GPU arm's Jacobians "
+                  f"(FP64 C oracle: clear-sky chain and the reverse mode of the ADA path, OpenMP over profiles)")
     value = statistics.median(v for v, _ in vals)
     ms = statistics.median(dt for _, dt in vals) * 1e3
-    cfg = workload_config(args.profiles, 1)
-    cfg["sample_profiles_per_step"] = P_sample
-    line = {"impl": "reference", "metric": METRIC,
+    line = {"impl": "reference", "metric": metric,
             "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{P_sample} profiles x 2211 channels K-matrix per step, "
-                                       f"H2O and O3 Jacobians as the GPU arm "
-                                       f"(FP64 C oracle, OpenMP over profiles)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -224,6 +260,14 @@ def run_reference(args):
 # Scattering workloads (optional: --workload C3 | C4 | C5)
 # ---------------------------------------------------------------------------
 
+SCATTER_WORKLOAD = {
+    "C3": "5000 profiles x 100 layers x 16 MW channels, 5 cloud types, ADA, forward + adjoint",
+    "C4": "1000 profiles x 100 layers x 616 IR channels, liquid + ice clouds and 3 aerosols, ADA, forward + "
+          "K-matrix",
+    "C5": "20000 profiles, layers U[60,137], one of 3 sensors each (22 MW / 616 IR / 2211 IR channels), 30% "
+          "cloudy (liquid + ice in IR, 5 types in MW) with the stream rule or Options%n_Streams 8 / 16, ADA, "
+          "forward + K-matrix with T / H2O / O3 per layer, skin T, emissivity, cloud water content and radius",
+}
 SCATTER_METRIC = {
     "C3": "forward+adjoint profile*channels/s (cloudy MW, ADA, mixed precision, inputs in HBM)",
     "C4": "forward+K-matrix profile*channels/s (all-sky IR with aerosols, ADA, mixed precision, inputs in HBM)",
@@ -298,12 +342,127 @@ def scatter_device_inputs(torch, h, atm, sfc, geo, opt, dev):
     return b, keep, t
 
 
+def sample_groups(groups, n: int):
+    """The first n profiles of each group: the workload's own mix of clear and
+    cloudy profiles and stream options."""
+    out = []
+    for sid, atm, sfc, geo, opt in groups:
+        w = slice(0, min(n, atm.n_profiles))
+        out.append((sid, atm.subset(w), sfc.subset(w), geo.subset(w), opt.subset(w)))
+    return out
+
+
+def k_selection(atm):
+    """User absorber indices of the H2O and O3 Jacobians that the K-matrix returns."""
+    ids = list(atm.absorber_id)
+    return [ids.index(j) for j in (1, 3) if j in ids]
+
+
+def oracle_scatter_k(groups, threads: int):
+    """The FP64 oracle's K-matrix (clear-sky chain + the reverse mode of the
+    ADA path) of each group, with the Jacobians the GPU arm returns; returns
+    (outputs per group, p*c, seconds)."""
+    from oracle.pyoracle import Oracle
+    outs, pc, t = [], 0, 0.0
+    for sid, atm, sfc, geo, opt in groups:
+        o = Oracle(COEFF_DIR, sid)
+        t0 = time.perf_counter()
+        r = o.k_matrix_scatter(atm, sfc, geo, opt, os.path.join(COEFF_DIR, "CloudCoeff.bin"),
+                               os.path.join(COEFF_DIR, "AerosolCoeff.bin") if atm.aerosol_type is not None else None,
+                               n_threads=threads, k_absorbers=k_selection(atm))
+        t += time.perf_counter() - t0
+        outs.append(r)
+        pc += atm.n_profiles * o.n_channels
+    return outs, pc, t
+
+
+def scatter_errors(gpu, ref, atm):
+    """Errors of one GPU form's outputs against the oracle's on the same
+    profiles: max |dBT| (K) and, per Jacobian, max |dK| / max |K_oracle| (the
+    cloud and aerosol Jacobians scaled by their variable)."""
+    sel = k_selection(atm)
+
+    def rel(x, y, scale=None):
+        return float(np.abs(x - y).max() / max(np.abs(y if scale is None else scale).max(), 1e-300))
+    e = {"max_abs_bt_K": float(np.abs(gpu["bt"] - ref["bt"]).max()),
+         "temperature": rel(gpu["temperature_k"], ref["temperature_k"]),
+         "water_temperature": rel(gpu["water_temperature_k"], ref["water_temperature_k"]),
+         "surface_emissivity": rel(gpu["surface_emissivity_k"], ref["surface_emissivity_k"])}
+    for i, j in enumerate(sel):
+        e[f"absorber_{int(atm.absorber_id[j])}"] = rel(gpu["absorber_k"][:, :, i], ref["absorber_k"][:, :, j])
+    for f in ("cloud_water_content", "cloud_effective_radius", "aerosol_concentration", "aerosol_effective_radius"):
+        if f + "_k" in gpu and ref[f + "_k"].size:
+            x = getattr(atm, f)[:, None]
+            e[f] = rel(gpu[f + "_k"] * x, ref[f + "_k"] * x)
+    return e
+
+
+def merge_errors(acc, e):
+    for k, v in e.items():
+        acc[k] = max(acc.get(k, 0.0), v)
+    return acc
+
+
+def pipe_peaks(torch, dev):
+    """cuBLAS FP64 and FP32 (TF32 off) matrix-multiply rates of this GPU
+    through torch.matmul, best of 5, TFLOP/s: the measured ceilings for
+    kernels bound by the FP64 or FP32 pipes."""
+    out = {}
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    for name, dt, n in (("fp64", torch.float64, 4096), ("fp32", torch.float32, 8192)):
+        a = torch.randn(n, n, dtype=dt, device=dev)
+        b = torch.randn(n, n, dtype=dt, device=dev)
+        torch.matmul(a, b)
+        torch.cuda.synchronize(dev)
+        best = 1e30
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            torch.cuda.synchronize(dev)
+            best = min(best, e0.elapsed_time(e1))
+        out[name] = 2.0 * n ** 3 / (best * 1e-3) / 1e12
+        del a, b
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    return out
+
+
+def adding_flops(groups, n_channels, wavenumbers):
+    """Algorithmic FP64 FLOPs of one step's adding and adding adjoint
+    (scatter_adding): 38 nZ^3 per scattering layer and (profile, channel) --
+    forward adding 10 nZ^3 (Gamma = (I - Rup R)^-1 by elimination, T Gamma,
+    Rup T, T Gamma Rup T) and its adjoint 28 nZ^3 (Gamma again, and the
+    products' transposes) -- with nZ the stream set's angles plus the sensor
+    angle: Options%n_Streams, else the stream rule on the largest effective
+    radius and the channel's wavenumber."""
+    total = 0.0
+    for (sid, atm, sfc, geo, opt), L, wn in zip(groups, n_channels, wavenumbers):
+        for p in range(atm.n_profiles):
+            nc = int(atm.n_clouds[p]) if atm.n_clouds is not None else 0
+            if nc == 0:
+                continue
+            wc = atm.cloud_water_content[p, :nc]
+            n_sl = int(((wc > 1e-6).any(axis=0)).sum())   # layers with an active cloud
+            ns = int(opt.n_streams[p]) if opt.n_streams is not None and opt.use_n_streams[p] else 0
+            if ns:
+                nz = np.full(L, (ns + 2) // 2 + 1)
+            else:
+                mie = 2.0 * np.pi * atm.cloud_effective_radius[p, :nc].max() * wn / 1.0e4
+                nleg = np.where(mie < 0.01, 2, np.where(mie < 1.0, 4, 6))
+                nz = (nleg + 2) // 2 + 1
+            total += n_sl * 38.0 * float((nz.astype(np.float64) ** 3).sum())
+    return total
+
+
 def run_scattering(args, torch, dev, rank, world, dist):
-    from crtmv3_gb300 import api
+    from crtmv3_gb300 import api, coefficients as co
     name = args.workload
-    # cloudy K-matrix intermediates take ~0.3 GB per IR profile: a larger
-    # chunk workspace keeps the scattering kernels' grids full
-    os.environ.setdefault("CRTM_GPU_WORKSPACE_MB", "32768")
+    # the K-matrix's scattering intermediates take ~0.4 GB per cloudy IR profile
+    # on the stream rule and ~1.3 GB with 16 streams: a large work space keeps
+    # the scattering kernels' grids full (the step's outputs take ~150 GB)
+    os.environ.setdefault("CRTM_GPU_WORKSPACE_MB", "49152")
     groups = scatter_groups(name, rank, args.profiles if args.profiles != 2000 else 0)
     if rank == 0:
         for sid, *_ in groups:
@@ -322,8 +481,7 @@ def run_scattering(args, torch, dev, rank, world, dist):
     for si, (sid, atm, sfc, geo, opt) in enumerate(groups):
         b, keep, t = scatter_device_inputs(torch, h, atm, sfc, geo, opt, dev)
         P, K, L = atm.n_profiles, atm.max_layers, h.n_channels[si]
-        ids = list(atm.absorber_id)
-        sel = [ids.index(j) for j in (1, 3) if j in ids]
+        sel = k_selection(atm)
         o = dict(radiance=torch.empty((P, L), **f64), bt=torch.empty((P, L), **f64),
                  status=torch.empty((P,), dtype=torch.int32, device=dev))
         if name == "C3":
@@ -342,7 +500,6 @@ def run_scattering(args, torch, dev, rank, world, dist):
             NC = atm.cloud_type.shape[1]
             o["cloud_water_content" + sfx] = torch.empty(lead + (NC, K), **f64)
             o["cloud_effective_radius" + sfx] = torch.empty(lead + (NC, K), **f64)
-            o["cloud_fraction" + sfx] = torch.empty(lead + (K,), **f64)
         if atm.aerosol_type is not None:
             NA = atm.aerosol_type.shape[1]
             o["aerosol_concentration" + sfx] = torch.empty(lead + (NA, K), **f64)
@@ -370,12 +527,16 @@ def run_scattering(args, torch, dev, rank, world, dist):
         torch.cuda.synchronize(dev)
         return max_over_ranks(e0.elapsed_time(e1), dist, dev)
 
-    # the FP64 form's outputs on the first 512 profiles of each group, for the
-    # accuracy of the mixed form (one output set: the full K-matrix of C5 with
-    # scattering Jacobians does not fit twice)
+    n_cmp = args.cpu_profiles
+
+    def sample_out():
+        return [{f: v[:n_cmp].cpu().numpy() for f, v in c["out"].items()} for c in calls]
+    # the FP64 form's outputs: the mixed form's accuracy against it on the first
+    # 512 profiles of each group, and both forms against the oracle on the sample
     step(0)
     torch.cuda.synchronize(dev)
     ref = [{f: v[:512].clone() for f, v in c["out"].items()} for c in calls]
+    fp64_sample = sample_out()
     for _ in range(args.warmup):
         step(1)
     torch.cuda.synchronize(dev)
@@ -387,6 +548,7 @@ def run_scattering(args, torch, dev, rank, world, dist):
     st = h.stage_times(reset=True)
     h.set_profiling(False)
     launches = h.launch_count() - launches0
+    mixed_sample = sample_out()
     bt_err, field_err = 0.0, {}
     for c, r in zip(calls, ref):
         a = c["out"]
@@ -396,13 +558,32 @@ def run_scattering(args, torch, dev, rank, world, dist):
                 continue
             e = float((a[f][:512] - r[f]).abs().max() / r[f].abs().max().clamp_min(1e-300))
             field_err[f] = max(field_err.get(f, 0.0), e)
+    del ref
     jac_err = max(field_err.values()) if field_err else 0.0
     fp64_steps = max(1, min(args.steps, 2))
     ms_fp64 = timed(0, fp64_steps)
     pc = sum(c["pc"] for c in calls) * world
     per_mixed, per_fp64 = ms_mixed / args.steps, ms_fp64 / fp64_steps
     value, fp64_value = pc / (per_mixed * 1e-3), pc / (per_fp64 * 1e-3)
+    stage_ms = {k: v[0] / args.steps for k, v in st.items() if v[1] > 0}
     extra = {}
+    # roofline of the step's dominant kernel stage
+    roofline = None
+    if rank == 0 and name in ("C4", "C5") and stage_ms:
+        dom = max(stage_ms, key=stage_ms.get)
+        pk = pipe_peaks(torch, dev)
+        if dom == "scatter_adding":
+            fl = adding_flops(groups, [h.n_channels[i] for i in range(len(groups))],
+                              [co.read_spccoeff(os.path.join(COEFF_DIR, f"{g[0]}.SpcCoeff.bin")).wavenumber
+                               for g in groups])
+            ach = fl / (stage_ms[dom] * 1e-3) / 1e12
+            roofline = {"bound": "fp64", "achieved": ach, "peak": pk["fp64"], "unit": "TFLOP/s",
+                        "frac": ach / pk["fp64"], "traffic": None, "kernel": "scatter_kmatrix_kernel (adding + adjoint)",
+                        "algorithmic_flops_per_step": fl,
+                        "peak_source": "measured in this run: cuBLAS FP64 GEMM through torch.matmul"}
+        else:
+            roofline = {"bound": None, "kernel": dom, "note": "no algorithmic count for this stage"}
+        extra["pipe_peaks_tflops"] = pk
     if name == "C4":   # SOI forward and K-matrix on the same inputs, ADA forward beside them
         sid, atm, sfc, geo, opt = groups[0]
         opt.rt_algorithm_id = np.full(atm.n_profiles, 168, np.int32)
@@ -425,24 +606,70 @@ def run_scattering(args, torch, dev, rank, world, dist):
             ms = e0.elapsed_time(e1) / args.steps
             extra[f"{lab}_forward_mixed"] = {"ms_per_step": ms, "value": calls[0]["pc"] / (ms * 1e-3)}
         extra["soi_vs_ada_max_abs_bt_K"] = float((fo["bt"] - fo2["bt"]).abs().max())
-        # SOI K-matrix (the orders' adjoint) into the main call's outputs
-        c0 = calls[0]
-        h.k_matrix_device(b, c0["out"], None, 0, sptr, k_absorbers=c0["sel"])
+        opt.rt_algorithm_id = None
+    # end to end through the host entry point (pinned host outputs), mixed
+    # form, on a sample of each group's profiles (the full step's ~150 GB of
+    # Jacobians exceed what this process pins)
+    e2e = None
+    if not args.no_e2e and name != "C3":
+        from crtmv3_gb300.structures import KMatrixBatch
+        frac = 8
+        sub = [(sid, a.subset(slice(0, a.n_profiles // frac)), s_.subset(slice(0, a.n_profiles // frac)),
+                g_.subset(slice(0, a.n_profiles // frac)), o_.subset(slice(0, a.n_profiles // frac)))
+               for sid, a, s_, g_, o_ in groups]
+
+        def pin(shape):
+            return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+        outs, h2d, d2h, epc = [], 0, 0, 0
+        for si, (sid, a, s_, g_, o_) in enumerate(sub):
+            P, K, L = a.n_profiles, a.max_layers, h.n_channels[si]
+            sel = k_selection(a)
+            km = KMatrixBatch(pin((P, L, K)), pin((P, L, len(sel), K)), pin((P, L)), pin((P, L)))
+            NC = a.cloud_type.shape[1] if a.cloud_type is not None else 0
+            if NC:
+                km.cloud_water_content = pin((P, L, NC, K))
+                km.cloud_effective_radius = pin((P, L, NC, K))
+            outs.append((km, sel))
+            h2d += sum(x.nbytes for x in (a.level_pressure, a.pressure, a.temperature, a.absorber, o_.emissivity,
+                                          a.cloud_water_content, a.cloud_effective_radius, a.cloud_fraction)
+                       if x is not None) + 14 * P * 8
+            d2h += P * L * 8 * (2 + K * (1 + len(sel) + 2 * NC) + 2) + P * 4
+            epc += P * L
+        h.set_precision(1)
+
+        def e2e_step():
+            for si, ((sid, a, s_, g_, o_), (km, sel)) in enumerate(zip(sub, outs)):
+                h.k_matrix(a, s_, g_, o_, None, si, k_absorbers=sel, out=km)
+        e2e_step()
+        n_e2e = max(1, min(args.steps, 2))
         torch.cuda.synchronize(dev)
-        ks = max(1, min(args.steps, 2))
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(ks):
-            h.k_matrix_device(b, c0["out"], None, 0, sptr, k_absorbers=c0["sel"])
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
-        ms = e0.elapsed_time(e1) / ks
-        extra["soi_kmatrix"] = {"ms_per_step": ms, "value": c0["pc"] / (ms * 1e-3), "steps": ks}
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            e2e_step()
+        dt = (time.perf_counter() - t0) / n_e2e
+        e2e = {"value": epc * world / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "ms_per_step": dt * 1e3, "sample": f"first 1/{frac} of each group's profiles per step"}
+        del outs
+    # CPU baseline (the FP64 oracle on the host cores) and both GPU forms
+    # against the oracle, on the first n_cmp profiles of each group
+    cpu, vs_oracle = None, None
+    if rank == 0 and not args.no_cpu and name != "C3":
+        threads = os.cpu_count() or 1
+        samp = sample_groups(groups, n_cmp)
+        ref_o, cpc, ct = oracle_scatter_k(samp, threads)
+        cpu = {"value": cpc / ct, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"the first {n_cmp} profiles of each sensor group ({cpc} profile*channels, the "
+                         f"workload's mix of clear and cloudy profiles and stream options), K-matrix with the same "
+                         f"Jacobians as the GPU arm, FP64 C oracle with OpenMP over profiles, {ct:.1f} s"}
+        vs_oracle = {"fp64": {}, "mixed": {}, "profiles_per_group": n_cmp}
+        for (sid, a, *_), r, g64, gmx in zip(samp, ref_o, fp64_sample, mixed_sample):
+            merge_errors(vs_oracle["fp64"], scatter_errors(g64, r, a))
+            merge_errors(vs_oracle["mixed"], scatter_errors(gmx, r, a))
     if rank == 0:
-        cfg = {"workload": name, "groups": [{"sensor": c_[0], "profiles": int(c_[1].n_profiles),
-                                              "layers_max": int(c_[1].max_layers),
-                                              "cloudy_profiles": int((c_[1].n_clouds > 0).sum())}
-                                             for c_ in groups],
+        cfg = {"workload": name + ": " + SCATTER_WORKLOAD[name],
+               "groups": [{"sensor": c_[0], "profiles": int(c_[1].n_profiles),
+                           "layers_max": int(c_[1].max_layers),
+                           "cloudy_profiles": int((c_[1].n_clouds > 0).sum())} for c_ in groups],
                "parallelism": f"replicas x{world}",
                "l2": "inputs and per-step intermediates far larger than L2, no flush"}
         line = {"metric": SCATTER_METRIC[name], "value": value, "unit": UNIT, "n_gpus": world,
@@ -453,9 +680,10 @@ def run_scattering(args, torch, dev, rank, world, dist):
                 "speedup_mixed_vs_fp64": value / fp64_value,
                 "accuracy_mixed_vs_fp64": {"max_abs_bt_K": bt_err, "max_rel_jacobian": jac_err,
                                            "by_output": field_err, "profiles_compared_per_group": 512},
-                "stages_ms_per_step": {k: v[0] / args.steps for k, v in st.items() if v[1] > 0},
+                "accuracy_vs_oracle": vs_oracle,
+                "stages_ms_per_step": stage_ms,
                 "stage_launches_per_step": {k: v[1] // args.steps for k, v in st.items() if v[1] > 0},
-                "gpu_launches": int(launches), "roofline": None, "cpu_baseline": None, "e2e": None,
+                "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clk.summary(), **extra}
         print(json.dumps(line))
     return 0
@@ -472,16 +700,21 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--profiles", type=int, default=2000)
-    ap.add_argument("--cpu-profiles", type=int, default=256)
+    ap.add_argument("--cpu-profiles", type=int, default=0,
+                    help="CPU-baseline / oracle sample: profiles (C2, default 256) or profiles per sensor "
+                         "group (C3-C5, default 16)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="C2", choices=["C2", "C3", "C4", "C5"],
-                    help="C2 (default): the headline clear-sky IR K-matrix; C3-C5: scattering workloads")
+    ap.add_argument("--workload", default="C5", choices=["C2", "C3", "C4", "C5"],
+                    help="C5 (default): the ragged mixed-sensor batch, 30%% cloudy, forward + K-matrix; "
+                         "C2: clear-sky IR K-matrix; C3, C4: cloudy MW adjoint, all-sky IR K-matrix")
     ap.add_argument("--autotune", action="store_true",
                     help="C2: pick the map tile and profiles per pass of each form with the "
                          "library's autotuner before the warm-up (default: the built-in 16 channels "
                          "per map CTA, no pass cap)")
     args = ap.parse_args()
+    if not args.cpu_profiles:
+        args.cpu_profiles = 256 if args.workload == "C2" else 16
     if args.impl == "reference":
         return run_reference(args)
 

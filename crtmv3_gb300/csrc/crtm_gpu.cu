@@ -606,15 +606,15 @@ struct Work {
   double* TSK;      // adjoint: [n][L]
   R* RA;            // [n][nv][K][L]
   R* LB;            // cloudy forward: [n][Kmax][NE][L] layer records
-  double* LBK;      // scattering K-matrix/adjoint: [n][Kmax][NE][L] layer records, FP64
+  R* LBK;           // scattering K-matrix/adjoint: [n][Kmax][NE][L] layer records
   double* FB;       // SOI: [n][2][2][Kmax+1][NZ][L] fields (forward), adjoint fields (K-matrix/adjoint)
   double* FS;       // SOI K-matrix/adjoint: [n][slots][2][Kmax+1][NZ][L] order fields
   double* maxreff;  // scattering: [n]
   double* cover;    // scattering: [n] total cloud cover
-  double* AS;       // scattering K-matrix/adjoint: [n][Kmax+1][NZ*NZ+NZ][L] adding states
+  R* AS;            // scattering K-matrix/adjoint: [n][Kmax+1][NZ*NZ+NZ][L] adding states
   R* TODc;          // scattering K-matrix/adjoint: [n][Kmax][L] cloudy dR/dtau
   double* CB;       // scattering K-matrix/adjoint: [n][4][L] cloudy radiance, surface terms, clear radiance
-  double* LBA;      // scattering K-matrix/adjoint: [n][Kmax][NE][L] layer record adjoints
+  R* LBA;           // scattering K-matrix/adjoint: [n][Kmax][NE][L] layer record adjoints
   double* CJ, *CR;  // species Jacobians: [n][slots][Kmax][L]
   double* CF;       // cloud-fraction Jacobian: [n][Kmax][L]
   double* CV;       // aerosol effective-variance Jacobians ('CMAQ'): [n][slots][Kmax][L]
@@ -683,7 +683,7 @@ size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w
   if (mode == 3) wk.TAU = (R*)carve(nn * Kmax * L * sizeof(R));
   if (sw.rec > 0) {
     if (sw.kstate)
-      wk.LBK = (double*)carve(nn * Kmax * (size_t)sw.rec * L * sizeof(double));
+      wk.LBK = (R*)carve(nn * Kmax * (size_t)sw.rec * L * sizeof(R));
     else
       wk.LB = (R*)carve(nn * Kmax * (size_t)sw.rec * L * sizeof(R));
     wk.maxreff = (double*)carve(nn * sizeof(double));
@@ -693,11 +693,11 @@ size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w
     wk.FS = sw.soi && sw.kstate
                 ? (double*)carve(nn * (size_t)sw.soi_slots * 2 * (Kmax + 1) * sw.nz * L * sizeof(double))
                 : nullptr;
-    wk.AS = sw.kstate ? (double*)carve(nn * (size_t)(Kmax + 1) * (sw.nz * sw.nz + sw.nz) * L * sizeof(double))
+    wk.AS = sw.kstate ? (R*)carve(nn * (size_t)(Kmax + 1) * (sw.nz * sw.nz + sw.nz) * L * sizeof(R))
                       : nullptr;
     wk.TODc = sw.kstate ? (R*)carve(nn * Kmax * L * sizeof(R)) : nullptr;
     wk.CB = sw.kstate ? (double*)carve(nn * 4 * L * sizeof(double)) : nullptr;
-    wk.LBA = sw.kstate ? (double*)carve(nn * Kmax * (size_t)sw.rec * L * sizeof(double)) : nullptr;
+    wk.LBA = sw.kstate ? (R*)carve(nn * Kmax * (size_t)sw.rec * L * sizeof(R)) : nullptr;
     const size_t sj = nn * (size_t)sw.slots * Kmax * L * sizeof(double);
     wk.CJ = sw.slots ? (double*)carve(sj) : nullptr;
     wk.CR = sw.slots ? (double*)carve(sj) : nullptr;

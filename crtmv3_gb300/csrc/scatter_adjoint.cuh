@@ -21,8 +21,8 @@
 //   - The forward quantities the adjoint needs are recomputed from the
 //     layer's inputs inside the call instead of being read from a tape.
 //   - The LUT interpolation of each species is differentiated in forward mode
-//     (its four inputs: amount, two LUT coordinates, temperature), which
-//     costs a few LUT evaluations and no matrix work.
+//     (its four inputs: amount, two LUT coordinates, temperature), in FP64,
+//     which costs a few LUT evaluations and no matrix work.
 #pragma once
 
 #include "scatter_physics.cuh"
@@ -487,18 +487,21 @@ CRTM_HD int bulk_to_inputs(const CloudyColumn& in, const CloudLut& lut, int nleg
   // Planck radiance of the layer temperature
   const double te = in.b1 + in.b2 * (double)tk, ee = exp(in.c2 / te);
   double gt = (double)A.B_b * in.c1 * in.c2 * ee * in.b2 / (te * te * (ee - 1.0) * (ee - 1.0));
-  // each species' share in forward mode: amount, c1, c2 and the temperature
-  using D4 = Dual<4, T>;
+  // each species' share in forward mode: amount, c1, c2 and the temperature,
+  // in FP64 in every form (the LUT derivatives are differences of nearby
+  // table values: in FP32 they cost the radius Jacobians ~1e-3; the LUT work
+  // is a small part of the layer's)
+  using D4 = Dual<4, double>;
   for (int sp = 0; sp < nsp; sp++) {
     D4 od(0.0), bs(0.0), ps[SC_NLEG_MAX + 1];
-    D4 td(tk, 0);
-    td.d[3] = T(1.0);
+    D4 td(double(tk), 0);
+    td.d[3] = 1.0;
     if (const int rc = species_share<D4>(in, lut, nleg, loff, k, sp, td, SpeciesSeed{sp}, &od, &bs, ps)) return rc;
     double gg[4];
     for (int d = 0; d < 4; d++) {
-      T v = od0_b * od.d[d] + bs_b * bs.d[d];
-      for (int l = 1; l <= nleg; l++) v += ps_b[l] * ps[l].d[d];
-      gg[d] = (double)v;
+      double v = double(od0_b) * od.d[d] + double(bs_b) * bs.d[d];
+      for (int l = 1; l <= nleg; l++) v += double(ps_b[l]) * ps[l].d[d];
+      gg[d] = v;
     }
     gs[sp][0] = gg[0];
     gs[sp][1] = gg[1];
@@ -562,9 +565,15 @@ CRTM_HD int layer_adjoint(const CloudyColumn& in, const CloudLut& lut, const Str
     }
     double gap = 1.0;
     T w_b, tau_b, Bb;
-    if (!ada_layer_adjoint<NZ, T>(nS, nZ, L.ssa, L.od, mu, wt, ff, bb, B, Tb, Rb, sb, &w_b, &tau_b, ffb, bbb, &Bb,
-                                  &gap))
-      return -5;
+    const bool ok = ada_layer_adjoint<NZ, T>(nS, nZ, L.ssa, L.od, mu, wt, ff, bb, B, Tb, Rb, sb, &w_b, &tau_b, ffb,
+                                             bbb, &Bb, &gap);
+    if constexpr (std::is_same<T, float>::value) {
+      // the FP32 reverse sweep near a nearly defective eigenbasis, or where
+      // its factorisation failed: this layer in FP64
+      if (!ok || gap < FP32_ADJ_GAP_MIN)
+        return layer_adjoint<NZ, double>(in, lut, St, k, gas_od, kind_rec, T_b, R_b, src_b, od_b, B_b, g, gs);
+    }
+    if (!ok) return -5;
     if (gap < SENSOR_GAP_MIN && nZ == nS + 1) {
       // A quadrature eigenvalue of MOM nearly meets the sensor angle's: the
       // derivatives through the nearly defective eigenbasis lose about

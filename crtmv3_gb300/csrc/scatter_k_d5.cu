@@ -14,7 +14,7 @@ int scatter_k_d5_set_gauss(const GaussTable& g) {
 
 template <int NZ, class R, class C>
 void launch_scatter_layers_k(const ScatterArgs<R>& a, unsigned grid, cudaStream_t st) {
-  scatter_layers_kernel<NZ, R, double, C><<<grid, SCATTER_THREADS, 0, st>>>(a, a.LBK);
+  scatter_layers_kernel<NZ, R, R, C><<<grid, SCATTER_THREADS, 0, st>>>(a, a.LBK);
 }
 
 template <int NZ, class R>

@@ -84,8 +84,8 @@ struct ScatterArgs {
   int soi_slots;
   const R* TAU;                 // [n][Kmax][L] gas layer optical depths
   R* LB;                        // [n][Kmax][NE][L] layer records (forward)
-  double* LBK;                  // [n][Kmax][NE][L] layer records of the K-matrix / adjoint, FP64 in
-                                // both forms: the species contractions cancel strongly
+  R* LBK;                       // [n][Kmax][NE][L] layer records of the K-matrix / adjoint (the
+                                // layer solver's T in loss form keeps FP32 records accurate)
   const double* cloud_fraction; // [P][Kmax] or null (1)
   const int* overlap;           // [P] Options%Overlap_Id or null (4, average)
   double* maxreff;              // [n]
@@ -98,8 +98,8 @@ struct ScatterArgs {
   R* TODc;                      // [n][Kmax][L] dR/dtau of the user layers
   R* PT;                        // [n][Kmax][L] dR/dT at fixed gas optical depth
   double* CB;                   // [n][4][L] radiance, dR/de, dR/d(surface Planck), clear radiance
-  double* AS;                   // [n][Kmax+1][NS][L] adding states
-  double* LBA;                  // [n][Kmax][NE][L] record adjoints
+  R* AS;                        // [n][Kmax+1][NS][L] adding states
+  R* LBA;                       // [n][Kmax][NE][L] record adjoints
   // species Jacobians: slots 0..max_clouds-1 clouds, then aerosols
   int n_slots;                  // max_clouds + max_aerosols when requested, else 0
   double* CJ, *CR;              // [n][n_slots][Kmax][L] amount and radius
@@ -383,10 +383,10 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_kmatrix_kernel(Scatte
   int code = stream_set<NZ, double>(c.nleg, c.mu_sensor, c.n_clouds > 0 ? a.lut.nleg : -1, c_gauss, S);
   if (!code) {
     const int nZ = S.nZ;
-    auto layer = [&](int k, int* kind, double* od, Mat<NZ, double>& Tm, Mat<NZ, double>& Rm, double* src) {
-      const double* rec = a.LBK + ((size_t)p * Kmax + k) * NE * L + l;
+    auto layer = [&](int k, int* kind, double* od, Mat<NZ, R>& Tm, Mat<NZ, R>& Rm, R* src) {
+      const R* rec = a.LBK + ((size_t)p * Kmax + k) * NE * L + l;
       *kind = (int)rec[0];
-      *od = rec[(size_t)L];
+      *od = double(rec[(size_t)L]);
       if (*kind != 1) return;
       for (int i = 0; i < nZ; i++) {
         for (int j = 0; j < nZ; j++) {
@@ -396,15 +396,15 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_kmatrix_kernel(Scatte
         src[i] = rec[(size_t)(2 + 2 * NZ * NZ + i) * L];
       }
     };
-    double* as = a.AS + (size_t)p * (Kmax + 1) * NS * L + l;
-    auto state = [&](int lev, int i) -> double& { return as[((size_t)lev * NS + i) * L]; };
-    auto adj = [&](int k, int kind, const Mat<NZ, double>& T_b, const Mat<NZ, double>& R_b, const double* src_b,
+    R* as = a.AS + (size_t)p * (Kmax + 1) * NS * L + l;
+    auto state = [&](int lev, int i) -> R& { return as[((size_t)lev * NS + i) * L]; };
+    auto adj = [&](int k, int kind, const Mat<NZ, R>& T_b, const Mat<NZ, R>& R_b, const R* src_b,
                    double od_b, double B_b) {
-      double* rb = a.LBA + ((size_t)p * Kmax + k) * NE * L + l;
-      rb[0] = kind;
-      rb[(size_t)L] = od_b;
+      R* rb = a.LBA + ((size_t)p * Kmax + k) * NE * L + l;
+      rb[0] = R(kind);
+      rb[(size_t)L] = R(od_b);
       if (kind != 1) {
-        rb[2 * (size_t)L] = B_b;
+        rb[2 * (size_t)L] = R(B_b);
         return;
       }
       for (int i = 0; i < nZ; i++) {
@@ -415,13 +415,14 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_kmatrix_kernel(Scatte
         rb[(size_t)(2 + 2 * NZ * NZ + i) * L] = src_b[i];
       }
     };
-    code = cloudy_adjoint<NZ>(c, S, layer, state, adj, &rad, &e_b, &Bs_b);
+    code = cloudy_adjoint<NZ, decltype(layer), decltype(state), decltype(adj), R>(c, S, layer, state, adj, &rad,
+                                                                                         &e_b, &Bs_b);
   }
   if (code) {
     atomicCAS(a.error, 0, code);
     if (a.status) atomicOr(a.status + gp, 1 << 4);
     rad = e_b = Bs_b = 0.0;
-    for (int k = 0; k < c.Ku; k++) a.LBA[((size_t)p * Kmax + k) * NE * L + l] = -1.0;
+    for (int k = 0; k < c.Ku; k++) a.LBA[((size_t)p * Kmax + k) * NE * L + l] = R(-1.0);
   }
   double* cb = a.CB + (size_t)p * 4 * L + l;
   cb[0] = rad;
@@ -626,7 +627,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_reverse_kernel(Scatte
       jac(a.CR, s) = 0.0;
       if (a.CV) jac(a.CV, s) = 0.0;
     }
-  const double* rb = a.LBA + ((size_t)p * Kmax + k) * NE * L + l;
+  const R* rb = a.LBA + ((size_t)p * Kmax + k) * NE * L + l;
   const int kind = (int)rb[0];
   if (kind < 0) {
     a.TODc[kl] = R(0);
@@ -638,14 +639,14 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_reverse_kernel(Scatte
   const int nZ = S.nZ;
   Mat<NZ, double> T_b, R_b;
   double src_b[NZ];
-  const double od_b = rb[(size_t)L], B_b = kind == 1 ? 0.0 : rb[2 * (size_t)L];
+  const double od_b = double(rb[(size_t)L]), B_b = kind == 1 ? 0.0 : double(rb[2 * (size_t)L]);
   if (kind == 1)
     for (int i = 0; i < nZ; i++) {
       for (int j = 0; j < nZ; j++) {
-        T_b.a[i][j] = rb[(size_t)(2 + i * NZ + j) * L];
-        R_b.a[i][j] = rb[(size_t)(2 + NZ * NZ + i * NZ + j) * L];
+        T_b.a[i][j] = double(rb[(size_t)(2 + i * NZ + j) * L]);
+        R_b.a[i][j] = double(rb[(size_t)(2 + NZ * NZ + i * NZ + j) * L]);
       }
-      src_b[i] = rb[(size_t)(2 + 2 * NZ * NZ + i) * L];
+      src_b[i] = double(rb[(size_t)(2 + 2 * NZ * NZ + i) * L]);
     }
   double g[2], gs[2 * SC_NC_MAX][3];
   const int kr = layer_adjoint<NZ, C>(c, a.lut, S, k, double(a.TAU[kl]), kind, T_b, R_b, src_b,

@@ -27,7 +27,7 @@ inline int scatter_k_set_gauss(const GaussTable& g) {
          scatter_k_d10f_set_gauss(g) | scatter_soi_d5_set_gauss(g) | scatter_soi_d10_set_gauss(g);
 }
 
-// layer records (FP64) with the layer solver in C
+// layer records (in R) with the layer solver in C
 template <int NZ, class R, class C>
 void launch_scatter_layers_k(const ScatterArgs<R>& a, unsigned grid, cudaStream_t st);
 // the ADA adding adjoint, then (FP64 form, soi) the SOI orders' adjoint of the SOI profiles

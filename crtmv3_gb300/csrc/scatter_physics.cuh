@@ -23,6 +23,8 @@
 
 #include <math.h>
 
+#include <type_traits>
+
 #include "dual.cuh"
 #include "odps_physics.cuh"
 
@@ -46,6 +48,12 @@ constexpr double ANGLE_THRESHOLD = 1.0e-7;           // RTV_Define.f90:70
 // angles mu (1 +- SENSOR_SHIFT)
 constexpr double SENSOR_GAP_MIN = 1.0e-3;
 constexpr double SENSOR_SHIFT = 1.0e-3;
+// FP32 layer solver: below these relative gaps (forward; reverse sweep) the
+// sensor angle's MOM eigenvector, which divides by the gap, loses too much
+// of FP32's precision (about eps/gap in T and R, eps/gap^2 in their
+// derivatives), and the layer is solved in FP64 instead.
+constexpr double FP32_GAP_MIN = 1.0e-2;
+constexpr double FP32_ADJ_GAP_MIN = 3.0e-2;
 
 // Device copy of the CloudCoeff LUT (phase element 1 only).  Tables keep the
 // file's Fortran order (frequency fastest).
@@ -967,7 +975,29 @@ CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const Stre
     if (!(mx > 0.0)) return 0;
     // loss form U = I - T: the record's T = I - U is formed in the record's
     // type, so a layer solved in FP32 keeps its relative precision in FP64 records
-    if (!ada_layer_loss<NZ, S>(St.nS, St.nZ, ssa, od, mu, wt, ff, bb, B, Td, Rd, srcd, gap)) return -5;
+    double g32 = 1.0;
+    const bool ok = ada_layer_loss<NZ, S>(St.nS, St.nZ, ssa, od, mu, wt, ff, bb, B, Td, Rd, srcd,
+                                          gap ? gap : &g32);
+    if constexpr (std::is_same<S, float>::value) {
+      if (!ok || (gap ? *gap : g32) < FP32_GAP_MIN) {   // this layer in FP64
+        Mat<NZ, double> f2, b2, T2, R2;
+        double m2[NZ], w2[NZ], s2[NZ];
+        for (int i = 0; i < St.nZ; i++) {
+          m2[i] = St.mu[i];
+          w2[i] = St.wt[i];
+          for (int j = 0; j < St.nZ; j++) { f2.a[i][j] = double(ff.a[i][j]); b2.a[i][j] = double(bb.a[i][j]); }
+        }
+        if (!ada_layer_loss<NZ, double>(St.nS, St.nZ, double(ssa), double(od), m2, w2, f2, b2, double(B), T2, R2,
+                                        s2))
+          return -5;
+        for (int i = 0; i < St.nZ; i++) {
+          srcd[i] = S(s2[i]);
+          for (int j = 0; j < St.nZ; j++) { Td.a[i][j] = S(T2.a[i][j]); Rd.a[i][j] = S(R2.a[i][j]); }
+        }
+      }
+    } else {
+      if (!ok) return -5;
+    }
     for (int i = 0; i < St.nZ; i++) {
       src[i] = T(srcd[i]);
       for (int j = 0; j < St.nZ; j++) {
@@ -985,78 +1015,97 @@ CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const Stre
 }
 
 // Adding state: reflectivity of everything below the current level (Rup) and
-// upwelling radiance there (rad), FP64 in every form.
-template <int NZ>
+// upwelling radiance there (rad), in the adding's arithmetic A (FP64 in the
+// FP64 form and the forward; the mixed form's K-matrix and adjoint run the
+// adding and its adjoint in FP32 with the (I - Rup R)^-1 inversions in FP64).
+template <int NZ, class A = double>
 struct AddingState {
-  Mat<NZ, double> Rup;
-  double rad[NZ];
+  Mat<NZ, A> Rup;
+  A rad[NZ];
 };
 
-template <int NZ>
-CRTM_HD void adding_init(AddingState<NZ>& A, int nZ, double emissivity, double planck_surface) {
+// Gamma = G^-1 in place, the elimination in FP64 whatever A is.
+template <int NZ, class A>
+CRTM_HD bool invert_fp64(int n, Mat<NZ, A>& G) {
+  if constexpr (sizeof(A) == sizeof(double)) {
+    return mat_invert<NZ, A>(n, G);
+  } else {
+    Mat<NZ, double> D;
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++) D.a[i][j] = double(G.a[i][j]);
+    if (!mat_invert<NZ, double>(n, D)) return false;
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++) G.a[i][j] = A(D.a[i][j]);
+    return true;
+  }
+}
+
+template <int NZ, class A = double>
+CRTM_HD void adding_init(AddingState<NZ, A>& S, int nZ, double emissivity, double planck_surface) {
   for (int i = 0; i < nZ; i++) {
-    for (int j = 0; j < nZ; j++) A.Rup.a[i][j] = 0.0;
-    A.Rup.a[i][i] = 1.0 - emissivity;
-    A.rad[i] = emissivity * planck_surface;
+    for (int j = 0; j < nZ; j++) S.Rup.a[i][j] = A(0.0);
+    S.Rup.a[i][i] = A(1.0 - emissivity);
+    S.rad[i] = A(emissivity * planck_surface);
   }
 }
 
 // Clear layer: diagonal transmission exp(-od/mu_i), source B (1 - t_i).
-template <int NZ>
-CRTM_HD void adding_clear(AddingState<NZ>& A, int nZ, const double* mu, double od, double B) {
-  double tr[NZ], src[NZ], tmp[NZ];
+template <int NZ, class A = double>
+CRTM_HD void adding_clear(AddingState<NZ, A>& S, int nZ, const double* mu, double od, double B) {
+  A tr[NZ], src[NZ], tmp[NZ];
   for (int i = 0; i < nZ; i++) {
-    tr[i] = exp(-od / mu[i]);
-    src[i] = B * (1.0 - tr[i]);
+    const A x = A(-od / mu[i]);
+    tr[i] = exp(x);
+    src[i] = -A(B) * expm1(x);
   }
   for (int i = 0; i < nZ; i++) {
-    double v = A.rad[i];
-    for (int j = 0; j < nZ; j++) v += A.Rup.a[i][j] * src[j];
+    A v = S.rad[i];
+    for (int j = 0; j < nZ; j++) v += S.Rup.a[i][j] * src[j];
     tmp[i] = src[i] + tr[i] * v;
   }
   for (int i = 0; i < nZ; i++) {
-    A.rad[i] = tmp[i];
-    for (int j = 0; j < nZ; j++) A.Rup.a[i][j] *= tr[i] * tr[j];
+    S.rad[i] = tmp[i];
+    for (int j = 0; j < nZ; j++) S.Rup.a[i][j] *= tr[i] * tr[j];
   }
 }
 
 // Scattering layer (ADA_Module.f90:169-190): Gamma = (I - Rup R)^-1,
 // rad <- src + T Gamma (Rup src + rad),  Rup <- R + T Gamma Rup T.
-template <int NZ>
-CRTM_HD bool adding_scatter(AddingState<NZ>& A, int nZ, const Mat<NZ, double>& Tm, const Mat<NZ, double>& Rm,
-                            const double* src) {
-  Mat<NZ, double> G, IGT;
-  double tmp[NZ];
+template <int NZ, class A = double>
+CRTM_HD bool adding_scatter(AddingState<NZ, A>& S, int nZ, const Mat<NZ, A>& Tm, const Mat<NZ, A>& Rm,
+                            const A* src) {
+  Mat<NZ, A> G, IGT;
+  A tmp[NZ];
   for (int i = 0; i < nZ; i++)
     for (int j = 0; j < nZ; j++) {
-      double v = 0.0;
-      for (int m = 0; m < nZ; m++) v += A.Rup.a[i][m] * Rm.a[m][j];
-      G.a[i][j] = (i == j ? 1.0 : 0.0) - v;
+      A v = A(0.0);
+      for (int m = 0; m < nZ; m++) v += S.Rup.a[i][m] * Rm.a[m][j];
+      G.a[i][j] = (i == j ? A(1.0) : A(0.0)) - v;
     }
-  if (!mat_invert<NZ, double>(nZ, G)) return false;
-  mat_mul<NZ, double>(nZ, Tm, G, IGT);
+  if (!invert_fp64<NZ, A>(nZ, G)) return false;
+  mat_mul<NZ, A>(nZ, Tm, G, IGT);
   for (int i = 0; i < nZ; i++) {
-    double v = A.rad[i];
-    for (int j = 0; j < nZ; j++) v += A.Rup.a[i][j] * src[j];
+    A v = S.rad[i];
+    for (int j = 0; j < nZ; j++) v += S.Rup.a[i][j] * src[j];
     tmp[i] = v;
   }
   for (int i = 0; i < nZ; i++) {
-    double v = src[i];
+    A v = src[i];
     for (int j = 0; j < nZ; j++) v += IGT.a[i][j] * tmp[j];
-    A.rad[i] = v;
+    S.rad[i] = v;
   }
-  mat_mul<NZ, double>(nZ, A.Rup, Tm, G);    // Rup T
-  mat_mul<NZ, double>(nZ, IGT, G, A.Rup);   // T Gamma Rup T
+  mat_mul<NZ, A>(nZ, S.Rup, Tm, G);    // Rup T
+  mat_mul<NZ, A>(nZ, IGT, G, S.Rup);   // T Gamma Rup T
   for (int i = 0; i < nZ; i++)
-    for (int j = 0; j < nZ; j++) A.Rup.a[i][j] += Rm.a[i][j];
+    for (int j = 0; j < nZ; j++) S.Rup.a[i][j] += Rm.a[i][j];
   return true;
 }
 
-template <int NZ>
-CRTM_HD double adding_toa(const AddingState<NZ>& A, int nZ, int isat, double cosmic) {
+template <int NZ, class A = double>
+CRTM_HD double adding_toa(const AddingState<NZ, A>& S, int nZ, int isat, double cosmic) {
   double s = 0.0;
-  for (int j = 0; j < nZ; j++) s += A.Rup.a[isat][j];
-  return A.rad[isat] + s * cosmic;
+  for (int j = 0; j < nZ; j++) s += double(S.Rup.a[isat][j]);
+  return double(S.rad[isat]) + s * cosmic;
 }
 
 // ---- adjoint of the adding (reverse mode), unit TOA radiance seed ----------
@@ -1066,17 +1115,19 @@ CRTM_HD double adding_toa(const AddingState<NZ>& A, int nZ, int isat, double cos
 
 // Clear layer (diagonal transmission t_i = exp(-od/mu_i), source B (1 - t_i)):
 // returns d/d(od) and d/dB.
-template <int NZ>
-CRTM_HD void adding_clear_adjoint(int nZ, const double* mu, double od, double B, const Mat<NZ, double>& Rup,
-                                  const double* rad, Mat<NZ, double>& Rup_b, double* rad_b, double* od_b,
-                                  double* B_b) {
-  double tr[NZ], src[NZ], t[NZ], tr_b[NZ], src_b[NZ], t_b[NZ];
+template <int NZ, class A = double>
+CRTM_HD void adding_clear_adjoint(int nZ, const double* mu, double od, double B, const Mat<NZ, A>& Rup,
+                                  const A* rad, Mat<NZ, A>& Rup_b, A* rad_b, double* od_b, double* B_b) {
+  A tr[NZ], src[NZ], om[NZ], t[NZ], tr_b[NZ], src_b[NZ], t_b[NZ];
+  const A Bw = A(B);
   for (int i = 0; i < nZ; i++) {
-    tr[i] = exp(-od / mu[i]);
-    src[i] = B * (1.0 - tr[i]);
+    const A x = A(-od / mu[i]);
+    tr[i] = exp(x);
+    om[i] = -expm1(x);   // 1 - t_i
+    src[i] = Bw * om[i];
   }
   for (int i = 0; i < nZ; i++) {
-    double v = rad[i];
+    A v = rad[i];
     for (int j = 0; j < nZ; j++) v += Rup.a[i][j] * src[j];
     t[i] = v;
   }
@@ -1088,7 +1139,7 @@ CRTM_HD void adding_clear_adjoint(int nZ, const double* mu, double od, double B,
   }
   for (int i = 0; i < nZ; i++)
     for (int j = 0; j < nZ; j++) {
-      const double g = Rup_b.a[i][j];
+      const A g = Rup_b.a[i][j];
       tr_b[i] += g * Rup.a[i][j] * tr[j];
       tr_b[j] += g * tr[i] * Rup.a[i][j];
       Rup_b.a[i][j] = g * tr[i] * tr[j];
@@ -1101,36 +1152,35 @@ CRTM_HD void adding_clear_adjoint(int nZ, const double* mu, double od, double B,
       src_b[j] += t_b[i] * Rup.a[i][j];
     }
   }
-  double ob = 0.0, bb = 0.0;
+  A ob = A(0.0), bb = A(0.0);
   for (int i = 0; i < nZ; i++) {
-    bb += src_b[i] * (1.0 - tr[i]);
-    tr_b[i] -= src_b[i] * B;
-    ob -= tr_b[i] * tr[i] / mu[i];
+    bb += src_b[i] * om[i];
+    tr_b[i] -= src_b[i] * Bw;
+    ob -= tr_b[i] * tr[i] / A(mu[i]);
   }
-  *od_b = ob;
-  *B_b = bb;
+  *od_b = double(ob);
+  *B_b = double(bb);
 }
 
 // Scattering layer (transmission T, reflection R, source src): adjoints of the
 // layer's T, R and src.  Returns false on a singular (I - Rup R).
-template <int NZ>
-CRTM_HD bool adding_scatter_adjoint(int nZ, const Mat<NZ, double>& Tm, const Mat<NZ, double>& Rm,
-                                    const double* src, const Mat<NZ, double>& Rup, const double* rad,
-                                    Mat<NZ, double>& Rup_b, double* rad_b, Mat<NZ, double>& T_b,
-                                    Mat<NZ, double>& R_b, double* src_b) {
-  Mat<NZ, double> G, IGT, RT, M1, M2;
-  double t[NZ], t_b[NZ];
+template <int NZ, class A = double>
+CRTM_HD bool adding_scatter_adjoint(int nZ, const Mat<NZ, A>& Tm, const Mat<NZ, A>& Rm, const A* src,
+                                    const Mat<NZ, A>& Rup, const A* rad, Mat<NZ, A>& Rup_b, A* rad_b,
+                                    Mat<NZ, A>& T_b, Mat<NZ, A>& R_b, A* src_b) {
+  Mat<NZ, A> G, IGT, RT, M1, M2;
+  A t[NZ], t_b[NZ];
   for (int i = 0; i < nZ; i++)
     for (int j = 0; j < nZ; j++) {
-      double v = 0.0;
+      A v = A(0.0);
       for (int m = 0; m < nZ; m++) v += Rup.a[i][m] * Rm.a[m][j];
-      G.a[i][j] = (i == j ? 1.0 : 0.0) - v;
+      G.a[i][j] = (i == j ? A(1.0) : A(0.0)) - v;
     }
-  if (!mat_invert<NZ, double>(nZ, G)) return false;     // G now holds Gamma
-  mat_mul<NZ, double>(nZ, Tm, G, IGT);
-  mat_mul<NZ, double>(nZ, Rup, Tm, RT);
+  if (!invert_fp64<NZ, A>(nZ, G)) return false;     // G now holds Gamma
+  mat_mul<NZ, A>(nZ, Tm, G, IGT);
+  mat_mul<NZ, A>(nZ, Rup, Tm, RT);
   for (int i = 0; i < nZ; i++) {
-    double v = rad[i];
+    A v = rad[i];
     for (int j = 0; j < nZ; j++) v += Rup.a[i][j] * src[j];
     t[i] = v;
   }
@@ -1138,28 +1188,28 @@ CRTM_HD bool adding_scatter_adjoint(int nZ, const Mat<NZ, double>& Tm, const Mat
   for (int i = 0; i < nZ; i++) {
     src_b[i] = rad_b[i];
     for (int j = 0; j < nZ; j++) {
-      double v = rad_b[i] * t[j];
+      A v = rad_b[i] * t[j];
       for (int m = 0; m < nZ; m++) v += Rup_b.a[i][m] * RT.a[j][m];
       M1.a[i][j] = v;
     }
   }
   for (int j = 0; j < nZ; j++) {
-    double v = 0.0;
+    A v = A(0.0);
     for (int i = 0; i < nZ; i++) v += IGT.a[i][j] * rad_b[i];
     t_b[j] = v;
   }
   for (int i = 0; i < nZ; i++)
     for (int j = 0; j < nZ; j++) {
-      double v = 0.0;
+      A v = A(0.0);
       for (int m = 0; m < nZ; m++) v += IGT.a[m][i] * Rup_b.a[m][j];
       M2.a[i][j] = v;
       R_b.a[i][j] = Rup_b.a[i][j];
     }
   // RT = Rup T:  Rup_b = RT_b T^T ;  T_b = Rup^T RT_b
-  Mat<NZ, double> Rb_new;
+  Mat<NZ, A> Rb_new;
   for (int i = 0; i < nZ; i++)
     for (int j = 0; j < nZ; j++) {
-      double a = 0.0, b = 0.0;
+      A a = A(0.0), b = A(0.0);
       for (int m = 0; m < nZ; m++) {
         a += M2.a[i][m] * Tm.a[j][m];
         b += Rup.a[m][i] * M2.a[m][j];
@@ -1178,7 +1228,7 @@ CRTM_HD bool adding_scatter_adjoint(int nZ, const Mat<NZ, double>& Tm, const Mat
   // IGT = T Gamma:  T_b += IGT_b Gamma^T ;  Gamma_b = T^T IGT_b (in M2)
   for (int i = 0; i < nZ; i++)
     for (int j = 0; j < nZ; j++) {
-      double a = 0.0, b = 0.0;
+      A a = A(0.0), b = A(0.0);
       for (int m = 0; m < nZ; m++) {
         a += M1.a[i][m] * G.a[j][m];
         b += Tm.a[m][i] * M1.a[m][j];
@@ -1189,20 +1239,20 @@ CRTM_HD bool adding_scatter_adjoint(int nZ, const Mat<NZ, double>& Tm, const Mat
   // Gamma = G^-1:  G_b = -Gamma^T Gamma_b Gamma^T (in M1)
   for (int i = 0; i < nZ; i++)
     for (int j = 0; j < nZ; j++) {
-      double v = 0.0;
+      A v = A(0.0);
       for (int m = 0; m < nZ; m++) v += M2.a[i][m] * G.a[j][m];
       IGT.a[i][j] = v;   // Gamma_b Gamma^T
     }
   for (int i = 0; i < nZ; i++)
     for (int j = 0; j < nZ; j++) {
-      double v = 0.0;
+      A v = A(0.0);
       for (int m = 0; m < nZ; m++) v += G.a[m][i] * IGT.a[m][j];
       M1.a[i][j] = -v;
     }
   // G = I - Rup R:  Rup_b -= G_b R^T ;  R_b -= Rup^T G_b
   for (int i = 0; i < nZ; i++)
     for (int j = 0; j < nZ; j++) {
-      double a = 0.0, b = 0.0;
+      A a = A(0.0), b = A(0.0);
       for (int m = 0; m < nZ; m++) {
         a += M1.a[i][m] * Rm.a[j][m];
         b += Rup.a[m][i] * M1.a[m][j];
@@ -1606,46 +1656,50 @@ CRTM_HD int layer_contract(const CloudyColumn& in, const CloudLut& lut, const St
 // clear layer: od_b and the Planck radiance's B_b).  Returns the radiance and
 // the derivatives with respect to the surface emissivity (reflectivity 1 - e)
 // and the surface Planck radiance.
-template <int NZ, class LayerFn, class StateFn, class AdjFn>
+template <int NZ, class LayerFn, class StateFn, class AdjFn, class A = double>
 CRTM_HD int cloudy_adjoint(const CloudyColumn& in, const StreamSet<NZ, double>& S, LayerFn layer,
                            StateFn state, AdjFn adj, double* radiance, double* e_b, double* Bs_b) {
   const int nZ = S.nZ, Ku = in.Ku;
-  AddingState<NZ> A;
-  adding_init<NZ>(A, nZ, in.emissivity, in.planck_surface);
+  auto planck = [&](int k) -> double {   // the layer's Planck radiance, in A
+    const A te = A(in.b1) + A(in.b2) * A(in.temperature[k]);
+    return double(A(in.c1) / (exp(A(in.c2) / te) - A(1.0)));
+  };
+  AddingState<NZ, A> St;
+  adding_init<NZ, A>(St, nZ, in.emissivity, in.planck_surface);
   auto save = [&](int lev) {
     for (int i = 0; i < nZ; i++) {
-      for (int j = 0; j < nZ; j++) state(lev, i * NZ + j) = A.Rup.a[i][j];
-      state(lev, NZ * NZ + i) = A.rad[i];
+      for (int j = 0; j < nZ; j++) state(lev, i * NZ + j) = St.Rup.a[i][j];
+      state(lev, NZ * NZ + i) = St.rad[i];
     }
   };
-  auto load = [&](int lev, Mat<NZ, double>& Rup, double* rad) {
+  auto load = [&](int lev, Mat<NZ, A>& Rup, A* rad) {
     for (int i = 0; i < nZ; i++) {
       for (int j = 0; j < nZ; j++) Rup.a[i][j] = state(lev, i * NZ + j);
       rad[i] = state(lev, NZ * NZ + i);
     }
   };
   save(Ku);
-  Mat<NZ, double> Tm, Rm;
-  double src[NZ];
+  Mat<NZ, A> Tm, Rm;
+  A src[NZ];
   for (int k = Ku - 1; k >= 0; k--) {
     int kind;
     double od;
     layer(k, &kind, &od, Tm, Rm, src);
     if (kind < 0) return -kind;
     if (kind == 1) {
-      if (!adding_scatter<NZ>(A, nZ, Tm, Rm, src)) return 6;
+      if (!adding_scatter<NZ, A>(St, nZ, Tm, Rm, src)) return 6;
     } else {
-      adding_clear<NZ>(A, nZ, S.mu, od, in.c1 / (exp(in.c2 / (in.b1 + in.b2 * in.temperature[k])) - 1.0));
+      adding_clear<NZ, A>(St, nZ, S.mu, od, planck(k));
     }
     save(k);
   }
-  *radiance = adding_toa<NZ>(A, nZ, S.isat, in.cosmic);
+  *radiance = adding_toa<NZ, A>(St, nZ, S.isat, in.cosmic);
   // adjoint of the TOA radiance
-  Mat<NZ, double> Rup_b, Rup, T_b, R_b;
-  double rad_b[NZ], rad[NZ], src_b[NZ];
+  Mat<NZ, A> Rup_b, Rup, T_b, R_b;
+  A rad_b[NZ], rad[NZ], src_b[NZ];
   for (int i = 0; i < nZ; i++) {
-    rad_b[i] = (i == S.isat) ? 1.0 : 0.0;
-    for (int j = 0; j < nZ; j++) Rup_b.a[i][j] = (i == S.isat) ? in.cosmic : 0.0;
+    rad_b[i] = (i == S.isat) ? A(1.0) : A(0.0);
+    for (int j = 0; j < nZ; j++) Rup_b.a[i][j] = (i == S.isat) ? A(in.cosmic) : A(0.0);
   }
   for (int k = 0; k < Ku; k++) {
     load(k + 1, Rup, rad);
@@ -1653,17 +1707,17 @@ CRTM_HD int cloudy_adjoint(const CloudyColumn& in, const StreamSet<NZ, double>& 
     double od;
     layer(k, &kind, &od, Tm, Rm, src);
     if (kind == 1) {
-      if (!adding_scatter_adjoint<NZ>(nZ, Tm, Rm, src, Rup, rad, Rup_b, rad_b, T_b, R_b, src_b)) return 6;
+      if (!adding_scatter_adjoint<NZ, A>(nZ, Tm, Rm, src, Rup, rad, Rup_b, rad_b, T_b, R_b, src_b)) return 6;
       adj(k, kind, T_b, R_b, src_b, 0.0, 0.0);
     } else {
-      const double B = in.c1 / (exp(in.c2 / (in.b1 + in.b2 * in.temperature[k])) - 1.0);
+      const double B = planck(k);
       double od_b, B_b;
-      adding_clear_adjoint<NZ>(nZ, S.mu, od, B, Rup, rad, Rup_b, rad_b, &od_b, &B_b);
+      adding_clear_adjoint<NZ, A>(nZ, S.mu, od, B, Rup, rad, Rup_b, rad_b, &od_b, &B_b);
       adj(k, kind, T_b, R_b, src_b, od_b, B_b);
     }
   }
   double tr = 0.0, sr = 0.0;
-  for (int i = 0; i < nZ; i++) { tr += Rup_b.a[i][i]; sr += rad_b[i]; }
+  for (int i = 0; i < nZ; i++) { tr += double(Rup_b.a[i][i]); sr += double(rad_b[i]); }
   *e_b = -tr + in.planck_surface * sr;
   *Bs_b = in.emissivity * sr;
   return 0;

@@ -14,17 +14,8 @@ GaussTable make_gauss() {
 }
 }  // namespace
 
-// precision experiments: FP32 records with FP64 for layers whose smallest
-// row absorptance is below g_fp64_absorptance (0: none)
-static double g_fp64_absorptance = 0.0;
-static long g_fp64_layers = 0, g_all_layers = 0;
-static int g_fp32_layer = -1;   // >= 0: only that layer in FP32
-
 extern "C" {
 
-void sx_set_fp64_absorptance(double a) { g_fp64_absorptance = a; g_fp64_layers = g_all_layers = 0; }
-void sx_set_fp32_layer(int k) { g_fp32_layer = k; }
-double sx_fp64_fraction() { return g_all_layers ? (double)g_fp64_layers / g_all_layers : 0.0; }
 
 int sx_ada_layer(int nS, int nZ, double w, double tau, const double* mu, const double* wt,
                  const double* ff, const double* bb, double B, double* T, double* R, double* src) {
@@ -100,8 +91,8 @@ int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, 
   c.n_aerosols = n_aer; c.wavenumber = wavenumber; c.aerosol_type = aer_type; c.conc = conc;
   c.aer_reff = aer_reff; c.aer_var = aer_var; c.rh = rh_layers; c.alut = &A;
   c.soi = soi != 0;
-  if (soi >= 2 && soi <= 4) {   // layered ADA as the GPU kernels run it (records with NZ = 10);
-    c.soi = false;               // layer optics in FP64 (2), double-float (3) or FP32 (4)
+  if (soi >= 2 && soi <= 5) {   // layered ADA as the GPU kernels run it (records with NZ = 10);
+    c.soi = false;               // layer optics in FP64 (2), double-float (3), FP32 (4; 5: FP32 records)
     constexpr int NZ = SC_NZ_MAX, NE = 2 + 2 * NZ * NZ + NZ;
     StreamSet<NZ, double> S;
     if (int rc = stream_set<NZ, double>(nleg, mu_sensor, n_clouds > 0 ? L.nleg : -1, gt, S)) return rc;
@@ -112,22 +103,17 @@ int sx_cloudy_radiance(const int* dims, const double* f_mw, const double* r_mw, 
       int kind;
       if (soi == 3)
         kind = layer_optics<NZ, double, DD>(c, L, S, k, DD(od[k]), DD(temp[k]), &o, Tm, Rm, srcv);
-      else if (soi == 4 && (g_fp32_layer < 0 || g_fp32_layer == k)) {
+      else if (soi == 4)
         kind = layer_optics<NZ, double, float>(c, L, S, k, float(od[k]), float(temp[k]), &o, Tm, Rm, srcv);
-        if (kind == 1 && g_fp64_absorptance > 0.0) {
-          double amin = 1.0;
-          for (int i = 0; i < S.nZ; i++) {
-            double th = 0.0;
-            for (int j = 0; j < S.nS; j++) th += Tm.a[i][j] + Rm.a[i][j];
-            if (S.nZ == S.nS + 1 && i == S.nZ - 1) th += Tm.a[i][i];
-            amin = 1.0 - th < amin ? 1.0 - th : amin;
-          }
-          if (amin < g_fp64_absorptance) {
-            g_fp64_layers++;
-            kind = layer_optics<NZ, double>(c, L, S, k, od[k], temp[k], &o, Tm, Rm, srcv);
-          }
+      else if (soi == 5) {   // FP32 layer solver and FP32 records (the mixed forward)
+        Mat<NZ, float> Tf, Rf;
+        float sf[NZ], of;
+        kind = layer_optics<NZ, float, float>(c, L, S, k, float(od[k]), float(temp[k]), &of, Tf, Rf, sf);
+        o = of;
+        for (int i = 0; i < NZ; i++) {
+          srcv[i] = sf[i];
+          for (int j = 0; j < NZ; j++) { Tm.a[i][j] = Tf.a[i][j]; Rm.a[i][j] = Rf.a[i][j]; }
         }
-        g_all_layers += kind == 1;
       }
       else
         kind = layer_optics<NZ, double>(c, L, S, k, od[k], temp[k], &o, Tm, Rm, srcv);
@@ -488,4 +474,74 @@ extern "C" int sx_layer_adjoint_compare(
     g_dual[4 + 3 * s] = gd[0];
   }
   return kr;
+}
+
+
+// K-matrix of one cloudy (profile, channel) through ADA as the mixed form
+// computes it (mixed != 0: layer records from the FP32 layer solver in loss
+// form, the adding and its adjoint in FP32 with the (I - Rup R)^-1 inversions
+// in FP64, the layers' reverse sweep in FP32) or the FP64 form (mixed = 0):
+// radiance, dR/d(gas OD_k), dR/dT_k, dR/de, dR/dB_surface and each cloud's
+// dR/dwc, dR/dre.  Arguments as sx_cloudy_kmatrix's.
+template <class A>
+static int cloudy_kmatrix_form(const CloudyColumn& c, const CloudLut& L, const StreamSet<SC_NZ_MAX, double>& S,
+                               const double* od, double* radiance, double* dgas, double* dT, double* e_b,
+                               double* Bs_b, double* dwc, double* dre, int cstride) {
+  constexpr int NZ = SC_NZ_MAX;
+  auto layer = [&](int k, int* kind, double* o, Mat<NZ, A>& Tm, Mat<NZ, A>& Rm, A* src) {
+    A ow;
+    *kind = layer_optics<NZ, A, A>(c, L, S, k, A(od[k]), A(c.temperature[k]), &ow, Tm, Rm, src);
+    *o = double(ow);
+  };
+  std::vector<A> st((size_t)(c.Ku + 1) * (NZ * NZ + NZ));
+  auto state = [&](int lev, int i) -> A& { return st[(size_t)lev * (NZ * NZ + NZ) + i]; };
+  int bad = 0;
+  auto adj = [&](int k, int kind, const Mat<NZ, A>& T_b, const Mat<NZ, A>& R_b, const A* src_b, double od_b,
+                 double B_b) {
+    Mat<NZ, double> Tb, Rb;
+    double sb[NZ];
+    for (int i = 0; i < NZ; i++) {
+      sb[i] = kind == 1 ? double(src_b[i]) : 0.0;
+      for (int j = 0; j < NZ; j++) {
+        Tb.a[i][j] = kind == 1 ? double(T_b.a[i][j]) : 0.0;
+        Rb.a[i][j] = kind == 1 ? double(R_b.a[i][j]) : 0.0;
+      }
+    }
+    double g[2], gs[2 * SC_NC_MAX][3];
+    const int kr = layer_adjoint<NZ, A>(c, L, S, k, od[k], kind, Tb, Rb, sb, kind == 1 ? 0.0 : od_b,
+                                        kind == 1 ? 0.0 : B_b, g, gs);
+    if (kr != kind) bad = 7;
+    dgas[k] = g[0];
+    dT[k] = g[1];
+    for (int cc = 0; cc < c.n_clouds; cc++) {
+      dwc[(size_t)cc * cstride + k] = gs[cc][0];
+      dre[(size_t)cc * cstride + k] = gs[cc][1];
+    }
+  };
+  const int rc = cloudy_adjoint<NZ, decltype(layer), decltype(state), decltype(adj), A>(c, S, layer, state, adj,
+                                                                                        radiance, e_b, Bs_b);
+  return rc ? rc : bad;
+}
+
+extern "C" int sx_cloudy_kmatrix_form(const int* dims, const double* f_mw, const double* r_mw, const double* t,
+                                      const double* f_ir, const double* r_ir, const double* ke_l, const double* w_l,
+                                      const double* pc_l, const double* ke_s, const double* w_s, const double* pc_s,
+                                      const double* ke_ir, const double* w_ir, const double* pc_ir, int Ku,
+                                      int n_clouds, int nleg, int microwave, double freq, double mu_sensor,
+                                      double emissivity, double planck_surface, double cosmic, const double* planck,
+                                      const double* temp, const int* cloud_type, const double* wc, const double* reff,
+                                      int cstride, const double* od, double* radiance, double* dgas, double* dT,
+                                      double* e_b, double* Bs_b, double* dwc, double* dre, int mixed) {
+  CloudLut L{dims[0], dims[1], dims[2], dims[3], dims[4], dims[5], dims[6], f_mw, r_mw, t, f_ir, r_ir,
+             ke_l, w_l, pc_l, ke_s, w_s, pc_s, ke_ir, w_ir, pc_ir};
+  static const GaussTable gt = make_gauss();
+  CloudyColumn c{};
+  c.Ku = Ku; c.n_clouds = n_clouds; c.nleg = nleg; c.microwave = microwave != 0; c.freq = freq;
+  c.mu_sensor = mu_sensor; c.emissivity = emissivity; c.planck_surface = planck_surface; c.cosmic = cosmic;
+  c.c1 = planck[0]; c.c2 = planck[1]; c.b1 = planck[2]; c.b2 = planck[3];
+  c.temperature = temp; c.cloud_type = cloud_type; c.wc = wc; c.reff = reff; c.cstride = (size_t)cstride;
+  StreamSet<SC_NZ_MAX, double> S;
+  if (int rc = stream_set<SC_NZ_MAX, double>(nleg, mu_sensor, L.nleg, gt, S)) return rc;
+  return mixed ? cloudy_kmatrix_form<float>(c, L, S, od, radiance, dgas, dT, e_b, Bs_b, dwc, dre, cstride)
+               : cloudy_kmatrix_form<double>(c, L, S, od, radiance, dgas, dT, e_b, Bs_b, dwc, dre, cstride);
 }
