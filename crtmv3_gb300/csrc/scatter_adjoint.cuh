@@ -104,15 +104,22 @@ CRTM_HD bool ada_layer_adjoint(int nS, int nZ, T w, T tau, const T* mu, const T*
     *B_b = bsum;
     return true;
   }
-  // ---- forward, keeping what the reverse sweep reads ----
+  // ---- forward in the loss form of ada_layer_loss, keeping what the
+  // reverse sweep reads.  With P = Gm^-1 Gp, D = diag(1 - exp(-ev tau)) and
+  // e = diag(exp(-ev tau)):  W = D P e + P D,  Q = Gm - Gp P,  GA = Q + Gp W,
+  // U = (Q D + Gp W) GA^-1 = I - T,  R = (Gp D + Gm D P e) GA^-1.  Every
+  // term of U and R is O(tau) for a thin layer, and so is every adjoint that
+  // reaches the eigen-decomposition below: the FP32 form keeps its relative
+  // accuracy where the plain form T = Tt GA^-1 loses it to cancellation.
   const T s = w < T(MAX_ALBEDO) ? w : T(MAX_ALBEDO);
-  Mat<NZ, T> E, iX, Gp, Gm, iGm, A2, iGA, Tm, Rm, M1, M2, M3;
-  T lam[NZ], ev[NZ], ex[NZ];
-  if (!mom_eigen<NZ, T>(nS, nZ, s, mu, wt, ff, bb, E, lam, iX, M1, M2, M3, gap)) return false;
+  Mat<NZ, T> E, iX, Gp, Gm, iGm, P, W, iGA, Um, Rm, T1, T2;
+  T lam[NZ], ev[NZ], ex[NZ], dx[NZ], buf[NZ];
+  if (!mom_eigen<NZ, T>(nS, nZ, s, mu, wt, ff, bb, E, lam, iX, T1, T2, Um, gap)) return false;
   if (!mat_invert(n, iX)) return false;   // (PP - PM)^-1
   for (int i = 0; i < n; i++) {
     ev[i] = lam[i] > T(0.0) ? sqrt(lam[i]) : T(0.0);
     ex[i] = exp(-ev[i] * tau);
+    dx[i] = -expm1(-ev[i] * tau);
   }
   // EF = (PP-PM)^-1 E diag(ev);  Gp = (E + EF)/2, Gm = (E - EF)/2
   for (int i = 0; i < n; i++)
@@ -125,117 +132,150 @@ CRTM_HD bool ada_layer_adjoint(int nS, int nZ, T w, T tau, const T* mu, const T*
     }
   iGm = Gm;
   if (!mat_invert(n, iGm)) return false;
-  // A2 = Gm^-1 Gp diag(ex)
+  mat_mul(n, iGm, Gp, P);
   for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) W.a[i][j] = dx[i] * P.a[i][j] * ex[j] + P.a[i][j] * dx[j];
+  for (int i = 0; i < n; i++)   // Q (T1)
     for (int j = 0; j < n; j++) {
       T v = T(0.0);
-      for (int k = 0; k < n; k++) v += iGm.a[i][k] * Gp.a[k][j];
-      A2.a[i][j] = v * ex[j];
+      for (int k = 0; k < n; k++) v += Gp.a[i][k] * P.a[k][j];
+      T1.a[i][j] = Gm.a[i][j] - v;
     }
-  // GA = Gm - Gp diag(ex) A2;  Tt = Gm diag(ex) - Gp A2 (M1);  Rt = Gp - Gm diag(ex) A2 (M2)
+  // GA (iGA), U numerator (T1, in place over Q), R numerator (T2)
   for (int i = 0; i < n; i++)
     for (int j = 0; j < n; j++) {
-      T a5 = T(0.0), a3 = T(0.0), a6 = T(0.0);
+      T gw = T(0.0), gd = T(0.0);
       for (int k = 0; k < n; k++) {
-        a5 += Gp.a[i][k] * ex[k] * A2.a[k][j];
-        a3 += Gp.a[i][k] * A2.a[k][j];
-        a6 += Gm.a[i][k] * ex[k] * A2.a[k][j];
+        gw += Gp.a[i][k] * W.a[k][j];
+        gd += Gm.a[i][k] * dx[k] * P.a[k][j];
       }
-      iGA.a[i][j] = Gm.a[i][j] - a5;
-      M1.a[i][j] = Gm.a[i][j] * ex[j] - a3;
-      M2.a[i][j] = Gp.a[i][j] - a6;
+      iGA.a[i][j] = T1.a[i][j] + gw;
+      T1.a[i][j] = T1.a[i][j] * dx[j] + gw;
+      T2.a[i][j] = Gp.a[i][j] * dx[j] + gd * ex[j];
     }
   if (!mat_invert(n, iGA)) return false;
-  mat_mul(n, M1, iGA, Tm);
-  mat_mul(n, M2, iGA, Rm);
+  mat_mul(n, T1, iGA, Um);
+  mat_mul(n, T2, iGA, Rm);
   // ---- reverse ----
-  // Scratch schedule (12 matrices): E, iX, Gp, Gm, iGm, A2, iGA are the
-  // forward's; Tm, Rm, M1, M2, M3 are reused as each earlier value dies.
-  // src_i = (1 - th_i) B with th_i the row sum of T + R over the quadrature
-  // columns (and T's diagonal on the sensor row).
-  Mat<NZ, T>& Tb = M1;   // total T adjoint
-  Mat<NZ, T>& Rb = M2;   // total R adjoint
+  // src_i = a_i B with a_i the row sum of U - R over the quadrature columns
+  // (and U's diagonal on the sensor row); U_b = -T_b.  U_b in T1, R_b in T2.
   T bsum = T(0.0);
   for (int i = 0; i < n; i++) {
-    T th = T(0.0);
-    for (int j = 0; j < nS; j++) th += Tm.a[i][j] + Rm.a[i][j];
-    if (sensor_row && i == n - 1) th += Tm.a[i][i];
-    bsum += src_b[i] * (T(1.0) - th);
-    const T th_b = -src_b[i] * B;
+    T a = T(0.0);
+    for (int j = 0; j < nS; j++) a += Um.a[i][j] - Rm.a[i][j];
+    if (sensor_row && i == n - 1) a += Um.a[i][i];
+    bsum += src_b[i] * a;
+    const T sb = src_b[i] * B;
     for (int j = 0; j < n; j++) {
-      const bool in_th = j < nS || (sensor_row && i == n - 1 && j == i);
-      Tb.a[i][j] = T_b.a[i][j] + (in_th ? th_b : T(0.0));
-      Rb.a[i][j] = R_b.a[i][j] + (j < nS ? th_b : T(0.0));
+      const bool in_a = j < nS || (sensor_row && i == n - 1 && j == i);
+      T1.a[i][j] = (in_a ? sb : T(0.0)) - T_b.a[i][j];
+      T2.a[i][j] = R_b.a[i][j] - (j < nS ? sb : T(0.0));
     }
   }
   *B_b = bsum;
-  // T = Tt GA^-1, R = Rt GA^-1:
-  //   GA_b = -(T^T Tb + R^T Rb) GA^-T;  Tt_b = Tb GA^-T;  Rt_b = Rb GA^-T
+  // U = Un GA^-1, R = Rn GA^-1:  Un_b = U_b GA^-T, Rn_b = R_b GA^-T (row by
+  // row in place), then GA_b = -(U^T Un_b + R^T Rn_b) into iGA
+  for (int i = 0; i < n; i++) {
+    for (int j = 0; j < n; j++) {
+      T v = T(0.0);
+      for (int k = 0; k < n; k++) v += T1.a[i][k] * iGA.a[j][k];
+      buf[j] = v;
+    }
+    for (int j = 0; j < n; j++) T1.a[i][j] = buf[j];
+    for (int j = 0; j < n; j++) {
+      T v = T(0.0);
+      for (int k = 0; k < n; k++) v += T2.a[i][k] * iGA.a[j][k];
+      buf[j] = v;
+    }
+    for (int j = 0; j < n; j++) T2.a[i][j] = buf[j];
+  }
   for (int i = 0; i < n; i++)
     for (int j = 0; j < n; j++) {
       T v = T(0.0);
-      for (int k = 0; k < n; k++) v += Tm.a[k][i] * Tb.a[k][j] + Rm.a[k][i] * Rb.a[k][j];
-      M3.a[i][j] = v;
+      for (int k = 0; k < n; k++) v += Um.a[k][i] * T1.a[k][j] + Rm.a[k][i] * T2.a[k][j];
+      iGA.a[i][j] = -v;
     }
-  Mat<NZ, T>& GAb = Tm;
-  mat_mul_nt(n, M3, iGA, GAb);
-  for (int i = 0; i < n; i++)
-    for (int j = 0; j < n; j++) GAb.a[i][j] = -GAb.a[i][j];
-  Mat<NZ, T>& Ttb = Rm;
-  Mat<NZ, T>& Rtb = M3;
-  mat_mul_nt(n, Tb, iGA, Ttb);
-  mat_mul_nt(n, Rb, iGA, Rtb);
-  // Tt = Gm diag(ex) - Gp A2;  Rt = Gp - Gm diag(ex) A2;  GA = Gm - Gp diag(ex) A2:
-  //   Gm_b = GA_b + (Tt_b - Rt_b A2^T) diag(ex)
-  //   Gp_b = Rt_b - Tt_b A2^T - GA_b A2^T diag(ex)
-  //   ex_b_j = sum_i Gm_ij (Tt_b - Rt_b A2^T)_ij - Gp_ij (GA_b A2^T)_ij
-  //   A2_b = -(Gp^T Tt_b + diag(ex) (Gm^T Rt_b + Gp^T GA_b))
-  Mat<NZ, T>& Gmb = M1;   // Tb, Rb are dead
-  Mat<NZ, T>& Gpb = M2;
-  T ex_b[NZ];
-  for (int j = 0; j < n; j++) ex_b[j] = T(0.0);
+  Mat<NZ, T>& GAb = iGA;
+  Mat<NZ, T>& Qb = Um;   // U, R are dead
+  Mat<NZ, T>& Wb = Rm;
+  T dx_b[NZ], ex_b[NZ];
+  for (int j = 0; j < n; j++) { dx_b[j] = T(0.0); ex_b[j] = T(0.0); }
+  // Un = Q D + Gp W, GA = Q + Gp W:  Q_b = Un_b D + GA_b;  dx_b_j += sum_i Un_b_ij Q_ij;
+  //   with S = Un_b + GA_b (T1):  W_b = Gp^T S;  Gp_b = S W^T
   for (int i = 0; i < n; i++)
     for (int j = 0; j < n; j++) {
-      T rA = T(0.0), tA = T(0.0), gA = T(0.0);
+      T v = T(0.0);
+      for (int k = 0; k < n; k++) v += Gp.a[i][k] * P.a[k][j];
+      dx_b[j] += T1.a[i][j] * (Gm.a[i][j] - v);
+      Qb.a[i][j] = T1.a[i][j] * dx[j] + GAb.a[i][j];
+      T1.a[i][j] += GAb.a[i][j];
+    }
+  mat_mul_tn(n, Gp, T1, Wb);
+  Mat<NZ, T>& Gpb = iGA;   // GA_b is dead
+  mat_mul_nt(n, T1, W, Gpb);
+  Mat<NZ, T>& Gmb = T1;    // S is dead
+  // Rn = Gp D + Gm D P e:  Gp_b += Rn_b D;  dx_b_j += sum_i Rn_b_ij Gp_ij;
+  //   ex_b_j += sum_i Rn_b_ij (Gm D P)_ij;  with Z = Rn_b e:  Gm_b = Z P^T D,
+  //   dx_b_k += sum_i Gm_ik (Z P^T)_ik;  P_b = D Gm^T Z (column by column into T2)
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) {
+      const T rb = T2.a[i][j];
+      Gpb.a[i][j] += rb * dx[j];
+      T g = T(0.0);
+      for (int k = 0; k < n; k++) g += Gm.a[i][k] * dx[k] * P.a[k][j];
+      dx_b[j] += rb * Gp.a[i][j];
+      ex_b[j] += rb * g;
+    }
+  for (int i = 0; i < n; i++)
+    for (int k = 0; k < n; k++) {
+      T zp = T(0.0);
+      for (int j = 0; j < n; j++) zp += T2.a[i][j] * ex[j] * P.a[k][j];
+      Gmb.a[i][k] = zp * dx[k];
+      dx_b[k] += Gm.a[i][k] * zp;
+    }
+  for (int j = 0; j < n; j++) {
+    for (int k = 0; k < n; k++) {
+      T v = T(0.0);
+      for (int i = 0; i < n; i++) v += Gm.a[i][k] * T2.a[i][j];
+      buf[k] = dx[k] * v * ex[j];
+    }
+    for (int k = 0; k < n; k++) T2.a[k][j] = buf[k];
+  }
+  Mat<NZ, T>& Pb = T2;
+  // Q = Gm - Gp P:  Gm_b += Q_b;  Gp_b -= Q_b P^T;  P_b -= Gp^T Q_b
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) {
+      T a = T(0.0), b = T(0.0);
       for (int k = 0; k < n; k++) {
-        rA += Rtb.a[i][k] * A2.a[j][k];
-        tA += Ttb.a[i][k] * A2.a[j][k];
-        gA += GAb.a[i][k] * A2.a[j][k];
+        a += Qb.a[i][k] * P.a[j][k];
+        b += Gp.a[k][i] * Qb.a[k][j];
       }
-      Gmb.a[i][j] = GAb.a[i][j] + (Ttb.a[i][j] - rA) * ex[j];
-      Gpb.a[i][j] = Rtb.a[i][j] - tA - gA * ex[j];
-      ex_b[j] += Gm.a[i][j] * (Ttb.a[i][j] - rA) - Gp.a[i][j] * gA;
+      Gmb.a[i][j] += Qb.a[i][j];
+      Gpb.a[i][j] -= a;
+      Pb.a[i][j] -= b;
     }
-  Mat<NZ, T>& A2b = iGA;  // iGA is dead
+  // W_ij = dx_i P_ij ex_j + P_ij dx_j
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) {
+      const T wb = Wb.a[i][j], pij = P.a[i][j];
+      Pb.a[i][j] += wb * (dx[i] * ex[j] + dx[j]);
+      dx_b[i] += wb * pij * ex[j];
+      ex_b[j] += wb * dx[i] * pij;
+      dx_b[j] += wb * pij;
+    }
+  // P = Gm^-1 Gp:  K = Gm^-T P_b;  Gp_b += K;  Gm_b -= K P^T
+  Mat<NZ, T>& Kt = Um;   // Q_b is dead
+  mat_mul_tn(n, iGm, Pb, Kt);
   for (int i = 0; i < n; i++)
     for (int j = 0; j < n; j++) {
       T v = T(0.0);
-      for (int k = 0; k < n; k++)
-        v += Gp.a[k][i] * Ttb.a[k][j] + ex[i] * (Gm.a[k][i] * Rtb.a[k][j] + Gp.a[k][i] * GAb.a[k][j]);
-      A2b.a[i][j] = -v;
+      for (int k = 0; k < n; k++) v += Kt.a[i][k] * P.a[j][k];
+      Gpb.a[i][j] += Kt.a[i][j];
+      Gmb.a[i][j] -= v;
     }
-  // A2 = Gm^-1 A1 with A1 = Gp diag(ex):  A1_b = Gm^-T A2_b;  (Gm^-1)_b = A2_b A1^T;
-  //   Gp_b += A1_b diag(ex);  ex_b_j += sum_i A1_b_ij Gp_ij;  Gm_b += -Gm^-T (Gm^-1)_b Gm^-T
-  Mat<NZ, T>& A1b = Tm;   // GA_b, Tt_b, Rt_b are dead
-  Mat<NZ, T>& iGmb = Rm;
-  mat_mul_tn(n, iGm, A2b, A1b);
-  for (int i = 0; i < n; i++)
-    for (int j = 0; j < n; j++) {
-      T v = T(0.0);
-      for (int k = 0; k < n; k++) v += A2b.a[i][k] * Gp.a[j][k] * ex[k];
-      iGmb.a[i][j] = v;
-    }
-  for (int i = 0; i < n; i++)
-    for (int j = 0; j < n; j++) {
-      Gpb.a[i][j] += A1b.a[i][j] * ex[j];
-      ex_b[j] += A1b.a[i][j] * Gp.a[i][j];
-    }
-  inverse_adjoint(n, iGm, iGmb, M3, A1b);
-  for (int i = 0; i < n; i++)
-    for (int j = 0; j < n; j++) Gmb.a[i][j] += M3.a[i][j];
   // Gp = (E + EF)/2, Gm = (E - EF)/2
-  Mat<NZ, T>& Eb = M2;
-  Mat<NZ, T>& EFb = M1;
+  Mat<NZ, T>& Eb = Gpb;
+  Mat<NZ, T>& EFb = Gmb;
   for (int i = 0; i < n; i++)
     for (int j = 0; j < n; j++) {
       const T p = Gpb.a[i][j], q = Gmb.a[i][j];
@@ -244,8 +284,8 @@ CRTM_HD bool ada_layer_adjoint(int nS, int nZ, T w, T tau, const T* mu, const T*
     }
   // EF = iX E diag(ev):  iX_b = EF_b (E diag(ev))^T;  EV_b = iX^T EF_b;
   //   E_b += EV_b diag(ev);  ev_b_j = sum_i EV_b_ij E_ij
-  Mat<NZ, T>& iXb = Tm;
-  Mat<NZ, T>& EVb = Rm;
+  Mat<NZ, T>& iXb = Um;   // K is dead
+  Mat<NZ, T>& EVb = Rm;   // W_b is dead
   for (int i = 0; i < n; i++)
     for (int j = 0; j < n; j++) {
       T v = T(0.0);
@@ -261,14 +301,16 @@ CRTM_HD bool ada_layer_adjoint(int nS, int nZ, T w, T tau, const T* mu, const T*
       v += EVb.a[i][j] * E.a[i][j];
       Eb.a[i][j] += EVb.a[i][j] * ev[j];
     }
-    // ex_j = exp(-ev_j tau), ev_j = sqrt(lam_j)
-    const T ev_b = v - tau * ex[j] * ex_b[j];
-    tb -= ev[j] * ex[j] * ex_b[j];
+    // ex_j = exp(-ev_j tau), dx_j = 1 - ex_j, ev_j = sqrt(lam_j)
+    const T d = dx_b[j] - ex_b[j];
+    const T ev_b = v + tau * ex[j] * d;
+    tb += ev[j] * ex[j] * d;
     lam_b[j] = lam[j] > T(0.0) ? T(0.5) * ev_b / ev[j] : T(0.0);
   }
   *tau_b = tb;
-  // X = PP - PM inverted:  X_b = -iX^T iX_b iX^T  (in M3)
-  inverse_adjoint(n, iX, iXb, M3, A2);
+  // X = PP - PM inverted:  X_b = -iX^T iX_b iX^T  (in P; W is scratch)
+  Mat<NZ, T>& Xb = P;
+  inverse_adjoint(n, iX, iXb, Xb, W);
   // HH = E diag(lam) E^-1:  HH_b = E^-T (diag(lam_b) + F o (E^T E_b)) E^T,
   // F_ij = 1 / (lam_j - lam_i) off the diagonal
   Mat<NZ, T>& Ei = Gp;    // Gp, Gm, iGm are dead
@@ -279,13 +321,13 @@ CRTM_HD bool ada_layer_adjoint(int nS, int nZ, T w, T tau, const T* mu, const T*
   for (int i = 0; i < n; i++)
     for (int j = 0; j < n; j++)
       Mx.a[i][j] = (i == j) ? lam_b[i] : Mx.a[i][j] / (lam[j] - lam[i]);
-  Mat<NZ, T>& HHb = Rm;
-  mat_mul_tn(n, Ei, Mx, Tm);   // E^-T M
-  mat_mul_nt(n, Tm, E, HHb);   // (E^-T M) E^T
+  Mat<NZ, T>& HHb = Rm;   // EV_b is dead
+  mat_mul_tn(n, Ei, Mx, T2);   // E^-T M  (P_b is dead)
+  mat_mul_nt(n, T2, E, HHb);   // (E^-T M) E^T
   // HH = X Y with X = PP - PM, Y = PP + PM (rebuilt from the phase blocks):
   //   X_b += HH_b Y^T;  Y_b = X^T HH_b
   Mat<NZ, T>& X = iGm;
-  Mat<NZ, T>& Y = A2;
+  Mat<NZ, T>& Y = W;
   for (int i = 0; i < n; i++) {
     const T c = s / mu[i];
     for (int j = 0; j < n; j++) {
@@ -294,9 +336,9 @@ CRTM_HD bool ada_layer_adjoint(int nS, int nZ, T w, T tau, const T* mu, const T*
       Y.a[i][j] = f + b;
     }
   }
-  Mat<NZ, T>& Yb = Tm;
+  Mat<NZ, T>& Yb = T2;
   mat_mul_tn(n, X, HHb, Yb);
-  mat_mul_nt(n, HHb, Y, M1);
+  mat_mul_nt(n, HHb, Y, Um);   // iX_b is dead
   // f = c_i ff_ij wt_j - delta_ij / mu_i, b = c_i bb_ij wt_j, c_i = s / mu_i;
   // X = f - b, Y = f + b
   T s_b = T(0.0);
@@ -304,7 +346,7 @@ CRTM_HD bool ada_layer_adjoint(int nS, int nZ, T w, T tau, const T* mu, const T*
     const T c = s / mu[i];
     T c_b = T(0.0);
     for (int j = 0; j < n; j++) {
-      const T xb = M3.a[i][j] + M1.a[i][j];
+      const T xb = Xb.a[i][j] + Um.a[i][j];
       const T fb = xb + Yb.a[i][j], bbv = Yb.a[i][j] - xb;
       ff_b.a[i][j] = fb * c * wt[j];
       bb_b.a[i][j] = bbv * c * wt[j];
@@ -567,27 +609,31 @@ CRTM_HD int layer_adjoint(const CloudyColumn& in, const CloudLut& lut, const Str
     T w_b, tau_b, Bb;
     const bool ok = ada_layer_adjoint<NZ, T>(nS, nZ, L.ssa, L.od, mu, wt, ff, bb, B, Tb, Rb, sb, &w_b, &tau_b, ffb,
                                              bbb, &Bb, &gap);
-    if constexpr (std::is_same<T, float>::value) {
-      // the FP32 reverse sweep near a nearly defective eigenbasis, or where
-      // its factorisation failed: this layer in FP64
-      if (!ok || gap < FP32_ADJ_GAP_MIN)
+    constexpr bool fp32 = std::is_same<T, float>::value;
+    if (!ok) {
+      // a failed FP32 factorisation: this layer in FP64
+      if constexpr (fp32)
         return layer_adjoint<NZ, double>(in, lut, St, k, gas_od, kind_rec, T_b, R_b, src_b, od_b, B_b, g, gs);
+      return -5;
     }
-    if (!ok) return -5;
-    if (gap < SENSOR_GAP_MIN && nZ == nS + 1) {
+    const double gap_min = fp32 ? FP32_ADJ_GAP_MIN : SENSOR_GAP_MIN;
+    if (gap < gap_min && nZ == nS + 1) {
       // A quadrature eigenvalue of MOM nearly meets the sensor angle's: the
       // derivatives through the nearly defective eigenbasis lose about
       // eps / gap^2.  T, R and the source are smooth in the sensor angle, so
-      // the layer's bulk adjoints are taken at sensor angles mu (1 +- h),
-      // h = 1e-3 and 2e-3, as the Richardson extrapolation
-      // (4 D(h) - D(2h)) / 3 of the symmetric means.
+      // the layer's bulk adjoints are taken at sensor angles mu (1 +- h) and
+      // mu (1 +- 2h), as the Richardson extrapolation (4 D(h) - D(2h)) / 3
+      // of the symmetric means (error O(h^4)): h = 1e-3 in FP64, 1e-2 in
+      // FP32, where the shifted gaps must be wider.  An FP32 layer whose
+      // shifted angles still meet an eigenvalue, or fail, is taken in FP64.
+      const double shift = fp32 ? FP32_SENSOR_SHIFT : SENSOR_SHIFT;
       BulkAdjoint<T> S2;
       S2.od_b = S2.ssa_b = S2.B_b = T(0.0);
       for (int l = 0; l <= nleg; l++) S2.p_b[l] = T(0.0);
       int n_ok = 0;
       const int zz = nZ - 1;
       for (int side = 0; side < 4; side++) {
-        const double fsh = (side & 1 ? -1.0 : 1.0) * (side < 2 ? SENSOR_SHIFT : 2.0 * SENSOR_SHIFT);
+        const double fsh = (side & 1 ? -1.0 : 1.0) * (side < 2 ? shift : 2.0 * shift);
         const T wgt = T((side < 2 ? 4.0 : -1.0) / 6.0);
         T mu2[NZ], P2[NZ][SC_NLEG_MAX + 1];
         for (int i = 0; i < nZ; i++) {
@@ -604,9 +650,11 @@ CRTM_HD int layer_adjoint(const CloudyColumn& in, const CloudLut& lut, const Str
         Mat<NZ, T> ff2, bb2, ffb2, bbb2;
         phase_blocks<NZ, T>(nS, nZ, nleg, L.p, P2, wt, ff2, bb2);
         T w2, t2, B2, pb2[SC_NLEG_MAX + 1];
+        double gap2 = 1.0;
         if (!ada_layer_adjoint<NZ, T>(nS, nZ, L.ssa, L.od, mu2, wt, ff2, bb2, B, Tb, Rb, sb, &w2, &t2, ffb2, bbb2,
-                                      &B2))
+                                      &B2, &gap2))
           break;
+        if (fp32 && gap2 < gap_min) break;
         phase_blocks_adjoint<NZ, T>(nS, nZ, nleg, L.p, P2, wt, ffb2, bbb2, pb2);
         S2.od_b += wgt * t2;
         S2.ssa_b += wgt * w2;
@@ -614,10 +662,13 @@ CRTM_HD int layer_adjoint(const CloudyColumn& in, const CloudLut& lut, const Str
         for (int l = 0; l < nleg; l++) S2.p_b[l] += wgt * pb2[l];
         n_ok++;
       }
-      if (n_ok == 4) {   // else (a shifted angle failed) keep the direct derivatives
+      if (n_ok == 4) {
         if (const int rc = bulk_to_inputs<T>(in, lut, nleg, St.loff, k, tk, L, S2, nsp, g, gs)) return rc;
         return 1;
       }
+      // a shifted angle failed: FP32 goes to FP64; FP64 keeps the direct derivatives
+      if constexpr (fp32)
+        return layer_adjoint<NZ, double>(in, lut, St, k, gas_od, kind_rec, T_b, R_b, src_b, od_b, B_b, g, gs);
     }
     A.od_b = tau_b;
     A.ssa_b = w_b;

@@ -51,9 +51,11 @@ constexpr double SENSOR_SHIFT = 1.0e-3;
 // FP32 layer solver: below these relative gaps (forward; reverse sweep) the
 // sensor angle's MOM eigenvector, which divides by the gap, loses too much
 // of FP32's precision (about eps/gap in T and R, eps/gap^2 in their
-// derivatives), and the layer is solved in FP64 instead.
-constexpr double FP32_GAP_MIN = 1.0e-2;
-constexpr double FP32_ADJ_GAP_MIN = 3.0e-2;
+// derivatives); such a layer is solved at sensor angles mu (1 +- h),
+// mu (1 +- 2h), h = FP32_SENSOR_SHIFT, and extrapolated, in FP32.
+constexpr double FP32_GAP_MIN = 3.0e-3;
+constexpr double FP32_ADJ_GAP_MIN = 3.0e-3;
+constexpr double FP32_SENSOR_SHIFT = 1.0e-2;
 
 // Device copy of the CloudCoeff LUT (phase element 1 only).  Tables keep the
 // file's Fortran order (frequency fastest).
@@ -979,7 +981,50 @@ CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const Stre
     const bool ok = ada_layer_loss<NZ, S>(St.nS, St.nZ, ssa, od, mu, wt, ff, bb, B, Td, Rd, srcd,
                                           gap ? gap : &g32);
     if constexpr (std::is_same<S, float>::value) {
-      if (!ok || (gap ? *gap : g32) < FP32_GAP_MIN) {   // this layer in FP64
+      bool in_fp64 = !ok;
+      if (ok && (gap ? *gap : g32) < FP32_GAP_MIN && St.nZ == St.nS + 1) {
+        // the sensor angle nearly meets a MOM eigenvalue: the layer at sensor
+        // angles mu (1 +- h), mu (1 +- 2h), combined as (4 M(h) - M(2h)) / 3
+        // of the symmetric means (T, R and the source are smooth in the
+        // sensor angle; error O(h^4)); FP64 if a shifted angle fails too
+        const int zz = St.nZ - 1;
+        Mat<NZ, S> Ta, Ra, f2, b2, T2, R2;
+        S sa[NZ], s2[NZ], m2[NZ], P2[NZ][SC_NLEG_MAX + 1];
+        for (int i = 0; i < St.nZ; i++) {
+          sa[i] = S(0.0);
+          m2[i] = mu[i];
+          for (int l = 0; l <= nleg; l++) P2[i][l] = P[i][l];
+          for (int j = 0; j < St.nZ; j++) { Ta.a[i][j] = S(0.0); Ra.a[i][j] = S(0.0); }
+        }
+        for (int side = 0; side < 4 && !in_fp64; side++) {
+          const double fsh = (side & 1 ? -1.0 : 1.0) * (side < 2 ? FP32_SENSOR_SHIFT : 2.0 * FP32_SENSOR_SHIFT);
+          const S wgt = S((side < 2 ? 4.0 : -1.0) / 6.0);
+          const double ms = St.mu[zz] * (1.0 + fsh);
+          double q[SC_NLEG_MAX + 1];
+          q[0] = 1.0;
+          if (nleg > 0) q[1] = ms;
+          for (int j = 1; j < nleg; j++) q[j + 1] = ((2 * j + 1) * ms * q[j] - j * q[j - 1]) / (j + 1);
+          m2[zz] = S(ms);
+          for (int l = 0; l <= nleg; l++) P2[zz][l] = S(q[l]);
+          phase_blocks<NZ, S>(St.nS, St.nZ, nleg, pcs, P2, wt, f2, b2);
+          double g2 = 1.0;
+          if (!ada_layer_loss<NZ, S>(St.nS, St.nZ, ssa, od, m2, wt, f2, b2, B, T2, R2, s2, &g2) ||
+              g2 < FP32_GAP_MIN) {
+            in_fp64 = true;
+            break;
+          }
+          for (int i = 0; i < St.nZ; i++) {
+            sa[i] += wgt * s2[i];
+            for (int j = 0; j < St.nZ; j++) { Ta.a[i][j] += wgt * T2.a[i][j]; Ra.a[i][j] += wgt * R2.a[i][j]; }
+          }
+        }
+        if (!in_fp64)
+          for (int i = 0; i < St.nZ; i++) {
+            srcd[i] = sa[i];
+            for (int j = 0; j < St.nZ; j++) { Td.a[i][j] = Ta.a[i][j]; Rd.a[i][j] = Ra.a[i][j]; }
+          }
+      }
+      if (in_fp64) {   // this layer in FP64
         Mat<NZ, double> f2, b2, T2, R2;
         double m2[NZ], w2[NZ], s2[NZ];
         for (int i = 0; i < St.nZ; i++) {

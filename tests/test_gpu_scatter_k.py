@@ -290,15 +290,16 @@ def test_mixed_cloudy_k_matrix_matches_fp64(gpu_lib, cloud_dir, sensor, n_stream
 
 @pytest.mark.parametrize("precision", [0, 1])
 def test_cloudy_k_matrix_radiance_matches_forward(gpu_lib, cloud_dir, precision):
-    """The K-matrix returns the forward radiance.  The mixed form's forward
-    keeps its layer records in FP32 and the K-matrix in FP64, so they agree to
-    1e-3 K there (both within 0.01 K of the FP64 form); exactly otherwise."""
+    """The K-matrix returns the forward radiance.  In the mixed form the
+    forward adds FP32 layer records in FP64 and the K-matrix adds them in FP32
+    (with the (I - Rup R)^-1 inversions in FP64), so the two agree within the
+    form's 0.01 K budget there; to 1e-6 K in the FP64 form."""
     atm, sfc, geo, opt = sy.cloudy_workload("mwsynth_c16", 12, 100, 86, wc_scale=300.0)
     h = gpu_lib.CRTM(["mwsynth_c16"], cloud_dir, precision)
     fw = h.forward(atm, sfc, geo, opt)
     _, rts = h.k_matrix(atm, sfc, geo, opt)
     assert np.abs(rts.brightness_temperature - fw.brightness_temperature).max() <= (1e-6 if precision == 0
-                                                                                   else 1e-3)
+                                                                                   else 1e-2)
 
 
 @pytest.mark.parametrize("precision", [0, 1])
