@@ -429,14 +429,22 @@ def pipe_peaks(torch, dev):
     return out
 
 
-def adding_flops(groups, n_channels, wavenumbers):
-    """Algorithmic FP64 FLOPs of one step's adding and adding adjoint
-    (scatter_adding): 38 nZ^3 per scattering layer and (profile, channel) --
-    forward adding 10 nZ^3 (Gamma = (I - Rup R)^-1 by elimination, T Gamma,
-    Rup T, T Gamma Rup T) and its adjoint 28 nZ^3 (Gamma again, and the
-    products' transposes) -- with nZ the stream set's angles plus the sensor
+# Operations of one scattering layer's MOM work in the cloudy K-matrix's
+# layer reverse sweep (scatter_reverse_kernel: phase blocks, the loss-form MOM
+# forward and its reverse sweep, the phase blocks' adjoint) by its angle
+# count nZ, counted by running the kernel's header code on an
+# operation-counting number type (tests/harness/flop_count.cpp; every +, -,
+# *, /, sqrt, exp counted, an FMA as two).  The species' LUT derivatives are
+# not counted.
+REVERSE_LAYER_OPS = {3: 3330, 4: 7660, 5: 14550, 6: 24700, 10: 113600}
+
+
+def scattering_layer_sum(groups, n_channels, wavenumbers, per_layer):
+    """Sum over the step's cloudy (profile, channel) pairs of their scattering
+    layers' per_layer(nZ), with nZ the stream set's angles plus the sensor
     angle: Options%n_Streams, else the stream rule on the largest effective
-    radius and the channel's wavenumber."""
+    radius and the channel's wavenumber.  A scattering layer is one with an
+    active cloud (water content above 1e-6)."""
     total = 0.0
     for (sid, atm, sfc, geo, opt), L, wn in zip(groups, n_channels, wavenumbers):
         for p in range(atm.n_profiles):
@@ -452,8 +460,23 @@ def adding_flops(groups, n_channels, wavenumbers):
                 mie = 2.0 * np.pi * atm.cloud_effective_radius[p, :nc].max() * wn / 1.0e4
                 nleg = np.where(mie < 0.01, 2, np.where(mie < 1.0, 4, 6))
                 nz = (nleg + 2) // 2 + 1
-            total += n_sl * 38.0 * float((nz.astype(np.float64) ** 3).sum())
+            total += n_sl * float(sum(per_layer(int(z)) * c for z, c in zip(*np.unique(nz, return_counts=True))))
     return total
+
+
+def adding_flops(groups, n_channels, wavenumbers):
+    """Algorithmic FP64 FLOPs of one step's adding and adding adjoint
+    (scatter_adding): 38 nZ^3 per scattering layer and (profile, channel) --
+    forward adding 10 nZ^3 (Gamma = (I - Rup R)^-1 by elimination, T Gamma,
+    Rup T, T Gamma Rup T) and its adjoint 28 nZ^3 (Gamma again, and the
+    products' transposes)."""
+    return scattering_layer_sum(groups, n_channels, wavenumbers, lambda z: 38.0 * z ** 3)
+
+
+def reverse_flops(groups, n_channels, wavenumbers):
+    """Operations of one step's layer reverse sweeps (scatter_contract stage):
+    REVERSE_LAYER_OPS[nZ] per scattering layer and (profile, channel)."""
+    return scattering_layer_sum(groups, n_channels, wavenumbers, lambda z: float(REVERSE_LAYER_OPS[z]))
 
 
 def run_scattering(args, torch, dev, rank, world, dist):
@@ -572,15 +595,21 @@ def run_scattering(args, torch, dev, rank, world, dist):
     if rank == 0 and name in ("C4", "C5") and stage_ms:
         dom = max(stage_ms, key=stage_ms.get)
         pk = pipe_peaks(torch, dev)
-        if dom == "scatter_adding":
-            fl = adding_flops(groups, [h.n_channels[i] for i in range(len(groups))],
-                              [co.read_spccoeff(os.path.join(COEFF_DIR, f"{g[0]}.SpcCoeff.bin")).wavenumber
-                               for g in groups])
+        chans = [h.n_channels[i] for i in range(len(groups))]
+        wns = [co.read_spccoeff(os.path.join(COEFF_DIR, f"{g[0]}.SpcCoeff.bin")).wavenumber for g in groups]
+        if dom in ("scatter_adding", "scatter_contract"):
+            fl = (adding_flops if dom == "scatter_adding" else reverse_flops)(groups, chans, wns)
             ach = fl / (stage_ms[dom] * 1e-3) / 1e12
-            roofline = {"bound": "fp64", "achieved": ach, "peak": pk["fp64"], "unit": "TFLOP/s",
-                        "frac": ach / pk["fp64"], "traffic": None, "kernel": "scatter_kmatrix_kernel (adding + adjoint)",
+            pipe = "fp32"   # the mixed form's adding and reverse sweep run in FP32
+            roofline = {"bound": pipe, "achieved": ach, "peak": pk[pipe], "unit": "TFLOP/s",
+                        "frac": ach / pk[pipe], "traffic": None,
+                        "kernel": ("scatter_kmatrix_kernel (adding + adjoint)" if dom == "scatter_adding" else
+                                   "scatter_reverse_kernel (MOM forward + reverse sweep per scattering layer)"),
                         "algorithmic_flops_per_step": fl,
-                        "peak_source": "measured in this run: cuBLAS FP64 GEMM through torch.matmul"}
+                        "flop_count": ("38 nZ^3 per scattering layer" if dom == "scatter_adding" else
+                                       "REVERSE_LAYER_OPS[nZ] per scattering layer, counted on an "
+                                       "operation-counting number type"),
+                        "peak_source": "measured in this run: cuBLAS FP32 GEMM (TF32 off) through torch.matmul"}
         else:
             roofline = {"bound": None, "kernel": dom, "note": "no algorithmic count for this stage"}
         extra["pipe_peaks_tflops"] = pk

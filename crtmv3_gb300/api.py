@@ -62,9 +62,40 @@ class CBatch(ct.Structure):
                 ("wind_speed", ct.c_void_p)]
 
 
+# RTSolution components beyond radiance and brightness temperature, in the
+# header's order (crtm_gpu_rtsolution); the last three are (P, L, max_layers)
+RTS_COMPONENTS = ("tb_clear", "r_clear", "total_cloud_cover", "sod", "surface_emissivity", "up_radiance",
+                  "down_radiance", "surface_planck_radiance", "n_full_streams", "layer_optical_depth",
+                  "upwelling_radiance", "upwelling_overcast_radiance")
+RTS_LAYER_COMPONENTS = ("layer_optical_depth", "upwelling_radiance", "upwelling_overcast_radiance")
+
+
 class CRTSolution(ct.Structure):
     _fields_ = [("radiance", ct.c_void_p), ("brightness_temperature", ct.c_void_p),
-                ("status", ct.c_void_p)]
+                ("status", ct.c_void_p)] + [(f, ct.c_void_p) for f in RTS_COMPONENTS]
+
+
+def _rts(P: int, L: int, K: int, components: bool) -> RTSolutionBatch:
+    """Host RTSolution arrays of a call; with ``components`` every further
+    RTSolution component too."""
+    r = RTSolutionBatch(np.zeros((P, L)), np.zeros((P, L)), status=np.zeros(P, np.int32))
+    if components:
+        for f in RTS_COMPONENTS:
+            shape = (P, L, K) if f in RTS_LAYER_COMPONENTS else (P, L)
+            setattr(r, f, np.zeros(shape, np.int32 if f == "n_full_streams" else np.float64))
+    return r
+
+
+def _crts(r: RTSolutionBatch) -> CRTSolution:
+    return CRTSolution(r.radiance.ctypes.data, r.brightness_temperature.ctypes.data, _addr(r.status),
+                       *[_addr(getattr(r, f, None)) for f in RTS_COMPONENTS])
+
+
+def _crts_device(out: dict) -> CRTSolution:
+    """Device RTSolution of an output dict: radiance, bt, optional status and
+    any of the further components under their RTS_COMPONENTS names."""
+    return CRTSolution(out["radiance"].data_ptr(), out["bt"].data_ptr(), _addr(out.get("status")),
+                       *[_addr(out.get(f)) for f in RTS_COMPONENTS])
 
 
 SCATTER_JACOBIANS = ("cloud_water_content", "cloud_effective_radius", "cloud_fraction",
@@ -307,31 +338,33 @@ class CRTM:
         if rc != SUCCESS:
             raise RuntimeError(self.error())
 
-    def forward(self, atm, sfc, geo, opt, sensor: int = 0) -> RTSolutionBatch:
+    def forward(self, atm, sfc, geo, opt, sensor: int = 0, components: bool = False) -> RTSolutionBatch:
+        """CRTM_Forward with host buffers.  ``components``: also return the
+        further RTSolution components (RTS_COMPONENTS)."""
         P, L = atm.n_profiles, self.n_channels[sensor]
         keep: list = []
         b = self._cbatch(atm, sfc, geo, opt, keep)
-        rts = RTSolutionBatch(np.zeros((P, L)), np.zeros((P, L)), status=np.zeros(P, np.int32))
-        cr = CRTSolution(rts.radiance.ctypes.data, rts.brightness_temperature.ctypes.data,
-                         rts.status.ctypes.data)
+        rts = _rts(P, L, atm.max_layers, components)
+        cr = _crts(rts)
         self._check(library().crtm_gpu_forward(self.h, sensor, ct.byref(b), ct.byref(cr)))
         return rts
 
     def k_matrix(self, atm, sfc, geo, opt, bt_k=None, sensor: int = 0, k_absorbers=None, out=None,
-                 scattering_jacobians: bool = True):
+                 scattering_jacobians: bool = True, components: bool = False):
         """K-matrix with host buffers.  ``k_absorbers``: optional list of user absorber
         indices whose Jacobians are returned (default: all).  ``out``: optional
         preallocated KMatrixBatch (e.g. in pinned memory).  ``scattering_jacobians``:
         also return the cloud water content / effective radius / fraction and
         aerosol concentration / effective radius Jacobians of a batch with clouds
-        or aerosols."""
+        or aerosols.  ``components``: also return the further RTSolution
+        components."""
         P, L, K, J = atm.n_profiles, self.n_channels[sensor], atm.max_layers, atm.n_absorbers
         keep: list = []
         b = self._cbatch(atm, sfc, geo, opt, keep)
         seed = None if bt_k is None else np.ascontiguousarray(bt_k, np.float64)
         sel = None if k_absorbers is None else np.ascontiguousarray(k_absorbers, np.int32)
         JK = J if sel is None else int(sel.shape[0])
-        rts = RTSolutionBatch(np.zeros((P, L)), np.zeros((P, L)), status=np.zeros(P, np.int32))
+        rts = _rts(P, L, K, components)
         km = out if out is not None else KMatrixBatch(np.zeros((P, L, K)), np.zeros((P, L, JK, K)),
                                                       np.zeros((P, L)), np.zeros((P, L)))
         if out is None and scattering_jacobians:
@@ -342,8 +375,7 @@ class CRTM:
                 setattr(km, f, np.zeros((P, L)))
             if opt is None or opt.emissivity is None:
                 km.wind_speed = np.zeros((P, L))
-        cr = CRTSolution(rts.radiance.ctypes.data, rts.brightness_temperature.ctypes.data,
-                         rts.status.ctypes.data)
+        cr = _crts(rts)
         ck = CKMatrix(km.temperature.ctypes.data, km.absorber.ctypes.data,
                       km.water_temperature.ctypes.data, km.surface_emissivity.ctypes.data,
                       0 if sel is None else JK, None if sel is None else sel.ctypes.data,
@@ -352,12 +384,12 @@ class CRTM:
                                                 ct.byref(ck), ct.byref(cr)))
         return km, rts
 
-    def adjoint(self, atm, sfc, geo, opt, bt_ad, sensor: int = 0):
+    def adjoint(self, atm, sfc, geo, opt, bt_ad, sensor: int = 0, components: bool = False):
         P, L, K, J = atm.n_profiles, self.n_channels[sensor], atm.max_layers, atm.n_absorbers
         keep: list = []
         b = self._cbatch(atm, sfc, geo, opt, keep)
         seed = np.ascontiguousarray(bt_ad, np.float64)
-        rts = RTSolutionBatch(np.zeros((P, L)), np.zeros((P, L)), status=np.zeros(P, np.int32))
+        rts = _rts(P, L, K, components)
         out = dict(temperature=np.zeros((P, K)), absorber=np.zeros((P, J, K)), water_temperature=np.zeros(P))
         for f, shp in _scatter_shapes(atm, self.aerosol_model).items():
             out[f] = np.zeros((P,) + shp)
@@ -365,8 +397,7 @@ class CRTM:
             out[f] = np.zeros(P)
         if opt is None or opt.emissivity is None:
             out["wind_speed"] = np.zeros(P)
-        cr = CRTSolution(rts.radiance.ctypes.data, rts.brightness_temperature.ctypes.data,
-                         rts.status.ctypes.data)
+        cr = _crts(rts)
         ca = CAdjoint(out["temperature"].ctypes.data, out["absorber"].ctypes.data,
                       out["water_temperature"].ctypes.data,
                       *[_addr(out.get(f)) for f in SCATTER_JACOBIANS + SURFACE_COVERS + SCHEME_JACOBIANS])
@@ -375,7 +406,7 @@ class CRTM:
         return out, rts
 
     def tangent_linear(self, atm, sfc, geo, opt, atm_tl=None, sfc_tl=None, emissivity_tl=None,
-                       sensor: int = 0):
+                       sensor: int = 0, components: bool = False):
         """CRTM_Tangent_Linear: the brightness-temperature perturbation (P, L)
         from perturbations of the atmosphere (``atm_tl``: an object with any of
         temperature, absorber, cloud_water_content, cloud_effective_radius,
@@ -404,9 +435,8 @@ class CRTM:
             keep.append(e)
             vals["emissivity"] = e.ctypes.data
         tl = CTLIn(*[vals.get(f) for f in TL_FIELDS])
-        rts = RTSolutionBatch(np.zeros((P, L)), np.zeros((P, L)), status=np.zeros(P, np.int32))
-        cr = CRTSolution(rts.radiance.ctypes.data, rts.brightness_temperature.ctypes.data,
-                         rts.status.ctypes.data)
+        rts = _rts(P, L, atm.max_layers, components)
+        cr = _crts(rts)
         bt_tl = np.zeros((P, L))
         self._check(library().crtm_gpu_tangent_linear(self.h, sensor, ct.byref(b), ct.byref(tl), ct.byref(cr),
                                                       bt_tl.ctypes.data))
@@ -454,8 +484,7 @@ class CRTM:
 
     @staticmethod
     def _kmatrix_structs(out: dict, k_absorbers=None):
-        cr = CRTSolution(out["radiance"].data_ptr(), out["bt"].data_ptr(),
-                         _addr(out.get("status")))
+        cr = _crts_device(out)
         sel = None if k_absorbers is None else np.ascontiguousarray(k_absorbers, np.int32)
         ck = CKMatrix(out["temperature_k"].data_ptr(), out["absorber_k"].data_ptr(),
                       out["water_temperature_k"].data_ptr(), out["surface_emissivity_k"].data_ptr(),
@@ -497,11 +526,11 @@ class CRTM:
         return dict(chosen=conv(best), trials=[conv(trials[i]) for i in range(min(n.value, 16))])
 
     def forward_device(self, b: CBatch, out: dict, sensor: int = 0, stream=None) -> None:
-        cr = CRTSolution(out["radiance"].data_ptr(), out["bt"].data_ptr(), _addr(out.get("status")))
+        cr = _crts_device(out)
         self._check(library().crtm_gpu_forward_device(self.h, sensor, ct.byref(b), ct.byref(cr), stream))
 
     def adjoint_device(self, b: CBatch, seed, out: dict, sensor: int = 0, stream=None) -> None:
-        cr = CRTSolution(out["radiance"].data_ptr(), out["bt"].data_ptr(), _addr(out.get("status")))
+        cr = _crts_device(out)
         ca = CAdjoint(out["temperature_ad"].data_ptr(), out["absorber_ad"].data_ptr(),
                       out["water_temperature_ad"].data_ptr(), *[_addr(out.get(f + "_ad")) for f in SCATTER_JACOBIANS])
         for f in SCHEME_JACOBIANS:
@@ -577,19 +606,30 @@ def CRTM_Forward(atmosphere: AtmosphereBatch, surface: SurfaceBatch, geometry: G
     """CRTM_Forward.  ``rts`` receives one RTSolutionBatch per sensor in ChannelInfo order.
     ``options.emissivity`` is (P, total channels) over all sensors."""
     rts.clear()
-    atmosphere, _ = _added_layers(atmosphere, "CRTM_Forward")
+    atmosphere, added = _added_layers(atmosphere, "CRTM_Forward")
     if atmosphere is None:
         return FAILURE
     off = 0
     for ci in channel_info:
         opt = _sensor_options(options, off, ci.n_channels)
         try:
-            rts.append(ci.handle.forward(atmosphere, surface, geometry, opt, ci.sensor_index))
+            r = ci.handle.forward(atmosphere, surface, geometry, opt, ci.sensor_index, components=True)
         except RuntimeError as e:
             print(f"CRTM_Forward(FAILURE): {e}")
             return FAILURE
+        rts.append(_user_layer_components(added, r))
         off += ci.n_channels
     return SUCCESS
+
+
+def _user_layer_components(added, r: RTSolutionBatch) -> RTSolutionBatch:
+    """The layer components of an RTSolution on the user's layers
+    (Layer_Optical_Depth(1:no) = the extended profile's na+1:nt,
+    Common_RTSolution.f90:239,1206-1207)."""
+    if not added.any:
+        return r
+    return dataclasses.replace(r, **{f: addlayers.user_layers(added, getattr(r, f))
+                                     for f in RTS_LAYER_COMPONENTS if getattr(r, f) is not None})
 
 
 def CRTM_K_Matrix(atmosphere, surface, rts_k: Optional[Sequence[np.ndarray]], geometry,
@@ -608,7 +648,7 @@ def CRTM_K_Matrix(atmosphere, surface, rts_k: Optional[Sequence[np.ndarray]], ge
         opt = _sensor_options(options, off, ci.n_channels)
         seed = None if rts_k is None else rts_k[i]
         try:
-            km, r = ci.handle.k_matrix(atmosphere, surface, geometry, opt, seed, ci.sensor_index)
+            km, r = ci.handle.k_matrix(atmosphere, surface, geometry, opt, seed, ci.sensor_index, components=True)
         except RuntimeError as e:
             print(f"CRTM_K_Matrix(FAILURE): {e}")
             return FAILURE
@@ -616,7 +656,7 @@ def CRTM_K_Matrix(atmosphere, surface, rts_k: Optional[Sequence[np.ndarray]], ge
             km = dataclasses.replace(km, **{f: addlayers.user_layers(added, getattr(km, f))
                                              for f in LAYER_FIELDS})
         atmosphere_k.append(km)
-        rts.append(r)
+        rts.append(_user_layer_components(added, r))
         off += ci.n_channels
     return SUCCESS
 
@@ -634,7 +674,8 @@ def CRTM_Adjoint(atmosphere, surface, rts_ad: Sequence[np.ndarray], geometry,
     for i, ci in enumerate(channel_info):
         opt = _sensor_options(options, off, ci.n_channels)
         try:
-            out, r = ci.handle.adjoint(atmosphere, surface, geometry, opt, rts_ad[i], ci.sensor_index)
+            out, r = ci.handle.adjoint(atmosphere, surface, geometry, opt, rts_ad[i], ci.sensor_index,
+                                       components=True)
         except RuntimeError as e:
             print(f"CRTM_Adjoint(FAILURE): {e}")
             return FAILURE
@@ -642,7 +683,7 @@ def CRTM_Adjoint(atmosphere, surface, rts_ad: Sequence[np.ndarray], geometry,
             out = {k: addlayers.user_layers(added, v) if k in LAYER_FIELDS else v for k, v in out.items()}
         for k, v in out.items():
             tot[k] = tot[k] + v if k in tot else v.copy()
-        rts.append(r)
+        rts.append(_user_layer_components(added, r))
         off += ci.n_channels
     atmosphere_ad.clear()
     atmosphere_ad.update(tot)
@@ -668,11 +709,11 @@ def CRTM_Tangent_Linear(atmosphere, surface, atmosphere_tl, surface_tl, geometry
         opt = _sensor_options(options, off, ci.n_channels)
         try:
             bt_tl, r = ci.handle.tangent_linear(atmosphere, surface, geometry, opt, atmosphere_tl, surface_tl,
-                                                sensor=ci.sensor_index)
+                                                sensor=ci.sensor_index, components=True)
         except RuntimeError as e:
             print(f"CRTM_Tangent_Linear(FAILURE): {e}")
             return FAILURE
-        rts.append(r)
+        rts.append(_user_layer_components(added, r))
         rts_tl.append(bt_tl)
         off += ci.n_channels
     return SUCCESS

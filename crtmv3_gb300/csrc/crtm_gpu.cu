@@ -751,11 +751,39 @@ int reserve_smem(crtm_gpu_handle h, F kernel, size_t bytes, const char* what) {
 // (host entry points only): element i covers bytes [p*per[i], (p+n)*per[i]).
 struct HostCopy {
   int n = 0;
-  void* dst[24];
-  const void* src[24];
-  size_t per[24];
+  void* dst[40];
+  const void* src[40];
+  size_t per[40];
   int max_chunk = 0;   // cap on the chunk size so that copies overlap compute
 };
+
+// The further RTSolution components of an output set, in a fixed order:
+// their pointers and byte sizes (P x L pairs, Km layers).
+constexpr int N_RTS_EXT = 12;
+void rts_ext_list(const crtm_gpu_rtsolution* r, size_t PL, size_t Km, void** ptr, size_t* bytes) {
+  void* const p[N_RTS_EXT] = {r->tb_clear, r->r_clear, r->total_cloud_cover, r->sod, r->surface_emissivity,
+                              r->up_radiance, r->down_radiance, r->surface_planck_radiance, r->n_full_streams,
+                              r->layer_optical_depth, r->upwelling_radiance, r->upwelling_overcast_radiance};
+  for (int i = 0; i < N_RTS_EXT; i++) {
+    ptr[i] = p[i];
+    bytes[i] = !p[i] ? 0 : i == 8 ? PL * sizeof(int) : i >= 9 ? PL * Km * sizeof(double) : PL * sizeof(double);
+  }
+}
+void rts_ext_set(crtm_gpu_rtsolution* r, void* const* p) {
+  r->tb_clear = (double*)p[0]; r->r_clear = (double*)p[1]; r->total_cloud_cover = (double*)p[2];
+  r->sod = (double*)p[3]; r->surface_emissivity = (double*)p[4]; r->up_radiance = (double*)p[5];
+  r->down_radiance = (double*)p[6]; r->surface_planck_radiance = (double*)p[7]; r->n_full_streams = (int*)p[8];
+  r->layer_optical_depth = (double*)p[9]; r->upwelling_radiance = (double*)p[10];
+  r->upwelling_overcast_radiance = (double*)p[11];
+}
+RtsExt make_ext(const crtm_gpu_rtsolution* r) {
+  RtsExt x;
+  x.tb_clear = r->tb_clear; x.r_clear = r->r_clear; x.tcc = r->total_cloud_cover; x.sod = r->sod;
+  x.emis = r->surface_emissivity; x.up = r->up_radiance; x.down = r->down_radiance;
+  x.bs = r->surface_planck_radiance; x.nfs = r->n_full_streams; x.lod = r->layer_optical_depth;
+  x.upw = r->upwelling_radiance; x.ovc = r->upwelling_overcast_radiance;
+  return x;
+}
 
 // Caller-owned scratch of fixed size used instead of the handle's workspace
 // (crtm_gpu_k_matrix_device_static).
@@ -961,6 +989,8 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       ca.wind_k = mode == 1 ? kk->wind_speed : (mode == 2 ? w.WS : nullptr);
     }
     ca.status = rts->status;
+    ca.x = make_ext(rts);
+    ca.n_streams = b->n_streams;
     // scattering K-matrix/adjoint: the column runs twice around the scattering kernels
     const bool split = scat && mode != 3;
     if (split) {
@@ -995,6 +1025,7 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       sa.overlap = sa.max_clouds > 0 ? b->overlap_id : nullptr;
       sa.radiance = rts->radiance; sa.bt = rts->brightness_temperature;
       sa.status = rts->status; sa.error = h->d_error;
+      sa.x = make_ext(rts);
       sa.TODc = w.TODc; sa.PT = w.PT; sa.CB = w.CB; sa.AS = w.AS; sa.LBA = w.LBA;
       sa.n_slots = sw.slots; sa.CJ = w.CJ; sa.CR = w.CR; sa.CF = w.CF; sa.TD = w.TD; sa.SC = w.SC;
       const long long nlay = (long long)n * Kmax * L;
@@ -1529,6 +1560,13 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
                              {ad->land_temperature, PD}, {ad->snow_temperature, PD}, {ad->ice_temperature, PD},
                              {ad->aerosol_effective_variance, NAo ? (size_t)P * NAo * Km * 8 : 0},
                              {ad->relative_humidity, NAo ? (size_t)P * Km * 8 : 0}, {ad->wind_speed, PD}});
+  const size_t ext0 = outs.size();
+  {
+    void* ep[N_RTS_EXT];
+    size_t eb[N_RTS_EXT];
+    rts_ext_list(rts, PL, (size_t)Km, ep, eb);
+    for (int i = 0; i < N_RTS_EXT; i++) outs.push_back({ep[i], eb[i]});
+  }
   size_t tout = 0;
   for (auto& o : outs) tout += align_up(o.second);
   if (!h->io_out.ensure(tout)) return fail(h, "cannot allocate %zu bytes for outputs", tout);
@@ -1539,6 +1577,7 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
     off += align_up(outs[i].second);
   }
   crtm_gpu_rtsolution drts{(double*)dout[0], (double*)dout[1], (int*)dout[2]};
+  rts_ext_set(&drts, dout.data() + ext0);
   crtm_gpu_kmatrix dk{};
   crtm_gpu_adjoint_out dad{};
   if (mode == 1)
@@ -1734,10 +1773,21 @@ int tl_host(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm_g
   // outputs
   const size_t PL = P * L;
   const size_t o_bt = align_up(PL * 8), o_tl = o_bt + align_up(PL * 8), o_st = o_tl + align_up(PL * 8);
-  if (!h->io_out.ensure(o_st + align_up(P * 4))) return fail(h, "cannot allocate the outputs");
+  void* ep[N_RTS_EXT];
+  size_t eb[N_RTS_EXT], eo[N_RTS_EXT];
+  rts_ext_list(rts, PL, Km, ep, eb);
+  size_t o_end = o_st + align_up(P * 4);
+  for (int i = 0; i < N_RTS_EXT; i++) { eo[i] = o_end; o_end += align_up(eb[i]); }
+  if (!h->io_out.ensure(o_end)) return fail(h, "cannot allocate the outputs");
   char* ob = (char*)h->io_out.p;
   crtm_gpu_rtsolution drts{(double*)ob, (double*)(ob + o_bt), rts->status ? (int*)(ob + o_st) : nullptr};
+  void* dep[N_RTS_EXT];
+  for (int i = 0; i < N_RTS_EXT; i++) dep[i] = ep[i] ? ob + eo[i] : nullptr;
+  rts_ext_set(&drts, dep);
   int rc = tl_device(h, sensor, &db, &dtl, &drts, (double*)(ob + o_tl), st);
+  for (int i = 0; i < N_RTS_EXT && rc == CRTM_GPU_SUCCESS; i++)
+    if (ep[i] && cudaMemcpyAsync(ep[i], dep[i], eb[i], cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      rc = fail(h, "device-to-host copy failed");
   if (rc == CRTM_GPU_SUCCESS) {
     if (cudaMemcpyAsync(rts->radiance, drts.radiance, PL * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaMemcpyAsync(rts->brightness_temperature, drts.brightness_temperature, PL * 8, cudaMemcpyDeviceToHost,

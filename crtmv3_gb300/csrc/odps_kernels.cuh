@@ -227,6 +227,23 @@ struct BatchView {
 // Batch profile of pipeline position i.
 CRTM_HD int batch_profile(const BatchView& b, int i) { return b.perm ? b.perm[i] : i; }
 
+// The RTSolution components beyond radiance and brightness temperature
+// (crtm_gpu_rtsolution), each null when not wanted: [P][L] and, for the
+// layer arrays, [P][L][Kmax].
+struct RtsExt {
+  double* tb_clear = nullptr, *r_clear = nullptr, *tcc = nullptr, *sod = nullptr, *emis = nullptr;
+  double* up = nullptr, *down = nullptr, *bs = nullptr;
+  int* nfs = nullptr;
+  double* lod = nullptr, *upw = nullptr, *ovc = nullptr;
+};
+
+// Zero the layer array row [from, Kmax) of output o at pair pl, if o is wanted.
+CRTM_HD void zero_row(double* o, size_t pl, int Kmax, int from) {
+  if (!o) return;
+  double* r = o + pl * Kmax;
+  for (int k = from; k < Kmax; k++) r[k] = 0.0;
+}
+
 struct SpecView {
   const double* c1, *c2, *b1, *b2, *cbr;
   const double* freq, *wn;   // GHz, cm^-1
@@ -627,6 +644,14 @@ struct ColumnArgs {
   const R* TODc;                 // [n][Kmax][L] cloudy dR/dtau (PT holds the cloudy dR/dT)
   const double* CB;              // [n][4][L] cloudy radiance, dR/de, dR/dBs, clear radiance
   const double* cover;           // [n] total cloud cover, -1: no clear part
+  // further RTSolution components.  A profile solved here with the Emission
+  // solver gets them all; for a profile with clouds or aerosols the launch
+  // before the scattering kernels (mode 3, pass 1) writes the emissivity and
+  // zeros the Emission-only components and the scattering optical depth
+  // (which the layer kernel accumulates), and pass 2 writes the cloud cover
+  // and the clear column.
+  RtsExt x;
+  const int* n_streams;          // [P] Options%n_Streams or null
 };
 
 template <class R>
@@ -657,11 +682,27 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   const int st = a.pv.status[p];
   const int Ku = a.b.n_layers[gp];
   if (blockIdx.x == 0 && tid == 0 && a.status) a.status[gp] = st;
+  const RtsExt& x = a.x;
+  auto ext_scalars = [&](size_t pl, double e, double up, double down, double bs) {
+    if (x.emis) x.emis[pl] = e;
+    if (x.up) x.up[pl] = up;
+    if (x.down) x.down[pl] = down;
+    if (x.bs) x.bs[pl] = bs;
+  };
   if (st != 0) {
     if (l < L) {
       const size_t pl = (size_t)gp * L + l;
       a.radiance[pl] = 0.0;
       a.bt[pl] = 0.0;
+      ext_scalars(pl, 0.0, 0.0, 0.0, 0.0);
+      if (x.tb_clear) x.tb_clear[pl] = 0.0;
+      if (x.r_clear) x.r_clear[pl] = 0.0;
+      if (x.tcc) x.tcc[pl] = 0.0;
+      if (x.sod) x.sod[pl] = 0.0;
+      if (x.nfs) x.nfs[pl] = 0;
+      zero_row(x.lod, pl, Kmax, 0);
+      zero_row(x.upw, pl, Kmax, 0);
+      zero_row(x.ovc, pl, Kmax, 0);
       if (a.mode == 1) { a.tsk[pl] = 0.0; a.ek[pl] = 0.0; }
       if (a.mode == 1 || a.mode == 2) a.SC[(size_t)p * L + l] = R(0);
       if (a.mode == 2) a.tsk[(size_t)p * L + l] = 0.0;
@@ -704,8 +745,18 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   // Reference levels are walked in order (OD loads prefetched two levels
   // ahead); each user level is emitted once the upper level of its bracket
   // is reached.
+  // a profile with clouds or aerosols (solved by the scattering kernels):
+  // every profile of a forward launch in mode 3, those with clouds or
+  // aerosols in the K-matrix / adjoint launches around the scattering kernels
+  const bool scat_p = a.mode == 3 ||
+                      ((a.pass == 1 || a.pass == 2) &&
+                       ((a.n_clouds && a.n_clouds[gp] > 0) || (a.n_aerosols && a.n_aerosols[gp] > 0)));
+  double* lod_row = (x.lod && a.pass != 2) ? x.lod + pl * Kmax : nullptr;
+  double* ovc_row = (x.ovc && a.pass != 2 && !scat_p) ? x.ovc + pl * Kmax : nullptr;
+  // mode 0: the layer optical depths wait in the upwelling row for the upwelling sweep
+  double* stash = (x.upw && a.mode == 0) ? x.upw + pl * Kmax : nullptr;
   R rad_down = R(a.sp.cbr[l]);
-  R src = R(0), tr = R(1), total = R(0);   // forward: TOA radiance accumulated top down
+  R src = R(0), tr = R(1), total = R(0);   // atmospheric upwelling at the top, accumulated top down
   R path_prev = R(0), path_cur = R(0), up_prev = R(0);
   R od1 = K > 0 ? od[0] : R(0), od2 = K > 1 ? od[L] : R(0);
   int i = 0;
@@ -719,13 +770,13 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
         const R t = exp(-tau * inv_u);
         const R te = b1 + b2 * tus[ku];
         const R B = c1 / (exp(c2 / te) - R(1));
-        if (a.mode == 0) {
-          src += tr * B * (R(1) - t);
-        } else {
-          if (a.pass != 2) {
-            a.TAU[cs + (size_t)ku * L] = tau;
-            if (a.mode != 3) a.DTOP[cs + (size_t)ku * L] = rad_down;
-          }
+        if (ovc_row) ovc_row[ku] = double(src + tr * B);   // a black cloud filling layer ku
+        if (lod_row) lod_row[ku] = double(tau);
+        if (stash) stash[ku] = double(tau);
+        src += tr * B * (R(1) - t);
+        if (a.mode != 0 && a.pass != 2) {
+          a.TAU[cs + (size_t)ku * L] = tau;
+          if (a.mode != 3) a.DTOP[cs + (size_t)ku * L] = rad_down;
         }
         tr *= t;
         total += tau;
@@ -742,14 +793,45 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
     path_cur += v;
   }
   const R Dn = rad_down, Tn = tr;
+  const int nsu = a.n_streams ? a.n_streams[gp] : 0;
   if (a.mode == 0) {
     const double Rd = double(src + Tn * (re * Bs + rr * Dn));
+    const double btv = planck_temperature(c1d, c2d, b1d, b2d, Rd);
     a.radiance[pl] = Rd;
-    a.bt[pl] = planck_temperature(c1d, c2d, b1d, b2d, Rd);
+    a.bt[pl] = btv;
+    ext_scalars(pl, e, double(src), double(Dn), double(Bs));
+    if (x.tb_clear) x.tb_clear[pl] = btv;   // no clouds (CRTM_Forward_Module.f90:1115-1119)
+    if (x.r_clear) x.r_clear[pl] = Rd;
+    if (x.tcc) x.tcc[pl] = 0.0;
+    if (x.sod) x.sod[pl] = 0.0;
+    if (x.nfs) x.nfs[pl] = nsu > 0 ? nsu + 2 : 0;
+    if (stash) {   // upwelling at each layer's bottom, surface to top
+      R U = re * Bs + rr * Dn;
+      for (int ku = Ku - 1; ku >= 0; ku--) {
+        const R tau = R(stash[ku]);
+        stash[ku] = double(U);
+        const R t = exp(-tau * inv_u);
+        const R B = c1 / (exp(c2 / (b1 + b2 * tus[ku])) - R(1));
+        U = t * U + B * (R(1) - t);
+      }
+    }
+    zero_row(x.lod, pl, Kmax, Ku);
+    zero_row(x.upw, pl, Kmax, Ku);
+    zero_row(x.ovc, pl, Kmax, Ku);
     return;
   }
-  if (a.mode == 3) return;   // gas layer optical depths only (the cloudy solver follows)
-  if (a.pass == 1) return;   // TAU/DTOP stored; the scattering K kernel runs next
+  if (a.mode == 3 || a.pass == 1) {
+    if (scat_p) {   // Emission-only components zero; the scattering kernels fill the rest
+      ext_scalars(pl, e, 0.0, 0.0, 0.0);
+      if (x.sod) x.sod[pl] = 0.0;
+      zero_row(x.lod, pl, Kmax, Ku);
+      zero_row(x.upw, pl, Kmax, 0);
+      zero_row(x.ovc, pl, Kmax, 0);
+    }
+    // mode 3: gas layer optical depths only (the cloudy solver follows);
+    // pass 1: TAU/DTOP stored, the scattering K kernel runs next
+    return;
+  }
   // ---- pass 2 (bottom up): upwelling, Emission adjoint, OD path adjoint (unit seed)
   R U = re * Bs + rr * Dn;
   R P = R(1);                 // transmittance of the layers below the current one
@@ -781,6 +863,7 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   double wcloud = 0.0;   // weight of the cloudy column
   if (scat) wcloud = a.cover[p] < 0.0 ? 1.0 : a.cover[p];
   const R wclr = R(1.0 - wcloud), wcl = R(wcloud);
+  double* upw_row = (x.upw && !scat) ? x.upw + pl * Kmax : nullptr;
   R tau_n = a.TAU[cs + (size_t)(Ku - 1) * L], dt_n = a.DTOP[cs + (size_t)(Ku - 1) * L];
   for (int ku = Ku - 1; ku >= 0; ku--) {
     const R tau = tau_n, Dtop = dt_n;
@@ -801,6 +884,7 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
     Bad += dad * (R(1) - t);
     tod -= ((Dtop - B) * t * dad) * inv_u;
     R ptv = dB * Bad;
+    if (upw_row) upw_row[ku] = double(U);   // upwelling at this layer's bottom
     if (scat) {
       ptv = wclr * ptv + wcl * a.PT[cs + (size_t)ku * L];
       tod = wclr * tod + wcl * a.TODc[cs + (size_t)ku * L];
@@ -834,6 +918,25 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   double btv, dtdr;
   planck_temperature_with_dR(c1d, c2d, b1d, b2d, Rd, &btv, &dtdr);
   a.bt[pl] = btv;
+  // further RTSolution components: the K-matrix and adjoint fill R_clear and
+  // Tb_clear for fractional profiles only (CRTM_K_Matrix_Module.f90:1328-1336)
+  if (scat) {
+    const bool frac = a.cover[p] >= 0.0;
+    const double Rc = double(U);
+    if (x.tcc) x.tcc[pl] = frac ? a.cover[p] : 0.0;
+    if (x.r_clear) x.r_clear[pl] = frac ? Rc : 0.0;
+    if (x.tb_clear) x.tb_clear[pl] = frac ? planck_temperature(c1d, c2d, b1d, b2d, Rc) : 0.0;
+  } else {
+    ext_scalars(pl, e, double(src), double(Dn), double(Bs));
+    if (x.tcc) x.tcc[pl] = 0.0;
+    if (x.r_clear) x.r_clear[pl] = 0.0;
+    if (x.tb_clear) x.tb_clear[pl] = 0.0;
+    if (x.sod) x.sod[pl] = 0.0;
+    if (x.nfs) x.nfs[pl] = nsu > 0 ? nsu + 2 : 0;
+    zero_row(x.lod, pl, Kmax, Ku);
+    zero_row(x.upw, pl, Kmax, Ku);
+    zero_row(x.ovc, pl, Kmax, Ku);
+  }
   const double seed = a.seed ? a.seed[pl] : 1.0;
   const double scale = dtdr * seed;
   a.SC[(size_t)p * L + l] = R(scale);

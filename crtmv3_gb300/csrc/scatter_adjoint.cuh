@@ -72,7 +72,7 @@ CRTM_HD void inverse_adjoint(int n, const Mat<NZ, T>& Y, const Mat<NZ, T>& Yb, M
 // entry is read) and Planck radiance (B_b).  Returns false where the forward
 // factorisation fails.  gap: as in ada_layer.
 template <int NZ, class T>
-CRTM_HD bool ada_layer_adjoint(int nS, int nZ, T w, T tau, const T* mu, const T* wt, const Mat<NZ, T>& ff,
+CRTM_HD_NOINLINE bool ada_layer_adjoint(int nS, int nZ, T w, T tau, const T* mu, const T* wt, const Mat<NZ, T>& ff,
                                const Mat<NZ, T>& bb, T B, const Mat<NZ, T>& T_b, const Mat<NZ, T>& R_b,
                                const T* src_b, T* w_b, T* tau_b, Mat<NZ, T>& ff_b, Mat<NZ, T>& bb_b, T* B_b,
                                double* gap = nullptr) {
@@ -368,7 +368,7 @@ CRTM_HD bool ada_layer_adjoint(int nS, int nZ, T w, T tau, const T* mu, const T*
 // entries left of the diagonal; the sensor angle's column is divided by the
 // carried sum of its row.  The forward values are recomputed here.
 template <int NZ, class T>
-CRTM_HD void phase_blocks_adjoint(int nS, int nZ, int nleg, const T* pc, const T (*P)[SC_NLEG_MAX + 1], const T* wt,
+CRTM_HD_NOINLINE void phase_blocks_adjoint(int nS, int nZ, int nleg, const T* pc, const T (*P)[SC_NLEG_MAX + 1], const T* wt,
                                   const Mat<NZ, T>& ff_b, const Mat<NZ, T>& bb_b, T* pc_b) {
   Mat<NZ, T> f0, b0, fb, bq;   // clamped unscaled blocks (upper triangle) and their adjoints
   unsigned clampf[NZ] = {0}, clampb[NZ] = {0};
@@ -503,31 +503,37 @@ struct BulkAdjoint {
 
 // Reverse of the combine and the species sums: from a layer's bulk adjoint to
 // the adjoints of its gas optical depth (g[0]), temperature (g[1]) and each
-// species' amount and LUT coordinates (gs[sp][0..2]; nsp species).
+// species' amount and LUT coordinates (gs[sp][0..2]; nsp species).  In FP64
+// whatever the adjoint's type: bs_b gathers -p_l pb_l / bs over the Legendre
+// terms, which cancel against the ps_b terms in the contraction with the
+// species' derivatives (a phase moment moves little while the scattering
+// coefficient moves much with the radius), so the bulk values L are FP64 too.
 template <class T>
-CRTM_HD int bulk_to_inputs(const CloudyColumn& in, const CloudLut& lut, int nleg, int loff, int k, T tk,
-                           const LayerBulk<T>& L, const BulkAdjoint<T>& A, int nsp, double* g, double (*gs)[3]) {
+CRTM_HD int bulk_to_inputs(const CloudyColumn& in, const CloudLut& lut, int nleg, int loff, int k, double tk,
+                           const LayerBulk<double>& L, const BulkAdjoint<T>& A, int nsp, double* g,
+                           double (*gs)[3]) {
   // combine: w = bs / od0, p_l = ps_l / bs, f = p_nleg,
   //   od = (1 - f w) od0, ssa = (1 - f) w / (1 - f w)
-  T od0_b = A.od_b, bs_b = T(0.0), ps_b[SC_NLEG_MAX + 1];
-  for (int l = 0; l <= nleg; l++) ps_b[l] = T(0.0);
-  if (L.bs > T(BS_THRESHOLD)) {
-    const T w = L.bs / L.od0, f = L.p[nleg], D = T(1.0) - f * w;
-    const T f_b = A.ssa_b * w * (w - T(1.0)) / (D * D) - A.od_b * w * L.od0;
-    const T w_b = A.ssa_b * (T(1.0) - f) / (D * D) - A.od_b * f * L.od0;
-    od0_b = A.od_b * D - w_b * w / L.od0;
+  const double od_b = double(A.od_b), ssa_b = double(A.ssa_b);
+  double od0_b = od_b, bs_b = 0.0, ps_b[SC_NLEG_MAX + 1];
+  for (int l = 0; l <= nleg; l++) ps_b[l] = 0.0;
+  if (L.bs > BS_THRESHOLD) {
+    const double w = L.bs / L.od0, f = L.p[nleg], D = 1.0 - f * w;
+    const double f_b = ssa_b * w * (w - 1.0) / (D * D) - od_b * w * L.od0;
+    const double w_b = ssa_b * (1.0 - f) / (D * D) - od_b * f * L.od0;
+    od0_b = od_b * D - w_b * w / L.od0;
     bs_b = w_b / L.od0;
     for (int l = 1; l <= nleg; l++) {
-      const T pb = l < nleg ? A.p_b[l] : f_b;
+      const double pb = l < nleg ? double(A.p_b[l]) : f_b;
       ps_b[l] = pb / L.bs;
       bs_b -= pb * L.p[l] / L.bs;
     }
   } else {
-    bs_b = A.ssa_b;
+    bs_b = ssa_b;
   }
-  g[0] = (double)od0_b;
+  g[0] = od0_b;
   // Planck radiance of the layer temperature
-  const double te = in.b1 + in.b2 * (double)tk, ee = exp(in.c2 / te);
+  const double te = in.b1 + in.b2 * tk, ee = exp(in.c2 / te);
   double gt = (double)A.B_b * in.c1 * in.c2 * ee * in.b2 / (te * te * (ee - 1.0) * (ee - 1.0));
   // each species' share in forward mode: amount, c1, c2 and the temperature,
   // in FP64 in every form (the LUT derivatives are differences of nearby
@@ -536,13 +542,13 @@ CRTM_HD int bulk_to_inputs(const CloudyColumn& in, const CloudLut& lut, int nleg
   using D4 = Dual<4, double>;
   for (int sp = 0; sp < nsp; sp++) {
     D4 od(0.0), bs(0.0), ps[SC_NLEG_MAX + 1];
-    D4 td(double(tk), 0);
+    D4 td(tk, 0);
     td.d[3] = 1.0;
     if (const int rc = species_share<D4>(in, lut, nleg, loff, k, sp, td, SpeciesSeed{sp}, &od, &bs, ps)) return rc;
     double gg[4];
     for (int d = 0; d < 4; d++) {
-      double v = double(od0_b) * od.d[d] + double(bs_b) * bs.d[d];
-      for (int l = 1; l <= nleg; l++) v += double(ps_b[l]) * ps[l].d[d];
+      double v = od0_b * od.d[d] + bs_b * bs.d[d];
+      for (int l = 1; l <= nleg; l++) v += ps_b[l] * ps[l].d[d];
       gg[d] = v;
     }
     gs[sp][0] = gg[0];
@@ -565,13 +571,17 @@ CRTM_HD int bulk_to_inputs(const CloudyColumn& in, const CloudLut& lut, int nleg
 // scattering, 0 clear) or a negative error; kind_rec is the record's kind
 // (the forward's); a mismatch returns -7.
 template <int NZ, class T>
-CRTM_HD int layer_adjoint(const CloudyColumn& in, const CloudLut& lut, const StreamSet<NZ, double>& St, int k,
+CRTM_HD_NOINLINE int layer_adjoint(const CloudyColumn& in, const CloudLut& lut, const StreamSet<NZ, double>& St, int k,
                           double gas_od, int kind_rec, const Mat<NZ, double>& T_b, const Mat<NZ, double>& R_b,
                           const double* src_b, double od_b, double B_b, double* g, double (*gs)[3]) {
   const int nleg = St.nleg, nS = St.nS, nZ = St.nZ;
-  const T tk = T(in.temperature[k]);
+  // the layer's bulk optics in FP64 (the combine's adjoint needs them there;
+  // the LUT work is small), and in T for the MOM work
+  LayerBulk<double> Ld;
+  if (const int rc = layer_bulk<double>(in, lut, nleg, St.loff, k, gas_od, in.temperature[k], Ld)) return rc;
   LayerBulk<T> L;
-  if (const int rc = layer_bulk<T>(in, lut, nleg, St.loff, k, T(gas_od), tk, L)) return rc;
+  L.od0 = T(Ld.od0); L.bs = T(Ld.bs); L.od = T(Ld.od); L.ssa = T(Ld.ssa);
+  for (int l = 0; l <= nleg; l++) { L.ps[l] = T(Ld.ps[l]); L.p[l] = T(Ld.p[l]); }
   const int nsp = scattering_species(in, nleg, St.loff);
   if (nsp < 0) return nsp;
   BulkAdjoint<T> A;
@@ -597,6 +607,13 @@ CRTM_HD int layer_adjoint(const CloudyColumn& in, const CloudLut& lut, const Str
     A.od_b = T(od_b);
     A.B_b = T(B_b);
   } else {
+    if constexpr (std::is_same<T, float>::value) {
+      // a nearly conservative layer: the smallest eigenvalue of MOM's
+      // (PP - PM)(PP + PM), about 1 - ssa, carries FP32's absolute error, and
+      // the single-scattering albedo's adjoint loses eps / (1 - ssa): in FP64
+      if (1.0 - Ld.ssa < FP32_COALBEDO_MIN)
+        return layer_adjoint<NZ, double>(in, lut, St, k, gas_od, kind_rec, T_b, R_b, src_b, od_b, B_b, g, gs);
+    }
     const double te = in.b1 + in.b2 * in.temperature[k];
     const T B = T(in.c1 / (exp(in.c2 / te) - 1.0));
     Mat<NZ, T> Tb, Rb, ffb, bbb;
@@ -663,7 +680,8 @@ CRTM_HD int layer_adjoint(const CloudyColumn& in, const CloudLut& lut, const Str
         n_ok++;
       }
       if (n_ok == 4) {
-        if (const int rc = bulk_to_inputs<T>(in, lut, nleg, St.loff, k, tk, L, S2, nsp, g, gs)) return rc;
+        if (const int rc = bulk_to_inputs<T>(in, lut, nleg, St.loff, k, in.temperature[k], Ld, S2, nsp, g, gs))
+          return rc;
         return 1;
       }
       // a shifted angle failed: FP32 goes to FP64; FP64 keeps the direct derivatives
@@ -675,7 +693,8 @@ CRTM_HD int layer_adjoint(const CloudyColumn& in, const CloudLut& lut, const Str
     A.B_b = Bb;
     phase_blocks_adjoint<NZ, T>(nS, nZ, nleg, L.p, P, wt, ffb, bbb, A.p_b);
   }
-  if (const int rc = bulk_to_inputs<T>(in, lut, nleg, St.loff, k, tk, L, A, nsp, g, gs)) return rc;
+  if (const int rc = bulk_to_inputs<T>(in, lut, nleg, St.loff, k, in.temperature[k], Ld, A, nsp, g, gs))
+    return rc;
   return kind;
 }
 }  // namespace crtm

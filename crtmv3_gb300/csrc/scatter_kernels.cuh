@@ -108,6 +108,11 @@ struct ScatterArgs {
   double* CH;                   // [n][Kmax][L] relative humidity ('GOCART-GEOS5', 'NAAPS'), or null
   double* TD;                   // [n][2][Kmax] d tcc / d cf, d tcc / d wc (fractional profiles)
   const R* SC;                  // [n][L] dBT/dR x seed (after the second column launch)
+  // further RTSolution components: the layer kernel writes the layers'
+  // optical depths and accumulates the scattering optical depth; the forward
+  // solvers write the cloud cover, the clear column and the stream count
+  // (the K-matrix kernels the stream count; the second column launch the rest)
+  RtsExt x;
 };
 
 constexpr int SCATTER_THREADS = 128;
@@ -236,7 +241,14 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_layers_kernel(Scatter
   Mat<NZ, Rec> Tm, Rm;
   Rec src[NZ], od;
   const double gas = double(a.TAU[((size_t)p * Kmax + k) * L + l]);
-  const int kind = layer_optics<NZ, Rec, C>(c, a.lut, S, k, C(gas), C(c.temperature[k]), &od, Tm, Rm, src);
+  double bs = 0.0;
+  const int kind = layer_optics<NZ, Rec, C>(c, a.lut, S, k, C(gas), C(c.temperature[k]), &od, Tm, Rm, src,
+                                            NoSeed(), nullptr, a.x.sod ? &bs : nullptr);
+  if (kind >= 0) {
+    const size_t pl = (size_t)gp * L + l;
+    if (a.x.lod) a.x.lod[pl * Kmax + k] = double(od);
+    if (a.x.sod && bs > 0.0) atomicAdd(a.x.sod + pl, bs);
+  }
   rec[0] = Rec(kind);
   rec[(size_t)L] = od;
   if (kind != 1) return;
@@ -247,6 +259,29 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_layers_kernel(Scatter
       rec[(size_t)(2 + NZ * NZ + i * NZ + j) * L] = Rm.a[i][j];
     }
   for (int i = 0; i < nZ; i++) rec[(size_t)(2 + 2 * NZ * NZ + i) * L] = src[i];
+}
+
+// The forward's further RTSolution components of pair pl (profile p of the
+// chunk): total cloud cover and the clear column of a fractional profile;
+// R_clear / Tb_clear the profile's own radiance where it has no clouds or
+// its cover is below 1e-12 (CRTM_Forward_Module.f90:1086-1119); the stream
+// count (CRTM_Forward_Module.f90:866-874).
+template <class R>
+__device__ void forward_rts_ext(const ScatterArgs<R>& a, const CloudyColumn& c, int p, int gp, size_t pl,
+                                int code, double rad_clear) {
+  const RtsExt& x = a.x;
+  const double tcc = a.cover[p];
+  const bool frac = tcc >= 0.0 && !code;
+  if (x.tcc) x.tcc[pl] = frac ? tcc : 0.0;
+  double rc = frac ? rad_clear : 0.0, bc = frac ? planck_temperature(c.c1, c.c2, c.b1, c.b2, rad_clear) : 0.0;
+  if (!code && (c.n_clouds == 0 || (tcc >= 0.0 && tcc < MIN_COVERAGE))) {
+    rc = a.radiance[pl];
+    bc = a.bt[pl];
+  }
+  if (x.r_clear) x.r_clear[pl] = rc;
+  if (x.tb_clear) x.tb_clear[pl] = bc;
+  const int ns = a.n_streams ? a.n_streams[gp] : 0;
+  if (x.nfs) x.nfs[pl] = (c.n_clouds > 0 || c.n_aerosols > 0) ? c.nleg + 2 : (ns > 0 ? ns + 2 : 0);
 }
 
 template <int NZ, class R>
@@ -264,7 +299,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_adding_kernel(Scatter
   }
   const CloudyColumn c = column_inputs(a, p, gp, l);
   const R* tau = a.TAU + (size_t)p * Kmax * L + l;
-  double rad = 0.0;
+  double rad = 0.0, rad_clear = 0.0;
   int code = 0;
   if (c.n_clouds == 0 && c.n_aerosols == 0) {   // clear profile: Emission solver, FP64 here
     rad = clear_column_radiance(c, tau, L);
@@ -299,7 +334,10 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_adding_kernel(Scatter
       }
       if (!code) rad = adding_toa<NZ>(A, nZ, S.isat, c.cosmic);
       const double tcc = a.cover[p];
-      if (!code && tcc >= 0.0) rad = (1.0 - tcc) * clear_column_radiance(c, tau, L) + tcc * rad;
+      if (!code && tcc >= 0.0) {
+        rad_clear = clear_column_radiance(c, tau, L);
+        rad = (1.0 - tcc) * rad_clear + tcc * rad;
+      }
     }
   }
   if (code) {
@@ -309,6 +347,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_adding_kernel(Scatter
   }
   a.radiance[pl] = rad;
   a.bt[pl] = code ? 0.0 : planck_temperature(c.c1, c.c2, c.b1, c.b2, rad);
+  forward_rts_ext(a, c, p, gp, pl, code, rad_clear);
 }
 
 
@@ -324,7 +363,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_soi_kernel(ScatterArg
   const CloudyColumn c = column_inputs(a, p, gp, l);
   if ((c.n_clouds == 0 && c.n_aerosols == 0) || !c.soi) return;
   const size_t pl = (size_t)gp * L + l;
-  double rad = 0.0;
+  double rad = 0.0, rad_clear = 0.0;
   int code = 0;
   StreamSet<NZ, double> S;
   code = stream_set<NZ, double>(c.nleg, c.mu_sensor, c.n_clouds > 0 ? a.lut.nleg : -1, c_gauss, S);
@@ -356,8 +395,10 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_soi_kernel(ScatterArg
     if (!code)
       soi_solve<NZ>(nZ, c.Ku, S.isat, S.mu, c.emissivity, c.planck_surface, c.cosmic, lod, lsrc, ltr, fld, &rad);
     const double tcc = a.cover[p];
-    if (!code && tcc >= 0.0)
-      rad = (1.0 - tcc) * clear_column_radiance(c, a.TAU + (size_t)p * Kmax * L + l, L) + tcc * rad;
+    if (!code && tcc >= 0.0) {
+      rad_clear = clear_column_radiance(c, a.TAU + (size_t)p * Kmax * L + l, L);
+      rad = (1.0 - tcc) * rad_clear + tcc * rad;
+    }
   }
   if (code) {
     atomicCAS(a.error, 0, code);
@@ -366,6 +407,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_soi_kernel(ScatterArg
   }
   a.radiance[pl] = rad;
   a.bt[pl] = code ? 0.0 : planck_temperature(c.c1, c.c2, c.b1, c.b2, rad);
+  forward_rts_ext(a, c, p, gp, pl, code, rad_clear);
 }
 
 template <int NZ, class R>
@@ -378,6 +420,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_kmatrix_kernel(Scatte
   const CloudyColumn c = column_inputs(a, p, gp, l);
   if (c.n_clouds == 0 && c.n_aerosols == 0) return;   // clear: the column kernel's Emission adjoint
   if (c.soi) return;                                   // scatter_soi_k_kernel
+  if (a.x.nfs) a.x.nfs[(size_t)gp * L + l] = c.nleg + 2;
   double rad = 0.0, e_b = 0.0, Bs_b = 0.0;
   StreamSet<NZ, double> S;
   int code = stream_set<NZ, double>(c.nleg, c.mu_sensor, c.n_clouds > 0 ? a.lut.nleg : -1, c_gauss, S);
@@ -446,6 +489,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_soi_k_kernel(ScatterA
   if (l >= L || a.pv.status[p] != 0) return;
   const CloudyColumn c = column_inputs(a, p, gp, l);
   if ((c.n_clouds == 0 && c.n_aerosols == 0) || !c.soi) return;
+  if (a.x.nfs) a.x.nfs[(size_t)gp * L + l] = c.nleg + 2;
   double rad = 0.0, e_b = 0.0, Bs_b = 0.0;
   StreamSet<NZ, double> S;
   int code = stream_set<NZ, double>(c.nleg, c.mu_sensor, c.n_clouds > 0 ? a.lut.nleg : -1, c_gauss, S);

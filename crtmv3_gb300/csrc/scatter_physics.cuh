@@ -28,6 +28,16 @@
 #include "dual.cuh"
 #include "odps_physics.cuh"
 
+// The large per-layer solvers are compiled once per instance and called
+// rather than inlined at every call site: the FP32 forms call them again at
+// shifted sensor angles and fall back to the FP64 instance, and inlining each
+// call multiplied the code and the compile time.
+#ifdef __CUDACC__
+#define CRTM_HD_NOINLINE __host__ __device__ __noinline__
+#else
+#define CRTM_HD_NOINLINE
+#endif
+
 namespace crtm {
 
 constexpr int SC_NLEG_MAX = 16;          // MAX_N_LEGENDRE_TERMS
@@ -56,6 +66,9 @@ constexpr double SENSOR_SHIFT = 1.0e-3;
 constexpr double FP32_GAP_MIN = 3.0e-3;
 constexpr double FP32_ADJ_GAP_MIN = 3.0e-3;
 constexpr double FP32_SENSOR_SHIFT = 1.0e-2;
+// FP32 reverse sweep: layers whose single-scattering albedo is within this
+// of 1 are differentiated in FP64 (the albedo's adjoint loses eps / (1 - ssa))
+constexpr double FP32_COALBEDO_MIN = 3.0e-4;
 
 // Device copy of the CloudCoeff LUT (phase element 1 only).  Tables keep the
 // file's Fortran order (frequency fastest).
@@ -415,7 +428,7 @@ CRTM_HD void jacobi(int n, Mat<NZ, Dual<N, Q>>& S, Dual<N, Q>* lam, Mat<NZ, Dual
 // all nZ angles; V and W are scratch.  Returns false on a failed
 // factorisation.  gap: see ada_layer.
 template <int NZ, class T>
-CRTM_HD bool mom_eigen(int nS, int nZ, T s, const T* mu, const T* wt, const Mat<NZ, T>& ff, const Mat<NZ, T>& bb,
+CRTM_HD_NOINLINE bool mom_eigen(int nS, int nZ, T s, const T* mu, const T* wt, const Mat<NZ, T>& ff, const Mat<NZ, T>& bb,
                        Mat<NZ, T>& E, T* lam, Mat<NZ, T>& X, Mat<NZ, T>& Y, Mat<NZ, T>& V, Mat<NZ, T>& W,
                        double* gap) {
   // symmetric form of the quadrature block
@@ -520,7 +533,7 @@ CRTM_HD bool mom_eigen(int nS, int nZ, T s, const T* mu, const T* wt, const Mat<
 // defective: the layer's T and R stay smooth, but their derivatives through
 // the eigenvectors lose about eps / gap^2 of their accuracy.
 template <int NZ, class T>
-CRTM_HD bool ada_layer_loss(int nS, int nZ, T w, T tau, const T* mu, const T* wt, const Mat<NZ, T>& ff,
+CRTM_HD_NOINLINE bool ada_layer_loss(int nS, int nZ, T w, T tau, const T* mu, const T* wt, const Mat<NZ, T>& ff,
                             const Mat<NZ, T>& bb, T B, Mat<NZ, T>& Um, Mat<NZ, T>& Rm, T* src,
                             double* gap = nullptr) {
   if (gap) *gap = 1.0;
@@ -933,19 +946,22 @@ CRTM_HD int species_sums(const CloudyColumn& in, const CloudLut& lut, int nleg, 
 // Optics of layer k for the adding method: cloud and aerosol optics summed
 // over the species, combine and delta truncation, and for a scattering layer
 // the phase blocks and the layer's transmission, reflection and source
-// (ada_layer, or SOI doubling).  Computed in S (FP64 in every form, or
-// derivative numbers for the K-matrix), stored in T.  Returns 1 for a
+// (ada_layer, or SOI doubling).  Computed in S (FP64, FP32 in the mixed
+// form's ADA layers, or derivative numbers), stored in T.  Returns 1 for a
 // scattering layer, 0 for a clear one (od is then the layer optical depth),
-// negative on failure.
+// negative on failure.  bs_out (optional): the layer's scattering
+// coefficient before the delta truncation where it is significant, else 0
+// (its term of the scattering optical depth, CRTM_AtmOptics.f90:425-427).
 template <int NZ, class T, class S = double, class Seed = NoSeed>
 CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const StreamSet<NZ, double>& St, int k,
                          S gas_od, S tk, T* od_out, Mat<NZ, T>& Tm, Mat<NZ, T>& Rm, T* src,
-                         Seed seed = Seed(), double* gap = nullptr) {
+                         Seed seed = Seed(), double* gap = nullptr, double* bs_out = nullptr) {
   const int nleg = St.nleg;
   S od = gas_od, bs_sum = S(0.0);
   S pcs[SC_NLEG_MAX + 1];
   for (int l = 0; l <= nleg; l++) pcs[l] = S(0.0);
   if (const int rc = species_sums<S>(in, lut, nleg, St.loff, k, tk, seed, &od, &bs_sum, pcs)) return rc;
+  if (bs_out) *bs_out = bs_sum > BS_THRESHOLD ? double(value_of(bs_sum)) : 0.0;
   S ssa = bs_sum;
   if (bs_sum > BS_THRESHOLD) {   // CRTM_AtmOptics_Combine
     const S w = bs_sum / od;

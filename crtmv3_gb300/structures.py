@@ -156,7 +156,11 @@ class OptionsBatch:
 
 @dataclasses.dataclass
 class RTSolutionBatch:
-    """Outputs per (profile, channel): (P, L) arrays."""
+    """Outputs per (profile, channel): (P, L) arrays; the layer components
+    (layer_optical_depth, upwelling_radiance, upwelling_overcast_radiance)
+    are (P, L, max_layers).  The components after the brightness temperature
+    are CRTM_RTSolution_type's (CRTM_RTSolution_Define.f90:201-245), filled
+    when a call asks for them."""
     radiance: np.ndarray
     brightness_temperature: np.ndarray
     up_radiance: Optional[np.ndarray] = None
@@ -164,6 +168,14 @@ class RTSolutionBatch:
     surface_emissivity: Optional[np.ndarray] = None
     n_full_streams: Optional[np.ndarray] = None
     status: Optional[np.ndarray] = None
+    tb_clear: Optional[np.ndarray] = None
+    r_clear: Optional[np.ndarray] = None
+    total_cloud_cover: Optional[np.ndarray] = None
+    sod: Optional[np.ndarray] = None
+    surface_planck_radiance: Optional[np.ndarray] = None
+    layer_optical_depth: Optional[np.ndarray] = None
+    upwelling_radiance: Optional[np.ndarray] = None
+    upwelling_overcast_radiance: Optional[np.ndarray] = None
 
 
 @dataclasses.dataclass

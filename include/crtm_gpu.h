@@ -140,6 +140,48 @@ typedef struct {
   double* radiance;                /* [P][L] */
   double* brightness_temperature;  /* [P][L] */
   int* status;                     /* [P] per-profile status bits, or NULL */
+  /* The other RTSolution components the reference fills on this path
+   * (CRTM_RTSolution_Define.f90:201-245), each NULL when not wanted; [P][L]
+   * unless noted, layer arrays [P][L][max_layers] on the batch's layers
+   * (zero past a profile's n_layers).  Thermal sources only: the solar,
+   * visible and active-sensor components stay with the reference.
+   *   tb_clear, r_clear: a fractional profile's clear column
+   *     (CRTM_Forward_Module.f90:1108-1114); a profile without clouds, or
+   *     whose total cloud cover is below 1e-12, its own brightness
+   *     temperature and radiance (:1115-1119); zero otherwise.
+   *   total_cloud_cover: a fractional profile's (:1092); zero otherwise.
+   *   sod: vertically integrated scattering optical depth, the sum of the
+   *     layers' scattering coefficients before the delta truncation
+   *     (CRTM_AtmOptics.f90:425-427; :978 of the forward module); zero for a
+   *     profile without clouds and aerosols.
+   *   surface_emissivity: the emissivity used (Common_RTSolution.f90:433).
+   *   up_radiance, down_radiance, surface_planck_radiance: the Emission
+   *     solver's atmospheric upwelling radiance at the top, downwelling
+   *     radiance at the surface and surface Planck radiance
+   *     (Common_RTSolution.f90:1195-1198); zero for a profile solved with
+   *     ADA or SOI, as in the reference.
+   *   n_full_streams: Options%n_Streams + 2, else the stream rule's count
+   *     + 2 for a profile with clouds or aerosols, else 0
+   *     (CRTM_Forward_Module.f90:866-874, CRTM_RTSolution.f90:1204-1260).
+   *   layer_optical_depth: the layers' optical depth after the AtmOptics
+   *     combine (Common_RTSolution.f90:239).
+   *   upwelling_radiance, upwelling_overcast_radiance: the Emission solver's
+   *     upwelling radiance at each layer's bottom and the top-of-atmosphere
+   *     radiance of a black cloud filling each layer (Emission_Module.f90:
+   *     132,166-172; Common_RTSolution.f90:1206-1207); zero for a profile
+   *     solved with ADA or SOI. */
+  double* tb_clear;
+  double* r_clear;
+  double* total_cloud_cover;
+  double* sod;
+  double* surface_emissivity;
+  double* up_radiance;
+  double* down_radiance;
+  double* surface_planck_radiance;
+  int* n_full_streams;
+  double* layer_optical_depth;          /* [P][L][max_layers] */
+  double* upwelling_radiance;           /* [P][L][max_layers] */
+  double* upwelling_overcast_radiance;  /* [P][L][max_layers] */
 } crtm_gpu_rtsolution;
 
 typedef struct {

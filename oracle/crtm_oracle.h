@@ -126,6 +126,23 @@ void or_aerosol_destroy(or_aerosol* a);
 int or_forward_scatter(const or_handle* h, const or_cloud* cc, const or_aerosol* ca, const or_batch* b,
                        const or_clouds* cl, double* radiance, double* bt, int n_threads);
 
+/* The RTSolution components beyond radiance and brightness temperature,
+ * each NULL when not wanted ([P][L]; the layer arrays [P][L][max_layers]),
+ * with the meanings of include/crtm_gpu.h's crtm_gpu_rtsolution. */
+typedef struct {
+  double* tb_clear, *r_clear, *total_cloud_cover, *sod, *surface_emissivity;
+  double* up_radiance, *down_radiance, *surface_planck_radiance;
+  int* n_full_streams;
+  double* layer_optical_depth, *upwelling_radiance, *upwelling_overcast_radiance;
+} or_rts_ext;
+
+/* or_forward_scatter with the further RTSolution components of CRTM_Forward
+ * (CRTM_Forward_Module.f90:866-874,978,1086-1119; Common_RTSolution.f90:239,
+ * 433,1195-1207; Emission_Module.f90:117-172).  cl->max_clouds and
+ * max_aerosols may be 0 (a clear-sky batch). */
+int or_forward_ext(const or_handle* h, const or_cloud* cc, const or_aerosol* ca, const or_batch* b,
+                   const or_clouds* cl, double* radiance, double* bt, const or_rts_ext* x, int n_threads);
+
 /* K-matrix of a batch with clouds and aerosols through ADA (reverse mode of
  * CRTM_ADA_AD / MOM_AD and the scattering, combine and LUT adjoints), with the
  * clear-sky gas chain; outputs as or_k_matrix plus the cloud water content

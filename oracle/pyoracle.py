@@ -33,6 +33,13 @@ class OrBatch(ct.Structure):
                 ("surface_altitude", _dp), ("emissivity", _dp), ("k_absorber_mask", _ip)]
 
 
+class OrRtsExt(ct.Structure):
+    _fields_ = [(f, ct.c_void_p) for f in (
+        "tb_clear", "r_clear", "total_cloud_cover", "sod", "surface_emissivity", "up_radiance", "down_radiance",
+        "surface_planck_radiance", "n_full_streams", "layer_optical_depth", "upwelling_radiance",
+        "upwelling_overcast_radiance")]
+
+
 class OrClouds(ct.Structure):
     _fields_ = [("max_clouds", ct.c_int), ("n_clouds", _ip), ("cloud_type", _ip),
                 ("water_content", _dp), ("effective_radius", _dp), ("n_streams", _ip),
@@ -76,6 +83,8 @@ def lib():
         L.or_cloud_destroy.argtypes = [ct.c_void_p]
         L.or_forward_scatter.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.POINTER(OrBatch),
                                          ct.POINTER(OrClouds), _dp, _dp, ct.c_int]
+        L.or_forward_ext.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.POINTER(OrBatch),
+                                     ct.POINTER(OrClouds), _dp, _dp, ct.POINTER(OrRtsExt), ct.c_int]
         L.or_k_matrix_scatter.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.POINTER(OrBatch),
                                           ct.POINTER(OrClouds)] + [_dp] * 11 + [ct.c_int]
         L.or_aerosol_init.restype = ct.c_void_p
@@ -258,6 +267,38 @@ class Oracle:
             if st:
                 raise RuntimeError(L.or_last_error().decode())
             return rad, bt
+        finally:
+            if ch:
+                L.or_cloud_destroy(ch)
+            if ah:
+                L.or_aerosol_destroy(ah)
+
+    def forward_components(self, atm, sfc, geo, opt, cloudcoeff_path: Optional[str] = None,
+                           aerosolcoeff_path: Optional[str] = None, n_threads: int = 1,
+                           aerosol_scheme: str = "CRTM") -> dict:
+        """CRTM_Forward's radiance, brightness temperature and further
+        RTSolution components (or_forward_ext) of a batch with or without
+        clouds and aerosols: a dict of (P, L) arrays and (P, L, max_layers)
+        layer arrays under the names of include/crtm_gpu.h."""
+        L = lib()
+        ch, ah = self._luts(cloudcoeff_path, aerosolcoeff_path, aerosol_scheme)
+        try:
+            P, nL, K = atm.n_profiles, self.n_channels, atm.max_layers
+            b, keep = self._batch(atm, sfc, geo, opt)
+            c = self._clouds(atm, opt, keep)
+            out = dict(radiance=np.zeros((P, nL)), bt=np.zeros((P, nL)))
+            x = OrRtsExt()
+            for f, _ in OrRtsExt._fields_:
+                shape = (P, nL, K) if f in ("layer_optical_depth", "upwelling_radiance",
+                                            "upwelling_overcast_radiance") else (P, nL)
+                a = np.zeros(shape, np.int32 if f == "n_full_streams" else np.float64)
+                out[f] = a
+                setattr(x, f, a.ctypes.data)
+            st = L.or_forward_ext(self.h, ch, ah, ct.byref(b), ct.byref(c), _p(out["radiance"]), _p(out["bt"]),
+                                  ct.byref(x), n_threads)
+            if st:
+                raise RuntimeError(L.or_last_error().decode())
+            return out
         finally:
             if ch:
                 L.or_cloud_destroy(ch)
