@@ -176,6 +176,8 @@ def library() -> ct.CDLL:
     L.crtm_gpu_destroy.argtypes = [ct.c_void_p]
     L.crtm_gpu_n_channels.argtypes = [ct.c_void_p, ct.c_int]
     L.crtm_gpu_set_precision.argtypes = [ct.c_void_p, ct.c_int]
+    L.crtm_gpu_set_channel_subset.argtypes = [ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p]
+    L.crtm_gpu_get_channel_subset.argtypes = [ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p]
     L.crtm_gpu_forward.argtypes = [ct.c_void_p, ct.c_int, ct.POINTER(CBatch), ct.POINTER(CRTSolution)]
     L.crtm_gpu_k_matrix.argtypes = [ct.c_void_p, ct.c_int, ct.POINTER(CBatch), ct.c_void_p,
                                     ct.POINTER(CKMatrix), ct.POINTER(CRTSolution)]
@@ -234,6 +236,24 @@ class CRTM:
         self.sensor_ids = list(sensor_ids)
         self.n_channels = [L.crtm_gpu_n_channels(h, i) for i in range(len(sensor_ids))]
         self.set_precision(precision)
+
+    def set_channel_subset(self, sensor: int, positions=None) -> None:
+        """Process only the channels at these 0-based file positions in later
+        calls for ``sensor`` (crtm_gpu_set_channel_subset); None: all channels."""
+        if positions is None:
+            rc = library().crtm_gpu_set_channel_subset(self.h, sensor, -1, None)
+        else:
+            idx = np.ascontiguousarray(positions, np.int32)
+            rc = library().crtm_gpu_set_channel_subset(self.h, sensor, int(idx.size), idx.ctypes.data)
+        self._check(rc)
+        self.n_channels[sensor] = library().crtm_gpu_n_channels(self.h, sensor)
+
+    def channel_subset(self, sensor: int) -> np.ndarray:
+        """0-based file positions of the channels calls for ``sensor`` process."""
+        n = library().crtm_gpu_n_channels(self.h, sensor)
+        out = np.zeros(max(n, 0), np.int32)
+        library().crtm_gpu_get_channel_subset(self.h, sensor, int(out.size), out.ctypes.data if n > 0 else None)
+        return out
 
     @staticmethod
     def _err(h) -> str:
@@ -546,11 +566,60 @@ class CRTM:
 @dataclasses.dataclass
 class ChannelInfo:
     """CRTM_ChannelInfo_type (src/ChannelInfo/CRTM_ChannelInfo_Define.f90:70-85), reduced to
-    what this path needs: the sensor, its index in the handle and its channel count."""
+    what this path needs: the sensor, its index in the handle, the count of
+    channels calls process, the Sensor_Channel numbers of the coefficient
+    files' channels and which of them are processed (Process_Channel)."""
     sensor_id: str
     sensor_index: int
     n_channels: int
     handle: CRTM
+    sensor_channel: Optional[np.ndarray] = None
+    process_channel: Optional[np.ndarray] = None
+
+
+def CRTM_ChannelInfo_n_Channels(channel_info: ChannelInfo) -> int:
+    """CRTM_ChannelInfo_n_Channels (CRTM_ChannelInfo_Define.f90:336-340)."""
+    return int(channel_info.n_channels)
+
+
+def CRTM_ChannelInfo_Channels(channel_info: ChannelInfo) -> np.ndarray:
+    """CRTM_ChannelInfo_Channels (CRTM_ChannelInfo_Define.f90:373-377): the
+    Sensor_Channel numbers of the processed channels."""
+    return channel_info.sensor_channel[channel_info.process_channel]
+
+
+def CRTM_ChannelInfo_Subset(channel_info: ChannelInfo, channel_subset=None, reset: bool = False) -> int:
+    """CRTM_ChannelInfo_Subset (CRTM_ChannelInfo_Define.f90:444-517): later
+    calls with this ChannelInfo process only the channels whose Sensor_Channel
+    number is in ``channel_subset`` (in the files' order; their RTSolution,
+    K-matrix and Options%Emissivity have that many channels).  ``reset``:
+    all channels again (the subset is then ignored).  An empty subset turns
+    every channel off.  A subset with more channels than the sensor's, or
+    with numbers outside the sensor's range, fails and turns every channel
+    off, as the reference does."""
+    ci = channel_info
+    if reset:
+        ci.handle.set_channel_subset(ci.sensor_index, None)
+        ci.process_channel = np.ones(ci.sensor_channel.size, bool)
+        ci.n_channels = int(ci.process_channel.sum())
+        return SUCCESS
+    if channel_subset is None:
+        return SUCCESS
+    sub = np.asarray(channel_subset, np.int64).ravel()
+    ci.process_channel = np.zeros(ci.sensor_channel.size, bool)
+    err = None
+    if sub.size > ci.sensor_channel.size:
+        err = "Specified Channel_Subset contains too many channels!"
+    elif sub.size and (sub.min() < ci.sensor_channel.min() or sub.max() > ci.sensor_channel.max()):
+        err = "Specified Channel_Subset contains invalid channels!"
+    else:
+        ci.process_channel = np.isin(ci.sensor_channel, sub)
+    ci.handle.set_channel_subset(ci.sensor_index, np.flatnonzero(ci.process_channel))
+    ci.n_channels = int(ci.process_channel.sum())
+    if err:
+        print(f"CRTM_ChannelInfo_Subset(FAILURE): {err}")
+        return FAILURE
+    return SUCCESS
 
 
 def CRTM_Init(sensor_ids: Sequence[str], channel_info: List[ChannelInfo], file_path: str = ".",
@@ -587,8 +656,11 @@ def CRTM_Init(sensor_ids: Sequence[str], channel_info: List[ChannelInfo], file_p
         print(f"CRTM_Init(FAILURE): {e}")
         return FAILURE
     channel_info.clear()
+    from .coefficients import read_spccoeff
     for i, s in enumerate(sensor_ids):
-        channel_info.append(ChannelInfo(s, i, h.n_channels[i], h))
+        sc = read_spccoeff(os.path.join(path, f"{s}.SpcCoeff.bin"))
+        channel_info.append(ChannelInfo(s, i, h.n_channels[i], h, np.asarray(sc.sensor_channel),
+                                        np.ones(h.n_channels[i], bool)))
     return SUCCESS
 
 
@@ -637,7 +709,17 @@ def CRTM_K_Matrix(atmosphere, surface, rts_k: Optional[Sequence[np.ndarray]], ge
                   rts: List[RTSolutionBatch], options: Optional[OptionsBatch] = None) -> int:
     """CRTM_K_Matrix.  ``rts_k[i]`` is the (P, L_i) brightness-temperature seed of sensor i
     (None: 1); ``atmosphere_k`` receives the K-matrix per sensor (the surface Jacobians
-    are in its water_temperature / surface_emissivity fields)."""
+    are in its water_temperature / surface_emissivity fields).  As the
+    reference's INTENT(IN OUT) Atmosphere_K / Surface_K (CRTM_K_Matrix_Module.f90:
+    300-322; the adjoints add into them, CRTM_Atmosphere.f90:583-586): a list
+    holding one KMatrixBatch per sensor on entry is accumulated into (zero it
+    first for the plain K-matrix); an empty list is filled."""
+    accumulate = len(atmosphere_k) > 0
+    if accumulate and len(atmosphere_k) != len(channel_info):
+        print("CRTM_K_Matrix(FAILURE): atmosphere_k holds %d structures for %d sensors"
+              % (len(atmosphere_k), len(channel_info)))
+        return FAILURE
+    given = list(atmosphere_k)
     atmosphere_k.clear()
     rts.clear()
     atmosphere, added = _added_layers(atmosphere, "CRTM_K_Matrix")
@@ -655,6 +737,12 @@ def CRTM_K_Matrix(atmosphere, surface, rts_k: Optional[Sequence[np.ndarray]], ge
         if added.any:
             km = dataclasses.replace(km, **{f: addlayers.user_layers(added, getattr(km, f))
                                              for f in LAYER_FIELDS})
+        if accumulate:
+            try:
+                km = _accumulate(given[i], km)
+            except ValueError as e:
+                print(f"CRTM_K_Matrix(FAILURE): {e}")
+                return FAILURE
         atmosphere_k.append(km)
         rts.append(_user_layer_components(added, r))
         off += ci.n_channels
@@ -664,7 +752,10 @@ def CRTM_K_Matrix(atmosphere, surface, rts_k: Optional[Sequence[np.ndarray]], ge
 def CRTM_Adjoint(atmosphere, surface, rts_ad: Sequence[np.ndarray], geometry,
                  channel_info: List[ChannelInfo], atmosphere_ad: dict, rts: List[RTSolutionBatch],
                  options: Optional[OptionsBatch] = None) -> int:
-    """CRTM_Adjoint: adjoints summed over the channels of all sensors into ``atmosphere_ad``."""
+    """CRTM_Adjoint: adjoints summed over the channels of all sensors into
+    ``atmosphere_ad``; arrays it holds on entry are accumulated into, as the
+    reference's INTENT(IN OUT) Atmosphere_AD / Surface_AD (zero them first for
+    the plain adjoint)."""
     rts.clear()
     atmosphere, added = _added_layers(atmosphere, "CRTM_Adjoint")
     if atmosphere is None:
@@ -685,9 +776,29 @@ def CRTM_Adjoint(atmosphere, surface, rts_ad: Sequence[np.ndarray], geometry,
             tot[k] = tot[k] + v if k in tot else v.copy()
         rts.append(_user_layer_components(added, r))
         off += ci.n_channels
-    atmosphere_ad.clear()
-    atmosphere_ad.update(tot)
+    for k, v in tot.items():
+        prev = atmosphere_ad.get(k)
+        if prev is not None:
+            if np.shape(prev) != v.shape:
+                print(f"CRTM_Adjoint(FAILURE): atmosphere_ad['{k}'] has shape {np.shape(prev)}, not {v.shape}")
+                return FAILURE
+            v = prev + v
+        atmosphere_ad[k] = v
     return SUCCESS
+
+
+def _accumulate(given: KMatrixBatch, new: KMatrixBatch) -> KMatrixBatch:
+    """The caller's K-matrix structure plus this call's (fields the caller's
+    structure lacks are taken as returned)."""
+    out = {}
+    for f in dataclasses.fields(KMatrixBatch):
+        a, b = getattr(given, f.name), getattr(new, f.name)
+        if a is not None and b is not None:
+            if np.shape(a) != np.shape(b):
+                raise ValueError(f"atmosphere_k field {f.name} has shape {np.shape(a)}, not {np.shape(b)}")
+            b = a + b
+        out[f.name] = b
+    return KMatrixBatch(**out)
 
 
 def CRTM_Tangent_Linear(atmosphere, surface, atmosphere_tl, surface_tl, geometry,

@@ -150,6 +150,14 @@ struct Sensor {
   int tune_map[2] = {0, 0};
   int tune_chunk[2] = {0, 0};
   double tune_ms[2] = {0.0, 0.0};
+  // all the file's channels (host copies), for channel subsets
+  // (crtm_gpu_set_channel_subset): L and the device arrays above hold the
+  // processed channels only
+  int L_all = 0, Lp_all = 0;
+  std::vector<float> C_all;          // [K][NS][Lp_all]
+  std::vector<unsigned> cmask_all;   // [L_all]
+  std::vector<double> spec_all;      // [7][L_all]
+  std::vector<int> processed;        // file positions of the processed channels; empty: all
 };
 
 bool load_sensor(const std::string& dir, const std::string& id, Sensor& s, std::string& err) {
@@ -288,6 +296,11 @@ bool load_sensor(const std::string& dir, const std::string& id, Sensor& s, std::
   size_t o_tzr = put(tzr), o_tzpr = put(tzpr), o_gzr = put(gzr), o_gtr = put(gtr);
   std::vector<double> spec;
   for (auto* v : {&s.c1, &s.c2, &s.b1, &s.b2, &s.cbr, &s.freq, &s.wn}) spec.insert(spec.end(), v->begin(), v->end());
+  s.L_all = L;
+  s.Lp_all = Lp;
+  s.C_all = Cd;
+  s.cmask_all = cmask;
+  s.spec_all = spec;
   cudaError_t ce;
   if ((ce = cudaMalloc(&s.d_C, Cd.size() * sizeof(float))) != cudaSuccess ||
       (ce = cudaMalloc(&s.d_cmask, cmask.size() * sizeof(unsigned))) != cudaSuccess ||
@@ -311,6 +324,51 @@ bool load_sensor(const std::string& dir, const std::string& id, Sensor& s, std::
   s.spec.c1 = s.d_spec; s.spec.c2 = s.d_spec + L; s.spec.b1 = s.d_spec + 2 * L;
   s.spec.b2 = s.d_spec + 3 * L; s.spec.cbr = s.d_spec + 4 * L;
   s.spec.freq = s.d_spec + 5 * L; s.spec.wn = s.d_spec + 6 * L;
+  return true;
+}
+
+// The device arrays of the channels at file positions `pos` (all channels
+// when empty): coefficients [K][NS][Lp], component masks and SpcCoeff
+// columns, gathered from the host copies.
+bool upload_channels(Sensor& s, const std::vector<int>& pos, std::string& err) {
+  const int K = s.K, NS = s.NS;
+  const bool all = pos.empty();
+  const int L = all ? s.L_all : (int)pos.size();
+  const int Lp = std::max(32, (L + 31) / 32 * 32);
+  std::vector<float> Cd((size_t)K * NS * Lp, 0.0f);
+  std::vector<unsigned> cmask(std::max(L, 1), 0u);
+  std::vector<double> spec((size_t)7 * std::max(L, 1), 0.0);
+  for (int l = 0; l < L; l++) {
+    const int q = all ? l : pos[l];
+    for (size_t r = 0; r < (size_t)K * NS; r++) Cd[r * Lp + l] = s.C_all[r * s.Lp_all + q];
+    cmask[l] = s.cmask_all[q];
+    for (int f = 0; f < 7; f++) spec[(size_t)f * L + l] = s.spec_all[(size_t)f * s.L_all + q];
+  }
+  float* dC = nullptr;
+  unsigned* dm = nullptr;
+  double* ds = nullptr;
+  cudaError_t ce;
+  if ((ce = cudaMalloc(&dC, Cd.size() * sizeof(float))) != cudaSuccess ||
+      (ce = cudaMalloc(&dm, cmask.size() * sizeof(unsigned))) != cudaSuccess ||
+      (ce = cudaMalloc(&ds, spec.size() * sizeof(double))) != cudaSuccess ||
+      (ce = cudaMemcpy(dC, Cd.data(), Cd.size() * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (ce = cudaMemcpy(dm, cmask.data(), cmask.size() * sizeof(unsigned), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (ce = cudaMemcpy(ds, spec.data(), spec.size() * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess) {
+    cudaFree(dC); cudaFree(dm); cudaFree(ds);
+    err = std::string("device upload of the channel subset failed: ") + cudaGetErrorString(ce);
+    return false;
+  }
+  cudaFree(s.d_C); cudaFree(s.d_cmask); cudaFree(s.d_spec);
+  s.d_C = dC; s.d_cmask = dm; s.d_spec = ds;
+  s.L = L; s.Lp = Lp; s.tables.L = L;
+  s.spec.c1 = ds; s.spec.c2 = ds + L; s.spec.b1 = ds + 2 * L;
+  s.spec.b2 = ds + 3 * L; s.spec.cbr = ds + 4 * L;
+  s.spec.freq = ds + 5 * L; s.spec.wn = ds + 6 * L;
+  for (int f = 0; f < 7; f++) {
+    std::vector<double>* v[7] = {&s.c1, &s.c2, &s.b1, &s.b2, &s.cbr, &s.freq, &s.wn};
+    v[f]->assign(spec.begin() + (size_t)f * L, spec.begin() + (size_t)f * L + L);
+  }
+  s.processed = pos;
   return true;
 }
 
@@ -1212,6 +1270,7 @@ int dispatch(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, c
              cudaStream_t st, const HostCopy* hc = nullptr, const FixedScratch* fixed = nullptr) {
   if (!h) return CRTM_GPU_FAILURE;
   if (sensor < 0 || sensor >= (int)h->sensors.size()) return fail(h, "sensor index %d out of range", sensor);
+  if (h->sensors[sensor].L == 0) return CRTM_GPU_SUCCESS;   // an empty channel subset: nothing to compute
   if (!b || !rts || !rts->radiance || !rts->brightness_temperature) return fail(h, "missing batch or RTSolution buffers");
   if (!b->n_layers || !b->level_pressure || !b->pressure || !b->temperature ||
       !b->land_coverage || !b->water_coverage || !b->snow_coverage || !b->ice_coverage ||
@@ -1519,7 +1578,7 @@ int host_call(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, int mode, 
   if (!b || b->n_profiles < 0 || b->max_layers < 1 || b->n_absorbers < 0) return fail(h, "bad batch dimensions");
   if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
   const int P = b->n_profiles, Km = b->max_layers, J = b->n_absorbers, L = h->sensors[sensor].L;
-  if (P == 0) return CRTM_GPU_SUCCESS;
+  if (P == 0 || L == 0) return CRTM_GPU_SUCCESS;
   for (int m = 0; m < P; m++)
     if (b->n_layers[m] < 2 || b->n_layers[m] > Km)
       return fail(h, "profile %d: n_layers %d outside [2, max_layers=%d]", m, b->n_layers[m], Km);
@@ -1684,7 +1743,7 @@ int tl_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm
   if (!b || b->n_profiles < 0 || b->max_layers < 1) return fail(h, "bad batch dimensions");
   const size_t P = b->n_profiles, L = h->sensors[sensor].L, Km = b->max_layers, J = b->n_absorbers;
   const size_t NC = b->max_clouds > 0 ? b->max_clouds : 0, NA = b->max_aerosols > 0 ? b->max_aerosols : 0;
-  if (P == 0) return CRTM_GPU_SUCCESS;
+  if (P == 0 || L == 0) return CRTM_GPU_SUCCESS;
   const bool wc = NC && (tl->cloud_water_content || tl->cloud_effective_radius);
   const bool cf = NC && tl->cloud_fraction;
   const bool aer = NA && (tl->aerosol_concentration || tl->aerosol_effective_radius);
@@ -1739,7 +1798,7 @@ int tl_host(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm_g
   if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
   const size_t P = b->n_profiles, L = h->sensors[sensor].L, Km = b->max_layers, J = b->n_absorbers;
   const size_t NC = b->max_clouds > 0 ? b->max_clouds : 0, NA = b->max_aerosols > 0 ? b->max_aerosols : 0;
-  if (P == 0) return CRTM_GPU_SUCCESS;
+  if (P == 0 || L == 0) return CRTM_GPU_SUCCESS;
   for (size_t m = 0; m < P; m++)
     if (b->n_layers[m] < 2 || b->n_layers[m] > (int)Km)
       return fail(h, "profile %zu: n_layers %d outside [2, max_layers=%zu]", m, b->n_layers[m], Km);
@@ -1989,6 +2048,44 @@ int crtm_gpu_destroy(crtm_gpu_handle h) {
 int crtm_gpu_n_channels(crtm_gpu_handle h, int sensor) {
   if (!h || sensor < 0 || sensor >= (int)h->sensors.size()) return -1;
   return h->sensors[sensor].L;
+}
+
+int crtm_gpu_set_channel_subset(crtm_gpu_handle h, int sensor, int n, const int* channel_index) {
+  if (!h) return CRTM_GPU_FAILURE;
+  if (sensor < 0 || sensor >= (int)h->sensors.size()) return fail(h, "sensor index %d out of range", sensor);
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
+  Sensor& s = h->sensors[sensor];
+  std::vector<int> pos;
+  if (n >= 0) {
+    if (n > 0 && !channel_index) return fail(h, "missing channel subset");
+    if (n > s.L_all) return fail(h, "channel subset of %d channels for a sensor of %d", n, s.L_all);
+    pos.assign(channel_index, channel_index + n);
+    std::sort(pos.begin(), pos.end());
+    for (int i = 0; i < n; i++) {
+      if (pos[i] < 0 || pos[i] >= s.L_all)
+        return fail(h, "channel subset index %d out of range [0, %d)", pos[i], s.L_all);
+      if (i > 0 && pos[i] == pos[i - 1]) return fail(h, "channel %d given twice in the subset", pos[i]);
+    }
+    if (n == 0) pos.push_back(-1);   // marker: no channels
+  }
+  // wait for calls in flight on the handle's stream before the tables change
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) return fail(h, "stream synchronisation failed");
+  std::string err;
+  if (!pos.empty() && pos[0] == -1) {
+    s.L = 0;
+    s.processed = pos;
+    return CRTM_GPU_SUCCESS;
+  }
+  if (!upload_channels(s, pos, err)) return fail(h, "%s", err.c_str());
+  return CRTM_GPU_SUCCESS;
+}
+
+int crtm_gpu_get_channel_subset(crtm_gpu_handle h, int sensor, int capacity, int* channel_index) {
+  if (!h || sensor < 0 || sensor >= (int)h->sensors.size()) return -1;
+  const Sensor& s = h->sensors[sensor];
+  for (int l = 0; l < s.L && channel_index && l < capacity; l++)
+    channel_index[l] = s.processed.empty() ? l : s.processed[l];
+  return s.L;
 }
 
 int crtm_gpu_set_precision(crtm_gpu_handle h, int precision) {

@@ -289,8 +289,24 @@ int crtm_gpu_init_aerosol(const char* coeff_path, int n_sensors, const char* con
 /* CRTM_Destroy */
 int crtm_gpu_destroy(crtm_gpu_handle handle);
 
-/* Number of channels of sensor index `sensor` (0-based, init order), or -1. */
+/* Number of channels of sensor index `sensor` (0-based, init order) that
+ * calls process (all of the coefficient files' channels unless a subset is
+ * set), or -1 (CRTM_ChannelInfo_n_Channels, ChannelInfo/
+ * CRTM_ChannelInfo_Define.f90:336-340). */
 int crtm_gpu_n_channels(crtm_gpu_handle handle, int sensor);
+
+/* CRTM_ChannelInfo_Subset (ChannelInfo/CRTM_ChannelInfo_Define.f90:444-517):
+ * later calls for `sensor` process only the n channels at the 0-based file
+ * positions channel_index[0..n-1], in file order; their outputs have n
+ * channels ([P][n]...), as do the emissivity and seed inputs.  n = 0: no
+ * channels (calls return at once); n < 0: all channels again (Reset).
+ * Positions out of range or given twice fail and leave the setting as it
+ * was.  The call waits for the handle's work in flight. */
+int crtm_gpu_set_channel_subset(crtm_gpu_handle handle, int sensor, int n, const int* channel_index);
+
+/* The processed channels' file positions (up to capacity of them written to
+ * channel_index, which may be NULL); returns their count, or -1. */
+int crtm_gpu_get_channel_subset(crtm_gpu_handle handle, int sensor, int capacity, int* channel_index);
 
 /* Select the arithmetic form for later calls (CRTM_GPU_FP64 or CRTM_GPU_MIXED). */
 int crtm_gpu_set_precision(crtm_gpu_handle handle, int precision);

@@ -171,18 +171,24 @@ class OracleHandle:
         self.o = Oracle(coeff_dir, SENSOR)
         self.seen = []
 
-    def forward(self, atm, sfc, geo, opt, sensor=0):
+    def forward(self, atm, sfc, geo, opt, sensor=0, components=False):
         self.seen.append(atm)
-        rad, bt = self.o.forward(atm, sfc, geo, opt)
-        return RTSolutionBatch(rad, bt, status=np.zeros(atm.n_profiles, np.int32))
+        if not components:
+            rad, bt = self.o.forward(atm, sfc, geo, opt)
+            return RTSolutionBatch(rad, bt, status=np.zeros(atm.n_profiles, np.int32))
+        x = self.o.forward_components(atm, sfc, geo, opt)
+        r = RTSolutionBatch(x.pop("radiance"), x.pop("bt"), status=np.zeros(atm.n_profiles, np.int32))
+        for f, v in x.items():
+            setattr(r, f, v)
+        return r
 
-    def k_matrix(self, atm, sfc, geo, opt, bt_k=None, sensor=0):
+    def k_matrix(self, atm, sfc, geo, opt, bt_k=None, sensor=0, components=False):
         self.seen.append(atm)
         r = self.o.k_matrix(atm, sfc, geo, opt, bt_k)
         km = KMatrixBatch(r["temperature_k"], r["absorber_k"], r["water_temperature_k"], r["surface_emissivity_k"])
         return km, RTSolutionBatch(r["radiance"], r["bt"], status=np.zeros(atm.n_profiles, np.int32))
 
-    def tangent_linear(self, atm, sfc, geo, opt, atm_tl=None, sfc_tl=None, sensor=0):
+    def tangent_linear(self, atm, sfc, geo, opt, atm_tl=None, sfc_tl=None, sensor=0, components=False):
         self.seen.append((atm, atm_tl))
         P, K = atm.n_profiles, atm.max_layers
         t_tl = np.ascontiguousarray(getattr(atm_tl, "temperature", None) if atm_tl is not None else None)
@@ -193,7 +199,7 @@ class OracleHandle:
         rad, bt = self.o.forward(atm, sfc, geo, opt)
         return bt_tl, RTSolutionBatch(rad, bt, status=np.zeros(P, np.int32))
 
-    def adjoint(self, atm, sfc, geo, opt, bt_ad, sensor=0):
+    def adjoint(self, atm, sfc, geo, opt, bt_ad, sensor=0, components=False):
         self.seen.append(atm)
         r = self.o.adjoint(atm, sfc, geo, opt, bt_ad)
         out = dict(temperature=r["temperature_ad"], absorber=r["absorber_ad"],
@@ -212,6 +218,13 @@ def test_entry_points_run_on_the_extended_profiles(coeff_dir):
     assert api.CRTM_Forward(atm, sfc, geo, ci, rts, opt) == api.SUCCESS
     assert h.seen[-1].max_layers == ext.max_layers
     np.testing.assert_array_equal(rts[0].brightness_temperature, h.o.forward(ext, sfc, geo, opt)[1])
+    # the layer components come back on the user's layers
+    lod = h.o.forward(ext, sfc, geo, opt, layer_od=True)[2]
+    assert rts[0].layer_optical_depth.shape == (3, L, atm.max_layers)
+    for p in range(3):
+        n, m = int(info.n_added[p]), int(atm.n_layers[p])
+        np.testing.assert_array_equal(rts[0].layer_optical_depth[p, :, :m], lod[p, :, n:n + m])
+        assert not rts[0].layer_optical_depth[p, :, m:].any()
 
     seed = np.random.default_rng(2).uniform(0.5, 1.5, (3, L))
     ks, rts = [], []
@@ -282,3 +295,56 @@ def test_tangent_linear_gives_the_added_layers_no_perturbation(coeff_dir):
     assert api.CRTM_K_Matrix(atm, sfc, None, geo, ci, ks, r2, opt) == api.SUCCESS
     lin = np.einsum("plk,pk->pl", ks[0].temperature, dT)
     assert np.abs(tl[0] - lin).max() < 1e-5 * np.abs(lin).max()
+
+
+def test_k_matrix_and_adjoint_accumulate_into_given_structures(coeff_dir):
+    """CRTM_K_Matrix / CRTM_Adjoint add into the structures the caller passes
+    (the reference's INTENT(IN OUT) Atmosphere_K and Atmosphere_AD), and fill
+    an empty list / dict."""
+    atm, sfc, geo, opt = _workload(P=2, cut=(5, 9))
+    h = OracleHandle(coeff_dir)
+    L = h.o.n_channels
+    ci = [api.ChannelInfo(SENSOR, 0, L, h)]
+    ks, rts = [], []
+    assert api.CRTM_K_Matrix(atm, sfc, None, geo, ci, ks, rts, opt) == api.SUCCESS
+    once = ks[0].temperature.copy()
+    assert api.CRTM_K_Matrix(atm, sfc, None, geo, ci, ks, rts, opt) == api.SUCCESS
+    np.testing.assert_allclose(ks[0].temperature, 2 * once, rtol=1e-15)
+    zero = [dataclasses.replace(ks[0], **{f: np.zeros_like(getattr(ks[0], f)) for f in
+                                          ("temperature", "absorber", "water_temperature", "surface_emissivity")})]
+    assert api.CRTM_K_Matrix(atm, sfc, None, geo, ci, zero, rts, opt) == api.SUCCESS
+    np.testing.assert_array_equal(zero[0].temperature, once)
+    assert api.CRTM_K_Matrix(atm, sfc, None, geo, ci, [ks[0], ks[0]], rts, opt) == api.FAILURE
+    seed = np.ones((2, L))
+    ad, rts = {}, []
+    assert api.CRTM_Adjoint(atm, sfc, [seed], geo, ci, ad, rts, opt) == api.SUCCESS
+    first = ad["temperature"].copy()
+    assert api.CRTM_Adjoint(atm, sfc, [seed], geo, ci, ad, rts, opt) == api.SUCCESS
+    np.testing.assert_allclose(ad["temperature"], 2 * first, rtol=1e-15)
+
+
+def test_channel_info_subset_host_logic(coeff_dir):
+    """CRTM_ChannelInfo_Subset's checks and bookkeeping (the handle records
+    the processed file positions): a subset in any order, too many channels,
+    numbers out of range (which turn every channel off), reset."""
+    class Handle:
+        def __init__(self):
+            self.calls = []
+
+        def set_channel_subset(self, sensor, positions):
+            self.calls.append(None if positions is None else list(positions))
+
+    h = Handle()
+    chans = np.array([3, 5, 9, 12, 40], np.int32)
+    ci = api.ChannelInfo("s", 0, 5, h, chans, np.ones(5, bool))
+    assert api.CRTM_ChannelInfo_Subset(ci, [40, 5]) == api.SUCCESS
+    assert h.calls[-1] == [1, 4] and api.CRTM_ChannelInfo_n_Channels(ci) == 2
+    assert list(api.CRTM_ChannelInfo_Channels(ci)) == [5, 40]
+    assert api.CRTM_ChannelInfo_Subset(ci, list(range(6))) == api.FAILURE
+    assert api.CRTM_ChannelInfo_n_Channels(ci) == 0 and h.calls[-1] == []
+    assert api.CRTM_ChannelInfo_Subset(ci, [2]) == api.FAILURE
+    assert api.CRTM_ChannelInfo_n_Channels(ci) == 0
+    assert api.CRTM_ChannelInfo_Subset(ci, [9], reset=True) == api.SUCCESS
+    assert api.CRTM_ChannelInfo_n_Channels(ci) == 5 and h.calls[-1] is None
+    assert api.CRTM_ChannelInfo_Subset(ci, []) == api.SUCCESS
+    assert api.CRTM_ChannelInfo_n_Channels(ci) == 0
