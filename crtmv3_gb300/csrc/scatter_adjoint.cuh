@@ -72,7 +72,7 @@ CRTM_HD void inverse_adjoint(int n, const Mat<NZ, T>& Y, const Mat<NZ, T>& Yb, M
 // entry is read) and Planck radiance (B_b).  Returns false where the forward
 // factorisation fails.  gap: as in ada_layer.
 template <int NZ, class T>
-CRTM_HD_NOINLINE bool ada_layer_adjoint(int nS, int nZ, T w, T tau, const T* mu, const T* wt, const Mat<NZ, T>& ff,
+CRTM_HD bool ada_layer_adjoint(int nS, int nZ, T w, T tau, const T* mu, const T* wt, const Mat<NZ, T>& ff,
                                const Mat<NZ, T>& bb, T B, const Mat<NZ, T>& T_b, const Mat<NZ, T>& R_b,
                                const T* src_b, T* w_b, T* tau_b, Mat<NZ, T>& ff_b, Mat<NZ, T>& bb_b, T* B_b,
                                double* gap = nullptr) {
@@ -368,7 +368,7 @@ CRTM_HD_NOINLINE bool ada_layer_adjoint(int nS, int nZ, T w, T tau, const T* mu,
 // entries left of the diagonal; the sensor angle's column is divided by the
 // carried sum of its row.  The forward values are recomputed here.
 template <int NZ, class T>
-CRTM_HD_NOINLINE void phase_blocks_adjoint(int nS, int nZ, int nleg, const T* pc, const T (*P)[SC_NLEG_MAX + 1], const T* wt,
+CRTM_HD void phase_blocks_adjoint(int nS, int nZ, int nleg, const T* pc, const T (*P)[SC_NLEG_MAX + 1], const T* wt,
                                   const Mat<NZ, T>& ff_b, const Mat<NZ, T>& bb_b, T* pc_b) {
   Mat<NZ, T> f0, b0, fb, bq;   // clamped unscaled blocks (upper triangle) and their adjoints
   unsigned clampf[NZ] = {0}, clampb[NZ] = {0};
@@ -569,11 +569,15 @@ CRTM_HD int bulk_to_inputs(const CloudyColumn& in, const CloudLut& lut, int nleg
 // eigenbasis is nearly defective take the derivatives through MOM at shifted
 // sensor angles, as layer_optics_dual does.  Returns the layer kind (1
 // scattering, 0 clear) or a negative error; kind_rec is the record's kind
-// (the forward's); a mismatch returns -7.
+// (the forward's); a mismatch returns -7.  In FP32, *in_fp64 is set (and
+// nothing written) where the layer must be taken in FP64; layer_adjoint
+// below then runs the FP64 instance.
 template <int NZ, class T>
-CRTM_HD_NOINLINE int layer_adjoint(const CloudyColumn& in, const CloudLut& lut, const StreamSet<NZ, double>& St, int k,
-                          double gas_od, int kind_rec, const Mat<NZ, double>& T_b, const Mat<NZ, double>& R_b,
-                          const double* src_b, double od_b, double B_b, double* g, double (*gs)[3]) {
+CRTM_HD int layer_adjoint_in(const CloudyColumn& in, const CloudLut& lut, const StreamSet<NZ, double>& St, int k,
+                             double gas_od, int kind_rec, const Mat<NZ, double>& T_b, const Mat<NZ, double>& R_b,
+                             const double* src_b, double od_b, double B_b, double* g, double (*gs)[3],
+                             bool* in_fp64) {
+  constexpr bool fp32 = std::is_same<T, float>::value;
   const int nleg = St.nleg, nS = St.nS, nZ = St.nZ;
   // the layer's bulk optics in FP64 (the combine's adjoint needs them there;
   // the LUT work is small), and in T for the MOM work
@@ -607,12 +611,12 @@ CRTM_HD_NOINLINE int layer_adjoint(const CloudyColumn& in, const CloudLut& lut, 
     A.od_b = T(od_b);
     A.B_b = T(B_b);
   } else {
-    if constexpr (std::is_same<T, float>::value) {
-      // a nearly conservative layer: the smallest eigenvalue of MOM's
-      // (PP - PM)(PP + PM), about 1 - ssa, carries FP32's absolute error, and
-      // the single-scattering albedo's adjoint loses eps / (1 - ssa): in FP64
-      if (1.0 - Ld.ssa < FP32_COALBEDO_MIN)
-        return layer_adjoint<NZ, double>(in, lut, St, k, gas_od, kind_rec, T_b, R_b, src_b, od_b, B_b, g, gs);
+    // FP32: a nearly conservative layer: the smallest eigenvalue of MOM's
+    // (PP - PM)(PP + PM), about 1 - ssa, carries FP32's absolute error, and
+    // the single-scattering albedo's adjoint loses eps / (1 - ssa): in FP64
+    if (fp32 && 1.0 - Ld.ssa < FP32_COALBEDO_MIN) {
+      *in_fp64 = true;
+      return 0;
     }
     const double te = in.b1 + in.b2 * in.temperature[k];
     const T B = T(in.c1 / (exp(in.c2 / te) - 1.0));
@@ -626,13 +630,12 @@ CRTM_HD_NOINLINE int layer_adjoint(const CloudyColumn& in, const CloudLut& lut, 
     T w_b, tau_b, Bb;
     const bool ok = ada_layer_adjoint<NZ, T>(nS, nZ, L.ssa, L.od, mu, wt, ff, bb, B, Tb, Rb, sb, &w_b, &tau_b, ffb,
                                              bbb, &Bb, &gap);
-    constexpr bool fp32 = std::is_same<T, float>::value;
     if (!ok) {
-      // a failed FP32 factorisation: this layer in FP64
-      if constexpr (fp32)
-        return layer_adjoint<NZ, double>(in, lut, St, k, gas_od, kind_rec, T_b, R_b, src_b, od_b, B_b, g, gs);
-      return -5;
+      if (!fp32) return -5;
+      *in_fp64 = true;   // a failed FP32 factorisation: this layer in FP64
+      return 0;
     }
+    bool rich = false;
     const double gap_min = fp32 ? FP32_ADJ_GAP_MIN : SENSOR_GAP_MIN;
     if (gap < gap_min && nZ == nS + 1) {
       // A quadrature eigenvalue of MOM nearly meets the sensor angle's: the
@@ -649,6 +652,7 @@ CRTM_HD_NOINLINE int layer_adjoint(const CloudyColumn& in, const CloudLut& lut, 
       for (int l = 0; l <= nleg; l++) S2.p_b[l] = T(0.0);
       int n_ok = 0;
       const int zz = nZ - 1;
+#pragma unroll 1
       for (int side = 0; side < 4; side++) {
         const double fsh = (side & 1 ? -1.0 : 1.0) * (side < 2 ? shift : 2.0 * shift);
         const T wgt = T((side < 2 ? 4.0 : -1.0) / 6.0);
@@ -680,21 +684,37 @@ CRTM_HD_NOINLINE int layer_adjoint(const CloudyColumn& in, const CloudLut& lut, 
         n_ok++;
       }
       if (n_ok == 4) {
-        if (const int rc = bulk_to_inputs<T>(in, lut, nleg, St.loff, k, in.temperature[k], Ld, S2, nsp, g, gs))
-          return rc;
-        return 1;
+        A = S2;
+        rich = true;
+      } else if (fp32) {   // a shifted angle failed: FP32 goes to FP64; FP64 keeps the direct derivatives
+        *in_fp64 = true;
+        return 0;
       }
-      // a shifted angle failed: FP32 goes to FP64; FP64 keeps the direct derivatives
-      if constexpr (fp32)
-        return layer_adjoint<NZ, double>(in, lut, St, k, gas_od, kind_rec, T_b, R_b, src_b, od_b, B_b, g, gs);
     }
-    A.od_b = tau_b;
-    A.ssa_b = w_b;
-    A.B_b = Bb;
-    phase_blocks_adjoint<NZ, T>(nS, nZ, nleg, L.p, P, wt, ffb, bbb, A.p_b);
+    if (!rich) {
+      A.od_b = tau_b;
+      A.ssa_b = w_b;
+      A.B_b = Bb;
+      phase_blocks_adjoint<NZ, T>(nS, nZ, nleg, L.p, P, wt, ffb, bbb, A.p_b);
+    }
   }
   if (const int rc = bulk_to_inputs<T>(in, lut, nleg, St.loff, k, in.temperature[k], Ld, A, nsp, g, gs))
     return rc;
   return kind;
+}
+template <int NZ, class T>
+CRTM_HD int layer_adjoint(const CloudyColumn& in, const CloudLut& lut, const StreamSet<NZ, double>& St, int k,
+                          double gas_od, int kind_rec, const Mat<NZ, double>& T_b, const Mat<NZ, double>& R_b,
+                          const double* src_b, double od_b, double B_b, double* g, double (*gs)[3]) {
+  bool in_fp64 = false;
+  const int r = layer_adjoint_in<NZ, T>(in, lut, St, k, gas_od, kind_rec, T_b, R_b, src_b, od_b, B_b, g, gs,
+                                        &in_fp64);
+  if constexpr (std::is_same<T, float>::value) {
+    // one call site of the FP64 instance for every FP32 fallback
+    if (in_fp64)
+      return layer_adjoint_in<NZ, double>(in, lut, St, k, gas_od, kind_rec, T_b, R_b, src_b, od_b, B_b, g, gs,
+                                          &in_fp64);
+  }
+  return r;
 }
 }  // namespace crtm

@@ -28,16 +28,6 @@
 #include "dual.cuh"
 #include "odps_physics.cuh"
 
-// The large per-layer solvers are compiled once per instance and called
-// rather than inlined at every call site: the FP32 forms call them again at
-// shifted sensor angles and fall back to the FP64 instance, and inlining each
-// call multiplied the code and the compile time.
-#ifdef __CUDACC__
-#define CRTM_HD_NOINLINE __host__ __device__ __noinline__
-#else
-#define CRTM_HD_NOINLINE
-#endif
-
 namespace crtm {
 
 constexpr int SC_NLEG_MAX = 16;          // MAX_N_LEGENDRE_TERMS
@@ -428,7 +418,7 @@ CRTM_HD void jacobi(int n, Mat<NZ, Dual<N, Q>>& S, Dual<N, Q>* lam, Mat<NZ, Dual
 // all nZ angles; V and W are scratch.  Returns false on a failed
 // factorisation.  gap: see ada_layer.
 template <int NZ, class T>
-CRTM_HD_NOINLINE bool mom_eigen(int nS, int nZ, T s, const T* mu, const T* wt, const Mat<NZ, T>& ff, const Mat<NZ, T>& bb,
+CRTM_HD bool mom_eigen(int nS, int nZ, T s, const T* mu, const T* wt, const Mat<NZ, T>& ff, const Mat<NZ, T>& bb,
                        Mat<NZ, T>& E, T* lam, Mat<NZ, T>& X, Mat<NZ, T>& Y, Mat<NZ, T>& V, Mat<NZ, T>& W,
                        double* gap) {
   // symmetric form of the quadrature block
@@ -533,7 +523,7 @@ CRTM_HD_NOINLINE bool mom_eigen(int nS, int nZ, T s, const T* mu, const T* wt, c
 // defective: the layer's T and R stay smooth, but their derivatives through
 // the eigenvectors lose about eps / gap^2 of their accuracy.
 template <int NZ, class T>
-CRTM_HD_NOINLINE bool ada_layer_loss(int nS, int nZ, T w, T tau, const T* mu, const T* wt, const Mat<NZ, T>& ff,
+CRTM_HD bool ada_layer_loss(int nS, int nZ, T w, T tau, const T* mu, const T* wt, const Mat<NZ, T>& ff,
                             const Mat<NZ, T>& bb, T B, Mat<NZ, T>& Um, Mat<NZ, T>& Rm, T* src,
                             double* gap = nullptr) {
   if (gap) *gap = 1.0;
@@ -1012,6 +1002,7 @@ CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const Stre
           for (int l = 0; l <= nleg; l++) P2[i][l] = P[i][l];
           for (int j = 0; j < St.nZ; j++) { Ta.a[i][j] = S(0.0); Ra.a[i][j] = S(0.0); }
         }
+#pragma unroll 1
         for (int side = 0; side < 4 && !in_fp64; side++) {
           const double fsh = (side & 1 ? -1.0 : 1.0) * (side < 2 ? FP32_SENSOR_SHIFT : 2.0 * FP32_SENSOR_SHIFT);
           const S wgt = S((side < 2 ? 4.0 : -1.0) / 6.0);
