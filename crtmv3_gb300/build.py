@@ -14,7 +14,7 @@ LIB = os.path.join(HERE, "libcrtm_gb300.so")
 # contraction.
 SOURCES = ["crtm_gpu.cu", "scatter_k_d5.cu", "scatter_k_d10.cu", "scatter_k_d5f.cu", "scatter_k_d10f.cu",
            "scatter_soi_d5.cu", "scatter_soi_d10.cu"]
-HEADERS = ["odps_physics.cuh", "odps_prep.cuh", "odps_kernels.cuh", "scatter_physics.cuh",
+HEADERS = ["odps_physics.cuh", "odps_prep.cuh", "odps_kernels.cuh", "optran.cuh", "scatter_physics.cuh",
            "scatter_kernels.cuh", "scatter_adjoint.cuh", "scatter_launch.h", "dual.cuh", "dd.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "--expt-relaxed-constexpr", "-lineinfo", "-Xcompiler", "-fPIC"]

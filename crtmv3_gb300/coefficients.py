@@ -55,9 +55,37 @@ MASS_MIXING_RATIO_UNITS = 3     # g/kg
 VOLUME_MIXING_RATIO_UNITS = 1   # ppmv
 
 
+# Compact-OPTRAN water-vapour-line term of an ODPS file (ODPS_Define.f90:103,
+# 186-203): predictors used per channel, polynomial order, channel flag value
+N_PREDICTOR_USED_OPTRAN = 6
+MAX_OPTRAN_ORDER = 10
+MAX_OPTRAN_PREDICTORS = 14
+SIGNIFICANCE_OPTRAN = 1
+
+
+@dataclasses.dataclass
+class OPTRANCoeff:
+    """The compact-OPTRAN part of an ODPS TauCoeff (``ODPS_Define.f90:186-203``):
+    per channel the flag OSignificance (1: the OComponent_Index component of
+    that channel is computed by OPTRAN), the polynomial Order, OP_Index
+    (OP_Index[0, l] the predictor count, then the predictor numbers 1-14;
+    Fortran index order, as the file's OP_Index(0:6, L)) and OPos_Index
+    (1-based start in OC); the coefficients OC and the absorber transform
+    Alpha, Alpha_C1, Alpha_C2."""
+    significance: np.ndarray        # (L,) int32
+    order: np.ndarray               # (L,) int32
+    op_index: np.ndarray            # (N_PREDICTOR_USED_OPTRAN + 1, L) int32
+    opos_index: np.ndarray          # (L,) int32, 1-based
+    oc: np.ndarray                  # (n_OCoeffs,) float64
+    alpha: float
+    alpha_c1: float
+    alpha_c2: float
+    component_index: int            # 1-based component the term replaces
+
+
 @dataclasses.dataclass
 class ODPSCoeff:
-    """The ODPS TauCoeff structure (``ODPS_Define.f90:110-200``), OPTRAN omitted."""
+    """The ODPS TauCoeff structure (``ODPS_Define.f90:110-203``)."""
     group_index: int
     sensor_id: str
     sensor_type: int
@@ -73,6 +101,7 @@ class ODPSCoeff:
     c: np.ndarray                       # (n_Coeffs,) float32
     wmo_satellite_id: int = 1023
     wmo_sensor_id: int = 2047
+    optran: Optional[OPTRANCoeff] = None
 
     @property
     def n_layers(self) -> int:
@@ -113,7 +142,8 @@ def write_odps(path: str, tc: ODPSCoeff, byteorder: str = "<") -> None:
         w = RecordWriter(f, byteorder)
         w.record(np.array([ODPS_RELEASE, ODPS_VERSION], np.int32))
         w.record(np.array([ODPS_ALGORITHM], np.int32))
-        w.record(np.array([K, J, Jm, L, tc.c.size, 6, 0], np.int32))
+        n_oc = 0 if tc.optran is None else int(tc.optran.oc.size)
+        w.record(np.array([K, J, Jm, L, tc.c.size, N_PREDICTOR_USED_OPTRAN, n_oc], np.int32))
         w.record(np.array([tc.group_index], np.int32))
         w.record(tc.sensor_id.ljust(SL)[:SL].encode("ascii"),
                  np.array([tc.wmo_satellite_id, tc.wmo_sensor_id, tc.sensor_type], np.int32))
@@ -126,6 +156,12 @@ def write_odps(path: str, tc: ODPSCoeff, byteorder: str = "<") -> None:
         w.record(tc.n_predictors.astype(np.int32), tc.pos_index.astype(np.int32))
         if tc.c.size > 0:
             w.record(tc.c.astype(np.float32))
+        if n_oc > 0:   # ODPS_Binary_IO.f90:1173-1180
+            o = tc.optran
+            w.record(o.significance.astype(np.int32), o.order.astype(np.int32),
+                     o.op_index.astype(np.int32), o.opos_index.astype(np.int32),
+                     o.oc.astype(np.float64), np.array([o.alpha, o.alpha_c1, o.alpha_c2], np.float64),
+                     np.array([o.component_index], np.int32))
 
 
 def read_odps(path: str) -> ODPSCoeff:
@@ -151,10 +187,16 @@ def read_odps(path: str) -> ODPSCoeff:
         c = np.zeros(0, np.float32)
         if n_coeffs > 0:
             c = r.split(r.record(), [("f4", (n_coeffs,))])[0]
-        if n_ocoeffs > 0:
-            raise IOError("ODPS files with OPTRAN coefficients are not supported")
+        optran = None
+        if n_ocoeffs > 0:   # ODPS_Binary_IO.f90:778-800
+            nu = N_PREDICTOR_USED_OPTRAN + 1
+            sig, order, opi, opos, oc, alph, ocomp = r.split(r.record(), [
+                ("i4", (L,)), ("i4", (L,)), ("i4", (nu, L)), ("i4", (L,)), ("f8", (n_ocoeffs,)),
+                ("f8", (3,)), ("i4", ())])
+            optran = OPTRANCoeff(sig, order, opi, opos, oc, float(alph[0]), float(alph[1]), float(alph[2]),
+                                 int(ocomp))
     return ODPSCoeff(int(group), sid, int(ids[2]), chans, lev, lay, temp, ra, mn, mx,
-                     npred, pos, c, int(ids[0]), int(ids[1]))
+                     npred, pos, c, int(ids[0]), int(ids[1]), optran)
 
 
 @dataclasses.dataclass

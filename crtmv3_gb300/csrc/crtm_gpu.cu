@@ -158,7 +158,49 @@ struct Sensor {
   std::vector<unsigned> cmask_all;   // [L_all]
   std::vector<double> spec_all;      // [7][L_all]
   std::vector<int> processed;        // file positions of the processed channels; empty: all
+  // compact-OPTRAN term (host copies per file channel; o_n[l] = 0: not an OPTRAN channel)
+  std::vector<int> o_n, o_idx;       // [L_all] predictor count; [L_all][8] count, OP_Index(1:6), order
+  std::vector<double> o_coef;        // [L_all][OPT_NU][OPT_ORDER+1]
+  double o_alpha = 1.0, o_c1 = 1.0, o_c2 = 0.0;
+  int* d_oidx = nullptr;             // device: the processed OPTRAN channels' tables
+  int* d_och = nullptr;
+  double* d_ocoef = nullptr;
+  OptranView ov{};
 };
+
+// The OPTRAN tables of the processed channels (file positions `pos`; all
+// when empty) on the device.
+bool upload_optran(Sensor& s, const std::vector<int>& pos, std::string& err) {
+  cudaFree(s.d_oidx); cudaFree(s.d_och); cudaFree(s.d_ocoef);
+  s.d_oidx = nullptr; s.d_och = nullptr; s.d_ocoef = nullptr;
+  s.ov = OptranView{};
+  s.ov.alpha = s.o_alpha; s.ov.alpha_c1 = s.o_c1; s.ov.alpha_c2 = s.o_c2;
+  std::vector<int> ch, ix;
+  std::vector<double> cf;
+  const int n = pos.empty() ? s.L_all : (int)pos.size();
+  const size_t nc = (size_t)OPT_NU * (OPT_ORDER + 1);
+  for (int l = 0; l < n; l++) {
+    const int q = pos.empty() ? l : pos[l];
+    if (q < 0 || q >= (int)s.o_n.size() || s.o_n[q] <= 0) continue;
+    ch.push_back(l);
+    ix.insert(ix.end(), s.o_idx.begin() + (size_t)q * 8, s.o_idx.begin() + (size_t)q * 8 + 8);
+    cf.insert(cf.end(), s.o_coef.begin() + (size_t)q * nc, s.o_coef.begin() + (size_t)q * nc + nc);
+  }
+  if (ch.empty()) return true;
+  cudaError_t ce;
+  if ((ce = cudaMalloc(&s.d_och, ch.size() * sizeof(int))) != cudaSuccess ||
+      (ce = cudaMalloc(&s.d_oidx, ix.size() * sizeof(int))) != cudaSuccess ||
+      (ce = cudaMalloc(&s.d_ocoef, cf.size() * sizeof(double))) != cudaSuccess ||
+      (ce = cudaMemcpy(s.d_och, ch.data(), ch.size() * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (ce = cudaMemcpy(s.d_oidx, ix.data(), ix.size() * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (ce = cudaMemcpy(s.d_ocoef, cf.data(), cf.size() * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess) {
+    err = std::string("device upload of the OPTRAN tables failed: ") + cudaGetErrorString(ce);
+    return false;
+  }
+  s.ov.n = (int)ch.size();
+  s.ov.ch = s.d_och; s.ov.idx = s.d_oidx; s.ov.coef = s.d_ocoef;
+  return true;
+}
 
 bool load_sensor(const std::string& dir, const std::string& id, Sensor& s, std::string& err) {
   s.id = id;
@@ -177,7 +219,6 @@ bool load_sensor(const std::string& dir, const std::string& id, Sensor& s, std::
   for (int i = 0; i < 7; i++) dims[i] = r.i32(d + 4 * i);
   s.K = dims[0]; s.J = dims[1]; s.Jm = dims[2]; s.L = dims[3];
   const long long n_coeffs = dims[4];
-  if (dims[6] > 0) return bad("ODPS OPTRAN coefficients are not supported by this build");
   if (s.K < 2 || s.K > MAX_LAYERS || s.L < 1) return bad("dimensions out of range");
   if (!r.next(d, len) || len != 4) return bad("corrupt Group record");
   s.group = r.i32(d);
@@ -219,6 +260,58 @@ bool load_sensor(const std::string& dir, const std::string& id, Sensor& s, std::
     if (!r.next(d, len) || len != 4u * (size_t)n_coeffs) return bad("corrupt coefficient record");
     for (long long i = 0; i < n_coeffs; i++) C[i] = r.f32(d + 4 * i);
   }
+  // compact OPTRAN (ODPS_Binary_IO.f90:778-800): OSignificance(L), Order(L),
+  // OP_Index(0:6, L), OPos_Index(L), OC(n), Alpha, Alpha_C1, Alpha_C2,
+  // OComponent_Index
+  const long long n_oc = dims[6];
+  int ocomp = -1;
+  s.o_n.assign(s.L, 0);
+  if (n_oc > 0) {
+    const size_t want = 4u * (size_t)s.L * (3 + OPT_NU) + 8u * (size_t)n_oc + 24 + 4;
+    if (!r.next(d, len) || len != want) return bad("corrupt OPTRAN record");
+    const int L = s.L;
+    size_t o2 = 0;
+    std::vector<int> sig(L), ord(L), opi((size_t)L * OPT_NU), opos(L);
+    for (int l = 0; l < L; l++) sig[l] = r.i32(d + o2 + 4 * l);
+    o2 += 4u * L;
+    for (int l = 0; l < L; l++) ord[l] = r.i32(d + o2 + 4 * l);
+    o2 += 4u * L;
+    for (size_t i = 0; i < opi.size(); i++) opi[i] = r.i32(d + o2 + 4 * i);
+    o2 += 4u * opi.size();
+    for (int l = 0; l < L; l++) opos[l] = r.i32(d + o2 + 4 * l);
+    o2 += 4u * L;
+    std::vector<double> oc(n_oc);
+    for (long long i = 0; i < n_oc; i++) oc[i] = r.f64(d + o2 + 8 * i);
+    o2 += 8u * (size_t)n_oc;
+    s.o_alpha = r.f64(d + o2); s.o_c1 = r.f64(d + o2 + 8); s.o_c2 = r.f64(d + o2 + 16);
+    ocomp = r.i32(d + o2 + 24) - 1;
+    if (ocomp < 0 || ocomp >= s.J) return bad("OPTRAN OComponent_Index out of range");
+    if (!(s.o_alpha != 0.0) || !(s.o_c1 != 0.0)) return bad("OPTRAN Alpha or Alpha_C1 is zero");
+    s.o_idx.assign((size_t)L * 8, 0);
+    s.o_coef.assign((size_t)L * OPT_NU * (OPT_ORDER + 1), 0.0);
+    for (int l = 0; l < L; l++) {
+      // OPTRAN replaces the component where the channel has it at all
+      // (ODPS_AtmAbsorption.f90:172-195); Add_OPTRAN_wloOD adds nothing
+      // where OP_Index(0) is 0
+      if (sig[l] != 1 || npred[(size_t)l * s.J + ocomp] <= 0) continue;
+      const int np = opi[(size_t)l * OPT_NU], od = ord[l];
+      if (np < 0 || np > OPT_NU - 1 || od < 0 || od > OPT_ORDER) return bad("OPTRAN order or predictor count");
+      s.o_n[l] = -1;   // the ODPS component is replaced
+      if (np == 0) continue;
+      for (int i = 1; i <= np; i++)
+        if (opi[(size_t)l * OPT_NU + i] < 1 || opi[(size_t)l * OPT_NU + i] > 14) return bad("OPTRAN OP_Index");
+      const long long p0 = (long long)opos[l] - 1;
+      if (p0 < 0 || p0 + (long long)(np + 1) * (od + 1) > n_oc) return bad("OPTRAN OPos_Index out of range");
+      s.o_n[l] = np;
+      int* ix = &s.o_idx[(size_t)l * 8];
+      ix[0] = np;
+      for (int i = 1; i <= np; i++) ix[i] = opi[(size_t)l * OPT_NU + i];
+      ix[7] = od;
+      double* cf = &s.o_coef[(size_t)l * OPT_NU * (OPT_ORDER + 1)];
+      for (int i = 0; i <= np; i++)
+        for (int j = 0; j <= od; j++) cf[i * (OPT_ORDER + 1) + j] = oc[p0 + (size_t)i * (od + 1) + j];
+    }
+  }
   // dense coefficient array [K][NS][L] and component masks
   const int K = s.K, L = s.L, NS = s.NS;
   s.Lp = (L + 31) / 32 * 32;   // 128-byte aligned coefficient rows
@@ -232,7 +325,7 @@ bool load_sensor(const std::string& dir, const std::string& id, Sensor& s, std::
       const int np = npred[(size_t)l * s.J + j];
       const int mx = npmax[s.group - 1][j];
       if (np > mx) return bad("n_Predictors exceeds the group's predictor count");
-      if (np > 0) {
+      if (np > 0 && !(j == ocomp && s.o_n[l] != 0)) {   // an OPTRAN channel's component: OPTRAN instead
         const long long p0 = (long long)pos[(size_t)l * s.J + j] - 1;
         if (p0 < 0 || p0 + (long long)np * K > n_coeffs) return bad("Pos_Index out of range");
         cmask[l] |= 1u << j;
@@ -277,6 +370,7 @@ bool load_sensor(const std::string& dir, const std::string& id, Sensor& s, std::
   auto put = [&](const std::vector<double>& v) { size_t at = tab.size(); tab.insert(tab.end(), v.begin(), v.end()); return at; };
   size_t o_lev = put(s.ref_lev), o_levl = put(lev_lnp), o_lnp = put(lnp), o_t = put(s.ref_t);
   size_t o_a = put(s.ref_a), o_mn = put(s.min_a), o_mx = put(s.max_a), o_pdp = put(pdp), o_z = put(z);
+  size_t o_rp = put(s.ref_p);
   // running sums of the reference profile (ODPS_Predictor.f90:707-759, the *_ref terms)
   std::vector<double> tzr(K), tzpr(K), gzr((size_t)s.Jm * K), gtr((size_t)s.Jm * K);
   {
@@ -318,7 +412,9 @@ bool load_sensor(const std::string& dir, const std::string& id, Sensor& s, std::
   t.h2o_idx = s.h2o_idx;
   t.ref_lev = s.d_tab + o_lev; t.ref_lev_lnp = s.d_tab + o_levl; t.ref_lnp = s.d_tab + o_lnp;
   t.ref_t = s.d_tab + o_t; t.ref_a = s.d_tab + o_a; t.min_a = s.d_tab + o_mn; t.max_a = s.d_tab + o_mx;
-  t.pdp = s.d_tab + o_pdp; t.zgeo = s.d_tab + o_z;
+  t.pdp = s.d_tab + o_pdp; t.zgeo = s.d_tab + o_z; t.ref_p = s.d_tab + o_rp;
+  t.o_alpha = s.o_alpha; t.o_c1 = s.o_c1; t.o_c2 = s.o_c2;
+  if (!upload_optran(s, std::vector<int>(), err)) return false;
   s.refsums.tz_ref = s.d_tab + o_tzr; s.refsums.tzp_ref = s.d_tab + o_tzpr;
   s.refsums.gazp_ref = s.d_tab + o_gzr; s.refsums.gatzp_ref = s.d_tab + o_gtr;
   s.spec.c1 = s.d_spec; s.spec.c2 = s.d_spec + L; s.spec.b1 = s.d_spec + 2 * L;
@@ -369,12 +465,14 @@ bool upload_channels(Sensor& s, const std::vector<int>& pos, std::string& err) {
     v[f]->assign(spec.begin() + (size_t)f * L, spec.begin() + (size_t)f * L + L);
   }
   s.processed = pos;
-  return true;
+  return upload_optran(s, pos, err);
 }
 
 void free_sensor(Sensor& s) {
   cudaFree(s.d_C); cudaFree(s.d_cmask); cudaFree(s.d_tab); cudaFree(s.d_spec);
+  cudaFree(s.d_oidx); cudaFree(s.d_och); cudaFree(s.d_ocoef);
   s.d_C = nullptr; s.d_cmask = nullptr; s.d_tab = nullptr; s.d_spec = nullptr;
+  s.d_oidx = nullptr; s.d_och = nullptr; s.d_ocoef = nullptr;
 }
 
 // CloudCoeff.bin (CloudCoeff_Binary_IO.f90:360-460): Release/Version, 8
@@ -734,6 +832,7 @@ size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w
   pv.ub_w = (double*)carve(nn * Kmax * MAX_UBAND * sizeof(double));
   pv.scal = (double*)carve(nn * 4 * sizeof(double));
   pv.status = (int*)carve(nn * sizeof(int));
+  pv.opt = s.ov.n > 0 ? (double*)carve(nn * K * OPT_NS * sizeof(double)) : nullptr;
   pv.K = K; pv.Kmax = Kmax; pv.npf = npf; pv.npa = adj ? npa : 0;
   Work<R> wk{};
   wk.pv = pv;
@@ -1032,6 +1131,10 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       absorb_fwd_kernel<G, R, NPF><<<gf, 32 * FWD_WARPS, fwd_smem, st>>>(K, L, s.Lp, n, s.d_C, s.d_cmask,
                                                                    w.pv.Xg, w.OD);
       CK_LAUNCH(h);
+      if (s.ov.n > 0) {   // the OPTRAN channels' water-vapour-line component
+        optran_fwd_kernel<R><<<dim3((s.ov.n + 127) / 128, n), 128, 0, st>>>(K, L, n, s.ov, w.pv.opt, w.OD);
+        CK_LAUNCH(h);
+      }
     }
     ColumnArgs<R> ca{};
     ca.K = K; ca.L = L; ca.Kmax = Kmax; ca.p_begin = p0; ca.n_chunk = n; ca.mode = mode;
@@ -1212,6 +1315,14 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
         absorb_ad_kernel<G, R, NPA, 0><<<ga, 32 * AD_WARPS, 0, st>>>(
             K, L, s.Lp, n, s.d_C, s.d_cmask, w.pv.Dg, s.tables.pdp, w.OD, w.SC, oa, w.RA);
       CK_LAUNCH(h);
+      if (s.ov.n > 0) {   // the OPTRAN terms' temperature and water vapour adjoints
+        int h2o_out = -1;
+        for (int j = 0; j < oa.n; j++)
+          if (oa.odps[j] == s.h2o_idx) h2o_out = j;
+        optran_ad_kernel<R><<<dim3((s.ov.n + 127) / 128, n), 128, 0, st>>>(
+            K, L, n, nv, h2o_out, s.h2o_idx, s.ov, w.pv.opt, s.tables.ref_lev, w.OD, w.SC, w.RA);
+        CK_LAUNCH(h);
+      }
     }
     if (mode == 1) {
       MapArgs<R> ma{};

@@ -29,6 +29,7 @@
 #include <utility>
 
 #include "odps_prep.cuh"
+#include "optran.cuh"
 
 namespace crtm {
 
@@ -274,6 +275,7 @@ struct PrepView {
   double* ub_w;        // [n][Kmax][MAX_UBAND]
   double* scal;        // [n][4]: sec_surface, u = cos(sensor zenith)
   int* status;         // [n]
+  double* opt;         // [n][K][OPT_NS] OPTRAN predictor state, or null (no OPTRAN channels)
   int K, Kmax, npf, npa;
 };
 
@@ -441,6 +443,20 @@ __global__ void __launch_bounds__(32) prep_kernel(SensorTables S, RefSums RS, Ba
       for (int a = 0; a < JM; a++) dO[(size_t)(NNZ + a) * pv.npa] = R(S.pdp[k] * sA[a * K + k]);
       dO[(size_t)(NNZ + JM) * pv.npa] = R(S.pdp[k] * sT[k]);
       dO[(size_t)(NNZ + JM + 1) * pv.npa] = R(float(sPass[k]));
+    }
+  }
+  // ---- compact-OPTRAN predictors (ODPS_Predictor.f90:336-347): a running
+  // sum over the layers, on lane 0, in FP64
+  if (pv.opt) {
+    __syncwarp();
+    if (lane == 0) {
+      double secl[MAX_LAYERS];
+      for (int k = 0; k < K; k++) {
+        const double sa = sv / (EARTH_RADIUS + (S.zgeo[k + 1] + zoff));
+        secl[k] = 1.0 / sqrt(1.0 - sa * sa);
+      }
+      optran_profile(K, sT, sA + (size_t)S.h2o_idx * K, secl, sPass, S.ref_lev, S.ref_p, S.o_alpha, S.o_c1,
+                     S.o_c2, pv.opt + (size_t)p * K * OPT_NS);
     }
   }
 #pragma unroll

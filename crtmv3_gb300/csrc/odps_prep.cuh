@@ -24,6 +24,8 @@ struct SensorTables {
   const double* max_a;         // [Jm][K]
   const double* pdp;           // [K]
   const double* zgeo;          // [K+1] geopotential height of the reference levels (Z(K)=0)
+  const double* ref_p;         // [K]   layer pressures (the OPTRAN predictors)
+  double o_alpha, o_c1, o_c2;  // OPTRAN absorber transform (Alpha, Alpha_C1, Alpha_C2)
 };
 
 // One profile of the batch (host or device pointers into the batch arrays).

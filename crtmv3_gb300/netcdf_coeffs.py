@@ -98,8 +98,10 @@ def read_spccoeff_nc(path: str) -> co.SpcCoeff:
 # ---------------------------------------------------------------------------
 
 def write_odps_nc(path: str, tc: co.ODPSCoeff) -> None:
-    """ODPS_netCDF_IO's layout (:63-240) without the OPTRAN part
-    (n_OCoeffs = 0)."""
+    """ODPS_netCDF_IO's layout (:63-240), with the compact-OPTRAN variables
+    (OSignificance, Order, OP_Index, OPos_Index, OC, Alpha, Alpha_C1,
+    Alpha_C2, OComponent_Index; dimensions n_OPIndex and n_OCoeffs, :80-107,
+    :232-240) when the file has them."""
     J, Jm, K, L = tc.n_components, tc.n_absorbers, tc.n_layers, int(tc.sensor_channel.shape[0])
     with netcdf_file(path, "w", version=1) as f:
         f.Release = np.int32(co.ODPS_RELEASE)
@@ -130,6 +132,19 @@ def write_odps_nc(path: str, tc: co.ODPSCoeff) -> None:
                 ("Pos_Index", "i4", ("n_Channels", "n_Components"), np.asarray(tc.pos_index).T),
                 ("ODPS_Coefficients", "f4", ("n_Coeffs",),
                  tc.c if tc.c.shape[0] else np.zeros(1, np.float32))]
+        o = tc.optran
+        if o is not None and o.oc.size > 0:
+            f.createDimension("n_OPIndex", co.N_PREDICTOR_USED_OPTRAN + 1)
+            f.createDimension("n_OCoeffs", int(o.oc.size))
+            for name, val, t in (("Alpha", o.alpha, "f8"), ("Alpha_C1", o.alpha_c1, "f8"),
+                                 ("Alpha_C2", o.alpha_c2, "f8"), ("OComponent_Index", o.component_index, "i4")):
+                v = f.createVariable(name, t, ())
+                v[...] = np.asarray(val).astype(t)
+            spec += [("OSignificance", "i4", ("n_Channels",), o.significance),
+                     ("Order", "i4", ("n_Channels",), o.order),
+                     ("OP_Index", "i4", ("n_Channels", "n_OPIndex"), np.asarray(o.op_index).T),
+                     ("OPos_Index", "i4", ("n_Channels",), o.opos_index),
+                     ("OC", "f8", ("n_OCoeffs",), o.oc)]
         for name, t, dims, data in spec:
             v = f.createVariable(name, t, dims)
             v[:] = np.asarray(data).astype(t)
@@ -137,9 +152,18 @@ def write_odps_nc(path: str, tc: co.ODPSCoeff) -> None:
 
 def read_odps_nc(path: str) -> co.ODPSCoeff:
     with netcdf_file(path, "r", mmap=False) as f:
+        optran = None
         if "n_OCoeffs" in f.dimensions and int(f.dimensions["n_OCoeffs"] or 0) > 0:
-            raise ValueError(f"{path}: ODPS file with OPTRAN water-vapour-line coefficients (n_OCoeffs > 0) "
-                             f"is not supported")
+            for name in ("OSignificance", "Order", "OP_Index", "OPos_Index", "OC", "Alpha", "Alpha_C1",
+                         "Alpha_C2", "OComponent_Index"):
+                if name not in f.variables:
+                    raise ValueError(f"{path}: OPTRAN variable {name} missing")
+            optran = co.OPTRANCoeff(
+                significance=_var(f, "OSignificance", np.int32), order=_var(f, "Order", np.int32),
+                op_index=_var(f, "OP_Index", np.int32).T.copy(), opos_index=_var(f, "OPos_Index", np.int32),
+                oc=_var(f, "OC", np.float64), alpha=float(f.variables["Alpha"].data[()]),
+                alpha_c1=float(f.variables["Alpha_C1"].data[()]), alpha_c2=float(f.variables["Alpha_C2"].data[()]),
+                component_index=int(f.variables["OComponent_Index"].data[()]))
         group = int(f.variables["Group_Index"].data[()])
         if group not in N_COMPONENTS_G:
             raise ValueError(f"{path}: unknown ODPS group index {group}")
@@ -161,7 +185,7 @@ def read_odps_nc(path: str) -> co.ODPSCoeff:
             max_absorber=_var(f, "Max_Absorber", np.float64).T.copy(),
             n_predictors=n_pred, pos_index=pos, c=c,
             wmo_satellite_id=int(_attr(f, "WMO_Satellite_Id", 1023)),
-            wmo_sensor_id=int(_attr(f, "WMO_Sensor_Id", 2047)))
+            wmo_sensor_id=int(_attr(f, "WMO_Sensor_Id", 2047)), optran=optran)
 
 
 # ---------------------------------------------------------------------------

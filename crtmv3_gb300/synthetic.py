@@ -360,7 +360,52 @@ SENSORS = {
     "irsynth_c2211": (1, 2211, co.INFRARED_SENSOR, 12),
     "mwsynth_c16": (3, 16, co.MICROWAVE_SENSOR, 13),
     "irsynth_c616": (1, 616, co.INFRARED_SENSOR, 14),
+    "irsynth_o120": (1, 120, co.INFRARED_SENSOR, 15),   # with a compact-OPTRAN water-vapour-line term
 }
+OPTRAN_SENSORS = ("irsynth_o120",)
+
+
+def generate_optran(tc: co.ODPSCoeff, seed: int, fraction: float = 0.6) -> co.OPTRANCoeff:
+    """A synthetic compact-OPTRAN term (ODPS_Define.f90:186-203) for the water
+    vapour line component (component 2) of ``fraction`` of the channels that
+    have one: 2-6 predictors among T, P, P^(1/4), the water vapour amount, its
+    ratio to T^2 and the integrated T* and P*, and polynomials of order 2-5 in
+    the transformed integrated water vapour Ap = ln((A - C2) / C1) / Alpha,
+    scaled so that ln(chi) stays near -4 +- 1 over the workload's profiles."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    L = tc.n_channels
+    nu = co.N_PREDICTOR_USED_OPTRAN + 1
+    sig = np.zeros(L, np.int32)
+    order = np.zeros(L, np.int32)
+    opi = np.zeros((nu, L), np.int32)
+    opos = np.zeros(L, np.int32)
+    # typical magnitudes of OX 1-14 (T, P, T^2, P^2, TP, T^2P, TP^2, T^2P^2, P^1/4, V, V/T^2, T*, P*, sec)
+    typ = np.array([250.0, 500.0, 6.0e4, 3.0e5, 1.2e5, 3.0e7, 6.0e7, 1.5e10, 4.0, 3.0, 5.0e-5, 500.0, 800.0, 1.3])
+    pool = np.array([1, 2, 9, 10, 11, 12, 13])
+    blocks = []
+    cursor = 1
+    for l in range(L):
+        if tc.n_predictors[1, l] <= 0 or rng.uniform() >= fraction:
+            continue
+        npred = int(rng.integers(2, co.N_PREDICTOR_USED_OPTRAN + 1))
+        preds = np.sort(rng.choice(pool, size=min(npred, pool.size), replace=False))
+        npred = preds.size
+        n_ord = int(rng.integers(2, 6))
+        c = np.zeros((npred + 1, n_ord + 1))
+        c[0, 0] = rng.uniform(-4.5, -3.5)
+        c[0, 1:] = rng.normal(0.0, 0.3, n_ord) / 3.0 ** np.arange(1, n_ord + 1)
+        for i, ii in enumerate(preds, start=1):
+            c[i, 0] = rng.normal(0.0, 0.4) / typ[ii - 1]
+            c[i, 1:] = rng.normal(0.0, 0.1, n_ord) / (typ[ii - 1] * 3.0 ** np.arange(1, n_ord + 1))
+        sig[l] = co.SIGNIFICANCE_OPTRAN
+        order[l] = n_ord
+        opi[0, l] = npred
+        opi[1:npred + 1, l] = preds
+        opos[l] = cursor
+        cursor += c.size
+        blocks.append(c.ravel())
+    oc = np.concatenate(blocks) if blocks else np.zeros(0)
+    return co.OPTRANCoeff(sig, order, opi, opos, oc, 2.0, 1.0, -1.0e-4, 2)
 
 
 def write_sensor_files(coeff_dir: str, sensor_id: str) -> None:
@@ -373,6 +418,8 @@ def write_sensor_files(coeff_dir: str, sensor_id: str) -> None:
     group, L, stype, seed = SENSORS[sensor_id]
     budget = 20 if sensor_id == "mwsynth_c22" else None
     tc = generate_odps(group, L, seed, sensor_id, stype, max_predictors_per_channel=budget)
+    if sensor_id in OPTRAN_SENSORS:
+        tc.optran = generate_optran(tc, seed + 50)
     sc = generate_spccoeff(sensor_id, stype, L, seed + 100)
     co.write_odps(tau + ".tmp", tc)
     co.write_spccoeff(spc + ".tmp", sc)

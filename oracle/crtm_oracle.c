@@ -56,6 +56,11 @@ struct or_handle_s {
   int* pos;    /* [L][J], 1-based */
   float* c;
   double *wn, *c1, *c2, *b1, *b2, *cbr, *solar, *freq;
+  /* compact-OPTRAN term (oracle_optran.inc); n_oc = 0: none */
+  int n_oc, ocomp;
+  int* osig, *oorder, *opidx, *opos;
+  double* oc;
+  double alpha, alpha_c1, alpha_c2;
 };
 
 /* ---------------- Fortran sequential record reader ------------------------ */
@@ -140,6 +145,8 @@ static int open_records(recrd* r, const unsigned char* buf, size_t n) {
 }
 
 /* Read_ODPS_Binary record order (ODPS_Binary_IO.f90:586-900). */
+static int load_optran(or_handle* h, recrd* r, int n_oc);
+
 static int load_taucoeff(or_handle* h, const char* path) {
   size_t n;
   unsigned char* buf = slurp(path, &n);
@@ -160,7 +167,6 @@ static int load_taucoeff(or_handle* h, const char* path) {
   if (h->K < 1 || h->K > MAXK || h->J > MAXJ || h->Jm > MAXJM || h->L < 1) {
     set_err("TauCoeff: dimensions out of range"); goto done;
   }
-  if (dims[6] > 0) { set_err("TauCoeff: OPTRAN coefficients not supported"); goto done; }
   if (next_record(&r, &d, &len) || len != 4) goto bad;
   h->group = (int)rd32(d, r.swap);
   if (h->group < 1 || h->group > 3 || N_COMPONENTS_G[h->group] != h->J ||
@@ -198,6 +204,7 @@ static int load_taucoeff(or_handle* h, const char* path) {
         set_err("TauCoeff: Pos_Index out of range"); goto done;
       }
     }
+  if (dims[6] > 0 && load_optran(h, &r, dims[6])) goto done;
   ok = 0;
   goto done;
 bad:
@@ -300,7 +307,18 @@ typedef struct {
   double pdp[MAXK], tz_ref[MAXK], tzp_ref[MAXK], tz[MAXK], tzp[MAXK];
   double gazp_ref[MAXJM][MAXK], gatzp_ref[MAXJM][MAXK], gazp[MAXJM][MAXK], gatzp[MAXJM][MAXK];
   double X[MAXK][MAXJ][MAXI];
+  /* OPTRAN predictors (index 1-14 as the reference's OX(k, 1:14)), powers of
+   * the transformed integrated water vapour, layer water vapour amounts and
+   * the integrated sums the adjoint reads */
+  double OX[MAXK][15], oAp[MAXK][11], odA[MAXK], oiv[MAXK], oave[MAXK], oinv[MAXK], ost[MAXK], osp[MAXK];
 } pstate;
+
+#include "oracle_optran.inc"
+
+/* adjoints of the OPTRAN predictors, accumulated over channels like X_AD */
+typedef struct {
+  double ox[MAXK][OPT_NX + 1], ap[MAXK][OPT_ORDER + 1], da[MAXK];
+} optran_adj;
 
 /* LayerAvg (ODPS_CoordinateMapping.f90:1108-1320): weights of the user layers
  * (ln p at px2, n2 of them) for each reference layer (ln p at px1, n1). */
@@ -572,13 +590,14 @@ static void compute_predictors(const or_handle* h, pstate* s) {
       np_[11] = ch4_a * gch4; np_[12] = co_a; np_[13] = co_a * sec * gco;
     }
   }
+  if (h->n_oc > 0) optran_predictors(h, s);   /* ODPS_Predictor.f90:336-347 */
 }
 
 /* Adjoint of compute_predictors: X_AD -> T_AD, A_AD on reference layers.
  * Exact reverse of the forward above; the reference's ODPS_Compute_Predictor_AD
  * (ODPS_Predictor.f90:1783-2643) is likewise the exact adjoint. */
 static void compute_predictors_ad(const or_handle* h, const pstate* s, double (*XA)[MAXJ][MAXI],
-                                  double* T_ad, double (*A_ad)[MAXK]) {
+                                  double* T_ad, double (*A_ad)[MAXK], optran_adj* oa) {
   const int K = h->K, Jm = h->Jm, G = h->group;
   double tz_ad[MAXK], tzp_ad[MAXK], gazp_ad[MAXJM][MAXK], gatzp_ad[MAXJM][MAXK];
   memset(tz_ad, 0, sizeof tz_ad); memset(tzp_ad, 0, sizeof tzp_ad);
@@ -731,6 +750,7 @@ static void compute_predictors_ad(const or_handle* h, const pstate* s, double (*
     tz_sum += tz_ad[k] / s->tz_ref[k];
     T_ad[k] += tz_sum + s->pdp[k] * tzp_sum;
   }
+  if (h->n_oc > 0) optran_predictors_ad(h, s, oa->ox, oa->ap, oa->da, T_ad, A_ad[0]);
 }
 
 /* ODPS_Compute_AtmAbsorption (ODPS_AtmAbsorption.f90:133-256): user-layer
@@ -742,6 +762,10 @@ static void atm_absorption(const or_handle* h, const pstate* s, int l, double* o
   for (int j = 0; j < h->J; j++) {
     int np = h->n_pred[l * h->J + j];
     if (np <= 0) continue;
+    if (j == h->ocomp - 1 && optran_channel(h, l)) {   /* ODPS_AtmAbsorption.f90:184-195 */
+      optran_od(h, s, l, od_ref);
+      continue;
+    }
     int j0 = h->pos[l * h->J + j] - 1;
     for (int i = 0; i < np; i++) {
       const float* c = h->c + j0 + (size_t)i * K;
@@ -770,7 +794,7 @@ static void atm_absorption(const or_handle* h, const pstate* s, int l, double* o
 
 /* ODPS_Compute_AtmAbsorption_AD (ODPS_AtmAbsorption.f90:487-600): adds C*OD_AD to X_AD. */
 static void atm_absorption_ad(const or_handle* h, const pstate* s, int l, const double* od_ref,
-                              const double* layer_od_ad, double (*XA)[MAXJ][MAXI]) {
+                              const double* layer_od_ad, double (*XA)[MAXJ][MAXI], optran_adj* oa) {
   const int K = h->K, Ku = s->Ku;
   double up_ad[MAXK + 1], path_ad[MAXK + 1], od_ad[MAXK];
   up_ad[Ku] = 0.0;
@@ -798,6 +822,10 @@ static void atm_absorption_ad(const or_handle* h, const pstate* s, int l, const 
   for (int j = 0; j < h->J; j++) {
     int np = h->n_pred[l * h->J + j];
     if (np <= 0) continue;
+    if (j == h->ocomp - 1 && optran_channel(h, l)) {   /* ODPS_AtmAbsorption.f90:573-580 */
+      optran_od_ad(h, s, l, od_ad, oa->ox, oa->ap, oa->da);
+      continue;
+    }
     int j0 = h->pos[l * h->J + j] - 1;
     for (int i = 0; i < np; i++) {
       const float* c = h->c + j0 + (size_t)i * K;
@@ -930,10 +958,14 @@ static void profile_solution(const or_handle* h, const or_batch* b, int m, const
   const double* tu = b->temperature + (size_t)m * Kmax;
   double od_ref[MAXK], lod_k[MAXK], B[MAXK], tod_ad[MAXK], B_ad[MAXK];
   double (*XA)[MAXJ][MAXI] = NULL;
+  optran_adj* oa = NULL;
   double T_ad[MAXK], A_ad[MAXJM][MAXK];
   rtv r;
   int want_ad = (tk != NULL) || adjoint_mode;
-  if (want_ad) XA = (double (*)[MAXJ][MAXI])calloc(MAXK, sizeof *XA);
+  if (want_ad) {
+    XA = (double (*)[MAXJ][MAXI])calloc(MAXK, sizeof *XA);
+    oa = (optran_adj*)calloc(1, sizeof *oa);
+  }
   for (int l = 0; l < L; l++) {
     atm_absorption(h, s, l, od_ref, lod_k);
     for (int k = 0; k < Ku; k++) B[k] = planck_radiance(h, l, tu[k]);
@@ -950,8 +982,11 @@ static void profile_solution(const or_handle* h, const or_batch* b, int m, const
     double r_ad = planck_temperature_dR(h, l, R) * seed_v;
     double Bs_ad, e_ad, refl_ad;
     emission_ad(Ku, u, B, Bs, e, 1.0 - e, &r, r_ad, tod_ad, B_ad, &Bs_ad, &e_ad, &refl_ad);
-    if (!adjoint_mode) memset(XA, 0, sizeof(double) * MAXK * MAXJ * MAXI);
-    atm_absorption_ad(h, s, l, od_ref, tod_ad, XA);
+    if (!adjoint_mode) {
+      memset(XA, 0, sizeof(double) * MAXK * MAXJ * MAXI);
+      memset(oa, 0, sizeof *oa);
+    }
+    atm_absorption_ad(h, s, l, od_ref, tod_ad, XA, oa);
     double* tko = adjoint_mode ? tad + (size_t)m * Kmax : tk + ml * Kmax;
     for (int k = 0; k < Ku; k++) tko[k] += planck_radiance_dT(h, l, tu[k]) * B_ad[k];
     double st_ad = planck_radiance_dT(h, l, ts) * Bs_ad;
@@ -962,7 +997,7 @@ static void profile_solution(const or_handle* h, const or_batch* b, int m, const
       ek[ml] = e_ad - refl_ad;
       memset(T_ad, 0, sizeof T_ad);
       memset(A_ad, 0, sizeof A_ad);
-      compute_predictors_ad(h, s, XA, T_ad, A_ad);
+      compute_predictors_ad(h, s, XA, T_ad, A_ad, oa);
       map_input_ad(h, b, s, T_ad, A_ad, tko, ak + ml * Jab * Kmax);
     }
   }
@@ -970,10 +1005,11 @@ static void profile_solution(const or_handle* h, const or_batch* b, int m, const
     /* CRTM_Adjoint_Module.f90:1396: predictor adjoint once, after the channel loop */
     memset(T_ad, 0, sizeof T_ad);
     memset(A_ad, 0, sizeof A_ad);
-    compute_predictors_ad(h, s, XA, T_ad, A_ad);
+    compute_predictors_ad(h, s, XA, T_ad, A_ad, oa);
     map_input_ad(h, b, s, T_ad, A_ad, tad + (size_t)m * Kmax, aad + (size_t)m * Jab * Kmax);
   }
   free(XA);
+  free(oa);
   free(s);
 }
 

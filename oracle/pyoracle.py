@@ -51,7 +51,7 @@ class OrClouds(ct.Structure):
 
 def build(force: bool = False) -> str:
     srcs = [os.path.join(HERE, f) for f in ("crtm_oracle.c", "crtm_oracle.h", "oracle_scatter.inc",
-                                             "oracle_scatter_k.inc")]
+                                             "oracle_scatter_k.inc", "oracle_optran.inc")]
     if force or not os.path.exists(LIB) or any(os.path.getmtime(LIB) < os.path.getmtime(f) for f in srcs):
         subprocess.run(["make", "-C", HERE, "-B", "liboracle.so"], check=True,
                        stdout=subprocess.DEVNULL)

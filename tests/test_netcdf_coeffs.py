@@ -1,7 +1,7 @@
 """netCDF-classic SpcCoeff / ODPS TauCoeff files (crtmv3_gb300/netcdf_coeffs.py):
 the reference's variable names, types and dimension order
 (SpcCoeff_netCDF_IO.f90:68-183, ODPS_netCDF_IO.f90:63-240), lossless round
-trips through the binary formats, the OPTRAN refusal, and CRTM_Init's
+trips through the binary formats, the OPTRAN variables, and CRTM_Init's
 SpcCoeff_Format / TauCoeff_Format options.  Exact comparisons throughout."""
 import filecmp
 import os
@@ -19,6 +19,8 @@ def _fields_equal(a, b):
         if isinstance(x, np.ndarray) or isinstance(y, np.ndarray):
             np.testing.assert_array_equal(np.asarray(x), np.asarray(y), err_msg=f)
             assert np.asarray(x).dtype == np.asarray(y).dtype, f
+        elif hasattr(x, "__dataclass_fields__") and hasattr(y, "__dataclass_fields__"):
+            _fields_equal(x, y)
         else:
             assert x == y, f
 
@@ -68,14 +70,29 @@ def test_reference_layout(coeff_dir, tmp_path):
         assert f.variables["Sensor_Type"].dimensions == ()
 
 
-def test_optran_files_are_refused(coeff_dir, tmp_path):
-    tc = co.read_odps(os.path.join(coeff_dir, "mwsynth_c22.TauCoeff.bin"))
+def test_optran_variables_round_trip(coeff_dir, tmp_path):
+    """A TauCoeff with the compact-OPTRAN term through netCDF and back to a
+    byte-identical binary file; a file whose n_OCoeffs dimension lacks the
+    OPTRAN variables is refused."""
+    sensor = "irsynth_o120"
+    src = os.path.join(coeff_dir, f"{sensor}.TauCoeff.bin")
+    tc = co.read_odps(src)
+    assert tc.optran is not None
     p = str(tmp_path / "o.nc")
     nc.write_odps_nc(p, tc)
-    with netcdf_file(p, "a") as f:
+    with netcdf_file(p, "r", mmap=False) as f:
+        assert f.variables["OP_Index"].dimensions == ("n_Channels", "n_OPIndex")
+        assert f.dimensions["n_OPIndex"] == 7 and f.dimensions["n_OCoeffs"] == tc.optran.oc.size
+    back = str(tmp_path / "o.bin")
+    co.write_odps(back, nc.read_odps_nc(p))
+    with open(back, "rb") as a, open(src, "rb") as b:
+        assert a.read() == b.read()
+    bad = str(tmp_path / "b.nc")
+    nc.write_odps_nc(bad, co.read_odps(os.path.join(coeff_dir, "mwsynth_c22.TauCoeff.bin")))
+    with netcdf_file(bad, "a") as f:
         f.createDimension("n_OCoeffs", 4)
     with pytest.raises(ValueError, match="OPTRAN"):
-        nc.read_odps_nc(p)
+        nc.read_odps_nc(bad)
 
 
 def test_crtm_init_formats(coeff_dir, tmp_path, monkeypatch):
