@@ -70,7 +70,7 @@ def test_clear_sky_components_match_oracle(gpu_lib, cloud_dir, precision, sensor
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("sensor", ["mwsynth_c16", "irsynth_c616"])
 def test_cloudy_components_match_oracle(gpu_lib, cloud_dir, precision, sensor):
-    """Profiles: 0 clear, 1 cloudy (fraction 1), 2 fractional, 3 fractional
+    """Profiles: 0 clear, 1 cloudy (fraction 1: fractional, cover 1), 2 fractional, 3 fractional
     with 16 streams, 4 aerosols only (IR), 5 fractional with 8 streams, 6 SOI
     (FP64 form), 7 cloudy with fractions of 1e-9 (kept, as above 1e-12, but
     not fractional, as below 1e-6)."""
@@ -95,8 +95,9 @@ def test_cloudy_components_match_oracle(gpu_lib, cloud_dir, precision, sensor):
         opt.rt_algorithm_id = np.array([56, 56, 56, 56, 56, 56, 168, 56], np.int32)
     aer = f"{cloud_dir}/AerosolCoeff.bin" if ir else None
     ref = Oracle(cloud_dir, sensor).forward_components(atm, sfc, geo, opt, f"{cloud_dir}/CloudCoeff.bin", aer)
-    assert (ref["total_cloud_cover"][[2, 3, 5]] > 0).all() and (ref["sod"][1] > 0).any()
-    assert not ref["total_cloud_cover"][[0, 1, 7]].any()
+    # cloud fraction 1 is above 1e-6: a fractional profile with cover 1
+    assert (ref["total_cloud_cover"][[2, 3, 5]] > 0).all() and (ref["total_cloud_cover"][1] == 1.0).all()
+    assert (ref["sod"][1] > 0).any() and not ref["total_cloud_cover"][[0, 7]].any()
     h = gpu_lib.CRTM([sensor], cloud_dir, precision)
     rts = h.forward(atm, sfc, geo, opt, components=True)
     _compare(rts, ref, precision)
