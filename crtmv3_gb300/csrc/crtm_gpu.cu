@@ -771,6 +771,8 @@ struct Work {
   R* TODc;          // scattering K-matrix/adjoint: [n][Kmax][L] cloudy dR/dtau
   double* CB;       // scattering K-matrix/adjoint: [n][4][L] cloudy radiance, surface terms, clear radiance
   R* LBA;           // scattering K-matrix/adjoint: [n][Kmax][NE][L] layer record adjoints
+  long long* rev_list;   // mixed-form scattering K-matrix/adjoint: [n][Kmax][L] layers for the FP64 pass
+  int* rev_count;
   double* CJ, *CR;  // species Jacobians: [n][slots][Kmax][L]
   double* CF;       // cloud-fraction Jacobian: [n][Kmax][L]
   double* CV;       // aerosol effective-variance Jacobians ('CMAQ'): [n][slots][Kmax][L]
@@ -855,6 +857,10 @@ size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w
     wk.TODc = sw.kstate ? (R*)carve(nn * Kmax * L * sizeof(R)) : nullptr;
     wk.CB = sw.kstate ? (double*)carve(nn * 4 * L * sizeof(double)) : nullptr;
     wk.LBA = sw.kstate ? (R*)carve(nn * Kmax * (size_t)sw.rec * L * sizeof(R)) : nullptr;
+    if (sw.kstate && std::is_same<R, float>::value) {
+      wk.rev_list = (long long*)carve(nn * Kmax * L * sizeof(long long));
+      wk.rev_count = (int*)carve(sizeof(int));
+    }
     const size_t sj = nn * (size_t)sw.slots * Kmax * L * sizeof(double);
     wk.CJ = sw.slots ? (double*)carve(sj) : nullptr;
     wk.CR = sw.slots ? (double*)carve(sj) : nullptr;
@@ -1189,6 +1195,7 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       sa.x = make_ext(rts);
       sa.TODc = w.TODc; sa.PT = w.PT; sa.CB = w.CB; sa.AS = w.AS; sa.LBA = w.LBA;
       sa.n_slots = sw.slots; sa.CJ = w.CJ; sa.CR = w.CR; sa.CF = w.CF; sa.TD = w.TD; sa.SC = w.SC;
+      sa.rev_list = w.rev_list; sa.rev_count = w.rev_count;
       const long long nlay = (long long)n * Kmax * L;
       const unsigned gl = (unsigned)((nlay + SCATTER_THREADS - 1) / SCATTER_THREADS);
       dim3 ga((L + SCATTER_THREADS - 1) / SCATTER_THREADS, n);
