@@ -200,7 +200,8 @@ def run_reference(args):
     """The reference's CPU path (the FP64 oracle, a restatement of it: the
     Fortran reference cannot be built here) on the host cores: each step is
     a bounded sample of the workload (C2: args.cpu_profiles profiles; C3-C5:
-    the first args.cpu_profiles profiles of each sensor group)."""
+    args.cpu_profiles profiles of each sensor group with the group's mix of
+    clear and cloudy profiles and stream options)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
@@ -241,8 +242,9 @@ def run_reference(args):
                "groups": [{"sensor": g[0], "profiles": int(g[1].n_profiles)} for g in groups],
                "parallelism": "replicas x1", "sample_profiles_per_group_per_step": args.cpu_profiles}
         metric = SCATTER_METRIC[args.workload]
-        sample = (f"the first {args.cpu_profiles} profiles of each sensor group per step (the workload's mix of "
-                  f"clear and cloudy profiles and stream options), K-matrix with the GPU arm's Jacobians "
+        sample = (f"{args.cpu_profiles} profiles of each sensor group per step whose mix of clear, stream-rule, "
+                  f"8- and 16-stream cloudy profiles is the group's (the throughput of the sample stands for the "
+                  f"whole workload's), K-matrix with the GPU arm's Jacobians "
                   f"(FP64 C oracle: clear-sky chain and the reverse mode of the ADA path, OpenMP over profiles)")
     value = statistics.median(v for v, _ in vals)
     ms = statistics.median(dt for _, dt in vals) * 1e3
@@ -342,12 +344,35 @@ def scatter_device_inputs(torch, h, atm, sfc, geo, opt, dev):
     return b, keep, t
 
 
+def stratified_indices(atm, opt, n: int) -> np.ndarray:
+    """n profile indices of a group whose mix of strata -- clear, cloudy on the
+    stream rule, cloudy with Options%n_Streams 8, with 16 -- matches the
+    group's (largest-remainder quotas; the first profiles of each stratum), so
+    a throughput measured on the sample stands for the whole group's."""
+    P = atm.n_profiles
+    n = min(n, P)
+    cloudy = np.zeros(P, bool)
+    if atm.n_clouds is not None:
+        cloudy |= atm.n_clouds > 0
+    if atm.n_aerosols is not None:
+        cloudy |= atm.n_aerosols > 0
+    ns = opt.n_streams if opt.n_streams is not None and opt.use_n_streams is not None else np.zeros(P, np.int32)
+    ns = np.where(opt.use_n_streams, ns, 0) if opt.use_n_streams is not None else ns
+    key = np.where(~cloudy, 0, np.where(ns == 8, 2, np.where(ns == 16, 3, 1)))
+    counts = np.bincount(key, minlength=4)
+    exact = counts * n / P
+    q = np.floor(exact).astype(int)
+    for s_ in np.argsort(-(exact - q))[: n - q.sum()]:
+        q[s_] += 1
+    return np.sort(np.concatenate([np.nonzero(key == s_)[0][:q[s_]] for s_ in range(4)]))
+
+
 def sample_groups(groups, n: int):
-    """The first n profiles of each group: the workload's own mix of clear and
-    cloudy profiles and stream options."""
+    """n profiles of each group with the group's own mix of clear and cloudy
+    profiles and stream options (stratified_indices)."""
     out = []
     for sid, atm, sfc, geo, opt in groups:
-        w = slice(0, min(n, atm.n_profiles))
+        w = stratified_indices(atm, opt, n)
         out.append((sid, atm.subset(w), sfc.subset(w), geo.subset(w), opt.subset(w)))
     return out
 
@@ -551,9 +576,10 @@ def run_scattering(args, torch, dev, rank, world, dist):
         return max_over_ranks(e0.elapsed_time(e1), dist, dev)
 
     n_cmp = args.cpu_profiles
+    samp_idx = [torch.from_numpy(stratified_indices(g[1], g[4], n_cmp)).to(dev) for g in groups]
 
     def sample_out():
-        return [{f: v[:n_cmp].cpu().numpy() for f, v in c["out"].items()} for c in calls]
+        return [{f: v[ix].cpu().numpy() for f, v in c["out"].items()} for c, ix in zip(calls, samp_idx)]
     # the FP64 form's outputs: the mixed form's accuracy against it on the first
     # 512 profiles of each group, and both forms against the oracle on the sample
     step(0)
@@ -680,15 +706,15 @@ def run_scattering(args, torch, dev, rank, world, dist):
                "ms_per_step": dt * 1e3, "sample": f"first 1/{frac} of each group's profiles per step"}
         del outs
     # CPU baseline (the FP64 oracle on the host cores) and both GPU forms
-    # against the oracle, on the first n_cmp profiles of each group
+    # against the oracle, on n_cmp profiles of each group (stratified_indices)
     cpu, vs_oracle = None, None
     if rank == 0 and not args.no_cpu and name != "C3":
         threads = os.cpu_count() or 1
         samp = sample_groups(groups, n_cmp)
         ref_o, cpc, ct = oracle_scatter_k(samp, threads)
         cpu = {"value": cpc / ct, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"the first {n_cmp} profiles of each sensor group ({cpc} profile*channels, the "
-                         f"workload's mix of clear and cloudy profiles and stream options), K-matrix with the same "
+               "sample": f"{n_cmp} profiles of each sensor group ({cpc} profile*channels) whose mix of clear, "
+                         f"stream-rule, 8- and 16-stream cloudy profiles is the group's, K-matrix with the same "
                          f"Jacobians as the GPU arm, FP64 C oracle with OpenMP over profiles, {ct:.1f} s"}
         vs_oracle = {"fp64": {}, "mixed": {}, "profiles_per_group": n_cmp}
         for (sid, a, *_), r, g64, gmx in zip(samp, ref_o, fp64_sample, mixed_sample):
@@ -731,7 +757,7 @@ def main():
     ap.add_argument("--profiles", type=int, default=2000)
     ap.add_argument("--cpu-profiles", type=int, default=0,
                     help="CPU-baseline / oracle sample: profiles (C2, default 256) or profiles per sensor "
-                         "group (C3-C5, default 16)")
+                         "group (C3-C5, default 32)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="C5", choices=["C2", "C3", "C4", "C5"],
@@ -743,7 +769,7 @@ def main():
                          "per map CTA, no pass cap)")
     args = ap.parse_args()
     if not args.cpu_profiles:
-        args.cpu_profiles = 256 if args.workload == "C2" else 16
+        args.cpu_profiles = 256 if args.workload == "C2" else 32
     if args.impl == "reference":
         return run_reference(args)
 

@@ -166,6 +166,9 @@ struct Sensor {
   int* d_och = nullptr;
   double* d_ocoef = nullptr;
   OptranView ov{};
+  // the cloud tables interpolated to the processed channels' frequencies
+  // (CloudChan layout; built when the handle has a CloudCoeff table)
+  double* d_zc = nullptr;
 };
 
 // The OPTRAN tables of the processed channels (file positions `pos`; all
@@ -470,9 +473,48 @@ bool upload_channels(Sensor& s, const std::vector<int>& pos, std::string& err) {
 
 void free_sensor(Sensor& s) {
   cudaFree(s.d_C); cudaFree(s.d_cmask); cudaFree(s.d_tab); cudaFree(s.d_spec);
-  cudaFree(s.d_oidx); cudaFree(s.d_och); cudaFree(s.d_ocoef);
+  cudaFree(s.d_oidx); cudaFree(s.d_och); cudaFree(s.d_ocoef); cudaFree(s.d_zc);
   s.d_C = nullptr; s.d_cmask = nullptr; s.d_tab = nullptr; s.d_spec = nullptr;
-  s.d_oidx = nullptr; s.d_och = nullptr; s.d_ocoef = nullptr;
+  s.d_oidx = nullptr; s.d_och = nullptr; s.d_ocoef = nullptr; s.d_zc = nullptr;
+}
+
+// The cloud tables at each processed channel's frequency (CloudChan layout):
+// one thread per (plane, radius row, channel), the frequency step of the
+// lookups' 4-point Lagrange interpolation.
+__global__ void cloud_chan_kernel(CloudLut C, int microwave, const double* freq, int L, long long n, double* z) {
+  const int rows = microwave ? C.nrm : C.nri, nf = microwave ? C.nfm : C.nfi;
+  const double* fax = microwave ? C.f_mw : C.f_ir;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int ch = (int)(i % L);
+    const long long qr = i / L;
+    const int r = (int)(qr % rows), q = (int)(qr / rows);
+    const Lagrange4 U = lagrange4(fax, nf, freq[ch]);
+    z[i] = lerp4(cloud_chan_source(C, microwave != 0, q) + (size_t)r * nf + U.i0, 1, U);
+  }
+}
+
+// (Re)build a sensor's channel-interpolated cloud tables for its processed
+// channels; none without a cloud table or channels.
+bool build_cloud_chan(const CloudLut& C, bool has_clouds, Sensor& s, std::string& err) {
+  cudaFree(s.d_zc);
+  s.d_zc = nullptr;
+  if (!has_clouds || s.L <= 0) return true;
+  const bool mw = s.sensor_type == 1;
+  const long long n = (long long)cloud_chan_planes(C, mw) * (mw ? C.nrm : C.nri) * s.L;
+  cudaError_t ce = cudaMalloc(&s.d_zc, (size_t)n * sizeof(double));
+  if (ce == cudaSuccess) {
+    const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
+    cloud_chan_kernel<<<(unsigned)blocks, 256>>>(C, mw ? 1 : 0, mw ? s.spec.freq : s.spec.wn, s.L, n, s.d_zc);
+    ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
+  }
+  if (ce != cudaSuccess) {
+    cudaFree(s.d_zc);
+    s.d_zc = nullptr;
+    err = std::string("channel cloud tables: ") + cudaGetErrorString(ce);
+    return false;
+  }
+  return true;
 }
 
 // CloudCoeff.bin (CloudCoeff_Binary_IO.f90:360-460): Release/Version, 8
@@ -771,8 +813,6 @@ struct Work {
   R* TODc;          // scattering K-matrix/adjoint: [n][Kmax][L] cloudy dR/dtau
   double* CB;       // scattering K-matrix/adjoint: [n][4][L] cloudy radiance, surface terms, clear radiance
   R* LBA;           // scattering K-matrix/adjoint: [n][Kmax][NE][L] layer record adjoints
-  long long* rev_list;   // mixed-form scattering K-matrix/adjoint: [n][Kmax][L] layers for the FP64 pass
-  int* rev_count;
   double* CJ, *CR;  // species Jacobians: [n][slots][Kmax][L]
   double* CF;       // cloud-fraction Jacobian: [n][Kmax][L]
   double* CV;       // aerosol effective-variance Jacobians ('CMAQ'): [n][slots][Kmax][L]
@@ -857,10 +897,6 @@ size_t work_bytes(const Sensor& s, int n, int Kmax, int nv, int mode, Work<R>* w
     wk.TODc = sw.kstate ? (R*)carve(nn * Kmax * L * sizeof(R)) : nullptr;
     wk.CB = sw.kstate ? (double*)carve(nn * 4 * L * sizeof(double)) : nullptr;
     wk.LBA = sw.kstate ? (R*)carve(nn * Kmax * (size_t)sw.rec * L * sizeof(R)) : nullptr;
-    if (sw.kstate && std::is_same<R, float>::value) {
-      wk.rev_list = (long long*)carve(nn * Kmax * L * sizeof(long long));
-      wk.rev_count = (int*)carve(sizeof(int));
-    }
     const size_t sj = nn * (size_t)sw.slots * Kmax * L * sizeof(double);
     wk.CJ = sw.slots ? (double*)carve(sj) : nullptr;
     wk.CR = sw.slots ? (double*)carve(sj) : nullptr;
@@ -1176,7 +1212,7 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       ScatterArgs<R> sa{};
       sa.K = K; sa.L = L; sa.Kmax = Kmax; sa.p_begin = p0; sa.n_chunk = n;
       sa.microwave = s.sensor_type == 1;
-      sa.b = bv; sa.sp = s.spec; sa.pv = w.pv; sa.lut = h->lut;
+      sa.b = bv; sa.sp = s.spec; sa.pv = w.pv; sa.lut = h->lut; sa.lut_chan = s.d_zc;
       sa.max_clouds = b->max_clouds; sa.n_clouds = b->n_clouds; sa.cloud_type = b->cloud_type;
       sa.wc = b->cloud_water_content; sa.reff = b->cloud_effective_radius; sa.n_streams = b->n_streams;
       sa.rt_algorithm = b->rt_algorithm_id; sa.FB = w.FB; sa.FS = w.FS; sa.soi_slots = sw.soi_slots;
@@ -1195,7 +1231,6 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       sa.x = make_ext(rts);
       sa.TODc = w.TODc; sa.PT = w.PT; sa.CB = w.CB; sa.AS = w.AS; sa.LBA = w.LBA;
       sa.n_slots = sw.slots; sa.CJ = w.CJ; sa.CR = w.CR; sa.CF = w.CF; sa.TD = w.TD; sa.SC = w.SC;
-      sa.rev_list = w.rev_list; sa.rev_count = w.rev_count;
       const long long nlay = (long long)n * Kmax * L;
       const unsigned gl = (unsigned)((nlay + SCATTER_THREADS - 1) / SCATTER_THREADS);
       dim3 ga((L + SCATTER_THREADS - 1) / SCATTER_THREADS, n);
@@ -2063,6 +2098,12 @@ int crtm_gpu_init_aerosol(const char* coeff_path, int n_sensors, const char* con
       L.ke_s = b0 + off[8]; L.w_s = b0 + off[9]; L.pc_s = b0 + off[10];
       L.ke_ir = b0 + off[11]; L.w_ir = b0 + off[12]; L.pc_ir = b0 + off[13];
       h->has_clouds = true;
+      for (auto& s : h->sensors)
+        if (!build_cloud_chan(h->lut, true, s, err)) {
+          g_init_error = err;
+          crtm_gpu_destroy(h);
+          return CRTM_GPU_FAILURE;
+        }
     }
     const std::string apath =
         std::string(coeff_path) + "/" + (aerosol_coeff_file ? aerosol_coeff_file : "AerosolCoeff.bin");
@@ -2192,9 +2233,11 @@ int crtm_gpu_set_channel_subset(crtm_gpu_handle h, int sensor, int n, const int*
   if (!pos.empty() && pos[0] == -1) {
     s.L = 0;
     s.processed = pos;
+    build_cloud_chan(h->lut, false, s, err);
     return CRTM_GPU_SUCCESS;
   }
   if (!upload_channels(s, pos, err)) return fail(h, "%s", err.c_str());
+  if (!build_cloud_chan(h->lut, h->has_clouds, s, err)) return fail(h, "%s", err.c_str());
   return CRTM_GPU_SUCCESS;
 }
 

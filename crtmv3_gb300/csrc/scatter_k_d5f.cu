@@ -26,10 +26,7 @@ void launch_scatter_kmatrix(const ScatterArgs<R>& a, dim3 grid, cudaStream_t st,
 
 template <int NZ, class R, class C>
 void launch_scatter_reverse(const ScatterArgs<R>& a, unsigned grid, cudaStream_t st) {
-  // FP32 sweep, then its FP64 layers (grid-stride over the list)
-  cudaMemsetAsync(a.rev_count, 0, sizeof(int), st);
   scatter_reverse_kernel<NZ, R, C><<<grid, SCATTER_THREADS, 0, st>>>(a);
-  scatter_reverse64_kernel<NZ, R><<<152 * 4, SCATTER_THREADS, 0, st>>>(a);
 }
 
 template void launch_scatter_layers_k<5, float, float>(const ScatterArgs<float>&, unsigned, cudaStream_t);

@@ -65,6 +65,7 @@ struct ScatterArgs {
   SpecView sp;
   PrepView<R> pv;
   CloudLut lut;
+  const double* lut_chan;   // the sensor's channel-interpolated cloud tables (CloudChan; null: none)
   int max_clouds;
   const int* n_clouds;          // [P]
   const int* cloud_type;        // [P][NC]
@@ -113,10 +114,6 @@ struct ScatterArgs {
   // solvers write the cloud cover, the clear column and the stream count
   // (the K-matrix kernels the stream count; the second column launch the rest)
   RtsExt x;
-  // mixed form: the layers the FP32 reverse sweep hands to FP64 (their
-  // (profile, layer, channel) index), and their count
-  long long* rev_list;
-  int* rev_count;
 };
 
 constexpr int SCATTER_THREADS = 128;
@@ -218,6 +215,9 @@ __device__ __forceinline__ CloudyColumn column_inputs(const ScatterArgs<R>& a, i
   c.rh = a.max_aerosols > 0 && a.rh ? a.rh + (size_t)gp * a.Kmax : nullptr;
   c.alut = &a.alut;
   c.cf = a.cloud_fraction && c.n_clouds > 0 ? a.cloud_fraction + (size_t)gp * a.Kmax : nullptr;
+  c.zc.z = a.lut_chan;
+  c.zc.L = (size_t)a.L;
+  c.zc.ch = l;
   const double tcc = a.cover[p];
   c.wc_div = tcc > MIN_COVERAGE ? tcc : 1.0;
   return c;
@@ -649,16 +649,13 @@ __global__ void __launch_bounds__(SCATTER_THREADS) scatter_contract_kernel(Scatt
 // The same contraction for the ADA profiles (and the clear layers of any
 // profile not on SOI), one thread per (profile, layer, channel), by the
 // reverse sweep through the layer's optics (layer_adjoint): all of the
-// layer's inputs in one pass, in the arithmetic C.  reverse_layer is one
-// (profile, layer, channel), index idx.  An FP32 sweep that needs the layer in FP64 (nearly
-// conservative or nearly defective beyond the shifted angles, or a failed
-// factorisation) appends idx to rev_list and writes nothing: the FP64 pass
-// (scatter_reverse64_kernel) takes it, so no warp of the FP32 pass waits on an
-// FP64 lane and the FP32 kernel keeps the FP32 stack frame only.
+// layer's inputs in one pass, in the arithmetic C.
 template <int NZ, class R, class C>
-__device__ __forceinline__ void reverse_layer(const ScatterArgs<R>& a, long long idx) {
+__global__ void __launch_bounds__(SCATTER_THREADS) scatter_reverse_kernel(ScatterArgs<R> a) {
   constexpr int NE = layer_record<NZ>();
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int L = a.L, Kmax = a.Kmax;
+  if (idx >= (long long)a.n_chunk * Kmax * L) return;
   const int l = (int)(idx % L);
   const int k = (int)((idx / L) % Kmax);
   const int p = (int)(idx / ((long long)L * Kmax));
@@ -700,13 +697,8 @@ __device__ __forceinline__ void reverse_layer(const ScatterArgs<R>& a, long long
       src_b[i] = double(rb[(size_t)(2 + 2 * NZ * NZ + i) * L]);
     }
   double g[2], gs[2 * SC_NC_MAX][3];
-  bool in_fp64 = false;
-  const int kr = layer_adjoint_in<NZ, C>(c, a.lut, S, k, double(a.TAU[kl]), kind, T_b, R_b, src_b,
-                                         kind == 1 ? 0.0 : od_b, B_b, g, gs, &in_fp64);
-  if (in_fp64) {
-    a.rev_list[atomicAdd(a.rev_count, 1)] = idx;
-    return;
-  }
+  const int kr = layer_adjoint<NZ, C>(c, a.lut, S, k, double(a.TAU[kl]), kind, T_b, R_b, src_b,
+                                      kind == 1 ? 0.0 : od_b, B_b, g, gs);
   if (kr < 0) {
     atomicCAS(a.error, 0, -kr);
     if (a.status) atomicOr(a.status + gp, 1 << 4);
@@ -724,21 +716,6 @@ __device__ __forceinline__ void reverse_layer(const ScatterArgs<R>& a, long long
       if (a.CV && a.alut.scheme == AEROSOL_CMAQ && s >= c.n_clouds) jac(a.CV, slot(s)) = gs[s][2];
     }
   }
-}
-
-template <int NZ, class R, class C>
-__global__ void __launch_bounds__(SCATTER_THREADS) scatter_reverse_kernel(ScatterArgs<R> a) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)a.n_chunk * a.Kmax * a.L) return;
-  reverse_layer<NZ, R, C>(a, idx);
-}
-
-// The FP32 sweep's FP64 layers, grid-stride over rev_list.
-template <int NZ, class R>
-__global__ void __launch_bounds__(SCATTER_THREADS) scatter_reverse64_kernel(ScatterArgs<R> a) {
-  const int n = *a.rev_count;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    reverse_layer<NZ, R, double>(a, a.rev_list[i]);
 }
 
 // Species and cloud-fraction Jacobians of one (profile, channel), in place:

@@ -137,6 +137,54 @@ CRTM_HD S lerp4x4x4(const double* z, int nu, int nv, const Lagrange4& U, const L
   return lerp4(a, 1, W);
 }
 
+// The cloud tables of one sensor already interpolated to each channel's
+// frequency (the frequency step of lerp4x4 / lerp4x4x4 done once per channel
+// at init, cloud_chan_kernel): plane q of the tables at radius row r for
+// channel ch is z[(q * rows + r) * L + ch], channels fastest, rows = the
+// radius axis.  Planes (cloud_chan_plane):
+//   infrared:  ke, w of the nd + 1 density slots, then Legendre term t
+//              (t = 0..nleg-1, the file's pc index) of each slot;
+//   microwave: liquid ke, w of the nt temperatures and term t (0..nleg) of
+//              each temperature, then solid ke, w of the nd density slots and
+//              term t of each slot.
+// A null z: the lookups interpolate in frequency themselves.
+struct CloudChan {
+  const double* z = nullptr;
+  size_t L = 0;
+  int ch = 0;
+};
+
+CRTM_HD int cloud_chan_planes(const CloudLut& C, bool microwave) {
+  return microwave ? (2 + C.nleg + 1) * (C.nt + C.nd) : (2 + C.nleg) * (C.nd + 1);
+}
+
+// Plane index of table `tab` (0 ke, 1 w, 2 + t Legendre term t) of slot j
+// (temperature index of a liquid table, density slot otherwise).
+CRTM_HD int cloud_chan_plane(const CloudLut& C, bool microwave, bool solid, int tab, int j) {
+  if (!microwave) return tab * (C.nd + 1) + j;
+  return solid ? (2 + C.nleg + 1) * C.nt + tab * C.nd + j : tab * C.nt + j;
+}
+
+// The file table behind plane q (rows of nf frequencies, stride nf).
+CRTM_HD const double* cloud_chan_source(const CloudLut& C, bool microwave, int q) {
+  if (!microwave) {
+    const size_t plane = (size_t)C.nfi * C.nri, vol = plane * (C.nd + 1);
+    const int tab = q / (C.nd + 1), j = q % (C.nd + 1);
+    return tab == 0 ? C.ke_ir + j * plane : (tab == 1 ? C.w_ir + j * plane : C.pc_ir + (tab - 2) * vol + j * plane);
+  }
+  const size_t plane = (size_t)C.nfm * C.nrm;
+  const int nliq = (2 + C.nleg + 1) * C.nt;
+  if (q < nliq) {
+    const size_t vol = plane * C.nt;
+    const int tab = q / C.nt, j = q % C.nt;
+    return tab == 0 ? C.ke_l + j * plane : (tab == 1 ? C.w_l + j * plane : C.pc_l + (tab - 2) * vol + j * plane);
+  }
+  q -= nliq;
+  const size_t vol = plane * C.nd;
+  const int tab = q / C.nd, j = q % C.nd;
+  return tab == 0 ? C.ke_s + j * plane : (tab == 1 ? C.w_s + j * plane : C.pc_s + (tab - 2) * vol + j * plane);
+}
+
 // Legendre offset of the stream set (CloudCoeff_Define.f90:83-84).
 CRTM_HD int legendre_offset(int nleg) {
   return nleg == 2 || nleg == 4 ? 0 : (nleg == 6 ? 5 : (nleg == 8 ? 12 : (nleg == 16 ? 21 : -1)));
@@ -145,12 +193,60 @@ CRTM_HD int legendre_offset(int nleg) {
 // Optical properties of one cloud layer: ke (m^2/kg), w and the phase terms
 // pc[0..nleg].  Only the liquid microwave tables depend on temperature; the
 // effective radius and the temperature carry S's derivatives.  Returns false
-// for an unknown cloud type.
+// for an unknown cloud type.  With the channel tables Z the same values come
+// from the frequency-interpolated planes (the same arithmetic, one step done
+// once per channel).
 template <class S>
 CRTM_HD bool cloud_layer_optics(const CloudLut& C, bool microwave, double freq, int type, S reff,
-                                S temp, int nleg, int loff, S* ke, S* w, S* pc) {
+                                S temp, int nleg, int loff, S* ke, S* w, S* pc, const CloudChan& Z = CloudChan()) {
   for (int l = 0; l <= nleg; l++) pc[l] = S(0.0);
   *w = S(0.0);
+  if (Z.z) {
+    const bool solid = microwave && !(type == 1 || type == 3);
+    const int rows = microwave ? C.nrm : C.nri;
+    const size_t ps = (size_t)rows * Z.L;
+    const double* zc = Z.z + Z.ch;
+    auto plane = [&](int tab, int j) { return zc + (size_t)cloud_chan_plane(C, microwave, solid, tab, j) * ps; };
+    int kd;
+    if (!microwave)
+      kd = (type == 1 || type == 3) ? 0 : (type == 4 ? 1 : (type == 5 ? 2 : (type == 2 || type == 6 ? 3 : -1)));
+    else
+      kd = solid ? (type == 4 ? 0 : (type == 5 ? 1 : (type == 2 || type == 6 ? 2 : -1))) : 0;
+    if (kd < 0) return false;
+    if (microwave && !solid) {    // liquid: temperature axis
+      const Lagrange4T<S> T = lagrange4(C.t, C.nt, temp);
+      if (type == 1) {            // cloud water: (frequency, temperature) at the first radius
+        double a[4];
+        for (int k = 0; k < 4; k++) a[k] = plane(0, T.i0 + k)[0];
+        *ke = lerp4(a, 1, T);
+        return true;
+      }
+      const Lagrange4T<S> R = lagrange4(C.r_mw, C.nrm, reff);
+      const size_t r0 = (size_t)R.i0 * Z.L;
+      auto tr = [&](int tab) {
+        S a[4];
+        for (int k = 0; k < 4; k++) a[k] = lerp4(plane(tab, T.i0 + k) + r0, Z.L, R);
+        return lerp4(a, 1, T);
+      };
+      *ke = tr(0);
+      *w = tr(1);
+      pc[0] = S(0.5);
+      for (int l = 1; l <= nleg; l++) pc[l] = tr(2 + l + loff);
+      return true;
+    }
+    if (microwave && type == 2) {   // cloud ice: frequency only, first radius
+      *ke = S(plane(0, kd)[0]);
+      return true;
+    }
+    const Lagrange4T<S> R = lagrange4(microwave ? C.r_mw : C.r_ir, rows, reff);
+    const size_t r0 = (size_t)R.i0 * Z.L;
+    *ke = lerp4(plane(0, kd) + r0, Z.L, R);
+    *w = lerp4(plane(1, kd) + r0, Z.L, R);
+    pc[0] = S(0.5);
+    const int t0 = microwave ? loff : loff - 1;   // the infrared tables have no term 0
+    for (int l = 1; l <= nleg; l++) pc[l] = lerp4(plane(2 + l + t0, kd) + r0, Z.L, R);
+    return true;
+  }
   if (!microwave) {
     // density slot of Get_Cloud_Opt_IR: liquid 1, snow 2, graupel 3, ice/hail 4
     const int kd = (type == 1 || type == 3) ? 0 : (type == 4 ? 1 : (type == 5 ? 2 : (type == 2 || type == 6 ? 3 : -1)));
@@ -810,6 +906,7 @@ struct CloudyColumn {
   // CRTM_CloudCover_Define.f90:512-519), 1 otherwise.
   const double* cf = nullptr;
   double wc_div = 1.0;
+  CloudChan zc;                          // the sensor's channel-interpolated cloud tables (optional)
 };
 
 // Stream angles of a (profile, channel): Gauss angles of the stream set plus
@@ -879,7 +976,8 @@ CRTM_HD int species_share(const CloudyColumn& in, const CloudLut& lut, int nleg,
     S wc(wcv), re(in.reff[sp * in.cstride + k]), unused(0.0);
     seed(sp, wc, re, unused);
     S ke, w;
-    if (!cloud_layer_optics<S>(lut, in.microwave, in.freq, in.cloud_type[sp], re, tk, nleg, loff, &ke, &w, pc))
+    if (!cloud_layer_optics<S>(lut, in.microwave, in.freq, in.cloud_type[sp], re, tk, nleg, loff, &ke, &w, pc,
+                               in.zc))
       return -4;
     if (ke <= 0.0) { ke = S(0.0); w = S(0.0); }
     if (w <= 0.0) { w = S(0.0); for (int l = 0; l <= nleg; l++) pc[l] = S(0.0); }

@@ -570,14 +570,22 @@ def cloudy_workload(sensor_id: str, n_profiles: int, n_layers, seed: int,
 # Aerosols: synthetic AerosolCoeff LUT (scheme 'CRTM') and aerosol profiles
 # ---------------------------------------------------------------------------
 
-DUST_AEROSOL, SEASALT_AEROSOL, SULFATE_AEROSOL = 1, 2, 5
+# the reference's aerosol type ids (CRTM_Parameters.f90:286-294), all eight in
+# the synthetic table; the synthetic workloads load dust, sea salt (SSAM) and
+# sulfate
+(DUST_AEROSOL, SEASALT_SSAM_AEROSOL, SEASALT_SSCM1_AEROSOL, SEASALT_SSCM2_AEROSOL, SEASALT_SSCM3_AEROSOL,
+ ORGANIC_CARBON_AEROSOL, BLACK_CARBON_AEROSOL, SULFATE_AEROSOL) = range(1, 9)
+SEASALT_AEROSOL = SEASALT_SSAM_AEROSOL
+AEROSOL_TABLE_TYPES = tuple(range(1, 9))
+AEROSOL_TABLE_NAMES = ["Dust", "SeaSalt(SSAM)", "SeaSalt(SSCM1)", "SeaSalt(SSCM2)", "SeaSalt(SSCM3)",
+                       "Organic carbon", "Black carbon", "Sulfate"]
 AEROSOL_TYPES = (DUST_AEROSOL, SEASALT_AEROSOL, SULFATE_AEROSOL)
 AEROSOL_REFF = {DUST_AEROSOL: (0.5, 5.0), SEASALT_AEROSOL: (0.3, 3.0), SULFATE_AEROSOL: (0.05, 0.5)}
 
 
 def generate_aerosolcoeff(seed: int = 9, scheme: str = "CRTM") -> co.AerosolCoeff:
     """Synthetic AerosolCoeff table for one scheme, 20 wavelengths
-    (frequencies increasing) x 3 types, 38 Legendre terms, smooth Mie-like
+    (frequencies increasing) x the reference's 8 types, 38 Legendre terms, smooth Mie-like
     optics (extinction efficiency 2x^2/(1+x^2) of the size parameter x):
 
     - 'CRTM': 10 RH x 40 radii x 1 sigma; the scheme reads the first RH;
@@ -585,51 +593,76 @@ def generate_aerosolcoeff(seed: int = 9, scheme: str = "CRTM") -> co.AerosolCoef
       distributions act as larger particles;
     - 'GOCART-GEOS5' / 'NAAPS': 8 RH x 1 radius x 1 sigma; hygroscopic growth
       (kappa per type) swells the dry radius with relative humidity."""
-    rng = np.random.Generator(np.random.PCG64(seed))
     wl = np.geomspace(25.0, 0.3, 20)                      # microns, decreasing
     nu = 1.0e4 / wl                                        # cm^-1, increasing
-    nt, nl = len(AEROSOL_TYPES), CLOUD_N_LEGENDRE
-    dens = np.array([2.6, 2.2, 1.7])                       # g/cm^3
-    w0 = np.array([0.75, 0.98, 0.95])
+    nl = CLOUD_N_LEGENDRE
+    #                    dust  SSAM SSCM1 SSCM2 SSCM3  OC    BC   sulfate
+    DENS = np.array([2.6, 2.2, 2.2, 2.2, 2.2, 1.8, 1.0, 1.7])            # g/cm^3
+    W0 = np.array([0.75, 0.98, 0.98, 0.98, 0.98, 0.9, 0.3, 0.95])
+    RDRY = np.array([1.5, 1.0, 0.5, 2.0, 4.0, 0.1, 0.05, 0.15])          # dry radius (RH schemes)
+    KAPPA = np.array([0.05, 1.0, 1.0, 1.0, 1.0, 0.2, 0.0, 0.6])
 
-    def optics(r_eff, r_mass):
-        """r_eff (..., type) optical radius, r_mass the radius of the dry mass:
-        ke [m^2/kg], w, g with the wavelength axis first."""
-        x = 2.0 * np.pi * r_eff[None] * nu.reshape((-1,) + (1,) * r_eff.ndim) / 1.0e4
-        q = 2.0 * x ** 2 / (1.0 + x ** 2)
-        ke = 0.75 * q * (r_eff / r_mass)[None] ** 2 / (dens * 1.0e3 * r_mass[None] * 1.0e-6)
-        w = np.clip(w0 * x / (1.0 + x) + 0.02, 0.01, 0.995)
-        g = 0.7 * x / (1.0 + x)
-        return ke * (1.0 + 0.02 * rng.standard_normal(ke.shape)), w, g
+    def tables(sel, rng):
+        """The scheme's axes and (w, rh, r, sigma, type) tables of the types
+        at positions sel of the parameter arrays."""
+        nt, dens, w0 = len(sel), DENS[sel], W0[sel]
 
-    if scheme in ("CRTM", "CMAQ"):
-        nrh, nr = (10, 40) if scheme == "CRTM" else (1, 40)
-        reff = np.stack([np.geomspace(0.01, 20.0, nr)] * nt, axis=1)            # (r, type)
-        rh = np.linspace(0.0, 0.99, nrh) if scheme == "CRTM" else np.zeros(1)
-        if scheme == "CRTM":
-            rsig = np.ones((1, nt))
-            ke, w, g = optics(reff, reff)                                        # (w, r, type)
-            ke5, w5, g5 = (np.repeat(a[:, None, :, None, :], nrh, axis=1) for a in (ke, w, g))
+        def optics(r_eff, r_mass):
+            """r_eff (..., type) optical radius, r_mass the radius of the dry
+            mass: ke [m^2/kg], w, g with the wavelength axis first."""
+            x = 2.0 * np.pi * r_eff[None] * nu.reshape((-1,) + (1,) * r_eff.ndim) / 1.0e4
+            q = 2.0 * x ** 2 / (1.0 + x ** 2)
+            ke = 0.75 * q * (r_eff / r_mass)[None] ** 2 / (dens * 1.0e3 * r_mass[None] * 1.0e-6)
+            w = np.clip(w0 * x / (1.0 + x) + 0.02, 0.01, 0.995)
+            g = 0.7 * x / (1.0 + x)
+            return ke * (1.0 + 0.02 * rng.standard_normal(ke.shape)), w, g
+
+        if scheme in ("CRTM", "CMAQ"):
+            nrh, nr = (10, 40) if scheme == "CRTM" else (1, 40)
+            reff = np.stack([np.geomspace(0.01, 20.0, nr)] * nt, axis=1)            # (r, type)
+            rh = np.linspace(0.0, 0.99, nrh) if scheme == "CRTM" else np.zeros(1)
+            if scheme == "CRTM":
+                rsig = np.ones((1, nt))
+                ke, w, g = optics(reff, reff)                                        # (w, r, type)
+                ke5, w5, g5 = (np.repeat(a[:, None, :, None, :], nrh, axis=1) for a in (ke, w, g))
+            else:
+                ns = 6
+                rsig = np.stack([np.linspace(1.1, 2.6, ns)] * nt, axis=1)            # (sigma, type)
+                broad = np.exp(0.5 * np.log(rsig) ** 2)                              # (sigma, type)
+                r_opt = reff[:, None, :] * broad[None, :, :]                         # (r, sigma, type)
+                ke, w, g = optics(r_opt, np.broadcast_to(reff[:, None, :], r_opt.shape))
+                ke5, w5, g5 = (a[:, None] for a in (ke, w, g))                       # (w, 1, r, sigma, type)
         else:
-            ns = 6
-            rsig = np.stack([np.linspace(1.1, 2.6, ns)] * nt, axis=1)            # (sigma, type)
-            broad = np.exp(0.5 * np.log(rsig) ** 2)                              # (sigma, type)
-            r_opt = reff[:, None, :] * broad[None, :, :]                         # (r, sigma, type)
-            ke, w, g = optics(r_opt, np.broadcast_to(reff[:, None, :], r_opt.shape))
-            ke5, w5, g5 = (a[:, None] for a in (ke, w, g))                       # (w, 1, r, sigma, type)
-    else:
-        nrh = 8
-        rh = np.array([0.0, 0.5, 0.7, 0.8, 0.9, 0.95, 0.98, 0.99])
-        rdry = np.array([1.5, 1.0, 0.15])
-        kappa = np.array([0.05, 1.0, 0.6])
-        gf = (1.0 + kappa[None, :] * rh[:, None] / (1.0 - rh[:, None])) ** (1.0 / 3.0)   # (rh, type)
-        r_wet = rdry[None, :] * gf
-        ke, w, g = optics(r_wet, np.broadcast_to(rdry[None, :], r_wet.shape))           # (w, rh, type)
-        reff = rdry[None, :].copy()
-        rsig = np.ones((1, nt))
-        ke5, w5, g5 = (a[:, :, None, None, :] for a in (ke, w, g))                      # (w, rh, 1, 1, type)
+            rh = np.array([0.0, 0.5, 0.7, 0.8, 0.9, 0.95, 0.98, 0.99])
+            rdry, kappa = RDRY[sel], KAPPA[sel]
+            gf = (1.0 + kappa[None, :] * rh[:, None] / (1.0 - rh[:, None])) ** (1.0 / 3.0)   # (rh, type)
+            r_wet = rdry[None, :] * gf
+            ke, w, g = optics(r_wet, np.broadcast_to(rdry[None, :], r_wet.shape))           # (w, rh, type)
+            reff = rdry[None, :].copy()
+            rsig = np.ones((1, nt))
+            ke5, w5, g5 = (a[:, :, None, None, :] for a in (ke, w, g))                      # (w, rh, 1, 1, type)
+        return reff, rsig, rh, ke5, w5, g5
+
+    # dust, sea salt (SSAM) and sulfate from the seed's own stream, the other
+    # five types from a second one, so the workloads' three types keep their
+    # tables whatever else the file holds
+    first = [0, 1, 7]
+    rest = [2, 3, 4, 5, 6]
+    a = tables(first, np.random.Generator(np.random.PCG64(seed)))
+    b = tables(rest, np.random.Generator(np.random.PCG64(seed + 1000)))
+    out = []
+    for x, y in zip(a[:2], b[:2]):          # reff, rsig: type last
+        z = np.empty(x.shape[:-1] + (8,))
+        z[..., first], z[..., rest] = x, y
+        out.append(z)
+    rh = a[2]
+    for x, y in zip(a[3:], b[3:]):
+        z = np.empty(x.shape[:-1] + (8,))
+        z[..., first], z[..., rest] = x, y
+        out.append(z)
+    reff, rsig, ke5, w5, g5 = out
     pc = 0.5 * g5[..., None] ** np.arange(nl + 1)
-    return co.AerosolCoeff(np.array(AEROSOL_TYPES, np.int32), ["Dust", "SeaSalt", "Sulfate"], wl, reff,
+    return co.AerosolCoeff(np.array(AEROSOL_TABLE_TYPES, np.int32), AEROSOL_TABLE_NAMES, wl, reff,
                            rsig, rh, np.ascontiguousarray(ke5), np.ascontiguousarray(w5),
                            np.ascontiguousarray(g5), pc[..., None])
 

@@ -52,8 +52,15 @@ extern "C" {
 #define CRTM_GPU_FAILURE 3
 
 /* Arithmetic forms.  FP64: every stage in double precision.  MIXED: predictors,
- * regression and layer optics in single precision; Planck inversion (radiance
- * to brightness temperature) and the surface terms in double precision. */
+ * regression, gas layer optics, the scattering layers' MOM solver, layer
+ * records, adding and their reverse sweeps in single precision; Map_Input,
+ * the Planck inversion (radiance to brightness temperature), the surface
+ * terms, the cloud/aerosol LUT lookups and their derivatives, the adding's
+ * matrix inversions, the OPTRAN term and the SOI solver in double precision,
+ * as are the scattering layers that single precision cannot resolve (nearly
+ * conservative, or with a nearly defective MOM eigenbasis).  Outputs are
+ * double precision in both forms; the mixed form keeps 0.01 K in brightness
+ * temperatures and 1e-3 of the largest Jacobian. */
 #define CRTM_GPU_FP64 0
 #define CRTM_GPU_MIXED 1
 
@@ -312,8 +319,8 @@ int crtm_gpu_get_channel_subset(crtm_gpu_handle handle, int sensor, int capacity
 int crtm_gpu_set_precision(crtm_gpu_handle handle, int precision);
 
 /* CRTM_Forward for one sensor: host buffers.  Profiles with clouds or
- * aerosols use the ADA or SOI scattering solver (FP64 in both arithmetic
- * forms), as do the K-matrix, adjoint and tangent-linear entry points. */
+ * aerosols use the ADA or SOI scattering solver (Options%RT_Algorithm_Id),
+ * as do the K-matrix, adjoint and tangent-linear entry points. */
 int crtm_gpu_forward(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* batch,
                      crtm_gpu_rtsolution* rts);
 
@@ -373,8 +380,7 @@ int crtm_gpu_k_matrix_device_static(crtm_gpu_handle handle, int sensor,
 /* Tuning of the pipeline (no reference counterpart: the reference's only
  * batching parameter is the OpenMP chunking of profiles and channels,
  * CRTM_Forward_Module.f90:328-357).  Kept per sensor and per arithmetic form
- * (CRTM_GPU_FP64 / CRTM_GPU_MIXED; the K-matrix of a batch with clouds or
- * aerosols runs in the FP64 form).  Neither setting changes any output's
+ * (CRTM_GPU_FP64 / CRTM_GPU_MIXED).  Neither setting changes any output's
  * arithmetic, only the work decomposition:
  *   map_channels    channels per map_kernel CTA: 8, 16 or 32; 0 = the handle
  *                   default (16, or the CRTM_GPU_MAP_CHANNELS environment

@@ -669,3 +669,32 @@ def test_mixed_column_kmatrix_matches_fp64(sx, coeff_dir, sensor, n_streams, wc_
             assert abs(e1.value - e0.value) <= 1e-3 * abs(e0.value) and abs(b1.value - b0.value) <= 1e-3 * abs(b0.value)
             n_cols += 1
     assert n_cols == 36
+
+
+@pytest.mark.parametrize("sensor", ["mwsynth_c16", "irsynth_c616"])
+def test_channel_cloud_tables_match_direct_lookups(sx, coeff_dir, sensor):
+    """The cloud lookups through the sensor's channel-interpolated tables (the
+    frequency step done once per channel at init, as the GPU library does)
+    equal the direct lookups: every cloud type, radii and temperatures on and
+    between the grid nodes and beyond both ends, every stream set's Legendre
+    terms, values and radius / temperature derivatives."""
+    cc = co.read_cloudcoeff(sy.write_cloud_files(coeff_dir))
+    sc = co.read_spccoeff(f"{coeff_dir}/{sensor}.SpcCoeff.bin")
+    f = lambda a: np.ascontiguousarray(np.ravel(a, order="F"))   # noqa: E731
+    arrs = [f(x) for x in (cc.frequency_mw, cc.reff_mw, cc.temperature, cc.frequency_ir, cc.reff_ir,
+                           cc.ke_l_mw, cc.w_l_mw, cc.pcoeff_l_mw, cc.ke_s_mw, cc.w_s_mw, cc.pcoeff_s_mw,
+                           cc.ke_ir, cc.w_ir, cc.pcoeff_ir)]
+    dims = np.array([cc.frequency_mw.size, cc.reff_mw.size, cc.temperature.size, cc.density_mw.size,
+                     cc.frequency_ir.size, cc.reff_ir.size, cc.n_legendre_terms], np.int32)
+    mw = sc.sensor_type == co.MICROWAVE_SENSOR
+    freq = np.ascontiguousarray((sc.frequency if mw else sc.wavenumber)[::7] if not mw else sc.frequency)
+    rax = cc.reff_mw if mw else cc.reff_ir
+    re = np.ascontiguousarray(np.concatenate([[rax[0] * 0.5], rax[::4], 0.5 * (rax[1:] + rax[:-1])[::3],
+                                              [rax[-1] * 2.0]]))
+    tg = np.ascontiguousarray(np.concatenate([[cc.temperature[0] - 10.0], cc.temperature,
+                                              0.5 * (cc.temperature[1:] + cc.temperature[:-1]),
+                                              [cc.temperature[-1] + 10.0]]))
+    sx.sx_cloud_chan_compare.restype = ct.c_double
+    worst = sx.sx_cloud_chan_compare(_p(dims, _ip), *[_p(a) for a in arrs], int(mw), freq.size, _p(freq),
+                                     re.size, _p(re), tg.size, _p(tg))
+    assert worst == 0.0
