@@ -2167,8 +2167,8 @@ int crtm_gpu_init_aerosol(const char* coeff_path, int n_sensors, const char* con
       W.temp = h->d_irw + wo[3]; W.e = h->d_irw + wo[4];
       h->has_irwater = true;
     }
-    GaussTable gt{};
-    for (int n = 1; n <= 9; n++) double_gauss_host(n, gt.mu[n], gt.w[n]);
+    GaussTable gt;
+    gauss_table_host(gt);
     if (cudaMemcpyToSymbol(c_gauss, &gt, sizeof gt) != cudaSuccess || scatter_k_set_gauss(gt) ||
         cudaMalloc(&h->d_error, sizeof(int)) != cudaSuccess) {
       g_init_error = "device set-up of the scattering tables failed";

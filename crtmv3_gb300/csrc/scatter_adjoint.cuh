@@ -470,7 +470,8 @@ CRTM_HD int layer_bulk(const CloudyColumn& in, const CloudLut& lut, int nleg, in
   L.ssa = L.bs;
   if (L.bs > T(BS_THRESHOLD)) {
     const T w = L.bs / L.od0;
-    for (int l = 1; l <= nleg; l++) L.p[l] = L.ps[l] / L.bs;
+    const T ib = T(1.0) / L.bs;
+    for (int l = 1; l <= nleg; l++) L.p[l] = L.ps[l] * ib;
     L.p[0] = T(0.5);
     const T f = L.p[nleg];
     L.od = (T(1.0) - f * w) * L.od0;
@@ -479,18 +480,41 @@ CRTM_HD int layer_bulk(const CloudyColumn& in, const CloudLut& lut, int nleg, in
   return 0;
 }
 
-// Seed of one species' forward-mode pass: amount, first and second LUT
-// coordinate on directions 0, 1, 2 (temperature on 3 is seeded by the caller).
+// Seed of one species' forward-mode pass: the amount on direction 0, the
+// first LUT coordinate on 1 and the second on c2 (-1: not a direction of this
+// pass; the temperature's direction is seeded by the caller).
 struct SpeciesSeed {
-  int sp;
+  int sp, c2;
   template <class S>
-  CRTM_HD void operator()(int s, S& amount, S& c1, S& c2) const {
+  CRTM_HD void operator()(int s, S& amount, S& a1, S& a2) const {
     if (s != sp) return;
     amount.d[0] = 1.0;
-    c1.d[1] = 1.0;
-    c2.d[2] = 1.0;
+    a1.d[1] = 1.0;
+    if (c2 >= 0) a2.d[c2] = 1.0;
   }
 };
+
+// One species' forward-mode pass on N directions (amount, first coordinate,
+// and, for N = 3, the second coordinate or the temperature), contracted with
+// the species sums' adjoints: gg[d] = od0_b dod/dd + bs_b dbs/dd
+// + sum_l ps_b[l] dps_l/dd.
+template <int N>
+CRTM_HD int species_contract(const CloudyColumn& in, const CloudLut& lut, int nleg, int loff, int k, int sp,
+                             double tk, int c2_dir, int t_dir, double od0_b, double bs_b, const double* ps_b,
+                             double* gg) {
+  using D = Dual<N, double>;
+  D od(0.0), bs(0.0), ps[SC_NLEG_MAX + 1];
+  D td(tk, 0);
+  if (t_dir >= 0) td.d[t_dir] = 1.0;
+  if (const int rc = species_share<D>(in, lut, nleg, loff, k, sp, td, SpeciesSeed{sp, c2_dir}, &od, &bs, ps))
+    return rc;
+  for (int d = 0; d < N; d++) {
+    double v = od0_b * od.d[d] + bs_b * bs.d[d];
+    for (int l = 1; l <= nleg; l++) v += ps_b[l] * ps[l].d[d];
+    gg[d] = v;
+  }
+  return 0;
+}
 
 // The adjoints a layer's record hands to its optics, folded to the bulk
 // quantities: optical depth (od_b), single-scattering albedo (ssa_b),
@@ -523,10 +547,11 @@ CRTM_HD int bulk_to_inputs(const CloudyColumn& in, const CloudLut& lut, int nleg
     const double w_b = ssa_b * (1.0 - f) / (D * D) - od_b * f * L.od0;
     od0_b = od_b * D - w_b * w / L.od0;
     bs_b = w_b / L.od0;
+    const double ib = 1.0 / L.bs;
     for (int l = 1; l <= nleg; l++) {
       const double pb = l < nleg ? double(A.p_b[l]) : f_b;
-      ps_b[l] = pb / L.bs;
-      bs_b -= pb * L.p[l] / L.bs;
+      ps_b[l] = pb * ib;
+      bs_b -= pb * L.p[l] * ib;
     }
   } else {
     bs_b = ssa_b;
@@ -535,26 +560,27 @@ CRTM_HD int bulk_to_inputs(const CloudyColumn& in, const CloudLut& lut, int nleg
   // Planck radiance of the layer temperature
   const double te = in.b1 + in.b2 * tk, ee = exp(in.c2 / te);
   double gt = (double)A.B_b * in.c1 * in.c2 * ee * in.b2 / (te * te * (ee - 1.0) * (ee - 1.0));
-  // each species' share in forward mode: amount, c1, c2 and the temperature,
-  // in FP64 in every form (the LUT derivatives are differences of nearby
-  // table values: in FP32 they cost the radius Jacobians ~1e-3; the LUT work
-  // is a small part of the layer's)
-  using D4 = Dual<4, double>;
+  // each species' share in forward mode on the directions its lookup has:
+  // the amount and the first coordinate (radius, or relative humidity for
+  // 'GOCART-GEOS5' / 'NAAPS'), and a third only for the liquid microwave
+  // tables (temperature) and 'CMAQ' (sigma); in FP64 in every form (the LUT
+  // derivatives are differences of nearby table values: in FP32 they cost
+  // the radius Jacobians ~1e-3)
   for (int sp = 0; sp < nsp; sp++) {
-    D4 od(0.0), bs(0.0), ps[SC_NLEG_MAX + 1];
-    D4 td(tk, 0);
-    td.d[3] = 1.0;
-    if (const int rc = species_share<D4>(in, lut, nleg, loff, k, sp, td, SpeciesSeed{sp}, &od, &bs, ps)) return rc;
-    double gg[4];
-    for (int d = 0; d < 4; d++) {
-      double v = od0_b * od.d[d] + bs_b * bs.d[d];
-      for (int l = 1; l <= nleg; l++) v += ps_b[l] * ps[l].d[d];
-      gg[d] = v;
-    }
+    const bool cloud = sp < in.n_clouds;
+    const int type = cloud ? in.cloud_type[sp] : 0;
+    const bool t_dep = cloud && in.microwave && (type == 1 || type == 3);
+    const bool c2_dep = !cloud && in.alut && in.alut->scheme == AEROSOL_CMAQ;
+    double gg[3] = {0.0, 0.0, 0.0};
+    const int rc = (t_dep || c2_dep)
+                       ? species_contract<3>(in, lut, nleg, loff, k, sp, tk, c2_dep ? 2 : -1, t_dep ? 2 : -1, od0_b,
+                                             bs_b, ps_b, gg)
+                       : species_contract<2>(in, lut, nleg, loff, k, sp, tk, -1, -1, od0_b, bs_b, ps_b, gg);
+    if (rc) return rc;
     gs[sp][0] = gg[0];
     gs[sp][1] = gg[1];
-    gs[sp][2] = gg[2];
-    gt += gg[3];
+    gs[sp][2] = c2_dep ? gg[2] : 0.0;
+    if (t_dep) gt += gg[2];
   }
   g[1] = gt;
   return 0;

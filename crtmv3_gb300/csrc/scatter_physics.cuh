@@ -71,9 +71,12 @@ struct CloudLut {
 };
 
 // Gauss-Legendre angles/weights on (0,1) for 1..9 streams (Double_Gauss_Quadrature).
+// P[n][i][l]: Legendre polynomial l of angle i of the n-point set, l up to
+// the largest stream set's term count (the streams' P of every layer).
 struct GaussTable {
   double mu[10][SC_NZ_MAX];
   double w[10][SC_NZ_MAX];
+  double P[10][9][SC_NLEG_MAX + 1];
 };
 
 // ---- interpolation ----------------------------------------------------------
@@ -100,16 +103,20 @@ CRTM_HD Lagrange4T<S> lagrange4(const double* ax, int n, S x) {
   const S a0 = x - p[0], a1 = x - p[1], a2 = x - p[2], a3 = x - p[3];
   const double d01 = p[0] - p[1], d02 = p[0] - p[2], d12 = p[1] - p[2], d13 = p[1] - p[3],
                d23 = p[2] - p[3];
-  S wr = (x < p[1]) ? S(0.0) : ((x > p[2]) ? S(1.0) : a1 / (-d12));
+  // the denominators' reciprocals in plain double: the weights carry S's
+  // derivative parts through multiplications only
+  const double r12 = 1.0 / d12, rl0 = 1.0 / (d01 * d02), rl1 = -1.0 / (d01 * d12), rl2 = 1.0 / (d02 * d12),
+               rr0 = 1.0 / (d12 * d13), rr1 = -1.0 / (d12 * d23), rr2 = 1.0 / (d13 * d23);
+  S wr = (x < p[1]) ? S(0.0) : ((x > p[2]) ? S(1.0) : a1 * (-r12));
   const S wl = 1.0 - wr;
   Lagrange4T<S> L;
   L.i0 = i0;
-  L.wl[0] = wl * (a1 * a2 / (d01 * d02));
-  L.wl[1] = wl * (a0 * a2 / (-d01 * d12));
-  L.wl[2] = wl * (a0 * a1 / (d02 * d12));
-  L.wr[0] = wr * (a2 * a3 / (d12 * d13));
-  L.wr[1] = wr * (a1 * a3 / (-d12 * d23));
-  L.wr[2] = wr * (a1 * a2 / (d13 * d23));
+  L.wl[0] = wl * (a1 * a2 * rl0);
+  L.wl[1] = wl * (a0 * a2 * rl1);
+  L.wl[2] = wl * (a0 * a1 * rl2);
+  L.wr[0] = wr * (a2 * a3 * rr0);
+  L.wr[1] = wr * (a1 * a3 * rr1);
+  L.wr[2] = wr * (a1 * a2 * rr2);
   return L;
 }
 
@@ -936,7 +943,11 @@ CRTM_HD int stream_set(int nleg, double mu_sensor, int lut_nleg, const GaussTabl
     if (S.isat < 0 && fabs(gt.mu[S.nS][i] - mu_sensor) < ANGLE_THRESHOLD) S.isat = i;
   }
   if (S.isat < 0) { S.nZ = S.nS + 1; S.isat = S.nS; S.mu[S.nS] = T(mu_sensor); S.wt[S.nS] = T(0); }
-  for (int i = 0; i < S.nZ; i++) {
+  // the quadrature angles' Legendre values from the table; the sensor
+  // angle's by the recurrence
+  for (int i = 0; i < S.nS; i++)
+    for (int l = 0; l <= nleg; l++) S.P[i][l] = T(gt.P[S.nS][i][l]);
+  for (int i = S.nS; i < S.nZ; i++) {
     S.P[i][0] = T(1);
     if (nleg > 0) S.P[i][1] = S.mu[i];
     for (int j = 1; j < nleg; j++)
@@ -1053,7 +1064,8 @@ CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const Stre
   S ssa = bs_sum;
   if (bs_sum > BS_THRESHOLD) {   // CRTM_AtmOptics_Combine
     const S w = bs_sum / od;
-    for (int l = 1; l <= nleg; l++) pcs[l] /= bs_sum;
+    const S ib = 1.0 / bs_sum;
+    for (int l = 1; l <= nleg; l++) pcs[l] *= ib;
     pcs[0] = S(0.5);
     const S f = pcs[nleg];
     od = (1.0 - f * w) * od;
@@ -1978,6 +1990,21 @@ inline void double_gauss_host(int n, double* x, double* w) {
     x[j - 1] = (1.0 - X) / 2.0;
     x[n - j] = (1.0 + X) / 2.0;
     w[j - 1] = w[n - j] = 1.0 / ((1.0 - X * X) * DPL * DPL);
+  }
+}
+
+// The Gauss table: angles and weights of the 1..9-point sets and their
+// Legendre values P_l(mu_i), l = 0..SC_NLEG_MAX (Legendre_M, m = 0).
+inline void gauss_table_host(GaussTable& g) {
+  g = GaussTable{};
+  for (int n = 1; n <= 9; n++) {
+    double_gauss_host(n, g.mu[n], g.w[n]);
+    for (int i = 0; i < n; i++) {
+      double* P = g.P[n][i];
+      P[0] = 1.0;
+      P[1] = g.mu[n][i];
+      for (int j = 1; j < SC_NLEG_MAX; j++) P[j + 1] = ((2 * j + 1) * g.mu[n][i] * P[j] - j * P[j - 1]) / (j + 1);
+    }
   }
 }
 

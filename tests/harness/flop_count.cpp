@@ -47,8 +47,8 @@ template <> struct JacobiEps<FC> { static constexpr double value = 1.0e-14; };
 using namespace crtm;
 
 static GaussTable make_gauss() {
-  GaussTable g{};
-  for (int n = 1; n <= 9; n++) double_gauss_host(n, g.mu[n], g.w[n]);
+  GaussTable g;
+  gauss_table_host(g);
   return g;
 }
 

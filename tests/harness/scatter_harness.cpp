@@ -10,8 +10,8 @@ using namespace crtm;
 
 namespace {
 GaussTable make_gauss() {
-  GaussTable g{};
-  for (int n = 1; n <= 9; n++) double_gauss_host(n, g.mu[n], g.w[n]);
+  GaussTable g;
+  gauss_table_host(g);
   return g;
 }
 }  // namespace
