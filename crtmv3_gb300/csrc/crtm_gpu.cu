@@ -2083,6 +2083,17 @@ int crtm_gpu_init_aerosol(const char* coeff_path, int n_sensors, const char* con
         crtm_gpu_destroy(h);
         return CRTM_GPU_FAILURE;
       }
+      // the radius and temperature axes' Lagrange reciprocals, after the tables
+      const int rc_n[3] = {dims[1], dims[5], dims[2]};   // r_mw, r_ir, t
+      const size_t rc_ax[3] = {off[2], off[3], off[4]};
+      size_t rc_off[3];
+      for (int a = 0; a < 3; a++) {
+        rc_off[a] = buf.size();
+        if (rc_n[a] >= 4) {
+          buf.resize(buf.size() + (size_t)(rc_n[a] - 3) * 7);
+          lagrange4_recip_table(buf.data() + rc_ax[a], rc_n[a], buf.data() + rc_off[a]);
+        }
+      }
       if (cudaMalloc(&h->d_cloud, buf.size() * sizeof(double)) != cudaSuccess ||
           cudaMemcpy(h->d_cloud, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
         g_init_error = "device upload of CloudCoeff.bin failed";
@@ -2097,6 +2108,9 @@ int crtm_gpu_init_aerosol(const char* coeff_path, int n_sensors, const char* con
       L.ke_l = b0 + off[5]; L.w_l = b0 + off[6]; L.pc_l = b0 + off[7];
       L.ke_s = b0 + off[8]; L.w_s = b0 + off[9]; L.pc_s = b0 + off[10];
       L.ke_ir = b0 + off[11]; L.w_ir = b0 + off[12]; L.pc_ir = b0 + off[13];
+      L.rc_rmw = rc_n[0] >= 4 ? b0 + rc_off[0] : nullptr;
+      L.rc_rir = rc_n[1] >= 4 ? b0 + rc_off[1] : nullptr;
+      L.rc_t = rc_n[2] >= 4 ? b0 + rc_off[2] : nullptr;
       h->has_clouds = true;
       for (auto& s : h->sensors)
         if (!build_cloud_chan(h->lut, true, s, err)) {
@@ -2125,6 +2139,21 @@ int crtm_gpu_init_aerosol(const char* coeff_path, int n_sensors, const char* con
         crtm_gpu_destroy(h);
         return CRTM_GPU_FAILURE;
       }
+      // the axes' Lagrange reciprocals (radius and sigma per type), after the tables
+      const int ant = adims[4], anr = adims[2], ans = adims[3];
+      size_t ar_off[4] = {0, 0, 0, 0};
+      auto add_rec = [&](size_t ax, int n, int rows) -> size_t {
+        const size_t o = abuf.size();
+        if (n < 4) return 0;
+        abuf.resize(abuf.size() + (size_t)rows * (n - 3) * 7);
+        for (int r = 0; r < rows; r++)
+          lagrange4_recip_table(abuf.data() + ax + (size_t)r * n, n, abuf.data() + o + (size_t)r * (n - 3) * 7);
+        return o;
+      };
+      ar_off[0] = add_rec(aoff[0], adims[0], 1);
+      ar_off[1] = add_rec(aoff[1], anr, ant);
+      ar_off[2] = add_rec(aoff[5], ans, ant);
+      ar_off[3] = add_rec(aoff[6], adims[6], 1);
       if (cudaMalloc(&h->d_aero, abuf.size() * sizeof(double)) != cudaSuccess ||
           cudaMalloc(&h->d_aero_type, types.size() * sizeof(int)) != cudaSuccess ||
           cudaMemcpy(h->d_aero, abuf.data(), abuf.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -2141,6 +2170,10 @@ int crtm_gpu_init_aerosol(const char* coeff_path, int n_sensors, const char* con
       A.freq = h->d_aero + aoff[0]; A.reff = h->d_aero + aoff[1]; A.ke = h->d_aero + aoff[2];
       A.w = h->d_aero + aoff[3]; A.pc = h->d_aero + aoff[4]; A.rsig = h->d_aero + aoff[5];
       A.rh = h->d_aero + aoff[6];
+      A.rc_freq = ar_off[0] ? h->d_aero + ar_off[0] : nullptr;
+      A.rc_reff = ar_off[1] ? h->d_aero + ar_off[1] : nullptr;
+      A.rc_rsig = ar_off[2] ? h->d_aero + ar_off[2] : nullptr;
+      A.rc_rh = ar_off[3] ? h->d_aero + ar_off[3] : nullptr;
       h->has_aerosols = true;
     }
     const std::string wpath = std::string(coeff_path) + "/Nalli.IRwater.EmisCoeff.bin";

@@ -68,6 +68,8 @@ struct CloudLut {
   const double* ke_l, *w_l, *pc_l;   // [nt][nrm][nfm], pc: [nleg+1][nt][nrm][nfm]
   const double* ke_s, *w_s, *pc_s;   // [nd][nrm][nfm],  pc: [nleg+1][nd][nrm][nfm]
   const double* ke_ir, *w_ir, *pc_ir; // [nd+1][nri][nfi], pc: [nleg][nd+1][nri][nfi]
+  // lagrange4_recip_table of the radius and temperature axes (null: formed per lookup)
+  const double* rc_rmw = nullptr, *rc_rir = nullptr, *rc_t = nullptr;
 };
 
 // Gauss-Legendre angles/weights on (0,1) for 1..9 streams (Double_Gauss_Quadrature).
@@ -89,24 +91,51 @@ struct Lagrange4T {
 };
 using Lagrange4 = Lagrange4T<double>;
 
+// The seven reciprocal denominators of the 4-point window starting at node
+// i0 of an axis: 1/d12 and the left and right quadratics' 1/(d..d..).
+CRTM_HD void lagrange4_recip(const double* p, double* r) {
+  const double d01 = p[0] - p[1], d02 = p[0] - p[2], d12 = p[1] - p[2], d13 = p[1] - p[3],
+               d23 = p[2] - p[3];
+  r[0] = 1.0 / d12;
+  r[1] = 1.0 / (d01 * d02);
+  r[2] = -1.0 / (d01 * d12);
+  r[3] = 1.0 / (d02 * d12);
+  r[4] = 1.0 / (d12 * d13);
+  r[5] = -1.0 / (d12 * d23);
+  r[6] = 1.0 / (d13 * d23);
+}
+
+// Host: an axis's table of lagrange4_recip for every window (n - 3 rows of 7;
+// empty for axes of fewer than 4 nodes).
+inline void lagrange4_recip_table(const double* ax, int n, double* out) {
+  for (int i0 = 0; i0 + 3 < n; i0++) lagrange4_recip(ax + i0, out + 7 * i0);
+}
+
 // Clamp x into the axis, bracket it with 4 points and form the blended
 // quadratic weights (the reference's LPoly applied to a 4-point window).
+// rec: the axis's lagrange4_recip_table (null: the reciprocals are formed
+// here); the weights carry S's derivative parts through multiplications only.
 template <class S>
-CRTM_HD Lagrange4T<S> lagrange4(const double* ax, int n, S x) {
+CRTM_HD Lagrange4T<S> lagrange4(const double* ax, int n, S x, const double* rec = nullptr) {
   if (x < ax[0]) x = S(ax[0]);
   if (x > ax[n - 1]) x = S(ax[n - 1]);
-  int k = 0;
-  while (k < n && x > ax[k]) k++;     // first node >= x
-  int i0 = k - 2;
+  int lo = 0, hi = n - 1;             // first node >= x, by bisection
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (x > ax[mid]) lo = mid + 1;
+    else hi = mid;
+  }
+  int i0 = lo - 2;
   i0 = i0 < 0 ? 0 : (i0 > n - 4 ? n - 4 : i0);
   const double* p = ax + i0;
   const S a0 = x - p[0], a1 = x - p[1], a2 = x - p[2], a3 = x - p[3];
-  const double d01 = p[0] - p[1], d02 = p[0] - p[2], d12 = p[1] - p[2], d13 = p[1] - p[3],
-               d23 = p[2] - p[3];
-  // the denominators' reciprocals in plain double: the weights carry S's
-  // derivative parts through multiplications only
-  const double r12 = 1.0 / d12, rl0 = 1.0 / (d01 * d02), rl1 = -1.0 / (d01 * d12), rl2 = 1.0 / (d02 * d12),
-               rr0 = 1.0 / (d12 * d13), rr1 = -1.0 / (d12 * d23), rr2 = 1.0 / (d13 * d23);
+  double rw[7];
+  if (rec) {
+    for (int q = 0; q < 7; q++) rw[q] = rec[7 * i0 + q];
+  } else {
+    lagrange4_recip(p, rw);
+  }
+  const double r12 = rw[0], rl0 = rw[1], rl1 = rw[2], rl2 = rw[3], rr0 = rw[4], rr1 = rw[5], rr2 = rw[6];
   S wr = (x < p[1]) ? S(0.0) : ((x > p[2]) ? S(1.0) : a1 * (-r12));
   const S wl = 1.0 - wr;
   Lagrange4T<S> L;
@@ -221,14 +250,14 @@ CRTM_HD bool cloud_layer_optics(const CloudLut& C, bool microwave, double freq, 
       kd = solid ? (type == 4 ? 0 : (type == 5 ? 1 : (type == 2 || type == 6 ? 2 : -1))) : 0;
     if (kd < 0) return false;
     if (microwave && !solid) {    // liquid: temperature axis
-      const Lagrange4T<S> T = lagrange4(C.t, C.nt, temp);
+      const Lagrange4T<S> T = lagrange4(C.t, C.nt, temp, C.rc_t);
       if (type == 1) {            // cloud water: (frequency, temperature) at the first radius
         double a[4];
         for (int k = 0; k < 4; k++) a[k] = plane(0, T.i0 + k)[0];
         *ke = lerp4(a, 1, T);
         return true;
       }
-      const Lagrange4T<S> R = lagrange4(C.r_mw, C.nrm, reff);
+      const Lagrange4T<S> R = lagrange4(C.r_mw, C.nrm, reff, C.rc_rmw);
       const size_t r0 = (size_t)R.i0 * Z.L;
       auto tr = [&](int tab) {
         S a[4];
@@ -245,7 +274,7 @@ CRTM_HD bool cloud_layer_optics(const CloudLut& C, bool microwave, double freq, 
       *ke = S(plane(0, kd)[0]);
       return true;
     }
-    const Lagrange4T<S> R = lagrange4(microwave ? C.r_mw : C.r_ir, rows, reff);
+    const Lagrange4T<S> R = lagrange4(microwave ? C.r_mw : C.r_ir, rows, reff, microwave ? C.rc_rmw : C.rc_rir);
     const size_t r0 = (size_t)R.i0 * Z.L;
     *ke = lerp4(plane(0, kd) + r0, Z.L, R);
     *w = lerp4(plane(1, kd) + r0, Z.L, R);
@@ -316,6 +345,9 @@ struct AerosolLut {
   const double* rh;         // [nrh_axis]
   const double* ke, *w;     // [nt][ns][nr][nrh][nw]
   const double* pc;         // [nleg+1][nt][ns][nr][nrh][nw]
+  // lagrange4_recip_table of the axes (per type for radius and sigma: rows of
+  // (nr - 3) * 7 and (ns - 3) * 7); null: formed per lookup
+  const double* rc_freq = nullptr, *rc_reff = nullptr, *rc_rsig = nullptr, *rc_rh = nullptr;
 };
 
 // Get_Aerosol_Opt (CRTM_AerosolScatter.f90:772-918).  'CRTM': frequency x
@@ -329,24 +361,26 @@ CRTM_HD bool aerosol_layer_optics(const AerosolLut& A, double wavenumber, int ty
   for (int t = 0; t < A.nt; t++)
     if (A.type_id[t] == type) { k = t; break; }
   if (k < 0) return false;
-  const Lagrange4 F = lagrange4(A.freq, A.nw, wavenumber);
+  const Lagrange4 F = lagrange4(A.freq, A.nw, wavenumber, A.rc_freq);
+  const double* rcr = A.rc_reff ? A.rc_reff + (size_t)k * (A.nr - 3) * 7 : nullptr;
+  const double* rcs = A.rc_rsig ? A.rc_rsig + (size_t)k * (A.ns - 3) * 7 : nullptr;
   const int nu = A.nw * A.nrh;                     // radius stride
   const size_t base = (size_t)k * A.nw * A.nrh * A.nr * A.ns;
   const size_t n5 = (size_t)A.nw * A.nrh * A.nr * A.ns * A.nt;
   pc[0] = S(0.5);
   if (A.scheme == AEROSOL_CRTM) {
-    const Lagrange4T<S> Rr = lagrange4(A.reff + (size_t)k * A.nr, A.nr, reff);
+    const Lagrange4T<S> Rr = lagrange4(A.reff + (size_t)k * A.nr, A.nr, reff, rcr);
     *ke = lerp4x4(A.ke + base, nu, F, Rr);
     *w = lerp4x4(A.w + base, nu, F, Rr);
     for (int l = 1; l <= nleg; l++) pc[l] = lerp4x4(A.pc + n5 * (l + loff) + base, nu, F, Rr);
   } else if (A.scheme == AEROSOL_CMAQ) {
-    const Lagrange4T<S> Rr = lagrange4(A.reff + (size_t)k * A.nr, A.nr, reff);
-    const Lagrange4T<S> Sg = lagrange4(A.rsig + (size_t)k * A.ns, A.ns, rsig);
+    const Lagrange4T<S> Rr = lagrange4(A.reff + (size_t)k * A.nr, A.nr, reff, rcr);
+    const Lagrange4T<S> Sg = lagrange4(A.rsig + (size_t)k * A.ns, A.ns, rsig, rcs);
     *ke = lerp4x4x4(A.ke + base, nu, A.nr, F, Rr, Sg);
     *w = lerp4x4x4(A.w + base, nu, A.nr, F, Rr, Sg);
     for (int l = 1; l <= nleg; l++) pc[l] = lerp4x4x4(A.pc + n5 * (l + loff) + base, nu, A.nr, F, Rr, Sg);
   } else {
-    const Lagrange4T<S> H = lagrange4(A.rh, A.nrh, rh);
+    const Lagrange4T<S> H = lagrange4(A.rh, A.nrh, rh, A.rc_rh);
     *ke = lerp4x4(A.ke + base, A.nw, F, H);
     *w = lerp4x4(A.w + base, A.nw, F, H);
     for (int l = 1; l <= nleg; l++) pc[l] = lerp4x4(A.pc + n5 * (l + loff) + base, A.nw, F, H);

@@ -574,6 +574,16 @@ extern "C" double sx_cloud_chan_compare(const int* dims, const double* f_mw, con
     const Lagrange4 U = lagrange4(mw ? C.f_mw : C.f_ir, nf, freq[ch]);
     z[(size_t)i] = lerp4(cloud_chan_source(C, mw, q) + (size_t)r * nf + U.i0, 1, U);
   }
+  // the radius and temperature axes' reciprocal tables, as the library builds them
+  std::vector<double> rmw((size_t)std::max(C.nrm - 3, 0) * 7), rir((size_t)std::max(C.nri - 3, 0) * 7),
+      rt((size_t)std::max(C.nt - 3, 0) * 7);
+  lagrange4_recip_table(C.r_mw, C.nrm, rmw.data());
+  lagrange4_recip_table(C.r_ir, C.nri, rir.data());
+  lagrange4_recip_table(C.t, C.nt, rt.data());
+  CloudLut CR = C;
+  CR.rc_rmw = C.nrm >= 4 ? rmw.data() : nullptr;
+  CR.rc_rir = C.nri >= 4 ? rir.data() : nullptr;
+  CR.rc_t = C.nt >= 4 ? rt.data() : nullptr;
   using D = Dual<2>;
   double worst = 0.0;
   const int nlegs[5] = {2, 4, 6, 8, 16};
@@ -590,7 +600,7 @@ extern "C" double sx_cloud_chan_compare(const int* dims, const double* f_mw, con
             D ke0, w0, pc0[SC_NLEG_MAX + 1], ke1, w1, pc1[SC_NLEG_MAX + 1];
             const CloudChan Z{z.data(), (size_t)L, ch};
             const bool ok0 = cloud_layer_optics<D>(C, mw, freq[ch], type, re, tk, nleg, loff, &ke0, &w0, pc0);
-            const bool ok1 = cloud_layer_optics<D>(C, mw, freq[ch], type, re, tk, nleg, loff, &ke1, &w1, pc1, Z);
+            const bool ok1 = cloud_layer_optics<D>(CR, mw, freq[ch], type, re, tk, nleg, loff, &ke1, &w1, pc1, Z);
             if (ok0 != ok1) return 1e300;
             if (!ok0) continue;
             auto cmp = [&](const D& x, const D& y) {

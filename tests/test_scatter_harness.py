@@ -674,8 +674,8 @@ def test_mixed_column_kmatrix_matches_fp64(sx, coeff_dir, sensor, n_streams, wc_
 @pytest.mark.parametrize("sensor", ["mwsynth_c16", "irsynth_c616"])
 def test_channel_cloud_tables_match_direct_lookups(sx, coeff_dir, sensor):
     """The cloud lookups through the sensor's channel-interpolated tables (the
-    frequency step done once per channel at init, as the GPU library does)
-    equal the direct lookups: every cloud type, radii and temperatures on and
+    frequency step done once per channel at init, as the GPU library does) and
+    the axes' precomputed Lagrange reciprocals equal the direct lookups: every cloud type, radii and temperatures on and
     between the grid nodes and beyond both ends, every stream set's Legendre
     terms, values and radius / temperature derivatives."""
     cc = co.read_cloudcoeff(sy.write_cloud_files(coeff_dir))
