@@ -186,6 +186,7 @@ CRTM_HD S lerp4x4x4(const double* z, int nu, int nv, const Lagrange4& U, const L
 // A null z: the lookups interpolate in frequency themselves.
 struct CloudChan {
   const double* z = nullptr;
+  const float* zf = nullptr;   // the same tables in FP32 (the FP32 lookups'), or null
   size_t L = 0;
   int ch = 0;
 };
@@ -226,6 +227,56 @@ CRTM_HD int legendre_offset(int nleg) {
   return nleg == 2 || nleg == 4 ? 0 : (nleg == 6 ? 5 : (nleg == 8 ? 12 : (nleg == 16 ? 21 : -1)));
 }
 
+// The lookups of cloud_layer_optics through channel tables of element type
+// TZ (zc: the tables at this channel; L: the channel stride).
+template <class S, class TZ>
+CRTM_HD bool cloud_optics_chan(const CloudLut& C, bool microwave, int type, S reff, S temp, int nleg, int loff,
+                               S* ke, S* w, S* pc, const TZ* zc, size_t L) {
+  const bool solid = microwave && !(type == 1 || type == 3);
+  const int rows = microwave ? C.nrm : C.nri;
+  const size_t ps = (size_t)rows * L;
+  auto plane = [&](int tab, int j) { return zc + (size_t)cloud_chan_plane(C, microwave, solid, tab, j) * ps; };
+  int kd;
+  if (!microwave)
+    kd = (type == 1 || type == 3) ? 0 : (type == 4 ? 1 : (type == 5 ? 2 : (type == 2 || type == 6 ? 3 : -1)));
+  else
+    kd = solid ? (type == 4 ? 0 : (type == 5 ? 1 : (type == 2 || type == 6 ? 2 : -1))) : 0;
+  if (kd < 0) return false;
+  if (microwave && !solid) {    // liquid: temperature axis
+    const Lagrange4T<S> T = lagrange4(C.t, C.nt, temp, C.rc_t);
+    if (type == 1) {            // cloud water: (frequency, temperature) at the first radius
+      double a[4];
+      for (int k = 0; k < 4; k++) a[k] = plane(0, T.i0 + k)[0];
+      *ke = lerp4(a, 1, T);
+      return true;
+    }
+    const Lagrange4T<S> R = lagrange4(C.r_mw, C.nrm, reff, C.rc_rmw);
+    const size_t r0 = (size_t)R.i0 * L;
+    auto tr = [&](int tab) {
+      S a[4];
+      for (int k = 0; k < 4; k++) a[k] = lerp4(plane(tab, T.i0 + k) + r0, L, R);
+      return lerp4(a, 1, T);
+    };
+    *ke = tr(0);
+    *w = tr(1);
+    pc[0] = S(0.5);
+    for (int l = 1; l <= nleg; l++) pc[l] = tr(2 + l + loff);
+    return true;
+  }
+  if (microwave && type == 2) {   // cloud ice: frequency only, first radius
+    *ke = S(plane(0, kd)[0]);
+    return true;
+  }
+  const Lagrange4T<S> R = lagrange4(microwave ? C.r_mw : C.r_ir, rows, reff, microwave ? C.rc_rmw : C.rc_rir);
+  const size_t r0 = (size_t)R.i0 * L;
+  *ke = lerp4(plane(0, kd) + r0, L, R);
+  *w = lerp4(plane(1, kd) + r0, L, R);
+  pc[0] = S(0.5);
+  const int t0 = microwave ? loff : loff - 1;   // the infrared tables have no term 0
+  for (int l = 1; l <= nleg; l++) pc[l] = lerp4(plane(2 + l + t0, kd) + r0, L, R);
+  return true;
+}
+
 // Optical properties of one cloud layer: ke (m^2/kg), w and the phase terms
 // pc[0..nleg].  Only the liquid microwave tables depend on temperature; the
 // effective radius and the temperature carry S's derivatives.  Returns false
@@ -238,50 +289,11 @@ CRTM_HD bool cloud_layer_optics(const CloudLut& C, bool microwave, double freq, 
   for (int l = 0; l <= nleg; l++) pc[l] = S(0.0);
   *w = S(0.0);
   if (Z.z) {
-    const bool solid = microwave && !(type == 1 || type == 3);
-    const int rows = microwave ? C.nrm : C.nri;
-    const size_t ps = (size_t)rows * Z.L;
-    const double* zc = Z.z + Z.ch;
-    auto plane = [&](int tab, int j) { return zc + (size_t)cloud_chan_plane(C, microwave, solid, tab, j) * ps; };
-    int kd;
-    if (!microwave)
-      kd = (type == 1 || type == 3) ? 0 : (type == 4 ? 1 : (type == 5 ? 2 : (type == 2 || type == 6 ? 3 : -1)));
-    else
-      kd = solid ? (type == 4 ? 0 : (type == 5 ? 1 : (type == 2 || type == 6 ? 2 : -1))) : 0;
-    if (kd < 0) return false;
-    if (microwave && !solid) {    // liquid: temperature axis
-      const Lagrange4T<S> T = lagrange4(C.t, C.nt, temp, C.rc_t);
-      if (type == 1) {            // cloud water: (frequency, temperature) at the first radius
-        double a[4];
-        for (int k = 0; k < 4; k++) a[k] = plane(0, T.i0 + k)[0];
-        *ke = lerp4(a, 1, T);
-        return true;
-      }
-      const Lagrange4T<S> R = lagrange4(C.r_mw, C.nrm, reff, C.rc_rmw);
-      const size_t r0 = (size_t)R.i0 * Z.L;
-      auto tr = [&](int tab) {
-        S a[4];
-        for (int k = 0; k < 4; k++) a[k] = lerp4(plane(tab, T.i0 + k) + r0, Z.L, R);
-        return lerp4(a, 1, T);
-      };
-      *ke = tr(0);
-      *w = tr(1);
-      pc[0] = S(0.5);
-      for (int l = 1; l <= nleg; l++) pc[l] = tr(2 + l + loff);
-      return true;
-    }
-    if (microwave && type == 2) {   // cloud ice: frequency only, first radius
-      *ke = S(plane(0, kd)[0]);
-      return true;
-    }
-    const Lagrange4T<S> R = lagrange4(microwave ? C.r_mw : C.r_ir, rows, reff, microwave ? C.rc_rmw : C.rc_rir);
-    const size_t r0 = (size_t)R.i0 * Z.L;
-    *ke = lerp4(plane(0, kd) + r0, Z.L, R);
-    *w = lerp4(plane(1, kd) + r0, Z.L, R);
-    pc[0] = S(0.5);
-    const int t0 = microwave ? loff : loff - 1;   // the infrared tables have no term 0
-    for (int l = 1; l <= nleg; l++) pc[l] = lerp4(plane(2 + l + t0, kd) + r0, Z.L, R);
-    return true;
+    // FP32 lookups read the tables' FP32 copy
+    if constexpr (std::is_same<S, float>::value)
+      if (Z.zf)
+        return cloud_optics_chan<S, float>(C, microwave, type, reff, temp, nleg, loff, ke, w, pc, Z.zf + Z.ch, Z.L);
+    return cloud_optics_chan<S, double>(C, microwave, type, reff, temp, nleg, loff, ke, w, pc, Z.z + Z.ch, Z.L);
   }
   if (!microwave) {
     // density slot of Get_Cloud_Opt_IR: liquid 1, snow 2, graupel 3, ice/hail 4
@@ -1116,7 +1128,11 @@ CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const Stre
     for (int l = 0; l <= nleg; l++) P[i][l] = S(St.P[i][l]);
   }
   phase_blocks<NZ, S>(St.nS, St.nZ, nleg, pcs, P, wt, ff, bb);
-  const S B = in.c1 / (exp(in.c2 / (in.b1 + in.b2 * tk)) - 1.0);
+  S B;
+  if constexpr (std::is_same<S, float>::value)   // the layer's Planck radiance in the solver's precision
+    B = float(in.c1) / (expf(float(in.c2) / (float(in.b1) + float(in.b2) * tk)) - 1.0f);
+  else
+    B = in.c1 / (exp(in.c2 / (in.b1 + in.b2 * tk)) - 1.0);
   if (in.soi) {   // SOI: doubling, then the direct beam taken out of the diagonal
     soi_doubling<NZ, S>(ssa < 0.8 && od < 4.0, St.nS, St.nZ, ssa, od, mu, wt, ff, bb, B, Td, Rd, srcd);
     for (int i = 0; i < St.nZ; i++) Td.a[i][i] -= exp(-od / mu[i]);
