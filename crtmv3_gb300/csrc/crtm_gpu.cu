@@ -169,7 +169,6 @@ struct Sensor {
   // the cloud tables interpolated to the processed channels' frequencies
   // (CloudChan layout; built when the handle has a CloudCoeff table)
   double* d_zc = nullptr;
-  float* d_zcf = nullptr;   // the same in FP32 (the mixed form's FP32 lookups)
 };
 
 // The OPTRAN tables of the processed channels (file positions `pos`; all
@@ -474,16 +473,15 @@ bool upload_channels(Sensor& s, const std::vector<int>& pos, std::string& err) {
 
 void free_sensor(Sensor& s) {
   cudaFree(s.d_C); cudaFree(s.d_cmask); cudaFree(s.d_tab); cudaFree(s.d_spec);
-  cudaFree(s.d_oidx); cudaFree(s.d_och); cudaFree(s.d_ocoef); cudaFree(s.d_zc); cudaFree(s.d_zcf);
+  cudaFree(s.d_oidx); cudaFree(s.d_och); cudaFree(s.d_ocoef); cudaFree(s.d_zc);
   s.d_C = nullptr; s.d_cmask = nullptr; s.d_tab = nullptr; s.d_spec = nullptr;
-  s.d_oidx = nullptr; s.d_och = nullptr; s.d_ocoef = nullptr; s.d_zc = nullptr; s.d_zcf = nullptr;
+  s.d_oidx = nullptr; s.d_och = nullptr; s.d_ocoef = nullptr; s.d_zc = nullptr;
 }
 
 // The cloud tables at each processed channel's frequency (CloudChan layout):
 // one thread per (plane, radius row, channel), the frequency step of the
 // lookups' 4-point Lagrange interpolation.
-__global__ void cloud_chan_kernel(CloudLut C, int microwave, const double* freq, int L, long long n, double* z,
-                                  float* zf) {
+__global__ void cloud_chan_kernel(CloudLut C, int microwave, const double* freq, int L, long long n, double* z) {
   const int rows = microwave ? C.nrm : C.nri, nf = microwave ? C.nfm : C.nfi;
   const double* fax = microwave ? C.f_mw : C.f_ir;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -492,7 +490,6 @@ __global__ void cloud_chan_kernel(CloudLut C, int microwave, const double* freq,
     const int r = (int)(qr % rows), q = (int)(qr / rows);
     const Lagrange4 U = lagrange4(fax, nf, freq[ch]);
     z[i] = lerp4(cloud_chan_source(C, microwave != 0, q) + (size_t)r * nf + U.i0, 1, U);
-    zf[i] = float(z[i]);
   }
 }
 
@@ -500,26 +497,20 @@ __global__ void cloud_chan_kernel(CloudLut C, int microwave, const double* freq,
 // channels; none without a cloud table or channels.
 bool build_cloud_chan(const CloudLut& C, bool has_clouds, Sensor& s, std::string& err) {
   cudaFree(s.d_zc);
-  cudaFree(s.d_zcf);
   s.d_zc = nullptr;
-  s.d_zcf = nullptr;
   if (!has_clouds || s.L <= 0) return true;
   const bool mw = s.sensor_type == 1;
   const long long n = (long long)cloud_chan_planes(C, mw) * (mw ? C.nrm : C.nri) * s.L;
   cudaError_t ce = cudaMalloc(&s.d_zc, (size_t)n * sizeof(double));
-  if (ce == cudaSuccess) ce = cudaMalloc(&s.d_zcf, (size_t)n * sizeof(float));
   if (ce == cudaSuccess) {
     const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
-    cloud_chan_kernel<<<(unsigned)blocks, 256>>>(C, mw ? 1 : 0, mw ? s.spec.freq : s.spec.wn, s.L, n, s.d_zc,
-                                                 s.d_zcf);
+    cloud_chan_kernel<<<(unsigned)blocks, 256>>>(C, mw ? 1 : 0, mw ? s.spec.freq : s.spec.wn, s.L, n, s.d_zc);
     ce = cudaGetLastError();
     if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
   }
   if (ce != cudaSuccess) {
     cudaFree(s.d_zc);
-    cudaFree(s.d_zcf);
     s.d_zc = nullptr;
-    s.d_zcf = nullptr;
     err = std::string("channel cloud tables: ") + cudaGetErrorString(ce);
     return false;
   }
@@ -1221,7 +1212,7 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
       ScatterArgs<R> sa{};
       sa.K = K; sa.L = L; sa.Kmax = Kmax; sa.p_begin = p0; sa.n_chunk = n;
       sa.microwave = s.sensor_type == 1;
-      sa.b = bv; sa.sp = s.spec; sa.pv = w.pv; sa.lut = h->lut; sa.lut_chan = s.d_zc; sa.lut_chanf = s.d_zcf;
+      sa.b = bv; sa.sp = s.spec; sa.pv = w.pv; sa.lut = h->lut; sa.lut_chan = s.d_zc;
       sa.max_clouds = b->max_clouds; sa.n_clouds = b->n_clouds; sa.cloud_type = b->cloud_type;
       sa.wc = b->cloud_water_content; sa.reff = b->cloud_effective_radius; sa.n_streams = b->n_streams;
       sa.rt_algorithm = b->rt_algorithm_id; sa.FB = w.FB; sa.FS = w.FS; sa.soi_slots = sw.soi_slots;

@@ -644,11 +644,8 @@ CRTM_HD int layer_adjoint_in(const CloudyColumn& in, const CloudLut& lut, const 
       *in_fp64 = true;
       return 0;
     }
-    T B;
-    if constexpr (fp32)
-      B = float(in.c1) / (expf(float(in.c2) / (float(in.b1) + float(in.b2) * float(in.temperature[k]))) - 1.0f);
-    else
-      B = in.c1 / (exp(in.c2 / (in.b1 + in.b2 * in.temperature[k])) - 1.0);
+    const double te = in.b1 + in.b2 * in.temperature[k];
+    const T B = T(in.c1 / (exp(in.c2 / te) - 1.0));
     Mat<NZ, T> Tb, Rb, ffb, bbb;
     T sb[NZ];
     for (int i = 0; i < nZ; i++) {

@@ -66,7 +66,6 @@ struct ScatterArgs {
   PrepView<R> pv;
   CloudLut lut;
   const double* lut_chan;   // the sensor's channel-interpolated cloud tables (CloudChan; null: none)
-  const float* lut_chanf;   // their FP32 copy
   int max_clouds;
   const int* n_clouds;          // [P]
   const int* cloud_type;        // [P][NC]
@@ -217,7 +216,6 @@ __device__ __forceinline__ CloudyColumn column_inputs(const ScatterArgs<R>& a, i
   c.alut = &a.alut;
   c.cf = a.cloud_fraction && c.n_clouds > 0 ? a.cloud_fraction + (size_t)gp * a.Kmax : nullptr;
   c.zc.z = a.lut_chan;
-  c.zc.zf = a.lut_chanf;
   c.zc.L = (size_t)a.L;
   c.zc.ch = l;
   const double tcc = a.cover[p];

@@ -186,7 +186,6 @@ CRTM_HD S lerp4x4x4(const double* z, int nu, int nv, const Lagrange4& U, const L
 // A null z: the lookups interpolate in frequency themselves.
 struct CloudChan {
   const double* z = nullptr;
-  const float* zf = nullptr;   // the same tables in FP32 (the FP32 lookups'), or null
   size_t L = 0;
   int ch = 0;
 };
@@ -288,13 +287,7 @@ CRTM_HD bool cloud_layer_optics(const CloudLut& C, bool microwave, double freq, 
                                 S temp, int nleg, int loff, S* ke, S* w, S* pc, const CloudChan& Z = CloudChan()) {
   for (int l = 0; l <= nleg; l++) pc[l] = S(0.0);
   *w = S(0.0);
-  if (Z.z) {
-    // FP32 lookups read the tables' FP32 copy
-    if constexpr (std::is_same<S, float>::value)
-      if (Z.zf)
-        return cloud_optics_chan<S, float>(C, microwave, type, reff, temp, nleg, loff, ke, w, pc, Z.zf + Z.ch, Z.L);
-    return cloud_optics_chan<S, double>(C, microwave, type, reff, temp, nleg, loff, ke, w, pc, Z.z + Z.ch, Z.L);
-  }
+  if (Z.z) return cloud_optics_chan<S, double>(C, microwave, type, reff, temp, nleg, loff, ke, w, pc, Z.z + Z.ch, Z.L);
   if (!microwave) {
     // density slot of Get_Cloud_Opt_IR: liquid 1, snow 2, graupel 3, ice/hail 4
     const int kd = (type == 1 || type == 3) ? 0 : (type == 4 ? 1 : (type == 5 ? 2 : (type == 2 || type == 6 ? 3 : -1)));
@@ -1128,11 +1121,7 @@ CRTM_HD int layer_optics(const CloudyColumn& in, const CloudLut& lut, const Stre
     for (int l = 0; l <= nleg; l++) P[i][l] = S(St.P[i][l]);
   }
   phase_blocks<NZ, S>(St.nS, St.nZ, nleg, pcs, P, wt, ff, bb);
-  S B;
-  if constexpr (std::is_same<S, float>::value)   // the layer's Planck radiance in the solver's precision
-    B = float(in.c1) / (expf(float(in.c2) / (float(in.b1) + float(in.b2) * tk)) - 1.0f);
-  else
-    B = in.c1 / (exp(in.c2 / (in.b1 + in.b2 * tk)) - 1.0);
+  const S B = in.c1 / (exp(in.c2 / (in.b1 + in.b2 * tk)) - 1.0);
   if (in.soi) {   // SOI: doubling, then the direct beam taken out of the diagonal
     soi_doubling<NZ, S>(ssa < 0.8 && od < 4.0, St.nS, St.nZ, ssa, od, mu, wt, ff, bb, B, Td, Rd, srcd);
     for (int i = 0; i < St.nZ; i++) Td.a[i][i] -= exp(-od / mu[i]);
@@ -1236,12 +1225,23 @@ struct AddingState {
   A rad[NZ];
 };
 
-// Gamma = G^-1 in place, the elimination in FP64 whatever A is.
+// Gamma = G^-1 in place for G = I - Rup R.  In FP32, where the coupling is
+// weak (||I - G||_inf < 1/2, so cond(G) < 3 and FP32 elimination keeps ~1e-7
+// relative) the elimination runs in FP32; otherwise in FP64 (thick, nearly
+// conservative layers over a reflecting column, where G nears singular).
+constexpr double ADDING_FP32_COUPLING = 0.5;
 template <int NZ, class A>
 CRTM_HD bool invert_fp64(int n, Mat<NZ, A>& G) {
   if constexpr (sizeof(A) == sizeof(double)) {
     return mat_invert<NZ, A>(n, G);
   } else {
+    A cpl = A(0.0);
+    for (int i = 0; i < n; i++) {
+      A r = A(0.0);
+      for (int j = 0; j < n; j++) r += fabs((i == j ? A(1.0) : A(0.0)) - G.a[i][j]);
+      cpl = r > cpl ? r : cpl;
+    }
+    if (cpl < A(ADDING_FP32_COUPLING)) return mat_invert<NZ, A>(n, G);
     Mat<NZ, double> D;
     for (int i = 0; i < n; i++)
       for (int j = 0; j < n; j++) D.a[i][j] = double(G.a[i][j]);

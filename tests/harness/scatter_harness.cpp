@@ -598,7 +598,7 @@ extern "C" double sx_cloud_chan_compare(const int* dims, const double* f_mw, con
             re.d[0] = 1.0;
             tk.d[1] = 1.0;
             D ke0, w0, pc0[SC_NLEG_MAX + 1], ke1, w1, pc1[SC_NLEG_MAX + 1];
-            const CloudChan Z{z.data(), nullptr, (size_t)L, ch};
+            const CloudChan Z{z.data(), (size_t)L, ch};
             const bool ok0 = cloud_layer_optics<D>(C, mw, freq[ch], type, re, tk, nleg, loff, &ke0, &w0, pc0);
             const bool ok1 = cloud_layer_optics<D>(CR, mw, freq[ch], type, re, tk, nleg, loff, &ke1, &w1, pc1, Z);
             if (ok0 != ok1) return 1e300;
@@ -614,53 +614,3 @@ extern "C" double sx_cloud_chan_compare(const int* dims, const double* f_mw, con
   return worst;
 }
 
-
-// The FP32 lookups through the tables' FP32 copy against the same lookups
-// through the FP64 tables (values rounded to FP32 at the end): the largest
-// relative difference over the channels, cloud types, radii, temperatures and
-// stream sets given.
-extern "C" double sx_cloud_chan_f32_compare(const int* dims, const double* f_mw, const double* r_mw,
-                                            const double* t, const double* f_ir, const double* r_ir,
-                                            const double* ke_l, const double* w_l, const double* pc_l,
-                                            const double* ke_s, const double* w_s, const double* pc_s,
-                                            const double* ke_ir, const double* w_ir, const double* pc_ir,
-                                            int microwave, int L, const double* freq, int n_re,
-                                            const double* re_grid, int n_t, const double* t_grid) {
-  CloudLut C{dims[0], dims[1], dims[2], dims[3], dims[4], dims[5], dims[6], f_mw, r_mw, t, f_ir, r_ir,
-             ke_l, w_l, pc_l, ke_s, w_s, pc_s, ke_ir, w_ir, pc_ir};
-  const bool mw = microwave != 0;
-  const int rows = mw ? C.nrm : C.nri, nf = mw ? C.nfm : C.nfi;
-  const long long n = (long long)cloud_chan_planes(C, mw) * rows * L;
-  std::vector<double> z((size_t)n);
-  std::vector<float> zf((size_t)n);
-  for (long long i = 0; i < n; i++) {
-    const int ch = (int)(i % L);
-    const long long qr = i / L;
-    const int r = (int)(qr % rows), q = (int)(qr / rows);
-    const Lagrange4 U = lagrange4(mw ? C.f_mw : C.f_ir, nf, freq[ch]);
-    z[(size_t)i] = lerp4(cloud_chan_source(C, mw, q) + (size_t)r * nf + U.i0, 1, U);
-    zf[(size_t)i] = float(z[(size_t)i]);
-  }
-  double worst = 0.0;
-  const int nlegs[5] = {2, 4, 6, 8, 16};
-  for (int ch = 0; ch < L; ch++)
-    for (int type = 1; type <= 6; type++)
-      for (int a = 0; a < n_re; a++)
-        for (int b = 0; b < n_t; b++)
-          for (int q = 0; q < 5; q++) {
-            const int nleg = nlegs[q], loff = legendre_offset(nleg);
-            if (nleg + loff > C.nleg) continue;
-            float ke0, w0, pc0[SC_NLEG_MAX + 1], ke1, w1, pc1[SC_NLEG_MAX + 1];
-            const CloudChan Z64{z.data(), nullptr, (size_t)L, ch}, Z32{z.data(), zf.data(), (size_t)L, ch};
-            const float re = float(re_grid[a]), tk = float(t_grid[b]);
-            if (!cloud_layer_optics<float>(C, mw, freq[ch], type, re, tk, nleg, loff, &ke0, &w0, pc0, Z64)) continue;
-            cloud_layer_optics<float>(C, mw, freq[ch], type, re, tk, nleg, loff, &ke1, &w1, pc1, Z32);
-            auto cmp = [&](float x, float y, float scale) {
-              worst = std::max(worst, std::fabs(double(x) - double(y)) / std::max(std::fabs(double(scale)), 1e-30));
-            };
-            cmp(ke1, ke0, ke0);
-            cmp(w1, w0, 1.0f);
-            for (int l = 0; l <= nleg; l++) cmp(pc1[l], pc0[l], 1.0f);
-          }
-  return worst;
-}
