@@ -597,6 +597,10 @@ def run_scattering(args, torch, dev, rank, world, dist):
     st = h.stage_times(reset=True)
     h.set_profiling(False)
     launches = h.launch_count() - launches0
+    # a device entry point reports failed profiles in its status words only
+    bad = sum(int((c["out"]["status"] != 0).sum()) for c in calls)
+    if bad:
+        raise RuntimeError(f"{bad} profiles failed in the timed mixed-form steps (status words)")
     mixed_sample = sample_out()
     bt_err, field_err = 0.0, {}
     for c, r in zip(calls, ref):
@@ -611,6 +615,9 @@ def run_scattering(args, torch, dev, rank, world, dist):
     jac_err = max(field_err.values()) if field_err else 0.0
     fp64_steps = max(1, min(args.steps, 2))
     ms_fp64 = timed(0, fp64_steps)
+    bad = sum(int((c["out"]["status"] != 0).sum()) for c in calls)
+    if bad:
+        raise RuntimeError(f"{bad} profiles failed in the timed FP64-form steps (status words)")
     pc = sum(c["pc"] for c in calls) * world
     per_mixed, per_fp64 = ms_mixed / args.steps, ms_fp64 / fp64_steps
     value, fp64_value = pc / (per_mixed * 1e-3), pc / (per_fp64 * 1e-3)

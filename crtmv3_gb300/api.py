@@ -190,6 +190,10 @@ def library() -> ct.CDLL:
     L.crtm_gpu_adjoint_device.argtypes = [ct.c_void_p, ct.c_int, ct.POINTER(CBatch), ct.c_void_p,
                                           ct.POINTER(CAdjoint), ct.POINTER(CRTSolution), ct.c_void_p]
     L.crtm_gpu_k_matrix_device_static.argtypes = L.crtm_gpu_k_matrix_device.argtypes
+    L.crtm_gpu_linearize.argtypes = [ct.c_void_p, ct.c_int, ct.POINTER(CBatch), ct.POINTER(CRTSolution),
+                                     ct.c_void_p]
+    L.crtm_gpu_tangent_linear_apply.argtypes = [ct.c_void_p, ct.POINTER(CTLIn), ct.c_void_p, ct.c_void_p]
+    L.crtm_gpu_adjoint_apply.argtypes = [ct.c_void_p, ct.c_void_p, ct.POINTER(CAdjoint), ct.c_void_p]
     L.crtm_gpu_get_tuning.argtypes = [ct.c_void_p, ct.c_int, ct.c_int, ct.POINTER(CTuning)]
     L.crtm_gpu_set_tuning.argtypes = [ct.c_void_p, ct.c_int, ct.c_int, ct.POINTER(CTuning)]
     L.crtm_gpu_autotune_k_matrix_device.argtypes = L.crtm_gpu_k_matrix_device.argtypes + [
@@ -557,6 +561,30 @@ class CRTM:
             setattr(ca, f, _addr(out.get(f + "_ad")))
         self._check(library().crtm_gpu_adjoint_device(self.h, sensor, ct.byref(b), seed.data_ptr(),
                                                       ct.byref(ca), ct.byref(cr), stream))
+
+
+    # -- a trajectory for variational inner loops (no reference counterpart) --
+    def linearize_device(self, b: CBatch, out: dict, sensor: int = 0, stream=None) -> None:
+        """crtm_gpu_linearize: the trajectory's forward (out: radiance, bt,
+        status) and its K-matrix, kept by the handle for the apply calls."""
+        cr = _crts_device(out)
+        self._check(library().crtm_gpu_linearize(self.h, sensor, ct.byref(b), ct.byref(cr), stream))
+
+    def tangent_linear_apply_device(self, tl: dict, bt_tl, stream=None) -> None:
+        """crtm_gpu_tangent_linear_apply: bt_tl (P, L) from the perturbations in
+        ``tl`` (device tensors under TL_FIELDS names) about the trajectory."""
+        ctl = CTLIn(*[_addr(tl.get(f)) for f in TL_FIELDS])
+        self._check(library().crtm_gpu_tangent_linear_apply(self.h, ct.byref(ctl), bt_tl.data_ptr(), stream))
+
+    def adjoint_apply_device(self, seed, out: dict, stream=None) -> None:
+        """crtm_gpu_adjoint_apply: the adjoint outputs (``out`` as
+        adjoint_device's: temperature_ad, absorber_ad, water_temperature_ad and
+        any scattering / surface / scheme ``*_ad``) for the seed (P, L)."""
+        ca = CAdjoint(out["temperature_ad"].data_ptr(), out["absorber_ad"].data_ptr(),
+                      out["water_temperature_ad"].data_ptr(), *[_addr(out.get(f + "_ad")) for f in SCATTER_JACOBIANS])
+        for f in SURFACE_COVERS + SCHEME_JACOBIANS:
+            setattr(ca, f, _addr(out.get(f + "_ad")))
+        self._check(library().crtm_gpu_adjoint_apply(self.h, seed.data_ptr(), ct.byref(ca), stream))
 
 
 # ---------------------------------------------------------------------------

@@ -696,6 +696,16 @@ struct crtm_gpu_context {
   DevBuf io_in, io_out;  // device copies for the host entry points
   DevBuf io_tl;          // tangent-linear inputs of the host entry point
   DevBuf tl_k;           // tangent linear: the K-matrix it contracts
+  // the trajectory of crtm_gpu_linearize (its K-matrix in tl_k, the profiles'
+  // layer counts and status in lin_meta)
+  struct {
+    bool valid = false;
+    int sensor = -1, P = 0, L = 0, Km = 0, J = 0, NC = 0, NA = 0;
+    crtm_gpu_kmatrix k{};
+    int* n_layers = nullptr;
+    int* status = nullptr;
+  } lin;
+  DevBuf lin_meta;
   DevBuf small;     // idx maps
   // cloud LUT (CloudCoeff.bin), when present
   bool has_clouds = false;
@@ -1888,27 +1898,40 @@ __global__ void tl_kernel(TLArgs a) {
   a.bt_tl[pl] = (a.status && a.status[p]) ? 0.0 : s;
 }
 
-int tl_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm_gpu_tl_in* tl,
-              crtm_gpu_rtsolution* rts, double* bt_tl, cudaStream_t st) {
+// The trajectory's K-matrix into the handle's scratch: every Jacobian the
+// batch has (want == NULL), or those of the perturbations `want` gives; the
+// profiles' layer counts and status words beside it.  Enqueued on st.
+int linearize(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, crtm_gpu_rtsolution* rts,
+              const crtm_gpu_tl_in* want, cudaStream_t st) {
   if (!h) return CRTM_GPU_FAILURE;
-  if (!tl || !bt_tl) return fail(h, "missing tangent-linear inputs or output");
+  h->lin.valid = false;
   if (sensor < 0 || sensor >= (int)h->sensors.size()) return fail(h, "sensor index %d out of range", sensor);
   if (!b || b->n_profiles < 0 || b->max_layers < 1) return fail(h, "bad batch dimensions");
+  if (!rts || !rts->radiance || !rts->brightness_temperature) return fail(h, "missing RTSolution buffers");
   const size_t P = b->n_profiles, L = h->sensors[sensor].L, Km = b->max_layers, J = b->n_absorbers;
   const size_t NC = b->max_clouds > 0 ? b->max_clouds : 0, NA = b->max_aerosols > 0 ? b->max_aerosols : 0;
-  if (P == 0 || L == 0) return CRTM_GPU_SUCCESS;
-  const bool wc = NC && (tl->cloud_water_content || tl->cloud_effective_radius);
-  const bool cf = NC && tl->cloud_fraction;
-  const bool aer = NA && (tl->aerosol_concentration || tl->aerosol_effective_radius);
-  const bool av = NA && tl->aerosol_effective_variance, rh = NA && tl->relative_humidity;
-  const bool ws = tl->wind_speed && !b->emissivity;   // the emissivity model's wind speed
+  const bool wc = NC && (!want || want->cloud_water_content || want->cloud_effective_radius);
+  const bool cf = NC && (!want || want->cloud_fraction);
+  const bool aer = NA && (!want || want->aerosol_concentration || want->aerosol_effective_radius);
+  const bool av = NA && (!want || want->aerosol_effective_variance);
+  const bool rh = NA && (!want || want->relative_humidity);
+  const bool ws = !b->emissivity && (!want || want->wind_speed);   // the emissivity model's wind speed
   const size_t PL = P * L;
   const size_t n_el = PL * Km * (1 + J) + 5 * PL + (wc ? 2 * PL * NC * Km : 0) + (cf ? PL * Km : 0) +
                       (aer ? 2 * PL * NA * Km : 0) + (av ? PL * NA * Km : 0) + (rh ? PL * Km : 0) +
                       (ws ? PL : 0);
   if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
-  if (!h->tl_k.ensure(n_el * sizeof(double)))
-    return fail(h, "cannot allocate %zu bytes for the tangent linear's K-matrix", n_el * sizeof(double));
+  if (!h->tl_k.ensure(std::max<size_t>(n_el, 1) * sizeof(double)))
+    return fail(h, "cannot allocate %zu bytes for the trajectory's K-matrix", n_el * sizeof(double));
+  if (!h->lin_meta.ensure(std::max<size_t>(2 * P, 1) * sizeof(int)))
+    return fail(h, "cannot allocate the trajectory's profile table");
+  if (P == 0 || L == 0) {
+    h->lin = {};
+    h->lin.valid = true;
+    h->lin.sensor = sensor;
+    h->lin.P = (int)P; h->lin.L = (int)L; h->lin.Km = (int)Km; h->lin.J = (int)J;
+    return CRTM_GPU_SUCCESS;
+  }
   double* q = (double*)h->tl_k.p;
   auto take = [&](size_t n) { double* r = q; q += n; return r; };
   crtm_gpu_kmatrix kk{};
@@ -1926,19 +1949,127 @@ int tl_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm
   if (rh) kk.relative_humidity = take(PL * Km);
   if (ws) kk.wind_speed = take(PL);
   if (int rc = dispatch(h, sensor, b, 1, nullptr, rts, &kk, nullptr, st)) return rc;
+  int* meta = (int*)h->lin_meta.p;
+  if (cudaMemcpyAsync(meta, b->n_layers, P * sizeof(int), cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+      (rts->status ? cudaMemcpyAsync(meta + P, rts->status, P * sizeof(int), cudaMemcpyDeviceToDevice, st)
+                   : cudaMemsetAsync(meta + P, 0, P * sizeof(int), st)) != cudaSuccess)
+    return fail(h, "trajectory profile table copy failed");
+  h->lin.valid = true;
+  h->lin.sensor = sensor;
+  h->lin.P = (int)P; h->lin.L = (int)L; h->lin.Km = (int)Km; h->lin.J = (int)J;
+  h->lin.NC = (int)NC; h->lin.NA = (int)NA;
+  h->lin.k = kk;
+  h->lin.n_layers = meta;
+  h->lin.status = meta + P;
+  mark_done(h, st);
+  return CRTM_GPU_SUCCESS;
+}
+
+// The tangent linear about the stored trajectory: bt_tl [P][L] from the
+// perturbations tl (device pointers), one read of the stored Jacobians.
+int tl_apply(crtm_gpu_handle h, const crtm_gpu_tl_in* tl, double* bt_tl, cudaStream_t st) {
+  if (!h) return CRTM_GPU_FAILURE;
+  if (!h->lin.valid) return fail(h, "no trajectory: call crtm_gpu_linearize first");
+  if (!tl || !bt_tl) return fail(h, "missing tangent-linear inputs or output");
+  const auto& g = h->lin;
+  auto need = [&](const double* d, const double* k, const char* what) {
+    return d && !k ? fail(h, "the trajectory holds no %s Jacobian", what) : CRTM_GPU_SUCCESS;
+  };
+  if (int rc = need(tl->cloud_water_content, g.k.cloud_water_content, "cloud water content")) return rc;
+  if (int rc = need(tl->cloud_effective_radius, g.k.cloud_effective_radius, "cloud effective radius")) return rc;
+  if (int rc = need(tl->cloud_fraction, g.k.cloud_fraction, "cloud fraction")) return rc;
+  if (int rc = need(tl->aerosol_concentration, g.k.aerosol_concentration, "aerosol concentration")) return rc;
+  if (int rc = need(tl->aerosol_effective_radius, g.k.aerosol_effective_radius, "aerosol radius")) return rc;
+  if (int rc = need(tl->aerosol_effective_variance, g.k.aerosol_effective_variance, "effective variance")) return rc;
+  if (int rc = need(tl->relative_humidity, g.k.relative_humidity, "relative humidity")) return rc;
+  if (g.P == 0 || g.L == 0) return CRTM_GPU_SUCCESS;
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
+  order_after_previous(h, st);
   TLArgs ta{};
-  ta.P = (int)P; ta.L = (int)L; ta.Km = (int)Km; ta.J = (int)J; ta.NC = (int)NC; ta.NA = (int)NA;
-  ta.n_layers = b->n_layers; ta.status = rts->status; ta.d = *tl; ta.bt_tl = bt_tl;
-  ta.kt = kk.temperature; ta.ka = kk.absorber; ta.kw = kk.water_temperature; ta.kl = kk.land_temperature;
-  ta.ks = kk.snow_temperature; ta.ki = kk.ice_temperature; ta.ke = kk.surface_emissivity;
-  ta.kwc = kk.cloud_water_content; ta.kre = kk.cloud_effective_radius; ta.kcf = kk.cloud_fraction;
-  ta.kac = kk.aerosol_concentration; ta.kar = kk.aerosol_effective_radius;
-  ta.kav = kk.aerosol_effective_variance; ta.krh = kk.relative_humidity; ta.kws = kk.wind_speed;
-  const long long threads = (long long)PL * 32;
+  ta.P = g.P; ta.L = g.L; ta.Km = g.Km; ta.J = g.J; ta.NC = g.NC; ta.NA = g.NA;
+  ta.n_layers = g.n_layers; ta.status = g.status; ta.d = *tl; ta.bt_tl = bt_tl;
+  ta.kt = g.k.temperature; ta.ka = g.k.absorber; ta.kw = g.k.water_temperature; ta.kl = g.k.land_temperature;
+  ta.ks = g.k.snow_temperature; ta.ki = g.k.ice_temperature; ta.ke = g.k.surface_emissivity;
+  ta.kwc = g.k.cloud_water_content; ta.kre = g.k.cloud_effective_radius; ta.kcf = g.k.cloud_fraction;
+  ta.kac = g.k.aerosol_concentration; ta.kar = g.k.aerosol_effective_radius;
+  ta.kav = g.k.aerosol_effective_variance; ta.krh = g.k.relative_humidity; ta.kws = g.k.wind_speed;
+  const long long threads = (long long)g.P * g.L * 32;
   tl_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(ta);
   CK_LAUNCH(h);
   mark_done(h, st);
   return CRTM_GPU_SUCCESS;
+}
+
+// out[p][j] = sum_l w[p][l] K[p][l][j] (j over a block's rows x layers), zero
+// for profiles whose trajectory status is not 0: one thread per (p, j), the
+// channels' rows read coalesced across j.
+__global__ void channel_contract_kernel(const double* __restrict__ K, int P, int L, int rowlen,
+                                        const double* __restrict__ w, const int* __restrict__ status,
+                                        double* __restrict__ out) {
+  const int p = blockIdx.y;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P || j >= rowlen) return;
+  double acc = 0.0;
+  if (!status[p]) {
+    const double* kp = K + (size_t)p * L * rowlen + j;
+    const double* wp = w + (size_t)p * L;
+    for (int l = 0; l < L; l++) acc += wp[l] * kp[(size_t)l * rowlen];
+  }
+  out[(size_t)p * rowlen + j] = acc;
+}
+
+// The adjoint about the stored trajectory: the outputs of CRTM_Adjoint for
+// the seed bt_ad [P][L] (device pointers), one read of the stored Jacobians.
+int ad_apply(crtm_gpu_handle h, const double* bt_ad, crtm_gpu_adjoint_out* ad, cudaStream_t st) {
+  if (!h) return CRTM_GPU_FAILURE;
+  if (!h->lin.valid) return fail(h, "no trajectory: call crtm_gpu_linearize first");
+  if (!bt_ad || !ad || !ad->temperature || !ad->absorber || !ad->water_temperature)
+    return fail(h, "missing adjoint seed or outputs");
+  const auto& g = h->lin;
+  if (g.P == 0) return CRTM_GPU_SUCCESS;
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, "cudaSetDevice failed");
+  order_after_previous(h, st);
+  const int Km = g.Km;
+  struct Block { const double* k; double* out; int rowlen; const char* what; };
+  const Block blocks[] = {
+      {g.k.temperature, ad->temperature, Km, "temperature"},
+      {g.k.absorber, ad->absorber, g.J * Km, "absorber"},
+      {g.k.water_temperature, ad->water_temperature, 1, "water temperature"},
+      {g.k.land_temperature, ad->land_temperature, 1, "land temperature"},
+      {g.k.snow_temperature, ad->snow_temperature, 1, "snow temperature"},
+      {g.k.ice_temperature, ad->ice_temperature, 1, "ice temperature"},
+      {g.k.cloud_water_content, ad->cloud_water_content, g.NC * Km, "cloud water content"},
+      {g.k.cloud_effective_radius, ad->cloud_effective_radius, g.NC * Km, "cloud effective radius"},
+      {g.k.cloud_fraction, ad->cloud_fraction, Km, "cloud fraction"},
+      {g.k.aerosol_concentration, ad->aerosol_concentration, g.NA * Km, "aerosol concentration"},
+      {g.k.aerosol_effective_radius, ad->aerosol_effective_radius, g.NA * Km, "aerosol radius"},
+      {g.k.aerosol_effective_variance, ad->aerosol_effective_variance, g.NA * Km, "effective variance"},
+      {g.k.relative_humidity, ad->relative_humidity, Km, "relative humidity"},
+      {g.k.wind_speed, ad->wind_speed, 1, "wind speed"},
+  };
+  for (const Block& x : blocks) {
+    if (!x.out) continue;
+    if (!x.k) return fail(h, "the trajectory holds no %s Jacobian", x.what);
+    if (x.rowlen <= 0) continue;
+    if (g.L == 0) {
+      if (cudaMemsetAsync(x.out, 0, (size_t)g.P * x.rowlen * sizeof(double), st) != cudaSuccess)
+        return fail(h, "cudaMemsetAsync failed");
+      continue;
+    }
+    const dim3 grid((unsigned)((x.rowlen + 127) / 128), (unsigned)g.P);
+    channel_contract_kernel<<<grid, 128, 0, st>>>(x.k, g.P, g.L, x.rowlen, bt_ad, g.status, x.out);
+    CK_LAUNCH(h);
+  }
+  mark_done(h, st);
+  return CRTM_GPU_SUCCESS;
+}
+
+int tl_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm_gpu_tl_in* tl,
+              crtm_gpu_rtsolution* rts, double* bt_tl, cudaStream_t st) {
+  if (!h) return CRTM_GPU_FAILURE;
+  if (!tl || !bt_tl) return fail(h, "missing tangent-linear inputs or output");
+  if (int rc = linearize(h, sensor, b, rts, tl, st)) return rc;
+  return tl_apply(h, tl, bt_tl, st);
 }
 
 int tl_host(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, const crtm_gpu_tl_in* tl,
@@ -2316,6 +2447,19 @@ int crtm_gpu_tangent_linear_device(crtm_gpu_handle h, int sensor, const crtm_gpu
                                    void* stream) {
   if (!rts || !rts->radiance || !rts->brightness_temperature) return fail(h, "missing RTSolution buffers");
   return tl_device(h, sensor, b, tl, rts, bt_tl, (cudaStream_t)stream);
+}
+
+int crtm_gpu_linearize(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b, crtm_gpu_rtsolution* rts,
+                       void* stream) {
+  return linearize(h, sensor, b, rts, nullptr, (cudaStream_t)stream);
+}
+
+int crtm_gpu_tangent_linear_apply(crtm_gpu_handle h, const crtm_gpu_tl_in* tl, double* bt_tl, void* stream) {
+  return tl_apply(h, tl, bt_tl, (cudaStream_t)stream);
+}
+
+int crtm_gpu_adjoint_apply(crtm_gpu_handle h, const double* bt_ad, crtm_gpu_adjoint_out* ad, void* stream) {
+  return ad_apply(h, bt_ad, ad, (cudaStream_t)stream);
 }
 
 int crtm_gpu_forward_device(crtm_gpu_handle h, int sensor, const crtm_gpu_batch* b,

@@ -357,6 +357,28 @@ int crtm_gpu_tangent_linear_device(crtm_gpu_handle handle, int sensor, const crt
                                    const crtm_gpu_tl_in* tl, crtm_gpu_rtsolution* rts, double* bt_tl,
                                    void* stream);
 
+/* No counterpart in the reference (CRTM_Tangent_Linear and CRTM_Adjoint run
+ * the forward model again on every call).  A variational inner loop applies
+ * the tangent linear and the adjoint many times about one trajectory:
+ * crtm_gpu_linearize evaluates the trajectory's forward (rts) and its
+ * K-matrix once, for every input the batch has, into device memory owned by
+ * the handle (device buffers, enqueued on `stream`); then
+ * crtm_gpu_tangent_linear_apply gives bt_tl [P][L] for perturbations tl, and
+ * crtm_gpu_adjoint_apply the outputs of CRTM_Adjoint for a seed bt_ad [P][L],
+ * each as one contraction with the stored Jacobians (the same numbers as
+ * crtm_gpu_tangent_linear / crtm_gpu_adjoint about that trajectory, to
+ * rounding).  All pointers are device pointers; tl and ad have the
+ * trajectory batch's shapes.  A later linearize or tangent-linear call
+ * replaces the trajectory; profiles whose trajectory status was not 0 give 0.
+ * The apply calls fail when they ask for a Jacobian the trajectory does not
+ * hold (for example cloud perturbations of a batch without clouds). */
+int crtm_gpu_linearize(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* batch,
+                       crtm_gpu_rtsolution* rts, void* stream);
+int crtm_gpu_tangent_linear_apply(crtm_gpu_handle handle, const crtm_gpu_tl_in* tl, double* bt_tl,
+                                  void* stream);
+int crtm_gpu_adjoint_apply(crtm_gpu_handle handle, const double* bt_ad, crtm_gpu_adjoint_out* ad,
+                           void* stream);
+
 /* No counterpart in the reference (CRTM_K_Matrix allocates its work arrays on
  * every call).  crtm_gpu_k_matrix_device without device-memory allocation:
  * the intermediates live in a static per-device scratch of
