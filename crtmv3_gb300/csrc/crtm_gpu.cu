@@ -1870,22 +1870,12 @@ __global__ void tl_kernel(TLArgs a) {
   const int Ku = a.n_layers[p];
   const size_t pl = (size_t)p * a.L + l;
   double s = 0.0;
-  // four independent loads in flight per lane (the rows are streamed once)
   auto rows = [&](const double* K, const double* D, int nrow) {
     if (!K || !D) return;
     for (int r = 0; r < nrow; r++) {
       const double* kr = K + (pl * nrow + r) * a.Km;
       const double* dr = D + ((size_t)p * nrow + r) * a.Km;
-      double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-      int k = lane;
-      for (; k + 96 < Ku; k += 128) {
-        s0 += kr[k] * dr[k];
-        s1 += kr[k + 32] * dr[k + 32];
-        s2 += kr[k + 64] * dr[k + 64];
-        s3 += kr[k + 96] * dr[k + 96];
-      }
-      for (; k < Ku; k += 32) s0 += kr[k] * dr[k];
-      s += (s0 + s1) + (s2 + s3);
+      for (int k = lane; k < Ku; k += 32) s += kr[k] * dr[k];
     }
   };
   rows(a.kt, a.d.temperature, 1);

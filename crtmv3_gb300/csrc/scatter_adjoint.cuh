@@ -672,7 +672,7 @@ CRTM_HD int layer_adjoint_in(const CloudyColumn& in, const CloudLut& lut, const 
       // of the symmetric means (error O(h^4)): h = 1e-3 in FP64, 1e-2 in
       // FP32, where the shifted gaps must be wider.  An FP32 layer whose
       // shifted angles still meet an eigenvalue, or fail, is taken in FP64.
-      const double shift = fp32 ? FP32_ADJ_SENSOR_SHIFT : SENSOR_SHIFT;
+      const double shift = fp32 ? FP32_SENSOR_SHIFT : SENSOR_SHIFT;
       BulkAdjoint<T> S2;
       S2.od_b = S2.ssa_b = S2.B_b = T(0.0);
       for (int l = 0; l <= nleg; l++) S2.p_b[l] = T(0.0);

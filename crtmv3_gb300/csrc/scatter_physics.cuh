@@ -52,14 +52,10 @@ constexpr double SENSOR_SHIFT = 1.0e-3;
 // sensor angle's MOM eigenvector, which divides by the gap, loses too much
 // of FP32's precision (about eps/gap in T and R, eps/gap^2 in their
 // derivatives); such a layer is solved at sensor angles mu (1 +- h),
-// mu (1 +- 2h), h = FP32_SENSOR_SHIFT (forward) or FP32_ADJ_SENSOR_SHIFT
-// (reverse sweep), and extrapolated, in FP32.
+// mu (1 +- 2h), h = FP32_SENSOR_SHIFT, and extrapolated, in FP32.
 constexpr double FP32_GAP_MIN = 3.0e-3;
-constexpr double FP32_ADJ_GAP_MIN = 6.0e-3;
+constexpr double FP32_ADJ_GAP_MIN = 3.0e-3;
 constexpr double FP32_SENSOR_SHIFT = 1.0e-2;
-// the reverse sweep's shift: its shifted gaps must stay above FP32_ADJ_GAP_MIN
-// (the derivatives' FP32 error is about 2 eps / gap^2 of the layer's share)
-constexpr double FP32_ADJ_SENSOR_SHIFT = 1.5e-2;
 // FP32 reverse sweep: layers whose single-scattering albedo is within this
 // of 1 are differentiated in FP64 (the albedo's adjoint loses eps / (1 - ssa))
 constexpr double FP32_COALBEDO_MIN = 3.0e-4;
