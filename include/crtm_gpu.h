@@ -389,11 +389,12 @@ int crtm_gpu_adjoint_apply(crtm_gpu_handle handle, const double* bt_ad, crtm_gpu
  * crtm_gpu_last_error) when one profile's intermediates do not fit.  With no
  * batch emissivity, the IR sea-surface emissivity model's 3 x P x L doubles
  * also come from the scratch (the call fails when they leave no room for one
- * profile).  crtm_gpu_init looks up the scratch address on its device; where
- * it has not, the first call on a device does, and that call should come
- * before any stream capture.  The scratch is shared by all handles on a
- * device: calls that overlap in time race and must be ordered by the
- * caller. */
+ * profile).  crtm_gpu_init looks up the scratch address on its device (the
+ * module's first use there); where it has not, the first call on a device
+ * does.  The entry points are not safe to capture into a CUDA graph: each
+ * call reads host tables (absorber maps, bucket counts) while it enqueues its
+ * work.  The scratch is shared by all handles on a device: calls that overlap
+ * in time race and must be ordered by the caller. */
 #define CRTM_GPU_STATIC_SCRATCH_MIB 128
 int crtm_gpu_k_matrix_device_static(crtm_gpu_handle handle, int sensor,
                                     const crtm_gpu_batch* batch, const double* bt_k,
