@@ -2393,6 +2393,7 @@ int crtm_gpu_set_channel_subset(crtm_gpu_handle h, int sensor, int n, const int*
   }
   // wait for calls in flight on the handle's stream before the tables change
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) return fail(h, "stream synchronisation failed");
+  if (h->lin.sensor == sensor) h->lin.valid = false;   // its Jacobians have the old channels
   std::string err;
   if (!pos.empty() && pos[0] == -1) {
     s.L = 0;

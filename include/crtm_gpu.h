@@ -369,7 +369,8 @@ int crtm_gpu_tangent_linear_device(crtm_gpu_handle handle, int sensor, const crt
  * crtm_gpu_tangent_linear / crtm_gpu_adjoint about that trajectory, to
  * rounding).  All pointers are device pointers; tl and ad have the
  * trajectory batch's shapes.  A later linearize or tangent-linear call
- * replaces the trajectory; profiles whose trajectory status was not 0 give 0.
+ * replaces the trajectory, and a channel-subset change of its sensor ends it;
+ * profiles whose trajectory status was not 0 give 0.
  * The apply calls fail when they ask for a Jacobian the trajectory does not
  * hold (for example cloud perturbations of a batch without clouds). */
 int crtm_gpu_linearize(crtm_gpu_handle handle, int sensor, const crtm_gpu_batch* batch,
