@@ -668,6 +668,19 @@ def run_scattering(args, torch, dev, rank, world, dist):
             ms = e0.elapsed_time(e1) / args.steps
             extra[f"{lab}_forward_mixed"] = {"ms_per_step": ms, "value": calls[0]["pc"] / (ms * 1e-3)}
         extra["soi_vs_ada_max_abs_bt_K"] = float((fo["bt"] - fo2["bt"]).abs().max())
+        # the SOI K-matrix of the same inputs (the orders' adjoint; FP64 in both
+        # forms), against the ADA K-matrix step above
+        c0 = calls[0]
+        h.k_matrix_device(b, c0["out"], None, 0, sptr, k_absorbers=c0["sel"])
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        h.k_matrix_device(b, c0["out"], None, 0, sptr, k_absorbers=c0["sel"])
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1)
+        extra["soi_k_matrix"] = {"ms_per_call": ms, "value": c0["pc"] / (ms * 1e-3),
+                                 "vs_ada_k_matrix_mixed": ms / per_mixed}
         opt.rt_algorithm_id = None
     # end to end through the host entry point (pinned host outputs), mixed
     # form, on a sample of each group's profiles (the full step's ~150 GB of
