@@ -178,7 +178,14 @@ def oracle_errors(h, sample, ref, prec):
 
     def rel(x, y):
         return float(np.abs(x - y).max() / max(np.abs(y).max(), 1e-300))
+
+    def over(x, y):   # entries off by more than 1e-3 of the largest (a clamp's kink crossed by rounding)
+        return int((np.abs(x - y) > 1e-3 * max(np.abs(y).max(), 1e-300)).sum())
+    n_over = {"temperature": over(km.temperature, ref["temperature_k"]),
+              "h2o": over(km.absorber[:, :, 0], ref["absorber_k"][:, :, sel[0]]),
+              "o3": over(km.absorber[:, :, 1], ref["absorber_k"][:, :, sel[1]])}
     return {"max_abs_bt_K": float(np.abs(rts.brightness_temperature - ref["bt"]).max()),
+            "entries_over_1e-3": n_over, "entries": int(km.temperature.size),
             "max_rel_jacobian": {
                 "temperature": rel(km.temperature, ref["temperature_k"]),
                 "h2o": rel(km.absorber[:, :, 0], ref["absorber_k"][:, :, sel[0]]),

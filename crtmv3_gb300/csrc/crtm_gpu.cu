@@ -985,6 +985,12 @@ void rts_ext_set(crtm_gpu_rtsolution* r, void* const* p) {
   r->layer_optical_depth = (double*)p[9]; r->upwelling_radiance = (double*)p[10];
   r->upwelling_overcast_radiance = (double*)p[11];
 }
+// Whether a call asks for any of the further RTSolution components.
+bool rts_ext_any(const RtsExt& x) {
+  return x.tb_clear || x.r_clear || x.tcc || x.sod || x.emis || x.up || x.down || x.bs || x.nfs || x.lod || x.upw ||
+         x.ovc;
+}
+
 RtsExt make_ext(const crtm_gpu_rtsolution* r) {
   RtsExt x;
   x.tb_clear = r->tb_clear; x.r_clear = r->r_clear; x.tcc = r->total_cloud_cover; x.sod = r->sod;
@@ -1162,7 +1168,8 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
   const size_t map_smem = map_smem_bytes<R>(K, Kmax, nv, map_ct);
   constexpr size_t fwd_smem = fwd_smem_bytes<G, R, NPF>();
   if (reserve_smem(h, absorb_fwd_kernel<G, R, NPF>, fwd_smem, "absorb_fwd") ||
-      reserve_smem(h, column_kernel<R>, col_smem, "column") ||
+      reserve_smem(h, column_kernel<R, false>, col_smem, "column") ||
+      reserve_smem(h, column_kernel<R, true>, col_smem, "column") ||
       reserve_smem(h, map_kernel<R>, map_smem, "map"))
     return CRTM_GPU_FAILURE;
   const bool ho_only = [&] {
@@ -1215,7 +1222,10 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
     dim3 gc((L + 127) / 128, n);
     {
       StageScope sc(h, 2, st);
-      column_kernel<R><<<gc, 128, col_smem, st>>>(ca);
+      if (rts_ext_any(ca.x))
+        column_kernel<R, true><<<gc, 128, col_smem, st>>>(ca);
+      else
+        column_kernel<R, false><<<gc, 128, col_smem, st>>>(ca);
       CK_LAUNCH(h);
     }
     if (scat) {   // layer optics, then the adding from the surface (and its adjoint)
@@ -1297,7 +1307,10 @@ int run_pipeline(crtm_gpu_handle h, const Sensor& s, const crtm_gpu_batch* b, in
         {
           ca.pass = 2;
           StageScope sc(h, 2, st);
-          column_kernel<R><<<gc, 128, col_smem, st>>>(ca);
+          if (rts_ext_any(ca.x))
+        column_kernel<R, true><<<gc, 128, col_smem, st>>>(ca);
+      else
+        column_kernel<R, false><<<gc, 128, col_smem, st>>>(ca);
           CK_LAUNCH(h);
         }
         if (sw.slots || sw.cf) {   // species and cloud-fraction Jacobians: cover chain rule, seed, outputs

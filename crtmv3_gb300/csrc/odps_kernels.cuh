@@ -681,7 +681,9 @@ inline size_t column_smem_bytes(int K, int Kmax) {
          sizeof(int) * (2 * (size_t)(Kmax + 1) + 2 * (size_t)(K + 1)) + 16;
 }
 
-template <class R>
+// EXT: the call asks for further RTSolution components (a.x); without them
+// the component code compiles out.
+template <class R, bool EXT>
 __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int K = a.K, L = a.L, Kmax = a.Kmax;
@@ -698,7 +700,7 @@ __global__ void __launch_bounds__(128) column_kernel(ColumnArgs<R> a) {
   const int st = a.pv.status[p];
   const int Ku = a.b.n_layers[gp];
   if (blockIdx.x == 0 && tid == 0 && a.status) a.status[gp] = st;
-  const RtsExt& x = a.x;
+  const RtsExt x = EXT ? a.x : RtsExt{};
   auto ext_scalars = [&](size_t pl, double e, double up, double down, double bs) {
     if (x.emis) x.emis[pl] = e;
     if (x.up) x.up[pl] = up;
