@@ -1864,8 +1864,7 @@ int check_call(crtm_gpu_handle h, const crtm_gpu_batch* b, const crtm_gpu_rtsolu
   return CRTM_GPU_SUCCESS;
 }
 
-// Tangent linear as the K-matrix contracted with the perturbations: one warp
-// per (profile, channel), lanes over the layers.
+// Tangent linear as the K-matrix contracted with the perturbations.
 struct TLArgs {
   int P, L, Km, J, NC, NA;
   const int* n_layers;
@@ -1875,20 +1874,36 @@ struct TLArgs {
   double* bt_tl;
 };
 
+// One warp per (profile, TL_CH consecutive channels), lanes over the layers:
+// each perturbation value is loaded once for the warp's channels, whose
+// TL_CH sums are independent accumulations (the same order per channel as a
+// warp per channel would take).
+constexpr int TL_CH = 8;
+
 __global__ void tl_kernel(TLArgs a) {
   const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (w >= (long long)a.P * a.L) return;
-  const int p = (int)(w / a.L), l = (int)(w % a.L);
+  const int groups = (a.L + TL_CH - 1) / TL_CH;
+  if (w >= (long long)a.P * groups) return;
+  const int p = (int)(w / groups), l0 = (int)(w % groups) * TL_CH;
+  const int nch = min(TL_CH, a.L - l0);
   const int Ku = a.n_layers[p];
-  const size_t pl = (size_t)p * a.L + l;
-  double s = 0.0;
+  double s[TL_CH];
+#pragma unroll
+  for (int c = 0; c < TL_CH; c++) s[c] = 0.0;
   auto rows = [&](const double* K, const double* D, int nrow) {
     if (!K || !D) return;
+    const size_t cstride = (size_t)nrow * a.Km;   // one channel's rows
+    const double* k0 = K + ((size_t)p * a.L + l0) * cstride;
     for (int r = 0; r < nrow; r++) {
-      const double* kr = K + (pl * nrow + r) * a.Km;
       const double* dr = D + ((size_t)p * nrow + r) * a.Km;
-      for (int k = lane; k < Ku; k += 32) s += kr[k] * dr[k];
+      const double* kr = k0 + (size_t)r * a.Km;
+      for (int k = lane; k < Ku; k += 32) {
+        const double d = dr[k];
+#pragma unroll
+        for (int c = 0; c < TL_CH; c++)
+          if (c < nch) s[c] += kr[c * cstride + k] * d;
+      }
     }
   };
   rows(a.kt, a.d.temperature, 1);
@@ -1900,15 +1915,23 @@ __global__ void tl_kernel(TLArgs a) {
   rows(a.kar, a.d.aerosol_effective_radius, a.NA);
   rows(a.kav, a.d.aerosol_effective_variance, a.NA);
   rows(a.krh, a.d.relative_humidity, 1);
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (lane) return;
-  if (a.d.water_temperature) s += a.kw[pl] * a.d.water_temperature[p];
-  if (a.d.land_temperature) s += a.kl[pl] * a.d.land_temperature[p];
-  if (a.d.snow_temperature) s += a.ks[pl] * a.d.snow_temperature[p];
-  if (a.d.ice_temperature) s += a.ki[pl] * a.d.ice_temperature[p];
-  if (a.d.emissivity) s += a.ke[pl] * a.d.emissivity[pl];
-  if (a.d.wind_speed && a.kws) s += a.kws[pl] * a.d.wind_speed[p];
-  a.bt_tl[pl] = (a.status && a.status[p]) ? 0.0 : s;
+  double mine = 0.0;
+#pragma unroll
+  for (int c = 0; c < TL_CH; c++) {
+    double v = s[c];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == c) mine = v;
+  }
+  if (lane >= nch) return;
+  const size_t pl = (size_t)p * a.L + l0 + lane;
+  double t = mine;
+  if (a.d.water_temperature) t += a.kw[pl] * a.d.water_temperature[p];
+  if (a.d.land_temperature) t += a.kl[pl] * a.d.land_temperature[p];
+  if (a.d.snow_temperature) t += a.ks[pl] * a.d.snow_temperature[p];
+  if (a.d.ice_temperature) t += a.ki[pl] * a.d.ice_temperature[p];
+  if (a.d.emissivity) t += a.ke[pl] * a.d.emissivity[pl];
+  if (a.d.wind_speed && a.kws) t += a.kws[pl] * a.d.wind_speed[p];
+  a.bt_tl[pl] = (a.status && a.status[p]) ? 0.0 : t;
 }
 
 // The trajectory's K-matrix into the handle's scratch: every Jacobian the
@@ -2006,7 +2029,7 @@ int tl_apply(crtm_gpu_handle h, const crtm_gpu_tl_in* tl, double* bt_tl, cudaStr
   ta.kwc = g.k.cloud_water_content; ta.kre = g.k.cloud_effective_radius; ta.kcf = g.k.cloud_fraction;
   ta.kac = g.k.aerosol_concentration; ta.kar = g.k.aerosol_effective_radius;
   ta.kav = g.k.aerosol_effective_variance; ta.krh = g.k.relative_humidity; ta.kws = g.k.wind_speed;
-  const long long threads = (long long)g.P * g.L * 32;
+  const long long threads = (long long)g.P * ((g.L + TL_CH - 1) / TL_CH) * 32;
   tl_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(ta);
   CK_LAUNCH(h);
   mark_done(h, st);
