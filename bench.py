@@ -348,6 +348,27 @@ def scatter_device_inputs(torch, h, atm, sfc, geo, opt, dev):
     return b, keep, t
 
 
+def pinned_copy(torch, obj):
+    """A copy of a batch dataclass with every numpy array in pinned host
+    memory (the end-to-end legs copy their inputs from pinned memory)."""
+    import dataclasses as dc
+    vals = {}
+    for f in dc.fields(obj):
+        v = getattr(obj, f.name)
+        if isinstance(v, np.ndarray) and v.dtype != object:
+            t = torch.empty(v.shape, dtype=torch.from_numpy(np.zeros(1, v.dtype)).dtype, pin_memory=True).numpy()
+            t[...] = v
+            vals[f.name] = t
+    return dc.replace(obj, **vals)
+
+
+def pinned_rts(torch, P: int, L: int):
+    from crtmv3_gb300.structures import RTSolutionBatch
+    return RTSolutionBatch(torch.empty((P, L), dtype=torch.float64, pin_memory=True).numpy(),
+                           torch.empty((P, L), dtype=torch.float64, pin_memory=True).numpy(),
+                           status=torch.empty((P,), dtype=torch.int32, pin_memory=True).numpy())
+
+
 def stratified_indices(atm, opt, n: int) -> np.ndarray:
     """n profile indices of a group whose mix of strata -- clear, cloudy on the
     stream rule, cloudy with Options%n_Streams 8, with 16 -- matches the
@@ -693,8 +714,8 @@ def run_scattering(args, torch, dev, rank, world, dist):
     if not args.no_e2e and name != "C3":
         from crtmv3_gb300.structures import KMatrixBatch
         frac = 8
-        sub = [(sid, a.subset(slice(0, a.n_profiles // frac)), s_.subset(slice(0, a.n_profiles // frac)),
-                g_.subset(slice(0, a.n_profiles // frac)), o_.subset(slice(0, a.n_profiles // frac)))
+        sub = [(sid,) + tuple(pinned_copy(torch, x.subset(slice(0, a.n_profiles // frac)))
+                              for x in (a, s_, g_, o_))
                for sid, a, s_, g_, o_ in groups]
 
         def pin(shape):
@@ -708,7 +729,7 @@ def run_scattering(args, torch, dev, rank, world, dist):
             if NC:
                 km.cloud_water_content = pin((P, L, NC, K))
                 km.cloud_effective_radius = pin((P, L, NC, K))
-            outs.append((km, sel))
+            outs.append((km, sel, pinned_rts(torch, P, L)))
             h2d += sum(x.nbytes for x in (a.level_pressure, a.pressure, a.temperature, a.absorber, o_.emissivity,
                                           a.cloud_water_content, a.cloud_effective_radius, a.cloud_fraction)
                        if x is not None) + 14 * P * 8
@@ -717,8 +738,8 @@ def run_scattering(args, torch, dev, rank, world, dist):
         h.set_precision(1)
 
         def e2e_step():
-            for si, ((sid, a, s_, g_, o_), (km, sel)) in enumerate(zip(sub, outs)):
-                h.k_matrix(a, s_, g_, o_, None, si, k_absorbers=sel, out=km)
+            for si, ((sid, a, s_, g_, o_), (km, sel, rt)) in enumerate(zip(sub, outs)):
+                h.k_matrix(a, s_, g_, o_, None, si, k_absorbers=sel, out=km, rts_out=rt)
         e2e_step()
         n_e2e = max(1, min(args.steps, 2))
         torch.cuda.synchronize(dev)
@@ -727,7 +748,8 @@ def run_scattering(args, torch, dev, rank, world, dist):
             e2e_step()
         dt = (time.perf_counter() - t0) / n_e2e
         e2e = {"value": epc * world / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-               "ms_per_step": dt * 1e3, "sample": f"first 1/{frac} of each group's profiles per step"}
+               "ms_per_step": dt * 1e3, "sample": f"first 1/{frac} of each group's profiles per step, inputs and "
+                                                 f"outputs in pinned host memory"}
         del outs
     # CPU baseline (the FP64 oracle on the host cores) and both GPU forms
     # against the oracle, on n_cmp profiles of each group (stratified_indices)
@@ -938,13 +960,15 @@ def main():
         def pin(shape):
             return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
         kout = KMatrixBatch(pin((P, L, K)), pin((P, L, JK, K)), pin((P, L)), pin((P, L)))
+        patm, psfc, pgeo, popt = (pinned_copy(torch, x) for x in (atm, sfc, geo, opt))
+        prts = pinned_rts(torch, P, L)
         h.set_precision(1)
-        h.k_matrix(atm, sfc, geo, opt, None, 0, k_absorbers=sel, out=kout)
+        h.k_matrix(patm, psfc, pgeo, popt, None, 0, k_absorbers=sel, out=kout, rts_out=prts)
         n_e2e = max(1, min(args.steps, 3))
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         for _ in range(n_e2e):
-            h.k_matrix(atm, sfc, geo, opt, None, 0, k_absorbers=sel, out=kout)
+            h.k_matrix(patm, psfc, pgeo, popt, None, 0, k_absorbers=sel, out=kout, rts_out=prts)
         dt = (time.perf_counter() - t0) / n_e2e
         h2d = sum(x.nbytes for x in (atm.level_pressure, atm.pressure, atm.temperature, atm.absorber,
                                      opt.emissivity)) + 10 * P * 8 + P * 4

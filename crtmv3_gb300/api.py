@@ -374,10 +374,10 @@ class CRTM:
         return rts
 
     def k_matrix(self, atm, sfc, geo, opt, bt_k=None, sensor: int = 0, k_absorbers=None, out=None,
-                 scattering_jacobians: bool = True, components: bool = False):
+                 scattering_jacobians: bool = True, components: bool = False, rts_out=None):
         """K-matrix with host buffers.  ``k_absorbers``: optional list of user absorber
-        indices whose Jacobians are returned (default: all).  ``out``: optional
-        preallocated KMatrixBatch (e.g. in pinned memory).  ``scattering_jacobians``:
+        indices whose Jacobians are returned (default: all).  ``out`` / ``rts_out``:
+        optional preallocated KMatrixBatch / RTSolutionBatch (e.g. in pinned memory).  ``scattering_jacobians``:
         also return the cloud water content / effective radius / fraction and
         aerosol concentration / effective radius Jacobians of a batch with clouds
         or aerosols.  ``components``: also return the further RTSolution
@@ -388,7 +388,7 @@ class CRTM:
         seed = None if bt_k is None else np.ascontiguousarray(bt_k, np.float64)
         sel = None if k_absorbers is None else np.ascontiguousarray(k_absorbers, np.int32)
         JK = J if sel is None else int(sel.shape[0])
-        rts = _rts(P, L, K, components)
+        rts = rts_out if rts_out is not None else _rts(P, L, K, components)
         km = out if out is not None else KMatrixBatch(np.zeros((P, L, K)), np.zeros((P, L, JK, K)),
                                                       np.zeros((P, L)), np.zeros((P, L)))
         if out is None and scattering_jacobians:
