@@ -653,20 +653,28 @@ def CRTM_ChannelInfo_Subset(channel_info: ChannelInfo, channel_subset=None, rese
 def CRTM_Init(sensor_ids: Sequence[str], channel_info: List[ChannelInfo], file_path: str = ".",
               precision: int = FP64, aerosol_model: Optional[str] = None,
               aerosolcoeff_file: Optional[str] = None, spccoeff_format: str = "Binary",
-              taucoeff_format: str = "Binary", irwatercoeff_format: str = "Binary") -> int:
+              taucoeff_format: str = "Binary", irwatercoeff_format: str = "Binary",
+              cloudcoeff_format: str = "Binary", aerosolcoeff_format: str = "Binary",
+              cloudcoeff_file: Optional[str] = None) -> int:
     """CRTM_Init: load the coefficients of ``sensor_ids`` and fill ``channel_info``
-    (Aerosol_Model, AerosolCoeff_File, SpcCoeff_Format and TauCoeff_Format as
-    the reference's optional arguments, src/CRTM_LifeCycle.f90:523-561, and
+    (Aerosol_Model, AerosolCoeff_File, AerosolCoeff_Format, CloudCoeff_File,
+    CloudCoeff_Format, SpcCoeff_Format and TauCoeff_Format as the reference's
+    optional arguments, src/CRTM_LifeCycle.f90:523-561, and
     IRwaterCoeff_Format).  With a format 'netCDF' the sensors'
-    <id>.SpcCoeff.nc / <id>.TauCoeff.nc files (and Nalli.IRwater.EmisCoeff.nc)
-    are converted to binary files in a private directory, which is loaded."""
+    <id>.SpcCoeff.nc / <id>.TauCoeff.nc files, Nalli.IRwater.EmisCoeff.nc,
+    the cloud table (CloudCoeff_File, default CloudCoeff.nc) or the aerosol
+    table (AerosolCoeff_File, default AerosolCoeff.nc, read for the
+    Aerosol_Model's layout) are converted to binary files in a private
+    directory, which is loaded.  A binary CloudCoeff_File other than
+    CloudCoeff.bin is linked into that directory under CloudCoeff.bin."""
     path = file_path
     try:
-        fmts = (spccoeff_format, taucoeff_format, irwatercoeff_format)
+        fmts = (spccoeff_format, taucoeff_format, irwatercoeff_format, cloudcoeff_format, aerosolcoeff_format)
         for fm in fmts:
             if fm.lower() not in ("binary", "netcdf"):
                 raise ValueError(f"coefficient format must be 'Binary' or 'netCDF' (got {fm!r})")
-        if any(fm.lower() == "netcdf" for fm in fmts):
+        cloud_nc = cloudcoeff_format.lower() == "netcdf"
+        if any(fm.lower() == "netcdf" for fm in fmts) or cloudcoeff_file not in (None, "CloudCoeff.bin"):
             import tempfile
             from . import netcdf_coeffs
             path = tempfile.mkdtemp(prefix="crtm_coeffs_")
@@ -674,6 +682,13 @@ def CRTM_Init(sensor_ids: Sequence[str], channel_info: List[ChannelInfo], file_p
                 netcdf_coeffs.convert_sensor(file_path, s, path, spccoeff_format, taucoeff_format)
             if irwatercoeff_format.lower() == "netcdf":
                 netcdf_coeffs.convert_irwater(file_path, path)
+            if cloud_nc:
+                netcdf_coeffs.convert_cloud(file_path, path, cloudcoeff_file or "CloudCoeff.nc")
+            elif cloudcoeff_file not in (None, "CloudCoeff.bin"):
+                netcdf_coeffs._link(os.path.join(file_path, cloudcoeff_file), os.path.join(path, "CloudCoeff.bin"))
+            if aerosolcoeff_format.lower() == "netcdf":
+                aerosolcoeff_file = netcdf_coeffs.convert_aerosol(file_path, path, aerosol_model or "CRTM",
+                                                                  aerosolcoeff_file or "AerosolCoeff.nc")
             netcdf_coeffs.link_shared_files(file_path, path, extra=(aerosolcoeff_file,) if aerosolcoeff_file else ())
     except (OSError, ValueError, KeyError) as e:
         print(f"CRTM_Init(FAILURE): {e}")

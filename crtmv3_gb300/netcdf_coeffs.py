@@ -1,18 +1,20 @@
-"""netCDF (classic format) SpcCoeff and ODPS TauCoeff files: readers, writers
-and the conversion to the binary files that crtm_gpu_init loads.
+"""netCDF (classic format) coefficient files -- SpcCoeff, ODPS TauCoeff,
+IRwaterCoeff, CloudCoeff and AerosolCoeff: readers, writers and the
+conversion to the binary files that crtm_gpu_init loads.
 
-The reference writes both with NF90_CREATE(..., NF90_CLOBBER), i.e. netCDF
+The reference writes them with NF90_CREATE(..., NF90_CLOBBER), i.e. netCDF
 classic (src/Coefficients/SpcCoeff/SpcCoeff_netCDF_IO.f90:1501,
 src/Coefficients/TauCoeff/ODPS/ODPS_netCDF_IO.f90:1471).  Names, types and
-dimensions follow SpcCoeff_netCDF_IO.f90:68-183 and ODPS_netCDF_IO.f90:63-240.
+dimensions follow each file's *_netCDF_IO.f90, cited at each writer.
 A Fortran variable dimensioned (a, b) is stored in netCDF as (b, a), so the
-2-D arrays are transposed on the way in and out.
+arrays are transposed on the way in and out.
 
-CRTM_Init's SpcCoeff_Format / TauCoeff_Format = 'netCDF'
-(src/CRTM_LifeCycle.f90) reads <Sensor_Id>.SpcCoeff.nc and
-<Sensor_Id>.TauCoeff.nc.  crtmv3_gb300.api.CRTM_Init does the same through
-``convert_sensor``: the files become binary files in a private directory,
-which the library then loads.
+CRTM_Init's SpcCoeff_Format / TauCoeff_Format / CloudCoeff_Format /
+AerosolCoeff_Format = 'netCDF' (src/CRTM_LifeCycle.f90:523-561, 783-800)
+reads <Sensor_Id>.SpcCoeff.nc, <Sensor_Id>.TauCoeff.nc, CloudCoeff.nc and
+AerosolCoeff.nc.  crtmv3_gb300.api.CRTM_Init does the same through the
+``convert_*`` functions: the files become binary files in a private
+directory, which the library then loads.
 """
 from __future__ import annotations
 
@@ -225,6 +227,169 @@ def read_irwater_nc(path: str) -> co.IRwaterCoeff:
 
 
 # ---------------------------------------------------------------------------
+# CloudCoeff (cloud optical property table)
+# ---------------------------------------------------------------------------
+
+CLOUDCOEFF_FILE = "CloudCoeff"
+
+
+def _nc_order(a):
+    """A Fortran-ordered array as netCDF stores it: the dimensions reversed."""
+    a = np.asarray(a, np.float64)
+    return a.transpose(tuple(range(a.ndim))[::-1])
+
+
+def write_cloudcoeff_nc(path: str, cc: co.CloudCoeff) -> None:
+    """CloudCoeff_netCDF_IO's layout (src/Coefficients/CloudCoeff/
+    CloudCoeff_netCDF_IO.f90:60-103 names, :229-253 types, :2020-2545
+    definitions).  Its dimensions for a table read from the binary file:
+    n_IR_Densities is the IR density axis (the MW densities and the liquid
+    entry), n_Legendre_Terms counts the terms 0..n_Legendre_Terms of the MW
+    phase coefficients.  pcoeff_IR is 4-D (no phase dimension, :2533-2537)
+    and holds the IR terms 1..n_Legendre_Terms in its first
+    n_Legendre_Terms slabs, the last slab zero, which is how the reference's
+    writer fills that variable from its array.  The kb variables are written
+    as zero and Water_Density_MW as zero (a table indexed by effective
+    radius, :1362-1372); Density_IR is 100 followed by the MW densities (the
+    reader's fallback, :1578-1586).  None of these three enters the binary
+    file."""
+    nfm, nrm, nt = cc.ke_l_mw.shape
+    nfi, nri, ndi = cc.ke_ir.shape
+    nd, nl, nph = cc.density_mw.size, cc.n_legendre_terms, cc.n_phase_elements
+    if nph != 1:
+        raise ValueError("CloudCoeff netCDF: pcoeff_IR has no phase dimension; n_Phase_Elements must be 1")
+    if ndi != nd + 1 or cc.pcoeff_ir.shape[3] != nl:
+        raise ValueError("CloudCoeff: IR tables do not match the density and Legendre axes")
+    with netcdf_file(path, "w", version=1) as f:
+        f.Release = np.int32(co.CLOUDCOEFF_RELEASE)
+        f.Version = np.int32(cc.version)
+        for dim, n in (("n_MW_Frequencies", nfm), ("n_MW_Radii", nrm), ("n_IR_Frequencies", nfi),
+                       ("n_IR_Radii", nri), ("n_Temperatures", nt), ("n_MW_Densities", nd),
+                       ("n_IR_Densities", nd + 1), ("n_Legendre_Terms", nl + 1), ("n_Phase_Elements", nph)):
+            f.createDimension(dim, int(n))
+        axes = (("Frequency_MW", "n_MW_Frequencies", cc.frequency_mw),
+                ("Frequency_IR", "n_IR_Frequencies", cc.frequency_ir),
+                ("Water_Density_MW", "n_MW_Radii", np.zeros(nrm)),
+                ("Reff_MW", "n_MW_Radii", cc.reff_mw), ("Reff_IR", "n_IR_Radii", cc.reff_ir),
+                ("Temperature", "n_Temperatures", cc.temperature),
+                ("Density_MW", "n_MW_Densities", cc.density_mw),
+                ("Density_IR", "n_IR_Densities", np.concatenate([[100.0], cc.density_mw])))
+        for name, dim, data in axes:
+            v = f.createVariable(name, "f8", (dim,))
+            v[:] = np.asarray(data, np.float64)
+        blocks = (("L_MW", ("n_Temperatures", "n_MW_Radii", "n_MW_Frequencies"),
+                   (cc.ke_l_mw, cc.w_l_mw, cc.g_l_mw, cc.pcoeff_l_mw)),
+                  ("S_MW", ("n_MW_Densities", "n_MW_Radii", "n_MW_Frequencies"),
+                   (cc.ke_s_mw, cc.w_s_mw, cc.g_s_mw, cc.pcoeff_s_mw)),
+                  ("IR", ("n_IR_Densities", "n_IR_Radii", "n_IR_Frequencies"),
+                   (cc.ke_ir, cc.w_ir, cc.g_ir, None)))
+        for suffix, dims, (ke, w, g, pc) in blocks:
+            for name, data in (("ke", ke), ("w", w), ("g", g), ("kb", np.zeros_like(ke))):
+                v = f.createVariable(f"{name}_{suffix}", "f8", dims)
+                v[:] = _nc_order(data)
+            if pc is not None:
+                v = f.createVariable(f"pcoeff_{suffix}", "f8", ("n_Phase_Elements", "n_Legendre_Terms") + dims)
+                v[:] = _nc_order(pc)
+        pir = np.zeros((nfi, nri, ndi, nl + 1))
+        pir[..., :nl] = cc.pcoeff_ir[..., 0]
+        v = f.createVariable("pcoeff_IR", "f8", ("n_Legendre_Terms",) + blocks[2][1])
+        v[:] = _nc_order(pir)
+
+
+def read_cloudcoeff_nc(path: str) -> co.CloudCoeff:
+    with netcdf_file(path, "r", mmap=False) as f:
+        rel = int(_attr(f, "Release", co.CLOUDCOEFF_RELEASE))
+        if rel != co.CLOUDCOEFF_RELEASE:
+            raise ValueError(f"CloudCoeff netCDF: release {rel} not supported")
+        nl = int(f.dimensions["n_Legendre_Terms"]) - 1
+
+        def fortran(name):
+            a = _var(f, name, np.float64)
+            return np.ascontiguousarray(a.transpose(tuple(range(a.ndim))[::-1]))
+        axes = [_var(f, n, np.float64) for n in ("Frequency_MW", "Frequency_IR", "Reff_MW", "Reff_IR",
+                                                 "Temperature", "Density_MW")]
+        tables = []
+        for suffix in ("L_MW", "S_MW"):
+            tables += [fortran(f"{n}_{suffix}") for n in ("ke", "w", "g", "pcoeff")]
+        pir = fortran("pcoeff_IR")
+        if pir.ndim != 4:
+            raise ValueError("CloudCoeff netCDF: pcoeff_IR must have four dimensions")
+        tables += [fortran(f"{n}_IR") for n in ("ke", "w", "g")]
+        tables.append(np.ascontiguousarray(pir[..., :nl, None]))
+        return co.CloudCoeff(*axes, *tables, version=int(_attr(f, "Version", co.MIE_TAMU_CLOUDCOEFF)))
+
+
+# ---------------------------------------------------------------------------
+# AerosolCoeff (aerosol optical property table)
+# ---------------------------------------------------------------------------
+
+AEROSOLCOEFF_FILE = "AerosolCoeff"
+
+
+def write_aerosolcoeff_nc(path: str, ac: co.AerosolCoeff, scheme: str = "CRTM") -> None:
+    """AerosolCoeff_netCDF_IO's layout (src/Coefficients/AerosolCoeff/
+    AerosolCoeff_netCDF_IO.f90:67-95 names, :152-162 types, :1540-1830
+    definitions): dimension n_RH for the tables' humidity axis and, for the
+    'CRTM' and 'CMAQ' tables, n_RH_Radii for the RH variable (:1728-1736);
+    n_Legendre_Terms counts the terms 0..n_Legendre_Terms; the type names are
+    characters over the tnsl dimension."""
+    nw, nrh, nr, ns, nt = ac.ke.shape
+    nl, nph = ac.pcoeff.shape[5] - 1, ac.pcoeff.shape[6]
+    rh_radii = co._rh_radii_record(scheme)
+    if not rh_radii and ac.rh.size != nrh:
+        raise ValueError("the RH axis of a GOCART-GEOS5 / NAAPS table has n_RH entries")
+    with netcdf_file(path, "w", version=1) as f:
+        f.Release = np.int32(co.AEROSOLCOEFF_RELEASE)
+        f.Version = np.int32(ac.version)
+        f.Data_Source = ac.data_source
+        for dim, n in (("n_Wavelengths", nw), ("n_Radii", nr), ("n_Sigma", ns), ("n_Types", nt), ("n_RH", nrh)):
+            f.createDimension(dim, int(n))
+        if rh_radii:
+            f.createDimension("n_RH_Radii", int(ac.rh.size))
+        f.createDimension("n_Legendre_Terms", nl + 1)
+        f.createDimension("n_Phase_Elements", nph)
+        f.createDimension("tnsl", co.AEROSOL_SL)
+        v = f.createVariable("Aerosol_Type", "i4", ("n_Types",))
+        v[:] = np.asarray(ac.type_id, np.int32)
+        v = f.createVariable("Aerosol_Type_Name", "c", ("n_Types", "tnsl"))
+        v[:] = np.array([list(n.ljust(co.AEROSOL_SL)[:co.AEROSOL_SL]) for n in ac.type_name], "S1")
+        for name, dims, data in (("Wavelength", ("n_Wavelengths",), ac.wavelength),
+                                 ("Reff", ("n_Types", "n_Radii"), ac.reff),
+                                 ("Rsig", ("n_Types", "n_Sigma"), ac.rsig),
+                                 ("RH", ("n_RH_Radii" if rh_radii else "n_RH",), ac.rh)):
+            v = f.createVariable(name, "f8", dims)
+            v[:] = _nc_order(data)
+        dims5 = ("n_Types", "n_Sigma", "n_Radii", "n_RH", "n_Wavelengths")
+        for name, data in (("ke", ac.ke), ("w", ac.w), ("g", ac.g)):
+            v = f.createVariable(name, "f8", dims5)
+            v[:] = _nc_order(data)
+        v = f.createVariable("pcoeff", "f8", ("n_Phase_Elements", "n_Legendre_Terms") + dims5)
+        v[:] = _nc_order(ac.pcoeff)
+
+
+def read_aerosolcoeff_nc(path: str, scheme: str = "CRTM") -> co.AerosolCoeff:
+    rh_radii = co._rh_radii_record(scheme)
+    with netcdf_file(path, "r", mmap=False) as f:
+        rel = int(_attr(f, "Release", co.AEROSOLCOEFF_RELEASE))
+        if rel != co.AEROSOLCOEFF_RELEASE:
+            raise ValueError(f"AerosolCoeff netCDF: release {rel} not supported")
+        if rh_radii != ("n_RH_Radii" in f.dimensions):
+            raise ValueError(f"AerosolCoeff netCDF: the n_RH_Radii dimension does not fit the {scheme!r} scheme")
+
+        def fortran(name, dtype=np.float64):
+            a = _var(f, name, dtype)
+            return np.ascontiguousarray(a.transpose(tuple(range(a.ndim))[::-1]))
+        names = [b"".join(row).decode("ascii", "replace").rstrip()
+                 for row in np.asarray(f.variables["Aerosol_Type_Name"].data)]
+        return co.AerosolCoeff(
+            type_id=_var(f, "Aerosol_Type", np.int32), type_name=names,
+            wavelength=_var(f, "Wavelength", np.float64), reff=fortran("Reff"), rsig=fortran("Rsig"),
+            rh=_var(f, "RH", np.float64), ke=fortran("ke"), w=fortran("w"), g=fortran("g"),
+            pcoeff=fortran("pcoeff"), data_source=str(_attr(f, "Data_Source", "")),
+            version=int(_attr(f, "Version", 1)))
+
+
+# ---------------------------------------------------------------------------
 # conversion for CRTM_Init
 # ---------------------------------------------------------------------------
 
@@ -248,6 +413,22 @@ def convert_irwater(src_dir: str, out_dir: str) -> None:
     """Nalli.IRwater.EmisCoeff.nc of src_dir as the binary file in out_dir."""
     co.write_irwatercoeff(os.path.join(out_dir, IRWATER_FILE + ".bin"),
                           read_irwater_nc(os.path.join(src_dir, IRWATER_FILE + ".nc")))
+
+
+def convert_cloud(src_dir: str, out_dir: str, nc_file: str = CLOUDCOEFF_FILE + ".nc") -> None:
+    """The netCDF CloudCoeff file of src_dir as CloudCoeff.bin in out_dir."""
+    co.write_cloudcoeff(os.path.join(out_dir, CLOUDCOEFF_FILE + ".bin"),
+                        read_cloudcoeff_nc(os.path.join(src_dir, nc_file)))
+
+
+def convert_aerosol(src_dir: str, out_dir: str, scheme: str = "CRTM",
+                    nc_file: str = AEROSOLCOEFF_FILE + ".nc") -> str:
+    """The netCDF AerosolCoeff file of src_dir, for the aerosol scheme, as
+    AerosolCoeff.bin in out_dir; returns that file's name."""
+    name = AEROSOLCOEFF_FILE + ".bin"
+    co.write_aerosolcoeff(os.path.join(out_dir, name),
+                          read_aerosolcoeff_nc(os.path.join(src_dir, nc_file), scheme), scheme=scheme)
+    return name
 
 
 def link_shared_files(src_dir: str, out_dir: str,

@@ -1,8 +1,8 @@
-"""netCDF-classic SpcCoeff / ODPS TauCoeff files (crtmv3_gb300/netcdf_coeffs.py):
-the reference's variable names, types and dimension order
-(SpcCoeff_netCDF_IO.f90:68-183, ODPS_netCDF_IO.f90:63-240), lossless round
-trips through the binary formats, the OPTRAN variables, and CRTM_Init's
-SpcCoeff_Format / TauCoeff_Format options.  Exact comparisons throughout."""
+"""netCDF-classic coefficient files (crtmv3_gb300/netcdf_coeffs.py): SpcCoeff,
+ODPS TauCoeff, IRwaterCoeff, CloudCoeff and AerosolCoeff in the reference's
+variable names, types and dimension order (each *_netCDF_IO.f90), lossless
+round trips through the binary formats, the OPTRAN variables, and CRTM_Init's
+*_Format options.  Exact comparisons throughout."""
 import filecmp
 import os
 
@@ -148,3 +148,108 @@ def test_irwater_round_trip_and_init(coeff_dir, tmp_path, monkeypatch):
     monkeypatch.setattr(api, "CRTM", FakeCRTM)
     assert api.CRTM_Init([sensor], [], str(src), irwatercoeff_format="netCDF") == api.SUCCESS
     assert filecmp.cmp(os.path.join(seen["path"], nc.IRWATER_FILE + ".bin"), binp, shallow=False)
+
+
+def test_cloudcoeff_round_trip_and_layout(tmp_path):
+    """CloudCoeff through netCDF and back to a byte-identical binary file, in
+    the layout of CloudCoeff_netCDF_IO.f90:2020-2545: the MW tables over
+    (n_Temperatures | n_MW_Densities, n_MW_Radii, n_MW_Frequencies), the IR
+    tables over the IR density axis, pcoeff_IR 4-D over n_Legendre_Terms."""
+    src = tmp_path / "src"
+    src.mkdir()
+    binp = sy.write_cloud_files(str(src))
+    cc = co.read_cloudcoeff(binp)
+    nc.write_cloudcoeff_nc(str(src / "CloudCoeff.nc"), cc)
+    _fields_equal(nc.read_cloudcoeff_nc(str(src / "CloudCoeff.nc")), cc)
+    out = tmp_path / "out"
+    out.mkdir()
+    nc.convert_cloud(str(src), str(out))
+    assert filecmp.cmp(str(out / "CloudCoeff.bin"), binp, shallow=False)
+    nl, nd = cc.n_legendre_terms, cc.density_mw.size
+    with netcdf_file(str(src / "CloudCoeff.nc"), "r", mmap=False) as f:
+        assert f.version_byte == 1
+        assert f.dimensions["n_Legendre_Terms"] == nl + 1
+        assert f.dimensions["n_IR_Densities"] == nd + 1
+        dims = {k: f.variables[k].dimensions for k in f.variables}
+        assert dims["ke_L_MW"] == ("n_Temperatures", "n_MW_Radii", "n_MW_Frequencies")
+        assert dims["kb_S_MW"] == ("n_MW_Densities", "n_MW_Radii", "n_MW_Frequencies")
+        assert dims["pcoeff_L_MW"] == ("n_Phase_Elements", "n_Legendre_Terms", "n_Temperatures",
+                                       "n_MW_Radii", "n_MW_Frequencies")
+        assert dims["pcoeff_IR"] == ("n_Legendre_Terms", "n_IR_Densities", "n_IR_Radii", "n_IR_Frequencies")
+        assert dims["Water_Density_MW"] == ("n_MW_Radii",) and dims["Density_IR"] == ("n_IR_Densities",)
+        assert f.variables["ke_IR"].data.dtype == np.dtype(">f8")
+        np.testing.assert_array_equal(f.variables["ke_L_MW"].data, cc.ke_l_mw.transpose(2, 1, 0))
+        np.testing.assert_array_equal(f.variables["pcoeff_IR"].data[:nl], cc.pcoeff_ir[..., 0].transpose(3, 2, 1, 0))
+        assert not f.variables["pcoeff_IR"].data[nl].any()
+        assert not f.variables["kb_IR"].data.any()
+
+
+@pytest.mark.parametrize("scheme", co.AEROSOL_SCHEMES)
+def test_aerosolcoeff_round_trip_and_layout(tmp_path, scheme):
+    """AerosolCoeff of each aerosol scheme through netCDF and back to a
+    byte-identical binary file (AerosolCoeff_netCDF_IO.f90:1540-1830): the
+    RH variable over n_RH_Radii for 'CRTM' / 'CMAQ', over n_RH otherwise;
+    a file read for a scheme whose layout it lacks is refused."""
+    src = tmp_path / "src"
+    src.mkdir()
+    binp = sy.write_aerosol_files(str(src), scheme)
+    ac = co.read_aerosolcoeff(binp, scheme)
+    ncp = str(src / "AerosolCoeff.nc")
+    nc.write_aerosolcoeff_nc(ncp, ac, scheme)
+    _fields_equal(nc.read_aerosolcoeff_nc(ncp, scheme), ac)
+    out = tmp_path / "out"
+    out.mkdir()
+    name = nc.convert_aerosol(str(src), str(out), scheme)
+    assert filecmp.cmp(str(out / name), binp, shallow=False)
+    rh_radii = scheme in ("CRTM", "CMAQ")
+    with netcdf_file(ncp, "r", mmap=False) as f:
+        dims = {k: f.variables[k].dimensions for k in f.variables}
+        assert dims["RH"] == (("n_RH_Radii",) if rh_radii else ("n_RH",))
+        assert dims["ke"] == ("n_Types", "n_Sigma", "n_Radii", "n_RH", "n_Wavelengths")
+        assert dims["pcoeff"] == ("n_Phase_Elements", "n_Legendre_Terms", "n_Types", "n_Sigma", "n_Radii",
+                                  "n_RH", "n_Wavelengths")
+        assert dims["Reff"] == ("n_Types", "n_Radii") and dims["Aerosol_Type_Name"] == ("n_Types", "tnsl")
+        assert f.dimensions["tnsl"] == co.AEROSOL_SL
+        np.testing.assert_array_equal(f.variables["Aerosol_Type"].data, ac.type_id)
+        np.testing.assert_array_equal(f.variables["ke"].data, ac.ke.transpose(4, 3, 2, 1, 0))
+    other = "NAAPS" if rh_radii else "CRTM"
+    with pytest.raises(ValueError, match="n_RH_Radii"):
+        nc.read_aerosolcoeff_nc(ncp, other)
+
+
+def test_crtm_init_cloud_and_aerosol_formats(coeff_dir, tmp_path, monkeypatch):
+    """CloudCoeff_Format / AerosolCoeff_Format = 'netCDF' and CloudCoeff_File
+    (src/CRTM_LifeCycle.f90:679-800): the tables the library loads are the
+    binary files the netCDF files came from."""
+    sensor = "irsynth_c616"
+    src = tmp_path / "src"
+    src.mkdir()
+    for kind in ("TauCoeff", "SpcCoeff"):
+        os.symlink(os.path.join(coeff_dir, f"{sensor}.{kind}.bin"), str(src / f"{sensor}.{kind}.bin"))
+    ref = tmp_path / "ref"
+    ref.mkdir()
+    cloud_bin = sy.write_cloud_files(str(ref))
+    aer_bin = sy.write_aerosol_files(str(ref), "CMAQ")
+    nc.write_cloudcoeff_nc(str(src / "MyClouds.nc"), co.read_cloudcoeff(cloud_bin))
+    nc.write_aerosolcoeff_nc(str(src / "AerosolCoeff.nc"), co.read_aerosolcoeff(aer_bin, "CMAQ"), "CMAQ")
+    seen = {}
+
+    class FakeCRTM:
+        def __init__(self, ids, path, *a):
+            seen["path"], seen["args"] = path, a
+            self.n_channels = [616]
+
+    monkeypatch.setattr(api, "CRTM", FakeCRTM)
+    assert api.CRTM_Init([sensor], [], str(src), aerosol_model="CMAQ", cloudcoeff_format="netCDF",
+                         cloudcoeff_file="MyClouds.nc", aerosolcoeff_format="netCDF") == api.SUCCESS
+    d = seen["path"]
+    assert filecmp.cmp(os.path.join(d, "CloudCoeff.bin"), cloud_bin, shallow=False)
+    assert seen["args"][1:] == ("CMAQ", "AerosolCoeff.bin")
+    assert filecmp.cmp(os.path.join(d, "AerosolCoeff.bin"), aer_bin, shallow=False)
+    # a binary cloud table under another name is loaded as CloudCoeff.bin
+    os.symlink(cloud_bin, str(src / "Other.bin"))
+    assert api.CRTM_Init([sensor], [], str(src), cloudcoeff_file="Other.bin") == api.SUCCESS
+    assert filecmp.cmp(os.path.join(seen["path"], "CloudCoeff.bin"), cloud_bin, shallow=False)
+    # the aerosol file read for a scheme whose layout it lacks fails the call
+    assert api.CRTM_Init([sensor], [], str(src), aerosol_model="NAAPS",
+                         aerosolcoeff_format="netCDF") == api.FAILURE
