@@ -655,41 +655,68 @@ def CRTM_Init(sensor_ids: Sequence[str], channel_info: List[ChannelInfo], file_p
               aerosolcoeff_file: Optional[str] = None, spccoeff_format: str = "Binary",
               taucoeff_format: str = "Binary", irwatercoeff_format: str = "Binary",
               cloudcoeff_format: str = "Binary", aerosolcoeff_format: str = "Binary",
-              cloudcoeff_file: Optional[str] = None) -> int:
-    """CRTM_Init: load the coefficients of ``sensor_ids`` and fill ``channel_info``
-    (Aerosol_Model, AerosolCoeff_File, AerosolCoeff_Format, CloudCoeff_File,
-    CloudCoeff_Format, SpcCoeff_Format and TauCoeff_Format as the reference's
-    optional arguments, src/CRTM_LifeCycle.f90:523-561, and
-    IRwaterCoeff_Format).  With a format 'netCDF' the sensors'
-    <id>.SpcCoeff.nc / <id>.TauCoeff.nc files, Nalli.IRwater.EmisCoeff.nc,
-    the cloud table (CloudCoeff_File, default CloudCoeff.nc) or the aerosol
-    table (AerosolCoeff_File, default AerosolCoeff.nc, read for the
-    Aerosol_Model's layout) are converted to binary files in a private
-    directory, which is loaded.  A binary CloudCoeff_File other than
-    CloudCoeff.bin is linked into that directory under CloudCoeff.bin."""
+              cloudcoeff_file: Optional[str] = None, cloud_model: Optional[str] = None,
+              irwatercoeff_file: Optional[str] = None, nc_file_path: Optional[str] = None,
+              load_cloudcoeff: bool = True, load_aerosolcoeff: bool = True) -> int:
+    """CRTM_Init: load the coefficients of ``sensor_ids`` and fill ``channel_info``.
+    The keyword arguments are the reference's optional arguments
+    (src/CRTM_LifeCycle.f90:519-591) for the tables this path reads:
+    Aerosol_Model, AerosolCoeff_Format / _File, Cloud_Model, CloudCoeff_Format
+    / _File, SpcCoeff_Format, TauCoeff_Format, IRwaterCoeff_Format / _File,
+    NC_File_Path, Load_CloudCoeff and Load_AerosolCoeff.
+
+    - A format 'netCDF' reads <id>.SpcCoeff.nc / <id>.TauCoeff.nc from
+      File_Path, and the cloud table (CloudCoeff_File, default CloudCoeff.nc),
+      the aerosol table (AerosolCoeff_File, default AerosolCoeff.nc, in the
+      Aerosol_Model's layout) and the IR water table (IRwaterCoeff_File,
+      default Nalli.IRwater.EmisCoeff.nc) from NC_File_Path when given, else
+      File_Path (:782-790, :811-815, :865-867).  They are converted to binary
+      files in a private directory, which the library loads.
+    - A binary CloudCoeff_File or IRwaterCoeff_File under another name is
+      linked into that directory under the default name.
+    - Load_CloudCoeff / Load_AerosolCoeff = False leave the table out
+      (:653-656, :782, :811); a batch with clouds or aerosols is then refused.
+    - Cloud_Model is accepted and, as in the reference, does not select the
+      table: CRTM_CloudCoeff_Load reads the file CloudCoeff_File names
+      (src/Coefficients/CRTM_CloudCoeff.f90:185-240)."""
+    from . import netcdf_coeffs as ncc
+    del cloud_model
     path = file_path
+    nc_path = nc_file_path or file_path
+    irwater_bin = ncc.IRWATER_FILE + ".bin"
     try:
         fmts = (spccoeff_format, taucoeff_format, irwatercoeff_format, cloudcoeff_format, aerosolcoeff_format)
         for fm in fmts:
             if fm.lower() not in ("binary", "netcdf"):
                 raise ValueError(f"coefficient format must be 'Binary' or 'netCDF' (got {fm!r})")
-        cloud_nc = cloudcoeff_format.lower() == "netcdf"
-        if any(fm.lower() == "netcdf" for fm in fmts) or cloudcoeff_file not in (None, "CloudCoeff.bin"):
+        cloud_nc, ir_nc, aer_nc = (fm.lower() == "netcdf" for fm in
+                                   (cloudcoeff_format, irwatercoeff_format, aerosolcoeff_format))
+        cloud_renamed = not cloud_nc and cloudcoeff_file not in (None, "CloudCoeff.bin")
+        ir_renamed = not ir_nc and irwatercoeff_file not in (None, irwater_bin)
+        if not load_aerosolcoeff:
+            aerosol_model = aerosolcoeff_file = None
+        if (any(fm.lower() == "netcdf" for fm in fmts) or cloud_renamed or ir_renamed
+                or not load_cloudcoeff or not load_aerosolcoeff):
             import tempfile
-            from . import netcdf_coeffs
             path = tempfile.mkdtemp(prefix="crtm_coeffs_")
             for s in sensor_ids:
-                netcdf_coeffs.convert_sensor(file_path, s, path, spccoeff_format, taucoeff_format)
-            if irwatercoeff_format.lower() == "netcdf":
-                netcdf_coeffs.convert_irwater(file_path, path)
-            if cloud_nc:
-                netcdf_coeffs.convert_cloud(file_path, path, cloudcoeff_file or "CloudCoeff.nc")
-            elif cloudcoeff_file not in (None, "CloudCoeff.bin"):
-                netcdf_coeffs._link(os.path.join(file_path, cloudcoeff_file), os.path.join(path, "CloudCoeff.bin"))
-            if aerosolcoeff_format.lower() == "netcdf":
-                aerosolcoeff_file = netcdf_coeffs.convert_aerosol(file_path, path, aerosol_model or "CRTM",
-                                                                  aerosolcoeff_file or "AerosolCoeff.nc")
-            netcdf_coeffs.link_shared_files(file_path, path, extra=(aerosolcoeff_file,) if aerosolcoeff_file else ())
+                ncc.convert_sensor(file_path, s, path, spccoeff_format, taucoeff_format)
+            if load_cloudcoeff and cloud_nc:
+                ncc.convert_cloud(nc_path, path, cloudcoeff_file or "CloudCoeff.nc")
+            elif load_cloudcoeff and cloud_renamed:
+                ncc._link(os.path.join(file_path, cloudcoeff_file), os.path.join(path, "CloudCoeff.bin"))
+            if ir_nc:
+                ncc.convert_irwater(nc_path, path, irwatercoeff_file or ncc.IRWATER_FILE + ".nc")
+            elif ir_renamed:
+                ncc._link(os.path.join(file_path, irwatercoeff_file), os.path.join(path, irwater_bin))
+            if load_aerosolcoeff and aer_nc:
+                aerosolcoeff_file = ncc.convert_aerosol(nc_path, path, aerosol_model or "CRTM",
+                                                        aerosolcoeff_file or "AerosolCoeff.nc")
+            names = [n for n in ncc.SHARED_FILES
+                     if (load_cloudcoeff or n != "CloudCoeff.bin")
+                     and (load_aerosolcoeff or not n.startswith("AerosolCoeff"))]
+            ncc.link_shared_files(file_path, path, names=names,
+                                  extra=(aerosolcoeff_file,) if aerosolcoeff_file else ())
     except (OSError, ValueError, KeyError) as e:
         print(f"CRTM_Init(FAILURE): {e}")
         return FAILURE

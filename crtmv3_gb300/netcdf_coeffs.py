@@ -409,10 +409,11 @@ def convert_sensor(src_dir: str, sensor_id: str, out_dir: str, spc_format: str =
             raise ValueError(f"{kind}_Format must be 'Binary' or 'netCDF' (got {fmt!r})")
 
 
-def convert_irwater(src_dir: str, out_dir: str) -> None:
-    """Nalli.IRwater.EmisCoeff.nc of src_dir as the binary file in out_dir."""
+def convert_irwater(src_dir: str, out_dir: str, nc_file: str = IRWATER_FILE + ".nc") -> None:
+    """The netCDF IRwaterCoeff file of src_dir (Nalli.IRwater.EmisCoeff.nc by
+    default) as Nalli.IRwater.EmisCoeff.bin in out_dir."""
     co.write_irwatercoeff(os.path.join(out_dir, IRWATER_FILE + ".bin"),
-                          read_irwater_nc(os.path.join(src_dir, IRWATER_FILE + ".nc")))
+                          read_irwater_nc(os.path.join(src_dir, nc_file)))
 
 
 def convert_cloud(src_dir: str, out_dir: str, nc_file: str = CLOUDCOEFF_FILE + ".nc") -> None:
@@ -431,10 +432,11 @@ def convert_aerosol(src_dir: str, out_dir: str, scheme: str = "CRTM",
     return name
 
 
-def link_shared_files(src_dir: str, out_dir: str,
-                      names=("CloudCoeff.bin", "AerosolCoeff.bin", "AerosolCoeff.CMAQ.bin",
-                             "AerosolCoeff.GOCART-GEOS5.bin", "AerosolCoeff.NAAPS.bin",
-                             "Nalli.IRwater.EmisCoeff.bin"), extra=()) -> None:
+SHARED_FILES = ("CloudCoeff.bin", "AerosolCoeff.bin", "AerosolCoeff.CMAQ.bin", "AerosolCoeff.GOCART-GEOS5.bin",
+                "AerosolCoeff.NAAPS.bin", IRWATER_FILE + ".bin")
+
+
+def link_shared_files(src_dir: str, out_dir: str, names=SHARED_FILES, extra=()) -> None:
     """The coefficient files shared by all sensors, as src_dir has them."""
     for n in tuple(names) + tuple(extra):
         p = os.path.join(src_dir, n)

@@ -253,3 +253,54 @@ def test_crtm_init_cloud_and_aerosol_formats(coeff_dir, tmp_path, monkeypatch):
     # the aerosol file read for a scheme whose layout it lacks fails the call
     assert api.CRTM_Init([sensor], [], str(src), aerosol_model="NAAPS",
                          aerosolcoeff_format="netCDF") == api.FAILURE
+
+
+def test_crtm_init_table_options(coeff_dir, tmp_path, monkeypatch):
+    """NC_File_Path (the netCDF tables' directory), IRwaterCoeff_File,
+    Load_CloudCoeff and Load_AerosolCoeff (src/CRTM_LifeCycle.f90:653-656,
+    :782-815, :865-867): the private directory holds exactly the tables the
+    options ask for."""
+    sensor = "irsynth_c616"
+    src, ncdir, ref = tmp_path / "src", tmp_path / "ncdir", tmp_path / "ref"
+    for d in (src, ncdir, ref):
+        d.mkdir()
+    for kind in ("TauCoeff", "SpcCoeff"):
+        os.symlink(os.path.join(coeff_dir, f"{sensor}.{kind}.bin"), str(src / f"{sensor}.{kind}.bin"))
+    cloud_bin = sy.write_cloud_files(str(ref))
+    aer_bin = sy.write_aerosol_files(str(ref))
+    os.symlink(cloud_bin, str(src / "CloudCoeff.bin"))
+    os.symlink(aer_bin, str(src / "AerosolCoeff.bin"))
+    wc = sy.generate_irwatercoeff()
+    co.write_irwatercoeff(str(ref / "water.bin"), wc)
+    nc.write_irwater_nc(str(ncdir / "MyWater.nc"), wc)
+    nc.write_cloudcoeff_nc(str(ncdir / "CloudCoeff.nc"), co.read_cloudcoeff(cloud_bin))
+    seen = {}
+
+    class FakeCRTM:
+        def __init__(self, ids, path, *a):
+            seen["path"], seen["args"] = path, a
+            self.n_channels = [616]
+
+    monkeypatch.setattr(api, "CRTM", FakeCRTM)
+    # netCDF tables from NC_File_Path; the sensors' files from File_Path
+    assert api.CRTM_Init([sensor], [], str(src), nc_file_path=str(ncdir), cloudcoeff_format="netCDF",
+                         irwatercoeff_format="netCDF", irwatercoeff_file="MyWater.nc",
+                         cloud_model="CRTM") == api.SUCCESS
+    d = seen["path"]
+    assert filecmp.cmp(os.path.join(d, "CloudCoeff.bin"), cloud_bin, shallow=False)
+    assert filecmp.cmp(os.path.join(d, nc.IRWATER_FILE + ".bin"), str(ref / "water.bin"), shallow=False)
+    assert filecmp.cmp(os.path.join(d, "AerosolCoeff.bin"), aer_bin, shallow=False)
+    # a binary IR water table under another name
+    os.symlink(str(ref / "water.bin"), str(src / "water.bin"))
+    assert api.CRTM_Init([sensor], [], str(src), irwatercoeff_file="water.bin") == api.SUCCESS
+    assert filecmp.cmp(os.path.join(seen["path"], nc.IRWATER_FILE + ".bin"), str(ref / "water.bin"),
+                       shallow=False)
+    # Load_CloudCoeff / Load_AerosolCoeff = False: the tables are left out
+    assert api.CRTM_Init([sensor], [], str(src), aerosol_model="CRTM", load_cloudcoeff=False,
+                         load_aerosolcoeff=False) == api.SUCCESS
+    d = seen["path"]
+    assert d != str(src)
+    assert not os.path.exists(os.path.join(d, "CloudCoeff.bin"))
+    assert not os.path.exists(os.path.join(d, "AerosolCoeff.bin"))
+    assert seen["args"][1:] == (None, None)
+    assert os.path.exists(os.path.join(d, f"{sensor}.TauCoeff.bin"))
