@@ -801,6 +801,73 @@ def run_scattering(args, torch, dev, rank, world, dist):
     return 0
 
 
+def run_case(args, torch, dev) -> int:
+    """Fixed cases for kernel captures and trajectory timing, one JSON line each.
+
+    cloudy-k48: one mixed-form K-matrix of 48 ``irsynth_c616`` profiles, 100
+    layers, liquid and ice clouds (``cloudy_workload(..., wc_scale=3.0)``),
+    stream rule -- the small case on which the scattering kernels are captured.
+    trajectory: ``linearize_device`` of ``--profiles`` clear-sky
+    ``irsynth_c2211`` profiles (101 layers, mixed form), then the tangent
+    linear (temperature and absorber perturbations) and the adjoint (a seed of
+    ones) applied from the stored Jacobians; CUDA events on the calling
+    stream, one untimed call first, linearize averaged over 3 calls and the
+    applications over 10."""
+    from crtmv3_gb300 import api, coefficients as co
+    d = tempfile.mkdtemp(prefix="crtm_case_")
+    if args.workload == "cloudy-k48":
+        sensor, P = "irsynth_c616", 48
+        sy.write_sensor_files(d, sensor)
+        sy.write_cloud_files(d)
+        atm, sfc, geo, opt = sy.cloudy_workload(sensor, P, 100, 7, cloud_types=(co.WATER_CLOUD, co.ICE_CLOUD),
+                                                wc_scale=3.0)
+        h = api.CRTM([sensor], d, api.MIXED)
+        km, rts = h.k_matrix(atm, sfc, geo, opt)
+        print(json.dumps({"workload": "cloudy-k48", "sensor": sensor, "profiles": P,
+                          "max_bt": float(np.abs(rts.brightness_temperature).max()),
+                          "status": int(np.abs(rts.status).max())}))
+        return 0
+    sensor, P = SENSOR, args.profiles
+    sy.write_sensor_files(d, sensor)
+    atm, sfc, geo, opt = sy.clear_sky_workload(sensor, P, N_LAYERS, 11)
+    h = api.CRTM([sensor], d, api.MIXED)
+    L, K, J = h.n_channels[0], atm.max_layers, atm.n_absorbers
+    b, keep, t = scatter_device_inputs(torch, h, atm, sfc, geo, opt, dev)
+    f64 = dict(dtype=torch.float64, device=dev)
+    traj = dict(radiance=torch.zeros((P, L), **f64), bt=torch.zeros((P, L), **f64),
+                status=torch.zeros((P,), dtype=torch.int32, device=dev))
+    st = torch.cuda.current_stream(dev)
+    sp = st.cuda_stream
+    rng = np.random.default_rng(1)
+    tl = dict(temperature=torch.from_numpy(rng.standard_normal((P, K))).to(dev),
+              absorber=torch.from_numpy(rng.standard_normal((P, J, K)) * 0.01).to(dev))
+    bt_tl = torch.zeros((P, L), **f64)
+    seed = torch.ones((P, L), **f64)
+    out = dict(temperature_ad=torch.zeros((P, K), **f64), absorber_ad=torch.zeros((P, J, K), **f64),
+               water_temperature_ad=torch.zeros((P,), **f64))
+
+    def timed(fn, n):
+        fn()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(n):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / n
+    t_lin = timed(lambda: h.linearize_device(b, traj, 0, sp), 3)
+    t_tl = timed(lambda: h.tangent_linear_apply_device(tl, bt_tl, sp), 10)
+    t_ad = timed(lambda: h.adjoint_apply_device(seed, out, sp), 10)
+    kbytes = P * L * (K * (1 + J) + 5) * 8     # stored T, absorber and surface Jacobians
+    print(json.dumps({"workload": "trajectory", "sensor": sensor, "profiles": P, "channels": L, "layers": K,
+                      "absorbers": J, "stored_jacobian_gb": kbytes / 1e9, "linearize_ms": t_lin,
+                      "tl_apply_ms": t_tl, "tl_apply_gbs": kbytes / t_tl / 1e6,
+                      "ad_apply_ms": t_ad, "ad_apply_gbs": kbytes / t_ad / 1e6,
+                      "status": int(traj["status"].abs().max().item())}))
+    return 0
+
+
 def local_rank() -> int:
     return int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -817,9 +884,10 @@ def main():
                          "group (C3-C5, default 32)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="C5", choices=["C2", "C3", "C4", "C5"],
+    ap.add_argument("--workload", default="C5", choices=["C2", "C3", "C4", "C5", "cloudy-k48", "trajectory"],
                     help="C5 (default): the ragged mixed-sensor batch, 30%% cloudy, forward + K-matrix; "
-                         "C2: clear-sky IR K-matrix; C3, C4: cloudy MW adjoint, all-sky IR K-matrix")
+                         "C2: clear-sky IR K-matrix; C3, C4: cloudy MW adjoint, all-sky IR K-matrix; "
+                         "cloudy-k48, trajectory: the fixed cases of run_case (not bench lines)")
     ap.add_argument("--autotune", action="store_true",
                     help="C2: pick the map tile and profiles per pass of each form with the "
                          "library's autotuner before the warm-up (default: the built-in 16 channels "
@@ -828,6 +896,10 @@ def main():
     if not args.cpu_profiles:
         args.cpu_profiles = 256 if args.workload == "C2" else 32
     if args.impl == "reference":
+        if args.workload in ("cloudy-k48", "trajectory"):
+            print(json.dumps({"impl": "reference", "unavailable": f"{args.workload} is a kernel-capture case, "
+                              "not a bench workload"}))
+            return 0
         return run_reference(args)
 
     import torch
@@ -842,6 +914,8 @@ def main():
     dev = torch.device("cuda", local)
     from crtmv3_gb300 import api, build
     build.build()
+    if args.workload in ("cloudy-k48", "trajectory"):
+        return run_case(args, torch, dev)
     if args.workload != "C2":
         rc = run_scattering(args, torch, dev, rank, world, dist)
         if dist:
