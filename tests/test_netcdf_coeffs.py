@@ -304,3 +304,19 @@ def test_crtm_init_table_options(coeff_dir, tmp_path, monkeypatch):
     assert not os.path.exists(os.path.join(d, "AerosolCoeff.bin"))
     assert seen["args"][1:] == (None, None)
     assert os.path.exists(os.path.join(d, f"{sensor}.TauCoeff.bin"))
+
+
+def test_cloudcoeff_nc_refuses_tables_it_cannot_hold(tmp_path):
+    """pcoeff_IR has no phase dimension in the reference's layout, so a table
+    with more than one phase element is refused rather than truncated; a file
+    of another release is refused on reading."""
+    cc = sy.generate_cloudcoeff()
+    many = co.CloudCoeff(**{f: getattr(cc, f) for f in cc.__dataclass_fields__})
+    many.pcoeff_l_mw = np.repeat(cc.pcoeff_l_mw, 2, axis=4)
+    with pytest.raises(ValueError, match="n_Phase_Elements"):
+        nc.write_cloudcoeff_nc(str(tmp_path / "x.nc"), many)
+    nc.write_cloudcoeff_nc(str(tmp_path / "c.nc"), cc)
+    with netcdf_file(str(tmp_path / "c.nc"), "a") as f:
+        f.Release = np.int32(co.CLOUDCOEFF_RELEASE + 1)
+    with pytest.raises(ValueError, match="release"):
+        nc.read_cloudcoeff_nc(str(tmp_path / "c.nc"))
