@@ -2,7 +2,8 @@
 
 Mirrors the reference's public interface for this path:
 
-* ``CRTM_Init`` / ``CRTM_Destroy``          (src/CRTM_LifeCycle.f90:520, :1131)
+* ``CRTM_Init`` / ``CRTM_Destroy`` / ``CRTM_IsInitialized``
+                                            (src/CRTM_LifeCycle.f90:520, :1131, :1291)
 * ``CRTM_Forward``                          (src/CRTM_Forward_Module.f90:229-245)
 * ``CRTM_K_Matrix``                         (src/CRTM_K_Matrix_Module.f90:300-322)
 * ``CRTM_Adjoint``                          (src/CRTM_Adjoint_Module.f90:299-309)
@@ -740,6 +741,13 @@ def CRTM_Destroy(channel_info: List[ChannelInfo]) -> int:
         h.close()
     channel_info.clear()
     return SUCCESS
+
+
+def CRTM_IsInitialized(channel_info: Sequence[ChannelInfo]) -> bool:
+    """CRTM_IsInitialized (src/CRTM_LifeCycle.f90:1291-1295): every ChannelInfo
+    holds a live library handle (ALL() of an empty list is true, as in
+    Fortran)."""
+    return all(ci.handle is not None and getattr(ci.handle, "h", None) for ci in channel_info)
 
 
 def CRTM_Forward(atmosphere: AtmosphereBatch, surface: SurfaceBatch, geometry: GeometryBatch,

@@ -320,3 +320,4 @@ def test_cloudcoeff_nc_refuses_tables_it_cannot_hold(tmp_path):
         f.Release = np.int32(co.CLOUDCOEFF_RELEASE + 1)
     with pytest.raises(ValueError, match="release"):
         nc.read_cloudcoeff_nc(str(tmp_path / "c.nc"))
+
